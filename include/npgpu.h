@@ -1,0 +1,300 @@
+/*
+ * npgpu.h -- C ABI of the GB300 rigid-body step for nphysics3d.
+ *
+ * This is the drop-in boundary for `MechanicalWorld::step`
+ * (src/world/mechanical_world.rs:182-396). A host binding (the Rust
+ * `GpuMechanicalWorld` shim, the C++ `npgpu::GpuMechanicalWorld`, or the
+ * Python ctypes mirror) owns the handle arenas (`DefaultBodySet`,
+ * `DefaultColliderSet`, src/object/body_set.rs:178, collider_set.rs) and
+ * forwards insertions, removals and the step through these entry points.
+ * The device owns the body/collider state and the impulse cache
+ * (src/solver/moreau_jean_solver.rs:14-23,
+ * src/solver/signorini_coulomb_pyramid_model.rs:19-25).
+ *
+ * Conventions
+ *  - Scalars are f32. Isometries are 7 floats: translation (x, y, z) then
+ *    a unit quaternion (i, j, k, w) -- nalgebra's `Isometry3` storage order.
+ *  - Velocities and forces are 6 floats: linear (x, y, z) then angular.
+ *  - Body and collider slots are the generational-arena indices of the host
+ *    sets; a handle is (index, generation). A slot whose generation does not
+ *    match is INVALID_HANDLE.
+ *  - No entry point aborts, traps or prints: every failure is a status code,
+ *    and npgpu_last_error() holds a one-line description.
+ *  - Calls on one world are not re-entrant and must come from one host
+ *    thread. Each world owns one CUDA stream (npgpu_stream()).
+ */
+#ifndef NPGPU_H
+#define NPGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NPGPU_ABI_VERSION 1u
+
+/* generational_arena::Index (src/object/body_set.rs:178). */
+typedef struct npgpu_handle {
+    uint64_t index;
+    uint64_t generation;
+} npgpu_handle;
+
+/* Errors: the reference panics or skips (src/solver/constraint.rs:89,234,
+ * src/solver/moreau_jean_solver.rs:147, src/world/geometrical_world.rs:66-73);
+ * the GPU world returns one of these instead. */
+typedef enum npgpu_status {
+    NPGPU_OK = 0,
+    NPGPU_ERR_INVALID_HANDLE = 1,
+    NPGPU_ERR_UNSUPPORTED_BODY = 2,   /* multibody, FEM, mass-spring, mass-constraint */
+    NPGPU_ERR_UNSUPPORTED_SHAPE = 3,  /* anything but Ball and Cuboid, or a sensor */
+    NPGPU_ERR_NONEMPTY_JOINTS = 4,
+    NPGPU_ERR_NONEMPTY_FORCES = 5,
+    NPGPU_ERR_CAPACITY = 6,           /* a fixed-capacity device buffer overflowed */
+    NPGPU_ERR_NAN = 7,                /* non-finite input or state */
+    NPGPU_ERR_TIMEOUT = 8,            /* a bounded device wait gave up */
+    NPGPU_ERR_CUDA = 9,
+    NPGPU_ERR_INVALID_ARGUMENT = 10
+} npgpu_status;
+
+/* BodyStatus (src/object/body.rs:50-59). */
+enum {
+    NPGPU_BODY_DISABLED = 0,
+    NPGPU_BODY_STATIC = 1,
+    NPGPU_BODY_DYNAMIC = 2,
+    NPGPU_BODY_KINEMATIC = 3
+};
+
+/* Body kinds. Only rigid bodies and grounds are accepted; the others exist
+ * so that a binding can forward them and receive UNSUPPORTED_BODY. */
+enum {
+    NPGPU_KIND_RIGID_BODY = 0,   /* src/object/rigid_body.rs */
+    NPGPU_KIND_GROUND = 1,       /* src/object/ground.rs: static, 0 dofs */
+    NPGPU_KIND_MULTIBODY = 2,
+    NPGPU_KIND_FEM_VOLUME = 3,
+    NPGPU_KIND_FEM_SURFACE = 4,
+    NPGPU_KIND_MASS_SPRING = 5,
+    NPGPU_KIND_MASS_CONSTRAINT = 6
+};
+
+/* Body flags (RigidBodyDesc, src/object/rigid_body.rs:949-1086). */
+enum {
+    NPGPU_BODY_GRAVITY = 1u << 0,          /* gravity_enabled (default on) */
+    NPGPU_BODY_LOCK_TX = 1u << 1,          /* kinematic_translations.x */
+    NPGPU_BODY_LOCK_TY = 1u << 2,
+    NPGPU_BODY_LOCK_TZ = 1u << 3,
+    NPGPU_BODY_LOCK_RX = 1u << 4,          /* kinematic_rotations.x */
+    NPGPU_BODY_LOCK_RY = 1u << 5,
+    NPGPU_BODY_LOCK_RZ = 1u << 6,
+    NPGPU_BODY_CAN_SLEEP = 1u << 7,        /* sleep_threshold is Some(..) */
+    NPGPU_BODY_LINEAR_INTERP = 1u << 8     /* linear_motion_interpolation (CCD only) */
+};
+
+/* One body as built by RigidBodyDesc::build (rigid_body.rs:1064-1084). */
+typedef struct npgpu_body_desc {
+    float position[7];          /* Isometry3 */
+    float velocity[6];          /* Velocity3 */
+    float local_inertia[7];     /* mass, then the angular tensor (xx, xy, xz, yy, yz, zz) */
+    float local_com[3];         /* local_center_of_mass */
+    float linear_damping;
+    float angular_damping;
+    float max_linear_velocity;  /* FLT_MAX = unbounded (rigid_body.rs:72) */
+    float max_angular_velocity;
+    float sleep_threshold;      /* used when NPGPU_BODY_CAN_SLEEP; default 0.01 (body.rs:73) */
+    uint32_t status;            /* NPGPU_BODY_* */
+    uint32_t kind;              /* NPGPU_KIND_* */
+    uint32_t flags;             /* NPGPU_BODY_* flag bits */
+    uint32_t world;             /* index of the world in a batch (0 for one world) */
+} npgpu_body_desc;
+
+/* Shapes (ncollide3d::shape). */
+enum {
+    NPGPU_SHAPE_BALL = 0,
+    NPGPU_SHAPE_CUBOID = 1,
+    NPGPU_SHAPE_OTHER = 2        /* rejected with UNSUPPORTED_SHAPE */
+};
+
+/* MaterialCombineMode (src/material/material.rs:49-64). */
+enum {
+    NPGPU_COMBINE_AVERAGE = 0,
+    NPGPU_COMBINE_MIN = 1,
+    NPGPU_COMBINE_MULTIPLY = 2,
+    NPGPU_COMBINE_MAX = 3
+};
+
+/* One collider as built by ColliderDesc::build (src/object/collider.rs:538-572)
+ * with a BasicMaterial (src/material/basic_material.rs). */
+typedef struct npgpu_collider_desc {
+    npgpu_handle body;          /* parent body (BodyPartHandle(body, 0)) */
+    float position_wrt_body[7]; /* ColliderDesc::position */
+    float shape_params[3];      /* ball: radius; cuboid: half extents */
+    float margin;               /* default 0.01 (collider.rs:476-479) */
+    float density;              /* default 0 (collider.rs:469) */
+    float linear_prediction;    /* default 0.001 (collider.rs:457) */
+    float angular_prediction;   /* default 5 degrees (collider.rs:458) */
+    float friction;             /* BasicMaterial default 0.5 (basic_material.rs:59-63) */
+    float restitution;          /* default 0 */
+    uint32_t friction_combine;  /* NPGPU_COMBINE_* */
+    uint32_t restitution_combine;
+    uint32_t shape;             /* NPGPU_SHAPE_* */
+    uint32_t is_sensor;         /* rejected when non-zero */
+    uint32_t ccd_enabled;       /* rejected when non-zero: CCD is not built */
+} npgpu_collider_desc;
+
+/* IntegrationParameters (src/solver/integration_parameters.rs:5-190),
+ * plus the GPU-only knobs at the end. */
+typedef struct npgpu_params {
+    float dt;                              /* 1/60 */
+    float erp;                             /* 0.2 */
+    float warmstart_coeff;                 /* 1.0 */
+    float restitution_velocity_threshold;  /* 1.0 */
+    float allowed_linear_error;            /* 0.001 */
+    float allowed_angular_error;           /* 0.001 */
+    float max_linear_correction;           /* 0.2 */
+    float max_angular_correction;          /* 0.2 */
+    float max_stabilization_multiplier;    /* 0.2 */
+    uint32_t max_velocity_iterations;      /* 8 */
+    uint32_t max_position_iterations;      /* 3 */
+    uint32_t max_ccd_position_iterations;  /* 10 (CCD is not built) */
+    uint32_t max_ccd_substeps;             /* 1 */
+    /* GPU-only. */
+    uint32_t solve_to_tolerance;           /* 0: run max_velocity_iterations; 1: stop when residual <= tol */
+    float residual_tolerance;              /* 1e-4 */
+    uint32_t max_iterations_to_tolerance;  /* cap when solve_to_tolerance (e.g. 256) */
+    uint32_t warmstart_mode;               /* 0: impulse cache (reference); 1: none */
+    float broad_phase_margin;              /* DBVTBroadPhase::new(0.01), geometrical_world.rs:60 */
+    float activation_mix;                  /* ActivationManager::new(0.01), mechanical_world.rs:80 */
+    uint32_t profile;                      /* non-zero: time each phase with CUDA events */
+} npgpu_params;
+
+/* Per-step counters: the stage names of src/counters/mod.rs:18-209 plus
+ * solver statistics. Times are milliseconds of the last step (0 unless
+ * params.profile). */
+typedef struct npgpu_counters {
+    double step_time;
+    double collision_detection_time;
+    double broad_phase_time;
+    double narrow_phase_time;
+    double island_construction_time;
+    double solver_time;
+    double assembly_time;
+    double velocity_resolution_time;
+    double velocity_update_time;
+    double position_resolution_time;
+    double colouring_time;
+    uint64_t steps;
+    uint32_t num_pairs;              /* broad-phase pairs */
+    uint32_t num_manifolds;          /* pairs with at least one contact */
+    uint32_t num_contacts;           /* contacts in all manifolds */
+    uint32_t num_solver_contacts;    /* contacts handed to the solver (awake islands) */
+    uint32_t num_constraints;        /* velocity rows: 3 per solver contact */
+    uint32_t num_colours;
+    uint32_t num_active_bodies;      /* dynamic bodies in awake islands */
+    uint32_t velocity_iterations;    /* iterations run in the last step */
+    double residual;                 /* FP64 complementarity residual after the last iteration */
+    double residual_initial;         /* ... after the warm start, before iteration 1 */
+    double max_penetration;          /* FP64 audit: max(depth + margins) over contacts */
+    double kinetic_energy;           /* FP64 audit: sum 1/2 (m v.v + w.I w) */
+} npgpu_counters;
+
+/* Contact record returned for parity checks (a TrackedContact,
+ * ncollide3d query::TrackedContact, plus the solver's impulses). */
+typedef struct npgpu_contact {
+    uint32_t collider1, collider2;   /* collider slots, collider1 < collider2 */
+    uint32_t feature_key;            /* our ContactId within the pair */
+    uint32_t kinematic;              /* approximation kinds (low byte: 1, next: 2) */
+    float world1[3];
+    float world2[3];
+    float normal[3];                 /* from collider1 toward collider2 */
+    float depth;                     /* > 0 means penetration */
+    float impulse[3];                /* cached (normal, tangent1, tangent2) */
+    uint32_t colour;                 /* solver colour of the manifold, or 0xffffffff */
+} npgpu_contact;
+
+typedef struct npgpu_world npgpu_world;
+
+/* Library version (NPGPU_ABI_VERSION). */
+uint32_t npgpu_abi_version(void);
+
+/* Fills `out` with IntegrationParameters::default() (integration_parameters.rs:169-189). */
+void npgpu_default_params(npgpu_params* out);
+
+/* MechanicalWorld::new(gravity) (mechanical_world.rs:76-99) plus
+ * GeometricalWorld::new() (geometrical_world.rs:57-63). Capacities bound the
+ * slot indices and the pair/contact buffers; *status receives the outcome. */
+npgpu_world* npgpu_create(const npgpu_params* params, const float gravity[3],
+                          uint32_t capacity_bodies, uint32_t capacity_colliders,
+                          uint32_t capacity_pairs, npgpu_status* status);
+void npgpu_destroy(npgpu_world* w);
+
+/* The world's CUDA stream (a cudaStream_t), for callers that time or order work. */
+void* npgpu_stream(npgpu_world* w);
+
+npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params);
+npgpu_status npgpu_set_gravity(npgpu_world* w, const float gravity[3]);
+
+/* DefaultBodySet::insert + the mass bookkeeping of maintain (mechanical_world.rs:114-179).
+ * Inserting or overwriting a body marks it changed (it is woken up on the
+ * next step, rigid_body.rs:563-565). */
+npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                 const npgpu_body_desc* descs);
+
+/* DefaultColliderSet::insert; the collider's mass properties are added to its
+ * body at the next step (geometrical_world.rs:102-143). */
+npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                    const npgpu_collider_desc* descs);
+
+/* DefaultBodySet::remove / DefaultColliderSet::remove. Removing a body removes
+ * its colliders (mechanical_world.rs:130-139). */
+npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle* handles);
+npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_handle* handles);
+
+/* RigidBody::apply_force(0, force, ForceType::Force, auto_wake_up)
+ * (rigid_body.rs:783-820): accumulates into the external force, which the
+ * next step uses and then clears. */
+npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                const float* forces6, int auto_wake_up);
+
+/* MechanicalWorld::step (mechanical_world.rs:182-396) run `nsteps` times,
+ * asynchronously on the world's stream. `num_joints` / `num_force_generators`
+ * are the sizes of the caller's sets: non-zero is rejected. */
+npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints,
+                        uint32_t num_force_generators);
+
+/* Waits for the world's stream and reports any device-side error flag. */
+npgpu_status npgpu_synchronize(npgpu_world* w);
+
+/* Copies body state to host arrays indexed by slot (any pointer may be NULL):
+ * position[7n], velocity[6n], energy[n] (activation energy), active[n]
+ * (1 when awake), for slots [first, first + n). */
+npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, float* position,
+                                   float* velocity, float* energy, uint8_t* active);
+
+/* The inertia the bodies carry after the colliders' mass was added:
+ * local_inertia[7n] (mass, xx, xy, xz, yy, yz, zz) and local_com[3n]. */
+npgpu_status npgpu_download_mass_properties(npgpu_world* w, uint32_t first, uint32_t n,
+                                            float* local_inertia, float* local_com);
+
+/* Broad-phase pairs as (collider1, collider2) with collider1 < collider2,
+ * sorted ascending. *count receives the number of pairs; at most `max` are written. */
+npgpu_status npgpu_get_pairs(npgpu_world* w, uint32_t* pairs2, uint32_t max, uint32_t* count);
+
+/* Fat AABBs (min xyz, max xyz) of colliders [first, first + n). */
+npgpu_status npgpu_get_aabbs(npgpu_world* w, uint32_t first, uint32_t n, float* aabb6);
+
+/* Contacts of every manifold, sorted by (collider1, collider2, feature_key). */
+npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max,
+                                uint32_t* count);
+
+npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out);
+
+/* One-line description of the last failure on this world (or of the last
+ * failed npgpu_create when w is NULL). */
+const char* npgpu_last_error(const npgpu_world* w);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NPGPU_H */

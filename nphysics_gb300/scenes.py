@@ -1,0 +1,316 @@
+"""Scene builders: the rigid-body scenes the step is measured and checked on.
+
+Each builder returns a `Scene`: structured numpy arrays laid out exactly as
+`npgpu_body_desc` / `npgpu_collider_desc` (include/npgpu.h), plus handles.
+Defaults follow RigidBodyDesc::new (src/object/rigid_body.rs:974-995),
+ColliderDesc::new (src/object/collider.rs:455-479) and BasicMaterial::default
+(src/material/basic_material.rs:59-63). Recipes follow examples3d/pyramid3.rs,
+balls3.rs and wall3.rs, scaled to the benchmark configurations.
+"""
+import math
+
+import numpy as np
+
+from . import abi
+
+BODY_DTYPE = np.dtype(abi.BodyDesc)
+COLLIDER_DTYPE = np.dtype(abi.ColliderDesc)
+HANDLE_DTYPE = np.dtype(abi.Handle)
+DEFAULT_SLEEP_THRESHOLD = 0.01   # ActivationStatus::default_threshold (src/object/body.rs:72-74)
+DEFAULT_MARGIN = 0.01
+DEFAULT_LINEAR_PREDICTION = 0.001
+DEFAULT_ANGULAR_PREDICTION = math.pi / 180.0 * 5.0
+
+
+class Scene:
+    def __init__(self, name, bodies, colliders, gravity=(0.0, -9.81, 0.0), dt=1.0 / 60.0, steps=1, info=None):
+        self.name = name
+        self.bodies = bodies
+        self.colliders = colliders
+        self.body_handles = make_handles(len(bodies))
+        self.collider_handles = make_handles(len(colliders))
+        self.gravity = tuple(float(g) for g in gravity)
+        self.dt = float(dt)
+        self.steps = int(steps)
+        self.info = dict(info or {})
+
+    @property
+    def num_dynamic(self):
+        return int(np.count_nonzero(self.bodies["status"] == abi.BODY_DYNAMIC))
+
+    def params(self):
+        p = abi.default_params()
+        p.dt = self.dt
+        return p
+
+
+def make_handles(n, generation=0):
+    h = np.zeros(n, HANDLE_DTYPE)
+    h["index"] = np.arange(n, dtype=np.uint64)
+    h["generation"] = generation
+    return h
+
+
+def body_descs(n):
+    """n copies of RigidBodyDesc::new().build()."""
+    b = np.zeros(n, BODY_DTYPE)
+    b["position"][:, 6] = 1.0
+    b["max_linear_velocity"] = abi.FLT_MAX
+    b["max_angular_velocity"] = abi.FLT_MAX
+    b["sleep_threshold"] = DEFAULT_SLEEP_THRESHOLD
+    b["status"] = abi.BODY_DYNAMIC
+    b["kind"] = abi.KIND_RIGID_BODY
+    b["flags"] = abi.BODY_GRAVITY | abi.BODY_CAN_SLEEP
+    return b
+
+
+def ground_descs(n):
+    """n copies of Ground::new() (src/object/ground.rs:21-27)."""
+    b = body_descs(n)
+    b["status"] = abi.BODY_STATIC
+    b["kind"] = abi.KIND_GROUND
+    b["flags"] = 0
+    return b
+
+
+def collider_descs(n, body_index, shape, params, density=0.0, friction=0.5, restitution=0.0):
+    c = np.zeros(n, COLLIDER_DTYPE)
+    c["body"]["index"] = body_index
+    c["body"]["generation"] = 0
+    c["position_wrt_body"][:, 6] = 1.0
+    c["shape_params"] = params
+    c["margin"] = DEFAULT_MARGIN
+    c["density"] = density
+    c["linear_prediction"] = DEFAULT_LINEAR_PREDICTION
+    c["angular_prediction"] = DEFAULT_ANGULAR_PREDICTION
+    c["friction"] = friction
+    c["restitution"] = restitution
+    c["shape"] = shape
+    return c
+
+
+def uniform_quaternions(rng, n):
+    """Uniform random rotations (Shoemake 1992), (i, j, k, w) order."""
+    u1, u2, u3 = rng.random(n), rng.random(n), rng.random(n)
+    a, b = np.sqrt(1.0 - u1), np.sqrt(u1)
+    q = np.stack([a * np.sin(2 * np.pi * u2), a * np.cos(2 * np.pi * u2),
+                  b * np.sin(2 * np.pi * u3), b * np.cos(2 * np.pi * u3)], axis=1)
+    return q.astype(np.float32)
+
+
+def _ground(half=(50.0, 1.0, 50.0), friction=0.5, world=0):
+    g = ground_descs(1)
+    g["world"] = world
+    gc = collider_descs(1, 0, abi.SHAPE_CUBOID, half, density=0.0, friction=friction)
+    gc["position_wrt_body"][0, 1] = -half[1]     # top face at y = 0
+    return g, gc
+
+
+def _concat(parts_b, parts_c):
+    """Concatenates (bodies, colliders) groups, re-pointing collider parents."""
+    bodies, colliders, off = [], [], 0
+    for b, c in zip(parts_b, parts_c):
+        c = c.copy()
+        c["body"]["index"] = c["body"]["index"] + off
+        bodies.append(b)
+        colliders.append(c)
+        off += len(b)
+    return np.concatenate(bodies), np.concatenate(colliders)
+
+
+def pyramid(base=20, half=0.5, friction=0.5):
+    """C1: a 2D triangle of cuboids (base 20 -> 210 boxes, half extents 0.5,
+    1.0 spacing) on a static 50 x 1 x 50 ground, density 1, friction 0.5."""
+    xs, ys = [], []
+    for row in range(base):
+        for i in range(base - row):
+            xs.append(i * 2 * half + row * half - (base - 1) * half)
+            ys.append(half + row * 2 * half)
+    n = len(xs)
+    g, gc = _ground(friction=friction)
+    b = body_descs(n)
+    b["position"][:, 0] = xs
+    b["position"][:, 1] = ys
+    c = collider_descs(n, np.arange(n), abi.SHAPE_CUBOID, (half, half, half), density=1.0, friction=friction)
+    bodies, colliders = _concat([g, b], [gc, c])
+    return Scene(f"box pyramid (base {base}, {n} cuboids)", bodies, colliders, steps=1000,
+                 info={"boxes": n})
+
+
+def ball_pile(side=32, radius=0.5, spacing=1.2, jitter=0.05, seed=1234, friction=0.3):
+    """C2: side^3 balls (radius 0.5) on a 1.2 lattice with U(-0.05, 0.05) jitter,
+    dropped on a static 100 x 1 x 100 ground; density 1, friction 0.3."""
+    rng = np.random.default_rng(seed)
+    n = side ** 3
+    i, j, k = np.meshgrid(np.arange(side), np.arange(side), np.arange(side), indexing="ij")
+    pos = np.stack([(i.ravel() - (side - 1) / 2) * spacing,
+                    1.0 + j.ravel() * spacing,
+                    (k.ravel() - (side - 1) / 2) * spacing], axis=1)
+    pos += rng.uniform(-jitter, jitter, size=pos.shape)
+    g, gc = _ground(half=(100.0, 1.0, 100.0), friction=friction)
+    b = body_descs(n)
+    b["position"][:, :3] = pos.astype(np.float32)
+    c = collider_descs(n, np.arange(n), abi.SHAPE_BALL, (radius, 0, 0), density=1.0, friction=friction)
+    bodies, colliders = _concat([g, b], [gc, c])
+    return Scene(f"ball pile ({side}^3 = {n} balls)", bodies, colliders, steps=600, info={"balls": n})
+
+
+def mixed_pile(n=100_000, seed=1234, friction=0.5, spacing=2.0, footprint=100.0):
+    """C3: n bodies, half balls with radius U(0.2, 0.8) and half cuboids with
+    half extents U(0.2, 0.8)^3 and uniform random orientation, density 1,
+    friction 0.5, over a 100 x 100 footprint. Bodies sit on a jittered 2.0
+    lattice of layers from y = 1 upward so that none overlap at t = 0."""
+    rng = np.random.default_rng(seed)
+    per_side = int(footprint // spacing)
+    per_layer = per_side * per_side
+    idx = np.arange(n)
+    layer, rem = idx // per_layer, idx % per_layer
+    gx, gz = rem % per_side, rem // per_side
+    pos = np.stack([(gx - (per_side - 1) / 2) * spacing, 1.0 + layer * spacing,
+                    (gz - (per_side - 1) / 2) * spacing], axis=1).astype(np.float64)
+    pos += rng.uniform(-0.1, 0.1, size=pos.shape)
+    is_ball = rng.permutation(n) < n // 2
+    g, gc = _ground(half=(footprint * 0.6, 1.0, footprint * 0.6), friction=friction)
+    b = body_descs(n)
+    b["position"][:, :3] = pos.astype(np.float32)
+    b["position"][:, 3:7] = uniform_quaternions(rng, n)
+    shape = np.where(is_ball, abi.SHAPE_BALL, abi.SHAPE_CUBOID).astype(np.uint32)
+    params = np.zeros((n, 3), np.float32)
+    params[is_ball, 0] = rng.uniform(0.2, 0.8, size=int(is_ball.sum()))
+    params[~is_ball] = rng.uniform(0.2, 0.8, size=(int((~is_ball).sum()), 3))
+    c = collider_descs(n, np.arange(n), abi.SHAPE_BALL, (0, 0, 0), density=1.0, friction=friction)
+    c["shape"] = shape
+    c["shape_params"] = params
+    bodies, colliders = _concat([g, b], [gc, c])
+    return Scene(f"mixed pile ({n} bodies)", bodies, colliders, steps=300, info={"bodies": n})
+
+
+def batched_worlds(n_worlds=4096, seed=1234, lo=16, hi=2048):
+    """C4: independent worlds with body counts log-uniform in [16, 2048], each
+    a scaled-down ball pile or a box stack of height U(3, 15) on its own ground.
+    Worlds share space; the world index keeps them apart."""
+    rng = np.random.default_rng(seed)
+    counts = np.round(np.exp(rng.uniform(math.log(lo), math.log(hi), size=n_worlds))).astype(int)
+    kinds = rng.random(n_worlds) < 0.5
+    parts_b, parts_c = [], []
+    for w in range(n_worlds):
+        nb = int(counts[w])
+        g, gc = _ground(half=(60.0, 1.0, 60.0), world=w)
+        b = body_descs(nb)
+        b["world"] = w
+        if kinds[w]:
+            side = int(math.ceil(nb ** (1.0 / 3.0)))
+            idx = np.arange(nb)
+            i, j, k = idx % side, (idx // side) % side, idx // (side * side)
+            pos = np.stack([(i - (side - 1) / 2) * 1.2, 1.0 + k * 1.2, (j - (side - 1) / 2) * 1.2], axis=1)
+            pos += rng.uniform(-0.05, 0.05, size=pos.shape)
+            c = collider_descs(nb, np.arange(nb), abi.SHAPE_BALL, (0.5, 0, 0), density=1.0, friction=0.3)
+        else:
+            height = int(rng.integers(3, 16))
+            cols = int(math.ceil(nb / height))
+            cs = int(math.ceil(math.sqrt(cols)))
+            idx = np.arange(nb)
+            col, lev = idx // height, idx % height
+            pos = np.stack([(col % cs - (cs - 1) / 2) * 1.5, 0.5 + lev * 1.0, (col // cs - (cs - 1) / 2) * 1.5],
+                           axis=1)
+            c = collider_descs(nb, np.arange(nb), abi.SHAPE_CUBOID, (0.5, 0.5, 0.5), density=1.0, friction=0.5)
+        b["position"][:, :3] = pos.astype(np.float32)
+        parts_b += [g, b]
+        parts_c += [gc, c]
+    bodies, colliders = _concat(parts_b, parts_c)
+    return Scene(f"{n_worlds} batched worlds", bodies, colliders, steps=100,
+                 info={"worlds": n_worlds, "bodies": int(counts.sum())})
+
+
+def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234):
+    """C5: walls of width x height bricks (half extents 0.5 x 0.25 x 0.25,
+    running bond) each struck by `balls` balls of radius 0.4, density 10, at
+    U(20, 40) m/s with a +-5 degree direction jitter; friction 0.6, dt 1/120."""
+    rng = np.random.default_rng(seed)
+    parts_b, parts_c = [], []
+    for w in range(n_walls):
+        g, gc = _ground(half=(60.0, 1.0, 60.0), friction=0.6, world=w)
+        xs, ys = [], []
+        for r in range(height):
+            off = 0.5 if r % 2 else 0.0
+            for i in range(width):
+                xs.append((i - width / 2) * 1.0 + off)
+                ys.append(0.25 + r * 0.5)
+        nb = len(xs)
+        b = body_descs(nb)
+        b["world"] = w
+        b["position"][:, 0] = xs
+        b["position"][:, 1] = ys
+        c = collider_descs(nb, np.arange(nb), abi.SHAPE_CUBOID, (0.5, 0.25, 0.25), density=1.0, friction=0.6)
+        bb = body_descs(balls)
+        bb["world"] = w
+        start = np.stack([rng.uniform(-width / 2, width / 2, balls), rng.uniform(1.0, height * 0.5, balls),
+                          np.full(balls, -15.0)], axis=1)
+        speed = rng.uniform(20.0, 40.0, balls)
+        yaw = np.radians(rng.uniform(-5.0, 5.0, balls))
+        pitch = np.radians(rng.uniform(-5.0, 5.0, balls))
+        vel = np.stack([np.sin(yaw) * np.cos(pitch), np.sin(pitch), np.cos(yaw) * np.cos(pitch)], axis=1) * speed[:, None]
+        bb["position"][:, :3] = start.astype(np.float32)
+        bb["velocity"][:, :3] = vel.astype(np.float32)
+        cb = collider_descs(balls, np.arange(balls), abi.SHAPE_BALL, (0.4, 0, 0), density=10.0, friction=0.6)
+        parts_b += [g, b, bb]
+        parts_c += [gc, c, cb]
+    bodies, colliders = _concat(parts_b, parts_c)
+    return Scene(f"{n_walls} brick walls", bodies, colliders, dt=1.0 / 120.0, steps=2000,
+                 info={"walls": n_walls, "bodies": n_walls * (width * height + balls)})
+
+
+# ---------------------------------------------------------------- small scenes
+def single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 5, 0), velocity=(0, 0, 0, 0, 0, 0),
+                rotation=(0, 0, 0, 1), ground=True, density=1.0, friction=0.5, restitution=0.0):
+    parts_b, parts_c = [], []
+    if ground:
+        g, gc = _ground(friction=friction)
+        parts_b.append(g)
+        parts_c.append(gc)
+    b = body_descs(1)
+    b["position"][0, :3] = position
+    b["position"][0, 3:7] = rotation
+    b["velocity"][0] = velocity
+    c = collider_descs(1, 0, shape, params, density=density, friction=friction, restitution=restitution)
+    parts_b.append(b)
+    parts_c.append(c)
+    bodies, colliders = _concat(parts_b, parts_c)
+    return Scene("single body", bodies, colliders)
+
+
+def random_cluster(n=64, seed=7, extent=3.0, boxes=True, balls=True, ground=True, rotate=True, world=0):
+    """A small random cluster of balls and cuboids with overlaps, for
+    collision-detection and solver parity checks."""
+    rng = np.random.default_rng(seed)
+    parts_b, parts_c = [], []
+    if ground:
+        g, gc = _ground(world=world)
+        parts_b.append(g)
+        parts_c.append(gc)
+    b = body_descs(n)
+    b["world"] = world
+    b["position"][:, 0] = rng.uniform(-extent, extent, n)
+    b["position"][:, 1] = rng.uniform(0.2, 2 * extent, n)
+    b["position"][:, 2] = rng.uniform(-extent, extent, n)
+    if rotate:
+        b["position"][:, 3:7] = uniform_quaternions(rng, n)
+    b["velocity"][:, :3] = rng.uniform(-1, 1, (n, 3))
+    b["velocity"][:, 3:] = rng.uniform(-1, 1, (n, 3))
+    kinds = rng.random(n)
+    if boxes and not balls:
+        is_ball = np.zeros(n, bool)
+    elif balls and not boxes:
+        is_ball = np.ones(n, bool)
+    else:
+        is_ball = kinds < 0.5
+    c = collider_descs(n, np.arange(n), abi.SHAPE_BALL, (0, 0, 0), density=1.0, friction=0.5)
+    c["shape"] = np.where(is_ball, abi.SHAPE_BALL, abi.SHAPE_CUBOID)
+    p = np.zeros((n, 3), np.float32)
+    p[is_ball, 0] = rng.uniform(0.2, 0.8, int(is_ball.sum()))
+    p[~is_ball] = rng.uniform(0.2, 0.8, (int((~is_ball).sum()), 3))
+    c["shape_params"] = p
+    parts_b.append(b)
+    parts_c.append(c)
+    bodies, colliders = _concat(parts_b, parts_c)
+    return Scene(f"random cluster ({n})", bodies, colliders)

@@ -1,0 +1,1498 @@
+// ref_world.hpp -- CPU oracle of the nphysics3d 0.23 rigid-body step.
+//
+// TEST INFRASTRUCTURE ONLY. This restates MechanicalWorld::step
+// (src/world/mechanical_world.rs:182-396) for scenes of static, dynamic and
+// kinematic rigid bodies with ball and cuboid colliders, single-threaded, in
+// R = float or double. It is the checker of the GPU step: tests, the smoke
+// check and the CPU-baseline leg of the benchmark load it; the product never
+// links it.
+//
+// Parity status. The reference (Rust) cannot be built here. The solver,
+// dynamics, activation and material code below restate the reference files
+// cited at each function. The collision arithmetic lives in ncollide3d 0.31,
+// which is not vendored; it is restated from published methods (loosened
+// AABBs with DBVT fat-AABB hysteresis, SAT + Sutherland-Hodgman clipping,
+// Ericson's segment-segment closest points) and is pinned only by analytic
+// known-answer tests, not by the reference's own outputs.
+//
+// Two Gauss-Seidel orders are provided:
+//  - ORDER_REFERENCE: the reference's row order (non-ground rows, then ground
+//    rows; manifolds in ascending collider-pair order);
+//  - ORDER_COLOUR: the order of the GPU solver (manifolds grouped by their
+//    Jones-Plassmann colour). It is a permutation of the same rows.
+#pragma once
+#include <cstdint>
+#include <cstring>
+#include <cfloat>
+#include <limits>
+#include <map>
+#include <string>
+#include <vector>
+#include <algorithm>
+#include "ref_math.hpp"
+#include "../include/npgpu.h"
+
+namespace oracle {
+
+enum { ORDER_REFERENCE = 0, ORDER_COLOUR = 1 };
+enum { AP_POINT = 1, AP_SEGMENT = 2, AP_PLANE = 3 };
+
+// Feature ids of a cuboid: vertices 0-7 (bit k set = +h along axis k),
+// edges 8-19 (8 + 4*axis + sign bits of the two other axes in increasing order),
+// faces 20-25 (20 + 2*axis + positive). A ball has the single feature 0.
+inline int box_vertex_id(int sx, int sy, int sz) { return sx | (sy << 1) | (sz << 2); }
+inline void edge_other_axes(int a, int& o1, int& o2) {
+    o1 = (a == 0) ? 1 : 0;
+    o2 = (a == 2) ? 1 : 2;
+}
+inline int box_edge_id(int axis, int s_o1, int s_o2) { return 8 + 4 * axis + (s_o1 | (s_o2 << 1)); }
+inline int box_face_id(int axis, int positive) { return 20 + 2 * axis + positive; }
+
+inline uint32_t pair_hash22(uint32_t c1, uint32_t c2) {
+    uint32_t h = c1 * 0x9E3779B1u ^ (c2 + 0x7F4A7C15u) * 0x85EBCA77u;
+    h ^= h >> 15;
+    h *= 0x2C1B3C6Du;
+    h ^= h >> 12;
+    h *= 0x297A2D39u;
+    h ^= h >> 15;
+    return h >> 10;
+}
+// Jones-Plassmann priority of a manifold: unique per collider pair.
+inline uint64_t pair_priority(uint32_t c1, uint32_t c2) {
+    return (uint64_t(pair_hash22(c1, c2)) << 42) | (uint64_t(c1) << 21) | uint64_t(c2);
+}
+
+template <class R> struct Approx {
+    int kind;
+    V3<R> a, b;  // point: a; segment: a..b; plane: point a, normal b
+};
+
+template <class R> inline Approx<R> box_feature(V3<R> h, int fid) {
+    Approx<R> ap;
+    if (fid < 8) {
+        ap.kind = AP_POINT;
+        ap.a = v3<R>((fid & 1) ? h.x : -h.x, (fid & 2) ? h.y : -h.y, (fid & 4) ? h.z : -h.z);
+        ap.b = v3<R>(R(0), R(0), R(0));
+    } else if (fid < 20) {
+        int e = fid - 8, axis = e / 4, bits = e % 4, o1, o2;
+        edge_other_axes(axis, o1, o2);
+        V3<R> p = v3<R>(R(0), R(0), R(0));
+        setc(p, o1, (bits & 1) ? comp(h, o1) : -comp(h, o1));
+        setc(p, o2, (bits & 2) ? comp(h, o2) : -comp(h, o2));
+        ap.kind = AP_SEGMENT;
+        ap.a = p;
+        ap.b = p;
+        setc(ap.a, axis, -comp(h, axis));
+        setc(ap.b, axis, comp(h, axis));
+    } else {
+        int f = fid - 20, axis = f / 2, pos = f % 2;
+        ap.kind = AP_PLANE;
+        ap.a = v3<R>(R(0), R(0), R(0));
+        ap.b = v3<R>(R(0), R(0), R(0));
+        setc(ap.a, axis, pos ? comp(h, axis) : -comp(h, axis));
+        setc(ap.b, axis, pos ? R(1) : R(-1));
+    }
+    return ap;
+}
+
+// Closest points of two segments (Ericson, Real-Time Collision Detection, 5.1.9).
+template <class R>
+inline void closest_segment_segment(V3<R> p1, V3<R> q1, V3<R> p2, V3<R> q2, V3<R>& c1, V3<R>& c2) {
+    const R eps = std::numeric_limits<R>::epsilon();
+    V3<R> d1 = q1 - p1, d2 = q2 - p2, r = p1 - p2;
+    R a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
+    R s, t;
+    if (a <= eps && e <= eps) {
+        s = R(0); t = R(0);
+    } else if (a <= eps) {
+        s = R(0);
+        t = std::min(std::max(f / e, R(0)), R(1));
+    } else {
+        R c = dot(d1, r);
+        if (e <= eps) {
+            t = R(0);
+            s = std::min(std::max(-c / a, R(0)), R(1));
+        } else {
+            R b = dot(d1, d2);
+            R denom = a * e - b * b;
+            s = (denom != R(0)) ? std::min(std::max((b * f - c * e) / denom, R(0)), R(1)) : R(0);
+            t = (b * s + f) / e;
+            if (t < R(0)) {
+                t = R(0);
+                s = std::min(std::max(-c / a, R(0)), R(1));
+            } else if (t > R(1)) {
+                t = R(1);
+                s = std::min(std::max((b - c) / a, R(0)), R(1));
+            }
+        }
+    }
+    c1 = p1 + d1 * s;
+    c2 = p2 + d2 * t;
+}
+
+template <class R> struct ContactGeom {
+    V3<R> world1, world2, normal;
+    R depth;
+};
+
+// ContactKinematic::contact restated for the Point / Segment / Plane
+// approximations (ncollide3d query::ContactKinematic, called at
+// src/solver/nonlinear_sor_prox.rs:221-229). `n0` is the world default
+// normal (from collider 1 toward collider 2), used when the feature
+// points coincide and to orient point/segment normals.
+template <class R>
+inline ContactGeom<R> kinematic_contact(const Approx<R>& a1, const Iso<R>& m1, R dil1, const Approx<R>& a2,
+                                        const Iso<R>& m2, R dil2, V3<R> n0) {
+    V3<R> q1, q2, n;
+    R s;
+    if (a1.kind == AP_PLANE && a2.kind == AP_POINT) {
+        n = qrot(m1.q, a1.b);
+        V3<R> p1 = iso_pt(m1, a1.a);
+        V3<R> p2 = iso_pt(m2, a2.a);
+        s = dot(p2 - p1, n);
+        q1 = p2 - n * s;
+        q2 = p2;
+    } else if (a1.kind == AP_POINT && a2.kind == AP_PLANE) {
+        V3<R> n2 = qrot(m2.q, a2.b);
+        V3<R> p1 = iso_pt(m1, a1.a);
+        V3<R> p2 = iso_pt(m2, a2.a);
+        s = dot(p1 - p2, n2);
+        q1 = p1;
+        q2 = p1 - n2 * s;
+        n = -n2;
+    } else {
+        V3<R> s1a = iso_pt(m1, a1.a);
+        V3<R> s1b = (a1.kind == AP_SEGMENT) ? iso_pt(m1, a1.b) : s1a;
+        V3<R> s2a = iso_pt(m2, a2.a);
+        V3<R> s2b = (a2.kind == AP_SEGMENT) ? iso_pt(m2, a2.b) : s2a;
+        closest_segment_segment(s1a, s1b, s2a, s2b, q1, q2);
+        V3<R> v = q2 - q1;
+        R l2 = dot(v, v);
+        const R eps = std::numeric_limits<R>::epsilon();
+        if (l2 > eps * eps) {
+            R l = std::sqrt(l2);
+            n = vdiv(v, l);
+            s = l;
+            if (dot(n, n0) < R(0)) {
+                n = -n;
+                s = -l;
+            }
+        } else {
+            n = n0;
+            s = R(0);
+        }
+    }
+    ContactGeom<R> g;
+    g.world1 = q1 + n * dil1;
+    g.world2 = q2 - n * dil2;
+    g.normal = n;
+    g.depth = (dil1 + dil2) - s;
+    return g;
+}
+
+template <class R> struct Body {
+    bool alive = false;
+    uint64_t generation = 0;
+    uint32_t status = NPGPU_BODY_DYNAMIC, kind = NPGPU_KIND_RIGID_BODY, flags = 0, world = 0;
+    Iso<R> pos;
+    V3<R> lin, ang;                 // velocity
+    Inertia<R> local_inertia, inertia, aug, inv_aug;
+    V3<R> local_com, com;
+    V3<R> acc_lin, acc_ang;         // generalized acceleration
+    V3<R> f_lin, f_ang;             // external forces
+    R lin_damp, ang_damp, max_lin, max_ang;
+    R sleep_threshold;
+    bool can_sleep = true;
+    R energy;
+    R mask[6];
+    bool changed = true;            // BodyUpdateStatus::inertia_needs_update / colliders_need_update
+    bool in_island = false;
+    bool dynamic() const { return status == NPGPU_BODY_DYNAMIC; }
+    bool kinematic() const { return status == NPGPU_BODY_KINEMATIC; }
+    int ndofs() const { return dynamic() ? 6 : 0; }
+    bool is_active() const {   // Body::is_active (src/object/body.rs:296-304)
+        if (status == NPGPU_BODY_DYNAMIC) return energy != R(0);
+        return status == NPGPU_BODY_KINEMATIC;
+    }
+};
+
+template <class R> struct Collider {
+    bool alive = false;
+    bool registered = false;   // mass added to the body (maintain ran)
+    uint64_t generation = 0;
+    uint32_t body = 0;
+    Iso<R> pos_wrt_body, pose;
+    uint32_t shape = NPGPU_SHAPE_BALL;
+    V3<R> half;                 // cuboid half extents
+    R radius = R(0);
+    R margin, density, linear_prediction, friction, restitution;
+    uint32_t friction_combine = 0, restitution_combine = 0;
+    R aabb_min[3], aabb_max[3];   // fat AABB
+    bool has_fat = false;
+    R query_limit() const { return margin + linear_prediction; }
+    R dilation() const { return shape == NPGPU_SHAPE_BALL ? radius : R(0); }
+};
+
+template <class R> struct MContact {
+    ContactGeom<R> g;
+    int fid1, fid2;
+    V3<R> normal1_local;   // contact normal in body 1's frame (signorini_model.rs:174)
+    R impulse[3];          // ImpulseCache entry (normal, tangent1, tangent2)
+    uint32_t key() const { return uint32_t(fid1 * 26 + fid2); }
+};
+
+template <class R> struct Manifold {
+    uint32_t c1, c2;
+    std::vector<MContact<R>> contacts;
+    uint32_t colour = 0xffffffffu;
+    bool in_solver = false;
+};
+
+template <class R> struct Row {
+    R impulse, r, rhs;
+    int b1, b2;            // dynamic body slots, -1 when the side has no dofs
+    R J1[6], J2[6], WJ1[6], WJ2[6];
+    int dep;               // friction: index of its normal row
+    R mu;
+    bool friction;
+    void* cache;           // MContact the impulse is cached to
+    int cache_slot;
+};
+
+template <class R> struct PosConstraint {
+    uint32_t c1, c2;
+    int fid1, fid2;
+    V3<R> normal1_local;
+};
+
+template <class R> class World {
+public:
+    npgpu_params params;
+    V3<R> gravity;
+    std::vector<Body<R>> bodies;
+    std::vector<Collider<R>> colliders;
+    std::map<uint64_t, Manifold<R>> manifolds;   // every broad-phase pair, keyed (c1 << 32) | c2
+    std::vector<uint64_t> pairs;                  // sorted broad-phase pair set
+    int order = ORDER_REFERENCE;
+    npgpu_counters counters;
+    std::string last_error;
+    bool cd_dirty = true;
+    uint32_t num_colours = 0;
+
+    World(const npgpu_params& p, const float g[3]) : params(p) {
+        gravity = v3<R>(R(g[0]), R(g[1]), R(g[2]));
+        std::memset(&counters, 0, sizeof(counters));
+    }
+
+    // ---------------------------------------------------------------- host API
+    npgpu_status fail(npgpu_status s, const std::string& m) {
+        last_error = m;
+        return s;
+    }
+
+    npgpu_status upsert_body(const npgpu_handle& h, const npgpu_body_desc& d) {
+        if (d.kind != NPGPU_KIND_RIGID_BODY && d.kind != NPGPU_KIND_GROUND)
+            return fail(NPGPU_ERR_UNSUPPORTED_BODY, "only rigid bodies and grounds are supported");
+        if (h.index >= (1u << 21)) return fail(NPGPU_ERR_CAPACITY, "body index too large");
+        if (h.index >= bodies.size()) bodies.resize(h.index + 1);
+        Body<R>& b = bodies[h.index];
+        bool existed = b.alive;
+        b.alive = true;
+        b.generation = h.generation;
+        b.kind = d.kind;
+        b.status = (d.kind == NPGPU_KIND_GROUND) ? NPGPU_BODY_STATIC : d.status;
+        b.flags = d.flags;
+        b.world = d.world;
+        b.pos.t = v3<R>(R(d.position[0]), R(d.position[1]), R(d.position[2]));
+        b.pos.q = Quat<R>{R(d.position[3]), R(d.position[4]), R(d.position[5]), R(d.position[6])};
+        b.lin = v3<R>(R(d.velocity[0]), R(d.velocity[1]), R(d.velocity[2]));
+        b.ang = v3<R>(R(d.velocity[3]), R(d.velocity[4]), R(d.velocity[5]));
+        if (d.kind == NPGPU_KIND_GROUND) {
+            b.pos = iso_identity<R>();
+            b.lin = b.ang = v3<R>(R(0), R(0), R(0));
+        }
+        if (!existed) {
+            // RigidBody::new + RigidBodyDesc::build (rigid_body.rs:54-83, 1064-1084).
+            b.local_inertia.linear = R(d.local_inertia[0]);
+            M3<R> a = mzero<R>();
+            a.m[0][0] = R(d.local_inertia[1]); a.m[0][1] = a.m[1][0] = R(d.local_inertia[2]);
+            a.m[0][2] = a.m[2][0] = R(d.local_inertia[3]); a.m[1][1] = R(d.local_inertia[4]);
+            a.m[1][2] = a.m[2][1] = R(d.local_inertia[5]); a.m[2][2] = R(d.local_inertia[6]);
+            b.local_inertia.angular = a;
+            b.local_com = v3<R>(R(d.local_com[0]), R(d.local_com[1]), R(d.local_com[2]));
+            b.acc_lin = b.acc_ang = v3<R>(R(0), R(0), R(0));
+            b.f_lin = b.f_ang = v3<R>(R(0), R(0), R(0));
+            // ActivationStatus::new_active (body.rs:79-84) uses the default threshold 0.01
+            // whatever threshold is set afterwards; a ground starts inactive (ground.rs:24).
+            b.energy = (d.kind == NPGPU_KIND_GROUND) ? R(0) : R(0.01) * R(4);
+        }
+        b.com = iso_pt(b.pos, b.local_com);
+        update_inertia_from_local_inertia(b);
+        b.lin_damp = R(d.linear_damping);
+        b.ang_damp = R(d.angular_damping);
+        b.max_lin = R(d.max_linear_velocity);
+        b.max_ang = R(d.max_angular_velocity);
+        b.sleep_threshold = R(d.sleep_threshold);
+        b.can_sleep = (d.flags & NPGPU_BODY_CAN_SLEEP) != 0;
+        for (int k = 0; k < 6; ++k) b.mask[k] = (d.flags & (NPGPU_BODY_LOCK_TX << k)) ? R(0) : R(1);
+        b.changed = true;
+        cd_dirty = true;
+        return NPGPU_OK;
+    }
+
+    npgpu_status upsert_collider(const npgpu_handle& h, const npgpu_collider_desc& d) {
+        if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID)
+            return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "only balls and cuboids are supported");
+        if (d.is_sensor) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "sensors are not supported");
+        if (d.ccd_enabled) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "CCD colliders are not supported");
+        if (d.body.index >= bodies.size() || !bodies[d.body.index].alive ||
+            bodies[d.body.index].generation != d.body.generation)
+            return fail(NPGPU_ERR_INVALID_HANDLE, "collider parent body handle is invalid");
+        if (h.index >= (1u << 21)) return fail(NPGPU_ERR_CAPACITY, "collider index too large");
+        if (h.index >= colliders.size()) colliders.resize(h.index + 1);
+        Collider<R>& c = colliders[h.index];
+        if (c.alive && c.registered) remove_collider_mass(c);
+        c = Collider<R>();
+        c.alive = true;
+        c.generation = h.generation;
+        c.body = uint32_t(d.body.index);
+        c.pos_wrt_body.t = v3<R>(R(d.position_wrt_body[0]), R(d.position_wrt_body[1]), R(d.position_wrt_body[2]));
+        c.pos_wrt_body.q = Quat<R>{R(d.position_wrt_body[3]), R(d.position_wrt_body[4]), R(d.position_wrt_body[5]),
+                                   R(d.position_wrt_body[6])};
+        c.shape = d.shape;
+        c.radius = R(d.shape_params[0]);
+        c.half = v3<R>(R(d.shape_params[0]), R(d.shape_params[1]), R(d.shape_params[2]));
+        c.margin = R(d.margin);
+        c.density = R(d.density);
+        c.linear_prediction = R(d.linear_prediction);
+        c.friction = R(d.friction);
+        c.restitution = R(d.restitution);
+        c.friction_combine = d.friction_combine;
+        c.restitution_combine = d.restitution_combine;
+        // Drop manifolds involving the replaced collider.
+        drop_manifolds_of(uint32_t(h.index));
+        cd_dirty = true;
+        return NPGPU_OK;
+    }
+
+    npgpu_status remove_body(const npgpu_handle& h) {
+        if (h.index >= bodies.size() || !bodies[h.index].alive || bodies[h.index].generation != h.generation)
+            return fail(NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
+        // Removing a body removes its colliders (mechanical_world.rs:130-139).
+        for (size_t i = 0; i < colliders.size(); ++i)
+            if (colliders[i].alive && colliders[i].body == h.index) remove_collider_slot(uint32_t(i), false);
+        bodies[h.index].alive = false;
+        cd_dirty = true;
+        return NPGPU_OK;
+    }
+
+    npgpu_status remove_collider(const npgpu_handle& h) {
+        if (h.index >= colliders.size() || !colliders[h.index].alive || colliders[h.index].generation != h.generation)
+            return fail(NPGPU_ERR_INVALID_HANDLE, "invalid collider handle");
+        remove_collider_slot(uint32_t(h.index), true);
+        cd_dirty = true;
+        return NPGPU_OK;
+    }
+
+    npgpu_status apply_force(const npgpu_handle& h, const float* f, bool wake) {
+        if (h.index >= bodies.size() || !bodies[h.index].alive || bodies[h.index].generation != h.generation)
+            return fail(NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
+        Body<R>& b = bodies[h.index];
+        // RigidBody::apply_force, ForceType::Force (rigid_body.rs:771-792).
+        if (b.status != NPGPU_BODY_DYNAMIC) return NPGPU_OK;
+        if (wake) activate(b);
+        b.f_lin = b.f_lin + v3<R>(R(f[0]) * b.mask[0], R(f[1]) * b.mask[1], R(f[2]) * b.mask[2]);
+        b.f_ang = b.f_ang + v3<R>(R(f[3]) * b.mask[3], R(f[4]) * b.mask[4], R(f[5]) * b.mask[5]);
+        return NPGPU_OK;
+    }
+
+    // ------------------------------------------------------- body dynamics
+    static void activate(Body<R>& b) {   // Body::activate (body.rs:335-340)
+        if (b.can_sleep) b.energy = b.sleep_threshold * R(2);
+    }
+    static void deactivate(Body<R>& b) {   // RigidBody::deactivate (rigid_body.rs:396-400)
+        b.changed = false;
+        b.energy = R(0);
+        b.lin = b.ang = v3<R>(R(0), R(0), R(0));
+    }
+    // Inertia3::transformed (inertia3.rs:68-71): R I R^-1.
+    static Inertia<R> transformed(const Inertia<R>& in, const Quat<R>& q) {
+        M3<R> rot = qmat(q);
+        Inertia<R> r;
+        r.linear = in.linear;
+        r.angular = mm(mm(rot, in.angular), mtr(rot));
+        return r;
+    }
+    static Inertia<R> inverse(const Inertia<R>& in) {   // inertia3.rs:75-86
+        Inertia<R> r;
+        r.linear = (in.linear == R(0)) ? R(0) : R(1) / in.linear;
+        r.angular = minv_or_zero(in.angular);
+        return r;
+    }
+    static void update_inertia_from_local_inertia(Body<R>& b) {   // rigid_body.rs:266-271
+        b.inertia = transformed(b.local_inertia, b.pos.q);
+        b.aug = b.inertia;
+        b.inv_aug = inverse(b.inertia);
+    }
+    // RigidBody::add_local_inertia_and_com (rigid_body.rs:747-766).
+    static void add_local_inertia_and_com(Body<R>& b, V3<R> com, const Inertia<R>& in) {
+        R mass_sum = b.inertia.linear + in.linear;
+        if (mass_sum != R(0)) {
+            b.local_com = vdiv(b.local_com * b.inertia.linear + com * in.linear, mass_sum);
+            b.com = iso_pt(b.pos, b.local_com);
+        } else {
+            b.local_com = v3<R>(R(0), R(0), R(0));
+            b.com = b.pos.t;
+        }
+        b.local_inertia.linear = b.local_inertia.linear + in.linear;
+        b.local_inertia.angular = madd(b.local_inertia.angular, in.angular);
+        update_inertia_from_local_inertia(b);
+        b.changed = true;
+    }
+    // Volumetric::transformed_mass_properties (volumetric.rs:55-59) for Ball
+    // (volumetric_ball.rs:8-47) and Cuboid (volumetric_cuboid.rs:9-78).
+    static void mass_properties(const Collider<R>& c, V3<R>& com, Inertia<R>& in) {
+        const R pi = R(3.14159265358979323846);
+        R mass;
+        M3<R> unit = mzero<R>();
+        if (c.shape == NPGPU_SHAPE_BALL) {
+            R r = c.radius;
+            R vol = pi * r * r * r * R(4.0 / 3.0);
+            mass = vol * c.density;
+            R diag = r * r * R(2.0 / 5.0);
+            unit.m[0][0] = unit.m[1][1] = unit.m[2][2] = diag;
+        } else {
+            R vol = R(1);
+            vol = vol * c.half.x * R(2);
+            vol = vol * c.half.y * R(2);
+            vol = vol * c.half.z * R(2);
+            mass = vol * c.density;
+            R w = R(1.0 / 12.0) * R(2) * R(2);
+            R ix = w * c.half.x * c.half.x, iy = w * c.half.y * c.half.y, iz = w * c.half.z * c.half.z;
+            unit.m[0][0] = iy + iz;
+            unit.m[1][1] = ix + iz;
+            unit.m[2][2] = ix + iy;
+        }
+        Inertia<R> local;
+        local.linear = mass;
+        local.angular = mscale(unit, mass);
+        com = iso_pt(c.pos_wrt_body, v3<R>(R(0), R(0), R(0)));
+        in = transformed(local, c.pos_wrt_body.q);
+    }
+    void remove_collider_mass(Collider<R>& c) {
+        Body<R>& b = bodies[c.body];
+        if (!b.alive) return;
+        if (c.density != R(0) && b.kind == NPGPU_KIND_RIGID_BODY) {
+            V3<R> com;
+            Inertia<R> in;
+            mass_properties(c, com, in);
+            Inertia<R> neg;
+            neg.linear = -in.linear;
+            neg.angular = mscale(in.angular, R(-1));
+            add_local_inertia_and_com(b, -com, neg);
+        }
+        activate(b);
+    }
+    void drop_manifolds_of(uint32_t ci) {
+        for (auto it = manifolds.begin(); it != manifolds.end();) {
+            if (it->second.c1 == ci || it->second.c2 == ci) it = manifolds.erase(it);
+            else ++it;
+        }
+    }
+    // GeometricalWorld::handle_removals (geometrical_world.rs:145-227).
+    void remove_collider_slot(uint32_t ci, bool body_remains) {
+        Collider<R>& c = colliders[ci];
+        for (auto& kv : manifolds) {
+            Manifold<R>& m = kv.second;
+            if (m.contacts.empty()) continue;
+            uint32_t other = (m.c1 == ci) ? m.c2 : ((m.c2 == ci) ? m.c1 : 0xffffffffu);
+            if (other != 0xffffffffu) activate(bodies[colliders[other].body]);
+        }
+        if (body_remains && c.registered) remove_collider_mass(c);
+        drop_manifolds_of(ci);
+        c.alive = false;
+    }
+
+    // RigidBody::update_dynamics (rigid_body.rs:558-588).
+    void update_dynamics(Body<R>& b, R dt) {
+        if (!b.changed || b.status != NPGPU_BODY_DYNAMIC) return;
+        if (!b.is_active()) activate(b);
+        b.inertia = transformed(b.local_inertia, b.pos.q);
+        b.aug = b.inertia;
+        const M3<R>& i = b.inertia.angular;
+        V3<R> w = b.ang;
+        V3<R> iw = mv(i, w);
+        V3<R> w_dt = w * dt;
+        M3<R> w_dt_cross = cross_matrix(w_dt);
+        M3<R> iw_dt_cross = cross_matrix(iw * dt);
+        b.aug.angular = madd(b.aug.angular, msub(mm(w_dt_cross, i), iw_dt_cross));
+        b.inv_aug = inverse(b.aug);
+    }
+    // RigidBody::update_acceleration (rigid_body.rs:590-619).
+    void update_acceleration(Body<R>& b) {
+        b.acc_lin = b.acc_ang = v3<R>(R(0), R(0), R(0));
+        if (b.status != NPGPU_BODY_DYNAMIC) return;
+        V3<R> iw = mv(b.inertia.angular, b.ang);
+        V3<R> gyro = -cross(b.ang, iw);
+        b.acc_ang = mv(b.inv_aug.angular, gyro);
+        if (b.inv_aug.linear != R(0) && (b.flags & NPGPU_BODY_GRAVITY)) b.acc_lin = gravity;
+        b.acc_lin = b.acc_lin + b.f_lin * b.inv_aug.linear;
+        b.acc_ang = b.acc_ang + mv(b.inv_aug.angular, b.f_ang);
+        b.acc_lin = v3<R>(b.acc_lin.x * b.mask[0], b.acc_lin.y * b.mask[1], b.acc_lin.z * b.mask[2]);
+        b.acc_ang = v3<R>(b.acc_ang.x * b.mask[3], b.acc_ang.y * b.mask[4], b.acc_ang.z * b.mask[5]);
+    }
+    // RigidBody::apply_displacement (rigid_body.rs:371-381) and set_position (:297-307).
+    static void apply_displacement(Body<R>& b, V3<R> dlin, V3<R> dang) {
+        Quat<R> qd = qexp_scaled_axis(dang);
+        // shift * disp * shift^-1 with shift = Translation(com).
+        V3<R> t = (b.com + dlin) + qrot(qd, -b.com);
+        Iso<R> np;
+        np.t = t + qrot(qd, b.pos.t);
+        np.q = qmul(qd, b.pos.q);
+        b.pos = np;
+        b.com = iso_pt(b.pos, b.local_com);
+        b.changed = true;
+    }
+    // RigidBody::integrate (rigid_body.rs:467-505).
+    void integrate(Body<R>& b) {
+        R dt = R(params.dt);
+        b.lin = b.lin * (R(1) / (R(1) + dt * b.lin_damp));
+        b.ang = b.ang * (R(1) / (R(1) + dt * b.ang_damp));
+        R ln = norm(b.lin);
+        if (ln > b.max_lin) {
+            if (b.max_lin == R(0)) b.lin = v3<R>(R(0), R(0), R(0));
+            else b.lin = b.lin * (b.max_lin / ln);
+        }
+        R an = norm(b.ang);
+        if (an > b.max_ang) {
+            if (b.max_ang == R(0)) b.ang = v3<R>(R(0), R(0), R(0));
+            else b.ang = b.ang * (b.max_ang / an);
+        }
+        apply_displacement(b, b.lin * dt, b.ang * dt);
+    }
+
+    // ------------------------------------------------------- collision detection
+    void collider_aabb(const Collider<R>& c, R mn[3], R mx[3]) const {
+        // Shape AABB at the collider pose (ncollide3d bounding_volume), loosened by
+        // the query limit margin + linear prediction (collider.rs:542-549).
+        V3<R> ctr = c.pose.t;
+        V3<R> half;
+        if (c.shape == NPGPU_SHAPE_BALL) {
+            half = v3<R>(c.radius, c.radius, c.radius);
+        } else {
+            M3<R> rot = qmat(c.pose.q);
+            for (int a = 0; a < 3; ++a) {
+                R s = std::fabs(rot.m[a][0]) * c.half.x + std::fabs(rot.m[a][1]) * c.half.y +
+                      std::fabs(rot.m[a][2]) * c.half.z;
+                setc(half, a, s);
+            }
+        }
+        R ql = c.query_limit();
+        for (int a = 0; a < 3; ++a) {
+            mn[a] = (comp(ctr, a) - comp(half, a)) - ql;
+            mx[a] = (comp(ctr, a) + comp(half, a)) + ql;
+        }
+    }
+    // sync_colliders (geometrical_world.rs:230-265) + the DBVT proxy update:
+    // the fat AABB is the tight one loosened by the broad-phase margin, and is
+    // replaced only when the tight AABB leaves it.
+    void sync_colliders() {
+        R margin = R(params.broad_phase_margin);
+        for (auto& c : colliders) {
+            if (!c.alive) continue;
+            const Body<R>& b = bodies[c.body];
+            c.pose = iso_mul(b.pos, c.pos_wrt_body);
+            R mn[3], mx[3];
+            collider_aabb(c, mn, mx);
+            bool inside = c.has_fat;
+            for (int a = 0; a < 3 && inside; ++a)
+                if (!(c.aabb_min[a] <= mn[a] && mx[a] <= c.aabb_max[a])) inside = false;
+            if (!inside) {
+                for (int a = 0; a < 3; ++a) {
+                    c.aabb_min[a] = mn[a] - margin;
+                    c.aabb_max[a] = mx[a] + margin;
+                }
+                c.has_fat = true;
+            }
+        }
+    }
+    static bool aabb_overlap(const Collider<R>& a, const Collider<R>& b) {
+        for (int k = 0; k < 3; ++k)
+            if (!(a.aabb_min[k] <= b.aabb_max[k] && b.aabb_min[k] <= a.aabb_max[k])) return false;
+        return true;
+    }
+    // DefaultCollisionFilter (geometrical_world.rs:926-970) + one world per batch entry.
+    bool pair_allowed(uint32_t i, uint32_t j) const {
+        const Collider<R>& a = colliders[i];
+        const Collider<R>& b = colliders[j];
+        if (a.body == b.body) return false;
+        const Body<R>& ba = bodies[a.body];
+        const Body<R>& bb = bodies[b.body];
+        if (ba.world != bb.world) return false;
+        return ba.ndofs() != 0 || bb.ndofs() != 0;
+    }
+    // Broad phase: the set of allowed pairs whose fat AABBs intersect, found by
+    // sweep-and-prune along x (the set equals the brute-force one).
+    void broad_phase() {
+        std::vector<uint32_t> idx;
+        for (uint32_t i = 0; i < colliders.size(); ++i)
+            if (colliders[i].alive) idx.push_back(i);
+        std::sort(idx.begin(), idx.end(), [&](uint32_t a, uint32_t b) {
+            if (colliders[a].aabb_min[0] != colliders[b].aabb_min[0])
+                return colliders[a].aabb_min[0] < colliders[b].aabb_min[0];
+            return a < b;
+        });
+        pairs.clear();
+        for (size_t s = 0; s < idx.size(); ++s) {
+            const Collider<R>& a = colliders[idx[s]];
+            for (size_t t = s + 1; t < idx.size(); ++t) {
+                const Collider<R>& b = colliders[idx[t]];
+                if (b.aabb_min[0] > a.aabb_max[0]) break;
+                if (!aabb_overlap(a, b)) continue;
+                uint32_t i = std::min(idx[s], idx[t]), j = std::max(idx[s], idx[t]);
+                if (!pair_allowed(i, j)) continue;
+                pairs.push_back((uint64_t(i) << 32) | j);
+            }
+        }
+        std::sort(pairs.begin(), pairs.end());
+    }
+    std::vector<uint64_t> broad_phase_brute_force() const {
+        std::vector<uint64_t> out;
+        for (uint32_t i = 0; i < colliders.size(); ++i) {
+            if (!colliders[i].alive) continue;
+            for (uint32_t j = i + 1; j < colliders.size(); ++j) {
+                if (!colliders[j].alive) continue;
+                if (aabb_overlap(colliders[i], colliders[j]) && pair_allowed(i, j)) out.push_back((uint64_t(i) << 32) | j);
+            }
+        }
+        return out;
+    }
+
+    Approx<R> feature(const Collider<R>& c, int fid) const {
+        if (c.shape == NPGPU_SHAPE_BALL) {
+            Approx<R> ap;
+            ap.kind = AP_POINT;
+            ap.a = ap.b = v3<R>(R(0), R(0), R(0));
+            return ap;
+        }
+        return box_feature(c.half, fid);
+    }
+
+    // Candidate contact: features + default normal; evaluated by kinematic_contact.
+    struct Cand {
+        int fid1, fid2;
+        ContactGeom<R> g;
+    };
+
+    void push_eval(std::vector<Cand>& out, const Collider<R>& c1, const Collider<R>& c2, int f1, int f2, V3<R> n0,
+                   R prediction) const {
+        ContactGeom<R> g = kinematic_contact(feature(c1, f1), c1.pose, c1.dilation(), feature(c2, f2), c2.pose,
+                                             c2.dilation(), n0);
+        if (g.depth >= -prediction) out.push_back(Cand{f1, f2, g});
+    }
+
+    // Ball-cuboid: closest point of the cuboid to the ball center.
+    void ball_box(const Collider<R>& cb, const Collider<R>& cx, bool box_first, R prediction, std::vector<Cand>& out) const {
+        V3<R> c = iso_inv_pt(cx.pose, cb.pose.t);
+        V3<R> h = cx.half;
+        int sign[3], nclamped = 0;
+        V3<R> p = c;
+        for (int k = 0; k < 3; ++k) {
+            R ck = comp(c, k), hk = comp(h, k);
+            if (ck > hk) { sign[k] = 1; setc(p, k, hk); ++nclamped; }
+            else if (ck < -hk) { sign[k] = -1; setc(p, k, -hk); ++nclamped; }
+            else sign[k] = 0;
+        }
+        int fid;
+        V3<R> nl;
+        if (nclamped == 0) {
+            int best = 0;
+            R bd = comp(h, 0) - std::fabs(comp(c, 0));
+            for (int k = 1; k < 3; ++k) {
+                R dk = comp(h, k) - std::fabs(comp(c, k));
+                if (dk < bd) { bd = dk; best = k; }
+            }
+            int pos = comp(c, best) >= R(0) ? 1 : 0;
+            fid = box_face_id(best, pos);
+            nl = v3<R>(R(0), R(0), R(0));
+            setc(nl, best, pos ? R(1) : R(-1));
+        } else {
+            if (nclamped == 1) {
+                int k = sign[0] ? 0 : (sign[1] ? 1 : 2);
+                fid = box_face_id(k, sign[k] > 0 ? 1 : 0);
+            } else if (nclamped == 2) {
+                int a = !sign[0] ? 0 : (!sign[1] ? 1 : 2), o1, o2;
+                edge_other_axes(a, o1, o2);
+                fid = box_edge_id(a, sign[o1] > 0 ? 1 : 0, sign[o2] > 0 ? 1 : 0);
+            } else {
+                fid = box_vertex_id(sign[0] > 0, sign[1] > 0, sign[2] > 0);
+            }
+            V3<R> v = c - p;
+            nl = vdiv(v, norm(v));
+        }
+        V3<R> n = qrot(cx.pose.q, nl);   // from the cuboid toward the ball
+        if (box_first) push_eval(out, cx, cb, fid, 0, n, prediction);
+        else push_eval(out, cb, cx, 0, fid, -n, prediction);
+    }
+
+    // Cuboid-cuboid: SAT over the 15 axes, then clipping of the incident face
+    // against the reference face (Sutherland-Hodgman) with feature tracking.
+    void box_box(const Collider<R>& A, const Collider<R>& B, R prediction, std::vector<Cand>& out) const {
+        M3<R> RA = qmat(A.pose.q), RB = qmat(B.pose.q);
+        V3<R> axA[3] = {mcol(RA, 0), mcol(RA, 1), mcol(RA, 2)};
+        V3<R> axB[3] = {mcol(RB, 0), mcol(RB, 1), mcol(RB, 2)};
+        V3<R> d = B.pose.t - A.pose.t;
+        R sepA = -std::numeric_limits<R>::max(), sepB = sepA, sepE = sepA;
+        int ia = 0, ib = 0, ea = -1, eb = -1;
+        V3<R> LE = v3<R>(R(0), R(0), R(0));
+        for (int i = 0; i < 3; ++i) {
+            V3<R> L = axA[i];
+            R rb = comp(B.half, 0) * std::fabs(dot(axB[0], L)) + comp(B.half, 1) * std::fabs(dot(axB[1], L)) +
+                   comp(B.half, 2) * std::fabs(dot(axB[2], L));
+            R sep = std::fabs(dot(d, L)) - (comp(A.half, i) + rb);
+            if (sep > prediction) return;
+            if (sep > sepA) { sepA = sep; ia = i; }
+        }
+        for (int j = 0; j < 3; ++j) {
+            V3<R> L = axB[j];
+            R ra = comp(A.half, 0) * std::fabs(dot(axA[0], L)) + comp(A.half, 1) * std::fabs(dot(axA[1], L)) +
+                   comp(A.half, 2) * std::fabs(dot(axA[2], L));
+            R sep = std::fabs(dot(d, L)) - (ra + comp(B.half, j));
+            if (sep > prediction) return;
+            if (sep > sepB) { sepB = sep; ib = j; }
+        }
+        for (int i = 0; i < 3; ++i) {
+            for (int j = 0; j < 3; ++j) {
+                V3<R> L = cross(axA[i], axB[j]);
+                R len = norm(L);
+                if (len < R(1e-5)) continue;
+                L = vdiv(L, len);
+                R ra = comp(A.half, 0) * std::fabs(dot(axA[0], L)) + comp(A.half, 1) * std::fabs(dot(axA[1], L)) +
+                       comp(A.half, 2) * std::fabs(dot(axA[2], L));
+                R rb = comp(B.half, 0) * std::fabs(dot(axB[0], L)) + comp(B.half, 1) * std::fabs(dot(axB[1], L)) +
+                       comp(B.half, 2) * std::fabs(dot(axB[2], L));
+                R sep = std::fabs(dot(d, L)) - (ra + rb);
+                if (sep > prediction) return;
+                if (sep > sepE) { sepE = sep; ea = i; eb = j; LE = L; }
+            }
+        }
+        bool refA = !(sepB > sepA + R(1e-4));
+        R sepF = refA ? sepA : sepB;
+        if (ea >= 0 && sepE > sepF + R(5e-3)) {
+            // Edge-edge: supporting edges along L (oriented from A to B).
+            V3<R> L = LE;
+            if (dot(d, L) < R(0)) L = -L;
+            int o1, o2;
+            edge_other_axes(ea, o1, o2);
+            int fa = box_edge_id(ea, dot(axA[o1], L) > R(0) ? 1 : 0, dot(axA[o2], L) > R(0) ? 1 : 0);
+            edge_other_axes(eb, o1, o2);
+            int fb = box_edge_id(eb, dot(axB[o1], L) < R(0) ? 1 : 0, dot(axB[o2], L) < R(0) ? 1 : 0);
+            push_eval(out, A, B, fa, fb, L, prediction);
+            return;
+        }
+        const Collider<R>& Rf = refA ? A : B;
+        const Collider<R>& In = refA ? B : A;
+        V3<R>* axR = refA ? axA : axB;
+        V3<R>* axI = refA ? axB : axA;
+        int ri = refA ? ia : ib;
+        V3<R> dRI = refA ? d : -d;
+        int rpos = dot(dRI, axR[ri]) >= R(0) ? 1 : 0;
+        V3<R> nref = rpos ? axR[ri] : -axR[ri];
+        int ik = 0;
+        R best = std::fabs(dot(axI[0], nref));
+        for (int k = 1; k < 3; ++k) {
+            R v = std::fabs(dot(axI[k], nref));
+            if (v > best) { best = v; ik = k; }
+        }
+        int ipos = dot(axI[ik], nref) < R(0) ? 1 : 0;
+        int ref_face = box_face_id(ri, rpos), inc_face = box_face_id(ik, ipos);
+        // Incident face polygon (vertex ids), in the reference box's local frame.
+        int u = (ik + 1) % 3, v = (ik + 2) % 3;
+        int vids[4];
+        int su[4] = {0, 1, 1, 0}, sv[4] = {0, 0, 1, 1};
+        struct PV { V3<R> p; int tag, a, b; int esrc; };   // tag 0: inc vertex a; 1: edge-edge (ref a, inc b); 2: ref vertex a
+        // esrc >= 0: incident edge id; esrc < 0: -(1 + reference side plane)
+        std::vector<PV> poly, next;
+        for (int k = 0; k < 4; ++k) {
+            int s[3];
+            s[ik] = ipos;
+            s[u] = su[k];
+            s[v] = sv[k];
+            vids[k] = box_vertex_id(s[0], s[1], s[2]);
+        }
+        for (int k = 0; k < 4; ++k) {
+            int a = vids[k], b = vids[(k + 1) % 4];
+            int diff = a ^ b, axis = diff == 1 ? 0 : (diff == 2 ? 1 : 2), o1, o2;
+            edge_other_axes(axis, o1, o2);
+            int eid = box_edge_id(axis, (a >> o1) & 1, (a >> o2) & 1);
+            Approx<R> ap = box_feature(In.half, a);
+            V3<R> w = iso_pt(In.pose, ap.a);
+            PV pv;
+            pv.p = iso_inv_pt(Rf.pose, w);
+            pv.tag = 0; pv.a = a; pv.b = -1; pv.esrc = eid;
+            poly.push_back(pv);
+        }
+        int ru = (ri + 1) % 3, rv = (ri + 2) % 3;
+        int planes_axis[4] = {ru, ru, rv, rv};
+        int planes_pos[4] = {1, 0, 1, 0};
+        for (int pl = 0; pl < 4 && !poly.empty(); ++pl) {
+            int ax = planes_axis[pl], pp = planes_pos[pl];
+            R hc = comp(Rf.half, ax);
+            next.clear();
+            size_t n = poly.size();
+            for (size_t k = 0; k < n; ++k) {
+                const PV& P = poly[k];
+                const PV& Q = poly[(k + 1) % n];
+                R dp = (pp ? comp(P.p, ax) : -comp(P.p, ax)) - hc;
+                R dq = (pp ? comp(Q.p, ax) : -comp(Q.p, ax)) - hc;
+                bool pin = dp <= R(0), qin = dq <= R(0);
+                if (pin) next.push_back(P);
+                if (pin != qin) {
+                    R t = dp / (dp - dq);
+                    PV X;
+                    X.p = P.p + (Q.p - P.p) * t;
+                    // Reference edge lying on this side plane of the reference face.
+                    int third = 3 - ri - ax;
+                    int s[3];
+                    s[ri] = rpos;
+                    s[ax] = pp;
+                    if (P.esrc >= 0) {
+                        int o1, o2;
+                        edge_other_axes(third, o1, o2);
+                        X.tag = 1;
+                        X.a = box_edge_id(third, s[o1], s[o2]);
+                        X.b = P.esrc;
+                    } else {
+                        int other_plane = -P.esrc - 1;
+                        s[planes_axis[other_plane]] = planes_pos[other_plane];
+                        X.tag = 2;
+                        X.a = box_vertex_id(s[0], s[1], s[2]);
+                        X.b = -1;
+                    }
+                    if (pin) {
+                        // Exit point: the edge that follows runs along this side plane.
+                        if (!next.empty()) next.back().esrc = P.esrc;
+                        X.esrc = -(1 + pl);
+                    } else {
+                        X.esrc = P.esrc;
+                    }
+                    next.push_back(X);
+                }
+            }
+            poly.swap(next);
+        }
+        V3<R> n0 = refA ? nref : -nref;
+        std::vector<Cand> cands;
+        for (const PV& P : poly) {
+            int fr, fi;
+            if (P.tag == 0) { fr = ref_face; fi = P.a; }
+            else if (P.tag == 1) { fr = P.a; fi = P.b; }
+            else { fr = P.a; fi = inc_face; }
+            if (refA) push_eval(cands, A, B, fr, fi, n0, prediction);
+            else push_eval(cands, A, B, fi, fr, n0, prediction);
+        }
+        reduce4(cands, out);
+    }
+
+    // Keeps at most 4 contacts: the deepest, the farthest from it, the one
+    // spanning the largest triangle with both, and the one that grows that
+    // triangle most; the kept contacts stay in clipping order.
+    static void reduce4(std::vector<Cand>& c, std::vector<Cand>& out) {
+        size_t n = c.size();
+        if (n <= 4) {
+            for (auto& x : c) out.push_back(x);
+            return;
+        }
+        int i0 = 0;
+        for (size_t k = 1; k < n; ++k)
+            if (c[k].g.depth > c[i0].g.depth) i0 = int(k);
+        int i1 = -1;
+        R bd = R(-1);
+        for (size_t k = 0; k < n; ++k) {
+            if (int(k) == i0) continue;
+            R dd = norm2(c[k].g.world1 - c[i0].g.world1);
+            if (dd > bd) { bd = dd; i1 = int(k); }
+        }
+        int i2 = -1;
+        R ba = R(-1);
+        V3<R> e01 = c[i1].g.world1 - c[i0].g.world1;
+        for (size_t k = 0; k < n; ++k) {
+            if (int(k) == i0 || int(k) == i1) continue;
+            R aa = norm2(cross(e01, c[k].g.world1 - c[i0].g.world1));
+            if (aa > ba) { ba = aa; i2 = int(k); }
+        }
+        int i3 = -1;
+        R bs = R(-1);
+        V3<R> a = c[i0].g.world1, b = c[i1].g.world1, cc = c[i2].g.world1;
+        for (size_t k = 0; k < n; ++k) {
+            if (int(k) == i0 || int(k) == i1 || int(k) == i2) continue;
+            V3<R> x = c[k].g.world1;
+            R s = norm(cross(x - a, x - b)) + norm(cross(x - b, x - cc)) + norm(cross(x - cc, x - a));
+            if (s > bs) { bs = s; i3 = int(k); }
+        }
+        for (size_t k = 0; k < n; ++k)
+            if (int(k) == i0 || int(k) == i1 || int(k) == i2 || int(k) == i3) out.push_back(c[k]);
+    }
+
+    // One-shot manifold of a pair (c1 < c2). Contacts keep the impulses cached
+    // under the same feature key in the pair's previous manifold.
+    void narrow_pair(Manifold<R>& m) const {
+        const Collider<R>& a = colliders[m.c1];
+        const Collider<R>& b = colliders[m.c2];
+        R prediction = a.query_limit() + b.query_limit();
+        std::vector<Cand> cands;
+        if (a.shape == NPGPU_SHAPE_BALL && b.shape == NPGPU_SHAPE_BALL) {
+            V3<R> v = b.pose.t - a.pose.t;
+            R l2 = dot(v, v);
+            V3<R> n0 = l2 > R(0) ? vdiv(v, std::sqrt(l2)) : v3<R>(R(1), R(0), R(0));
+            push_eval(cands, a, b, 0, 0, n0, prediction);
+        } else if (a.shape == NPGPU_SHAPE_CUBOID && b.shape == NPGPU_SHAPE_BALL) {
+            ball_box(b, a, true, prediction, cands);
+        } else if (a.shape == NPGPU_SHAPE_BALL && b.shape == NPGPU_SHAPE_CUBOID) {
+            ball_box(a, b, false, prediction, cands);
+        } else {
+            box_box(a, b, prediction, cands);
+        }
+        std::vector<MContact<R>> nc;
+        const Body<R>& b1 = bodies[a.body];
+        for (const Cand& cd : cands) {
+            MContact<R> k;
+            k.g = cd.g;
+            k.fid1 = cd.fid1;
+            k.fid2 = cd.fid2;
+            k.normal1_local = qrot_inv(b1.pos.q, cd.g.normal);
+            k.impulse[0] = k.impulse[1] = k.impulse[2] = R(0);
+            for (const MContact<R>& old : m.contacts)
+                if (old.key() == k.key()) {
+                    k.impulse[0] = old.impulse[0];
+                    k.impulse[1] = old.impulse[1];
+                    k.impulse[2] = old.impulse[2];
+                    break;
+                }
+            nc.push_back(k);
+        }
+        m.contacts.swap(nc);
+    }
+
+    void collision_detection() {
+        sync_colliders();
+        broad_phase();
+        std::map<uint64_t, Manifold<R>> next;
+        for (uint64_t key : pairs) {
+            Manifold<R> m;
+            auto it = manifolds.find(key);
+            if (it != manifolds.end()) m = it->second;
+            m.c1 = uint32_t(key >> 32);
+            m.c2 = uint32_t(key & 0xffffffffu);
+            narrow_pair(m);
+            next[key] = m;
+        }
+        manifolds.swap(next);
+        cd_dirty = false;
+    }
+
+    // ------------------------------------------------------- activation
+    // ActivationManager::update (src/detection/activation_manager.rs:61-201)
+    // with the union-find of src/utils/union_find.rs.
+    std::vector<uint32_t> uf_parent, uf_rank;
+    uint32_t uf_find(uint32_t x) {
+        if (uf_parent[x] != x) uf_parent[x] = uf_find(uf_parent[x]);
+        return uf_parent[x];
+    }
+    void uf_union(uint32_t x, uint32_t y) {
+        uint32_t xr = uf_find(x), yr = uf_find(y);
+        if (xr == yr) return;
+        if (uf_rank[xr] < uf_rank[yr]) uf_parent[xr] = yr;
+        else if (uf_rank[xr] > uf_rank[yr]) uf_parent[yr] = xr;
+        else { uf_parent[yr] = xr; uf_rank[xr] += 1; }
+    }
+    void activation_update() {
+        R mix = R(params.activation_mix);
+        std::vector<int> comp_id(bodies.size(), -1);
+        std::vector<uint32_t> id_to_body;
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<R>& b = bodies[i];
+            if (!b.alive) continue;
+            if (b.ndofs() != 0) {
+                if (b.is_active() && b.can_sleep) {
+                    R v2 = b.lin.x * b.lin.x + b.lin.y * b.lin.y + b.lin.z * b.lin.z + b.ang.x * b.ang.x +
+                         b.ang.y * b.ang.y + b.ang.z * b.ang.z;
+                    R e = (R(1) - mix) * b.energy + mix * v2;
+                    b.energy = std::min(e, b.sleep_threshold * R(4));
+                }
+                comp_id[i] = int(id_to_body.size());
+                id_to_body.push_back(i);
+            }
+            if (b.kinematic()) {
+                comp_id[i] = int(id_to_body.size());
+                id_to_body.push_back(i);
+            }
+        }
+        uf_parent.resize(id_to_body.size());
+        uf_rank.assign(id_to_body.size(), 0);
+        for (uint32_t i = 0; i < id_to_body.size(); ++i) uf_parent[i] = i;
+        for (auto& kv : manifolds) {
+            const Manifold<R>& m = kv.second;
+            if (m.contacts.empty()) continue;
+            int a = comp_id[colliders[m.c1].body], b = comp_id[colliders[m.c2].body];
+            if (a >= 0 && b >= 0) uf_union(uint32_t(a), uint32_t(b));
+        }
+        std::vector<char> can_deactivate(id_to_body.size(), 1);
+        for (uint32_t i = 0; i < id_to_body.size(); ++i) {
+            uint32_t root = uf_find(i);
+            const Body<R>& b = bodies[id_to_body[i]];
+            can_deactivate[root] = b.can_sleep ? (can_deactivate[root] && b.energy < b.sleep_threshold) : 0;
+        }
+        for (auto& b : bodies) b.in_island = false;
+        for (uint32_t i = 0; i < id_to_body.size(); ++i) {
+            uint32_t root = uf_find(i);
+            Body<R>& b = bodies[id_to_body[i]];
+            if (can_deactivate[root]) {
+                if (b.is_active()) deactivate(b);
+            } else if (!b.kinematic()) {
+                b.in_island = true;
+                if (!(b.energy != R(0)) && b.can_sleep) activate(b);
+            }
+        }
+    }
+
+    // ------------------------------------------------------- solver
+    static R combine(R a, uint32_t ma, R b, uint32_t mb) {   // MaterialCombineMode::combine (material.rs:71-86)
+        if (ma == NPGPU_COMBINE_MAX || mb == NPGPU_COMBINE_MAX) return std::max(a, b);
+        if (ma == NPGPU_COMBINE_MULTIPLY || mb == NPGPU_COMBINE_MULTIPLY) return a * b;
+        if (ma == NPGPU_COMBINE_MIN || mb == NPGPU_COMBINE_MIN) return std::min(a, b);
+        return (a + b) * R(0.5);
+    }
+
+    // RigidBody::fill_constraint_geometry (rigid_body.rs:672-722).
+    void fill(const Body<R>& b, V3<R> point, V3<R> dir, R* J, R* WJ, R& inv_r, R& rhs, bool with_ext) const {
+        V3<R> pos = point - b.com;
+        V3<R> fl = dir, fa = cross(pos, dir);
+        R f[6] = {fl.x, fl.y, fl.z, fa.x, fa.y, fa.z};
+        R mf[6];
+        for (int k = 0; k < 6; ++k) mf[k] = f[k] * b.mask[k];
+        R vel[6] = {b.lin.x, b.lin.y, b.lin.z, b.ang.x, b.ang.y, b.ang.z};
+        if (b.status == NPGPU_BODY_KINEMATIC) {
+            R s = R(0);
+            for (int k = 0; k < 6; ++k) s = s + f[k] * vel[k];
+            rhs = rhs + s;
+        } else if (b.status == NPGPU_BODY_DYNAMIC) {
+            for (int k = 0; k < 6; ++k) J[k] = mf[k];
+            V3<R> ml = v3<R>(mf[0], mf[1], mf[2]), ma = v3<R>(mf[3], mf[4], mf[5]);
+            V3<R> wl = ml * b.inv_aug.linear;
+            V3<R> wa = mv(b.inv_aug.angular, ma);
+            WJ[0] = wl.x; WJ[1] = wl.y; WJ[2] = wl.z; WJ[3] = wa.x; WJ[4] = wa.y; WJ[5] = wa.z;
+            inv_r = inv_r + (b.inv_aug.linear + dot(ma, wa));
+            R s = R(0);
+            for (int k = 0; k < 6; ++k) s = s + f[k] * vel[k];
+            rhs = rhs + s;
+            if (with_ext) {
+                R dt = R(params.dt);
+                R ext[6] = {b.acc_lin.x * dt, b.acc_lin.y * dt, b.acc_lin.z * dt,
+                            b.acc_ang.x * dt, b.acc_ang.y * dt, b.acc_ang.z * dt};
+                R e = R(0);
+                for (int k = 0; k < 6; ++k) e = e + mf[k] * ext[k];
+                rhs = rhs + e;
+            }
+        }
+    }
+
+    // helper::constraint_pair_geometry (solver/helper.rs:53-135) for one row.
+    Row<R> make_row(const Body<R>& b1, uint32_t s1, const Body<R>& b2, uint32_t s2, V3<R> center1, V3<R> center2,
+                    V3<R> dir, R rhs0) const {
+        Row<R> r;
+        std::memset(&r, 0, sizeof(r));
+        r.b1 = b1.dynamic() ? int(s1) : -1;
+        r.b2 = b2.dynamic() ? int(s2) : -1;
+        R inv_r = R(0), rhs = rhs0;
+        fill(b1, center1, dir, r.J1, r.WJ1, inv_r, rhs, true);
+        fill(b2, center2, -dir, r.J2, r.WJ2, inv_r, rhs, true);
+        r.r = (inv_r != R(0)) ? R(1) / inv_r : R(1);
+        r.rhs = rhs;
+        return r;
+    }
+
+    // nalgebra Vector3::orthonormal_subspace_basis for one vector.
+    static void tangent_basis(V3<R> n, V3<R>& t1, V3<R>& t2) {
+        V3<R> a;
+        if (std::fabs(n.x) > std::fabs(n.y)) a = v3<R>(n.z, R(0), -n.x);
+        else a = v3<R>(R(0), -n.z, n.y);
+        t1 = vdiv(a, norm(a));
+        V3<R> b = cross(n, a);
+        t2 = vdiv(b, norm(b));
+    }
+
+    std::vector<Row<R>> rows;
+    std::vector<PosConstraint<R>> pos_constraints;
+    std::vector<int> seq_warm, seq_friction, seq_normal, seq_pos;
+    std::vector<Manifold<R>*> solver_manifolds;
+
+    // JP colouring with first-fit colours (the GPU solver's schedule).
+    uint32_t colour_manifolds(std::vector<Manifold<R>*>& ms) {
+        std::vector<uint64_t> best(bodies.size(), 0);
+        std::vector<uint64_t> used(bodies.size(), 0);
+        std::vector<Manifold<R>*> todo = ms;
+        uint32_t ncol = 0;
+        while (!todo.empty()) {
+            for (Manifold<R>* m : todo) {
+                uint64_t p = pair_priority(m->c1, m->c2);
+                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
+                if (bodies[b1].dynamic()) best[b1] = std::max(best[b1], p);
+                if (bodies[b2].dynamic()) best[b2] = std::max(best[b2], p);
+            }
+            std::vector<Manifold<R>*> rest, won;
+            for (Manifold<R>* m : todo) {
+                uint64_t p = pair_priority(m->c1, m->c2);
+                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
+                bool w = (!bodies[b1].dynamic() || best[b1] == p) && (!bodies[b2].dynamic() || best[b2] == p);
+                (w ? won : rest).push_back(m);
+            }
+            for (Manifold<R>* m : won) {
+                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
+                uint64_t mask = 0;
+                if (bodies[b1].dynamic()) mask |= used[b1];
+                if (bodies[b2].dynamic()) mask |= used[b2];
+                uint32_t c = 0;
+                while (c < 64 && (mask >> c) & 1u) ++c;
+                m->colour = c;
+                if (c >= 64) continue;
+                if (bodies[b1].dynamic()) used[b1] |= (uint64_t(1) << c);
+                if (bodies[b2].dynamic()) used[b2] |= (uint64_t(1) << c);
+                ncol = std::max(ncol, c + 1);
+            }
+            for (Manifold<R>* m : todo) {
+                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
+                best[b1] = 0;
+                best[b2] = 0;
+            }
+            todo.swap(rest);
+        }
+        return ncol;
+    }
+
+    // MoreauJeanSolver::assemble_system + SignoriniCoulombPyramidModel::constraints
+    // (moreau_jean_solver.rs:129-260, signorini_coulomb_pyramid_model.rs:56-224,
+    // signorini_model.rs:37-197).
+    bool assemble() {
+        rows.clear();
+        pos_constraints.clear();
+        seq_warm.clear(); seq_friction.clear(); seq_normal.clear(); seq_pos.clear();
+        solver_manifolds.clear();
+        // Manifold collection (mechanical_world.rs:287-300).
+        for (auto& kv : manifolds) {
+            Manifold<R>& m = kv.second;
+            m.colour = 0xffffffffu;
+            m.in_solver = false;
+            if (m.contacts.empty()) continue;
+            const Body<R>& b1 = bodies[colliders[m.c1].body];
+            const Body<R>& b2 = bodies[colliders[m.c2].body];
+            if (b1.status == NPGPU_BODY_DISABLED || b2.status == NPGPU_BODY_DISABLED) continue;
+            if ((b1.ndofs() != 0 && b1.is_active()) || (b2.ndofs() != 0 && b2.is_active())) {
+                m.in_solver = true;
+                solver_manifolds.push_back(&m);
+            }
+        }
+        num_colours = 0;
+        std::vector<Manifold<R>*> seq = solver_manifolds;
+        if (order == ORDER_COLOUR) {
+            num_colours = colour_manifolds(seq);
+            if (num_colours >= 64 || std::any_of(seq.begin(), seq.end(), [](Manifold<R>* m) { return m->colour >= 64; })) {
+                last_error = "colour overflow";
+                return false;
+            }
+            std::stable_sort(seq.begin(), seq.end(),
+                             [](Manifold<R>* a, Manifold<R>* b) { return a->colour < b->colour; });
+        }
+        R inv_dt = (params.dt == 0.0f) ? R(0) : R(1) / R(params.dt);
+        std::vector<int> ug, un, bg, bn;   // unilateral ground / non-ground, bilateral ...
+        for (Manifold<R>* m : seq) {
+            const Collider<R>& c1 = colliders[m->c1];
+            const Collider<R>& c2 = colliders[m->c2];
+            const Body<R>& b1 = bodies[c1.body];
+            const Body<R>& b2 = bodies[c2.body];
+            R mu = combine(c1.friction, c1.friction_combine, c2.friction, c2.friction_combine);
+            R e = combine(c1.restitution, c1.restitution_combine, c2.restitution, c2.restitution_combine);
+            bool ground = b1.ndofs() == 0 || b2.ndofs() == 0;
+            for (MContact<R>& k : m->contacts) {
+                V3<R> n = k.g.normal;
+                V3<R> center1 = k.g.world1 + n * c1.margin;
+                V3<R> center2 = k.g.world2 - n * c2.margin;
+                // Normal row (SignoriniModel::build_velocity_constraint).
+                Row<R> rn = make_row(b1, c1.body, b2, c2.body, center1, center2, -n, R(0));
+                if (rn.rhs <= -R(params.restitution_velocity_threshold)) rn.rhs = rn.rhs + e * rn.rhs;
+                R depth = k.g.depth + c1.margin + c2.margin;
+                if (depth < R(0)) rn.rhs = rn.rhs + (-depth) * inv_dt;
+                rn.impulse = k.impulse[0] * R(params.warmstart_coeff);
+                if (params.warmstart_mode == 1) rn.impulse = R(0);
+                rn.friction = false;
+                rn.cache = &k;
+                rn.cache_slot = 0;
+                int in = int(rows.size());
+                rows.push_back(rn);
+                pos_constraints.push_back(PosConstraint<R>{m->c1, m->c2, k.fid1, k.fid2, k.normal1_local});
+                V3<R> t[2];
+                tangent_basis(n, t[0], t[1]);
+                int it[2];
+                for (int s = 0; s < 2; ++s) {
+                    Row<R> rt = make_row(b1, c1.body, b2, c2.body, center1, center2, t[s], R(0));
+                    rt.impulse = k.impulse[1 + s] * R(params.warmstart_coeff);
+                    if (params.warmstart_mode == 1) rt.impulse = R(0);
+                    rt.friction = true;
+                    rt.dep = in;
+                    rt.mu = mu;
+                    rt.cache = &k;
+                    rt.cache_slot = 1 + s;
+                    it[s] = int(rows.size());
+                    rows.push_back(rt);
+                }
+                if (order == ORDER_COLOUR) {
+                    seq_warm.push_back(in);
+                    seq_warm.push_back(it[0]);
+                    seq_warm.push_back(it[1]);
+                    seq_friction.push_back(it[0]);
+                    seq_friction.push_back(it[1]);
+                    seq_normal.push_back(in);
+                } else {
+                    (ground ? ug : un).push_back(in);
+                    (ground ? bg : bn).push_back(it[0]);
+                    (ground ? bg : bn).push_back(it[1]);
+                }
+                seq_pos.push_back(int(pos_constraints.size()) - 1);
+            }
+        }
+        if (order == ORDER_REFERENCE) {
+            // SORProx::warmstart_set / step (sor_prox.rs:19-45, 159-179).
+            for (int i : un) seq_warm.push_back(i);
+            for (int i : ug) seq_warm.push_back(i);
+            for (int i : bn) seq_warm.push_back(i);
+            for (int i : bg) seq_warm.push_back(i);
+            for (int i : bn) seq_friction.push_back(i);
+            for (int i : bg) seq_friction.push_back(i);
+            for (int i : un) seq_normal.push_back(i);
+            for (int i : ug) seq_normal.push_back(i);
+        }
+        return true;
+    }
+
+    std::vector<R> dv;   // mj_lambda, 6 per body slot
+
+    R jdot(const Row<R>& r) const {
+        R d = R(0);
+        if (r.b1 >= 0 && r.b2 >= 0) {
+            R s1 = R(0), s2 = R(0);
+            for (int k = 0; k < 6; ++k) s1 = s1 + r.J1[k] * dv[6 * r.b1 + k];
+            for (int k = 0; k < 6; ++k) s2 = s2 + r.J2[k] * dv[6 * r.b2 + k];
+            d = s1 + s2;
+        } else if (r.b1 >= 0) {
+            for (int k = 0; k < 6; ++k) d = d + r.J1[k] * dv[6 * r.b1 + k];
+        } else if (r.b2 >= 0) {
+            for (int k = 0; k < 6; ++k) d = d + r.J2[k] * dv[6 * r.b2 + k];
+        }
+        return d;
+    }
+    void axpy(const Row<R>& r, R a) {
+        if (r.b1 >= 0)
+            for (int k = 0; k < 6; ++k) dv[6 * r.b1 + k] = a * r.WJ1[k] + dv[6 * r.b1 + k];
+        if (r.b2 >= 0)
+            for (int k = 0; k < 6; ++k) dv[6 * r.b2 + k] = a * r.WJ2[k] + dv[6 * r.b2 + k];
+    }
+    // SORProx::solve_unilateral[_ground] (sor_prox.rs:181-230).
+    void solve_normal(Row<R>& r) {
+        R dimpulse = jdot(r) + r.rhs;
+        R ni = r.impulse - r.r * dimpulse;
+        ni = ni > R(0) ? ni : R(0);
+        R dl = ni - r.impulse;
+        r.impulse = ni;
+        axpy(r, dl);
+    }
+    // SORProx::solve_bilateral[_ground] with ImpulseLimits::Dependent (sor_prox.rs:232-343).
+    void solve_friction(Row<R>& r) {
+        R li = rows[r.dep].impulse;
+        if (li == R(0)) {
+            if (r.impulse != R(0)) {
+                axpy(r, -r.impulse);
+                r.impulse = R(0);
+            }
+            return;
+        }
+        R mx = r.mu * li, mn = -mx;
+        R dimpulse = jdot(r) + r.rhs;
+        R ni = r.impulse - r.r * dimpulse;
+        if (ni < mn) ni = mn;
+        else if (ni > mx) ni = mx;
+        R dl = ni - r.impulse;
+        r.impulse = ni;
+        axpy(r, dl);
+    }
+    // FP64 complementarity residual: ||lambda - proj(lambda - r (J dv + rhs))|| / max(1, ||lambda||).
+    double residual() const {
+        double s2 = 0, l2 = 0;
+        for (const Row<R>& r : rows) {
+            double d = 0;
+            if (r.b1 >= 0)
+                for (int k = 0; k < 6; ++k) d += double(r.J1[k]) * double(dv[6 * r.b1 + k]);
+            if (r.b2 >= 0)
+                for (int k = 0; k < 6; ++k) d += double(r.J2[k]) * double(dv[6 * r.b2 + k]);
+            d += double(r.rhs);
+            double lam = double(r.impulse);
+            double x = lam - double(r.r) * d;
+            double p;
+            if (!r.friction) p = x > 0 ? x : 0;
+            else {
+                double mx = double(r.mu) * double(rows[r.dep].impulse);
+                p = std::min(std::max(x, -mx), mx);
+            }
+            double phi = lam - p;
+            s2 += phi * phi;
+            l2 += lam * lam;
+        }
+        return std::sqrt(s2) / std::max(1.0, std::sqrt(l2));
+    }
+    void sor_prox() {
+        // SORProx::solve (sor_prox.rs:48-80).
+        std::fill(dv.begin(), dv.end(), R(0));
+        for (int i : seq_warm) {
+            const Row<R>& r = rows[i];
+            if (r.impulse != R(0)) axpy(r, r.impulse);
+        }
+        counters.residual_initial = residual();
+        uint32_t iters = 0;
+        uint32_t maxit = params.solve_to_tolerance ? params.max_iterations_to_tolerance : params.max_velocity_iterations;
+        double res = counters.residual_initial;
+        for (uint32_t it = 0; it < maxit; ++it) {
+            if (params.solve_to_tolerance && res <= double(params.residual_tolerance)) break;
+            for (int i : seq_friction) solve_friction(rows[i]);
+            for (int i : seq_normal) solve_normal(rows[i]);
+            ++iters;
+            if (params.solve_to_tolerance) res = residual();
+        }
+        if (!params.solve_to_tolerance) res = residual();
+        counters.residual = res;
+        counters.velocity_iterations = iters;
+    }
+    // SignoriniCoulombPyramidModel::cache_impulses (signorini_coulomb_pyramid_model.rs:226-261).
+    void cache_impulses() {
+        for (const Row<R>& r : rows) static_cast<MContact<R>*>(r.cache)->impulse[r.cache_slot] = r.impulse;
+    }
+
+    // NonlinearSORProx::solve_unilateral + update_contact_constraint
+    // (nonlinear_sor_prox.rs:121-294).
+    void solve_position(const PosConstraint<R>& pc) {
+        const Collider<R>& c1 = colliders[pc.c1];
+        const Collider<R>& c2 = colliders[pc.c2];
+        Body<R>& b1 = bodies[c1.body];
+        Body<R>& b2 = bodies[c2.body];
+        Iso<R> m1 = iso_mul(b1.pos, c1.pos_wrt_body);
+        Iso<R> m2 = iso_mul(b2.pos, c2.pos_wrt_body);
+        V3<R> n0 = qrot(m1.q, pc.normal1_local);
+        ContactGeom<R> g = kinematic_contact(feature(c1, pc.fid1), m1, c1.dilation() + c1.margin, feature(c2, pc.fid2),
+                                             m2, c2.dilation() + c2.margin, n0);
+        // clamp_rhs (nonlinear_sor_prox.rs:296-309).
+        R rhs = (-g.depth + R(params.allowed_linear_error)) * R(params.erp);
+        rhs = std::max(rhs, -R(params.max_linear_correction));
+        if (rhs >= R(0)) return;
+        R inv_r = R(0), dummy = R(0);
+        R J1[6], J2[6], W1[6], W2[6];
+        if (b1.ndofs() != 0) fill(b1, g.world1, -g.normal, J1, W1, inv_r, dummy, false);
+        if (b2.ndofs() != 0) fill(b2, g.world2, g.normal, J2, W2, inv_r, dummy, false);
+        if (inv_r == R(0)) return;
+        R r = R(1) / inv_r;
+        R impulse = -rhs * r;
+        if (b1.ndofs() != 0) {
+            for (int k = 0; k < 6; ++k) W1[k] = W1[k] * impulse;
+            apply_displacement(b1, v3<R>(W1[0], W1[1], W1[2]), v3<R>(W1[3], W1[4], W1[5]));
+        }
+        if (b2.ndofs() != 0) {
+            for (int k = 0; k < 6; ++k) W2[k] = W2[k] * impulse;
+            apply_displacement(b2, v3<R>(W2[0], W2[1], W2[2]), v3<R>(W2[3], W2[4], W2[5]));
+        }
+    }
+
+    // ------------------------------------------------------- the step
+    // MechanicalWorld::step_with_filter (mechanical_world.rs:199-396).
+    npgpu_status step() {
+        R dt = R(params.dt);
+        // maintain: register new colliders (geometrical_world.rs:102-143).
+        for (auto& c : colliders) {
+            if (!c.alive || c.registered) continue;
+            c.registered = true;
+            Body<R>& b = bodies[c.body];
+            if (c.density != R(0) && b.kind == NPGPU_KIND_RIGID_BODY) {
+                V3<R> com;
+                Inertia<R> in;
+                mass_properties(c, com, in);
+                add_local_inertia_and_com(b, com, in);
+            }
+            cd_dirty = true;
+        }
+        for (auto& b : bodies) {
+            if (!b.alive) continue;
+            update_dynamics(b, dt);
+        }
+        for (auto& b : bodies)
+            if (b.alive) update_acceleration(b);
+        if (cd_dirty) collision_detection();
+        activation_update();
+        if (!assemble()) return NPGPU_ERR_CAPACITY;
+        dv.assign(6 * bodies.size(), R(0));
+        sor_prox();
+        cache_impulses();
+        // update_velocities_and_integrate (moreau_jean_solver.rs:328-347).
+        for (uint32_t i = 0; i < bodies.size(); ++i) {
+            Body<R>& b = bodies[i];
+            if (!b.alive || !b.in_island) continue;
+            V3<R> el = b.acc_lin * dt, ea = b.acc_ang * dt;
+            b.lin = (b.lin + el) + v3<R>(dv[6 * i + 0], dv[6 * i + 1], dv[6 * i + 2]);
+            b.ang = (b.ang + ea) + v3<R>(dv[6 * i + 3], dv[6 * i + 4], dv[6 * i + 5]);
+            b.changed = true;
+            integrate(b);
+        }
+        // NonlinearSORProx::solve (nonlinear_sor_prox.rs:17-55).
+        for (uint32_t it = 0; it < params.max_position_iterations; ++it)
+            for (int i : seq_pos) solve_position(pos_constraints[i]);
+        for (auto& b : bodies)
+            if (b.alive && b.kinematic()) integrate(b);
+        for (auto& b : bodies)
+            if (b.alive) update_dynamics(b, dt);
+        for (auto& b : bodies)
+            if (b.alive) b.f_lin = b.f_ang = v3<R>(R(0), R(0), R(0));
+        collision_detection();
+        for (auto& b : bodies) b.changed = false;
+        counters.steps += 1;
+        fill_counters();
+        return NPGPU_OK;
+    }
+
+    void fill_counters() {
+        uint32_t nm = 0, nc = 0, nsc = 0, na = 0;
+        double maxpen = -1e30, ke = 0;
+        for (auto& kv : manifolds) {
+            const Manifold<R>& m = kv.second;
+            if (!m.contacts.empty()) ++nm;
+            nc += uint32_t(m.contacts.size());
+            if (m.in_solver) nsc += uint32_t(m.contacts.size());
+            for (auto& k : m.contacts)
+                maxpen = std::max(maxpen, double(k.g.depth) + double(colliders[m.c1].margin) + double(colliders[m.c2].margin));
+        }
+        for (auto& b : bodies) {
+            if (!b.alive || !b.dynamic()) continue;
+            if (b.in_island) ++na;
+            double m = double(b.inertia.linear);
+            double v2 = double(b.lin.x) * b.lin.x + double(b.lin.y) * b.lin.y + double(b.lin.z) * b.lin.z;
+            V3<R> iw = mv(b.inertia.angular, b.ang);
+            double wiw = double(b.ang.x) * iw.x + double(b.ang.y) * iw.y + double(b.ang.z) * iw.z;
+            ke += 0.5 * (m * v2 + wiw);
+        }
+        counters.num_pairs = uint32_t(pairs.size());
+        counters.num_manifolds = nm;
+        counters.num_contacts = nc;
+        counters.num_solver_contacts = nsc;
+        counters.num_constraints = 3 * nsc;
+        counters.num_colours = num_colours;
+        counters.num_active_bodies = na;
+        counters.max_penetration = nc ? maxpen : 0.0;
+        counters.kinetic_energy = ke;
+    }
+};
+
+}  // namespace oracle
