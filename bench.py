@@ -1,0 +1,294 @@
+"""Benchmark of the GPU rigid-body step: body-steps/s on the 32^3 ball pile.
+
+Workload: 32768 balls of radius 0.5 on a 1.2 lattice (seeded jitter),
+dropped on a static ground, density 1, friction 0.3, dt 1/60, the
+reference's 8 velocity / 3 position iterations. The pile is simulated
+untimed for --settle steps (it reaches the ground and forms contacts), then
+--warmup steps, then --steps timed steps.
+
+  value  body-steps/s with the world resident in HBM: CUDA events on the
+         world's stream around each step, an L2 flush (256 MiB write)
+         between steps, outside the timed region.
+  e2e    the same metric through the C ABI as a host would drive it: per
+         step, upload of the step's applied forces from pinned host memory,
+         npgpu_step, download of every body's pose and velocity into host
+         buffers; wall time of the loop.
+  --impl reference  times the CPU oracle (the restated reference step) on
+         this host instead (the Rust reference cannot be built here).
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "body-steps/s"
+L2_FLUSH_BYTES = 256 << 20
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--settle", type=int, default=200)
+    ap.add_argument("--side", type=int, default=32)
+    ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """Samples nvidia-smi clocks and throttle reasons during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device=0):
+        self.device = device
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.thread.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, parts[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def cpu_baseline(scene_fn, seconds, settle_steps):
+    """Times the oracle (restated reference step, f32, one thread) on a bounded
+    sample of the same workload: the pile settled for `settle_steps` steps on
+    the CPU would take too long, so the sample is the first steps of the run
+    from t = 0 until about `seconds` of CPU time have been spent."""
+    from oracle.oracle_py import ORDER_REFERENCE, OracleWorld
+    sc = scene_fn()
+    o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_REFERENCE)
+    o.load_scene(sc)
+    steps = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < seconds:
+        o.step(1)
+        steps += 1
+    dt = time.perf_counter() - t0
+    c = o.counters()
+    return {"value": sc.num_dynamic * steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"{steps} steps from t=0 of the same {sc.num_dynamic}-ball pile, single-threaded f32 "
+                      f"oracle in the reference's row order ({c['num_contacts']} contacts at the end)"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    from nphysics_gb300 import scenes
+    from oracle.oracle_py import ORDER_REFERENCE, OracleWorld
+    sc = scenes.ball_pile(side=args.side)
+    o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_REFERENCE)
+    o.load_scene(sc)
+    budget = max(5.0, args.cpu_seconds)
+    for _ in range(max(args.warmup, 0)):
+        o.step(1)
+    t0 = time.perf_counter()
+    steps = 0
+    for _ in range(args.steps):
+        o.step(1)
+        steps += 1
+        if time.perf_counter() - t0 > budget:
+            break
+    dt = time.perf_counter() - t0
+    value = sc.num_dynamic * steps / dt
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
+        "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, "
+                               f"seeded jitter), dt 1/60, 8 velocity / 3 position iterations",
+                   "sample": f"first {args.warmup + steps} steps from t=0"},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
+                         "sample": f"{steps} timed steps after {args.warmup} warm-up steps, single-threaded f32 "
+                                   "oracle (restated nphysics3d step, reference row order); the Rust reference "
+                                   "has no toolchain on this host"},
+        "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    from nphysics_gb300 import build, scenes
+    from nphysics_gb300.world import GpuWorld
+
+    rank = int(os.environ.get("RANK", "0"))
+    world_size = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local_rank)
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build.build()
+    torch.cuda.init()
+    # Replicas: every rank runs its own copy of the workload (one world per GPU).
+    sc = scenes.ball_pile(side=args.side)
+    p = sc.params()
+    p.profile = 1
+    w = GpuWorld.for_scene(sc, p)
+    stream = torch.cuda.ExternalStream(w.stream)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+    n_dyn = sc.num_dynamic
+    w.step(args.settle)
+    w.step(args.warmup)
+    c0 = w.counters()
+
+    # ---- device-resident timing -------------------------------------------------------
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    solver_ms, counters = [], []
+    if world_size > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clocks:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.fill_(k & 0xff)
+            a, b = evs[k]
+            a.record(stream)
+            w.step(1, sync=False)
+            b.record(stream)
+            c = w.counters()
+            solver_ms.append(c["solver_time"])
+            counters.append(c)
+        torch.cuda.synchronize()
+    if world_size > 1:
+        torch.distributed.barrier()
+    step_ms = [a.elapsed_time(b) for a, b in evs]
+    total_ms = sum(step_ms)
+    if world_size > 1:
+        t = torch.tensor([total_ms], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = world_size * n_dyn * args.steps / (total_ms * 1e-3)
+
+    # ---- end to end through the C ABI with host buffers ------------------------------------
+    pos = np.zeros((len(sc.bodies), 7), np.float32)
+    vel = np.zeros((len(sc.bodies), 6), np.float32)
+    dyn = np.nonzero(sc.bodies["status"] == 2)[0]
+    handles = np.ascontiguousarray(sc.body_handles[dyn])
+    forces = np.zeros((len(dyn), 6), np.float32)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        w.apply_forces(handles, forces, wake=False)
+        w.step(1, sync=False)
+        w.download_into(pos, vel)
+    e2e_s = time.perf_counter() - t0
+    h2d = len(dyn) * (4 + 4 + 24)
+    d2h = len(sc.bodies) * (7 + 6) * 4
+    e2e_value = world_size * n_dyn * args.steps / e2e_s
+
+    # ---- roofline of the dominant kernel (the persistent solver kernel) --------------------
+    peak, peak_kind = measured_peaks()
+    K = statistics.mean(c["num_solver_contacts"] for c in counters)
+    B = statistics.mean(c["num_active_bodies"] for c in counters)
+    it = statistics.mean(c["velocity_iterations"] for c in counters)
+    pos_it = p.max_position_iterations
+    bytes_launch = it * (128 * K + 76 * B) + pos_it * 96 * K + 104 * B
+    solve_ms = statistics.mean(solver_ms)
+    achieved = bytes_launch / (solve_ms * 1e-3) / 1e9
+    cl = clocks.summary()
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"ball pile {args.side}^3 = {n_dyn} balls (radius 0.5, 1.2 lattice, seeded jitter) "
+                               f"on a static ground, dt 1/60, 8 velocity / 3 position iterations; timed steps "
+                               f"{args.settle + args.warmup}..{args.settle + args.warmup + args.steps - 1} of the run",
+                   "l2": "flushed (256 MiB write) between timed steps", "parallelism": "replicas",
+                   "contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
+                   "solver_contacts": int(K), "active_bodies": int(B),
+                   "colours": int(statistics.mean(c["num_colours"] for c in counters))},
+        "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "roofline": {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+                     "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
+        "clocks": {"sm_mhz": cl["sm_mhz"], "sm_max_mhz": cl["sm_max_mhz"], "reasons": cl["reasons"]},
+        "gpu_launches": 9 * args.steps,
+        "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
+                     ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
+                      "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",
+                      "velocity_update_time", "position_resolution_time")},
+    }
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(lambda: scenes.ball_pile(side=args.side), args.cpu_seconds, args.settle)
+    if rank == 0:
+        print(json.dumps(line))
+    if world_size > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,385 @@
+// k_cd.cu -- collision detection on the device.
+//
+// GeometricalWorld::sync_colliders + perform_broad_phase + perform_narrow_phase
+// (src/world/geometrical_world.rs:230-265, 285-320) for ball and cuboid
+// colliders. The broad phase keeps ncollide's DBVTBroadPhase semantics
+// (geometrical_world.rs:60): every collider carries a fat AABB (its tight AABB
+// loosened by the query limit, then by the 0.01 margin) that is refreshed only
+// when the tight box leaves it, and the pair set is every allowed pair whose
+// fat AABBs intersect. It is found with a linear BVH (Karras 2012) over
+// 64-bit keys (world index | 48-bit Morton code), rebuilt every pass:
+//   sync_aabb -> radix sort -> build -> refit -> count -> scan -> write -> narrow.
+// Each pair is written by its owner (the collider with the smaller bounding
+// radius, ties by slot) so the list is deterministic and the previous step's
+// pairs of a collider are found without hashing.
+#include <cub/device/device_radix_sort.cuh>
+#include <cub/device/device_scan.cuh>
+
+#include "narrow.cuh"
+
+namespace npgpu_dev {
+
+constexpr int kThreads = 256;
+static inline unsigned nblocks(uint32_t n) { return (n + kThreads - 1) / kThreads; }
+
+__device__ __forceinline__ uint64_t expand16(uint32_t v) {
+    uint64_t x = v & 0xffffu;
+    x = (x | (x << 32)) & 0x1f00000000ffffull;
+    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
+    x = (x | (x << 8)) & 0x100f00f00f00f00full;
+    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
+    x = (x | (x << 2)) & 0x1249249249249249ull;
+    return x;
+}
+__device__ __forceinline__ uint32_t quantize(float c) {
+    float q = floorf(c * 4.0f) + 32768.0f;
+    q = q < 0.0f ? 0.0f : (q > 65535.0f ? 65535.0f : q);
+    return (uint32_t)q;
+}
+
+__device__ __forceinline__ Shape load_shape(const Colliders& c, uint32_t i) {
+    Shape s;
+    uint32_t info = c.info[i];
+    s.shape = info & 0xfu;
+    float4 p = c.params[i];
+    s.h = np::mk(p.x, p.y, p.z);
+    s.radius = p.x;
+    s.pose.t = v3(c.pose_t[i]);
+    s.pose.q = q4(c.pose_q[i]);
+    return s;
+}
+
+// Collider pose, tight AABB (loosened by margin + linear prediction,
+// src/object/collider.rs:542-549), fat AABB update and sort key.
+__global__ void k_sync_aabb(World w, float bp_margin) {
+    uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= w.nc_slots) return;
+    const Colliders& c = w.c;
+    if (!(c.info[i] & CI_ALIVE)) {
+        c.keys[i] = ~0ull;
+        c.vals[i] = i;
+        return;
+    }
+    uint32_t bi = c.body[i];
+    np::Iso bp{v3(w.b.pos_t[bi]), q4(w.b.pos_q[bi])};
+    np::Iso wrt{v3(c.wrt_t[i]), q4(c.wrt_q[i])};
+    np::Iso pose = np::iso_mul(bp, wrt);
+    c.pose_t[i] = f4(pose.t);
+    c.pose_q[i] = f4q(pose.q);
+    uint32_t shape = c.info[i] & 0xfu;
+    float4 prm = c.params[i];
+    np::V half;
+    if (shape == SHAPE_BALL) {
+        half = np::mk(prm.x, prm.x, prm.x);
+    } else {
+        np::M rot = np::qmat(pose.q);
+        for (int a = 0; a < 3; ++a) {
+            float s = fabsf(rot.m[a][0]) * prm.x + fabsf(rot.m[a][1]) * prm.y + fabsf(rot.m[a][2]) * prm.z;
+            np::setc(half, a, s);
+        }
+    }
+    float ql = c.margin[i] + c.lin_pred[i];
+    float mn[3], mx[3];
+    for (int a = 0; a < 3; ++a) {
+        mn[a] = (np::comp(pose.t, a) - np::comp(half, a)) - ql;
+        mx[a] = (np::comp(pose.t, a) + np::comp(half, a)) + ql;
+    }
+    float4 fmn = c.aabb_min[i], fmx = c.aabb_max[i];
+    bool inside = fmn.w != 0.0f && fmn.x <= mn[0] && mx[0] <= fmx.x && fmn.y <= mn[1] && mx[1] <= fmx.y &&
+                  fmn.z <= mn[2] && mx[2] <= fmx.z;
+    if (!inside) {
+        fmn = make_float4(mn[0] - bp_margin, mn[1] - bp_margin, mn[2] - bp_margin, 1.0f);
+        fmx = make_float4(mx[0] + bp_margin, mx[1] + bp_margin, mx[2] + bp_margin, 0.0f);
+        c.aabb_min[i] = fmn;
+        c.aabb_max[i] = fmx;
+    }
+    float cx = 0.5f * (fmn.x + fmx.x), cy = 0.5f * (fmn.y + fmx.y), cz = 0.5f * (fmn.z + fmx.z);
+    uint64_t morton = expand16(quantize(cx)) | (expand16(quantize(cy)) << 1) | (expand16(quantize(cz)) << 2);
+    uint64_t world = w.b.world[bi] & 0xffffu;
+    c.keys[i] = (world << 48) | morton;
+    c.vals[i] = i;
+}
+
+__device__ __forceinline__ int lbvh_delta(const unsigned long long* k, int n, int i, int j) {
+    if (j < 0 || j >= n) return -1;
+    unsigned long long a = k[i], b = k[j];
+    if (a == b) return 64 + __clz((unsigned)(i ^ j));
+    return __clzll((long long)(a ^ b));
+}
+
+// Karras 2012: internal node i of n - 1; leaves are nodes n - 1 .. 2n - 2.
+__global__ void k_lbvh_build(World w, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n - 1) return;
+    const unsigned long long* k = w.c.keys_sorted;
+    int d = (lbvh_delta(k, n, i, i + 1) - lbvh_delta(k, n, i, i - 1)) >= 0 ? 1 : -1;
+    int dmin = lbvh_delta(k, n, i, i - d);
+    int lmax = 2;
+    while (lbvh_delta(k, n, i, i + lmax * d) > dmin) lmax <<= 1;
+    int l = 0;
+    for (int t = lmax >> 1; t >= 1; t >>= 1)
+        if (lbvh_delta(k, n, i, i + (l + t) * d) > dmin) l += t;
+    int j = i + l * d;
+    int dnode = lbvh_delta(k, n, i, j);
+    int s = 0, t = l;
+    do {
+        t = (t + 1) >> 1;
+        if (lbvh_delta(k, n, i, i + (s + t) * d) > dnode) s += t;
+    } while (t > 1);
+    int gamma = i + s * d + (d < 0 ? d : 0);
+    int lo = i < j ? i : j, hi = i < j ? j : i;
+    int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
+    int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
+    w.c.left[i] = left;
+    w.c.right[i] = right;
+    w.c.parent[left] = i;
+    w.c.parent[right] = i;
+    if (i == 0) w.c.parent[0] = -1;
+}
+
+__device__ __forceinline__ float4 ld_cg(const float4* p) { return __ldcg(p); }
+
+// Bottom-up refit: the second child to arrive computes the parent.
+__global__ void k_lbvh_refit(World w, int n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    uint32_t ci = w.c.vals_sorted[k];
+    int node = n - 1 + k;
+    w.c.node_min[node] = w.c.aabb_min[ci];
+    w.c.node_max[node] = w.c.aabb_max[ci];
+    if (n == 1) return;
+    __threadfence();
+    int p = w.c.parent[node];
+    for (int guard = 0; p >= 0; ++guard) {
+        if (guard > 256) {   // deeper than any tree over 64-bit keys plus 32-bit tie-breaks
+            atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+            return;
+        }
+        if (atomicAdd(&w.c.node_flag[p], 1) == 0) return;
+        int l = w.c.left[p], r = w.c.right[p];
+        float4 a0 = ld_cg(&w.c.node_min[l]), a1 = ld_cg(&w.c.node_max[l]);
+        float4 b0 = ld_cg(&w.c.node_min[r]), b1 = ld_cg(&w.c.node_max[r]);
+        w.c.node_min[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 1.0f);
+        w.c.node_max[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
+        __threadfence();
+        p = w.c.parent[p];
+    }
+}
+
+// The owner of a pair is the collider with the smaller bounding radius (ties: smaller slot).
+__device__ __forceinline__ bool owns(const Colliders& c, uint32_t a, uint32_t b) {
+    float ra = c.rank[a], rb = c.rank[b];
+    return ra < rb || (ra == rb && a < b);
+}
+
+// DefaultCollisionFilter (geometrical_world.rs:926-970): not on the same body,
+// at least one body with dofs; plus: both in the same world of a batch.
+__device__ __forceinline__ bool pair_allowed(const World& w, uint32_t a, uint32_t b) {
+    uint32_t ba = w.c.body[a], bb = w.c.body[b];
+    if (ba == bb) return false;
+    if (w.b.world[ba] != w.b.world[bb]) return false;
+    return bi_status(w.b.info[ba]) == 2u || bi_status(w.b.info[bb]) == 2u;
+}
+
+__device__ __forceinline__ bool overlap(float4 amin, float4 amax, float4 bmin, float4 bmax) {
+    return amin.x <= bmax.x && bmin.x <= amax.x && amin.y <= bmax.y && bmin.y <= amax.y && amin.z <= bmax.z &&
+           bmin.z <= amax.z;
+}
+
+// Traverses the tree with leaf k's fat AABB. WRITE = false counts the pairs
+// leaf k owns; WRITE = true stores them at its offset.
+template <bool WRITE>
+__global__ void k_bp_traverse(World w, int n) {
+    int k = blockIdx.x * blockDim.x + threadIdx.x;
+    if (k >= n) return;
+    const Colliders& c = w.c;
+    uint32_t a = c.vals_sorted[k];
+    float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
+    uint32_t count = 0, base = 0;
+    if (WRITE) base = c.leaf_offset[k];
+    if (n >= 2) {
+        int stack[64];
+        int sp = 0;
+        stack[sp++] = 0;
+        while (sp > 0) {
+            int node = stack[--sp];
+            if (!overlap(amin, amax, c.node_min[node], c.node_max[node])) continue;
+            if (node >= n - 1) {
+                uint32_t b = c.vals_sorted[node - (n - 1)];
+                if (b != a && owns(c, a, b) && pair_allowed(w, a, b)) {
+                    if (WRITE) {
+                        uint32_t slot = base + count;
+                        if (slot < w.cap_pairs) w.cur.pair[slot] = make_uint2(a < b ? a : b, a < b ? b : a);
+                    }
+                    ++count;
+                }
+            } else if (sp < 62) {
+                stack[sp++] = c.left[node];
+                stack[sp++] = c.right[node];
+            } else {
+                atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+            }
+        }
+    }
+    if (!WRITE) {
+        c.leaf_count[k] = count;
+    } else {
+        // Only the pairs that fit in the buffer are visible to the next pass.
+        uint32_t stored = base >= w.cap_pairs ? 0u : (count < w.cap_pairs - base ? count : w.cap_pairs - base);
+        w.cur.owner_start[a] = base;
+        w.cur.owner_count[a] = stored;
+    }
+}
+
+__global__ void k_bp_total(World w, int n) {
+    uint32_t total = 0;
+    if (n > 0) total = w.c.leaf_offset[n - 1] + w.c.leaf_count[n - 1];
+    if (total > w.cap_pairs) {
+        atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        total = w.cap_pairs;
+    }
+    w.ctl->npairs = total;
+    w.ctl->ncontacts = 0;
+    w.ctl->nmanifolds = 0;
+    w.ctl->max_pen_bits = 0;
+}
+
+__device__ __forceinline__ unsigned long long order_bits(double v) {
+    unsigned long long b = (unsigned long long)__double_as_longlong(v);
+    return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
+}
+
+// One-shot manifold of pair p, keeping the impulses cached under the same
+// feature key in the pair's previous manifold.
+__device__ __noinline__ void narrow_pair(const World& w, uint32_t p) {
+    uint2 pr = w.cur.pair[p];
+    uint32_t c1 = pr.x, c2 = pr.y;
+    const Colliders& c = w.c;
+    Shape a = load_shape(c, c1), b = load_shape(c, c2);
+    float m1 = c.margin[c1], m2 = c.margin[c2];
+    float prediction = (m1 + c.lin_pred[c1]) + (m2 + c.lin_pred[c2]);
+    CandList out;
+    out.n = 0;
+    if (a.shape == SHAPE_BALL && b.shape == SHAPE_BALL) {
+        np::V v = np::sub(b.pose.t, a.pose.t);
+        float l2 = np::dot(v, v);
+        np::V n0 = l2 > 0.0f ? np::divs(v, sqrtf(l2)) : np::mk(1.0f, 0.0f, 0.0f);
+        push_eval(out, a, b, 0, 0, n0, prediction);
+    } else if (a.shape == SHAPE_CUBOID && b.shape == SHAPE_BALL) {
+        ball_box(b, a, true, prediction, out);
+    } else if (a.shape == SHAPE_BALL && b.shape == SHAPE_CUBOID) {
+        ball_box(a, b, false, prediction, out);
+    } else {
+        box_box(a, b, prediction, out);
+    }
+    // Previous manifold of this pair: among the pairs its owner wrote last pass.
+    uint32_t owner = owns(c, c1, c2) ? c1 : c2;
+    uint32_t qs = w.prev.owner_start[owner], qn = w.prev.owner_count[owner];
+    int prev = -1;
+    for (uint32_t q = 0; q < qn; ++q) {
+        uint2 o = w.prev.pair[qs + q];
+        if (o.x == c1 && o.y == c2) {
+            prev = int(qs + q);
+            break;
+        }
+    }
+    uint32_t pkeys[kMaxContacts];
+    int pn = 0;
+    if (prev >= 0) {
+        pn = w.prev.ncont[prev];
+        for (int k = 0; k < pn; ++k) pkeys[k] = w.prev.key[prev * kMaxContacts + k];
+    }
+    np::Q bq = q4(w.b.pos_q[c.body[c1]]);
+    int nc = out.n > kMaxContacts ? kMaxContacts : out.n;
+    double maxpen = -1e300;
+    for (int k = 0; k < nc; ++k) {
+        const Cand& cd = out.c[k];
+        uint32_t key = uint32_t(cd.f1 * 26 + cd.f2);
+        float4 imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        for (int j = 0; j < pn; ++j)
+            if (pkeys[j] == key) {
+                imp = w.prev.imp[prev * kMaxContacts + j];
+                break;
+            }
+        uint32_t slot = p * kMaxContacts + k;
+        w.cur.key[slot] = key;
+        w.cur.w1[slot] = f4(cd.g.w1, cd.g.depth);
+        w.cur.w2[slot] = f4(cd.g.w2);
+        w.cur.n[slot] = f4(cd.g.n);
+        w.cur.imp[slot] = imp;
+        w.cur.nl[slot] = f4(np::qrot_inv(bq, cd.g.n));
+        double pen = (double)cd.g.depth + (double)m1 + (double)m2;
+        maxpen = pen > maxpen ? pen : maxpen;
+    }
+    w.cur.ncont[p] = (uint8_t)nc;
+    if (nc > 0) {
+        atomicAdd(&w.ctl->ncontacts, (uint32_t)nc);
+        atomicAdd(&w.ctl->nmanifolds, 1u);
+        atomicMax(&w.ctl->max_pen_bits, order_bits(maxpen));
+    }
+}
+
+__global__ void k_narrow(World w) {
+    uint32_t npairs = w.ctl->npairs;
+    for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x)
+        narrow_pair(w, p);
+}
+
+size_t sort_temp_bytes(uint32_t n) {
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
+                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
+    return bytes;
+}
+size_t scan_temp_bytes(uint32_t n) {
+    size_t bytes = 0;
+    cub::DeviceScan::ExclusiveSum(nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
+    return bytes;
+}
+
+cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t st) {
+    if (w.nc_slots == 0) return cudaSuccess;
+    k_sync_aabb<<<nblocks(w.nc_slots), kThreads, 0, st>>>(w, p.broad_phase_margin);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st) {
+    if (w.nc_slots == 0) return cudaSuccess;
+    return cub::DeviceRadixSort::SortPairs(temp, temp_bytes, w.c.keys, w.c.keys_sorted, w.c.vals, w.c.vals_sorted,
+                                           (int)w.nc_slots, 0, 64, st);
+}
+
+cudaError_t launch_lbvh(const World& w, cudaStream_t st) {
+    int n = (int)w.nc_alive;
+    if (n >= 2) {
+        cudaMemsetAsync(w.c.node_flag, 0, sizeof(int) * (size_t)(n - 1), st);
+        k_lbvh_build<<<nblocks(n - 1), kThreads, 0, st>>>(w, n);
+    }
+    if (n >= 1) k_lbvh_refit<<<nblocks(n), kThreads, 0, st>>>(w, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStream_t st) {
+    int n = (int)w.nc_alive;
+    cudaMemsetAsync(w.cur.owner_count, 0, sizeof(uint32_t) * w.nc_slots, st);
+    if (n >= 1) {
+        k_bp_traverse<false><<<nblocks(n), kThreads, 0, st>>>(w, n);
+        cudaError_t e = cub::DeviceScan::ExclusiveSum(temp, temp_bytes, w.c.leaf_count, w.c.leaf_offset, n, st);
+        if (e != cudaSuccess) return e;
+        k_bp_traverse<true><<<nblocks(n), kThreads, 0, st>>>(w, n);
+    }
+    k_bp_total<<<1, 1, 0, st>>>(w, n);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_narrow(const World& w, cudaStream_t st) {
+    // The pair count lives on the device: a grid-stride launch sized for the
+    // capacity, capped at 16 blocks per SM of a 152-SM part.
+    uint32_t blocks = nblocks(w.cap_pairs);
+    if (blocks == 0) return cudaSuccess;
+    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    k_narrow<<<blocks, kThreads, 0, st>>>(w);
+    return cudaGetLastError();
+}
+
+}  // namespace npgpu_dev

@@ -1,0 +1,486 @@
+// narrow.cuh -- contact geometry on the device: cuboid features, the contact
+// kinematic re-evaluation (ncollide3d query::ContactKinematic::contact, used by
+// NonlinearSORProx at src/solver/nonlinear_sor_prox.rs:221-229) and one-shot
+// manifolds for ball-ball, ball-cuboid and cuboid-cuboid pairs (ncollide3d's
+// NarrowPhase, driven by src/world/geometrical_world.rs:315-320).
+//
+// Methods: SAT over the 15 box axes with a bias toward face axes, then
+// Sutherland-Hodgman clipping of the incident face against the reference
+// face with per-point feature tracking, and a 4-point reduction; Ericson's
+// segment-segment closest points. Feature ids of a cuboid: vertices 0-7,
+// edges 8-19, faces 20-25; a ball has the single feature 0.
+#pragma once
+#include <cfloat>
+#include "dyn.cuh"
+
+namespace npgpu_dev {
+
+enum { AP_POINT = 1, AP_SEGMENT = 2, AP_PLANE = 3 };
+enum { SHAPE_BALL = 0, SHAPE_CUBOID = 1 };
+
+struct Approx {
+    int kind;
+    np::V a, b;
+};
+
+__device__ __forceinline__ int box_vertex_id(int sx, int sy, int sz) { return sx | (sy << 1) | (sz << 2); }
+__device__ __forceinline__ void edge_other_axes(int a, int& o1, int& o2) {
+    o1 = (a == 0) ? 1 : 0;
+    o2 = (a == 2) ? 1 : 2;
+}
+__device__ __forceinline__ int box_edge_id(int axis, int s1, int s2) { return 8 + 4 * axis + (s1 | (s2 << 1)); }
+__device__ __forceinline__ int box_face_id(int axis, int pos) { return 20 + 2 * axis + pos; }
+
+__device__ __forceinline__ Approx box_feature(np::V h, int fid) {
+    Approx ap;
+    np::V z = np::mk(0.0f, 0.0f, 0.0f);
+    if (fid < 8) {
+        ap.kind = AP_POINT;
+        ap.a = np::mk((fid & 1) ? h.x : -h.x, (fid & 2) ? h.y : -h.y, (fid & 4) ? h.z : -h.z);
+        ap.b = z;
+    } else if (fid < 20) {
+        int e = fid - 8, axis = e / 4, bits = e % 4, o1, o2;
+        edge_other_axes(axis, o1, o2);
+        np::V p = z;
+        np::setc(p, o1, (bits & 1) ? np::comp(h, o1) : -np::comp(h, o1));
+        np::setc(p, o2, (bits & 2) ? np::comp(h, o2) : -np::comp(h, o2));
+        ap.kind = AP_SEGMENT;
+        ap.a = p;
+        ap.b = p;
+        np::setc(ap.a, axis, -np::comp(h, axis));
+        np::setc(ap.b, axis, np::comp(h, axis));
+    } else {
+        int f = fid - 20, axis = f / 2, pos = f % 2;
+        ap.kind = AP_PLANE;
+        ap.a = z;
+        ap.b = z;
+        np::setc(ap.a, axis, pos ? np::comp(h, axis) : -np::comp(h, axis));
+        np::setc(ap.b, axis, pos ? 1.0f : -1.0f);
+    }
+    return ap;
+}
+
+__device__ __forceinline__ Approx feature_of(uint32_t shape, np::V h, int fid) {
+    if (shape == SHAPE_BALL) {
+        Approx ap;
+        ap.kind = AP_POINT;
+        ap.a = ap.b = np::mk(0.0f, 0.0f, 0.0f);
+        return ap;
+    }
+    return box_feature(h, fid);
+}
+
+__device__ __forceinline__ float clamp01(float x) { return np_min(np_max(x, 0.0f), 1.0f); }
+
+// Ericson, Real-Time Collision Detection 5.1.9.
+__device__ __forceinline__ void closest_segment_segment(np::V p1, np::V q1, np::V p2, np::V q2, np::V& c1, np::V& c2) {
+    const float eps = FLT_EPSILON;
+    np::V d1 = np::sub(q1, p1), d2 = np::sub(q2, p2), r = np::sub(p1, p2);
+    float a = np::dot(d1, d1), e = np::dot(d2, d2), f = np::dot(d2, r);
+    float s, t;
+    if (a <= eps && e <= eps) {
+        s = 0.0f;
+        t = 0.0f;
+    } else if (a <= eps) {
+        s = 0.0f;
+        t = clamp01(f / e);
+    } else {
+        float c = np::dot(d1, r);
+        if (e <= eps) {
+            t = 0.0f;
+            s = clamp01(-c / a);
+        } else {
+            float b = np::dot(d1, d2);
+            float denom = a * e - b * b;
+            s = (denom != 0.0f) ? clamp01((b * f - c * e) / denom) : 0.0f;
+            t = (b * s + f) / e;
+            if (t < 0.0f) {
+                t = 0.0f;
+                s = clamp01(-c / a);
+            } else if (t > 1.0f) {
+                t = 1.0f;
+                s = clamp01((b - c) / a);
+            }
+        }
+    }
+    c1 = np::add(p1, np::mul(d1, s));
+    c2 = np::add(p2, np::mul(d2, t));
+}
+
+struct Geom {
+    np::V w1, w2, n;
+    float depth;
+};
+
+// ContactKinematic::contact for Point / Segment / Plane approximations.
+__device__ __forceinline__ Geom kinematic_contact(const Approx& a1, const np::Iso& m1, float dil1, const Approx& a2,
+                                                  const np::Iso& m2, float dil2, np::V n0) {
+    np::V q1, q2, n;
+    float s;
+    if (a1.kind == AP_PLANE && a2.kind == AP_POINT) {
+        n = np::qrot(m1.q, a1.b);
+        np::V p1 = np::iso_pt(m1, a1.a);
+        np::V p2 = np::iso_pt(m2, a2.a);
+        s = np::dot(np::sub(p2, p1), n);
+        q1 = np::sub(p2, np::mul(n, s));
+        q2 = p2;
+    } else if (a1.kind == AP_POINT && a2.kind == AP_PLANE) {
+        np::V n2 = np::qrot(m2.q, a2.b);
+        np::V p1 = np::iso_pt(m1, a1.a);
+        np::V p2 = np::iso_pt(m2, a2.a);
+        s = np::dot(np::sub(p1, p2), n2);
+        q1 = p1;
+        q2 = np::sub(p1, np::mul(n2, s));
+        n = np::neg(n2);
+    } else {
+        np::V s1a = np::iso_pt(m1, a1.a);
+        np::V s1b = (a1.kind == AP_SEGMENT) ? np::iso_pt(m1, a1.b) : s1a;
+        np::V s2a = np::iso_pt(m2, a2.a);
+        np::V s2b = (a2.kind == AP_SEGMENT) ? np::iso_pt(m2, a2.b) : s2a;
+        closest_segment_segment(s1a, s1b, s2a, s2b, q1, q2);
+        np::V v = np::sub(q2, q1);
+        float l2 = np::dot(v, v);
+        const float eps = FLT_EPSILON;
+        if (l2 > eps * eps) {
+            float l = sqrtf(l2);
+            n = np::divs(v, l);
+            s = l;
+            if (np::dot(n, n0) < 0.0f) {
+                n = np::neg(n);
+                s = -l;
+            }
+        } else {
+            n = n0;
+            s = 0.0f;
+        }
+    }
+    Geom g;
+    g.w1 = np::add(q1, np::mul(n, dil1));
+    g.w2 = np::sub(q2, np::mul(n, dil2));
+    g.n = n;
+    g.depth = (dil1 + dil2) - s;
+    return g;
+}
+
+// A collider as seen by the narrow phase.
+struct Shape {
+    uint32_t shape;
+    np::V h;         // half extents (cuboid) or (radius, 0, 0)
+    float radius;
+    np::Iso pose;
+    __device__ float dil() const { return shape == SHAPE_BALL ? radius : 0.0f; }
+};
+
+struct Cand {
+    int f1, f2;
+    Geom g;
+};
+
+struct CandList {
+    Cand c[8];
+    int n;
+};
+
+__device__ __forceinline__ void push_eval(CandList& out, const Shape& s1, const Shape& s2, int f1, int f2, np::V n0,
+                                          float prediction) {
+    Geom g = kinematic_contact(feature_of(s1.shape, s1.h, f1), s1.pose, s1.dil(), feature_of(s2.shape, s2.h, f2),
+                               s2.pose, s2.dil(), n0);
+    if (g.depth >= -prediction && out.n < 8) {
+        out.c[out.n].f1 = f1;
+        out.c[out.n].f2 = f2;
+        out.c[out.n].g = g;
+        out.n++;
+    }
+}
+
+// Ball (sb) against cuboid (sx): closest point of the cuboid to the center.
+__device__ __forceinline__ void ball_box(const Shape& sb, const Shape& sx, bool box_first, float prediction,
+                                         CandList& out) {
+    np::V c = np::iso_inv_pt(sx.pose, sb.pose.t);
+    np::V h = sx.h;
+    int sign[3], nclamped = 0;
+    np::V p = c;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        float ck = np::comp(c, k), hk = np::comp(h, k);
+        if (ck > hk) {
+            sign[k] = 1;
+            np::setc(p, k, hk);
+            ++nclamped;
+        } else if (ck < -hk) {
+            sign[k] = -1;
+            np::setc(p, k, -hk);
+            ++nclamped;
+        } else {
+            sign[k] = 0;
+        }
+    }
+    int fid;
+    np::V nl;
+    if (nclamped == 0) {
+        int best = 0;
+        float bd = np::comp(h, 0) - fabsf(np::comp(c, 0));
+        for (int k = 1; k < 3; ++k) {
+            float dk = np::comp(h, k) - fabsf(np::comp(c, k));
+            if (dk < bd) {
+                bd = dk;
+                best = k;
+            }
+        }
+        int pos = np::comp(c, best) >= 0.0f ? 1 : 0;
+        fid = box_face_id(best, pos);
+        nl = np::mk(0.0f, 0.0f, 0.0f);
+        np::setc(nl, best, pos ? 1.0f : -1.0f);
+    } else {
+        if (nclamped == 1) {
+            int k = sign[0] ? 0 : (sign[1] ? 1 : 2);
+            fid = box_face_id(k, sign[k] > 0 ? 1 : 0);
+        } else if (nclamped == 2) {
+            int a = !sign[0] ? 0 : (!sign[1] ? 1 : 2), o1, o2;
+            edge_other_axes(a, o1, o2);
+            fid = box_edge_id(a, sign[o1] > 0 ? 1 : 0, sign[o2] > 0 ? 1 : 0);
+        } else {
+            fid = box_vertex_id(sign[0] > 0, sign[1] > 0, sign[2] > 0);
+        }
+        np::V v = np::sub(c, p);
+        nl = np::divs(v, np::norm(v));
+    }
+    np::V n = np::qrot(sx.pose.q, nl);
+    if (box_first) push_eval(out, sx, sb, fid, 0, n, prediction);
+    else push_eval(out, sb, sx, 0, fid, np::neg(n), prediction);
+}
+
+struct PV {
+    np::V p;
+    int tag, a, b, esrc;
+};
+
+// Keeps at most 4 candidates (deepest, farthest, largest triangle, largest
+// growth), in their original order. Writes the kept indices to keep[].
+__device__ __forceinline__ int reduce4(const CandList& c, int keep[4]) {
+    int n = c.n;
+    if (n <= 4) {
+        for (int k = 0; k < n; ++k) keep[k] = k;
+        return n;
+    }
+    int i0 = 0;
+    for (int k = 1; k < n; ++k)
+        if (c.c[k].g.depth > c.c[i0].g.depth) i0 = k;
+    int i1 = -1;
+    float bd = -1.0f;
+    for (int k = 0; k < n; ++k) {
+        if (k == i0) continue;
+        np::V d = np::sub(c.c[k].g.w1, c.c[i0].g.w1);
+        float dd = np::dot(d, d);
+        if (dd > bd) {
+            bd = dd;
+            i1 = k;
+        }
+    }
+    int i2 = -1;
+    float ba = -1.0f;
+    np::V e01 = np::sub(c.c[i1].g.w1, c.c[i0].g.w1);
+    for (int k = 0; k < n; ++k) {
+        if (k == i0 || k == i1) continue;
+        np::V cr = np::cross(e01, np::sub(c.c[k].g.w1, c.c[i0].g.w1));
+        float aa = np::dot(cr, cr);
+        if (aa > ba) {
+            ba = aa;
+            i2 = k;
+        }
+    }
+    int i3 = -1;
+    float bs = -1.0f;
+    np::V a = c.c[i0].g.w1, b = c.c[i1].g.w1, cc = c.c[i2].g.w1;
+    for (int k = 0; k < n; ++k) {
+        if (k == i0 || k == i1 || k == i2) continue;
+        np::V x = c.c[k].g.w1;
+        float s = np::norm(np::cross(np::sub(x, a), np::sub(x, b))) + np::norm(np::cross(np::sub(x, b), np::sub(x, cc))) +
+                  np::norm(np::cross(np::sub(x, cc), np::sub(x, a)));
+        if (s > bs) {
+            bs = s;
+            i3 = k;
+        }
+    }
+    int m = 0;
+    for (int k = 0; k < n; ++k)
+        if (k == i0 || k == i1 || k == i2 || k == i3) keep[m++] = k;
+    return m;
+}
+
+__device__ __forceinline__ float box_radius_along(const np::V ax[3], np::V h, np::V L) {
+    return h.x * fabsf(np::dot(ax[0], L)) + h.y * fabsf(np::dot(ax[1], L)) + h.z * fabsf(np::dot(ax[2], L));
+}
+
+// Cuboid A (collider 1) against cuboid B (collider 2).
+static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, float prediction, CandList& out) {
+    np::M RA = np::qmat(A.pose.q), RB = np::qmat(B.pose.q);
+    np::V axA[3] = {np::mcol(RA, 0), np::mcol(RA, 1), np::mcol(RA, 2)};
+    np::V axB[3] = {np::mcol(RB, 0), np::mcol(RB, 1), np::mcol(RB, 2)};
+    np::V d = np::sub(B.pose.t, A.pose.t);
+    float sepA = -FLT_MAX, sepB = -FLT_MAX, sepE = -FLT_MAX;
+    int ia = 0, ib = 0, ea = -1, eb = -1;
+    np::V LE = np::mk(0.0f, 0.0f, 0.0f);
+    for (int i = 0; i < 3; ++i) {
+        np::V L = axA[i];
+        float rb = box_radius_along(axB, B.h, L);
+        float sep = fabsf(np::dot(d, L)) - (np::comp(A.h, i) + rb);
+        if (sep > prediction) return;
+        if (sep > sepA) {
+            sepA = sep;
+            ia = i;
+        }
+    }
+    for (int j = 0; j < 3; ++j) {
+        np::V L = axB[j];
+        float ra = box_radius_along(axA, A.h, L);
+        float sep = fabsf(np::dot(d, L)) - (ra + np::comp(B.h, j));
+        if (sep > prediction) return;
+        if (sep > sepB) {
+            sepB = sep;
+            ib = j;
+        }
+    }
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) {
+            np::V L = np::cross(axA[i], axB[j]);
+            float len = np::norm(L);
+            if (len < 1e-5f) continue;
+            L = np::divs(L, len);
+            float ra = box_radius_along(axA, A.h, L);
+            float rb = box_radius_along(axB, B.h, L);
+            float sep = fabsf(np::dot(d, L)) - (ra + rb);
+            if (sep > prediction) return;
+            if (sep > sepE) {
+                sepE = sep;
+                ea = i;
+                eb = j;
+                LE = L;
+            }
+        }
+    }
+    bool refA = !(sepB > sepA + 1e-4f);
+    float sepF = refA ? sepA : sepB;
+    if (ea >= 0 && sepE > sepF + 5e-3f) {
+        np::V L = LE;
+        if (np::dot(d, L) < 0.0f) L = np::neg(L);
+        int o1, o2;
+        edge_other_axes(ea, o1, o2);
+        int fa = box_edge_id(ea, np::dot(axA[o1], L) > 0.0f ? 1 : 0, np::dot(axA[o2], L) > 0.0f ? 1 : 0);
+        edge_other_axes(eb, o1, o2);
+        int fb = box_edge_id(eb, np::dot(axB[o1], L) < 0.0f ? 1 : 0, np::dot(axB[o2], L) < 0.0f ? 1 : 0);
+        push_eval(out, A, B, fa, fb, L, prediction);
+        return;
+    }
+    const Shape& Rf = refA ? A : B;
+    const Shape& In = refA ? B : A;
+    const np::V* axR = refA ? axA : axB;
+    const np::V* axI = refA ? axB : axA;
+    int ri = refA ? ia : ib;
+    np::V dRI = refA ? d : np::neg(d);
+    int rpos = np::dot(dRI, axR[ri]) >= 0.0f ? 1 : 0;
+    np::V nref = rpos ? axR[ri] : np::neg(axR[ri]);
+    int ik = 0;
+    float best = fabsf(np::dot(axI[0], nref));
+    for (int k = 1; k < 3; ++k) {
+        float v = fabsf(np::dot(axI[k], nref));
+        if (v > best) {
+            best = v;
+            ik = k;
+        }
+    }
+    int ipos = np::dot(axI[ik], nref) < 0.0f ? 1 : 0;
+    int ref_face = box_face_id(ri, rpos), inc_face = box_face_id(ik, ipos);
+    int u = (ik + 1) % 3, v = (ik + 2) % 3;
+    const int su[4] = {0, 1, 1, 0}, sv[4] = {0, 0, 1, 1};
+    PV poly[8], next[8];
+    int np_ = 0, nn = 0;
+    int vids[4];
+    for (int k = 0; k < 4; ++k) {
+        int s[3];
+        s[ik] = ipos;
+        s[u] = su[k];
+        s[v] = sv[k];
+        vids[k] = box_vertex_id(s[0], s[1], s[2]);
+    }
+    for (int k = 0; k < 4; ++k) {
+        int a = vids[k], b = vids[(k + 1) % 4];
+        int diff = a ^ b, axis = diff == 1 ? 0 : (diff == 2 ? 1 : 2), o1, o2;
+        edge_other_axes(axis, o1, o2);
+        int eid = box_edge_id(axis, (a >> o1) & 1, (a >> o2) & 1);
+        Approx ap = box_feature(In.h, a);
+        np::V w = np::iso_pt(In.pose, ap.a);
+        poly[np_].p = np::iso_inv_pt(Rf.pose, w);
+        poly[np_].tag = 0;
+        poly[np_].a = a;
+        poly[np_].b = -1;
+        poly[np_].esrc = eid;
+        ++np_;
+    }
+    int ru = (ri + 1) % 3, rv = (ri + 2) % 3;
+    const int planes_axis[4] = {ru, ru, rv, rv};
+    const int planes_pos[4] = {1, 0, 1, 0};
+    for (int pl = 0; pl < 4 && np_ > 0; ++pl) {
+        int ax = planes_axis[pl], pp = planes_pos[pl];
+        float hc = np::comp(Rf.h, ax);
+        nn = 0;
+        for (int k = 0; k < np_; ++k) {
+            const PV P = poly[k];
+            const PV Q = poly[(k + 1) % np_];
+            float dp = (pp ? np::comp(P.p, ax) : -np::comp(P.p, ax)) - hc;
+            float dq = (pp ? np::comp(Q.p, ax) : -np::comp(Q.p, ax)) - hc;
+            bool pin = dp <= 0.0f, qin = dq <= 0.0f;
+            if (pin && nn < 8) next[nn++] = P;
+            if (pin != qin) {
+                float t = dp / (dp - dq);
+                PV X;
+                X.p = np::add(P.p, np::mul(np::sub(Q.p, P.p), t));
+                int third = 3 - ri - ax;
+                int s[3];
+                s[ri] = rpos;
+                s[ax] = pp;
+                if (P.esrc >= 0) {
+                    int o1, o2;
+                    edge_other_axes(third, o1, o2);
+                    X.tag = 1;
+                    X.a = box_edge_id(third, s[o1], s[o2]);
+                    X.b = P.esrc;
+                } else {
+                    int other_plane = -P.esrc - 1;
+                    s[planes_axis[other_plane]] = planes_pos[other_plane];
+                    X.tag = 2;
+                    X.a = box_vertex_id(s[0], s[1], s[2]);
+                    X.b = -1;
+                }
+                X.esrc = pin ? -(1 + pl) : P.esrc;
+                if (nn < 8) next[nn++] = X;
+            }
+        }
+        for (int k = 0; k < nn; ++k) poly[k] = next[k];
+        np_ = nn;
+    }
+    np::V n0 = refA ? nref : np::neg(nref);
+    CandList cands;
+    cands.n = 0;
+    for (int k = 0; k < np_; ++k) {
+        const PV& P = poly[k];
+        int fr, fi;
+        if (P.tag == 0) {
+            fr = ref_face;
+            fi = P.a;
+        } else if (P.tag == 1) {
+            fr = P.a;
+            fi = P.b;
+        } else {
+            fr = P.a;
+            fi = inc_face;
+        }
+        if (refA) push_eval(cands, A, B, fr, fi, n0, prediction);
+        else push_eval(cands, A, B, fi, fr, n0, prediction);
+    }
+    int keep[4];
+    int m = reduce4(cands, keep);
+    for (int k = 0; k < m; ++k) out.c[out.n++] = cands.c[keep[k]];
+}
+
+}  // namespace npgpu_dev

@@ -1,0 +1,964 @@
+// npgpu_world.cu -- host side of the GPU mechanical world and the C ABI of
+// include/npgpu.h.
+//
+// The host keeps what the reference's sets and GeometricalWorld keep on the
+// CPU (handles, generations, the mass bookkeeping of collider insertion and
+// removal, src/world/geometrical_world.rs:102-227); everything the step
+// touches lives on the device (world_dev.cuh).
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/npgpu.h"
+#include "world_dev.cuh"
+
+using namespace npgpu_dev;
+
+namespace {
+
+struct HostBody {
+    bool alive = false;
+    uint64_t gen = 0;
+    uint32_t kind = 0, status = 0, flags = 0, world = 0;
+    float mass = 0.0f;
+    np::M local_I;
+    np::V local_com{0.0f, 0.0f, 0.0f};
+};
+
+struct HostCollider {
+    bool alive = false;
+    bool registered = false;
+    uint64_t gen = 0;
+    npgpu_collider_desc desc;
+};
+
+bool finite_n(const float* v, int n) {
+    for (int k = 0; k < n; ++k)
+        if (!std::isfinite(v[k])) return false;
+    return true;
+}
+
+// Volumetric::transformed_mass_properties for Ball / Cuboid
+// (src/volumetric/volumetric.rs:55-59, volumetric_ball.rs:8-47, volumetric_cuboid.rs:9-78).
+void collider_mass_properties(const npgpu_collider_desc& d, np::V& com, float& mass, np::M& ang) {
+    const float pi = 3.14159265358979323846f;
+    np::M unit = np::mzero();
+    if (d.shape == NPGPU_SHAPE_BALL) {
+        float r = d.shape_params[0];
+        float vol = pi * r * r * r * (float)(4.0 / 3.0);
+        mass = vol * d.density;
+        float diag = r * r * (float)(2.0 / 5.0);
+        unit.m[0][0] = unit.m[1][1] = unit.m[2][2] = diag;
+    } else {
+        float vol = 1.0f;
+        vol = vol * d.shape_params[0] * 2.0f;
+        vol = vol * d.shape_params[1] * 2.0f;
+        vol = vol * d.shape_params[2] * 2.0f;
+        mass = vol * d.density;
+        float w = (float)(1.0 / 12.0) * 2.0f * 2.0f;
+        float ix = w * d.shape_params[0] * d.shape_params[0];
+        float iy = w * d.shape_params[1] * d.shape_params[1];
+        float iz = w * d.shape_params[2] * d.shape_params[2];
+        unit.m[0][0] = iy + iz;
+        unit.m[1][1] = ix + iz;
+        unit.m[2][2] = ix + iy;
+    }
+    np::M local = np::mscale(unit, mass);
+    np::Iso wrt{np::mk(d.position_wrt_body[0], d.position_wrt_body[1], d.position_wrt_body[2]),
+                np::Q{d.position_wrt_body[3], d.position_wrt_body[4], d.position_wrt_body[5], d.position_wrt_body[6]}};
+    com = np::iso_pt(wrt, np::mk(0.0f, 0.0f, 0.0f));
+    np::M rot = np::qmat(wrt.q);
+    ang = np::mm(np::mm(rot, local), np::mtr(rot));
+}
+
+// RigidBody::add_local_inertia_and_com, the part that does not need the pose
+// (src/object/rigid_body.rs:747-766).
+void add_local_inertia_and_com(HostBody& b, np::V com, float mass, const np::M& ang) {
+    float mass_sum = b.mass + mass;
+    if (mass_sum != 0.0f) b.local_com = np::divs(np::add(np::mul(b.local_com, b.mass), np::mul(com, mass)), mass_sum);
+    else b.local_com = np::mk(0.0f, 0.0f, 0.0f);
+    b.mass = b.mass + mass;
+    b.local_I = np::madd(b.local_I, ang);
+}
+
+template <class T>
+cudaError_t dalloc(T** p, size_t n, std::vector<void*>& owned) {
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMalloc((void**)p, sizeof(T) * n);
+    if (e == cudaSuccess) {
+        owned.push_back(*p);
+        cudaMemset(*p, 0, sizeof(T) * n);
+    }
+    return e;
+}
+
+}  // namespace
+
+struct npgpu_world {
+    npgpu_params params;
+    float gravity[3];
+    uint32_t cap_b = 0, cap_c = 0, cap_p = 0;
+    std::vector<HostBody> hb;
+    std::vector<HostCollider> hc;
+    uint32_t nb_slots = 0, nc_slots = 0, nc_alive = 0;
+    World dw;
+    Pairs pa, pb;
+    Control* ctl = nullptr;
+    cudaStream_t stream = nullptr;
+    int device = 0;
+    int solve_grid = 0;
+    void* sort_temp = nullptr;
+    size_t sort_bytes = 0;
+    void* scan_temp = nullptr;
+    size_t scan_bytes = 0;
+    uint8_t* d_forget = nullptr;
+    std::vector<uint8_t> forget;
+    bool forget_pending = false;
+    bool cd_dirty = true;
+    std::vector<MassUpdate> pending_mass;
+    // Staging.
+    void* h_stage = nullptr;
+    size_t h_stage_bytes = 0;
+    void* d_stage = nullptr;
+    size_t d_stage_bytes = 0;
+    cudaEvent_t ev_stage = nullptr;
+    std::vector<void*> owned;
+    std::string last_error;
+    npgpu_counters counters;
+    cudaEvent_t ev[8];
+    bool ev_recorded = false;
+    bool cd_start_ran = false;
+};
+
+static std::string g_create_error;
+
+static npgpu_status fail(npgpu_world* w, npgpu_status s, const std::string& msg) {
+    if (w) w->last_error = msg;
+    else g_create_error = msg;
+    return s;
+}
+
+static npgpu_status cuda_fail(npgpu_world* w, cudaError_t e, const char* what) {
+    return fail(w, NPGPU_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(expr, what)                                        \
+    do {                                                      \
+        cudaError_t _e = (expr);                              \
+        if (_e != cudaSuccess) return cuda_fail(w, _e, what); \
+    } while (0)
+
+static StepParams step_params(const npgpu_world* w) {
+    const npgpu_params& p = w->params;
+    StepParams s;
+    s.dt = p.dt;
+    s.inv_dt = (p.dt == 0.0f) ? 0.0f : 1.0f / p.dt;
+    s.erp = p.erp;
+    s.warmstart_coeff = p.warmstart_coeff;
+    s.restitution_threshold = p.restitution_velocity_threshold;
+    s.allowed_linear_error = p.allowed_linear_error;
+    s.max_linear_correction = p.max_linear_correction;
+    s.activation_mix = p.activation_mix;
+    s.broad_phase_margin = p.broad_phase_margin;
+    s.gx = w->gravity[0];
+    s.gy = w->gravity[1];
+    s.gz = w->gravity[2];
+    s.residual_tolerance = p.residual_tolerance;
+    s.max_velocity_iterations = p.max_velocity_iterations;
+    s.max_position_iterations = p.max_position_iterations;
+    s.solve_to_tolerance = p.solve_to_tolerance;
+    s.max_iterations_to_tolerance = p.max_iterations_to_tolerance;
+    s.warmstart_mode = p.warmstart_mode;
+    s.profile = p.profile;
+    return s;
+}
+
+// Copies `bytes` from host memory to the device staging area (synchronously
+// with respect to earlier uses of the staging area) and returns its device pointer.
+static npgpu_status stage_upload(npgpu_world* w, const void* src, size_t bytes, void** dptr) {
+    CK(cudaEventSynchronize(w->ev_stage), "staging wait");
+    if (bytes > w->h_stage_bytes) {
+        if (w->h_stage) cudaFreeHost(w->h_stage);
+        w->h_stage = nullptr;
+        size_t nb = std::max(bytes, w->h_stage_bytes * 2);
+        CK(cudaMallocHost(&w->h_stage, nb), "pinned staging");
+        w->h_stage_bytes = nb;
+    }
+    if (bytes > w->d_stage_bytes) {
+        if (w->d_stage) cudaFree(w->d_stage);
+        w->d_stage = nullptr;
+        size_t nb = std::max(bytes, w->d_stage_bytes * 2);
+        CK(cudaMalloc(&w->d_stage, nb), "device staging");
+        w->d_stage_bytes = nb;
+    }
+    std::memcpy(w->h_stage, src, bytes);
+    CK(cudaMemcpyAsync(w->d_stage, w->h_stage, bytes, cudaMemcpyHostToDevice, w->stream), "staging copy");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    *dptr = w->d_stage;
+    return NPGPU_OK;
+}
+
+static void sync_world_view(npgpu_world* w) {
+    w->dw.nb_slots = w->nb_slots;
+    w->dw.nc_slots = w->nc_slots;
+    w->dw.nc_alive = w->nc_alive;
+}
+
+extern "C" {
+
+uint32_t npgpu_abi_version(void) { return NPGPU_ABI_VERSION; }
+
+void npgpu_default_params(npgpu_params* p) {
+    if (!p) return;
+    std::memset(p, 0, sizeof(*p));
+    p->dt = 1.0f / 60.0f;
+    p->erp = 0.2f;
+    p->warmstart_coeff = 1.0f;
+    p->restitution_velocity_threshold = 1.0f;
+    p->allowed_linear_error = 0.001f;
+    p->allowed_angular_error = 0.001f;
+    p->max_linear_correction = 0.2f;
+    p->max_angular_correction = 0.2f;
+    p->max_stabilization_multiplier = 0.2f;
+    p->max_velocity_iterations = 8;
+    p->max_position_iterations = 3;
+    p->max_ccd_position_iterations = 10;
+    p->max_ccd_substeps = 1;
+    p->solve_to_tolerance = 0;
+    p->residual_tolerance = 1e-4f;
+    p->max_iterations_to_tolerance = 256;
+    p->warmstart_mode = 0;
+    p->broad_phase_margin = 0.01f;
+    p->activation_mix = 0.01f;
+    p->profile = 0;
+}
+
+static npgpu_status create_buffers(npgpu_world* w) {
+    auto& o = w->owned;
+    uint32_t B = w->cap_b, Cn = w->cap_c, P = w->cap_p;
+    Bodies& b = w->dw.b;
+#define A(ptr, n) CK(dalloc(&(ptr), (n), o), "cudaMalloc")
+    A(b.pos_t, B); A(b.pos_q, B); A(b.lin, B); A(b.ang, B); A(b.com, B); A(b.local_com, B);
+    A(b.mass, B); A(b.local_I, 9 * (size_t)B); A(b.I, 9 * (size_t)B); A(b.inv_mass, B); A(b.inv_I, 9 * (size_t)B);
+    A(b.acc_lin, B); A(b.acc_ang, B); A(b.f_lin, B); A(b.f_ang, B);
+    A(b.lin_damp, B); A(b.ang_damp, B); A(b.max_lin, B); A(b.max_ang, B); A(b.sleep_thr, B); A(b.energy, B);
+    A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
+    A(b.jp_best, B); A(b.jp_used, B);
+    Colliders& c = w->dw.c;
+    A(c.body, Cn); A(c.info, Cn); A(c.params, Cn); A(c.wrt_t, Cn); A(c.wrt_q, Cn);
+    A(c.margin, Cn); A(c.lin_pred, Cn); A(c.friction, Cn); A(c.restitution, Cn); A(c.rank, Cn);
+    A(c.pose_t, Cn); A(c.pose_q, Cn); A(c.aabb_min, Cn); A(c.aabb_max, Cn);
+    A(c.keys, Cn); A(c.keys_sorted, Cn); A(c.vals, Cn); A(c.vals_sorted, Cn);
+    A(c.left, Cn); A(c.right, Cn); A(c.parent, 2 * (size_t)Cn); A(c.node_min, 2 * (size_t)Cn);
+    A(c.node_max, 2 * (size_t)Cn); A(c.node_flag, Cn); A(c.leaf_count, Cn); A(c.leaf_offset, Cn);
+    for (Pairs* pp : {&w->pa, &w->pb}) {
+        A(pp->pair, P); A(pp->owner_start, Cn); A(pp->owner_count, Cn); A(pp->ncont, P);
+        A(pp->key, 4 * (size_t)P); A(pp->w1, 4 * (size_t)P); A(pp->w2, 4 * (size_t)P); A(pp->n, 4 * (size_t)P);
+        A(pp->imp, 4 * (size_t)P); A(pp->nl, 4 * (size_t)P);
+    }
+    Solver& s = w->dw.s;
+    A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_state, P); A(s.sm_sorted, P); A(s.sm_b1, P); A(s.sm_b2, P);
+    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats);
+    A(s.colour_count, kMaxColours); A(s.colour_start, kMaxColours + 1); A(s.colour_cursor, kMaxColours);
+    A(w->ctl, 1);
+    A(w->d_forget, Cn);
+#undef A
+    w->dw.ctl = w->ctl;
+    w->dw.cur = w->pa;
+    w->dw.prev = w->pb;
+    w->dw.cap_pairs = P;
+    w->sort_bytes = sort_temp_bytes(Cn);
+    w->scan_bytes = scan_temp_bytes(Cn);
+    CK(cudaMalloc(&w->sort_temp, std::max<size_t>(w->sort_bytes, 16)), "sort temp");
+    o.push_back(w->sort_temp);
+    CK(cudaMalloc(&w->scan_temp, std::max<size_t>(w->scan_bytes, 16)), "scan temp");
+    o.push_back(w->scan_temp);
+    CK(cudaDeviceSynchronize(), "create");
+    return NPGPU_OK;
+}
+
+npgpu_world* npgpu_create(const npgpu_params* params, const float gravity[3], uint32_t capacity_bodies,
+                          uint32_t capacity_colliders, uint32_t capacity_pairs, npgpu_status* status) {
+    npgpu_status st = NPGPU_OK;
+    npgpu_world* w = nullptr;
+    do {
+        if (!params || !gravity) {
+            st = fail(nullptr, NPGPU_ERR_INVALID_ARGUMENT, "params and gravity are required");
+            break;
+        }
+        if (capacity_bodies >= (1u << 21) || capacity_colliders >= (1u << 21)) {
+            st = fail(nullptr, NPGPU_ERR_CAPACITY, "at most 2^21 - 1 bodies and colliders per world");
+            break;
+        }
+        int ndev = 0;
+        if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+            cudaGetLastError();
+            st = fail(nullptr, NPGPU_ERR_CUDA, "no CUDA device");
+            break;
+        }
+        w = new npgpu_world;
+        w->params = *params;
+        std::memcpy(w->gravity, gravity, sizeof(w->gravity));
+        w->cap_b = std::max(capacity_bodies, 1u);
+        w->cap_c = std::max(capacity_colliders, 1u);
+        w->cap_p = std::max(capacity_pairs, 1u);
+        w->hb.resize(w->cap_b);
+        w->hc.resize(w->cap_c);
+        for (auto& b : w->hb) b.local_I = np::mzero();
+        w->forget.assign(w->cap_c, 0);
+        std::memset(&w->counters, 0, sizeof(w->counters));
+        cudaGetDevice(&w->device);
+        int coop = 0;
+        cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, w->device);
+        if (!coop) {
+            st = fail(nullptr, NPGPU_ERR_CUDA, "device does not support cooperative launches");
+            break;
+        }
+        if (cudaStreamCreateWithFlags(&w->stream, cudaStreamNonBlocking) != cudaSuccess) {
+            st = fail(nullptr, NPGPU_ERR_CUDA, "stream creation failed");
+            break;
+        }
+        cudaEventCreateWithFlags(&w->ev_stage, cudaEventDisableTiming);
+        cudaEventRecord(w->ev_stage, w->stream);
+        for (auto& e : w->ev) cudaEventCreate(&e);
+        st = create_buffers(w);
+        if (st != NPGPU_OK) {
+            g_create_error = w->last_error;
+            break;
+        }
+        w->solve_grid = solve_grid_size(w->device);
+    } while (0);
+    if (status) *status = st;
+    if (st != NPGPU_OK && w) {
+        npgpu_destroy(w);
+        w = nullptr;
+    }
+    return w;
+}
+
+void npgpu_destroy(npgpu_world* w) {
+    if (!w) return;
+    if (w->stream) cudaStreamSynchronize(w->stream);
+    for (void* p : w->owned) cudaFree(p);
+    if (w->d_stage) cudaFree(w->d_stage);
+    if (w->h_stage) cudaFreeHost(w->h_stage);
+    if (w->ev_stage) cudaEventDestroy(w->ev_stage);
+    for (auto& e : w->ev)
+        if (e) cudaEventDestroy(e);
+    if (w->stream) cudaStreamDestroy(w->stream);
+    delete w;
+}
+
+void* npgpu_stream(npgpu_world* w) { return w ? (void*)w->stream : nullptr; }
+
+npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params) {
+    if (!w || !params) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (!(params->dt >= 0.0f)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "dt must be >= 0");
+    w->params = *params;
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_set_gravity(npgpu_world* w, const float gravity[3]) {
+    if (!w || !gravity) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (!finite_n(gravity, 3)) return fail(w, NPGPU_ERR_NAN, "gravity is not finite");
+    std::memcpy(w->gravity, gravity, sizeof(w->gravity));
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                 const npgpu_body_desc* descs) {
+    if (!w || (n && (!handles || !descs))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<BodyUpload> up;
+    up.reserve(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const npgpu_body_desc& d = descs[k];
+        uint64_t slot = handles[k].index;
+        if (d.kind != NPGPU_KIND_RIGID_BODY && d.kind != NPGPU_KIND_GROUND)
+            return fail(w, NPGPU_ERR_UNSUPPORTED_BODY,
+                        "only rigid bodies and grounds are supported (multibody / FEM / mass-spring bodies are rejected)");
+        if (slot >= w->cap_b) return fail(w, NPGPU_ERR_CAPACITY, "body index beyond the world's capacity");
+        if (d.status > NPGPU_BODY_KINEMATIC) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "invalid body status");
+        if (!finite_n(d.position, 7) || !finite_n(d.velocity, 6) || !finite_n(d.local_inertia, 7) ||
+            !finite_n(d.local_com, 3) || !std::isfinite(d.linear_damping) || !std::isfinite(d.angular_damping) ||
+            std::isnan(d.max_linear_velocity) || std::isnan(d.max_angular_velocity) || !std::isfinite(d.sleep_threshold))
+            return fail(w, NPGPU_ERR_NAN, "body description has a non-finite value");
+        if (d.world >= 0xffffu) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "world index must be < 65535");
+        HostBody& hb = w->hb[slot];
+        bool is_new = !hb.alive;
+        BodyUpload u;
+        std::memset(&u, 0, sizeof(u));
+        u.slot = (uint32_t)slot;
+        uint32_t status = d.kind == NPGPU_KIND_GROUND ? (uint32_t)NPGPU_BODY_STATIC : d.status;
+        u.info = status | (d.kind << BI_KIND_SHIFT) | ((d.flags & 0x1ffu) << BI_FLAGS_SHIFT);
+        u.world = d.world;
+        u.reset_energy = is_new ? 1u : 0u;
+        std::memcpy(u.pos, d.position, sizeof(u.pos));
+        std::memcpy(u.vel, d.velocity, sizeof(u.vel));
+        if (d.kind == NPGPU_KIND_GROUND) {
+            float id[7] = {0, 0, 0, 0, 0, 0, 1};
+            std::memcpy(u.pos, id, sizeof(u.pos));
+            std::memset(u.vel, 0, sizeof(u.vel));
+        }
+        if (is_new) {
+            hb.mass = d.local_inertia[0];
+            np::M a = np::mzero();
+            a.m[0][0] = d.local_inertia[1];
+            a.m[0][1] = a.m[1][0] = d.local_inertia[2];
+            a.m[0][2] = a.m[2][0] = d.local_inertia[3];
+            a.m[1][1] = d.local_inertia[4];
+            a.m[1][2] = a.m[2][1] = d.local_inertia[5];
+            a.m[2][2] = d.local_inertia[6];
+            hb.local_I = a;
+            hb.local_com = np::mk(d.local_com[0], d.local_com[1], d.local_com[2]);
+        }
+        u.mass = hb.mass;
+        for (int r = 0; r < 3; ++r)
+            for (int cc = 0; cc < 3; ++cc) u.local_I[3 * r + cc] = hb.local_I.m[r][cc];
+        u.local_com[0] = hb.local_com.x;
+        u.local_com[1] = hb.local_com.y;
+        u.local_com[2] = hb.local_com.z;
+        u.lin_damp = d.linear_damping;
+        u.ang_damp = d.angular_damping;
+        u.max_lin = d.max_linear_velocity;
+        u.max_ang = d.max_angular_velocity;
+        u.sleep_thr = d.sleep_threshold;
+        hb.alive = true;
+        hb.gen = handles[k].generation;
+        hb.kind = d.kind;
+        hb.status = status;
+        hb.flags = d.flags;
+        hb.world = d.world;
+        w->nb_slots = std::max(w->nb_slots, (uint32_t)slot + 1);
+        up.push_back(u);
+    }
+    if (up.empty()) return NPGPU_OK;
+    void* dp = nullptr;
+    npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(BodyUpload), &dp);
+    if (st != NPGPU_OK) return st;
+    sync_world_view(w);
+    CK(launch_upload_bodies(w->dw, (const BodyUpload*)dp, (uint32_t)up.size(), w->stream), "upload bodies");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    w->cd_dirty = true;
+    return NPGPU_OK;
+}
+
+static bool body_handle_ok(const npgpu_world* w, const npgpu_handle& h) {
+    return h.index < w->cap_b && w->hb[h.index].alive && w->hb[h.index].gen == h.generation;
+}
+
+// Subtracts a registered collider's mass from its body and wakes the body
+// (geometrical_world.rs:179-194).
+static void unregister_collider_mass(npgpu_world* w, HostCollider& c, bool body_remains) {
+    if (!body_remains || !c.registered) return;
+    HostBody& b = w->hb[c.desc.body.index];
+    MassUpdate u;
+    std::memset(&u, 0, sizeof(u));
+    u.slot = (uint32_t)c.desc.body.index;
+    u.activate = 2u;   // bit 1: activate
+    if (c.desc.density != 0.0f && b.kind == NPGPU_KIND_RIGID_BODY) {
+        np::V com;
+        float mass;
+        np::M ang;
+        collider_mass_properties(c.desc, com, mass, ang);
+        add_local_inertia_and_com(b, np::neg(com), -mass, np::mscale(ang, -1.0f));
+        u.activate |= 1u;   // bit 0: the mass changed
+    }
+    u.mass = b.mass;
+    for (int r = 0; r < 3; ++r)
+        for (int cc = 0; cc < 3; ++cc) u.local_I[3 * r + cc] = b.local_I.m[r][cc];
+    u.local_com[0] = b.local_com.x;
+    u.local_com[1] = b.local_com.y;
+    u.local_com[2] = b.local_com.z;
+    w->pending_mass.push_back(u);
+}
+
+npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                    const npgpu_collider_desc* descs) {
+    if (!w || (n && (!handles || !descs))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<ColliderUpload> up;
+    up.reserve(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const npgpu_collider_desc& d = descs[k];
+        uint64_t slot = handles[k].index;
+        if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID)
+            return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "only Ball and Cuboid shapes are supported");
+        if (d.is_sensor) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "sensor colliders are not supported");
+        if (d.ccd_enabled) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "CCD-enabled colliders are not supported");
+        if (slot >= w->cap_c) return fail(w, NPGPU_ERR_CAPACITY, "collider index beyond the world's capacity");
+        if (!body_handle_ok(w, d.body)) return fail(w, NPGPU_ERR_INVALID_HANDLE, "collider parent body handle is invalid");
+        if (!finite_n(d.position_wrt_body, 7) || !finite_n(d.shape_params, 3) || !std::isfinite(d.margin) ||
+            !std::isfinite(d.density) || !std::isfinite(d.linear_prediction) || !std::isfinite(d.friction) ||
+            !std::isfinite(d.restitution))
+            return fail(w, NPGPU_ERR_NAN, "collider description has a non-finite value");
+        if (d.friction_combine > 3 || d.restitution_combine > 3)
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "invalid material combine mode");
+        HostCollider& hc = w->hc[slot];
+        if (hc.alive) {
+            unregister_collider_mass(w, hc, true);
+        } else {
+            w->nc_alive += 1;
+        }
+        hc.alive = true;
+        hc.registered = false;
+        hc.gen = handles[k].generation;
+        hc.desc = d;
+        w->forget[slot] = std::max<uint8_t>(w->forget[slot], 1);
+        w->forget_pending = true;
+        ColliderUpload u;
+        std::memset(&u, 0, sizeof(u));
+        u.slot = (uint32_t)slot;
+        u.body = (uint32_t)d.body.index;
+        u.info = d.shape | (d.friction_combine << 4) | (d.restitution_combine << 8);
+        u.params[0] = d.shape_params[0];
+        u.params[1] = d.shape_params[1];
+        u.params[2] = d.shape_params[2];
+        std::memcpy(u.wrt, d.position_wrt_body, sizeof(u.wrt));
+        u.margin = d.margin;
+        u.lin_pred = d.linear_prediction;
+        u.friction = d.friction;
+        u.restitution = d.restitution;
+        if (d.shape == NPGPU_SHAPE_BALL) u.rank = d.shape_params[0];
+        else u.rank = std::sqrt(d.shape_params[0] * d.shape_params[0] + d.shape_params[1] * d.shape_params[1] +
+                                d.shape_params[2] * d.shape_params[2]);
+        w->nc_slots = std::max(w->nc_slots, (uint32_t)slot + 1);
+        up.push_back(u);
+    }
+    if (up.empty()) return NPGPU_OK;
+    void* dp = nullptr;
+    npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(ColliderUpload), &dp);
+    if (st != NPGPU_OK) return st;
+    sync_world_view(w);
+    CK(launch_upload_colliders(w->dw, (const ColliderUpload*)dp, (uint32_t)up.size(), w->stream), "upload colliders");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    w->cd_dirty = true;
+    return NPGPU_OK;
+}
+
+static npgpu_status kill_slots(npgpu_world* w, const std::vector<uint32_t>& slots, int colliders) {
+    if (slots.empty()) return NPGPU_OK;
+    void* dp = nullptr;
+    npgpu_status st = stage_upload(w, slots.data(), slots.size() * sizeof(uint32_t), &dp);
+    if (st != NPGPU_OK) return st;
+    CK(launch_kill(w->dw, (const uint32_t*)dp, (uint32_t)slots.size(), colliders, w->stream), "kill");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_handle* handles) {
+    if (!w || (n && !handles)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    for (uint32_t k = 0; k < n; ++k) {
+        const npgpu_handle& h = handles[k];
+        if (h.index >= w->cap_c || !w->hc[h.index].alive || w->hc[h.index].gen != h.generation)
+            return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid collider handle");
+    }
+    std::vector<uint32_t> slots;
+    for (uint32_t k = 0; k < n; ++k) {
+        HostCollider& c = w->hc[handles[k].index];
+        unregister_collider_mass(w, c, true);
+        c.alive = false;
+        w->nc_alive -= 1;
+        w->forget[handles[k].index] = 2;
+        slots.push_back((uint32_t)handles[k].index);
+    }
+    w->forget_pending = true;
+    w->cd_dirty = true;
+    return kill_slots(w, slots, 1);
+}
+
+npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle* handles) {
+    if (!w || (n && !handles)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    for (uint32_t k = 0; k < n; ++k)
+        if (!body_handle_ok(w, handles[k])) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
+    std::vector<uint32_t> bslots, cslots;
+    for (uint32_t k = 0; k < n; ++k) {
+        uint64_t bi = handles[k].index;
+        for (uint32_t ci = 0; ci < w->nc_slots; ++ci) {
+            HostCollider& c = w->hc[ci];
+            if (c.alive && c.desc.body.index == bi) {
+                c.alive = false;
+                w->nc_alive -= 1;
+                w->forget[ci] = 2;
+                cslots.push_back(ci);
+            }
+        }
+        w->hb[bi].alive = false;
+        bslots.push_back((uint32_t)bi);
+    }
+    w->forget_pending = true;
+    w->cd_dirty = true;
+    npgpu_status st = kill_slots(w, cslots, 1);
+    if (st != NPGPU_OK) return st;
+    return kill_slots(w, bslots, 0);
+}
+
+npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* handles, const float* forces6,
+                                int auto_wake_up) {
+    if (!w || (n && (!handles || !forces6))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<ForceUpload> up(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        if (!body_handle_ok(w, handles[k])) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
+        if (!finite_n(forces6 + 6 * k, 6)) return fail(w, NPGPU_ERR_NAN, "force is not finite");
+        up[k].slot = (uint32_t)handles[k].index;
+        up[k].wake = auto_wake_up ? 1u : 0u;
+        std::memcpy(up[k].f, forces6 + 6 * k, sizeof(up[k].f));
+    }
+    if (up.empty()) return NPGPU_OK;
+    void* dp = nullptr;
+    npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(ForceUpload), &dp);
+    if (st != NPGPU_OK) return st;
+    CK(launch_forces(w->dw, (const ForceUpload*)dp, n, w->stream), "apply forces");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    return NPGPU_OK;
+}
+
+// GeometricalWorld::maintain at the start of a step: register the colliders
+// inserted since the last step, adding their mass to their body
+// (geometrical_world.rs:102-143), and forget the manifolds of removed colliders.
+static npgpu_status maintain(npgpu_world* w) {
+    for (uint32_t ci = 0; ci < w->nc_slots; ++ci) {
+        HostCollider& c = w->hc[ci];
+        if (!c.alive || c.registered) continue;
+        c.registered = true;
+        HostBody& b = w->hb[c.desc.body.index];
+        if (c.desc.density != 0.0f && b.kind == NPGPU_KIND_RIGID_BODY) {
+            np::V com;
+            float mass;
+            np::M ang;
+            collider_mass_properties(c.desc, com, mass, ang);
+            add_local_inertia_and_com(b, com, mass, ang);
+            MassUpdate u;
+            std::memset(&u, 0, sizeof(u));
+            u.slot = (uint32_t)c.desc.body.index;
+            u.activate = 1u;
+            u.mass = b.mass;
+            for (int r = 0; r < 3; ++r)
+                for (int cc = 0; cc < 3; ++cc) u.local_I[3 * r + cc] = b.local_I.m[r][cc];
+            u.local_com[0] = b.local_com.x;
+            u.local_com[1] = b.local_com.y;
+            u.local_com[2] = b.local_com.z;
+            w->pending_mass.push_back(u);
+        }
+        w->cd_dirty = true;
+    }
+    if (!w->pending_mass.empty()) {
+        // Each update carries the body's mass state after it was applied, so the
+        // last update of a body supersedes the earlier ones; their flags are merged.
+        std::vector<int32_t> last(w->nb_slots, -1);
+        std::vector<MassUpdate> merged;
+        for (const MassUpdate& u : w->pending_mass) {
+            int32_t& l = last[u.slot];
+            if (l < 0) {
+                l = (int32_t)merged.size();
+                merged.push_back(u);
+            } else {
+                uint32_t flags = merged[l].activate | u.activate;
+                merged[l] = u;
+                merged[l].activate = flags;
+            }
+        }
+        void* dp = nullptr;
+        npgpu_status st = stage_upload(w, merged.data(), merged.size() * sizeof(MassUpdate), &dp);
+        if (st != NPGPU_OK) return st;
+        CK(launch_mass_updates(w->dw, (const MassUpdate*)dp, (uint32_t)merged.size(), w->stream), "mass updates");
+        CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+        w->pending_mass.clear();
+    }
+    if (w->forget_pending) {
+        CK(cudaEventSynchronize(w->ev_stage), "staging wait");
+        CK(cudaMemcpyAsync(w->d_forget, w->forget.data(), w->cap_c, cudaMemcpyHostToDevice, w->stream), "forget copy");
+        CK(launch_forget_pairs(w->dw, w->d_forget, w->stream), "forget pairs");
+        CK(cudaStreamSynchronize(w->stream), "forget");
+        std::fill(w->forget.begin(), w->forget.end(), 0);
+        w->forget_pending = false;
+    }
+    return NPGPU_OK;
+}
+
+static npgpu_status run_cd(npgpu_world* w, const StepParams& sp) {
+    std::swap(w->dw.cur, w->dw.prev);
+    sync_world_view(w);
+    CK(launch_sync_aabb(w->dw, sp, w->stream), "sync aabb");
+    CK(launch_sort(w->dw, w->sort_temp, w->sort_bytes, w->stream), "radix sort");
+    CK(launch_lbvh(w->dw, w->stream), "lbvh");
+    CK(launch_pairs(w->dw, w->scan_temp, w->scan_bytes, w->stream), "pairs");
+    if (w->params.profile) CK(cudaEventRecord(w->ev[5], w->stream), "event");
+    CK(launch_narrow(w->dw, w->stream), "narrow phase");
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, uint32_t num_force_generators) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (num_joints) return fail(w, NPGPU_ERR_NONEMPTY_JOINTS, "joint constraints are not supported");
+    if (num_force_generators) return fail(w, NPGPU_ERR_NONEMPTY_FORCES, "force generators are not supported");
+    StepParams sp = step_params(w);
+    for (uint32_t s = 0; s < nsteps; ++s) {
+        npgpu_status st = maintain(w);
+        if (st != NPGPU_OK) return st;
+        sync_world_view(w);
+        bool prof = w->params.profile != 0;
+        if (prof) CK(cudaEventRecord(w->ev[0], w->stream), "event");
+        CK(launch_body_start(w->dw, sp, w->stream), "body start");
+        w->cd_start_ran = w->cd_dirty;
+        if (w->cd_dirty) {
+            st = run_cd(w, sp);
+            if (st != NPGPU_OK) return st;
+            w->cd_dirty = false;
+        }
+        if (prof) CK(cudaEventRecord(w->ev[1], w->stream), "event");
+        CK(launch_solve(w->dw, sp, w->solve_grid, w->stream), "solve");
+        if (prof) CK(cudaEventRecord(w->ev[2], w->stream), "event");
+        st = run_cd(w, sp);
+        if (st != NPGPU_OK) return st;
+        if (prof) {
+            CK(cudaEventRecord(w->ev[3], w->stream), "event");
+            w->ev_recorded = true;
+        }
+        w->counters.steps += 1;
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_synchronize(npgpu_world* w) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    uint32_t err = 0;
+    CK(cudaMemcpy(&err, &w->ctl->err, sizeof(err), cudaMemcpyDeviceToHost), "read error flag");
+    if (err) {
+        uint32_t zero = 0;
+        cudaMemcpy(&w->ctl->err, &zero, sizeof(zero), cudaMemcpyHostToDevice);
+        if (err & ERRF_TIMEOUT) return fail(w, NPGPU_ERR_TIMEOUT, "a bounded device wait gave up");
+        if (err & ERRF_UNION_FIND) return fail(w, NPGPU_ERR_TIMEOUT, "island union-find did not converge");
+        if (err & ERRF_NAN) return fail(w, NPGPU_ERR_NAN, "non-finite body state after the step");
+        if (err & ERRF_PAIR_CAPACITY) return fail(w, NPGPU_ERR_CAPACITY, "pair capacity exceeded");
+        if (err & ERRF_COLOURS) return fail(w, NPGPU_ERR_CAPACITY, "more than 64 solver colours needed");
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, float* position, float* velocity,
+                                   float* energy, uint8_t* active) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    if ((uint64_t)first + n > w->cap_b) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "range beyond capacity");
+    if (n == 0) return NPGPU_OK;
+    size_t bytes = (size_t)n * (7 + 6 + 1) * sizeof(float) + n;
+    CK(cudaEventSynchronize(w->ev_stage), "staging wait");
+    if (bytes > w->d_stage_bytes) {
+        if (w->d_stage) cudaFree(w->d_stage);
+        w->d_stage = nullptr;
+        CK(cudaMalloc(&w->d_stage, bytes), "device staging");
+        w->d_stage_bytes = bytes;
+    }
+    if (bytes > w->h_stage_bytes) {
+        if (w->h_stage) cudaFreeHost(w->h_stage);
+        w->h_stage = nullptr;
+        CK(cudaMallocHost(&w->h_stage, bytes), "pinned staging");
+        w->h_stage_bytes = bytes;
+    }
+    float* dpos = (float*)w->d_stage;
+    float* dvel = dpos + 7 * (size_t)n;
+    float* den = dvel + 6 * (size_t)n;
+    uint8_t* dact = (uint8_t*)(den + n);
+    CK(launch_pack_bodies(w->dw, first, n, position ? dpos : nullptr, velocity ? dvel : nullptr, energy ? den : nullptr,
+                          active ? dact : nullptr, w->stream),
+       "pack bodies");
+    char* h = (char*)w->h_stage;
+    if (position) CK(cudaMemcpyAsync(h, dpos, 7 * sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+    if (velocity)
+        CK(cudaMemcpyAsync(h + 7 * sizeof(float) * n, dvel, 6 * sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream),
+           "d2h");
+    if (energy) CK(cudaMemcpyAsync(h + 13 * sizeof(float) * n, den, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+    if (active) CK(cudaMemcpyAsync(h + 14 * sizeof(float) * n, dact, n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    CK(cudaStreamSynchronize(w->stream), "download");
+    if (position) std::memcpy(position, h, 7 * sizeof(float) * n);
+    if (velocity) std::memcpy(velocity, h + 7 * sizeof(float) * n, 6 * sizeof(float) * n);
+    if (energy) std::memcpy(energy, h + 13 * sizeof(float) * n, sizeof(float) * n);
+    if (active) std::memcpy(active, h + 14 * sizeof(float) * n, n);
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_download_mass_properties(npgpu_world* w, uint32_t first, uint32_t n, float* local_inertia,
+                                            float* local_com) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    if ((uint64_t)first + n > w->cap_b) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "range beyond capacity");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    std::vector<float> mass(n), I(9 * (size_t)n);
+    std::vector<float4> com(n);
+    if (n) {
+        CK(cudaMemcpy(mass.data(), w->dw.b.mass + first, sizeof(float) * n, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(I.data(), w->dw.b.local_I + 9 * (size_t)first, sizeof(float) * 9 * n, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(com.data(), w->dw.b.local_com + first, sizeof(float4) * n, cudaMemcpyDeviceToHost), "d2h");
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+        if (local_inertia) {
+            float* o = local_inertia + 7 * (size_t)k;
+            const float* a = I.data() + 9 * (size_t)k;
+            o[0] = mass[k]; o[1] = a[0]; o[2] = a[1]; o[3] = a[2]; o[4] = a[4]; o[5] = a[5]; o[6] = a[8];
+        }
+        if (local_com) {
+            local_com[3 * k] = com[k].x;
+            local_com[3 * k + 1] = com[k].y;
+            local_com[3 * k + 2] = com[k].z;
+        }
+    }
+    return NPGPU_OK;
+}
+
+static npgpu_status read_npairs(npgpu_world* w, uint32_t* np_) {
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    CK(cudaMemcpy(np_, &w->ctl->npairs, sizeof(uint32_t), cudaMemcpyDeviceToHost), "d2h");
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_get_pairs(npgpu_world* w, uint32_t* pairs2, uint32_t max, uint32_t* count) {
+    if (!w || !count) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    uint32_t np_ = 0;
+    npgpu_status st = read_npairs(w, &np_);
+    if (st != NPGPU_OK) return st;
+    std::vector<uint2> pr(np_);
+    if (np_) CK(cudaMemcpy(pr.data(), w->dw.cur.pair, sizeof(uint2) * np_, cudaMemcpyDeviceToHost), "d2h");
+    std::vector<uint64_t> keys;
+    keys.reserve(np_);
+    for (auto& p : pr)
+        if (p.x != 0xffffffffu) keys.push_back(((uint64_t)p.x << 32) | p.y);
+    std::sort(keys.begin(), keys.end());
+    *count = (uint32_t)keys.size();
+    for (uint32_t k = 0; k < keys.size() && k < max && pairs2; ++k) {
+        pairs2[2 * k] = (uint32_t)(keys[k] >> 32);
+        pairs2[2 * k + 1] = (uint32_t)keys[k];
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_get_aabbs(npgpu_world* w, uint32_t first, uint32_t n, float* aabb6) {
+    if (!w || (n && !aabb6)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if ((uint64_t)first + n > w->cap_c) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "range beyond capacity");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    std::vector<float4> mn(n), mx(n);
+    if (n) {
+        CK(cudaMemcpy(mn.data(), w->dw.c.aabb_min + first, sizeof(float4) * n, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(mx.data(), w->dw.c.aabb_max + first, sizeof(float4) * n, cudaMemcpyDeviceToHost), "d2h");
+    }
+    for (uint32_t k = 0; k < n; ++k) {
+        float* o = aabb6 + 6 * (size_t)k;
+        o[0] = mn[k].x; o[1] = mn[k].y; o[2] = mn[k].z; o[3] = mx[k].x; o[4] = mx[k].y; o[5] = mx[k].z;
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max, uint32_t* count) {
+    if (!w || !count) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    uint32_t np_ = 0;
+    npgpu_status st = read_npairs(w, &np_);
+    if (st != NPGPU_OK) return st;
+    const Pairs& P = w->dw.cur;
+    std::vector<uint2> pr(np_);
+    std::vector<uint8_t> nc(np_);
+    size_t ns = 4 * (size_t)np_;
+    std::vector<uint32_t> key(ns);
+    std::vector<float4> w1(ns), w2(ns), nn(ns), imp(ns);
+    if (np_) {
+        CK(cudaMemcpy(pr.data(), P.pair, sizeof(uint2) * np_, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(nc.data(), P.ncont, np_, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(key.data(), P.key, 4 * ns, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(w1.data(), P.w1, 16 * ns, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(w2.data(), P.w2, 16 * ns, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(nn.data(), P.n, 16 * ns, cudaMemcpyDeviceToHost), "d2h");
+        CK(cudaMemcpy(imp.data(), P.imp, 16 * ns, cudaMemcpyDeviceToHost), "d2h");
+    }
+    std::vector<npgpu_contact> all;
+    for (uint32_t p = 0; p < np_; ++p) {
+        if (pr[p].x == 0xffffffffu) continue;
+        for (uint32_t k = 0; k < nc[p]; ++k) {
+            size_t s = 4 * (size_t)p + k;
+            npgpu_contact c;
+            std::memset(&c, 0, sizeof(c));
+            c.collider1 = pr[p].x;
+            c.collider2 = pr[p].y;
+            c.feature_key = key[s];
+            uint32_t f1 = key[s] / 26u, f2 = key[s] % 26u;
+            auto kind = [](const HostCollider& hc, uint32_t f) -> uint32_t {
+                if (hc.desc.shape == NPGPU_SHAPE_BALL) return 1u;
+                return f < 8 ? 1u : (f < 20 ? 2u : 3u);
+            };
+            c.kinematic = kind(w->hc[c.collider1], f1) | (kind(w->hc[c.collider2], f2) << 8);
+            c.world1[0] = w1[s].x; c.world1[1] = w1[s].y; c.world1[2] = w1[s].z;
+            c.world2[0] = w2[s].x; c.world2[1] = w2[s].y; c.world2[2] = w2[s].z;
+            c.normal[0] = nn[s].x; c.normal[1] = nn[s].y; c.normal[2] = nn[s].z;
+            c.depth = w1[s].w;
+            c.impulse[0] = imp[s].x; c.impulse[1] = imp[s].y; c.impulse[2] = imp[s].z;
+            c.colour = 0xffffffffu;
+            all.push_back(c);
+        }
+    }
+    std::sort(all.begin(), all.end(), [](const npgpu_contact& a, const npgpu_contact& b) {
+        if (a.collider1 != b.collider1) return a.collider1 < b.collider1;
+        if (a.collider2 != b.collider2) return a.collider2 < b.collider2;
+        return a.feature_key < b.feature_key;
+    });
+    *count = (uint32_t)all.size();
+    if (out)
+        for (uint32_t k = 0; k < all.size() && k < max; ++k) out[k] = all[k];
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
+    if (!w || !out) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    Control c;
+    CK(cudaMemcpy(&c, w->ctl, sizeof(Control), cudaMemcpyDeviceToHost), "d2h");
+    npgpu_counters& k = w->counters;
+    k.num_pairs = c.npairs;
+    k.num_manifolds = c.nmanifolds;
+    k.num_contacts = c.ncontacts;
+    k.num_solver_contacts = c.nsolver_contacts;
+    k.num_constraints = 3 * c.nsolver_contacts;
+    k.num_colours = c.ncolours;
+    k.num_active_bodies = c.nactive;
+    k.velocity_iterations = c.iterations;
+    k.residual = c.residual;
+    k.residual_initial = c.residual_initial;
+    unsigned long long bits = c.max_pen_bits;
+    if (c.ncontacts == 0 || bits == 0) {
+        k.max_penetration = 0.0;
+    } else {
+        unsigned long long raw = (bits & 0x8000000000000000ull) ? (bits & ~0x8000000000000000ull) : ~bits;
+        double v;
+        std::memcpy(&v, &raw, sizeof(v));
+        k.max_penetration = v;
+    }
+    k.kinetic_energy = c.kinetic_energy;
+    if (w->params.profile && w->ev_recorded) {
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, w->ev[0], w->ev[3]);
+        k.step_time = ms;
+        cudaEventElapsedTime(&ms, w->ev[1], w->ev[2]);
+        k.solver_time = ms;
+        cudaEventElapsedTime(&ms, w->ev[2], w->ev[3]);
+        k.collision_detection_time = ms;
+        cudaEventElapsedTime(&ms, w->ev[2], w->ev[5]);
+        k.broad_phase_time = ms;
+        cudaEventElapsedTime(&ms, w->ev[5], w->ev[3]);
+        k.narrow_phase_time = ms;
+        auto d = [&](int a, int b) { return (double)(c.t_phase[b] - c.t_phase[a]) * 1e-6; };
+        k.island_construction_time = d(0, 1);
+        k.colouring_time = d(1, 2);
+        k.assembly_time = d(2, 3);
+        k.velocity_resolution_time = d(3, 4);
+        k.velocity_update_time = d(4, 5);
+        k.position_resolution_time = d(5, 6);
+    }
+    *out = k;
+    return NPGPU_OK;
+}
+
+const char* npgpu_last_error(const npgpu_world* w) {
+    if (!w) return g_create_error.c_str();
+    return w->last_error.c_str();
+}
+
+}  // extern "C"

@@ -1,0 +1,199 @@
+// world_dev.cuh -- device-resident state of one GPU mechanical world and the
+// kernel entry points of each phase of the step.
+//
+// Layout in HBM (all arrays sized by capacity at npgpu_create):
+//  bodies     SoA by body slot (= generational-arena index of the host set)
+//  colliders  SoA by collider slot
+//  pairs      broad-phase pairs, double-buffered (current / previous step),
+//             4 contact slots per pair; the previous buffer feeds the impulse
+//             cache of the next narrow phase
+//  solver     one record per solver manifold, sorted by colour; 3 rows per
+//             contact (normal, tangent 1, tangent 2), 28 floats per row
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "np_math.cuh"
+
+namespace npgpu_dev {
+
+// Body info word.
+enum : uint32_t {
+    BI_STATUS_MASK = 0x3u,           // NPGPU_BODY_*
+    BI_KIND_SHIFT = 2,               // 3 bits
+    BI_FLAGS_SHIFT = 8,              // NPGPU_BODY_* flag bits, 9 bits
+    BI_ALIVE = 1u << 20,
+    BI_CHANGED = 1u << 21,           // BodyUpdateStatus: inertia / colliders need update
+    BI_ISLAND = 1u << 22,            // in an awake island this step
+};
+inline __host__ __device__ uint32_t bi_status(uint32_t i) { return i & BI_STATUS_MASK; }
+inline __host__ __device__ uint32_t bi_flags(uint32_t i) { return (i >> BI_FLAGS_SHIFT) & 0x1ffu; }
+
+// Error flag bits (device word, read by npgpu_synchronize).
+enum : uint32_t {
+    ERRF_PAIR_CAPACITY = 1u << 0,
+    ERRF_TIMEOUT = 1u << 1,
+    ERRF_NAN = 1u << 2,
+    ERRF_COLOURS = 1u << 3,
+    ERRF_UNION_FIND = 1u << 4,
+};
+
+constexpr int kMaxContacts = 4;      // contacts per manifold
+constexpr int kRowFloats = 28;       // J1[6] J2[6] WJ1[6] WJ2[6] r rhs impulse mu
+constexpr int kMaxColours = 64;
+
+// Row field offsets.
+enum { RF_J1 = 0, RF_J2 = 6, RF_WJ1 = 12, RF_WJ2 = 18, RF_R = 24, RF_RHS = 25, RF_IMP = 26, RF_MU = 27 };
+
+struct Bodies {
+    float4 *pos_t, *pos_q;           // Isometry3 (translation, quaternion i j k w)
+    float4 *lin, *ang;               // velocity
+    float4 *com, *local_com;
+    float *mass;                     // inertia.linear
+    float *local_I;                  // 9 per body, local angular inertia
+    float *I;                        // 9 per body, world angular inertia
+    float *inv_mass;                 // inv_augmented_mass.linear
+    float *inv_I;                    // 9 per body, inv_augmented_mass.angular
+    float4 *acc_lin, *acc_ang;       // generalized acceleration
+    float4 *f_lin, *f_ang;           // external forces
+    float *lin_damp, *ang_damp, *max_lin, *max_ang, *sleep_thr, *energy;
+    uint32_t *info;
+    uint32_t *world;
+    float *dv;                       // mj_lambda, 6 per body
+    uint32_t *uf_parent;
+    int *can_deact;
+    unsigned long long *jp_best, *jp_used;
+};
+
+struct Colliders {
+    uint32_t *body;
+    uint32_t *info;                  // shape | friction_combine << 4 | restitution_combine << 8 | alive << 16
+    float4 *params;                  // ball: radius in x; cuboid: half extents
+    float4 *wrt_t, *wrt_q;           // position_wrt_body
+    float *margin, *lin_pred, *friction, *restitution, *rank;
+    float4 *pose_t, *pose_q;
+    float4 *aabb_min, *aabb_max;     // fat AABB; aabb_min.w = 1 when set
+    unsigned long long *keys, *keys_sorted;
+    uint32_t *vals, *vals_sorted;
+    // LBVH over the alive colliders (n - 1 internal nodes, n leaves).
+    int *left, *right, *parent;
+    float4 *node_min, *node_max;
+    int *node_flag;
+    uint32_t *leaf_count, *leaf_offset;
+};
+enum : uint32_t { CI_ALIVE = 1u << 16 };
+
+struct Pairs {
+    uint2 *pair;                     // (collider1, collider2), collider1 < collider2
+    uint32_t *owner_start, *owner_count;   // by collider slot: the pairs it owns
+    uint8_t *ncont;                  // contacts in the manifold
+    uint32_t *key;                   // 4 per pair: feature key (fid1 * 26 + fid2)
+    float4 *w1;                      // world1 xyz, depth
+    float4 *w2;                      // world2 xyz
+    float4 *n;                       // normal xyz
+    float4 *imp;                     // cached impulses (normal, tangent 1, tangent 2)
+    float4 *nl;                      // normal in body 1's frame
+};
+
+struct Solver {
+    uint32_t *sm_list;               // solver manifolds (pair indices), unordered
+    uint32_t *sm_colour;             // colour per sm_list entry
+    uint8_t *sm_state;
+    uint32_t *sm_sorted;             // pair indices sorted by colour
+    int *sm_b1, *sm_b2;              // dynamic body slots (-1 when the side has no dofs)
+    uint32_t *sm_nc;
+    float *rows;                     // 12 rows per sorted manifold
+    uint32_t *colour_count, *colour_start, *colour_cursor;
+};
+
+// Device counters and control words (one struct in device memory).
+struct Control {
+    uint32_t npairs;
+    uint32_t nsolver;                // solver manifolds
+    uint32_t ncolours;
+    uint32_t err;
+    uint32_t barrier_count;
+    uint32_t barrier_gen;
+    uint32_t jp_remaining[2];
+    uint32_t ncontacts;
+    uint32_t nmanifolds;
+    uint32_t nsolver_contacts;
+    uint32_t nactive;
+    uint32_t iterations;
+    uint32_t pad0;
+    double res_acc[2];               // FP64 residual accumulators (phi^2, lambda^2)
+    double residual, residual_initial;
+    double kinetic_energy;
+    unsigned long long max_pen_bits; // order-preserving bits of the max penetration
+    unsigned long long t_phase[16];  // %globaltimer stamps
+};
+
+struct StepParams {
+    float dt, inv_dt;
+    float erp, warmstart_coeff, restitution_threshold;
+    float allowed_linear_error, max_linear_correction;
+    float activation_mix, broad_phase_margin;
+    float gx, gy, gz;
+    float residual_tolerance;
+    uint32_t max_velocity_iterations, max_position_iterations;
+    uint32_t solve_to_tolerance, max_iterations_to_tolerance;
+    uint32_t warmstart_mode;
+    uint32_t profile;
+};
+
+struct World {
+    Bodies b;
+    Colliders c;
+    Pairs cur, prev;
+    Solver s;
+    Control* ctl;
+    uint32_t nb_slots, nc_slots, cap_pairs, nc_alive;
+};
+
+// ---- launchers (defined in the kernel translation units) ----
+cudaError_t launch_body_start(const World& w, const StepParams& p, cudaStream_t st);
+cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t st);
+cudaError_t launch_lbvh(const World& w, cudaStream_t st);
+cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);
+cudaError_t launch_narrow(const World& w, cudaStream_t st);
+cudaError_t launch_solve(const World& w, const StepParams& p, int grid, cudaStream_t st);
+int solve_grid_size(int device);
+size_t sort_temp_bytes(uint32_t n_items);
+size_t scan_temp_bytes(uint32_t n_items);
+cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);
+
+// Uploads / maintenance kernels.
+struct BodyUpload {
+    uint32_t slot;
+    uint32_t info;
+    uint32_t world;
+    uint32_t reset_energy;           // 1 for a new body: energy = 0.04 (or 0 for a ground)
+    float pos[7], vel[6];
+    float mass, local_I[9], local_com[3];
+    float lin_damp, ang_damp, max_lin, max_ang, sleep_thr;
+};
+struct ColliderUpload {
+    uint32_t slot, body, info;
+    float params[4], wrt[7];
+    float margin, lin_pred, friction, restitution, rank;
+};
+struct MassUpdate {                  // new local inertia / com of a body
+    uint32_t slot;
+    uint32_t activate;               // bit 0: inertia changed; bit 1: Body::activate (collider removal)
+    float mass, local_I[9], local_com[3];
+};
+struct ForceUpload {
+    uint32_t slot;
+    uint32_t wake;
+    float f[6];
+};
+cudaError_t launch_upload_bodies(const World& w, const BodyUpload* d, uint32_t n, cudaStream_t st);
+cudaError_t launch_upload_colliders(const World& w, const ColliderUpload* d, uint32_t n, cudaStream_t st);
+cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n, cudaStream_t st);
+cudaError_t launch_forces(const World& w, const ForceUpload* d, uint32_t n, cudaStream_t st);
+cudaError_t launch_kill(const World& w, const uint32_t* slots, uint32_t n, int colliders, cudaStream_t st);
+cudaError_t launch_forget_pairs(const World& w, const uint8_t* flags, cudaStream_t st);
+cudaError_t launch_pack_bodies(const World& w, uint32_t first, uint32_t n, float* pos7, float* vel6, float* energy,
+                               uint8_t* active, cudaStream_t st);
+
+}  // namespace npgpu_dev

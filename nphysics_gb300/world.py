@@ -1,0 +1,173 @@
+"""ctypes binding of libnpgpu.so: the GPU mechanical world as seen from Python.
+
+`GpuWorld` exposes the C ABI of include/npgpu.h one call per entry point. It
+is what the tests, the smoke check and the benchmark drive. There is no CPU
+fallback: constructing a world without the built library or without a CUDA
+device raises.
+"""
+import ctypes as C
+
+import numpy as np
+
+from . import abi
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        _lib = abi.load_library()
+    return _lib
+
+
+def _ptr(a, ctype):
+    return a.ctypes.data_as(C.POINTER(ctype)) if a is not None else None
+
+
+class NpgpuError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+class GpuWorld:
+    def __init__(self, params=None, gravity=(0.0, -9.81, 0.0), capacity_bodies=1024, capacity_colliders=1024,
+                 capacity_pairs=None):
+        self.L = lib()
+        self.params = params if params is not None else abi.default_params()
+        g = (C.c_float * 3)(*gravity)
+        st = C.c_int(0)
+        cap_p = capacity_pairs if capacity_pairs is not None else max(1024, 16 * capacity_colliders)
+        self.w = self.L.npgpu_create(C.byref(self.params), g, capacity_bodies, capacity_colliders, cap_p,
+                                     C.byref(st))
+        if not self.w:
+            raise NpgpuError(st.value, self.L.npgpu_last_error(None).decode())
+        self.num_bodies = 0
+        self.num_colliders = 0
+
+    @classmethod
+    def for_scene(cls, scene, params=None, pairs_per_collider=16):
+        p = params if params is not None else scene.params()
+        w = cls(p, scene.gravity, capacity_bodies=len(scene.bodies), capacity_colliders=len(scene.colliders),
+                capacity_pairs=max(1024, pairs_per_collider * len(scene.colliders)))
+        w.load_scene(scene)
+        return w
+
+    def close(self):
+        if getattr(self, "w", None):
+            self.L.npgpu_destroy(self.w)
+            self.w = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, s, what=""):
+        if s != abi.OK:
+            raise NpgpuError(s, f"{what}: {self.L.npgpu_last_error(self.w).decode()}")
+
+    @property
+    def stream(self):
+        return self.L.npgpu_stream(self.w)
+
+    def set_params(self, params):
+        self.params = params
+        self._check(self.L.npgpu_set_params(self.w, C.byref(params)), "set_params")
+
+    def set_gravity(self, g):
+        self._check(self.L.npgpu_set_gravity(self.w, (C.c_float * 3)(*g)), "set_gravity")
+
+    def upsert_bodies(self, handles, descs):
+        descs = np.ascontiguousarray(descs)
+        handles = np.ascontiguousarray(handles)
+        self._check(self.L.npgpu_upsert_bodies(self.w, len(descs), _ptr(handles, abi.Handle), _ptr(descs, abi.BodyDesc)),
+                    "upsert_bodies")
+        if len(handles):
+            self.num_bodies = max(self.num_bodies, int(handles["index"].max()) + 1)
+
+    def upsert_colliders(self, handles, descs):
+        descs = np.ascontiguousarray(descs)
+        handles = np.ascontiguousarray(handles)
+        self._check(self.L.npgpu_upsert_colliders(self.w, len(descs), _ptr(handles, abi.Handle),
+                                                  _ptr(descs, abi.ColliderDesc)), "upsert_colliders")
+        if len(handles):
+            self.num_colliders = max(self.num_colliders, int(handles["index"].max()) + 1)
+
+    def load_scene(self, scene):
+        self.upsert_bodies(scene.body_handles, scene.bodies)
+        self.upsert_colliders(scene.collider_handles, scene.colliders)
+
+    def remove_bodies(self, handles):
+        handles = np.ascontiguousarray(handles)
+        self._check(self.L.npgpu_remove_bodies(self.w, len(handles), _ptr(handles, abi.Handle)), "remove_bodies")
+
+    def remove_colliders(self, handles):
+        handles = np.ascontiguousarray(handles)
+        self._check(self.L.npgpu_remove_colliders(self.w, len(handles), _ptr(handles, abi.Handle)), "remove_colliders")
+
+    def apply_forces(self, handles, forces, wake=True):
+        handles = np.ascontiguousarray(handles)
+        f = np.ascontiguousarray(forces, np.float32)
+        self._check(self.L.npgpu_apply_forces(self.w, len(handles), _ptr(handles, abi.Handle), _ptr(f, C.c_float),
+                                              int(wake)), "apply_forces")
+
+    def step(self, n=1, joints=0, force_generators=0, sync=True):
+        self._check(self.L.npgpu_step(self.w, n, joints, force_generators), "step")
+        if sync:
+            self.synchronize()
+
+    def synchronize(self):
+        self._check(self.L.npgpu_synchronize(self.w), "synchronize")
+
+    def bodies(self, first=0, n=None):
+        n = self.num_bodies - first if n is None else n
+        pos = np.zeros((n, 7), np.float32)
+        vel = np.zeros((n, 6), np.float32)
+        energy = np.zeros(n, np.float32)
+        active = np.zeros(n, np.uint8)
+        self._check(self.L.npgpu_download_bodies(self.w, first, n, _ptr(pos, C.c_float), _ptr(vel, C.c_float),
+                                                 _ptr(energy, C.c_float), _ptr(active, C.c_uint8)), "download_bodies")
+        return {"position": pos, "velocity": vel, "energy": energy, "active": active}
+
+    def download_into(self, pos, vel, first=0):
+        """Copies positions and velocities into caller-owned host arrays."""
+        n = pos.shape[0]
+        self._check(self.L.npgpu_download_bodies(self.w, first, n, _ptr(pos, C.c_float), _ptr(vel, C.c_float),
+                                                 None, None), "download_bodies")
+
+    def mass_properties(self, first=0, n=None):
+        n = self.num_bodies - first if n is None else n
+        inertia = np.zeros((n, 7), np.float32)
+        com = np.zeros((n, 3), np.float32)
+        self._check(self.L.npgpu_download_mass_properties(self.w, first, n, _ptr(inertia, C.c_float),
+                                                          _ptr(com, C.c_float)), "mass_properties")
+        return inertia, com
+
+    def pairs(self):
+        cnt = C.c_uint32(0)
+        self._check(self.L.npgpu_get_pairs(self.w, None, 0, C.byref(cnt)), "get_pairs")
+        out = np.zeros((max(cnt.value, 1), 2), np.uint32)
+        self._check(self.L.npgpu_get_pairs(self.w, _ptr(out, C.c_uint32), cnt.value, C.byref(cnt)), "get_pairs")
+        return out[:cnt.value]
+
+    def aabbs(self, first=0, n=None):
+        n = self.num_colliders - first if n is None else n
+        out = np.zeros((n, 6), np.float32)
+        self._check(self.L.npgpu_get_aabbs(self.w, first, n, _ptr(out, C.c_float)), "get_aabbs")
+        return out
+
+    def contacts(self):
+        cnt = C.c_uint32(0)
+        self._check(self.L.npgpu_get_contacts(self.w, None, 0, C.byref(cnt)), "get_contacts")
+        n = cnt.value
+        arr = (abi.Contact * max(n, 1))()
+        self._check(self.L.npgpu_get_contacts(self.w, arr, n, C.byref(cnt)), "get_contacts")
+        return abi.contacts_to_numpy(arr, n)
+
+    def counters(self):
+        c = abi.Counters()
+        self._check(self.L.npgpu_get_counters(self.w, C.byref(c)), "get_counters")
+        return c.as_dict()

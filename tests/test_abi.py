@@ -1,0 +1,82 @@
+"""The C ABI library loads and exports every entry point include/npgpu.h
+declares, and the ctypes mirror has the header's struct layouts (no GPU)."""
+import ctypes as C
+import os
+import re
+import subprocess
+import tempfile
+
+import pytest
+
+from nphysics_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "npgpu.h")
+
+
+def declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(npgpu_[a-z_0-9]+)\s*\(", src)))
+
+
+@pytest.fixture(scope="module")
+def built():
+    from nphysics_gb300 import build
+    return build.build()
+
+
+def test_library_exports_every_declared_entry_point(built):
+    names = declared_functions()
+    assert set(names) == set(abi.EXPORTED)
+    lib = C.CDLL(built)
+    for n in names:
+        assert hasattr(lib, n), n
+    out = subprocess.run(["nm", "-D", "--defined-only", built], capture_output=True, text=True, check=True).stdout
+    for n in names:
+        assert re.search(rf"\bT {n}\b", out), n
+
+
+def test_version_and_default_params_without_gpu(built):
+    lib = abi.load_library(built)
+    assert lib.npgpu_abi_version() == abi.NPGPU_ABI_VERSION
+    p = abi.Params()
+    lib.npgpu_default_params(C.byref(p))
+    ref = abi.default_params()
+    for name, _ in abi.Params._fields_:
+        assert getattr(p, name) == pytest.approx(getattr(ref, name)), name
+
+
+def test_create_without_a_device_reports_an_error(built):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = abi.load_library(built)
+    st = C.c_int(-1)
+    w = lib.npgpu_create(C.byref(abi.default_params()), (C.c_float * 3)(0, -9.81, 0), 8, 8, 64, C.byref(st))
+    assert not w
+    assert st.value == abi.ERR_CUDA
+    assert b"device" in lib.npgpu_last_error(None)
+
+
+def test_struct_layouts_match_the_header():
+    prog = r"""
+#include <stdio.h>
+#include <stddef.h>
+#include "npgpu.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu\n", sizeof(npgpu_handle), sizeof(npgpu_body_desc),
+         sizeof(npgpu_collider_desc), sizeof(npgpu_params), sizeof(npgpu_counters), sizeof(npgpu_contact),
+         offsetof(npgpu_counters, residual));
+  return 0;
+}
+"""
+    with tempfile.TemporaryDirectory() as d:
+        src = os.path.join(d, "sz.c")
+        exe = os.path.join(d, "sz")
+        open(src, "w").write(prog)
+        subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), src, "-o", exe], check=True)
+        got = [int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split()]
+    want = [C.sizeof(abi.Handle), C.sizeof(abi.BodyDesc), C.sizeof(abi.ColliderDesc), C.sizeof(abi.Params),
+            C.sizeof(abi.Counters), C.sizeof(abi.Contact), abi.Counters.residual.offset]
+    assert got == want

@@ -1,0 +1,81 @@
+"""Error behaviour of the C ABI on a GPU: statuses instead of aborts."""
+import numpy as np
+import pytest
+
+from nphysics_gb300 import abi, scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def world(**kw):
+    from nphysics_gb300.world import GpuWorld
+    return GpuWorld(**kw)
+
+
+def test_rejects_unsupported_bodies_and_shapes(gpu_lib):
+    from nphysics_gb300.world import NpgpuError
+    w = world()
+    b = scenes.body_descs(1)
+    b["kind"] = abi.KIND_MULTIBODY
+    with pytest.raises(NpgpuError) as e:
+        w.upsert_bodies(scenes.make_handles(1), b)
+    assert e.value.status == abi.ERR_UNSUPPORTED_BODY
+    b["kind"] = abi.KIND_RIGID_BODY
+    w.upsert_bodies(scenes.make_handles(1), b)
+    c = scenes.collider_descs(1, 0, abi.SHAPE_OTHER, (1, 1, 1), density=1.0)
+    with pytest.raises(NpgpuError) as e:
+        w.upsert_colliders(scenes.make_handles(1), c)
+    assert e.value.status == abi.ERR_UNSUPPORTED_SHAPE
+
+
+def test_rejects_joints_and_force_generators(gpu_lib):
+    from nphysics_gb300.world import NpgpuError
+    w = world()
+    with pytest.raises(NpgpuError) as e:
+        w.step(1, joints=1)
+    assert e.value.status == abi.ERR_NONEMPTY_JOINTS
+    with pytest.raises(NpgpuError) as e:
+        w.step(1, force_generators=2)
+    assert e.value.status == abi.ERR_NONEMPTY_FORCES
+
+
+def test_invalid_handles_and_nan(gpu_lib):
+    from nphysics_gb300.world import NpgpuError
+    w = world()
+    b = scenes.body_descs(2)
+    w.upsert_bodies(scenes.make_handles(2), b)
+    stale = scenes.make_handles(1, generation=7)
+    with pytest.raises(NpgpuError) as e:
+        w.remove_bodies(stale)
+    assert e.value.status == abi.ERR_INVALID_HANDLE
+    c = scenes.collider_descs(1, 0, abi.SHAPE_BALL, (0.5, 0, 0), density=1.0)
+    c["body"]["generation"] = 3
+    with pytest.raises(NpgpuError) as e:
+        w.upsert_colliders(scenes.make_handles(1), c)
+    assert e.value.status == abi.ERR_INVALID_HANDLE
+    b["position"][0, 0] = np.nan
+    with pytest.raises(NpgpuError) as e:
+        w.upsert_bodies(scenes.make_handles(2), b)
+    assert e.value.status == abi.ERR_NAN
+
+
+def test_pair_capacity_overflow_is_reported(gpu_lib):
+    from nphysics_gb300.world import GpuWorld, NpgpuError
+    sc = scenes.ball_pile(side=4, spacing=1.0)
+    w = GpuWorld(sc.params(), sc.gravity, capacity_bodies=len(sc.bodies), capacity_colliders=len(sc.colliders),
+                 capacity_pairs=8)
+    w.load_scene(sc)
+    with pytest.raises(NpgpuError) as e:
+        w.step(1)
+    assert e.value.status == abi.ERR_CAPACITY
+    # The world stays usable: the error is cleared after it was reported.
+    w.synchronize()
+
+
+def test_capacity_of_slots(gpu_lib):
+    from nphysics_gb300.world import NpgpuError
+    w = world(capacity_bodies=4, capacity_colliders=4)
+    h = scenes.make_handles(5)
+    with pytest.raises(NpgpuError) as e:
+        w.upsert_bodies(h, scenes.body_descs(5))
+    assert e.value.status == abi.ERR_CAPACITY

@@ -1,0 +1,207 @@
+"""Parity of the GPU step (through the C ABI) with the CPU oracle.
+
+The GPU solver visits manifolds colour by colour; the oracle's colour order
+(ORDER_COLOUR) is the same Gauss-Seidel sequence written sequentially, and
+both evaluate every expression in the same order without fused multiply-add.
+Tolerances: 1e-5 relative on contact geometry, 1e-4 relative on impulses,
+1e-3 on 1000-step resting poses (the bars the path is specified to).
+"""
+import numpy as np
+import pytest
+
+from nphysics_gb300 import abi, scenes
+from oracle.oracle_py import ORDER_COLOUR, ORDER_REFERENCE, OracleWorld
+
+pytestmark = pytest.mark.gpu
+
+
+def make_pair(scene, params=None, precision=32, order=ORDER_COLOUR, pairs_per_collider=16):
+    from nphysics_gb300.world import GpuWorld
+    p = params if params is not None else scene.params()
+    g = GpuWorld.for_scene(scene, p, pairs_per_collider=pairs_per_collider)
+    o = OracleWorld(p, scene.gravity, precision=precision, order=order)
+    o.load_scene(scene)
+    return g, o
+
+
+def contact_table(c):
+    key = (c["collider1"].astype(np.uint64) << np.uint64(40)) | (c["collider2"].astype(np.uint64) << np.uint64(10)) | \
+        c["feature_key"].astype(np.uint64)
+    order = np.argsort(key, kind="stable")
+    return key[order], {k: v[order] for k, v in c.items()}
+
+
+def assert_close_rel(a, b, rtol, atol, what):
+    a = np.asarray(a, np.float64)
+    b = np.asarray(b, np.float64)
+    err = np.abs(a - b)
+    bound = atol + rtol * np.abs(b)
+    bad = err > bound
+    assert not bad.any(), f"{what}: {bad.sum()} of {bad.size} beyond tolerance; max err {err.max():.3e}"
+
+
+def test_mass_properties_match(gpu_lib):
+    sc = scenes.random_cluster(n=40, seed=11)
+    g, o = make_pair(sc)
+    g.step(1)
+    o.step(1)
+    gi, gc = g.mass_properties()
+    oi, oc = o.mass_properties()
+    assert_close_rel(gi, oi, 1e-6, 1e-7, "local inertia")
+    assert_close_rel(gc, oc, 1e-6, 1e-7, "local com")
+
+
+def test_free_motion_no_contacts(gpu_lib):
+    # Spinning, falling bodies far apart: update_dynamics (gyroscopic augmented
+    # mass), update_acceleration and integrate only.
+    sc = scenes.random_cluster(n=32, seed=5, extent=400.0, ground=False)
+    sc.bodies["velocity"][:, 3:] *= 5.0
+    g, o = make_pair(sc)
+    for _ in range(3):
+        g.step(10)
+        o.step(10)
+        gb, ob = g.bodies(), o.bodies()
+        assert_close_rel(gb["position"], ob["position"], 1e-6, 1e-6, "positions")
+        assert_close_rel(gb["velocity"], ob["velocity"], 1e-6, 1e-6, "velocities")
+    assert g.counters()["num_contacts"] == 0
+
+
+def test_broad_phase_is_the_brute_force_set(gpu_lib):
+    sc = scenes.random_cluster(n=400, seed=9, extent=5.0)
+    g, o = make_pair(sc)
+    g.step(2)
+    pairs = g.pairs()
+    aabb = g.aabbs()
+    body = sc.colliders["body"]["index"].astype(np.int64)
+    status = sc.bodies["status"]
+    n = len(aabb)
+    mn, mx = aabb[:, :3], aabb[:, 3:]
+    ov = np.all((mn[:, None, :] <= mx[None, :, :]) & (mn[None, :, :] <= mx[:, None, :]), axis=2)
+    iu = np.triu_indices(n, 1)
+    ok = ov[iu] & (body[iu[0]] != body[iu[1]]) & ((status[body[iu[0]]] == abi.BODY_DYNAMIC) |
+                                                  (status[body[iu[1]]] == abi.BODY_DYNAMIC))
+    brute = np.stack([iu[0][ok], iu[1][ok]], axis=1).astype(np.uint32)
+    assert len(pairs) > 200
+    np.testing.assert_array_equal(pairs, brute)
+
+
+def test_broad_phase_and_aabbs_match_oracle(gpu_lib):
+    sc = scenes.random_cluster(n=200, seed=2, extent=4.0)
+    g, o = make_pair(sc)
+    g.step(1)
+    o.step(1)
+    np.testing.assert_array_equal(g.pairs(), o.pairs())
+    assert_close_rel(g.aabbs(), o.aabbs(), 1e-6, 1e-6, "fat AABBs")
+
+
+@pytest.mark.parametrize("boxes,balls", [(True, False), (False, True), (True, True)])
+def test_contacts_match_oracle(gpu_lib, boxes, balls):
+    sc = scenes.random_cluster(n=120, seed=17, extent=2.5, boxes=boxes, balls=balls)
+    g, o = make_pair(sc)
+    g.step(1)
+    o.step(1)
+    kg, cg = contact_table(g.contacts())
+    ko, co = contact_table(o.contacts())
+    assert len(kg) > 50
+    np.testing.assert_array_equal(kg, ko)
+    for f in ("world1", "world2", "normal"):
+        assert_close_rel(cg[f], co[f], 1e-5, 1e-5, f)
+    assert_close_rel(cg["depth"], co["depth"], 1e-5, 1e-5, "depth")
+    assert_close_rel(cg["impulse"], co["impulse"], 1e-4, 1e-6, "impulses")
+
+
+def test_single_step_impulses_pyramid(gpu_lib):
+    sc = scenes.pyramid(base=20)
+    g, o = make_pair(sc)
+    g.step(1)
+    o.step(1)
+    kg, cg = contact_table(g.contacts())
+    ko, co = contact_table(o.contacts())
+    np.testing.assert_array_equal(kg, ko)
+    assert_close_rel(cg["impulse"], co["impulse"], 1e-4, 1e-6, "impulses")
+    cgc, coc = g.counters(), o.counters()
+    assert cgc["num_colours"] == coc["num_colours"]
+    assert cgc["num_solver_contacts"] == coc["num_solver_contacts"]
+    assert abs(cgc["residual"] - coc["residual"]) <= 1e-6 * max(1.0, coc["residual"])
+
+
+def test_converged_velocities_match_reference_order(gpu_lib):
+    # Run to a tight residual: the colour order and the reference's order reach
+    # the same velocities.
+    sc = scenes.pyramid(base=8)
+    p = sc.params()
+    p.solve_to_tolerance = 1
+    p.residual_tolerance = 1e-7
+    p.max_iterations_to_tolerance = 4000
+    p.max_position_iterations = 0
+    g, o = make_pair(sc, params=p, precision=64, order=ORDER_REFERENCE)
+    g.step(1)
+    o.step(1)
+    assert g.counters()["residual"] <= 1e-7
+    assert_close_rel(g.bodies()["velocity"], o.bodies()["velocity"], 1e-4, 1e-5, "converged velocities")
+
+
+def test_pyramid_1000_steps_resting_poses(gpu_lib):
+    sc = scenes.pyramid(base=20)
+    g, o = make_pair(sc)
+    g.step(1000)
+    o.step(1000)
+    gp, op = g.bodies()["position"], o.bodies()["position"]
+    assert np.abs(gp[:, :3] - op[:, :3]).max() < 1e-3
+    assert np.abs(np.abs(gp[:, 3:]) - np.abs(op[:, 3:])).max() < 1e-3
+    # Against the f64 oracle in the reference's own order.
+    o64 = OracleWorld(sc.params(), sc.gravity, precision=64, order=ORDER_REFERENCE)
+    o64.load_scene(sc)
+    o64.step(1000)
+    ref = o64.bodies()["position"]
+    drift = np.abs(gp[:, :3] - ref[:, :3]).max()
+    assert drift < 0.1, drift
+    assert g.counters()["max_penetration"] < 0.05
+
+
+def test_ball_pile_statistics(gpu_lib):
+    sc = scenes.ball_pile(side=8)
+    g, o = make_pair(sc)
+    g.step(120)
+    o.step(120)
+    cg, co = g.counters(), o.counters()
+    assert abs(cg["kinetic_energy"] - co["kinetic_energy"]) <= 0.05 * max(co["kinetic_energy"], 1.0)
+    assert cg["max_penetration"] < 0.05 and co["max_penetration"] < 0.05
+    assert abs(cg["num_contacts"] - co["num_contacts"]) <= 0.05 * max(co["num_contacts"], 10)
+
+
+def test_batched_worlds_do_not_interact(gpu_lib):
+    from nphysics_gb300.world import GpuWorld
+    one = scenes.random_cluster(n=30, seed=4, world=0)
+    two_b = np.concatenate([one.bodies, one.bodies.copy()])
+    two_b["world"][len(one.bodies):] = 1
+    two_c = np.concatenate([one.colliders, one.colliders.copy()])
+    two_c["body"]["index"][len(one.colliders):] += len(one.bodies)
+    two = scenes.Scene("two worlds", two_b, two_c)
+    g1 = GpuWorld.for_scene(one)
+    g2 = GpuWorld.for_scene(two)
+    g1.step(20)
+    g2.step(20)
+    p1 = g1.bodies()["position"]
+    p2 = g2.bodies()["position"]
+    np.testing.assert_array_equal(p2[:len(p1)], p1)
+    np.testing.assert_array_equal(p2[len(p1):], p1)
+    pr = g2.pairs()
+    nb1 = len(one.colliders)
+    assert not np.any((pr[:, 0] < nb1) & (pr[:, 1] >= nb1))
+
+
+def test_removal_wakes_the_stack(gpu_lib):
+    sc = scenes.pyramid(base=3)
+    g, o = make_pair(sc)
+    g.step(300)
+    o.step(300)
+    assert g.bodies()["active"][1:].sum() == 0
+    # Remove the ground collider: the bodies touching it wake up and fall.
+    h = sc.collider_handles[:1]
+    g.remove_colliders(h)
+    o.remove_colliders(h)
+    g.step(30)
+    o.step(30)
+    assert g.bodies()["active"][1:].sum() == len(sc.bodies) - 1
+    assert_close_rel(g.bodies()["position"], o.bodies()["position"], 1e-5, 1e-5, "positions after removal")

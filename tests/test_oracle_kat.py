@@ -1,0 +1,192 @@
+"""Known-answer tests of the CPU oracle (no GPU).
+
+The reference's own test of this path is the cuboid mass-properties check of
+src/volumetric/volumetric_convex3.rs:285-346 (a 0.96 half-extent cube, density
+2.37689, epsilon 1e-8). The rest are analytic checks of the restated step:
+free fall under the semi-implicit Euler step, friction deceleration, resting
+contact impulses and sleeping.
+"""
+import math
+
+import numpy as np
+import pytest
+
+from nphysics_gb300 import abi, scenes
+from oracle.oracle_py import ORDER_COLOUR, ORDER_REFERENCE, OracleWorld
+
+
+def _convex_box_mass_properties(half, shift, density):
+    """Mass, COM and inertia of a triangulated box by signed tetrahedra (the
+    method a convex-hull volumetric uses), independent of the cuboid formula."""
+    hx, hy, hz = half
+    v = np.array([[sx * hx, sy * hy, sz * hz] for sx in (-1, 1) for sy in (-1, 1) for sz in (-1, 1)]) + shift
+    # 12 outward-facing triangles of the box (vertex index = 4 sx + 2 sy + sz).
+    faces = [(0, 1, 3), (0, 3, 2), (4, 6, 7), (4, 7, 5), (0, 4, 5), (0, 5, 1), (2, 3, 7), (2, 7, 6),
+             (0, 2, 6), (0, 6, 4), (1, 5, 7), (1, 7, 3)]
+    vol = 0.0
+    com = np.zeros(3)
+    cov = np.zeros((3, 3))
+    canon = np.array([[2, 1, 1], [1, 2, 1], [1, 1, 2]]) / 120.0
+    for a, b, c in faces:
+        A = np.stack([v[a], v[b], v[c]], axis=1)
+        d = np.linalg.det(A)
+        vol += d / 6.0
+        com += d / 6.0 * (v[a] + v[b] + v[c]) / 4.0
+        cov += d * A @ canon @ A.T
+    com /= vol
+    cov = density * cov
+    mass = density * vol
+    cov -= mass * np.outer(com, com)
+    inertia = np.trace(cov) * np.eye(3) - cov
+    return mass, com, inertia
+
+
+def test_cuboid_mass_properties_match_reference_kat():
+    # volumetric_convex3.rs:292-345: the convex hull of a shifted 2 - 0.08 wide
+    # cube matches Cuboid(0.96) unit inertia and mass_properties(2.37689), eps 1e-8.
+    # The descriptors carry f32; the KAT uses the same f32-rounded inputs.
+    h32 = float(np.float32(0.96))
+    half = (h32, h32, h32)
+    density = float(np.float32(2.37689))
+    m_hull, _, i_hull = _convex_box_mass_properties(half, np.array([10.0, 10.0, 10.0]), density)
+    sc = scenes.single_body(shape=abi.SHAPE_CUBOID, params=half, ground=False, density=density)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(1)
+    inertia, com = w.mass_properties()
+    assert abs(inertia[0, 0] - m_hull) < 1e-8 * max(1.0, m_hull)
+    expected = [i_hull[0, 0], i_hull[0, 1], i_hull[0, 2], i_hull[1, 1], i_hull[1, 2], i_hull[2, 2]]
+    np.testing.assert_allclose(inertia[0, 1:], expected, rtol=0, atol=1e-8 * m_hull)
+    # Unit inertia (4/12)(hy^2 + hz^2) = 0.6144 for 0.96 (f32-rounded input).
+    assert abs(inertia[0, 1] / inertia[0, 0] - (4.0 / 12.0) * 2 * h32 * h32) < 1e-12
+    np.testing.assert_allclose(com[0], 0.0, atol=1e-15)
+
+
+def test_ball_mass_properties():
+    r, density = float(np.float32(0.7)), 3.0
+    sc = scenes.single_body(shape=abi.SHAPE_BALL, params=(r, 0, 0), ground=False, density=density)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(1)
+    inertia, _ = w.mass_properties()
+    m = 4.0 / 3.0 * math.pi * r ** 3 * density
+    assert abs(inertia[0, 0] - m) < 1e-12 * m
+    assert abs(inertia[0, 1] - 0.4 * m * r * r) < 1e-12 * m
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_free_fall_is_semi_implicit_euler(precision):
+    sc = scenes.single_body(shape=abi.SHAPE_BALL, params=(0.5, 0, 0), position=(0, 100, 0), ground=False)
+    w = OracleWorld(sc.params(), sc.gravity, precision=precision)
+    w.load_scene(sc)
+    dt, g = float(np.float32(1.0 / 60.0)), float(np.float32(-9.81))   # the parameters travel as f32
+    n = 60
+    w.step(n)
+    b = w.bodies()
+    v = g * dt * n
+    y = 100.0 + g * dt * dt * n * (n + 1) / 2.0
+    tol = 1e-9 if precision == 64 else 2e-4
+    assert abs(b["velocity"][0, 1] - v) < tol * 10
+    assert abs(b["position"][0, 1] - y) < tol * 100
+
+
+def test_torque_free_spin_keeps_angular_momentum_direction():
+    # Gyroscopic term (rigid_body.rs:575-581, 598-605) on an asymmetric box spinning about a
+    # near-principal axis: |L| stays nearly constant over a second.
+    sc = scenes.single_body(shape=abi.SHAPE_CUBOID, params=(0.2, 0.5, 1.0), position=(0, 100, 0),
+                            velocity=(0, 0, 0, 5.0, 0.1, 0.1), ground=False)
+    sc.bodies["flags"] = sc.bodies["flags"] & np.uint32(0xffffffff ^ abi.BODY_GRAVITY)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(1)
+
+    def ang_momentum():
+        b = w.bodies()
+        q = b["position"][0, 3:7]
+        x, y, z, ww = q
+        R = np.array([[1 - 2 * (y * y + z * z), 2 * (x * y - z * ww), 2 * (x * z + y * ww)],
+                      [2 * (x * y + z * ww), 1 - 2 * (x * x + z * z), 2 * (y * z - x * ww)],
+                      [2 * (x * z - y * ww), 2 * (y * z + x * ww), 1 - 2 * (x * x + y * y)]])
+        inertia, _ = w.mass_properties()
+        I = np.diag([inertia[0, 1], inertia[0, 4], inertia[0, 6]])
+        return R @ I @ R.T @ b["velocity"][0, 3:]
+
+    L0 = ang_momentum()
+    w.step(60)
+    L1 = ang_momentum()
+    assert np.linalg.norm(L1 - L0) < 0.02 * np.linalg.norm(L0)
+
+
+def test_resting_box_normal_impulse_balances_gravity():
+    sc = scenes.single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 0.5, 0))
+    p = sc.params()
+    p.solve_to_tolerance = 1
+    p.residual_tolerance = 1e-7
+    p.max_iterations_to_tolerance = 500
+    w = OracleWorld(p, sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(30)
+    c = w.contacts_f64()
+    m = 1.0   # 1 x 1 x 1 box, density 1
+    total = c[:, 10].sum()
+    assert abs(total - m * 9.81 / 60.0) < 1e-6
+    b = w.bodies()
+    # Rests with the margins overlapping by the allowed linear error (0.001).
+    assert abs(b["position"][1, 1] - (0.5 + 0.02 - 0.001)) < 2e-4
+
+
+def test_friction_stops_a_sliding_box_at_mu_g():
+    sc = scenes.single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 0.5, 0),
+                            velocity=(1.0, 0, 0, 0, 0, 0))
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(5)
+    v5 = w.bodies()["velocity"][1, 0]
+    w.step(1)
+    v6 = w.bodies()["velocity"][1, 0]
+    decel = (v5 - v6) * 60.0
+    assert abs(decel - 0.5 * 9.81) < 0.05 * 0.5 * 9.81
+    w.step(30)
+    assert abs(w.bodies()["velocity"][1, 0]) < 1e-6
+
+
+def test_resting_body_falls_asleep_and_zeroes_velocity():
+    sc = scenes.single_body(shape=abi.SHAPE_BALL, params=(0.5, 0, 0), position=(0, 0.5, 0))
+    w = OracleWorld(sc.params(), sc.gravity, precision=32)
+    w.load_scene(sc)
+    w.step(400)
+    b = w.bodies()
+    assert b["active"][1] == 0
+    assert np.all(b["velocity"][1] == 0)
+    assert w.counters()["num_active_bodies"] == 0
+
+
+def test_orders_converge_to_the_same_velocities():
+    # The colour order is a permutation of the reference's Gauss-Seidel order; run to a
+    # tight residual both converge to the same post-solve velocities.
+    sc = scenes.pyramid(base=6)
+    out = []
+    for order in (ORDER_REFERENCE, ORDER_COLOUR):
+        p = sc.params()
+        p.solve_to_tolerance = 1
+        p.residual_tolerance = 1e-9
+        p.max_iterations_to_tolerance = 5000
+        p.max_position_iterations = 0
+        w = OracleWorld(p, sc.gravity, precision=64, order=order)
+        w.load_scene(sc)
+        w.step(1)
+        out.append(w.bodies()["velocity"])
+        assert w.counters()["residual"] <= 1e-9
+    np.testing.assert_allclose(out[0], out[1], atol=1e-6)
+
+
+def test_sweep_and_prune_equals_brute_force():
+    sc = scenes.random_cluster(n=300, seed=3, extent=4.0)
+    w = OracleWorld(sc.params(), sc.gravity, precision=32)
+    w.load_scene(sc)
+    w.step(3)
+    w.collision_detection()
+    a = w.pairs()
+    b = w.brute_force_pairs()
+    assert len(a) > 100
+    np.testing.assert_array_equal(a, b)
