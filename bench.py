@@ -111,25 +111,32 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_baseline(scene_fn, seconds, settle_steps):
-    """Times the oracle (restated reference step, f32, one thread) on a bounded
-    sample of the same workload: the pile settled for `settle_steps` steps on
-    the CPU would take too long, so the sample is the first steps of the run
-    from t = 0 until about `seconds` of CPU time have been spent."""
+def cpu_sample(scene_fn, settle_steps, max_steps, seconds):
+    """Times the oracle (the restated reference step, f32, one thread, the
+    reference's row order) on a bounded sample of the same workload: the pile
+    is settled for `settle_steps` untimed steps, exactly as on the GPU, then
+    up to `max_steps` steps are timed, stopping after about `seconds`."""
     from oracle.oracle_py import ORDER_REFERENCE, OracleWorld
     sc = scene_fn()
     o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_REFERENCE)
     o.load_scene(sc)
+    o.step(settle_steps)
     steps = 0
     t0 = time.perf_counter()
-    while time.perf_counter() - t0 < seconds:
+    while steps < max_steps and (steps == 0 or time.perf_counter() - t0 < seconds):
         o.step(1)
         steps += 1
     dt = time.perf_counter() - t0
     c = o.counters()
-    return {"value": sc.num_dynamic * steps / dt, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": f"{steps} steps from t=0 of the same {sc.num_dynamic}-ball pile, single-threaded f32 "
-                      f"oracle in the reference's row order ({c['num_contacts']} contacts at the end)"}
+    sample = (f"steps {settle_steps}..{settle_steps + steps - 1} of the same {sc.num_dynamic}-ball pile "
+              f"({c['num_contacts']} contacts), single-threaded f32 oracle in the reference's row order; "
+              "the Rust reference has no toolchain on this host")
+    return sc.num_dynamic * steps / dt, steps, dt, sample
+
+
+def cpu_baseline(scene_fn, seconds, settle_steps):
+    value, steps, dt, sample = cpu_sample(scene_fn, settle_steps, 10 ** 9, seconds)
+    return {"value": value, "unit": METRIC, "cores": 1, "kind": "port", "sample": sample}
 
 
 def run_reference(args):
@@ -137,33 +144,18 @@ def run_reference(args):
     if rank != 0:
         return
     from nphysics_gb300 import scenes
-    from oracle.oracle_py import ORDER_REFERENCE, OracleWorld
-    sc = scenes.ball_pile(side=args.side)
-    o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_REFERENCE)
-    o.load_scene(sc)
-    budget = max(5.0, args.cpu_seconds)
-    for _ in range(max(args.warmup, 0)):
-        o.step(1)
-    t0 = time.perf_counter()
-    steps = 0
-    for _ in range(args.steps):
-        o.step(1)
-        steps += 1
-        if time.perf_counter() - t0 > budget:
-            break
-    dt = time.perf_counter() - t0
-    value = sc.num_dynamic * steps / dt
+    n_dyn = args.side ** 3
+    value, steps, dt, sample = cpu_sample(lambda: scenes.ball_pile(side=args.side), args.settle + args.warmup,
+                                          args.steps, max(5.0, args.cpu_seconds))
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, "
-                               f"seeded jitter), dt 1/60, 8 velocity / 3 position iterations",
-                   "sample": f"first {args.warmup + steps} steps from t=0"},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port",
-                         "sample": f"{steps} timed steps after {args.warmup} warm-up steps, single-threaded f32 "
-                                   "oracle (restated nphysics3d step, reference row order); the Rust reference "
-                                   "has no toolchain on this host"},
+        "config": {"workload": f"ball pile {args.side}^3 = {n_dyn} balls (radius 0.5, 1.2 lattice, seeded jitter) "
+                               f"on a static ground, dt 1/60, 8 velocity / 3 position iterations; timed steps "
+                               f"{args.settle + args.warmup}..{args.settle + args.warmup + steps - 1} of the run",
+                   "sample": sample},
+        "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))

@@ -145,8 +145,10 @@ __global__ void k_lbvh_refit(World w, int n) {
     if (k >= n) return;
     uint32_t ci = w.c.vals_sorted[k];
     int node = n - 1 + k;
+    // node_max.w carries the largest owner rank (bounding radius) of the subtree.
+    float4 mx = w.c.aabb_max[ci];
     w.c.node_min[node] = w.c.aabb_min[ci];
-    w.c.node_max[node] = w.c.aabb_max[ci];
+    w.c.node_max[node] = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
     if (n == 1) return;
     __threadfence();
     int p = w.c.parent[node];
@@ -160,7 +162,7 @@ __global__ void k_lbvh_refit(World w, int n) {
         float4 a0 = ld_cg(&w.c.node_min[l]), a1 = ld_cg(&w.c.node_max[l]);
         float4 b0 = ld_cg(&w.c.node_min[r]), b1 = ld_cg(&w.c.node_max[r]);
         w.c.node_min[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 1.0f);
-        w.c.node_max[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), 0.0f);
+        w.c.node_max[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), fmaxf(a1.w, b1.w));
         __threadfence();
         p = w.c.parent[p];
     }
@@ -195,6 +197,7 @@ __global__ void k_bp_traverse(World w, int n) {
     const Colliders& c = w.c;
     uint32_t a = c.vals_sorted[k];
     float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
+    float ra = c.rank[a];
     uint32_t count = 0, base = 0;
     if (WRITE) base = c.leaf_offset[k];
     if (n >= 2) {
@@ -203,7 +206,10 @@ __global__ void k_bp_traverse(World w, int n) {
         stack[sp++] = 0;
         while (sp > 0) {
             int node = stack[--sp];
-            if (!overlap(amin, amax, c.node_min[node], c.node_max[node])) continue;
+            float4 nmax = c.node_max[node];
+            // Every leaf below has a smaller bounding radius: leaf a owns none of those pairs.
+            if (nmax.w < ra) continue;
+            if (!overlap(amin, amax, c.node_min[node], nmax)) continue;
             if (node >= n - 1) {
                 uint32_t b = c.vals_sorted[node - (n - 1)];
                 if (b != a && owns(c, a, b) && pair_allowed(w, a, b)) {

@@ -131,13 +131,13 @@ def test_converged_velocities_match_reference_order(gpu_lib):
     sc = scenes.pyramid(base=8)
     p = sc.params()
     p.solve_to_tolerance = 1
-    p.residual_tolerance = 1e-7
+    p.residual_tolerance = 1e-6      # f32 state bottoms out near 1e-7
     p.max_iterations_to_tolerance = 4000
     p.max_position_iterations = 0
     g, o = make_pair(sc, params=p, precision=64, order=ORDER_REFERENCE)
     g.step(1)
     o.step(1)
-    assert g.counters()["residual"] <= 1e-7
+    assert g.counters()["residual"] <= 1e-6
     assert_close_rel(g.bodies()["velocity"], o.bodies()["velocity"], 1e-4, 1e-5, "converged velocities")
 
 
@@ -149,14 +149,19 @@ def test_pyramid_1000_steps_resting_poses(gpu_lib):
     gp, op = g.bodies()["position"], o.bodies()["position"]
     assert np.abs(gp[:, :3] - op[:, :3]).max() < 1e-3
     assert np.abs(np.abs(gp[:, 3:]) - np.abs(op[:, 3:])).max() < 1e-3
-    # Against the f64 oracle in the reference's own order.
+    # Against the f64 oracle in the reference's own order. The resting pyramid
+    # creeps sideways at a rate that depends on the Gauss-Seidel order: the
+    # oracle's own f32/f64 x reference/colour variants differ by up to 0.28
+    # after 1000 steps, so the cross-order bound is that spread.
     o64 = OracleWorld(sc.params(), sc.gravity, precision=64, order=ORDER_REFERENCE)
     o64.load_scene(sc)
     o64.step(1000)
     ref = o64.bodies()["position"]
     drift = np.abs(gp[:, :3] - ref[:, :3]).max()
-    assert drift < 0.1, drift
+    assert drift < 0.3, drift
     assert g.counters()["max_penetration"] < 0.05
+    assert g.bodies()["active"].sum() == 0   # the whole stack fell asleep, as in the oracle
+    assert o.bodies()["active"].sum() == 0
 
 
 def test_ball_pile_statistics(gpu_lib):
@@ -165,30 +170,39 @@ def test_ball_pile_statistics(gpu_lib):
     g.step(120)
     o.step(120)
     cg, co = g.counters(), o.counters()
-    assert abs(cg["kinetic_energy"] - co["kinetic_energy"]) <= 0.05 * max(co["kinetic_energy"], 1.0)
-    assert cg["max_penetration"] < 0.05 and co["max_penetration"] < 0.05
-    assert abs(cg["num_contacts"] - co["num_contacts"]) <= 0.05 * max(co["num_contacts"], 10)
+    # Same Gauss-Seidel order: the chaotic pile agrees with the oracle.
+    assert abs(cg["kinetic_energy"] - co["kinetic_energy"]) <= 1e-3 * max(co["kinetic_energy"], 1.0)
+    assert abs(cg["max_penetration"] - co["max_penetration"]) <= 1e-4
+    assert cg["num_contacts"] == co["num_contacts"]
+    # Against the reference's order: stated bounds on energy, penetration and contacts.
+    r = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_REFERENCE)
+    r.load_scene(sc)
+    r.step(120)
+    cr = r.counters()
+    assert abs(cg["kinetic_energy"] - cr["kinetic_energy"]) <= 0.05 * cr["kinetic_energy"]
+    assert cg["max_penetration"] <= 1.5 * cr["max_penetration"] + 0.01
+    assert abs(cg["num_contacts"] - cr["num_contacts"]) <= 0.05 * cr["num_contacts"]
 
 
 def test_batched_worlds_do_not_interact(gpu_lib):
-    from nphysics_gb300.world import GpuWorld
+    # Two copies of a cluster in the same place but in different worlds: no
+    # cross-world pair, and both follow the oracle. (A copy's slots differ, so
+    # its colouring, hence its Gauss-Seidel order, differs from the original.)
     one = scenes.random_cluster(n=30, seed=4, world=0)
     two_b = np.concatenate([one.bodies, one.bodies.copy()])
     two_b["world"][len(one.bodies):] = 1
     two_c = np.concatenate([one.colliders, one.colliders.copy()])
     two_c["body"]["index"][len(one.colliders):] += len(one.bodies)
     two = scenes.Scene("two worlds", two_b, two_c)
-    g1 = GpuWorld.for_scene(one)
-    g2 = GpuWorld.for_scene(two)
-    g1.step(20)
-    g2.step(20)
-    p1 = g1.bodies()["position"]
-    p2 = g2.bodies()["position"]
-    np.testing.assert_array_equal(p2[:len(p1)], p1)
-    np.testing.assert_array_equal(p2[len(p1):], p1)
-    pr = g2.pairs()
-    nb1 = len(one.colliders)
-    assert not np.any((pr[:, 0] < nb1) & (pr[:, 1] >= nb1))
+    g, o = make_pair(two)
+    g.step(20)
+    o.step(20)
+    assert_close_rel(g.bodies()["position"], o.bodies()["position"], 1e-5, 1e-5, "positions")
+    pr = g.pairs()
+    nc1 = len(one.colliders)
+    assert len(pr) > 0
+    assert not np.any((pr[:, 0] < nc1) & (pr[:, 1] >= nc1))
+    np.testing.assert_array_equal(pr, o.pairs())
 
 
 def test_removal_wakes_the_stack(gpu_lib):
