@@ -38,12 +38,17 @@ def _stale(obj, src):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
+# The persistent solver kernel reads, after a grid barrier, data that other
+# SMs wrote: its global loads bypass L1 (-dlcm=cg) so none is served stale.
+EXTRA = {"k_solve.cu": ["-Xptxas", "-dlcm=cg"]}
+
+
 def _compile(src):
     s = os.path.join(CSRC, src)
     o = os.path.join(OUT, src.replace(".cu", ".o"))
     if not _stale(o, s):
         return o, False
-    cmd = [nvcc()] + _flags() + ["-c", s, "-o", o + ".tmp"]
+    cmd = [nvcc()] + _flags() + EXTRA.get(src, []) + ["-c", s, "-o", o + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")

@@ -26,7 +26,13 @@
 namespace npgpu_dev {
 
 constexpr int kSolveThreads = 256;
-constexpr unsigned kSpinLimit = 1u << 25;   // about a second of __nanosleep(32)
+constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // a bounded wait gives up after one second
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 // Grid-wide barrier. Returns false when the wait gave up (ERRF_TIMEOUT set);
 // the caller then leaves the kernel.
@@ -42,14 +48,16 @@ __device__ __forceinline__ bool grid_sync(Control* ctl) {
             __threadfence();
             atomicAdd(&ctl->barrier_gen, 1u);
         } else {
+            unsigned long long t0 = global_ns();
             unsigned spins = 0;
             while (*genp == gen) {
-                if (((volatile uint32_t*)&ctl->err)[0] & ERRF_TIMEOUT) break;
-                if (++spins > kSpinLimit) {
-                    atomicOr(&ctl->err, ERRF_TIMEOUT);
-                    break;
+                if ((++spins & 255u) == 0u) {
+                    if (((volatile uint32_t*)&ctl->err)[0] & ERRF_TIMEOUT) break;
+                    if (global_ns() - t0 > kWaitLimitNs) {
+                        atomicOr(&ctl->err, ERRF_TIMEOUT);
+                        break;
+                    }
                 }
-                __nanosleep(32);
             }
         }
         __threadfence();
@@ -221,6 +229,19 @@ __device__ __forceinline__ void axpy(const float* row, DV& dv, float a, bool has
         for (int k = 0; k < 6; ++k) dv.b[k] = a * row[RF_WJ2 + k] + dv.b[k];
     }
 }
+// A row is 7 float4 (112 bytes, 16-byte aligned): loaded into registers at once.
+__device__ __forceinline__ void load_row(const float* p, float* r) {
+    const float4* q = reinterpret_cast<const float4*>(p);
+#pragma unroll
+    for (int k = 0; k < 7; ++k) {
+        float4 x = q[k];
+        r[4 * k] = x.x;
+        r[4 * k + 1] = x.y;
+        r[4 * k + 2] = x.z;
+        r[4 * k + 3] = x.w;
+    }
+}
+
 __device__ __forceinline__ void load_dv(const float* dvg, int i, float* o) {
     if (i < 0) return;
 #pragma unroll
@@ -576,13 +597,18 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
                 uint32_t nc = w.s.sm_nc[s];
                 for (uint32_t k = 0; k < nc; ++k) {
                     float li = rows[(3 * k) * kRowFloats + RF_IMP];
-                    for (int sdir = 1; sdir <= 2; ++sdir) {
-                        float* r = rows + (3 * k + sdir) * kRowFloats;
+                    float rr[2][kRowFloats];
+                    load_row(rows + (3 * k + 1) * kRowFloats, rr[0]);
+                    load_row(rows + (3 * k + 2) * kRowFloats, rr[1]);
+#pragma unroll
+                    for (int sdir = 0; sdir < 2; ++sdir) {
+                        const float* r = rr[sdir];
+                        float* rg = rows + (3 * k + 1 + sdir) * kRowFloats;
                         float imp = r[RF_IMP];
                         if (li == 0.0f) {
                             if (imp != 0.0f) {
                                 axpy(r, dv, -imp, h1, h2);
-                                r[RF_IMP] = 0.0f;
+                                rg[RF_IMP] = 0.0f;
                             }
                             continue;
                         }
@@ -592,7 +618,7 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
                         if (ni < mn) ni = mn;
                         else if (ni > mx) ni = mx;
                         float dl = ni - imp;
-                        r[RF_IMP] = ni;
+                        rg[RF_IMP] = ni;
                         axpy(r, dv, dl, h1, h2);
                     }
                 }
@@ -613,13 +639,15 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
                 float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
                 uint32_t nc = w.s.sm_nc[s];
                 for (uint32_t k = 0; k < nc; ++k) {
-                    float* r = rows + (3 * k) * kRowFloats;
+                    float r[kRowFloats];
+                    float* rg = rows + (3 * k) * kRowFloats;
+                    load_row(rg, r);
                     float imp = r[RF_IMP];
                     float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
                     float ni = imp - r[RF_R] * dimp;
                     ni = ni > 0.0f ? ni : 0.0f;
                     float dl = ni - imp;
-                    r[RF_IMP] = ni;
+                    rg[RF_IMP] = ni;
                     axpy(r, dv, dl, h1, h2);
                 }
                 store_dv(b.dv, b1, dv.a);

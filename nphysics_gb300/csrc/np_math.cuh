@@ -58,16 +58,31 @@ NP_HD Q qmul(Q a, Q b) {
     r.k = a.w * b.k + a.i * b.j - a.j * b.i + a.k * b.w;
     return r;
 }
-// UnitQuaternion::new(axisangle): the quaternion exponential of axisangle / 2.
-// sin and cos are taken in double and rounded to f32.
+// UnitQuaternion::new(axisangle): the quaternion exponential of axisangle / 2,
+// w = cos(n), v = h sin(n) / n with h = axisangle / 2, n = |h|.
+// For n < 1/4 (every rotation of less than 1/2 rad per step) cos(n) and
+// sin(n)/n come from their Maclaurin series truncated after the n^10 term
+// (remainder below 2e-16), evaluated by Horner's rule in f32; larger angles
+// take sin and cos in double, rounded to f32.
+NP_HD void sinc_cos_small(float nn, float& sinc, float& c) {
+    c = 1.0f + nn * (-0.5f + nn * (4.16666679e-02f + nn * (-1.38888892e-03f + nn * (2.48015876e-05f +
+                                                                                   nn * (-2.75573188e-07f)))));
+    sinc = 1.0f + nn * (-1.66666672e-01f + nn * (8.33333377e-03f + nn * (-1.98412701e-04f + nn * (2.75573188e-06f +
+                                                                                                 nn * (-2.50521079e-08f)))));
+}
 NP_HD Q qexp(V axisangle) {
     V h = divs(axisangle, 2.0f);
     float nn = dot(h, h);
     if (nn == 0.0f) return Q{0.0f, 0.0f, 0.0f, 1.0f};
-    float n = sqrtf(nn);
-    float s = (float)sin((double)n);
-    float c = (float)cos((double)n);
-    float f = s / n;
+    float f, c;
+    if (nn < 0.0625f) {
+        sinc_cos_small(nn, f, c);
+    } else {
+        float n = sqrtf(nn);
+        float s = (float)sin((double)n);
+        c = (float)cos((double)n);
+        f = s / n;
+    }
     V v = mul(h, f);
     return Q{v.x, v.y, v.z, c};
 }

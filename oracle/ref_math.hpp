@@ -63,16 +63,38 @@ template <class R> inline Quat<R> qmul(Quat<R> a, Quat<R> b) {
     return r;
 }
 // UnitQuaternion::new(axisangle) = exp(axisangle / 2): w = cos(n), v = h sin(n)/n
-// with h = axisangle/2 and n = |h|. sin and cos are evaluated in double and
-// rounded, so that the single-precision result does not depend on the libm.
+// with h = axisangle/2 and n = |h|.
+// f32: for n < 1/4, cos(n) and sin(n)/n are their Maclaurin series truncated
+// after the n^10 term, by Horner's rule in f32 (the GPU evaluates the same
+// polynomial); larger angles use sin and cos in double, rounded to f32.
+// f64: std::sin / std::cos.
+inline void sinc_cos_small(float nn, float& sinc, float& c) {
+    c = 1.0f + nn * (-0.5f + nn * (4.16666679e-02f + nn * (-1.38888892e-03f + nn * (2.48015876e-05f +
+                                                                                   nn * (-2.75573188e-07f)))));
+    sinc = 1.0f + nn * (-1.66666672e-01f + nn * (8.33333377e-03f + nn * (-1.98412701e-04f + nn * (2.75573188e-06f +
+                                                                                                 nn * (-2.50521079e-08f)))));
+}
+template <class R> inline void sinc_cos(R nn, R& f, R& c) {
+    R n = std::sqrt(nn);
+    c = std::cos(n);
+    f = std::sin(n) / n;
+}
+template <> inline void sinc_cos<float>(float nn, float& f, float& c) {
+    if (nn < 0.0625f) {
+        sinc_cos_small(nn, f, c);
+        return;
+    }
+    float n = std::sqrt(nn);
+    float s = float(std::sin(double(n)));
+    c = float(std::cos(double(n)));
+    f = s / n;
+}
 template <class R> inline Quat<R> qexp_scaled_axis(V3<R> axisangle) {
     V3<R> h = vdiv(axisangle, R(2));
     R nn = dot(h, h);
     if (nn == R(0)) return Quat<R>{R(0), R(0), R(0), R(1)};
-    R n = std::sqrt(nn);
-    R s = R(std::sin(double(n)));
-    R c = R(std::cos(double(n)));
-    R f = s / n;
+    R f, c;
+    sinc_cos(nn, f, c);
     V3<R> v = h * f;
     return Quat<R>{v.x, v.y, v.z, c};
 }
