@@ -290,8 +290,31 @@ npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max
 npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out);
 
 /* One-line description of the last failure on this world (or of the last
- * failed npgpu_create when w is NULL). */
+ * failed npgpu_create / npgpu_find_pairs_static when w is NULL). */
 const char* npgpu_last_error(const npgpu_world* w);
+
+/* Broad phase over caller-provided boxes that allocates nothing. This entry
+ * point has no counterpart in the reference: it exists for callers that
+ * cannot call cudaMalloc (code running while a CUDA graph is captured,
+ * real-time loops that must not block on the allocator, hosts whose device
+ * memory belongs to another runtime's pool).
+ *
+ * Inputs (device memory): aabbs6[6n] = (min x, y, z, max x, y, z) per box;
+ * groups[n] (or NULL): boxes pair only within the same group (< 65536).
+ * Outputs (device memory): pairs2[2 * max_pairs] receives the pairs (i, j),
+ * i < j, of boxes whose closed boxes intersect, in no particular order;
+ * *count receives the number of pairs (only the first max_pairs are written),
+ * or UINT32_MAX if a tree bound was hit. Work is queued on `stream` (a
+ * cudaStream_t, NULL = default stream); results are ready when it completes.
+ *
+ * Limits: at most 32768 boxes per call (NPGPU_ERR_CAPACITY otherwise). The
+ * scratch memory is one fixed 8 MiB __device__ array in the library, held on
+ * every GPU that loads the library until the process exits. The first call on
+ * a device (that device current) looks up the array's address; make it before
+ * any stream capture. Calls share the array: calls whose work overlaps on the
+ * GPU race. No call allocates or frees memory. */
+npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint32_t* groups, uint32_t n, uint32_t* pairs2,
+                                     uint32_t max_pairs, uint32_t* count, void* stream);
 
 #ifdef __cplusplus
 }

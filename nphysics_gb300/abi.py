@@ -232,6 +232,8 @@ def load_library(path=LIB_PATH):
         "npgpu_get_contacts": (C.c_int, [W, P(Contact), C.c_uint32, P(C.c_uint32)]),
         "npgpu_get_counters": (C.c_int, [W, P(Counters)]),
         "npgpu_last_error": (C.c_char_p, [W]),
+        "npgpu_find_pairs_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                                              C.c_void_p, C.c_void_p]),
     }
     for name, (res, args) in decl.items():
         fn = getattr(lib, name)
@@ -246,5 +248,5 @@ EXPORTED = [
     "npgpu_set_params", "npgpu_set_gravity", "npgpu_upsert_bodies", "npgpu_upsert_colliders",
     "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_step",
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
-    "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error",
+    "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
 ]

@@ -136,6 +136,11 @@ struct npgpu_world {
 
 static std::string g_create_error;
 
+namespace npgpu_dev {
+// Message returned by npgpu_last_error(NULL) for calls without a world.
+void set_global_error(const std::string& msg) { g_create_error = msg; }
+}  // namespace npgpu_dev
+
 static npgpu_status fail(npgpu_world* w, npgpu_status s, const std::string& msg) {
     if (w) w->last_error = msg;
     else g_create_error = msg;
