@@ -1,31 +1,42 @@
-// k_solve.cu -- the solver half of MechanicalWorld::step as one persistent,
-// cooperatively launched kernel (grid = co-resident blocks, phases separated
-// by a bounded software grid barrier):
+// k_solve.cu -- the solver half of MechanicalWorld::step on the device.
 //
 //   activation   ActivationManager::update (src/detection/activation_manager.rs:61-201):
 //                RWA energies, islands by lock-free union-find, sleep / wake
 //   collection   manifolds handed to the solver (src/world/mechanical_world.rs:287-300)
-//   colouring    Jones-Plassmann rounds with first-fit colours over dynamic-body
-//                conflicts; manifolds of one colour share no dynamic body
+//   colouring    greedy first-fit colouring of the manifolds in decreasing hash
+//                priority (the Jones-Plassmann first-fit colouring); manifolds of
+//                one colour share no dynamic body
 //   assembly     SignoriniCoulombPyramidModel::constraints
 //                (src/solver/signorini_coulomb_pyramid_model.rs:56-224,
 //                signorini_model.rs:37-138, helper.rs:53-135, rigid_body.rs:672-722)
 //   SOR-Prox     SORProx::solve (src/solver/sor_prox.rs:48-179): warm start, then per
-//                iteration every friction row, then every normal row, colour by colour
+//                iteration every friction row, then every normal row
 //   residual     FP64 complementarity residual
 //   cache        cache_impulses (signorini_coulomb_pyramid_model.rs:226-261)
 //   integrate    update_velocities_and_integrate (moreau_jean_solver.rs:328-347)
-//   position     NonlinearSORProx::solve (src/solver/nonlinear_sor_prox.rs:17-309), colour by colour
+//   position     NonlinearSORProx::solve (src/solver/nonlinear_sor_prox.rs:17-309)
 //   post         kinematic integration, update_dynamics, clear_forces (mechanical_world.rs:328-367)
 //
-// Within one colour every manifold is handled by one thread, which walks its
-// contacts in order; the result equals a sequential Gauss-Seidel sweep over
-// the manifolds sorted by colour.
+// Gauss-Seidel order. The sequential order the GPU reproduces is: manifolds
+// sorted by colour, each manifold's contacts in order. Instead of a grid
+// barrier between colours, every dynamic body carries a version counter: the
+// task (sweep s, manifold m) may touch body b once b's counter equals
+// s * k_b + r, where k_b is the number of b's solver manifolds and r the
+// number of them with a smaller colour; it then publishes b's new state and
+// the counter r + 1 with release semantics. Each body therefore sees its
+// updates in exactly the sequential order, and the critical path is a chain of
+// dependent manifolds rather than a barrier per colour. The colouring uses the
+// same scheme over priorities. Threads poll their tasks without blocking, so
+// any assignment of manifolds to resident threads makes progress.
+#include <cub/device/device_scan.cuh>
+
 #include "narrow.cuh"
 
 namespace npgpu_dev {
 
-constexpr int kSolveThreads = 256;
+constexpr int kItemThreads = 256;
+constexpr int kCoopThreads = 256;
+constexpr int kMaxPerThread = 16;
 constexpr unsigned long long kWaitLimitNs = 1000000000ull;   // a bounded wait gives up after one second
 
 __device__ __forceinline__ unsigned long long global_ns() {
@@ -33,44 +44,51 @@ __device__ __forceinline__ unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void red_release_add(uint32_t* p, uint32_t v) {
+    asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ bool err_set(const Control* ctl, uint32_t bits) {
+    return (ld_acquire(&ctl->err) & bits) != 0;
+}
 
-// Grid-wide barrier. Returns false when the wait gave up (ERRF_TIMEOUT set);
-// the caller then leaves the kernel.
-__device__ __forceinline__ bool grid_sync(Control* ctl) {
+// Grid-wide barrier over a monotonic arrival counter (zeroed before the launch).
+// Returns false when the wait gave up (ERRF_TIMEOUT); the caller then leaves.
+__device__ __forceinline__ bool grid_sync(Control* ctl, uint32_t& epoch) {
     __syncthreads();
+    ++epoch;
+    __shared__ int s_ok;
     if (threadIdx.x == 0) {
-        volatile uint32_t* genp = &ctl->barrier_gen;
-        uint32_t gen = *genp;
-        __threadfence();
-        uint32_t arrived = atomicAdd(&ctl->barrier_count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&ctl->barrier_count, 0u);
-            __threadfence();
-            atomicAdd(&ctl->barrier_gen, 1u);
-        } else {
+        int ok = 1;
+        uint32_t target = epoch * gridDim.x;
+        red_release_add(&ctl->barrier_count, 1u);
+        if (ld_acquire(&ctl->barrier_count) < target) {
             unsigned long long t0 = global_ns();
             unsigned spins = 0;
-            while (*genp == gen) {
-                if ((++spins & 255u) == 0u) {
-                    if (((volatile uint32_t*)&ctl->err)[0] & ERRF_TIMEOUT) break;
-                    if (global_ns() - t0 > kWaitLimitNs) {
+            while (ld_acquire(&ctl->barrier_count) < target) {
+                if ((++spins & 63u) == 0u) {
+                    if (err_set(ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs) {
                         atomicOr(&ctl->err, ERRF_TIMEOUT);
+                        ok = 0;
                         break;
                     }
                 }
             }
         }
-        __threadfence();
+        s_ok = ok;
     }
     __syncthreads();
-    return !(((volatile uint32_t*)&ctl->err)[0] & ERRF_TIMEOUT);
+    return s_ok != 0;
 }
 
 #define GRID_FOR(i, n) for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
-#define SYNC_OR_RETURN() \
-    do {                 \
-        if (!grid_sync(w.ctl)) return; \
-    } while (0)
 
 __device__ __forceinline__ uint32_t pair_hash22(uint32_t c1, uint32_t c2) {
     uint32_t h = c1 * 0x9E3779B1u ^ (c2 + 0x7F4A7C15u) * 0x85EBCA77u;
@@ -85,7 +103,7 @@ __device__ __forceinline__ unsigned long long pair_priority(uint32_t c1, uint32_
     return ((unsigned long long)pair_hash22(c1, c2) << 42) | ((unsigned long long)c1 << 21) | (unsigned long long)c2;
 }
 
-// Lock-free union-find over body slots (link the larger root under the smaller).
+// Lock-free union-find over body slots (the larger root is linked under the smaller).
 __device__ __forceinline__ uint32_t uf_find(uint32_t* parent, uint32_t x) {
     uint32_t p = ((volatile uint32_t*)parent)[x];
     int guard = 0;
@@ -196,7 +214,6 @@ __device__ __forceinline__ void tangent_basis(np::V n, np::V& t1, np::V& t2) {
     t2 = np::divs(b, np::norm(b));
 }
 
-// Velocity-solver state of one manifold: the dv of its dynamic bodies.
 struct DV {
     float a[6], b[6];
 };
@@ -241,7 +258,6 @@ __device__ __forceinline__ void load_row(const float* p, float* r) {
         r[4 * k + 3] = x.w;
     }
 }
-
 __device__ __forceinline__ void load_dv(const float* dvg, int i, float* o) {
     if (i < 0) return;
 #pragma unroll
@@ -253,7 +269,6 @@ __device__ __forceinline__ void store_dv(float* dvg, int i, const float* o) {
     for (int k = 0; k < 6; ++k) dvg[6 * i + k] = o[k];
 }
 
-// FP64 residual terms of one row.
 __device__ __forceinline__ void residual_row(const float* row, const DV& dv, bool has1, bool has2, bool friction,
                                              double normal_impulse, double& s2, double& l2) {
     double d = 0.0;
@@ -285,66 +300,22 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
     double t = 0.0;
     if (threadIdx.x == 0)
         for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += sh[k];
+    __syncthreads();
     return t;
 }
 
-// Evaluates the FP64 residual over all solver rows; the result lands in ctl->residual.
-__device__ bool eval_residual(const World& w, uint32_t ms, double* sh, bool initial) {
-    double s2 = 0.0, l2 = 0.0;
-    GRID_FOR(s, ms) {
-        int b1 = w.s.sm_b1[s], b2 = w.s.sm_b2[s];
-        uint32_t nc = w.s.sm_nc[s];
-        DV dv;
-        load_dv(w.b.dv, b1, dv.a);
-        load_dv(w.b.dv, b2, dv.b);
-        const float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
-        for (uint32_t k = 0; k < nc; ++k) {
-            const float* rn = rows + (3 * k) * kRowFloats;
-            residual_row(rn, dv, b1 >= 0, b2 >= 0, false, 0.0, s2, l2);
-            residual_row(rn + kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
-            residual_row(rn + 2 * kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
-        }
-    }
-    double ts = block_sum(s2, sh);
-    double tl = block_sum(l2, sh);
-    if (threadIdx.x == 0) {
-        atomicAdd(&w.ctl->res_acc[0], ts);
-        atomicAdd(&w.ctl->res_acc[1], tl);
-    }
-    if (!grid_sync(w.ctl)) return false;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        double a = w.ctl->res_acc[0], b = w.ctl->res_acc[1];
-        double r = sqrt(a) / fmax(1.0, sqrt(b));
-        w.ctl->residual = r;
-        if (initial) w.ctl->residual_initial = r;
-        w.ctl->res_acc[0] = 0.0;
-        w.ctl->res_acc[1] = 0.0;
-    }
-    return grid_sync(w.ctl);
-}
-
-__device__ __forceinline__ void stamp(const World& w, const StepParams& p, int k) {
-    if (p.profile && blockIdx.x == 0 && threadIdx.x == 0) {
-        unsigned long long t;
-        asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
-        w.ctl->t_phase[k] = t;
-    }
-}
-
-__global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) {
-    __shared__ double sh[32];
-    __shared__ uint32_t sh_scan[kMaxColours + 1];
+// ================================================================ activation
+__global__ void k_act_init(World w, StepParams p) {
     const Bodies& b = w.b;
-    const Colliders& c = w.c;
-    const uint32_t nb = w.nb_slots;
-    stamp(w, p, 0);
-
-    // ---- activation: energies, union-find init -------------------------------------------
-    GRID_FOR(i, nb) {
+    GRID_FOR(i, w.nb_slots) {
         uint32_t info = b.info[i];
         b.uf_parent[i] = i;
         b.can_deact[i] = 1;
-        b.jp_used[i] = 0ull;
+        b.used[i] = 0ull;
+        b.adj_count[i] = 0;
+        b.adj_fill[i] = 0;
+        b.col_cnt[i] = 0;
+        b.vel_ver[i] = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) b.dv[6 * i + k] = 0.0f;
         info &= ~BI_ISLAND;
@@ -359,31 +330,35 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
             b.energy[i] = (cap < e) ? cap : e;
         }
     }
-    if (blockIdx.x == 0 && threadIdx.x < kMaxColours) {
-        w.s.colour_count[threadIdx.x] = 0;
-        if (threadIdx.x == 0) {
-            w.ctl->nsolver = 0;
-            w.ctl->ncolours = 0;
-            w.ctl->jp_remaining[0] = 0;
-            w.ctl->jp_remaining[1] = 0;
-            w.ctl->nsolver_contacts = 0;
-            w.ctl->nactive = 0;
-            w.ctl->res_acc[0] = 0.0;
-            w.ctl->res_acc[1] = 0.0;
-            w.ctl->kinetic_energy = 0.0;
-        }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        Control* c = w.ctl;
+        c->nsolver = 0;
+        c->ncolours = 0;
+        c->nsolver_contacts = 0;
+        c->nactive = 0;
+        c->iterations = 0;
+        c->res_acc[0] = 0.0;
+        c->res_acc[1] = 0.0;
+        c->residual = 0.0;
+        c->residual_initial = 0.0;
+        c->kinetic_energy = 0.0;
     }
-    SYNC_OR_RETURN();
+}
+
+__global__ void k_act_union(World w) {
     const uint32_t npairs = w.ctl->npairs;
     GRID_FOR(q, npairs) {
         if (w.cur.ncont[q] == 0) continue;
         uint2 pr = w.cur.pair[q];
-        uint32_t b1 = c.body[pr.x], b2 = c.body[pr.y];
-        uint32_t s1 = bi_status(b.info[b1]), s2 = bi_status(b.info[b2]);
-        if ((s1 == 2u || s1 == 3u) && (s2 == 2u || s2 == 3u)) uf_union(b.uf_parent, b1, b2, &w.ctl->err);
+        uint32_t b1 = w.c.body[pr.x], b2 = w.c.body[pr.y];
+        uint32_t s1 = bi_status(w.b.info[b1]), s2 = bi_status(w.b.info[b2]);
+        if ((s1 == 2u || s1 == 3u) && (s2 == 2u || s2 == 3u)) uf_union(w.b.uf_parent, b1, b2, &w.ctl->err);
     }
-    SYNC_OR_RETURN();
-    GRID_FOR(i, nb) {
+}
+
+__global__ void k_act_root(World w) {
+    const Bodies& b = w.b;
+    GRID_FOR(i, w.nb_slots) {
         uint32_t info = b.info[i];
         uint32_t st = bi_status(info);
         if (!(info & BI_ALIVE) || !(st == 2u || st == 3u)) continue;
@@ -391,8 +366,11 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
         bool ok = body_can_sleep(info) && b.energy[i] < b.sleep_thr[i];
         if (!ok) atomicAnd(&b.can_deact[r], 0);
     }
-    SYNC_OR_RETURN();
-    GRID_FOR(i, nb) {
+}
+
+__global__ void k_act_apply(World w) {
+    const Bodies& b = w.b;
+    GRID_FOR(i, w.nb_slots) {
         uint32_t info = b.info[i];
         uint32_t st = bi_status(info);
         if (!(info & BI_ALIVE) || !(st == 2u || st == 3u)) continue;
@@ -412,123 +390,160 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
             if (!(en != 0.0f) && body_can_sleep(info)) body_activate(b, i);
         }
     }
-    SYNC_OR_RETURN();
-    stamp(w, p, 1);
+}
 
-    // ---- manifold collection ----------------------------------------------------------------
+// ================================================================ collection + colouring
+__global__ void k_collect(World w) {
+    const uint32_t npairs = w.ctl->npairs;
+    const Bodies& b = w.b;
     GRID_FOR(q, npairs) {
         uint32_t nc = w.cur.ncont[q];
         if (nc == 0) continue;
         uint2 pr = w.cur.pair[q];
-        uint32_t b1 = c.body[pr.x], b2 = c.body[pr.y];
-        uint32_t i1 = b.info[b1], i2 = b.info[b2];
-        uint32_t s1 = bi_status(i1), s2 = bi_status(i2);
+        uint32_t b1 = w.c.body[pr.x], b2 = w.c.body[pr.y];
+        uint32_t s1 = bi_status(b.info[b1]), s2 = bi_status(b.info[b2]);
         if (s1 == 0u || s2 == 0u) continue;
         bool a1 = s1 == 2u && b.energy[b1] != 0.0f;
         bool a2 = s2 == 2u && b.energy[b2] != 0.0f;
         if (!(a1 || a2)) continue;
-        uint32_t idx = atomicAdd(&w.ctl->nsolver, 1u);
-        w.s.sm_list[idx] = q;
-        w.s.sm_state[idx] = 0;
+        uint32_t m = atomicAdd(&w.ctl->nsolver, 1u);
+        w.s.sm_list[m] = q;
+        w.s.sm_b1[m] = s1 == 2u ? (int)b1 : -1;
+        w.s.sm_b2[m] = s2 == 2u ? (int)b2 : -1;
+        w.s.sm_nc[m] = nc;
+        if (s1 == 2u) atomicAdd(&b.adj_count[b1], 1u);
+        if (s2 == 2u) atomicAdd(&b.adj_count[b2], 1u);
         atomicAdd(&w.ctl->nsolver_contacts, nc);
     }
-    SYNC_OR_RETURN();
-    const uint32_t ms = w.ctl->nsolver;
+}
 
-    // ---- colouring: Jones-Plassmann rounds, first-fit colours -------------------------------
-    for (uint32_t round = 0;; ++round) {
-        GRID_FOR(m, ms) {
-            if (w.s.sm_state[m] != 0) continue;
-            uint2 pr = w.cur.pair[w.s.sm_list[m]];
-            unsigned long long pri = pair_priority(pr.x, pr.y);
-            uint32_t b1 = c.body[pr.x], b2 = c.body[pr.y];
-            if (bi_status(b.info[b1]) == 2u) atomicMax(&b.jp_best[b1], pri);
-            if (bi_status(b.info[b2]) == 2u) atomicMax(&b.jp_best[b2], pri);
-        }
-        SYNC_OR_RETURN();
-        GRID_FOR(m, ms) {
-            if (w.s.sm_state[m] != 0) continue;
-            uint2 pr = w.cur.pair[w.s.sm_list[m]];
-            unsigned long long pri = pair_priority(pr.x, pr.y);
-            uint32_t b1 = c.body[pr.x], b2 = c.body[pr.y];
-            bool d1 = bi_status(b.info[b1]) == 2u, d2 = bi_status(b.info[b2]) == 2u;
-            bool won = (!d1 || b.jp_best[b1] == pri) && (!d2 || b.jp_best[b2] == pri);
-            if (!won) {
-                atomicAdd(&w.ctl->jp_remaining[round & 1u], 1u);
-                continue;
+__global__ void k_adj_fill(World w) {
+    const uint32_t ms = w.ctl->nsolver;
+    GRID_FOR(m, ms) {
+        int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+        if (b1 >= 0) w.s.adj[w.b.adj_start[b1] + atomicAdd(&w.b.adj_fill[b1], 1u)] = m;
+        if (b2 >= 0) w.s.adj[w.b.adj_start[b2] + atomicAdd(&w.b.adj_fill[b2], 1u)] = m;
+    }
+}
+
+__device__ __forceinline__ unsigned long long sm_priority(const World& w, uint32_t m) {
+    uint2 pr = w.cur.pair[w.s.sm_list[m]];
+    return pair_priority(pr.x, pr.y);
+}
+
+// Rank of each manifold among the solver manifolds of each of its dynamic
+// bodies, by decreasing priority.
+__global__ void k_prank(World w) {
+    const uint32_t ms = w.ctl->nsolver;
+    GRID_FOR(m, ms) {
+        unsigned long long pm = sm_priority(w, m);
+        uint32_t r[2] = {0u, 0u};
+        int bs[2] = {w.s.sm_b1[m], w.s.sm_b2[m]};
+        for (int side = 0; side < 2; ++side) {
+            int b = bs[side];
+            if (b < 0) continue;
+            uint32_t s0 = w.b.adj_start[b], n = w.b.adj_count[b], cnt = 0;
+            for (uint32_t e = 0; e < n; ++e) {
+                uint32_t o = w.s.adj[s0 + e];
+                if (o != m && sm_priority(w, o) > pm) ++cnt;
             }
+            r[side] = cnt;
+        }
+        w.s.sm_prank[m] = r[0] | (r[1] << 16);
+    }
+}
+
+// Greedy first-fit colouring in decreasing priority: a manifold takes the
+// smallest colour unused by the higher-priority manifolds of its dynamic
+// bodies, as soon as those are coloured.
+__global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
+    const uint32_t ms = w.ctl->nsolver;
+    const uint32_t T = gridDim.x * blockDim.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nmine = t < ms ? (ms - t + T - 1) / T : 0u;
+    if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
+        if (t == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        return;
+    }
+    const Bodies& b = w.b;
+    uint32_t done = 0, todo = (nmine >= 32u) ? 0xffffffffu : ((1u << nmine) - 1u);
+    unsigned long long t0 = 0;
+    unsigned spins = 0;
+    while (done != todo) {
+        bool progress = false;
+        for (uint32_t k = 0; k < nmine; ++k) {
+            if (done & (1u << k)) continue;
+            uint32_t m = t + k * T;
+            int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+            uint32_t pr = w.s.sm_prank[m];
+            uint32_t r1 = pr & 0xffffu, r2 = pr >> 16;
+            if (b1 >= 0 && ld_acquire(b.col_cnt + b1) != r1) continue;
+            if (b2 >= 0 && ld_acquire(b.col_cnt + b2) != r2) continue;
             unsigned long long mask = 0ull;
-            if (d1) mask |= b.jp_used[b1];
-            if (d2) mask |= b.jp_used[b2];
-            uint32_t col = (uint32_t)(__ffsll((long long)~mask) - 1);
+            if (b1 >= 0) mask |= b.used[b1];
+            if (b2 >= 0) mask |= b.used[b2];
+            uint32_t col;
             if (mask == ~0ull) {
                 atomicOr(&w.ctl->err, ERRF_COLOURS);
                 col = kMaxColours - 1;
+            } else {
+                col = (uint32_t)(__ffsll((long long)~mask) - 1);
             }
             w.s.sm_colour[m] = col;
-            w.s.sm_state[m] = 1;
-            if (d1) b.jp_used[b1] |= (1ull << col);
-            if (d2) b.jp_used[b2] |= (1ull << col);
-            atomicMax(&w.ctl->ncolours, col + 1);
-            atomicAdd(&w.s.colour_count[col], 1u);
+            if (b1 >= 0) {
+                b.used[b1] = b.used[b1] | (1ull << col);
+                st_release(b.col_cnt + b1, r1 + 1u);
+            }
+            if (b2 >= 0) {
+                b.used[b2] = b.used[b2] | (1ull << col);
+                st_release(b.col_cnt + b2, r2 + 1u);
+            }
+            atomicMax(&w.ctl->ncolours, col + 1u);
+            done |= 1u << k;
+            progress = true;
         }
-        SYNC_OR_RETURN();
-        GRID_FOR(m, ms) {
-            uint8_t stt = w.s.sm_state[m];
-            if (stt == 2) continue;
-            uint2 pr = w.cur.pair[w.s.sm_list[m]];
-            b.jp_best[c.body[pr.x]] = 0ull;
-            b.jp_best[c.body[pr.y]] = 0ull;
-            if (stt == 1) w.s.sm_state[m] = 2;
-        }
-        if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->jp_remaining[(round + 1) & 1u] = 0;
-        SYNC_OR_RETURN();
-        if (((volatile uint32_t*)w.ctl->jp_remaining)[round & 1u] == 0) break;
-        if (round > 4096) {
-            if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_COLOURS);
-            return;
+        if (!progress) {
+            if (t0 == 0) t0 = global_ns();
+            if ((++spins & 63u) == 0u && (err_set(w.ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs)) {
+                atomicOr(&w.ctl->err, ERRF_TIMEOUT);
+                return;
+            }
         }
     }
-    // Bucket the manifolds by colour.
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int k = 0; k < kMaxColours; ++k) {
-            w.s.colour_start[k] = acc;
-            w.s.colour_cursor[k] = acc;
-            acc += w.s.colour_count[k];
-        }
-        w.s.colour_start[kMaxColours] = acc;
-    }
-    SYNC_OR_RETURN();
-    GRID_FOR(m, ms) {
-        uint32_t col = w.s.sm_colour[m];
-        uint32_t pos = atomicAdd(&w.s.colour_cursor[col], 1u);
-        w.s.sm_sorted[pos] = w.s.sm_list[m];
-    }
-    SYNC_OR_RETURN();
-    const uint32_t ncol = w.ctl->ncolours;
-    if (threadIdx.x <= kMaxColours) sh_scan[threadIdx.x] = w.s.colour_start[threadIdx.x];
-    __syncthreads();
-    stamp(w, p, 2);
+}
 
-    // ---- assembly -----------------------------------------------------------------------
+// ================================================================ assembly
+__global__ void k_assemble(World w, StepParams p) {
+    const uint32_t ms = w.ctl->nsolver;
+    const Bodies& b = w.b;
+    const Colliders& c = w.c;
     const float dt = p.dt;
-    GRID_FOR(s, ms) {
-        uint32_t q = w.s.sm_sorted[s];
+    GRID_FOR(m, ms) {
+        uint32_t q = w.s.sm_list[m];
         uint2 pr = w.cur.pair[q];
         uint32_t c1 = pr.x, c2 = pr.y;
         uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
         BodyView v1 = load_view(b, bb1), v2 = load_view(b, bb2);
-        bool d1 = bi_status(v1.info) == 2u, d2 = bi_status(v2.info) == 2u;
-        w.s.sm_b1[s] = d1 ? (int)bb1 : -1;
-        w.s.sm_b2[s] = d2 ? (int)bb2 : -1;
-        uint32_t nc = w.cur.ncont[q];
-        w.s.sm_nc[s] = nc;
+        int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+        // Colour rank and manifold count on each dynamic body.
+        uint32_t col = w.s.sm_colour[m];
+        unsigned long long below = (col == 0u) ? 0ull : ((1ull << col) - 1ull);
+        uint32_t rk = 0;
+        if (b1 >= 0) {
+            unsigned long long u = b.used[b1];
+            rk |= (uint32_t)__popcll(u & below) | ((uint32_t)__popcll(u) << 8);
+        }
+        if (b2 >= 0) {
+            unsigned long long u = b.used[b2];
+            rk |= ((uint32_t)__popcll(u & below) << 16) | ((uint32_t)__popcll(u) << 24);
+        }
+        w.s.sm_rk[m] = rk;
+        uint32_t nc = w.s.sm_nc[m];
         uint32_t ci1 = c.info[c1], ci2 = c.info[c2];
         float mu = combine(c.friction[c1], (ci1 >> 4) & 0xfu, c.friction[c2], (ci2 >> 4) & 0xfu);
         float e = combine(c.restitution[c1], (ci1 >> 8) & 0xfu, c.restitution[c2], (ci2 >> 8) & 0xfu);
         float m1 = c.margin[c1], m2 = c.margin[c2];
-        float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
+        float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
         for (uint32_t k = 0; k < nc; ++k) {
             uint32_t slot = q * kMaxContacts + k;
             float4 w1 = w.cur.w1[slot], w2 = w.cur.w2[slot], nn = w.cur.n[slot], imp = w.cur.imp[slot];
@@ -554,128 +569,197 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
             }
         }
     }
-    SYNC_OR_RETURN();
-    stamp(w, p, 3);
+}
 
-    // ---- warm start (sor_prox.rs:19-45), colour by colour -----------------------------------
-    for (uint32_t col = 0; col < ncol; ++col) {
-        uint32_t lo = sh_scan[col], hi = sh_scan[col + 1];
-        for (uint32_t s = lo + blockIdx.x * blockDim.x + threadIdx.x; s < hi; s += gridDim.x * blockDim.x) {
-            int b1 = w.s.sm_b1[s], b2 = w.s.sm_b2[s];
-            DV dv;
-            load_dv(b.dv, b1, dv.a);
-            load_dv(b.dv, b2, dv.b);
-            const float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
-            uint32_t nc = w.s.sm_nc[s];
-            for (uint32_t k = 0; k < 3 * nc; ++k) {
-                const float* r = rows + k * kRowFloats;
-                float imp = r[RF_IMP];
-                if (imp != 0.0f) axpy(r, dv, imp, b1 >= 0, b2 >= 0);
-            }
-            store_dv(b.dv, b1, dv.a);
-            store_dv(b.dv, b2, dv.b);
+// ================================================================ SOR-Prox
+// One velocity task: sweep 0 is the warm start (sor_prox.rs:19-45), odd sweeps
+// the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
+// normal rows (sor_prox.rs:181-230).
+__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int b1, int b2) {
+    const bool h1 = b1 >= 0, h2 = b2 >= 0;
+    DV dv;
+    load_dv(w.b.dv, b1, dv.a);
+    load_dv(w.b.dv, b2, dv.b);
+    float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
+    const uint32_t nc = w.s.sm_nc[m];
+    if (sweep == 0) {
+        for (uint32_t k = 0; k < 3 * nc; ++k) {
+            float r[kRowFloats];
+            load_row(rows + k * kRowFloats, r);
+            float imp = r[RF_IMP];
+            if (imp != 0.0f) axpy(r, dv, imp, h1, h2);
         }
-        SYNC_OR_RETURN();
-    }
-    if (!eval_residual(w, ms, sh, true)) return;
-
-    // ---- SOR-Prox iterations ---------------------------------------------------------------
-    uint32_t maxit = p.solve_to_tolerance ? p.max_iterations_to_tolerance : p.max_velocity_iterations;
-    uint32_t iters = 0;
-    for (uint32_t it = 0; it < maxit; ++it) {
-        if (p.solve_to_tolerance && ((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
-        // Friction rows (bilateral, ImpulseLimits::Dependent), sor_prox.rs:232-343.
-        for (uint32_t col = 0; col < ncol; ++col) {
-            uint32_t lo = sh_scan[col], hi = sh_scan[col + 1];
-            for (uint32_t s = lo + blockIdx.x * blockDim.x + threadIdx.x; s < hi; s += gridDim.x * blockDim.x) {
-                int b1 = w.s.sm_b1[s], b2 = w.s.sm_b2[s];
-                bool h1 = b1 >= 0, h2 = b2 >= 0;
-                DV dv;
-                load_dv(b.dv, b1, dv.a);
-                load_dv(b.dv, b2, dv.b);
-                float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
-                uint32_t nc = w.s.sm_nc[s];
-                for (uint32_t k = 0; k < nc; ++k) {
-                    float li = rows[(3 * k) * kRowFloats + RF_IMP];
-                    float rr[2][kRowFloats];
-                    load_row(rows + (3 * k + 1) * kRowFloats, rr[0]);
-                    load_row(rows + (3 * k + 2) * kRowFloats, rr[1]);
+    } else if (sweep & 1u) {
+        for (uint32_t k = 0; k < nc; ++k) {
+            float li = rows[(3 * k) * kRowFloats + RF_IMP];
+            float rr[2][kRowFloats];
+            load_row(rows + (3 * k + 1) * kRowFloats, rr[0]);
+            load_row(rows + (3 * k + 2) * kRowFloats, rr[1]);
 #pragma unroll
-                    for (int sdir = 0; sdir < 2; ++sdir) {
-                        const float* r = rr[sdir];
-                        float* rg = rows + (3 * k + 1 + sdir) * kRowFloats;
-                        float imp = r[RF_IMP];
-                        if (li == 0.0f) {
-                            if (imp != 0.0f) {
-                                axpy(r, dv, -imp, h1, h2);
-                                rg[RF_IMP] = 0.0f;
-                            }
-                            continue;
-                        }
-                        float mx = r[RF_MU] * li, mn = -mx;
-                        float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
-                        float ni = imp - r[RF_R] * dimp;
-                        if (ni < mn) ni = mn;
-                        else if (ni > mx) ni = mx;
-                        float dl = ni - imp;
-                        rg[RF_IMP] = ni;
-                        axpy(r, dv, dl, h1, h2);
+            for (int sdir = 0; sdir < 2; ++sdir) {
+                const float* r = rr[sdir];
+                float* rg = rows + (3 * k + 1 + sdir) * kRowFloats;
+                float imp = r[RF_IMP];
+                if (li == 0.0f) {
+                    if (imp != 0.0f) {
+                        axpy(r, dv, -imp, h1, h2);
+                        rg[RF_IMP] = 0.0f;
                     }
+                    continue;
                 }
-                store_dv(b.dv, b1, dv.a);
-                store_dv(b.dv, b2, dv.b);
+                float mx = r[RF_MU] * li, mn = -mx;
+                float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
+                float ni = imp - r[RF_R] * dimp;
+                if (ni < mn) ni = mn;
+                else if (ni > mx) ni = mx;
+                float dl = ni - imp;
+                rg[RF_IMP] = ni;
+                axpy(r, dv, dl, h1, h2);
             }
-            SYNC_OR_RETURN();
         }
-        // Normal rows (unilateral), sor_prox.rs:181-230.
-        for (uint32_t col = 0; col < ncol; ++col) {
-            uint32_t lo = sh_scan[col], hi = sh_scan[col + 1];
-            for (uint32_t s = lo + blockIdx.x * blockDim.x + threadIdx.x; s < hi; s += gridDim.x * blockDim.x) {
-                int b1 = w.s.sm_b1[s], b2 = w.s.sm_b2[s];
-                bool h1 = b1 >= 0, h2 = b2 >= 0;
-                DV dv;
-                load_dv(b.dv, b1, dv.a);
-                load_dv(b.dv, b2, dv.b);
-                float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
-                uint32_t nc = w.s.sm_nc[s];
-                for (uint32_t k = 0; k < nc; ++k) {
-                    float r[kRowFloats];
-                    float* rg = rows + (3 * k) * kRowFloats;
-                    load_row(rg, r);
-                    float imp = r[RF_IMP];
-                    float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
-                    float ni = imp - r[RF_R] * dimp;
-                    ni = ni > 0.0f ? ni : 0.0f;
-                    float dl = ni - imp;
-                    rg[RF_IMP] = ni;
-                    axpy(r, dv, dl, h1, h2);
-                }
-                store_dv(b.dv, b1, dv.a);
-                store_dv(b.dv, b2, dv.b);
-            }
-            SYNC_OR_RETURN();
+    } else {
+        for (uint32_t k = 0; k < nc; ++k) {
+            float r[kRowFloats];
+            float* rg = rows + (3 * k) * kRowFloats;
+            load_row(rg, r);
+            float imp = r[RF_IMP];
+            float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
+            float ni = imp - r[RF_R] * dimp;
+            ni = ni > 0.0f ? ni : 0.0f;
+            float dl = ni - imp;
+            rg[RF_IMP] = ni;
+            axpy(r, dv, dl, h1, h2);
         }
-        ++iters;
-        if (p.solve_to_tolerance)
-            if (!eval_residual(w, ms, sh, false)) return;
     }
-    if (!p.solve_to_tolerance)
-        if (!eval_residual(w, ms, sh, false)) return;
-    if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->iterations = iters;
-    stamp(w, p, 4);
+    store_dv(w.b.dv, b1, dv.a);
+    store_dv(w.b.dv, b2, dv.b);
+}
 
-    // ---- cache impulses + integrate ------------------------------------------------------
-    GRID_FOR(s, ms) {
-        uint32_t q = w.s.sm_sorted[s];
-        const float* rows = w.s.rows + (size_t)s * 12 * kRowFloats;
-        uint32_t nc = w.s.sm_nc[s];
+// Runs sweeps [s_begin, s_end) of this thread's manifolds as their bodies'
+// versions allow. Returns false on timeout.
+__device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms) {
+    const uint32_t T = gridDim.x * blockDim.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    const uint32_t nmine = t < ms ? (ms - t + T - 1) / T : 0u;
+    uint16_t next[kMaxPerThread];
+    for (uint32_t k = 0; k < nmine; ++k) next[k] = (uint16_t)s_begin;
+    uint32_t left = nmine * (s_end - s_begin);
+    unsigned long long t0 = 0;
+    unsigned spins = 0;
+    while (left > 0) {
+        bool progress = false;
+        for (uint32_t k = 0; k < nmine; ++k) {
+            uint32_t sw = next[k];
+            if (sw >= s_end) continue;
+            uint32_t m = t + k * T;
+            int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+            uint32_t rk = w.s.sm_rk[m];
+            uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
+            uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
+            if (b1 >= 0 && ld_acquire(w.b.vel_ver + b1) != t1) continue;
+            if (b2 >= 0 && ld_acquire(w.b.vel_ver + b2) != t2) continue;
+            velocity_task(w, m, sw, b1, b2);
+            if (b1 >= 0) st_release(w.b.vel_ver + b1, t1 + 1u);
+            if (b2 >= 0) st_release(w.b.vel_ver + b2, t2 + 1u);
+            next[k] = (uint16_t)(sw + 1u);
+            --left;
+            progress = true;
+        }
+        if (!progress) {
+            if (t0 == 0) t0 = global_ns();
+            if ((++spins & 63u) == 0u && (err_set(w.ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs)) {
+                atomicOr(&w.ctl->err, ERRF_TIMEOUT);
+                return false;
+            }
+        } else {
+            t0 = 0;
+        }
+    }
+    return true;
+}
+
+// FP64 residual over all rows; the result lands in ctl->residual.
+__device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t& epoch, bool initial) {
+    double s2 = 0.0, l2 = 0.0;
+    GRID_FOR(m, ms) {
+        int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+        uint32_t nc = w.s.sm_nc[m];
+        DV dv;
+        load_dv(w.b.dv, b1, dv.a);
+        load_dv(w.b.dv, b2, dv.b);
+        const float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
+        for (uint32_t k = 0; k < nc; ++k) {
+            const float* rn = rows + (3 * k) * kRowFloats;
+            residual_row(rn, dv, b1 >= 0, b2 >= 0, false, 0.0, s2, l2);
+            residual_row(rn + kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
+            residual_row(rn + 2 * kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
+        }
+    }
+    double ts = block_sum(s2, sh);
+    double tl = block_sum(l2, sh);
+    if (threadIdx.x == 0) {
+        atomicAdd(&w.ctl->res_acc[0], ts);
+        atomicAdd(&w.ctl->res_acc[1], tl);
+    }
+    if (!grid_sync(w.ctl, epoch)) return false;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        double a = w.ctl->res_acc[0], bsum = w.ctl->res_acc[1];
+        double r = sqrt(a) / fmax(1.0, sqrt(bsum));
+        w.ctl->residual = r;
+        if (initial) w.ctl->residual_initial = r;
+        w.ctl->res_acc[0] = 0.0;
+        w.ctl->res_acc[1] = 0.0;
+    }
+    return grid_sync(w.ctl, epoch);
+}
+
+__global__ void __launch_bounds__(kCoopThreads) k_velocity(World w, StepParams p) {
+    __shared__ double sh[32];
+    const uint32_t ms = w.ctl->nsolver;
+    const uint32_t T = gridDim.x * blockDim.x;
+    if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        return;
+    }
+    uint32_t epoch = 0;
+    if (!velocity_sweeps(w, 0, 1, ms)) return;
+    if (!grid_sync(w.ctl, epoch)) return;
+    if (!eval_residual(w, ms, sh, epoch, true)) return;
+    uint32_t iters = 0;
+    if (!p.solve_to_tolerance) {
+        iters = p.max_velocity_iterations;
+        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms)) return;
+        if (!grid_sync(w.ctl, epoch)) return;
+        if (!eval_residual(w, ms, sh, epoch, false)) return;
+    } else {
+        for (uint32_t it = 0; it < p.max_iterations_to_tolerance; ++it) {
+            if (((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
+            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms)) return;
+            ++iters;
+            if (!grid_sync(w.ctl, epoch)) return;
+            if (!eval_residual(w, ms, sh, epoch, false)) return;
+        }
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->iterations = iters;
+}
+
+// ================================================================ integrate
+__global__ void k_cache_integrate(World w, StepParams p) {
+    const uint32_t ms = w.ctl->nsolver;
+    const Bodies& b = w.b;
+    GRID_FOR(m, ms) {
+        uint32_t q = w.s.sm_list[m];
+        const float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
+        uint32_t nc = w.s.sm_nc[m];
         for (uint32_t k = 0; k < nc; ++k) {
             float4 imp = make_float4(rows[(3 * k) * kRowFloats + RF_IMP], rows[(3 * k + 1) * kRowFloats + RF_IMP],
                                      rows[(3 * k + 2) * kRowFloats + RF_IMP], 0.0f);
             w.cur.imp[q * kMaxContacts + k] = imp;
         }
     }
-    GRID_FOR(i, nb) {
+    const float dt = p.dt;
+    GRID_FOR(i, w.nb_slots) {
+        b.pos_ver[i] = 0;
         uint32_t info = b.info[i];
         if (!(info & BI_ISLAND)) continue;
         np::V el = np::mul(v3(b.acc_lin[i]), dt), ea = np::mul(v3(b.acc_ang[i]), dt);
@@ -687,105 +771,147 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
         b.info[i] = info | BI_CHANGED;
         body_integrate(b, i, dt);
     }
-    SYNC_OR_RETURN();
-    stamp(w, p, 5);
+}
 
-    // ---- NonlinearSORProx, colour by colour -------------------------------------------------
-    for (uint32_t it = 0; it < p.max_position_iterations; ++it) {
-        for (uint32_t col = 0; col < ncol; ++col) {
-            uint32_t lo = sh_scan[col], hi = sh_scan[col + 1];
-            for (uint32_t s = lo + blockIdx.x * blockDim.x + threadIdx.x; s < hi; s += gridDim.x * blockDim.x) {
-                uint32_t q = w.s.sm_sorted[s];
-                uint2 pr = w.cur.pair[q];
-                uint32_t c1 = pr.x, c2 = pr.y;
-                uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
-                uint32_t i1 = b.info[bb1], i2 = b.info[bb2];
-                bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
-                // Poses of both bodies (static and kinematic ones are read only).
-                np::V t1 = v3(b.pos_t[bb1]), t2 = v3(b.pos_t[bb2]);
-                np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
-                np::V com1 = v3(b.com[bb1]), com2 = v3(b.com[bb2]);
-                np::V lc1 = v3(b.local_com[bb1]), lc2 = v3(b.local_com[bb2]);
-                float im1 = b.inv_mass[bb1], im2 = b.inv_mass[bb2];
-                np::M iI1 = load_m9(b.inv_I + 9 * bb1), iI2 = load_m9(b.inv_I + 9 * bb2);
-                np::Iso wrt1{v3(c.wrt_t[c1]), q4(c.wrt_q[c1])}, wrt2{v3(c.wrt_t[c2]), q4(c.wrt_q[c2])};
-                uint32_t sh1 = c.info[c1] & 0xfu, sh2 = c.info[c2] & 0xfu;
-                float4 pp1 = c.params[c1], pp2 = c.params[c2];
-                np::V hh1 = v3(pp1), hh2 = v3(pp2);
-                float dil1 = (sh1 == SHAPE_BALL ? pp1.x : 0.0f) + c.margin[c1];
-                float dil2 = (sh2 == SHAPE_BALL ? pp2.x : 0.0f) + c.margin[c2];
-                uint32_t nc = w.cur.ncont[q];
-                bool moved1 = false, moved2 = false;
-                for (uint32_t k = 0; k < nc; ++k) {
-                    uint32_t slot = q * kMaxContacts + k;
-                    uint32_t key = w.cur.key[slot];
-                    int f1 = (int)(key / 26u), f2 = (int)(key % 26u);
-                    np::Iso m1 = np::iso_mul(np::Iso{t1, q1}, wrt1);
-                    np::Iso m2 = np::iso_mul(np::Iso{t2, q2}, wrt2);
-                    np::V n0 = np::qrot(m1.q, v3(w.cur.nl[slot]));
-                    Geom g = kinematic_contact(feature_of(sh1, hh1, f1), m1, dil1, feature_of(sh2, hh2, f2), m2, dil2, n0);
-                    // NonlinearSORProx::clamp_rhs.
-                    float rhs = (-g.depth + p.allowed_linear_error) * p.erp;
-                    float lim = -p.max_linear_correction;
-                    rhs = (rhs < lim) ? lim : rhs;
-                    if (rhs >= 0.0f) continue;
-                    float inv_r = 0.0f, dummy = 0.0f;
-                    float J1[6], J2[6], W1[6], W2[6];
-                    if (d1) {
-                        BodyView v;
-                        v.com = com1; v.inv_mass = im1; v.inv_I = iI1; v.info = i1;
-                        v.lin = v.ang = v.acc_lin = v.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
-                        fill_row_side(v, g.w1, np::neg(g.n), J1, W1, inv_r, dummy, false, dt);
-                    }
-                    if (d2) {
-                        BodyView v;
-                        v.com = com2; v.inv_mass = im2; v.inv_I = iI2; v.info = i2;
-                        v.lin = v.ang = v.acc_lin = v.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
-                        fill_row_side(v, g.w2, g.n, J2, W2, inv_r, dummy, false, dt);
-                    }
-                    if (inv_r == 0.0f) continue;
-                    float r = 1.0f / inv_r;
-                    float impulse = -rhs * r;
-                    if (d1) {
-                        for (int kk = 0; kk < 6; ++kk) W1[kk] = W1[kk] * impulse;
-                        apply_displacement(t1, q1, com1, lc1, np::mk(W1[0], W1[1], W1[2]), np::mk(W1[3], W1[4], W1[5]));
-                        moved1 = true;
-                    }
-                    if (d2) {
-                        for (int kk = 0; kk < 6; ++kk) W2[kk] = W2[kk] * impulse;
-                        apply_displacement(t2, q2, com2, lc2, np::mk(W2[0], W2[1], W2[2]), np::mk(W2[3], W2[4], W2[5]));
-                        moved2 = true;
-                    }
-                }
-                if (moved1) {
-                    b.pos_t[bb1] = f4(t1);
-                    b.pos_q[bb1] = f4q(q1);
-                    b.com[bb1] = f4(com1);
-                    b.info[bb1] = b.info[bb1] | BI_CHANGED;
-                }
-                if (moved2) {
-                    b.pos_t[bb2] = f4(t2);
-                    b.pos_q[bb2] = f4q(q2);
-                    b.com[bb2] = f4(com2);
-                    b.info[bb2] = b.info[bb2] | BI_CHANGED;
-                }
-            }
-            SYNC_OR_RETURN();
+// ================================================================ NonlinearSORProx
+__device__ __forceinline__ void position_task(const World& w, const StepParams& p, uint32_t m) {
+    const Bodies& b = w.b;
+    const Colliders& c = w.c;
+    uint32_t q = w.s.sm_list[m];
+    uint2 pr = w.cur.pair[q];
+    uint32_t c1 = pr.x, c2 = pr.y;
+    uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
+    uint32_t i1 = b.info[bb1], i2 = b.info[bb2];
+    bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
+    np::V t1 = v3(b.pos_t[bb1]), t2 = v3(b.pos_t[bb2]);
+    np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
+    np::V com1 = v3(b.com[bb1]), com2 = v3(b.com[bb2]);
+    np::V lc1 = v3(b.local_com[bb1]), lc2 = v3(b.local_com[bb2]);
+    float im1 = b.inv_mass[bb1], im2 = b.inv_mass[bb2];
+    np::M iI1 = load_m9(b.inv_I + 9 * bb1), iI2 = load_m9(b.inv_I + 9 * bb2);
+    np::Iso wrt1{v3(c.wrt_t[c1]), q4(c.wrt_q[c1])}, wrt2{v3(c.wrt_t[c2]), q4(c.wrt_q[c2])};
+    uint32_t sh1 = c.info[c1] & 0xfu, sh2 = c.info[c2] & 0xfu;
+    float4 pp1 = c.params[c1], pp2 = c.params[c2];
+    np::V hh1 = v3(pp1), hh2 = v3(pp2);
+    float dil1 = (sh1 == SHAPE_BALL ? pp1.x : 0.0f) + c.margin[c1];
+    float dil2 = (sh2 == SHAPE_BALL ? pp2.x : 0.0f) + c.margin[c2];
+    uint32_t nc = w.cur.ncont[q];
+    bool moved1 = false, moved2 = false;
+    for (uint32_t k = 0; k < nc; ++k) {
+        uint32_t slot = q * kMaxContacts + k;
+        uint32_t key = w.cur.key[slot];
+        int f1 = (int)(key / 26u), f2 = (int)(key % 26u);
+        np::Iso m1 = np::iso_mul(np::Iso{t1, q1}, wrt1);
+        np::Iso m2 = np::iso_mul(np::Iso{t2, q2}, wrt2);
+        np::V n0 = np::qrot(m1.q, v3(w.cur.nl[slot]));
+        Geom g = kinematic_contact(feature_of(sh1, hh1, f1), m1, dil1, feature_of(sh2, hh2, f2), m2, dil2, n0);
+        // NonlinearSORProx::clamp_rhs.
+        float rhs = (-g.depth + p.allowed_linear_error) * p.erp;
+        float lim = -p.max_linear_correction;
+        rhs = (rhs < lim) ? lim : rhs;
+        if (rhs >= 0.0f) continue;
+        float inv_r = 0.0f, dummy = 0.0f;
+        float J1[6], J2[6], W1[6], W2[6];
+        if (d1) {
+            BodyView v;
+            v.com = com1; v.inv_mass = im1; v.inv_I = iI1; v.info = i1;
+            v.lin = v.ang = v.acc_lin = v.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
+            fill_row_side(v, g.w1, np::neg(g.n), J1, W1, inv_r, dummy, false, p.dt);
+        }
+        if (d2) {
+            BodyView v;
+            v.com = com2; v.inv_mass = im2; v.inv_I = iI2; v.info = i2;
+            v.lin = v.ang = v.acc_lin = v.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
+            fill_row_side(v, g.w2, g.n, J2, W2, inv_r, dummy, false, p.dt);
+        }
+        if (inv_r == 0.0f) continue;
+        float r = 1.0f / inv_r;
+        float impulse = -rhs * r;
+        if (d1) {
+            for (int kk = 0; kk < 6; ++kk) W1[kk] = W1[kk] * impulse;
+            apply_displacement(t1, q1, com1, lc1, np::mk(W1[0], W1[1], W1[2]), np::mk(W1[3], W1[4], W1[5]));
+            moved1 = true;
+        }
+        if (d2) {
+            for (int kk = 0; kk < 6; ++kk) W2[kk] = W2[kk] * impulse;
+            apply_displacement(t2, q2, com2, lc2, np::mk(W2[0], W2[1], W2[2]), np::mk(W2[3], W2[4], W2[5]));
+            moved2 = true;
         }
     }
-    stamp(w, p, 6);
+    if (moved1) {
+        b.pos_t[bb1] = f4(t1);
+        b.pos_q[bb1] = f4q(q1);
+        b.com[bb1] = f4(com1);
+        b.info[bb1] = i1 | BI_CHANGED;
+    }
+    if (moved2) {
+        b.pos_t[bb2] = f4(t2);
+        b.pos_q[bb2] = f4q(q2);
+        b.com[bb2] = f4(com2);
+        b.info[bb2] = i2 | BI_CHANGED;
+    }
+}
 
-    // ---- kinematic integration, update_dynamics, clear_forces, audit ------------------------
+__global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p) {
+    const uint32_t ms = w.ctl->nsolver;
+    const uint32_t T = gridDim.x * blockDim.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
+        if (t == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        return;
+    }
+    const uint32_t nmine = t < ms ? (ms - t + T - 1) / T : 0u;
+    const uint32_t nsw = p.max_position_iterations;
+    uint16_t next[kMaxPerThread];
+    for (uint32_t k = 0; k < nmine; ++k) next[k] = 0;
+    uint32_t left = nmine * nsw;
+    unsigned long long t0 = 0;
+    unsigned spins = 0;
+    while (left > 0) {
+        bool progress = false;
+        for (uint32_t k = 0; k < nmine; ++k) {
+            uint32_t sw = next[k];
+            if (sw >= nsw) continue;
+            uint32_t m = t + k * T;
+            int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+            uint32_t rk = w.s.sm_rk[m];
+            uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
+            uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
+            if (b1 >= 0 && ld_acquire(w.b.pos_ver + b1) != t1) continue;
+            if (b2 >= 0 && ld_acquire(w.b.pos_ver + b2) != t2) continue;
+            position_task(w, p, m);
+            if (b1 >= 0) st_release(w.b.pos_ver + b1, t1 + 1u);
+            if (b2 >= 0) st_release(w.b.pos_ver + b2, t2 + 1u);
+            next[k] = (uint16_t)(sw + 1u);
+            --left;
+            progress = true;
+        }
+        if (!progress) {
+            if (t0 == 0) t0 = global_ns();
+            if ((++spins & 63u) == 0u && (err_set(w.ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs)) {
+                atomicOr(&w.ctl->err, ERRF_TIMEOUT);
+                return;
+            }
+        } else {
+            t0 = 0;
+        }
+    }
+}
+
+// ================================================================ post
+__global__ void k_post(World w, StepParams p) {
+    __shared__ double sh[32];
+    const Bodies& b = w.b;
     double ke = 0.0;
-    GRID_FOR(i, nb) {
+    GRID_FOR(i, w.nb_slots) {
         uint32_t info = b.info[i];
         if (!(info & BI_ALIVE)) continue;
         uint32_t st = bi_status(info);
         if (st == 3u) {
-            body_integrate(b, i, dt);
+            body_integrate(b, i, p.dt);
             info = b.info[i];
         }
-        if ((info & BI_CHANGED) && st == 2u) body_update_dynamics(b, i, dt);
+        if ((info & BI_CHANGED) && st == 2u) body_update_dynamics(b, i, p.dt);
         b.f_lin[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         b.f_ang[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         b.info[i] = b.info[i] & ~BI_CHANGED;
@@ -804,25 +930,71 @@ __global__ void __launch_bounds__(kSolveThreads) k_solve(World w, StepParams p) 
         }
     }
     double tke = block_sum(ke, sh);
-    if (threadIdx.x == 0) atomicAdd(&w.ctl->kinetic_energy, tke);
-    stamp(w, p, 7);
+    if (threadIdx.x == 0 && tke != 0.0) atomicAdd(&w.ctl->kinetic_energy, tke);
 }
 
-int solve_grid_size(int device) {
-    int sms = 0, per_sm = 0;
+// ================================================================ launchers
+static unsigned item_blocks(uint32_t n) {
+    unsigned b = (n + kItemThreads - 1) / kItemThreads;
+    if (b < 1) b = 1;
+    if (b > 152u * 16u) b = 152u * 16u;
+    return b;
+}
+
+void solver_grid_sizes(int device, SolverLaunch& L) {
+    int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_solve, kSolveThreads, 0);
-    if (per_sm < 1) per_sm = 1;
-    return sms * per_sm;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_colour, kCoopThreads, 0);
+    L.grid_colour = sms * (per < 1 ? 1 : per);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_velocity, kCoopThreads, 0);
+    L.grid_velocity = sms * (per < 1 ? 1 : per);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_position, kCoopThreads, 0);
+    L.grid_position = sms * (per < 1 ? 1 : per);
 }
 
-cudaError_t launch_solve(const World& w, const StepParams& p, int grid, cudaStream_t st) {
-    cudaError_t e = cudaMemsetAsync(&w.ctl->barrier_count, 0, 2 * sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
+static cudaError_t coop(const void* fn, int grid, void** args, cudaStream_t st) {
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kCoopThreads), args, 0, st);
+}
+
+cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st) {
     World wc = w;
     StepParams pc = p;
-    void* args[] = {&wc, &pc};
-    return cudaLaunchCooperativeKernel((const void*)k_solve, dim3(grid), dim3(kSolveThreads), args, 0, st);
+    void* args1[] = {&wc};
+    void* args2[] = {&wc, &pc};
+    const unsigned nbb = item_blocks(w.nb_slots), npb = item_blocks(w.cap_pairs);
+    auto rec = [&](int k) {
+        if (L.ev) cudaEventRecord(L.ev[k], st);
+    };
+    rec(0);
+    k_act_init<<<nbb, kItemThreads, 0, st>>>(wc, pc);
+    k_act_union<<<npb, kItemThreads, 0, st>>>(wc);
+    k_act_root<<<nbb, kItemThreads, 0, st>>>(wc);
+    k_act_apply<<<nbb, kItemThreads, 0, st>>>(wc);
+    rec(1);
+    k_collect<<<npb, kItemThreads, 0, st>>>(wc);
+    size_t scan_bytes = L.scan_bytes;
+    cudaError_t e = cub::DeviceScan::ExclusiveSum(L.scan_temp, scan_bytes, w.b.adj_count, w.b.adj_start,
+                                                  (int)(w.nb_slots ? w.nb_slots : 1), st);
+    if (e != cudaSuccess) return e;
+    k_adj_fill<<<npb, kItemThreads, 0, st>>>(wc);
+    k_prank<<<npb, kItemThreads, 0, st>>>(wc);
+    e = coop((const void*)k_colour, L.grid_colour, args1, st);
+    if (e != cudaSuccess) return e;
+    rec(2);
+    k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc);
+    rec(3);
+    e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
+    if (e != cudaSuccess) return e;
+    e = coop((const void*)k_velocity, L.grid_velocity, args2, st);
+    if (e != cudaSuccess) return e;
+    rec(4);
+    k_cache_integrate<<<nbb > npb ? nbb : npb, kItemThreads, 0, st>>>(wc, pc);
+    rec(5);
+    e = coop((const void*)k_position, L.grid_position, args2, st);
+    if (e != cudaSuccess) return e;
+    rec(6);
+    k_post<<<nbb, kItemThreads, 0, st>>>(wc, pc);
+    return cudaGetLastError();
 }
 
 }  // namespace npgpu_dev

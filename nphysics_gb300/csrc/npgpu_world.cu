@@ -130,6 +130,8 @@ struct npgpu_world {
     std::string last_error;
     npgpu_counters counters;
     cudaEvent_t ev[8];
+    cudaEvent_t ev_solver[7];
+    SolverLaunch solver;
     bool ev_recorded = false;
     bool cd_start_ran = false;
 };
@@ -252,7 +254,8 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(b.acc_lin, B); A(b.acc_ang, B); A(b.f_lin, B); A(b.f_ang, B);
     A(b.lin_damp, B); A(b.ang_damp, B); A(b.max_lin, B); A(b.max_ang, B); A(b.sleep_thr, B); A(b.energy, B);
     A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
-    A(b.jp_best, B); A(b.jp_used, B);
+    A(b.used, B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B); A(b.col_cnt, B); A(b.vel_ver, B);
+    A(b.pos_ver, B);
     Colliders& c = w->dw.c;
     A(c.body, Cn); A(c.info, Cn); A(c.params, Cn); A(c.wrt_t, Cn); A(c.wrt_q, Cn);
     A(c.margin, Cn); A(c.lin_pred, Cn); A(c.friction, Cn); A(c.restitution, Cn); A(c.rank, Cn);
@@ -266,9 +269,8 @@ static npgpu_status create_buffers(npgpu_world* w) {
         A(pp->imp, 4 * (size_t)P); A(pp->nl, 4 * (size_t)P);
     }
     Solver& s = w->dw.s;
-    A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_state, P); A(s.sm_sorted, P); A(s.sm_b1, P); A(s.sm_b2, P);
-    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats);
-    A(s.colour_count, kMaxColours); A(s.colour_start, kMaxColours + 1); A(s.colour_cursor, kMaxColours);
+    A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_prank, P); A(s.sm_rk, P); A(s.sm_b1, P); A(s.sm_b2, P);
+    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats); A(s.adj, 2 * (size_t)P);
     A(w->ctl, 1);
     A(w->d_forget, Cn);
 #undef A
@@ -277,7 +279,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     w->dw.prev = w->pb;
     w->dw.cap_pairs = P;
     w->sort_bytes = sort_temp_bytes(Cn);
-    w->scan_bytes = scan_temp_bytes(Cn);
+    w->scan_bytes = std::max(scan_temp_bytes(Cn), scan_temp_bytes(B));
     CK(cudaMalloc(&w->sort_temp, std::max<size_t>(w->sort_bytes, 16)), "sort temp");
     o.push_back(w->sort_temp);
     CK(cudaMalloc(&w->scan_temp, std::max<size_t>(w->scan_bytes, 16)), "scan temp");
@@ -330,12 +332,16 @@ npgpu_world* npgpu_create(const npgpu_params* params, const float gravity[3], ui
         cudaEventCreateWithFlags(&w->ev_stage, cudaEventDisableTiming);
         cudaEventRecord(w->ev_stage, w->stream);
         for (auto& e : w->ev) cudaEventCreate(&e);
+        for (auto& e : w->ev_solver) cudaEventCreate(&e);
         st = create_buffers(w);
         if (st != NPGPU_OK) {
             g_create_error = w->last_error;
             break;
         }
-        w->solve_grid = solve_grid_size(w->device);
+        solver_grid_sizes(w->device, w->solver);
+        w->solver.scan_temp = w->scan_temp;
+        w->solver.scan_bytes = w->scan_bytes;
+        w->solver.ev = nullptr;
     } while (0);
     if (status) *status = st;
     if (st != NPGPU_OK && w) {
@@ -353,6 +359,8 @@ void npgpu_destroy(npgpu_world* w) {
     if (w->h_stage) cudaFreeHost(w->h_stage);
     if (w->ev_stage) cudaEventDestroy(w->ev_stage);
     for (auto& e : w->ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : w->ev_solver)
         if (e) cudaEventDestroy(e);
     if (w->stream) cudaStreamDestroy(w->stream);
     delete w;
@@ -714,7 +722,8 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
             w->cd_dirty = false;
         }
         if (prof) CK(cudaEventRecord(w->ev[1], w->stream), "event");
-        CK(launch_solve(w->dw, sp, w->solve_grid, w->stream), "solve");
+        w->solver.ev = prof ? w->ev_solver : nullptr;
+        CK(launch_solver(w->dw, sp, w->solver, w->stream), "solve");
         if (prof) CK(cudaEventRecord(w->ev[2], w->stream), "event");
         st = run_cd(w, sp);
         if (st != NPGPU_OK) return st;
@@ -949,7 +958,11 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
         k.broad_phase_time = ms;
         cudaEventElapsedTime(&ms, w->ev[5], w->ev[3]);
         k.narrow_phase_time = ms;
-        auto d = [&](int a, int b) { return (double)(c.t_phase[b] - c.t_phase[a]) * 1e-6; };
+        auto d = [&](int a, int b) {
+            float t = 0.0f;
+            cudaEventElapsedTime(&t, w->ev_solver[a], w->ev_solver[b]);
+            return (double)t;
+        };
         k.island_construction_time = d(0, 1);
         k.colouring_time = d(1, 2);
         k.assembly_time = d(2, 3);

@@ -62,7 +62,10 @@ struct Bodies {
     float *dv;                       // mj_lambda, 6 per body
     uint32_t *uf_parent;
     int *can_deact;
-    unsigned long long *jp_best, *jp_used;
+    unsigned long long *used;        // colours of the body's solver manifolds (one bit each)
+    uint32_t *adj_count, *adj_start, *adj_fill;   // solver manifolds per body (CSR)
+    uint32_t *col_cnt;               // manifolds of the body coloured so far
+    uint32_t *vel_ver, *pos_ver;     // velocity / position updates applied to the body this step
 };
 
 struct Colliders {
@@ -96,14 +99,14 @@ struct Pairs {
 };
 
 struct Solver {
-    uint32_t *sm_list;               // solver manifolds (pair indices), unordered
-    uint32_t *sm_colour;             // colour per sm_list entry
-    uint8_t *sm_state;
-    uint32_t *sm_sorted;             // pair indices sorted by colour
+    uint32_t *sm_list;               // solver manifolds (pair indices), in no particular order
+    uint32_t *sm_colour;             // colour of each solver manifold
+    uint32_t *sm_prank;              // priority rank among the manifolds of body 1 | body 2 << 16
+    uint32_t *sm_rk;                 // colour rank / manifold count on body 1 and body 2 (8 bits each)
     int *sm_b1, *sm_b2;              // dynamic body slots (-1 when the side has no dofs)
     uint32_t *sm_nc;
-    float *rows;                     // 12 rows per sorted manifold
-    uint32_t *colour_count, *colour_start, *colour_cursor;
+    float *rows;                     // 12 rows per solver manifold
+    uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
 };
 
 // Device counters and control words (one struct in device memory).
@@ -112,8 +115,8 @@ struct Control {
     uint32_t nsolver;                // solver manifolds
     uint32_t ncolours;
     uint32_t err;
-    uint32_t barrier_count;
-    uint32_t barrier_gen;
+    uint32_t barrier_count;          // monotonic grid-barrier arrivals of the running cooperative kernel
+    uint32_t pad1;
     uint32_t jp_remaining[2];
     uint32_t ncontacts;
     uint32_t nmanifolds;
@@ -156,8 +159,17 @@ cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t s
 cudaError_t launch_lbvh(const World& w, cudaStream_t st);
 cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);
 cudaError_t launch_narrow(const World& w, cudaStream_t st);
-cudaError_t launch_solve(const World& w, const StepParams& p, int grid, cudaStream_t st);
-int solve_grid_size(int device);
+// The solver half of a step (activation, colouring, assembly, SOR-Prox,
+// integration, position correction, post-step updates). ev[0..6], when
+// non-null, receive the phase boundaries for profiling.
+struct SolverLaunch {
+    int grid_colour, grid_velocity, grid_position;   // co-resident blocks of the cooperative kernels
+    void* scan_temp;
+    size_t scan_bytes;
+    cudaEvent_t* ev;
+};
+cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st);
+void solver_grid_sizes(int device, SolverLaunch& L);
 size_t sort_temp_bytes(uint32_t n_items);
 size_t scan_temp_bytes(uint32_t n_items);
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);
