@@ -88,6 +88,20 @@ __device__ __forceinline__ bool grid_sync(Control* ctl, uint32_t& epoch) {
     return s_ok != 0;
 }
 
+// Backs off while waiting: 32 ns doubling up to 1 us, so that waiting threads
+// do not crowd the L2 that the running ones need. Returns false on timeout.
+__device__ __forceinline__ bool wait_backoff(const Control* ctl, unsigned long long& t0, unsigned& backoff) {
+    if (t0 == 0) t0 = global_ns();
+    __nanosleep(backoff);
+    backoff = backoff < 1024u ? backoff * 2u : 1024u;
+    if (err_set(ctl, ERRF_TIMEOUT)) return false;
+    if (global_ns() - t0 > kWaitLimitNs) {
+        atomicOr((uint32_t*)&ctl->err, ERRF_TIMEOUT);
+        return false;
+    }
+    return true;
+}
+
 #define GRID_FOR(i, n) for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < (n); i += gridDim.x * blockDim.x)
 
 __device__ __forceinline__ uint32_t pair_hash22(uint32_t c1, uint32_t c2) {
@@ -467,15 +481,23 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     }
     const Bodies& b = w.b;
     uint32_t done = 0, todo = (nmine >= 32u) ? 0xffffffffu : ((1u << nmine) - 1u);
+    int mb1[kMaxPerThread], mb2[kMaxPerThread];
+    uint32_t mpr[kMaxPerThread];
+    for (uint32_t k = 0; k < nmine; ++k) {
+        uint32_t m = t + k * T;
+        mb1[k] = w.s.sm_b1[m];
+        mb2[k] = w.s.sm_b2[m];
+        mpr[k] = w.s.sm_prank[m];
+    }
     unsigned long long t0 = 0;
-    unsigned spins = 0;
+    unsigned backoff = 32;
     while (done != todo) {
         bool progress = false;
         for (uint32_t k = 0; k < nmine; ++k) {
             if (done & (1u << k)) continue;
             uint32_t m = t + k * T;
-            int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
-            uint32_t pr = w.s.sm_prank[m];
+            int b1 = mb1[k], b2 = mb2[k];
+            uint32_t pr = mpr[k];
             uint32_t r1 = pr & 0xffffu, r2 = pr >> 16;
             if (b1 >= 0 && ld_acquire(b.col_cnt + b1) != r1) continue;
             if (b2 >= 0 && ld_acquire(b.col_cnt + b2) != r2) continue;
@@ -502,12 +524,11 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             done |= 1u << k;
             progress = true;
         }
-        if (!progress) {
-            if (t0 == 0) t0 = global_ns();
-            if ((++spins & 63u) == 0u && (err_set(w.ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs)) {
-                atomicOr(&w.ctl->err, ERRF_TIMEOUT);
-                return;
-            }
+        if (progress) {
+            t0 = 0;
+            backoff = 32;
+        } else if (!wait_backoff(w.ctl, t0, backoff)) {
+            return;
         }
     }
 }
@@ -635,44 +656,61 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     store_dv(w.b.dv, b2, dv.b);
 }
 
+// The dataflow tasks of one thread: its manifolds m = t + k T, with their
+// dynamic bodies and colour ranks read once.
+struct MyTasks {
+    uint32_t n;
+    int b1[kMaxPerThread], b2[kMaxPerThread];
+    uint32_t rk[kMaxPerThread];
+    uint16_t next[kMaxPerThread];
+};
+
+__device__ __forceinline__ void load_tasks(const World& w, uint32_t ms, MyTasks& mt, uint32_t s_begin) {
+    const uint32_t T = gridDim.x * blockDim.x;
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    mt.n = t < ms ? (ms - t + T - 1) / T : 0u;
+    for (uint32_t k = 0; k < mt.n; ++k) {
+        uint32_t m = t + k * T;
+        mt.b1[k] = w.s.sm_b1[m];
+        mt.b2[k] = w.s.sm_b2[m];
+        mt.rk[k] = w.s.sm_rk[m];
+        mt.next[k] = (uint16_t)s_begin;
+    }
+}
+
 // Runs sweeps [s_begin, s_end) of this thread's manifolds as their bodies'
 // versions allow. Returns false on timeout.
 __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms) {
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    const uint32_t nmine = t < ms ? (ms - t + T - 1) / T : 0u;
-    uint16_t next[kMaxPerThread];
-    for (uint32_t k = 0; k < nmine; ++k) next[k] = (uint16_t)s_begin;
-    uint32_t left = nmine * (s_end - s_begin);
+    MyTasks mt;
+    load_tasks(w, ms, mt, s_begin);
+    uint32_t left = mt.n * (s_end - s_begin);
     unsigned long long t0 = 0;
-    unsigned spins = 0;
+    unsigned backoff = 32;
     while (left > 0) {
         bool progress = false;
-        for (uint32_t k = 0; k < nmine; ++k) {
-            uint32_t sw = next[k];
+        for (uint32_t k = 0; k < mt.n; ++k) {
+            uint32_t sw = mt.next[k];
             if (sw >= s_end) continue;
-            uint32_t m = t + k * T;
-            int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
-            uint32_t rk = w.s.sm_rk[m];
+            int b1 = mt.b1[k], b2 = mt.b2[k];
+            uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
             if (b1 >= 0 && ld_acquire(w.b.vel_ver + b1) != t1) continue;
             if (b2 >= 0 && ld_acquire(w.b.vel_ver + b2) != t2) continue;
-            velocity_task(w, m, sw, b1, b2);
+            velocity_task(w, t + k * T, sw, b1, b2);
             if (b1 >= 0) st_release(w.b.vel_ver + b1, t1 + 1u);
             if (b2 >= 0) st_release(w.b.vel_ver + b2, t2 + 1u);
-            next[k] = (uint16_t)(sw + 1u);
+            mt.next[k] = (uint16_t)(sw + 1u);
             --left;
             progress = true;
         }
-        if (!progress) {
-            if (t0 == 0) t0 = global_ns();
-            if ((++spins & 63u) == 0u && (err_set(w.ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs)) {
-                atomicOr(&w.ctl->err, ERRF_TIMEOUT);
-                return false;
-            }
-        } else {
+        if (progress) {
             t0 = 0;
+            backoff = 32;
+        } else if (!wait_backoff(w.ctl, t0, backoff)) {
+            return false;
         }
     }
     return true;
@@ -860,40 +898,35 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
         if (t == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
         return;
     }
-    const uint32_t nmine = t < ms ? (ms - t + T - 1) / T : 0u;
     const uint32_t nsw = p.max_position_iterations;
-    uint16_t next[kMaxPerThread];
-    for (uint32_t k = 0; k < nmine; ++k) next[k] = 0;
-    uint32_t left = nmine * nsw;
+    MyTasks mt;
+    load_tasks(w, ms, mt, 0);
+    uint32_t left = mt.n * nsw;
     unsigned long long t0 = 0;
-    unsigned spins = 0;
+    unsigned backoff = 32;
     while (left > 0) {
         bool progress = false;
-        for (uint32_t k = 0; k < nmine; ++k) {
-            uint32_t sw = next[k];
+        for (uint32_t k = 0; k < mt.n; ++k) {
+            uint32_t sw = mt.next[k];
             if (sw >= nsw) continue;
-            uint32_t m = t + k * T;
-            int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
-            uint32_t rk = w.s.sm_rk[m];
+            int b1 = mt.b1[k], b2 = mt.b2[k];
+            uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
             if (b1 >= 0 && ld_acquire(w.b.pos_ver + b1) != t1) continue;
             if (b2 >= 0 && ld_acquire(w.b.pos_ver + b2) != t2) continue;
-            position_task(w, p, m);
+            position_task(w, p, t + k * T);
             if (b1 >= 0) st_release(w.b.pos_ver + b1, t1 + 1u);
             if (b2 >= 0) st_release(w.b.pos_ver + b2, t2 + 1u);
-            next[k] = (uint16_t)(sw + 1u);
+            mt.next[k] = (uint16_t)(sw + 1u);
             --left;
             progress = true;
         }
-        if (!progress) {
-            if (t0 == 0) t0 = global_ns();
-            if ((++spins & 63u) == 0u && (err_set(w.ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs)) {
-                atomicOr(&w.ctl->err, ERRF_TIMEOUT);
-                return;
-            }
-        } else {
+        if (progress) {
             t0 = 0;
+            backoff = 32;
+        } else if (!wait_backoff(w.ctl, t0, backoff)) {
+            return;
         }
     }
 }
