@@ -196,6 +196,11 @@ typedef struct npgpu_counters {
     double residual_initial;         /* ... after the warm start, before iteration 1 */
     double max_penetration;          /* FP64 audit: max(depth + margins) over contacts */
     double kinetic_energy;           /* FP64 audit: sum 1/2 (m v.v + w.I w) */
+    /* Profile only (params.profile): velocity-solver task statistics. */
+    double velocity_task_ms;         /* summed execution time of all velocity tasks */
+    double velocity_wait_ms;         /* summed time threads spent waiting for their bodies */
+    double velocity_kernel_ms;       /* duration of the velocity kernel on the device clock */
+    uint64_t velocity_tasks;         /* tasks executed */
 } npgpu_counters;
 
 /* Contact record returned for parity checks (a TrackedContact,

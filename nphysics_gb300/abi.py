@@ -142,6 +142,10 @@ class Counters(C.Structure):
         ("residual_initial", C.c_double),
         ("max_penetration", C.c_double),
         ("kinetic_energy", C.c_double),
+        ("velocity_task_ms", C.c_double),
+        ("velocity_wait_ms", C.c_double),
+        ("velocity_kernel_ms", C.c_double),
+        ("velocity_tasks", C.c_uint64),
     ]
 
     def as_dict(self):

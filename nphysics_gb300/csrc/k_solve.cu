@@ -356,6 +356,9 @@ __global__ void k_act_init(World w, StepParams p) {
         c->residual = 0.0;
         c->residual_initial = 0.0;
         c->kinetic_energy = 0.0;
+        c->task_ns = 0ull;
+        c->wait_ns = 0ull;
+        c->tasks = 0ull;
     }
 }
 
@@ -680,13 +683,18 @@ __device__ __forceinline__ void load_tasks(const World& w, uint32_t ms, MyTasks&
 
 // Runs sweeps [s_begin, s_end) of this thread's manifolds as their bodies'
 // versions allow. Returns false on timeout.
-__device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms) {
+struct TaskStats {
+    unsigned long long exec_ns, wait_ns, tasks;
+};
+
+__device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
+                                TaskStats& ts) {
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     MyTasks mt;
     load_tasks(w, ms, mt, s_begin);
     uint32_t left = mt.n * (s_end - s_begin);
-    unsigned long long t0 = 0;
+    unsigned long long t0 = 0, tw = prof ? global_ns() : 0ull;
     unsigned backoff = 32;
     while (left > 0) {
         bool progress = false;
@@ -699,9 +707,16 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
             if (b1 >= 0 && ld_acquire(w.b.vel_ver + b1) != t1) continue;
             if (b2 >= 0 && ld_acquire(w.b.vel_ver + b2) != t2) continue;
+            unsigned long long te = prof ? global_ns() : 0ull;
+            if (prof) ts.wait_ns += te - tw;
             velocity_task(w, t + k * T, sw, b1, b2);
             if (b1 >= 0) st_release(w.b.vel_ver + b1, t1 + 1u);
             if (b2 >= 0) st_release(w.b.vel_ver + b2, t2 + 1u);
+            if (prof) {
+                tw = global_ns();
+                ts.exec_ns += tw - te;
+                ts.tasks += 1;
+            }
             mt.next[k] = (uint16_t)(sw + 1u);
             --left;
             progress = true;
@@ -759,26 +774,38 @@ __global__ void __launch_bounds__(kCoopThreads) k_velocity(World w, StepParams p
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
         return;
     }
+    const bool prof = p.profile != 0;
+    TaskStats ts{0ull, 0ull, 0ull};
+    unsigned long long k0 = 0;
+    if (prof && blockIdx.x == 0 && threadIdx.x == 0) k0 = global_ns();
     uint32_t epoch = 0;
-    if (!velocity_sweeps(w, 0, 1, ms)) return;
+    if (!velocity_sweeps(w, 0, 1, ms, prof, ts)) return;
     if (!grid_sync(w.ctl, epoch)) return;
     if (!eval_residual(w, ms, sh, epoch, true)) return;
     uint32_t iters = 0;
     if (!p.solve_to_tolerance) {
         iters = p.max_velocity_iterations;
-        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms)) return;
+        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms, prof, ts)) return;
         if (!grid_sync(w.ctl, epoch)) return;
         if (!eval_residual(w, ms, sh, epoch, false)) return;
     } else {
         for (uint32_t it = 0; it < p.max_iterations_to_tolerance; ++it) {
             if (((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
-            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms)) return;
+            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms, prof, ts)) return;
             ++iters;
             if (!grid_sync(w.ctl, epoch)) return;
             if (!eval_residual(w, ms, sh, epoch, false)) return;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->iterations = iters;
+    if (prof) {
+        if (ts.tasks) {
+            atomicAdd(&w.ctl->task_ns, ts.exec_ns);
+            atomicAdd(&w.ctl->wait_ns, ts.wait_ns);
+            atomicAdd(&w.ctl->tasks, ts.tasks);
+        }
+        if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->t_phase[0] = global_ns() - k0;
+    }
 }
 
 // ================================================================ integrate

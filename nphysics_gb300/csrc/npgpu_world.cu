@@ -969,6 +969,10 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
         k.velocity_resolution_time = d(3, 4);
         k.velocity_update_time = d(4, 5);
         k.position_resolution_time = d(5, 6);
+        k.velocity_task_ms = (double)c.task_ns * 1e-6;
+        k.velocity_wait_ms = (double)c.wait_ns * 1e-6;
+        k.velocity_kernel_ms = (double)c.t_phase[0] * 1e-6;
+        k.velocity_tasks = c.tasks;
     }
     *out = k;
     return NPGPU_OK;

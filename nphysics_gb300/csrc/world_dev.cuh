@@ -129,6 +129,7 @@ struct Control {
     double kinetic_energy;
     unsigned long long max_pen_bits; // order-preserving bits of the max penetration
     unsigned long long t_phase[16];  // %globaltimer stamps
+    unsigned long long task_ns, wait_ns, tasks;   // velocity-task statistics (profile mode)
 };
 
 struct StepParams {
