@@ -55,6 +55,15 @@ __device__ __forceinline__ void st_release(uint32_t* p, uint32_t v) {
 __device__ __forceinline__ void red_release_add(uint32_t* p, uint32_t v) {
     asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
+__device__ __forceinline__ uint32_t ld_relaxed(const uint32_t* p) {
+    uint32_t v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
+    asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+__device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
 __device__ __forceinline__ bool err_set(const Control* ctl, uint32_t bits) {
     return (ld_acquire(&ctl->err) & bits) != 0;
 }
@@ -88,15 +97,16 @@ __device__ __forceinline__ bool grid_sync(Control* ctl, uint32_t& epoch) {
     return s_ok != 0;
 }
 
-// Backs off while waiting: 32 ns doubling up to 1 us, so that waiting threads
-// do not crowd the L2 that the running ones need. Returns false on timeout.
-__device__ __forceinline__ bool wait_backoff(const Control* ctl, unsigned long long& t0, unsigned& backoff) {
+// Backs off while a whole warp waits: 32 ns doubling up to 1 us, so that
+// waiting warps do not crowd the L2 that the running ones need. Called by all
+// 32 lanes together; the decision is warp-uniform. Returns false on timeout.
+__device__ __forceinline__ bool warp_wait_backoff(const Control* ctl, unsigned long long& t0, unsigned& backoff) {
     if (t0 == 0) t0 = global_ns();
     __nanosleep(backoff);
     backoff = backoff < 1024u ? backoff * 2u : 1024u;
-    if (err_set(ctl, ERRF_TIMEOUT)) return false;
-    if (global_ns() - t0 > kWaitLimitNs) {
-        atomicOr((uint32_t*)&ctl->err, ERRF_TIMEOUT);
+    bool give_up = err_set(ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs;
+    if (__any_sync(0xffffffffu, give_up)) {
+        if ((threadIdx.x & 31u) == 0u) atomicOr((uint32_t*)&ctl->err, ERRF_TIMEOUT);
         return false;
     }
     return true;
@@ -494,7 +504,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     }
     unsigned long long t0 = 0;
     unsigned backoff = 32;
-    while (done != todo) {
+    while (__any_sync(0xffffffffu, done != todo)) {
         bool progress = false;
         for (uint32_t k = 0; k < nmine; ++k) {
             if (done & (1u << k)) continue;
@@ -502,8 +512,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             int b1 = mb1[k], b2 = mb2[k];
             uint32_t pr = mpr[k];
             uint32_t r1 = pr & 0xffffu, r2 = pr >> 16;
-            if (b1 >= 0 && ld_acquire(b.col_cnt + b1) != r1) continue;
-            if (b2 >= 0 && ld_acquire(b.col_cnt + b2) != r2) continue;
+            if (b1 >= 0 && ld_relaxed(b.col_cnt + b1) != r1) continue;
+            if (b2 >= 0 && ld_relaxed(b.col_cnt + b2) != r2) continue;
+            fence_acq_rel();
             unsigned long long mask = 0ull;
             if (b1 >= 0) mask |= b.used[b1];
             if (b2 >= 0) mask |= b.used[b2];
@@ -515,22 +526,19 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
                 col = (uint32_t)(__ffsll((long long)~mask) - 1);
             }
             w.s.sm_colour[m] = col;
-            if (b1 >= 0) {
-                b.used[b1] = b.used[b1] | (1ull << col);
-                st_release(b.col_cnt + b1, r1 + 1u);
-            }
-            if (b2 >= 0) {
-                b.used[b2] = b.used[b2] | (1ull << col);
-                st_release(b.col_cnt + b2, r2 + 1u);
-            }
+            if (b1 >= 0) b.used[b1] = b.used[b1] | (1ull << col);
+            if (b2 >= 0) b.used[b2] = b.used[b2] | (1ull << col);
+            fence_acq_rel();
+            if (b1 >= 0) st_relaxed(b.col_cnt + b1, r1 + 1u);
+            if (b2 >= 0) st_relaxed(b.col_cnt + b2, r2 + 1u);
             atomicMax(&w.ctl->ncolours, col + 1u);
             done |= 1u << k;
             progress = true;
         }
-        if (progress) {
+        if (__any_sync(0xffffffffu, progress)) {
             t0 = 0;
             backoff = 32;
-        } else if (!wait_backoff(w.ctl, t0, backoff)) {
+        } else if (!warp_wait_backoff(w.ctl, t0, backoff)) {
             return;
         }
     }
@@ -696,7 +704,9 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
     uint32_t left = mt.n * (s_end - s_begin);
     unsigned long long t0 = 0, tw = prof ? global_ns() : 0ull;
     unsigned backoff = 32;
-    while (left > 0) {
+    // Warp-uniform loop: each pass, the lanes whose next task is ready run it
+    // together; the warp sleeps only when no lane could run anything.
+    while (__any_sync(0xffffffffu, left > 0)) {
         bool progress = false;
         for (uint32_t k = 0; k < mt.n; ++k) {
             uint32_t sw = mt.next[k];
@@ -705,13 +715,15 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
-            if (b1 >= 0 && ld_acquire(w.b.vel_ver + b1) != t1) continue;
-            if (b2 >= 0 && ld_acquire(w.b.vel_ver + b2) != t2) continue;
+            if (b1 >= 0 && ld_relaxed(w.b.vel_ver + b1) != t1) continue;
+            if (b2 >= 0 && ld_relaxed(w.b.vel_ver + b2) != t2) continue;
+            fence_acq_rel();   // acquire: the bodies' latest dv is visible
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
             velocity_task(w, t + k * T, sw, b1, b2);
-            if (b1 >= 0) st_release(w.b.vel_ver + b1, t1 + 1u);
-            if (b2 >= 0) st_release(w.b.vel_ver + b2, t2 + 1u);
+            fence_acq_rel();   // release: dv and impulses before the new versions
+            if (b1 >= 0) st_relaxed(w.b.vel_ver + b1, t1 + 1u);
+            if (b2 >= 0) st_relaxed(w.b.vel_ver + b2, t2 + 1u);
             if (prof) {
                 tw = global_ns();
                 ts.exec_ns += tw - te;
@@ -721,10 +733,10 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             --left;
             progress = true;
         }
-        if (progress) {
+        if (__any_sync(0xffffffffu, progress)) {
             t0 = 0;
             backoff = 32;
-        } else if (!wait_backoff(w.ctl, t0, backoff)) {
+        } else if (!warp_wait_backoff(w.ctl, t0, backoff)) {
             return false;
         }
     }
@@ -931,7 +943,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
     uint32_t left = mt.n * nsw;
     unsigned long long t0 = 0;
     unsigned backoff = 32;
-    while (left > 0) {
+    while (__any_sync(0xffffffffu, left > 0)) {
         bool progress = false;
         for (uint32_t k = 0; k < mt.n; ++k) {
             uint32_t sw = mt.next[k];
@@ -940,19 +952,21 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
             uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
-            if (b1 >= 0 && ld_acquire(w.b.pos_ver + b1) != t1) continue;
-            if (b2 >= 0 && ld_acquire(w.b.pos_ver + b2) != t2) continue;
+            if (b1 >= 0 && ld_relaxed(w.b.pos_ver + b1) != t1) continue;
+            if (b2 >= 0 && ld_relaxed(w.b.pos_ver + b2) != t2) continue;
+            fence_acq_rel();
             position_task(w, p, t + k * T);
-            if (b1 >= 0) st_release(w.b.pos_ver + b1, t1 + 1u);
-            if (b2 >= 0) st_release(w.b.pos_ver + b2, t2 + 1u);
+            fence_acq_rel();
+            if (b1 >= 0) st_relaxed(w.b.pos_ver + b1, t1 + 1u);
+            if (b2 >= 0) st_relaxed(w.b.pos_ver + b2, t2 + 1u);
             mt.next[k] = (uint16_t)(sw + 1u);
             --left;
             progress = true;
         }
-        if (progress) {
+        if (__any_sync(0xffffffffu, progress)) {
             t0 = 0;
             backoff = 32;
-        } else if (!wait_backoff(w.ctl, t0, backoff)) {
+        } else if (!warp_wait_backoff(w.ctl, t0, backoff)) {
             return;
         }
     }
