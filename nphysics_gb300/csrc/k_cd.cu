@@ -189,17 +189,33 @@ __device__ __forceinline__ bool overlap(float4 amin, float4 amax, float4 bmin, f
 }
 
 // Traverses the tree with leaf k's fat AABB. WRITE = false counts the pairs
-// leaf k owns; WRITE = true stores them at its offset.
+// leaf k owns and keeps up to kLeafCap partners in leaf_tmp; WRITE = true
+// stores the pairs at the leaf's offset, from leaf_tmp when they fit there,
+// by traversing again otherwise.
 template <bool WRITE>
 __global__ void k_bp_traverse(World w, int n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
     if (k >= n) return;
     const Colliders& c = w.c;
     uint32_t a = c.vals_sorted[k];
+    uint32_t count = 0, base = 0;
+    if (WRITE) {
+        base = c.leaf_offset[k];
+        uint32_t kept = c.leaf_count[k];
+        if (kept <= (uint32_t)kLeafCap) {
+            for (uint32_t i = 0; i < kept; ++i) {
+                uint32_t b = c.leaf_tmp[(size_t)k * kLeafCap + i];
+                uint32_t slot = base + i;
+                if (slot < w.cap_pairs) w.cur.pair[slot] = make_uint2(a < b ? a : b, a < b ? b : a);
+            }
+            uint32_t stored = base >= w.cap_pairs ? 0u : (kept < w.cap_pairs - base ? kept : w.cap_pairs - base);
+            w.cur.owner_start[a] = base;
+            w.cur.owner_count[a] = stored;
+            return;
+        }
+    }
     float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
     float ra = c.rank[a];
-    uint32_t count = 0, base = 0;
-    if (WRITE) base = c.leaf_offset[k];
     if (n >= 2) {
         int stack[64];
         int sp = 0;
@@ -216,6 +232,8 @@ __global__ void k_bp_traverse(World w, int n) {
                     if (WRITE) {
                         uint32_t slot = base + count;
                         if (slot < w.cap_pairs) w.cur.pair[slot] = make_uint2(a < b ? a : b, a < b ? b : a);
+                    } else if (count < (uint32_t)kLeafCap) {
+                        c.leaf_tmp[(size_t)k * kLeafCap + count] = b;
                     }
                     ++count;
                 }

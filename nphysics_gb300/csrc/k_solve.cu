@@ -372,14 +372,29 @@ __global__ void k_act_init(World w, StepParams p) {
     }
 }
 
+// A body is sleepy when it may sleep and its energy is below its threshold
+// (the per-body condition of activation_manager.rs:172-175).
+__device__ __forceinline__ bool body_sleepy(const Bodies& b, uint32_t i, uint32_t info) {
+    return body_can_sleep(info) && b.energy[i] < b.sleep_thr[i];
+}
+
+// Islands: an island sleeps only if every body in it is sleepy, so only the
+// contact edges with a sleepy end matter (a path from a sleepy body to the
+// nearest non-sleepy one uses only such edges); edges between two non-sleepy
+// bodies are skipped. The resulting sleep decisions equal the union-find over
+// all edges (activation_manager.rs:148-200).
 __global__ void k_act_union(World w) {
     const uint32_t npairs = w.ctl->npairs;
+    const Bodies& b = w.b;
     GRID_FOR(q, npairs) {
         if (w.cur.ncont[q] == 0) continue;
         uint2 pr = w.cur.pair[q];
         uint32_t b1 = w.c.body[pr.x], b2 = w.c.body[pr.y];
-        uint32_t s1 = bi_status(w.b.info[b1]), s2 = bi_status(w.b.info[b2]);
-        if ((s1 == 2u || s1 == 3u) && (s2 == 2u || s2 == 3u)) uf_union(w.b.uf_parent, b1, b2, &w.ctl->err);
+        uint32_t i1 = b.info[b1], i2 = b.info[b2];
+        uint32_t s1 = bi_status(i1), s2 = bi_status(i2);
+        if (!((s1 == 2u || s1 == 3u) && (s2 == 2u || s2 == 3u))) continue;
+        if (!body_sleepy(b, b1, i1) && !body_sleepy(b, b2, i2)) continue;
+        uf_union(b.uf_parent, b1, b2, &w.ctl->err);
     }
 }
 
@@ -389,9 +404,7 @@ __global__ void k_act_root(World w) {
         uint32_t info = b.info[i];
         uint32_t st = bi_status(info);
         if (!(info & BI_ALIVE) || !(st == 2u || st == 3u)) continue;
-        uint32_t r = uf_find(b.uf_parent, i);
-        bool ok = body_can_sleep(info) && b.energy[i] < b.sleep_thr[i];
-        if (!ok) atomicAnd(&b.can_deact[r], 0);
+        if (!body_sleepy(b, i, info)) atomicAnd(&b.can_deact[uf_find(b.uf_parent, i)], 0);
     }
 }
 

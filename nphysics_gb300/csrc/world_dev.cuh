@@ -41,6 +41,7 @@ enum : uint32_t {
 constexpr int kMaxContacts = 4;      // contacts per manifold
 constexpr int kRowFloats = 28;       // J1[6] J2[6] WJ1[6] WJ2[6] r rhs impulse mu
 constexpr int kMaxColours = 64;
+constexpr int kLeafCap = 16;         // partners a broad-phase leaf keeps between its two passes
 
 // Row field offsets.
 enum { RF_J1 = 0, RF_J2 = 6, RF_WJ1 = 12, RF_WJ2 = 18, RF_R = 24, RF_RHS = 25, RF_IMP = 26, RF_MU = 27 };
@@ -83,6 +84,7 @@ struct Colliders {
     float4 *node_min, *node_max;
     int *node_flag;
     uint32_t *leaf_count, *leaf_offset;
+    uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
 };
 enum : uint32_t { CI_ALIVE = 1u << 16 };
 
