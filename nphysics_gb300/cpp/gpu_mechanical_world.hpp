@@ -1,0 +1,573 @@
+// gpu_mechanical_world.hpp -- C++ host mirror of nphysics3d's world API over
+// the GPU step (include/npgpu.h).
+//
+// A drop-in for code written against DefaultMechanicalWorld
+// (src/world/mechanical_world.rs:24, 182-396): the same set types, handle
+// semantics and `step(gworld, bodies, colliders, joints, forces)` call, with
+// the step running on the GPU. Sets are generational arenas
+// (generational_arena::Index, src/object/body_set.rs:178) whose slot indices
+// are the device slots. Insertions, removals and user edits are forwarded to
+// the device on the next step (the reference's `maintain`,
+// mechanical_world.rs:114-179); after the step the bodies' poses and
+// velocities are copied back into the set.
+//
+// Header-only; link against libnpgpu.so. Errors throw nphysics_gpu::Error
+// carrying the npgpu_status (the reference panics or silently skips).
+#pragma once
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <optional>
+#include <stdexcept>
+#include <string>
+#include <utility>
+#include <variant>
+#include <vector>
+
+#include "../../include/npgpu.h"
+
+namespace nphysics_gpu {
+
+struct Error : std::runtime_error {
+    npgpu_status status;
+    Error(npgpu_status s, const std::string& m) : std::runtime_error(m), status(s) {}
+};
+
+struct Vector3 {
+    float x = 0.0f, y = 0.0f, z = 0.0f;
+};
+
+// Isometry3: translation + unit quaternion (i, j, k, w).
+struct Isometry3 {
+    Vector3 translation;
+    float rotation[4] = {0.0f, 0.0f, 0.0f, 1.0f};
+    static Isometry3 identity() { return Isometry3(); }
+    static Isometry3 from_translation(float x, float y, float z) {
+        Isometry3 r;
+        r.translation = {x, y, z};
+        return r;
+    }
+    // UnitQuaternion::from_scaled_axis.
+    static Isometry3 new_(Vector3 t, Vector3 axisangle) {
+        Isometry3 r;
+        r.translation = t;
+        double n = std::sqrt(double(axisangle.x) * axisangle.x + double(axisangle.y) * axisangle.y +
+                             double(axisangle.z) * axisangle.z);
+        if (n > 0.0) {
+            double s = std::sin(0.5 * n) / n;
+            r.rotation[0] = float(axisangle.x * s);
+            r.rotation[1] = float(axisangle.y * s);
+            r.rotation[2] = float(axisangle.z * s);
+            r.rotation[3] = float(std::cos(0.5 * n));
+        }
+        return r;
+    }
+};
+
+struct Velocity3 {
+    Vector3 linear, angular;
+};
+
+enum class BodyStatus : uint32_t {
+    Disabled = NPGPU_BODY_DISABLED,
+    Static = NPGPU_BODY_STATIC,
+    Dynamic = NPGPU_BODY_DYNAMIC,
+    Kinematic = NPGPU_BODY_KINEMATIC
+};
+
+// generational_arena::Index.
+struct Index {
+    uint64_t index = 0, generation = 0;
+    bool operator==(const Index& o) const { return index == o.index && generation == o.generation; }
+    npgpu_handle raw() const { return npgpu_handle{index, generation}; }
+};
+using DefaultBodyHandle = Index;
+using DefaultColliderHandle = Index;
+struct BodyPartHandle {
+    DefaultBodyHandle body;
+    size_t part = 0;
+};
+
+// Arena with generation bumps on removal and LIFO slot reuse (generational_arena 0.2).
+template <class T> class Arena {
+public:
+    Index insert(T value) {
+        Index h;
+        if (!free_.empty()) {
+            h.index = free_.back();
+            free_.pop_back();
+            slots_[h.index].emplace(std::move(value));
+        } else {
+            h.index = slots_.size();
+            slots_.emplace_back(std::move(value));
+            gens_.push_back(0);
+        }
+        h.generation = generation_;
+        gens_[h.index] = generation_;
+        return h;
+    }
+    std::optional<T> remove(Index h) {
+        if (!contains(h)) return std::nullopt;
+        std::optional<T> out = std::move(slots_[h.index]);
+        slots_[h.index].reset();
+        free_.push_back(h.index);
+        ++generation_;
+        return out;
+    }
+    bool contains(Index h) const {
+        return h.index < slots_.size() && slots_[h.index].has_value() && gens_[h.index] == h.generation;
+    }
+    T* get(Index h) { return contains(h) ? &*slots_[h.index] : nullptr; }
+    const T* get(Index h) const { return contains(h) ? &*slots_[h.index] : nullptr; }
+    Index handle_at(size_t i) const { return Index{i, gens_[i]}; }
+    bool occupied(size_t i) const { return i < slots_.size() && slots_[i].has_value(); }
+    size_t capacity_used() const { return slots_.size(); }
+
+private:
+    std::vector<std::optional<T>> slots_;
+    std::vector<uint64_t> gens_;
+    std::vector<uint64_t> free_;
+    uint64_t generation_ = 0;
+};
+
+// A rigid body as built by RigidBodyDesc::build (src/object/rigid_body.rs:1064-1084).
+class RigidBody {
+public:
+    npgpu_body_desc desc;
+
+    RigidBody() {
+        std::memset(&desc, 0, sizeof(desc));
+        desc.position[6] = 1.0f;
+        desc.max_linear_velocity = std::numeric_limits<float>::max();
+        desc.max_angular_velocity = std::numeric_limits<float>::max();
+        desc.sleep_threshold = 0.01f;
+        desc.status = NPGPU_BODY_DYNAMIC;
+        desc.kind = NPGPU_KIND_RIGID_BODY;
+        desc.flags = NPGPU_BODY_GRAVITY | NPGPU_BODY_CAN_SLEEP;
+    }
+    Isometry3 position() const {
+        Isometry3 r;
+        r.translation = {desc.position[0], desc.position[1], desc.position[2]};
+        for (int k = 0; k < 4; ++k) r.rotation[k] = desc.position[3 + k];
+        return r;
+    }
+    Velocity3 velocity() const {
+        return Velocity3{{desc.velocity[0], desc.velocity[1], desc.velocity[2]},
+                         {desc.velocity[3], desc.velocity[4], desc.velocity[5]}};
+    }
+    BodyStatus status() const { return BodyStatus(desc.status); }
+    bool is_active() const { return active_; }
+    // Setters mark the body changed: it is re-uploaded (and woken) on the next step.
+    void set_position(const Isometry3& p) {
+        desc.position[0] = p.translation.x;
+        desc.position[1] = p.translation.y;
+        desc.position[2] = p.translation.z;
+        for (int k = 0; k < 4; ++k) desc.position[3 + k] = p.rotation[k];
+        dirty_ = true;
+    }
+    void set_velocity(const Velocity3& v) {
+        float a[6] = {v.linear.x, v.linear.y, v.linear.z, v.angular.x, v.angular.y, v.angular.z};
+        std::memcpy(desc.velocity, a, sizeof(a));
+        dirty_ = true;
+    }
+    void set_status(BodyStatus s) {
+        desc.status = uint32_t(s);
+        dirty_ = true;
+    }
+    // RigidBody::apply_force(0, force, ForceType::Force, auto_wake_up).
+    void apply_force(const Velocity3& f, bool auto_wake_up) {
+        float a[6] = {f.linear.x, f.linear.y, f.linear.z, f.angular.x, f.angular.y, f.angular.z};
+        for (int k = 0; k < 6; ++k) force_.v[k] += a[k];
+        force_.wake = force_.wake || auto_wake_up;
+        force_.any = true;
+    }
+
+    struct Force {
+        float v[6] = {0, 0, 0, 0, 0, 0};
+        bool wake = false, any = false;
+    };
+
+private:
+    friend class GpuMechanicalWorld;
+    Force force_;
+    bool dirty_ = true;
+    bool active_ = true;
+};
+
+// RigidBodyDesc builder (src/object/rigid_body.rs:949-1086).
+class RigidBodyDesc {
+public:
+    RigidBodyDesc& translation(Vector3 t) {
+        b_.desc.position[0] = t.x;
+        b_.desc.position[1] = t.y;
+        b_.desc.position[2] = t.z;
+        return *this;
+    }
+    RigidBodyDesc& rotation(Vector3 axisangle) {
+        Isometry3 r = Isometry3::new_({}, axisangle);
+        for (int k = 0; k < 4; ++k) b_.desc.position[3 + k] = r.rotation[k];
+        return *this;
+    }
+    RigidBodyDesc& position(const Isometry3& p) {
+        b_.set_position(p);
+        return *this;
+    }
+    RigidBodyDesc& velocity(const Velocity3& v) {
+        b_.set_velocity(v);
+        return *this;
+    }
+    RigidBodyDesc& status(BodyStatus s) {
+        b_.desc.status = uint32_t(s);
+        return *this;
+    }
+    RigidBodyDesc& mass(float m) {
+        b_.desc.local_inertia[0] = m;
+        return *this;
+    }
+    RigidBodyDesc& gravity_enabled(bool on) {
+        b_.desc.flags = on ? (b_.desc.flags | NPGPU_BODY_GRAVITY) : (b_.desc.flags & ~NPGPU_BODY_GRAVITY);
+        return *this;
+    }
+    RigidBodyDesc& linear_damping(float d) {
+        b_.desc.linear_damping = d;
+        return *this;
+    }
+    RigidBodyDesc& angular_damping(float d) {
+        b_.desc.angular_damping = d;
+        return *this;
+    }
+    RigidBodyDesc& max_linear_velocity(float v) {
+        b_.desc.max_linear_velocity = v;
+        return *this;
+    }
+    RigidBodyDesc& max_angular_velocity(float v) {
+        b_.desc.max_angular_velocity = v;
+        return *this;
+    }
+    // None disables sleeping.
+    RigidBodyDesc& sleep_threshold(std::optional<float> t) {
+        if (t) {
+            b_.desc.sleep_threshold = *t;
+            b_.desc.flags |= NPGPU_BODY_CAN_SLEEP;
+        } else {
+            b_.desc.flags &= ~NPGPU_BODY_CAN_SLEEP;
+        }
+        return *this;
+    }
+    RigidBodyDesc& kinematic_translations(bool x, bool y, bool z) {
+        set_flag(NPGPU_BODY_LOCK_TX, x);
+        set_flag(NPGPU_BODY_LOCK_TY, y);
+        set_flag(NPGPU_BODY_LOCK_TZ, z);
+        return *this;
+    }
+    RigidBodyDesc& kinematic_rotations(bool x, bool y, bool z) {
+        set_flag(NPGPU_BODY_LOCK_RX, x);
+        set_flag(NPGPU_BODY_LOCK_RY, y);
+        set_flag(NPGPU_BODY_LOCK_RZ, z);
+        return *this;
+    }
+    RigidBody build() const { return b_; }
+
+private:
+    void set_flag(uint32_t f, bool on) { b_.desc.flags = on ? (b_.desc.flags | f) : (b_.desc.flags & ~f); }
+    RigidBody b_;
+};
+
+// Ground::new() (src/object/ground.rs): a static body with no dofs.
+struct Ground {};
+
+// A body of a kind the GPU world rejects (multibody, FEM, mass-spring...): it
+// can sit in the set, and the step reports NPGPU_ERR_UNSUPPORTED_BODY.
+struct UnsupportedBody {
+    uint32_t kind;
+};
+
+using BodyVariant = std::variant<RigidBody, Ground, UnsupportedBody>;
+
+class DefaultBodySet {
+public:
+    DefaultBodyHandle insert(BodyVariant b) {
+        DefaultBodyHandle h = arena_.insert(std::move(b));
+        inserted_.push_back(h);
+        return h;
+    }
+    std::optional<BodyVariant> remove(DefaultBodyHandle h) {
+        auto r = arena_.remove(h);
+        if (r) removed_.push_back(h);
+        return r;
+    }
+    RigidBody* rigid_body(DefaultBodyHandle h) {
+        BodyVariant* v = arena_.get(h);
+        return v ? std::get_if<RigidBody>(v) : nullptr;
+    }
+    const RigidBody* rigid_body(DefaultBodyHandle h) const {
+        const BodyVariant* v = arena_.get(h);
+        return v ? std::get_if<RigidBody>(v) : nullptr;
+    }
+    bool contains(DefaultBodyHandle h) const { return arena_.contains(h); }
+
+private:
+    friend class GpuMechanicalWorld;
+    Arena<BodyVariant> arena_;
+    std::vector<DefaultBodyHandle> inserted_, removed_;
+};
+
+enum class Shape { Ball, Cuboid };
+
+struct BasicMaterial {
+    float restitution = 0.0f, friction = 0.5f;   // basic_material.rs:59-63
+    uint32_t restitution_combine = NPGPU_COMBINE_AVERAGE, friction_combine = NPGPU_COMBINE_AVERAGE;
+};
+
+class Collider {
+public:
+    npgpu_collider_desc desc;
+    DefaultBodyHandle body() const { return DefaultBodyHandle{desc.body.index, desc.body.generation}; }
+};
+
+// ColliderDesc builder (src/object/collider.rs:441-573).
+class ColliderDesc {
+public:
+    static ColliderDesc ball(float radius) { return ColliderDesc(NPGPU_SHAPE_BALL, radius, 0.0f, 0.0f); }
+    static ColliderDesc cuboid(Vector3 half) { return ColliderDesc(NPGPU_SHAPE_CUBOID, half.x, half.y, half.z); }
+    static ColliderDesc other_shape() { return ColliderDesc(NPGPU_SHAPE_OTHER, 0.0f, 0.0f, 0.0f); }
+    ColliderDesc& translation(Vector3 t) {
+        d_.position_wrt_body[0] = t.x;
+        d_.position_wrt_body[1] = t.y;
+        d_.position_wrt_body[2] = t.z;
+        return *this;
+    }
+    ColliderDesc& rotation(Vector3 axisangle) {
+        Isometry3 r = Isometry3::new_({}, axisangle);
+        for (int k = 0; k < 4; ++k) d_.position_wrt_body[3 + k] = r.rotation[k];
+        return *this;
+    }
+    ColliderDesc& density(float v) {
+        d_.density = v;
+        return *this;
+    }
+    ColliderDesc& margin(float v) {
+        d_.margin = v;
+        return *this;
+    }
+    ColliderDesc& linear_prediction(float v) {
+        d_.linear_prediction = v;
+        return *this;
+    }
+    ColliderDesc& material(const BasicMaterial& m) {
+        d_.friction = m.friction;
+        d_.restitution = m.restitution;
+        d_.friction_combine = m.friction_combine;
+        d_.restitution_combine = m.restitution_combine;
+        return *this;
+    }
+    ColliderDesc& sensor(bool s) {
+        d_.is_sensor = s;
+        return *this;
+    }
+    ColliderDesc& ccd_enabled(bool s) {
+        d_.ccd_enabled = s;
+        return *this;
+    }
+    Collider build(BodyPartHandle parent) const {
+        Collider c;
+        c.desc = d_;
+        c.desc.body = parent.body.raw();
+        return c;
+    }
+
+private:
+    ColliderDesc(uint32_t shape, float a, float b, float c) {
+        std::memset(&d_, 0, sizeof(d_));
+        d_.position_wrt_body[6] = 1.0f;
+        d_.shape = shape;
+        d_.shape_params[0] = a;
+        d_.shape_params[1] = b;
+        d_.shape_params[2] = c;
+        d_.margin = 0.01f;
+        d_.linear_prediction = 0.001f;
+        d_.angular_prediction = 3.14159265358979323846f / 180.0f * 5.0f;
+        d_.friction = 0.5f;
+    }
+    npgpu_collider_desc d_;
+};
+
+class DefaultColliderSet {
+public:
+    DefaultColliderHandle insert(Collider c) {
+        DefaultColliderHandle h = arena_.insert(std::move(c));
+        inserted_.push_back(h);
+        return h;
+    }
+    std::optional<Collider> remove(DefaultColliderHandle h) {
+        auto r = arena_.remove(h);
+        if (r) removed_.push_back(h);
+        return r;
+    }
+    const Collider* get(DefaultColliderHandle h) const { return arena_.get(h); }
+
+private:
+    friend class GpuMechanicalWorld;
+    Arena<Collider> arena_;
+    std::vector<DefaultColliderHandle> inserted_, removed_;
+};
+
+// The collision state lives on the device; this type exists for the signature.
+class DefaultGeometricalWorld {};
+
+// Joint constraints and force generators are not run on the GPU: a non-empty
+// set makes the step fail with NPGPU_ERR_NONEMPTY_JOINTS / _FORCES.
+class DefaultJointConstraintSet {
+public:
+    size_t len() const { return n_; }
+    void insert_placeholder() { ++n_; }
+
+private:
+    size_t n_ = 0;
+};
+class DefaultForceGeneratorSet {
+public:
+    size_t len() const { return n_; }
+    void insert_placeholder() { ++n_; }
+
+private:
+    size_t n_ = 0;
+};
+
+class GpuMechanicalWorld {
+public:
+    npgpu_params integration_parameters;
+    // Copy poses and velocities back into the body set after each step.
+    bool write_back = true;
+
+    explicit GpuMechanicalWorld(Vector3 gravity, uint32_t capacity_bodies = 1u << 16,
+                                uint32_t capacity_colliders = 1u << 16, uint32_t capacity_pairs = 0)
+        : gravity_(gravity) {
+        npgpu_default_params(&integration_parameters);
+        float g[3] = {gravity.x, gravity.y, gravity.z};
+        npgpu_status st = NPGPU_OK;
+        if (capacity_pairs == 0) capacity_pairs = 16u * capacity_colliders;
+        w_ = npgpu_create(&integration_parameters, g, capacity_bodies, capacity_colliders, capacity_pairs, &st);
+        if (!w_) throw Error(st, npgpu_last_error(nullptr));
+    }
+    ~GpuMechanicalWorld() { npgpu_destroy(w_); }
+    GpuMechanicalWorld(const GpuMechanicalWorld&) = delete;
+    GpuMechanicalWorld& operator=(const GpuMechanicalWorld&) = delete;
+
+    float timestep() const { return integration_parameters.dt; }
+    void set_timestep(float dt) { integration_parameters.dt = dt; }
+    npgpu_world* raw() { return w_; }
+
+    // MechanicalWorld::step (mechanical_world.rs:182-196).
+    void step(DefaultGeometricalWorld&, DefaultBodySet& bodies, DefaultColliderSet& colliders,
+              DefaultJointConstraintSet& joints, DefaultForceGeneratorSet& forces) {
+        check(npgpu_set_params(w_, &integration_parameters));
+        maintain(bodies, colliders);
+        check(npgpu_step(w_, 1, uint32_t(joints.len()), uint32_t(forces.len())));
+        check(npgpu_synchronize(w_));
+        if (write_back) download(bodies);
+    }
+
+private:
+    void check(npgpu_status s) {
+        if (s != NPGPU_OK) throw Error(s, npgpu_last_error(w_));
+    }
+
+    // MechanicalWorld::maintain: removals first, then insertions and edits.
+    void maintain(DefaultBodySet& bodies, DefaultColliderSet& colliders) {
+        std::vector<npgpu_handle> h;
+        for (auto& c : colliders.removed_) h.push_back(c.raw());
+        colliders.removed_.clear();
+        if (!h.empty()) check(npgpu_remove_colliders(w_, uint32_t(h.size()), h.data()));
+        h.clear();
+        for (auto& b : bodies.removed_) h.push_back(b.raw());
+        bodies.removed_.clear();
+        if (!h.empty()) check(npgpu_remove_bodies(w_, uint32_t(h.size()), h.data()));
+
+        std::vector<npgpu_handle> bh;
+        std::vector<npgpu_body_desc> bd;
+        std::vector<npgpu_handle> fh;
+        std::vector<float> fv;
+        std::vector<int> fw;
+        for (size_t i = 0; i < bodies.arena_.capacity_used(); ++i) {
+            if (!bodies.arena_.occupied(i)) continue;
+            Index hi = bodies.arena_.handle_at(i);
+            BodyVariant* v = bodies.arena_.get(hi);
+            if (auto* rb = std::get_if<RigidBody>(v)) {
+                if (rb->dirty_) {
+                    bh.push_back(hi.raw());
+                    bd.push_back(rb->desc);
+                    rb->dirty_ = false;
+                }
+                if (rb->force_.any) {
+                    fh.push_back(hi.raw());
+                    fv.insert(fv.end(), rb->force_.v, rb->force_.v + 6);
+                    fw.push_back(rb->force_.wake);
+                    rb->force_ = RigidBody::Force();
+                }
+            } else if (std::holds_alternative<Ground>(*v) || std::holds_alternative<UnsupportedBody>(*v)) {
+                bool known = known_static_.size() > i && known_static_[i] == hi.generation + 1;
+                if (!known) {
+                    npgpu_body_desc d = RigidBody().desc;
+                    d.kind = std::holds_alternative<Ground>(*v) ? uint32_t(NPGPU_KIND_GROUND)
+                                                                : std::get<UnsupportedBody>(*v).kind;
+                    d.status = NPGPU_BODY_STATIC;
+                    bh.push_back(hi.raw());
+                    bd.push_back(d);
+                    if (known_static_.size() <= i) known_static_.resize(i + 1, 0);
+                    known_static_[i] = hi.generation + 1;
+                }
+            }
+        }
+        if (!bh.empty()) check(npgpu_upsert_bodies(w_, uint32_t(bh.size()), bh.data(), bd.data()));
+        // Forces are applied per wake flag.
+        for (int wake = 0; wake < 2; ++wake) {
+            std::vector<npgpu_handle> hh;
+            std::vector<float> ff;
+            for (size_t k = 0; k < fh.size(); ++k)
+                if (fw[k] == wake) {
+                    hh.push_back(fh[k]);
+                    ff.insert(ff.end(), fv.begin() + 6 * k, fv.begin() + 6 * k + 6);
+                }
+            if (!hh.empty()) check(npgpu_apply_forces(w_, uint32_t(hh.size()), hh.data(), ff.data(), wake));
+        }
+        std::vector<npgpu_handle> ch;
+        std::vector<npgpu_collider_desc> cd;
+        for (auto& c : colliders.inserted_) {
+            const Collider* col = colliders.get(c);
+            if (!col) continue;
+            ch.push_back(c.raw());
+            cd.push_back(col->desc);
+        }
+        colliders.inserted_.clear();
+        bodies.inserted_.clear();
+        if (!ch.empty()) check(npgpu_upsert_colliders(w_, uint32_t(ch.size()), ch.data(), cd.data()));
+    }
+
+    void download(DefaultBodySet& bodies) {
+        uint32_t n = uint32_t(bodies.arena_.capacity_used());
+        if (n == 0) return;
+        pos_.resize(7 * size_t(n));
+        vel_.resize(6 * size_t(n));
+        act_.resize(n);
+        check(npgpu_download_bodies(w_, 0, n, pos_.data(), vel_.data(), nullptr, act_.data()));
+        for (uint32_t i = 0; i < n; ++i) {
+            if (!bodies.arena_.occupied(i)) continue;
+            BodyVariant* v = bodies.arena_.get(bodies.arena_.handle_at(i));
+            if (auto* rb = std::get_if<RigidBody>(v)) {
+                std::memcpy(rb->desc.position, &pos_[7 * size_t(i)], 7 * sizeof(float));
+                std::memcpy(rb->desc.velocity, &vel_[6 * size_t(i)], 6 * sizeof(float));
+                rb->active_ = act_[i] != 0;
+            }
+        }
+    }
+
+    npgpu_world* w_ = nullptr;
+    Vector3 gravity_;
+    std::vector<float> pos_, vel_;
+    std::vector<uint8_t> act_;
+    std::vector<uint64_t> known_static_;
+};
+
+}  // namespace nphysics_gpu
