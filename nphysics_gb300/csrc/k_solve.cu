@@ -557,29 +557,6 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     }
 }
 
-// Groups the solver manifolds by colour for the thread assignment of the
-// dataflow kernels, so that the 32 lanes of a warp hold tasks that become
-// ready at about the same time. (The order within a colour does not matter:
-// the version counters fix the order of the updates.)
-__global__ void k_colour_count(World w) {
-    const uint32_t ms = w.ctl->nsolver;
-    GRID_FOR(m, ms) atomicAdd(&w.s.colour_count[w.s.sm_colour[m]], 1u);
-}
-__global__ void k_colour_scan(World w) {
-    if (threadIdx.x == 0) {
-        uint32_t acc = 0;
-        for (int c = 0; c < kMaxColours; ++c) {
-            w.s.colour_cursor[c] = acc;
-            acc += w.s.colour_count[c];
-            w.s.colour_count[c] = 0;   // ready for the next step
-        }
-    }
-}
-__global__ void k_colour_scatter(World w) {
-    const uint32_t ms = w.ctl->nsolver;
-    GRID_FOR(m, ms) w.s.order[atomicAdd(&w.s.colour_cursor[w.s.sm_colour[m]], 1u)] = m;
-}
-
 // ================================================================ assembly
 __global__ void k_assemble(World w, StepParams p) {
     const uint32_t ms = w.ctl->nsolver;
@@ -707,7 +684,6 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
 // dynamic bodies and colour ranks read once.
 struct MyTasks {
     uint32_t n;
-    uint32_t m[kMaxPerThread];
     int b1[kMaxPerThread], b2[kMaxPerThread];
     uint32_t rk[kMaxPerThread];
     uint16_t next[kMaxPerThread];
@@ -718,8 +694,7 @@ __device__ __forceinline__ void load_tasks(const World& w, uint32_t ms, MyTasks&
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     mt.n = t < ms ? (ms - t + T - 1) / T : 0u;
     for (uint32_t k = 0; k < mt.n; ++k) {
-        uint32_t m = w.s.order[t + k * T];
-        mt.m[k] = m;
+        uint32_t m = t + k * T;
         mt.b1[k] = w.s.sm_b1[m];
         mt.b2[k] = w.s.sm_b2[m];
         mt.rk[k] = w.s.sm_rk[m];
@@ -758,7 +733,7 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             fence_acq_rel();   // acquire: the bodies' latest dv is visible
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
-            velocity_task(w, mt.m[k], sw, b1, b2);
+            velocity_task(w, t + k * T, sw, b1, b2);
             fence_acq_rel();   // release: dv and impulses before the new versions
             if (b1 >= 0) st_relaxed(w.b.vel_ver + b1, t1 + 1u);
             if (b2 >= 0) st_relaxed(w.b.vel_ver + b2, t2 + 1u);
@@ -993,7 +968,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
             if (b1 >= 0 && ld_relaxed(w.b.pos_ver + b1) != t1) continue;
             if (b2 >= 0 && ld_relaxed(w.b.pos_ver + b2) != t2) continue;
             fence_acq_rel();
-            position_task(w, p, mt.m[k]);
+            position_task(w, p, t + k * T);
             fence_acq_rel();
             if (b1 >= 0) st_relaxed(w.b.pos_ver + b1, t1 + 1u);
             if (b2 >= 0) st_relaxed(w.b.pos_ver + b2, t2 + 1u);
@@ -1092,9 +1067,6 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     k_prank<<<npb, kItemThreads, 0, st>>>(wc);
     e = coop((const void*)k_colour, L.grid_colour, args1, st);
     if (e != cudaSuccess) return e;
-    k_colour_count<<<npb, kItemThreads, 0, st>>>(wc);
-    k_colour_scan<<<1, 32, 0, st>>>(wc);
-    k_colour_scatter<<<npb, kItemThreads, 0, st>>>(wc);
     rec(2);
     k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc);
     rec(3);

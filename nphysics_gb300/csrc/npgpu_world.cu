@@ -271,8 +271,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     }
     Solver& s = w->dw.s;
     A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_prank, P); A(s.sm_rk, P); A(s.sm_b1, P); A(s.sm_b2, P);
-    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats); A(s.adj, 2 * (size_t)P); A(s.order, P);
-    A(s.colour_count, kMaxColours); A(s.colour_cursor, kMaxColours);
+    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats); A(s.adj, 2 * (size_t)P);
     A(w->ctl, 1);
     A(w->d_forget, Cn);
 #undef A

@@ -109,8 +109,6 @@ struct Solver {
     uint32_t *sm_nc;
     float *rows;                     // 12 rows per solver manifold
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
-    uint32_t *order;                 // solver manifolds grouped by colour (thread assignment)
-    uint32_t *colour_count, *colour_cursor;   // kMaxColours each
 };
 
 // Device counters and control words (one struct in device memory).
