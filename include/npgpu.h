@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 1u
+#define NPGPU_ABI_VERSION 2u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -144,6 +144,17 @@ typedef struct npgpu_collider_desc {
 
 /* IntegrationParameters (src/solver/integration_parameters.rs:5-190),
  * plus the GPU-only knobs at the end. */
+/* Solver schedules. AUTO picks WORLDS when the step qualifies (at least two
+ * worlds, each world's alive bodies in one contiguous run of slots with
+ * world indices non-decreasing in slot order, no world wider than 4096 slots,
+ * solve_to_tolerance off), else GRID. Both give identical results. */
+enum {
+    NPGPU_SCHEDULE_AUTO = 0,
+    NPGPU_SCHEDULE_GRID = 1,      /* one cooperative grid, per-body dataflow between colours */
+    NPGPU_SCHEDULE_WORLDS = 2     /* one block per world, world Δv in shared memory; falls back to GRID
+                                     when the step does not qualify */
+};
+
 typedef struct npgpu_params {
     float dt;                              /* 1/60 */
     float erp;                             /* 0.2 */
@@ -166,6 +177,7 @@ typedef struct npgpu_params {
     float broad_phase_margin;              /* DBVTBroadPhase::new(0.01), geometrical_world.rs:60 */
     float activation_mix;                  /* ActivationManager::new(0.01), mechanical_world.rs:80 */
     uint32_t profile;                      /* non-zero: time each phase with CUDA events */
+    uint32_t solver_schedule;              /* NPGPU_SCHEDULE_*: how the velocity and position solvers run */
 } npgpu_params;
 
 /* Per-step counters: the stage names of src/counters/mod.rs:18-209 plus

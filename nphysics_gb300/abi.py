@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 1
+NPGPU_ABI_VERSION = 2
 
 # npgpu_status
 OK = 0
@@ -41,6 +41,9 @@ BODY_GRAVITY = 1 << 0
 BODY_LOCK_TX, BODY_LOCK_TY, BODY_LOCK_TZ = 1 << 1, 1 << 2, 1 << 3
 BODY_LOCK_RX, BODY_LOCK_RY, BODY_LOCK_RZ = 1 << 4, 1 << 5, 1 << 6
 BODY_CAN_SLEEP = 1 << 7
+
+# npgpu_params.solver_schedule
+SCHEDULE_AUTO, SCHEDULE_GRID, SCHEDULE_WORLDS = 0, 1, 2
 BODY_LINEAR_INTERP = 1 << 8
 # Shapes
 SHAPE_BALL, SHAPE_CUBOID, SHAPE_OTHER = 0, 1, 2
@@ -113,6 +116,7 @@ class Params(C.Structure):
         ("broad_phase_margin", C.c_float),
         ("activation_mix", C.c_float),
         ("profile", C.c_uint32),
+        ("solver_schedule", C.c_uint32),
     ]
 
 
@@ -191,6 +195,7 @@ def default_params():
     p.broad_phase_margin = 0.01
     p.activation_mix = 0.01
     p.profile = 0
+    p.solver_schedule = SCHEDULE_AUTO
     return p
 
 

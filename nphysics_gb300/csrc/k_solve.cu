@@ -369,6 +369,10 @@ __global__ void k_act_init(World w, StepParams p) {
         c->task_ns = 0ull;
         c->wait_ns = 0ull;
         c->tasks = 0ull;
+        c->res_acc_init[0] = 0.0;
+        c->res_acc_init[1] = 0.0;
+        c->world_next[0] = 0u;
+        c->world_next[1] = 0u;
     }
 }
 
@@ -620,11 +624,14 @@ __global__ void k_assemble(World w, StepParams p) {
 // One velocity task: sweep 0 is the warm start (sor_prox.rs:19-45), odd sweeps
 // the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
 // normal rows (sor_prox.rs:181-230).
-__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int b1, int b2) {
+// `dvbase` is the global Δv array (with b1, b2 body slots) or a world's
+// shared-memory Δv (with world-local indices).
+__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int b1, int b2,
+                                              float* dvbase) {
     const bool h1 = b1 >= 0, h2 = b2 >= 0;
     DV dv;
-    load_dv(w.b.dv, b1, dv.a);
-    load_dv(w.b.dv, b2, dv.b);
+    load_dv(dvbase, b1, dv.a);
+    load_dv(dvbase, b2, dv.b);
     float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
     const uint32_t nc = w.s.sm_nc[m];
     if (sweep == 0) {
@@ -676,8 +683,8 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
             axpy(r, dv, dl, h1, h2);
         }
     }
-    store_dv(w.b.dv, b1, dv.a);
-    store_dv(w.b.dv, b2, dv.b);
+    store_dv(dvbase, b1, dv.a);
+    store_dv(dvbase, b2, dv.b);
 }
 
 // The dataflow tasks of one thread: its manifolds m = t + k T, with their
@@ -733,7 +740,7 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             fence_acq_rel();   // acquire: the bodies' latest dv is visible
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
-            velocity_task(w, t + k * T, sw, b1, b2);
+            velocity_task(w, t + k * T, sw, b1, b2, w.b.dv);
             fence_acq_rel();   // release: dv and impulses before the new versions
             if (b1 >= 0) st_relaxed(w.b.vel_ver + b1, t1 + 1u);
             if (b2 >= 0) st_relaxed(w.b.vel_ver + b2, t2 + 1u);
@@ -831,6 +838,144 @@ __global__ void __launch_bounds__(kCoopThreads) k_velocity(World w, StepParams p
         }
         if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->t_phase[0] = global_ns() - k0;
     }
+}
+
+// ================================================================ batched worlds
+// Thousands of independent worlds: one block per world, the world's Δv in
+// shared memory, colours swept with __syncthreads. A world's manifolds are
+// bucketed by colour; two manifolds of one colour share no dynamic body, so
+// every body sees its updates in the same colour order as in the dataflow
+// kernels (and in the oracle's colour order), and the results are identical.
+
+__device__ __forceinline__ uint32_t manifold_world(const World& w, uint32_t m) {
+    int b = w.s.sm_b1[m];
+    if (b < 0) b = w.s.sm_b2[m];
+    return b < 0 ? 0xffffffffu : w.b.world[b];
+}
+
+// Bucket of manifold m, or UINT32_MAX (with the error flag set) when its world
+// or colour is out of range.
+__device__ __forceinline__ uint32_t world_bucket(const World& w, uint32_t m, uint32_t n_worlds) {
+    uint32_t wd = manifold_world(w, m), col = w.s.sm_colour[m];
+    if (wd >= n_worlds || col >= (uint32_t)kMaxColours) {
+        atomicOr(&w.ctl->err, ERRF_WORLD_RANGE);
+        return 0xffffffffu;
+    }
+    return wd * kMaxColours + col;
+}
+
+__global__ void k_world_count(World w, uint32_t n_worlds) {
+    const uint32_t ms = w.ctl->nsolver;
+    GRID_FOR(m, ms) {
+        uint32_t bucket = world_bucket(w, m, n_worlds);
+        if (bucket != 0xffffffffu) atomicAdd(&w.s.bucket_count[bucket], 1u);
+    }
+}
+
+__global__ void k_world_scatter(World w, uint32_t n_worlds) {
+    const uint32_t ms = w.ctl->nsolver;
+    GRID_FOR(m, ms) {
+        uint32_t bucket = world_bucket(w, m, n_worlds);
+        if (bucket == 0xffffffffu) continue;
+        w.s.wm_order[w.s.bucket_start[bucket] + atomicAdd(&w.s.bucket_cursor[bucket], 1u)] = m;
+    }
+}
+
+// World-local index of body slot b (-1 stays -1). A body outside the world's
+// slot range flags an error and the task is skipped.
+__device__ __forceinline__ bool world_locals(const World& w, uint32_t m, uint32_t base, uint32_t nbw, int& l1, int& l2) {
+    int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
+    l1 = b1 < 0 ? -1 : b1 - (int)base;
+    l2 = b2 < 0 ? -1 : b2 - (int)base;
+    if ((b1 >= 0 && (uint32_t)l1 >= nbw) || (b2 >= 0 && (uint32_t)l2 >= nbw)) {
+        atomicOr(&w.ctl->err, ERRF_WORLD_RANGE);
+        return false;
+    }
+    return true;
+}
+
+// One sweep (warm start, friction or normal rows) over a world's manifolds,
+// colour by colour.
+__device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_t base, uint32_t nbw, uint32_t ncol,
+                                            uint32_t sweep, float* s_dv) {
+    const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
+    for (uint32_t c = 0; c < ncol; ++c) {
+        uint32_t lo = bs[c], hi = bs[c + 1];
+        if (lo == hi) continue;
+        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+            uint32_t m = w.s.wm_order[i];
+            int l1, l2;
+            if (world_locals(w, m, base, nbw, l1, l2)) velocity_task(w, m, sweep, l1, l2, s_dv);
+        }
+        __syncthreads();
+    }
+}
+
+// FP64 residual partial sums of one world, added to acc[0..1].
+__device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint32_t base, uint32_t nbw,
+                                               const float* s_dv, double* sh, double* acc) {
+    uint32_t lo = w.s.bucket_start[wd * kMaxColours], hi = w.s.bucket_start[wd * kMaxColours + kMaxColours];
+    double s2 = 0.0, l2 = 0.0;
+    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        uint32_t m = w.s.wm_order[i];
+        int b1, b2;
+        if (!world_locals(w, m, base, nbw, b1, b2)) continue;
+        DV dv;
+        load_dv(s_dv, b1, dv.a);
+        load_dv(s_dv, b2, dv.b);
+        const float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
+        uint32_t nc = w.s.sm_nc[m];
+        for (uint32_t k = 0; k < nc; ++k) {
+            const float* rn = rows + (3 * k) * kRowFloats;
+            residual_row(rn, dv, b1 >= 0, b2 >= 0, false, 0.0, s2, l2);
+            residual_row(rn + kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
+            residual_row(rn + 2 * kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
+        }
+    }
+    double ts = block_sum(s2, sh);
+    double tl = block_sum(l2, sh);
+    if (threadIdx.x == 0 && (ts != 0.0 || tl != 0.0)) {
+        atomicAdd(&acc[0], ts);
+        atomicAdd(&acc[1], tl);
+    }
+}
+
+// Persistent: each block takes worlds from a counter until none is left.
+// Dynamic shared memory: 6 floats per body slot of the largest world.
+__global__ void __launch_bounds__(kWorldThreads) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
+                                                                  uint32_t max_world_bodies) {
+    extern __shared__ float s_dv[];
+    __shared__ double sh[32];
+    __shared__ uint32_t s_world;
+    const uint32_t ncol = w.ctl->ncolours;
+    for (;;) {
+        if (threadIdx.x == 0) s_world = atomicAdd(&w.ctl->world_next[0], 1u);
+        __syncthreads();
+        const uint32_t wd = s_world;
+        if (wd >= n_worlds) break;
+        const uint32_t base = w.s.world_start[wd];
+        uint32_t nbw = w.s.world_start[wd + 1] - base;
+        if (nbw > max_world_bodies) {
+            if (threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_WORLD_RANGE);
+            nbw = 0;
+        }
+        for (uint32_t i = threadIdx.x; i < 6 * nbw; i += blockDim.x) s_dv[i] = 0.0f;
+        __syncthreads();
+        world_sweep(w, wd, base, nbw, ncol, 0, s_dv);
+        world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc_init);
+        for (uint32_t sw = 1; sw < 1 + 2 * p.max_velocity_iterations; ++sw) world_sweep(w, wd, base, nbw, ncol, sw, s_dv);
+        world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc);
+        for (uint32_t i = threadIdx.x; i < 6 * nbw; i += blockDim.x) w.b.dv[6 * base + i] = s_dv[i];
+        __syncthreads();
+    }
+}
+
+__global__ void k_world_finish(World w, StepParams p) {
+    Control* c = w.ctl;
+    c->residual_initial = sqrt(c->res_acc_init[0]) / fmax(1.0, sqrt(c->res_acc_init[1]));
+    c->residual = sqrt(c->res_acc[0]) / fmax(1.0, sqrt(c->res_acc[1]));
+    c->res_acc[0] = c->res_acc[1] = 0.0;
+    c->iterations = p.max_velocity_iterations;
 }
 
 // ================================================================ integrate
@@ -985,6 +1130,28 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
     }
 }
 
+// Batched worlds: block per world, colour by colour, poses in global memory.
+__global__ void __launch_bounds__(kWorldThreads) k_world_position(World w, StepParams p, uint32_t n_worlds) {
+    __shared__ uint32_t s_world;
+    const uint32_t ncol = w.ctl->ncolours;
+    for (;;) {
+        if (threadIdx.x == 0) s_world = atomicAdd(&w.ctl->world_next[1], 1u);
+        __syncthreads();
+        const uint32_t wd = s_world;
+        if (wd >= n_worlds) break;
+        const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
+        for (uint32_t it = 0; it < p.max_position_iterations; ++it) {
+            for (uint32_t c = 0; c < ncol; ++c) {
+                uint32_t lo = bs[c], hi = bs[c + 1];
+                if (lo == hi) continue;
+                for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) position_task(w, p, w.s.wm_order[i]);
+                __syncthreads();
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // ================================================================ post
 __global__ void k_post(World w, StepParams p) {
     __shared__ double sh[32];
@@ -1037,6 +1204,18 @@ void solver_grid_sizes(int device, SolverLaunch& L) {
     L.grid_velocity = sms * (per < 1 ? 1 : per);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_position, kCoopThreads, 0);
     L.grid_position = sms * (per < 1 ? 1 : per);
+    cudaFuncSetAttribute(k_world_velocity, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(6 * kMaxWorldBodies * sizeof(float)));
+}
+
+int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds) {
+    int sms = 0, per = 0;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_world_velocity, kWorldThreads,
+                                                  6 * (size_t)max_world_bodies * sizeof(float));
+    long g = (long)sms * (per < 1 ? 1 : per);
+    if (g > (long)n_worlds) g = n_worlds;
+    return g < 1 ? 1 : (int)g;
 }
 
 static cudaError_t coop(const void* fn, int grid, void** args, cudaStream_t st) {
@@ -1070,15 +1249,34 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     rec(2);
     k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc);
     rec(3);
-    e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
-    if (e != cudaSuccess) return e;
-    e = coop((const void*)k_velocity, L.grid_velocity, args2, st);
-    if (e != cudaSuccess) return e;
+    if (L.batched) {
+        const uint32_t nbk = L.n_worlds * kMaxColours;
+        e = cudaMemsetAsync(w.s.bucket_count, 0, (2 * (size_t)nbk + 1) * sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+        k_world_count<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
+        scan_bytes = L.scan_bytes;
+        e = cub::DeviceScan::ExclusiveSum(L.scan_temp, scan_bytes, w.s.bucket_count, w.s.bucket_start, (int)(nbk + 1),
+                                          st);
+        if (e != cudaSuccess) return e;
+        k_world_scatter<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
+        k_world_velocity<<<L.grid_world, kWorldThreads, 6 * (size_t)L.max_world_bodies * sizeof(float), st>>>(
+            wc, pc, L.n_worlds, L.max_world_bodies);
+        k_world_finish<<<1, 1, 0, st>>>(wc, pc);
+    } else {
+        e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
+        if (e != cudaSuccess) return e;
+        e = coop((const void*)k_velocity, L.grid_velocity, args2, st);
+        if (e != cudaSuccess) return e;
+    }
     rec(4);
     k_cache_integrate<<<nbb > npb ? nbb : npb, kItemThreads, 0, st>>>(wc, pc);
     rec(5);
-    e = coop((const void*)k_position, L.grid_position, args2, st);
-    if (e != cudaSuccess) return e;
+    if (L.batched) {
+        k_world_position<<<L.grid_world, kWorldThreads, 0, st>>>(wc, pc, L.n_worlds);
+    } else {
+        e = coop((const void*)k_position, L.grid_position, args2, st);
+        if (e != cudaSuccess) return e;
+    }
     rec(6);
     k_post<<<nbb, kItemThreads, 0, st>>>(wc, pc);
     return cudaGetLastError();

@@ -134,6 +134,14 @@ struct npgpu_world {
     SolverLaunch solver;
     bool ev_recorded = false;
     bool cd_start_ran = false;
+    // Batched-world layout: recomputed when bodies are added, removed or
+    // moved between worlds.
+    bool layout_dirty = true;
+    bool layout_ok = false;              // the worlds qualify for the per-world schedule
+    uint32_t n_worlds = 0, max_world_bodies = 0;
+    std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries
+    uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
+    int grid_world = 0;
 };
 
 static std::string g_create_error;
@@ -215,6 +223,88 @@ static void sync_world_view(npgpu_world* w) {
     w->dw.nc_alive = w->nc_alive;
 }
 
+// Finds each world's slot range. The per-world schedule needs the alive
+// bodies' world indices non-decreasing in slot order (so a world is one run of
+// slots), at least two worlds and no world wider than the shared-memory limit.
+static void compute_layout(npgpu_world* w) {
+    w->layout_dirty = false;
+    w->layout_ok = false;
+    uint32_t last = 0;
+    bool any = false;
+    for (uint32_t i = 0; i < w->nb_slots; ++i) {
+        const HostBody& b = w->hb[i];
+        if (!b.alive) continue;
+        if (any && b.world < last) return;
+        last = b.world;
+        any = true;
+    }
+    if (!any || last == 0) return;
+    const uint32_t nw = last + 1;
+    std::vector<uint32_t> st(nw + 1, 0xffffffffu);
+    for (uint32_t i = 0; i < w->nb_slots; ++i) {
+        const HostBody& b = w->hb[i];
+        if (b.alive && st[b.world] == 0xffffffffu) st[b.world] = i;
+    }
+    st[nw] = w->nb_slots;
+    for (uint32_t k = nw; k-- > 0;)
+        if (st[k] == 0xffffffffu) st[k] = st[k + 1];
+    st[0] = 0;
+    uint32_t widest = 0;
+    for (uint32_t k = 0; k < nw; ++k) widest = std::max(widest, st[k + 1] - st[k]);
+    if (widest > kMaxWorldBodies) return;
+    w->world_start.swap(st);
+    w->n_worlds = nw;
+    w->max_world_bodies = widest;
+    w->layout_ok = true;
+}
+
+// Chooses the schedule of this step and, for the per-world one, makes sure
+// the bucket buffers hold every world and the world ranges are on the device.
+static npgpu_status prepare_schedule(npgpu_world* w) {
+    const bool was_dirty = w->layout_dirty;
+    if (w->layout_dirty) compute_layout(w);
+    const uint32_t sched = w->params.solver_schedule;
+    w->solver.batched = w->layout_ok && sched != NPGPU_SCHEDULE_GRID && !w->params.solve_to_tolerance;
+    if (!w->solver.batched) return NPGPU_OK;
+    Solver& s = w->dw.s;
+    const size_t nbk = (size_t)w->n_worlds * kMaxColours;
+    if (w->n_worlds > w->worlds_cap) {
+        CK(cudaStreamSynchronize(w->stream), "synchronize");
+        cudaFree(s.world_start);
+        cudaFree(s.bucket_count);
+        cudaFree(s.bucket_start);
+        s.world_start = s.bucket_count = s.bucket_start = s.bucket_cursor = nullptr;
+        uint32_t cap = std::max(w->n_worlds, 2 * w->worlds_cap);
+        size_t cbk = (size_t)cap * kMaxColours;
+        CK(cudaMalloc(&s.world_start, sizeof(uint32_t) * (cap + 1)), "world ranges");
+        CK(cudaMalloc(&s.bucket_count, sizeof(uint32_t) * (2 * cbk + 1)), "world buckets");
+        CK(cudaMalloc(&s.bucket_start, sizeof(uint32_t) * (cbk + 1)), "world bucket starts");
+        w->worlds_cap = cap;
+        size_t need = scan_temp_bytes((uint32_t)(cbk + 1));
+        if (need > w->scan_bytes) {
+            void* old = w->scan_temp;
+            CK(cudaMalloc(&w->scan_temp, need), "scan temp");
+            for (void*& o : w->owned)
+                if (o == old) o = w->scan_temp;
+            cudaFree(old);
+            w->scan_bytes = need;
+            w->solver.scan_temp = w->scan_temp;
+            w->solver.scan_bytes = w->scan_bytes;
+        }
+    }
+    s.bucket_cursor = s.bucket_count + nbk + 1;
+    if (was_dirty) {
+        CK(cudaMemcpyAsync(s.world_start, w->world_start.data(), sizeof(uint32_t) * (w->n_worlds + 1),
+                           cudaMemcpyHostToDevice, w->stream),
+           "world ranges");
+        w->grid_world = world_grid(w->device, w->max_world_bodies, w->n_worlds);
+    }
+    w->solver.n_worlds = w->n_worlds;
+    w->solver.max_world_bodies = w->max_world_bodies;
+    w->solver.grid_world = w->grid_world;
+    return NPGPU_OK;
+}
+
 extern "C" {
 
 uint32_t npgpu_abi_version(void) { return NPGPU_ABI_VERSION; }
@@ -242,6 +332,7 @@ void npgpu_default_params(npgpu_params* p) {
     p->broad_phase_margin = 0.01f;
     p->activation_mix = 0.01f;
     p->profile = 0;
+    p->solver_schedule = NPGPU_SCHEDULE_AUTO;
 }
 
 static npgpu_status create_buffers(npgpu_world* w) {
@@ -271,7 +362,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     }
     Solver& s = w->dw.s;
     A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_prank, P); A(s.sm_rk, P); A(s.sm_b1, P); A(s.sm_b2, P);
-    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats); A(s.adj, 2 * (size_t)P);
+    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats); A(s.adj, 2 * (size_t)P); A(s.wm_order, P);
     A(w->ctl, 1);
     A(w->d_forget, Cn);
 #undef A
@@ -356,6 +447,9 @@ void npgpu_destroy(npgpu_world* w) {
     if (!w) return;
     if (w->stream) cudaStreamSynchronize(w->stream);
     for (void* p : w->owned) cudaFree(p);
+    cudaFree(w->dw.s.world_start);
+    cudaFree(w->dw.s.bucket_count);
+    cudaFree(w->dw.s.bucket_start);
     if (w->d_stage) cudaFree(w->d_stage);
     if (w->h_stage) cudaFreeHost(w->h_stage);
     if (w->ev_stage) cudaEventDestroy(w->ev_stage);
@@ -372,6 +466,8 @@ void* npgpu_stream(npgpu_world* w) { return w ? (void*)w->stream : nullptr; }
 npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params) {
     if (!w || !params) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
     if (!(params->dt >= 0.0f)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "dt must be >= 0");
+    if (params->solver_schedule > NPGPU_SCHEDULE_WORLDS)
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown solver_schedule");
     w->params = *params;
     return NPGPU_OK;
 }
@@ -440,6 +536,7 @@ npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
         u.max_lin = d.max_linear_velocity;
         u.max_ang = d.max_angular_velocity;
         u.sleep_thr = d.sleep_threshold;
+        if (!hb.alive || hb.world != d.world) w->layout_dirty = true;
         hb.alive = true;
         hb.gen = handles[k].generation;
         hb.kind = d.kind;
@@ -600,6 +697,7 @@ npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
             }
         }
         w->hb[bi].alive = false;
+        w->layout_dirty = true;
         bslots.push_back((uint32_t)bi);
     }
     w->forget_pending = true;
@@ -724,6 +822,8 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
         }
         if (prof) CK(cudaEventRecord(w->ev[1], w->stream), "event");
         w->solver.ev = prof ? w->ev_solver : nullptr;
+        st = prepare_schedule(w);
+        if (st != NPGPU_OK) return st;
         CK(launch_solver(w->dw, sp, w->solver, w->stream), "solve");
         if (prof) CK(cudaEventRecord(w->ev[2], w->stream), "event");
         st = run_cd(w, sp);
@@ -750,6 +850,7 @@ npgpu_status npgpu_synchronize(npgpu_world* w) {
         if (err & ERRF_NAN) return fail(w, NPGPU_ERR_NAN, "non-finite body state after the step");
         if (err & ERRF_PAIR_CAPACITY) return fail(w, NPGPU_ERR_CAPACITY, "pair capacity exceeded");
         if (err & ERRF_COLOURS) return fail(w, NPGPU_ERR_CAPACITY, "more than 64 solver colours needed");
+        if (err & ERRF_WORLD_RANGE) return fail(w, NPGPU_ERR_CUDA, "a solver manifold left its world's slot range");
     }
     return NPGPU_OK;
 }

@@ -36,6 +36,7 @@ enum : uint32_t {
     ERRF_NAN = 1u << 2,
     ERRF_COLOURS = 1u << 3,
     ERRF_UNION_FIND = 1u << 4,
+    ERRF_WORLD_RANGE = 1u << 5,      // a batched world's body outside its slot range
 };
 
 constexpr int kMaxContacts = 4;      // contacts per manifold
@@ -109,6 +110,12 @@ struct Solver {
     uint32_t *sm_nc;
     float *rows;                     // 12 rows per solver manifold
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
+    // Batched worlds: manifolds bucketed by (world, colour).
+    uint32_t *world_start;           // body slot range of each world (n_worlds + 1)
+    // bucket_count (n_worlds * kMaxColours + 1) and bucket_cursor follow each
+    // other in one allocation, cleared by one memset each step.
+    uint32_t *bucket_count, *bucket_start, *bucket_cursor;
+    uint32_t *wm_order;              // solver manifolds ordered by (world, colour)
 };
 
 // Device counters and control words (one struct in device memory).
@@ -132,6 +139,8 @@ struct Control {
     unsigned long long max_pen_bits; // order-preserving bits of the max penetration
     unsigned long long t_phase[16];  // %globaltimer stamps
     unsigned long long task_ns, wait_ns, tasks;   // velocity-task statistics (profile mode)
+    double res_acc_init[2];          // batched worlds: residual sums after the warm start
+    uint32_t world_next[2];          // batched worlds: work counters of the velocity / position kernels
 };
 
 struct StepParams {
@@ -170,9 +179,19 @@ struct SolverLaunch {
     void* scan_temp;
     size_t scan_bytes;
     cudaEvent_t* ev;
+    // Batched worlds (one block per world, Δv in shared memory).
+    bool batched;
+    uint32_t n_worlds;
+    uint32_t max_world_bodies;       // largest body slot range of a world
+    int grid_world;                  // blocks of the per-world kernels
 };
+constexpr int kWorldThreads = 128;
+constexpr uint32_t kMaxWorldBodies = 4096;    // per-world shared-memory Δv limit (96 KiB)
 cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st);
 void solver_grid_sizes(int device, SolverLaunch& L);
+// Blocks of the per-world kernels: resident blocks at this shared-memory size,
+// at most one per world.
+int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds);
 size_t sort_temp_bytes(uint32_t n_items);
 size_t scan_temp_bytes(uint32_t n_items);
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);

@@ -1,0 +1,82 @@
+"""Batched worlds: the block-per-world schedule against the one-grid schedule
+and the oracle.
+
+Many independent worlds of uneven size, each on its own ground. Both GPU
+schedules visit every body's manifolds in colour order, so they must agree
+bit for bit; the oracle's colour order is the same sequence on the CPU.
+"""
+import numpy as np
+import pytest
+
+from nphysics_gb300 import abi, scenes
+from oracle.oracle_py import ORDER_COLOUR, OracleWorld
+
+pytestmark = pytest.mark.gpu
+
+
+def run(scene, schedule, steps):
+    from nphysics_gb300.world import GpuWorld
+    p = scene.params()
+    p.solver_schedule = schedule
+    g = GpuWorld.for_scene(scene, p)
+    g.step(steps)
+    return g
+
+
+def small_batch(n_worlds=10, seed=7):
+    return scenes.batched_worlds(n_worlds=n_worlds, seed=seed, lo=8, hi=120)
+
+
+def test_worlds_schedule_equals_grid_schedule(gpu_lib):
+    sc = small_batch()
+    a = run(sc, abi.SCHEDULE_GRID, 40)
+    b = run(sc, abi.SCHEDULE_WORLDS, 40)
+    ba, bb = a.bodies(), b.bodies()
+    np.testing.assert_array_equal(ba["position"], bb["position"])
+    np.testing.assert_array_equal(ba["velocity"], bb["velocity"])
+    np.testing.assert_array_equal(a.pairs(), b.pairs())
+    ca, cb = a.counters(), b.counters()
+    assert ca["num_constraints"] == cb["num_constraints"] > 0
+    assert ca["velocity_iterations"] == cb["velocity_iterations"]
+    # FP64 sums in a different order.
+    assert abs(ca["residual"] - cb["residual"]) <= 1e-12 + 1e-9 * abs(ca["residual"])
+
+
+def test_worlds_schedule_matches_oracle(gpu_lib):
+    sc = small_batch(n_worlds=6, seed=3)
+    g = run(sc, abi.SCHEDULE_WORLDS, 25)
+    o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_COLOUR)
+    o.load_scene(sc)
+    o.step(25)
+    gb, ob = g.bodies(), o.bodies()
+    err = np.abs(gb["position"].astype(np.float64) - ob["position"])
+    assert err.max() <= 1e-5 + 1e-5 * np.abs(ob["position"]).max(), err.max()
+    np.testing.assert_array_equal(g.pairs(), o.pairs())
+
+
+def test_interleaved_worlds_fall_back_to_grid(gpu_lib):
+    # World indices that are not contiguous in slot order cannot run one block
+    # per world; the step still runs (on the grid schedule) and matches it.
+    sc = small_batch(n_worlds=4, seed=9)
+    b = sc.bodies.copy()
+    w = b["world"].copy()
+    b["world"] = w[::-1].copy()          # reverse the world order over the slots
+    inter = scenes.Scene("interleaved", b, sc.colliders)
+    a = run(inter, abi.SCHEDULE_GRID, 15)
+    c = run(inter, abi.SCHEDULE_WORLDS, 15)
+    np.testing.assert_array_equal(a.bodies()["position"], c.bodies()["position"])
+
+
+def test_world_ranges_follow_removals(gpu_lib):
+    # Removing every body of one world leaves an empty world in the middle of
+    # the batch; the per-world schedule must keep matching the grid schedule.
+    sc = small_batch(n_worlds=5, seed=21)
+    worlds = sc.bodies["world"]
+    gone = np.nonzero(worlds == 2)[0]
+    res = []
+    for sched in (abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS):
+        g = run(sc, sched, 5)
+        g.remove_bodies(sc.body_handles[gone])
+        g.step(10)
+        res.append(g.bodies()["position"])
+    np.testing.assert_array_equal(res[0], res[1])
