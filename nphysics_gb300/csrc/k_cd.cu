@@ -130,6 +130,7 @@ __global__ void k_lbvh_build(World w, int n) {
     int lo = i < j ? i : j, hi = i < j ? j : i;
     int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
     int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
+    w.c.node_world[i] = (uint32_t)(k[lo] >> 48) << 16 | (uint32_t)(k[hi] >> 48);
     w.c.left[i] = left;
     w.c.right[i] = right;
     w.c.parent[left] = i;
@@ -149,6 +150,8 @@ __global__ void k_lbvh_refit(World w, int n) {
     float4 mx = w.c.aabb_max[ci];
     w.c.node_min[node] = w.c.aabb_min[ci];
     w.c.node_max[node] = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
+    uint32_t wk = (uint32_t)(w.c.keys_sorted[k] >> 48);
+    w.c.node_world[node] = wk << 16 | wk;
     if (n == 1) return;
     __threadfence();
     int p = w.c.parent[node];
@@ -216,12 +219,16 @@ __global__ void k_bp_traverse(World w, int n) {
     }
     float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
     float ra = c.rank[a];
+    const uint32_t qw = (uint32_t)(c.keys_sorted[k] >> 48);
     if (n >= 2) {
         int stack[64];
         int sp = 0;
         stack[sp++] = 0;
         while (sp > 0) {
             int node = stack[--sp];
+            // Batched worlds share space: skip subtrees of other worlds.
+            uint32_t nw = c.node_world[node];
+            if (qw < (nw >> 16) || qw > (nw & 0xffffu)) continue;
             float4 nmax = c.node_max[node];
             // Every leaf below has a smaller bounding radius: leaf a owns none of those pairs.
             if (nmax.w < ra) continue;

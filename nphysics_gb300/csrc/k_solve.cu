@@ -242,46 +242,96 @@ struct DV {
     float a[6], b[6];
 };
 
-__device__ __forceinline__ float jdot(const float* row, const DV& dv, bool has1, bool has2) {
-    float d = 0.0f;
+// Inverse augmented mass of a dynamic body as the solver reads it: three
+// float4 per body, (inv_I row k, inv_mass in the first .w).
+struct SB {
+    np::M I;
+    float im;
+};
+__device__ __forceinline__ SB load_sb(const float4* sb, int i) {
+    SB s;
+    float4 a = sb[3 * i], b = sb[3 * i + 1], c = sb[3 * i + 2];
+    s.I.m[0][0] = a.x; s.I.m[0][1] = a.y; s.I.m[0][2] = a.z;
+    s.I.m[1][0] = b.x; s.I.m[1][1] = b.y; s.I.m[1][2] = b.z;
+    s.I.m[2][0] = c.x; s.I.m[2][1] = c.y; s.I.m[2][2] = c.z;
+    s.im = a.w;
+    return s;
+}
+
+// The Jacobians of one row, J_b = mask_b . [d_b, pos_b x d_b] and
+// WJ_b = (inv_mass_b J_b.lin, inv_I_b J_b.ang) with d_1 = dir, d_2 = -dir
+// (helper.rs:53-135, rigid_body.rs:672-722). The solver rebuilds them from the
+// row direction and the lever arms with the same operations as assembly, so
+// they carry the same bits as rows stored in full; they are formed where they
+// are used rather than kept in registers.
+__device__ __forceinline__ void side_j(np::V pos, np::V dir, uint32_t m6, float* J) {
+    np::V fa = np::cross(pos, dir);
+    float f[6] = {dir.x, dir.y, dir.z, fa.x, fa.y, fa.z};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) J[k] = f[k] * (((m6 >> k) & 1u) ? 1.0f : 0.0f);
+}
+
+__device__ __forceinline__ float side_dot(np::V pos, np::V dir, uint32_t m6, const float* dv) {
+    float J[6];
+    side_j(pos, dir, m6, J);
+    float s = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s = s + J[k] * dv[k];
+    return s;
+}
+
+__device__ __forceinline__ void side_axpy(np::V pos, np::V dir, uint32_t m6, const SB& sb, float a, float* dv) {
+    float J[6];
+    side_j(pos, dir, m6, J);
+    np::V wl = np::mul(np::mk(J[0], J[1], J[2]), sb.im);
+    np::V wa = np::mv(sb.I, np::mk(J[3], J[4], J[5]));
+    float W[6] = {wl.x, wl.y, wl.z, wa.x, wa.y, wa.z};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) dv[k] = a * W[k] + dv[k];
+}
+
+// J . dv over both sides: side sums, then their sum, when both sides have dofs.
+__device__ __forceinline__ float jdot(np::V dir, np::V pos1, np::V pos2, uint32_t mask, const DV& dv, bool has1,
+                                      bool has2) {
     if (has1 && has2) {
-        float s1 = 0.0f, s2 = 0.0f;
-#pragma unroll
-        for (int k = 0; k < 6; ++k) s1 = s1 + row[RF_J1 + k] * dv.a[k];
-#pragma unroll
-        for (int k = 0; k < 6; ++k) s2 = s2 + row[RF_J2 + k] * dv.b[k];
-        d = s1 + s2;
-    } else if (has1) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) d = d + row[RF_J1 + k] * dv.a[k];
-    } else if (has2) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) d = d + row[RF_J2 + k] * dv.b[k];
+        float s1 = side_dot(pos1, dir, mask & 0x3fu, dv.a);
+        float s2 = side_dot(pos2, np::neg(dir), (mask >> 8) & 0x3fu, dv.b);
+        return s1 + s2;
     }
-    return d;
+    if (has1) return side_dot(pos1, dir, mask & 0x3fu, dv.a);
+    if (has2) return side_dot(pos2, np::neg(dir), (mask >> 8) & 0x3fu, dv.b);
+    return 0.0f;
 }
-__device__ __forceinline__ void axpy(const float* row, DV& dv, float a, bool has1, bool has2) {
-    if (has1) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) dv.a[k] = a * row[RF_WJ1 + k] + dv.a[k];
-    }
-    if (has2) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) dv.b[k] = a * row[RF_WJ2 + k] + dv.b[k];
-    }
+
+__device__ __forceinline__ void axpy(np::V dir, np::V pos1, np::V pos2, uint32_t mask, const SB& s1, const SB& s2,
+                                     DV& dv, float a, bool has1, bool has2) {
+    if (has1) side_axpy(pos1, dir, mask & 0x3fu, s1, a, dv.a);
+    if (has2) side_axpy(pos2, np::neg(dir), (mask >> 8) & 0x3fu, s2, a, dv.b);
 }
-// A row is 7 float4 (112 bytes, 16-byte aligned): loaded into registers at once.
-__device__ __forceinline__ void load_row(const float* p, float* r) {
-    const float4* q = reinterpret_cast<const float4*>(p);
-#pragma unroll
-    for (int k = 0; k < 7; ++k) {
-        float4 x = q[k];
-        r[4 * k] = x.x;
-        r[4 * k + 1] = x.y;
-        r[4 * k + 2] = x.z;
-        r[4 * k + 3] = x.w;
-    }
+
+// One contact of a solver manifold: 4 float4 (64 bytes), constant during the
+// velocity solve, read through the non-coherent path.
+//   c0 = (n, mu)   c1 = (pos1, r_n)   c2 = (pos2, rhs_n)   c3 = (r_t1, rhs_t1, r_t2, rhs_t2)
+// pos1 / pos2 are the contact points minus the body centres of mass; n points
+// from body 1 to body 2. The impulses (normal, tangent 1, tangent 2) live in a
+// separate float4 per contact.
+struct ContactRec {
+    np::V n, pos1, pos2;
+    float mu, r[3], rhs[3];
+};
+__device__ __forceinline__ ContactRec load_con(const float4* con, size_t i) {
+    float4 c0 = __ldg(con + 4 * i), c1 = __ldg(con + 4 * i + 1), c2 = __ldg(con + 4 * i + 2), c3 = __ldg(con + 4 * i + 3);
+    ContactRec c;
+    c.n = np::mk(c0.x, c0.y, c0.z);
+    c.mu = c0.w;
+    c.pos1 = np::mk(c1.x, c1.y, c1.z);
+    c.r[0] = c1.w;
+    c.pos2 = np::mk(c2.x, c2.y, c2.z);
+    c.rhs[0] = c2.w;
+    c.r[1] = c3.x; c.rhs[1] = c3.y; c.r[2] = c3.z; c.rhs[2] = c3.w;
+    return c;
 }
+
 __device__ __forceinline__ void load_dv(const float* dvg, int i, float* o) {
     if (i < 0) return;
 #pragma unroll
@@ -293,21 +343,27 @@ __device__ __forceinline__ void store_dv(float* dvg, int i, const float* o) {
     for (int k = 0; k < 6; ++k) dvg[6 * i + k] = o[k];
 }
 
-__device__ __forceinline__ void residual_row(const float* row, const DV& dv, bool has1, bool has2, bool friction,
-                                             double normal_impulse, double& s2, double& l2) {
+__device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, uint32_t mask, float r, float rhs,
+                                             float lam_f, const DV& dv, bool has1, bool has2, bool friction,
+                                             double normal_impulse, float mu, double& s2, double& l2) {
     double d = 0.0;
-    if (has1)
-        for (int k = 0; k < 6; ++k) d += (double)row[RF_J1 + k] * (double)dv.a[k];
-    if (has2)
-        for (int k = 0; k < 6; ++k) d += (double)row[RF_J2 + k] * (double)dv.b[k];
-    d += (double)row[RF_RHS];
-    double lam = (double)row[RF_IMP];
-    double x = lam - (double)row[RF_R] * d;
+    float J[6];
+    if (has1) {
+        side_j(pos1, dir, mask & 0x3fu, J);
+        for (int k = 0; k < 6; ++k) d += (double)J[k] * (double)dv.a[k];
+    }
+    if (has2) {
+        side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J);
+        for (int k = 0; k < 6; ++k) d += (double)J[k] * (double)dv.b[k];
+    }
+    d += (double)rhs;
+    double lam = (double)lam_f;
+    double x = lam - (double)r * d;
     double p;
     if (!friction) {
         p = x > 0.0 ? x : 0.0;
     } else {
-        double mx = (double)row[RF_MU] * normal_impulse;
+        double mx = (double)mu * normal_impulse;
         p = x < -mx ? -mx : (x > mx ? mx : x);
     }
     double phi = lam - p;
@@ -342,6 +398,13 @@ __global__ void k_act_init(World w, StepParams p) {
         b.vel_ver[i] = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) b.dv[6 * i + k] = 0.0f;
+        if ((info & BI_ALIVE) && bi_status(info) == 2u) {
+            const float* iI = b.inv_I + 9 * i;
+            float im = b.inv_mass[i];
+            b.sb[3 * i] = make_float4(iI[0], iI[1], iI[2], im);
+            b.sb[3 * i + 1] = make_float4(iI[3], iI[4], iI[5], 0.0f);
+            b.sb[3 * i + 2] = make_float4(iI[6], iI[7], iI[8], 0.0f);
+        }
         info &= ~BI_ISLAND;
         b.info[i] = info;
         if (!(info & BI_ALIVE)) continue;
@@ -506,7 +569,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     const uint32_t nmine = t < ms ? (ms - t + T - 1) / T : 0u;
     if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
-        if (t == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        if (t == 0) atomicOr(&w.ctl->err, ERRF_TASKS);
         return;
     }
     const Bodies& b = w.b;
@@ -592,99 +655,133 @@ __global__ void k_assemble(World w, StepParams p) {
         float mu = combine(c.friction[c1], (ci1 >> 4) & 0xfu, c.friction[c2], (ci2 >> 4) & 0xfu);
         float e = combine(c.restitution[c1], (ci1 >> 8) & 0xfu, c.restitution[c2], (ci2 >> 8) & 0xfu);
         float m1 = c.margin[c1], m2 = c.margin[c2];
-        float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
+        // Unlocked dofs of each dynamic side (jacobian_mask, rigid_body.rs:708).
+        uint32_t mask = 0;
+        if (b1 >= 0) mask |= ~(bi_flags(v1.info) >> 1) & 0x3fu;
+        if (b2 >= 0) mask |= (~(bi_flags(v2.info) >> 1) & 0x3fu) << 8;
+        w.s.sm_mask[m] = mask;
+        float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+        float4* lam = w.s.lam + (size_t)m * kMaxContacts;
         for (uint32_t k = 0; k < nc; ++k) {
             uint32_t slot = q * kMaxContacts + k;
             float4 w1 = w.cur.w1[slot], w2 = w.cur.w2[slot], nn = w.cur.n[slot], imp = w.cur.imp[slot];
             np::V n = v3(nn);
             np::V center1 = np::add(v3(w1), np::mul(n, m1));
             np::V center2 = np::sub(v3(w2), np::mul(n, m2));
-            float* rn = rows + (3 * k) * kRowFloats;
+            float rn[kRowFloats], rt[2][kRowFloats];
             make_row(rn, v1, v2, center1, center2, np::neg(n), dt);
             float rhs = rn[RF_RHS];
             if (rhs <= -p.restitution_threshold) rhs = rhs + e * rhs;
             float depth = w1.w + m1 + m2;
             if (depth < 0.0f) rhs = rhs + (-depth) * p.inv_dt;
-            rn[RF_RHS] = rhs;
-            rn[RF_IMP] = p.warmstart_mode == 1u ? 0.0f : imp.x * p.warmstart_coeff;
             np::V t[2];
             tangent_basis(n, t[0], t[1]);
-            for (int sdir = 0; sdir < 2; ++sdir) {
-                float* rt = rn + (1 + sdir) * kRowFloats;
-                make_row(rt, v1, v2, center1, center2, t[sdir], dt);
-                float ci = sdir == 0 ? imp.y : imp.z;
-                rt[RF_IMP] = p.warmstart_mode == 1u ? 0.0f : ci * p.warmstart_coeff;
-                rt[RF_MU] = mu;
-            }
+            for (int sdir = 0; sdir < 2; ++sdir) make_row(rt[sdir], v1, v2, center1, center2, t[sdir], dt);
+            np::V pos1 = np::sub(center1, v1.com), pos2 = np::sub(center2, v2.com);
+            con[4 * k] = make_float4(n.x, n.y, n.z, mu);
+            con[4 * k + 1] = make_float4(pos1.x, pos1.y, pos1.z, rn[RF_R]);
+            con[4 * k + 2] = make_float4(pos2.x, pos2.y, pos2.z, rhs);
+            con[4 * k + 3] = make_float4(rt[0][RF_R], rt[0][RF_RHS], rt[1][RF_R], rt[1][RF_RHS]);
+            const bool cold = p.warmstart_mode == 1u;
+            lam[k] = make_float4(cold ? 0.0f : imp.x * p.warmstart_coeff, cold ? 0.0f : imp.y * p.warmstart_coeff,
+                                 cold ? 0.0f : imp.z * p.warmstart_coeff, 0.0f);
         }
     }
 }
 
 // ================================================================ SOR-Prox
+// Row directions of a contact: -n for the normal row (body 1 side), and the
+// orthonormal basis of n for the friction rows.
+__device__ __forceinline__ np::V row_dir(const ContactRec& c, int row, const np::V* t) {
+    return row == 0 ? np::neg(c.n) : t[row - 1];
+}
+
 // One velocity task: sweep 0 is the warm start (sor_prox.rs:19-45), odd sweeps
 // the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
-// normal rows (sor_prox.rs:181-230).
-// `dvbase` is the global Δv array (with b1, b2 body slots) or a world's
-// shared-memory Δv (with world-local indices).
-__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int b1, int b2,
+// normal rows (sor_prox.rs:181-230). g1, g2 are the dynamic bodies' slots (-1:
+// no dofs); l1, l2 their rows in `dvbase`, the global Δv array (l = g) or a
+// world's shared-memory Δv (world-local indices).
+__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
                                               float* dvbase) {
-    const bool h1 = b1 >= 0, h2 = b2 >= 0;
+    const bool h1 = g1 >= 0, h2 = g2 >= 0;
     DV dv;
-    load_dv(dvbase, b1, dv.a);
-    load_dv(dvbase, b2, dv.b);
-    float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
-    const uint32_t nc = w.s.sm_nc[m];
-    if (sweep == 0) {
-        for (uint32_t k = 0; k < 3 * nc; ++k) {
-            float r[kRowFloats];
-            load_row(rows + k * kRowFloats, r);
-            float imp = r[RF_IMP];
-            if (imp != 0.0f) axpy(r, dv, imp, h1, h2);
-        }
-    } else if (sweep & 1u) {
-        for (uint32_t k = 0; k < nc; ++k) {
-            float li = rows[(3 * k) * kRowFloats + RF_IMP];
-            float rr[2][kRowFloats];
-            load_row(rows + (3 * k + 1) * kRowFloats, rr[0]);
-            load_row(rows + (3 * k + 2) * kRowFloats, rr[1]);
+    load_dv(dvbase, l1, dv.a);
+    load_dv(dvbase, l2, dv.b);
+    SB s1, s2;
+    if (h1) s1 = load_sb(w.b.sb, g1);
+    if (h2) s2 = load_sb(w.b.sb, g2);
+    const uint32_t nc = w.s.sm_nc[m], mask = w.s.sm_mask[m];
+    float4* lam = w.s.lam + (size_t)m * kMaxContacts;
+    const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+    for (uint32_t k = 0; k < nc; ++k) {
+        const ContactRec c = load_con(con, k);
+        float4 l = lam[k];
+        if (sweep == 0) {
+            np::V t[2];
+            tangent_basis(c.n, t[0], t[1]);
+            float li[3] = {l.x, l.y, l.z};
+#pragma unroll 1
+            for (int row = 0; row < 3; ++row) {
+                if (li[row] == 0.0f) continue;
+                axpy(row_dir(c, row, t), c.pos1, c.pos2, mask, s1, s2, dv, li[row], h1, h2);
+            }
+        } else if (sweep & 1u) {
+            np::V t[2];
+            tangent_basis(c.n, t[0], t[1]);
+            float li = l.x;
+            float imps[2] = {l.y, l.z};
 #pragma unroll
             for (int sdir = 0; sdir < 2; ++sdir) {
-                const float* r = rr[sdir];
-                float* rg = rows + (3 * k + 1 + sdir) * kRowFloats;
-                float imp = r[RF_IMP];
+                float imp = imps[sdir];
                 if (li == 0.0f) {
                     if (imp != 0.0f) {
-                        axpy(r, dv, -imp, h1, h2);
-                        rg[RF_IMP] = 0.0f;
+                        axpy(t[sdir], c.pos1, c.pos2, mask, s1, s2, dv, -imp, h1, h2);
+                        imps[sdir] = 0.0f;
                     }
                     continue;
                 }
-                float mx = r[RF_MU] * li, mn = -mx;
-                float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
-                float ni = imp - r[RF_R] * dimp;
+                float mx = c.mu * li, mn = -mx;
+                float dimp = jdot(t[sdir], c.pos1, c.pos2, mask, dv, h1, h2) + c.rhs[1 + sdir];
+                float ni = imp - c.r[1 + sdir] * dimp;
                 if (ni < mn) ni = mn;
                 else if (ni > mx) ni = mx;
                 float dl = ni - imp;
-                rg[RF_IMP] = ni;
-                axpy(r, dv, dl, h1, h2);
+                imps[sdir] = ni;
+                axpy(t[sdir], c.pos1, c.pos2, mask, s1, s2, dv, dl, h1, h2);
             }
-        }
-    } else {
-        for (uint32_t k = 0; k < nc; ++k) {
-            float r[kRowFloats];
-            float* rg = rows + (3 * k) * kRowFloats;
-            load_row(rg, r);
-            float imp = r[RF_IMP];
-            float dimp = jdot(r, dv, h1, h2) + r[RF_RHS];
-            float ni = imp - r[RF_R] * dimp;
+            lam[k] = make_float4(li, imps[0], imps[1], 0.0f);
+        } else {
+            const np::V dn = np::neg(c.n);
+            float imp = l.x;
+            float dimp = jdot(dn, c.pos1, c.pos2, mask, dv, h1, h2) + c.rhs[0];
+            float ni = imp - c.r[0] * dimp;
             ni = ni > 0.0f ? ni : 0.0f;
             float dl = ni - imp;
-            rg[RF_IMP] = ni;
-            axpy(r, dv, dl, h1, h2);
+            lam[k] = make_float4(ni, l.y, l.z, 0.0f);
+            axpy(dn, c.pos1, c.pos2, mask, s1, s2, dv, dl, h1, h2);
         }
     }
-    store_dv(dvbase, b1, dv.a);
-    store_dv(dvbase, b2, dv.b);
+    store_dv(dvbase, l1, dv.a);
+    store_dv(dvbase, l2, dv.b);
+}
+
+// FP64 residual terms of one manifold (normal rows, then friction rows with
+// the normal impulse as the limit).
+__device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, int g1, int g2, const DV& dv, double& s2,
+                                                  double& l2) {
+    const bool h1 = g1 >= 0, h2 = g2 >= 0;
+    const uint32_t nc = w.s.sm_nc[m], mask = w.s.sm_mask[m];
+    const float4* lam = w.s.lam + (size_t)m * kMaxContacts;
+    const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+    for (uint32_t k = 0; k < nc; ++k) {
+        const ContactRec c = load_con(con, k);
+        float4 l = lam[k];
+        np::V t[2];
+        tangent_basis(c.n, t[0], t[1]);
+        residual_row(np::neg(c.n), c.pos1, c.pos2, mask, c.r[0], c.rhs[0], l.x, dv, h1, h2, false, 0.0, c.mu, s2, l2);
+        residual_row(t[0], c.pos1, c.pos2, mask, c.r[1], c.rhs[1], l.y, dv, h1, h2, true, (double)l.x, c.mu, s2, l2);
+        residual_row(t[1], c.pos1, c.pos2, mask, c.r[2], c.rhs[2], l.z, dv, h1, h2, true, (double)l.x, c.mu, s2, l2);
+    }
 }
 
 // The dataflow tasks of one thread: its manifolds m = t + k T, with their
@@ -740,7 +837,7 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             fence_acq_rel();   // acquire: the bodies' latest dv is visible
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
-            velocity_task(w, t + k * T, sw, b1, b2, w.b.dv);
+            velocity_task(w, t + k * T, sw, b1, b2, b1, b2, w.b.dv);
             fence_acq_rel();   // release: dv and impulses before the new versions
             if (b1 >= 0) st_relaxed(w.b.vel_ver + b1, t1 + 1u);
             if (b2 >= 0) st_relaxed(w.b.vel_ver + b2, t2 + 1u);
@@ -768,17 +865,10 @@ __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t&
     double s2 = 0.0, l2 = 0.0;
     GRID_FOR(m, ms) {
         int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
-        uint32_t nc = w.s.sm_nc[m];
         DV dv;
         load_dv(w.b.dv, b1, dv.a);
         load_dv(w.b.dv, b2, dv.b);
-        const float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
-        for (uint32_t k = 0; k < nc; ++k) {
-            const float* rn = rows + (3 * k) * kRowFloats;
-            residual_row(rn, dv, b1 >= 0, b2 >= 0, false, 0.0, s2, l2);
-            residual_row(rn + kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
-            residual_row(rn + 2 * kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
-        }
+        manifold_residual(w, m, b1, b2, dv, s2, l2);
     }
     double ts = block_sum(s2, sh);
     double tl = block_sum(l2, sh);
@@ -798,12 +888,12 @@ __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t&
     return grid_sync(w.ctl, epoch);
 }
 
-__global__ void __launch_bounds__(kCoopThreads) k_velocity(World w, StepParams p) {
+__global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParams p) {
     __shared__ double sh[32];
     const uint32_t ms = w.ctl->nsolver;
     const uint32_t T = gridDim.x * blockDim.x;
     if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_TASKS);
         return;
     }
     const bool prof = p.profile != 0;
@@ -905,7 +995,8 @@ __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_
         for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
             uint32_t m = w.s.wm_order[i];
             int l1, l2;
-            if (world_locals(w, m, base, nbw, l1, l2)) velocity_task(w, m, sweep, l1, l2, s_dv);
+            if (world_locals(w, m, base, nbw, l1, l2))
+                velocity_task(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, s_dv);
         }
         __syncthreads();
     }
@@ -923,14 +1014,7 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
         DV dv;
         load_dv(s_dv, b1, dv.a);
         load_dv(s_dv, b2, dv.b);
-        const float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
-        uint32_t nc = w.s.sm_nc[m];
-        for (uint32_t k = 0; k < nc; ++k) {
-            const float* rn = rows + (3 * k) * kRowFloats;
-            residual_row(rn, dv, b1 >= 0, b2 >= 0, false, 0.0, s2, l2);
-            residual_row(rn + kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
-            residual_row(rn + 2 * kRowFloats, dv, b1 >= 0, b2 >= 0, true, (double)rn[RF_IMP], s2, l2);
-        }
+        manifold_residual(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, s2, l2);
     }
     double ts = block_sum(s2, sh);
     double tl = block_sum(l2, sh);
@@ -940,16 +1024,20 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
     }
 }
 
-// Persistent: each block takes worlds from a counter until none is left.
+// Persistent: each block takes worlds from a counter until none is left,
+// largest first, so that the last worlds to start are short ones.
 // Dynamic shared memory: 6 floats per body slot of the largest world.
-__global__ void __launch_bounds__(kWorldThreads) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
+__global__ void __launch_bounds__(kWorldThreads, 4) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
                                                                   uint32_t max_world_bodies) {
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
     __shared__ uint32_t s_world;
     const uint32_t ncol = w.ctl->ncolours;
     for (;;) {
-        if (threadIdx.x == 0) s_world = atomicAdd(&w.ctl->world_next[0], 1u);
+        if (threadIdx.x == 0) {
+            uint32_t k = atomicAdd(&w.ctl->world_next[0], 1u);
+            s_world = k < n_worlds ? w.s.world_order[k] : 0xffffffffu;
+        }
         __syncthreads();
         const uint32_t wd = s_world;
         if (wd >= n_worlds) break;
@@ -984,13 +1072,8 @@ __global__ void k_cache_integrate(World w, StepParams p) {
     const Bodies& b = w.b;
     GRID_FOR(m, ms) {
         uint32_t q = w.s.sm_list[m];
-        const float* rows = w.s.rows + (size_t)m * 12 * kRowFloats;
         uint32_t nc = w.s.sm_nc[m];
-        for (uint32_t k = 0; k < nc; ++k) {
-            float4 imp = make_float4(rows[(3 * k) * kRowFloats + RF_IMP], rows[(3 * k + 1) * kRowFloats + RF_IMP],
-                                     rows[(3 * k + 2) * kRowFloats + RF_IMP], 0.0f);
-            w.cur.imp[q * kMaxContacts + k] = imp;
-        }
+        for (uint32_t k = 0; k < nc; ++k) w.cur.imp[q * kMaxContacts + k] = w.s.lam[(size_t)m * kMaxContacts + k];
     }
     const float dt = p.dt;
     GRID_FOR(i, w.nb_slots) {
@@ -1092,7 +1175,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
-        if (t == 0) atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+        if (t == 0) atomicOr(&w.ctl->err, ERRF_TASKS);
         return;
     }
     const uint32_t nsw = p.max_position_iterations;
@@ -1135,7 +1218,10 @@ __global__ void __launch_bounds__(kWorldThreads) k_world_position(World w, StepP
     __shared__ uint32_t s_world;
     const uint32_t ncol = w.ctl->ncolours;
     for (;;) {
-        if (threadIdx.x == 0) s_world = atomicAdd(&w.ctl->world_next[1], 1u);
+        if (threadIdx.x == 0) {
+            uint32_t k = atomicAdd(&w.ctl->world_next[1], 1u);
+            s_world = k < n_worlds ? w.s.world_order[k] : 0xffffffffu;
+        }
         __syncthreads();
         const uint32_t wd = s_world;
         if (wd >= n_worlds) break;

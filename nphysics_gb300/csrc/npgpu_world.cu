@@ -105,8 +105,8 @@ struct npgpu_world {
     std::vector<HostBody> hb;
     std::vector<HostCollider> hc;
     uint32_t nb_slots = 0, nc_slots = 0, nc_alive = 0;
-    World dw;
-    Pairs pa, pb;
+    World dw{};                          // value-initialised: pointers not allocated at creation stay null
+    Pairs pa{}, pb{};
     Control* ctl = nullptr;
     cudaStream_t stream = nullptr;
     int device = 0;
@@ -139,8 +139,9 @@ struct npgpu_world {
     bool layout_dirty = true;
     bool layout_ok = false;              // the worlds qualify for the per-world schedule
     uint32_t n_worlds = 0, max_world_bodies = 0;
-    std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries
+    std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries, then the n_worlds largest-first order
     uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
+    bool layout_on_device = false;
     int grid_world = 0;
 };
 
@@ -252,6 +253,11 @@ static void compute_layout(npgpu_world* w) {
     uint32_t widest = 0;
     for (uint32_t k = 0; k < nw; ++k) widest = std::max(widest, st[k + 1] - st[k]);
     if (widest > kMaxWorldBodies) return;
+    std::vector<uint32_t> order(nw);
+    for (uint32_t k = 0; k < nw; ++k) order[k] = k;
+    std::stable_sort(order.begin(), order.end(),
+                     [&](uint32_t a, uint32_t b) { return st[a + 1] - st[a] > st[b + 1] - st[b]; });
+    st.insert(st.end(), order.begin(), order.end());
     w->world_start.swap(st);
     w->n_worlds = nw;
     w->max_world_bodies = widest;
@@ -261,8 +267,10 @@ static void compute_layout(npgpu_world* w) {
 // Chooses the schedule of this step and, for the per-world one, makes sure
 // the bucket buffers hold every world and the world ranges are on the device.
 static npgpu_status prepare_schedule(npgpu_world* w) {
-    const bool was_dirty = w->layout_dirty;
-    if (w->layout_dirty) compute_layout(w);
+    if (w->layout_dirty) {
+        compute_layout(w);
+        w->layout_on_device = false;
+    }
     const uint32_t sched = w->params.solver_schedule;
     w->solver.batched = w->layout_ok && sched != NPGPU_SCHEDULE_GRID && !w->params.solve_to_tolerance;
     if (!w->solver.batched) return NPGPU_OK;
@@ -273,10 +281,10 @@ static npgpu_status prepare_schedule(npgpu_world* w) {
         cudaFree(s.world_start);
         cudaFree(s.bucket_count);
         cudaFree(s.bucket_start);
-        s.world_start = s.bucket_count = s.bucket_start = s.bucket_cursor = nullptr;
+        s.world_start = s.world_order = s.bucket_count = s.bucket_start = s.bucket_cursor = nullptr;
         uint32_t cap = std::max(w->n_worlds, 2 * w->worlds_cap);
         size_t cbk = (size_t)cap * kMaxColours;
-        CK(cudaMalloc(&s.world_start, sizeof(uint32_t) * (cap + 1)), "world ranges");
+        CK(cudaMalloc(&s.world_start, sizeof(uint32_t) * (2 * (size_t)cap + 1)), "world ranges");
         CK(cudaMalloc(&s.bucket_count, sizeof(uint32_t) * (2 * cbk + 1)), "world buckets");
         CK(cudaMalloc(&s.bucket_start, sizeof(uint32_t) * (cbk + 1)), "world bucket starts");
         w->worlds_cap = cap;
@@ -293,8 +301,10 @@ static npgpu_status prepare_schedule(npgpu_world* w) {
         }
     }
     s.bucket_cursor = s.bucket_count + nbk + 1;
-    if (was_dirty) {
-        CK(cudaMemcpyAsync(s.world_start, w->world_start.data(), sizeof(uint32_t) * (w->n_worlds + 1),
+    s.world_order = s.world_start + w->n_worlds + 1;
+    if (!w->layout_on_device) {
+        w->layout_on_device = true;
+        CK(cudaMemcpyAsync(s.world_start, w->world_start.data(), sizeof(uint32_t) * (2 * (size_t)w->n_worlds + 1),
                            cudaMemcpyHostToDevice, w->stream),
            "world ranges");
         w->grid_world = world_grid(w->device, w->max_world_bodies, w->n_worlds);
@@ -344,7 +354,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(b.mass, B); A(b.local_I, 9 * (size_t)B); A(b.I, 9 * (size_t)B); A(b.inv_mass, B); A(b.inv_I, 9 * (size_t)B);
     A(b.acc_lin, B); A(b.acc_ang, B); A(b.f_lin, B); A(b.f_ang, B);
     A(b.lin_damp, B); A(b.ang_damp, B); A(b.max_lin, B); A(b.max_ang, B); A(b.sleep_thr, B); A(b.energy, B);
-    A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
+    A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
     A(b.used, B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B); A(b.col_cnt, B); A(b.vel_ver, B);
     A(b.pos_ver, B);
     Colliders& c = w->dw.c;
@@ -354,7 +364,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(c.keys, Cn); A(c.keys_sorted, Cn); A(c.vals, Cn); A(c.vals_sorted, Cn);
     A(c.left, Cn); A(c.right, Cn); A(c.parent, 2 * (size_t)Cn); A(c.node_min, 2 * (size_t)Cn);
     A(c.node_max, 2 * (size_t)Cn); A(c.node_flag, Cn); A(c.leaf_count, Cn); A(c.leaf_offset, Cn);
-    A(c.leaf_tmp, (size_t)kLeafCap * Cn);
+    A(c.leaf_tmp, (size_t)kLeafCap * Cn); A(c.node_world, 2 * (size_t)Cn);
     for (Pairs* pp : {&w->pa, &w->pb}) {
         A(pp->pair, P); A(pp->owner_start, Cn); A(pp->owner_count, Cn); A(pp->ncont, P);
         A(pp->key, 4 * (size_t)P); A(pp->w1, 4 * (size_t)P); A(pp->w2, 4 * (size_t)P); A(pp->n, 4 * (size_t)P);
@@ -362,7 +372,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     }
     Solver& s = w->dw.s;
     A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_prank, P); A(s.sm_rk, P); A(s.sm_b1, P); A(s.sm_b2, P);
-    A(s.sm_nc, P); A(s.rows, (size_t)P * 12 * kRowFloats); A(s.adj, 2 * (size_t)P); A(s.wm_order, P);
+    A(s.sm_nc, P); A(s.con, (size_t)P * kMaxContacts * 4); A(s.lam, (size_t)P * kMaxContacts); A(s.sm_mask, P); A(s.adj, 2 * (size_t)P); A(s.wm_order, P);
     A(w->ctl, 1);
     A(w->d_forget, Cn);
 #undef A
@@ -850,6 +860,8 @@ npgpu_status npgpu_synchronize(npgpu_world* w) {
         if (err & ERRF_NAN) return fail(w, NPGPU_ERR_NAN, "non-finite body state after the step");
         if (err & ERRF_PAIR_CAPACITY) return fail(w, NPGPU_ERR_CAPACITY, "pair capacity exceeded");
         if (err & ERRF_COLOURS) return fail(w, NPGPU_ERR_CAPACITY, "more than 64 solver colours needed");
+        if (err & ERRF_TASKS)
+            return fail(w, NPGPU_ERR_CAPACITY, "more solver manifolds than the cooperative grid holds (16 per thread)");
         if (err & ERRF_WORLD_RANGE) return fail(w, NPGPU_ERR_CUDA, "a solver manifold left its world's slot range");
     }
     return NPGPU_OK;

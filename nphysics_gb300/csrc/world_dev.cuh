@@ -7,8 +7,9 @@
 //  pairs      broad-phase pairs, double-buffered (current / previous step),
 //             4 contact slots per pair; the previous buffer feeds the impulse
 //             cache of the next narrow phase
-//  solver     one record per solver manifold, sorted by colour; 3 rows per
-//             contact (normal, tangent 1, tangent 2), 28 floats per row
+//  solver     one record per solver manifold; per contact 64 bytes of
+//             constant row data (normal, lever arms, r and rhs of the normal
+//             and two friction rows, friction) and 16 bytes of impulses
 #pragma once
 #include <cstdint>
 #include <cuda_runtime.h>
@@ -37,6 +38,7 @@ enum : uint32_t {
     ERRF_COLOURS = 1u << 3,
     ERRF_UNION_FIND = 1u << 4,
     ERRF_WORLD_RANGE = 1u << 5,      // a batched world's body outside its slot range
+    ERRF_TASKS = 1u << 6,            // more solver manifolds than a cooperative grid holds
 };
 
 constexpr int kMaxContacts = 4;      // contacts per manifold
@@ -62,6 +64,7 @@ struct Bodies {
     uint32_t *info;
     uint32_t *world;
     float *dv;                       // mj_lambda, 6 per body
+    float4 *sb;                      // 3 per body: inverse augmented mass as the solver reads it
     uint32_t *uf_parent;
     int *can_deact;
     unsigned long long *used;        // colours of the body's solver manifolds (one bit each)
@@ -86,6 +89,7 @@ struct Colliders {
     int *node_flag;
     uint32_t *leaf_count, *leaf_offset;
     uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
+    uint32_t *node_world;            // worlds under a node: first << 16 | last (leaves sort by world first)
 };
 enum : uint32_t { CI_ALIVE = 1u << 16 };
 
@@ -108,10 +112,13 @@ struct Solver {
     uint32_t *sm_rk;                 // colour rank / manifold count on body 1 and body 2 (8 bits each)
     int *sm_b1, *sm_b2;              // dynamic body slots (-1 when the side has no dofs)
     uint32_t *sm_nc;
-    float *rows;                     // 12 rows per solver manifold
+    float4 *con;                     // 4 contacts x 4 float4 per solver manifold (constant during the solve)
+    float4 *lam;                     // 4 contacts per solver manifold: impulses (normal, tangent 1, tangent 2)
+    uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13)
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
     // Batched worlds: manifolds bucketed by (world, colour).
     uint32_t *world_start;           // body slot range of each world (n_worlds + 1)
+    uint32_t *world_order;           // worlds by decreasing slot range: the order blocks take them in
     // bucket_count (n_worlds * kMaxColours + 1) and bucket_cursor follow each
     // other in one allocation, cleared by one memset each step.
     uint32_t *bucket_count, *bucket_start, *bucket_cursor;
