@@ -64,6 +64,53 @@ __device__ __forceinline__ void st_relaxed(uint32_t* p, uint32_t v) {
     asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 __device__ __forceinline__ void fence_acq_rel() { asm volatile("fence.acq_rel.gpu;" ::: "memory"); }
+
+// Flagged Δv of the dataflow velocity solver: per body 8 words of 64 bits
+// (6 used), each = update count << 32 | float bits. A 64-bit aligned word is
+// written and read as a whole, so a reader that finds the expected count in
+// all six words holds the Δv of exactly that update, with no fence on either
+// side: the count is the flag.
+__device__ __forceinline__ bool poll_dvf(const unsigned long long* dvf, int b, uint32_t t, float* out) {
+    if (b < 0) return true;
+    const unsigned long long* p = dvf + 8 * (size_t)b;
+    unsigned long long w0, w1, w2, w3, w4, w5;
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w0), "=l"(w1) : "l"(p) : "memory");
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w2), "=l"(w3) : "l"(p + 2) : "memory");
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w4), "=l"(w5) : "l"(p + 4) : "memory");
+    const unsigned long long w[6] = {w0, w1, w2, w3, w4, w5};
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        ok = ok && (uint32_t)(w[k] >> 32) == t;
+        out[k] = __uint_as_float((uint32_t)w[k]);
+    }
+    return ok;
+}
+// The Δv part of a body's flagged words (after a grid-wide sync).
+__device__ __forceinline__ void load_dvf(const unsigned long long* dvf, int b, float* out) {
+    if (b < 0) return;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) out[k] = __uint_as_float((uint32_t)__ldcg(dvf + 8 * (size_t)b + k));
+}
+__device__ __forceinline__ void publish_dvf(unsigned long long* dvf, int b, uint32_t t, const float* v) {
+    if (b < 0) return;
+    unsigned long long* p = dvf + 8 * (size_t)b;
+    const unsigned long long hi = (unsigned long long)t << 32;
+    unsigned long long w[6];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) w[k] = hi | __float_as_uint(v[k]);
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(w[0]), "l"(w[1]) : "memory");
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p + 2), "l"(w[2]), "l"(w[3]) : "memory");
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p + 4), "l"(w[4]), "l"(w[5]) : "memory");
+}
+
+// Both bodies' update counters at their expected values (a body < 0 has no
+// counter); the two loads are in flight together.
+__device__ __forceinline__ bool versions_ready(const uint32_t* ver, int b1, uint32_t t1, int b2, uint32_t t2) {
+    uint32_t v1 = b1 >= 0 ? ld_relaxed(ver + b1) : t1;
+    uint32_t v2 = b2 >= 0 ? ld_relaxed(ver + b2) : t2;
+    return v1 == t1 && v2 == t2;
+}
 __device__ __forceinline__ bool err_set(const Control* ctl, uint32_t bits) {
     return (ld_acquire(&ctl->err) & bits) != 0;
 }
@@ -97,13 +144,17 @@ __device__ __forceinline__ bool grid_sync(Control* ctl, uint32_t& epoch) {
     return s_ok != 0;
 }
 
-// Backs off while a whole warp waits: 32 ns doubling up to 1 us, so that
+// Backs off while a whole warp waits: 32 ns doubling up to 256 ns, so that
 // waiting warps do not crowd the L2 that the running ones need. Called by all
-// 32 lanes together; the decision is warp-uniform. Returns false on timeout.
+// 32 lanes together; the decision is warp-uniform. The time limit and the
+// error word are looked at every 64th wait. Returns false on timeout.
 __device__ __forceinline__ bool warp_wait_backoff(const Control* ctl, unsigned long long& t0, unsigned& backoff) {
     if (t0 == 0) t0 = global_ns();
-    __nanosleep(backoff);
-    backoff = backoff < 1024u ? backoff * 2u : 1024u;
+    __nanosleep(backoff & 0xffffu);
+    unsigned waits = (backoff >> 16) + 1u;
+    unsigned ns = backoff & 0xffffu;
+    backoff = ((waits & 0xffffu) << 16) | (ns < 256u ? ns * 2u : 256u);
+    if ((waits & 63u) != 0u) return true;
     bool give_up = err_set(ctl, ERRF_TIMEOUT) || global_ns() - t0 > kWaitLimitNs;
     if (__any_sync(0xffffffffu, give_up)) {
         if ((threadIdx.x & 31u) == 0u) atomicOr((uint32_t*)&ctl->err, ERRF_TIMEOUT);
@@ -303,10 +354,17 @@ __device__ __forceinline__ float jdot(np::V dir, np::V pos1, np::V pos2, uint32_
     return 0.0f;
 }
 
-__device__ __forceinline__ void axpy(np::V dir, np::V pos1, np::V pos2, uint32_t mask, const SB& s1, const SB& s2,
-                                     DV& dv, float a, bool has1, bool has2) {
-    if (has1) side_axpy(pos1, dir, mask & 0x3fu, s1, a, dv.a);
-    if (has2) side_axpy(pos2, np::neg(dir), (mask >> 8) & 0x3fu, s2, a, dv.b);
+// Inverse masses of a task's two bodies, held in registers.
+struct BodyMasses {
+    SB s[2];
+    __device__ __forceinline__ SB get(int side) const { return s[side]; }
+};
+
+template <class BM>
+__device__ __forceinline__ void axpy(np::V dir, np::V pos1, np::V pos2, uint32_t mask, const BM& bm, DV& dv, float a,
+                                     bool has1, bool has2) {
+    if (has1) side_axpy(pos1, dir, mask & 0x3fu, bm.get(0), a, dv.a);
+    if (has2) side_axpy(pos2, np::neg(dir), (mask >> 8) & 0x3fu, bm.get(1), a, dv.b);
 }
 
 // One contact of a solver manifold: 4 float4 (64 bytes), constant during the
@@ -398,6 +456,8 @@ __global__ void k_act_init(World w, StepParams p) {
         b.vel_ver[i] = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) b.dv[6 * i + k] = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 8; ++k) b.dvf[8 * i + k] = 0ull;   // Δv 0 at update count 0
         if ((info & BI_ALIVE) && bi_status(info) == 2u) {
             const float* iI = b.inv_I + 9 * i;
             float im = b.inv_mass[i];
@@ -592,8 +652,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             int b1 = mb1[k], b2 = mb2[k];
             uint32_t pr = mpr[k];
             uint32_t r1 = pr & 0xffffu, r2 = pr >> 16;
-            if (b1 >= 0 && ld_relaxed(b.col_cnt + b1) != r1) continue;
-            if (b2 >= 0 && ld_relaxed(b.col_cnt + b2) != r2) continue;
+            if (!versions_ready(b.col_cnt, b1, r1, b2, r2)) continue;
             fence_acq_rel();
             unsigned long long mask = 0ull;
             if (b1 >= 0) mask |= b.used[b1];
@@ -696,38 +755,79 @@ __device__ __forceinline__ np::V row_dir(const ContactRec& c, int row, const np:
     return row == 0 ? np::neg(c.n) : t[row - 1];
 }
 
+// Where a velocity task reads its contacts: global memory, or the running
+// thread's slice of a shared-memory cache (element e at base[e * blockDim.x],
+// so that the lanes of a warp read consecutive float4).
+struct GlobalContacts {
+    const float4* con;
+    float4* lam;
+    __device__ __forceinline__ ContactRec rec(uint32_t k) const { return load_con(con, k); }
+    __device__ __forceinline__ void tangents(const ContactRec& c, uint32_t, np::V* t) const {
+        tangent_basis(c.n, t[0], t[1]);
+    }
+    __device__ __forceinline__ float4 get_lam(uint32_t k) const { return lam[k]; }
+    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { lam[k] = v; }
+};
+
+// Shared-memory cache of one task: 3 + 3 float4 of inverse mass, then per
+// contact its 4 record float4, the two tangents and the impulses.
+constexpr int kCacheContacts = 2;
+constexpr int kCacheF4 = 6 + 7 * kCacheContacts;
+struct CachedContacts {
+    float4* base;
+    __device__ __forceinline__ float4& at(int e) const { return base[e * (int)blockDim.x]; }
+    __device__ __forceinline__ ContactRec rec(uint32_t k) const {
+        float4 c0 = at(6 + 7 * k), c1 = at(7 + 7 * k), c2 = at(8 + 7 * k), c3 = at(9 + 7 * k);
+        ContactRec c;
+        c.n = np::mk(c0.x, c0.y, c0.z);
+        c.mu = c0.w;
+        c.pos1 = np::mk(c1.x, c1.y, c1.z);
+        c.r[0] = c1.w;
+        c.pos2 = np::mk(c2.x, c2.y, c2.z);
+        c.rhs[0] = c2.w;
+        c.r[1] = c3.x; c.rhs[1] = c3.y; c.r[2] = c3.z; c.rhs[2] = c3.w;
+        return c;
+    }
+    __device__ __forceinline__ void tangents(const ContactRec&, uint32_t k, np::V* t) const {
+        float4 a = at(10 + 7 * k), b = at(11 + 7 * k);
+        t[0] = np::mk(a.x, a.y, a.z);
+        t[1] = np::mk(b.x, b.y, b.z);
+    }
+    __device__ __forceinline__ float4 get_lam(uint32_t k) const { return at(12 + 7 * k); }
+    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { at(12 + 7 * k) = v; }
+    __device__ __forceinline__ SB get(int side) const {
+        SB s;
+        float4 a = at(3 * side), b = at(3 * side + 1), c = at(3 * side + 2);
+        s.I.m[0][0] = a.x; s.I.m[0][1] = a.y; s.I.m[0][2] = a.z;
+        s.I.m[1][0] = b.x; s.I.m[1][1] = b.y; s.I.m[1][2] = b.z;
+        s.I.m[2][0] = c.x; s.I.m[2][1] = c.y; s.I.m[2][2] = c.z;
+        s.im = a.w;
+        return s;
+    }
+};
+
 // One velocity task: sweep 0 is the warm start (sor_prox.rs:19-45), odd sweeps
 // the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
-// normal rows (sor_prox.rs:181-230). g1, g2 are the dynamic bodies' slots (-1:
-// no dofs); l1, l2 their rows in `dvbase`, the global Δv array (l = g) or a
-// world's shared-memory Δv (world-local indices).
-__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
-                                              float* dvbase) {
-    const bool h1 = g1 >= 0, h2 = g2 >= 0;
-    DV dv;
-    load_dv(dvbase, l1, dv.a);
-    load_dv(dvbase, l2, dv.b);
-    SB s1, s2;
-    if (h1) s1 = load_sb(w.b.sb, g1);
-    if (h2) s2 = load_sb(w.b.sb, g2);
-    const uint32_t nc = w.s.sm_nc[m], mask = w.s.sm_mask[m];
-    float4* lam = w.s.lam + (size_t)m * kMaxContacts;
-    const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+// normal rows (sor_prox.rs:181-230). l1, l2 are the dynamic bodies' rows in
+// `dvbase` (-1: no dofs), the global Δv array or a world's shared-memory Δv.
+template <class Src, class BM>
+__device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, uint32_t mask, uint32_t sweep,
+                                                  const BM& bm, bool h1, bool h2, DV& dv) {
     for (uint32_t k = 0; k < nc; ++k) {
-        const ContactRec c = load_con(con, k);
-        float4 l = lam[k];
+        const ContactRec c = src.rec(k);
+        float4 l = src.get_lam(k);
         if (sweep == 0) {
             np::V t[2];
-            tangent_basis(c.n, t[0], t[1]);
+            src.tangents(c, k, t);
             float li[3] = {l.x, l.y, l.z};
 #pragma unroll 1
             for (int row = 0; row < 3; ++row) {
                 if (li[row] == 0.0f) continue;
-                axpy(row_dir(c, row, t), c.pos1, c.pos2, mask, s1, s2, dv, li[row], h1, h2);
+                axpy(row_dir(c, row, t), c.pos1, c.pos2, mask, bm, dv, li[row], h1, h2);
             }
         } else if (sweep & 1u) {
             np::V t[2];
-            tangent_basis(c.n, t[0], t[1]);
+            src.tangents(c, k, t);
             float li = l.x;
             float imps[2] = {l.y, l.z};
 #pragma unroll
@@ -735,7 +835,7 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
                 float imp = imps[sdir];
                 if (li == 0.0f) {
                     if (imp != 0.0f) {
-                        axpy(t[sdir], c.pos1, c.pos2, mask, s1, s2, dv, -imp, h1, h2);
+                        axpy(t[sdir], c.pos1, c.pos2, mask, bm, dv, -imp, h1, h2);
                         imps[sdir] = 0.0f;
                     }
                     continue;
@@ -747,9 +847,9 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
                 else if (ni > mx) ni = mx;
                 float dl = ni - imp;
                 imps[sdir] = ni;
-                axpy(t[sdir], c.pos1, c.pos2, mask, s1, s2, dv, dl, h1, h2);
+                axpy(t[sdir], c.pos1, c.pos2, mask, bm, dv, dl, h1, h2);
             }
-            lam[k] = make_float4(li, imps[0], imps[1], 0.0f);
+            src.set_lam(k, make_float4(li, imps[0], imps[1], 0.0f));
         } else {
             const np::V dn = np::neg(c.n);
             float imp = l.x;
@@ -757,12 +857,46 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
             float ni = imp - c.r[0] * dimp;
             ni = ni > 0.0f ? ni : 0.0f;
             float dl = ni - imp;
-            lam[k] = make_float4(ni, l.y, l.z, 0.0f);
-            axpy(dn, c.pos1, c.pos2, mask, s1, s2, dv, dl, h1, h2);
+            src.set_lam(k, make_float4(ni, l.y, l.z, 0.0f));
+            axpy(dn, c.pos1, c.pos2, mask, bm, dv, dl, h1, h2);
         }
     }
-    store_dv(dvbase, l1, dv.a);
-    store_dv(dvbase, l2, dv.b);
+}
+
+// Velocity task of manifold m read from global memory; g1, g2 are the dynamic
+// bodies' slots (-1: no dofs), l1, l2 their Δv rows.
+__device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
+                                              float* dvbase) {
+    BodyMasses bm;
+    if (g1 >= 0) bm.s[0] = load_sb(w.b.sb, g1);
+    if (g2 >= 0) bm.s[1] = load_sb(w.b.sb, g2);
+    GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
+    DV dv;
+    load_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
+    load_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
+    velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv);
+    store_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
+    store_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
+}
+
+// Fills the running thread's cache with manifold m (nc <= kCacheContacts).
+__device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t nc, int b1, int b2,
+                                           const CachedContacts& cc) {
+    for (int side = 0; side < 2; ++side) {
+        int b = side == 0 ? b1 : b2;
+        if (b < 0) continue;
+        for (int e = 0; e < 3; ++e) cc.at(3 * side + e) = w.b.sb[3 * b + e];
+    }
+    const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+    for (uint32_t k = 0; k < nc; ++k) {
+        ContactRec c = load_con(con, k);
+        for (int e = 0; e < 4; ++e) cc.at(6 + 7 * k + e) = con[4 * k + e];
+        np::V t[2];
+        tangent_basis(c.n, t[0], t[1]);
+        cc.at(10 + 7 * k) = make_float4(t[0].x, t[0].y, t[0].z, 0.0f);
+        cc.at(11 + 7 * k) = make_float4(t[1].x, t[1].y, t[1].z, 0.0f);
+        cc.at(12 + 7 * k) = w.s.lam[(size_t)m * kMaxContacts + k];
+    }
 }
 
 // FP64 residual terms of one manifold (normal rows, then friction rows with
@@ -813,14 +947,28 @@ struct TaskStats {
 };
 
 __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
-                                TaskStats& ts) {
+                                TaskStats& ts, float4* cache) {
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     MyTasks mt;
     load_tasks(w, ms, mt, s_begin);
+    // The first task's contacts, inverse masses and tangents stay in shared
+    // memory for the whole call, its impulses too (written back at the end).
+    const CachedContacts cc{cache + threadIdx.x};
+    uint32_t nc0 = 0, mask0 = 0;
+    bool cached = false;
+    if (mt.n > 0 && cache != nullptr) {
+        nc0 = w.s.sm_nc[t];
+        if (nc0 <= (uint32_t)kCacheContacts) {
+            cached = true;
+            mask0 = w.s.sm_mask[t];
+            cache_task(w, t, nc0, mt.b1[0], mt.b2[0], cc);
+        }
+    }
     uint32_t left = mt.n * (s_end - s_begin);
     unsigned long long t0 = 0, tw = prof ? global_ns() : 0ull;
     unsigned backoff = 32;
+    bool ok = true;
     // Warp-uniform loop: each pass, the lanes whose next task is ready run it
     // together; the warp sleeps only when no lane could run anything.
     while (__any_sync(0xffffffffu, left > 0)) {
@@ -832,15 +980,24 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
-            if (b1 >= 0 && ld_relaxed(w.b.vel_ver + b1) != t1) continue;
-            if (b2 >= 0 && ld_relaxed(w.b.vel_ver + b2) != t2) continue;
-            fence_acq_rel();   // acquire: the bodies' latest dv is visible
+            DV dv;
+            bool r1 = poll_dvf(w.b.dvf, b1, t1, dv.a);
+            bool r2 = poll_dvf(w.b.dvf, b2, t2, dv.b);
+            if (!(r1 && r2)) continue;
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
-            velocity_task(w, t + k * T, sw, b1, b2, b1, b2, w.b.dv);
-            fence_acq_rel();   // release: dv and impulses before the new versions
-            if (b1 >= 0) st_relaxed(w.b.vel_ver + b1, t1 + 1u);
-            if (b2 >= 0) st_relaxed(w.b.vel_ver + b2, t2 + 1u);
+            if (k == 0 && cached) {
+                velocity_task_src(cc, nc0, mask0, sw, cc, b1 >= 0, b2 >= 0, dv);
+            } else {
+                const uint32_t m = t + k * T;
+                BodyMasses bm;
+                if (b1 >= 0) bm.s[0] = load_sb(w.b.sb, b1);
+                if (b2 >= 0) bm.s[1] = load_sb(w.b.sb, b2);
+                GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
+                velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv);
+            }
+            publish_dvf(w.b.dvf, b1, t1 + 1u, dv.a);
+            publish_dvf(w.b.dvf, b2, t2 + 1u, dv.b);
             if (prof) {
                 tw = global_ns();
                 ts.exec_ns += tw - te;
@@ -854,10 +1011,13 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             t0 = 0;
             backoff = 32;
         } else if (!warp_wait_backoff(w.ctl, t0, backoff)) {
-            return false;
+            ok = false;
+            break;
         }
     }
-    return true;
+    if (cached)
+        for (uint32_t k = 0; k < nc0; ++k) w.s.lam[(size_t)t * kMaxContacts + k] = cc.get_lam(k);
+    return ok;
 }
 
 // FP64 residual over all rows; the result lands in ctl->residual.
@@ -866,8 +1026,8 @@ __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t&
     GRID_FOR(m, ms) {
         int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
         DV dv;
-        load_dv(w.b.dv, b1, dv.a);
-        load_dv(w.b.dv, b2, dv.b);
+        load_dvf(w.b.dvf, b1, dv.a);
+        load_dvf(w.b.dvf, b2, dv.b);
         manifold_residual(w, m, b1, b2, dv, s2, l2);
     }
     double ts = block_sum(s2, sh);
@@ -890,6 +1050,7 @@ __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t&
 
 __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParams p) {
     __shared__ double sh[32];
+    extern __shared__ float4 s_cache[];   // kCacheF4 per thread
     const uint32_t ms = w.ctl->nsolver;
     const uint32_t T = gridDim.x * blockDim.x;
     if ((ms + T - 1) / T > (uint32_t)kMaxPerThread) {
@@ -901,25 +1062,27 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
     unsigned long long k0 = 0;
     if (prof && blockIdx.x == 0 && threadIdx.x == 0) k0 = global_ns();
     uint32_t epoch = 0;
-    if (!velocity_sweeps(w, 0, 1, ms, prof, ts)) return;
+    if (!velocity_sweeps(w, 0, 1, ms, prof, ts, s_cache)) return;
     if (!grid_sync(w.ctl, epoch)) return;
     if (!eval_residual(w, ms, sh, epoch, true)) return;
     uint32_t iters = 0;
     if (!p.solve_to_tolerance) {
         iters = p.max_velocity_iterations;
-        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms, prof, ts)) return;
+        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms, prof, ts, s_cache)) return;
         if (!grid_sync(w.ctl, epoch)) return;
         if (!eval_residual(w, ms, sh, epoch, false)) return;
     } else {
         for (uint32_t it = 0; it < p.max_iterations_to_tolerance; ++it) {
             if (((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
-            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms, prof, ts)) return;
+            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms, prof, ts, s_cache)) return;
             ++iters;
             if (!grid_sync(w.ctl, epoch)) return;
             if (!eval_residual(w, ms, sh, epoch, false)) return;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->iterations = iters;
+    // The solved Δv of every body, for the integration that follows.
+    GRID_FOR(i, w.nb_slots) load_dvf(w.b.dvf, (int)i, w.b.dv + 6 * i);
     if (prof) {
         if (ts.tasks) {
             atomicAdd(&w.ctl->task_ns, ts.exec_ns);
@@ -1193,8 +1356,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
             uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
-            if (b1 >= 0 && ld_relaxed(w.b.pos_ver + b1) != t1) continue;
-            if (b2 >= 0 && ld_relaxed(w.b.pos_ver + b2) != t2) continue;
+            if (!versions_ready(w.b.pos_ver, b1, t1, b2, t2)) continue;
             fence_acq_rel();
             position_task(w, p, t + k * T);
             fence_acq_rel();
@@ -1281,12 +1443,15 @@ static unsigned item_blocks(uint32_t n) {
     return b;
 }
 
+static const size_t kVelocitySmem = (size_t)kCoopThreads * kCacheF4 * sizeof(float4);
+
 void solver_grid_sizes(int device, SolverLaunch& L) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_colour, kCoopThreads, 0);
     L.grid_colour = sms * (per < 1 ? 1 : per);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_velocity, kCoopThreads, 0);
+    cudaFuncSetAttribute(k_velocity, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVelocitySmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_velocity, kCoopThreads, kVelocitySmem);
     L.grid_velocity = sms * (per < 1 ? 1 : per);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_position, kCoopThreads, 0);
     L.grid_position = sms * (per < 1 ? 1 : per);
@@ -1304,8 +1469,8 @@ int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds) {
     return g < 1 ? 1 : (int)g;
 }
 
-static cudaError_t coop(const void* fn, int grid, void** args, cudaStream_t st) {
-    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kCoopThreads), args, 0, st);
+static cudaError_t coop(const void* fn, int grid, void** args, cudaStream_t st, size_t smem = 0) {
+    return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kCoopThreads), args, smem, st);
 }
 
 cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st) {
@@ -1351,7 +1516,7 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
-        e = coop((const void*)k_velocity, L.grid_velocity, args2, st);
+        e = coop((const void*)k_velocity, L.grid_velocity, args2, st, kVelocitySmem);
         if (e != cudaSuccess) return e;
     }
     rec(4);
