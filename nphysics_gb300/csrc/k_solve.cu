@@ -1229,8 +1229,62 @@ __global__ void k_world_finish(World w, StepParams p) {
     c->iterations = p.max_velocity_iterations;
 }
 
+// A body pose as the position solver moves it.
+struct Pose {
+    np::V t, com;
+    np::Q q;
+};
+
+__device__ __forceinline__ Pose load_pose(const Bodies& b, uint32_t i) {
+    return Pose{v3(b.pos_t[i]), v3(b.com[i]), q4(b.pos_q[i])};
+}
+__device__ __forceinline__ void store_pose(const Bodies& b, uint32_t i, const Pose& P) {
+    b.pos_t[i] = f4(P.t);
+    b.pos_q[i] = f4q(P.q);
+    b.com[i] = f4(P.com);
+    atomicOr(&b.info[i], BI_CHANGED);
+}
+
+// Flagged poses of the dataflow position solver: per body 12 words of 64 bits
+// (10 used: translation, centre of mass, rotation), each = update count << 32
+// | float bits, the same protocol as the flagged Δv; word 10 holds the moved
+// flag in its float bits.
+__device__ __forceinline__ bool poll_posef(const unsigned long long* pf, int b, uint32_t t, Pose& P, bool& moved) {
+    const unsigned long long* p = pf + 12 * (size_t)b;
+    unsigned long long w[12];
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(w[2 * k]), "=l"(w[2 * k + 1]) : "l"(p + 2 * k)
+                     : "memory");
+    bool ok = true;
+#pragma unroll
+    for (int k = 0; k < 11; ++k) ok = ok && (uint32_t)(w[k] >> 32) == t;
+    float f[10];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) f[k] = __uint_as_float((uint32_t)w[k]);
+    P.t = np::mk(f[0], f[1], f[2]);
+    P.com = np::mk(f[3], f[4], f[5]);
+    P.q = np::Q{f[6], f[7], f[8], f[9]};
+    moved = (uint32_t)w[10] != 0u;
+    return ok;
+}
+__device__ __forceinline__ void publish_posef(unsigned long long* pf, int b, uint32_t t, const Pose& P, bool moved) {
+    unsigned long long* p = pf + 12 * (size_t)b;
+    const unsigned long long hi = (unsigned long long)t << 32;
+    const float f[10] = {P.t.x, P.t.y, P.t.z, P.com.x, P.com.y, P.com.z, P.q.i, P.q.j, P.q.k, P.q.w};
+    unsigned long long w[12];
+#pragma unroll
+    for (int k = 0; k < 10; ++k) w[k] = hi | __float_as_uint(f[k]);
+    w[10] = hi | (moved ? 1u : 0u);
+    w[11] = 0ull;
+#pragma unroll
+    for (int k = 0; k < 6; ++k)
+        asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p + 2 * k), "l"(w[2 * k]), "l"(w[2 * k + 1])
+                     : "memory");
+}
+
 // ================================================================ integrate
-__global__ void k_cache_integrate(World w, StepParams p) {
+__global__ void k_cache_integrate(World w, StepParams p, bool posef) {
     const uint32_t ms = w.ctl->nsolver;
     const Bodies& b = w.b;
     GRID_FOR(m, ms) {
@@ -1251,11 +1305,17 @@ __global__ void k_cache_integrate(World w, StepParams p) {
         b.ang[i] = f4(ang);
         b.info[i] = info | BI_CHANGED;
         body_integrate(b, i, dt);
+        if (posef) publish_posef(b.posef, (int)i, 0u, load_pose(b, i), false);
     }
 }
 
 // ================================================================ NonlinearSORProx
-__device__ __forceinline__ void position_task(const World& w, const StepParams& p, uint32_t m) {
+// NonlinearSORProx::solve_unilateral for the contacts of manifold m
+// (nonlinear_sor_prox.rs:121-154), on the two bodies' poses P1, P2 (the
+// poses of sides without dofs are not changed). moved1 / moved2 report a
+// displacement.
+__device__ __forceinline__ void position_core(const World& w, const StepParams& p, uint32_t m, Pose& P1, Pose& P2,
+                                              bool& moved1, bool& moved2) {
     const Bodies& b = w.b;
     const Colliders& c = w.c;
     uint32_t q = w.s.sm_list[m];
@@ -1264,9 +1324,9 @@ __device__ __forceinline__ void position_task(const World& w, const StepParams& 
     uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
     uint32_t i1 = b.info[bb1], i2 = b.info[bb2];
     bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
-    np::V t1 = v3(b.pos_t[bb1]), t2 = v3(b.pos_t[bb2]);
-    np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
-    np::V com1 = v3(b.com[bb1]), com2 = v3(b.com[bb2]);
+    np::V t1 = P1.t, t2 = P2.t;
+    np::Q q1 = P1.q, q2 = P2.q;
+    np::V com1 = P1.com, com2 = P2.com;
     np::V lc1 = v3(b.local_com[bb1]), lc2 = v3(b.local_com[bb2]);
     float im1 = b.inv_mass[bb1], im2 = b.inv_mass[bb2];
     np::M iI1 = load_m9(b.inv_I + 9 * bb1), iI2 = load_m9(b.inv_I + 9 * bb2);
@@ -1277,7 +1337,7 @@ __device__ __forceinline__ void position_task(const World& w, const StepParams& 
     float dil1 = (sh1 == SHAPE_BALL ? pp1.x : 0.0f) + c.margin[c1];
     float dil2 = (sh2 == SHAPE_BALL ? pp2.x : 0.0f) + c.margin[c2];
     uint32_t nc = w.cur.ncont[q];
-    bool moved1 = false, moved2 = false;
+    moved1 = moved2 = false;
     for (uint32_t k = 0; k < nc; ++k) {
         uint32_t slot = q * kMaxContacts + k;
         uint32_t key = w.cur.key[slot];
@@ -1319,18 +1379,20 @@ __device__ __forceinline__ void position_task(const World& w, const StepParams& 
             moved2 = true;
         }
     }
-    if (moved1) {
-        b.pos_t[bb1] = f4(t1);
-        b.pos_q[bb1] = f4q(q1);
-        b.com[bb1] = f4(com1);
-        b.info[bb1] = i1 | BI_CHANGED;
-    }
-    if (moved2) {
-        b.pos_t[bb2] = f4(t2);
-        b.pos_q[bb2] = f4q(q2);
-        b.com[bb2] = f4(com2);
-        b.info[bb2] = i2 | BI_CHANGED;
-    }
+    P1.t = t1; P1.q = q1; P1.com = com1;
+    P2.t = t2; P2.q = q2; P2.com = com2;
+}
+
+// Position task on poses in global memory (one block per world, where
+// __syncthreads orders the tasks of successive colours).
+__device__ __forceinline__ void position_task(const World& w, const StepParams& p, uint32_t m) {
+    uint2 pr = w.cur.pair[w.s.sm_list[m]];
+    uint32_t bb1 = w.c.body[pr.x], bb2 = w.c.body[pr.y];
+    Pose P1 = load_pose(w.b, bb1), P2 = load_pose(w.b, bb2);
+    bool moved1, moved2;
+    position_core(w, p, m, P1, P2, moved1, moved2);
+    if (moved1) store_pose(w.b, bb1, P1);
+    if (moved2) store_pose(w.b, bb2, P2);
 }
 
 __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p) {
@@ -1356,12 +1418,22 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
             uint32_t rk = mt.rk[k];
             uint32_t t1 = sw * ((rk >> 8) & 0xffu) + (rk & 0xffu);
             uint32_t t2 = sw * (rk >> 24) + ((rk >> 16) & 0xffu);
-            if (!versions_ready(w.b.pos_ver, b1, t1, b2, t2)) continue;
-            fence_acq_rel();
-            position_task(w, p, t + k * T);
-            fence_acq_rel();
-            if (b1 >= 0) st_relaxed(w.b.pos_ver + b1, t1 + 1u);
-            if (b2 >= 0) st_relaxed(w.b.pos_ver + b2, t2 + 1u);
+            const uint32_t m = t + k * T;
+            Pose P1, P2;
+            bool mv1 = false, mv2 = false;
+            bool r1 = true, r2 = true;
+            if (b1 >= 0) r1 = poll_posef(w.b.posef, b1, t1, P1, mv1);
+            if (b2 >= 0) r2 = poll_posef(w.b.posef, b2, t2, P2, mv2);
+            if (!(r1 && r2)) continue;
+            if (b1 < 0 || b2 < 0) {
+                uint2 pr = w.cur.pair[w.s.sm_list[m]];
+                if (b1 < 0) P1 = load_pose(w.b, w.c.body[pr.x]);
+                if (b2 < 0) P2 = load_pose(w.b, w.c.body[pr.y]);
+            }
+            bool n1, n2;
+            position_core(w, p, m, P1, P2, n1, n2);
+            if (b1 >= 0) publish_posef(w.b.posef, b1, t1 + 1u, P1, mv1 || n1);
+            if (b2 >= 0) publish_posef(w.b.posef, b2, t2 + 1u, P2, mv2 || n2);
             mt.next[k] = (uint16_t)(sw + 1u);
             --left;
             progress = true;
@@ -1401,7 +1473,7 @@ __global__ void __launch_bounds__(kWorldThreads) k_world_position(World w, StepP
 }
 
 // ================================================================ post
-__global__ void k_post(World w, StepParams p) {
+__global__ void k_post(World w, StepParams p, bool posef) {
     __shared__ double sh[32];
     const Bodies& b = w.b;
     double ke = 0.0;
@@ -1409,6 +1481,17 @@ __global__ void k_post(World w, StepParams p) {
         uint32_t info = b.info[i];
         if (!(info & BI_ALIVE)) continue;
         uint32_t st = bi_status(info);
+        if (posef && st == 2u && (info & BI_ISLAND)) {
+            // The dataflow position solver's result.
+            Pose P;
+            bool moved;
+            poll_posef(b.posef, (int)i, 0u, P, moved);
+            if (moved) {
+                b.pos_t[i] = f4(P.t);
+                b.pos_q[i] = f4q(P.q);
+                b.com[i] = f4(P.com);
+            }
+        }
         if (st == 3u) {
             body_integrate(b, i, p.dt);
             info = b.info[i];
@@ -1520,7 +1603,8 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         if (e != cudaSuccess) return e;
     }
     rec(4);
-    k_cache_integrate<<<nbb > npb ? nbb : npb, kItemThreads, 0, st>>>(wc, pc);
+    const bool posef = !L.batched;
+    k_cache_integrate<<<nbb > npb ? nbb : npb, kItemThreads, 0, st>>>(wc, pc, posef);
     rec(5);
     if (L.batched) {
         k_world_position<<<L.grid_world, kWorldThreads, 0, st>>>(wc, pc, L.n_worlds);
@@ -1529,7 +1613,7 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         if (e != cudaSuccess) return e;
     }
     rec(6);
-    k_post<<<nbb, kItemThreads, 0, st>>>(wc, pc);
+    k_post<<<nbb, kItemThreads, 0, st>>>(wc, pc, posef);
     return cudaGetLastError();
 }
 

@@ -354,7 +354,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(b.mass, B); A(b.local_I, 9 * (size_t)B); A(b.I, 9 * (size_t)B); A(b.inv_mass, B); A(b.inv_I, 9 * (size_t)B);
     A(b.acc_lin, B); A(b.acc_ang, B); A(b.f_lin, B); A(b.f_ang, B);
     A(b.lin_damp, B); A(b.ang_damp, B); A(b.max_lin, B); A(b.max_ang, B); A(b.sleep_thr, B); A(b.energy, B);
-    A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.dvf, 8 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
+    A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.dvf, 8 * (size_t)B); A(b.posef, 12 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
     A(b.used, B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B); A(b.col_cnt, B); A(b.vel_ver, B);
     A(b.pos_ver, B);
     Colliders& c = w->dw.c;

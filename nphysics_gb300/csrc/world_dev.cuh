@@ -66,6 +66,7 @@ struct Bodies {
     float *dv;                       // mj_lambda, 6 per body
     float4 *sb;                      // 3 per body: inverse augmented mass as the solver reads it
     unsigned long long *dvf;         // 8 per body: Δv words flagged with the body's update count
+    unsigned long long *posef;       // 12 per body: pose words flagged with the body's update count
     uint32_t *uf_parent;
     int *can_deact;
     unsigned long long *used;        // colours of the body's solver manifolds (one bit each)
