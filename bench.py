@@ -30,6 +30,13 @@ sys.path.insert(0, ROOT)
 
 METRIC = "body-steps/s"
 L2_FLUSH_BYTES = 256 << 20
+PROFILE_STEPS = 10
+# Kernels of one step of this workload (ours and CUB's radix sort and scans),
+# counted from the ncu launch list of this command (profiles/launches_ball_pile_32k.md).
+LAUNCHES_PER_STEP = 21
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_velocity launch on this
+# workload, from one ncu capture (profiles/k_velocity_ball_pile_32k.md).
+VELOCITY_TRAFFIC_PER_LAUNCH = 16809728
 
 
 def parse():
@@ -180,7 +187,6 @@ def run_gpu(args):
     # Replicas: every rank runs its own copy of the workload (one world per GPU).
     sc = scenes.ball_pile(side=args.side)
     p = sc.params()
-    p.profile = 1
     w = GpuWorld.for_scene(sc, p)
     stream = torch.cuda.ExternalStream(w.stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
@@ -191,7 +197,6 @@ def run_gpu(args):
 
     # ---- device-resident timing -------------------------------------------------------
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-    solver_ms, counters = [], []
     if world_size > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
@@ -203,10 +208,8 @@ def run_gpu(args):
             a.record(stream)
             w.step(1, sync=False)
             b.record(stream)
-            c = w.counters()
-            solver_ms.append(c["solver_time"])
-            counters.append(c)
         torch.cuda.synchronize()
+        w.synchronize()
     if world_size > 1:
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
@@ -234,14 +237,27 @@ def run_gpu(args):
     d2h = len(sc.bodies) * (7 + 6) * 4
     e2e_value = world_size * n_dyn * args.steps / e2e_s
 
-    # ---- roofline of the dominant kernel (the persistent solver kernel) --------------------
+    # ---- phase times (CUDA events on the world's stream), after the timed region ----------
+    p.profile = 1
+    w.set_params(p)
+    counters = []
+    for _ in range(PROFILE_STEPS):
+        w.step(1)
+        counters.append(w.counters())
+    p.profile = 0
+    w.set_params(p)
+
+    # ---- roofline of the dominant kernel: the velocity solver (k_velocity) ------------------
+    # Algorithmic bytes of one SOR-Prox iteration: 128 per solver contact
+    # (normal, two lever arms, r / rhs / impulse of 3 rows, friction, 2 body
+    # indices read; 3 impulses written) + 76 per dynamic body (Δv read and
+    # written, inverse mass and inverse inertia read).
     peak, peak_kind = measured_peaks()
     K = statistics.mean(c["num_solver_contacts"] for c in counters)
     B = statistics.mean(c["num_active_bodies"] for c in counters)
     it = statistics.mean(c["velocity_iterations"] for c in counters)
-    pos_it = p.max_position_iterations
-    bytes_launch = it * (128 * K + 76 * B) + pos_it * 96 * K + 104 * B
-    solve_ms = statistics.mean(solver_ms)
+    bytes_launch = it * (128 * K + 76 * B)
+    solve_ms = statistics.mean(c["velocity_resolution_time"] for c in counters)
     achieved = bytes_launch / (solve_ms * 1e-3) / 1e9
     cl = clocks.summary()
     line = {
@@ -256,11 +272,11 @@ def run_gpu(args):
                    "solver_contacts": int(K), "active_bodies": int(B),
                    "colours": int(statistics.mean(c["num_colours"] for c in counters))},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "k_solve", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": peak_kind,
+        "roofline": {"bound": "hbm", "kernel": "k_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": VELOCITY_TRAFFIC_PER_LAUNCH, "peak_source": peak_kind,
                      "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
         "clocks": {"sm_mhz": cl["sm_mhz"], "sm_max_mhz": cl["sm_max_mhz"], "reasons": cl["reasons"]},
-        "gpu_launches": 9 * args.steps,
+        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
         "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
                      ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",

@@ -22,20 +22,26 @@ namespace npgpu_dev {
 constexpr int kThreads = 256;
 static inline unsigned nblocks(uint32_t n) { return (n + kThreads - 1) / kThreads; }
 
-__device__ __forceinline__ uint64_t expand16(uint32_t v) {
-    uint64_t x = v & 0xffffu;
-    x = (x | (x << 32)) & 0x1f00000000ffffull;
-    x = (x | (x << 16)) & 0x1f0000ff0000ffull;
-    x = (x | (x << 8)) & 0x100f00f00f00f00full;
-    x = (x | (x << 4)) & 0x10c30c30c30c30c3ull;
-    x = (x | (x << 2)) & 0x1249249249249249ull;
+// Sort keys: dead bit | world index | 30-bit Morton code of the fat-AABB
+// centre on a 1 m grid (10 bits per axis, +-512 m; farther centres clamp to the
+// edge cells, which only affects the tree's shape, never the pairs). The
+// dead bit sits just above the highest world bit in use, so that the radix
+// sort only looks at 31 + world-bit bits.
+constexpr int kMortonBits = 30;
+__device__ __forceinline__ uint64_t expand10(uint32_t v) {
+    uint64_t x = v & 0x3ffu;
+    x = (x | (x << 16)) & 0x30000ffull;
+    x = (x | (x << 8)) & 0x300f00full;
+    x = (x | (x << 4)) & 0x30c30c3ull;
+    x = (x | (x << 2)) & 0x9249249ull;
     return x;
 }
 __device__ __forceinline__ uint32_t quantize(float c) {
-    float q = floorf(c * 4.0f) + 32768.0f;
-    q = q < 0.0f ? 0.0f : (q > 65535.0f ? 65535.0f : q);
+    float q = floorf(c) + 512.0f;
+    q = q < 0.0f ? 0.0f : (q > 1023.0f ? 1023.0f : q);
     return (uint32_t)q;
 }
+__device__ __forceinline__ uint32_t key_world(unsigned long long k) { return (uint32_t)(k >> kMortonBits) & 0xffffu; }
 
 __device__ __forceinline__ Shape load_shape(const Colliders& c, uint32_t i) {
     Shape s;
@@ -51,12 +57,12 @@ __device__ __forceinline__ Shape load_shape(const Colliders& c, uint32_t i) {
 
 // Collider pose, tight AABB (loosened by margin + linear prediction,
 // src/object/collider.rs:542-549), fat AABB update and sort key.
-__global__ void k_sync_aabb(World w, float bp_margin) {
+__global__ void k_sync_aabb(World w, float bp_margin, int world_bits) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= w.nc_slots) return;
     const Colliders& c = w.c;
     if (!(c.info[i] & CI_ALIVE)) {
-        c.keys[i] = ~0ull;
+        c.keys[i] = 1ull << (kMortonBits + world_bits);
         c.vals[i] = i;
         return;
     }
@@ -94,9 +100,9 @@ __global__ void k_sync_aabb(World w, float bp_margin) {
         c.aabb_max[i] = fmx;
     }
     float cx = 0.5f * (fmn.x + fmx.x), cy = 0.5f * (fmn.y + fmx.y), cz = 0.5f * (fmn.z + fmx.z);
-    uint64_t morton = expand16(quantize(cx)) | (expand16(quantize(cy)) << 1) | (expand16(quantize(cz)) << 2);
+    uint64_t morton = expand10(quantize(cx)) | (expand10(quantize(cy)) << 1) | (expand10(quantize(cz)) << 2);
     uint64_t world = w.b.world[bi] & 0xffffu;
-    c.keys[i] = (world << 48) | morton;
+    c.keys[i] = (world << kMortonBits) | morton;
     c.vals[i] = i;
 }
 
@@ -130,7 +136,7 @@ __global__ void k_lbvh_build(World w, int n) {
     int lo = i < j ? i : j, hi = i < j ? j : i;
     int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
     int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
-    w.c.node_world[i] = (uint32_t)(k[lo] >> 48) << 16 | (uint32_t)(k[hi] >> 48);
+    w.c.node_world[i] = key_world(k[lo]) << 16 | key_world(k[hi]);
     w.c.left[i] = left;
     w.c.right[i] = right;
     w.c.parent[left] = i;
@@ -150,7 +156,7 @@ __global__ void k_lbvh_refit(World w, int n) {
     float4 mx = w.c.aabb_max[ci];
     w.c.node_min[node] = w.c.aabb_min[ci];
     w.c.node_max[node] = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
-    uint32_t wk = (uint32_t)(w.c.keys_sorted[k] >> 48);
+    uint32_t wk = key_world(w.c.keys_sorted[k]);
     w.c.node_world[node] = wk << 16 | wk;
     if (n == 1) return;
     __threadfence();
@@ -219,7 +225,7 @@ __global__ void k_bp_traverse(World w, int n) {
     }
     float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
     float ra = c.rank[a];
-    const uint32_t qw = (uint32_t)(c.keys_sorted[k] >> 48);
+    const uint32_t qw = key_world(c.keys_sorted[k]);
     if (n >= 2) {
         int stack[64];
         int sp = 0;
@@ -370,14 +376,14 @@ size_t scan_temp_bytes(uint32_t n) {
 
 cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t st) {
     if (w.nc_slots == 0) return cudaSuccess;
-    k_sync_aabb<<<nblocks(w.nc_slots), kThreads, 0, st>>>(w, p.broad_phase_margin);
+    k_sync_aabb<<<nblocks(w.nc_slots), kThreads, 0, st>>>(w, p.broad_phase_margin, (int)w.world_bits);
     return cudaGetLastError();
 }
 
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st) {
     if (w.nc_slots == 0) return cudaSuccess;
     return cub::DeviceRadixSort::SortPairs(temp, temp_bytes, w.c.keys, w.c.keys_sorted, w.c.vals, w.c.vals_sorted,
-                                           (int)w.nc_slots, 0, 64, st);
+                                           (int)w.nc_slots, 0, kMortonBits + w.world_bits + 1, st);
 }
 
 cudaError_t launch_lbvh(const World& w, cudaStream_t st) {

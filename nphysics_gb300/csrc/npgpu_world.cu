@@ -142,6 +142,7 @@ struct npgpu_world {
     std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries, then the n_worlds largest-first order
     uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
     bool layout_on_device = false;
+    uint32_t max_world = 0;              // largest world index any body had (never lowered)
     int grid_world = 0;
 };
 
@@ -222,6 +223,9 @@ static void sync_world_view(npgpu_world* w) {
     w->dw.nb_slots = w->nb_slots;
     w->dw.nc_slots = w->nc_slots;
     w->dw.nc_alive = w->nc_alive;
+    uint32_t wb = 0;
+    while (wb < 16 && (w->max_world >> wb) != 0u) ++wb;
+    w->dw.world_bits = wb;
 }
 
 // Finds each world's slot range. The per-world schedule needs the alive
@@ -547,6 +551,7 @@ npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
         u.max_ang = d.max_angular_velocity;
         u.sleep_thr = d.sleep_threshold;
         if (!hb.alive || hb.world != d.world) w->layout_dirty = true;
+        w->max_world = std::max(w->max_world, d.world);
         hb.alive = true;
         hb.gen = handles[k].generation;
         hb.kind = d.kind;

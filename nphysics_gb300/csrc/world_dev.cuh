@@ -172,6 +172,7 @@ struct World {
     Solver s;
     Control* ctl;
     uint32_t nb_slots, nc_slots, cap_pairs, nc_alive;
+    uint32_t world_bits;             // bits of the largest world index of any body so far
 };
 
 // ---- launchers (defined in the kernel translation units) ----
