@@ -173,7 +173,8 @@ typedef struct npgpu_params {
     uint32_t solve_to_tolerance;           /* 0: run max_velocity_iterations; 1: stop when residual <= tol */
     float residual_tolerance;              /* 1e-4 */
     uint32_t max_iterations_to_tolerance;  /* cap when solve_to_tolerance (e.g. 256) */
-    uint32_t warmstart_mode;               /* 0: impulse cache (reference); 1: none */
+    uint32_t warmstart_mode;               /* 0: impulse cache (reference); 1: none; 2: impulse cache, and the
+                                              learned network for contacts without a cache entry */
     float broad_phase_margin;              /* DBVTBroadPhase::new(0.01), geometrical_world.rs:60 */
     float activation_mix;                  /* ActivationManager::new(0.01), mechanical_world.rs:80 */
     uint32_t profile;                      /* non-zero: time each phase with CUDA events */
@@ -332,6 +333,47 @@ const char* npgpu_last_error(const npgpu_world* w);
  * GPU race. No call allocates or frees memory. */
 npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint32_t* groups, uint32_t n, uint32_t* pairs2,
                                      uint32_t max_pairs, uint32_t* count, void* stream);
+
+/* ---- Learned warm start (no counterpart in the reference) ----
+ * A 24 -> 64 -> 64 -> 3 perceptron (ReLU, bf16 weights, fp32 accumulation)
+ * predicts the starting impulses (normal, tangent 1, tangent 2) of contacts
+ * that have no impulse-cache entry when params.warmstart_mode == 2. The
+ * warm-start sweep keeps a prediction only if the contact's local residual is
+ * no larger than with a zero start, so the iteration count to a residual
+ * tolerance stays the measure.
+ *
+ * Parameters (fp32, NPGPU_MLP_PARAMS floats): W1[64][24] b1[64] W2[64][64]
+ * b2[64] W3[3][64] b3[3], then the normalisation x_mean[24] x_inv_std[24]
+ * y_mean[3] y_std[3] (network input = (feature - mean) * inv_std; impulse =
+ * output * y_std + y_mean). A training sample is NPGPU_MLP_SAMPLE_FLOATS
+ * floats: the 24 features, the 3 converged impulses, and 1 if the contact had
+ * no cache entry when it was assembled (else 0). */
+#define NPGPU_MLP_PARAMS 6009u
+#define NPGPU_MLP_TRAINABLE 5955u
+#define NPGPU_MLP_SAMPLE_FLOATS 28u
+#define NPGPU_MLP_INIT 1u      /* npgpu_mlp_train flag: new weights from the seed, normalisation from the samples */
+
+/* Sets the network (n == NPGPU_MLP_PARAMS) and resets the optimiser state. */
+npgpu_status npgpu_mlp_set(npgpu_world* w, const float* params, uint32_t n);
+/* Copies the network's fp32 parameters out (n >= NPGPU_MLP_PARAMS). */
+npgpu_status npgpu_mlp_get(npgpu_world* w, float* params, uint32_t n);
+/* Records a training sample for every solver contact of the following steps
+ * (features at assembly, impulses after the velocity solve) until `capacity`
+ * samples are held; capacity 0 stops recording and keeps what was recorded. A
+ * new capacity discards earlier samples. */
+npgpu_status npgpu_mlp_record(npgpu_world* w, uint32_t capacity);
+/* Number of recorded samples, and up to max_samples of them when out != NULL. */
+npgpu_status npgpu_mlp_samples(npgpu_world* w, float* out, uint32_t max_samples, uint32_t* count);
+/* Trains on the recorded samples with Adam (lr, batch a multiple of 64):
+ * `steps` batches drawn from the samples by a hash of (seed, step). With
+ * NPGPU_MLP_INIT, or when no network is set yet, starts from He-uniform
+ * weights drawn from `seed` and normalisation from the samples' statistics.
+ * *final_loss (may be NULL) receives the last batch's loss. */
+npgpu_status npgpu_mlp_train(npgpu_world* w, uint32_t steps, uint32_t batch, float lr, uint32_t seed, uint32_t flags,
+                             float* final_loss);
+/* Loss and gradient (NPGPU_MLP_TRAINABLE floats, parameter layout above) of
+ * the current network over n host samples, without updating it (n <= 65536). */
+npgpu_status npgpu_mlp_grad(npgpu_world* w, const float* samples, uint32_t n, float* grad, float* loss);
 
 #ifdef __cplusplus
 }

@@ -243,6 +243,13 @@ def load_library(path=LIB_PATH):
         "npgpu_last_error": (C.c_char_p, [W]),
         "npgpu_find_pairs_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
                                               C.c_void_p, C.c_void_p]),
+        "npgpu_mlp_set": (C.c_int, [W, P(C.c_float), C.c_uint32]),
+        "npgpu_mlp_get": (C.c_int, [W, P(C.c_float), C.c_uint32]),
+        "npgpu_mlp_record": (C.c_int, [W, C.c_uint32]),
+        "npgpu_mlp_samples": (C.c_int, [W, P(C.c_float), C.c_uint32, P(C.c_uint32)]),
+        "npgpu_mlp_train": (C.c_int, [W, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32,
+                                      P(C.c_float)]),
+        "npgpu_mlp_grad": (C.c_int, [W, P(C.c_float), C.c_uint32, P(C.c_float), P(C.c_float)]),
     }
     for name, (res, args) in decl.items():
         fn = getattr(lib, name)
@@ -258,4 +265,13 @@ EXPORTED = [
     "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_step",
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
     "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
+    "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
 ]
+
+# Learned warm start (npgpu_mlp_*).
+WARMSTART_CACHE, WARMSTART_NONE, WARMSTART_LEARNED = 0, 1, 2
+MLP_IN, MLP_HIDDEN, MLP_OUT = 24, 64, 3
+MLP_PARAMS = 6009
+MLP_TRAINABLE = 5955
+MLP_SAMPLE_FLOATS = 28
+MLP_INIT = 1

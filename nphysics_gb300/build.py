@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnpgpu.so")
-SOURCES = ["npgpu_world.cu", "k_bodies.cu", "k_cd.cu", "k_solve.cu", "k_static_pairs.cu"]
+SOURCES = ["npgpu_world.cu", "k_bodies.cu", "k_cd.cu", "k_solve.cu", "k_static_pairs.cu", "k_mlp.cu"]
 HEADERS = ["np_math.cuh", "world_dev.cuh", "dyn.cuh", "narrow.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

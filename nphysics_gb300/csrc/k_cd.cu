@@ -336,6 +336,7 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p) {
         for (int j = 0; j < pn; ++j)
             if (pkeys[j] == key) {
                 imp = w.prev.imp[prev * kMaxContacts + j];
+                imp.w = 1.0f;   // found in the impulse cache
                 break;
             }
         uint32_t slot = p * kMaxContacts + k;

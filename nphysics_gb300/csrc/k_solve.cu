@@ -30,6 +30,7 @@
 // any assignment of manifolds to resident threads makes progress.
 #include <cub/device/device_scan.cuh>
 
+#include "mlp.cuh"
 #include "narrow.cuh"
 
 namespace npgpu_dev {
@@ -721,6 +722,9 @@ __global__ void k_assemble(World w, StepParams p) {
         w.s.sm_mask[m] = mask;
         float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
         float4* lam = w.s.lam + (size_t)m * kMaxContacts;
+        const bool learned = p.warmstart_mode == 2u && w.mlp != nullptr;
+        const bool record = w.s.feat != nullptr;
+        const float k1 = (float)((rk >> 8) & 0xffu), k2 = (float)(rk >> 24);
         for (uint32_t k = 0; k < nc; ++k) {
             uint32_t slot = q * kMaxContacts + k;
             float4 w1 = w.cur.w1[slot], w2 = w.cur.w2[slot], nn = w.cur.n[slot], imp = w.cur.imp[slot];
@@ -744,6 +748,26 @@ __global__ void k_assemble(World w, StepParams p) {
             const bool cold = p.warmstart_mode == 1u;
             lam[k] = make_float4(cold ? 0.0f : imp.x * p.warmstart_coeff, cold ? 0.0f : imp.y * p.warmstart_coeff,
                                  cold ? 0.0f : imp.z * p.warmstart_coeff, 0.0f);
+            const bool fresh = imp.w == 0.0f;   // no impulse-cache entry
+            if (record || (learned && fresh)) {
+                rn[RF_RHS] = rhs;
+                float feat[kMlpIn];
+                float gn_dt = (p.gx * n.x + p.gy * n.y + p.gz * n.z) * dt;
+                mlp_features(rn, rt[0], rt[1], depth, b1 >= 0 ? v1.inv_mass : 0.0f, b2 >= 0 ? v2.inv_mass : 0.0f, mu,
+                             gn_dt, (float)nc, k1, k2, feat);
+                if (record) {
+                    float* fo = w.s.feat + ((size_t)m * kMaxContacts + k) * kMlpIn;
+#pragma unroll
+                    for (int i = 0; i < kMlpIn; ++i) fo[i] = feat[i];
+                }
+                if (learned && fresh) {
+                    float pl[kMlpOut];
+                    mlp_forward(w.mlp, feat, pl);
+                    mlp_project(mu, pl);
+                    // .w = 1: a predicted start, checked in the warm-start sweep.
+                    lam[k] = make_float4(pl[0], pl[1], pl[2], 1.0f);
+                }
+            }
         }
     }
 }
@@ -753,6 +777,30 @@ __global__ void k_assemble(World w, StepParams p) {
 // orthonormal basis of n for the friction rows.
 __device__ __forceinline__ np::V row_dir(const ContactRec& c, int row, const np::V* t) {
     return row == 0 ? np::neg(c.n) : t[row - 1];
+}
+
+// Squared projected-gradient residual of one contact's three rows at Δv for
+// impulses lam (fp32; the friction limit follows lam's normal impulse).
+__device__ __forceinline__ float local_residual(const ContactRec& c, const np::V* t, uint32_t mask, const DV& dv,
+                                                const float* lam, bool h1, bool h2) {
+    float s = 0.0f;
+    {
+        float d = jdot(np::neg(c.n), c.pos1, c.pos2, mask, dv, h1, h2) + c.rhs[0];
+        float x = lam[0] - c.r[0] * d;
+        float pr = x > 0.0f ? x : 0.0f;
+        float phi = lam[0] - pr;
+        s = s + phi * phi;
+    }
+    const float lim = c.mu * lam[0];
+#pragma unroll
+    for (int r = 0; r < 2; ++r) {
+        float d = jdot(t[r], c.pos1, c.pos2, mask, dv, h1, h2) + c.rhs[1 + r];
+        float x = lam[1 + r] - c.r[1 + r] * d;
+        float pr = x < -lim ? -lim : (x > lim ? lim : x);
+        float phi = lam[1 + r] - pr;
+        s = s + phi * phi;
+    }
+    return s;
 }
 
 // Where a velocity task reads its contacts: global memory, or the running
@@ -820,10 +868,26 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
             np::V t[2];
             src.tangents(c, k, t);
             float li[3] = {l.x, l.y, l.z};
+            const bool predicted = l.w != 0.0f;
+            DV before;
+            if (predicted) before = dv;
 #pragma unroll 1
             for (int row = 0; row < 3; ++row) {
                 if (li[row] == 0.0f) continue;
                 axpy(row_dir(c, row, t), c.pos1, c.pos2, mask, bm, dv, li[row], h1, h2);
+            }
+            if (predicted) {
+                // A learned start stays only if its local residual is no larger
+                // than the zero start's.
+                const float zero[3] = {0.0f, 0.0f, 0.0f};
+                float with = local_residual(c, t, mask, dv, li, h1, h2);
+                float without = local_residual(c, t, mask, before, zero, h1, h2);
+                if (with > without) {
+                    dv = before;
+                    src.set_lam(k, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+                } else {
+                    src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
+                }
             }
         } else if (sweep & 1u) {
             np::V t[2];
@@ -1290,7 +1354,23 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
     GRID_FOR(m, ms) {
         uint32_t q = w.s.sm_list[m];
         uint32_t nc = w.s.sm_nc[m];
-        for (uint32_t k = 0; k < nc; ++k) w.cur.imp[q * kMaxContacts + k] = w.s.lam[(size_t)m * kMaxContacts + k];
+        for (uint32_t k = 0; k < nc; ++k) {
+            float4 l = w.s.lam[(size_t)m * kMaxContacts + k];
+            if (w.s.feat != nullptr) {
+                // Training sample: the contact's features and converged impulses.
+                uint32_t at = atomicAdd(&w.ctl->mlp_samples, 1u);
+                if (at < w.s.sample_cap) {
+                    float* so = w.s.samples + (size_t)at * kMlpSampleFloats;
+                    const float* fi = w.s.feat + ((size_t)m * kMaxContacts + k) * kMlpIn;
+                    for (int i = 0; i < kMlpIn; ++i) so[i] = fi[i];
+                    so[kMlpIn] = l.x;
+                    so[kMlpIn + 1] = l.y;
+                    so[kMlpIn + 2] = l.z;
+                    so[kMlpIn + 3] = w.cur.imp[q * kMaxContacts + k].w == 0.0f ? 1.0f : 0.0f;
+                }
+            }
+            w.cur.imp[q * kMaxContacts + k] = l;
+        }
     }
     const float dt = p.dt;
     GRID_FOR(i, w.nb_slots) {

@@ -15,6 +15,7 @@
 
 #include "../../include/npgpu.h"
 #include "world_dev.cuh"
+#include "mlp.cuh"
 
 using namespace npgpu_dev;
 
@@ -142,6 +143,16 @@ struct npgpu_world {
     std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries, then the n_worlds largest-first order
     uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
     bool layout_on_device = false;
+    // Learned warm start.
+    MlpDev* d_net = nullptr;             // inference copy (bf16 weights)
+    float* d_prm = nullptr;              // fp32 parameters (NPGPU_MLP_PARAMS)
+    float *d_m1 = nullptr, *d_m2 = nullptr, *d_grad = nullptr;   // Adam moments, gradient
+    double* d_stats = nullptr;
+    bool net_ready = false;
+    uint32_t adam_t = 0;
+    float* d_samples = nullptr;
+    uint32_t sample_cap = 0;
+    float* d_feat = nullptr;
     uint32_t max_world = 0;              // largest world index any body had (never lowered)
     int grid_world = 0;
 };
@@ -464,6 +475,9 @@ void npgpu_destroy(npgpu_world* w) {
     cudaFree(w->dw.s.world_start);
     cudaFree(w->dw.s.bucket_count);
     cudaFree(w->dw.s.bucket_start);
+    for (void* p : {(void*)w->d_net, (void*)w->d_prm, (void*)w->d_m1, (void*)w->d_m2, (void*)w->d_grad,
+                    (void*)w->d_stats, (void*)w->d_samples, (void*)w->d_feat})
+        cudaFree(p);
     if (w->d_stage) cudaFree(w->d_stage);
     if (w->h_stage) cudaFreeHost(w->h_stage);
     if (w->ev_stage) cudaEventDestroy(w->ev_stage);
@@ -821,6 +835,9 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
     if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
     if (num_joints) return fail(w, NPGPU_ERR_NONEMPTY_JOINTS, "joint constraints are not supported");
     if (num_force_generators) return fail(w, NPGPU_ERR_NONEMPTY_FORCES, "force generators are not supported");
+    if (w->params.warmstart_mode == 2 && !w->net_ready)
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "warmstart_mode 2 needs a network (npgpu_mlp_set or npgpu_mlp_train)");
+    if (w->params.warmstart_mode > 2) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown warmstart_mode");
     StepParams sp = step_params(w);
     for (uint32_t s = 0; s < nsteps; ++s) {
         npgpu_status st = maintain(w);
@@ -1036,6 +1053,150 @@ npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max
     *count = (uint32_t)all.size();
     if (out)
         for (uint32_t k = 0; k < all.size() && k < max; ++k) out[k] = all[k];
+    return NPGPU_OK;
+}
+
+// ---------------------------------------------------------------- learned warm start
+static_assert(NPGPU_MLP_PARAMS == (unsigned)kMlpParams, "parameter layout");
+static_assert(NPGPU_MLP_TRAINABLE == (unsigned)kMlpTrainable, "parameter layout");
+static_assert(NPGPU_MLP_SAMPLE_FLOATS == (unsigned)kMlpSampleFloats, "sample layout");
+
+static npgpu_status mlp_alloc(npgpu_world* w) {
+    if (w->d_net) return NPGPU_OK;
+    CK(cudaMalloc(&w->d_net, sizeof(MlpDev)), "network");
+    CK(cudaMalloc(&w->d_prm, sizeof(float) * kMlpParams), "network parameters");
+    CK(cudaMalloc(&w->d_m1, sizeof(float) * kMlpTrainable), "adam");
+    CK(cudaMalloc(&w->d_m2, sizeof(float) * kMlpTrainable), "adam");
+    CK(cudaMalloc(&w->d_grad, sizeof(float) * kMlpTrainable), "gradient");
+    CK(cudaMalloc(&w->d_stats, sizeof(double) * 2 * (kMlpIn + kMlpOut)), "statistics");
+    return NPGPU_OK;
+}
+
+static npgpu_status mlp_reset_adam(npgpu_world* w) {
+    CK(cudaMemsetAsync(w->d_m1, 0, sizeof(float) * kMlpTrainable, w->stream), "adam");
+    CK(cudaMemsetAsync(w->d_m2, 0, sizeof(float) * kMlpTrainable, w->stream), "adam");
+    w->adam_t = 0;
+    return NPGPU_OK;
+}
+
+static uint32_t mlp_count(npgpu_world* w) {
+    uint32_t n = 0;
+    if (cudaMemcpy(&n, &w->ctl->mlp_samples, sizeof(n), cudaMemcpyDeviceToHost) != cudaSuccess) return 0;
+    return std::min(n, w->sample_cap);
+}
+
+npgpu_status npgpu_mlp_set(npgpu_world* w, const float* params, uint32_t n) {
+    if (!w || !params) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (n != kMlpParams) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "expected NPGPU_MLP_PARAMS parameters");
+    if (!finite_n(params, (int)n)) return fail(w, NPGPU_ERR_NAN, "network parameters are not finite");
+    npgpu_status st = mlp_alloc(w);
+    if (st != NPGPU_OK) return st;
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    CK(cudaMemcpy(w->d_prm, params, sizeof(float) * kMlpParams, cudaMemcpyHostToDevice), "network upload");
+    CK(mlp_upload(w->d_prm, w->d_net, w->stream), "network upload");
+    st = mlp_reset_adam(w);
+    if (st != NPGPU_OK) return st;
+    w->net_ready = true;
+    w->dw.mlp = w->d_net;
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_mlp_get(npgpu_world* w, float* params, uint32_t n) {
+    if (!w || !params) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (n < kMlpParams) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "buffer smaller than NPGPU_MLP_PARAMS");
+    if (!w->net_ready) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "no network");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    CK(cudaMemcpy(params, w->d_prm, sizeof(float) * kMlpParams, cudaMemcpyDeviceToHost), "network download");
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_mlp_record(npgpu_world* w, uint32_t capacity) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    if (capacity == 0) {
+        w->dw.s.feat = nullptr;
+        return NPGPU_OK;
+    }
+    if (!w->d_feat) CK(cudaMalloc(&w->d_feat, sizeof(float) * kMlpIn * kMaxContacts * (size_t)w->cap_p), "features");
+    if (capacity > w->sample_cap) {
+        cudaFree(w->d_samples);
+        w->d_samples = nullptr;
+        w->sample_cap = 0;
+        CK(cudaMalloc(&w->d_samples, sizeof(float) * kMlpSampleFloats * (size_t)capacity), "samples");
+    }
+    w->sample_cap = capacity;
+    uint32_t zero = 0;
+    CK(cudaMemcpy(&w->ctl->mlp_samples, &zero, sizeof(zero), cudaMemcpyHostToDevice), "samples");
+    w->dw.s.feat = w->d_feat;
+    w->dw.s.samples = w->d_samples;
+    w->dw.s.sample_cap = capacity;
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_mlp_samples(npgpu_world* w, float* out, uint32_t max_samples, uint32_t* count) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    uint32_t n = w->d_samples ? mlp_count(w) : 0;
+    if (count) *count = n;
+    if (out && n) {
+        uint32_t k = std::min(n, max_samples);
+        CK(cudaMemcpy(out, w->d_samples, sizeof(float) * kMlpSampleFloats * (size_t)k, cudaMemcpyDeviceToHost),
+           "samples download");
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_mlp_train(npgpu_world* w, uint32_t steps, uint32_t batch, float lr, uint32_t seed, uint32_t flags,
+                             float* final_loss) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (batch == 0 || batch % 64 != 0 || batch > (1u << 20))
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "batch must be a positive multiple of 64 (at most 2^20)");
+    if (!(lr > 0.0f)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "lr must be positive");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    const uint32_t n = w->d_samples ? mlp_count(w) : 0;
+    if (n == 0) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "no recorded samples (npgpu_mlp_record)");
+    npgpu_status st = mlp_alloc(w);
+    if (st != NPGPU_OK) return st;
+    if ((flags & NPGPU_MLP_INIT) || !w->net_ready) {
+        CK(mlp_init(w->d_prm, seed, w->stream), "network init");
+        CK(mlp_normalise(w->d_samples, n, w->d_stats, w->d_prm, w->stream), "normalisation");
+        CK(mlp_upload(w->d_prm, w->d_net, w->stream), "network upload");
+        st = mlp_reset_adam(w);
+        if (st != NPGPU_OK) return st;
+        w->net_ready = true;
+        w->dw.mlp = w->d_net;
+    }
+    const uint32_t bseed = (seed * 2654435761u) | 1u;   // non-zero: batches drawn by hash
+    for (uint32_t k = 0; k < steps; ++k) {
+        CK(mlp_grad(w->d_net, w->d_samples, n, batch, bseed, w->adam_t, w->d_grad, &w->ctl->mlp_loss, w->stream),
+           "network gradient");
+        CK(mlp_adam(w->d_prm, w->d_m1, w->d_m2, w->d_grad, lr, ++w->adam_t, w->d_net, w->stream), "adam");
+    }
+    CK(cudaStreamSynchronize(w->stream), "training");
+    if (final_loss) {
+        double l = 0.0;
+        CK(cudaMemcpy(&l, &w->ctl->mlp_loss, sizeof(l), cudaMemcpyDeviceToHost), "loss");
+        *final_loss = (float)l;
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_mlp_grad(npgpu_world* w, const float* samples, uint32_t n, float* grad, float* loss) {
+    if (!w || !samples || !grad) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (n == 0 || n > 65536) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "1 <= n <= 65536 samples");
+    if (!w->net_ready) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "no network");
+    void* dp = nullptr;
+    npgpu_status st = stage_upload(w, samples, sizeof(float) * kMlpSampleFloats * (size_t)n, &dp);
+    if (st != NPGPU_OK) return st;
+    CK(mlp_grad(w->d_net, (const float*)dp, n, n, 0u, 0u, w->d_grad, &w->ctl->mlp_loss, w->stream), "network gradient");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    CK(cudaStreamSynchronize(w->stream), "gradient");
+    CK(cudaMemcpy(grad, w->d_grad, sizeof(float) * kMlpTrainable, cudaMemcpyDeviceToHost), "gradient download");
+    if (loss) {
+        double l = 0.0;
+        CK(cudaMemcpy(&l, &w->ctl->mlp_loss, sizeof(l), cudaMemcpyDeviceToHost), "loss");
+        *loss = (float)l;
+    }
     return NPGPU_OK;
 }
 

@@ -125,6 +125,11 @@ struct Solver {
     // other in one allocation, cleared by one memset each step.
     uint32_t *bucket_count, *bucket_start, *bucket_cursor;
     uint32_t *wm_order;              // solver manifolds ordered by (world, colour)
+    // Learned warm start: per-contact features while recording (null otherwise)
+    // and the sample buffer they are appended to after the solve.
+    float *feat;
+    float *samples;
+    uint32_t sample_cap;
 };
 
 // Device counters and control words (one struct in device memory).
@@ -150,6 +155,9 @@ struct Control {
     unsigned long long task_ns, wait_ns, tasks;   // velocity-task statistics (profile mode)
     double res_acc_init[2];          // batched worlds: residual sums after the warm start
     uint32_t world_next[2];          // batched worlds: work counters of the velocity / position kernels
+    uint32_t mlp_samples;            // training samples recorded so far
+    uint32_t pad2;
+    double mlp_loss;                 // loss of the last training step
 };
 
 struct StepParams {
@@ -165,7 +173,10 @@ struct StepParams {
     uint32_t profile;
 };
 
+struct MlpDev;
+
 struct World {
+    const MlpDev* mlp;               // the learned warm start's network (null when none is set)
     Bodies b;
     Colliders c;
     Pairs cur, prev;
@@ -205,6 +216,15 @@ int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds);
 size_t sort_temp_bytes(uint32_t n_items);
 size_t scan_temp_bytes(uint32_t n_items);
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);
+
+// Learned warm start (k_mlp.cu).
+cudaError_t mlp_upload(const float* prm_dev, MlpDev* net, cudaStream_t st);
+cudaError_t mlp_normalise(const float* samples, uint32_t n, double* acc, float* prm, cudaStream_t st);
+cudaError_t mlp_init(float* prm, uint32_t seed, cudaStream_t st);
+cudaError_t mlp_grad(const MlpDev* net, const float* samples, uint32_t n, uint32_t batch, uint32_t seed, uint32_t step,
+                     float* grad, double* loss, cudaStream_t st);
+cudaError_t mlp_adam(float* prm, float* m1, float* m2, const float* grad, float lr, uint32_t t, MlpDev* net,
+                     cudaStream_t st);
 
 // Uploads / maintenance kernels.
 struct BodyUpload {

@@ -167,6 +167,43 @@ class GpuWorld:
         self._check(self.L.npgpu_get_contacts(self.w, arr, n, C.byref(cnt)), "get_contacts")
         return abi.contacts_to_numpy(arr, n)
 
+    # ---- learned warm start ----
+    def mlp_set(self, params):
+        params = np.ascontiguousarray(params, np.float32)
+        self._check(self.L.npgpu_mlp_set(self.w, _ptr(params, C.c_float), params.size), "mlp_set")
+
+    def mlp_get(self):
+        out = np.zeros(abi.MLP_PARAMS, np.float32)
+        self._check(self.L.npgpu_mlp_get(self.w, _ptr(out, C.c_float), out.size), "mlp_get")
+        return out
+
+    def mlp_record(self, capacity):
+        self._check(self.L.npgpu_mlp_record(self.w, capacity), "mlp_record")
+
+    def mlp_samples(self, download=True):
+        n = C.c_uint32(0)
+        self._check(self.L.npgpu_mlp_samples(self.w, None, 0, C.byref(n)), "mlp_samples")
+        if not download:
+            return n.value
+        out = np.zeros((n.value, abi.MLP_SAMPLE_FLOATS), np.float32)
+        if n.value:
+            self._check(self.L.npgpu_mlp_samples(self.w, _ptr(out, C.c_float), n.value, C.byref(n)), "mlp_samples")
+        return out
+
+    def mlp_train(self, steps, batch=4096, lr=1e-3, seed=1, init=False):
+        loss = C.c_float(0.0)
+        self._check(self.L.npgpu_mlp_train(self.w, steps, batch, lr, seed, abi.MLP_INIT if init else 0,
+                                           C.byref(loss)), "mlp_train")
+        return loss.value
+
+    def mlp_grad(self, samples):
+        samples = np.ascontiguousarray(samples, np.float32)
+        grad = np.zeros(abi.MLP_TRAINABLE, np.float32)
+        loss = C.c_float(0.0)
+        self._check(self.L.npgpu_mlp_grad(self.w, _ptr(samples, C.c_float), samples.shape[0], _ptr(grad, C.c_float),
+                                          C.byref(loss)), "mlp_grad")
+        return grad, loss.value
+
     def counters(self):
         c = abi.Counters()
         self._check(self.L.npgpu_get_counters(self.w, C.byref(c)), "get_counters")

@@ -63,6 +63,7 @@ orc_world* orc_create(int precision, const npgpu_params* p, const float gravity[
 void orc_destroy(orc_world* o) { delete o; }
 
 void orc_set_order(orc_world* o, int order) { DISPATCH(o, w.order = order); }
+void orc_mlp_set(orc_world* o, const float* params, uint32_t n) { DISPATCH(o, w.set_mlp(params, n)); }
 
 void orc_set_params(orc_world* o, const npgpu_params* p) { DISPATCH(o, w.params = *p); }
 

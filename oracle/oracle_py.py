@@ -29,6 +29,7 @@ def lib():
             "orc_create": (W, [C.c_int, P(abi.Params), P(C.c_float)]),
             "orc_destroy": (None, [W]),
             "orc_set_order": (None, [W, C.c_int]),
+            "orc_mlp_set": (None, [W, C.POINTER(C.c_float), C.c_uint32]),
             "orc_set_params": (None, [W, P(abi.Params)]),
             "orc_upsert_bodies": (C.c_int, [W, C.c_uint32, C.c_void_p, C.c_void_p]),
             "orc_upsert_colliders": (C.c_int, [W, C.c_uint32, C.c_void_p, C.c_void_p]),
@@ -91,6 +92,11 @@ class OracleWorld:
 
     def set_order(self, order):
         self.L.orc_set_order(self.w, order)
+
+    def mlp_set(self, params):
+        """The learned warm start's network (the fp32 layout of npgpu_mlp_set)."""
+        params = np.ascontiguousarray(params, np.float32)
+        self.L.orc_mlp_set(self.w, params.ctypes.data_as(C.POINTER(C.c_float)), params.size)
 
     def set_params(self, params):
         self.params = params

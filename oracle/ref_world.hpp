@@ -238,6 +238,7 @@ template <class R> struct MContact {
     int fid1, fid2;
     V3<R> normal1_local;   // contact normal in body 1's frame (signorini_model.rs:174)
     R impulse[3];          // ImpulseCache entry (normal, tangent1, tangent2)
+    bool cached = false;   // the entry came from the cache (false: a new contact)
     uint32_t key() const { return uint32_t(fid1 * 26 + fid2); }
 };
 
@@ -257,6 +258,7 @@ template <class R> struct Row {
     bool friction;
     void* cache;           // MContact the impulse is cached to
     int cache_slot;
+    bool predicted;        // normal row of a contact started from the learned network
 };
 
 template <class R> struct PosConstraint {
@@ -967,6 +969,7 @@ public:
                     k.impulse[0] = old.impulse[0];
                     k.impulse[1] = old.impulse[1];
                     k.impulse[2] = old.impulse[2];
+                    k.cached = true;
                     break;
                 }
             nc.push_back(k);
@@ -1122,6 +1125,108 @@ public:
         t2 = vdiv(b, norm(b));
     }
 
+    // ---- learned warm start (the network of the GPU's npgpu_mlp_*) ----
+    // Parameters in the fp32 layout W1[64][24] b1[64] W2[64][64] b2[64]
+    // W3[3][64] b3[3] x_mean[24] x_inv_std[24] y_mean[3] y_std[3]; the
+    // weights as the forward pass reads them are rounded to bf16.
+    std::vector<float> mlp;
+    static float bf16_round(float v) {
+        uint32_t u;
+        std::memcpy(&u, &v, 4);
+        if ((u & 0x7f800000u) != 0x7f800000u) {   // finite: round to nearest, ties to even
+            u += 0x7fffu + ((u >> 16) & 1u);
+        }
+        u &= 0xffff0000u;
+        float r;
+        std::memcpy(&r, &u, 4);
+        return r;
+    }
+    void set_mlp(const float* p, size_t n) {
+        mlp.assign(p, p + n);
+        for (size_t i = 0; i < n; ++i) {
+            bool weight = i < 1536 || (i >= 1600 && i < 1600 + 4096) || (i >= 5760 && i < 5760 + 192);
+            if (weight) mlp[i] = bf16_round(mlp[i]);
+        }
+    }
+    // Forward pass in fp32 with sums in index order (no fused multiply-add).
+    void mlp_forward(const float* feat, float* out) const {
+        const float* W1 = mlp.data();
+        const float* b1 = W1 + 1536;
+        const float* W2 = b1 + 64;
+        const float* b2 = W2 + 4096;
+        const float* W3 = b2 + 64;
+        const float* b3 = W3 + 192;
+        const float* xm = b3 + 3;
+        const float* xs = xm + 24;
+        const float* ym = xs + 24;
+        const float* ys = ym + 3;
+        float x[24], h1[64], y[3];
+        for (int i = 0; i < 24; ++i) x[i] = (feat[i] - xm[i]) * xs[i];
+        for (int j = 0; j < 64; ++j) {
+            float a = b1[j];
+            for (int i = 0; i < 24; ++i) a = a + W1[j * 24 + i] * x[i];
+            h1[j] = a > 0.0f ? a : 0.0f;
+        }
+        for (int o = 0; o < 3; ++o) y[o] = b3[o];
+        for (int j = 0; j < 64; ++j) {
+            float a = b2[j];
+            for (int i = 0; i < 64; ++i) a = a + W2[j * 64 + i] * h1[i];
+            float h = a > 0.0f ? a : 0.0f;
+            for (int o = 0; o < 3; ++o) y[o] = y[o] + W3[o * 64 + j] * h;
+        }
+        for (int o = 0; o < 3; ++o) out[o] = y[o] * ys[o] + ym[o];
+    }
+    // The 24 contact features (see the GPU's mlp_features for the list).
+    static void mlp_features(const Row<R>* rows3, R depth, R im1, R im2, R mu, R gn_dt, R nc, R k1, R k2, R* f) {
+        for (int r = 0; r < 3; ++r) {
+            f[r] = rows3[r].rhs;
+            f[3 + r] = rows3[r].r;
+        }
+        f[6] = depth;
+        f[7] = im1;
+        f[8] = im2;
+        for (int r = 0; r < 3; ++r) {
+            R a1 = R(0), a2 = R(0);
+            for (int k = 3; k < 6; ++k) {
+                a1 = a1 + rows3[r].J1[k] * rows3[r].WJ1[k];
+                a2 = a2 + rows3[r].J2[k] * rows3[r].WJ2[k];
+            }
+            f[9 + r] = a1;
+            f[12 + r] = a2;
+        }
+        f[15] = mu;
+        f[16] = gn_dt;
+        f[17] = nc;
+        f[18] = k1;
+        f[19] = k2;
+        R iso = -(f[3] * f[0]);
+        f[20] = iso > R(0) ? iso : R(0);
+        f[21] = -(f[4] * f[1]);
+        f[22] = -(f[5] * f[2]);
+        f[23] = f[3] * gn_dt;
+    }
+    // Squared residual of one contact's rows (normal, tangent 1, tangent 2)
+    // at the current Δv for impulses lam.
+    R local_residual(const Row<R>* r3, const R* lam) const {
+        R s = R(0);
+        {
+            R d = jdot(r3[0]) + r3[0].rhs;
+            R x = lam[0] - r3[0].r * d;
+            R pr = x > R(0) ? x : R(0);
+            R phi = lam[0] - pr;
+            s = s + phi * phi;
+        }
+        R lim = r3[1].mu * lam[0];
+        for (int k = 1; k < 3; ++k) {
+            R d = jdot(r3[k]) + r3[k].rhs;
+            R x = lam[k] - r3[k].r * d;
+            R pr = x < -lim ? -lim : (x > lim ? lim : x);
+            R phi = lam[k] - pr;
+            s = s + phi * phi;
+        }
+        return s;
+    }
+
     std::vector<Row<R>> rows;
     std::vector<PosConstraint<R>> pos_constraints;
     std::vector<int> seq_warm, seq_friction, seq_normal, seq_pos;
@@ -1204,6 +1309,17 @@ public:
                              [](Manifold<R>* a, Manifold<R>* b) { return a->colour < b->colour; });
         }
         R inv_dt = (params.dt == 0.0f) ? R(0) : R(1) / R(params.dt);
+        const bool learned = params.warmstart_mode == 2;
+        if (learned && (mlp.size() != 6009 || order != ORDER_COLOUR)) {
+            last_error = "learned warm start needs a network and the colour order";
+            return false;
+        }
+        std::vector<uint32_t> kb(bodies.size(), 0);   // solver manifolds per dynamic body
+        for (Manifold<R>* m : seq) {
+            uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
+            if (bodies[b1].dynamic()) ++kb[b1];
+            if (bodies[b2].dynamic()) ++kb[b2];
+        }
         std::vector<int> ug, un, bg, bn;   // unilateral ground / non-ground, bilateral ...
         for (Manifold<R>* m : seq) {
             const Collider<R>& c1 = colliders[m->c1];
@@ -1244,6 +1360,25 @@ public:
                     rt.cache_slot = 1 + s;
                     it[s] = int(rows.size());
                     rows.push_back(rt);
+                }
+                if (learned && !k.cached) {
+                    Row<R> r3[3] = {rows[in], rows[it[0]], rows[it[1]]};
+                    R f[24];
+                    R gn_dt = (gravity.x * n.x + gravity.y * n.y + gravity.z * n.z) * R(params.dt);
+                    R im1 = b1.dynamic() ? b1.inv_aug.linear : R(0), im2 = b2.dynamic() ? b2.inv_aug.linear : R(0);
+                    mlp_features(r3, depth, im1, im2, mu, gn_dt, R(m->contacts.size()),
+                                 b1.dynamic() ? R(kb[c1.body]) : R(0), b2.dynamic() ? R(kb[c2.body]) : R(0), f);
+                    float ff[24], pl[3];
+                    for (int i = 0; i < 24; ++i) ff[i] = float(f[i]);
+                    mlp_forward(ff, pl);
+                    float ln = pl[0] > 0.0f ? pl[0] : 0.0f;
+                    float mx = float(mu) * ln;
+                    pl[0] = ln;
+                    for (int q = 1; q < 3; ++q) pl[q] = pl[q] < -mx ? -mx : (pl[q] > mx ? mx : pl[q]);
+                    rows[in].impulse = R(pl[0]);
+                    rows[it[0]].impulse = R(pl[1]);
+                    rows[it[1]].impulse = R(pl[2]);
+                    rows[in].predicted = true;
                 }
                 if (order == ORDER_COLOUR) {
                     seq_warm.push_back(in);
@@ -1351,9 +1486,32 @@ public:
     void sor_prox() {
         // SORProx::solve (sor_prox.rs:48-80).
         std::fill(dv.begin(), dv.end(), R(0));
-        for (int i : seq_warm) {
-            const Row<R>& r = rows[i];
-            if (r.impulse != R(0)) axpy(r, r.impulse);
+        for (size_t q = 0; q < seq_warm.size(); ++q) {
+            Row<R>& r = rows[seq_warm[q]];
+            if (!r.predicted) {
+                if (r.impulse != R(0)) axpy(r, r.impulse);
+                continue;
+            }
+            // A learned start (colour order: the contact's three rows follow
+            // each other) stays only if its local residual is no larger than
+            // the zero start's.
+            Row<R>* r3[3] = {&rows[seq_warm[q]], &rows[seq_warm[q + 1]], &rows[seq_warm[q + 2]]};
+            Row<R> c3[3] = {*r3[0], *r3[1], *r3[2]};
+            std::vector<R> before = dv;
+            R lam[3] = {c3[0].impulse, c3[1].impulse, c3[2].impulse};
+            for (int k = 0; k < 3; ++k)
+                if (lam[k] != R(0)) axpy(c3[k], lam[k]);
+            const R zero[3] = {R(0), R(0), R(0)};
+            R with = local_residual(c3, lam);
+            std::vector<R> after = dv;
+            dv = before;
+            R without = local_residual(c3, zero);
+            if (with > without) {
+                for (int k = 0; k < 3; ++k) r3[k]->impulse = R(0);
+            } else {
+                dv = after;
+            }
+            q += 2;
         }
         counters.residual_initial = residual();
         uint32_t iters = 0;
