@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 2u
+#define NPGPU_ABI_VERSION 3u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -179,6 +179,9 @@ typedef struct npgpu_params {
     float activation_mix;                  /* ActivationManager::new(0.01), mechanical_world.rs:80 */
     uint32_t profile;                      /* non-zero: time each phase with CUDA events */
     uint32_t solver_schedule;              /* NPGPU_SCHEDULE_*: how the velocity and position solvers run */
+    uint32_t use_graph;                    /* 1: run each step from a CUDA graph, captured on first use and
+                                              replayed while nothing the launches bake in changes (the
+                                              world's shape, parameters, buffers); ignored when profiling */
 } npgpu_params;
 
 /* Per-step counters: the stage names of src/counters/mod.rs:18-209 plus
@@ -214,6 +217,11 @@ typedef struct npgpu_counters {
     double velocity_wait_ms;         /* summed time threads spent waiting for their bodies */
     double velocity_kernel_ms;       /* duration of the velocity kernel on the device clock */
     uint64_t velocity_tasks;         /* tasks executed */
+    /* Learned warm start (params.warmstart_mode == 2). */
+    uint32_t learned_starts;         /* new contacts started from the network's prediction */
+    uint32_t learned_kept;           /* ... of which the warm-start sweep kept the prediction */
+    uint32_t graph_replay;           /* 1 if the last step ran from a CUDA graph */
+    uint32_t reserved;
 } npgpu_counters;
 
 /* Contact record returned for parity checks (a TrackedContact,

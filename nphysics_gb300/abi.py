@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 2
+NPGPU_ABI_VERSION = 3
 
 # npgpu_status
 OK = 0
@@ -117,6 +117,7 @@ class Params(C.Structure):
         ("activation_mix", C.c_float),
         ("profile", C.c_uint32),
         ("solver_schedule", C.c_uint32),
+        ("use_graph", C.c_uint32),
     ]
 
 
@@ -150,6 +151,10 @@ class Counters(C.Structure):
         ("velocity_wait_ms", C.c_double),
         ("velocity_kernel_ms", C.c_double),
         ("velocity_tasks", C.c_uint64),
+        ("learned_starts", C.c_uint32),
+        ("learned_kept", C.c_uint32),
+        ("graph_replay", C.c_uint32),
+        ("reserved", C.c_uint32),
     ]
 
     def as_dict(self):
@@ -196,6 +201,7 @@ def default_params():
     p.activation_mix = 0.01
     p.profile = 0
     p.solver_schedule = SCHEDULE_AUTO
+    p.use_graph = 1
     return p
 
 

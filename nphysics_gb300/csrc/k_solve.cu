@@ -497,6 +497,8 @@ __global__ void k_act_init(World w, StepParams p) {
         c->res_acc_init[1] = 0.0;
         c->world_next[0] = 0u;
         c->world_next[1] = 0u;
+        c->learned_starts = 0u;
+        c->learned_kept = 0u;
     }
 }
 
@@ -766,6 +768,7 @@ __global__ void k_assemble(World w, StepParams p) {
                     mlp_project(mu, pl);
                     // .w = 1: a predicted start, checked in the warm-start sweep.
                     lam[k] = make_float4(pl[0], pl[1], pl[2], 1.0f);
+                    atomicAdd(&w.ctl->learned_starts, 1u);
                 }
             }
         }
@@ -860,7 +863,7 @@ struct CachedContacts {
 // `dvbase` (-1: no dofs), the global Δv array or a world's shared-memory Δv.
 template <class Src, class BM>
 __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, uint32_t mask, uint32_t sweep,
-                                                  const BM& bm, bool h1, bool h2, DV& dv) {
+                                                  const BM& bm, bool h1, bool h2, DV& dv, Control* ctl) {
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = src.rec(k);
         float4 l = src.get_lam(k);
@@ -887,6 +890,7 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
                     src.set_lam(k, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
                 } else {
                     src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
+                    atomicAdd(&ctl->learned_kept, 1u);
                 }
             }
         } else if (sweep & 1u) {
@@ -938,7 +942,7 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     DV dv;
     load_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
     load_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
-    velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv);
+    velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
     store_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
     store_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
 }
@@ -1051,14 +1055,14 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
             if (k == 0 && cached) {
-                velocity_task_src(cc, nc0, mask0, sw, cc, b1 >= 0, b2 >= 0, dv);
+                velocity_task_src(cc, nc0, mask0, sw, cc, b1 >= 0, b2 >= 0, dv, w.ctl);
             } else {
                 const uint32_t m = t + k * T;
                 BodyMasses bm;
                 if (b1 >= 0) bm.s[0] = load_sb(w.b.sb, b1);
                 if (b2 >= 0) bm.s[1] = load_sb(w.b.sb, b2);
                 GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
-                velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv);
+                velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv, w.ctl);
             }
             publish_dvf(w.b.dvf, b1, t1 + 1u, dv.a);
             publish_dvf(w.b.dvf, b2, t2 + 1u, dv.b);

@@ -154,6 +154,17 @@ struct npgpu_world {
     uint32_t sample_cap = 0;
     float* d_feat = nullptr;
     uint32_t max_world = 0;              // largest world index any body had (never lowered)
+    std::vector<uint32_t> unregistered;  // colliders whose mass is not yet added to their body
+    // CUDA graphs of one step (body start, solver, end-of-step collision
+    // detection), one per parity of the double-buffered pair sets, keyed by
+    // every value their launches bake in.
+    struct GraphSlot {
+        std::vector<uint8_t> key;
+        cudaGraphExec_t exec = nullptr;
+    } graphs[2];
+    int graph_next = 0;
+    bool graphs_broken = false;          // capture failed once: run eagerly from then on
+    bool last_step_graphed = false;
     int grid_world = 0;
 };
 
@@ -182,7 +193,7 @@ static npgpu_status cuda_fail(npgpu_world* w, cudaError_t e, const char* what) {
 
 static StepParams step_params(const npgpu_world* w) {
     const npgpu_params& p = w->params;
-    StepParams s;
+    StepParams s{};
     s.dt = p.dt;
     s.inv_dt = (p.dt == 0.0f) ? 0.0f : 1.0f / p.dt;
     s.erp = p.erp;
@@ -358,6 +369,7 @@ void npgpu_default_params(npgpu_params* p) {
     p->activation_mix = 0.01f;
     p->profile = 0;
     p->solver_schedule = NPGPU_SCHEDULE_AUTO;
+    p->use_graph = 1;
 }
 
 static npgpu_status create_buffers(npgpu_world* w) {
@@ -475,6 +487,8 @@ void npgpu_destroy(npgpu_world* w) {
     cudaFree(w->dw.s.world_start);
     cudaFree(w->dw.s.bucket_count);
     cudaFree(w->dw.s.bucket_start);
+    for (auto& g : w->graphs)
+        if (g.exec) cudaGraphExecDestroy(g.exec);
     for (void* p : {(void*)w->d_net, (void*)w->d_prm, (void*)w->d_m1, (void*)w->d_m2, (void*)w->d_grad,
                     (void*)w->d_stats, (void*)w->d_samples, (void*)w->d_feat})
         cudaFree(p);
@@ -644,6 +658,7 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         }
         hc.alive = true;
         hc.registered = false;
+        w->unregistered.push_back((uint32_t)slot);
         hc.gen = handles[k].generation;
         hc.desc = d;
         w->forget[slot] = std::max<uint8_t>(w->forget[slot], 1);
@@ -760,7 +775,12 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
 // inserted since the last step, adding their mass to their body
 // (geometrical_world.rs:102-143), and forget the manifolds of removed colliders.
 static npgpu_status maintain(npgpu_world* w) {
-    for (uint32_t ci = 0; ci < w->nc_slots; ++ci) {
+    // Colliders inserted or replaced since the last step, in slot order.
+    std::sort(w->unregistered.begin(), w->unregistered.end());
+    w->unregistered.erase(std::unique(w->unregistered.begin(), w->unregistered.end()), w->unregistered.end());
+    std::vector<uint32_t> todo;
+    todo.swap(w->unregistered);
+    for (uint32_t ci : todo) {
         HostCollider& c = w->hc[ci];
         if (!c.alive || c.registered) continue;
         c.registered = true;
@@ -831,6 +851,75 @@ static npgpu_status run_cd(npgpu_world* w, const StepParams& sp) {
     return NPGPU_OK;
 }
 
+// Every value a step's launches bake in: the device view of the world, the
+// step parameters and the solver's launch shape.
+static std::vector<uint8_t> graph_key(const npgpu_world* w, const StepParams& sp) {
+    std::vector<uint8_t> k;
+    auto put = [&](const void* p, size_t n) {
+        const uint8_t* b = (const uint8_t*)p;
+        k.insert(k.end(), b, b + n);
+    };
+    put(&w->dw, sizeof(w->dw));
+    put(&sp, sizeof(sp));
+    const SolverLaunch& L = w->solver;
+    int ints[5] = {L.grid_colour, L.grid_velocity, L.grid_position, L.grid_world, L.batched ? 1 : 0};
+    put(ints, sizeof(ints));
+    put(&L.scan_temp, sizeof(L.scan_temp));
+    put(&L.scan_bytes, sizeof(L.scan_bytes));
+    put(&L.n_worlds, sizeof(L.n_worlds));
+    put(&L.max_world_bodies, sizeof(L.max_world_bodies));
+    put(&w->sort_temp, sizeof(w->sort_temp));
+    put(&w->sort_bytes, sizeof(w->sort_bytes));
+    return k;
+}
+
+// One step (body start, solver, end-of-step collision detection) from a CUDA
+// graph: replayed when a graph with the same key exists, else captured from
+// the stream and then launched. Sets last_step_graphed; when capture is not
+// possible it leaves the step to the eager path and stops trying.
+static npgpu_status step_graphed(npgpu_world* w, const StepParams& sp) {
+    w->solver.ev = nullptr;
+    std::vector<uint8_t> key = graph_key(w, sp);
+    npgpu_world::GraphSlot* g = nullptr;
+    for (auto& s : w->graphs)
+        if (s.exec && s.key == key) g = &s;
+    if (g) {
+        std::swap(w->dw.cur, w->dw.prev);   // what run_cd does on the host side
+        sync_world_view(w);
+    } else {
+        g = &w->graphs[w->graph_next];
+        w->graph_next ^= 1;
+        if (g->exec) cudaGraphExecDestroy(g->exec);
+        g->exec = nullptr;
+        g->key.clear();
+        World before = w->dw;
+        cudaGraph_t graph = nullptr;
+        cudaError_t e = cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaError_t e1 = launch_body_start(w->dw, sp, w->stream);
+            cudaError_t e2 = e1 == cudaSuccess ? launch_solver(w->dw, sp, w->solver, w->stream) : e1;
+            npgpu_status s3 = e2 == cudaSuccess ? run_cd(w, sp) : NPGPU_ERR_CUDA;
+            e = cudaStreamEndCapture(w->stream, &graph);
+            if (s3 != NPGPU_OK && e == cudaSuccess) e = cudaErrorStreamCaptureInvalidated;
+        }
+        cudaGraphExec_t exec = nullptr;
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&exec, graph, 0);
+        if (graph) cudaGraphDestroy(graph);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            w->graphs_broken = true;
+            w->dw = before;                  // nothing ran: the eager path takes the step
+            sync_world_view(w);
+            return NPGPU_OK;
+        }
+        g->exec = exec;
+        g->key = key;
+    }
+    CK(cudaGraphLaunch(g->exec, w->stream), "graph launch");
+    w->last_step_graphed = true;
+    return NPGPU_OK;
+}
+
 npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, uint32_t num_force_generators) {
     if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
     if (num_joints) return fail(w, NPGPU_ERR_NONEMPTY_JOINTS, "joint constraints are not supported");
@@ -843,7 +932,19 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
         npgpu_status st = maintain(w);
         if (st != NPGPU_OK) return st;
         sync_world_view(w);
+        st = prepare_schedule(w);
+        if (st != NPGPU_OK) return st;
         bool prof = w->params.profile != 0;
+        w->last_step_graphed = false;
+        if (!prof && w->params.use_graph && !w->cd_dirty && !w->graphs_broken) {
+            st = step_graphed(w, sp);
+            if (st != NPGPU_OK) return st;
+            if (w->last_step_graphed) {
+                w->cd_start_ran = false;
+                w->counters.steps += 1;
+                continue;
+            }
+        }
         if (prof) CK(cudaEventRecord(w->ev[0], w->stream), "event");
         CK(launch_body_start(w->dw, sp, w->stream), "body start");
         w->cd_start_ran = w->cd_dirty;
@@ -854,8 +955,6 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
         }
         if (prof) CK(cudaEventRecord(w->ev[1], w->stream), "event");
         w->solver.ev = prof ? w->ev_solver : nullptr;
-        st = prepare_schedule(w);
-        if (st != NPGPU_OK) return st;
         CK(launch_solver(w->dw, sp, w->solver, w->stream), "solve");
         if (prof) CK(cudaEventRecord(w->ev[2], w->stream), "event");
         st = run_cd(w, sp);
@@ -1226,6 +1325,9 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
         k.max_penetration = v;
     }
     k.kinetic_energy = c.kinetic_energy;
+    k.learned_starts = c.learned_starts;
+    k.learned_kept = c.learned_kept;
+    k.graph_replay = w->last_step_graphed ? 1u : 0u;
     if (w->params.profile && w->ev_recorded) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, w->ev[0], w->ev[3]);

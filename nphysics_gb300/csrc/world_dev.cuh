@@ -156,6 +156,7 @@ struct Control {
     double res_acc_init[2];          // batched worlds: residual sums after the warm start
     uint32_t world_next[2];          // batched worlds: work counters of the velocity / position kernels
     uint32_t mlp_samples;            // training samples recorded so far
+    uint32_t learned_starts, learned_kept;   // learned warm start: predictions made / kept this step
     uint32_t pad2;
     double mlp_loss;                 // loss of the last training step
 };

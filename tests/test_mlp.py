@@ -117,3 +117,35 @@ def test_training_reduces_loss(gpu_lib):
     first = g.mlp_train(1, batch=1024, lr=1e-3, seed=3, init=True)
     last = g.mlp_train(400, batch=1024, lr=1e-3, seed=4)
     assert last < 0.5 * first, (first, last)
+
+
+@pytest.mark.gpu
+def test_trained_network_lowers_the_warm_start_residual(gpu_lib):
+    # Train on the solver's own converged impulses of a 1000-ball pile, then
+    # run the pile again with and without the network (8 iterations a step):
+    # the residual after the warm start, averaged over the steps with
+    # contacts, drops (measured: about 30% on a 4096-ball pile).
+    from nphysics_gb300.world import GpuWorld
+    sc = scenes.ball_pile(side=10)
+    g = _record(sc, steps=150)
+    g.mlp_train(1, batch=4096, lr=1e-3, seed=1, init=True)
+    g.mlp_train(1500, batch=4096, lr=1e-3, seed=2)
+    net = g.mlp_get()
+    out = {}
+    for mode in (abi.WARMSTART_CACHE, abi.WARMSTART_LEARNED):
+        p = sc.params()
+        p.warmstart_mode = mode
+        w = GpuWorld.for_scene(sc, p)
+        if mode == abi.WARMSTART_LEARNED:
+            w.mlp_set(net)
+        r0, kept = [], 0
+        for _ in range(150):
+            w.step(1)
+            c = w.counters()
+            if c["num_solver_contacts"]:
+                r0.append(c["residual_initial"])
+            kept += c["learned_kept"]
+        out[mode] = (float(np.mean(r0)), kept)
+    plain, learned = out[abi.WARMSTART_CACHE], out[abi.WARMSTART_LEARNED]
+    assert learned[1] > 0
+    assert learned[0] < 0.9 * plain[0], (plain, learned)
