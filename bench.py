@@ -34,6 +34,9 @@ PROFILE_STEPS = 10
 # Kernels of one step of this workload (ours and CUB's radix sort and scans),
 # counted from the ncu launch list of this command (profiles/launches_ball_pile_32k.md).
 LAUNCHES_PER_STEP = 21
+# The batched-worlds schedule: the two cooperative solver kernels become five
+# per-world kernels (bucket count and scatter, velocity, residual, position).
+LAUNCHES_PER_STEP_BATCHED = 24
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_velocity launch on this
 # workload, from one ncu capture (profiles/k_velocity_ball_pile_32k.md).
 VELOCITY_TRAFFIC_PER_LAUNCH = 16809728
@@ -46,6 +49,10 @@ def parse():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--settle", type=int, default=200)
     ap.add_argument("--side", type=int, default=32)
+    ap.add_argument("--workload", default="pile", choices=["pile", "batched"],
+                    help="pile: the 32^3 ball pile (replicas on N GPUs); batched: --worlds-per-rank worlds "
+                         "of the batched-worlds scene per GPU (the batch sharded across ranks)")
+    ap.add_argument("--worlds-per-rank", type=int, default=4096)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -175,25 +182,34 @@ def run_gpu(args):
     from nphysics_gb300 import build, scenes
     from nphysics_gb300.world import GpuWorld
 
-    rank = int(os.environ.get("RANK", "0"))
-    world_size = int(os.environ.get("WORLD_SIZE", "1"))
-    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    from nphysics_gb300 import multirank
+    rank, world_size, local_rank = multirank.rank_env()
     torch.cuda.set_device(local_rank)
     if world_size > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
     build.build()
     torch.cuda.init()
-    # Replicas: every rank runs its own copy of the workload (one world per GPU).
-    sc = scenes.ball_pile(side=args.side)
+    if args.workload == "pile":
+        # Replicas: every rank runs its own copy of the pile (one world per GPU).
+        sc = scenes.ball_pile(side=args.side)
+        w = GpuWorld.for_scene(sc, sc.params())
+        workload = (f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, seeded jitter) "
+                    f"on a static ground, dt 1/60, 8 velocity / 3 position iterations")
+    else:
+        # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
+        n_all = args.worlds_per_rank * world_size
+        sc = scenes.batched_worlds(n_worlds=n_all, worlds=multirank.shard(n_all, rank, world_size))
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=6)
+        workload = (f"batched worlds: {args.worlds_per_rank} worlds per GPU (of {n_all}), body counts "
+                    f"log-uniform in [16, 2048] ({sc.num_dynamic} bodies on rank 0), ball piles and box stacks "
+                    f"on their own grounds, dt 1/60, 8 velocity / 3 position iterations, one block per world")
     p = sc.params()
-    w = GpuWorld.for_scene(sc, p)
     stream = torch.cuda.ExternalStream(w.stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     n_dyn = sc.num_dynamic
     w.step(args.settle)
     w.step(args.warmup)
-    c0 = w.counters()
 
     # ---- device-resident timing -------------------------------------------------------
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
@@ -213,12 +229,8 @@ def run_gpu(args):
     if world_size > 1:
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = sum(step_ms)
-    if world_size > 1:
-        t = torch.tensor([total_ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        total_ms = float(t.item())
-    value = world_size * n_dyn * args.steps / (total_ms * 1e-3)
+    total_ms = multirank.reduce_max(sum(step_ms), device="cuda")
+    value = multirank.reduce_sum(n_dyn * args.steps, device="cuda") / (total_ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ------------------------------------
     pos = np.zeros((len(sc.bodies), 7), np.float32)
@@ -233,9 +245,9 @@ def run_gpu(args):
         w.step(1, sync=False)
         w.download_into(pos, vel)
     e2e_s = time.perf_counter() - t0
-    h2d = len(dyn) * (4 + 4 + 24)
-    d2h = len(sc.bodies) * (7 + 6) * 4
-    e2e_value = world_size * n_dyn * args.steps / e2e_s
+    h2d = handles.nbytes + forces.nbytes          # 16-byte handles and 6 force floats per dynamic body
+    d2h = pos.nbytes + vel.nbytes                 # every body's pose and velocity
+    e2e_value = multirank.reduce_sum(n_dyn * args.steps, device="cuda") / multirank.reduce_max(e2e_s, device="cuda")
 
     # ---- phase times (CUDA events on the world's stream), after the timed region ----------
     p.profile = 1
@@ -264,25 +276,27 @@ def run_gpu(args):
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"ball pile {args.side}^3 = {n_dyn} balls (radius 0.5, 1.2 lattice, seeded jitter) "
-                               f"on a static ground, dt 1/60, 8 velocity / 3 position iterations; timed steps "
+        "config": {"workload": f"{workload}; timed steps "
                                f"{args.settle + args.warmup}..{args.settle + args.warmup + args.steps - 1} of the run",
-                   "l2": "flushed (256 MiB write) between timed steps", "parallelism": "replicas",
+                   "l2": "flushed (256 MiB write) between timed steps",
+                   "parallelism": "replicas" if args.workload == "pile" else f"worlds sharded over {world_size} GPUs",
                    "contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
                    "solver_contacts": int(K), "active_bodies": int(B),
                    "colours": int(statistics.mean(c["num_colours"] for c in counters))},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "k_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": VELOCITY_TRAFFIC_PER_LAUNCH, "peak_source": peak_kind,
+        "roofline": {"bound": "hbm", "kernel": "k_velocity" if args.workload == "pile" else "k_world_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "traffic": VELOCITY_TRAFFIC_PER_LAUNCH if args.workload == "pile" else None,
+                     "peak_source": peak_kind,
                      "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
         "clocks": {"sm_mhz": cl["sm_mhz"], "sm_max_mhz": cl["sm_max_mhz"], "reasons": cl["reasons"]},
-        "gpu_launches": LAUNCHES_PER_STEP * args.steps,
+        "gpu_launches": (LAUNCHES_PER_STEP if args.workload == "pile" else LAUNCHES_PER_STEP_BATCHED) * args.steps,
         "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
                      ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",
                       "velocity_update_time", "position_resolution_time")},
     }
-    if rank == 0 and world_size == 1 and not args.no_cpu_baseline:
+    if rank == 0 and world_size == 1 and not args.no_cpu_baseline and args.workload == "pile":
         line["cpu_baseline"] = cpu_baseline(lambda: scenes.ball_pile(side=args.side), args.cpu_seconds, args.settle)
     if rank == 0:
         print(json.dumps(line))

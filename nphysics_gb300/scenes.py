@@ -185,28 +185,34 @@ def mixed_pile(n=100_000, seed=1234, friction=0.5, spacing=2.0, footprint=100.0)
     return Scene(f"mixed pile ({n} bodies)", bodies, colliders, steps=300, info={"bodies": n})
 
 
-def batched_worlds(n_worlds=4096, seed=1234, lo=16, hi=2048):
+def batched_worlds(n_worlds=4096, seed=1234, lo=16, hi=2048, worlds=None):
     """C4: independent worlds with body counts log-uniform in [16, 2048], each
     a scaled-down ball pile or a box stack of height U(3, 15) on its own ground.
-    Worlds share space; the world index keeps them apart."""
+    Worlds share space; the world index keeps them apart.
+
+    `worlds` (a range, default all) builds only those worlds of the batch, with
+    the same bodies as in the whole batch, renumbered from world 0: the shard
+    of one rank when the batch is split across GPUs."""
     rng = np.random.default_rng(seed)
     counts = np.round(np.exp(rng.uniform(math.log(lo), math.log(hi), size=n_worlds))).astype(int)
     kinds = rng.random(n_worlds) < 0.5
+    worlds = range(n_worlds) if worlds is None else worlds
     parts_b, parts_c = [], []
-    for w in range(n_worlds):
+    for local, w in enumerate(worlds):
+        wr = np.random.default_rng([seed, w])       # the world's own draws
         nb = int(counts[w])
-        g, gc = _ground(half=(60.0, 1.0, 60.0), world=w)
+        g, gc = _ground(half=(60.0, 1.0, 60.0), world=local)
         b = body_descs(nb)
-        b["world"] = w
+        b["world"] = local
         if kinds[w]:
             side = int(math.ceil(nb ** (1.0 / 3.0)))
             idx = np.arange(nb)
             i, j, k = idx % side, (idx // side) % side, idx // (side * side)
             pos = np.stack([(i - (side - 1) / 2) * 1.2, 1.0 + k * 1.2, (j - (side - 1) / 2) * 1.2], axis=1)
-            pos += rng.uniform(-0.05, 0.05, size=pos.shape)
+            pos += wr.uniform(-0.05, 0.05, size=pos.shape)
             c = collider_descs(nb, np.arange(nb), abi.SHAPE_BALL, (0.5, 0, 0), density=1.0, friction=0.3)
         else:
-            height = int(rng.integers(3, 16))
+            height = int(wr.integers(3, 16))
             cols = int(math.ceil(nb / height))
             cs = int(math.ceil(math.sqrt(cols)))
             idx = np.arange(nb)
@@ -218,8 +224,8 @@ def batched_worlds(n_worlds=4096, seed=1234, lo=16, hi=2048):
         parts_b += [g, b]
         parts_c += [gc, c]
     bodies, colliders = _concat(parts_b, parts_c)
-    return Scene(f"{n_worlds} batched worlds", bodies, colliders, steps=100,
-                 info={"worlds": n_worlds, "bodies": int(counts.sum())})
+    return Scene(f"{len(worlds)} of {n_worlds} batched worlds", bodies, colliders, steps=100,
+                 info={"worlds": len(worlds), "bodies": int(counts[list(worlds)].sum())})
 
 
 def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234):
