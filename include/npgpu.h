@@ -182,6 +182,8 @@ typedef struct npgpu_params {
     uint32_t use_graph;                    /* 1: run each step from a CUDA graph, captured on first use and
                                               replayed while nothing the launches bake in changes (the
                                               world's shape, parameters, buffers); ignored when profiling */
+    uint32_t world_threads;                /* threads per world block of NPGPU_SCHEDULE_WORLDS: 64, 128 or
+                                              256 (0: 128); npgpu_autotune chooses it */
 } npgpu_params;
 
 /* Per-step counters: the stage names of src/counters/mod.rs:18-209 plus
@@ -290,6 +292,16 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints,
 
 /* Waits for the world's stream and reports any device-side error flag. */
 npgpu_status npgpu_synchronize(npgpu_world* w);
+
+/* Chooses the solver's launch shape for the current scene by timing real
+ * steps: the one-grid schedule and, when the worlds qualify, one block per
+ * world with 64, 128 and 256 threads, each for 1 + steps_per_candidate steps.
+ * Every candidate computes the same bits, so the world simply advances by
+ * those steps. Sets params.solver_schedule and params.world_threads to the
+ * fastest and reports them (any out pointer may be NULL). No counterpart in
+ * the reference. */
+npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32_t* schedule,
+                            uint32_t* world_threads, float* ms_per_step);
 
 /* Copies body state to host arrays indexed by slot (any pointer may be NULL):
  * position[7n], velocity[6n], energy[n] (activation energy), active[n]

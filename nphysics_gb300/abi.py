@@ -118,6 +118,7 @@ class Params(C.Structure):
         ("profile", C.c_uint32),
         ("solver_schedule", C.c_uint32),
         ("use_graph", C.c_uint32),
+        ("world_threads", C.c_uint32),
     ]
 
 
@@ -202,6 +203,7 @@ def default_params():
     p.profile = 0
     p.solver_schedule = SCHEDULE_AUTO
     p.use_graph = 1
+    p.world_threads = 0
     return p
 
 
@@ -249,6 +251,7 @@ def load_library(path=LIB_PATH):
         "npgpu_last_error": (C.c_char_p, [W]),
         "npgpu_find_pairs_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
                                               C.c_void_p, C.c_void_p]),
+        "npgpu_autotune": (C.c_int, [W, C.c_uint32, P(C.c_uint32), P(C.c_uint32), P(C.c_float)]),
         "npgpu_mlp_set": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_get": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_record": (C.c_int, [W, C.c_uint32]),
@@ -271,7 +274,7 @@ EXPORTED = [
     "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_step",
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
     "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
-    "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
+    "npgpu_autotune", "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
 ]
 
 # Learned warm start (npgpu_mlp_*).

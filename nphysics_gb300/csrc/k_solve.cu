@@ -1258,7 +1258,8 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
 // Persistent: each block takes worlds from a counter until none is left,
 // largest first, so that the last worlds to start are short ones.
 // Dynamic shared memory: 6 floats per body slot of the largest world.
-__global__ void __launch_bounds__(kWorldThreads, 4) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
                                                                   uint32_t max_world_bodies) {
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
@@ -1532,7 +1533,8 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
 }
 
 // Batched worlds: block per world, colour by colour, poses in global memory.
-__global__ void __launch_bounds__(kWorldThreads) k_world_position(World w, StepParams p, uint32_t n_worlds) {
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds) {
     __shared__ uint32_t s_world;
     const uint32_t ncol = w.ctl->ncolours;
     for (;;) {
@@ -1622,15 +1624,22 @@ void solver_grid_sizes(int device, SolverLaunch& L) {
     L.grid_velocity = sms * (per < 1 ? 1 : per);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_position, kCoopThreads, 0);
     L.grid_position = sms * (per < 1 ? 1 : per);
-    cudaFuncSetAttribute(k_world_velocity, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(6 * kMaxWorldBodies * sizeof(float)));
+    for (const void* f : {(const void*)k_world_velocity<64>, (const void*)k_world_velocity<128>,
+                          (const void*)k_world_velocity<256>})
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(6 * kMaxWorldBodies * sizeof(float)));
 }
 
-int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds) {
+uint64_t grid_task_capacity(const SolverLaunch& L) {
+    int g = L.grid_velocity < L.grid_position ? L.grid_velocity : L.grid_position;
+    return (uint64_t)g * kCoopThreads * kMaxPerThread;
+}
+
+int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds, int threads) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_world_velocity, kWorldThreads,
-                                                  6 * (size_t)max_world_bodies * sizeof(float));
+    const void* f = threads == 64 ? (const void*)k_world_velocity<64>
+                                  : threads == 256 ? (const void*)k_world_velocity<256> : (const void*)k_world_velocity<128>;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, threads, 6 * (size_t)max_world_bodies * sizeof(float));
     long g = (long)sms * (per < 1 ? 1 : per);
     if (g > (long)n_worlds) g = n_worlds;
     return g < 1 ? 1 : (int)g;
@@ -1677,8 +1686,13 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
                                           st);
         if (e != cudaSuccess) return e;
         k_world_scatter<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
-        k_world_velocity<<<L.grid_world, kWorldThreads, 6 * (size_t)L.max_world_bodies * sizeof(float), st>>>(
-            wc, pc, L.n_worlds, L.max_world_bodies);
+        const size_t smem = 6 * (size_t)L.max_world_bodies * sizeof(float);
+        if (L.world_threads == 64)
+            k_world_velocity<64><<<L.grid_world, 64, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies);
+        else if (L.world_threads == 256)
+            k_world_velocity<256><<<L.grid_world, 256, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies);
+        else
+            k_world_velocity<128><<<L.grid_world, 128, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies);
         k_world_finish<<<1, 1, 0, st>>>(wc, pc);
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
@@ -1691,7 +1705,12 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     k_cache_integrate<<<nbb > npb ? nbb : npb, kItemThreads, 0, st>>>(wc, pc, posef);
     rec(5);
     if (L.batched) {
-        k_world_position<<<L.grid_world, kWorldThreads, 0, st>>>(wc, pc, L.n_worlds);
+        if (L.world_threads == 64)
+            k_world_position<64><<<L.grid_world, 64, 0, st>>>(wc, pc, L.n_worlds);
+        else if (L.world_threads == 256)
+            k_world_position<256><<<L.grid_world, 256, 0, st>>>(wc, pc, L.n_worlds);
+        else
+            k_world_position<128><<<L.grid_world, 128, 0, st>>>(wc, pc, L.n_worlds);
     } else {
         e = coop((const void*)k_position, L.grid_position, args2, st);
         if (e != cudaSuccess) return e;

@@ -333,7 +333,13 @@ static npgpu_status prepare_schedule(npgpu_world* w) {
         CK(cudaMemcpyAsync(s.world_start, w->world_start.data(), sizeof(uint32_t) * (2 * (size_t)w->n_worlds + 1),
                            cudaMemcpyHostToDevice, w->stream),
            "world ranges");
-        w->grid_world = world_grid(w->device, w->max_world_bodies, w->n_worlds);
+        w->solver.world_threads = 0;   // grid size below
+    }
+    const uint32_t wt = w->params.world_threads;
+    const int threads = (wt == 64 || wt == 256) ? (int)wt : 128;
+    if (threads != w->solver.world_threads) {
+        w->grid_world = world_grid(w->device, w->max_world_bodies, w->n_worlds, threads);
+        w->solver.world_threads = threads;
     }
     w->solver.n_worlds = w->n_worlds;
     w->solver.max_world_bodies = w->max_world_bodies;
@@ -370,6 +376,7 @@ void npgpu_default_params(npgpu_params* p) {
     p->profile = 0;
     p->solver_schedule = NPGPU_SCHEDULE_AUTO;
     p->use_graph = 1;
+    p->world_threads = 0;
 }
 
 static npgpu_status create_buffers(npgpu_world* w) {
@@ -510,6 +517,9 @@ npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params) {
     if (!(params->dt >= 0.0f)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "dt must be >= 0");
     if (params->solver_schedule > NPGPU_SCHEDULE_WORLDS)
         return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown solver_schedule");
+    if (params->world_threads != 0 && params->world_threads != 64 && params->world_threads != 128 &&
+        params->world_threads != 256)
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "world_threads must be 0, 64, 128 or 256");
     w->params = *params;
     return NPGPU_OK;
 }
@@ -862,7 +872,7 @@ static std::vector<uint8_t> graph_key(const npgpu_world* w, const StepParams& sp
     put(&w->dw, sizeof(w->dw));
     put(&sp, sizeof(sp));
     const SolverLaunch& L = w->solver;
-    int ints[5] = {L.grid_colour, L.grid_velocity, L.grid_position, L.grid_world, L.batched ? 1 : 0};
+    int ints[6] = {L.grid_colour, L.grid_velocity, L.grid_position, L.grid_world, L.batched ? 1 : 0, L.world_threads};
     put(ints, sizeof(ints));
     put(&L.scan_temp, sizeof(L.scan_temp));
     put(&L.scan_bytes, sizeof(L.scan_bytes));
@@ -985,6 +995,64 @@ npgpu_status npgpu_synchronize(npgpu_world* w) {
             return fail(w, NPGPU_ERR_CAPACITY, "more solver manifolds than the cooperative grid holds (16 per thread)");
         if (err & ERRF_WORLD_RANGE) return fail(w, NPGPU_ERR_CUDA, "a solver manifold left its world's slot range");
     }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32_t* schedule, uint32_t* world_threads,
+                            float* ms_per_step) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (steps_per_candidate == 0) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "steps_per_candidate must be > 0");
+    if (w->params.profile) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "autotune with profiling off");
+    struct Cand {
+        uint32_t schedule, threads;
+    };
+    // The one-grid schedule is a candidate while the last step's solver
+    // manifolds fit its cooperative grid (with a 2x margin for growth).
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    uint32_t nsolver = 0;
+    CK(cudaMemcpy(&nsolver, &w->ctl->nsolver, sizeof(nsolver), cudaMemcpyDeviceToHost), "solver manifolds");
+    std::vector<Cand> cands;
+    if (2ull * nsolver <= grid_task_capacity(w->solver)) cands.push_back({NPGPU_SCHEDULE_GRID, 0});
+    if (w->layout_dirty) compute_layout(w), w->layout_on_device = false;
+    if (w->layout_ok && !w->params.solve_to_tolerance)
+        for (uint32_t t : {64u, 128u, 256u}) cands.push_back({NPGPU_SCHEDULE_WORLDS, t});
+    if (cands.empty()) cands.push_back({w->params.solver_schedule, w->params.world_threads});
+    const npgpu_params saved = w->params;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    CK(cudaEventCreate(&e0), "event");
+    CK(cudaEventCreate(&e1), "event");
+    float best_ms = 0.0f;
+    Cand best = cands[0];
+    npgpu_status st = NPGPU_OK;
+    for (const Cand& c : cands) {
+        w->params.solver_schedule = c.schedule;
+        w->params.world_threads = c.threads;
+        st = npgpu_step(w, 1, 0, 0);   // capture (when graphs are on) outside the timing
+        if (st != NPGPU_OK) break;
+        cudaEventRecord(e0, w->stream);
+        st = npgpu_step(w, steps_per_candidate, 0, 0);
+        if (st != NPGPU_OK) break;
+        cudaEventRecord(e1, w->stream);
+        st = npgpu_synchronize(w);
+        if (st != NPGPU_OK) break;
+        float ms = 0.0f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        ms /= (float)steps_per_candidate;
+        if (&c == &cands[0] || ms < best_ms) {
+            best_ms = ms;
+            best = c;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    w->params = saved;
+    if (st != NPGPU_OK) return st;
+    // Every candidate computes the same bits; only the launch shape is chosen.
+    w->params.solver_schedule = best.schedule;
+    w->params.world_threads = best.threads;
+    if (schedule) *schedule = best.schedule;
+    if (world_threads) *world_threads = best.threads;
+    if (ms_per_step) *ms_per_step = best_ms;
     return NPGPU_OK;
 }
 

@@ -206,14 +206,16 @@ struct SolverLaunch {
     uint32_t n_worlds;
     uint32_t max_world_bodies;       // largest body slot range of a world
     int grid_world;                  // blocks of the per-world kernels
+    int world_threads;               // threads per world block: 64, 128 or 256
 };
-constexpr int kWorldThreads = 128;
 constexpr uint32_t kMaxWorldBodies = 4096;    // per-world shared-memory Δv limit (96 KiB)
 cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st);
 void solver_grid_sizes(int device, SolverLaunch& L);
 // Blocks of the per-world kernels: resident blocks at this shared-memory size,
 // at most one per world.
-int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds);
+int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds, int threads);
+// Solver manifolds the one-grid schedule's cooperative kernels can hold.
+uint64_t grid_task_capacity(const SolverLaunch& L);
 size_t sort_temp_bytes(uint32_t n_items);
 size_t scan_temp_bytes(uint32_t n_items);
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);

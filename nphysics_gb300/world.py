@@ -167,6 +167,16 @@ class GpuWorld:
         self._check(self.L.npgpu_get_contacts(self.w, arr, n, C.byref(cnt)), "get_contacts")
         return abi.contacts_to_numpy(arr, n)
 
+    def autotune(self, steps_per_candidate=5):
+        """Times the solver's launch shapes on real steps (all give the same
+        bits) and keeps the fastest: (schedule, world_threads, ms per step)."""
+        s, t, ms = C.c_uint32(0), C.c_uint32(0), C.c_float(0.0)
+        self._check(self.L.npgpu_autotune(self.w, steps_per_candidate, C.byref(s), C.byref(t), C.byref(ms)),
+                    "autotune")
+        self.params.solver_schedule = s.value
+        self.params.world_threads = t.value
+        return s.value, t.value, ms.value
+
     # ---- learned warm start ----
     def mlp_set(self, params):
         params = np.ascontiguousarray(params, np.float32)

@@ -41,3 +41,19 @@ def test_graph_steps_match_eager_steps(gpu_lib, which):
     np.testing.assert_array_equal(a.bodies()["position"], b.bodies()["position"])
     np.testing.assert_array_equal(a.bodies()["velocity"], b.bodies()["velocity"])
     np.testing.assert_array_equal(a.pairs(), b.pairs())
+
+
+def test_autotune_keeps_the_bits(gpu_lib):
+    # The tuner advances the world by real steps under each candidate launch
+    # shape; since every shape computes the same bits, the tuned world equals
+    # one stepped the same number of times without tuning.
+    from nphysics_gb300.world import GpuWorld
+    sc = scenes.batched_worlds(n_worlds=8, seed=2, lo=8, hi=80)
+    a = GpuWorld.for_scene(sc)
+    sched, threads, ms = a.autotune(steps_per_candidate=3)
+    assert sched in (abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS) and ms > 0
+    a.step(10)
+    b = GpuWorld.for_scene(sc)
+    b.step(4 * (1 + 3) + 10)          # one grid and three world-block candidates
+    np.testing.assert_array_equal(a.bodies()["position"], b.bodies()["position"])
+    np.testing.assert_array_equal(a.bodies()["velocity"], b.bodies()["velocity"])
