@@ -47,16 +47,22 @@ def parse():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
-    ap.add_argument("--settle", type=int, default=200)
+    ap.add_argument("--settle", type=int, default=None,
+                    help="untimed steps first (default: 200 for piles and the pyramid, 60 for batched worlds, "
+                         "0 for the brick walls, whose impact phase is the workload)")
     ap.add_argument("--side", type=int, default=32)
-    ap.add_argument("--workload", default="pile", choices=["pile", "batched"],
+    ap.add_argument("--workload", default="pile", choices=["pile", "batched", "pyramid", "walls"],
                     help="pile: the 32^3 ball pile (replicas on N GPUs); batched: --worlds-per-rank worlds "
-                         "of the batched-worlds scene per GPU (the batch sharded across ranks)")
+                         "of the batched-worlds scene per GPU (the batch sharded across ranks); pyramid: the "
+                         "210-box pyramid (replicas); walls: 256 brick walls struck by balls per GPU")
     ap.add_argument("--worlds-per-rank", type=int, default=4096)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    return ap.parse_args()
+    args = ap.parse_args()
+    if args.settle is None:
+        args.settle = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0}[args.workload]
+    return args
 
 
 class ClockSampler:
@@ -196,6 +202,18 @@ def run_gpu(args):
         w = GpuWorld.for_scene(sc, sc.params())
         workload = (f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, seeded jitter) "
                     f"on a static ground, dt 1/60, 8 velocity / 3 position iterations")
+    elif args.workload == "pyramid":
+        sc = scenes.pyramid(base=20)
+        w = GpuWorld.for_scene(sc, sc.params())
+        workload = ("box pyramid: 210 cuboids of half extent 0.5 in a 20-base triangle on a static ground, "
+                    "density 1, friction 0.5, dt 1/60, 8 velocity / 3 position iterations")
+    elif args.workload == "walls":
+        # Each rank steps its own 256 walls (weak scaling).
+        sc = scenes.brick_walls(n_walls=256, seed=1234 + rank)
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
+        workload = ("brick walls: 256 walls per GPU of 50 x 40 bricks (half extents 0.5 x 0.25 x 0.25, running "
+                    "bond), each struck by 64 balls of radius 0.4, density 10, at U(20, 40) m/s; friction 0.6, "
+                    "dt 1/120, 8 velocity / 3 position iterations")
     else:
         # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
         n_all = args.worlds_per_rank * world_size
@@ -285,18 +303,19 @@ def run_gpu(args):
                    "l2": "flushed (256 MiB write) between timed steps",
                    "solver_schedule": {1: "one cooperative grid", 2: "one block per world"}[tuned[0]],
                    "world_threads": tuned[1],
-                   "parallelism": "replicas" if args.workload == "pile" else f"worlds sharded over {world_size} GPUs",
+                   "parallelism": ("replicas" if args.workload in ("pile", "pyramid")
+                                   else f"worlds sharded over {world_size} GPUs"),
                    "contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
                    "solver_contacts": int(K), "active_bodies": int(B),
                    "colours": int(statistics.mean(c["num_colours"] for c in counters))},
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "k_velocity" if args.workload == "pile" else "k_world_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
+        "roofline": {"bound": "hbm", "kernel": "k_velocity" if tuned[0] == 1 else "k_world_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": VELOCITY_TRAFFIC_PER_LAUNCH if args.workload == "pile" else None,
                      "peak_source": peak_kind,
                      "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
         "clocks": {"sm_mhz": cl["sm_mhz"], "sm_max_mhz": cl["sm_max_mhz"], "reasons": cl["reasons"]},
-        "gpu_launches": (LAUNCHES_PER_STEP if args.workload == "pile" else LAUNCHES_PER_STEP_BATCHED) * args.steps,
+        "gpu_launches": (LAUNCHES_PER_STEP if tuned[0] == 1 else LAUNCHES_PER_STEP_BATCHED) * args.steps,
         "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
                      ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",

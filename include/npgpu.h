@@ -295,7 +295,8 @@ npgpu_status npgpu_synchronize(npgpu_world* w);
 
 /* Chooses the solver's launch shape for the current scene by timing real
  * steps: the one-grid schedule and, when the worlds qualify, one block per
- * world with 64, 128 and 256 threads, each for 1 + steps_per_candidate steps.
+ * world with 64, 128 and 256 threads, each for 1 + steps_per_candidate steps,
+ * after one step with the automatic schedule that sizes the candidates.
  * Every candidate computes the same bits, so the world simply advances by
  * those steps. Sets params.solver_schedule and params.world_threads to the
  * fastest and reports them (any out pointer may be NULL). No counterpart in

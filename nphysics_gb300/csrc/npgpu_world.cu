@@ -1006,9 +1006,18 @@ npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32
     struct Cand {
         uint32_t schedule, threads;
     };
-    // The one-grid schedule is a candidate while the last step's solver
-    // manifolds fit its cooperative grid (with a 2x margin for growth).
-    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    // One step with the automatic schedule first: it gives the solver
+    // manifold count the candidates are checked against. The one-grid
+    // schedule is a candidate while that count fits its cooperative grid
+    // (with a 2x margin for growth).
+    {
+        const npgpu_params saved = w->params;
+        w->params.solver_schedule = NPGPU_SCHEDULE_AUTO;
+        npgpu_status st0 = npgpu_step(w, 1, 0, 0);
+        if (st0 == NPGPU_OK) st0 = npgpu_synchronize(w);
+        w->params = saved;
+        if (st0 != NPGPU_OK) return st0;
+    }
     uint32_t nsolver = 0;
     CK(cudaMemcpy(&nsolver, &w->ctl->nsolver, sizeof(nsolver), cudaMemcpyDeviceToHost), "solver manifolds");
     std::vector<Cand> cands;

@@ -54,6 +54,6 @@ def test_autotune_keeps_the_bits(gpu_lib):
     assert sched in (abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS) and ms > 0
     a.step(10)
     b = GpuWorld.for_scene(sc)
-    b.step(4 * (1 + 3) + 10)          # one grid and three world-block candidates
+    b.step(1 + 4 * (1 + 3) + 10)      # the sizing step, one grid and three world-block candidates
     np.testing.assert_array_equal(a.bodies()["position"], b.bodies()["position"])
     np.testing.assert_array_equal(a.bodies()["velocity"], b.bodies()["velocity"])
