@@ -469,6 +469,26 @@ public:
         if (write_back) download(bodies);
     }
 
+    // Times the solver's launch shapes on real steps and keeps the fastest in
+    // integration_parameters (npgpu_autotune). Every shape computes the same
+    // bits, so this is the same as stepping the world that many times.
+    void autotune(DefaultBodySet& bodies, DefaultColliderSet& colliders, uint32_t steps_per_candidate = 5) {
+        check(npgpu_set_params(w_, &integration_parameters));
+        maintain(bodies, colliders);
+        uint32_t schedule = 0, threads = 0;
+        check(npgpu_autotune(w_, steps_per_candidate, &schedule, &threads, nullptr));
+        integration_parameters.solver_schedule = schedule;
+        integration_parameters.world_threads = threads;
+        if (write_back) download(bodies);
+    }
+
+    // The learned warm start (npgpu_mlp_set): NPGPU_MLP_PARAMS floats, used
+    // for contacts without a cache entry once warmstart_mode is 2.
+    void set_warmstart_network(const std::vector<float>& params) {
+        check(npgpu_mlp_set(w_, params.data(), uint32_t(params.size())));
+        integration_parameters.warmstart_mode = 2;
+    }
+
 private:
     void check(npgpu_status s) {
         if (s != NPGPU_OK) throw Error(s, npgpu_last_error(w_));
