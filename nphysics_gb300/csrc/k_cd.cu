@@ -136,7 +136,6 @@ __global__ void k_lbvh_build(World w, int n) {
     int lo = i < j ? i : j, hi = i < j ? j : i;
     int left = (lo == gamma) ? (n - 1 + gamma) : gamma;
     int right = (hi == gamma + 1) ? (n - 1 + gamma + 1) : (gamma + 1);
-    w.c.node_world[i] = key_world(k[lo]) << 16 | key_world(k[hi]);
     w.c.left[i] = left;
     w.c.right[i] = right;
     w.c.parent[left] = i;
@@ -152,12 +151,13 @@ __global__ void k_lbvh_refit(World w, int n) {
     if (k >= n) return;
     uint32_t ci = w.c.vals_sorted[k];
     int node = n - 1 + k;
-    // node_max.w carries the largest owner rank (bounding radius) of the subtree.
-    float4 mx = w.c.aabb_max[ci];
-    w.c.node_min[node] = w.c.aabb_min[ci];
-    w.c.node_max[node] = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
+    // node_min.w carries the worlds under the node (first << 16 | last; the
+    // leaves sort by world first), node_max.w the largest owner rank
+    // (bounding radius) of the subtree.
+    float4 mn = w.c.aabb_min[ci], mx = w.c.aabb_max[ci];
     uint32_t wk = key_world(w.c.keys_sorted[k]);
-    w.c.node_world[node] = wk << 16 | wk;
+    w.c.node_min[node] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(wk << 16 | wk));
+    w.c.node_max[node] = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
     if (n == 1) return;
     __threadfence();
     int p = w.c.parent[node];
@@ -170,7 +170,8 @@ __global__ void k_lbvh_refit(World w, int n) {
         int l = w.c.left[p], r = w.c.right[p];
         float4 a0 = ld_cg(&w.c.node_min[l]), a1 = ld_cg(&w.c.node_max[l]);
         float4 b0 = ld_cg(&w.c.node_min[r]), b1 = ld_cg(&w.c.node_max[r]);
-        w.c.node_min[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), 1.0f);
+        uint32_t wr = (__float_as_uint(a0.w) & 0xffff0000u) | (__float_as_uint(b0.w) & 0xffffu);
+        w.c.node_min[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), __uint_as_float(wr));
         w.c.node_max[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), fmaxf(a1.w, b1.w));
         __threadfence();
         p = w.c.parent[p];
@@ -226,19 +227,22 @@ __global__ void k_bp_traverse(World w, int n) {
     float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
     float ra = c.rank[a];
     const uint32_t qw = key_world(c.keys_sorted[k]);
-    if (n >= 2) {
+    // A node is entered when its subtree holds the query's world (batched
+    // worlds share space), a collider the query may own (a larger bounding
+    // radius somewhere below) and an AABB overlapping the query's. Both
+    // children are tested at their parent, so their data loads together and
+    // only entered nodes go on the stack.
+    auto enter = [&](int node) {
+        float4 nmin = c.node_min[node], nmax = c.node_max[node];
+        uint32_t nw = __float_as_uint(nmin.w);
+        return qw >= (nw >> 16) && qw <= (nw & 0xffffu) && !(nmax.w < ra) && overlap(amin, amax, nmin, nmax);
+    };
+    if (n >= 2 && enter(0)) {
         int stack[64];
         int sp = 0;
         stack[sp++] = 0;
         while (sp > 0) {
             int node = stack[--sp];
-            // Batched worlds share space: skip subtrees of other worlds.
-            uint32_t nw = c.node_world[node];
-            if (qw < (nw >> 16) || qw > (nw & 0xffffu)) continue;
-            float4 nmax = c.node_max[node];
-            // Every leaf below has a smaller bounding radius: leaf a owns none of those pairs.
-            if (nmax.w < ra) continue;
-            if (!overlap(amin, amax, c.node_min[node], nmax)) continue;
             if (node >= n - 1) {
                 uint32_t b = c.vals_sorted[node - (n - 1)];
                 if (b != a && owns(c, a, b) && pair_allowed(w, a, b)) {
@@ -250,12 +254,16 @@ __global__ void k_bp_traverse(World w, int n) {
                     }
                     ++count;
                 }
-            } else if (sp < 62) {
-                stack[sp++] = c.left[node];
-                stack[sp++] = c.right[node];
-            } else {
-                atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+                continue;
             }
+            const int l = c.left[node], r = c.right[node];
+            const bool el = enter(l), er = enter(r);
+            if (sp + (int)el + (int)er > 64) {
+                atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+                break;
+            }
+            if (er) stack[sp++] = r;
+            if (el) stack[sp++] = l;
         }
     }
     if (!WRITE) {

@@ -91,7 +91,6 @@ struct Colliders {
     int *node_flag;
     uint32_t *leaf_count, *leaf_offset;
     uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
-    uint32_t *node_world;            // worlds under a node: first << 16 | last (leaves sort by world first)
 };
 enum : uint32_t { CI_ALIVE = 1u << 16 };
 
