@@ -13,6 +13,9 @@ untimed for --settle steps (it reaches the ground and forms contacts), then
          step, upload of the step's applied forces from pinned host memory,
          npgpu_step, download of every body's pose and velocity into host
          buffers; wall time of the loop.
+  pgs_iterations  the metric's second half on the same pile: mean SOR-Prox
+         iterations to a residual of 1e-4, impulse cache alone vs the learned
+         warm start (network trained in the run on the solver's own impulses).
   --impl reference  times the CPU oracle (the restated reference step) on
          this host instead (the Rust reference cannot be built here).
 """
@@ -59,6 +62,8 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-pgs-iterations", action="store_true",
+                    help="skip the iterations-to-1e-4 comparison of the learned and plain warm starts")
     args = ap.parse_args()
     if args.settle is None:
         args.settle = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0}[args.workload]
@@ -179,6 +184,52 @@ def run_reference(args):
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
+
+
+def pgs_iterations(scene_fn, settle, steps=30, record_steps=100, train_steps=2000):
+    """The metric's second half on the same workload: mean SOR-Prox iterations
+    to a residual of 1e-4 (at most 256), with the impulse cache alone and
+    with the learned warm start. The network is trained in this run on the
+    solver's own converged impulses of the workload (record_steps steps solved
+    to 1e-5). Both worlds are stepped `settle` steps with the default
+    parameters first, so they start the comparison from the same bits."""
+    from nphysics_gb300 import abi
+    from nphysics_gb300.train_warmstart import record
+    t0 = time.perf_counter()
+    rec = record(scene_fn(), record_steps, 1e-5, 4_000_000)
+    n_samples = rec.mlp_samples(download=False)
+    rec.mlp_train(1, batch=4096, lr=1e-3, seed=1, init=True)
+    loss = rec.mlp_train(train_steps, batch=4096, lr=1e-3, seed=2)
+    net = rec.mlp_get()
+    rec.close()
+    out = {"tolerance": 1e-4, "max_iterations": 256, "steps": steps,
+           "network": f"trained in this run: {n_samples} samples from {record_steps} steps solved to 1e-5, "
+                      f"{train_steps} Adam steps (batch 4096, lr 1e-3), final loss {loss:.3f}"}
+    from nphysics_gb300.world import GpuWorld
+    for name, mode in (("plain", abi.WARMSTART_CACHE), ("learned", abi.WARMSTART_LEARNED)):
+        sc = scene_fn()
+        w = GpuWorld.for_scene(sc, sc.params())
+        w.mlp_set(net)
+        w.step(settle)
+        p = w.params
+        p.warmstart_mode = mode
+        p.solve_to_tolerance = 1
+        p.residual_tolerance = 1e-4
+        p.max_iterations_to_tolerance = 256
+        w.set_params(p)
+        its, r0, ms = [], [], []
+        for _ in range(steps):
+            a = time.perf_counter()
+            w.step(1)
+            ms.append(time.perf_counter() - a)
+            c = w.counters()
+            its.append(c["velocity_iterations"])
+            r0.append(c["residual_initial"])
+        out[name] = {"iterations_mean": statistics.mean(its), "residual_after_warm_start": statistics.mean(r0),
+                     "body_steps_per_s": sc.num_dynamic * steps / sum(ms)}
+        w.close()
+    out["seconds"] = time.perf_counter() - t0
+    return out
 
 
 def run_gpu(args):
@@ -321,6 +372,8 @@ def run_gpu(args):
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",
                       "velocity_update_time", "position_resolution_time")},
     }
+    if rank == 0 and world_size == 1 and args.workload == "pile" and not args.no_pgs_iterations:
+        line["pgs_iterations"] = pgs_iterations(lambda: scenes.ball_pile(side=args.side), args.settle)
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline and args.workload == "pile":
         line["cpu_baseline"] = cpu_baseline(lambda: scenes.ball_pile(side=args.side), args.cpu_seconds, args.settle)
     if rank == 0:

@@ -105,12 +105,13 @@ __device__ __forceinline__ void publish_dvf(unsigned long long* dvf, int b, uint
     asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p + 4), "l"(w[4]), "l"(w[5]) : "memory");
 }
 
-// Both bodies' update counters at their expected values (a body < 0 has no
-// counter); the two loads are in flight together.
-__device__ __forceinline__ bool versions_ready(const uint32_t* ver, int b1, uint32_t t1, int b2, uint32_t t2) {
-    uint32_t v1 = b1 >= 0 ? ld_relaxed(ver + b1) : t1;
-    uint32_t v2 = b2 >= 0 ? ld_relaxed(ver + b2) : t2;
-    return v1 == t1 && v2 == t2;
+__device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long long* p) {
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
+    asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 __device__ __forceinline__ bool err_set(const Control* ctl, uint32_t bits) {
     return (ld_acquire(&ctl->err) & bits) != 0;
@@ -450,11 +451,9 @@ __global__ void k_act_init(World w, StepParams p) {
         uint32_t info = b.info[i];
         b.uf_parent[i] = i;
         b.can_deact[i] = 1;
-        b.used[i] = 0ull;
+        b.cw[i] = 0ull;
         b.adj_count[i] = 0;
         b.adj_fill[i] = 0;
-        b.col_cnt[i] = 0;
-        b.vel_ver[i] = 0;
 #pragma unroll
         for (int k = 0; k < 6; ++k) b.dv[6 * i + k] = 0.0f;
 #pragma unroll
@@ -655,24 +654,23 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             int b1 = mb1[k], b2 = mb2[k];
             uint32_t pr = mpr[k];
             uint32_t r1 = pr & 0xffffu, r2 = pr >> 16;
-            if (!versions_ready(b.col_cnt, b1, r1, b2, r2)) continue;
-            fence_acq_rel();
-            unsigned long long mask = 0ull;
-            if (b1 >= 0) mask |= b.used[b1];
-            if (b2 >= 0) mask |= b.used[b2];
+            // Each body's colour word holds its colour mask and how many of
+            // its manifolds have been coloured: the count is the flag.
+            unsigned long long u1 = b1 >= 0 ? ld_relaxed64(b.cw + b1) : ((unsigned long long)r1 << 56);
+            unsigned long long u2 = b2 >= 0 ? ld_relaxed64(b.cw + b2) : ((unsigned long long)r2 << 56);
+            if ((u1 >> 56) != r1 || (u2 >> 56) != r2) continue;
+            unsigned long long mask = (u1 | u2) & kColourMask;
             uint32_t col;
-            if (mask == ~0ull) {
+            if (mask == kColourMask) {
                 atomicOr(&w.ctl->err, ERRF_COLOURS);
-                col = kMaxColours - 1;
+                col = kColourBits - 1;
             } else {
                 col = (uint32_t)(__ffsll((long long)~mask) - 1);
             }
             w.s.sm_colour[m] = col;
-            if (b1 >= 0) b.used[b1] = b.used[b1] | (1ull << col);
-            if (b2 >= 0) b.used[b2] = b.used[b2] | (1ull << col);
-            fence_acq_rel();
-            if (b1 >= 0) st_relaxed(b.col_cnt + b1, r1 + 1u);
-            if (b2 >= 0) st_relaxed(b.col_cnt + b2, r2 + 1u);
+            const unsigned long long bit = 1ull << col;
+            if (b1 >= 0) st_relaxed64(b.cw + b1, ((unsigned long long)(r1 + 1u) << 56) | (u1 & kColourMask) | bit);
+            if (b2 >= 0) st_relaxed64(b.cw + b2, ((unsigned long long)(r2 + 1u) << 56) | (u2 & kColourMask) | bit);
             atomicMax(&w.ctl->ncolours, col + 1u);
             done |= 1u << k;
             progress = true;
@@ -704,11 +702,11 @@ __global__ void k_assemble(World w, StepParams p) {
         unsigned long long below = (col == 0u) ? 0ull : ((1ull << col) - 1ull);
         uint32_t rk = 0;
         if (b1 >= 0) {
-            unsigned long long u = b.used[b1];
+            unsigned long long u = b.cw[b1] & kColourMask;
             rk |= (uint32_t)__popcll(u & below) | ((uint32_t)__popcll(u) << 8);
         }
         if (b2 >= 0) {
-            unsigned long long u = b.used[b2];
+            unsigned long long u = b.cw[b2] & kColourMask;
             rk |= ((uint32_t)__popcll(u & below) << 16) | ((uint32_t)__popcll(u) << 24);
         }
         w.s.sm_rk[m] = rk;
@@ -1379,7 +1377,6 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
     }
     const float dt = p.dt;
     GRID_FOR(i, w.nb_slots) {
-        b.pos_ver[i] = 0;
         uint32_t info = b.info[i];
         if (!(info & BI_ISLAND)) continue;
         np::V el = np::mul(v3(b.acc_lin[i]), dt), ea = np::mul(v3(b.acc_ang[i]), dt);

@@ -43,7 +43,9 @@ enum : uint32_t {
 
 constexpr int kMaxContacts = 4;      // contacts per manifold
 constexpr int kRowFloats = 28;       // J1[6] J2[6] WJ1[6] WJ2[6] r rhs impulse mu
-constexpr int kMaxColours = 64;
+constexpr int kMaxColours = 64;      // colour buckets of the per-world schedule
+constexpr int kColourBits = 56;      // colours a step may use (the colour word's mask)
+constexpr unsigned long long kColourMask = (1ull << kColourBits) - 1ull;
 constexpr int kLeafCap = 16;         // partners a broad-phase leaf keeps between its two passes
 
 // Row field offsets.
@@ -69,10 +71,8 @@ struct Bodies {
     unsigned long long *posef;       // 12 per body: pose words flagged with the body's update count
     uint32_t *uf_parent;
     int *can_deact;
-    unsigned long long *used;        // colours of the body's solver manifolds (one bit each)
+    unsigned long long *cw;          // colour word: manifolds coloured so far << 56 | colour mask (56 bits)
     uint32_t *adj_count, *adj_start, *adj_fill;   // solver manifolds per body (CSR)
-    uint32_t *col_cnt;               // manifolds of the body coloured so far
-    uint32_t *vel_ver, *pos_ver;     // velocity / position updates applied to the body this step
 };
 
 struct Colliders {

@@ -1258,9 +1258,9 @@ public:
                 if (bodies[b1].dynamic()) mask |= used[b1];
                 if (bodies[b2].dynamic()) mask |= used[b2];
                 uint32_t c = 0;
-                while (c < 64 && (mask >> c) & 1u) ++c;
+                while (c < 56 && (mask >> c) & 1u) ++c;
                 m->colour = c;
-                if (c >= 64) continue;
+                if (c >= 56) continue;
                 if (bodies[b1].dynamic()) used[b1] |= (uint64_t(1) << c);
                 if (bodies[b2].dynamic()) used[b2] |= (uint64_t(1) << c);
                 ncol = std::max(ncol, c + 1);
@@ -1301,7 +1301,7 @@ public:
         std::vector<Manifold<R>*> seq = solver_manifolds;
         if (order == ORDER_COLOUR) {
             num_colours = colour_manifolds(seq);
-            if (num_colours >= 64 || std::any_of(seq.begin(), seq.end(), [](Manifold<R>* m) { return m->colour >= 64; })) {
+            if (std::any_of(seq.begin(), seq.end(), [](Manifold<R>* m) { return m->colour >= 56; })) {
                 last_error = "colour overflow";
                 return false;
             }
