@@ -494,8 +494,7 @@ __global__ void k_act_init(World w, StepParams p) {
         c->tasks = 0ull;
         c->res_acc_init[0] = 0.0;
         c->res_acc_init[1] = 0.0;
-        c->world_next[0] = 0u;
-        c->world_next[1] = 0u;
+        for (int k = 0; k < 4; ++k) c->world_next[k] = 0u;
         c->learned_starts = 0u;
         c->learned_kept = 0u;
     }
@@ -1213,30 +1212,42 @@ __device__ __forceinline__ bool world_locals(const World& w, uint32_t m, uint32_
     return true;
 }
 
+// A world is processed by a group of threads: a whole block (large worlds)
+// or one warp (small worlds, several per block). `lane` and `width` place the
+// thread in its group; the group's barrier orders the colours.
+struct WorldGroup {
+    uint32_t lane, width;
+    bool warp;
+    __device__ __forceinline__ void sync() const {
+        if (warp) __syncwarp();
+        else __syncthreads();
+    }
+};
+
 // One sweep (warm start, friction or normal rows) over a world's manifolds,
 // colour by colour.
 __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_t base, uint32_t nbw, uint32_t ncol,
-                                            uint32_t sweep, float* s_dv) {
+                                            uint32_t sweep, float* s_dv, const WorldGroup& g) {
     const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
     for (uint32_t c = 0; c < ncol; ++c) {
         uint32_t lo = bs[c], hi = bs[c + 1];
         if (lo == hi) continue;
-        for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+        for (uint32_t i = lo + g.lane; i < hi; i += g.width) {
             uint32_t m = w.s.wm_order[i];
             int l1, l2;
             if (world_locals(w, m, base, nbw, l1, l2))
                 velocity_task(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, s_dv);
         }
-        __syncthreads();
+        g.sync();
     }
 }
 
 // FP64 residual partial sums of one world, added to acc[0..1].
 __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint32_t base, uint32_t nbw,
-                                               const float* s_dv, double* sh, double* acc) {
+                                               const float* s_dv, double* sh, double* acc, const WorldGroup& g) {
     uint32_t lo = w.s.bucket_start[wd * kMaxColours], hi = w.s.bucket_start[wd * kMaxColours + kMaxColours];
     double s2 = 0.0, l2 = 0.0;
-    for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
+    for (uint32_t i = lo + g.lane; i < hi; i += g.width) {
         uint32_t m = w.s.wm_order[i];
         int b1, b2;
         if (!world_locals(w, m, base, nbw, b1, b2)) continue;
@@ -1245,46 +1256,76 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
         load_dv(s_dv, b2, dv.b);
         manifold_residual(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, s2, l2);
     }
-    double ts = block_sum(s2, sh);
-    double tl = block_sum(l2, sh);
-    if (threadIdx.x == 0 && (ts != 0.0 || tl != 0.0)) {
+    double ts, tl;
+    if (g.warp) {
+        for (int o = 16; o > 0; o >>= 1) {
+            s2 += __shfl_down_sync(0xffffffffu, s2, o);
+            l2 += __shfl_down_sync(0xffffffffu, l2, o);
+        }
+        ts = s2;
+        tl = l2;
+    } else {
+        ts = block_sum(s2, sh);
+        tl = block_sum(l2, sh);
+    }
+    if (g.lane == 0 && (ts != 0.0 || tl != 0.0)) {
         atomicAdd(&acc[0], ts);
         atomicAdd(&acc[1], tl);
     }
 }
 
-// Persistent: each block takes worlds from a counter until none is left,
-// largest first, so that the last worlds to start are short ones.
-// Dynamic shared memory: 6 floats per body slot of the largest world.
+// The whole velocity solve of one world by one group, its Δv in s_dv.
+__device__ __forceinline__ void world_velocity(const World& w, const StepParams& p, uint32_t wd, uint32_t max_bodies,
+                                               float* s_dv, double* sh, const WorldGroup& g) {
+    const uint32_t base = w.s.world_start[wd];
+    uint32_t nbw = w.s.world_start[wd + 1] - base;
+    if (nbw > max_bodies) {
+        if (g.lane == 0) atomicOr(&w.ctl->err, ERRF_WORLD_RANGE);
+        nbw = 0;
+    }
+    const uint32_t ncol = w.ctl->ncolours;
+    for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) s_dv[i] = 0.0f;
+    g.sync();
+    world_sweep(w, wd, base, nbw, ncol, 0, s_dv, g);
+    world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc_init, g);
+    for (uint32_t sw = 1; sw < 1 + 2 * p.max_velocity_iterations; ++sw) world_sweep(w, wd, base, nbw, ncol, sw, s_dv, g);
+    world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc, g);
+    for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) w.b.dv[6 * base + i] = s_dv[i];
+    g.sync();
+}
+
+// Persistent. Blocks first take the n_big large worlds from a counter,
+// largest first, one world per block; when none is left each warp takes
+// small worlds (at most kWarpWorldBodies body slots) from a second counter.
+// Dynamic shared memory: the larger of 6 floats per body slot of the largest
+// world and 6 floats per slot of a small world for each warp.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
-                                                                  uint32_t max_world_bodies) {
+                                                                  uint32_t max_world_bodies, uint32_t n_big) {
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
     __shared__ uint32_t s_world;
-    const uint32_t ncol = w.ctl->ncolours;
+    const WorldGroup block{threadIdx.x, blockDim.x, false};
     for (;;) {
         if (threadIdx.x == 0) {
             uint32_t k = atomicAdd(&w.ctl->world_next[0], 1u);
-            s_world = k < n_worlds ? w.s.world_order[k] : 0xffffffffu;
+            s_world = k < n_big ? w.s.world_order[k] : 0xffffffffu;
         }
         __syncthreads();
         const uint32_t wd = s_world;
+        __syncthreads();
         if (wd >= n_worlds) break;
-        const uint32_t base = w.s.world_start[wd];
-        uint32_t nbw = w.s.world_start[wd + 1] - base;
-        if (nbw > max_world_bodies) {
-            if (threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_WORLD_RANGE);
-            nbw = 0;
-        }
-        for (uint32_t i = threadIdx.x; i < 6 * nbw; i += blockDim.x) s_dv[i] = 0.0f;
-        __syncthreads();
-        world_sweep(w, wd, base, nbw, ncol, 0, s_dv);
-        world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc_init);
-        for (uint32_t sw = 1; sw < 1 + 2 * p.max_velocity_iterations; ++sw) world_sweep(w, wd, base, nbw, ncol, sw, s_dv);
-        world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc);
-        for (uint32_t i = threadIdx.x; i < 6 * nbw; i += blockDim.x) w.b.dv[6 * base + i] = s_dv[i];
-        __syncthreads();
+        world_velocity(w, p, wd, max_world_bodies, s_dv, sh, block);
+    }
+    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+    const WorldGroup wg{lane, 32u, true};
+    float* my_dv = s_dv + (size_t)warp * 6 * kWarpWorldBodies;
+    for (;;) {
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(&w.ctl->world_next[2], 1u);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (n_big + k >= n_worlds) break;
+        world_velocity(w, p, w.s.world_order[n_big + k], kWarpWorldBodies, my_dv, nullptr, wg);
     }
 }
 
@@ -1530,28 +1571,46 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
 }
 
 // Batched worlds: block per world, colour by colour, poses in global memory.
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds) {
-    __shared__ uint32_t s_world;
+// NonlinearSORProx sweeps of one world by one group, poses in global memory.
+__device__ __forceinline__ void world_position(const World& w, const StepParams& p, uint32_t wd, const WorldGroup& g) {
     const uint32_t ncol = w.ctl->ncolours;
+    const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
+    for (uint32_t it = 0; it < p.max_position_iterations; ++it) {
+        for (uint32_t c = 0; c < ncol; ++c) {
+            uint32_t lo = bs[c], hi = bs[c + 1];
+            if (lo == hi) continue;
+            for (uint32_t i = lo + g.lane; i < hi; i += g.width) position_task(w, p, w.s.wm_order[i]);
+            g.sync();
+        }
+    }
+    g.sync();
+}
+
+// Batched worlds: large worlds one per block, then small worlds one per warp,
+// as in the velocity kernel.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big) {
+    __shared__ uint32_t s_world;
+    const WorldGroup block{threadIdx.x, blockDim.x, false};
     for (;;) {
         if (threadIdx.x == 0) {
             uint32_t k = atomicAdd(&w.ctl->world_next[1], 1u);
-            s_world = k < n_worlds ? w.s.world_order[k] : 0xffffffffu;
+            s_world = k < n_big ? w.s.world_order[k] : 0xffffffffu;
         }
         __syncthreads();
         const uint32_t wd = s_world;
-        if (wd >= n_worlds) break;
-        const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
-        for (uint32_t it = 0; it < p.max_position_iterations; ++it) {
-            for (uint32_t c = 0; c < ncol; ++c) {
-                uint32_t lo = bs[c], hi = bs[c + 1];
-                if (lo == hi) continue;
-                for (uint32_t i = lo + threadIdx.x; i < hi; i += blockDim.x) position_task(w, p, w.s.wm_order[i]);
-                __syncthreads();
-            }
-        }
         __syncthreads();
+        if (wd >= n_worlds) break;
+        world_position(w, p, wd, block);
+    }
+    const uint32_t lane = threadIdx.x & 31u;
+    const WorldGroup wg{lane, 32u, true};
+    for (;;) {
+        uint32_t k = 0;
+        if (lane == 0) k = atomicAdd(&w.ctl->world_next[3], 1u);
+        k = __shfl_sync(0xffffffffu, k, 0);
+        if (n_big + k >= n_worlds) break;
+        world_position(w, p, w.s.world_order[n_big + k], wg);
     }
 }
 
@@ -1611,6 +1670,13 @@ static unsigned item_blocks(uint32_t n) {
 
 static const size_t kVelocitySmem = (size_t)kCoopThreads * kCacheF4 * sizeof(float4);
 
+// Dynamic shared memory of the per-world velocity kernel: Δv (6 floats) per
+// body slot of the largest world, or per slot of a small world for each warp.
+static size_t world_smem(uint32_t max_world_bodies, int threads) {
+    size_t big = 6 * (size_t)max_world_bodies, warps = (size_t)(threads / 32) * 6 * kWarpWorldBodies;
+    return (big > warps ? big : warps) * sizeof(float);
+}
+
 void solver_grid_sizes(int device, SolverLaunch& L) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
@@ -1621,9 +1687,11 @@ void solver_grid_sizes(int device, SolverLaunch& L) {
     L.grid_velocity = sms * (per < 1 ? 1 : per);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_position, kCoopThreads, 0);
     L.grid_position = sms * (per < 1 ? 1 : per);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_world_position<128>, 128, 0);
+    L.grid_world_position = sms * (per < 1 ? 1 : per);
     for (const void* f : {(const void*)k_world_velocity<64>, (const void*)k_world_velocity<128>,
                           (const void*)k_world_velocity<256>})
-        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(6 * kMaxWorldBodies * sizeof(float)));
+        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)world_smem(kMaxWorldBodies, 256));
 }
 
 uint64_t grid_task_capacity(const SolverLaunch& L) {
@@ -1636,7 +1704,7 @@ int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds, int thr
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     const void* f = threads == 64 ? (const void*)k_world_velocity<64>
                                   : threads == 256 ? (const void*)k_world_velocity<256> : (const void*)k_world_velocity<128>;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, threads, 6 * (size_t)max_world_bodies * sizeof(float));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, threads, world_smem(max_world_bodies, threads));
     long g = (long)sms * (per < 1 ? 1 : per);
     if (g > (long)n_worlds) g = n_worlds;
     return g < 1 ? 1 : (int)g;
@@ -1683,13 +1751,13 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
                                           st);
         if (e != cudaSuccess) return e;
         k_world_scatter<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
-        const size_t smem = 6 * (size_t)L.max_world_bodies * sizeof(float);
+        const size_t smem = world_smem(L.max_world_bodies, L.world_threads);
         if (L.world_threads == 64)
-            k_world_velocity<64><<<L.grid_world, 64, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies);
+            k_world_velocity<64><<<L.grid_world, 64, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies, L.n_big);
         else if (L.world_threads == 256)
-            k_world_velocity<256><<<L.grid_world, 256, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies);
+            k_world_velocity<256><<<L.grid_world, 256, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies, L.n_big);
         else
-            k_world_velocity<128><<<L.grid_world, 128, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies);
+            k_world_velocity<128><<<L.grid_world, 128, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies, L.n_big);
         k_world_finish<<<1, 1, 0, st>>>(wc, pc);
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
@@ -1702,12 +1770,9 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     k_cache_integrate<<<nbb > npb ? nbb : npb, kItemThreads, 0, st>>>(wc, pc, posef);
     rec(5);
     if (L.batched) {
-        if (L.world_threads == 64)
-            k_world_position<64><<<L.grid_world, 64, 0, st>>>(wc, pc, L.n_worlds);
-        else if (L.world_threads == 256)
-            k_world_position<256><<<L.grid_world, 256, 0, st>>>(wc, pc, L.n_worlds);
-        else
-            k_world_position<128><<<L.grid_world, 128, 0, st>>>(wc, pc, L.n_worlds);
+        // The position sweeps run 128 threads a block whatever the velocity
+        // kernel's block size: large worlds a block each, small ones a warp.
+        k_world_position<128><<<L.grid_world_position, 128, 0, st>>>(wc, pc, L.n_worlds, L.n_big);
     } else {
         e = coop((const void*)k_position, L.grid_position, args2, st);
         if (e != cudaSuccess) return e;

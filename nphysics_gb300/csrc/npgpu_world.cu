@@ -139,7 +139,7 @@ struct npgpu_world {
     // moved between worlds.
     bool layout_dirty = true;
     bool layout_ok = false;              // the worlds qualify for the per-world schedule
-    uint32_t n_worlds = 0, max_world_bodies = 0;
+    uint32_t n_worlds = 0, max_world_bodies = 0, n_big_worlds = 0;
     std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries, then the n_worlds largest-first order
     uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
     bool layout_on_device = false;
@@ -287,6 +287,8 @@ static void compute_layout(npgpu_world* w) {
     w->world_start.swap(st);
     w->n_worlds = nw;
     w->max_world_bodies = widest;
+    w->n_big_worlds = 0;
+    for (uint32_t k = 0; k < nw; ++k) w->n_big_worlds += (w->world_start[k + 1] - w->world_start[k] > kWarpWorldBodies) ? 1u : 0u;
     w->layout_ok = true;
 }
 
@@ -343,6 +345,7 @@ static npgpu_status prepare_schedule(npgpu_world* w) {
     }
     w->solver.n_worlds = w->n_worlds;
     w->solver.max_world_bodies = w->max_world_bodies;
+    w->solver.n_big = w->n_big_worlds;
     w->solver.grid_world = w->grid_world;
     return NPGPU_OK;
 }
@@ -871,12 +874,14 @@ static std::vector<uint8_t> graph_key(const npgpu_world* w, const StepParams& sp
     put(&w->dw, sizeof(w->dw));
     put(&sp, sizeof(sp));
     const SolverLaunch& L = w->solver;
-    int ints[6] = {L.grid_colour, L.grid_velocity, L.grid_position, L.grid_world, L.batched ? 1 : 0, L.world_threads};
+    int ints[7] = {L.grid_colour,      L.grid_velocity, L.grid_position,       L.grid_world,
+                   L.batched ? 1 : 0, L.world_threads, L.grid_world_position};
     put(ints, sizeof(ints));
     put(&L.scan_temp, sizeof(L.scan_temp));
     put(&L.scan_bytes, sizeof(L.scan_bytes));
     put(&L.n_worlds, sizeof(L.n_worlds));
     put(&L.max_world_bodies, sizeof(L.max_world_bodies));
+    put(&L.n_big, sizeof(L.n_big));
     put(&w->sort_temp, sizeof(w->sort_temp));
     put(&w->sort_bytes, sizeof(w->sort_bytes));
     return k;

@@ -153,7 +153,7 @@ struct Control {
     unsigned long long t_phase[16];  // %globaltimer stamps
     unsigned long long task_ns, wait_ns, tasks;   // velocity-task statistics (profile mode)
     double res_acc_init[2];          // batched worlds: residual sums after the warm start
-    uint32_t world_next[2];          // batched worlds: work counters of the velocity / position kernels
+    uint32_t world_next[4];          // batched worlds: block and warp work counters of the velocity / position kernels
     uint32_t mlp_samples;            // training samples recorded so far
     uint32_t learned_starts, learned_kept;   // learned warm start: predictions made / kept this step
     uint32_t pad2;
@@ -204,9 +204,12 @@ struct SolverLaunch {
     bool batched;
     uint32_t n_worlds;
     uint32_t max_world_bodies;       // largest body slot range of a world
+    uint32_t n_big;                  // worlds wider than kWarpWorldBodies: one block each; the rest one warp each
     int grid_world;                  // blocks of the per-world kernels
-    int world_threads;               // threads per world block: 64, 128 or 256
+    int world_threads;               // threads per world block of the velocity kernel: 64, 128 or 256
+    int grid_world_position;         // blocks of the per-world position kernel (128 threads each)
 };
+constexpr uint32_t kWarpWorldBodies = 256;    // widest world a single warp solves
 constexpr uint32_t kMaxWorldBodies = 4096;    // per-world shared-memory Δv limit (96 KiB)
 cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st);
 void solver_grid_sizes(int device, SolverLaunch& L);

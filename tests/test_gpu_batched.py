@@ -27,8 +27,11 @@ def small_batch(n_worlds=10, seed=7):
     return scenes.batched_worlds(n_worlds=n_worlds, seed=seed, lo=8, hi=120)
 
 
-def test_worlds_schedule_equals_grid_schedule(gpu_lib):
-    sc = small_batch()
+@pytest.mark.parametrize("hi", [120, 700])
+def test_worlds_schedule_equals_grid_schedule(gpu_lib, hi):
+    # hi 120: every world is solved by one warp; hi 700: the worlds wider than
+    # 256 body slots take a whole block, the rest a warp.
+    sc = scenes.batched_worlds(n_worlds=10, seed=7, lo=8, hi=hi)
     a = run(sc, abi.SCHEDULE_GRID, 40)
     b = run(sc, abi.SCHEDULE_WORLDS, 40)
     ba, bb = a.bodies(), b.bodies()
