@@ -7,7 +7,10 @@
 // the network's output against the normalised impulses, averaged over the
 // batch and the three outputs. Weights are read in bf16 (the precision
 // inference uses) and every sum accumulates in fp32; the fp32 master weights
-// take the Adam updates.
+// take the Adam updates. The hidden layer's three 64 x 64 x 64 products per
+// tile (forward, weight gradient, back-propagated gradient) run on the tensor
+// cores with bf16 operands; the other layers (24 inputs, 3 outputs) on the
+// fp32 pipes.
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -26,6 +29,52 @@ __device__ __forceinline__ uint32_t mix32(uint32_t x) {
     x *= 0xc2b2ae35u;
     x ^= x >> 16;
     return x;
+}
+
+// Tensor-core tiles for the 64 x 64 x 64 products of the hidden layer:
+// operands in shared memory as bf16 with a padded row of kLd elements, fp32
+// accumulation (mma.sync m16n8k16; fragment layout of the PTX ISA:
+// g = lane / 4, t = lane % 4; A rows g and g + 8, columns 2t, 2t + 1 (+ 8);
+// B column g, rows 2t, 2t + 1 (+ 8); C rows g, g + 8, columns 2t, 2t + 1).
+constexpr int kLd = 72;
+
+// c += A[m0 .. m0 + 16][0 .. 64) * B[0 .. 64)[n0 .. n0 + 8), with A row-major
+// and B given as Bt[n][k] (both bf16, leading dimension kLd).
+__device__ __forceinline__ void mma_16x8x64(const __nv_bfloat16* A, const __nv_bfloat16* Bt, int m0, int n0, float* c) {
+    const int lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+#pragma unroll
+    for (int k0 = 0; k0 < 64; k0 += 16) {
+        const uint32_t a0 = *reinterpret_cast<const uint32_t*>(A + (m0 + g) * kLd + k0 + 2 * t);
+        const uint32_t a1 = *reinterpret_cast<const uint32_t*>(A + (m0 + g + 8) * kLd + k0 + 2 * t);
+        const uint32_t a2 = *reinterpret_cast<const uint32_t*>(A + (m0 + g) * kLd + k0 + 8 + 2 * t);
+        const uint32_t a3 = *reinterpret_cast<const uint32_t*>(A + (m0 + g + 8) * kLd + k0 + 8 + 2 * t);
+        const uint32_t b0 = *reinterpret_cast<const uint32_t*>(Bt + (n0 + g) * kLd + k0 + 2 * t);
+        const uint32_t b1 = *reinterpret_cast<const uint32_t*>(Bt + (n0 + g) * kLd + k0 + 8 + 2 * t);
+        asm volatile(
+            "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0, %1, %2, %3}, {%4, %5, %6, %7}, {%8, %9}, "
+            "{%0, %1, %2, %3};"
+            : "+f"(c[0]), "+f"(c[1]), "+f"(c[2]), "+f"(c[3])
+            : "r"(a0), "r"(a1), "r"(a2), "r"(a3), "r"(b0), "r"(b1));
+    }
+}
+
+// One 64 x 64 product on the block's 8 warps: warp w owns rows 16 (w / 2) and
+// columns 32 (w % 2) .. + 32, four 16 x 8 tiles. f(row, col, value) receives
+// every output element once.
+template <class F>
+__device__ __forceinline__ void mma_64x64x64(const __nv_bfloat16* A, const __nv_bfloat16* Bt, F f) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, g = lane >> 2, t = lane & 3;
+    const int m0 = (warp >> 1) * 16;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const int n0 = (warp & 1) * 32 + q * 8;
+        float c[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        mma_16x8x64(A, Bt, m0, n0, c);
+        f(m0 + g, n0 + 2 * t, c[0]);
+        f(m0 + g, n0 + 2 * t + 1, c[1]);
+        f(m0 + g + 8, n0 + 2 * t, c[2]);
+        f(m0 + g + 8, n0 + 2 * t + 1, c[3]);
+    }
 }
 
 // The inference copy of the parameters: weights rounded to bf16 (nearest,
@@ -118,9 +167,7 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const MlpDev* __restri
                                                           double* loss) {
     extern __shared__ float sm[];
     float* W1T = sm;                                   // [24][64]
-    float* W2T = W1T + kMlpIn * kMlpHidden;            // [64][64], W2T[i][j] = W2[j][i]
-    float* W2 = W2T + kMlpHidden * kMlpHidden;         // [64][64]
-    float* W3 = W2 + kMlpHidden * kMlpHidden;          // [3][64]
+    float* W3 = W1T + kMlpIn * kMlpHidden;             // [3][64]
     float* B1 = W3 + kMlpOut * kMlpHidden;
     float* B2 = B1 + kMlpHidden;
     float* B3 = B2 + kMlpHidden;                       // 4 floats
@@ -130,6 +177,13 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const MlpDev* __restri
     float* H2 = H1 + kTile * kMlpHidden;               // [64][64], later dH1
     float* D2 = H2 + kTile * kMlpHidden;               // [64][64] dH2
     float* DY = D2 + kTile * kMlpHidden;               // [64][3]
+    // bf16 operands of the hidden layer's products (rows padded to kLd).
+    __nv_bfloat16* H1b = reinterpret_cast<__nv_bfloat16*>(DY + kTile * 4);   // H1[s][i]
+    __nv_bfloat16* H1Tb = H1b + kTile * kLd;                                   // H1[s][i] at [i][s]
+    __nv_bfloat16* W2b = H1Tb + kTile * kLd;                                   // W2[j][i]
+    __nv_bfloat16* W2Tb = W2b + kTile * kLd;                                   // W2[j][i] at [i][j]
+    __nv_bfloat16* D2b = W2Tb + kTile * kLd;                                   // dH2[s][j]
+    __nv_bfloat16* D2Tb = D2b + kTile * kLd;                                   // dH2[s][j] at [j][s]
     __shared__ double s_loss[kMlpThreads / 32];
     const int tid = threadIdx.x;
 
@@ -139,9 +193,8 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const MlpDev* __restri
     }
     for (int i = tid; i < kMlpHidden * kMlpHidden; i += kMlpThreads) {
         int j = i / kMlpHidden, k = i % kMlpHidden;
-        float v = bf(net->w2, i);
-        W2[i] = v;
-        W2T[k * kMlpHidden + j] = v;
+        W2b[j * kLd + k] = net->w2[i];
+        W2Tb[k * kLd + j] = net->w2[i];
     }
     for (int i = tid; i < kMlpOut * kMlpHidden; i += kMlpThreads) W3[i] = bf(net->w3, i);
     for (int i = tid; i < kMlpHidden; i += kMlpThreads) {
@@ -179,15 +232,18 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const MlpDev* __restri
         int s = e / kMlpHidden, j = e % kMlpHidden;
         float a = B1[j];
         for (int i = 0; i < kMlpIn; ++i) a = a + W1T[i * kMlpHidden + j] * X[s * kMlpIn + i];
-        H1[e] = a > 0.0f ? a : 0.0f;
+        const float h = a > 0.0f ? a : 0.0f;
+        H1[e] = h;
+        const __nv_bfloat16 hb = __float2bfloat16_rn(h);
+        H1b[s * kLd + j] = hb;
+        H1Tb[j * kLd + s] = hb;
     }
     __syncthreads();
-    for (int e = tid; e < kTile * kMlpHidden; e += kMlpThreads) {
-        int s = e / kMlpHidden, j = e % kMlpHidden;
-        float a = B2[j];
-        for (int i = 0; i < kMlpHidden; ++i) a = a + W2T[i * kMlpHidden + j] * H1[s * kMlpHidden + i];
-        H2[e] = a > 0.0f ? a : 0.0f;
-    }
+    // Hidden layer 2 on the tensor cores: H2 = relu(H1 W2^T + b2).
+    mma_64x64x64(H1b, W2b, [&](int s, int j, float v) {
+        const float a = v + B2[j];
+        H2[s * kMlpHidden + j] = a > 0.0f ? a : 0.0f;
+    });
     __syncthreads();
     double lsum = 0.0;
     const float scale = 2.0f / (float)(batch * kMlpOut);
@@ -229,28 +285,25 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const MlpDev* __restri
         int s = e / kMlpHidden, j = e % kMlpHidden;
         float g = 0.0f;
         for (int o = 0; o < kMlpOut; ++o) g = g + DY[s * 4 + o] * W3[o * kMlpHidden + j];
-        D2[e] = H2[e] > 0.0f ? g : 0.0f;
+        const float d = H2[e] > 0.0f ? g : 0.0f;
+        D2[e] = d;
+        const __nv_bfloat16 db = __float2bfloat16_rn(d);
+        D2b[s * kLd + j] = db;
+        D2Tb[j * kLd + s] = db;
     }
     __syncthreads();
-    // Hidden layer 2: dW2[j][i] = sum_s dH2[s][j] H1[s][i]; dH1 = dH2 W2 (into H2's space).
+    // Hidden layer 2 backward on the tensor cores: dW2[j][i] = sum_s
+    // dH2[s][j] H1[s][i]; dH1 = (dH2 W2) masked by H1 > 0, into H2's space.
     float* D1 = H2;
-    for (int e = tid; e < kMlpHidden * kMlpHidden; e += kMlpThreads) {
-        int j = e / kMlpHidden, i = e % kMlpHidden;
-        float g = 0.0f;
-        for (int s = 0; s < kTile; ++s) g = g + D2[s * kMlpHidden + j] * H1[s * kMlpHidden + i];
-        atomicAdd(&grad[kMlpW2 + e], g);
-    }
+    mma_64x64x64(D2Tb, H1Tb, [&](int j, int i, float v) { atomicAdd(&grad[kMlpW2 + j * kMlpHidden + i], v); });
     for (int j = tid; j < kMlpHidden; j += kMlpThreads) {
         float g = 0.0f;
         for (int s = 0; s < kTile; ++s) g = g + D2[s * kMlpHidden + j];
         atomicAdd(&grad[kMlpB2 + j], g);
     }
-    for (int e = tid; e < kTile * kMlpHidden; e += kMlpThreads) {
-        int s = e / kMlpHidden, i = e % kMlpHidden;
-        float g = 0.0f;
-        for (int j = 0; j < kMlpHidden; ++j) g = g + D2[s * kMlpHidden + j] * W2[j * kMlpHidden + i];
-        D1[e] = H1[e] > 0.0f ? g : 0.0f;
-    }
+    mma_64x64x64(D2b, W2Tb, [&](int s, int i, float v) {
+        D1[s * kMlpHidden + i] = H1[s * kMlpHidden + i] > 0.0f ? v : 0.0f;
+    });
     __syncthreads();
     // Hidden layer 1.
     for (int e = tid; e < kMlpHidden * kMlpIn; e += kMlpThreads) {
@@ -266,9 +319,10 @@ __global__ void __launch_bounds__(kMlpThreads) k_mlp_grad(const MlpDev* __restri
     }
 }
 
-constexpr size_t kGradSmem = sizeof(float) * (kMlpIn * kMlpHidden + 2 * kMlpHidden * kMlpHidden + kMlpOut * kMlpHidden +
+constexpr size_t kGradSmem = sizeof(float) * (kMlpIn * kMlpHidden + kMlpOut * kMlpHidden +
                                               2 * kMlpHidden + 4 + kTile * kMlpIn + kTile * 4 +
-                                              3 * kTile * kMlpHidden + kTile * 4);
+                                              3 * kTile * kMlpHidden + kTile * 4) +
+                             sizeof(__nv_bfloat16) * 6 * kTile * kLd;
 
 // Adam (beta1 0.9, beta2 0.999, eps 1e-8) on the fp32 master weights, then
 // the inference copy.
