@@ -719,6 +719,25 @@ __global__ void k_assemble(World w, StepParams p) {
         if (b1 >= 0) mask |= ~(bi_flags(v1.info) >> 1) & 0x3fu;
         if (b2 >= 0) mask |= (~(bi_flags(v2.info) >> 1) & 0x3fu) << 8;
         w.s.sm_mask[m] = mask;
+        {
+            // The position solver's record of this manifold (position_core).
+            float4* pr4 = w.s.pos_rec + (size_t)m * kPosRec;
+            const uint32_t sh1 = ci1 & 0xfu, sh2 = ci2 & 0xfu;
+            const float4 pp1 = c.params[c1], pp2 = c.params[c2];
+            const float4 wt1 = c.wrt_t[c1], wt2 = c.wrt_t[c2];
+            pr4[0] = make_float4(wt1.x, wt1.y, wt1.z, (sh1 == SHAPE_BALL ? pp1.x : 0.0f) + m1);
+            pr4[1] = c.wrt_q[c1];
+            pr4[2] = make_float4(wt2.x, wt2.y, wt2.z, (sh2 == SHAPE_BALL ? pp2.x : 0.0f) + m2);
+            pr4[3] = c.wrt_q[c2];
+            pr4[4] = make_float4(pp1.x, pp1.y, pp1.z, __uint_as_float(sh1 | (nc << 8)));
+            pr4[5] = make_float4(pp2.x, pp2.y, pp2.z, __uint_as_float(sh2));
+            pr4[6] = make_float4(__uint_as_float(bb1), __uint_as_float(bb2), __uint_as_float(v1.info),
+                                 __uint_as_float(v2.info));
+            for (uint32_t k = 0; k < nc; ++k) {
+                const float4 nl = w.cur.nl[q * kMaxContacts + k];
+                pr4[7 + k] = make_float4(nl.x, nl.y, nl.z, __uint_as_float(w.cur.key[q * kMaxContacts + k]));
+            }
+        }
         float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
         float4* lam = w.s.lam + (size_t)m * kMaxContacts;
         const bool learned = p.warmstart_mode == 2u && w.mlp != nullptr;
@@ -1437,37 +1456,50 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
 // (nonlinear_sor_prox.rs:121-154), on the two bodies' poses P1, P2 (the
 // poses of sides without dofs are not changed). moved1 / moved2 report a
 // displacement.
+// What a position task of manifold m reads besides the poses, gathered by
+// assembly into one record (kPosRec float4) so that a task waits for memory
+// once rather than through the pair -> collider -> body chain:
+//   0 (wrt1.t, dil1)  1 wrt1.q  2 (wrt2.t, dil2)  3 wrt2.q
+//   4 (half extents 1, shape1 | nc << 8)  5 (half extents 2, shape2)
+//   6 (body1, body2, info1, info2)  7..10 per contact (normal in body 1's frame, feature key)
 __device__ __forceinline__ void position_core(const World& w, const StepParams& p, uint32_t m, Pose& P1, Pose& P2,
                                               bool& moved1, bool& moved2) {
     const Bodies& b = w.b;
-    const Colliders& c = w.c;
-    uint32_t q = w.s.sm_list[m];
-    uint2 pr = w.cur.pair[q];
-    uint32_t c1 = pr.x, c2 = pr.y;
-    uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
-    uint32_t i1 = b.info[bb1], i2 = b.info[bb2];
+    const float4* rec = w.s.pos_rec + (size_t)m * kPosRec;
+    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2), r3 = __ldg(rec + 3);
+    const float4 r4 = __ldg(rec + 4), r5 = __ldg(rec + 5), r6 = __ldg(rec + 6);
+    const uint32_t bb1 = __float_as_uint(r6.x), bb2 = __float_as_uint(r6.y);
+    const uint32_t i1 = __float_as_uint(r6.z), i2 = __float_as_uint(r6.w);
     bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
     np::V t1 = P1.t, t2 = P2.t;
     np::Q q1 = P1.q, q2 = P2.q;
     np::V com1 = P1.com, com2 = P2.com;
-    np::V lc1 = v3(b.local_com[bb1]), lc2 = v3(b.local_com[bb2]);
-    float im1 = b.inv_mass[bb1], im2 = b.inv_mass[bb2];
-    np::M iI1 = load_m9(b.inv_I + 9 * bb1), iI2 = load_m9(b.inv_I + 9 * bb2);
-    np::Iso wrt1{v3(c.wrt_t[c1]), q4(c.wrt_q[c1])}, wrt2{v3(c.wrt_t[c2]), q4(c.wrt_q[c2])};
-    uint32_t sh1 = c.info[c1] & 0xfu, sh2 = c.info[c2] & 0xfu;
-    float4 pp1 = c.params[c1], pp2 = c.params[c2];
-    np::V hh1 = v3(pp1), hh2 = v3(pp2);
-    float dil1 = (sh1 == SHAPE_BALL ? pp1.x : 0.0f) + c.margin[c1];
-    float dil2 = (sh2 == SHAPE_BALL ? pp2.x : 0.0f) + c.margin[c2];
-    uint32_t nc = w.cur.ncont[q];
+    np::V lc1 = np::mk(0.0f, 0.0f, 0.0f), lc2 = lc1;
+    SB s1, s2;
+    s1.im = s2.im = 0.0f;
+    if (d1) {
+        lc1 = v3(__ldg(b.local_com + bb1));
+        s1 = load_sb(b.sb, (int)bb1);
+    }
+    if (d2) {
+        lc2 = v3(__ldg(b.local_com + bb2));
+        s2 = load_sb(b.sb, (int)bb2);
+    }
+    const float im1 = s1.im, im2 = s2.im;
+    const np::M iI1 = s1.I, iI2 = s2.I;
+    np::Iso wrt1{v3(r0), q4(r1)}, wrt2{v3(r2), q4(r3)};
+    const uint32_t sh1 = __float_as_uint(r4.w) & 0xfu, sh2 = __float_as_uint(r5.w) & 0xfu;
+    np::V hh1 = v3(r4), hh2 = v3(r5);
+    const float dil1 = r0.w, dil2 = r2.w;
+    const uint32_t nc = __float_as_uint(r4.w) >> 8;
     moved1 = moved2 = false;
     for (uint32_t k = 0; k < nc; ++k) {
-        uint32_t slot = q * kMaxContacts + k;
-        uint32_t key = w.cur.key[slot];
+        const float4 ck = __ldg(rec + 7 + k);
+        uint32_t key = __float_as_uint(ck.w);
         int f1 = (int)(key / 26u), f2 = (int)(key % 26u);
         np::Iso m1 = np::iso_mul(np::Iso{t1, q1}, wrt1);
         np::Iso m2 = np::iso_mul(np::Iso{t2, q2}, wrt2);
-        np::V n0 = np::qrot(m1.q, v3(w.cur.nl[slot]));
+        np::V n0 = np::qrot(m1.q, v3(ck));
         Geom g = kinematic_contact(feature_of(sh1, hh1, f1), m1, dil1, feature_of(sh2, hh2, f2), m2, dil2, n0);
         // NonlinearSORProx::clamp_rhs.
         float rhs = (-g.depth + p.allowed_linear_error) * p.erp;
@@ -1509,8 +1541,8 @@ __device__ __forceinline__ void position_core(const World& w, const StepParams& 
 // Position task on poses in global memory (one block per world, where
 // __syncthreads orders the tasks of successive colours).
 __device__ __forceinline__ void position_task(const World& w, const StepParams& p, uint32_t m) {
-    uint2 pr = w.cur.pair[w.s.sm_list[m]];
-    uint32_t bb1 = w.c.body[pr.x], bb2 = w.c.body[pr.y];
+    const float4 r6 = __ldg(w.s.pos_rec + (size_t)m * kPosRec + 6);
+    const uint32_t bb1 = __float_as_uint(r6.x), bb2 = __float_as_uint(r6.y);
     Pose P1 = load_pose(w.b, bb1), P2 = load_pose(w.b, bb2);
     bool moved1, moved2;
     position_core(w, p, m, P1, P2, moved1, moved2);
@@ -1549,9 +1581,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p
             if (b2 >= 0) r2 = poll_posef(w.b.posef, b2, t2, P2, mv2);
             if (!(r1 && r2)) continue;
             if (b1 < 0 || b2 < 0) {
-                uint2 pr = w.cur.pair[w.s.sm_list[m]];
-                if (b1 < 0) P1 = load_pose(w.b, w.c.body[pr.x]);
-                if (b2 < 0) P2 = load_pose(w.b, w.c.body[pr.y]);
+                const float4 r6 = __ldg(w.s.pos_rec + (size_t)m * kPosRec + 6);
+                if (b1 < 0) P1 = load_pose(w.b, __float_as_uint(r6.x));
+                if (b2 < 0) P2 = load_pose(w.b, __float_as_uint(r6.y));
             }
             bool n1, n2;
             position_core(w, p, m, P1, P2, n1, n2);

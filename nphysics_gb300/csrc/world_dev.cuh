@@ -46,7 +46,8 @@ constexpr int kRowFloats = 28;       // J1[6] J2[6] WJ1[6] WJ2[6] r rhs impulse 
 constexpr int kMaxColours = 64;      // colour buckets of the per-world schedule
 constexpr int kColourBits = 56;      // colours a step may use (the colour word's mask)
 constexpr unsigned long long kColourMask = (1ull << kColourBits) - 1ull;
-constexpr int kLeafCap = 16;         // partners a broad-phase leaf keeps between its two passes
+constexpr int kLeafCap = 16;
+constexpr int kPosRec = 7 + 4;       // float4 of a manifold's position-solver record         // partners a broad-phase leaf keeps between its two passes
 
 // Row field offsets.
 enum { RF_J1 = 0, RF_J2 = 6, RF_WJ1 = 12, RF_WJ2 = 18, RF_R = 24, RF_RHS = 25, RF_IMP = 26, RF_MU = 27 };
@@ -116,6 +117,7 @@ struct Solver {
     float4 *con;                     // 4 contacts x 4 float4 per solver manifold (constant during the solve)
     float4 *lam;                     // 4 contacts per solver manifold: impulses (normal, tangent 1, tangent 2)
     uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13)
+    float4 *pos_rec;                 // kPosRec per solver manifold: what the position solver reads besides poses
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
     // Batched worlds: manifolds bucketed by (world, colour).
     uint32_t *world_start;           // body slot range of each world (n_worlds + 1)
