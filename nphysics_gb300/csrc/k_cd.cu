@@ -173,6 +173,16 @@ __global__ void k_lbvh_refit(World w, int n) {
         uint32_t wr = (__float_as_uint(a0.w) & 0xffff0000u) | (__float_as_uint(b0.w) & 0xffffu);
         w.c.node_min[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), __uint_as_float(wr));
         w.c.node_max[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), fmaxf(a1.w, b1.w));
+        // The traversal's copy: both children's boxes and references in one
+        // 80-byte record, a leaf child referenced by its collider (top bit set).
+        float4* wd = w.c.wide + 5 * (size_t)p;
+        wd[0] = a0;
+        wd[1] = a1;
+        wd[2] = b0;
+        wd[3] = b1;
+        uint32_t lref = l >= n - 1 ? (0x80000000u | w.c.vals_sorted[l - (n - 1)]) : (uint32_t)l;
+        uint32_t rref = r >= n - 1 ? (0x80000000u | w.c.vals_sorted[r - (n - 1)]) : (uint32_t)r;
+        wd[4] = make_float4(__uint_as_float(lref), __uint_as_float(rref), 0.0f, 0.0f);
         __threadfence();
         p = w.c.parent[p];
     }
@@ -227,43 +237,46 @@ __global__ void k_bp_traverse(World w, int n) {
     float4 amin = c.aabb_min[a], amax = c.aabb_max[a];
     float ra = c.rank[a];
     const uint32_t qw = key_world(c.keys_sorted[k]);
-    // A node is entered when its subtree holds the query's world (batched
-    // worlds share space), a collider the query may own (a larger bounding
-    // radius somewhere below) and an AABB overlapping the query's. Both
-    // children are tested at their parent, so their data loads together and
-    // only entered nodes go on the stack.
-    auto enter = [&](int node) {
-        float4 nmin = c.node_min[node], nmax = c.node_max[node];
+    // A subtree is entered when it holds the query's world (batched worlds
+    // share space), a collider the query may own (a larger bounding radius
+    // somewhere below) and an AABB overlapping the query's. An internal node's
+    // record carries both children's boxes, so a visited node costs one
+    // memory round trip, and leaf children are tested without visiting them.
+    auto enter = [&](float4 nmin, float4 nmax) {
         uint32_t nw = __float_as_uint(nmin.w);
         return qw >= (nw >> 16) && qw <= (nw & 0xffffu) && !(nmax.w < ra) && overlap(amin, amax, nmin, nmax);
     };
-    if (n >= 2 && enter(0)) {
+    auto emit = [&](uint32_t b, float rb) {
+        // owns(): the smaller bounding radius owns the pair, ties by slot.
+        const bool own = ra < rb || (ra == rb && a < b);
+        if (b != a && own && pair_allowed(w, a, b)) {
+            if (WRITE) {
+                uint32_t slot = base + count;
+                if (slot < w.cap_pairs) w.cur.pair[slot] = make_uint2(a < b ? a : b, a < b ? b : a);
+            } else if (count < (uint32_t)kLeafCap) {
+                c.leaf_tmp[(size_t)k * kLeafCap + count] = b;
+            }
+            ++count;
+        }
+    };
+    if (n >= 2 && enter(c.node_min[0], c.node_max[0])) {
         int stack[64];
         int sp = 0;
         stack[sp++] = 0;
         while (sp > 0) {
-            int node = stack[--sp];
-            if (node >= n - 1) {
-                uint32_t b = c.vals_sorted[node - (n - 1)];
-                if (b != a && owns(c, a, b) && pair_allowed(w, a, b)) {
-                    if (WRITE) {
-                        uint32_t slot = base + count;
-                        if (slot < w.cap_pairs) w.cur.pair[slot] = make_uint2(a < b ? a : b, a < b ? b : a);
-                    } else if (count < (uint32_t)kLeafCap) {
-                        c.leaf_tmp[(size_t)k * kLeafCap + count] = b;
-                    }
-                    ++count;
-                }
-                continue;
-            }
-            const int l = c.left[node], r = c.right[node];
-            const bool el = enter(l), er = enter(r);
-            if (sp + (int)el + (int)er > 64) {
+            const float4* wd = c.wide + 5 * (size_t)stack[--sp];
+            const float4 lmin = wd[0], lmax = wd[1], rmin = wd[2], rmax = wd[3], refs = wd[4];
+            const uint32_t lref = __float_as_uint(refs.x), rref = __float_as_uint(refs.y);
+            const bool el = enter(lmin, lmax), er = enter(rmin, rmax);
+            if (el && (lref & 0x80000000u)) emit(lref & 0x7fffffffu, lmax.w);
+            if (er && (rref & 0x80000000u)) emit(rref & 0x7fffffffu, rmax.w);
+            const bool pl = el && !(lref & 0x80000000u), pr = er && !(rref & 0x80000000u);
+            if (sp + (int)pl + (int)pr > 64) {
                 atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
                 break;
             }
-            if (er) stack[sp++] = r;
-            if (el) stack[sp++] = l;
+            if (pr) stack[sp++] = (int)rref;
+            if (pl) stack[sp++] = (int)lref;
         }
     }
     if (!WRITE) {

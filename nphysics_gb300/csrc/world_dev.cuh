@@ -46,8 +46,8 @@ constexpr int kRowFloats = 28;       // J1[6] J2[6] WJ1[6] WJ2[6] r rhs impulse 
 constexpr int kMaxColours = 64;      // colour buckets of the per-world schedule
 constexpr int kColourBits = 56;      // colours a step may use (the colour word's mask)
 constexpr unsigned long long kColourMask = (1ull << kColourBits) - 1ull;
-constexpr int kLeafCap = 16;
-constexpr int kPosRec = 7 + 4;       // float4 of a manifold's position-solver record         // partners a broad-phase leaf keeps between its two passes
+constexpr int kLeafCap = 16;        // partners a broad-phase leaf keeps between its two passes
+constexpr int kPosRec = 7 + 4;       // float4 of a manifold's position-solver record
 
 // Row field offsets.
 enum { RF_J1 = 0, RF_J2 = 6, RF_WJ1 = 12, RF_WJ2 = 18, RF_R = 24, RF_RHS = 25, RF_IMP = 26, RF_MU = 27 };
@@ -89,6 +89,7 @@ struct Colliders {
     // LBVH over the alive colliders (n - 1 internal nodes, n leaves).
     int *left, *right, *parent;
     float4 *node_min, *node_max;
+    float4 *wide;                    // 5 per internal node: both children's boxes and references
     int *node_flag;
     uint32_t *leaf_count, *leaf_offset;
     uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
