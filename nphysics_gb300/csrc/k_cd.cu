@@ -307,9 +307,16 @@ __device__ __forceinline__ unsigned long long order_bits(double v) {
     return (b & 0x8000000000000000ull) ? ~b : (b | 0x8000000000000000ull);
 }
 
+// Per-thread totals of the narrow phase, folded into the step's counters once
+// per block: same-address atomics from every pair serialise in L2.
+struct NarrowTotals {
+    uint32_t contacts = 0, manifolds = 0;
+    unsigned long long pen_bits = 0;   // order_bits of the deepest penetration
+};
+
 // One-shot manifold of pair p, keeping the impulses cached under the same
 // feature key in the pair's previous manifold.
-__device__ __noinline__ void narrow_pair(const World& w, uint32_t p) {
+__device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotals& tot) {
     uint2 pr = w.cur.pair[p];
     uint32_t c1 = pr.x, c2 = pr.y;
     const Colliders& c = w.c;
@@ -372,16 +379,43 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p) {
     }
     w.cur.ncont[p] = (uint8_t)nc;
     if (nc > 0) {
-        atomicAdd(&w.ctl->ncontacts, (uint32_t)nc);
-        atomicAdd(&w.ctl->nmanifolds, 1u);
-        atomicMax(&w.ctl->max_pen_bits, order_bits(maxpen));
+        tot.contacts += (uint32_t)nc;
+        tot.manifolds += 1u;
+        const unsigned long long pb = order_bits(maxpen);
+        tot.pen_bits = pb > tot.pen_bits ? pb : tot.pen_bits;
     }
 }
 
 __global__ void k_narrow(World w) {
     uint32_t npairs = w.ctl->npairs;
+    NarrowTotals tot;
     for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < npairs; p += gridDim.x * blockDim.x)
-        narrow_pair(w, p);
+        narrow_pair(w, p, tot);
+    // Block totals: warp shuffles, then one warp over the per-warp partials.
+    __shared__ NarrowTotals part[kThreads / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        tot.contacts += __shfl_xor_sync(0xffffffffu, tot.contacts, o);
+        tot.manifolds += __shfl_xor_sync(0xffffffffu, tot.manifolds, o);
+        const unsigned long long pb = __shfl_xor_sync(0xffffffffu, tot.pen_bits, o);
+        tot.pen_bits = pb > tot.pen_bits ? pb : tot.pen_bits;
+    }
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    if (lane == 0) part[warp] = tot;
+    __syncthreads();
+    if (warp == 0) {
+        tot = lane < (int)(blockDim.x >> 5) ? part[lane] : NarrowTotals{};
+        for (int o = 16; o > 0; o >>= 1) {
+            tot.contacts += __shfl_xor_sync(0xffffffffu, tot.contacts, o);
+            tot.manifolds += __shfl_xor_sync(0xffffffffu, tot.manifolds, o);
+            const unsigned long long pb = __shfl_xor_sync(0xffffffffu, tot.pen_bits, o);
+            tot.pen_bits = pb > tot.pen_bits ? pb : tot.pen_bits;
+        }
+        if (lane == 0 && tot.manifolds > 0) {
+            atomicAdd(&w.ctl->ncontacts, tot.contacts);
+            atomicAdd(&w.ctl->nmanifolds, tot.manifolds);
+            atomicMax(&w.ctl->max_pen_bits, tot.pen_bits);
+        }
+    }
 }
 
 size_t sort_temp_bytes(uint32_t n) {

@@ -538,6 +538,7 @@ __global__ void k_act_root(World w) {
 
 __global__ void k_act_apply(World w) {
     const Bodies& b = w.b;
+    uint32_t active = 0;   // folded per warp below
     GRID_FOR(i, w.nb_slots) {
         uint32_t info = b.info[i];
         uint32_t st = bi_status(info);
@@ -554,34 +555,56 @@ __global__ void k_act_apply(World w) {
             }
         } else if (st != 3u) {
             b.info[i] = info | BI_ISLAND;
-            atomicAdd(&w.ctl->nactive, 1u);
+            ++active;
             if (!(en != 0.0f) && body_can_sleep(info)) body_activate(b, i);
         }
     }
+    active = __reduce_add_sync(0xffffffffu, active);
+    if ((threadIdx.x & 31u) == 0u && active > 0u) atomicAdd(&w.ctl->nactive, active);
 }
 
 // ================================================================ collection + colouring
+// Whole warps walk the pairs together, so a warp takes the solver slots of
+// its manifolds with one atomic (same-address atomics serialise in L2). The
+// slot order is free: everything downstream orders manifolds by priority.
 __global__ void k_collect(World w) {
     const uint32_t npairs = w.ctl->npairs;
     const Bodies& b = w.b;
-    GRID_FOR(q, npairs) {
-        uint32_t nc = w.cur.ncont[q];
-        if (nc == 0) continue;
-        uint2 pr = w.cur.pair[q];
-        uint32_t b1 = w.c.body[pr.x], b2 = w.c.body[pr.y];
-        uint32_t s1 = bi_status(b.info[b1]), s2 = bi_status(b.info[b2]);
-        if (s1 == 0u || s2 == 0u) continue;
-        bool a1 = s1 == 2u && b.energy[b1] != 0.0f;
-        bool a2 = s2 == 2u && b.energy[b2] != 0.0f;
-        if (!(a1 || a2)) continue;
-        uint32_t m = atomicAdd(&w.ctl->nsolver, 1u);
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t q0 = blockIdx.x * blockDim.x + (threadIdx.x & ~31u); q0 < npairs; q0 += gridDim.x * blockDim.x) {
+        const uint32_t q = q0 + lane;
+        uint32_t nc = 0, b1 = 0, b2 = 0, s1 = 0, s2 = 0;
+        bool take = false;
+        if (q < npairs) nc = w.cur.ncont[q];
+        if (nc != 0) {
+            uint2 pr = w.cur.pair[q];
+            b1 = w.c.body[pr.x];
+            b2 = w.c.body[pr.y];
+            s1 = bi_status(b.info[b1]);
+            s2 = bi_status(b.info[b2]);
+            if (s1 != 0u && s2 != 0u) {
+                bool a1 = s1 == 2u && b.energy[b1] != 0.0f;
+                bool a2 = s2 == 2u && b.energy[b2] != 0.0f;
+                take = a1 || a2;
+            }
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, take);
+        if (bal == 0u) continue;
+        const uint32_t contacts = __reduce_add_sync(0xffffffffu, take ? nc : 0u);
+        uint32_t base = 0;
+        if (lane == 0) {
+            base = atomicAdd(&w.ctl->nsolver, (uint32_t)__popc(bal));
+            atomicAdd(&w.ctl->nsolver_contacts, contacts);
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (!take) continue;
+        const uint32_t m = base + (uint32_t)__popc(bal & ((1u << lane) - 1u));
         w.s.sm_list[m] = q;
         w.s.sm_b1[m] = s1 == 2u ? (int)b1 : -1;
         w.s.sm_b2[m] = s2 == 2u ? (int)b2 : -1;
         w.s.sm_nc[m] = nc;
         if (s1 == 2u) atomicAdd(&b.adj_count[b1], 1u);
         if (s2 == 2u) atomicAdd(&b.adj_count[b2], 1u);
-        atomicAdd(&w.ctl->nsolver_contacts, nc);
     }
 }
 
@@ -645,6 +668,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     }
     unsigned long long t0 = 0;
     unsigned backoff = 32;
+    uint32_t ncol = 0;   // colours this thread used, folded per warp below
     while (__any_sync(0xffffffffu, done != todo)) {
         bool progress = false;
         for (uint32_t k = 0; k < nmine; ++k) {
@@ -670,7 +694,7 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             const unsigned long long bit = 1ull << col;
             if (b1 >= 0) st_relaxed64(b.cw + b1, ((unsigned long long)(r1 + 1u) << 56) | (u1 & kColourMask) | bit);
             if (b2 >= 0) st_relaxed64(b.cw + b2, ((unsigned long long)(r2 + 1u) << 56) | (u2 & kColourMask) | bit);
-            atomicMax(&w.ctl->ncolours, col + 1u);
+            ncol = col + 1u > ncol ? col + 1u : ncol;
             done |= 1u << k;
             progress = true;
         }
@@ -681,6 +705,8 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             return;
         }
     }
+    ncol = __reduce_max_sync(0xffffffffu, ncol);
+    if ((threadIdx.x & 31u) == 0u && ncol > 0u) atomicMax(&w.ctl->ncolours, ncol);
 }
 
 // ================================================================ assembly
