@@ -45,6 +45,15 @@ LAUNCHES_PER_STEP_BATCHED = 24
 VELOCITY_TRAFFIC_PER_LAUNCH = 16809728
 
 
+def pinned(a):
+    """A copy of `a` in page-locked host memory (a numpy view of a pinned torch buffer)."""
+    import torch
+    buf = torch.empty(max(a.nbytes, 1), dtype=torch.uint8, pin_memory=True).numpy()
+    out = buf[:a.nbytes].view(a.dtype).reshape(a.shape)
+    out[...] = a
+    return out
+
+
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -62,6 +71,11 @@ def parse():
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--schedule", default="auto", choices=["auto", "grid", "worlds"],
+                    help="solver launch shape: timed candidates (auto), the one cooperative grid, or one "
+                         "block or warp per world (batched worlds)")
+    ap.add_argument("--world-threads", type=int, default=256, choices=[64, 128, 256],
+                    help="threads per block of the per-world schedule when --schedule worlds")
     ap.add_argument("--no-pgs-iterations", action="store_true",
                     help="skip the iterations-to-1e-4 comparison of the learned and plain warm starts")
     args = ap.parse_args()
@@ -279,7 +293,13 @@ def run_gpu(args):
     n_dyn = sc.num_dynamic
     w.step(args.settle)
     # Launch shape chosen on real steps (every candidate gives the same bits).
-    tuned = w.autotune(5)
+    if args.schedule == "auto":
+        tuned = w.autotune(5)
+    else:
+        tuned = ((1, 0) if args.schedule == "grid" else (2, args.world_threads)) + (0.0,)
+        q = w.params
+        q.solver_schedule, q.world_threads = tuned[0], tuned[1]
+        w.set_params(q)
     p = w.params
     w.step(args.warmup)
     first_timed = int(w.counters()["steps"])
@@ -306,11 +326,12 @@ def run_gpu(args):
     value = multirank.reduce_sum(n_dyn * args.steps, device="cuda") / (total_ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ------------------------------------
-    pos = np.zeros((len(sc.bodies), 7), np.float32)
-    vel = np.zeros((len(sc.bodies), 6), np.float32)
+    # Page-locked host arrays, as a host that streams every step would keep them.
+    pos = pinned(np.zeros((len(sc.bodies), 7), np.float32))
+    vel = pinned(np.zeros((len(sc.bodies), 6), np.float32))
     dyn = np.nonzero(sc.bodies["status"] == 2)[0]
-    handles = np.ascontiguousarray(sc.body_handles[dyn])
-    forces = np.zeros((len(dyn), 6), np.float32)
+    handles = pinned(np.ascontiguousarray(sc.body_handles[dyn]))
+    forces = pinned(np.zeros((len(dyn), 6), np.float32))
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):

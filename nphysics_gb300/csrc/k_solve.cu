@@ -903,13 +903,17 @@ struct CachedContacts {
 // the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
 // normal rows (sor_prox.rs:181-230). l1, l2 are the dynamic bodies' rows in
 // `dvbase` (-1: no dofs), the global Δv array or a world's shared-memory Δv.
-template <class Src, class BM>
+// KIND fixes the sweep kind at compile time (0 warm start, 1 friction rows,
+// 2 normal rows) where the caller knows it; -1 decides from `sweep`.
+enum { SWEEP_ANY = -1, SWEEP_WARM = 0, SWEEP_FRICTION = 1, SWEEP_NORMAL = 2 };
+template <int KIND, class Src, class BM>
 __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, uint32_t mask, uint32_t sweep,
                                                   const BM& bm, bool h1, bool h2, DV& dv, Control* ctl) {
+    const int kind = KIND != SWEEP_ANY ? KIND : (sweep == 0 ? SWEEP_WARM : (sweep & 1u) ? SWEEP_FRICTION : SWEEP_NORMAL);
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = src.rec(k);
         float4 l = src.get_lam(k);
-        if (sweep == 0) {
+        if (kind == SWEEP_WARM) {
             np::V t[2];
             src.tangents(c, k, t);
             float li[3] = {l.x, l.y, l.z};
@@ -935,7 +939,7 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
                     atomicAdd(&ctl->learned_kept, 1u);
                 }
             }
-        } else if (sweep & 1u) {
+        } else if (kind == SWEEP_FRICTION) {
             np::V t[2];
             src.tangents(c, k, t);
             float li = l.x;
@@ -975,6 +979,7 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
 
 // Velocity task of manifold m read from global memory; g1, g2 are the dynamic
 // bodies' slots (-1: no dofs), l1, l2 their Δv rows.
+template <int KIND>
 __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
                                               float* dvbase) {
     BodyMasses bm;
@@ -984,7 +989,7 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     DV dv;
     load_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
     load_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
-    velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
+    velocity_task_src<KIND>(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
     store_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
     store_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
 }
@@ -1097,14 +1102,14 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
             if (k == 0 && cached) {
-                velocity_task_src(cc, nc0, mask0, sw, cc, b1 >= 0, b2 >= 0, dv, w.ctl);
+                velocity_task_src<SWEEP_ANY>(cc, nc0, mask0, sw, cc, b1 >= 0, b2 >= 0, dv, w.ctl);
             } else {
                 const uint32_t m = t + k * T;
                 BodyMasses bm;
                 if (b1 >= 0) bm.s[0] = load_sb(w.b.sb, b1);
                 if (b2 >= 0) bm.s[1] = load_sb(w.b.sb, b2);
                 GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
-                velocity_task_src(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv, w.ctl);
+                velocity_task_src<SWEEP_ANY>(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv, w.ctl);
             }
             publish_dvf(w.b.dvf, b1, t1 + 1u, dv.a);
             publish_dvf(w.b.dvf, b2, t2 + 1u, dv.b);
@@ -1271,6 +1276,7 @@ struct WorldGroup {
 
 // One sweep (warm start, friction or normal rows) over a world's manifolds,
 // colour by colour.
+template <int KIND>
 __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_t base, uint32_t nbw, uint32_t ncol,
                                             uint32_t sweep, float* s_dv, const WorldGroup& g) {
     const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
@@ -1281,7 +1287,7 @@ __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_
             uint32_t m = w.s.wm_order[i];
             int l1, l2;
             if (world_locals(w, m, base, nbw, l1, l2))
-                velocity_task(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, s_dv);
+                velocity_task<KIND>(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, s_dv);
         }
         g.sync();
     }
@@ -1331,9 +1337,12 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
     const uint32_t ncol = w.ctl->ncolours;
     for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) s_dv[i] = 0.0f;
     g.sync();
-    world_sweep(w, wd, base, nbw, ncol, 0, s_dv, g);
+    world_sweep<SWEEP_WARM>(w, wd, base, nbw, ncol, 0, s_dv, g);
     world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc_init, g);
-    for (uint32_t sw = 1; sw < 1 + 2 * p.max_velocity_iterations; ++sw) world_sweep(w, wd, base, nbw, ncol, sw, s_dv, g);
+    for (uint32_t it = 0; it < p.max_velocity_iterations; ++it) {
+        world_sweep<SWEEP_FRICTION>(w, wd, base, nbw, ncol, 1 + 2 * it, s_dv, g);
+        world_sweep<SWEEP_NORMAL>(w, wd, base, nbw, ncol, 2 + 2 * it, s_dv, g);
+    }
     world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc, g);
     for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) w.b.dv[6 * base + i] = s_dv[i];
     g.sync();
@@ -1730,6 +1739,15 @@ static const size_t kVelocitySmem = (size_t)kCoopThreads * kCacheF4 * sizeof(flo
 
 // Dynamic shared memory of the per-world velocity kernel: Δv (6 floats) per
 // body slot of the largest world, or per slot of a small world for each warp.
+// The per-world velocity kernel for a block size (64, 128 or 256).
+static const void* world_velocity_fn(int threads) {
+    switch (threads) {
+    case 64: return (const void*)k_world_velocity<64>;
+    case 256: return (const void*)k_world_velocity<256>;
+    default: return (const void*)k_world_velocity<128>;
+    }
+}
+
 static size_t world_smem(uint32_t max_world_bodies, int threads) {
     size_t big = 6 * (size_t)max_world_bodies, warps = (size_t)(threads / 32) * 6 * kWarpWorldBodies;
     return (big > warps ? big : warps) * sizeof(float);
@@ -1747,9 +1765,9 @@ void solver_grid_sizes(int device, SolverLaunch& L) {
     L.grid_position = sms * (per < 1 ? 1 : per);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_world_position<128>, 128, 0);
     L.grid_world_position = sms * (per < 1 ? 1 : per);
-    for (const void* f : {(const void*)k_world_velocity<64>, (const void*)k_world_velocity<128>,
-                          (const void*)k_world_velocity<256>})
-        cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)world_smem(kMaxWorldBodies, 256));
+    for (int t : {64, 128, 256})
+        cudaFuncSetAttribute(world_velocity_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)world_smem(kMaxWorldBodies, t));
 }
 
 uint64_t grid_task_capacity(const SolverLaunch& L) {
@@ -1760,9 +1778,8 @@ uint64_t grid_task_capacity(const SolverLaunch& L) {
 int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds, int threads) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    const void* f = threads == 64 ? (const void*)k_world_velocity<64>
-                                  : threads == 256 ? (const void*)k_world_velocity<256> : (const void*)k_world_velocity<128>;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, f, threads, world_smem(max_world_bodies, threads));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, world_velocity_fn(threads), threads,
+                                                  world_smem(max_world_bodies, threads));
     long g = (long)sms * (per < 1 ? 1 : per);
     if (g > (long)n_worlds) g = n_worlds;
     return g < 1 ? 1 : (int)g;
@@ -1810,12 +1827,11 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         if (e != cudaSuccess) return e;
         k_world_scatter<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
         const size_t smem = world_smem(L.max_world_bodies, L.world_threads);
-        if (L.world_threads == 64)
-            k_world_velocity<64><<<L.grid_world, 64, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies, L.n_big);
-        else if (L.world_threads == 256)
-            k_world_velocity<256><<<L.grid_world, 256, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies, L.n_big);
-        else
-            k_world_velocity<128><<<L.grid_world, 128, smem, st>>>(wc, pc, L.n_worlds, L.max_world_bodies, L.n_big);
+        uint32_t nw = L.n_worlds, mwb = L.max_world_bodies, nbig = L.n_big;
+        void* wargs[] = {&wc, &pc, &nw, &mwb, &nbig};
+        e = cudaLaunchKernel(world_velocity_fn(L.world_threads), dim3(L.grid_world), dim3(L.world_threads), wargs, smem,
+                             st);
+        if (e != cudaSuccess) return e;
         k_world_finish<<<1, 1, 0, st>>>(wc, pc);
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);

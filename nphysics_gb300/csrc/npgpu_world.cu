@@ -216,9 +216,10 @@ static StepParams step_params(const npgpu_world* w) {
     return s;
 }
 
-// Copies `bytes` from host memory to the device staging area (synchronously
-// with respect to earlier uses of the staging area) and returns its device pointer.
-static npgpu_status stage_upload(npgpu_world* w, const void* src, size_t bytes, void** dptr) {
+// The pinned host staging area, at least `bytes` long, once earlier uses of
+// it are done; stage_commit then copies its first `bytes` to the device
+// staging area and returns the device pointer.
+static npgpu_status stage_reserve(npgpu_world* w, size_t bytes, void** hptr) {
     CK(cudaEventSynchronize(w->ev_stage), "staging wait");
     if (bytes > w->h_stage_bytes) {
         if (w->h_stage) cudaFreeHost(w->h_stage);
@@ -234,11 +235,36 @@ static npgpu_status stage_upload(npgpu_world* w, const void* src, size_t bytes, 
         CK(cudaMalloc(&w->d_stage, nb), "device staging");
         w->d_stage_bytes = nb;
     }
-    std::memcpy(w->h_stage, src, bytes);
+    *hptr = w->h_stage;
+    return NPGPU_OK;
+}
+
+static npgpu_status stage_commit(npgpu_world* w, size_t bytes, void** dptr) {
     CK(cudaMemcpyAsync(w->d_stage, w->h_stage, bytes, cudaMemcpyHostToDevice, w->stream), "staging copy");
     CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
     *dptr = w->d_stage;
     return NPGPU_OK;
+}
+
+// Copies `bytes` from host memory to the device staging area (synchronously
+// with respect to earlier uses of the staging area) and returns its device pointer.
+static npgpu_status stage_upload(npgpu_world* w, const void* src, size_t bytes, void** dptr) {
+    void* h = nullptr;
+    npgpu_status st = stage_reserve(w, bytes, &h);
+    if (st != NPGPU_OK) return st;
+    std::memcpy(h, src, bytes);
+    return stage_commit(w, bytes, dptr);
+}
+
+// True when `p` is page-locked host memory the copy engines can reach directly.
+static bool host_pinned(const void* p) {
+    if (!p) return true;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return a.type == cudaMemoryTypeHost;
 }
 
 static void sync_world_view(npgpu_world* w) {
@@ -766,7 +792,13 @@ npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
 npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* handles, const float* forces6,
                                 int auto_wake_up) {
     if (!w || (n && (!handles || !forces6))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
-    std::vector<ForceUpload> up(n);
+    if (n == 0) return NPGPU_OK;
+    // Checked and packed straight into the pinned staging area; nothing is
+    // copied to the device unless every force is valid.
+    void* hp = nullptr;
+    npgpu_status st = stage_reserve(w, (size_t)n * sizeof(ForceUpload), &hp);
+    if (st != NPGPU_OK) return st;
+    ForceUpload* up = (ForceUpload*)hp;
     for (uint32_t k = 0; k < n; ++k) {
         if (!body_handle_ok(w, handles[k])) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
         if (!finite_n(forces6 + 6 * k, 6)) return fail(w, NPGPU_ERR_NAN, "force is not finite");
@@ -774,9 +806,8 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
         up[k].wake = auto_wake_up ? 1u : 0u;
         std::memcpy(up[k].f, forces6 + 6 * k, sizeof(up[k].f));
     }
-    if (up.empty()) return NPGPU_OK;
     void* dp = nullptr;
-    npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(ForceUpload), &dp);
+    st = stage_commit(w, (size_t)n * sizeof(ForceUpload), &dp);
     if (st != NPGPU_OK) return st;
     CK(launch_forces(w->dw, (const ForceUpload*)dp, n, w->stream), "apply forces");
     CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
@@ -1095,6 +1126,16 @@ npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, f
     CK(launch_pack_bodies(w->dw, first, n, position ? dpos : nullptr, velocity ? dvel : nullptr, energy ? den : nullptr,
                           active ? dact : nullptr, w->stream),
        "pack bodies");
+    if (host_pinned(position) && host_pinned(velocity) && host_pinned(energy) && host_pinned(active)) {
+        // Page-locked destinations: the copy engines write them directly.
+        if (position) CK(cudaMemcpyAsync(position, dpos, 7 * sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+        if (velocity) CK(cudaMemcpyAsync(velocity, dvel, 6 * sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+        if (energy) CK(cudaMemcpyAsync(energy, den, sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+        if (active) CK(cudaMemcpyAsync(active, dact, n, cudaMemcpyDeviceToHost, w->stream), "d2h");
+        CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+        CK(cudaStreamSynchronize(w->stream), "download");
+        return NPGPU_OK;
+    }
     char* h = (char*)w->h_stage;
     if (position) CK(cudaMemcpyAsync(h, dpos, 7 * sizeof(float) * n, cudaMemcpyDeviceToHost, w->stream), "d2h");
     if (velocity)

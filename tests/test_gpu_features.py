@@ -168,3 +168,43 @@ def test_applied_forces_and_sleep(gpu_lib):
         o.step(1)
     same(g, o, "pushed")
     assert g.bodies()["active"][[1, 4, 7]].all()
+
+
+def test_pinned_host_buffers(gpu_lib):
+    # Forces read from and poses written to page-locked host arrays (the
+    # copy engines reach them directly) give what pageable arrays give; a
+    # force batch with one bad handle is rejected whole.
+    import torch
+
+    def pinned(a):
+        buf = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True).numpy()
+        out = buf.view(a.dtype).reshape(a.shape)
+        out[...] = a
+        return out
+
+    pb, pc = balls_on_ground(9, seed=3)
+    bodies, colliders = scenes._concat(pb, pc)
+    sc = scenes.Scene("pinned", bodies, colliders)
+    g, o = pair(sc)
+    h = np.ascontiguousarray(sc.body_handles[[2, 5]])
+    f = np.zeros((2, 6), np.float32)
+    f[:, 1] = (40.0, 25.0)
+    hp, fp = pinned(h), pinned(f)
+    bad = h.copy()
+    bad[1]["generation"] += 1
+    from nphysics_gb300.world import NpgpuError
+    with pytest.raises(NpgpuError) as e:
+        g.apply_forces(pinned(bad), fp)
+    assert e.value.status == abi.ERR_INVALID_HANDLE
+    for _ in range(30):
+        g.apply_forces(hp, fp, wake=True)
+        o.apply_forces(h, f, wake=True)
+        g.step(1)
+        o.step(1)
+    same(g, o, "pinned forces")
+    n = g.num_bodies
+    pos, vel = pinned(np.zeros((n, 7), np.float32)), pinned(np.zeros((n, 6), np.float32))
+    g.download_into(pos, vel)
+    ref = g.bodies()
+    np.testing.assert_array_equal(pos, ref["position"])
+    np.testing.assert_array_equal(vel, ref["velocity"])
