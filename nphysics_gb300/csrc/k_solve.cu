@@ -28,12 +28,15 @@
 // dependent manifolds rather than a barrier per colour. The colouring uses the
 // same scheme over priorities. Threads poll their tasks without blocking, so
 // any assignment of manifolds to resident threads makes progress.
+#include <cooperative_groups.h>
 #include <cub/device/device_scan.cuh>
 
 #include "mlp.cuh"
 #include "narrow.cuh"
 
 namespace npgpu_dev {
+
+namespace cg = cooperative_groups;
 
 constexpr int kItemThreads = 256;
 constexpr int kCoopThreads = 256;
@@ -977,21 +980,52 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
     }
 }
 
+// Where a world's Δv rows live during its velocity solve: one array in the
+// block's shared memory (6 floats per body), or spread over the shared
+// memories of a thread-block cluster, 2^shift bodies per block, reached
+// through distributed shared memory.
+struct SharedDv {
+    float* base;
+    __device__ __forceinline__ void load(int l, float* o) const { load_dv(base, l, o); }
+    __device__ __forceinline__ void store(int l, const float* o) const { store_dv(base, l, o); }
+};
+struct ClusterDv {
+    float* base;
+    uint32_t shift;
+    __device__ __forceinline__ float2* row(int l) const {
+        float* r = cg::this_cluster().map_shared_rank(base, (unsigned)((uint32_t)l >> shift));
+        return (float2*)(r + 6 * ((uint32_t)l & ((1u << shift) - 1u)));
+    }
+    __device__ __forceinline__ void load(int l, float* o) const {
+        if (l < 0) return;
+        const float2* r = row(l);
+        float2 a = r[0], b = r[1], c = r[2];
+        o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y; o[4] = c.x; o[5] = c.y;
+    }
+    __device__ __forceinline__ void store(int l, const float* o) const {
+        if (l < 0) return;
+        float2* r = row(l);
+        r[0] = make_float2(o[0], o[1]);
+        r[1] = make_float2(o[2], o[3]);
+        r[2] = make_float2(o[4], o[5]);
+    }
+};
+
 // Velocity task of manifold m read from global memory; g1, g2 are the dynamic
-// bodies' slots (-1: no dofs), l1, l2 their Δv rows.
-template <int KIND>
+// bodies' slots (-1: no dofs), l1, l2 their Δv rows in `dva`.
+template <int KIND, class DvA>
 __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
-                                              float* dvbase) {
+                                              const DvA& dva) {
     BodyMasses bm;
     if (g1 >= 0) bm.s[0] = load_sb(w.b.sb, g1);
     if (g2 >= 0) bm.s[1] = load_sb(w.b.sb, g2);
     GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
     DV dv;
-    load_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
-    load_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
+    dva.load(g1 >= 0 ? l1 : -1, dv.a);
+    dva.load(g2 >= 0 ? l2 : -1, dv.b);
     velocity_task_src<KIND>(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
-    store_dv(dvbase, g1 >= 0 ? l1 : -1, dv.a);
-    store_dv(dvbase, g2 >= 0 ? l2 : -1, dv.b);
+    dva.store(g1 >= 0 ? l1 : -1, dv.a);
+    dva.store(g2 >= 0 ? l2 : -1, dv.b);
 }
 
 // Fills the running thread's cache with manifold m (nc <= kCacheContacts).
@@ -1249,6 +1283,37 @@ __global__ void k_world_scatter(World w, uint32_t n_worlds) {
     }
 }
 
+// Renumbers the solver manifolds in (world, colour) order: manifold i of the
+// new numbering is wm_order[i] of the old. Gathered into the scratch arrays
+// first, then copied back; assembly and everything after it use the new
+// numbering, so a colour of a world is one run of indices.
+__global__ void k_world_permute(World w, uint32_t n_worlds) {
+    const uint32_t ms = w.ctl->nsolver, total = w.s.bucket_start[n_worlds * kMaxColours];
+    const size_t P = w.cap_pairs;
+    uint32_t* t = w.s.perm;
+    GRID_FOR(i, ms) {
+        const uint32_t m = i < total ? w.s.wm_order[i] : i;
+        t[i] = w.s.sm_list[m];
+        t[P + i] = (uint32_t)w.s.sm_b1[m];
+        t[2 * P + i] = (uint32_t)w.s.sm_b2[m];
+        t[3 * P + i] = w.s.sm_nc[m];
+        t[4 * P + i] = w.s.sm_colour[m];
+    }
+}
+
+__global__ void k_world_permute_back(World w) {
+    const uint32_t ms = w.ctl->nsolver;
+    const size_t P = w.cap_pairs;
+    const uint32_t* t = w.s.perm;
+    GRID_FOR(i, ms) {
+        w.s.sm_list[i] = t[i];
+        w.s.sm_b1[i] = (int)t[P + i];
+        w.s.sm_b2[i] = (int)t[2 * P + i];
+        w.s.sm_nc[i] = t[3 * P + i];
+        w.s.sm_colour[i] = t[4 * P + i];
+    }
+}
+
 // World-local index of body slot b (-1 stays -1). A body outside the world's
 // slot range flags an error and the task is skipped.
 __device__ __forceinline__ bool world_locals(const World& w, uint32_t m, uint32_t base, uint32_t nbw, int& l1, int& l2) {
@@ -1262,53 +1327,58 @@ __device__ __forceinline__ bool world_locals(const World& w, uint32_t m, uint32_
     return true;
 }
 
-// A world is processed by a group of threads: a whole block (large worlds)
-// or one warp (small worlds, several per block). `lane` and `width` place the
-// thread in its group; the group's barrier orders the colours.
+// A world is processed by a group of threads: a thread-block cluster (the
+// widest worlds), a whole block (large worlds) or one warp (small worlds,
+// several per block). `lane` and `width` place the thread in its group; the
+// group's barrier orders the colours.
+enum : uint32_t { GROUP_BLOCK = 0, GROUP_WARP = 1, GROUP_CLUSTER = 2 };
 struct WorldGroup {
     uint32_t lane, width;
-    bool warp;
+    uint32_t kind;
+    __device__ __forceinline__ bool warp() const { return kind == GROUP_WARP; }
     __device__ __forceinline__ void sync() const {
-        if (warp) __syncwarp();
+        if (kind == GROUP_WARP) __syncwarp();
+        else if (kind == GROUP_CLUSTER) cg::this_cluster().sync();
         else __syncthreads();
     }
+    // The thread that adds this block's (or warp's) partial sums.
+    __device__ __forceinline__ bool leader() const { return kind == GROUP_WARP ? lane == 0 : threadIdx.x == 0; }
 };
 
 // One sweep (warm start, friction or normal rows) over a world's manifolds,
 // colour by colour.
-template <int KIND>
+template <int KIND, class DvA>
 __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_t base, uint32_t nbw, uint32_t ncol,
-                                            uint32_t sweep, float* s_dv, const WorldGroup& g) {
+                                            uint32_t sweep, const DvA& dva, const WorldGroup& g) {
     const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
     for (uint32_t c = 0; c < ncol; ++c) {
         uint32_t lo = bs[c], hi = bs[c + 1];
         if (lo == hi) continue;
-        for (uint32_t i = lo + g.lane; i < hi; i += g.width) {
-            uint32_t m = w.s.wm_order[i];
+        for (uint32_t m = lo + g.lane; m < hi; m += g.width) {
             int l1, l2;
             if (world_locals(w, m, base, nbw, l1, l2))
-                velocity_task<KIND>(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, s_dv);
+                velocity_task<KIND>(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, dva);
         }
         g.sync();
     }
 }
 
 // FP64 residual partial sums of one world, added to acc[0..1].
+template <class DvA>
 __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint32_t base, uint32_t nbw,
-                                               const float* s_dv, double* sh, double* acc, const WorldGroup& g) {
+                                               const DvA& dva, double* sh, double* acc, const WorldGroup& g) {
     uint32_t lo = w.s.bucket_start[wd * kMaxColours], hi = w.s.bucket_start[wd * kMaxColours + kMaxColours];
     double s2 = 0.0, l2 = 0.0;
-    for (uint32_t i = lo + g.lane; i < hi; i += g.width) {
-        uint32_t m = w.s.wm_order[i];
+    for (uint32_t m = lo + g.lane; m < hi; m += g.width) {
         int b1, b2;
         if (!world_locals(w, m, base, nbw, b1, b2)) continue;
         DV dv;
-        load_dv(s_dv, b1, dv.a);
-        load_dv(s_dv, b2, dv.b);
+        dva.load(b1, dv.a);
+        dva.load(b2, dv.b);
         manifold_residual(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, s2, l2);
     }
     double ts, tl;
-    if (g.warp) {
+    if (g.warp()) {
         for (int o = 16; o > 0; o >>= 1) {
             s2 += __shfl_down_sync(0xffffffffu, s2, o);
             l2 += __shfl_down_sync(0xffffffffu, l2, o);
@@ -1319,10 +1389,24 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
         ts = block_sum(s2, sh);
         tl = block_sum(l2, sh);
     }
-    if (g.lane == 0 && (ts != 0.0 || tl != 0.0)) {
+    if (g.leader() && (ts != 0.0 || tl != 0.0)) {
         atomicAdd(&acc[0], ts);
         atomicAdd(&acc[1], tl);
     }
+}
+
+// The sweeps and residuals of one world's velocity solve by one group.
+template <class DvA>
+__device__ __forceinline__ void world_solve(const World& w, const StepParams& p, uint32_t wd, uint32_t base,
+                                            uint32_t nbw, uint32_t ncol, const DvA& dva, double* sh,
+                                            const WorldGroup& g) {
+    world_sweep<SWEEP_WARM>(w, wd, base, nbw, ncol, 0, dva, g);
+    world_residual(w, wd, base, nbw, dva, sh, w.ctl->res_acc_init, g);
+    for (uint32_t it = 0; it < p.max_velocity_iterations; ++it) {
+        world_sweep<SWEEP_FRICTION>(w, wd, base, nbw, ncol, 1 + 2 * it, dva, g);
+        world_sweep<SWEEP_NORMAL>(w, wd, base, nbw, ncol, 2 + 2 * it, dva, g);
+    }
+    world_residual(w, wd, base, nbw, dva, sh, w.ctl->res_acc, g);
 }
 
 // The whole velocity solve of one world by one group, its Δv in s_dv.
@@ -1337,13 +1421,7 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
     const uint32_t ncol = w.ctl->ncolours;
     for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) s_dv[i] = 0.0f;
     g.sync();
-    world_sweep<SWEEP_WARM>(w, wd, base, nbw, ncol, 0, s_dv, g);
-    world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc_init, g);
-    for (uint32_t it = 0; it < p.max_velocity_iterations; ++it) {
-        world_sweep<SWEEP_FRICTION>(w, wd, base, nbw, ncol, 1 + 2 * it, s_dv, g);
-        world_sweep<SWEEP_NORMAL>(w, wd, base, nbw, ncol, 2 + 2 * it, s_dv, g);
-    }
-    world_residual(w, wd, base, nbw, s_dv, sh, w.ctl->res_acc, g);
+    world_solve(w, p, wd, base, nbw, ncol, SharedDv{s_dv}, sh, g);
     for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) w.b.dv[6 * base + i] = s_dv[i];
     g.sync();
 }
@@ -1351,19 +1429,22 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
 // Persistent. Blocks first take the n_big large worlds from a counter,
 // largest first, one world per block; when none is left each warp takes
 // small worlds (at most kWarpWorldBodies body slots) from a second counter.
+// The first n_cluster worlds of the order are the cluster kernel's.
 // Dynamic shared memory: the larger of 6 floats per body slot of the largest
 // world and 6 floats per slot of a small world for each warp.
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
-                                                                  uint32_t max_world_bodies, uint32_t n_big) {
+                                                                  uint32_t max_world_bodies, uint32_t n_big,
+                                                                  uint32_t n_cluster) {
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
     __shared__ uint32_t s_world;
-    const WorldGroup block{threadIdx.x, blockDim.x, false};
+    const WorldGroup block{threadIdx.x, blockDim.x, GROUP_BLOCK};
+    const uint32_t* order = w.s.world_order + n_cluster;
     for (;;) {
         if (threadIdx.x == 0) {
             uint32_t k = atomicAdd(&w.ctl->world_next[0], 1u);
-            s_world = k < n_big ? w.s.world_order[k] : 0xffffffffu;
+            s_world = k < n_big ? order[k] : 0xffffffffu;
         }
         __syncthreads();
         const uint32_t wd = s_world;
@@ -1372,15 +1453,43 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World
         world_velocity(w, p, wd, max_world_bodies, s_dv, sh, block);
     }
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-    const WorldGroup wg{lane, 32u, true};
+    const WorldGroup wg{lane, 32u, GROUP_WARP};
     float* my_dv = s_dv + (size_t)warp * 6 * kWarpWorldBodies;
     for (;;) {
         uint32_t k = 0;
         if (lane == 0) k = atomicAdd(&w.ctl->world_next[2], 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
-        if (n_big + k >= n_worlds) break;
-        world_velocity(w, p, w.s.world_order[n_big + k], kWarpWorldBodies, my_dv, nullptr, wg);
+        if (n_cluster + n_big + k >= n_worlds) break;
+        world_velocity(w, p, order[n_big + k], kWarpWorldBodies, my_dv, nullptr, wg);
     }
+}
+
+// The widest worlds, one thread-block cluster each (cluster c takes world
+// order[c]): the world's Δv rows are spread over the cluster's shared
+// memories, 2^shift bodies per block, and the cluster barrier orders the
+// colours. Each block writes its own rows back to global memory.
+template <int THREADS>
+__global__ void __launch_bounds__(THREADS, 1) k_cluster_velocity(World w, StepParams p, uint32_t shift) {
+    extern __shared__ float s_dv[];
+    __shared__ double sh[32];
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t nct = cl.num_blocks(), rank = cl.block_rank();
+    const uint32_t wd = w.s.world_order[blockIdx.x / nct];
+    const uint32_t base = w.s.world_start[wd];
+    uint32_t nbw = w.s.world_start[wd + 1] - base;
+    if (nbw > (nct << shift)) {
+        if (threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_WORLD_RANGE);
+        nbw = 0;
+    }
+    for (uint32_t i = threadIdx.x; i < (6u << shift); i += blockDim.x) s_dv[i] = 0.0f;
+    cl.sync();
+    const WorldGroup g{rank * blockDim.x + threadIdx.x, nct * blockDim.x, GROUP_CLUSTER};
+    world_solve(w, p, wd, base, nbw, w.ctl->ncolours, ClusterDv{s_dv, shift}, sh, g);
+    const uint32_t lo = rank << shift, hi = nbw < lo + (1u << shift) ? nbw : lo + (1u << shift);
+    for (uint32_t i = threadIdx.x; lo + i / 6u < hi && i < (6u << shift); i += blockDim.x)
+        w.b.dv[6 * (size_t)(base + lo) + i] = s_dv[i];
+    // No block leaves while another may still read its shared memory.
+    cl.sync();
 }
 
 __global__ void k_world_finish(World w, StepParams p) {
@@ -1646,7 +1755,7 @@ __device__ __forceinline__ void world_position(const World& w, const StepParams&
         for (uint32_t c = 0; c < ncol; ++c) {
             uint32_t lo = bs[c], hi = bs[c + 1];
             if (lo == hi) continue;
-            for (uint32_t i = lo + g.lane; i < hi; i += g.width) position_task(w, p, w.s.wm_order[i]);
+            for (uint32_t m = lo + g.lane; m < hi; m += g.width) position_task(w, p, m);
             g.sync();
         }
     }
@@ -1656,13 +1765,15 @@ __device__ __forceinline__ void world_position(const World& w, const StepParams&
 // Batched worlds: large worlds one per block, then small worlds one per warp,
 // as in the velocity kernel.
 template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big) {
+__global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big,
+                                                            uint32_t n_cluster) {
     __shared__ uint32_t s_world;
-    const WorldGroup block{threadIdx.x, blockDim.x, false};
+    const WorldGroup block{threadIdx.x, blockDim.x, GROUP_BLOCK};
+    const uint32_t* order = w.s.world_order + n_cluster;
     for (;;) {
         if (threadIdx.x == 0) {
             uint32_t k = atomicAdd(&w.ctl->world_next[1], 1u);
-            s_world = k < n_big ? w.s.world_order[k] : 0xffffffffu;
+            s_world = k < n_big ? order[k] : 0xffffffffu;
         }
         __syncthreads();
         const uint32_t wd = s_world;
@@ -1671,14 +1782,23 @@ __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams 
         world_position(w, p, wd, block);
     }
     const uint32_t lane = threadIdx.x & 31u;
-    const WorldGroup wg{lane, 32u, true};
+    const WorldGroup wg{lane, 32u, GROUP_WARP};
     for (;;) {
         uint32_t k = 0;
         if (lane == 0) k = atomicAdd(&w.ctl->world_next[3], 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
-        if (n_big + k >= n_worlds) break;
-        world_position(w, p, w.s.world_order[n_big + k], wg);
+        if (n_cluster + n_big + k >= n_worlds) break;
+        world_position(w, p, order[n_big + k], wg);
     }
+}
+
+// The cluster worlds' position sweeps: cluster c takes world order[c], the
+// cluster barrier between colours (poses stay in global memory).
+__global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_position(World w, StepParams p) {
+    cg::cluster_group cl = cg::this_cluster();
+    const uint32_t nct = cl.num_blocks();
+    const WorldGroup g{cl.block_rank() * blockDim.x + threadIdx.x, nct * blockDim.x, GROUP_CLUSTER};
+    world_position(w, p, w.s.world_order[blockIdx.x / nct], g);
 }
 
 // ================================================================ post
@@ -1768,6 +1888,7 @@ void solver_grid_sizes(int device, SolverLaunch& L) {
     for (int t : {64, 128, 256})
         cudaFuncSetAttribute(world_velocity_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)world_smem(kMaxWorldBodies, t));
+    L.cluster_ctas = cluster_ctas(device);
 }
 
 uint64_t grid_task_capacity(const SolverLaunch& L) {
@@ -1787,6 +1908,51 @@ int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds, int thr
 
 static cudaError_t coop(const void* fn, int grid, void** args, cudaStream_t st, size_t smem = 0) {
     return cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kCoopThreads), args, smem, st);
+}
+
+static size_t cluster_smem(uint32_t shift) { return (6u * sizeof(float)) << shift; }
+
+int cluster_ctas(int device) {
+    int ok = 0;
+    cudaDeviceGetAttribute(&ok, cudaDevAttrClusterLaunch, device);
+    if (!ok) return 0;
+    const void* fn = (const void*)k_cluster_velocity<kClusterThreads>;
+    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cluster_smem(kClusterShiftMax));
+    cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute((const void*)k_cluster_position, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (int c : {16, 8}) {
+        cudaLaunchConfig_t cfg = {};
+        cudaLaunchAttribute at[1];
+        at[0].id = cudaLaunchAttributeClusterDimension;
+        at[0].val.clusterDim.x = (unsigned)c;
+        at[0].val.clusterDim.y = 1;
+        at[0].val.clusterDim.z = 1;
+        cfg.gridDim = dim3((unsigned)c);
+        cfg.blockDim = dim3(kClusterThreads);
+        cfg.dynamicSmemBytes = cluster_smem(kClusterShiftMax);
+        cfg.attrs = at;
+        cfg.numAttrs = 1;
+        int n = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) == cudaSuccess && n > 0) return c;
+        cudaGetLastError();
+    }
+    return 0;
+}
+
+static cudaError_t launch_cluster(const void* fn, const SolverLaunch& L, size_t smem, void** args, cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = (unsigned)L.cluster_ctas;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3((unsigned)L.cluster_ctas * L.n_cluster);
+    cfg.blockDim = dim3(kClusterThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = st;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelExC(&cfg, fn, args);
 }
 
 cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st) {
@@ -1813,10 +1979,8 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     k_prank<<<npb, kItemThreads, 0, st>>>(wc);
     e = coop((const void*)k_colour, L.grid_colour, args1, st);
     if (e != cudaSuccess) return e;
-    rec(2);
-    k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc);
-    rec(3);
     if (L.batched) {
+        // Bucket the manifolds by (world, colour) and renumber them in that order.
         const uint32_t nbk = L.n_worlds * kMaxColours;
         e = cudaMemsetAsync(w.s.bucket_count, 0, (2 * (size_t)nbk + 1) * sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
@@ -1826,12 +1990,27 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
                                           st);
         if (e != cudaSuccess) return e;
         k_world_scatter<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
-        const size_t smem = world_smem(L.max_world_bodies, L.world_threads);
-        uint32_t nw = L.n_worlds, mwb = L.max_world_bodies, nbig = L.n_big;
-        void* wargs[] = {&wc, &pc, &nw, &mwb, &nbig};
-        e = cudaLaunchKernel(world_velocity_fn(L.world_threads), dim3(L.grid_world), dim3(L.world_threads), wargs, smem,
-                             st);
-        if (e != cudaSuccess) return e;
+        k_world_permute<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
+        k_world_permute_back<<<npb, kItemThreads, 0, st>>>(wc);
+    }
+    rec(2);
+    k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc);
+    rec(3);
+    if (L.batched) {
+        if (L.n_cluster > 0) {
+            uint32_t shift = L.cluster_shift;
+            void* cargs[] = {&wc, &pc, &shift};
+            e = launch_cluster((const void*)k_cluster_velocity<kClusterThreads>, L, cluster_smem(shift), cargs, st);
+            if (e != cudaSuccess) return e;
+        }
+        if (L.n_worlds > L.n_cluster) {
+            const size_t smem = world_smem(L.max_world_bodies, L.world_threads);
+            uint32_t nw = L.n_worlds, mwb = L.max_world_bodies, nbig = L.n_big, ncl = L.n_cluster;
+            void* wargs[] = {&wc, &pc, &nw, &mwb, &nbig, &ncl};
+            e = cudaLaunchKernel(world_velocity_fn(L.world_threads), dim3(L.grid_world), dim3(L.world_threads), wargs,
+                                 smem, st);
+            if (e != cudaSuccess) return e;
+        }
         k_world_finish<<<1, 1, 0, st>>>(wc, pc);
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
@@ -1846,7 +2025,13 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     if (L.batched) {
         // The position sweeps run 128 threads a block whatever the velocity
         // kernel's block size: large worlds a block each, small ones a warp.
-        k_world_position<128><<<L.grid_world_position, 128, 0, st>>>(wc, pc, L.n_worlds, L.n_big);
+        if (L.n_cluster > 0) {
+            void* cargs[] = {&wc, &pc};
+            e = launch_cluster((const void*)k_cluster_position, L, 0, cargs, st);
+            if (e != cudaSuccess) return e;
+        }
+        if (L.n_worlds > L.n_cluster)
+            k_world_position<128><<<L.grid_world_position, 128, 0, st>>>(wc, pc, L.n_worlds, L.n_big, L.n_cluster);
     } else {
         e = coop((const void*)k_position, L.grid_position, args2, st);
         if (e != cudaSuccess) return e;

@@ -140,6 +140,7 @@ struct npgpu_world {
     bool layout_dirty = true;
     bool layout_ok = false;              // the worlds qualify for the per-world schedule
     uint32_t n_worlds = 0, max_world_bodies = 0, n_big_worlds = 0;
+    uint32_t n_cluster_worlds = 0, cluster_shift = 0;   // worlds solved by a thread-block cluster
     std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries, then the n_worlds largest-first order
     uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
     bool layout_on_device = false;
@@ -278,7 +279,9 @@ static void sync_world_view(npgpu_world* w) {
 
 // Finds each world's slot range. The per-world schedule needs the alive
 // bodies' world indices non-decreasing in slot order (so a world is one run of
-// slots), at least two worlds and no world wider than the shared-memory limit.
+// slots). Worlds up to kMaxWorldBodies slots are solved by a block or a warp;
+// wider ones by a thread-block cluster, up to its distributed shared-memory
+// limit.
 static void compute_layout(npgpu_world* w) {
     w->layout_dirty = false;
     w->layout_ok = false;
@@ -291,7 +294,7 @@ static void compute_layout(npgpu_world* w) {
         last = b.world;
         any = true;
     }
-    if (!any || last == 0) return;
+    if (!any) return;
     const uint32_t nw = last + 1;
     std::vector<uint32_t> st(nw + 1, 0xffffffffu);
     for (uint32_t i = 0; i < w->nb_slots; ++i) {
@@ -302,9 +305,17 @@ static void compute_layout(npgpu_world* w) {
     for (uint32_t k = nw; k-- > 0;)
         if (st[k] == 0xffffffffu) st[k] = st[k + 1];
     st[0] = 0;
-    uint32_t widest = 0;
-    for (uint32_t k = 0; k < nw; ++k) widest = std::max(widest, st[k + 1] - st[k]);
-    if (widest > kMaxWorldBodies) return;
+    uint32_t widest = 0, widest_block = 0, n_cluster = 0;
+    for (uint32_t k = 0; k < nw; ++k) {
+        const uint32_t wk = st[k + 1] - st[k];
+        widest = std::max(widest, wk);
+        if (wk > kMaxWorldBodies) ++n_cluster;
+        else widest_block = std::max(widest_block, wk);
+    }
+    const uint32_t ctas = (uint32_t)w->solver.cluster_ctas;
+    if (n_cluster > 0 && (ctas == 0 || widest > (ctas << kClusterShiftMax))) return;
+    uint32_t shift = 0;
+    while (n_cluster > 0 && (ctas << shift) < widest) ++shift;
     std::vector<uint32_t> order(nw);
     for (uint32_t k = 0; k < nw; ++k) order[k] = k;
     std::stable_sort(order.begin(), order.end(),
@@ -312,9 +323,14 @@ static void compute_layout(npgpu_world* w) {
     st.insert(st.end(), order.begin(), order.end());
     w->world_start.swap(st);
     w->n_worlds = nw;
-    w->max_world_bodies = widest;
+    w->max_world_bodies = widest_block;
+    w->n_cluster_worlds = n_cluster;
+    w->cluster_shift = shift;
     w->n_big_worlds = 0;
-    for (uint32_t k = 0; k < nw; ++k) w->n_big_worlds += (w->world_start[k + 1] - w->world_start[k] > kWarpWorldBodies) ? 1u : 0u;
+    for (uint32_t k = 0; k < nw; ++k) {
+        const uint32_t wk = w->world_start[k + 1] - w->world_start[k];
+        w->n_big_worlds += (wk > kWarpWorldBodies && wk <= kMaxWorldBodies) ? 1u : 0u;
+    }
     w->layout_ok = true;
 }
 
@@ -326,7 +342,12 @@ static npgpu_status prepare_schedule(npgpu_world* w) {
         w->layout_on_device = false;
     }
     const uint32_t sched = w->params.solver_schedule;
-    w->solver.batched = w->layout_ok && sched != NPGPU_SCHEDULE_GRID && !w->params.solve_to_tolerance;
+    // The automatic choice keeps one grid for a single world and for batches
+    // with cluster-sized worlds; the per-world schedule is theirs on request
+    // (npgpu_autotune times it).
+    const bool eligible = sched == NPGPU_SCHEDULE_WORLDS ||
+                          (sched == NPGPU_SCHEDULE_AUTO && w->n_worlds >= 2 && w->n_cluster_worlds == 0);
+    w->solver.batched = w->layout_ok && eligible && !w->params.solve_to_tolerance;
     if (!w->solver.batched) return NPGPU_OK;
     Solver& s = w->dw.s;
     const size_t nbk = (size_t)w->n_worlds * kMaxColours;
@@ -366,12 +387,14 @@ static npgpu_status prepare_schedule(npgpu_world* w) {
     const uint32_t wt = w->params.world_threads;
     const int threads = (wt == 64 || wt == 256) ? (int)wt : 128;
     if (threads != w->solver.world_threads) {
-        w->grid_world = world_grid(w->device, w->max_world_bodies, w->n_worlds, threads);
+        w->grid_world = world_grid(w->device, w->max_world_bodies, w->n_worlds - w->n_cluster_worlds, threads);
         w->solver.world_threads = threads;
     }
     w->solver.n_worlds = w->n_worlds;
     w->solver.max_world_bodies = w->max_world_bodies;
     w->solver.n_big = w->n_big_worlds;
+    w->solver.n_cluster = w->n_cluster_worlds;
+    w->solver.cluster_shift = w->cluster_shift;
     w->solver.grid_world = w->grid_world;
     return NPGPU_OK;
 }
@@ -435,6 +458,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     Solver& s = w->dw.s;
     A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_prank, P); A(s.sm_rk, P); A(s.sm_b1, P); A(s.sm_b2, P);
     A(s.sm_nc, P); A(s.con, (size_t)P * kMaxContacts * 4); A(s.lam, (size_t)P * kMaxContacts); A(s.sm_mask, P); A(s.pos_rec, (size_t)P * kPosRec); A(s.adj, 2 * (size_t)P); A(s.wm_order, P);
+    A(s.perm, 5 * (size_t)P);
     A(w->ctl, 1);
     A(w->d_forget, Cn);
 #undef A
@@ -913,6 +937,9 @@ static std::vector<uint8_t> graph_key(const npgpu_world* w, const StepParams& sp
     put(&L.n_worlds, sizeof(L.n_worlds));
     put(&L.max_world_bodies, sizeof(L.max_world_bodies));
     put(&L.n_big, sizeof(L.n_big));
+    put(&L.n_cluster, sizeof(L.n_cluster));
+    put(&L.cluster_ctas, sizeof(L.cluster_ctas));
+    put(&L.cluster_shift, sizeof(L.cluster_shift));
     put(&w->sort_temp, sizeof(w->sort_temp));
     put(&w->sort_bytes, sizeof(w->sort_bytes));
     return k;
@@ -1058,8 +1085,12 @@ npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32
     std::vector<Cand> cands;
     if (2ull * nsolver <= grid_task_capacity(w->solver)) cands.push_back({NPGPU_SCHEDULE_GRID, 0});
     if (w->layout_dirty) compute_layout(w), w->layout_on_device = false;
-    if (w->layout_ok && !w->params.solve_to_tolerance)
-        for (uint32_t t : {64u, 128u, 256u}) cands.push_back({NPGPU_SCHEDULE_WORLDS, t});
+    if (w->layout_ok && !w->params.solve_to_tolerance) {
+        // The block size only shapes the block and warp worlds' kernel.
+        if (w->n_cluster_worlds == w->n_worlds) cands.push_back({NPGPU_SCHEDULE_WORLDS, 128u});
+        else
+            for (uint32_t t : {64u, 128u, 256u}) cands.push_back({NPGPU_SCHEDULE_WORLDS, t});
+    }
     if (cands.empty()) cands.push_back({w->params.solver_schedule, w->params.world_threads});
     const npgpu_params saved = w->params;
     cudaEvent_t e0 = nullptr, e1 = nullptr;

@@ -127,6 +127,10 @@ struct Solver {
     // other in one allocation, cleared by one memset each step.
     uint32_t *bucket_count, *bucket_start, *bucket_cursor;
     uint32_t *wm_order;              // solver manifolds ordered by (world, colour)
+    // The per-world schedule renumbers the solver manifolds in that order
+    // before assembly (through `perm`, 5 arrays of scratch), so each colour
+    // of a world is one run of manifold indices.
+    uint32_t *perm;
     // Learned warm start: per-contact features while recording (null otherwise)
     // and the sample buffer they are appended to after the solve.
     float *feat;
@@ -211,9 +215,17 @@ struct SolverLaunch {
     int grid_world;                  // blocks of the per-world kernels
     int world_threads;               // threads per world block of the velocity kernel: 64, 128 or 256
     int grid_world_position;         // blocks of the per-world position kernel (128 threads each)
+    // Worlds wider than kMaxWorldBodies: one thread-block cluster each, first in the world order.
+    uint32_t n_cluster;
+    int cluster_ctas;                // blocks per cluster (16 where the part allows, else 8)
+    uint32_t cluster_shift;          // 2^shift body rows per block
 };
 constexpr uint32_t kWarpWorldBodies = 256;    // widest world a single warp solves
 constexpr uint32_t kMaxWorldBodies = 4096;    // per-world shared-memory Δv limit (96 KiB)
+constexpr int kClusterThreads = 512;          // threads per block of the cluster kernels
+constexpr uint32_t kClusterShiftMax = 13;     // at most 8192 body rows (192 KiB) per cluster block
+// Blocks per cluster of the cluster kernels on this device (0: clusters unavailable).
+int cluster_ctas(int device);
 cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunch& L, cudaStream_t st);
 void solver_grid_sizes(int device, SolverLaunch& L);
 // Blocks of the per-world kernels: resident blocks at this shared-memory size,

@@ -45,6 +45,20 @@ def test_worlds_schedule_equals_grid_schedule(gpu_lib, hi):
     assert abs(ca["residual"] - cb["residual"]) <= 1e-12 + 1e-9 * abs(ca["residual"])
 
 
+def test_cluster_worlds_mixed_with_block_worlds(gpu_lib):
+    # Worlds wider than 4096 body slots are solved by a thread-block cluster
+    # (Δv in distributed shared memory), the others by a block or a warp, in
+    # the same step; the bits are the one grid's.
+    sc = scenes.batched_worlds(n_worlds=5, seed=3, lo=200, hi=9000)
+    widths = np.bincount(sc.bodies["world"])
+    assert (widths > 4097).any() and (widths <= 4097).any()
+    a = run(sc, abi.SCHEDULE_GRID, 30)
+    b = run(sc, abi.SCHEDULE_WORLDS, 30)
+    ba, bb = a.bodies(), b.bodies()
+    np.testing.assert_array_equal(ba["position"], bb["position"])
+    np.testing.assert_array_equal(ba["velocity"], bb["velocity"])
+
+
 def test_worlds_schedule_matches_oracle(gpu_lib):
     sc = small_batch(n_worlds=6, seed=3)
     g = run(sc, abi.SCHEDULE_WORLDS, 25)

@@ -1,7 +1,8 @@
 """Parity at the benchmark's own sizes.
 
-The 32^3 ball pile (C2) is stepped on the GPU and by the oracle in the colour
-order, and the two agree bit for bit, pair set included. A batch of a few
+The 32^3 ball pile (C2) is stepped on the GPU, under both solver schedules,
+and by the oracle in the colour order, and they agree bit for bit, pair set
+included. A batch of a few
 hundred worlds of the batched-worlds scene (C4's recipe) gives the same bits
 under the one-grid and the per-world schedules."""
 import numpy as np
@@ -14,18 +15,25 @@ pytestmark = pytest.mark.gpu
 
 
 def test_ball_pile_32k_matches_oracle(gpu_lib):
+    # Both schedules: the one cooperative grid, and the per-world schedule,
+    # where the pile is one world solved by a thread-block cluster.
     from nphysics_gb300.world import GpuWorld
     sc = scenes.ball_pile(side=32)
-    g = GpuWorld.for_scene(sc)
     o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_COLOUR)
     o.load_scene(sc)
-    g.step(100)
     o.step(100)
-    assert g.counters()["num_contacts"] > 30000      # most of the pile has landed
-    np.testing.assert_array_equal(g.pairs(), o.pairs())
-    gb, ob = g.bodies(), o.bodies()
-    np.testing.assert_array_equal(gb["position"], ob["position"])
-    np.testing.assert_array_equal(gb["velocity"], ob["velocity"])
+    ob = o.bodies()
+    for sched in (abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS):
+        p = sc.params()
+        p.solver_schedule = sched
+        g = GpuWorld.for_scene(sc, p)
+        g.step(100)
+        assert g.counters()["num_contacts"] > 30000      # most of the pile has landed
+        np.testing.assert_array_equal(g.pairs(), o.pairs())
+        gb = g.bodies()
+        np.testing.assert_array_equal(gb["position"], ob["position"])
+        np.testing.assert_array_equal(gb["velocity"], ob["velocity"])
+        del g
 
 
 def test_batched_worlds_schedules_agree_at_scale(gpu_lib):
