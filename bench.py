@@ -34,15 +34,21 @@ sys.path.insert(0, ROOT)
 METRIC = "body-steps/s"
 L2_FLUSH_BYTES = 256 << 20
 PROFILE_STEPS = 10
-# Kernels of one step of this workload (ours and CUB's radix sort and scans),
-# counted from the ncu launch list of this command (profiles/launches_ball_pile_32k.md).
+# Kernels of this library launched per step (CUB's radix sort and scans not
+# counted), from the ncu launch list of this workload.
 LAUNCHES_PER_STEP = 21
-# The batched-worlds schedule: the two cooperative solver kernels become five
-# per-world kernels (bucket count and scatter, velocity, residual, position).
-LAUNCHES_PER_STEP_BATCHED = 24
+# The per-world schedule: the two cooperative solver kernels become seven
+# per-world kernels (bucket count and scatter, the two renumbering passes,
+# velocity, residual, position), from the launch list of the batched workload.
+LAUNCHES_PER_STEP_BATCHED = 26
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_velocity launch on this
-# workload, from one ncu capture (profiles/k_velocity_ball_pile_32k.md).
-VELOCITY_TRAFFIC_PER_LAUNCH = 16809728
+# workload, from one ncu capture.
+VELOCITY_TRAFFIC_PER_LAUNCH = 16875776
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_world_velocity launch
+# on a 1024-world batch (1 046 697 solver contacts), per solver contact: the
+# batched line scales it by its own solver contacts (the traffic of the
+# per-world kernel grows with the contacts it sweeps).
+WORLD_VELOCITY_TRAFFIC_PER_CONTACT = 218672384 / 1046697
 
 
 def pinned(a):
@@ -373,7 +379,8 @@ def run_gpu(args):
         "config": {"workload": f"{workload}; timed steps "
                                f"{first_timed}..{first_timed + args.steps - 1} of the run",
                    "l2": "flushed (256 MiB write) between timed steps",
-                   "solver_schedule": {1: "one cooperative grid", 2: "one block per world"}[tuned[0]],
+                   "solver_schedule": {1: "one cooperative grid",
+                                       2: "per world: a cluster, a block or a warp each"}[tuned[0]],
                    "world_threads": tuned[1],
                    "parallelism": ("replicas" if args.workload in ("pile", "pyramid")
                                    else f"worlds sharded over {world_size} GPUs"),
@@ -383,7 +390,9 @@ def run_gpu(args):
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": "k_velocity" if tuned[0] == 1 else "k_world_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
-                     "traffic": VELOCITY_TRAFFIC_PER_LAUNCH if args.workload == "pile" else None,
+                     "traffic": (VELOCITY_TRAFFIC_PER_LAUNCH if args.workload == "pile" and tuned[0] == 1
+                                 else int(WORLD_VELOCITY_TRAFFIC_PER_CONTACT * K)
+                                 if args.workload == "batched" and tuned[0] == 2 else None),
                      "peak_source": peak_kind,
                      "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
         "clocks": {"sm_mhz": cl["sm_mhz"], "sm_max_mhz": cl["sm_max_mhz"], "reasons": cl["reasons"]},
