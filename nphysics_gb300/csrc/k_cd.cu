@@ -325,17 +325,22 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
     float prediction = (m1 + c.lin_pred[c1]) + (m2 + c.lin_pred[c2]);
     CandList out;
     out.n = 0;
+    int keep[kMaxContacts] = {0, 1, 2, 3};
+    int nk;
     if (a.shape == SHAPE_BALL && b.shape == SHAPE_BALL) {
         np::V v = np::sub(b.pose.t, a.pose.t);
         float l2 = np::dot(v, v);
         np::V n0 = l2 > 0.0f ? np::divs(v, sqrtf(l2)) : np::mk(1.0f, 0.0f, 0.0f);
         push_eval(out, a, b, 0, 0, n0, prediction);
+        nk = out.n;
     } else if (a.shape == SHAPE_CUBOID && b.shape == SHAPE_BALL) {
         ball_box(b, a, true, prediction, out);
+        nk = out.n;
     } else if (a.shape == SHAPE_BALL && b.shape == SHAPE_CUBOID) {
         ball_box(a, b, false, prediction, out);
+        nk = out.n;
     } else {
-        box_box(a, b, prediction, out);
+        nk = box_box(a, b, prediction, out, keep);
     }
     // Previous manifold of this pair: among the pairs its owner wrote last pass.
     uint32_t owner = owns(c, c1, c2) ? c1 : c2;
@@ -355,10 +360,10 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
         for (int k = 0; k < pn; ++k) pkeys[k] = w.prev.key[prev * kMaxContacts + k];
     }
     np::Q bq = q4(w.b.pos_q[c.body[c1]]);
-    int nc = out.n > kMaxContacts ? kMaxContacts : out.n;
+    int nc = nk > kMaxContacts ? kMaxContacts : nk;
     double maxpen = -1e300;
     for (int k = 0; k < nc; ++k) {
-        const Cand& cd = out.c[k];
+        const Cand& cd = out.c[keep[k]];
         uint32_t key = uint32_t(cd.f1 * 26 + cd.f2);
         float4 imp = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         for (int j = 0; j < pn; ++j)

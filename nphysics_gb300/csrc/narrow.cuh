@@ -176,16 +176,21 @@ struct Cand {
     Geom g;
 };
 
-struct CandList {
-    Cand c[8];
+// Candidate contacts: up to 8 from a clipped polygon, of which a manifold
+// keeps at most 4.
+template <int N>
+struct CandListN {
+    Cand c[N];
     int n;
 };
+using CandList = CandListN<8>;
 
-__device__ __forceinline__ void push_eval(CandList& out, const Shape& s1, const Shape& s2, int f1, int f2, np::V n0,
+template <int N>
+__device__ __forceinline__ void push_eval(CandListN<N>& out, const Shape& s1, const Shape& s2, int f1, int f2, np::V n0,
                                           float prediction) {
     Geom g = kinematic_contact(feature_of(s1.shape, s1.h, f1), s1.pose, s1.dil(), feature_of(s2.shape, s2.h, f2),
                                s2.pose, s2.dil(), n0);
-    if (g.depth >= -prediction && out.n < 8) {
+    if (g.depth >= -prediction && out.n < N) {
         out.c[out.n].f1 = f1;
         out.c[out.n].f2 = f2;
         out.c[out.n].g = g;
@@ -250,14 +255,25 @@ __device__ __forceinline__ void ball_box(const Shape& sb, const Shape& sx, bool 
     else push_eval(out, sb, sx, 0, fid, np::neg(n), prediction);
 }
 
+// A vertex of the clipped polygon and where it comes from, packed in one
+// word: tag (2 bits: incident vertex, edge crossing, reference corner), a and
+// b (feature ids, -1 allowed) and esrc (the incident edge it lies on, or
+// -(1 + clipping plane)).
 struct PV {
     np::V p;
-    int tag, a, b, esrc;
+    uint32_t bits;
+    __device__ __forceinline__ int tag() const { return (int)(bits & 3u); }
+    __device__ __forceinline__ int a() const { return (int)((bits >> 2) & 63u) - 1; }
+    __device__ __forceinline__ int b() const { return (int)((bits >> 8) & 63u) - 1; }
+    __device__ __forceinline__ int esrc() const { return (int)((bits >> 14) & 63u) - 8; }
+    __device__ __forceinline__ void set(int tag, int a, int b, int esrc) {
+        bits = (uint32_t)tag | ((uint32_t)(a + 1) << 2) | ((uint32_t)(b + 1) << 8) | ((uint32_t)(esrc + 8) << 14);
+    }
 };
 
 // Keeps at most 4 candidates (deepest, farthest, largest triangle, largest
 // growth), in their original order. Writes the kept indices to keep[].
-__device__ __forceinline__ int reduce4(const CandList& c, int keep[4]) {
+__device__ __forceinline__ int reduce4(const CandListN<8>& c, int keep[4]) {
     int n = c.n;
     if (n <= 4) {
         for (int k = 0; k < n; ++k) keep[k] = k;
@@ -308,12 +324,18 @@ __device__ __forceinline__ int reduce4(const CandList& c, int keep[4]) {
     return m;
 }
 
+// ax[k] for a k known only at run time, by selects (keeps ax in registers).
+__device__ __forceinline__ np::V pick3(const np::V ax[3], int k) { return k == 0 ? ax[0] : (k == 1 ? ax[1] : ax[2]); }
+
 __device__ __forceinline__ float box_radius_along(const np::V ax[3], np::V h, np::V L) {
     return h.x * fabsf(np::dot(ax[0], L)) + h.y * fabsf(np::dot(ax[1], L)) + h.z * fabsf(np::dot(ax[2], L));
 }
 
 // Cuboid A (collider 1) against cuboid B (collider 2).
-static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, float prediction, CandList& out) {
+// The candidates go to `out`; keep[0..return) are the indices the manifold
+// keeps, in increasing order.
+static __device__ __noinline__ int box_box(const Shape& A, const Shape& B, float prediction, CandList& out,
+                                           int keep[kMaxContacts]) {
     np::M RA = np::qmat(A.pose.q), RB = np::qmat(B.pose.q);
     np::V axA[3] = {np::mcol(RA, 0), np::mcol(RA, 1), np::mcol(RA, 2)};
     np::V axB[3] = {np::mcol(RB, 0), np::mcol(RB, 1), np::mcol(RB, 2)};
@@ -325,7 +347,7 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
         np::V L = axA[i];
         float rb = box_radius_along(axB, B.h, L);
         float sep = fabsf(np::dot(d, L)) - (np::comp(A.h, i) + rb);
-        if (sep > prediction) return;
+        if (sep > prediction) return 0;
         if (sep > sepA) {
             sepA = sep;
             ia = i;
@@ -335,7 +357,7 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
         np::V L = axB[j];
         float ra = box_radius_along(axA, A.h, L);
         float sep = fabsf(np::dot(d, L)) - (ra + np::comp(B.h, j));
-        if (sep > prediction) return;
+        if (sep > prediction) return 0;
         if (sep > sepB) {
             sepB = sep;
             ib = j;
@@ -350,7 +372,7 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
             float ra = box_radius_along(axA, A.h, L);
             float rb = box_radius_along(axB, B.h, L);
             float sep = fabsf(np::dot(d, L)) - (ra + rb);
-            if (sep > prediction) return;
+            if (sep > prediction) return 0;
             if (sep > sepE) {
                 sepE = sep;
                 ea = i;
@@ -366,20 +388,22 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
         if (np::dot(d, L) < 0.0f) L = np::neg(L);
         int o1, o2;
         edge_other_axes(ea, o1, o2);
-        int fa = box_edge_id(ea, np::dot(axA[o1], L) > 0.0f ? 1 : 0, np::dot(axA[o2], L) > 0.0f ? 1 : 0);
+        int fa = box_edge_id(ea, np::dot(pick3(axA, o1), L) > 0.0f ? 1 : 0, np::dot(pick3(axA, o2), L) > 0.0f ? 1 : 0);
         edge_other_axes(eb, o1, o2);
-        int fb = box_edge_id(eb, np::dot(axB[o1], L) < 0.0f ? 1 : 0, np::dot(axB[o2], L) < 0.0f ? 1 : 0);
+        int fb = box_edge_id(eb, np::dot(pick3(axB, o1), L) < 0.0f ? 1 : 0, np::dot(pick3(axB, o2), L) < 0.0f ? 1 : 0);
         push_eval(out, A, B, fa, fb, L, prediction);
-        return;
+        keep[0] = 0;
+        return out.n;
     }
     const Shape& Rf = refA ? A : B;
     const Shape& In = refA ? B : A;
-    const np::V* axR = refA ? axA : axB;
-    const np::V* axI = refA ? axB : axA;
+    const np::V axR[3] = {refA ? axA[0] : axB[0], refA ? axA[1] : axB[1], refA ? axA[2] : axB[2]};
+    const np::V axI[3] = {refA ? axB[0] : axA[0], refA ? axB[1] : axA[1], refA ? axB[2] : axA[2]};
     int ri = refA ? ia : ib;
     np::V dRI = refA ? d : np::neg(d);
-    int rpos = np::dot(dRI, axR[ri]) >= 0.0f ? 1 : 0;
-    np::V nref = rpos ? axR[ri] : np::neg(axR[ri]);
+    const np::V axr = pick3(axR, ri);
+    int rpos = np::dot(dRI, axr) >= 0.0f ? 1 : 0;
+    np::V nref = rpos ? axr : np::neg(axr);
     int ik = 0;
     float best = fabsf(np::dot(axI[0], nref));
     for (int k = 1; k < 3; ++k) {
@@ -389,7 +413,7 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
             ik = k;
         }
     }
-    int ipos = np::dot(axI[ik], nref) < 0.0f ? 1 : 0;
+    int ipos = np::dot(pick3(axI, ik), nref) < 0.0f ? 1 : 0;
     int ref_face = box_face_id(ri, rpos), inc_face = box_face_id(ik, ipos);
     int u = (ik + 1) % 3, v = (ik + 2) % 3;
     const int su[4] = {0, 1, 1, 0}, sv[4] = {0, 0, 1, 1};
@@ -411,10 +435,7 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
         Approx ap = box_feature(In.h, a);
         np::V w = np::iso_pt(In.pose, ap.a);
         poly[np_].p = np::iso_inv_pt(Rf.pose, w);
-        poly[np_].tag = 0;
-        poly[np_].a = a;
-        poly[np_].b = -1;
-        poly[np_].esrc = eid;
+        poly[np_].set(0, a, -1, eid);
         ++np_;
     }
     int ru = (ri + 1) % 3, rv = (ri + 2) % 3;
@@ -439,20 +460,17 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
                 int s[3];
                 s[ri] = rpos;
                 s[ax] = pp;
-                if (P.esrc >= 0) {
+                const int pe = P.esrc();
+                const int xe = pin ? -(1 + pl) : pe;
+                if (pe >= 0) {
                     int o1, o2;
                     edge_other_axes(third, o1, o2);
-                    X.tag = 1;
-                    X.a = box_edge_id(third, s[o1], s[o2]);
-                    X.b = P.esrc;
+                    X.set(1, box_edge_id(third, s[o1], s[o2]), pe, xe);
                 } else {
-                    int other_plane = -P.esrc - 1;
+                    int other_plane = -pe - 1;
                     s[planes_axis[other_plane]] = planes_pos[other_plane];
-                    X.tag = 2;
-                    X.a = box_vertex_id(s[0], s[1], s[2]);
-                    X.b = -1;
+                    X.set(2, box_vertex_id(s[0], s[1], s[2]), -1, xe);
                 }
-                X.esrc = pin ? -(1 + pl) : P.esrc;
                 if (nn < 8) next[nn++] = X;
             }
         }
@@ -460,27 +478,24 @@ static __device__ __noinline__ void box_box(const Shape& A, const Shape& B, floa
         np_ = nn;
     }
     np::V n0 = refA ? nref : np::neg(nref);
-    CandList cands;
-    cands.n = 0;
+    CandList& cands = out;
     for (int k = 0; k < np_; ++k) {
         const PV& P = poly[k];
         int fr, fi;
-        if (P.tag == 0) {
+        if (P.tag() == 0) {
             fr = ref_face;
-            fi = P.a;
-        } else if (P.tag == 1) {
-            fr = P.a;
-            fi = P.b;
+            fi = P.a();
+        } else if (P.tag() == 1) {
+            fr = P.a();
+            fi = P.b();
         } else {
-            fr = P.a;
+            fr = P.a();
             fi = inc_face;
         }
         if (refA) push_eval(cands, A, B, fr, fi, n0, prediction);
         else push_eval(cands, A, B, fi, fr, n0, prediction);
     }
-    int keep[4];
-    int m = reduce4(cands, keep);
-    for (int k = 0; k < m; ++k) out.c[out.n++] = cands.c[keep[k]];
+    return reduce4(cands, keep);
 }
 
 }  // namespace npgpu_dev
