@@ -786,6 +786,8 @@ __global__ void k_assemble(World w, StepParams p) {
             if (depth < 0.0f) rhs = rhs + (-depth) * p.inv_dt;
             np::V t[2];
             tangent_basis(n, t[0], t[1]);
+            w.s.tan[((size_t)m * kMaxContacts + k) * 2] = make_float4(t[0].x, t[0].y, t[0].z, 0.0f);
+            w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1] = make_float4(t[1].x, t[1].y, t[1].z, 0.0f);
             for (int sdir = 0; sdir < 2; ++sdir) make_row(rt[sdir], v1, v2, center1, center2, t[sdir], dt);
             np::V pos1 = np::sub(center1, v1.com), pos2 = np::sub(center2, v2.com);
             con[4 * k] = make_float4(n.x, n.y, n.z, mu);
@@ -857,9 +859,12 @@ __device__ __forceinline__ float local_residual(const ContactRec& c, const np::V
 struct GlobalContacts {
     const float4* con;
     float4* lam;
+    const float4* tan;               // the friction directions assembly stored
     __device__ __forceinline__ ContactRec rec(uint32_t k) const { return load_con(con, k); }
-    __device__ __forceinline__ void tangents(const ContactRec& c, uint32_t, np::V* t) const {
-        tangent_basis(c.n, t[0], t[1]);
+    __device__ __forceinline__ void tangents(const ContactRec&, uint32_t k, np::V* t) const {
+        const float4 a = __ldg(tan + 2 * k), b = __ldg(tan + 2 * k + 1);
+        t[0] = np::mk(a.x, a.y, a.z);
+        t[1] = np::mk(b.x, b.y, b.z);
     }
     __device__ __forceinline__ float4 get_lam(uint32_t k) const { return lam[k]; }
     __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { lam[k] = v; }
@@ -1019,7 +1024,8 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     BodyMasses bm;
     if (g1 >= 0) bm.s[0] = load_sb(w.b.sb, g1);
     if (g2 >= 0) bm.s[1] = load_sb(w.b.sb, g2);
-    GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
+    GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts,
+                       w.s.tan + (size_t)m * kMaxContacts * 2};
     DV dv;
     dva.load(g1 >= 0 ? l1 : -1, dv.a);
     dva.load(g2 >= 0 ? l2 : -1, dv.b);
@@ -1038,12 +1044,9 @@ __device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t 
     }
     const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
     for (uint32_t k = 0; k < nc; ++k) {
-        ContactRec c = load_con(con, k);
         for (int e = 0; e < 4; ++e) cc.at(6 + 7 * k + e) = con[4 * k + e];
-        np::V t[2];
-        tangent_basis(c.n, t[0], t[1]);
-        cc.at(10 + 7 * k) = make_float4(t[0].x, t[0].y, t[0].z, 0.0f);
-        cc.at(11 + 7 * k) = make_float4(t[1].x, t[1].y, t[1].z, 0.0f);
+        cc.at(10 + 7 * k) = w.s.tan[((size_t)m * kMaxContacts + k) * 2];
+        cc.at(11 + 7 * k) = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
         cc.at(12 + 7 * k) = w.s.lam[(size_t)m * kMaxContacts + k];
     }
 }
@@ -1059,8 +1062,8 @@ __device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, in
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = load_con(con, k);
         float4 l = lam[k];
-        np::V t[2];
-        tangent_basis(c.n, t[0], t[1]);
+        const float4 ta = w.s.tan[((size_t)m * kMaxContacts + k) * 2], tb = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
+        const np::V t[2] = {np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
         residual_row(np::neg(c.n), c.pos1, c.pos2, mask, c.r[0], c.rhs[0], l.x, dv, h1, h2, false, 0.0, c.mu, s2, l2);
         residual_row(t[0], c.pos1, c.pos2, mask, c.r[1], c.rhs[1], l.y, dv, h1, h2, true, (double)l.x, c.mu, s2, l2);
         residual_row(t[1], c.pos1, c.pos2, mask, c.r[2], c.rhs[2], l.z, dv, h1, h2, true, (double)l.x, c.mu, s2, l2);
@@ -1142,7 +1145,8 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
                 BodyMasses bm;
                 if (b1 >= 0) bm.s[0] = load_sb(w.b.sb, b1);
                 if (b2 >= 0) bm.s[1] = load_sb(w.b.sb, b2);
-                GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts};
+                GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts,
+                                   w.s.tan + (size_t)m * kMaxContacts * 2};
                 velocity_task_src<SWEEP_ANY>(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv, w.ctl);
             }
             publish_dvf(w.b.dvf, b1, t1 + 1u, dv.a);

@@ -117,6 +117,7 @@ struct Solver {
     uint32_t *sm_nc;
     float4 *con;                     // 4 contacts x 4 float4 per solver manifold (constant during the solve)
     float4 *lam;                     // 4 contacts per solver manifold: impulses (normal, tangent 1, tangent 2)
+    float4 *tan;                     // 4 contacts x 2 per solver manifold: the friction directions (xyz)
     uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13)
     float4 *pos_rec;                 // kPosRec per solver manifold: what the position solver reads besides poses
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
