@@ -22,12 +22,17 @@ namespace npgpu_dev {
 constexpr int kThreads = 256;
 static inline unsigned nblocks(uint32_t n) { return (n + kThreads - 1) / kThreads; }
 
-// Sort keys: dead bit | world index | 30-bit Morton code of the fat-AABB
-// centre on a 1 m grid (10 bits per axis, +-512 m; farther centres clamp to the
-// edge cells, which only affects the tree's shape, never the pairs). The
-// dead bit sits just above the highest world bit in use, so that the radix
-// sort only looks at 31 + world-bit bits.
+// Sort keys: dead bit | world index | static bit | 30-bit Morton code of the
+// fat-AABB centre on a 1 m grid (10 bits per axis, +-512 m; farther centres
+// clamp to the edge cells, which only affects the tree's shape, never the
+// pairs). The static bit puts a world's colliders of static bodies after its
+// moving ones, so the tree splits each world into a moving and a static
+// subtree at its top: a query reaches a large static collider (a ground)
+// through one node instead of down the long path its box spans in a mixed
+// tree. The dead bit sits just above the highest world bit in use, so that
+// the radix sort only looks at 32 + world-bit bits.
 constexpr int kMortonBits = 30;
+constexpr int kWorldShift = kMortonBits + 1;
 __device__ __forceinline__ uint64_t expand10(uint32_t v) {
     uint64_t x = v & 0x3ffu;
     x = (x | (x << 16)) & 0x30000ffull;
@@ -41,7 +46,7 @@ __device__ __forceinline__ uint32_t quantize(float c) {
     q = q < 0.0f ? 0.0f : (q > 1023.0f ? 1023.0f : q);
     return (uint32_t)q;
 }
-__device__ __forceinline__ uint32_t key_world(unsigned long long k) { return (uint32_t)(k >> kMortonBits) & 0xffffu; }
+__device__ __forceinline__ uint32_t key_world(unsigned long long k) { return (uint32_t)(k >> kWorldShift) & 0xffffu; }
 
 __device__ __forceinline__ Shape load_shape(const Colliders& c, uint32_t i) {
     Shape s;
@@ -62,7 +67,7 @@ __global__ void k_sync_aabb(World w, float bp_margin, int world_bits) {
     if (i >= w.nc_slots) return;
     const Colliders& c = w.c;
     if (!(c.info[i] & CI_ALIVE)) {
-        c.keys[i] = 1ull << (kMortonBits + world_bits);
+        c.keys[i] = 1ull << (kWorldShift + world_bits);
         c.vals[i] = i;
         return;
     }
@@ -102,7 +107,8 @@ __global__ void k_sync_aabb(World w, float bp_margin, int world_bits) {
     float cx = 0.5f * (fmn.x + fmx.x), cy = 0.5f * (fmn.y + fmx.y), cz = 0.5f * (fmn.z + fmx.z);
     uint64_t morton = expand10(quantize(cx)) | (expand10(quantize(cy)) << 1) | (expand10(quantize(cz)) << 2);
     uint64_t world = w.b.world[bi] & 0xffffu;
-    c.keys[i] = (world << kMortonBits) | morton;
+    uint64_t stat = bi_status(w.b.info[bi]) == 1u ? 1ull : 0ull;   // NPGPU_BODY_STATIC
+    c.keys[i] = (world << kWorldShift) | (stat << kMortonBits) | morton;
     c.vals[i] = i;
 }
 
@@ -444,7 +450,7 @@ cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t s
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st) {
     if (w.nc_slots == 0) return cudaSuccess;
     return cub::DeviceRadixSort::SortPairs(temp, temp_bytes, w.c.keys, w.c.keys_sorted, w.c.vals, w.c.vals_sorted,
-                                           (int)w.nc_slots, 0, kMortonBits + w.world_bits + 1, st);
+                                           (int)w.nc_slots, 0, kWorldShift + w.world_bits + 1, st);
 }
 
 cudaError_t launch_lbvh(const World& w, cudaStream_t st) {
