@@ -151,6 +151,15 @@ __global__ void k_lbvh_build(World w, int n) {
 
 __device__ __forceinline__ float4 ld_cg(const float4* p) { return __ldcg(p); }
 
+// Arrival count of a node: release orders this thread's writes of the child
+// before the count, acquire orders the second arrival's reads of the sibling
+// after it (one ordered atomic instead of a full fence and a plain atomic).
+__device__ __forceinline__ int arrive_acq_rel(int* p) {
+    int old;
+    asm volatile("atom.acq_rel.gpu.global.add.s32 %0, [%1], 1;" : "=r"(old) : "l"(p) : "memory");
+    return old;
+}
+
 // Bottom-up refit: the second child to arrive computes the parent.
 __global__ void k_lbvh_refit(World w, int n) {
     int k = blockIdx.x * blockDim.x + threadIdx.x;
@@ -162,23 +171,30 @@ __global__ void k_lbvh_refit(World w, int n) {
     // (bounding radius) of the subtree.
     float4 mn = w.c.aabb_min[ci], mx = w.c.aabb_max[ci];
     uint32_t wk = key_world(w.c.keys_sorted[k]);
-    w.c.node_min[node] = make_float4(mn.x, mn.y, mn.z, __uint_as_float(wk << 16 | wk));
-    w.c.node_max[node] = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
+    float4 c0 = make_float4(mn.x, mn.y, mn.z, __uint_as_float(wk << 16 | wk));
+    float4 c1 = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
+    w.c.node_min[node] = c0;
+    w.c.node_max[node] = c1;
     if (n == 1) return;
-    __threadfence();
     int p = w.c.parent[node];
     for (int guard = 0; p >= 0; ++guard) {
         if (guard > 256) {   // deeper than any tree over 64-bit keys plus 32-bit tie-breaks
             atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
             return;
         }
-        if (atomicAdd(&w.c.node_flag[p], 1) == 0) return;
+        if (arrive_acq_rel(&w.c.node_flag[p]) == 0) return;
+        // This thread holds its own child's box; only the sibling's is read.
         int l = w.c.left[p], r = w.c.right[p];
-        float4 a0 = ld_cg(&w.c.node_min[l]), a1 = ld_cg(&w.c.node_max[l]);
-        float4 b0 = ld_cg(&w.c.node_min[r]), b1 = ld_cg(&w.c.node_max[r]);
+        const bool from_left = l == node;
+        const int sib = from_left ? r : l;
+        const float4 s0 = ld_cg(&w.c.node_min[sib]), s1 = ld_cg(&w.c.node_max[sib]);
+        const float4 a0 = from_left ? c0 : s0, a1 = from_left ? c1 : s1;
+        const float4 b0 = from_left ? s0 : c0, b1 = from_left ? s1 : c1;
         uint32_t wr = (__float_as_uint(a0.w) & 0xffff0000u) | (__float_as_uint(b0.w) & 0xffffu);
-        w.c.node_min[p] = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), __uint_as_float(wr));
-        w.c.node_max[p] = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), fmaxf(a1.w, b1.w));
+        c0 = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), __uint_as_float(wr));
+        c1 = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), fmaxf(a1.w, b1.w));
+        w.c.node_min[p] = c0;
+        w.c.node_max[p] = c1;
         // The traversal's copy: both children's boxes and references in one
         // 80-byte record, a leaf child referenced by its collider (top bit set).
         float4* wd = w.c.wide + 5 * (size_t)p;
@@ -189,7 +205,7 @@ __global__ void k_lbvh_refit(World w, int n) {
         uint32_t lref = l >= n - 1 ? (0x80000000u | w.c.vals_sorted[l - (n - 1)]) : (uint32_t)l;
         uint32_t rref = r >= n - 1 ? (0x80000000u | w.c.vals_sorted[r - (n - 1)]) : (uint32_t)r;
         wd[4] = make_float4(__uint_as_float(lref), __uint_as_float(rref), 0.0f, 0.0f);
-        __threadfence();
+        node = p;
         p = w.c.parent[p];
     }
 }
