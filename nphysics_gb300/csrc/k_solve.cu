@@ -713,7 +713,9 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
 }
 
 // ================================================================ assembly
-__global__ void k_assemble(World w, StepParams p) {
+// `rows`: also store each contact's three rows in full, for the one-grid
+// schedule's iterations.
+__global__ void k_assemble(World w, StepParams p, bool rows) {
     const uint32_t ms = w.ctl->nsolver;
     const Bodies& b = w.b;
     const Colliders& c = w.c;
@@ -794,6 +796,20 @@ __global__ void k_assemble(World w, StepParams p) {
             con[4 * k + 1] = make_float4(pos1.x, pos1.y, pos1.z, rn[RF_R]);
             con[4 * k + 2] = make_float4(pos2.x, pos2.y, pos2.z, rhs);
             con[4 * k + 3] = make_float4(rt[0][RF_R], rt[0][RF_RHS], rt[1][RF_R], rt[1][RF_RHS]);
+            if (rows) {
+                // The three rows in full for the iterations (J and WJ as
+                // fill_constraint_geometry forms them, r, rhs, friction).
+                float4* ro = w.s.rows + ((size_t)m * kMaxContacts + k) * kRowsF4;
+                const float* src[3] = {rn, rt[0], rt[1]};
+                const float rhs3[3] = {rhs, rt[0][RF_RHS], rt[1][RF_RHS]};
+#pragma unroll
+                for (int r = 0; r < 3; ++r) {
+                    const float* R = src[r];
+#pragma unroll
+                    for (int q = 0; q < 6; ++q) ro[kRowF4 * r + q] = make_float4(R[4 * q], R[4 * q + 1], R[4 * q + 2], R[4 * q + 3]);
+                    ro[kRowF4 * r + 6] = make_float4(R[RF_R], rhs3[r], mu, 0.0f);
+                }
+            }
             const bool cold = p.warmstart_mode == 1u;
             lam[k] = make_float4(cold ? 0.0f : imp.x * p.warmstart_coeff, cold ? 0.0f : imp.y * p.warmstart_coeff,
                                  cold ? 0.0f : imp.z * p.warmstart_coeff, 0.0f);
@@ -870,42 +886,131 @@ struct GlobalContacts {
     __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { lam[k] = v; }
 };
 
-// Shared-memory cache of one task: 3 + 3 float4 of inverse mass, then per
-// contact its 4 record float4, the two tangents and the impulses.
-constexpr int kCacheContacts = 2;
-constexpr int kCacheF4 = 6 + 7 * kCacheContacts;
-struct CachedContacts {
+// A contact row as the iterations read it (stored in full at assembly).
+struct RowRec {
+    float J1[6], J2[6], W1[6], W2[6];
+    float r, rhs, mu;
+};
+__device__ __forceinline__ RowRec unpack_row(const float4* q) {
+    RowRec R;
+    const float4 q0 = q[0], q1 = q[1], q2 = q[2], q3 = q[3], q4 = q[4], q5 = q[5], q6 = q[6];
+    const float f[24] = {q0.x, q0.y, q0.z, q0.w, q1.x, q1.y, q1.z, q1.w, q2.x, q2.y, q2.z, q2.w,
+                         q3.x, q3.y, q3.z, q3.w, q4.x, q4.y, q4.z, q4.w, q5.x, q5.y, q5.z, q5.w};
+#pragma unroll
+    for (int k = 0; k < 6; ++k) {
+        R.J1[k] = f[RF_J1 + k];
+        R.J2[k] = f[RF_J2 + k];
+        R.W1[k] = f[RF_WJ1 + k];
+        R.W2[k] = f[RF_WJ2 + k];
+    }
+    R.r = q6.x;
+    R.rhs = q6.y;
+    R.mu = q6.z;
+    return R;
+}
+
+// J . dv and dv += a WJ of one row, in the order jdot / axpy use (side sums,
+// then their sum; side 1, then side 2), so stored and rebuilt rows give the
+// same bits.
+__device__ __forceinline__ float row_dot(const RowRec& R, const DV& dv, bool h1, bool h2) {
+    float s1 = 0.0f, s2 = 0.0f;
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s1 = s1 + R.J1[k] * dv.a[k];
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s2 = s2 + R.J2[k] * dv.b[k];
+    if (h1 && h2) return s1 + s2;
+    if (h1) return s1;
+    if (h2) return s2;
+    return 0.0f;
+}
+__device__ __forceinline__ void row_axpy(const RowRec& R, DV& dv, float a, bool h1, bool h2) {
+    if (h1) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dv.a[k] = a * R.W1[k] + dv.a[k];
+    }
+    if (h2) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) dv.b[k] = a * R.W2[k] + dv.b[k];
+    }
+}
+
+// Where the iterations read a task's rows and impulses: global memory, or
+// the running thread's slice of a shared-memory cache (element e at
+// base[e * blockDim.x], so that the lanes of a warp read consecutive float4):
+// the impulses, then the rows, of one contact.
+struct GlobalRows {
+    const float4* rows;
+    float4* lam;
+    __device__ __forceinline__ RowRec row(uint32_t k, int r) const {
+        const float4* q = rows + (size_t)k * kRowsF4 + r * kRowF4;
+        float4 v[kRowF4];
+#pragma unroll
+        for (int e = 0; e < kRowF4; ++e) v[e] = __ldg(q + e);
+        return unpack_row(v);
+    }
+    __device__ __forceinline__ float4 get_lam(uint32_t k) const { return lam[k]; }
+    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { lam[k] = v; }
+};
+constexpr int kCacheContacts = 1;
+constexpr int kCacheF4 = kCacheContacts * (1 + kRowsF4);
+struct CachedRows {
     float4* base;
     __device__ __forceinline__ float4& at(int e) const { return base[e * (int)blockDim.x]; }
-    __device__ __forceinline__ ContactRec rec(uint32_t k) const {
-        float4 c0 = at(6 + 7 * k), c1 = at(7 + 7 * k), c2 = at(8 + 7 * k), c3 = at(9 + 7 * k);
-        ContactRec c;
-        c.n = np::mk(c0.x, c0.y, c0.z);
-        c.mu = c0.w;
-        c.pos1 = np::mk(c1.x, c1.y, c1.z);
-        c.r[0] = c1.w;
-        c.pos2 = np::mk(c2.x, c2.y, c2.z);
-        c.rhs[0] = c2.w;
-        c.r[1] = c3.x; c.rhs[1] = c3.y; c.r[2] = c3.z; c.rhs[2] = c3.w;
-        return c;
+    __device__ __forceinline__ RowRec row(uint32_t k, int r) const {
+        float4 v[kRowF4];
+#pragma unroll
+        for (int e = 0; e < kRowF4; ++e) v[e] = at((int)k * (1 + kRowsF4) + 1 + r * kRowF4 + e);
+        return unpack_row(v);
     }
-    __device__ __forceinline__ void tangents(const ContactRec&, uint32_t k, np::V* t) const {
-        float4 a = at(10 + 7 * k), b = at(11 + 7 * k);
-        t[0] = np::mk(a.x, a.y, a.z);
-        t[1] = np::mk(b.x, b.y, b.z);
-    }
-    __device__ __forceinline__ float4 get_lam(uint32_t k) const { return at(12 + 7 * k); }
-    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { at(12 + 7 * k) = v; }
-    __device__ __forceinline__ SB get(int side) const {
-        SB s;
-        float4 a = at(3 * side), b = at(3 * side + 1), c = at(3 * side + 2);
-        s.I.m[0][0] = a.x; s.I.m[0][1] = a.y; s.I.m[0][2] = a.z;
-        s.I.m[1][0] = b.x; s.I.m[1][1] = b.y; s.I.m[1][2] = b.z;
-        s.I.m[2][0] = c.x; s.I.m[2][1] = c.y; s.I.m[2][2] = c.z;
-        s.im = a.w;
-        return s;
-    }
+    __device__ __forceinline__ float4 get_lam(uint32_t k) const { return at((int)k * (1 + kRowsF4)); }
+    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { at((int)k * (1 + kRowsF4)) = v; }
 };
+
+// The friction rows (sor_prox.rs:232-343) and the normal rows
+// (sor_prox.rs:181-230) of one task's contacts, from stored rows.
+template <class RS>
+__device__ __forceinline__ void friction_rows(const RS& src, uint32_t nc, bool h1, bool h2, DV& dv) {
+    for (uint32_t k = 0; k < nc; ++k) {
+        const float4 l = src.get_lam(k);
+        const float li = l.x;
+        float imps[2] = {l.y, l.z};
+#pragma unroll
+        for (int sdir = 0; sdir < 2; ++sdir) {
+            const float imp = imps[sdir];
+            if (li == 0.0f) {
+                if (imp != 0.0f) {
+                    row_axpy(src.row(k, 1 + sdir), dv, -imp, h1, h2);
+                    imps[sdir] = 0.0f;
+                }
+                continue;
+            }
+            const RowRec R = src.row(k, 1 + sdir);
+            float mx = R.mu * li, mn = -mx;
+            float dimp = row_dot(R, dv, h1, h2) + R.rhs;
+            float ni = imp - R.r * dimp;
+            if (ni < mn) ni = mn;
+            else if (ni > mx) ni = mx;
+            float dl = ni - imp;
+            imps[sdir] = ni;
+            row_axpy(R, dv, dl, h1, h2);
+        }
+        src.set_lam(k, make_float4(li, imps[0], imps[1], 0.0f));
+    }
+}
+template <class RS>
+__device__ __forceinline__ void normal_rows(const RS& src, uint32_t nc, bool h1, bool h2, DV& dv) {
+    for (uint32_t k = 0; k < nc; ++k) {
+        const float4 l = src.get_lam(k);
+        const RowRec R = src.row(k, 0);
+        float imp = l.x;
+        float dimp = row_dot(R, dv, h1, h2) + R.rhs;
+        float ni = imp - R.r * dimp;
+        ni = ni > 0.0f ? ni : 0.0f;
+        float dl = ni - imp;
+        src.set_lam(k, make_float4(ni, l.y, l.z, 0.0f));
+        row_axpy(R, dv, dl, h1, h2);
+    }
+}
 
 // One velocity task: sweep 0 is the warm start (sor_prox.rs:19-45), odd sweeps
 // the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
@@ -1018,6 +1123,26 @@ struct ClusterDv {
 
 // Velocity task of manifold m read from global memory; g1, g2 are the dynamic
 // bodies' slots (-1: no dofs), l1, l2 their Δv rows in `dva`.
+// The warm start of manifold m (sweep 0), from the compact records, the
+// stored friction directions and the bodies' inverse masses.
+__device__ __forceinline__ void warm_task(const World& w, uint32_t m, int g1, int g2, DV& dv) {
+    BodyMasses bm;
+    if (g1 >= 0) bm.s[0] = load_sb(w.b.sb, g1);
+    if (g2 >= 0) bm.s[1] = load_sb(w.b.sb, g2);
+    GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts,
+                       w.s.tan + (size_t)m * kMaxContacts * 2};
+    velocity_task_src<SWEEP_WARM>(src, w.s.sm_nc[m], w.s.sm_mask[m], 0u, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
+}
+
+__device__ __forceinline__ GlobalRows global_rows(const World& w, uint32_t m) {
+    return GlobalRows{w.s.rows + (size_t)m * kMaxContacts * kRowsF4, w.s.lam + (size_t)m * kMaxContacts};
+}
+
+// Velocity task of manifold m read from global memory; g1, g2 are the dynamic
+// bodies' slots (-1: no dofs), l1, l2 their Δv rows in `dva`.
+// The per-world kernels rebuild the rows from the compact records (their
+// batches are large enough for the stored rows' bytes to cost more than the
+// arithmetic they save).
 template <int KIND, class DvA>
 __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
                                               const DvA& dva) {
@@ -1034,20 +1159,12 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     dva.store(g2 >= 0 ? l2 : -1, dv.b);
 }
 
-// Fills the running thread's cache with manifold m (nc <= kCacheContacts).
-__device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t nc, int b1, int b2,
-                                           const CachedContacts& cc) {
-    for (int side = 0; side < 2; ++side) {
-        int b = side == 0 ? b1 : b2;
-        if (b < 0) continue;
-        for (int e = 0; e < 3; ++e) cc.at(3 * side + e) = w.b.sb[3 * b + e];
-    }
-    const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+// Fills the running thread's cache with manifold m's impulses and rows (nc <= kCacheContacts).
+__device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t nc, const CachedRows& cc) {
+    const float4* rows = w.s.rows + (size_t)m * kMaxContacts * kRowsF4;
     for (uint32_t k = 0; k < nc; ++k) {
-        for (int e = 0; e < 4; ++e) cc.at(6 + 7 * k + e) = con[4 * k + e];
-        cc.at(10 + 7 * k) = w.s.tan[((size_t)m * kMaxContacts + k) * 2];
-        cc.at(11 + 7 * k) = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
-        cc.at(12 + 7 * k) = w.s.lam[(size_t)m * kMaxContacts + k];
+        cc.at((int)k * (1 + kRowsF4)) = w.s.lam[(size_t)m * kMaxContacts + k];
+        for (int e = 0; e < kRowsF4; ++e) cc.at((int)k * (1 + kRowsF4) + 1 + e) = rows[(size_t)k * kRowsF4 + e];
     }
 }
 
@@ -1104,17 +1221,17 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     MyTasks mt;
     load_tasks(w, ms, mt, s_begin);
-    // The first task's contacts, inverse masses and tangents stay in shared
-    // memory for the whole call, its impulses too (written back at the end).
-    const CachedContacts cc{cache + threadIdx.x};
-    uint32_t nc0 = 0, mask0 = 0;
+    // For the iterations (not the warm start), the first task's rows and
+    // impulses stay in shared memory for the whole call (the impulses are
+    // written back at the end).
+    const CachedRows cc{cache + threadIdx.x};
+    uint32_t nc0 = 0;
     bool cached = false;
-    if (mt.n > 0 && cache != nullptr) {
+    if (mt.n > 0 && cache != nullptr && s_begin > 0) {
         nc0 = w.s.sm_nc[t];
         if (nc0 <= (uint32_t)kCacheContacts) {
             cached = true;
-            mask0 = w.s.sm_mask[t];
-            cache_task(w, t, nc0, mt.b1[0], mt.b2[0], cc);
+            cache_task(w, t, nc0, cc);
         }
     }
     uint32_t left = mt.n * (s_end - s_begin);
@@ -1138,16 +1255,17 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             if (!(r1 && r2)) continue;
             unsigned long long te = prof ? global_ns() : 0ull;
             if (prof) ts.wait_ns += te - tw;
-            if (k == 0 && cached) {
-                velocity_task_src<SWEEP_ANY>(cc, nc0, mask0, sw, cc, b1 >= 0, b2 >= 0, dv, w.ctl);
+            const uint32_t m = t + k * T;
+            const bool h1 = b1 >= 0, h2 = b2 >= 0;
+            if (sw == 0) {
+                warm_task(w, m, b1, b2, dv);
+            } else if (k == 0 && cached) {
+                if (sw & 1u) friction_rows(cc, nc0, h1, h2, dv);
+                else normal_rows(cc, nc0, h1, h2, dv);
             } else {
-                const uint32_t m = t + k * T;
-                BodyMasses bm;
-                if (b1 >= 0) bm.s[0] = load_sb(w.b.sb, b1);
-                if (b2 >= 0) bm.s[1] = load_sb(w.b.sb, b2);
-                GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts,
-                                   w.s.tan + (size_t)m * kMaxContacts * 2};
-                velocity_task_src<SWEEP_ANY>(src, w.s.sm_nc[m], w.s.sm_mask[m], sw, bm, b1 >= 0, b2 >= 0, dv, w.ctl);
+                const uint32_t nc = w.s.sm_nc[m];
+                if (sw & 1u) friction_rows(global_rows(w, m), nc, h1, h2, dv);
+                else normal_rows(global_rows(w, m), nc, h1, h2, dv);
             }
             publish_dvf(w.b.dvf, b1, t1 + 1u, dv.a);
             publish_dvf(w.b.dvf, b2, t2 + 1u, dv.b);
@@ -1998,7 +2116,7 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         k_world_permute_back<<<npb, kItemThreads, 0, st>>>(wc);
     }
     rec(2);
-    k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc);
+    k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc, !L.batched);
     rec(3);
     if (L.batched) {
         if (L.n_cluster > 0) {

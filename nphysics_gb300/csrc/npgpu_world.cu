@@ -459,6 +459,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(s.sm_list, P); A(s.sm_colour, P); A(s.sm_prank, P); A(s.sm_rk, P); A(s.sm_b1, P); A(s.sm_b2, P);
     A(s.sm_nc, P); A(s.con, (size_t)P * kMaxContacts * 4); A(s.lam, (size_t)P * kMaxContacts); A(s.sm_mask, P); A(s.pos_rec, (size_t)P * kPosRec); A(s.adj, 2 * (size_t)P); A(s.wm_order, P);
     A(s.perm, 5 * (size_t)P); A(s.tan, (size_t)P * kMaxContacts * 2);
+    A(s.rows, (size_t)P * kMaxContacts * kRowsF4);
     A(w->ctl, 1);
     A(w->d_forget, Cn);
 #undef A

@@ -48,6 +48,10 @@ constexpr int kColourBits = 56;      // colours a step may use (the colour word'
 constexpr unsigned long long kColourMask = (1ull << kColourBits) - 1ull;
 constexpr int kLeafCap = 16;        // partners a broad-phase leaf keeps between its two passes
 constexpr int kPosRec = 7 + 4;       // float4 of a manifold's position-solver record
+// A contact's three rows as the iterations read them: per row 7 float4 =
+// J1[6] J2[6] WJ1[6] WJ2[6] r rhs mu (one spare).
+constexpr int kRowF4 = 7;
+constexpr int kRowsF4 = 3 * kRowF4;
 
 // Row field offsets.
 enum { RF_J1 = 0, RF_J2 = 6, RF_WJ1 = 12, RF_WJ2 = 18, RF_R = 24, RF_RHS = 25, RF_IMP = 26, RF_MU = 27 };
@@ -118,6 +122,7 @@ struct Solver {
     float4 *con;                     // 4 contacts x 4 float4 per solver manifold (constant during the solve)
     float4 *lam;                     // 4 contacts per solver manifold: impulses (normal, tangent 1, tangent 2)
     float4 *tan;                     // 4 contacts x 2 per solver manifold: the friction directions (xyz)
+    float4 *rows;                    // 4 contacts x kRowsF4 per solver manifold: normal, friction 1, friction 2 rows
     uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13)
     float4 *pos_rec;                 // kPosRec per solver manifold: what the position solver reads besides poses
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
