@@ -173,8 +173,10 @@ __global__ void k_lbvh_refit(World w, int n) {
     uint32_t wk = key_world(w.c.keys_sorted[k]);
     float4 c0 = make_float4(mn.x, mn.y, mn.z, __uint_as_float(wk << 16 | wk));
     float4 c1 = make_float4(mx.x, mx.y, mx.z, w.c.rank[ci]);
+    uint32_t cs = ci;   // node_slot: with the largest rank in node_max.w, the owner test's (rank, slot) maximum
     w.c.node_min[node] = c0;
     w.c.node_max[node] = c1;
+    w.c.node_slot[node] = cs;
     if (n == 1) return;
     int p = w.c.parent[node];
     for (int guard = 0; p >= 0; ++guard) {
@@ -188,13 +190,17 @@ __global__ void k_lbvh_refit(World w, int n) {
         const bool from_left = l == node;
         const int sib = from_left ? r : l;
         const float4 s0 = ld_cg(&w.c.node_min[sib]), s1 = ld_cg(&w.c.node_max[sib]);
+        const uint32_t ss = __ldcg(&w.c.node_slot[sib]);
         const float4 a0 = from_left ? c0 : s0, a1 = from_left ? c1 : s1;
         const float4 b0 = from_left ? s0 : c0, b1 = from_left ? s1 : c1;
+        const uint32_t as = from_left ? cs : ss, bs = from_left ? ss : cs;
+        cs = a1.w > b1.w ? as : (b1.w > a1.w ? bs : (as > bs ? as : bs));
         uint32_t wr = (__float_as_uint(a0.w) & 0xffff0000u) | (__float_as_uint(b0.w) & 0xffffu);
         c0 = make_float4(fminf(a0.x, b0.x), fminf(a0.y, b0.y), fminf(a0.z, b0.z), __uint_as_float(wr));
         c1 = make_float4(fmaxf(a1.x, b1.x), fmaxf(a1.y, b1.y), fmaxf(a1.z, b1.z), fmaxf(a1.w, b1.w));
         w.c.node_min[p] = c0;
         w.c.node_max[p] = c1;
+        w.c.node_slot[p] = cs;
         // The traversal's copy: both children's boxes and references in one
         // 80-byte record, a leaf child referenced by its collider (top bit set).
         float4* wd = w.c.wide + 5 * (size_t)p;
@@ -204,7 +210,7 @@ __global__ void k_lbvh_refit(World w, int n) {
         wd[3] = b1;
         uint32_t lref = l >= n - 1 ? (0x80000000u | w.c.vals_sorted[l - (n - 1)]) : (uint32_t)l;
         uint32_t rref = r >= n - 1 ? (0x80000000u | w.c.vals_sorted[r - (n - 1)]) : (uint32_t)r;
-        wd[4] = make_float4(__uint_as_float(lref), __uint_as_float(rref), 0.0f, 0.0f);
+        wd[4] = make_float4(__uint_as_float(lref), __uint_as_float(rref), __uint_as_float(as), __uint_as_float(bs));
         node = p;
         p = w.c.parent[p];
     }
@@ -264,9 +270,13 @@ __global__ void k_bp_traverse(World w, int n) {
     // somewhere below) and an AABB overlapping the query's. An internal node's
     // record carries both children's boxes, so a visited node costs one
     // memory round trip, and leaf children are tested without visiting them.
-    auto enter = [&](float4 nmin, float4 nmax) {
+    // The query owns a collider of the subtree only if the subtree's largest
+    // (rank, slot) pair is above its own: a larger rank, or the same rank
+    // and a larger slot (owns()).
+    auto enter = [&](float4 nmin, float4 nmax, uint32_t nslot) {
         uint32_t nw = __float_as_uint(nmin.w);
-        return qw >= (nw >> 16) && qw <= (nw & 0xffffu) && !(nmax.w < ra) && overlap(amin, amax, nmin, nmax);
+        const bool may_own = ra < nmax.w || (ra == nmax.w && a < nslot);
+        return qw >= (nw >> 16) && qw <= (nw & 0xffffu) && may_own && overlap(amin, amax, nmin, nmax);
     };
     auto emit = [&](uint32_t b, float rb) {
         // owns(): the smaller bounding radius owns the pair, ties by slot.
@@ -281,7 +291,7 @@ __global__ void k_bp_traverse(World w, int n) {
             ++count;
         }
     };
-    if (n >= 2 && enter(c.node_min[0], c.node_max[0])) {
+    if (n >= 2 && enter(c.node_min[0], c.node_max[0], c.node_slot[0])) {
         int stack[64];
         int sp = 0;
         stack[sp++] = 0;
@@ -289,7 +299,7 @@ __global__ void k_bp_traverse(World w, int n) {
             const float4* wd = c.wide + 5 * (size_t)stack[--sp];
             const float4 lmin = wd[0], lmax = wd[1], rmin = wd[2], rmax = wd[3], refs = wd[4];
             const uint32_t lref = __float_as_uint(refs.x), rref = __float_as_uint(refs.y);
-            const bool el = enter(lmin, lmax), er = enter(rmin, rmax);
+            const bool el = enter(lmin, lmax, __float_as_uint(refs.z)), er = enter(rmin, rmax, __float_as_uint(refs.w));
             if (el && (lref & 0x80000000u)) emit(lref & 0x7fffffffu, lmax.w);
             if (er && (rref & 0x80000000u)) emit(rref & 0x7fffffffu, rmax.w);
             const bool pl = el && !(lref & 0x80000000u), pr = er && !(rref & 0x80000000u);

@@ -966,6 +966,21 @@ struct CachedRows {
     __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { at((int)k * (1 + kRowsF4)) = v; }
 };
 
+// The warm start (sor_prox.rs:19-45) of a task without learned starts: the
+// cached impulses applied along the stored rows.
+template <class RS>
+__device__ __forceinline__ void warm_rows(const RS& src, uint32_t nc, bool h1, bool h2, DV& dv) {
+    for (uint32_t k = 0; k < nc; ++k) {
+        const float4 l = src.get_lam(k);
+        const float li[3] = {l.x, l.y, l.z};
+#pragma unroll 1
+        for (int r = 0; r < 3; ++r) {
+            if (li[r] == 0.0f) continue;
+            row_axpy(src.row(k, r), dv, li[r], h1, h2);
+        }
+    }
+}
+
 // The friction rows (sor_prox.rs:232-343) and the normal rows
 // (sor_prox.rs:181-230) of one task's contacts, from stored rows.
 template <class RS>
@@ -1216,7 +1231,7 @@ struct TaskStats {
 };
 
 __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
-                                TaskStats& ts, float4* cache) {
+                                bool learned, TaskStats& ts, float4* cache) {
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     MyTasks mt;
@@ -1258,7 +1273,9 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
             const uint32_t m = t + k * T;
             const bool h1 = b1 >= 0, h2 = b2 >= 0;
             if (sw == 0) {
-                warm_task(w, m, b1, b2, dv);
+                // Learned starts need the check on the compact records.
+                if (learned) warm_task(w, m, b1, b2, dv);
+                else warm_rows(global_rows(w, m), w.s.sm_nc[m], h1, h2, dv);
             } else if (k == 0 && cached) {
                 if (sw & 1u) friction_rows(cc, nc0, h1, h2, dv);
                 else normal_rows(cc, nc0, h1, h2, dv);
@@ -1329,23 +1346,24 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
         return;
     }
     const bool prof = p.profile != 0;
+    const bool learned = p.warmstart_mode == 2u;
     TaskStats ts{0ull, 0ull, 0ull};
     unsigned long long k0 = 0;
     if (prof && blockIdx.x == 0 && threadIdx.x == 0) k0 = global_ns();
     uint32_t epoch = 0;
-    if (!velocity_sweeps(w, 0, 1, ms, prof, ts, s_cache)) return;
+    if (!velocity_sweeps(w, 0, 1, ms, prof, learned, ts, s_cache)) return;
     if (!grid_sync(w.ctl, epoch)) return;
     if (!eval_residual(w, ms, sh, epoch, true)) return;
     uint32_t iters = 0;
     if (!p.solve_to_tolerance) {
         iters = p.max_velocity_iterations;
-        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms, prof, ts, s_cache)) return;
+        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms, prof, learned, ts, s_cache)) return;
         if (!grid_sync(w.ctl, epoch)) return;
         if (!eval_residual(w, ms, sh, epoch, false)) return;
     } else {
         for (uint32_t it = 0; it < p.max_iterations_to_tolerance; ++it) {
             if (((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
-            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms, prof, ts, s_cache)) return;
+            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms, prof, learned, ts, s_cache)) return;
             ++iters;
             if (!grid_sync(w.ctl, epoch)) return;
             if (!eval_residual(w, ms, sh, epoch, false)) return;

@@ -448,7 +448,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(c.pose_t, Cn); A(c.pose_q, Cn); A(c.aabb_min, Cn); A(c.aabb_max, Cn);
     A(c.keys, Cn); A(c.keys_sorted, Cn); A(c.vals, Cn); A(c.vals_sorted, Cn);
     A(c.left, Cn); A(c.right, Cn); A(c.parent, 2 * (size_t)Cn); A(c.node_min, 2 * (size_t)Cn);
-    A(c.node_max, 2 * (size_t)Cn); A(c.wide, 5 * (size_t)Cn); A(c.node_flag, Cn); A(c.leaf_count, Cn); A(c.leaf_offset, Cn);
+    A(c.node_max, 2 * (size_t)Cn); A(c.wide, 5 * (size_t)Cn); A(c.node_slot, 2 * (size_t)Cn); A(c.node_flag, Cn); A(c.leaf_count, Cn); A(c.leaf_offset, Cn);
     A(c.leaf_tmp, (size_t)kLeafCap * Cn);
     for (Pairs* pp : {&w->pa, &w->pb}) {
         A(pp->pair, P); A(pp->owner_start, Cn); A(pp->owner_count, Cn); A(pp->ncont, P);

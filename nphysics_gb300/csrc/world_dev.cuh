@@ -94,6 +94,7 @@ struct Colliders {
     int *left, *right, *parent;
     float4 *node_min, *node_max;
     float4 *wide;                    // 5 per internal node: both children's boxes and references
+    uint32_t *node_slot;             // per node: the largest slot among its colliders of the largest rank
     int *node_flag;
     uint32_t *leaf_count, *leaf_offset;
     uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
