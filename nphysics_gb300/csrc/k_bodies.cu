@@ -15,6 +15,7 @@ __global__ void k_upload_bodies(World w, const BodyUpload* d, uint32_t n) {
     const BodyUpload u = d[t];
     const Bodies& b = w.b;
     uint32_t i = u.slot;
+    b.gen[i] = u.gen;
     b.pos_t[i] = make_float4(u.pos[0], u.pos[1], u.pos[2], 0.0f);
     b.pos_q[i] = make_float4(u.pos[3], u.pos[4], u.pos[5], u.pos[6]);
     b.lin[i] = make_float4(u.vel[0], u.vel[1], u.vel[2], 0.0f);
@@ -82,19 +83,41 @@ __global__ void k_mass_updates(World w, const MassUpdate* d, uint32_t n) {
 }
 
 // RigidBody::apply_force with ForceType::Force (rigid_body.rs:771-792).
-__global__ void k_forces(World w, const ForceUpload* d, uint32_t n) {
-    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= n) return;
-    const ForceUpload u = d[t];
-    const Bodies& b = w.b;
-    uint32_t i = u.slot;
+__device__ __forceinline__ void apply_force(const Bodies& b, uint32_t i, const float* f, bool wake) {
     uint32_t info = b.info[i];
     if (bi_status(info) != 2u) return;
-    if (u.wake) body_activate(b, i);
-    np::V fl = np::mk(u.f[0] * body_mask(info, 0), u.f[1] * body_mask(info, 1), u.f[2] * body_mask(info, 2));
-    np::V fa = np::mk(u.f[3] * body_mask(info, 3), u.f[4] * body_mask(info, 4), u.f[5] * body_mask(info, 5));
+    if (wake) body_activate(b, i);
+    np::V fl = np::mk(f[0] * body_mask(info, 0), f[1] * body_mask(info, 1), f[2] * body_mask(info, 2));
+    np::V fa = np::mk(f[3] * body_mask(info, 3), f[4] * body_mask(info, 4), f[5] * body_mask(info, 5));
     b.f_lin[i] = f4(np::add(v3(b.f_lin[i]), fl));
     b.f_ang[i] = f4(np::add(v3(b.f_ang[i]), fa));
+}
+
+__global__ void k_force_check(World w, const npgpu_handle* h, const float* f, uint32_t n, uint32_t batch,
+                              uint64_t cap) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const uint64_t idx = h[t].index;
+    uint32_t fl = 0;
+    if (idx >= cap || !(w.b.info[idx] & BI_ALIVE) || w.b.gen[idx] != h[t].generation) fl |= 1u;
+    else if (atomicExch(&w.b.fstamp[idx], batch) == batch) fl |= 4u;
+#pragma unroll
+    for (int e = 0; e < 6; ++e)
+        if (!isfinite(f[6 * (size_t)t + e])) fl |= 2u;
+    if (fl) atomicOr(&w.ctl->force_flags, fl);
+}
+
+// One force per thread (the batch names each body once), or the whole batch
+// in order on one thread.
+__global__ void k_forces(World w, const npgpu_handle* h, const float* f, uint32_t n, bool wake, bool serial) {
+    if (serial) {
+        if (blockIdx.x == 0 && threadIdx.x == 0)
+            for (uint32_t k = 0; k < n; ++k) apply_force(w.b, (uint32_t)h[k].index, f + 6 * (size_t)k, wake);
+        return;
+    }
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    apply_force(w.b, (uint32_t)h[t].index, f + 6 * (size_t)t, wake);
 }
 
 __global__ void k_kill(World w, const uint32_t* slots, uint32_t n, int colliders) {
@@ -170,9 +193,16 @@ cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n,
     k_mass_updates<<<nblocks(n), kThreads, 0, st>>>(w, d, n);
     return cudaGetLastError();
 }
-cudaError_t launch_forces(const World& w, const ForceUpload* d, uint32_t n, cudaStream_t st) {
+cudaError_t launch_force_check(const World& w, const npgpu_handle* h, const float* f, uint32_t n, uint32_t batch,
+                               uint64_t cap, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_forces<<<nblocks(n), kThreads, 0, st>>>(w, d, n);
+    k_force_check<<<nblocks(n), kThreads, 0, st>>>(w, h, f, n, batch, cap);
+    return cudaGetLastError();
+}
+cudaError_t launch_forces(const World& w, const npgpu_handle* h, const float* f, uint32_t n, bool wake, bool serial,
+                          cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_forces<<<serial ? 1u : nblocks(n), kThreads, 0, st>>>(w, h, f, n, wake, serial);
     return cudaGetLastError();
 }
 cudaError_t launch_kill(const World& w, const uint32_t* slots, uint32_t n, int colliders, cudaStream_t st) {

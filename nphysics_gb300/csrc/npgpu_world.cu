@@ -123,6 +123,7 @@ struct npgpu_world {
     std::vector<MassUpdate> pending_mass;
     // Staging.
     void* h_stage = nullptr;
+    uint32_t* h_flags = nullptr;         // pinned: the device checks of a force batch
     size_t h_stage_bytes = 0;
     void* d_stage = nullptr;
     size_t d_stage_bytes = 0;
@@ -141,6 +142,7 @@ struct npgpu_world {
     bool layout_ok = false;              // the worlds qualify for the per-world schedule
     uint32_t n_worlds = 0, max_world_bodies = 0, n_big_worlds = 0;
     uint32_t n_cluster_worlds = 0, cluster_shift = 0;   // worlds solved by a thread-block cluster
+    uint32_t force_batch = 0;
     std::vector<uint32_t> world_start;   // n_worlds + 1 slot boundaries, then the n_worlds largest-first order
     uint32_t worlds_cap = 0;             // worlds the device bucket buffers hold
     bool layout_on_device = false;
@@ -440,7 +442,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(b.mass, B); A(b.local_I, 9 * (size_t)B); A(b.I, 9 * (size_t)B); A(b.inv_mass, B); A(b.inv_I, 9 * (size_t)B);
     A(b.acc_lin, B); A(b.acc_ang, B); A(b.f_lin, B); A(b.f_ang, B);
     A(b.lin_damp, B); A(b.ang_damp, B); A(b.max_lin, B); A(b.max_ang, B); A(b.sleep_thr, B); A(b.energy, B);
-    A(b.info, B); A(b.world, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.dvf, 8 * (size_t)B); A(b.posef, 12 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
+    A(b.info, B); A(b.world, B); A(b.gen, B); A(b.fstamp, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.dvf, 8 * (size_t)B); A(b.posef, 12 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
     A(b.cw, B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B);
     Colliders& c = w->dw.c;
     A(c.body, Cn); A(c.info, Cn); A(c.params, Cn); A(c.wrt_t, Cn); A(c.wrt_q, Cn);
@@ -553,6 +555,7 @@ void npgpu_destroy(npgpu_world* w) {
                     (void*)w->d_stats, (void*)w->d_samples, (void*)w->d_feat})
         cudaFree(p);
     if (w->d_stage) cudaFree(w->d_stage);
+    if (w->h_flags) cudaFreeHost(w->h_flags);
     if (w->h_stage) cudaFreeHost(w->h_stage);
     if (w->ev_stage) cudaEventDestroy(w->ev_stage);
     for (auto& e : w->ev)
@@ -645,6 +648,7 @@ npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
         w->max_world = std::max(w->max_world, d.world);
         hb.alive = true;
         hb.gen = handles[k].generation;
+        u.gen = handles[k].generation;
         hb.kind = d.kind;
         hb.status = status;
         hb.flags = d.flags;
@@ -818,23 +822,44 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
                                 int auto_wake_up) {
     if (!w || (n && (!handles || !forces6))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
     if (n == 0) return NPGPU_OK;
-    // Checked and packed straight into the pinned staging area; nothing is
-    // copied to the device unless every force is valid.
+    // The batch goes to the device staging area (page-locked arrays straight
+    // from the caller, pageable ones through the pinned staging area), the
+    // device checks it (handles against the slots' generations, finite
+    // forces, a body named twice), and the forces are applied only if every
+    // handle and force is valid. The call returns once the checks are known,
+    // so the caller may reuse its arrays.
+    const size_t hb = sizeof(npgpu_handle) * (size_t)n, fb = 6 * sizeof(float) * (size_t)n;
+    const bool direct = host_pinned(handles) && host_pinned(forces6);
     void* hp = nullptr;
-    npgpu_status st = stage_reserve(w, (size_t)n * sizeof(ForceUpload), &hp);
+    npgpu_status st = stage_reserve(w, hb + fb, &hp);
     if (st != NPGPU_OK) return st;
-    ForceUpload* up = (ForceUpload*)hp;
-    for (uint32_t k = 0; k < n; ++k) {
-        if (!body_handle_ok(w, handles[k])) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
-        if (!finite_n(forces6 + 6 * k, 6)) return fail(w, NPGPU_ERR_NAN, "force is not finite");
-        up[k].slot = (uint32_t)handles[k].index;
-        up[k].wake = auto_wake_up ? 1u : 0u;
-        std::memcpy(up[k].f, forces6 + 6 * k, sizeof(up[k].f));
+    void* dp = w->d_stage;
+    if (direct) {
+        CK(cudaMemcpyAsync(dp, handles, hb, cudaMemcpyHostToDevice, w->stream), "force handles");
+        CK(cudaMemcpyAsync((char*)dp + hb, forces6, fb, cudaMemcpyHostToDevice, w->stream), "forces");
+    } else {
+        std::memcpy(hp, handles, hb);
+        std::memcpy((char*)hp + hb, forces6, fb);
+        st = stage_commit(w, hb + fb, &dp);
+        if (st != NPGPU_OK) return st;
     }
-    void* dp = nullptr;
-    st = stage_commit(w, (size_t)n * sizeof(ForceUpload), &dp);
-    if (st != NPGPU_OK) return st;
-    CK(launch_forces(w->dw, (const ForceUpload*)dp, n, w->stream), "apply forces");
+    if (!w->h_flags) CK(cudaMallocHost(&w->h_flags, sizeof(uint32_t)), "pinned flags");
+    if (++w->force_batch == 0) {
+        CK(cudaMemsetAsync(w->dw.b.fstamp, 0, sizeof(uint32_t) * w->cap_b, w->stream), "force stamps");
+        w->force_batch = 1;
+    }
+    const npgpu_handle* dh = (const npgpu_handle*)dp;
+    const float* df = (const float*)((const char*)dp + hb);
+    CK(cudaMemsetAsync(&w->ctl->force_flags, 0, sizeof(uint32_t), w->stream), "force flags");
+    CK(launch_force_check(w->dw, dh, df, n, w->force_batch, w->cap_b, w->stream), "force check");
+    CK(cudaMemcpyAsync(w->h_flags, &w->ctl->force_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream),
+       "force flags");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    CK(cudaEventSynchronize(w->ev_stage), "force check");
+    const uint32_t flags = *w->h_flags;
+    if (flags & 1u) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid body handle");
+    if (flags & 2u) return fail(w, NPGPU_ERR_NAN, "force is not finite");
+    CK(launch_forces(w->dw, dh, df, n, auto_wake_up != 0, (flags & 4u) != 0, w->stream), "apply forces");
     CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
     return NPGPU_OK;
 }

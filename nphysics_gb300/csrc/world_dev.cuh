@@ -14,6 +14,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "npgpu.h"
+
 #include "np_math.cuh"
 
 namespace npgpu_dev {
@@ -70,6 +72,8 @@ struct Bodies {
     float *lin_damp, *ang_damp, *max_lin, *max_ang, *sleep_thr, *energy;
     uint32_t *info;
     uint32_t *world;
+    unsigned long long *gen;         // generation of the body in each slot (handles are checked against it)
+    uint32_t *fstamp;                // the last force batch that named the body
     float *dv;                       // mj_lambda, 6 per body
     float4 *sb;                      // 3 per body: inverse augmented mass as the solver reads it
     unsigned long long *dvf;         // 8 per body: Δv words flagged with the body's update count
@@ -170,7 +174,7 @@ struct Control {
     uint32_t world_next[4];          // batched worlds: block and warp work counters of the velocity / position kernels
     uint32_t mlp_samples;            // training samples recorded so far
     uint32_t learned_starts, learned_kept;   // learned warm start: predictions made / kept this step
-    uint32_t pad2;
+    uint32_t force_flags;            // checks of the last force batch: 1 bad handle, 2 non-finite, 4 a body twice
     double mlp_loss;                 // loss of the last training step
 };
 
@@ -255,6 +259,7 @@ cudaError_t mlp_adam(float* prm, float* m1, float* m2, const float* grad, float 
 
 // Uploads / maintenance kernels.
 struct BodyUpload {
+    unsigned long long gen;
     uint32_t slot;
     uint32_t info;
     uint32_t world;
@@ -273,15 +278,18 @@ struct MassUpdate {                  // new local inertia / com of a body
     uint32_t activate;               // bit 0: inertia changed; bit 1: Body::activate (collider removal)
     float mass, local_I[9], local_com[3];
 };
-struct ForceUpload {
-    uint32_t slot;
-    uint32_t wake;
-    float f[6];
-};
 cudaError_t launch_upload_bodies(const World& w, const BodyUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_upload_colliders(const World& w, const ColliderUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n, cudaStream_t st);
-cudaError_t launch_forces(const World& w, const ForceUpload* d, uint32_t n, cudaStream_t st);
+// Checks a force batch on the device (handles against the slots' generations,
+// finite forces, a body named twice) into ctl->force_flags, which the caller
+// clears first. cap: body slots allocated.
+cudaError_t launch_force_check(const World& w, const npgpu_handle* handles, const float* forces6, uint32_t n,
+                               uint32_t batch, uint64_t cap, cudaStream_t st);
+// Adds forces6[k] (linear, angular) to body handles[k].index; `serial`: in
+// order on one thread, for batches that name a body twice.
+cudaError_t launch_forces(const World& w, const npgpu_handle* handles, const float* forces6, uint32_t n, bool wake,
+                          bool serial, cudaStream_t st);
 cudaError_t launch_kill(const World& w, const uint32_t* slots, uint32_t n, int colliders, cudaStream_t st);
 cudaError_t launch_forget_pairs(const World& w, const uint8_t* flags, cudaStream_t st);
 cudaError_t launch_pack_bodies(const World& w, uint32_t first, uint32_t n, float* pos7, float* vel6, float* energy,

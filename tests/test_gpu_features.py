@@ -208,3 +208,22 @@ def test_pinned_host_buffers(gpu_lib):
     ref = g.bodies()
     np.testing.assert_array_equal(pos, ref["position"])
     np.testing.assert_array_equal(vel, ref["velocity"])
+
+
+def test_forces_naming_a_body_twice(gpu_lib):
+    # A batch that names one body twice adds both forces in the batch's order,
+    # as the reference's successive apply_force calls do.
+    pb, pc = balls_on_ground(9, seed=4)
+    bodies, colliders = scenes._concat(pb, pc)
+    sc = scenes.Scene("twice", bodies, colliders)
+    g, o = pair(sc)
+    h = np.ascontiguousarray(sc.body_handles[[3, 6, 3, 3]])
+    f = np.zeros((4, 6), np.float32)
+    f[:, 0] = (0.1, 5.0, 1e-3, 7.0)
+    f[:, 4] = (1e-4, -2.0, 3.0, 0.3)
+    for _ in range(10):
+        g.apply_forces(h, f, wake=True)
+        o.apply_forces(h, f, wake=True)
+        g.step(1)
+        o.step(1)
+    same(g, o, "twice")
