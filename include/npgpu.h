@@ -280,7 +280,11 @@ npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
 
 /* RigidBody::apply_force(0, force, ForceType::Force, auto_wake_up)
  * (rigid_body.rs:783-820): accumulates into the external force, which the
- * next step uses and then clears. */
+ * next step uses and then clears. forces6[6n]: linear, then angular. The
+ * batch is checked whole before any force is applied (an invalid handle or a
+ * non-finite force applies nothing); a body named twice gets both forces in
+ * order. Page-locked arrays are read by the copy engines directly; the call
+ * returns once the arrays have been read. */
 npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
                                 const float* forces6, int auto_wake_up);
 
@@ -294,8 +298,10 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints,
 npgpu_status npgpu_synchronize(npgpu_world* w);
 
 /* Chooses the solver's launch shape for the current scene by timing real
- * steps: the one-grid schedule and, when the worlds qualify, one block per
- * world with 64, 128 and 256 threads, each for 1 + steps_per_candidate steps,
+ * steps: the one-grid schedule and, when the worlds qualify, the per-world
+ * schedule with 64, 128 and 256 threads per world block (one candidate when
+ * every world is solved by a thread-block cluster), each for 1 +
+ * steps_per_candidate steps,
  * after one step with the automatic schedule that sizes the candidates.
  * Every candidate computes the same bits, so the world simply advances by
  * those steps. Sets params.solver_schedule and params.world_threads to the
@@ -306,7 +312,8 @@ npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32
 
 /* Copies body state to host arrays indexed by slot (any pointer may be NULL):
  * position[7n], velocity[6n], energy[n] (activation energy), active[n]
- * (1 when awake), for slots [first, first + n). */
+ * (1 when awake), for slots [first, first + n). Waits for the world's
+ * stream; page-locked arrays are written by the copy engines directly. */
 npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, float* position,
                                    float* velocity, float* energy, uint8_t* active);
 
