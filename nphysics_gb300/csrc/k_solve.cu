@@ -1027,17 +1027,15 @@ __device__ __forceinline__ void normal_rows(const RS& src, uint32_t nc, bool h1,
     }
 }
 
-// One velocity task: sweep 0 is the warm start (sor_prox.rs:19-45), odd sweeps
-// the friction rows of an iteration (sor_prox.rs:232-343), even sweeps > 0 its
-// normal rows (sor_prox.rs:181-230). l1, l2 are the dynamic bodies' rows in
-// `dvbase` (-1: no dofs), the global Δv array or a world's shared-memory Δv.
-// KIND fixes the sweep kind at compile time (0 warm start, 1 friction rows,
-// 2 normal rows) where the caller knows it; -1 decides from `sweep`.
-enum { SWEEP_ANY = -1, SWEEP_WARM = 0, SWEEP_FRICTION = 1, SWEEP_NORMAL = 2 };
+// One velocity task from the compact records, rows rebuilt from the normal,
+// the friction directions and the lever arms: KIND 0 is the warm start
+// (sor_prox.rs:19-45), 1 the friction rows of an iteration
+// (sor_prox.rs:232-343), 2 its normal rows (sor_prox.rs:181-230).
+enum { SWEEP_WARM = 0, SWEEP_FRICTION = 1, SWEEP_NORMAL = 2 };
 template <int KIND, class Src, class BM>
 __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, uint32_t mask, uint32_t sweep,
                                                   const BM& bm, bool h1, bool h2, DV& dv, Control* ctl) {
-    const int kind = KIND != SWEEP_ANY ? KIND : (sweep == 0 ? SWEEP_WARM : (sweep & 1u) ? SWEEP_FRICTION : SWEEP_NORMAL);
+    const int kind = KIND;
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = src.rec(k);
         float4 l = src.get_lam(k);
