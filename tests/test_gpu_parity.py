@@ -222,3 +222,34 @@ def test_removal_wakes_the_stack(gpu_lib):
     o.step(30)
     assert g.bodies()["active"][1:].sum() == len(sc.bodies) - 1
     assert_close_rel(g.bodies()["position"], o.bodies()["position"], 1e-5, 1e-5, "positions after removal")
+
+
+@pytest.mark.parametrize("sched", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
+def test_degenerate_worlds(gpu_lib, sched):
+    # Edge cases of the step: a world with no body at all, one with a static
+    # ground alone, and one dynamic body falling beside the ground without
+    # touching it (no pair, no contact, no solver manifold), under both
+    # schedules.
+    from nphysics_gb300.world import GpuWorld
+    p = abi.default_params()
+    p.solver_schedule = sched
+    empty = GpuWorld(p)
+    empty.step(3)
+    assert empty.counters()["num_contacts"] == 0
+    g, gc = scenes._ground()
+    sc = scenes.Scene("ground alone", *scenes._concat([g], [gc]))
+    w = GpuWorld.for_scene(sc, p)
+    w.step(3)
+    assert w.counters()["num_contacts"] == 0
+    b = scenes.body_descs(1)
+    b["position"][0, :3] = (500.0, 40.0, 0.0)
+    c = scenes.collider_descs(1, 0, abi.SHAPE_BALL, (0.5, 0, 0), density=1.0)
+    sc = scenes.Scene("one body", *scenes._concat([g, b], [gc, c]))
+    q = sc.params()
+    q.solver_schedule = sched
+    gw, o = make_pair(sc, q)
+    gw.step(20)
+    o.step(20)
+    assert gw.counters()["num_contacts"] == 0
+    np.testing.assert_array_equal(gw.bodies()["position"], o.bodies()["position"])
+    np.testing.assert_array_equal(gw.bodies()["velocity"], o.bodies()["velocity"])
