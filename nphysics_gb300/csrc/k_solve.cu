@@ -1832,7 +1832,7 @@ __device__ __forceinline__ void position_task(const World& w, const StepParams& 
     if (moved2) store_pose(w.b, bb2, P2);
 }
 
-__global__ void __launch_bounds__(kCoopThreads) k_position(World w, StepParams p) {
+__global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParams p) {
     const uint32_t ms = w.ctl->nsolver;
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
