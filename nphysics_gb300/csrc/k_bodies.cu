@@ -93,17 +93,29 @@ __device__ __forceinline__ void apply_force(const Bodies& b, uint32_t i, const f
     b.f_ang[i] = f4(np::add(v3(b.f_ang[i]), fa));
 }
 
-__global__ void k_force_check(World w, const npgpu_handle* h, const float* f, uint32_t n, uint32_t batch,
-                              uint64_t cap) {
+// Reads the batch from (h, f) (device memory, or page-locked host memory
+// through its device-side address), keeps a copy in (hd, fd) when they
+// differ, and checks it.
+__global__ void k_force_check(World w, const npgpu_handle* h, const float* f, npgpu_handle* hd, float* fd, uint32_t n,
+                              uint32_t batch, uint64_t cap) {
     uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t >= n) return;
-    const uint64_t idx = h[t].index;
+    const npgpu_handle ht = h[t];
+    float ft[6];
+#pragma unroll
+    for (int e = 0; e < 6; ++e) ft[e] = f[6 * (size_t)t + e];
+    if (hd != h) {
+        hd[t] = ht;
+#pragma unroll
+        for (int e = 0; e < 6; ++e) fd[6 * (size_t)t + e] = ft[e];
+    }
+    const uint64_t idx = ht.index;
     uint32_t fl = 0;
-    if (idx >= cap || !(w.b.info[idx] & BI_ALIVE) || w.b.gen[idx] != h[t].generation) fl |= 1u;
+    if (idx >= cap || !(w.b.info[idx] & BI_ALIVE) || w.b.gen[idx] != ht.generation) fl |= 1u;
     else if (atomicExch(&w.b.fstamp[idx], batch) == batch) fl |= 4u;
 #pragma unroll
     for (int e = 0; e < 6; ++e)
-        if (!isfinite(f[6 * (size_t)t + e])) fl |= 2u;
+        if (!isfinite(ft[e])) fl |= 2u;
     if (fl) atomicOr(&w.ctl->force_flags, fl);
 }
 
@@ -178,6 +190,36 @@ __global__ void k_pack_bodies(World w, uint32_t first, uint32_t n, float* pos7, 
     if (active) active[t] = body_is_active(b.info[i], b.energy[i]) ? 1 : 0;
 }
 
+// Poses and velocities of slots [first, first + n) written straight into
+// page-locked host arrays (their device-side addresses): each block packs
+// its bodies in shared memory and writes contiguous runs, so the stores to
+// host memory coalesce.
+__global__ void k_pack_bodies_host(World w, uint32_t first, uint32_t n, float* pos7, float* vel6) {
+    __shared__ float sp[kThreads * 7], sv[kThreads * 6];
+    const uint32_t b0 = blockIdx.x * kThreads, t = threadIdx.x;
+    const uint32_t cnt = n - b0 < (uint32_t)kThreads ? n - b0 : (uint32_t)kThreads;
+    if (t < cnt) {
+        const uint32_t i = first + b0 + t;
+        const float4 a = w.b.pos_t[i], q = w.b.pos_q[i], l = w.b.lin[i], g = w.b.ang[i];
+        float* o = sp + 7 * t;
+        o[0] = a.x; o[1] = a.y; o[2] = a.z; o[3] = q.x; o[4] = q.y; o[5] = q.z; o[6] = q.w;
+        float* v = sv + 6 * t;
+        v[0] = l.x; v[1] = l.y; v[2] = l.z; v[3] = g.x; v[4] = g.y; v[5] = g.z;
+    }
+    __syncthreads();
+    if (pos7)
+        for (uint32_t j = t; j < 7 * cnt; j += kThreads) pos7[7 * (size_t)b0 + j] = sp[j];
+    if (vel6)
+        for (uint32_t j = t; j < 6 * cnt; j += kThreads) vel6[6 * (size_t)b0 + j] = sv[j];
+}
+
+cudaError_t launch_pack_bodies_host(const World& w, uint32_t first, uint32_t n, float* pos7, float* vel6,
+                                    cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_pack_bodies_host<<<nblocks(n), kThreads, 0, st>>>(w, first, n, pos7, vel6);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_upload_bodies(const World& w, const BodyUpload* d, uint32_t n, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     k_upload_bodies<<<nblocks(n), kThreads, 0, st>>>(w, d, n);
@@ -193,10 +235,10 @@ cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n,
     k_mass_updates<<<nblocks(n), kThreads, 0, st>>>(w, d, n);
     return cudaGetLastError();
 }
-cudaError_t launch_force_check(const World& w, const npgpu_handle* h, const float* f, uint32_t n, uint32_t batch,
-                               uint64_t cap, cudaStream_t st) {
+cudaError_t launch_force_check(const World& w, const npgpu_handle* h, const float* f, npgpu_handle* hd, float* fd,
+                               uint32_t n, uint32_t batch, uint64_t cap, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
-    k_force_check<<<nblocks(n), kThreads, 0, st>>>(w, h, f, n, batch, cap);
+    k_force_check<<<nblocks(n), kThreads, 0, st>>>(w, h, f, hd, fd, n, batch, cap);
     return cudaGetLastError();
 }
 cudaError_t launch_forces(const World& w, const npgpu_handle* h, const float* f, uint32_t n, bool wake, bool serial,

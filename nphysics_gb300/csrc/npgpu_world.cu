@@ -270,6 +270,16 @@ static bool host_pinned(const void* p) {
     return a.type == cudaMemoryTypeHost;
 }
 
+// The device-side address of page-locked host memory (null when there is none).
+static void* host_device_ptr(void* p) {
+    cudaPointerAttributes a{};
+    if (!p || cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 static void sync_world_view(npgpu_world* w) {
     w->dw.nb_slots = w->nb_slots;
     w->dw.nc_slots = w->nc_slots;
@@ -822,22 +832,21 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
                                 int auto_wake_up) {
     if (!w || (n && (!handles || !forces6))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
     if (n == 0) return NPGPU_OK;
-    // The batch goes to the device staging area (page-locked arrays straight
-    // from the caller, pageable ones through the pinned staging area), the
-    // device checks it (handles against the slots' generations, finite
-    // forces, a body named twice), and the forces are applied only if every
-    // handle and force is valid. The call returns once the checks are known,
-    // so the caller may reuse its arrays.
+    // The device checks the batch (handles against the slots' generations,
+    // finite forces, a body named twice) as it copies it into the device
+    // staging area, reading page-locked arrays over the host link itself and
+    // pageable ones from the pinned staging area; the forces are applied from
+    // that copy only if every handle and force is valid. The call returns once
+    // the checks are known, so the caller may reuse its arrays.
     const size_t hb = sizeof(npgpu_handle) * (size_t)n, fb = 6 * sizeof(float) * (size_t)n;
-    const bool direct = host_pinned(handles) && host_pinned(forces6);
+    const npgpu_handle* src_h = (const npgpu_handle*)host_device_ptr((void*)handles);
+    const float* src_f = (const float*)host_device_ptr((void*)forces6);
+    const bool direct = src_h && src_f;
     void* hp = nullptr;
     npgpu_status st = stage_reserve(w, hb + fb, &hp);
     if (st != NPGPU_OK) return st;
     void* dp = w->d_stage;
-    if (direct) {
-        CK(cudaMemcpyAsync(dp, handles, hb, cudaMemcpyHostToDevice, w->stream), "force handles");
-        CK(cudaMemcpyAsync((char*)dp + hb, forces6, fb, cudaMemcpyHostToDevice, w->stream), "forces");
-    } else {
+    if (!direct) {
         std::memcpy(hp, handles, hb);
         std::memcpy((char*)hp + hb, forces6, fb);
         st = stage_commit(w, hb + fb, &dp);
@@ -848,10 +857,12 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
         CK(cudaMemsetAsync(w->dw.b.fstamp, 0, sizeof(uint32_t) * w->cap_b, w->stream), "force stamps");
         w->force_batch = 1;
     }
-    const npgpu_handle* dh = (const npgpu_handle*)dp;
-    const float* df = (const float*)((const char*)dp + hb);
+    npgpu_handle* dh = (npgpu_handle*)dp;
+    float* df = (float*)((char*)dp + hb);
     CK(cudaMemsetAsync(&w->ctl->force_flags, 0, sizeof(uint32_t), w->stream), "force flags");
-    CK(launch_force_check(w->dw, dh, df, n, w->force_batch, w->cap_b, w->stream), "force check");
+    CK(launch_force_check(w->dw, direct ? src_h : dh, direct ? src_f : df, dh, df, n, w->force_batch, w->cap_b,
+                          w->stream),
+       "force check");
     CK(cudaMemcpyAsync(w->h_flags, &w->ctl->force_flags, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream),
        "force flags");
     CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
@@ -1164,6 +1175,18 @@ npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, f
     if (n == 0) return NPGPU_OK;
     size_t bytes = (size_t)n * (7 + 6 + 1) * sizeof(float) + n;
     CK(cudaEventSynchronize(w->ev_stage), "staging wait");
+    if (!energy && !active && (position || velocity)) {
+        // Page-locked destinations the device can address: the pack kernel
+        // writes them over the host link itself, with no copy afterwards.
+        float* dpos_h = (float*)host_device_ptr(position);
+        float* dvel_h = (float*)host_device_ptr(velocity);
+        if ((!position || dpos_h) && (!velocity || dvel_h)) {
+            CK(launch_pack_bodies_host(w->dw, first, n, dpos_h, dvel_h, w->stream), "pack bodies");
+            CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+            CK(cudaStreamSynchronize(w->stream), "download");
+            return NPGPU_OK;
+        }
+    }
     if (bytes > w->d_stage_bytes) {
         if (w->d_stage) cudaFree(w->d_stage);
         w->d_stage = nullptr;

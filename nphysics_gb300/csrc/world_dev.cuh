@@ -281,11 +281,16 @@ struct MassUpdate {                  // new local inertia / com of a body
 cudaError_t launch_upload_bodies(const World& w, const BodyUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_upload_colliders(const World& w, const ColliderUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n, cudaStream_t st);
+// Poses (7 floats) and velocities (6) of slots [first, first + n) into
+// page-locked host arrays, given by their device-side addresses.
+cudaError_t launch_pack_bodies_host(const World& w, uint32_t first, uint32_t n, float* pos7, float* vel6,
+                                    cudaStream_t st);
 // Checks a force batch on the device (handles against the slots' generations,
 // finite forces, a body named twice) into ctl->force_flags, which the caller
-// clears first. cap: body slots allocated.
-cudaError_t launch_force_check(const World& w, const npgpu_handle* handles, const float* forces6, uint32_t n,
-                               uint32_t batch, uint64_t cap, cudaStream_t st);
+// clears first, reading it from (handles, forces6) and keeping a copy in
+// (hd, fd) when those differ. cap: body slots allocated.
+cudaError_t launch_force_check(const World& w, const npgpu_handle* handles, const float* forces6, npgpu_handle* hd,
+                               float* fd, uint32_t n, uint32_t batch, uint64_t cap, cudaStream_t st);
 // Adds forces6[k] (linear, angular) to body handles[k].index; `serial`: in
 // order on one thread, for batches that name a body twice.
 cudaError_t launch_forces(const World& w, const npgpu_handle* handles, const float* forces6, uint32_t n, bool wake,
