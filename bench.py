@@ -338,6 +338,10 @@ def run_gpu(args):
     dyn = np.nonzero(sc.bodies["status"] == 2)[0]
     handles = pinned(np.ascontiguousarray(sc.body_handles[dyn]))
     forces = pinned(np.zeros((len(dyn), 6), np.float32))
+    # One untimed pass first: it sizes the world's staging area for this batch.
+    w.apply_forces(handles, forces, wake=False)
+    w.step(1, sync=False)
+    w.download_into(pos, vel)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(args.steps):

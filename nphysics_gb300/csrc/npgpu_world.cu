@@ -222,9 +222,11 @@ static StepParams step_params(const npgpu_world* w) {
 // The pinned host staging area, at least `bytes` long, once earlier uses of
 // it are done; stage_commit then copies its first `bytes` to the device
 // staging area and returns the device pointer.
+// hptr null: only the device area is needed (the host side is read over
+// the link from the caller's page-locked memory).
 static npgpu_status stage_reserve(npgpu_world* w, size_t bytes, void** hptr) {
     CK(cudaEventSynchronize(w->ev_stage), "staging wait");
-    if (bytes > w->h_stage_bytes) {
+    if (hptr && bytes > w->h_stage_bytes) {
         if (w->h_stage) cudaFreeHost(w->h_stage);
         w->h_stage = nullptr;
         size_t nb = std::max(bytes, w->h_stage_bytes * 2);
@@ -238,7 +240,7 @@ static npgpu_status stage_reserve(npgpu_world* w, size_t bytes, void** hptr) {
         CK(cudaMalloc(&w->d_stage, nb), "device staging");
         w->d_stage_bytes = nb;
     }
-    *hptr = w->h_stage;
+    if (hptr) *hptr = w->h_stage;
     return NPGPU_OK;
 }
 
@@ -843,7 +845,7 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
     const float* src_f = (const float*)host_device_ptr((void*)forces6);
     const bool direct = src_h && src_f;
     void* hp = nullptr;
-    npgpu_status st = stage_reserve(w, hb + fb, &hp);
+    npgpu_status st = stage_reserve(w, hb + fb, direct ? nullptr : &hp);
     if (st != NPGPU_OK) return st;
     void* dp = w->d_stage;
     if (!direct) {
