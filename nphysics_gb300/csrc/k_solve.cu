@@ -1108,9 +1108,20 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
 // memories of a thread-block cluster, 2^shift bodies per block, reached
 // through distributed shared memory.
 struct SharedDv {
-    float* base;
-    __device__ __forceinline__ void load(int l, float* o) const { load_dv(base, l, o); }
-    __device__ __forceinline__ void store(int l, const float* o) const { store_dv(base, l, o); }
+    float* base;   // 8-byte aligned: a row is three float2
+    __device__ __forceinline__ void load(int l, float* o) const {
+        if (l < 0) return;
+        const float2* r = (const float2*)(base + 6 * l);
+        const float2 a = r[0], b = r[1], c = r[2];
+        o[0] = a.x; o[1] = a.y; o[2] = b.x; o[3] = b.y; o[4] = c.x; o[5] = c.y;
+    }
+    __device__ __forceinline__ void store(int l, const float* o) const {
+        if (l < 0) return;
+        float2* r = (float2*)(base + 6 * l);
+        r[0] = make_float2(o[0], o[1]);
+        r[1] = make_float2(o[2], o[3]);
+        r[2] = make_float2(o[4], o[5]);
+    }
 };
 struct ClusterDv {
     float* base;
