@@ -66,13 +66,14 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--settle", type=int, default=None,
-                    help="untimed steps first (default: 200 for piles and the pyramid, 60 for batched worlds, "
-                         "0 for the brick walls, whose impact phase is the workload)")
+                    help="untimed steps first (default: 200 for the ball pile and the pyramid, 150 for the mixed "
+                         "pile, 60 for batched worlds, 0 for the brick walls, whose impact phase is the workload)")
     ap.add_argument("--side", type=int, default=32)
-    ap.add_argument("--workload", default="pile", choices=["pile", "batched", "pyramid", "walls"],
+    ap.add_argument("--workload", default="pile", choices=["pile", "batched", "pyramid", "walls", "mixed"],
                     help="pile: the 32^3 ball pile (replicas on N GPUs); batched: --worlds-per-rank worlds "
                          "of the batched-worlds scene per GPU (the batch sharded across ranks); pyramid: the "
-                         "210-box pyramid (replicas); walls: 256 brick walls struck by balls per GPU")
+                         "210-box pyramid (replicas); walls: 256 brick walls struck by balls per GPU; mixed: "
+                         "the 100k pile of balls and cuboids (replicas)")
     ap.add_argument("--worlds-per-rank", type=int, default=4096)
     ap.add_argument("--impl", default="gpu", choices=["gpu", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -86,7 +87,7 @@ def parse():
                     help="skip the iterations-to-1e-4 comparison of the learned and plain warm starts")
     args = ap.parse_args()
     if args.settle is None:
-        args.settle = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0}[args.workload]
+        args.settle = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0, "mixed": 150}[args.workload]
     return args
 
 
@@ -278,6 +279,13 @@ def run_gpu(args):
         w = GpuWorld.for_scene(sc, sc.params())
         workload = ("box pyramid: 210 cuboids of half extent 0.5 in a 20-base triangle on a static ground, "
                     "density 1, friction 0.5, dt 1/60, 8 velocity / 3 position iterations")
+    elif args.workload == "mixed":
+        # Replicas: the 100k mixed pile of balls and cuboids on every rank.
+        sc = scenes.mixed_pile(n=100_000)
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=12)
+        workload = ("mixed pile: 100000 bodies, half balls of radius U(0.2, 0.8), half cuboids of half extents "
+                    "U(0.2, 0.8)^3 at random orientations, density 1, friction 0.5, dropped from a jittered 2.0 "
+                    "lattice onto a static ground, dt 1/60, 8 velocity / 3 position iterations")
     elif args.workload == "walls":
         # Each rank steps its own 256 walls (weak scaling).
         sc = scenes.brick_walls(n_walls=256, seed=1234 + rank)
@@ -386,7 +394,7 @@ def run_gpu(args):
                    "solver_schedule": {1: "one cooperative grid",
                                        2: "per world: a cluster, a block or a warp each"}[tuned[0]],
                    "world_threads": tuned[1],
-                   "parallelism": ("replicas" if args.workload in ("pile", "pyramid")
+                   "parallelism": ("replicas" if args.workload in ("pile", "pyramid", "mixed")
                                    else f"worlds sharded over {world_size} GPUs"),
                    "contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
                    "solver_contacts": int(K), "active_bodies": int(B),
