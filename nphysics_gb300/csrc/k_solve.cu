@@ -953,17 +953,26 @@ struct GlobalRows {
 };
 constexpr int kCacheContacts = 1;
 constexpr int kCacheF4 = kCacheContacts * (1 + kRowsF4);
+// The first kCacheContacts contacts of a manifold from the cache, the rest
+// from global memory.
 struct CachedRows {
     float4* base;
+    GlobalRows g;
     __device__ __forceinline__ float4& at(int e) const { return base[e * (int)blockDim.x]; }
     __device__ __forceinline__ RowRec row(uint32_t k, int r) const {
+        if (k >= (uint32_t)kCacheContacts) return g.row(k, r);
         float4 v[kRowF4];
 #pragma unroll
         for (int e = 0; e < kRowF4; ++e) v[e] = at((int)k * (1 + kRowsF4) + 1 + r * kRowF4 + e);
         return unpack_row(v);
     }
-    __device__ __forceinline__ float4 get_lam(uint32_t k) const { return at((int)k * (1 + kRowsF4)); }
-    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { at((int)k * (1 + kRowsF4)) = v; }
+    __device__ __forceinline__ float4 get_lam(uint32_t k) const {
+        return k < (uint32_t)kCacheContacts ? at((int)k * (1 + kRowsF4)) : g.get_lam(k);
+    }
+    __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const {
+        if (k < (uint32_t)kCacheContacts) at((int)k * (1 + kRowsF4)) = v;
+        else g.set_lam(k, v);
+    }
 };
 
 // The warm start (sor_prox.rs:19-45) of a task without learned starts: the
@@ -1186,7 +1195,7 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
 // Fills the running thread's cache with manifold m's impulses and rows (nc <= kCacheContacts).
 __device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t nc, const CachedRows& cc) {
     const float4* rows = w.s.rows + (size_t)m * kMaxContacts * kRowsF4;
-    for (uint32_t k = 0; k < nc; ++k) {
+    for (uint32_t k = 0; k < nc && k < (uint32_t)kCacheContacts; ++k) {
         cc.at((int)k * (1 + kRowsF4)) = w.s.lam[(size_t)m * kMaxContacts + k];
         for (int e = 0; e < kRowsF4; ++e) cc.at((int)k * (1 + kRowsF4) + 1 + e) = rows[(size_t)k * kRowsF4 + e];
     }
@@ -1245,18 +1254,17 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     MyTasks mt;
     load_tasks(w, ms, mt, s_begin);
-    // For the iterations (not the warm start), the first task's rows and
-    // impulses stay in shared memory for the whole call (the impulses are
-    // written back at the end).
-    const CachedRows cc{cache + threadIdx.x};
+    // For the iterations (not the warm start), the rows and impulses of the
+    // first task's first contact stay in shared memory for the whole call
+    // (the impulses are written back at the end); its other contacts are
+    // read from global memory.
+    const CachedRows cc{cache + threadIdx.x, global_rows(w, t)};
     uint32_t nc0 = 0;
     bool cached = false;
     if (mt.n > 0 && cache != nullptr && s_begin > 0) {
         nc0 = w.s.sm_nc[t];
-        if (nc0 <= (uint32_t)kCacheContacts) {
-            cached = true;
-            cache_task(w, t, nc0, cc);
-        }
+        cached = true;
+        cache_task(w, t, nc0, cc);
     }
     uint32_t left = mt.n * (s_end - s_begin);
     unsigned long long t0 = 0, tw = prof ? global_ns() : 0ull;
@@ -1313,7 +1321,8 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
         }
     }
     if (cached)
-        for (uint32_t k = 0; k < nc0; ++k) w.s.lam[(size_t)t * kMaxContacts + k] = cc.get_lam(k);
+        for (uint32_t k = 0; k < nc0 && k < (uint32_t)kCacheContacts; ++k)
+            w.s.lam[(size_t)t * kMaxContacts + k] = cc.get_lam(k);
     return ok;
 }
 
