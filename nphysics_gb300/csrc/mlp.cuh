@@ -6,7 +6,7 @@
 // perceptron with ReLU hidden layers, bf16 weights and fp32 accumulation. The
 // prediction is checked in the warm-start sweep of the velocity solver: a
 // contact whose predicted start leaves a larger local residual than the zero
-// start falls back to the zero start, so SOR-Prox iterations stay the judge.
+// start falls back to the zero start, so the SOR-Prox iterations decide the result.
 #pragma once
 #include <cstdint>
 #include <cuda_bf16.h>
