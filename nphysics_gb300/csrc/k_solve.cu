@@ -1363,6 +1363,9 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
         if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_TASKS);
         return;
     }
+    // A failed colouring leaves no consistent order to wait on: the step
+    // reports it instead of solving.
+    if (w.ctl->err & ERRF_COLOURS) return;
     const bool prof = p.profile != 0;
     const bool learned = p.warmstart_mode == 2u;
     TaskStats ts{0ull, 0ull, 0ull};
@@ -1597,6 +1600,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
     __shared__ uint32_t s_world;
+    if (w.ctl->err & ERRF_COLOURS) return;   // no consistent colour order to sweep
     const WorldGroup block{threadIdx.x, blockDim.x, GROUP_BLOCK};
     const uint32_t* order = w.s.world_order + n_cluster;
     for (;;) {
@@ -1630,6 +1634,7 @@ template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 1) k_cluster_velocity(World w, StepParams p, uint32_t shift) {
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
+    if (w.ctl->err & ERRF_COLOURS) return;   // every block of every cluster leaves together
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nct = cl.num_blocks(), rank = cl.block_rank();
     const uint32_t wd = w.s.world_order[blockIdx.x / nct];
@@ -1860,6 +1865,7 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParam
         if (t == 0) atomicOr(&w.ctl->err, ERRF_TASKS);
         return;
     }
+    if (w.ctl->err & ERRF_COLOURS) return;
     const uint32_t nsw = p.max_position_iterations;
     MyTasks mt;
     load_tasks(w, ms, mt, 0);
@@ -1926,6 +1932,7 @@ template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big,
                                                             uint32_t n_cluster) {
     __shared__ uint32_t s_world;
+    if (w.ctl->err & ERRF_COLOURS) return;
     const WorldGroup block{threadIdx.x, blockDim.x, GROUP_BLOCK};
     const uint32_t* order = w.s.world_order + n_cluster;
     for (;;) {
@@ -1953,6 +1960,7 @@ __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams 
 // The cluster worlds' position sweeps: cluster c takes world order[c], the
 // cluster barrier between colours (poses stay in global memory).
 __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_position(World w, StepParams p) {
+    if (w.ctl->err & ERRF_COLOURS) return;
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nct = cl.num_blocks();
     const WorldGroup g{cl.block_rank() * blockDim.x + threadIdx.x, nct * blockDim.x, GROUP_CLUSTER};

@@ -79,3 +79,34 @@ def test_capacity_of_slots(gpu_lib):
     with pytest.raises(NpgpuError) as e:
         w.upsert_bodies(h, scenes.body_descs(5))
     assert e.value.status == abi.ERR_CAPACITY
+
+
+@pytest.mark.parametrize("sched", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
+def test_too_many_colours_is_reported(gpu_lib, sched):
+    # 64 balls resting on one dynamic platform give the platform 65 solver
+    # manifolds, more than the 56 colours a step can use: the step reports a
+    # capacity error (the solver kernels stand down at once rather than wait
+    # on an inconsistent order), and the world stays usable.
+    import time
+    from nphysics_gb300.world import GpuWorld, NpgpuError
+    g, gc = scenes._ground()
+    plat = scenes.body_descs(1)
+    plat["position"][0, :3] = (0.0, 0.5, 0.0)
+    pc = scenes.collider_descs(1, 0, abi.SHAPE_CUBOID, (6.0, 0.5, 6.0), density=1.0)
+    b = scenes.body_descs(64)
+    i = np.arange(64)
+    b["position"][:, 0] = (i % 8 - 3.5) * 1.1
+    b["position"][:, 1] = 1.49
+    b["position"][:, 2] = (i // 8 - 3.5) * 1.1
+    bc = scenes.collider_descs(64, np.arange(64), abi.SHAPE_BALL, (0.5, 0, 0), density=1.0)
+    sc = scenes.Scene("platform", *scenes._concat([g, plat, b], [gc, pc, bc]))
+    p = sc.params()
+    p.solver_schedule = sched
+    w = GpuWorld.for_scene(sc, p)
+    t0 = time.perf_counter()
+    with pytest.raises(NpgpuError) as e:
+        w.step(1)
+    assert e.value.status == abi.ERR_CAPACITY
+    assert "colours" in str(e.value)
+    assert time.perf_counter() - t0 < 0.9          # no bounded wait ran out
+    w.synchronize()
