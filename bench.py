@@ -43,7 +43,7 @@ LAUNCHES_PER_STEP = 21
 LAUNCHES_PER_STEP_BATCHED = 26
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_velocity launch on this
 # workload, from one ncu capture.
-VELOCITY_TRAFFIC_PER_LAUNCH = 45916160
+VELOCITY_TRAFFIC_PER_LAUNCH = 45684480
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_world_velocity launch
 # on a 1024-world batch (1 046 697 solver contacts), per solver contact: the
 # batched line scales it by its own solver contacts (the traffic of the
