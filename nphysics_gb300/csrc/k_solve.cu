@@ -116,6 +116,13 @@ __device__ __forceinline__ unsigned long long ld_relaxed64(const unsigned long l
 __device__ __forceinline__ void st_relaxed64(unsigned long long* p, unsigned long long v) {
     asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
+__device__ __forceinline__ void ld_relaxed_v2(const unsigned long long* p, unsigned long long& a,
+                                              unsigned long long& b) {
+    asm volatile("ld.relaxed.gpu.global.v2.u64 {%0, %1}, [%2];" : "=l"(a), "=l"(b) : "l"(p) : "memory");
+}
+__device__ __forceinline__ void st_relaxed_v2(unsigned long long* p, unsigned long long a, unsigned long long b) {
+    asm volatile("st.relaxed.gpu.global.v2.u64 [%0], {%1, %2};" ::"l"(p), "l"(a), "l"(b) : "memory");
+}
 __device__ __forceinline__ bool err_set(const Control* ctl, uint32_t bits) {
     return (ld_acquire(&ctl->err) & bits) != 0;
 }
@@ -454,7 +461,8 @@ __global__ void k_act_init(World w, StepParams p) {
         uint32_t info = b.info[i];
         b.uf_parent[i] = i;
         b.can_deact[i] = 1;
-        b.cw[i] = 0ull;
+        b.cw[2 * i] = 0ull;
+        b.cw[2 * i + 1] = 0ull;
         b.adj_count[i] = 0;
         b.adj_fill[i] = 0;
 #pragma unroll
@@ -680,23 +688,35 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
             int b1 = mb1[k], b2 = mb2[k];
             uint32_t pr = mpr[k];
             uint32_t r1 = pr & 0xffffu, r2 = pr >> 16;
-            // Each body's colour word holds its colour mask and how many of
-            // its manifolds have been coloured: the count is the flag.
-            unsigned long long u1 = b1 >= 0 ? ld_relaxed64(b.cw + b1) : ((unsigned long long)r1 << 56);
-            unsigned long long u2 = b2 >= 0 ? ld_relaxed64(b.cw + b2) : ((unsigned long long)r2 << 56);
-            if ((u1 >> 56) != r1 || (u2 >> 56) != r2) continue;
-            unsigned long long mask = (u1 | u2) & kColourMask;
+            // Each body's two colour words hold its colour mask (colours
+            // 0-55, then 56-111) and, in both, how many of its manifolds have
+            // been coloured: the count is the flag.
+            unsigned long long u1a = (unsigned long long)r1 << 56, u1b = u1a;
+            unsigned long long u2a = (unsigned long long)r2 << 56, u2b = u2a;
+            if (b1 >= 0) ld_relaxed_v2(b.cw + 2 * (size_t)b1, u1a, u1b);
+            if (b2 >= 0) ld_relaxed_v2(b.cw + 2 * (size_t)b2, u2a, u2b);
+            if ((u1a >> 56) != r1 || (u1b >> 56) != r1 || (u2a >> 56) != r2 || (u2b >> 56) != r2) continue;
+            const unsigned long long ma = (u1a | u2a) & kColourMask, mb = (u1b | u2b) & kColourMask;
             uint32_t col;
-            if (mask == kColourMask) {
-                atomicOr(&w.ctl->err, ERRF_COLOURS);
-                col = kColourBits - 1;
+            if (ma != kColourMask) {
+                col = (uint32_t)(__ffsll((long long)~ma) - 1);
+            } else if (mb != kColourMask) {
+                col = (uint32_t)kColourBits + (uint32_t)(__ffsll((long long)~mb) - 1);
             } else {
-                col = (uint32_t)(__ffsll((long long)~mask) - 1);
+                atomicOr(&w.ctl->err, ERRF_COLOURS);
+                col = kStepColours - 1;
             }
             w.s.sm_colour[m] = col;
-            const unsigned long long bit = 1ull << col;
-            if (b1 >= 0) st_relaxed64(b.cw + b1, ((unsigned long long)(r1 + 1u) << 56) | (u1 & kColourMask) | bit);
-            if (b2 >= 0) st_relaxed64(b.cw + b2, ((unsigned long long)(r2 + 1u) << 56) | (u2 & kColourMask) | bit);
+            const unsigned long long bita = col < (uint32_t)kColourBits ? 1ull << col : 0ull;
+            const unsigned long long bitb = col < (uint32_t)kColourBits ? 0ull : 1ull << (col - kColourBits);
+            if (b1 >= 0) {
+                const unsigned long long hi = (unsigned long long)(r1 + 1u) << 56;
+                st_relaxed_v2(b.cw + 2 * (size_t)b1, hi | (u1a & kColourMask) | bita, hi | (u1b & kColourMask) | bitb);
+            }
+            if (b2 >= 0) {
+                const unsigned long long hi = (unsigned long long)(r2 + 1u) << 56;
+                st_relaxed_v2(b.cw + 2 * (size_t)b2, hi | (u2a & kColourMask) | bita, hi | (u2b & kColourMask) | bitb);
+            }
             ncol = col + 1u > ncol ? col + 1u : ncol;
             done |= 1u << k;
             progress = true;
@@ -729,15 +749,21 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
         int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
         // Colour rank and manifold count on each dynamic body.
         uint32_t col = w.s.sm_colour[m];
-        unsigned long long below = (col == 0u) ? 0ull : ((1ull << col) - 1ull);
+        // The colours below col in each of the two words.
+        const unsigned long long below_a =
+            col >= (uint32_t)kColourBits ? kColourMask : ((col == 0u) ? 0ull : ((1ull << col) - 1ull));
+        const unsigned long long below_b =
+            col <= (uint32_t)kColourBits ? 0ull : ((1ull << (col - kColourBits)) - 1ull);
         uint32_t rk = 0;
         if (b1 >= 0) {
-            unsigned long long u = b.cw[b1] & kColourMask;
-            rk |= (uint32_t)__popcll(u & below) | ((uint32_t)__popcll(u) << 8);
+            const unsigned long long ua = b.cw[2 * (size_t)b1] & kColourMask, ub = b.cw[2 * (size_t)b1 + 1] & kColourMask;
+            rk |= (uint32_t)(__popcll(ua & below_a) + __popcll(ub & below_b)) |
+                  ((uint32_t)(__popcll(ua) + __popcll(ub)) << 8);
         }
         if (b2 >= 0) {
-            unsigned long long u = b.cw[b2] & kColourMask;
-            rk |= ((uint32_t)__popcll(u & below) << 16) | ((uint32_t)__popcll(u) << 24);
+            const unsigned long long ua = b.cw[2 * (size_t)b2] & kColourMask, ub = b.cw[2 * (size_t)b2 + 1] & kColourMask;
+            rk |= ((uint32_t)(__popcll(ua & below_a) + __popcll(ub & below_b)) << 16) |
+                  ((uint32_t)(__popcll(ua) + __popcll(ub)) << 24);
         }
         w.s.sm_rk[m] = rk;
         uint32_t nc = w.s.sm_nc[m];

@@ -455,7 +455,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(b.acc_lin, B); A(b.acc_ang, B); A(b.f_lin, B); A(b.f_ang, B);
     A(b.lin_damp, B); A(b.ang_damp, B); A(b.max_lin, B); A(b.max_ang, B); A(b.sleep_thr, B); A(b.energy, B);
     A(b.info, B); A(b.world, B); A(b.gen, B); A(b.fstamp, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.dvf, 8 * (size_t)B); A(b.posef, 12 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
-    A(b.cw, B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B);
+    A(b.cw, 2 * (size_t)B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B);
     Colliders& c = w->dw.c;
     A(c.body, Cn); A(c.info, Cn); A(c.params, Cn); A(c.wrt_t, Cn); A(c.wrt_q, Cn);
     A(c.margin, Cn); A(c.lin_pred, Cn); A(c.friction, Cn); A(c.restitution, Cn); A(c.rank, Cn);
@@ -1091,7 +1091,7 @@ npgpu_status npgpu_synchronize(npgpu_world* w) {
         if (err & ERRF_UNION_FIND) return fail(w, NPGPU_ERR_TIMEOUT, "island union-find did not converge");
         if (err & ERRF_NAN) return fail(w, NPGPU_ERR_NAN, "non-finite body state after the step");
         if (err & ERRF_PAIR_CAPACITY) return fail(w, NPGPU_ERR_CAPACITY, "pair capacity exceeded");
-        if (err & ERRF_COLOURS) return fail(w, NPGPU_ERR_CAPACITY, "more than 56 solver colours needed");
+        if (err & ERRF_COLOURS) return fail(w, NPGPU_ERR_CAPACITY, "more than 112 solver colours needed");
         if (err & ERRF_TASKS)
             return fail(w, NPGPU_ERR_CAPACITY, "more solver manifolds than the cooperative grid holds (16 per thread)");
         if (err & ERRF_WORLD_RANGE) return fail(w, NPGPU_ERR_CUDA, "a solver manifold left its world's slot range");

@@ -45,8 +45,9 @@ enum : uint32_t {
 
 constexpr int kMaxContacts = 4;      // contacts per manifold
 constexpr int kRowFloats = 28;       // J1[6] J2[6] WJ1[6] WJ2[6] r rhs impulse mu
-constexpr int kMaxColours = 64;      // colour buckets of the per-world schedule
-constexpr int kColourBits = 56;      // colours a step may use (the colour word's mask)
+constexpr int kColourBits = 56;      // colours in one colour word's mask
+constexpr int kStepColours = 2 * kColourBits;   // colours a step may use: two words per body
+constexpr int kMaxColours = 128;     // colour buckets of the per-world schedule (>= kStepColours)
 constexpr unsigned long long kColourMask = (1ull << kColourBits) - 1ull;
 constexpr int kLeafCap = 16;        // partners a broad-phase leaf keeps between its two passes
 constexpr int kPosRec = 7 + 4;       // float4 of a manifold's position-solver record
@@ -80,7 +81,8 @@ struct Bodies {
     unsigned long long *posef;       // 12 per body: pose words flagged with the body's update count
     uint32_t *uf_parent;
     int *can_deact;
-    unsigned long long *cw;          // colour word: manifolds coloured so far << 56 | colour mask (56 bits)
+    unsigned long long *cw;          // 2 colour words per body: manifolds coloured so far << 56 | 56 mask bits
+                                     // (colours 0-55 in the first word, 56-111 in the second)
     uint32_t *adj_count, *adj_start, *adj_fill;   // solver manifolds per body (CSR)
 };
 

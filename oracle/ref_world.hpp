@@ -1232,10 +1232,13 @@ public:
     std::vector<int> seq_warm, seq_friction, seq_normal, seq_pos;
     std::vector<Manifold<R>*> solver_manifolds;
 
-    // JP colouring with first-fit colours (the GPU solver's schedule).
+    // JP colouring with first-fit colours (the GPU solver's schedule), at
+    // most kOracleColours colours (the GPU keeps a body's colour mask in two
+    // 56-bit words).
+    static constexpr uint32_t kOracleColours = 112;
     uint32_t colour_manifolds(std::vector<Manifold<R>*>& ms) {
         std::vector<uint64_t> best(bodies.size(), 0);
-        std::vector<uint64_t> used(bodies.size(), 0);
+        std::vector<uint64_t> used(2 * bodies.size(), 0);   // colours 0-63 and 64-127 of each body
         std::vector<Manifold<R>*> todo = ms;
         uint32_t ncol = 0;
         while (!todo.empty()) {
@@ -1254,15 +1257,17 @@ public:
             }
             for (Manifold<R>* m : won) {
                 uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
-                uint64_t mask = 0;
-                if (bodies[b1].dynamic()) mask |= used[b1];
-                if (bodies[b2].dynamic()) mask |= used[b2];
+                uint64_t mask[2] = {0, 0};
+                for (int h = 0; h < 2; ++h) {
+                    if (bodies[b1].dynamic()) mask[h] |= used[2 * b1 + h];
+                    if (bodies[b2].dynamic()) mask[h] |= used[2 * b2 + h];
+                }
                 uint32_t c = 0;
-                while (c < 56 && (mask >> c) & 1u) ++c;
+                while (c < kOracleColours && (mask[c >> 6] >> (c & 63u)) & 1u) ++c;
                 m->colour = c;
-                if (c >= 56) continue;
-                if (bodies[b1].dynamic()) used[b1] |= (uint64_t(1) << c);
-                if (bodies[b2].dynamic()) used[b2] |= (uint64_t(1) << c);
+                if (c >= kOracleColours) continue;
+                if (bodies[b1].dynamic()) used[2 * b1 + (c >> 6)] |= (uint64_t(1) << (c & 63u));
+                if (bodies[b2].dynamic()) used[2 * b2 + (c >> 6)] |= (uint64_t(1) << (c & 63u));
                 ncol = std::max(ncol, c + 1);
             }
             for (Manifold<R>* m : todo) {
@@ -1301,7 +1306,7 @@ public:
         std::vector<Manifold<R>*> seq = solver_manifolds;
         if (order == ORDER_COLOUR) {
             num_colours = colour_manifolds(seq);
-            if (std::any_of(seq.begin(), seq.end(), [](Manifold<R>* m) { return m->colour >= 56; })) {
+            if (std::any_of(seq.begin(), seq.end(), [](Manifold<R>* m) { return m->colour >= kOracleColours; })) {
                 last_error = "colour overflow";
                 return false;
             }

@@ -81,25 +81,53 @@ def test_capacity_of_slots(gpu_lib):
     assert e.value.status == abi.ERR_CAPACITY
 
 
-@pytest.mark.parametrize("sched", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
-def test_too_many_colours_is_reported(gpu_lib, sched):
-    # 64 balls resting on one dynamic platform give the platform 65 solver
-    # manifolds, more than the 56 colours a step can use: the step reports a
-    # capacity error (the solver kernels stand down at once rather than wait
-    # on an inconsistent order), and the world stays usable.
-    import time
-    from nphysics_gb300.world import GpuWorld, NpgpuError
+def platform_scene(side):
+    """side x side balls resting on one dynamic platform on the ground: the
+    platform takes part in side^2 + 1 solver manifolds, so it needs as many
+    colours."""
     g, gc = scenes._ground()
     plat = scenes.body_descs(1)
     plat["position"][0, :3] = (0.0, 0.5, 0.0)
     pc = scenes.collider_descs(1, 0, abi.SHAPE_CUBOID, (6.0, 0.5, 6.0), density=1.0)
-    b = scenes.body_descs(64)
-    i = np.arange(64)
-    b["position"][:, 0] = (i % 8 - 3.5) * 1.1
+    n = side * side
+    b = scenes.body_descs(n)
+    i = np.arange(n)
+    b["position"][:, 0] = (i % side - (side - 1) / 2) * 1.05
     b["position"][:, 1] = 1.49
-    b["position"][:, 2] = (i // 8 - 3.5) * 1.1
-    bc = scenes.collider_descs(64, np.arange(64), abi.SHAPE_BALL, (0.5, 0, 0), density=1.0)
-    sc = scenes.Scene("platform", *scenes._concat([g, plat, b], [gc, pc, bc]))
+    b["position"][:, 2] = (i // side - (side - 1) / 2) * 1.05
+    bc = scenes.collider_descs(n, np.arange(n), abi.SHAPE_BALL, (0.5, 0, 0), density=1.0)
+    return scenes.Scene("platform", *scenes._concat([g, plat, b], [gc, pc, bc]))
+
+
+@pytest.mark.parametrize("sched", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
+def test_more_than_56_colours_match_the_oracle(gpu_lib, sched):
+    # 64 balls on the platform: 65 colours, past one colour word; the second
+    # word carries colours 56-111 and the bits still match the oracle.
+    from nphysics_gb300.world import GpuWorld
+    from oracle.oracle_py import ORDER_COLOUR, OracleWorld
+    sc = platform_scene(8)
+    p = sc.params()
+    p.solver_schedule = sched
+    g = GpuWorld.for_scene(sc, p)
+    o = OracleWorld(p, sc.gravity, precision=32, order=ORDER_COLOUR)
+    o.load_scene(sc)
+    g.step(5)
+    o.step(5)
+    assert g.counters()["num_colours"] > 56
+    gb, ob = g.bodies(), o.bodies()
+    np.testing.assert_array_equal(gb["position"], ob["position"])
+    np.testing.assert_array_equal(gb["velocity"], ob["velocity"])
+
+
+@pytest.mark.parametrize("sched", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
+def test_too_many_colours_is_reported(gpu_lib, sched):
+    # 121 balls give the platform 122 solver manifolds, more than the 112
+    # colours a step can use: the step reports a capacity error (the solver
+    # kernels stand down at once rather than wait on an inconsistent order),
+    # and the world stays usable.
+    import time
+    from nphysics_gb300.world import GpuWorld, NpgpuError
+    sc = platform_scene(11)
     p = sc.params()
     p.solver_schedule = sched
     w = GpuWorld.for_scene(sc, p)
