@@ -280,6 +280,7 @@ public:
     std::string last_error;
     bool cd_dirty = true;
     uint32_t num_colours = 0;
+    uint32_t num_solver_contacts = 0;   // contacts the last solve took, counted when they were collected
 
     World(const npgpu_params& p, const float g[3]) : params(p) {
         gravity = v3<R>(R(g[0]), R(g[1]), R(g[2]));
@@ -1302,6 +1303,8 @@ public:
                 solver_manifolds.push_back(&m);
             }
         }
+        num_solver_contacts = 0;
+        for (const Manifold<R>* m : solver_manifolds) num_solver_contacts += uint32_t(m->contacts.size());
         num_colours = 0;
         std::vector<Manifold<R>*> seq = solver_manifolds;
         if (order == ORDER_COLOUR) {
@@ -1627,13 +1630,12 @@ public:
     }
 
     void fill_counters() {
-        uint32_t nm = 0, nc = 0, nsc = 0, na = 0;
+        uint32_t nm = 0, nc = 0, na = 0;
         double maxpen = -1e30, ke = 0;
         for (auto& kv : manifolds) {
             const Manifold<R>& m = kv.second;
             if (!m.contacts.empty()) ++nm;
             nc += uint32_t(m.contacts.size());
-            if (m.in_solver) nsc += uint32_t(m.contacts.size());
             for (auto& k : m.contacts)
                 maxpen = std::max(maxpen, double(k.g.depth) + double(colliders[m.c1].margin) + double(colliders[m.c2].margin));
         }
@@ -1649,8 +1651,8 @@ public:
         counters.num_pairs = uint32_t(pairs.size());
         counters.num_manifolds = nm;
         counters.num_contacts = nc;
-        counters.num_solver_contacts = nsc;
-        counters.num_constraints = 3 * nsc;
+        counters.num_solver_contacts = num_solver_contacts;
+        counters.num_constraints = 3 * num_solver_contacts;
         counters.num_colours = num_colours;
         counters.num_active_bodies = na;
         counters.max_penetration = nc ? maxpen : 0.0;

@@ -190,3 +190,177 @@ def test_sweep_and_prune_equals_brute_force():
     b = w.brute_force_pairs()
     assert len(a) > 100
     np.testing.assert_array_equal(a, b)
+
+
+def _no_gravity(sc):
+    sc.bodies["flags"] = sc.bodies["flags"] & np.uint32(0xffffffff ^ abi.BODY_GRAVITY)
+    return sc
+
+
+F32_DT = float(np.float32(1.0 / 60.0))
+F32_G = float(np.float32(9.81))
+
+
+def test_damping_follows_the_integrate_recurrence():
+    # RigidBody::integrate (rigid_body.rs:467-469, 503-504): each step v *= 1 / (1 + dt d),
+    # then the pose moves by v dt. A free ball without gravity: nothing else acts on it.
+    sc = _no_gravity(scenes.single_body(shape=abi.SHAPE_BALL, params=(0.5, 0, 0), position=(0, 100, 0),
+                                        velocity=(3.0, 0, 0, 0, 0, 2.0), ground=False))
+    sc.bodies["linear_damping"] = 0.5
+    sc.bodies["angular_damping"] = 0.25
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    n = 30
+    w.step(n)
+    v, x, om, th = 3.0, 0.0, 2.0, 0.0
+    for _ in range(n):
+        v *= 1.0 / (1.0 + F32_DT * 0.5)
+        om *= 1.0 / (1.0 + F32_DT * 0.25)
+        x += v * F32_DT
+        th += om * F32_DT
+    b = w.bodies()
+    assert abs(b["velocity"][0, 0] - v) < 1e-12
+    assert abs(b["velocity"][0, 5] - om) < 1e-12
+    assert abs(b["position"][0, 0] - x) < 1e-12
+    q = b["position"][0, 3:7]            # (i, j, k, w): a rotation by th about z
+    assert abs(abs(q[2]) - math.sin(th / 2)) < 1e-9 and abs(abs(q[3]) - math.cos(th / 2)) < 1e-9
+    assert abs(q[0]) < 1e-12 and abs(q[1]) < 1e-12
+
+
+@pytest.mark.parametrize("max_lin,max_ang", [(2.0, 1.0), (0.0, 0.0), (10.0, 10.0)])
+def test_velocity_clamps_scale_to_the_maximum(max_lin, max_ang):
+    # rigid_body.rs:471-501: a velocity whose norm is above the maximum is scaled to it; a zero
+    # maximum zeroes it; below the maximum nothing changes.
+    sc = _no_gravity(scenes.single_body(shape=abi.SHAPE_BALL, params=(0.5, 0, 0), position=(0, 100, 0),
+                                        velocity=(3.0, 4.0, 0, 0, 0, 5.0), ground=False))
+    sc.bodies["max_linear_velocity"] = max_lin
+    sc.bodies["max_angular_velocity"] = max_ang
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(1)
+    b = w.bodies()
+    lin = np.array([3.0, 4.0, 0.0]) * min(1.0, max_lin / 5.0)
+    ang = np.array([0.0, 0.0, 5.0]) * min(1.0, max_ang / 5.0)
+    np.testing.assert_allclose(b["velocity"][0, :3], lin, atol=1e-12)
+    np.testing.assert_allclose(b["velocity"][0, 3:], ang, atol=1e-12)
+    np.testing.assert_allclose(b["position"][0, :3], np.array([0.0, 100.0, 0.0]) + lin * F32_DT, atol=1e-12)
+
+
+def test_kinematic_body_keeps_its_velocity_through_contacts():
+    # A kinematic box pushes a dynamic ball along the ground: gravity and the contact leave the
+    # kinematic body's velocity alone, its pose advances by v dt each step, and the ball is pushed.
+    parts_b, parts_c = [], []
+    g, gc = scenes._ground()
+    kb = scenes.body_descs(1)
+    kb["status"] = abi.BODY_KINEMATIC
+    kb["position"][0, :3] = (0.0, 0.5, 0.0)
+    kb["velocity"][0, :3] = (1.0, 0.0, 0.0)
+    kc = scenes.collider_descs(1, 0, abi.SHAPE_CUBOID, (0.5, 0.5, 0.5), density=1.0)
+    bb = scenes.body_descs(1)
+    bb["position"][0, :3] = (1.6, 0.5, 0.0)
+    bc = scenes.collider_descs(1, 0, abi.SHAPE_BALL, (0.5, 0, 0), density=1.0)
+    bodies, colliders = scenes._concat([g, kb, bb], [gc, kc, bc])
+    sc = scenes.Scene("kinematic pusher", bodies, colliders)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    n = 90
+    w.step(n)
+    x = 0.0
+    for _ in range(n):
+        x += 1.0 * F32_DT
+    b = w.bodies()
+    np.testing.assert_array_equal(b["velocity"][1], [1.0, 0, 0, 0, 0, 0])
+    assert abs(b["position"][1, 0] - x) < 1e-12 and b["position"][1, 1] == np.float32(0.5)
+    assert b["position"][2, 0] > 1.6 + 0.3          # the ball was pushed ahead of the box
+    assert b["position"][2, 0] >= b["position"][1, 0] + 1.0 - 0.02 - 1e-3
+
+
+def test_locked_translation_axis_does_not_move():
+    # update_acceleration / the velocity update mask by jacobian_mask (rigid_body.rs:590-619):
+    # with Y locked gravity does not move the body; the free X axis keeps its velocity.
+    sc = scenes.single_body(shape=abi.SHAPE_BALL, params=(0.5, 0, 0), position=(0, 5, 0),
+                            velocity=(1.0, 0, 0, 0, 0, 0))
+    sc.bodies["flags"][1] |= np.uint32(abi.BODY_LOCK_TY)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    n = 60
+    w.step(n)
+    x = 0.0
+    for _ in range(n):
+        x += 1.0 * F32_DT
+    b = w.bodies()
+    assert b["position"][1, 1] == 5.0 and b["velocity"][1, 1] == 0.0
+    assert abs(b["position"][1, 0] - x) < 1e-12 and b["velocity"][1, 0] == 1.0
+
+
+A, MN, MU, MX = abi.COMBINE_AVERAGE, abi.COMBINE_MIN, abi.COMBINE_MULTIPLY, abi.COMBINE_MAX
+
+
+def _combine(a, b):
+    """MaterialCombineMode::combine (material.rs:66-87): the mode of higher precedence wins."""
+    modes = (a[1], b[1])
+    if MX in modes:
+        return max(a[0], b[0])
+    if MU in modes:
+        return a[0] * b[0]
+    if MN in modes:
+        return min(a[0], b[0])
+    return (a[0] + b[0]) * 0.5
+
+
+@pytest.mark.parametrize("speed,e_ball,m_ball,e_ground,m_ground,e", [
+    (5.0, 1.0, A, 1.0, A, 1.0),
+    (5.0, 1.0, A, 0.0, A, 0.5),      # Average
+    (5.0, 0.8, MX, 0.2, A, 0.8),     # Max over Average
+    (5.0, 0.8, MU, 0.5, MN, 0.4),    # Multiply over Min
+    (5.0, 0.8, MN, 0.2, A, 0.2),     # Min over Average
+    (5.0, 0.2, A, 0.8, MX, 0.8),     # either side's mode counts
+    (0.5, 1.0, A, 1.0, A, 1.0),      # below restitution_velocity_threshold: no bounce (vy = 0)
+])
+def test_restitution_and_its_combine_rule(speed, e_ball, m_ball, e_ground, m_ground, e):
+    # signorini_model.rs:94-97: if rhs <= -threshold then rhs += e rhs, e combined by
+    # MaterialCombineMode::combine (material.rs:66-87: Max > Multiply > Min > Average). A ball
+    # touching the ground (gap = the two margins, so no speculative term) hits it at `speed`;
+    # solved to convergence, it leaves at e times its approach speed, gravity's dt g included.
+    sc = scenes.single_body(shape=abi.SHAPE_BALL, params=(0.5, 0, 0), position=(0, 0.52, 0),
+                            velocity=(0, -speed, 0, 0, 0, 0))
+    c = sc.colliders
+    c["restitution"][1], c["restitution_combine"][1] = e_ball, m_ball
+    c["restitution"][0], c["restitution_combine"][0] = e_ground, m_ground
+    p = sc.params()
+    p.solve_to_tolerance = 1
+    p.residual_tolerance = 1e-12
+    p.max_iterations_to_tolerance = 200
+    w = OracleWorld(p, sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(1)
+    vy = w.bodies()["velocity"][1, 1]
+    approach = speed + F32_G * F32_DT
+    # The descriptors carry f32: combine the f32-rounded coefficients.
+    ec = _combine((float(np.float32(e_ball)), m_ball), (float(np.float32(e_ground)), m_ground))
+    assert abs(ec - e) < 1e-7
+    if speed + F32_G * F32_DT < 1.0:
+        ec = 0.0
+    assert abs(vy - ec * approach) < 1e-9, (vy, ec * approach)
+
+
+@pytest.mark.parametrize("mu_box,m_box,mu_ground,m_ground,mu", [
+    (0.2, MU, 0.6, A, 0.12),
+    (0.2, A, 0.6, MN, 0.2),
+    (0.2, MX, 0.6, A, 0.6),
+    (0.2, A, 0.6, A, 0.4),
+])
+def test_friction_combine_rule_sets_the_deceleration(mu_box, m_box, mu_ground, m_ground, mu):
+    sc = scenes.single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 0.5, 0),
+                            velocity=(3.0, 0, 0, 0, 0, 0))
+    c = sc.colliders
+    c["friction"][1], c["friction_combine"][1] = mu_box, m_box
+    c["friction"][0], c["friction_combine"][0] = mu_ground, m_ground
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(5)
+    v5 = w.bodies()["velocity"][1, 0]
+    w.step(1)
+    v6 = w.bodies()["velocity"][1, 0]
+    decel = (v5 - v6) / F32_DT
+    assert abs(decel - mu * F32_G) < 0.05 * mu * F32_G, (decel, mu * F32_G)
