@@ -413,20 +413,45 @@ __device__ __forceinline__ void store_dv(float* dvg, int i, const float* o) {
     for (int k = 0; k < 6; ++k) dvg[6 * i + k] = o[k];
 }
 
+// J dv + rhs of a residual row as the unevaluated sum s + c of two floats:
+// the compensated dot product Dot2 of Ogita, Rump and Oishi ("Accurate sum
+// and dot product", SIAM J. Sci. Comput. 26(6), 2005). Each product is split
+// exactly by a fused multiply-add (Dekker's TwoProduct), each running sum by
+// Knuth's TwoSum, and the error terms are summed on the side; the result is
+// as accurate as the sum evaluated in twice the f32 precision. The row's
+// arithmetic so stays on the f32 pipes, and only the residual's reduction
+// runs in FP64 (issued on GB300 at a small fraction of the f32 rate).
+struct Dot2 {
+    float s = 0.0f, c = 0.0f;
+    __device__ __forceinline__ void sum(float h, float e) {
+        const float t = __fadd_rn(s, h);
+        const float z = __fsub_rn(t, s);
+        const float q = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(h, z));
+        s = t;
+        c = __fadd_rn(c, __fadd_rn(q, e));
+    }
+    __device__ __forceinline__ void prod(float x, float y) {
+        const float h = __fmul_rn(x, y);
+        sum(h, __fmaf_rn(x, y, -h));
+    }
+    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
+};
+
 __device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, uint32_t mask, float r, float rhs,
                                              float lam_f, const DV& dv, bool has1, bool has2, bool friction,
                                              double normal_impulse, float mu, double& s2, double& l2) {
-    double d = 0.0;
+    Dot2 acc;
     float J[6];
     if (has1) {
         side_j(pos1, dir, mask & 0x3fu, J);
-        for (int k = 0; k < 6; ++k) d += (double)J[k] * (double)dv.a[k];
+        for (int k = 0; k < 6; ++k) acc.prod(J[k], dv.a[k]);
     }
     if (has2) {
         side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J);
-        for (int k = 0; k < 6; ++k) d += (double)J[k] * (double)dv.b[k];
+        for (int k = 0; k < 6; ++k) acc.prod(J[k], dv.b[k]);
     }
-    d += (double)rhs;
+    acc.sum(rhs, 0.0f);
+    const double d = acc.value();
     double lam = (double)lam_f;
     double x = lam - (double)r * d;
     double p;

@@ -26,6 +26,7 @@
 #include <cfloat>
 #include <limits>
 #include <map>
+#include <type_traits>
 #include <string>
 #include <vector>
 #include <algorithm>
@@ -1467,16 +1468,45 @@ public:
         r.impulse = ni;
         axpy(r, dl);
     }
-    // FP64 complementarity residual: ||lambda - proj(lambda - r (J dv + rhs))|| / max(1, ||lambda||).
-    double residual() const {
-        double s2 = 0, l2 = 0;
-        for (const Row<R>& r : rows) {
+    // J dv + rhs of a row, for the residual. f32: the compensated dot product
+    // Dot2 of Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26(6), 2005) as the
+    // unevaluated float sum s + c (TwoProduct by a fused multiply-add, TwoSum,
+    // error terms summed on the side), as accurate as a sum in twice the f32
+    // precision; f64: plain sums.
+    double residual_dot(const Row<R>& r) const {
+        if constexpr (std::is_same<R, float>::value) {
+            float s = 0.0f, c = 0.0f;
+            auto sum = [&](float h, float e) {
+                float t = s + h;
+                float z = t - s;
+                float q = (s - (t - z)) + (h - z);
+                s = t;
+                c = c + (q + e);
+            };
+            auto prod = [&](float x, float y) {
+                float h = x * y;
+                sum(h, std::fma(x, y, -h));
+            };
+            if (r.b1 >= 0)
+                for (int k = 0; k < 6; ++k) prod(r.J1[k], dv[6 * r.b1 + k]);
+            if (r.b2 >= 0)
+                for (int k = 0; k < 6; ++k) prod(r.J2[k], dv[6 * r.b2 + k]);
+            sum(r.rhs, 0.0f);
+            return double(s) + double(c);
+        } else {
             double d = 0;
             if (r.b1 >= 0)
                 for (int k = 0; k < 6; ++k) d += double(r.J1[k]) * double(dv[6 * r.b1 + k]);
             if (r.b2 >= 0)
                 for (int k = 0; k < 6; ++k) d += double(r.J2[k]) * double(dv[6 * r.b2 + k]);
-            d += double(r.rhs);
+            return d + double(r.rhs);
+        }
+    }
+    // FP64 complementarity residual: ||lambda - proj(lambda - r (J dv + rhs))|| / max(1, ||lambda||).
+    double residual() const {
+        double s2 = 0, l2 = 0;
+        for (const Row<R>& r : rows) {
+            const double d = residual_dot(r);
             double lam = double(r.impulse);
             double x = lam - double(r.r) * d;
             double p;
