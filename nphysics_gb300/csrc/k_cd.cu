@@ -393,7 +393,9 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
     }
     np::Q bq = q4(w.b.pos_q[c.body[c1]]);
     int nc = nk > kMaxContacts ? kMaxContacts : nk;
-    double maxpen = -1e300;
+    // The deepest contact, in f32: the penetration depth + m1 + m2 (in FP64)
+    // rises with the depth, and the margins are the manifold's.
+    float maxdepth = -INFINITY;
     for (int k = 0; k < nc; ++k) {
         const Cand& cd = out.c[keep[k]];
         uint32_t key = uint32_t(cd.f1 * 26 + cd.f2);
@@ -411,13 +413,13 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
         w.cur.n[slot] = f4(cd.g.n);
         w.cur.imp[slot] = imp;
         w.cur.nl[slot] = f4(np::qrot_inv(bq, cd.g.n));
-        double pen = (double)cd.g.depth + (double)m1 + (double)m2;
-        maxpen = pen > maxpen ? pen : maxpen;
+        maxdepth = cd.g.depth > maxdepth ? cd.g.depth : maxdepth;
     }
     w.cur.ncont[p] = (uint8_t)nc;
     if (nc > 0) {
         tot.contacts += (uint32_t)nc;
         tot.manifolds += 1u;
+        const double maxpen = maxdepth == -INFINITY ? -1e300 : (double)maxdepth + (double)m1 + (double)m2;
         const unsigned long long pb = order_bits(maxpen);
         tot.pen_bits = pb > tot.pen_bits ? pb : tot.pen_bits;
     }

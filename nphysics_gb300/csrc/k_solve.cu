@@ -413,57 +413,104 @@ __device__ __forceinline__ void store_dv(float* dvg, int i, const float* o) {
     for (int k = 0; k < 6; ++k) dvg[6 * i + k] = o[k];
 }
 
-// J dv + rhs of a residual row as the unevaluated sum s + c of two floats:
-// the compensated dot product Dot2 of Ogita, Rump and Oishi ("Accurate sum
-// and dot product", SIAM J. Sci. Comput. 26(6), 2005). Each product is split
-// exactly by a fused multiply-add (Dekker's TwoProduct), each running sum by
-// Knuth's TwoSum, and the error terms are summed on the side; the result is
-// as accurate as the sum evaluated in twice the f32 precision. The row's
-// arithmetic so stays on the f32 pipes, and only the residual's reduction
-// runs in FP64 (issued on GB300 at a small fraction of the f32 rate).
+// The FP64 residual's rows in float-float arithmetic: a value is the
+// unevaluated sum hi + lo of two floats, built from the error-free
+// transformations TwoSum (Knuth), FastTwoSum and TwoProduct by a fused
+// multiply-add (Dekker), which carry about twice the f32 precision. J dv + rhs
+// is the compensated dot product Dot2 of Ogita, Rump and Oishi ("Accurate sum
+// and dot product", SIAM J. Sci. Comput. 26(6), 2005). A thread sums its rows'
+// phi^2 and lambda^2 the same way and widens them to double once; the
+// reduction across threads is FP64. The rows' arithmetic so stays on the f32
+// pipes (GB300 issues FP64 at a small fraction of the f32 rate).
+struct FF {
+    float hi, lo;
+};
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float z = __fsub_rn(s, a);
+    return {s, __fadd_rn(__fsub_rn(a, __fsub_rn(s, z)), __fsub_rn(b, z))};
+}
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {   // |a| >= |b| or a == 0
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+__device__ __forceinline__ FF ff_norm(FF a) {
+    return two_sum(a.hi, a.lo);
+}
+__device__ __forceinline__ bool ff_less(FF a, FF b) {
+    return a.hi < b.hi || (a.hi == b.hi && a.lo < b.lo);
+}
+// a + b for normalised a, b.
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    FF s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+// a^2 for normalised a.
+__device__ __forceinline__ FF ff_sq(FF a) {
+    FF p = two_prod(a.hi, a.hi);
+    return fast_two_sum(p.hi, __fadd_rn(p.lo, __fmul_rn(2.0f, __fmul_rn(a.hi, a.lo))));
+}
+// Per-thread sums of phi^2 and lambda^2.
+struct ResidualSums {
+    FF s2{0.0f, 0.0f}, l2{0.0f, 0.0f};
+    __device__ __forceinline__ double phi2() const { return (double)s2.hi + (double)s2.lo; }
+    __device__ __forceinline__ double lam2() const { return (double)l2.hi + (double)l2.lo; }
+};
 struct Dot2 {
     float s = 0.0f, c = 0.0f;
     __device__ __forceinline__ void sum(float h, float e) {
-        const float t = __fadd_rn(s, h);
-        const float z = __fsub_rn(t, s);
-        const float q = __fadd_rn(__fsub_rn(s, __fsub_rn(t, z)), __fsub_rn(h, z));
-        s = t;
-        c = __fadd_rn(c, __fadd_rn(q, e));
+        const FF t = two_sum(s, h);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
     }
     __device__ __forceinline__ void prod(float x, float y) {
-        const float h = __fmul_rn(x, y);
-        sum(h, __fmaf_rn(x, y, -h));
+        const FF p = two_prod(x, y);
+        sum(p.hi, p.lo);
     }
-    __device__ __forceinline__ double value() const { return (double)s + (double)c; }
 };
 
+// phi = lambda - proj(lambda - r (J dv + rhs)) of one row, squared and summed
+// with lambda^2 into `acc`; proj = max(., 0) for a normal row and the clamp
+// to +-mu lambda_n for a friction row.
 __device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, uint32_t mask, float r, float rhs,
-                                             float lam_f, const DV& dv, bool has1, bool has2, bool friction,
-                                             double normal_impulse, float mu, double& s2, double& l2) {
-    Dot2 acc;
+                                             float lam, const DV& dv, bool has1, bool has2, bool friction,
+                                             float normal_impulse, float mu, ResidualSums& acc) {
+    Dot2 dot;
     float J[6];
     if (has1) {
         side_j(pos1, dir, mask & 0x3fu, J);
-        for (int k = 0; k < 6; ++k) acc.prod(J[k], dv.a[k]);
+        for (int k = 0; k < 6; ++k) dot.prod(J[k], dv.a[k]);
     }
     if (has2) {
         side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J);
-        for (int k = 0; k < 6; ++k) acc.prod(J[k], dv.b[k]);
+        for (int k = 0; k < 6; ++k) dot.prod(J[k], dv.b[k]);
     }
-    acc.sum(rhs, 0.0f);
-    const double d = acc.value();
-    double lam = (double)lam_f;
-    double x = lam - (double)r * d;
-    double p;
+    dot.sum(rhs, 0.0f);
+    const FF d = two_sum(dot.s, dot.c);
+    // rd = r d; x = lambda - rd; lambda - x = rd when the projection keeps x.
+    FF rd = two_prod(r, d.hi);
+    rd = fast_two_sum(rd.hi, __fadd_rn(rd.lo, __fmul_rn(r, d.lo)));
+    FF x = two_sum(lam, -rd.hi);
+    x = ff_norm(FF{x.hi, __fsub_rn(x.lo, rd.lo)});
+    FF phi = rd;
     if (!friction) {
-        p = x > 0.0 ? x : 0.0;
+        if (!(x.hi > 0.0f || (x.hi == 0.0f && x.lo > 0.0f))) phi = FF{lam, 0.0f};
     } else {
-        double mx = (double)mu * normal_impulse;
-        p = x < -mx ? -mx : (x > mx ? mx : x);
+        const FF mx = two_prod(mu, normal_impulse);
+        if (ff_less(x, FF{-mx.hi, -mx.lo})) {
+            FF t = two_sum(lam, mx.hi);
+            phi = ff_norm(FF{t.hi, __fadd_rn(t.lo, mx.lo)});
+        } else if (ff_less(mx, x)) {
+            FF t = two_sum(lam, -mx.hi);
+            phi = ff_norm(FF{t.hi, __fsub_rn(t.lo, mx.lo)});
+        }
     }
-    double phi = lam - p;
-    s2 += phi * phi;
-    l2 += lam * lam;
+    acc.s2 = ff_add(acc.s2, ff_sq(phi));
+    acc.l2 = ff_add(acc.l2, two_prod(lam, lam));
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -1254,8 +1301,8 @@ __device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t 
 
 // FP64 residual terms of one manifold (normal rows, then friction rows with
 // the normal impulse as the limit).
-__device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, int g1, int g2, const DV& dv, double& s2,
-                                                  double& l2) {
+__device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, int g1, int g2, const DV& dv,
+                                                  ResidualSums& acc) {
     const bool h1 = g1 >= 0, h2 = g2 >= 0;
     const uint32_t nc = w.s.sm_nc[m], mask = w.s.sm_mask[m];
     const float4* lam = w.s.lam + (size_t)m * kMaxContacts;
@@ -1265,9 +1312,9 @@ __device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, in
         float4 l = lam[k];
         const float4 ta = w.s.tan[((size_t)m * kMaxContacts + k) * 2], tb = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
         const np::V t[2] = {np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
-        residual_row(np::neg(c.n), c.pos1, c.pos2, mask, c.r[0], c.rhs[0], l.x, dv, h1, h2, false, 0.0, c.mu, s2, l2);
-        residual_row(t[0], c.pos1, c.pos2, mask, c.r[1], c.rhs[1], l.y, dv, h1, h2, true, (double)l.x, c.mu, s2, l2);
-        residual_row(t[1], c.pos1, c.pos2, mask, c.r[2], c.rhs[2], l.z, dv, h1, h2, true, (double)l.x, c.mu, s2, l2);
+        residual_row(np::neg(c.n), c.pos1, c.pos2, mask, c.r[0], c.rhs[0], l.x, dv, h1, h2, false, 0.0f, c.mu, acc);
+        residual_row(t[0], c.pos1, c.pos2, mask, c.r[1], c.rhs[1], l.y, dv, h1, h2, true, l.x, c.mu, acc);
+        residual_row(t[1], c.pos1, c.pos2, mask, c.r[2], c.rhs[2], l.z, dv, h1, h2, true, l.x, c.mu, acc);
     }
 }
 
@@ -1379,16 +1426,16 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
 
 // FP64 residual over all rows; the result lands in ctl->residual.
 __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t& epoch, bool initial) {
-    double s2 = 0.0, l2 = 0.0;
+    ResidualSums acc;
     GRID_FOR(m, ms) {
         int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
         DV dv;
         load_dvf(w.b.dvf, b1, dv.a);
         load_dvf(w.b.dvf, b2, dv.b);
-        manifold_residual(w, m, b1, b2, dv, s2, l2);
+        manifold_residual(w, m, b1, b2, dv, acc);
     }
-    double ts = block_sum(s2, sh);
-    double tl = block_sum(l2, sh);
+    double ts = block_sum(acc.phi2(), sh);
+    double tl = block_sum(acc.lam2(), sh);
     if (threadIdx.x == 0) {
         atomicAdd(&w.ctl->res_acc[0], ts);
         atomicAdd(&w.ctl->res_acc[1], tl);
@@ -1580,15 +1627,16 @@ template <class DvA>
 __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint32_t base, uint32_t nbw,
                                                const DvA& dva, double* sh, double* acc, const WorldGroup& g) {
     uint32_t lo = w.s.bucket_start[wd * kMaxColours], hi = w.s.bucket_start[wd * kMaxColours + kMaxColours];
-    double s2 = 0.0, l2 = 0.0;
+    ResidualSums rs;
     for (uint32_t m = lo + g.lane; m < hi; m += g.width) {
         int b1, b2;
         if (!world_locals(w, m, base, nbw, b1, b2)) continue;
         DV dv;
         dva.load(b1, dv.a);
         dva.load(b2, dv.b);
-        manifold_residual(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, s2, l2);
+        manifold_residual(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, rs);
     }
+    double s2 = rs.phi2(), l2 = rs.lam2();
     double ts, tl;
     if (g.warp()) {
         for (int o = 16; o > 0; o >>= 1) {
