@@ -45,10 +45,10 @@ LAUNCHES_PER_STEP_BATCHED = 26
 # workload, from one ncu capture.
 VELOCITY_TRAFFIC_PER_LAUNCH = 45684480
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_world_velocity launch
-# on a 1024-world batch (1 046 697 solver contacts), per solver contact: the
+# on a 1024-world batch (1 057 024 solver contacts), per solver contact: the
 # batched line scales it by its own solver contacts (the traffic of the
 # per-world kernel grows with the contacts it sweeps).
-WORLD_VELOCITY_TRAFFIC_PER_CONTACT = 397366272 / 1046697
+WORLD_VELOCITY_TRAFFIC_PER_CONTACT = 580477184 / 1057024
 
 
 def pinned(a):
