@@ -80,3 +80,31 @@ int main(void) {
     want = [C.sizeof(abi.Handle), C.sizeof(abi.BodyDesc), C.sizeof(abi.ColliderDesc), C.sizeof(abi.Params),
             C.sizeof(abi.Counters), C.sizeof(abi.Contact), abi.Counters.residual.offset]
     assert got == want
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    # No CPU fallback: the product without its built library raises.
+    with pytest.raises(RuntimeError, match="not built"):
+        abi.load_library(str(tmp_path / "libnpgpu.so"))
+
+
+def test_product_never_uses_the_oracle():
+    # The CPU oracle is test infrastructure: no module, kernel or header of
+    # the product imports, includes or loads it.
+    pkg = os.path.join(ROOT, "nphysics_gb300")
+    bad = []
+    for dirpath, _, files in os.walk(pkg):
+        if "_build" in dirpath or "__pycache__" in dirpath:
+            continue
+        for f in files:
+            if not f.endswith((".py", ".cu", ".cuh", ".hpp", ".cpp", ".h")):
+                continue
+            path = os.path.join(dirpath, f)
+            for n, line in enumerate(open(path, encoding="utf-8"), 1):
+                code = line.split("#")[0] if f.endswith(".py") else line.split("//")[0]
+                if re.search(r"\b(from|import)\s+oracle\b|#include\s*[<\"][^>\"]*oracle|liboracle|oracle_py|ref_world",
+                             code):
+                    bad.append(f"{os.path.relpath(path, ROOT)}:{n}: {line.strip()}")
+    assert not bad, bad
+    hdr = open(HEADER).read()
+    assert "oracle" not in hdr
