@@ -11,8 +11,10 @@ GPU: the step through the C ABI, on the stored inputs, reproduces the
 colour-order f32 fixtures bit for bit in poses, velocities, activation and
 the broad-phase pair set; contact geometry within 1e-5 relative and impulses
 within 1e-4 relative (the path's stated bars; in practice they agree bit for
-bit too), and the contact, solver-contact, colour and awake-body counts
-exactly.
+bit too), the contact, solver-contact, colour and awake-body counts exactly,
+and the residual, kinetic energy and maximum penetration within 1e-9
+relative (FP64 sums taken in another order; the residual's rows in
+float-float arithmetic on the GPU).
 """
 import glob
 import json
@@ -118,4 +120,6 @@ def test_gpu_reproduces_fixture(gpu_lib, name):
         co = dict(zip(meta["counter_keys"], f[f"counters_{s}"]))
         for k in EXACT_COUNTERS:
             assert cg[k] == co[k], (name, s, k, cg[k], co[k])
+        for k in ("residual", "kinetic_energy", "max_penetration"):
+            assert abs(cg[k] - co[k]) <= 1e-9 * abs(co[k]) + 1e-15, (name, s, k, cg[k], co[k])
     g.close()
