@@ -242,7 +242,8 @@ typedef struct npgpu_contact {
 
 typedef struct npgpu_world npgpu_world;
 
-/* Library version (NPGPU_ABI_VERSION). */
+/* Library version (NPGPU_ABI_VERSION).
+ * No counterpart in the reference (a crate version). */
 uint32_t npgpu_abi_version(void);
 
 /* Fills `out` with IntegrationParameters::default() (integration_parameters.rs:169-189). */
@@ -256,7 +257,8 @@ npgpu_world* npgpu_create(const npgpu_params* params, const float gravity[3],
                           uint32_t capacity_pairs, npgpu_status* status);
 void npgpu_destroy(npgpu_world* w);
 
-/* The world's CUDA stream (a cudaStream_t), for callers that time or order work. */
+/* The world's CUDA stream (a cudaStream_t), for callers that time or order work.
+ * No counterpart in the reference, whose step runs on the calling thread. */
 void* npgpu_stream(npgpu_world* w);
 
 npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params);
@@ -294,7 +296,8 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
 npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints,
                         uint32_t num_force_generators);
 
-/* Waits for the world's stream and reports any device-side error flag. */
+/* Waits for the world's stream and reports any device-side error flag.
+ * No counterpart in the reference: its step returns when done. */
 npgpu_status npgpu_synchronize(npgpu_world* w);
 
 /* Chooses the solver's launch shape for the current scene by timing real
@@ -313,30 +316,46 @@ npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32
 /* Copies body state to host arrays indexed by slot (any pointer may be NULL):
  * position[7n], velocity[6n], energy[n] (activation energy), active[n]
  * (1 when awake), for slots [first, first + n). Waits for the world's
- * stream; page-locked arrays are written by the copy engines directly. */
+ * stream; page-locked arrays are written by the copy engines directly.
+ * Replaces reading RigidBody::position / velocity
+ * (src/object/rigid_body.rs:361-369) and Body::activation_status
+ * (src/object/body.rs:181) after MechanicalWorld::step. */
 npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, float* position,
                                    float* velocity, float* energy, uint8_t* active);
 
 /* The inertia the bodies carry after the colliders' mass was added:
- * local_inertia[7n] (mass, xx, xy, xz, yy, yz, zz) and local_com[3n]. */
+ * local_inertia[7n] (mass, xx, xy, xz, yy, yz, zz) and local_com[3n].
+ * Replaces Body::local_inertia / local_center_of_mass
+ * (src/object/rigid_body.rs:913-930) once GeometricalWorld::maintain has
+ * added the colliders' mass (src/world/geometrical_world.rs:102-227). */
 npgpu_status npgpu_download_mass_properties(npgpu_world* w, uint32_t first, uint32_t n,
                                             float* local_inertia, float* local_com);
 
 /* Broad-phase pairs as (collider1, collider2) with collider1 < collider2,
- * sorted ascending. *count receives the number of pairs; at most `max` are written. */
+ * sorted ascending. *count receives the number of pairs; at most `max` are written.
+ * Replaces the pair set of GeometricalWorld::perform_broad_phase
+ * (src/world/geometrical_world.rs:285-312). */
 npgpu_status npgpu_get_pairs(npgpu_world* w, uint32_t* pairs2, uint32_t max, uint32_t* count);
 
-/* Fat AABBs (min xyz, max xyz) of colliders [first, first + n). */
+/* Fat AABBs (min xyz, max xyz) of colliders [first, first + n).
+ * Replaces the broad-phase proxies' AABBs that
+ * GeometricalWorld::sync_colliders updates
+ * (src/world/geometrical_world.rs:230-265). */
 npgpu_status npgpu_get_aabbs(npgpu_world* w, uint32_t first, uint32_t n, float* aabb6);
 
-/* Contacts of every manifold, sorted by (collider1, collider2, feature_key). */
+/* Contacts of every manifold, sorted by (collider1, collider2, feature_key).
+ * Replaces GeometricalWorld::contact_pairs
+ * (src/world/geometrical_world.rs:534-618) with each manifold's contacts and
+ * the solver's impulses. */
 npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max,
                                 uint32_t* count);
 
 npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out);
 
 /* One-line description of the last failure on this world (or of the last
- * failed npgpu_create / npgpu_find_pairs_static when w is NULL). */
+ * failed npgpu_create / npgpu_find_pairs_static when w is NULL).
+ * No counterpart in the reference, which panics or skips (try_ret! /
+ * try_continue!, src/lib.rs:93-114). */
 const char* npgpu_last_error(const npgpu_world* w);
 
 /* Broad phase over caller-provided boxes that allocates nothing. This entry
@@ -381,26 +400,33 @@ npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint32_t* groups
 #define NPGPU_MLP_SAMPLE_FLOATS 28u
 #define NPGPU_MLP_INIT 1u      /* npgpu_mlp_train flag: new weights from the seed, normalisation from the samples */
 
-/* Sets the network (n == NPGPU_MLP_PARAMS) and resets the optimiser state. */
+/* Sets the network (n == NPGPU_MLP_PARAMS) and resets the optimiser state.
+ * No counterpart in the reference (the learned warm start is this
+ * library's). */
 npgpu_status npgpu_mlp_set(npgpu_world* w, const float* params, uint32_t n);
-/* Copies the network's fp32 parameters out (n >= NPGPU_MLP_PARAMS). */
+/* Copies the network's fp32 parameters out (n >= NPGPU_MLP_PARAMS).
+ * No counterpart in the reference. */
 npgpu_status npgpu_mlp_get(npgpu_world* w, float* params, uint32_t n);
 /* Records a training sample for every solver contact of the following steps
  * (features at assembly, impulses after the velocity solve) until `capacity`
  * samples are held; capacity 0 stops recording and keeps what was recorded. A
- * new capacity discards earlier samples. */
+ * new capacity discards earlier samples.
+ * No counterpart in the reference. */
 npgpu_status npgpu_mlp_record(npgpu_world* w, uint32_t capacity);
-/* Number of recorded samples, and up to max_samples of them when out != NULL. */
+/* Number of recorded samples, and up to max_samples of them when out != NULL.
+ * No counterpart in the reference. */
 npgpu_status npgpu_mlp_samples(npgpu_world* w, float* out, uint32_t max_samples, uint32_t* count);
 /* Trains on the recorded samples with Adam (lr, batch a multiple of 64):
  * `steps` batches drawn from the samples by a hash of (seed, step). With
  * NPGPU_MLP_INIT, or when no network is set yet, starts from He-uniform
  * weights drawn from `seed` and normalisation from the samples' statistics.
- * *final_loss (may be NULL) receives the last batch's loss. */
+ * *final_loss (may be NULL) receives the last batch's loss.
+ * No counterpart in the reference. */
 npgpu_status npgpu_mlp_train(npgpu_world* w, uint32_t steps, uint32_t batch, float lr, uint32_t seed, uint32_t flags,
                              float* final_loss);
 /* Loss and gradient (NPGPU_MLP_TRAINABLE floats, parameter layout above) of
- * the current network over n host samples, without updating it (n <= 65536). */
+ * the current network over n host samples, without updating it (n <= 65536).
+ * No counterpart in the reference. */
 npgpu_status npgpu_mlp_grad(npgpu_world* w, const float* samples, uint32_t n, float* grad, float* loss);
 
 #ifdef __cplusplus

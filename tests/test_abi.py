@@ -118,3 +118,17 @@ def test_rust_binding_declares_every_entry_point():
     block = text[i:text.index("}\n```", i)]
     missing = [f for f in declared_functions() if re.search(r"\bfn " + f + r"\(", block) is None]
     assert not missing, missing
+
+
+def test_every_entry_point_cites_the_reference():
+    # Each declaration's comment names the reference interface it replaces
+    # (a src/...rs file:line) or says that the reference has no counterpart.
+    src = open(HEADER).read()
+    uncited = []
+    for m in re.finditer(r"(/\*(?:(?!\*/).)*\*/)\s*((?:[A-Za-z_0-9]+[ \*]+)+\b(npgpu_[a-z_0-9]+)\s*\()", src, flags=re.S):
+        comment, name = m.group(1), m.group(3)
+        if not (re.search(r"\.rs[:)]", comment) or "counterpart" in comment.lower() or ".rs" in comment):
+            uncited.append(name)
+    assert not uncited, uncited
+    assert set(declared_functions()) <= {m.group(3) for m in re.finditer(
+        r"(/\*(?:(?!\*/).)*\*/)\s*((?:[A-Za-z_0-9]+[ \*]+)+\b(npgpu_[a-z_0-9]+)\s*\()", src, flags=re.S)}
