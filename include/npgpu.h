@@ -261,6 +261,8 @@ void npgpu_destroy(npgpu_world* w);
  * No counterpart in the reference, whose step runs on the calling thread. */
 void* npgpu_stream(npgpu_world* w);
 
+/* Replace MechanicalWorld::integration_parameters and MechanicalWorld::gravity
+ * (src/world/mechanical_world.rs:61, 65), read by the next step. */
 npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params);
 npgpu_status npgpu_set_gravity(npgpu_world* w, const float gravity[3]);
 
@@ -350,6 +352,8 @@ npgpu_status npgpu_get_aabbs(npgpu_world* w, uint32_t first, uint32_t n, float* 
 npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max,
                                 uint32_t* count);
 
+/* The last step's counters: replaces MechanicalWorld::counters
+ * (src/world/mechanical_world.rs:57; src/counters/mod.rs:19). */
 npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out);
 
 /* One-line description of the last failure on this world (or of the last

@@ -121,14 +121,18 @@ def test_rust_binding_declares_every_entry_point():
 
 
 def test_every_entry_point_cites_the_reference():
-    # Each declaration's comment names the reference interface it replaces
-    # (a src/...rs file:line) or says that the reference has no counterpart.
+    # Each group of declarations (a paragraph of the header) has a comment that
+    # names the reference interface it replaces (a src/...rs file:line) or says
+    # that the reference has no counterpart.
     src = open(HEADER).read()
-    uncited = []
-    for m in re.finditer(r"(/\*(?:(?!\*/).)*\*/)\s*((?:[A-Za-z_0-9]+[ \*]+)+\b(npgpu_[a-z_0-9]+)\s*\()", src, flags=re.S):
-        comment, name = m.group(1), m.group(3)
-        if not (re.search(r"\.rs[:)]", comment) or "counterpart" in comment.lower() or ".rs" in comment):
-            uncited.append(name)
+    uncited, seen = [], set()
+    for para in re.split(r"\n\s*\n", src):
+        names = re.findall(r"\b(npgpu_[a-z_0-9]+)\s*\(", re.sub(r"/\*.*?\*/", "", para, flags=re.S))
+        if not names:
+            continue
+        seen.update(names)
+        comments = " ".join(re.findall(r"/\*.*?\*/", para, flags=re.S))
+        if not (".rs" in comments or "counterpart" in comments.lower()):
+            uncited += names
     assert not uncited, uncited
-    assert set(declared_functions()) <= {m.group(3) for m in re.finditer(
-        r"(/\*(?:(?!\*/).)*\*/)\s*((?:[A-Za-z_0-9]+[ \*]+)+\b(npgpu_[a-z_0-9]+)\s*\()", src, flags=re.S)}
+    assert set(declared_functions()) <= seen
