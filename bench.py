@@ -1,10 +1,10 @@
-"""Benchmark of the GPU rigid-body step: body-steps/s on the 32^3 ball pile.
+"""Benchmark of the GPU rigid-body step: body-steps/s and PGS iterations to 1e-4.
 
-Workload: 32768 balls of radius 0.5 on a 1.2 lattice (seeded jitter),
-dropped on a static ground, density 1, friction 0.3, dt 1/60, the
-reference's 8 velocity / 3 position iterations. The pile is simulated
-untimed for --settle steps (it reaches the ground and forms contacts), then
---warmup steps, then --steps timed steps.
+Headline workload (value, e2e, roofline): the 32^3 ball pile, 32768 balls of
+radius 0.5 on a 1.2 lattice (seeded jitter), dropped on a static ground,
+density 1, friction 0.3, dt 1/60, the reference's 8 velocity / 3 position
+iterations. The pile is simulated untimed for --settle steps, then the
+autotuner's steps, then --warmup steps, then --steps timed steps.
 
   value  body-steps/s with the world resident in HBM: CUDA events on the
          world's stream around each step, an L2 flush (256 MiB write)
@@ -13,11 +13,20 @@ untimed for --settle steps (it reaches the ground and forms contacts), then
          step, upload of the step's applied forces from pinned host memory,
          npgpu_step, download of every body's pose and velocity into host
          buffers; wall time of the loop.
-  pgs_iterations  the metric's second half on the same pile: mean SOR-Prox
-         iterations to a residual of 1e-4, impulse cache alone vs the learned
-         warm start (network trained in the run on the solver's own impulses).
-  --impl reference  times the CPU oracle (the restated reference step) on
-         this host instead (the Rust reference cannot be built here).
+  c4_batched  the batched-worlds record: 4096 worlds (body counts
+         log-uniform in [16, 2048]) in one world object, timed the same way,
+         roofline on the per-world velocity kernel.
+  pgs_iterations  the metric's second half on the 100k mixed pile of balls
+         and cuboids: SOR-Prox iterations to a residual of 1e-4 (cap 4096),
+         impulse cache alone vs the learned warm start, whose network is
+         trained in the run on 2M solver-converged contacts of this pile and
+         of the 210-box pyramid.
+  cpu_baseline  the CPU oracle (the restated reference step, f32, one
+         thread) on the same pile and step window; cpu_configs adds the
+         pyramid and a 10k-body subset of the mixed pile beside the GPU's
+         own figure on the same steps.
+  --impl reference  times the CPU oracle on this host instead (the Rust
+         reference cannot be built here).
 """
 import argparse
 import json
@@ -66,7 +75,7 @@ def parse():
     ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--settle", type=int, default=None,
-                    help="untimed steps first (default: 200 for the ball pile and the pyramid, 150 for the mixed "
+                    help="untimed steps first (default: 200 for the ball pile and the pyramid, 300 for the mixed "
                          "pile, 60 for batched worlds, 0 for the brick walls, whose impact phase is the workload)")
     ap.add_argument("--side", type=int, default=32)
     ap.add_argument("--workload", default="pile", choices=["pile", "batched", "pyramid", "walls", "mixed"],
@@ -85,9 +94,11 @@ def parse():
                     help="threads per block of the per-world schedule when --schedule worlds")
     ap.add_argument("--no-pgs-iterations", action="store_true",
                     help="skip the iterations-to-1e-4 comparison of the learned and plain warm starts")
+    ap.add_argument("--no-batched", action="store_true",
+                    help="skip the batched-worlds record of the default (pile) run")
     args = ap.parse_args()
     if args.settle is None:
-        args.settle = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0, "mixed": 150}[args.workload]
+        args.settle = SETTLE[args.workload]
     return args
 
 
@@ -157,16 +168,44 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def cpu_sample(scene_fn, settle_steps, max_steps, seconds):
+# Steps npgpu_autotune advances a single-world scene by: one automatic step,
+# then 1 + 5 steps for each of its two candidates (the one grid, and the
+# per-world schedule with the world on one thread-block cluster).
+AUTOTUNE_STEPS_SINGLE_WORLD = 1 + 2 * (1 + 5)
+
+
+def host_cpu():
+    """Core count and model name of this host."""
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True).stdout
+            for line in out.splitlines():
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except OSError:
+            pass
+    return os.cpu_count(), model
+
+
+def cpu_sample(scene, first_step, max_steps, seconds, what):
     """Times the oracle (the restated reference step, f32, one thread, the
-    reference's row order) on a bounded sample of the same workload: the pile
-    is settled for `settle_steps` untimed steps, exactly as on the GPU, then
-    up to `max_steps` steps are timed, stopping after about `seconds`."""
+    reference's row order) on a bounded sample of a workload: the scene is
+    stepped `first_step` untimed steps, then up to `max_steps` steps are timed,
+    stopping after about `seconds`."""
     from oracle.oracle_py import ORDER_REFERENCE, OracleWorld
-    sc = scene_fn()
-    o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_REFERENCE)
-    o.load_scene(sc)
-    o.step(settle_steps)
+    o = OracleWorld(scene.params(), scene.gravity, precision=32, order=ORDER_REFERENCE)
+    o.load_scene(scene)
+    o.step(first_step)
     steps = 0
     t0 = time.perf_counter()
     while steps < max_steps and (steps == 0 or time.perf_counter() - t0 < seconds):
@@ -174,15 +213,23 @@ def cpu_sample(scene_fn, settle_steps, max_steps, seconds):
         steps += 1
     dt = time.perf_counter() - t0
     c = o.counters()
-    sample = (f"steps {settle_steps}..{settle_steps + steps - 1} of the same {sc.num_dynamic}-ball pile "
-              f"({c['num_contacts']} contacts), single-threaded f32 oracle in the reference's row order; "
-              "the Rust reference has no toolchain on this host")
-    return sc.num_dynamic * steps / dt, steps, dt, sample
+    o.close()
+    sample = (f"steps {first_step}..{first_step + steps - 1} of {what} ({c['num_contacts']} contacts at the "
+              "end), single-threaded f32 oracle in the reference's row order, built -O3; the Rust reference "
+              "has no toolchain on this host")
+    return scene.num_dynamic * steps / dt, steps, dt, sample
 
 
-def cpu_baseline(scene_fn, seconds, settle_steps):
-    value, steps, dt, sample = cpu_sample(scene_fn, settle_steps, 10 ** 9, seconds)
-    return {"value": value, "unit": METRIC, "cores": 1, "kind": "port", "sample": sample}
+def cpu_baseline_line(value, sample):
+    cores, model = host_cpu()
+    return {"value": value, "unit": METRIC, "cores": 1, "host_cores": cores, "cpu_model": model, "kind": "port",
+            "sample": sample}
+
+
+def pile_window(args):
+    """First timed step of the ball-pile workload on the GPU arm: the settle
+    steps, the autotuner's steps, then the warm-up steps."""
+    return args.settle + AUTOTUNE_STEPS_SINGLE_WORLD + args.warmup
 
 
 def run_reference(args):
@@ -191,54 +238,104 @@ def run_reference(args):
         return
     from nphysics_gb300 import scenes
     n_dyn = args.side ** 3
-    value, steps, dt, sample = cpu_sample(lambda: scenes.ball_pile(side=args.side), args.settle + args.warmup,
-                                          args.steps, max(5.0, args.cpu_seconds))
+    first = pile_window(args)
+    value, steps, dt, sample = cpu_sample(scenes.ball_pile(side=args.side), first, args.steps,
+                                          max(5.0, args.cpu_seconds), f"the {n_dyn}-ball pile")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "impl": "reference", "n_gpus": args.gpus,
         "steps": steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": f"ball pile {args.side}^3 = {n_dyn} balls (radius 0.5, 1.2 lattice, seeded jitter) "
                                f"on a static ground, dt 1/60, 8 velocity / 3 position iterations; timed steps "
-                               f"{args.settle + args.warmup}..{args.settle + args.warmup + steps - 1} of the run",
+                               f"{first}..{first + steps - 1} of the run (the GPU arm's window starts at the "
+                               "same step)",
                    "sample": sample},
-        "cpu_baseline": {"value": value, "unit": METRIC, "cores": 1, "kind": "port", "sample": sample},
+        "cpu_baseline": cpu_baseline_line(value, sample),
         "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line))
 
 
-def pgs_iterations(scene_fn, settle, steps=30, record_steps=100, train_steps=2000):
-    """The metric's second half on the same workload: mean SOR-Prox iterations
-    to a residual of 1e-4 (at most 256), with the impulse cache alone and
-    with the learned warm start. The network is trained in this run on the
-    solver's own converged impulses of the workload (record_steps steps solved
-    to 1e-5). Both worlds are stepped `settle` steps with the default
-    parameters first, so they start the comparison from the same bits."""
-    from nphysics_gb300 import abi
-    from nphysics_gb300.train_warmstart import record
+def _iteration_stats(its, cap):
+    s = sorted(its)
+    return {"iterations_mean": statistics.mean(its), "iterations_p95": s[min(len(s) - 1, int(0.95 * len(s)))],
+            "iterations_max": s[-1], "steps_at_cap": sum(1 for i in its if i >= cap)}
+
+
+def _record_steps(w, steps, tolerance, max_iterations, capacity):
+    """Samples (features, converged impulses) of every solver contact of the
+    next `steps` steps of `w`, each solved to `tolerance`."""
+    import numpy as np
+    saved = w.params
+    p = w.params
+    p.solve_to_tolerance = 1
+    p.residual_tolerance = tolerance
+    p.max_iterations_to_tolerance = max_iterations
+    w.set_params(p)
+    out = []
+    for _ in range(steps):
+        w.mlp_record(capacity)
+        w.step(1)
+        out.append(w.mlp_samples())
+        w.mlp_record(0)
+    p.solve_to_tolerance = 0
+    w.set_params(p)
+    return np.concatenate(out) if out else np.zeros((0, 28), np.float32)
+
+
+def pgs_iterations(mixed, settle=300, steps=20, cap=4096, samples_total=2_000_000, train_steps=4000):
+    """The metric's second half on the 100k mixed pile (C3): SOR-Prox
+    iterations to a residual of 1e-4 (at most `cap`) with the impulse cache
+    alone and with the learned warm start, over `steps` steps after `settle`
+    steps with the default parameters (both worlds reach the comparison with
+    the same bits).
+
+    Training set: 2M solver-converged contacts (each step solved to 1e-5),
+    80 % from the mixed pile (one step in 30 of its settle, from step 60 on)
+    and 20 % from the 210-box pyramid (its first 300 steps), drawn by a seeded
+    subsample; the network trains on the GPU with Adam (lr 1e-3, batch 4096)."""
+    import numpy as np
+
+    from nphysics_gb300 import abi, scenes
+    from nphysics_gb300.world import GpuWorld
     t0 = time.perf_counter()
-    rec = record(scene_fn(), record_steps, 1e-5, 4_000_000)
-    n_samples = rec.mlp_samples(download=False)
+    rng = np.random.default_rng(2024)
+    rec = GpuWorld.for_scene(mixed, mixed.params(), pairs_per_collider=12)
+    parts = []
+    done = 0
+    for mark in range(60, settle + 1, 30):
+        rec.step(mark - done)
+        parts.append(_record_steps(rec, 1, 1e-5, 1024, 4_000_000))
+        done = mark + 1
+    c3 = np.concatenate(parts)
+    pyr = GpuWorld.for_scene(scenes.pyramid(base=20))
+    c1 = _record_steps(pyr, 300, 1e-5, 1024, 4_000_000)
+    pyr.close()
+    n3 = min(len(c3), int(0.8 * samples_total))
+    n1 = min(len(c1), samples_total - n3)
+    data = np.concatenate([c3[rng.choice(len(c3), n3, replace=False)], c1[rng.choice(len(c1), n1, replace=False)]])
+    rec.mlp_load_samples(data)
     rec.mlp_train(1, batch=4096, lr=1e-3, seed=1, init=True)
     loss = rec.mlp_train(train_steps, batch=4096, lr=1e-3, seed=2)
     net = rec.mlp_get()
     rec.close()
-    out = {"tolerance": 1e-4, "max_iterations": 256, "steps": steps,
-           "network": f"trained in this run: {n_samples} samples from {record_steps} steps solved to 1e-5, "
-                      f"{train_steps} Adam steps (batch 4096, lr 1e-3), final loss {loss:.3f}"}
-    from nphysics_gb300.world import GpuWorld
+    t_train = time.perf_counter() - t0
+    out = {"scene": "mixed pile, 100000 balls and cuboids dropped from U(1, 60) over 100 x 100",
+           "tolerance": 1e-4, "max_iterations": cap, "steps": f"{settle}..{settle + steps - 1}",
+           "network": f"trained in this run: {len(data)} samples ({n3} from the mixed pile, {n1} from the "
+                      f"210-box pyramid), solved to 1e-5, {train_steps} Adam steps (batch 4096, lr 1e-3), "
+                      f"final loss {loss:.3f}, {t_train:.1f} s"}
     for name, mode in (("plain", abi.WARMSTART_CACHE), ("learned", abi.WARMSTART_LEARNED)):
-        sc = scene_fn()
-        w = GpuWorld.for_scene(sc, sc.params())
+        w = GpuWorld.for_scene(mixed, mixed.params(), pairs_per_collider=12)
         w.mlp_set(net)
         w.step(settle)
         p = w.params
         p.warmstart_mode = mode
         p.solve_to_tolerance = 1
         p.residual_tolerance = 1e-4
-        p.max_iterations_to_tolerance = 256
+        p.max_iterations_to_tolerance = cap
         w.set_params(p)
-        its, r0, ms = [], [], []
+        its, r0, ms, starts, kept, contacts = [], [], [], 0, 0, []
         for _ in range(steps):
             a = time.perf_counter()
             w.step(1)
@@ -246,66 +343,86 @@ def pgs_iterations(scene_fn, settle, steps=30, record_steps=100, train_steps=200
             c = w.counters()
             its.append(c["velocity_iterations"])
             r0.append(c["residual_initial"])
-        out[name] = {"iterations_mean": statistics.mean(its), "residual_after_warm_start": statistics.mean(r0),
-                     "body_steps_per_s": sc.num_dynamic * steps / sum(ms)}
+            starts += c["learned_starts"]
+            kept += c["learned_kept"]
+            contacts.append(c["num_solver_contacts"])
+        out[name] = dict(_iteration_stats(its, cap), residual_after_warm_start=statistics.mean(r0),
+                         body_steps_per_s=mixed.num_dynamic * steps / sum(ms),
+                         solver_contacts_mean=statistics.mean(contacts))
+        if mode == abi.WARMSTART_LEARNED:
+            out[name]["learned_starts"] = starts
+            out[name]["learned_kept"] = kept
         w.close()
+    out["iterations_ratio_plain_over_learned"] = out["plain"]["iterations_mean"] / out["learned"]["iterations_mean"]
+    out["body_steps_ratio_learned_over_plain"] = (out["learned"]["body_steps_per_s"] /
+                                                  out["plain"]["body_steps_per_s"])
     out["seconds"] = time.perf_counter() - t0
     return out
 
 
-def run_gpu(args):
+def gpu_window_rate(scene, first, steps, **kw):
+    """Body-steps/s of the GPU step over steps first..first+steps-1 of the
+    scene (CUDA events on the world's stream around the window), with the
+    launch shape the autotuner picks for it on a separate copy of the world."""
+    import torch
+
+    from nphysics_gb300.world import GpuWorld
+    probe = GpuWorld.for_scene(scene, scene.params(), **kw)
+    probe.step(first)
+    schedule, threads, _ = probe.autotune(3)
+    probe.close()
+    p = scene.params()
+    p.solver_schedule, p.world_threads = schedule, threads
+    w = GpuWorld.for_scene(scene, p, **kw)
+    w.step(first)
+    stream = torch.cuda.ExternalStream(w.stream)
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    w.step(steps, sync=False)
+    b.record(stream)
+    w.synchronize()
+    torch.cuda.synchronize()
+    w.close()
+    return scene.num_dynamic * steps / (a.elapsed_time(b) * 1e-3)
+
+
+def cpu_configs(seconds):
+    """The oracle beside the GPU on the pyramid and a 10k-body subset of the
+    mixed pile, each on the same step window on both sides."""
+    from nphysics_gb300 import scenes
+    out = []
+    for name, scene, first, steps, kw in (
+            ("C1 box pyramid, 210 cuboids", scenes.pyramid(base=20), 5, 200, {}),
+            ("C3 subset: 10000 balls and cuboids at the mixed pile's density (footprint 31.6 x 31.6, heights "
+             "U(1, 60))", scenes.mixed_pile(n=10_000, footprint=31.6), 5, 120, {"pairs_per_collider": 12})):
+        cpu, n, dt, sample = cpu_sample(scene, first, steps, seconds, name)
+        gpu = gpu_window_rate(scene, first, n, **kw)
+        out.append({"config": name, "steps": f"{first}..{first + n - 1}", "cpu_body_steps_per_s": cpu,
+                    "gpu_body_steps_per_s": gpu, "sample": sample})
+    return out
+
+
+def whole_job(units_per_rank, device_ms, e2e_s, device="cuda"):
+    """The whole job's value and e2e of a run on every rank: the units all
+    ranks processed over the slowest rank's device time and end-to-end time
+    (one process: its own figures)."""
+    from nphysics_gb300 import multirank
+    total_ms = multirank.reduce_max(device_ms, device)
+    units = multirank.reduce_sum(units_per_rank, device)
+    return units / (total_ms * 1e-3), units / multirank.reduce_max(e2e_s, device), total_ms
+
+
+def measure(args, sc, w, kind, rank, world_size, local_rank):
+    """Device-resident and end-to-end body-steps/s of world `w` on scene `sc`,
+    plus the phase times and the velocity solver's roofline."""
     import numpy as np
     import torch
 
-    from nphysics_gb300 import build, scenes
-    from nphysics_gb300.world import GpuWorld
-
-    from nphysics_gb300 import multirank
-    rank, world_size, local_rank = multirank.rank_env()
-    torch.cuda.set_device(local_rank)
-    if world_size > 1:
-        import torch.distributed as dist
-        dist.init_process_group("nccl")
-    build.build()
-    torch.cuda.init()
-    if args.workload == "pile":
-        # Replicas: every rank runs its own copy of the pile (one world per GPU).
-        sc = scenes.ball_pile(side=args.side)
-        w = GpuWorld.for_scene(sc, sc.params())
-        workload = (f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, seeded jitter) "
-                    f"on a static ground, dt 1/60, 8 velocity / 3 position iterations")
-    elif args.workload == "pyramid":
-        sc = scenes.pyramid(base=20)
-        w = GpuWorld.for_scene(sc, sc.params())
-        workload = ("box pyramid: 210 cuboids of half extent 0.5 in a 20-base triangle on a static ground, "
-                    "density 1, friction 0.5, dt 1/60, 8 velocity / 3 position iterations")
-    elif args.workload == "mixed":
-        # Replicas: the 100k mixed pile of balls and cuboids on every rank.
-        sc = scenes.mixed_pile(n=100_000)
-        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=12)
-        workload = ("mixed pile: 100000 bodies, half balls of radius U(0.2, 0.8), half cuboids of half extents "
-                    "U(0.2, 0.8)^3 at random orientations, density 1, friction 0.5, dropped from a jittered 2.0 "
-                    "lattice onto a static ground, dt 1/60, 8 velocity / 3 position iterations")
-    elif args.workload == "walls":
-        # Each rank steps its own 256 walls (weak scaling).
-        sc = scenes.brick_walls(n_walls=256, seed=1234 + rank)
-        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
-        workload = ("brick walls: 256 walls per GPU of 50 x 40 bricks (half extents 0.5 x 0.25 x 0.25, running "
-                    "bond), each struck by 64 balls of radius 0.4, density 10, at U(20, 40) m/s; friction 0.6, "
-                    "dt 1/120, 8 velocity / 3 position iterations")
-    else:
-        # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
-        n_all = args.worlds_per_rank * world_size
-        sc = scenes.batched_worlds(n_worlds=n_all, worlds=multirank.shard(n_all, rank, world_size))
-        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=6)
-        workload = (f"batched worlds: {args.worlds_per_rank} worlds per GPU (of {n_all}), body counts "
-                    f"log-uniform in [16, 2048] ({sc.num_dynamic} bodies on rank 0), ball piles and box stacks "
-                    f"on their own grounds, dt 1/60, 8 velocity / 3 position iterations, one block per world")
-    p = sc.params()
     stream = torch.cuda.ExternalStream(w.stream)
     flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
     n_dyn = sc.num_dynamic
-    w.step(args.settle)
+    w.step(args.settle if kind == args.workload else SETTLE[kind])
     # Launch shape chosen on real steps (every candidate gives the same bits).
     if args.schedule == "auto":
         tuned = w.autotune(5)
@@ -336,8 +453,6 @@ def run_gpu(args):
     if world_size > 1:
         torch.distributed.barrier()
     step_ms = [a.elapsed_time(b) for a, b in evs]
-    total_ms = multirank.reduce_max(sum(step_ms), device="cuda")
-    value = multirank.reduce_sum(n_dyn * args.steps, device="cuda") / (total_ms * 1e-3)
 
     # ---- end to end through the C ABI with host buffers ------------------------------------
     # Page-locked host arrays, as a host that streams every step would keep them.
@@ -359,7 +474,7 @@ def run_gpu(args):
     e2e_s = time.perf_counter() - t0
     h2d = handles.nbytes + forces.nbytes          # 16-byte handles and 6 force floats per dynamic body
     d2h = pos.nbytes + vel.nbytes                 # every body's pose and velocity
-    e2e_value = multirank.reduce_sum(n_dyn * args.steps, device="cuda") / multirank.reduce_max(e2e_s, device="cuda")
+    value, e2e_value, total_ms = whole_job(n_dyn * args.steps, sum(step_ms), e2e_s)
 
     # ---- phase times (CUDA events on the world's stream), after the timed region ----------
     p.profile = 1
@@ -371,7 +486,7 @@ def run_gpu(args):
     p.profile = 0
     w.set_params(p)
 
-    # ---- roofline of the dominant kernel: the velocity solver (k_velocity) ------------------
+    # ---- roofline of the dominant kernel: the velocity solver -------------------------------
     # Algorithmic bytes of one SOR-Prox iteration: 128 per solver contact
     # (normal, two lever arms, r / rhs / impulse of 3 rows, friction, 2 body
     # indices read; 3 impulses written) + 76 per dynamic body (Δv read and
@@ -384,40 +499,124 @@ def run_gpu(args):
     solve_ms = statistics.mean(c["velocity_resolution_time"] for c in counters)
     achieved = bytes_launch / (solve_ms * 1e-3) / 1e9
     cl = clocks.summary()
-    line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": f"{workload}; timed steps "
-                               f"{first_timed}..{first_timed + args.steps - 1} of the run",
-                   "l2": "flushed (256 MiB write) between timed steps",
-                   "solver_schedule": {1: "one cooperative grid",
-                                       2: "per world: a cluster, a block or a warp each"}[tuned[0]],
-                   "world_threads": tuned[1],
-                   "parallelism": ("replicas" if args.workload in ("pile", "pyramid", "mixed")
-                                   else f"worlds sharded over {world_size} GPUs"),
-                   "contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
-                   "solver_contacts": int(K), "active_bodies": int(B),
-                   "colours": int(statistics.mean(c["num_colours"] for c in counters))},
+    launches = LAUNCHES_PER_STEP if tuned[0] == 1 else LAUNCHES_PER_STEP_BATCHED
+    return {
+        "value": value, "ms_per_step": total_ms / args.steps, "first_timed_step": first_timed,
+        "tuned": tuned,
         "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
-        "roofline": {"bound": "hbm", "kernel": "k_velocity" if tuned[0] == 1 else "k_world_velocity", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak,
-                     "traffic": (VELOCITY_TRAFFIC_PER_LAUNCH if args.workload == "pile" and tuned[0] == 1
+        "roofline": {"bound": "hbm", "kernel": "k_velocity" if tuned[0] == 1 else "k_world_velocity",
+                     "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": (VELOCITY_TRAFFIC_PER_LAUNCH if kind == "pile" and tuned[0] == 1
                                  else int(WORLD_VELOCITY_TRAFFIC_PER_CONTACT * K)
-                                 if args.workload == "batched" and tuned[0] == 2 else None),
-                     "peak_source": peak_kind,
-                     "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
+                                 if kind == "batched" and tuned[0] == 2 else None),
+                     "peak_source": peak_kind, "bytes_per_launch": bytes_launch, "launch_ms": solve_ms},
         "clocks": {"sm_mhz": cl["sm_mhz"], "sm_max_mhz": cl["sm_max_mhz"], "reasons": cl["reasons"]},
-        "gpu_launches": (LAUNCHES_PER_STEP if tuned[0] == 1 else LAUNCHES_PER_STEP_BATCHED) * args.steps,
+        "gpu_launches": launches * args.steps,
+        "counters": {"contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
+                     "solver_contacts": int(K), "active_bodies": int(B),
+                     "colours": int(statistics.mean(c["num_colours"] for c in counters))},
         "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
                      ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",
                       "velocity_update_time", "position_resolution_time")},
     }
+
+
+SETTLE = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0, "mixed": 300}
+
+
+def build_workload(kind, args, rank, world_size):
+    from nphysics_gb300 import multirank, scenes
+    from nphysics_gb300.world import GpuWorld
+    if kind == "pile":
+        # Replicas: every rank runs its own copy of the pile (one world per GPU).
+        sc = scenes.ball_pile(side=args.side)
+        w = GpuWorld.for_scene(sc, sc.params())
+        desc = (f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, seeded jitter) "
+                f"on a static ground, dt 1/60, 8 velocity / 3 position iterations")
+    elif kind == "pyramid":
+        sc = scenes.pyramid(base=20)
+        w = GpuWorld.for_scene(sc, sc.params())
+        desc = ("box pyramid: 210 cuboids of half extent 0.5 in a 20-base triangle on a static ground, "
+                "density 1, friction 0.5, dt 1/60, 8 velocity / 3 position iterations")
+    elif kind == "mixed":
+        # Replicas: the 100k mixed pile of balls and cuboids on every rank.
+        sc = scenes.mixed_pile(n=100_000)
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=12)
+        desc = ("mixed pile: 100000 bodies, half balls of radius U(0.2, 0.8), half cuboids of half extents "
+                "U(0.2, 0.8)^3 at uniform random orientations, density 1, friction 0.5, dropped from heights "
+                "U(1, 60) over a 100 x 100 footprint onto a static ground, dt 1/60, 8 velocity / 3 position "
+                "iterations")
+    elif kind == "walls":
+        # Each rank steps its own 256 walls (weak scaling).
+        sc = scenes.brick_walls(n_walls=256, seed=1234 + rank)
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
+        desc = ("brick walls: 256 walls per GPU of 50 x 40 bricks (half extents 0.5 x 0.25 x 0.25, running "
+                "bond), each struck by 64 balls of radius 0.4, density 10, at U(20, 40) m/s; friction 0.6, "
+                "dt 1/120, 8 velocity / 3 position iterations")
+    else:
+        # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
+        n_all = args.worlds_per_rank * world_size
+        sc = scenes.batched_worlds(n_worlds=n_all, worlds=multirank.shard(n_all, rank, world_size))
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=6)
+        desc = (f"batched worlds: {args.worlds_per_rank} worlds per GPU (of {n_all}), body counts "
+                f"log-uniform in [16, 2048] ({sc.num_dynamic} bodies on rank 0), ball piles and box stacks "
+                f"on their own grounds, dt 1/60, 8 velocity / 3 position iterations, one block per world")
+    return sc, w, desc
+
+
+def run_gpu(args):
+    import torch
+
+    from nphysics_gb300 import build, multirank, scenes
+
+    rank, world_size, local_rank = multirank.rank_env()
+    torch.cuda.set_device(local_rank)
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    build.build()
+    torch.cuda.init()
+    sc, w, desc = build_workload(args.workload, args, rank, world_size)
+    m = measure(args, sc, w, args.workload, rank, world_size, local_rank)
+    w.close()
+    tuned = m["tuned"]
+    line = {
+        "metric": METRIC, "value": m["value"], "unit": METRIC, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": m["ms_per_step"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict({"workload": f"{desc}; timed steps {m['first_timed_step']}..."
+                                    f"{m['first_timed_step'] + args.steps - 1} of the run",
+                        "l2": "flushed (256 MiB write) between timed steps",
+                        "solver_schedule": {1: "one cooperative grid",
+                                            2: "per world: a cluster, a block or a warp each"}[tuned[0]],
+                        "world_threads": tuned[1],
+                        "parallelism": ("replicas" if args.workload in ("pile", "pyramid", "mixed")
+                                        else f"worlds sharded over {world_size} GPUs")}, **m["counters"]),
+        "e2e": m["e2e"], "roofline": m["roofline"], "clocks": m["clocks"], "gpu_launches": m["gpu_launches"],
+        "phase_ms": m["phase_ms"],
+    }
+    if args.workload == "pile" and m["first_timed_step"] != pile_window(args):
+        line["config"]["window_note"] = (f"the reference arm's window starts at step {pile_window(args)}, this "
+                                         f"arm's at {m['first_timed_step']}")
+    if args.workload == "pile" and not args.no_batched:
+        # The batched-worlds record (C4), measured the same way on this GPU.
+        bsc, bw, bdesc = build_workload("batched", args, rank, world_size)
+        bm = measure(args, bsc, bw, "batched", rank, world_size, local_rank)
+        bw.close()
+        line["c4_batched"] = {"workload": bdesc, "value": bm["value"], "unit": METRIC,
+                              "ms_per_step": bm["ms_per_step"], "e2e": bm["e2e"], "roofline": bm["roofline"],
+                              "clocks": bm["clocks"], "gpu_launches": bm["gpu_launches"], "phase_ms": bm["phase_ms"],
+                              "timed_steps": f"{bm['first_timed_step']}..{bm['first_timed_step'] + args.steps - 1}",
+                              "world_threads": bm["tuned"][1], **bm["counters"]}
     if rank == 0 and world_size == 1 and args.workload == "pile" and not args.no_pgs_iterations:
-        line["pgs_iterations"] = pgs_iterations(lambda: scenes.ball_pile(side=args.side), args.settle)
+        line["pgs_iterations"] = pgs_iterations(scenes.mixed_pile(n=100_000))
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline and args.workload == "pile":
-        line["cpu_baseline"] = cpu_baseline(lambda: scenes.ball_pile(side=args.side), args.cpu_seconds, args.settle)
+        first = m["first_timed_step"]
+        value, steps, dt, sample = cpu_sample(scenes.ball_pile(side=args.side), first, 10 ** 9, args.cpu_seconds,
+                                              f"the same {sc.num_dynamic}-ball pile")
+        line["cpu_baseline"] = cpu_baseline_line(value, sample)
+        line["cpu_configs"] = cpu_configs(args.cpu_seconds)
     if rank == 0:
         print(json.dumps(line))
     if world_size > 1:

@@ -356,8 +356,10 @@ npgpu_status npgpu_get_contacts(npgpu_world* w, npgpu_contact* out, uint32_t max
  * (src/world/mechanical_world.rs:57; src/counters/mod.rs:19). */
 npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out);
 
-/* One-line description of the last failure on this world (or of the last
- * failed npgpu_create / npgpu_find_pairs_static when w is NULL).
+/* One-line description of the last failure on this world (or, when w is
+ * NULL, of the calling thread's last failed npgpu_create /
+ * npgpu_find_pairs_static; the string stays valid until that thread's next
+ * such failure).
  * No counterpart in the reference, which panics or skips (try_ret! /
  * try_continue!, src/lib.rs:93-114). */
 const char* npgpu_last_error(const npgpu_world* w);
@@ -420,6 +422,11 @@ npgpu_status npgpu_mlp_record(npgpu_world* w, uint32_t capacity);
 /* Number of recorded samples, and up to max_samples of them when out != NULL.
  * No counterpart in the reference. */
 npgpu_status npgpu_mlp_samples(npgpu_world* w, float* out, uint32_t max_samples, uint32_t* count);
+/* Replaces the recorded samples with n host samples (NPGPU_MLP_SAMPLE_FLOATS
+ * floats each, as npgpu_mlp_samples returns them) and stops recording: a
+ * training set gathered from several worlds or runs trains one network.
+ * No counterpart in the reference. */
+npgpu_status npgpu_mlp_load_samples(npgpu_world* w, const float* samples, uint32_t n);
 /* Trains on the recorded samples with Adam (lr, batch a multiple of 64):
  * `steps` batches drawn from the samples by a hash of (seed, step). With
  * NPGPU_MLP_INIT, or when no network is set yet, starts from He-uniform

@@ -256,6 +256,7 @@ def load_library(path=LIB_PATH):
         "npgpu_mlp_get": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_record": (C.c_int, [W, C.c_uint32]),
         "npgpu_mlp_samples": (C.c_int, [W, P(C.c_float), C.c_uint32, P(C.c_uint32)]),
+        "npgpu_mlp_load_samples": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_train": (C.c_int, [W, C.c_uint32, C.c_uint32, C.c_float, C.c_uint32, C.c_uint32,
                                       P(C.c_float)]),
         "npgpu_mlp_grad": (C.c_int, [W, P(C.c_float), C.c_uint32, P(C.c_float), P(C.c_float)]),
@@ -274,7 +275,7 @@ EXPORTED = [
     "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_step",
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
     "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
-    "npgpu_autotune", "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
+    "npgpu_autotune", "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_load_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
 ]
 
 # Learned warm start (npgpu_mlp_*).

@@ -15,8 +15,13 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT, "libnpgpu.so")
-SOURCES = ["npgpu_world.cu", "k_bodies.cu", "k_cd.cu", "k_solve.cu", "k_static_pairs.cu", "k_mlp.cu"]
-HEADERS = ["np_math.cuh", "world_dev.cuh", "dyn.cuh", "narrow.cuh"]
+# (source, object, extra flags): k_solve.cu is compiled twice, see EXTRA.
+SOURCES = [("npgpu_world.cu", "npgpu_world.o", []), ("k_bodies.cu", "k_bodies.o", []), ("k_cd.cu", "k_cd.o", []),
+           ("k_solve.cu", "k_solve.o", ["-DNPGPU_EXCHANGE_TU=0"]),
+           ("k_solve.cu", "k_solve_exchange.o", ["-DNPGPU_EXCHANGE_TU=1", "-Xptxas", "-dlcm=cg"]),
+           ("k_static_pairs.cu", "k_static_pairs.o", []), ("k_mlp.cu", "k_mlp.o", []),
+           ("sortscan.cu", "sortscan.o", [])]
+HEADERS = ["np_math.cuh", "world_dev.cuh", "dyn.cuh", "narrow.cuh", "mlp.cuh", "sortscan.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -38,20 +43,24 @@ def _stale(obj, src):
     return any(os.path.getmtime(d) > t for d in deps)
 
 
-# The persistent solver kernel reads, after a grid barrier, data that other
-# SMs wrote: its global loads bypass L1 (-dlcm=cg) so none is served stale.
-EXTRA = {"k_solve.cu": ["-Xptxas", "-dlcm=cg"]}
+# The kernels whose blocks exchange data through global memory within one
+# launch (the persistent solvers, the dataflow colouring, the islands'
+# union-find, the cluster solvers) read, after a barrier or a flag, data that
+# other SMs wrote: their translation unit (k_solve.cu with
+# NPGPU_EXCHANGE_TU=1) has its global loads bypass L1 (-dlcm=cg) so none is
+# served stale. The other kernels keep L1 caching.
 
 
-def _compile(src):
+def _compile(entry):
+    src, obj, extra = entry
     s = os.path.join(CSRC, src)
-    o = os.path.join(OUT, src.replace(".cu", ".o"))
+    o = os.path.join(OUT, obj)
     if not _stale(o, s):
         return o, False
-    cmd = [nvcc()] + _flags() + EXTRA.get(src, []) + ["-c", s, "-o", o + ".tmp"]
+    cmd = [nvcc()] + _flags() + extra + ["-c", s, "-o", o + ".tmp"]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
-        raise RuntimeError(f"nvcc failed for {src}:\n{r.stdout}\n{r.stderr}")
+        raise RuntimeError(f"nvcc failed for {src} ({obj}):\n{r.stdout}\n{r.stderr}")
     os.replace(o + ".tmp", o)
     return o, True
 

@@ -12,10 +12,8 @@
 // Each pair is written by its owner (the collider with the smaller bounding
 // radius, ties by slot) so the list is deterministic and the previous step's
 // pairs of a collider are found without hashing.
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
-
 #include "narrow.cuh"
+#include "sortscan.cuh"
 
 namespace npgpu_dev {
 
@@ -457,17 +455,8 @@ __global__ void k_narrow(World w) {
     }
 }
 
-size_t sort_temp_bytes(uint32_t n) {
-    size_t bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, bytes, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
-                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
-    return bytes;
-}
-size_t scan_temp_bytes(uint32_t n) {
-    size_t bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
-    return bytes;
-}
+size_t sort_temp_bytes(uint32_t n) { return radix_sort_temp_bytes(n); }
+size_t scan_temp_bytes(uint32_t n) { return exclusive_scan_temp_bytes(n); }
 
 cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t st) {
     if (w.nc_slots == 0) return cudaSuccess;
@@ -477,8 +466,8 @@ cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t s
 
 cudaError_t launch_sort(const World& w, void* temp, size_t temp_bytes, cudaStream_t st) {
     if (w.nc_slots == 0) return cudaSuccess;
-    return cub::DeviceRadixSort::SortPairs(temp, temp_bytes, w.c.keys, w.c.keys_sorted, w.c.vals, w.c.vals_sorted,
-                                           (int)w.nc_slots, 0, kWorldShift + w.world_bits + 1, st);
+    return radix_sort_pairs(temp, temp_bytes, w.c.keys, w.c.keys_sorted, w.c.vals, w.c.vals_sorted, w.nc_slots,
+                            kWorldShift + (int)w.world_bits + 1, st);
 }
 
 cudaError_t launch_lbvh(const World& w, cudaStream_t st) {
@@ -496,7 +485,7 @@ cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStre
     cudaMemsetAsync(w.cur.owner_count, 0, sizeof(uint32_t) * w.nc_slots, st);
     if (n >= 1) {
         k_bp_traverse<false><<<nblocks(n), kThreads, 0, st>>>(w, n);
-        cudaError_t e = cub::DeviceScan::ExclusiveSum(temp, temp_bytes, w.c.leaf_count, w.c.leaf_offset, n, st);
+        cudaError_t e = exclusive_scan(temp, temp_bytes, w.c.leaf_count, w.c.leaf_offset, (uint32_t)n, st);
         if (e != cudaSuccess) return e;
         k_bp_traverse<true><<<nblocks(n), kThreads, 0, st>>>(w, n);
     }

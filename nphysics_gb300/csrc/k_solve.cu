@@ -29,14 +29,28 @@
 // same scheme over priorities. Threads poll their tasks without blocking, so
 // any assignment of manifolds to resident threads makes progress.
 #include <cooperative_groups.h>
-#include <cub/device/device_scan.cuh>
 
 #include "mlp.cuh"
 #include "narrow.cuh"
+#include "sortscan.cuh"
 
 namespace npgpu_dev {
 
 namespace cg = cooperative_groups;
+
+// This file is compiled twice. With NPGPU_EXCHANGE_TU=1 (and -dlcm=cg: global
+// loads bypass L1, so none is served stale) it holds the kernels whose blocks
+// exchange data through global memory within one launch: the islands'
+// union-find, the dataflow colouring, the one-grid velocity and position
+// solvers and the thread-block-cluster solvers. With NPGPU_EXCHANGE_TU=0 it
+// holds the other kernels, whose global reads may be cached in L1, and the
+// launchers, which reach the first group through exchange_kernel().
+#ifndef NPGPU_EXCHANGE_TU
+#define NPGPU_EXCHANGE_TU 0
+#endif
+enum ExchangeKernel { XK_COLOUR, XK_VELOCITY, XK_POSITION, XK_CLUSTER_VELOCITY, XK_CLUSTER_POSITION };
+const void* exchange_kernel(ExchangeKernel k);
+cudaError_t launch_activation(const World& w, const StepParams& p, unsigned nbb, unsigned npb, cudaStream_t st);
 
 constexpr int kItemThreads = 256;
 constexpr int kCoopThreads = 256;
@@ -186,8 +200,12 @@ __device__ __forceinline__ uint32_t pair_hash22(uint32_t c1, uint32_t c2) {
     h ^= h >> 15;
     return h >> 10;
 }
-__device__ __forceinline__ unsigned long long pair_priority(uint32_t c1, uint32_t c2) {
-    return ((unsigned long long)pair_hash22(c1, c2) << 42) | ((unsigned long long)c1 << 21) | (unsigned long long)c2;
+// Jones-Plassmann priority of a manifold, unique per collider pair: a hash of
+// the colliders' world-local slots (l1, l2), ties broken by the slots. Two
+// manifolds are compared only when they share a body, hence a world, so a
+// world's colouring does not change when its slots are shifted together.
+__device__ __forceinline__ unsigned long long pair_priority(uint32_t l1, uint32_t l2, uint32_t c1, uint32_t c2) {
+    return ((unsigned long long)pair_hash22(l1, l2) << 42) | ((unsigned long long)c1 << 21) | (unsigned long long)c2;
 }
 
 // Lock-free union-find over body slots (the larger root is linked under the smaller).
@@ -527,6 +545,7 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 }
 
 // ================================================================ activation
+#if NPGPU_EXCHANGE_TU
 __global__ void k_act_init(World w, StepParams p) {
     const Bodies& b = w.b;
     GRID_FOR(i, w.nb_slots) {
@@ -582,6 +601,7 @@ __global__ void k_act_init(World w, StepParams p) {
         c->learned_kept = 0u;
     }
 }
+#endif
 
 // A body is sleepy when it may sleep and its energy is below its threshold
 // (the per-body condition of activation_manager.rs:172-175).
@@ -594,6 +614,7 @@ __device__ __forceinline__ bool body_sleepy(const Bodies& b, uint32_t i, uint32_
 // nearest non-sleepy one uses only such edges); edges between two non-sleepy
 // bodies are skipped. The resulting sleep decisions equal the union-find over
 // all edges (activation_manager.rs:148-200).
+#if NPGPU_EXCHANGE_TU
 __global__ void k_act_union(World w) {
     const uint32_t npairs = w.ctl->npairs;
     const Bodies& b = w.b;
@@ -608,7 +629,9 @@ __global__ void k_act_union(World w) {
         uf_union(b.uf_parent, b1, b2, &w.ctl->err);
     }
 }
+#endif
 
+#if NPGPU_EXCHANGE_TU
 __global__ void k_act_root(World w) {
     const Bodies& b = w.b;
     GRID_FOR(i, w.nb_slots) {
@@ -618,7 +641,9 @@ __global__ void k_act_root(World w) {
         if (!body_sleepy(b, i, info)) atomicAnd(&b.can_deact[uf_find(b.uf_parent, i)], 0);
     }
 }
+#endif
 
+#if NPGPU_EXCHANGE_TU
 __global__ void k_act_apply(World w) {
     const Bodies& b = w.b;
     uint32_t active = 0;   // folded per warp below
@@ -645,11 +670,13 @@ __global__ void k_act_apply(World w) {
     active = __reduce_add_sync(0xffffffffu, active);
     if ((threadIdx.x & 31u) == 0u && active > 0u) atomicAdd(&w.ctl->nactive, active);
 }
+#endif
 
 // ================================================================ collection + colouring
 // Whole warps walk the pairs together, so a warp takes the solver slots of
 // its manifolds with one atomic (same-address atomics serialise in L2). The
 // slot order is free: everything downstream orders manifolds by priority.
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_collect(World w) {
     const uint32_t npairs = w.ctl->npairs;
     const Bodies& b = w.b;
@@ -690,7 +717,9 @@ __global__ void k_collect(World w) {
         if (s2 == 2u) atomicAdd(&b.adj_count[b2], 1u);
     }
 }
+#endif
 
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_adj_fill(World w) {
     const uint32_t ms = w.ctl->nsolver;
     GRID_FOR(m, ms) {
@@ -699,14 +728,16 @@ __global__ void k_adj_fill(World w) {
         if (b2 >= 0) w.s.adj[w.b.adj_start[b2] + atomicAdd(&w.b.adj_fill[b2], 1u)] = m;
     }
 }
+#endif
 
 __device__ __forceinline__ unsigned long long sm_priority(const World& w, uint32_t m) {
     uint2 pr = w.cur.pair[w.s.sm_list[m]];
-    return pair_priority(pr.x, pr.y);
+    return pair_priority(w.c.local[pr.x], w.c.local[pr.y], pr.x, pr.y);
 }
 
 // Rank of each manifold among the solver manifolds of each of its dynamic
 // bodies, by decreasing priority.
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_prank(World w) {
     const uint32_t ms = w.ctl->nsolver;
     GRID_FOR(m, ms) {
@@ -726,10 +757,12 @@ __global__ void k_prank(World w) {
         w.s.sm_prank[m] = r[0] | (r[1] << 16);
     }
 }
+#endif
 
 // Greedy first-fit colouring in decreasing priority: a manifold takes the
 // smallest colour unused by the higher-priority manifolds of its dynamic
 // bodies, as soon as those are coloured.
+#if NPGPU_EXCHANGE_TU
 __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     const uint32_t ms = w.ctl->nsolver;
     const uint32_t T = gridDim.x * blockDim.x;
@@ -803,10 +836,12 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
     ncol = __reduce_max_sync(0xffffffffu, ncol);
     if ((threadIdx.x & 31u) == 0u && ncol > 0u) atomicMax(&w.ctl->ncolours, ncol);
 }
+#endif
 
 // ================================================================ assembly
 // `rows`: also store each contact's three rows in full, for the one-grid
 // schedule's iterations.
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_assemble(World w, StepParams p, bool rows) {
     const uint32_t ms = w.ctl->nsolver;
     const Bodies& b = w.b;
@@ -935,6 +970,7 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
         }
     }
 }
+#endif
 
 // ================================================================ SOR-Prox
 // Row directions of a contact: -n for the normal row (body 1 side), and the
@@ -1346,7 +1382,7 @@ struct TaskStats {
     unsigned long long exec_ns, wait_ns, tasks;
 };
 
-__device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
+static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
                                 bool learned, TaskStats& ts, float4* cache) {
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
@@ -1425,7 +1461,7 @@ __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end
 }
 
 // FP64 residual over all rows; the result lands in ctl->residual.
-__device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t& epoch, bool initial) {
+static __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t& epoch, bool initial) {
     ResidualSums acc;
     GRID_FOR(m, ms) {
         int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
@@ -1452,6 +1488,7 @@ __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t&
     return grid_sync(w.ctl, epoch);
 }
 
+#if NPGPU_EXCHANGE_TU
 __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParams p) {
     __shared__ double sh[32];
     extern __shared__ float4 s_cache[];   // kCacheF4 per thread
@@ -1500,6 +1537,7 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
         if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->t_phase[0] = global_ns() - k0;
     }
 }
+#endif
 
 // ================================================================ batched worlds
 // Thousands of independent worlds: one block per world, the world's Δv in
@@ -1525,6 +1563,7 @@ __device__ __forceinline__ uint32_t world_bucket(const World& w, uint32_t m, uin
     return wd * kMaxColours + col;
 }
 
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_world_count(World w, uint32_t n_worlds) {
     const uint32_t ms = w.ctl->nsolver;
     GRID_FOR(m, ms) {
@@ -1532,7 +1571,9 @@ __global__ void k_world_count(World w, uint32_t n_worlds) {
         if (bucket != 0xffffffffu) atomicAdd(&w.s.bucket_count[bucket], 1u);
     }
 }
+#endif
 
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_world_scatter(World w, uint32_t n_worlds) {
     const uint32_t ms = w.ctl->nsolver;
     GRID_FOR(m, ms) {
@@ -1541,11 +1582,13 @@ __global__ void k_world_scatter(World w, uint32_t n_worlds) {
         w.s.wm_order[w.s.bucket_start[bucket] + atomicAdd(&w.s.bucket_cursor[bucket], 1u)] = m;
     }
 }
+#endif
 
 // Renumbers the solver manifolds in (world, colour) order: manifold i of the
 // new numbering is wm_order[i] of the old. Gathered into the scratch arrays
 // first, then copied back; assembly and everything after it use the new
 // numbering, so a colour of a world is one run of indices.
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_world_permute(World w, uint32_t n_worlds) {
     const uint32_t ms = w.ctl->nsolver, total = w.s.bucket_start[n_worlds * kMaxColours];
     const size_t P = w.cap_pairs;
@@ -1559,7 +1602,9 @@ __global__ void k_world_permute(World w, uint32_t n_worlds) {
         t[4 * P + i] = w.s.sm_colour[m];
     }
 }
+#endif
 
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_world_permute_back(World w) {
     const uint32_t ms = w.ctl->nsolver;
     const size_t P = w.cap_pairs;
@@ -1572,6 +1617,7 @@ __global__ void k_world_permute_back(World w) {
         w.s.sm_colour[i] = t[4 * P + i];
     }
 }
+#endif
 
 // World-local index of body slot b (-1 stays -1). A body outside the world's
 // slot range flags an error and the task is skipped.
@@ -1692,6 +1738,7 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
 // The first n_cluster worlds of the order are the cluster kernel's.
 // Dynamic shared memory: the larger of 6 floats per body slot of the largest
 // world and 6 floats per slot of a small world for each warp.
+#if !NPGPU_EXCHANGE_TU
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
                                                                   uint32_t max_world_bodies, uint32_t n_big,
@@ -1724,11 +1771,13 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World
         world_velocity(w, p, order[n_big + k], kWarpWorldBodies, my_dv, nullptr, wg);
     }
 }
+#endif
 
 // The widest worlds, one thread-block cluster each (cluster c takes world
 // order[c]): the world's Δv rows are spread over the cluster's shared
 // memories, 2^shift bodies per block, and the cluster barrier orders the
 // colours. Each block writes its own rows back to global memory.
+#if NPGPU_EXCHANGE_TU
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS, 1) k_cluster_velocity(World w, StepParams p, uint32_t shift) {
     extern __shared__ float s_dv[];
@@ -1753,7 +1802,9 @@ __global__ void __launch_bounds__(THREADS, 1) k_cluster_velocity(World w, StepPa
     // No block leaves while another may still read its shared memory.
     cl.sync();
 }
+#endif
 
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_world_finish(World w, StepParams p) {
     Control* c = w.ctl;
     c->residual_initial = sqrt(c->res_acc_init[0]) / fmax(1.0, sqrt(c->res_acc_init[1]));
@@ -1761,6 +1812,7 @@ __global__ void k_world_finish(World w, StepParams p) {
     c->res_acc[0] = c->res_acc[1] = 0.0;
     c->iterations = p.max_velocity_iterations;
 }
+#endif
 
 // A body pose as the position solver moves it.
 struct Pose {
@@ -1817,6 +1869,7 @@ __device__ __forceinline__ void publish_posef(unsigned long long* pf, int b, uin
 }
 
 // ================================================================ integrate
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
     const uint32_t ms = w.ctl->nsolver;
     const Bodies& b = w.b;
@@ -1856,6 +1909,7 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
         if (posef) publish_posef(b.posef, (int)i, 0u, load_pose(b, i), false);
     }
 }
+#endif
 
 // ================================================================ NonlinearSORProx
 // NonlinearSORProx::solve_unilateral for the contacts of manifold m
@@ -1956,6 +2010,7 @@ __device__ __forceinline__ void position_task(const World& w, const StepParams& 
     if (moved2) store_pose(w.b, bb2, P2);
 }
 
+#if NPGPU_EXCHANGE_TU
 __global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParams p) {
     const uint32_t ms = w.ctl->nsolver;
     const uint32_t T = gridDim.x * blockDim.x;
@@ -2008,6 +2063,7 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParam
         }
     }
 }
+#endif
 
 // Batched worlds: block per world, colour by colour, poses in global memory.
 // NonlinearSORProx sweeps of one world by one group, poses in global memory.
@@ -2027,6 +2083,7 @@ __device__ __forceinline__ void world_position(const World& w, const StepParams&
 
 // Batched worlds: large worlds one per block, then small worlds one per warp,
 // as in the velocity kernel.
+#if !NPGPU_EXCHANGE_TU
 template <int THREADS>
 __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big,
                                                             uint32_t n_cluster) {
@@ -2055,9 +2112,11 @@ __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams 
         world_position(w, p, order[n_big + k], wg);
     }
 }
+#endif
 
 // The cluster worlds' position sweeps: cluster c takes world order[c], the
 // cluster barrier between colours (poses stay in global memory).
+#if NPGPU_EXCHANGE_TU
 __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_position(World w, StepParams p) {
     if (w.ctl->err & ERRF_COLOURS) return;
     cg::cluster_group cl = cg::this_cluster();
@@ -2065,8 +2124,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_position(World w
     const WorldGroup g{cl.block_rank() * blockDim.x + threadIdx.x, nct * blockDim.x, GROUP_CLUSTER};
     world_position(w, p, w.s.world_order[blockIdx.x / nct], g);
 }
+#endif
 
 // ================================================================ post
+#if !NPGPU_EXCHANGE_TU
 __global__ void k_post(World w, StepParams p, bool posef) {
     __shared__ double sh[32];
     const Bodies& b = w.b;
@@ -2111,7 +2172,30 @@ __global__ void k_post(World w, StepParams p, bool posef) {
     double tke = block_sum(ke, sh);
     if (threadIdx.x == 0 && tke != 0.0) atomicAdd(&w.ctl->kinetic_energy, tke);
 }
+#endif
 
+#if NPGPU_EXCHANGE_TU
+const void* exchange_kernel(ExchangeKernel k) {
+    switch (k) {
+    case XK_COLOUR: return (const void*)k_colour;
+    case XK_VELOCITY: return (const void*)k_velocity;
+    case XK_POSITION: return (const void*)k_position;
+    case XK_CLUSTER_VELOCITY: return (const void*)k_cluster_velocity<kClusterThreads>;
+    case XK_CLUSTER_POSITION: return (const void*)k_cluster_position;
+    }
+    return nullptr;
+}
+
+// ActivationManager::update on the device: energies, the islands' union-find
+// over the contact pairs, and the islands' sleep decision.
+cudaError_t launch_activation(const World& w, const StepParams& p, unsigned nbb, unsigned npb, cudaStream_t st) {
+    k_act_init<<<nbb, kItemThreads, 0, st>>>(w, p);
+    k_act_union<<<npb, kItemThreads, 0, st>>>(w);
+    k_act_root<<<nbb, kItemThreads, 0, st>>>(w);
+    k_act_apply<<<nbb, kItemThreads, 0, st>>>(w);
+    return cudaGetLastError();
+}
+#else
 // ================================================================ launchers
 static unsigned item_blocks(uint32_t n) {
     unsigned b = (n + kItemThreads - 1) / kItemThreads;
@@ -2141,12 +2225,12 @@ static size_t world_smem(uint32_t max_world_bodies, int threads) {
 void solver_grid_sizes(int device, SolverLaunch& L) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_colour, kCoopThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, exchange_kernel(XK_COLOUR), kCoopThreads, 0);
     L.grid_colour = sms * (per < 1 ? 1 : per);
-    cudaFuncSetAttribute(k_velocity, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVelocitySmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_velocity, kCoopThreads, kVelocitySmem);
+    cudaFuncSetAttribute(exchange_kernel(XK_VELOCITY), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVelocitySmem);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, exchange_kernel(XK_VELOCITY), kCoopThreads, kVelocitySmem);
     L.grid_velocity = sms * (per < 1 ? 1 : per);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_position, kCoopThreads, 0);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, exchange_kernel(XK_POSITION), kCoopThreads, 0);
     L.grid_position = sms * (per < 1 ? 1 : per);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_world_position<128>, 128, 0);
     L.grid_world_position = sms * (per < 1 ? 1 : per);
@@ -2181,10 +2265,10 @@ int cluster_ctas(int device) {
     int ok = 0;
     cudaDeviceGetAttribute(&ok, cudaDevAttrClusterLaunch, device);
     if (!ok) return 0;
-    const void* fn = (const void*)k_cluster_velocity<kClusterThreads>;
+    const void* fn = exchange_kernel(XK_CLUSTER_VELOCITY);
     cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cluster_smem(kClusterShiftMax));
     cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    cudaFuncSetAttribute((const void*)k_cluster_position, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    cudaFuncSetAttribute(exchange_kernel(XK_CLUSTER_POSITION), cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
     for (int c : {16, 8}) {
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
@@ -2230,19 +2314,17 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         if (L.ev) cudaEventRecord(L.ev[k], st);
     };
     rec(0);
-    k_act_init<<<nbb, kItemThreads, 0, st>>>(wc, pc);
-    k_act_union<<<npb, kItemThreads, 0, st>>>(wc);
-    k_act_root<<<nbb, kItemThreads, 0, st>>>(wc);
-    k_act_apply<<<nbb, kItemThreads, 0, st>>>(wc);
+    cudaError_t e = launch_activation(wc, pc, nbb, npb, st);
+    if (e != cudaSuccess) return e;
     rec(1);
     k_collect<<<npb, kItemThreads, 0, st>>>(wc);
     size_t scan_bytes = L.scan_bytes;
-    cudaError_t e = cub::DeviceScan::ExclusiveSum(L.scan_temp, scan_bytes, w.b.adj_count, w.b.adj_start,
-                                                  (int)(w.nb_slots ? w.nb_slots : 1), st);
+    e = exclusive_scan(L.scan_temp, scan_bytes, w.b.adj_count, w.b.adj_start,
+                                   w.nb_slots ? w.nb_slots : 1u, st);
     if (e != cudaSuccess) return e;
     k_adj_fill<<<npb, kItemThreads, 0, st>>>(wc);
     k_prank<<<npb, kItemThreads, 0, st>>>(wc);
-    e = coop((const void*)k_colour, L.grid_colour, args1, st);
+    e = coop(exchange_kernel(XK_COLOUR), L.grid_colour, args1, st);
     if (e != cudaSuccess) return e;
     if (L.batched) {
         // Bucket the manifolds by (world, colour) and renumber them in that order.
@@ -2251,8 +2333,7 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         if (e != cudaSuccess) return e;
         k_world_count<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
         scan_bytes = L.scan_bytes;
-        e = cub::DeviceScan::ExclusiveSum(L.scan_temp, scan_bytes, w.s.bucket_count, w.s.bucket_start, (int)(nbk + 1),
-                                          st);
+        e = exclusive_scan(L.scan_temp, scan_bytes, w.s.bucket_count, w.s.bucket_start, nbk + 1u, st);
         if (e != cudaSuccess) return e;
         k_world_scatter<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
         k_world_permute<<<npb, kItemThreads, 0, st>>>(wc, L.n_worlds);
@@ -2265,7 +2346,7 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         if (L.n_cluster > 0) {
             uint32_t shift = L.cluster_shift;
             void* cargs[] = {&wc, &pc, &shift};
-            e = launch_cluster((const void*)k_cluster_velocity<kClusterThreads>, L, cluster_smem(shift), cargs, st);
+            e = launch_cluster(exchange_kernel(XK_CLUSTER_VELOCITY), L, cluster_smem(shift), cargs, st);
             if (e != cudaSuccess) return e;
         }
         if (L.n_worlds > L.n_cluster) {
@@ -2280,7 +2361,7 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
-        e = coop((const void*)k_velocity, L.grid_velocity, args2, st, kVelocitySmem);
+        e = coop(exchange_kernel(XK_VELOCITY), L.grid_velocity, args2, st, kVelocitySmem);
         if (e != cudaSuccess) return e;
     }
     rec(4);
@@ -2292,18 +2373,20 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         // kernel's block size: large worlds a block each, small ones a warp.
         if (L.n_cluster > 0) {
             void* cargs[] = {&wc, &pc};
-            e = launch_cluster((const void*)k_cluster_position, L, 0, cargs, st);
+            e = launch_cluster(exchange_kernel(XK_CLUSTER_POSITION), L, 0, cargs, st);
             if (e != cudaSuccess) return e;
         }
         if (L.n_worlds > L.n_cluster)
             k_world_position<128><<<L.grid_world_position, 128, 0, st>>>(wc, pc, L.n_worlds, L.n_big, L.n_cluster);
     } else {
-        e = coop((const void*)k_position, L.grid_position, args2, st);
+        e = coop(exchange_kernel(XK_POSITION), L.grid_position, args2, st);
         if (e != cudaSuccess) return e;
     }
     rec(6);
     k_post<<<nbb, kItemThreads, 0, st>>>(wc, pc, posef);
     return cudaGetLastError();
 }
+
+#endif  // NPGPU_EXCHANGE_TU
 
 }  // namespace npgpu_dev

@@ -1,10 +1,11 @@
 // k_static_pairs.cu -- broad phase over caller-provided AABBs with no
 // allocation: npgpu_find_pairs_static.
 //
-// Some callers cannot call cudaMalloc: code that runs while a CUDA graph is
-// being captured, real-time loops that must not block on the allocator, and
-// hosts whose device memory is owned by another runtime's pool. For them this
-// entry point runs the broad phase of the step (Morton keys, radix sort,
+// Some callers cannot call cudaMalloc: real-time control loops that must not
+// block on the allocator (cudaMalloc can synchronise the device and take
+// milliseconds), and plugins hosted by an application that owns all device
+// memory through its own pool and forbids allocations behind its back. For
+// them this entry point runs the broad phase of the step (Morton keys, radix sort,
 // linear BVH, owner traversal) on device buffers they already hold, with every
 // piece of scratch memory taken from one file-scope __device__ array of fixed
 // size (kScratchBytes, enough for kMaxAabbs boxes). Every GPU that loads the
@@ -13,16 +14,17 @@
 // Set-up: the first call on a device (with that device current) looks up the
 // array's device address with cudaGetSymbolAddress and checks the scratch
 // needs of the sort and scan; make that first call before any stream capture.
+// The address belongs to the device's current context: after the context is
+// destroyed and recreated (cudaDeviceReset), the next call sees a new
+// context id and does the set-up again.
 // Calls share the array: two calls whose work overlaps on the GPU (on
 // different streams, or on the same stream from different threads before the
 // first finishes) race on it.
-#include <cub/device/device_radix_sort.cuh>
-#include <cub/device/device_scan.cuh>
-
 #include <mutex>
 #include <string>
 
 #include "../../include/npgpu.h"
+#include "sortscan.cuh"
 
 namespace {
 
@@ -60,11 +62,8 @@ Layout make_layout(uint32_t n) {
     l.leaf_count = take(4ull * n);
     l.leaf_offset = take(4ull * n);
     l.total = take(16);
-    l.sort_bytes = 0;
-    cub::DeviceRadixSort::SortPairs(nullptr, l.sort_bytes, (unsigned long long*)nullptr, (unsigned long long*)nullptr,
-                                    (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
-    l.scan_bytes = 0;
-    cub::DeviceScan::ExclusiveSum(nullptr, l.scan_bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (int)n);
+    l.sort_bytes = npgpu_dev::radix_sort_temp_bytes(n);
+    l.scan_bytes = npgpu_dev::exclusive_scan_temp_bytes(n);
     l.sort_temp = take(l.sort_bytes);
     l.scan_temp = take(l.scan_bytes);
     l.end = o;
@@ -73,7 +72,36 @@ Layout make_layout(uint32_t n) {
 
 std::mutex g_mu;
 unsigned char* g_scratch_ptr[64];
+unsigned long long g_ctx_id[64];
 bool g_ready[64];
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId, reached
+// through the runtime's driver entry points so that the library needs no
+// link-time dependency on the driver library), or 0 if it cannot be read.
+typedef int (*CtxGetCurrentFn)(void**);
+typedef int (*CtxGetIdFn)(void*, unsigned long long*);
+unsigned long long current_context_id() {
+    static CtxGetCurrentFn get_current = nullptr;
+    static CtxGetIdFn get_id = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_current = (CtxGetCurrentFn)f;
+        f = nullptr;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            get_id = (CtxGetIdFn)f;
+        cudaGetLastError();
+    });
+    if (!get_current || !get_id) return 0;
+    void* ctx = nullptr;
+    unsigned long long id = 0;
+    if (get_current(&ctx) != 0 || !ctx || get_id(ctx, &id) != 0) return 0;
+    return id;
+}
 
 __device__ __forceinline__ uint64_t expand16s(uint32_t v) {
     uint64_t x = v & 0xffffu;
@@ -279,9 +307,14 @@ extern "C" npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint3
         return NPGPU_ERR_CUDA;
     }
     Layout layout = make_layout(kMaxAabbs);
+    unsigned char* base = nullptr;
     {
         std::lock_guard<std::mutex> lock(g_mu);
-        if (!g_ready[dev]) {
+        // 0 when no context is current yet (before the runtime's lazy
+        // initialisation): the set-up then runs and records the context the
+        // symbol lookup made current.
+        unsigned long long ctx = current_context_id();
+        if (!g_ready[dev] || ctx != g_ctx_id[dev]) {
             // Set-up, once per device: the device address of the scratch array.
             void* p = nullptr;
             cudaError_t e = cudaGetSymbolAddress(&p, g_pair_scratch);
@@ -295,11 +328,12 @@ extern "C" npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint3
                 return NPGPU_ERR_CAPACITY;
             }
             g_scratch_ptr[dev] = (unsigned char*)p;
+            g_ctx_id[dev] = current_context_id();
             g_ready[dev] = true;
         }
+        base = g_scratch_ptr[dev];
     }
     cudaStream_t st = (cudaStream_t)stream;
-    unsigned char* base = g_scratch_ptr[dev];
     Scratch s = scratch_at(base, layout);
     uint32_t* err = s.total + 1;
     cudaError_t e = cudaMemsetAsync(s.total, 0, 16, st);
@@ -309,8 +343,9 @@ extern "C" npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint3
     if (e == cudaSuccess && n > 0) {
         ks_keys<<<nb, T, 0, st>>>(s, aabbs6, groups, n);
         size_t sb = layout.sort_bytes;
-        e = cub::DeviceRadixSort::SortPairs(base + layout.sort_temp, sb, s.keys, s.keys_sorted, s.vals, s.vals_sorted,
-                                            (int)n, 0, 64, st);
+        // Without groups the keys' top 16 bits are zero: sort the 48 Morton bits only.
+        e = npgpu_dev::radix_sort_pairs(base + layout.sort_temp, sb, s.keys, s.keys_sorted, s.vals, s.vals_sorted,
+                                        n, groups ? 64 : 48, st);
         if (e == cudaSuccess && n >= 2) {
             e = cudaMemsetAsync(s.node_flag, 0, sizeof(int) * (size_t)(n - 1), st);
             ks_build<<<(n - 1 + T - 1) / T, T, 0, st>>>(s, (int)n);
@@ -319,7 +354,7 @@ extern "C" npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint3
             ks_refit<<<nb, T, 0, st>>>(s, aabbs6, (int)n, err);
             ks_traverse<false><<<nb, T, 0, st>>>(s, aabbs6, groups, (int)n, pairs2, max_pairs, err);
             size_t cb = layout.scan_bytes;
-            e = cub::DeviceScan::ExclusiveSum(base + layout.scan_temp, cb, s.leaf_count, s.leaf_offset, (int)n, st);
+            e = npgpu_dev::exclusive_scan(base + layout.scan_temp, cb, s.leaf_count, s.leaf_offset, n, st);
         }
         if (e == cudaSuccess) {
             ks_traverse<true><<<nb, T, 0, st>>>(s, aabbs6, groups, (int)n, pairs2, max_pairs, err);

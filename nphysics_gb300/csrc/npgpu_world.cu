@@ -157,6 +157,8 @@ struct npgpu_world {
     uint32_t sample_cap = 0;
     float* d_feat = nullptr;
     uint32_t max_world = 0;              // largest world index any body had (never lowered)
+    bool local_dirty = true;             // colliders or worlds changed: the colliders' world-local slots
+    std::vector<uint32_t> h_local;       // (Colliders::local) are recomputed before the next step
     std::vector<uint32_t> unregistered;  // colliders whose mass is not yet added to their body
     // CUDA graphs of one step (body start, solver, end-of-step collision
     // detection), one per parity of the double-buffered pair sets, keyed by
@@ -171,7 +173,10 @@ struct npgpu_world {
     int grid_world = 0;
 };
 
-static std::string g_create_error;
+// The message of the last failure without a world (npgpu_create, the
+// allocation-free pair finder), kept per host thread: a failing call on one
+// thread never rewrites the string another thread is reading.
+static thread_local std::string g_create_error;
 
 namespace npgpu_dev {
 // Message returned by npgpu_last_error(NULL) for calls without a world.
@@ -457,7 +462,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(b.info, B); A(b.world, B); A(b.gen, B); A(b.fstamp, B); A(b.dv, 6 * (size_t)B); A(b.sb, 3 * (size_t)B); A(b.dvf, 8 * (size_t)B); A(b.posef, 12 * (size_t)B); A(b.uf_parent, B); A(b.can_deact, B);
     A(b.cw, 2 * (size_t)B); A(b.adj_count, B); A(b.adj_start, B); A(b.adj_fill, B);
     Colliders& c = w->dw.c;
-    A(c.body, Cn); A(c.info, Cn); A(c.params, Cn); A(c.wrt_t, Cn); A(c.wrt_q, Cn);
+    A(c.body, Cn); A(c.local, Cn); A(c.info, Cn); A(c.params, Cn); A(c.wrt_t, Cn); A(c.wrt_q, Cn);
     A(c.margin, Cn); A(c.lin_pred, Cn); A(c.friction, Cn); A(c.restitution, Cn); A(c.rank, Cn);
     A(c.pose_t, Cn); A(c.pose_q, Cn); A(c.aabb_min, Cn); A(c.aabb_max, Cn);
     A(c.keys, Cn); A(c.keys_sorted, Cn); A(c.vals, Cn); A(c.vals_sorted, Cn);
@@ -482,7 +487,9 @@ static npgpu_status create_buffers(npgpu_world* w) {
     w->dw.prev = w->pb;
     w->dw.cap_pairs = P;
     w->sort_bytes = sort_temp_bytes(Cn);
-    w->scan_bytes = std::max(scan_temp_bytes(Cn), scan_temp_bytes(B));
+    // Scans: leaf counts (colliders), adjacency counts (bodies), and the
+    // per-world colour buckets (at most 128 per world, at most one world per body).
+    w->scan_bytes = std::max({scan_temp_bytes(Cn), scan_temp_bytes(B), scan_temp_bytes(128u * B + 1u)});
     CK(cudaMalloc(&w->sort_temp, std::max<size_t>(w->sort_bytes, 16)), "sort temp");
     o.push_back(w->sort_temp);
     CK(cudaMalloc(&w->scan_temp, std::max<size_t>(w->scan_bytes, 16)), "scan temp");
@@ -656,7 +663,7 @@ npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
         u.max_lin = d.max_linear_velocity;
         u.max_ang = d.max_angular_velocity;
         u.sleep_thr = d.sleep_threshold;
-        if (!hb.alive || hb.world != d.world) w->layout_dirty = true;
+        if (!hb.alive || hb.world != d.world) w->layout_dirty = w->local_dirty = true;
         w->max_world = std::max(w->max_world, d.world);
         hb.alive = true;
         hb.gen = handles[k].generation;
@@ -762,6 +769,7 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         up.push_back(u);
     }
     if (up.empty()) return NPGPU_OK;
+    w->local_dirty = true;
     void* dp = nullptr;
     npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(ColliderUpload), &dp);
     if (st != NPGPU_OK) return st;
@@ -800,6 +808,7 @@ npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
     }
     w->forget_pending = true;
     w->cd_dirty = true;
+    w->local_dirty = true;
     return kill_slots(w, slots, 1);
 }
 
@@ -820,7 +829,7 @@ npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
             }
         }
         w->hb[bi].alive = false;
-        w->layout_dirty = true;
+        w->layout_dirty = w->local_dirty = true;
         bslots.push_back((uint32_t)bi);
     }
     w->forget_pending = true;
@@ -941,6 +950,27 @@ static npgpu_status maintain(npgpu_world* w) {
         CK(cudaStreamSynchronize(w->stream), "forget");
         std::fill(w->forget.begin(), w->forget.end(), 0);
         w->forget_pending = false;
+    }
+    if (w->local_dirty) {
+        // World-local collider slots: slot minus the smallest alive collider
+        // slot of the same world (the colouring priority's hash input).
+        std::vector<uint32_t> base((size_t)w->max_world + 1, 0xffffffffu);
+        for (uint32_t ci = 0; ci < w->nc_slots; ++ci) {
+            const HostCollider& c = w->hc[ci];
+            if (!c.alive) continue;
+            uint32_t wd = w->hb[c.desc.body.index].world;
+            if (wd < base.size()) base[wd] = std::min(base[wd], ci);
+        }
+        w->h_local.assign(std::max<uint32_t>(w->nc_slots, 1u), 0u);
+        for (uint32_t ci = 0; ci < w->nc_slots; ++ci) {
+            const HostCollider& c = w->hc[ci];
+            uint32_t wd = c.alive ? w->hb[c.desc.body.index].world : 0xffffffffu;
+            w->h_local[ci] = (wd < base.size() && base[wd] <= ci) ? ci - base[wd] : ci;
+        }
+        CK(cudaMemcpyAsync(w->dw.c.local, w->h_local.data(), sizeof(uint32_t) * w->h_local.size(),
+                           cudaMemcpyHostToDevice, w->stream), "world-local collider slots");
+        CK(cudaStreamSynchronize(w->stream), "world-local collider slots");
+        w->local_dirty = false;
     }
     return NPGPU_OK;
 }
@@ -1446,6 +1476,27 @@ npgpu_status npgpu_mlp_samples(npgpu_world* w, float* out, uint32_t max_samples,
         CK(cudaMemcpy(out, w->d_samples, sizeof(float) * kMlpSampleFloats * (size_t)k, cudaMemcpyDeviceToHost),
            "samples download");
     }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_mlp_load_samples(npgpu_world* w, const float* samples, uint32_t n) {
+    if (!w || (n && !samples)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (!finite_n(samples, (int)std::min<uint64_t>((uint64_t)n * kMlpSampleFloats, 0x7fffffffu)))
+        return fail(w, NPGPU_ERR_NAN, "samples are not finite");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    w->dw.s.feat = nullptr;   // recording stops
+    if (n > w->sample_cap || !w->d_samples) {
+        cudaFree(w->d_samples);
+        w->d_samples = nullptr;
+        w->sample_cap = 0;
+        CK(cudaMalloc(&w->d_samples, sizeof(float) * kMlpSampleFloats * (size_t)std::max(n, 1u)), "samples");
+    }
+    w->sample_cap = std::max(n, 1u);
+    if (n) CK(cudaMemcpy(w->d_samples, samples, sizeof(float) * kMlpSampleFloats * (size_t)n, cudaMemcpyHostToDevice),
+              "samples upload");
+    CK(cudaMemcpy(&w->ctl->mlp_samples, &n, sizeof(n), cudaMemcpyHostToDevice), "samples");
+    w->dw.s.samples = w->d_samples;
+    w->dw.s.sample_cap = 0;
     return NPGPU_OK;
 }
 

@@ -88,6 +88,9 @@ struct Bodies {
 
 struct Colliders {
     uint32_t *body;
+    uint32_t *local;                 // slot minus the smallest alive collider slot of its body's world: the
+                                     // colouring priority hashes these, so that a world's colouring does not
+                                     // depend on where its slots start
     uint32_t *info;                  // shape | friction_combine << 4 | restitution_combine << 8 | alive << 16
     float4 *params;                  // ball: radius in x; cuboid: half extents
     float4 *wrt_t, *wrt_q;           // position_wrt_body

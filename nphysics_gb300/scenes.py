@@ -155,8 +155,8 @@ def ball_pile(side=32, radius=0.5, spacing=1.2, jitter=0.05, seed=1234, friction
     return Scene(f"ball pile ({side}^3 = {n} balls)", bodies, colliders, steps=600, info={"balls": n})
 
 
-def mixed_pile(n=100_000, seed=1234, friction=0.5, spacing=2.0, footprint=100.0):
-    """C3: n bodies, half balls with radius U(0.2, 0.8) and half cuboids with
+def mixed_lattice(n=100_000, seed=1234, friction=0.5, spacing=2.0, footprint=100.0):
+    """A lattice-placed mixed pile: n bodies, half balls with radius U(0.2, 0.8) and half cuboids with
     half extents U(0.2, 0.8)^3 and uniform random orientation, density 1,
     friction 0.5, over a 100 x 100 footprint. Bodies sit on a jittered 2.0
     lattice of layers from y = 1 upward so that none overlap at t = 0."""
@@ -182,7 +182,143 @@ def mixed_pile(n=100_000, seed=1234, friction=0.5, spacing=2.0, footprint=100.0)
     c["shape"] = shape
     c["shape_params"] = params
     bodies, colliders = _concat([g, b], [gc, c])
-    return Scene(f"mixed pile ({n} bodies)", bodies, colliders, steps=300, info={"bodies": n})
+    return Scene(f"mixed lattice pile ({n} bodies)", bodies, colliders, steps=300, info={"bodies": n})
+
+
+def _quat_matrices(q):
+    """Rotation matrices of unit quaternions in (i, j, k, w) order."""
+    x, y, z, w = (q[:, k].astype(np.float64) for k in range(4))
+    return np.stack([
+        np.stack([1 - 2 * (y * y + z * z), 2 * (x * y - z * w), 2 * (x * z + y * w)], axis=1),
+        np.stack([2 * (x * y + z * w), 1 - 2 * (x * x + z * z), 2 * (y * z - x * w)], axis=1),
+        np.stack([2 * (x * z - y * w), 2 * (y * z + x * w), 1 - 2 * (x * x + y * y)], axis=1)], axis=1)
+
+
+def _close_pairs(pos_q, rad_q, pos_o, rad_o, gap):
+    """Pairs (q, o) of a query set and another set of bodies whose bounding
+    spheres come within `gap` of each other (k-d tree range search)."""
+    from scipy.spatial import cKDTree
+    r = float(rad_q.max()) + float(rad_o.max()) + gap
+    m = cKDTree(pos_q).sparse_distance_matrix(cKDTree(pos_o), r, output_type="ndarray")
+    q, o = m["i"].astype(np.int64), m["j"].astype(np.int64)
+    near = m["v"] < rad_q[q] + rad_o[o] + gap
+    return q[near], o[near]
+
+
+def _shapes_overlap(i, j, pos, rot, is_ball, half, gap):
+    """Exact overlap test, inflated by `gap`, of the (ball or cuboid) shapes of
+    bodies i and j: distance of centres for two balls, the closest point of the
+    box for a ball and a box, the 15 separating axes for two boxes."""
+    out = np.zeros(len(i), bool)
+    bb = is_ball[i] & is_ball[j]
+    out[bb] = np.linalg.norm(pos[i[bb]] - pos[j[bb]], axis=1) < half[i[bb], 0] + half[j[bb], 0] + gap
+    mixed = is_ball[i] != is_ball[j]
+    if mixed.any():
+        b = np.where(is_ball[i[mixed]], i[mixed], j[mixed])
+        x = np.where(is_ball[i[mixed]], j[mixed], i[mixed])
+        local = np.einsum("nji,nj->ni", rot[x], pos[b] - pos[x])
+        closest = np.clip(local, -half[x], half[x])
+        out[mixed] = np.linalg.norm(local - closest, axis=1) < half[b, 0] + gap
+    xx = ~is_ball[i] & ~is_ball[j]
+    if xx.any():
+        a, b = i[xx], j[xx]
+        Ra, Rb, ha, hb = rot[a], rot[b], half[a], half[b]
+        d = pos[b] - pos[a]
+        axes = [Ra[:, :, k] for k in range(3)] + [Rb[:, :, k] for k in range(3)]
+        axes += [np.cross(Ra[:, :, p], Rb[:, :, q]) for p in range(3) for q in range(3)]
+        sep = np.zeros(len(a), bool)
+        for L in axes:
+            ln = np.linalg.norm(L, axis=1)
+            ok = ln > 1e-9
+            ra = sum(ha[:, k] * np.abs(np.einsum("ni,ni->n", Ra[:, :, k], L)) for k in range(3))
+            rb = sum(hb[:, k] * np.abs(np.einsum("ni,ni->n", Rb[:, :, k], L)) for k in range(3))
+            sep |= ok & (np.abs(np.einsum("ni,ni->n", d, L)) > ra + rb + gap * ln)
+        out[xx] = ~sep
+    return out
+
+
+def mixed_pile(n=100_000, seed=1234, friction=0.5, footprint=100.0, heights=(1.0, 60.0), gap=0.05):
+    """C3: n bodies, half balls with radius U(0.2, 0.8) and half cuboids with
+    half extents U(0.2, 0.8)^3 and uniform random orientation (Shoemake),
+    density 1, friction 0.5, dropped from centre heights U(1, 60) over a
+    100 x 100 footprint (x, z in U(-50, 50)) onto a static ground.
+
+    Initial overlaps are resolved by seeded rejection: the draws are made in
+    body order from one generator, then, pass after pass, every body that
+    overlaps an earlier one (exact ball / cuboid tests, inflated by `gap`) or
+    reaches below the ground's top face draws a new position from the same
+    distribution, until no body overlaps. Shapes and orientations are kept."""
+    rng = np.random.default_rng(seed)
+    is_ball = rng.permutation(n) < n // 2
+    half = np.zeros((n, 3), np.float32)
+    half[is_ball, 0] = rng.uniform(0.2, 0.8, size=int(is_ball.sum()))
+    half[~is_ball] = rng.uniform(0.2, 0.8, size=(int((~is_ball).sum()), 3))
+    quat = uniform_quaternions(rng, n)
+    quat[is_ball] = (0.0, 0.0, 0.0, 1.0)
+    lo = -footprint / 2
+
+    def draw(k):
+        p = np.stack([rng.uniform(lo, -lo, k), rng.uniform(heights[0], heights[1], k), rng.uniform(lo, -lo, k)],
+                     axis=1)
+        return p.astype(np.float32).astype(np.float64)
+
+    pos = draw(n)
+    rot = _quat_matrices(quat)
+    h64 = half.astype(np.float64)
+    radius = np.where(is_ball, h64[:, 0], np.linalg.norm(h64, axis=1))
+    # Lowest point of each shape above the ground's top face (y = 0).
+    reach = np.where(is_ball, h64[:, 0], np.einsum("nk,nk->n", np.abs(rot[:, 1, :]), h64))
+    # Seeded random sequential addition in body order: a pending body is
+    # placed once it overlaps neither a placed body nor an earlier pending one;
+    # one that overlaps a placed body or the ground moves to the first of a
+    # batch of fresh draws that is clear of every other body (the batch's last
+    # draw when none is).
+    pending = np.ones(n, bool)
+    passes = 0
+    while pending.any():
+        q_idx = np.nonzero(pending)[0]
+        q, o = _close_pairs(pos[q_idx], radius[q_idx], pos, radius, gap)
+        q = q_idx[q]
+        keep = q != o
+        q, o = q[keep], o[keep]
+        hit = _shapes_overlap(q, o, pos, rot, is_ball, h64, gap)
+        q, o = q[hit], o[hit]
+        redraw = np.zeros(n, bool)
+        wait = np.zeros(n, bool)
+        redraw[q[~pending[o]]] = True
+        wait[q[pending[o] & (o < q)]] = True
+        redraw |= pending & (pos[:, 1] - reach < gap)
+        pending &= redraw | wait
+        movers = np.nonzero(redraw)[0]
+        if len(movers):
+            m = int(max(1, min(64, 65536 // len(movers))))
+            cand = draw(len(movers) * m)
+            owner = np.repeat(movers, m)
+            cq, co = _close_pairs(cand, radius[owner], pos, radius, gap)
+            keep = co != owner[cq]
+            cq, co = cq[keep], co[keep]
+            ext = np.concatenate([pos, cand])
+            ov = _shapes_overlap(cq + n, co, ext, np.concatenate([rot, rot[owner]]),
+                                 np.concatenate([is_ball, is_ball[owner]]), np.concatenate([h64, h64[owner]]), gap)
+            blocked = np.zeros(len(cand), bool)
+            blocked[cq[ov]] = True
+            blocked |= cand[:, 1] - reach[owner] < gap
+            free = ~blocked.reshape(len(movers), m)
+            pick = np.where(free.any(axis=1), free.argmax(axis=1), m - 1)
+            pos[movers] = cand.reshape(len(movers), m, 3)[np.arange(len(movers)), pick]
+        passes += 1
+        if passes > 1000:
+            raise RuntimeError("mixed_pile: overlaps not resolved in 1000 passes")
+    g, gc = _ground(half=(footprint * 0.8, 1.0, footprint * 0.8), friction=friction)
+    b = body_descs(n)
+    b["position"][:, :3] = pos.astype(np.float32)
+    b["position"][:, 3:7] = quat
+    c = collider_descs(n, np.arange(n), abi.SHAPE_BALL, (0, 0, 0), density=1.0, friction=friction)
+    c["shape"] = np.where(is_ball, abi.SHAPE_BALL, abi.SHAPE_CUBOID).astype(np.uint32)
+    c["shape_params"] = half
+    bodies, colliders = _concat([g, b], [gc, c])
+    return Scene(f"mixed pile ({n} bodies)", bodies, colliders, steps=300,
+                 info={"bodies": n, "placement_passes": passes})
 
 
 def batched_worlds(n_worlds=4096, seed=1234, lo=16, hi=2048, worlds=None):

@@ -200,6 +200,11 @@ class GpuWorld:
             self._check(self.L.npgpu_mlp_samples(self.w, _ptr(out, C.c_float), n.value, C.byref(n)), "mlp_samples")
         return out
 
+    def mlp_load_samples(self, samples):
+        samples = np.ascontiguousarray(samples, np.float32).reshape(-1, abi.MLP_SAMPLE_FLOATS)
+        self._check(self.L.npgpu_mlp_load_samples(self.w, _ptr(samples, C.c_float), samples.shape[0]),
+                    "mlp_load_samples")
+
     def mlp_train(self, steps, batch=4096, lr=1e-3, seed=1, init=False):
         loss = C.c_float(0.0)
         self._check(self.L.npgpu_mlp_train(self.w, steps, batch, lr, seed, abi.MLP_INIT if init else 0,

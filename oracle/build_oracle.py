@@ -28,7 +28,7 @@ def build(force=False):
     if not force and not _stale():
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
-    cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
+    cmd = ["g++", "-std=c++17", "-O3", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
            "-Wall", "-Wno-unused-function", "-o", LIB + ".tmp"] + SOURCES
     subprocess.run(cmd, check=True)
     os.replace(LIB + ".tmp", LIB)

@@ -58,9 +58,12 @@ inline uint32_t pair_hash22(uint32_t c1, uint32_t c2) {
     h ^= h >> 15;
     return h >> 10;
 }
-// Jones-Plassmann priority of a manifold: unique per collider pair.
-inline uint64_t pair_priority(uint32_t c1, uint32_t c2) {
-    return (uint64_t(pair_hash22(c1, c2)) << 42) | (uint64_t(c1) << 21) | uint64_t(c2);
+// Jones-Plassmann priority of a manifold: unique per collider pair. The hash
+// takes the colliders' world-local slots (slot minus the smallest alive
+// collider slot of the world), so a world's colouring does not depend on
+// where its slots start; ties are broken by the slots themselves.
+inline uint64_t pair_priority(uint32_t l1, uint32_t l2, uint32_t c1, uint32_t c2) {
+    return (uint64_t(pair_hash22(l1, l2)) << 42) | (uint64_t(c1) << 21) | uint64_t(c2);
 }
 
 template <class R> struct Approx {
@@ -1242,17 +1245,30 @@ public:
         std::vector<uint64_t> best(bodies.size(), 0);
         std::vector<uint64_t> used(2 * bodies.size(), 0);   // colours 0-63 and 64-127 of each body
         std::vector<Manifold<R>*> todo = ms;
+        // World-local collider slots.
+        std::vector<uint32_t> base, local(colliders.size());
+        for (uint32_t c = 0; c < colliders.size(); ++c) {
+            if (!colliders[c].alive) continue;
+            uint32_t wd = bodies[colliders[c].body].world;
+            if (wd >= base.size()) base.resize(wd + 1, 0xffffffffu);
+            base[wd] = std::min(base[wd], c);
+        }
+        for (uint32_t c = 0; c < colliders.size(); ++c) {
+            uint32_t wd = colliders[c].alive ? bodies[colliders[c].body].world : 0xffffffffu;
+            local[c] = (wd < base.size() && base[wd] <= c) ? c - base[wd] : c;
+        }
+        auto prio = [&](const Manifold<R>* m) { return pair_priority(local[m->c1], local[m->c2], m->c1, m->c2); };
         uint32_t ncol = 0;
         while (!todo.empty()) {
             for (Manifold<R>* m : todo) {
-                uint64_t p = pair_priority(m->c1, m->c2);
+                uint64_t p = prio(m);
                 uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
                 if (bodies[b1].dynamic()) best[b1] = std::max(best[b1], p);
                 if (bodies[b2].dynamic()) best[b2] = std::max(best[b2], p);
             }
             std::vector<Manifold<R>*> rest, won;
             for (Manifold<R>* m : todo) {
-                uint64_t p = pair_priority(m->c1, m->c2);
+                uint64_t p = prio(m);
                 uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
                 bool w = (!bodies[b1].dynamic() || best[b1] == p) && (!bodies[b2].dynamic() || best[b2] == p);
                 (w ? won : rest).push_back(m);

@@ -38,7 +38,7 @@ CASES = {
     "pyramid_base6": (lambda: scenes.pyramid(base=6), 32, ORDER_COLOUR, (1, 20, 120)),
     "ball_pile_side5": (lambda: scenes.ball_pile(side=5), 32, ORDER_COLOUR, (1, 30, 90)),
     "cluster_64": (lambda: scenes.random_cluster(n=64, seed=7, extent=3.0), 32, ORDER_COLOUR, (1, 10, 40)),
-    "mixed_300": (lambda: scenes.mixed_pile(n=300, seed=5, footprint=12.0), 32, ORDER_COLOUR, (1, 90, 200)),
+    "mixed_300": (lambda: scenes.mixed_lattice(n=300, seed=5, footprint=12.0), 32, ORDER_COLOUR, (1, 90, 200)),
     "batched_6": (lambda: scenes.batched_worlds(n_worlds=6, seed=3, lo=8, hi=120), 32, ORDER_COLOUR, (1, 25)),
     "brick_walls_2x48": (lambda: scenes.brick_walls(n_walls=2, width=8, height=6, balls=3, seed=5), 32, ORDER_COLOUR,
                          (1, 60, 150)),

@@ -111,11 +111,11 @@ def test_product_never_uses_the_oracle():
 
 
 def test_rust_binding_declares_every_entry_point():
-    # The reference-side binding (INTEGRATION.md's extern "C" block) names every
-    # function include/npgpu.h declares.
-    text = open(os.path.join(ROOT, "INTEGRATION.md")).read()
+    # The reference-side binding (the Rust crate's extern "C" block) names
+    # every function include/npgpu.h declares.
+    text = open(os.path.join(ROOT, "rust", "nphysics3d-gpu", "src", "ffi.rs")).read()
     i = text.index('extern "C" {')
-    block = text[i:text.index("}\n```", i)]
+    block = text[i:text.index("\n}", i)]
     missing = [f for f in declared_functions() if re.search(r"\bfn " + f + r"\(", block) is None]
     assert not missing, missing
 

@@ -23,6 +23,10 @@ def test_reference_arm_prints_one_contract_line():
     assert d["metric"] == "body-steps/s" and d["higher_is_better"] is True and d["value"] > 0
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("reference", "port") and cb["cores"] >= 1 and cb["sample"] and cb["value"] == d["value"]
+    assert cb["host_cores"] >= 1 and "cpu_model" in cb
+    # The timed window starts where the GPU arm's does: settle, the
+    # autotuner's 13 steps on a single world, then the warm-up.
+    assert "timed steps 15..16 of the run" in d["config"]["workload"]
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0

@@ -141,6 +141,54 @@ def test_converged_velocities_match_reference_order(gpu_lib):
     assert_close_rel(g.bodies()["velocity"], o.bodies()["velocity"], 1e-4, 1e-5, "converged velocities")
 
 
+def ball_stack(k, radius=0.5):
+    """k balls stacked vertically, each touching the next, the lowest on the ground."""
+    g, gc = scenes._ground(friction=0.5)
+    b = scenes.body_descs(k)
+    b["position"][:, 0] = 0.3
+    b["position"][:, 1] = radius + 2 * radius * np.arange(k)
+    b["position"][:, 2] = -0.7
+    c = scenes.collider_descs(k, np.arange(k), abi.SHAPE_BALL, (radius, 0, 0), density=1.0, friction=0.5)
+    bodies, colliders = scenes._concat([g, b], [gc, c])
+    return scenes.Scene(f"stack of {k} balls", bodies, colliders)
+
+
+@pytest.mark.parametrize("k", [1, 2, 5])
+def test_converged_impulses_match_f64(gpu_lib, k):
+    # A ball on the ground and stacks of balls: one contact per touching pair,
+    # so the converged impulses are unique. A single step from rest solved to a
+    # tight residual: the GPU (f32, colour order) matches the f64 oracle in the
+    # reference's order within 1e-4 relative, and both match the statics:
+    # contact i from the top carries i ball weights, m g dt each.
+    from nphysics_gb300.world import GpuWorld
+    sc = ball_stack(k)
+    p = sc.params()
+    p.solve_to_tolerance = 1
+    p.residual_tolerance = 1e-6
+    p.max_iterations_to_tolerance = 4000
+    g = GpuWorld.for_scene(sc, p)
+    g.step(1)
+    q = sc.params()
+    q.solve_to_tolerance = 1
+    q.residual_tolerance = 1e-12
+    q.max_iterations_to_tolerance = 4000
+    o = OracleWorld(q, sc.gravity, precision=64, order=ORDER_REFERENCE)
+    o.load_scene(sc)
+    o.step(1)
+    kg, cg = contact_table(g.contacts())
+    oc = o.contacts()                      # keys, in the same order as the f64 rows
+    oc["impulse"] = o.contacts_f64()[:, 10:13]
+    ko, co = contact_table(oc)
+    np.testing.assert_array_equal(kg, ko)
+    assert len(kg) == k
+    assert_close_rel(cg["impulse"][:, 0], co["impulse"][:, 0], 1e-4, 0.0, "converged normal impulses")
+    m = 4.0 / 3.0 * np.pi * 0.5 ** 3
+    # The contact with the ground is (0, 1); ball j sits on ball j - 1.
+    weights = np.array([k - (int(c2) - 1) for c2 in cg["collider2"]], np.float64)
+    assert_close_rel(cg["impulse"][:, 0], weights * m * 9.81 / 60.0, 1e-4, 0.0, "statics")
+    assert np.abs(cg["impulse"][:, 1:]).max() <= 1e-6
+
+
 def test_pyramid_1000_steps_resting_poses(gpu_lib):
     sc = scenes.pyramid(base=20)
     g, o = make_pair(sc)
@@ -149,19 +197,23 @@ def test_pyramid_1000_steps_resting_poses(gpu_lib):
     gp, op = g.bodies()["position"], o.bodies()["position"]
     assert np.abs(gp[:, :3] - op[:, :3]).max() < 1e-3
     assert np.abs(np.abs(gp[:, 3:]) - np.abs(op[:, 3:])).max() < 1e-3
-    # Against the f64 oracle in the reference's own order. The resting pyramid
-    # creeps sideways at a rate that depends on the Gauss-Seidel order and the
-    # precision, so the bound is the oracle's own spread: f32 vs f64, both in
-    # the reference's order, and f64 reference vs f64 colour order.
+    # Against the f64 oracle. The pyramid does not rest exactly: its layers
+    # first separate by the collider margins (the top box rises 0.24-0.28 m),
+    # and at 8 velocity iterations the stack creeps sideways at a rate that
+    # depends on the Gauss-Seidel order and the precision. Measured drifts
+    # after 1000 steps (maximum over boxes and axes):
+    #   GPU (= f32 oracle, colour order) vs f64 oracle, colour order: 0.054 m
+    #   GPU vs f64 oracle, the reference's order:                     0.328 m
+    #   f64 colour order vs f64 reference order (the orders alone):   0.275 m
+    #   f32 vs f64, both in the reference's order:                    0.027 m
+    # The bounds are those measurements with a 20 % margin.
     def run(prec, order):
         w = OracleWorld(sc.params(), sc.gravity, precision=prec, order=order)
         w.load_scene(sc)
         w.step(1000)
         return w.bodies()["position"][:, :3]
-    ref = run(64, ORDER_REFERENCE)
-    spread = max(np.abs(run(32, ORDER_REFERENCE) - ref).max(), np.abs(run(64, ORDER_COLOUR) - ref).max())
-    drift = np.abs(gp[:, :3] - ref).max()
-    assert drift <= 1.5 * spread + 0.02, (drift, spread)
+    assert np.abs(gp[:, :3] - run(64, ORDER_COLOUR)).max() <= 0.065
+    assert np.abs(gp[:, :3] - run(64, ORDER_REFERENCE)).max() <= 0.40
     assert g.counters()["max_penetration"] < 0.05
     assert g.bodies()["active"].sum() == 0   # the whole stack fell asleep, as in the oracle
     assert o.bodies()["active"].sum() == 0

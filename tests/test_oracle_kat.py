@@ -364,3 +364,35 @@ def test_friction_combine_rule_sets_the_deceleration(mu_box, m_box, mu_ground, m
     v6 = w.bodies()["velocity"][1, 0]
     decel = (v5 - v6) / F32_DT
     assert abs(decel - mu * F32_G) < 0.05 * mu * F32_G, (decel, mu * F32_G)
+
+
+@pytest.mark.parametrize("k", [1, 2, 5])
+def test_converged_stack_impulses_f32_colour_vs_f64(k):
+    # The oracle's own f32 colour order (the GPU's sequence) solved to 1e-6
+    # against its f64 build in the reference's order solved to 1e-12: the
+    # converged normal impulses of a ball stack agree within 1e-4 relative
+    # and equal the statics, i ball weights m g dt at the i-th contact from
+    # the top.
+    from nphysics_gb300 import abi as _abi
+    g, gc = scenes._ground(friction=0.5)
+    b = scenes.body_descs(k)
+    b["position"][:, 1] = 0.5 + np.arange(k)
+    c = scenes.collider_descs(k, np.arange(k), _abi.SHAPE_BALL, (0.5, 0, 0), density=1.0, friction=0.5)
+    bodies, colliders = scenes._concat([g, b], [gc, c])
+    sc = scenes.Scene("ball stack", bodies, colliders)
+    out = []
+    for prec, order, tol in ((32, ORDER_COLOUR, 1e-6), (64, ORDER_REFERENCE, 1e-12)):
+        p = sc.params()
+        p.solve_to_tolerance = 1
+        p.residual_tolerance = tol
+        p.max_iterations_to_tolerance = 4000
+        o = OracleWorld(p, sc.gravity, precision=prec, order=order)
+        o.load_scene(sc)
+        o.step(1)
+        cs = o.contacts()
+        order_ = np.argsort(cs["collider2"])
+        out.append(o.contacts_f64()[order_, 10])
+    m = 4.0 / 3.0 * np.pi * 0.5 ** 3
+    statics = (k - np.arange(k)) * m * 9.81 / 60.0
+    np.testing.assert_allclose(out[0], out[1], rtol=1e-4)
+    np.testing.assert_allclose(out[1], statics, rtol=1e-6)
