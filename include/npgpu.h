@@ -174,7 +174,9 @@ typedef struct npgpu_params {
     float residual_tolerance;              /* 1e-4 */
     uint32_t max_iterations_to_tolerance;  /* cap when solve_to_tolerance (e.g. 256) */
     uint32_t warmstart_mode;               /* 0: impulse cache (reference); 1: none; 2: impulse cache, and the
-                                              learned network for contacts without a cache entry */
+                                              learned network for contacts without a cache entry; 3: the
+                                              network for every contact, each prediction kept only where
+                                              it beats the start it replaces (cache or zero) */
     float broad_phase_margin;              /* DBVTBroadPhase::new(0.01), geometrical_world.rs:60 */
     float activation_mix;                  /* ActivationManager::new(0.01), mechanical_world.rs:80 */
     uint32_t profile;                      /* non-zero: time each phase with CUDA events */
@@ -390,9 +392,10 @@ npgpu_status npgpu_find_pairs_static(const float* aabbs6, const uint32_t* groups
 /* ---- Learned warm start (no counterpart in the reference) ----
  * A 24 -> 64 -> 64 -> 3 perceptron (ReLU, bf16 weights, fp32 accumulation)
  * predicts the starting impulses (normal, tangent 1, tangent 2) of contacts
- * that have no impulse-cache entry when params.warmstart_mode == 2. The
- * warm-start sweep keeps a prediction only if the contact's local residual is
- * no larger than with a zero start, so the iteration count to a residual
+ * that have no impulse-cache entry when params.warmstart_mode == 2, and of
+ * every contact when it is 3. The warm-start sweep keeps a prediction only if
+ * the contact's local residual is no larger than with the start it replaced
+ * (the cached impulses, or zero), so the iteration count to a residual
  * tolerance stays the measure.
  *
  * Parameters (fp32, NPGPU_MLP_PARAMS floats): W1[64][24] b1[64] W2[64][64]

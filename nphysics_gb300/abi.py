@@ -279,7 +279,7 @@ EXPORTED = [
 ]
 
 # Learned warm start (npgpu_mlp_*).
-WARMSTART_CACHE, WARMSTART_NONE, WARMSTART_LEARNED = 0, 1, 2
+WARMSTART_CACHE, WARMSTART_NONE, WARMSTART_LEARNED, WARMSTART_LEARNED_ALL = 0, 1, 2, 3
 MLP_IN, MLP_HIDDEN, MLP_OUT = 24, 64, 3
 MLP_PARAMS = 6009
 MLP_TRAINABLE = 5955

@@ -904,7 +904,9 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
         }
         float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
         float4* lam = w.s.lam + (size_t)m * kMaxContacts;
-        const bool learned = p.warmstart_mode == 2u && w.mlp != nullptr;
+        // Learned starts: mode 2 for contacts without a cache entry, mode 3
+        // for every contact.
+        const bool learned = (p.warmstart_mode == 2u || p.warmstart_mode == 3u) && w.mlp != nullptr;
         const bool record = w.s.feat != nullptr;
         const float k1 = (float)((rk >> 8) & 0xffu), k2 = (float)(rk >> 24);
         for (uint32_t k = 0; k < nc; ++k) {
@@ -944,10 +946,13 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
                 }
             }
             const bool cold = p.warmstart_mode == 1u;
-            lam[k] = make_float4(cold ? 0.0f : imp.x * p.warmstart_coeff, cold ? 0.0f : imp.y * p.warmstart_coeff,
-                                 cold ? 0.0f : imp.z * p.warmstart_coeff, 0.0f);
+            const float4 start = make_float4(cold ? 0.0f : imp.x * p.warmstart_coeff,
+                                             cold ? 0.0f : imp.y * p.warmstart_coeff,
+                                             cold ? 0.0f : imp.z * p.warmstart_coeff, 0.0f);
+            lam[k] = start;
             const bool fresh = imp.w == 0.0f;   // no impulse-cache entry
-            if (record || (learned && fresh)) {
+            const bool predict = learned && (fresh || p.warmstart_mode == 3u);
+            if (record || predict) {
                 rn[RF_RHS] = rhs;
                 float feat[kMlpIn];
                 float gn_dt = (p.gx * n.x + p.gy * n.y + p.gz * n.z) * dt;
@@ -958,11 +963,13 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
 #pragma unroll
                     for (int i = 0; i < kMlpIn; ++i) fo[i] = feat[i];
                 }
-                if (learned && fresh) {
+                if (predict) {
                     float pl[kMlpOut];
                     mlp_forward(w.mlp, feat, pl);
                     mlp_project(mu, pl);
-                    // .w = 1: a predicted start, checked in the warm-start sweep.
+                    // .w = 1: a predicted start, checked in the warm-start
+                    // sweep against the start it replaces (kept beside it).
+                    w.s.lam_alt[(size_t)m * kMaxContacts + k] = fresh ? make_float4(0.0f, 0.0f, 0.0f, 0.0f) : start;
                     lam[k] = make_float4(pl[0], pl[1], pl[2], 1.0f);
                     atomicAdd(&w.ctl->learned_starts, 1u);
                 }
@@ -1010,6 +1017,7 @@ struct GlobalContacts {
     const float4* con;
     float4* lam;
     const float4* tan;               // the friction directions assembly stored
+    const float4* alt;               // learned starts: the start each prediction replaced
     __device__ __forceinline__ ContactRec rec(uint32_t k) const { return load_con(con, k); }
     __device__ __forceinline__ void tangents(const ContactRec&, uint32_t k, np::V* t) const {
         const float4 a = __ldg(tan + 2 * k), b = __ldg(tan + 2 * k + 1);
@@ -1018,6 +1026,7 @@ struct GlobalContacts {
     }
     __device__ __forceinline__ float4 get_lam(uint32_t k) const { return lam[k]; }
     __device__ __forceinline__ void set_lam(uint32_t k, float4 v) const { lam[k] = v; }
+    __device__ __forceinline__ float4 get_alt(uint32_t k) const { return alt[k]; }
 };
 
 // A contact row as the iterations read it (stored in full at assembly).
@@ -1196,13 +1205,21 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
             }
             if (predicted) {
                 // A learned start stays only if its local residual is no larger
-                // than the zero start's.
-                const float zero[3] = {0.0f, 0.0f, 0.0f};
+                // than that of the start it replaced (the cached impulses, or
+                // zero), which is otherwise applied instead.
+                const float4 a4 = src.get_alt(k);
+                const float alt[3] = {a4.x, a4.y, a4.z};
                 float with = local_residual(c, t, mask, dv, li, h1, h2);
-                float without = local_residual(c, t, mask, before, zero, h1, h2);
+                DV dv_alt = before;
+#pragma unroll 1
+                for (int row = 0; row < 3; ++row) {
+                    if (alt[row] == 0.0f) continue;
+                    axpy(row_dir(c, row, t), c.pos1, c.pos2, mask, bm, dv_alt, alt[row], h1, h2);
+                }
+                float without = local_residual(c, t, mask, dv_alt, alt, h1, h2);
                 if (with > without) {
-                    dv = before;
-                    src.set_lam(k, make_float4(0.0f, 0.0f, 0.0f, 0.0f));
+                    dv = dv_alt;
+                    src.set_lam(k, make_float4(alt[0], alt[1], alt[2], 0.0f));
                 } else {
                     src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
                     atomicAdd(&ctl->learned_kept, 1u);
@@ -1297,7 +1314,8 @@ __device__ __forceinline__ void warm_task(const World& w, uint32_t m, int g1, in
     if (g1 >= 0) bm.s[0] = load_sb(w.b.sb, g1);
     if (g2 >= 0) bm.s[1] = load_sb(w.b.sb, g2);
     GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts,
-                       w.s.tan + (size_t)m * kMaxContacts * 2};
+                       w.s.tan + (size_t)m * kMaxContacts * 2,
+                       w.s.lam_alt ? w.s.lam_alt + (size_t)m * kMaxContacts : nullptr};
     velocity_task_src<SWEEP_WARM>(src, w.s.sm_nc[m], w.s.sm_mask[m], 0u, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
 }
 
@@ -1317,7 +1335,8 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     if (g1 >= 0) bm.s[0] = load_sb(w.b.sb, g1);
     if (g2 >= 0) bm.s[1] = load_sb(w.b.sb, g2);
     GlobalContacts src{w.s.con + (size_t)m * kMaxContacts * 4, w.s.lam + (size_t)m * kMaxContacts,
-                       w.s.tan + (size_t)m * kMaxContacts * 2};
+                       w.s.tan + (size_t)m * kMaxContacts * 2,
+                       w.s.lam_alt ? w.s.lam_alt + (size_t)m * kMaxContacts : nullptr};
     DV dv;
     dva.load(g1 >= 0 ? l1 : -1, dv.a);
     dva.load(g2 >= 0 ? l2 : -1, dv.b);
@@ -1502,7 +1521,7 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
     // reports it instead of solving.
     if (w.ctl->err & ERRF_COLOURS) return;
     const bool prof = p.profile != 0;
-    const bool learned = p.warmstart_mode == 2u;
+    const bool learned = p.warmstart_mode == 2u || p.warmstart_mode == 3u;
     TaskStats ts{0ull, 0ull, 0ull};
     unsigned long long k0 = 0;
     if (prof && blockIdx.x == 0 && threadIdx.x == 0) k0 = global_ns();

@@ -1065,9 +1065,10 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
     if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
     if (num_joints) return fail(w, NPGPU_ERR_NONEMPTY_JOINTS, "joint constraints are not supported");
     if (num_force_generators) return fail(w, NPGPU_ERR_NONEMPTY_FORCES, "force generators are not supported");
-    if (w->params.warmstart_mode == 2 && !w->net_ready)
-        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "warmstart_mode 2 needs a network (npgpu_mlp_set or npgpu_mlp_train)");
-    if (w->params.warmstart_mode > 2) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown warmstart_mode");
+    if ((w->params.warmstart_mode == 2 || w->params.warmstart_mode == 3) && !w->net_ready)
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT,
+                    "warmstart_mode 2 and 3 need a network (npgpu_mlp_set or npgpu_mlp_train)");
+    if (w->params.warmstart_mode > 3) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown warmstart_mode");
     StepParams sp = step_params(w);
     for (uint32_t s = 0; s < nsteps; ++s) {
         npgpu_status st = maintain(w);
@@ -1402,6 +1403,9 @@ static npgpu_status mlp_alloc(npgpu_world* w) {
     CK(cudaMalloc(&w->d_m2, sizeof(float) * kMlpTrainable), "adam");
     CK(cudaMalloc(&w->d_grad, sizeof(float) * kMlpTrainable), "gradient");
     CK(cudaMalloc(&w->d_stats, sizeof(double) * 2 * (kMlpIn + kMlpOut)), "statistics");
+    // The starts that learned predictions replace, one per contact slot.
+    CK(cudaMalloc(&w->dw.s.lam_alt, sizeof(float4) * kMaxContacts * (size_t)w->cap_p), "replaced starts");
+    w->owned.push_back(w->dw.s.lam_alt);
     return NPGPU_OK;
 }
 

@@ -131,6 +131,8 @@ struct Solver {
     uint32_t *sm_nc;
     float4 *con;                     // 4 contacts x 4 float4 per solver manifold (constant during the solve)
     float4 *lam;                     // 4 contacts per solver manifold: impulses (normal, tangent 1, tangent 2)
+    float4 *lam_alt;                 // learned warm start: the start each prediction replaced (the cached
+                                     // impulses, or zero for a contact without a cache entry)
     float4 *tan;                     // 4 contacts x 2 per solver manifold: the friction directions (xyz)
     float4 *rows;                    // 4 contacts x kRowsF4 per solver manifold: normal, friction 1, friction 2 rows
     uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13)

@@ -263,6 +263,7 @@ template <class R> struct Row {
     void* cache;           // MContact the impulse is cached to
     int cache_slot;
     bool predicted;        // normal row of a contact started from the learned network
+    R alt[3];              // ... and the start the prediction replaced (cached impulses, or zero)
 };
 
 template <class R> struct PosConstraint {
@@ -1334,7 +1335,9 @@ public:
                              [](Manifold<R>* a, Manifold<R>* b) { return a->colour < b->colour; });
         }
         R inv_dt = (params.dt == 0.0f) ? R(0) : R(1) / R(params.dt);
-        const bool learned = params.warmstart_mode == 2;
+        // Learned starts: mode 2 for contacts without a cache entry, mode 3
+        // for every contact.
+        const bool learned = params.warmstart_mode == 2 || params.warmstart_mode == 3;
         if (learned && (mlp.size() != 6009 || order != ORDER_COLOUR)) {
             last_error = "learned warm start needs a network and the colour order";
             return false;
@@ -1386,7 +1389,7 @@ public:
                     it[s] = int(rows.size());
                     rows.push_back(rt);
                 }
-                if (learned && !k.cached) {
+                if (learned && (!k.cached || params.warmstart_mode == 3)) {
                     Row<R> r3[3] = {rows[in], rows[it[0]], rows[it[1]]};
                     R f[24];
                     R gn_dt = (gravity.x * n.x + gravity.y * n.y + gravity.z * n.z) * R(params.dt);
@@ -1400,6 +1403,10 @@ public:
                     float mx = float(mu) * ln;
                     pl[0] = ln;
                     for (int q = 1; q < 3; ++q) pl[q] = pl[q] < -mx ? -mx : (pl[q] > mx ? mx : pl[q]);
+                    const bool fresh = !k.cached;
+                    rows[in].alt[0] = fresh ? R(0) : rows[in].impulse;
+                    rows[in].alt[1] = fresh ? R(0) : rows[it[0]].impulse;
+                    rows[in].alt[2] = fresh ? R(0) : rows[it[1]].impulse;
                     rows[in].impulse = R(pl[0]);
                     rows[it[0]].impulse = R(pl[1]);
                     rows[it[1]].impulse = R(pl[2]);
@@ -1548,20 +1555,23 @@ public:
             }
             // A learned start (colour order: the contact's three rows follow
             // each other) stays only if its local residual is no larger than
-            // the zero start's.
+            // that of the start it replaced (the cached impulses, or zero),
+            // which is otherwise applied instead.
             Row<R>* r3[3] = {&rows[seq_warm[q]], &rows[seq_warm[q + 1]], &rows[seq_warm[q + 2]]};
             Row<R> c3[3] = {*r3[0], *r3[1], *r3[2]};
             std::vector<R> before = dv;
             R lam[3] = {c3[0].impulse, c3[1].impulse, c3[2].impulse};
             for (int k = 0; k < 3; ++k)
                 if (lam[k] != R(0)) axpy(c3[k], lam[k]);
-            const R zero[3] = {R(0), R(0), R(0)};
+            const R alt[3] = {c3[0].alt[0], c3[0].alt[1], c3[0].alt[2]};
             R with = local_residual(c3, lam);
             std::vector<R> after = dv;
             dv = before;
-            R without = local_residual(c3, zero);
+            for (int k = 0; k < 3; ++k)
+                if (alt[k] != R(0)) axpy(c3[k], alt[k]);
+            R without = local_residual(c3, alt);
             if (with > without) {
-                for (int k = 0; k < 3; ++k) r3[k]->impulse = R(0);
+                for (int k = 0; k < 3; ++k) r3[k]->impulse = alt[k];
             } else {
                 dv = after;
             }

@@ -61,14 +61,17 @@ def test_gradient_matches_reference(gpu_lib):
 
 
 @pytest.mark.gpu
+@pytest.mark.parametrize("mode", [abi.WARMSTART_LEARNED, abi.WARMSTART_LEARNED_ALL])
 @pytest.mark.parametrize("schedule", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
-def test_learned_step_matches_oracle(gpu_lib, schedule):
+def test_learned_step_matches_oracle(gpu_lib, schedule, mode):
+    # Mode 2 starts new contacts from the network, mode 3 every contact; each
+    # prediction is checked against the start it replaces.
     from nphysics_gb300.world import GpuWorld
     sc = scenes.random_cluster(n=30, seed=6)
     if schedule == abi.SCHEDULE_WORLDS:
         sc = scenes.batched_worlds(n_worlds=4, seed=5, lo=8, hi=40)
     p = sc.params()
-    p.warmstart_mode = abi.WARMSTART_LEARNED
+    p.warmstart_mode = mode
     p.solver_schedule = schedule
     net = mlp_ref.random_params(np.random.default_rng(7))
     net[mlp_ref.YS:mlp_ref.PARAMS] = 0.05     # predictions of a plausible impulse size
