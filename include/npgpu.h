@@ -366,6 +366,56 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out);
  * try_continue!, src/lib.rs:93-114). */
 const char* npgpu_last_error(const npgpu_world* w);
 
+/* ---- Geometric queries and contact events ----
+ * The queries read the world as the last step left it: the broad phase's fat
+ * AABBs and the colliders' poses of its final collision-detection pass, as
+ * the reference's queries read its DBVT proxies and synced colliders.
+ * `world` restricts a batch to one world of a batched world object
+ * (0xffffffff: every world). Collision groups are not modelled: every
+ * collider of the supported scenes has the default groups, which interact
+ * with everything. Hits come sorted by (query, collider); *count receives the
+ * number of hits and at most max_hits are written. */
+typedef struct npgpu_ray_hit {
+    uint32_t ray, collider;
+    float toi;                       /* hit point = origin + toi * dir */
+    float normal[3];                 /* outward surface normal; zero when the ray starts inside */
+} npgpu_ray_hit;
+
+/* GeometricalWorld::interferences_with_ray (src/world/geometrical_world.rs:327-341)
+ * for n rays: rays6[6n] = origin, direction (not normalised), max_toi[n].
+ * Shapes are solid: a ray starting inside a shape hits it at toi 0. */
+npgpu_status npgpu_interferences_with_rays(npgpu_world* w, uint32_t n, const float* rays6, const float* max_toi,
+                                           uint32_t world, npgpu_ray_hit* hits, uint32_t max_hits, uint32_t* count);
+/* GeometricalWorld::interferences_with_point (geometrical_world.rs:343-355) for
+ * n points: hits2[2k] = point index, hits2[2k + 1] = collider slot of each
+ * collider whose shape contains the point (boundary included). */
+npgpu_status npgpu_interferences_with_points(npgpu_world* w, uint32_t n, const float* points3, uint32_t world,
+                                             uint32_t* hits2, uint32_t max_hits, uint32_t* count);
+/* GeometricalWorld::interferences_with_aabb (geometrical_world.rs:357-370) for
+ * n boxes (min xyz, max xyz): every collider whose broad-phase AABB
+ * intersects the box; hits2 as above. */
+npgpu_status npgpu_interferences_with_aabbs(npgpu_world* w, uint32_t n, const float* aabbs6, uint32_t world,
+                                            uint32_t* hits2, uint32_t max_hits, uint32_t* count);
+
+/* ContactEvent::Started / Stopped of the last step (stopped = 0 / 1). */
+typedef struct npgpu_contact_event {
+    uint32_t collider1, collider2;   /* collider1 < collider2 */
+    uint32_t stopped;
+} npgpu_contact_event;
+/* Starts (capacity > 0) or stops (0) recording contact events: each step then
+ * records, over its collision-detection passes, the pairs whose manifold
+ * gains its first contact (started) or loses its last (stopped), as
+ * GeometricalWorld::contact_events holds them after MechanicalWorld::step
+ * (geometrical_world.rs:373-376, cleared at mechanical_world.rs:250). Pairs of
+ * a removed or replaced collider give no event, as in the reference, whose
+ * removal events are cleared before the step's first pass. */
+npgpu_status npgpu_enable_contact_events(npgpu_world* w, uint32_t capacity);
+/* The last step's contact events sorted by (collider1, collider2, stopped);
+ * *count receives their number. NPGPU_ERR_CAPACITY if the step had more events
+ * than the capacity (the first `capacity` recorded are returned).
+ * Replaces GeometricalWorld::contact_events (geometrical_world.rs:373-376). */
+npgpu_status npgpu_contact_events(npgpu_world* w, npgpu_contact_event* out, uint32_t max, uint32_t* count);
+
 /* Broad phase over caller-provided boxes that allocates nothing. This entry
  * point has no counterpart in the reference: it exists for callers that
  * cannot call cudaMalloc (code running while a CUDA graph is captured,

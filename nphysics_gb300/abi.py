@@ -207,6 +207,17 @@ def default_params():
     return p
 
 
+class RayHit(C.Structure):
+    _fields_ = [("ray", C.c_uint32), ("collider", C.c_uint32), ("toi", C.c_float), ("normal", C.c_float * 3)]
+
+
+class ContactEvent(C.Structure):
+    _fields_ = [("collider1", C.c_uint32), ("collider2", C.c_uint32), ("stopped", C.c_uint32)]
+
+
+ALL_WORLDS = 0xffffffff
+
+
 def contacts_to_numpy(arr, n):
     """Converts a ctypes Contact array into a dict of numpy arrays."""
     raw = np.ctypeslib.as_array(arr, shape=(n,)) if n else None
@@ -252,6 +263,14 @@ def load_library(path=LIB_PATH):
         "npgpu_find_pairs_static": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
                                               C.c_void_p, C.c_void_p]),
         "npgpu_autotune": (C.c_int, [W, C.c_uint32, P(C.c_uint32), P(C.c_uint32), P(C.c_float)]),
+        "npgpu_interferences_with_rays": (C.c_int, [W, C.c_uint32, P(C.c_float), P(C.c_float), C.c_uint32,
+                                                    P(RayHit), C.c_uint32, P(C.c_uint32)]),
+        "npgpu_interferences_with_points": (C.c_int, [W, C.c_uint32, P(C.c_float), C.c_uint32, P(C.c_uint32),
+                                                      C.c_uint32, P(C.c_uint32)]),
+        "npgpu_interferences_with_aabbs": (C.c_int, [W, C.c_uint32, P(C.c_float), C.c_uint32, P(C.c_uint32),
+                                                     C.c_uint32, P(C.c_uint32)]),
+        "npgpu_enable_contact_events": (C.c_int, [W, C.c_uint32]),
+        "npgpu_contact_events": (C.c_int, [W, P(ContactEvent), C.c_uint32, P(C.c_uint32)]),
         "npgpu_mlp_set": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_get": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_record": (C.c_int, [W, C.c_uint32]),
@@ -275,6 +294,8 @@ EXPORTED = [
     "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_step",
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
     "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
+    "npgpu_interferences_with_rays", "npgpu_interferences_with_points", "npgpu_interferences_with_aabbs",
+    "npgpu_enable_contact_events", "npgpu_contact_events",
     "npgpu_autotune", "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_load_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
 ]
 

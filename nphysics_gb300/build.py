@@ -20,7 +20,7 @@ SOURCES = [("npgpu_world.cu", "npgpu_world.o", []), ("k_bodies.cu", "k_bodies.o"
            ("k_solve.cu", "k_solve.o", ["-DNPGPU_EXCHANGE_TU=0"]),
            ("k_solve.cu", "k_solve_exchange.o", ["-DNPGPU_EXCHANGE_TU=1", "-Xptxas", "-dlcm=cg"]),
            ("k_static_pairs.cu", "k_static_pairs.o", []), ("k_mlp.cu", "k_mlp.o", []),
-           ("sortscan.cu", "sortscan.o", [])]
+           ("sortscan.cu", "sortscan.o", []), ("k_query.cu", "k_query.o", [])]
 HEADERS = ["np_math.cuh", "world_dev.cuh", "dyn.cuh", "narrow.cuh", "mlp.cuh", "sortscan.cuh"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

@@ -163,6 +163,7 @@ __global__ void k_forget_pairs(World w, const uint8_t* flags) {
 // changed, then update_acceleration (mechanical_world.rs:225-245).
 __global__ void k_body_start(World w, StepParams p) {
     uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i == 0) w.ctl->nevents = 0;   // MechanicalWorld::step clears the contact events first
     if (i >= w.nb_slots) return;
     uint32_t info = w.b.info[i];
     if (!(info & BI_ALIVE)) return;

@@ -344,6 +344,17 @@ struct NarrowTotals {
     unsigned long long pen_bits = 0;   // order_bits of the deepest penetration
 };
 
+// ContactEvent::Started / Stopped (ncollide3d's narrow phase, read through
+// GeometricalWorld::contact_events, src/world/geometrical_world.rs:373-376):
+// a pair whose manifold gains its first contact, or loses its last, in a
+// collision-detection pass. Events accumulate over the step's passes (the
+// body-start kernel clears the count, as MechanicalWorld::step clears them
+// before its first pass, mechanical_world.rs:250).
+__device__ __forceinline__ void emit_event(const World& w, uint32_t c1, uint32_t c2, bool stopped) {
+    const uint32_t at = atomicAdd(&w.ctl->nevents, 1u);
+    if (at < w.events_cap) w.events[at] = make_uint2(c1, c2 | (stopped ? 0x80000000u : 0u));
+}
+
 // One-shot manifold of pair p, keeping the impulses cached under the same
 // feature key in the pair's previous manifold.
 __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotals& tot) {
@@ -414,6 +425,7 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
         maxdepth = cd.g.depth > maxdepth ? cd.g.depth : maxdepth;
     }
     w.cur.ncont[p] = (uint8_t)nc;
+    if (w.events != nullptr && (nc > 0) != (pn > 0)) emit_event(w, c1, c2, nc == 0);
     if (nc > 0) {
         tot.contacts += (uint32_t)nc;
         tot.manifolds += 1u;
@@ -490,6 +502,36 @@ cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStre
         k_bp_traverse<true><<<nblocks(n), kThreads, 0, st>>>(w, n);
     }
     k_bp_total<<<1, 1, 0, st>>>(w, n);
+    return cudaGetLastError();
+}
+
+// Stopped events of the pairs that had contacts in the previous pass and are
+// no longer broad-phase pairs (the pairs present in both passes are handled
+// by the narrow phase). A pair's owner is the same collider in both passes,
+// so it is looked up among its owner's pairs of this pass.
+__global__ void k_events_vanished(World w) {
+    for (uint32_t a = blockIdx.x * blockDim.x + threadIdx.x; a < w.nc_slots; a += gridDim.x * blockDim.x) {
+        const uint32_t qs = w.prev.owner_start[a], qn = w.prev.owner_count[a];
+        if (qn == 0) continue;
+        const uint32_t cs = w.cur.owner_start[a], cn = w.cur.owner_count[a];
+        for (uint32_t q = 0; q < qn; ++q) {
+            const uint2 o = w.prev.pair[qs + q];
+            if (o.x == 0xffffffffu || w.prev.ncont[qs + q] == 0) continue;
+            bool found = false;
+            for (uint32_t r = 0; r < cn && !found; ++r) {
+                const uint2 x = w.cur.pair[cs + r];
+                found = x.x == o.x && x.y == o.y;
+            }
+            if (!found) emit_event(w, o.x, o.y, true);
+        }
+    }
+}
+
+cudaError_t launch_events(const World& w, cudaStream_t st) {
+    if (w.events == nullptr || w.nc_slots == 0) return cudaSuccess;
+    unsigned blocks = nblocks(w.nc_slots);
+    if (blocks > 152u * 16u) blocks = 152u * 16u;
+    k_events_vanished<<<blocks, kThreads, 0, st>>>(w);
     return cudaGetLastError();
 }
 

@@ -157,6 +157,10 @@ struct npgpu_world {
     uint32_t sample_cap = 0;
     float* d_feat = nullptr;
     uint32_t max_world = 0;              // largest world index any body had (never lowered)
+    // Geometric queries: device copies of a batch, per-query counts and
+    // offsets, the hits; grown on demand, kept between calls.
+    void* d_query = nullptr;
+    size_t query_bytes = 0;
     bool local_dirty = true;             // colliders or worlds changed: the colliders' world-local slots
     std::vector<uint32_t> h_local;       // (Colliders::local) are recomputed before the next step
     std::vector<uint32_t> unregistered;  // colliders whose mass is not yet added to their body
@@ -177,6 +181,13 @@ struct npgpu_world {
 // allocation-free pair finder), kept per host thread: a failing call on one
 // thread never rewrites the string another thread is reading.
 static thread_local std::string g_create_error;
+
+namespace npgpu_dev {
+size_t query_hit_bytes();
+cudaError_t launch_query(const World& w, int kind, const float* qd, const float* max_toi, uint32_t nq, uint32_t world,
+                         uint32_t* counts, uint32_t* offsets, void* scan_temp, size_t scan_bytes, void* out,
+                         uint32_t cap_out, cudaStream_t st);
+}
 
 namespace npgpu_dev {
 // Message returned by npgpu_last_error(NULL) for calls without a world.
@@ -240,6 +251,8 @@ static npgpu_status stage_reserve(npgpu_world* w, size_t bytes, void** hptr) {
     }
     if (bytes > w->d_stage_bytes) {
         if (w->d_stage) cudaFree(w->d_stage);
+    if (w->d_query) cudaFree(w->d_query);
+    if (w->dw.events) cudaFree(w->dw.events);
         w->d_stage = nullptr;
         size_t nb = std::max(bytes, w->d_stage_bytes * 2);
         CK(cudaMalloc(&w->d_stage, nb), "device staging");
@@ -574,6 +587,8 @@ void npgpu_destroy(npgpu_world* w) {
                     (void*)w->d_stats, (void*)w->d_samples, (void*)w->d_feat})
         cudaFree(p);
     if (w->d_stage) cudaFree(w->d_stage);
+    if (w->d_query) cudaFree(w->d_query);
+    if (w->dw.events) cudaFree(w->dw.events);
     if (w->h_flags) cudaFreeHost(w->h_flags);
     if (w->h_stage) cudaFreeHost(w->h_stage);
     if (w->ev_stage) cudaEventDestroy(w->ev_stage);
@@ -984,6 +999,7 @@ static npgpu_status run_cd(npgpu_world* w, const StepParams& sp) {
     CK(launch_pairs(w->dw, w->scan_temp, w->scan_bytes, w->stream), "pairs");
     if (w->params.profile) CK(cudaEventRecord(w->ev[5], w->stream), "event");
     CK(launch_narrow(w->dw, w->stream), "narrow phase");
+    CK(launch_events(w->dw, w->stream), "contact events");
     return NPGPU_OK;
 }
 
@@ -1222,6 +1238,8 @@ npgpu_status npgpu_download_bodies(npgpu_world* w, uint32_t first, uint32_t n, f
     }
     if (bytes > w->d_stage_bytes) {
         if (w->d_stage) cudaFree(w->d_stage);
+    if (w->d_query) cudaFree(w->d_query);
+    if (w->dw.events) cudaFree(w->dw.events);
         w->d_stage = nullptr;
         CK(cudaMalloc(&w->d_stage, bytes), "device staging");
         w->d_stage_bytes = bytes;
@@ -1616,6 +1634,151 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
         k.velocity_tasks = c.tasks;
     }
     *out = k;
+    return NPGPU_OK;
+}
+
+// ---------------------------------------------------------------- queries and events
+
+struct HostHit {
+    uint32_t q, collider;
+    float toi, nx, ny, nz;
+};
+
+// Runs one batch of queries (kind 0 rays, 1 points, 2 boxes) and returns every
+// hit sorted by (query, collider).
+static npgpu_status run_queries(npgpu_world* w, int kind, uint32_t n, const float* qd, const float* max_toi,
+                                uint32_t world, std::vector<HostHit>& hits) {
+    hits.clear();
+    if (n == 0 || w->nc_alive == 0) return NPGPU_OK;
+    const int per = kind == 1 ? 3 : 6;
+    if (!finite_n(qd, (int)std::min<uint64_t>((uint64_t)n * per, 0x7fffffffu)) ||
+        (max_toi && !finite_n(max_toi, (int)n)))
+        return fail(w, NPGPU_ERR_NAN, "query values are not finite");
+    auto a256 = [](size_t x) { return (x + 255) & ~size_t(255); };
+    const size_t in_b = a256(sizeof(float) * per * (size_t)n), toi_b = a256(sizeof(float) * (size_t)n);
+    const size_t cnt_b = a256(sizeof(uint32_t) * (size_t)n), scan_b = a256(scan_temp_bytes(n));
+    size_t need = in_b + toi_b + 2 * cnt_b + scan_b;
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    if (need > w->query_bytes) {
+        if (w->d_query) cudaFree(w->d_query);
+        w->d_query = nullptr;
+        w->query_bytes = 0;
+        CK(cudaMalloc(&w->d_query, need), "query buffers");
+        w->query_bytes = need;
+    }
+    unsigned char* base = (unsigned char*)w->d_query;
+    float* d_in = (float*)base;
+    float* d_toi = (float*)(base + in_b);
+    uint32_t* d_cnt = (uint32_t*)(base + in_b + toi_b);
+    uint32_t* d_off = (uint32_t*)(base + in_b + toi_b + cnt_b);
+    void* d_scan = base + in_b + toi_b + 2 * cnt_b;
+    CK(cudaMemcpy(d_in, qd, sizeof(float) * per * (size_t)n, cudaMemcpyHostToDevice), "query upload");
+    if (max_toi) CK(cudaMemcpy(d_toi, max_toi, sizeof(float) * n, cudaMemcpyHostToDevice), "query upload");
+    sync_world_view(w);
+    CK(launch_query(w->dw, kind, d_in, d_toi, n, world, d_cnt, d_off, d_scan, scan_b, nullptr, 0, w->stream),
+       "query count");
+    uint32_t last_off = 0, last_cnt = 0;
+    CK(cudaMemcpyAsync(&last_off, d_off + n - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream), "d2h");
+    CK(cudaMemcpyAsync(&last_cnt, d_cnt + n - 1, sizeof(uint32_t), cudaMemcpyDeviceToHost, w->stream), "d2h");
+    CK(cudaStreamSynchronize(w->stream), "query count");
+    const uint32_t total = last_off + last_cnt;
+    if (total == 0) return NPGPU_OK;
+    void* d_out = nullptr;
+    CK(cudaMalloc(&d_out, query_hit_bytes() * total), "query hits");
+    cudaError_t e = launch_query(w->dw, kind, d_in, d_toi, n, world, d_cnt, d_off, d_scan, scan_b, d_out, total,
+                                 w->stream);
+    if (e == cudaSuccess) {
+        hits.resize(total);
+        e = cudaMemcpyAsync(hits.data(), d_out, sizeof(HostHit) * total, cudaMemcpyDeviceToHost, w->stream);
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(w->stream);
+    cudaFree(d_out);
+    if (e != cudaSuccess) return cuda_fail(w, e, "query hits");
+    std::sort(hits.begin(), hits.end(),
+              [](const HostHit& a, const HostHit& b) { return a.q != b.q ? a.q < b.q : a.collider < b.collider; });
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_interferences_with_rays(npgpu_world* w, uint32_t n, const float* rays6, const float* max_toi,
+                                           uint32_t world, npgpu_ray_hit* hits, uint32_t max_hits, uint32_t* count) {
+    if (!w || !count || (n && (!rays6 || !max_toi)) || (max_hits && !hits))
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    static_assert(sizeof(HostHit) == 24, "hit record layout");
+    std::vector<HostHit> h;
+    npgpu_status st = run_queries(w, 0, n, rays6, max_toi, world, h);
+    if (st != NPGPU_OK) return st;
+    *count = (uint32_t)h.size();
+    for (uint32_t k = 0; k < h.size() && k < max_hits; ++k) {
+        hits[k].ray = h[k].q;
+        hits[k].collider = h[k].collider;
+        hits[k].toi = h[k].toi;
+        hits[k].normal[0] = h[k].nx;
+        hits[k].normal[1] = h[k].ny;
+        hits[k].normal[2] = h[k].nz;
+    }
+    return NPGPU_OK;
+}
+
+static npgpu_status pair_queries(npgpu_world* w, int kind, uint32_t n, const float* q, uint32_t world, uint32_t* hits2,
+                                 uint32_t max_hits, uint32_t* count) {
+    if (!w || !count || (n && !q) || (max_hits && !hits2)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<HostHit> h;
+    npgpu_status st = run_queries(w, kind, n, q, nullptr, world, h);
+    if (st != NPGPU_OK) return st;
+    *count = (uint32_t)h.size();
+    for (uint32_t k = 0; k < h.size() && k < max_hits; ++k) {
+        hits2[2 * k] = h[k].q;
+        hits2[2 * k + 1] = h[k].collider;
+    }
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_interferences_with_points(npgpu_world* w, uint32_t n, const float* points3, uint32_t world,
+                                             uint32_t* hits2, uint32_t max_hits, uint32_t* count) {
+    return pair_queries(w, 1, n, points3, world, hits2, max_hits, count);
+}
+
+npgpu_status npgpu_interferences_with_aabbs(npgpu_world* w, uint32_t n, const float* aabbs6, uint32_t world,
+                                            uint32_t* hits2, uint32_t max_hits, uint32_t* count) {
+    return pair_queries(w, 2, n, aabbs6, world, hits2, max_hits, count);
+}
+
+npgpu_status npgpu_enable_contact_events(npgpu_world* w, uint32_t capacity) {
+    if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    if (w->dw.events) cudaFree(w->dw.events);
+    w->dw.events = nullptr;
+    w->dw.events_cap = 0;
+    if (capacity) {
+        CK(cudaMalloc(&w->dw.events, sizeof(uint2) * (size_t)capacity), "contact events");
+        w->dw.events_cap = capacity;
+    }
+    uint32_t zero = 0;
+    CK(cudaMemcpy(&w->ctl->nevents, &zero, sizeof(zero), cudaMemcpyHostToDevice), "contact events");
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_contact_events(npgpu_world* w, npgpu_contact_event* out, uint32_t max, uint32_t* count) {
+    if (!w || !count || (max && !out)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    if (!w->dw.events) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "contact events are off (npgpu_enable_contact_events)");
+    CK(cudaStreamSynchronize(w->stream), "synchronize");
+    uint32_t n = 0;
+    CK(cudaMemcpy(&n, &w->ctl->nevents, sizeof(n), cudaMemcpyDeviceToHost), "d2h");
+    const uint32_t kept = std::min(n, w->dw.events_cap);
+    std::vector<uint2> ev(kept);
+    if (kept) CK(cudaMemcpy(ev.data(), w->dw.events, sizeof(uint2) * kept, cudaMemcpyDeviceToHost), "d2h");
+    std::vector<uint64_t> keys(kept);
+    for (uint32_t k = 0; k < kept; ++k)
+        keys[k] = ((uint64_t)ev[k].x << 33) | ((uint64_t)(ev[k].y & 0x7fffffffu) << 1) | (ev[k].y >> 31);
+    std::sort(keys.begin(), keys.end());
+    *count = kept;
+    for (uint32_t k = 0; k < kept && k < max; ++k) {
+        out[k].collider1 = (uint32_t)(keys[k] >> 33);
+        out[k].collider2 = (uint32_t)((keys[k] >> 1) & 0xffffffffu);
+        out[k].stopped = (uint32_t)(keys[k] & 1u);
+    }
+    if (n > w->dw.events_cap)
+        return fail(w, NPGPU_ERR_CAPACITY, "more contact events than the capacity given to npgpu_enable_contact_events");
     return NPGPU_OK;
 }
 

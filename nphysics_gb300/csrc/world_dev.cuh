@@ -183,6 +183,8 @@ struct Control {
     uint32_t learned_starts, learned_kept;   // learned warm start: predictions made / kept this step
     uint32_t force_flags;            // checks of the last force batch: 1 bad handle, 2 non-finite, 4 a body twice
     double mlp_loss;                 // loss of the last training step
+    uint32_t nevents;                // contact events of this step so far (may exceed World::events_cap)
+    uint32_t pad2;
 };
 
 struct StepParams {
@@ -209,6 +211,8 @@ struct World {
     Control* ctl;
     uint32_t nb_slots, nc_slots, cap_pairs, nc_alive;
     uint32_t world_bits;             // bits of the largest world index of any body so far
+    uint2* events;                   // contact events (collider1, collider2 | stopped << 31), null when off
+    uint32_t events_cap;
 };
 
 // ---- launchers (defined in the kernel translation units) ----
@@ -217,6 +221,7 @@ cudaError_t launch_sync_aabb(const World& w, const StepParams& p, cudaStream_t s
 cudaError_t launch_lbvh(const World& w, cudaStream_t st);
 cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStream_t st);
 cudaError_t launch_narrow(const World& w, cudaStream_t st);
+cudaError_t launch_events(const World& w, cudaStream_t st);   // contact events of pairs no longer in the broad phase
 // The solver half of a step (activation, colouring, assembly, SOR-Prox,
 // integration, position correction, post-step updates). ev[0..6], when
 // non-null, receive the phase boundaries for profiling.

@@ -12,8 +12,13 @@ captures that region's launches and nothing else. Regions:
   step      one npgpu_step of the workload (every kernel of the step)
   e2e       one end-to-end round trip through the C ABI: npgpu_apply_forces
             from page-locked host arrays, npgpu_step, npgpu_download_bodies
-  train     --train-steps Adam steps of the learned warm start on samples the
-            workload's solver recorded (the network's kernels)
+  train     the learned warm start trained on samples the workload's solver
+            recorded: normalisation and initialisation, then --train-steps
+            Adam steps (the network's kernels)
+  query     one batch each of --queries rays, points and boxes against the
+            world (interferences_with_ray / _point / _aabb)
+  events    one step with contact events recorded
+  static    the allocation-free pair finder on the world's fat AABBs
 
 Workloads: pile (the 32^3 ball pile, one cooperative grid), cluster (the same
 pile under the per-world schedule: one thread-block cluster), batched
@@ -59,7 +64,8 @@ def main(argv=None):
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
     ap.add_argument("--workload", default="pile", choices=["pile", "cluster", "batched", "mixed"])
-    ap.add_argument("--region", default="step", choices=["step", "e2e", "train"])
+    ap.add_argument("--region", default="step", choices=["step", "e2e", "train", "query", "events", "static"])
+    ap.add_argument("--queries", type=int, default=100_000)
     ap.add_argument("--side", type=int, default=32)
     ap.add_argument("--worlds", type=int, default=1024)
     ap.add_argument("--bodies", type=int, default=100_000)
@@ -80,7 +86,6 @@ def main(argv=None):
         w.mlp_record(1_000_000)
         w.step(1)
         w.mlp_record(0)
-        w.mlp_train(1, batch=4096, lr=1e-3, seed=1, init=True)
     pos = vel = handles = forces = None
     if args.region == "e2e":
         pos = pinned(np.zeros((len(sc.bodies), 7), np.float32))
@@ -91,15 +96,42 @@ def main(argv=None):
         w.apply_forces(handles, forces, wake=False)
         w.step(1, sync=False)
         w.download_into(pos, vel)
+    rng = np.random.default_rng(1)
+    if args.region == "query":
+        lo, hi = sc.bodies["position"][:, :3].min(axis=0), sc.bodies["position"][:, :3].max(axis=0)
+        org = rng.uniform(lo, hi, (args.queries, 3)).astype(np.float32)
+        rays = np.concatenate([org, rng.normal(size=(args.queries, 3)).astype(np.float32)], axis=1)
+        toi = np.full(args.queries, 5.0, np.float32)
+        boxes = np.concatenate([org, org + 1.0], axis=1)
+    if args.region == "events":
+        w.enable_contact_events(1 << 20)
+        w.step(1)
+    if args.region == "static":
+        from . import abi
+        import ctypes as C
+        aabbs = torch.from_numpy(w.aabbs()).cuda()
+        n = min(len(aabbs), 32768)
+        pairs = torch.empty((16 * n, 2), dtype=torch.int32, device="cuda")
+        count = torch.empty(1, dtype=torch.int32, device="cuda")
+        args_static = (C.c_void_p(aabbs.data_ptr()), None, n, C.c_void_p(pairs.data_ptr()), 16 * n,
+                       C.c_void_p(count.data_ptr()), None)
+        assert w.L.npgpu_find_pairs_static(*args_static) == abi.OK     # set-up call
     torch.cuda.synchronize()
     torch.cuda.profiler.start()
-    if args.region == "step":
+    if args.region in ("step", "events"):
         w.step(1)
+    elif args.region == "query":
+        w.rays(rays, toi)
+        w.points(org)
+        w.aabb_query(boxes)
+    elif args.region == "static":
+        w.L.npgpu_find_pairs_static(*args_static)
     elif args.region == "e2e":
         w.apply_forces(handles, forces, wake=False)
         w.step(1, sync=False)
         w.download_into(pos, vel)
     else:
+        w.mlp_train(1, batch=4096, lr=1e-3, seed=1, init=True)
         w.mlp_train(args.train_steps, batch=4096, lr=1e-3, seed=2)
     torch.cuda.synchronize()
     torch.cuda.profiler.stop()

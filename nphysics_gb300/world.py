@@ -167,6 +167,59 @@ class GpuWorld:
         self._check(self.L.npgpu_get_contacts(self.w, arr, n, C.byref(cnt)), "get_contacts")
         return abi.contacts_to_numpy(arr, n)
 
+    # ---- geometric queries and contact events ----
+    def rays(self, rays6, max_toi, world=abi.ALL_WORLDS):
+        """GeometricalWorld::interferences_with_ray for a batch: an array of
+        (ray, collider, toi, nx, ny, nz) rows sorted by (ray, collider)."""
+        rays6 = np.ascontiguousarray(rays6, np.float32).reshape(-1, 6)
+        max_toi = np.ascontiguousarray(max_toi, np.float32).reshape(-1)
+        cnt = C.c_uint32(0)
+        self._check(self.L.npgpu_interferences_with_rays(self.w, len(rays6), _ptr(rays6, C.c_float),
+                                                         _ptr(max_toi, C.c_float), world, None, 0, C.byref(cnt)),
+                    "interferences_with_rays")
+        n = cnt.value
+        arr = (abi.RayHit * max(n, 1))()
+        self._check(self.L.npgpu_interferences_with_rays(self.w, len(rays6), _ptr(rays6, C.c_float),
+                                                         _ptr(max_toi, C.c_float), world, arr, n, C.byref(cnt)),
+                    "interferences_with_rays")
+        out = np.zeros((n, 6), np.float64)
+        for k in range(n):
+            h = arr[k]
+            out[k] = (h.ray, h.collider, h.toi, h.normal[0], h.normal[1], h.normal[2])
+        return out
+
+    def _pair_query(self, fn, q, per, world):
+        q = np.ascontiguousarray(q, np.float32).reshape(-1, per)
+        cnt = C.c_uint32(0)
+        self._check(fn(self.w, len(q), _ptr(q, C.c_float), world, None, 0, C.byref(cnt)), "interferences")
+        out = np.zeros((max(cnt.value, 1), 2), np.uint32)
+        self._check(fn(self.w, len(q), _ptr(q, C.c_float), world, _ptr(out, C.c_uint32), cnt.value, C.byref(cnt)),
+                    "interferences")
+        return out[:cnt.value]
+
+    def points(self, points3, world=abi.ALL_WORLDS):
+        """interferences_with_point: (point, collider) rows."""
+        return self._pair_query(self.L.npgpu_interferences_with_points, points3, 3, world)
+
+    def aabb_query(self, aabbs6, world=abi.ALL_WORLDS):
+        """interferences_with_aabb: (box, collider) rows."""
+        return self._pair_query(self.L.npgpu_interferences_with_aabbs, aabbs6, 6, world)
+
+    def enable_contact_events(self, capacity=1 << 20):
+        self._check(self.L.npgpu_enable_contact_events(self.w, capacity), "enable_contact_events")
+
+    def contact_events(self):
+        """The last step's (collider1, collider2, stopped) rows, sorted."""
+        cnt = C.c_uint32(0)
+        self._check(self.L.npgpu_contact_events(self.w, None, 0, C.byref(cnt)), "contact_events")
+        n = cnt.value
+        arr = (abi.ContactEvent * max(n, 1))()
+        self._check(self.L.npgpu_contact_events(self.w, arr, n, C.byref(cnt)), "contact_events")
+        out = np.zeros((n, 3), np.uint32)
+        for k in range(n):
+            out[k] = (arr[k].collider1, arr[k].collider2, arr[k].stopped)
+        return out
+
     def autotune(self, steps_per_candidate=5):
         """Times the solver's launch shapes on real steps (all give the same
         bits) and keeps the fastest: (schedule, world_threads, ms per step)."""

@@ -202,6 +202,79 @@ uint32_t orc_get_pairs(orc_world* o, uint32_t* out, uint32_t max) {
     return n;
 }
 
+// Contact events of the last step as (collider1, collider2, stopped), in the
+// order the passes produced them.
+void orc_record_events(orc_world* o, int on) { DISPATCH(o, { w.record_events = on != 0; w.events.clear(); }); }
+uint32_t orc_contact_events(orc_world* o, uint32_t* out3, uint32_t max) {
+    uint32_t n = 0;
+    DISPATCH(o, {
+        n = uint32_t(w.events.size());
+        for (uint32_t i = 0; i < n && i < max; ++i)
+            for (int k = 0; k < 3; ++k) out3[3 * i + k] = w.events[i][k];
+    });
+    return n;
+}
+
+// Ray queries by brute force over the alive colliders: (ray, collider, toi,
+// nx, ny, nz) per hit as doubles, in ray then collider order.
+uint32_t orc_rays(orc_world* o, uint32_t n, const float* rays6, const float* max_toi, uint32_t world, double* out6,
+                  uint32_t max) {
+    uint32_t cnt = 0;
+    DISPATCH(o, {
+        using R = typename std::remove_reference<decltype(w)>::type::Real;
+        for (uint32_t r = 0; r < n; ++r) {
+            V3<R> org = v3<R>(R(rays6[6 * r]), R(rays6[6 * r + 1]), R(rays6[6 * r + 2]));
+            V3<R> dir = v3<R>(R(rays6[6 * r + 3]), R(rays6[6 * r + 4]), R(rays6[6 * r + 5]));
+            for (uint32_t c = 0; c < w.colliders.size(); ++c) {
+                const auto& col = w.colliders[c];
+                if (!col.alive || !w.in_world(col, world)) continue;
+                R toi;
+                V3<R> nn;
+                if (!w.ray_shape(col, org, dir, R(max_toi[r]), toi, nn)) continue;
+                if (cnt < max) {
+                    double* q = out6 + 6 * cnt;
+                    q[0] = r; q[1] = c; q[2] = double(toi); q[3] = double(nn.x); q[4] = double(nn.y); q[5] = double(nn.z);
+                }
+                ++cnt;
+            }
+        }
+    });
+    return cnt;
+}
+
+// Point (kind 1) or fat-AABB (kind 2) queries: (query, collider) pairs.
+uint32_t orc_overlaps(orc_world* o, int kind, uint32_t n, const float* q, uint32_t world, uint32_t* out2, uint32_t max) {
+    uint32_t cnt = 0;
+    DISPATCH(o, {
+        using R = typename std::remove_reference<decltype(w)>::type::Real;
+        for (uint32_t i = 0; i < n; ++i) {
+            for (uint32_t c = 0; c < w.colliders.size(); ++c) {
+                const auto& col = w.colliders[c];
+                if (!col.alive || !w.in_world(col, world)) continue;
+                bool hit;
+                if (kind == 1) {
+                    V3<R> p = v3<R>(R(q[3 * i]), R(q[3 * i + 1]), R(q[3 * i + 2]));
+                    hit = col.has_fat && R(q[3 * i]) >= col.aabb_min[0] && R(q[3 * i]) <= col.aabb_max[0] &&
+                          R(q[3 * i + 1]) >= col.aabb_min[1] && R(q[3 * i + 1]) <= col.aabb_max[1] &&
+                          R(q[3 * i + 2]) >= col.aabb_min[2] && R(q[3 * i + 2]) <= col.aabb_max[2] &&
+                          w.point_in_shape(col, p);
+                } else {
+                    hit = col.has_fat;
+                    for (int a = 0; a < 3 && hit; ++a)
+                        hit = R(q[6 * i + a]) <= col.aabb_max[a] && col.aabb_min[a] <= R(q[6 * i + 3 + a]);
+                }
+                if (!hit) continue;
+                if (cnt < max) {
+                    out2[2 * cnt] = i;
+                    out2[2 * cnt + 1] = c;
+                }
+                ++cnt;
+            }
+        }
+    });
+    return cnt;
+}
+
 uint32_t orc_brute_force_pairs(orc_world* o, uint32_t* out, uint32_t max) {
     uint32_t n = 0;
     DISPATCH(o, {

@@ -49,6 +49,10 @@ def lib():
             "orc_get_contacts_f64": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
             "orc_get_counters": (None, [W, P(abi.Counters)]),
             "orc_last_error": (C.c_char_p, [W]),
+            "orc_record_events": (None, [W, C.c_int]),
+            "orc_contact_events": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
+            "orc_rays": (C.c_uint32, [W, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+            "orc_overlaps": (C.c_uint32, [W, C.c_int, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
         }
         for name, (res, args) in decl.items():
             fn = getattr(L, name)
@@ -192,3 +196,37 @@ class OracleWorld:
         c = abi.Counters()
         self.L.orc_get_counters(self.w, C.byref(c))
         return c.as_dict()
+
+    # ---- contact events and geometric queries (same surface as GpuWorld) ----
+    def enable_contact_events(self, capacity=1 << 20):
+        self.L.orc_record_events(self.w, 1 if capacity else 0)
+
+    def contact_events(self):
+        """(collider1, collider2, stopped) rows, sorted."""
+        n = self.L.orc_contact_events(self.w, None, 0)
+        out = np.zeros((max(n, 1), 3), np.uint32)
+        self.L.orc_contact_events(self.w, _ptr(out), n)
+        out = out[:n]
+        return out[np.lexsort((out[:, 2], out[:, 1], out[:, 0]))] if n else out
+
+    def rays(self, rays6, max_toi, world=0xffffffff):
+        rays6 = np.ascontiguousarray(rays6, np.float32).reshape(-1, 6)
+        max_toi = np.ascontiguousarray(max_toi, np.float32).reshape(-1)
+        n = self.L.orc_rays(self.w, len(rays6), _ptr(rays6), _ptr(max_toi), world, None, 0)
+        out = np.zeros((max(n, 1), 6), np.float64)
+        self.L.orc_rays(self.w, len(rays6), _ptr(rays6), _ptr(max_toi), world, _ptr(out), n)
+        return out[:n]
+
+    def overlaps(self, kind, q, world=0xffffffff):
+        q = np.ascontiguousarray(q, np.float32)
+        nq = len(q)
+        n = self.L.orc_overlaps(self.w, kind, nq, _ptr(q), world, None, 0)
+        out = np.zeros((max(n, 1), 2), np.uint32)
+        self.L.orc_overlaps(self.w, kind, nq, _ptr(q), world, _ptr(out), n)
+        return out[:n]
+
+    def points(self, points3, world=0xffffffff):
+        return self.overlaps(1, np.ascontiguousarray(points3, np.float32).reshape(-1, 3), world)
+
+    def aabb_query(self, aabbs6, world=0xffffffff):
+        return self.overlaps(2, np.ascontiguousarray(aabbs6, np.float32).reshape(-1, 6), world)

@@ -25,6 +25,8 @@
 #include <cstring>
 #include <cfloat>
 #include <limits>
+#include <array>
+#include <limits>
 #include <map>
 #include <type_traits>
 #include <string>
@@ -274,6 +276,7 @@ template <class R> struct PosConstraint {
 
 template <class R> class World {
 public:
+    using Real = R;
     npgpu_params params;
     V3<R> gravity;
     std::vector<Body<R>> bodies;
@@ -990,14 +993,106 @@ public:
         for (uint64_t key : pairs) {
             Manifold<R> m;
             auto it = manifolds.find(key);
+            const bool had = it != manifolds.end() && !it->second.contacts.empty();
             if (it != manifolds.end()) m = it->second;
             m.c1 = uint32_t(key >> 32);
             m.c2 = uint32_t(key & 0xffffffffu);
             narrow_pair(m);
+            // ContactEvent::Started / Stopped of this pass.
+            if (record_events && had != !m.contacts.empty()) events.push_back({m.c1, m.c2, had ? 1u : 0u});
             next[key] = m;
         }
+        if (record_events)
+            for (auto& kv : manifolds)
+                if (!kv.second.contacts.empty() && next.find(kv.first) == next.end())
+                    events.push_back({kv.second.c1, kv.second.c2, 1u});
         manifolds.swap(next);
         cd_dirty = false;
+    }
+
+    // ---- contact events and geometric queries ----
+    // GeometricalWorld::contact_events (geometrical_world.rs:373-376): the
+    // started / stopped pairs of the step's collision-detection passes,
+    // cleared when the step begins (mechanical_world.rs:250).
+    bool record_events = false;
+    std::vector<std::array<uint32_t, 3>> events;
+
+    // interferences_with_ray (geometrical_world.rs:327-341) for one ray on
+    // solid shapes: the sphere's quadratic, or the cuboid's three slabs in its
+    // frame (the face of the last slab entered gives the normal).
+    bool ray_shape(const Collider<R>& c, V3<R> o, V3<R> d, R max_toi, R& toi, V3<R>& n) const {
+        const V3<R> zero = v3<R>(R(0), R(0), R(0));
+        if (c.shape == NPGPU_SHAPE_BALL) {
+            const V3<R> m = o - c.pose.t;
+            const R a = dot(d, d), b = dot(m, d), cc = dot(m, m) - c.radius * c.radius;
+            if (cc > R(0) && b > R(0)) return false;
+            const R disc = b * b - a * cc;
+            if (disc < R(0) || a == R(0)) {
+                if (cc <= R(0)) {
+                    toi = R(0);
+                    n = zero;
+                    return true;
+                }
+                return false;
+            }
+            const R t = (-b - std::sqrt(disc)) / a;
+            if (t <= R(0)) {
+                toi = R(0);
+                n = zero;
+                return true;
+            }
+            if (t > max_toi) return false;
+            toi = t;
+            const V3<R> hit = m + d * t;
+            const R l = std::sqrt(dot(hit, hit));
+            n = l > R(0) ? vdiv(hit, l) : zero;
+            return true;
+        }
+        const V3<R> lo = qrot_inv(c.pose.q, o - c.pose.t), ld = qrot_inv(c.pose.q, d);
+        const R os[3] = {lo.x, lo.y, lo.z}, ds[3] = {ld.x, ld.y, ld.z}, hs[3] = {c.half.x, c.half.y, c.half.z};
+        R tmin = -std::numeric_limits<R>::infinity(), tmax = std::numeric_limits<R>::infinity();
+        int axis = -1;
+        R sign = R(0);
+        for (int i = 0; i < 3; ++i) {
+            if (ds[i] == R(0)) {
+                if (os[i] < -hs[i] || os[i] > hs[i]) return false;
+                continue;
+            }
+            R t1 = (-hs[i] - os[i]) / ds[i], t2 = (hs[i] - os[i]) / ds[i];
+            R sg = R(-1);
+            if (t1 > t2) {
+                std::swap(t1, t2);
+                sg = R(1);
+            }
+            if (t1 > tmin) {
+                tmin = t1;
+                axis = i;
+                sign = sg;
+            }
+            if (t2 < tmax) tmax = t2;
+            if (tmin > tmax) return false;
+        }
+        if (tmax < R(0)) return false;
+        if (tmin <= R(0) || axis < 0) {
+            toi = R(0);
+            n = zero;
+            return true;
+        }
+        if (tmin > max_toi) return false;
+        toi = tmin;
+        n = qrot(c.pose.q, v3<R>(axis == 0 ? sign : R(0), axis == 1 ? sign : R(0), axis == 2 ? sign : R(0)));
+        return true;
+    }
+    bool point_in_shape(const Collider<R>& c, V3<R> p) const {
+        if (c.shape == NPGPU_SHAPE_BALL) {
+            const V3<R> m = p - c.pose.t;
+            return dot(m, m) <= c.radius * c.radius;
+        }
+        const V3<R> l = qrot_inv(c.pose.q, p - c.pose.t);
+        return std::fabs(l.x) <= c.half.x && std::fabs(l.y) <= c.half.y && std::fabs(l.z) <= c.half.z;
+    }
+    bool in_world(const Collider<R>& c, uint32_t world) const {
+        return world == 0xffffffffu || bodies[c.body].world == world;
     }
 
     // ------------------------------------------------------- activation
@@ -1634,6 +1729,7 @@ public:
     // MechanicalWorld::step_with_filter (mechanical_world.rs:199-396).
     npgpu_status step() {
         R dt = R(params.dt);
+        events.clear();
         // maintain: register new colliders (geometrical_world.rs:102-143).
         for (auto& c : colliders) {
             if (!c.alive || c.registered) continue;

@@ -144,6 +144,23 @@ pub struct npgpu_counters {
     pub reserved: u32,
 }
 
+#[repr(C)]
+#[derive(Copy, Clone, Default)]
+pub struct npgpu_ray_hit {
+    pub ray: u32,
+    pub collider: u32,
+    pub toi: f32,
+    pub normal: [f32; 3],
+}
+
+#[repr(C)]
+#[derive(Copy, Clone, Default)]
+pub struct npgpu_contact_event {
+    pub collider1: u32,
+    pub collider2: u32,
+    pub stopped: u32,
+}
+
 /// Opaque world handle (`npgpu_world*`).
 pub enum npgpu_world {}
 
@@ -180,6 +197,16 @@ extern "C" {
     pub fn npgpu_last_error(w: *const npgpu_world) -> *const c_char;
     pub fn npgpu_find_pairs_static(aabbs6: *const f32, groups: *const u32, n: u32, pairs2: *mut u32,
                                    max_pairs: u32, count: *mut u32, stream: *mut c_void) -> c_int;
+    pub fn npgpu_interferences_with_rays(w: *mut npgpu_world, n: u32, rays6: *const f32, max_toi: *const f32,
+                                         world: u32, hits: *mut npgpu_ray_hit, max_hits: u32,
+                                         count: *mut u32) -> c_int;
+    pub fn npgpu_interferences_with_points(w: *mut npgpu_world, n: u32, points3: *const f32, world: u32,
+                                           hits2: *mut u32, max_hits: u32, count: *mut u32) -> c_int;
+    pub fn npgpu_interferences_with_aabbs(w: *mut npgpu_world, n: u32, aabbs6: *const f32, world: u32,
+                                          hits2: *mut u32, max_hits: u32, count: *mut u32) -> c_int;
+    pub fn npgpu_enable_contact_events(w: *mut npgpu_world, capacity: u32) -> c_int;
+    pub fn npgpu_contact_events(w: *mut npgpu_world, out: *mut npgpu_contact_event, max: u32,
+                                count: *mut u32) -> c_int;
     pub fn npgpu_mlp_set(w: *mut npgpu_world, params: *const f32, n: u32) -> c_int;
     pub fn npgpu_mlp_get(w: *mut npgpu_world, params: *mut f32, n: u32) -> c_int;
     pub fn npgpu_mlp_record(w: *mut npgpu_world, capacity: u32) -> c_int;
