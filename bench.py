@@ -43,21 +43,22 @@ sys.path.insert(0, ROOT)
 METRIC = "body-steps/s"
 L2_FLUSH_BYTES = 256 << 20
 PROFILE_STEPS = 10
-# Kernels of this library launched per step (CUB's radix sort and scans not
-# counted), from the ncu launch list of this workload.
-LAUNCHES_PER_STEP = 21
-# The per-world schedule: the two cooperative solver kernels become seven
-# per-world kernels (bucket count and scatter, the two renumbering passes,
-# velocity, residual, position), from the launch list of the batched workload.
-LAUNCHES_PER_STEP_BATCHED = 26
+# Kernels of this library launched per step, from the ncu launch list of one
+# step of this workload (every kernel is this library's: the broad phase's
+# radix sort is 4 passes of 3 launches over 32-bit keys).
+LAUNCHES_PER_STEP = 47
+# The per-world schedule (6 sort passes over the batched worlds' 44-bit keys,
+# the per-world bucketing, velocity, finish and position kernels), from the
+# launch list of one step of a 1024-world batch.
+LAUNCHES_PER_STEP_BATCHED = 65
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_velocity launch on this
-# workload, from one ncu capture.
-VELOCITY_TRAFFIC_PER_LAUNCH = 45684480
+# workload, from the ncu launch list of one step.
+VELOCITY_TRAFFIC_PER_LAUNCH = 45570304 + 1165312
 # dram__bytes_read.sum + dram__bytes_write.sum of one k_world_velocity launch
-# on a 1024-world batch (1 057 024 solver contacts), per solver contact: the
-# batched line scales it by its own solver contacts (the traffic of the
-# per-world kernel grows with the contacts it sweeps).
-WORLD_VELOCITY_TRAFFIC_PER_CONTACT = 580477184 / 1057024
+# on a 1024-world batch at step 63 (1 142 644 contacts, records larger than
+# L2, so every sweep streams them), per contact: the batched line scales it by
+# its own solver contacts.
+WORLD_VELOCITY_TRAFFIC_PER_CONTACT = (1969872000 + 293148160) / 1142644
 
 
 def pinned(a):

@@ -48,7 +48,7 @@ typedef enum npgpu_status {
     NPGPU_OK = 0,
     NPGPU_ERR_INVALID_HANDLE = 1,
     NPGPU_ERR_UNSUPPORTED_BODY = 2,   /* multibody, FEM, mass-spring, mass-constraint */
-    NPGPU_ERR_UNSUPPORTED_SHAPE = 3,  /* anything but Ball and Cuboid, or a sensor */
+    NPGPU_ERR_UNSUPPORTED_SHAPE = 3,  /* anything but Ball, Cuboid and Capsule, or a sensor */
     NPGPU_ERR_NONEMPTY_JOINTS = 4,
     NPGPU_ERR_NONEMPTY_FORCES = 5,
     NPGPU_ERR_CAPACITY = 6,           /* a fixed-capacity device buffer overflowed */
@@ -110,9 +110,11 @@ typedef struct npgpu_body_desc {
 
 /* Shapes (ncollide3d::shape). */
 enum {
-    NPGPU_SHAPE_BALL = 0,
-    NPGPU_SHAPE_CUBOID = 1,
-    NPGPU_SHAPE_OTHER = 2        /* rejected with UNSUPPORTED_SHAPE */
+    NPGPU_SHAPE_BALL = 0,        /* shape_params: radius */
+    NPGPU_SHAPE_CUBOID = 1,      /* shape_params: half extents */
+    NPGPU_SHAPE_OTHER = 2,       /* rejected with UNSUPPORTED_SHAPE */
+    NPGPU_SHAPE_CAPSULE = 3      /* shape_params: radius, half height; the axis is the local y axis
+                                    (ncollide3d::shape::Capsule::new(half_height, radius)) */
 };
 
 /* MaterialCombineMode (src/material/material.rs:49-64). */
@@ -128,7 +130,7 @@ enum {
 typedef struct npgpu_collider_desc {
     npgpu_handle body;          /* parent body (BodyPartHandle(body, 0)) */
     float position_wrt_body[7]; /* ColliderDesc::position */
-    float shape_params[3];      /* ball: radius; cuboid: half extents */
+    float shape_params[3];      /* ball: radius; cuboid: half extents; capsule: radius, half height */
     float margin;               /* default 0.01 (collider.rs:476-479) */
     float density;              /* default 0 (collider.rs:469) */
     float linear_prediction;    /* default 0.001 (collider.rs:457) */

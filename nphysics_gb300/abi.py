@@ -46,7 +46,7 @@ BODY_CAN_SLEEP = 1 << 7
 SCHEDULE_AUTO, SCHEDULE_GRID, SCHEDULE_WORLDS = 0, 1, 2
 BODY_LINEAR_INTERP = 1 << 8
 # Shapes
-SHAPE_BALL, SHAPE_CUBOID, SHAPE_OTHER = 0, 1, 2
+SHAPE_BALL, SHAPE_CUBOID, SHAPE_OTHER, SHAPE_CAPSULE = 0, 1, 2, 3
 # Combine modes
 COMBINE_AVERAGE, COMBINE_MIN, COMBINE_MULTIPLY, COMBINE_MAX = 0, 1, 2, 3
 

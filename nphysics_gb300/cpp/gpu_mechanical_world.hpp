@@ -331,6 +331,10 @@ class ColliderDesc {
 public:
     static ColliderDesc ball(float radius) { return ColliderDesc(NPGPU_SHAPE_BALL, radius, 0.0f, 0.0f); }
     static ColliderDesc cuboid(Vector3 half) { return ColliderDesc(NPGPU_SHAPE_CUBOID, half.x, half.y, half.z); }
+    // ColliderDesc::new(ShapeHandle::new(Capsule::new(half_height, radius))): axis along local y.
+    static ColliderDesc capsule(float half_height, float radius) {
+        return ColliderDesc(NPGPU_SHAPE_CAPSULE, radius, half_height, 0.0f);
+    }
     static ColliderDesc other_shape() { return ColliderDesc(NPGPU_SHAPE_OTHER, 0.0f, 0.0f, 0.0f); }
     ColliderDesc& translation(Vector3 t) {
         d_.position_wrt_body[0] = t.x;

@@ -80,6 +80,10 @@ __global__ void k_sync_aabb(World w, float bp_margin, int world_bits) {
     np::V half;
     if (shape == SHAPE_BALL) {
         half = np::mk(prm.x, prm.x, prm.x);
+    } else if (shape == SHAPE_CAPSULE) {
+        // The axis's extent along each world axis, loosened by the radius.
+        np::M rot = np::qmat(pose.q);
+        for (int a = 0; a < 3; ++a) np::setc(half, a, fabsf(rot.m[a][1]) * prm.y + prm.x);
     } else {
         np::M rot = np::qmat(pose.q);
         for (int a = 0; a < 3; ++a) {
@@ -379,6 +383,13 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
         nk = out.n;
     } else if (a.shape == SHAPE_BALL && b.shape == SHAPE_CUBOID) {
         ball_box(a, b, false, prediction, out);
+        nk = out.n;
+    } else if (a.shape == SHAPE_CAPSULE || b.shape == SHAPE_CAPSULE) {
+        if (a.shape == SHAPE_CAPSULE && b.shape == SHAPE_CAPSULE) capsule_capsule(a, b, prediction, out);
+        else if (a.shape == SHAPE_BALL) ball_capsule(a, b, false, prediction, out);
+        else if (b.shape == SHAPE_BALL) ball_capsule(b, a, true, prediction, out);
+        else if (a.shape == SHAPE_CUBOID) capsule_box(b, a, true, prediction, out);
+        else capsule_box(a, b, false, prediction, out);
         nk = out.n;
     } else {
         nk = box_box(a, b, prediction, out, keep);

@@ -10,7 +10,8 @@
 //    starts inside hits at t = 0 with a zero normal. The ball test solves the
 //    sphere's quadratic, the cuboid test clips the ray against the three slabs
 //    in the cuboid's frame (Kay and Kajiya), the normal being the face of the
-//    last slab entered.
+//    last slab entered; a capsule is the union of its cylinder (clipped to the
+//    axis's extent) and its two end spheres, the first hit the earliest.
 //  - point: every collider whose shape contains the point (boundary included).
 //  - aabb: every collider whose fat AABB intersects the box (closed boxes),
 //    the broad-phase test the reference's query makes.
@@ -41,6 +42,61 @@ __device__ __forceinline__ Shape query_shape(const Colliders& c, uint32_t i) {
     const float4 q = c.pose_q[i];
     s.pose.q = np::Q{q.x, q.y, q.z, q.w};
     return s;
+}
+
+// First entry of a ray into the sphere of centre c and radius r, from a
+// start outside it (t = -1 when it misses).
+__device__ __forceinline__ float ray_sphere_entry(np::V o, np::V d, np::V c, float r) {
+    const np::V m = np::sub(o, c);
+    const float a = np::dot(d, d), b = np::dot(m, d), cc = np::dot(m, m) - r * r;
+    if ((cc > 0.0f && b > 0.0f) || a == 0.0f) return -1.0f;
+    const float disc = b * b - a * cc;
+    if (disc < 0.0f) return -1.0f;
+    return (-b - sqrtf(disc)) / a;
+}
+
+// Ray against a solid capsule (axis along its local y, half height h.y, radius h.x).
+__device__ __forceinline__ bool ray_capsule(np::V o, np::V d, const Shape& s, float max_toi, float& toi, np::V& n) {
+    const np::V lo = np::qrot_inv(s.pose.q, np::sub(o, s.pose.t));
+    const np::V ld = np::qrot_inv(s.pose.q, d);
+    const float r = s.h.x, hh = s.h.y;
+    {
+        np::V qa, qb;
+        closest_segment_segment(np::mk(0.0f, -hh, 0.0f), np::mk(0.0f, hh, 0.0f), lo, lo, qa, qb);
+        const np::V v = np::sub(qb, qa);
+        if (np::dot(v, v) <= r * r) {
+            toi = 0.0f;
+            n = np::mk(0.0f, 0.0f, 0.0f);
+            return true;
+        }
+    }
+    float best = INFINITY;
+    np::V bn = np::mk(0.0f, 0.0f, 0.0f);
+    const float a = ld.x * ld.x + ld.z * ld.z;
+    if (a > 0.0f) {
+        const float b = lo.x * ld.x + lo.z * ld.z, c = lo.x * lo.x + lo.z * lo.z - r * r;
+        const float disc = b * b - a * c;
+        if (disc >= 0.0f) {
+            const float t = (-b - sqrtf(disc)) / a;
+            const float y = lo.y + t * ld.y;
+            if (t >= 0.0f && fabsf(y) <= hh) {
+                best = t;
+                bn = np::divs(np::mk(lo.x + t * ld.x, 0.0f, lo.z + t * ld.z), r);
+            }
+        }
+    }
+    for (int e = 0; e < 2; ++e) {
+        const np::V c = np::mk(0.0f, e ? hh : -hh, 0.0f);
+        const float t = ray_sphere_entry(lo, ld, c, r);
+        if (t >= 0.0f && t < best) {
+            best = t;
+            bn = np::divs(np::sub(np::add(lo, np::mul(ld, t)), c), r);
+        }
+    }
+    if (!(best <= max_toi)) return false;
+    toi = best;
+    n = np::qrot(s.pose.q, bn);
+    return true;
 }
 
 // Ray against a solid ball: the smaller root of |o + t d - c|^2 = r^2.
@@ -120,6 +176,13 @@ __device__ __forceinline__ bool point_in(np::V p, const Shape& s) {
         const np::V m = np::sub(p, s.pose.t);
         return np::dot(m, m) <= s.radius * s.radius;
     }
+    if (s.shape == SHAPE_CAPSULE) {
+        const np::V l = np::qrot_inv(s.pose.q, np::sub(p, s.pose.t));
+        np::V qa, qb;
+        closest_segment_segment(np::mk(0.0f, -s.h.y, 0.0f), np::mk(0.0f, s.h.y, 0.0f), l, l, qa, qb);
+        const np::V v = np::sub(qb, qa);
+        return np::dot(v, v) <= s.h.x * s.h.x;
+    }
     const np::V l = np::qrot_inv(s.pose.q, np::sub(p, s.pose.t));
     return fabsf(l.x) <= s.h.x && fabsf(l.y) <= s.h.y && fabsf(l.z) <= s.h.z;
 }
@@ -174,8 +237,9 @@ __device__ __forceinline__ bool leaf_hit(const World& w, const Query& q, uint32_
     if (q.kind == Q_POINT) return point_in(q.o, s);
     float toi = 0.0f;
     np::V n;
-    const bool hit = s.shape == SHAPE_BALL ? ray_ball(q.o, q.d, s, q.max_toi, toi, n)
-                                           : ray_cuboid(q.o, q.d, s, q.max_toi, toi, n);
+    const bool hit = s.shape == SHAPE_BALL      ? ray_ball(q.o, q.d, s, q.max_toi, toi, n)
+                     : s.shape == SHAPE_CAPSULE ? ray_capsule(q.o, q.d, s, q.max_toi, toi, n)
+                                                : ray_cuboid(q.o, q.d, s, q.max_toi, toi, n);
     if (hit) {
         h.toi = toi;
         h.nx = n.x;

@@ -889,9 +889,9 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
             const uint32_t sh1 = ci1 & 0xfu, sh2 = ci2 & 0xfu;
             const float4 pp1 = c.params[c1], pp2 = c.params[c2];
             const float4 wt1 = c.wrt_t[c1], wt2 = c.wrt_t[c2];
-            pr4[0] = make_float4(wt1.x, wt1.y, wt1.z, (sh1 == SHAPE_BALL ? pp1.x : 0.0f) + m1);
+            pr4[0] = make_float4(wt1.x, wt1.y, wt1.z, (sh1 == SHAPE_BALL || sh1 == SHAPE_CAPSULE ? pp1.x : 0.0f) + m1);
             pr4[1] = c.wrt_q[c1];
-            pr4[2] = make_float4(wt2.x, wt2.y, wt2.z, (sh2 == SHAPE_BALL ? pp2.x : 0.0f) + m2);
+            pr4[2] = make_float4(wt2.x, wt2.y, wt2.z, (sh2 == SHAPE_BALL || sh2 == SHAPE_CAPSULE ? pp2.x : 0.0f) + m2);
             pr4[3] = c.wrt_q[c2];
             pr4[4] = make_float4(pp1.x, pp1.y, pp1.z, __uint_as_float(sh1 | (nc << 8)));
             pr4[5] = make_float4(pp2.x, pp2.y, pp2.z, __uint_as_float(sh2));

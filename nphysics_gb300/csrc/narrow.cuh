@@ -2,13 +2,17 @@
 // kinematic re-evaluation (ncollide3d query::ContactKinematic::contact, used by
 // NonlinearSORProx at src/solver/nonlinear_sor_prox.rs:221-229) and one-shot
 // manifolds for ball-ball, ball-cuboid and cuboid-cuboid pairs (ncollide3d's
-// NarrowPhase, driven by src/world/geometrical_world.rs:315-320).
+// NarrowPhase, driven by src/world/geometrical_world.rs:315-320), and for
+// capsules (a segment along the local y axis dilated by a radius) against
+// balls, capsules and cuboids.
 //
 // Methods: SAT over the 15 box axes with a bias toward face axes, then
 // Sutherland-Hodgman clipping of the incident face against the reference
 // face with per-point feature tracking, and a 4-point reduction; Ericson's
 // segment-segment closest points. Feature ids of a cuboid: vertices 0-7,
-// edges 8-19, faces 20-25; a ball has the single feature 0.
+// edges 8-19, faces 20-25; a ball has the single feature 0; a capsule has its
+// axis (0, a segment) and its two ends (1 at -half_height, 2 at +half_height,
+// points), each dilated by the radius.
 #pragma once
 #include <cfloat>
 #include "dyn.cuh"
@@ -16,7 +20,7 @@
 namespace npgpu_dev {
 
 enum { AP_POINT = 1, AP_SEGMENT = 2, AP_PLANE = 3 };
-enum { SHAPE_BALL = 0, SHAPE_CUBOID = 1 };
+enum { SHAPE_BALL = 0, SHAPE_CUBOID = 1, SHAPE_CAPSULE = 3 };
 
 struct Approx {
     int kind;
@@ -60,6 +64,21 @@ __device__ __forceinline__ Approx box_feature(np::V h, int fid) {
     return ap;
 }
 
+// A capsule's feature: its axis (fid 0) or one of its ends (1, 2); h = (radius, half_height, 0).
+__device__ __forceinline__ Approx capsule_feature(np::V h, int fid) {
+    Approx ap;
+    const np::V lo = np::mk(0.0f, -h.y, 0.0f), hi = np::mk(0.0f, h.y, 0.0f);
+    if (fid == 0) {
+        ap.kind = AP_SEGMENT;
+        ap.a = lo;
+        ap.b = hi;
+    } else {
+        ap.kind = AP_POINT;
+        ap.a = ap.b = fid == 1 ? lo : hi;
+    }
+    return ap;
+}
+
 __device__ __forceinline__ Approx feature_of(uint32_t shape, np::V h, int fid) {
     if (shape == SHAPE_BALL) {
         Approx ap;
@@ -67,13 +86,16 @@ __device__ __forceinline__ Approx feature_of(uint32_t shape, np::V h, int fid) {
         ap.a = ap.b = np::mk(0.0f, 0.0f, 0.0f);
         return ap;
     }
+    if (shape == SHAPE_CAPSULE) return capsule_feature(h, fid);
     return box_feature(h, fid);
 }
 
 __device__ __forceinline__ float clamp01(float x) { return np_min(np_max(x, 0.0f), 1.0f); }
 
-// Ericson, Real-Time Collision Detection 5.1.9.
-__device__ __forceinline__ void closest_segment_segment(np::V p1, np::V q1, np::V p2, np::V q2, np::V& c1, np::V& c2) {
+// Ericson, Real-Time Collision Detection 5.1.9. The segments' parameters of
+// the closest points go to *so and *to when given.
+__device__ __forceinline__ void closest_segment_segment(np::V p1, np::V q1, np::V p2, np::V q2, np::V& c1, np::V& c2,
+                                                        float* so = nullptr, float* to = nullptr) {
     const float eps = FLT_EPSILON;
     np::V d1 = np::sub(q1, p1), d2 = np::sub(q2, p2), r = np::sub(p1, p2);
     float a = np::dot(d1, d1), e = np::dot(d2, d2), f = np::dot(d2, r);
@@ -105,6 +127,8 @@ __device__ __forceinline__ void closest_segment_segment(np::V p1, np::V q1, np::
     }
     c1 = np::add(p1, np::mul(d1, s));
     c2 = np::add(p2, np::mul(d2, t));
+    if (so) *so = s;
+    if (to) *to = t;
 }
 
 struct Geom {
@@ -168,7 +192,7 @@ struct Shape {
     np::V h;         // half extents (cuboid) or (radius, 0, 0)
     float radius;
     np::Iso pose;
-    __device__ float dil() const { return shape == SHAPE_BALL ? radius : 0.0f; }
+    __device__ float dil() const { return (shape == SHAPE_BALL || shape == SHAPE_CAPSULE) ? radius : 0.0f; }
 };
 
 struct Cand {
@@ -198,10 +222,11 @@ __device__ __forceinline__ void push_eval(CandListN<N>& out, const Shape& s1, co
     }
 }
 
-// Ball (sb) against cuboid (sx): closest point of the cuboid to the center.
-__device__ __forceinline__ void ball_box(const Shape& sb, const Shape& sx, bool box_first, float prediction,
-                                         CandList& out) {
-    np::V c = np::iso_inv_pt(sx.pose, sb.pose.t);
+// A sphere around `centre` (feature sfid of shape sb: a ball, or a capsule's
+// end) against cuboid sx: the closest point of the cuboid to the centre.
+__device__ __forceinline__ void sphere_box(const Shape& sb, int sfid, np::V centre, const Shape& sx, bool box_first,
+                                           float prediction, CandList& out) {
+    np::V c = np::iso_inv_pt(sx.pose, centre);
     np::V h = sx.h;
     int sign[3], nclamped = 0;
     np::V p = c;
@@ -251,8 +276,204 @@ __device__ __forceinline__ void ball_box(const Shape& sb, const Shape& sx, bool 
         nl = np::divs(v, np::norm(v));
     }
     np::V n = np::qrot(sx.pose.q, nl);
-    if (box_first) push_eval(out, sx, sb, fid, 0, n, prediction);
-    else push_eval(out, sb, sx, 0, fid, np::neg(n), prediction);
+    if (box_first) push_eval(out, sx, sb, fid, sfid, n, prediction);
+    else push_eval(out, sb, sx, sfid, fid, np::neg(n), prediction);
+}
+
+// Ball (sb) against cuboid (sx): closest point of the cuboid to the center.
+__device__ __forceinline__ void ball_box(const Shape& sb, const Shape& sx, bool box_first, float prediction,
+                                         CandList& out) {
+    sphere_box(sb, 0, sb.pose.t, sx, box_first, prediction, out);
+}
+
+// A capsule's axis in world coordinates.
+__device__ __forceinline__ void capsule_axis(const Shape& s, np::V& p0, np::V& p1) {
+    p0 = np::iso_pt(s.pose, np::mk(0.0f, -s.h.y, 0.0f));
+    p1 = np::iso_pt(s.pose, np::mk(0.0f, s.h.y, 0.0f));
+}
+
+// Unit vector along v, or `fallback` for a null v.
+__device__ __forceinline__ np::V unit_or(np::V v, np::V fallback) {
+    const float l2 = np::dot(v, v);
+    return l2 > FLT_EPSILON * FLT_EPSILON ? np::divs(v, sqrtf(l2)) : fallback;
+}
+
+// Ball (sb) against capsule (sc): the closest point of the capsule's axis.
+__device__ __forceinline__ void ball_capsule(const Shape& sb, const Shape& sc, bool capsule_first, float prediction,
+                                             CandList& out) {
+    np::V p0, p1, qa, qb;
+    capsule_axis(sc, p0, p1);
+    closest_segment_segment(p0, p1, sb.pose.t, sb.pose.t, qa, qb);
+    const np::V n0 = unit_or(np::sub(qb, qa), np::mk(1.0f, 0.0f, 0.0f));   // from the capsule toward the ball
+    if (capsule_first) push_eval(out, sc, sb, 0, 0, n0, prediction);
+    else push_eval(out, sb, sc, 0, 0, np::neg(n0), prediction);
+}
+
+// Capsule A (collider 1) against capsule B: the closest points of the axes;
+// for parallel axes (sine below 1e-3), the two ends of their overlap.
+__device__ __forceinline__ void capsule_capsule(const Shape& A, const Shape& B, float prediction, CandList& out) {
+    np::V a0, a1, b0, b1, qa, qb;
+    capsule_axis(A, a0, a1);
+    capsule_axis(B, b0, b1);
+    closest_segment_segment(a0, a1, b0, b1, qa, qb);
+    const np::V da = np::sub(a1, a0), db = np::sub(b1, b0);
+    const np::V cr = np::cross(da, db);
+    const np::V n0 = unit_or(np::sub(qb, qa), unit_or(cr, np::mk(1.0f, 0.0f, 0.0f)));
+    const float la2 = np::dot(da, da), lb2 = np::dot(db, db);
+    if (np::dot(cr, cr) > 1e-6f * la2 * lb2 || la2 <= FLT_EPSILON) {
+        push_eval(out, A, B, 0, 0, n0, prediction);
+        return;
+    }
+    // Parallel: B's ends projected on A's axis (parameters in A's length).
+    const float tb0 = np::dot(np::sub(b0, a0), da) / la2, tb1 = np::dot(np::sub(b1, a0), da) / la2;
+    const int flo = tb0 <= tb1 ? 1 : 2, fhi = tb0 <= tb1 ? 2 : 1;
+    const float blo = tb0 <= tb1 ? tb0 : tb1, bhi = tb0 <= tb1 ? tb1 : tb0;
+    if (bhi < 0.0f || blo > 1.0f) {
+        push_eval(out, A, B, 0, 0, n0, prediction);
+        return;
+    }
+    if (blo > 0.0f) push_eval(out, A, B, 0, flo, n0, prediction);
+    else push_eval(out, A, B, 1, 0, n0, prediction);
+    if (bhi < 1.0f) push_eval(out, A, B, 0, fhi, n0, prediction);
+    else push_eval(out, A, B, 2, 0, n0, prediction);
+}
+
+// push_eval for a candidate whose feature pair is not already in `out`.
+template <int N>
+__device__ __forceinline__ void push_eval_unique(CandListN<N>& out, const Shape& s1, const Shape& s2, int f1, int f2,
+                                                 np::V n0, float prediction) {
+    for (int k = 0; k < out.n; ++k)
+        if (out.c[k].f1 == f1 && out.c[k].f2 == f2) return;
+    push_eval(out, s1, s2, f1, f2, n0, prediction);
+}
+
+// The cuboid edge where face (k, sk) meets the side plane (o, so); sk, so = +-1.
+__device__ __forceinline__ int face_side_edge(int k, int sk, int o, int so) {
+    const int a = 3 - k - o;
+    int o1, o2;
+    edge_other_axes(a, o1, o2);
+    const int s1 = (o1 == k ? sk : so) > 0 ? 1 : 0, s2 = (o2 == k ? sk : so) > 0 ? 1 : 0;
+    return box_edge_id(a, s1, s2);
+}
+
+__device__ __forceinline__ int vertex_at(np::V p) { return box_vertex_id(p.x > 0.0f, p.y > 0.0f, p.z > 0.0f); }
+
+// Capsule (sc) against cuboid (sx). The reference face is the cuboid face
+// farthest from the capsule's axis (the largest of the six face separations
+// of the axis's nearer end); the axis is clipped to that face's rectangle and
+// each end of the clipped axis gives a candidate: an end of the capsule
+// against the face (point-plane), or the axis against the face edge that
+// clipped it (segment-segment). When the axis does not overlap the face's
+// rectangle, the candidates are each end of the capsule as a sphere against
+// the cuboid, and the axis against the nearest cuboid edge: an edge-edge
+// contact when both closest points lie inside their segments, or, for an
+// axis parallel to the edge (sine below 1e-3), the two ends of their overlap.
+__device__ __forceinline__ void capsule_box(const Shape& sc, const Shape& sx, bool box_first, float prediction,
+                                            CandList& out) {
+    np::V p0, p1;
+    capsule_axis(sc, p0, p1);
+    const np::V l0 = np::iso_inv_pt(sx.pose, p0), l1 = np::iso_inv_pt(sx.pose, p1);
+    const np::V h = sx.h;
+    // A candidate (cuboid feature fb, capsule feature fc) with the default
+    // normal nl (cuboid frame, from the cuboid toward the capsule).
+    auto cand = [&](int fb, int fc, np::V nl) {
+        const np::V n = np::qrot(sx.pose.q, nl);
+        if (box_first) push_eval_unique(out, sx, sc, fb, fc, n, prediction);
+        else push_eval_unique(out, sc, sx, fc, fb, np::neg(n), prediction);
+    };
+    int k = 0, sk = 1;
+    float best = -FLT_MAX;
+    for (int a = 0; a < 3; ++a) {
+        for (int sg = 1; sg >= -1; sg -= 2) {
+            const float e0 = (float)sg * np::comp(l0, a), e1 = (float)sg * np::comp(l1, a);
+            const float sep = (e0 < e1 ? e0 : e1) - np::comp(h, a);
+            if (sep > best) {
+                best = sep;
+                k = a;
+                sk = sg;
+            }
+        }
+    }
+    np::V nf = np::mk(0.0f, 0.0f, 0.0f);
+    np::setc(nf, k, (float)sk);
+    const int face = box_face_id(k, sk > 0 ? 1 : 0);
+    float tlo = 0.0f, thi = 1.0f;
+    int elo = -1, ehi = -1;
+    bool empty = false;
+    for (int o = 0; o < 3 && !empty; ++o) {
+        if (o == k) continue;
+        for (int so = 1; so >= -1 && !empty; so -= 2) {
+            const float f0 = (float)so * np::comp(l0, o) - np::comp(h, o);
+            const float f1 = (float)so * np::comp(l1, o) - np::comp(h, o);
+            if (f0 > 0.0f && f1 > 0.0f) {
+                empty = true;
+            } else if (f0 > 0.0f) {
+                const float t = f0 / (f0 - f1);
+                if (t > tlo) {
+                    tlo = t;
+                    elo = face_side_edge(k, sk, o, so);
+                }
+            } else if (f1 > 0.0f) {
+                const float t = f0 / (f0 - f1);
+                if (t < thi) {
+                    thi = t;
+                    ehi = face_side_edge(k, sk, o, so);
+                }
+            }
+        }
+    }
+    if (!empty && tlo <= thi) {
+        if (elo < 0) cand(face, 1, nf);
+        else cand(elo, 0, nf);
+        if (ehi < 0) cand(face, 2, nf);
+        else cand(ehi, 0, nf);
+        return;
+    }
+    sphere_box(sc, 1, p0, sx, box_first, prediction, out);
+    sphere_box(sc, 2, p1, sx, box_first, prediction, out);
+    // The nearest edge; at equal distances (a shared vertex) the edge most
+    // parallel to the axis.
+    int be = -1;
+    float bd = FLT_MAX, bp = -1.0f, bs = 0.0f, bt = 0.0f;
+    np::V bq = np::mk(0.0f, 0.0f, 0.0f), bqe = bq;
+    const np::V dl0 = np::sub(l1, l0);
+    for (int e = 0; e < 12; ++e) {
+        const Approx ed = box_feature(h, 8 + e);
+        np::V qa, qe;
+        float sa, te;
+        closest_segment_segment(l0, l1, ed.a, ed.b, qa, qe, &sa, &te);
+        const np::V v = np::sub(qa, qe);
+        const float d2 = np::dot(v, v);
+        const np::V de0 = np::sub(ed.b, ed.a);
+        const float c = np::dot(dl0, de0), par = c * c / (np::dot(dl0, dl0) * np::dot(de0, de0) + FLT_MIN);
+        if (d2 < bd || (d2 == bd && par > bp)) {
+            bp = par;
+            bd = d2;
+            be = e;
+            bs = sa;
+            bt = te;
+            bq = qa;
+            bqe = qe;
+        }
+    }
+    const Approx ed = box_feature(h, 8 + be);
+    const np::V nl = unit_or(np::sub(bq, bqe), unit_or(bq, np::mk(0.0f, 1.0f, 0.0f)));
+    const np::V dl = np::sub(l1, l0), de = np::sub(ed.b, ed.a);
+    const np::V cr = np::cross(dl, de);
+    const float ll2 = np::dot(dl, dl);
+    if (np::dot(cr, cr) > 1e-6f * ll2 * np::dot(de, de) || ll2 <= FLT_EPSILON) {
+        if (bs > 0.0f && bs < 1.0f && bt > 0.0f && bt < 1.0f) cand(8 + be, 0, nl);
+        return;
+    }
+    // Parallel: the edge's ends projected on the axis (parameters in its length).
+    const float ta = np::dot(np::sub(ed.a, l0), dl) / ll2, tb = np::dot(np::sub(ed.b, l0), dl) / ll2;
+    const np::V vlo = ta <= tb ? ed.a : ed.b, vhi = ta <= tb ? ed.b : ed.a;
+    const float lo = ta <= tb ? ta : tb, hi = ta <= tb ? tb : ta;
+    if (hi < 0.0f || lo > 1.0f) return;
+    if (lo > 0.0f) cand(vertex_at(vlo), 0, nl);
+    else cand(8 + be, 1, nl);
+    if (hi < 1.0f) cand(vertex_at(vhi), 0, nl);
+    else cand(8 + be, 2, nl);
 }
 
 // A vertex of the clipped polygon and where it comes from, packed in one

@@ -43,8 +43,9 @@ bool finite_n(const float* v, int n) {
     return true;
 }
 
-// Volumetric::transformed_mass_properties for Ball / Cuboid
-// (src/volumetric/volumetric.rs:55-59, volumetric_ball.rs:8-47, volumetric_cuboid.rs:9-78).
+// Volumetric::transformed_mass_properties for Ball / Cuboid / Capsule
+// (src/volumetric/volumetric.rs:55-59, volumetric_ball.rs:8-47, volumetric_cuboid.rs:9-78,
+// volumetric_capsule.rs:7-37 with volumetric_cylinder.rs:7-60).
 void collider_mass_properties(const npgpu_collider_desc& d, np::V& com, float& mass, np::M& ang) {
     const float pi = 3.14159265358979323846f;
     np::M unit = np::mzero();
@@ -54,6 +55,22 @@ void collider_mass_properties(const npgpu_collider_desc& d, np::V& com, float& m
         mass = vol * d.density;
         float diag = r * r * (float)(2.0 / 5.0);
         unit.m[0][0] = unit.m[1][1] = unit.m[2][2] = diag;
+    } else if (d.shape == NPGPU_SHAPE_CAPSULE) {
+        // capsule_volume = cylinder_volume + ball_volume; the unit inertia is
+        // the cylinder's plus the ball's plus the hemispheres' parallel-axis
+        // term on the two axes across the capsule.
+        float r = d.shape_params[0], hh = d.shape_params[1];
+        float vol = hh * r * r * pi * 2.0f + pi * r * r * r * (float)(4.0 / 3.0);
+        mass = vol * d.density;
+        float sq_radius = r * r;
+        float sq_height = hh * hh * 4.0f;
+        float off = (sq_radius * 3.0f + sq_height) / 12.0f;
+        float diag = r * r * (float)(2.0 / 5.0);
+        float h = hh * 2.0f;
+        float extra = h * h * 0.5f + h * r * (float)(3.0 / 8.0);
+        unit.m[0][0] = (off + diag) + extra;
+        unit.m[1][1] = sq_radius / 2.0f + diag;
+        unit.m[2][2] = (off + diag) + extra;
     } else {
         float vol = 1.0f;
         vol = vol * d.shape_params[0] * 2.0f;
@@ -739,8 +756,8 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
     for (uint32_t k = 0; k < n; ++k) {
         const npgpu_collider_desc& d = descs[k];
         uint64_t slot = handles[k].index;
-        if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID)
-            return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "only Ball and Cuboid shapes are supported");
+        if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID && d.shape != NPGPU_SHAPE_CAPSULE)
+            return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "only Ball, Cuboid and Capsule shapes are supported");
         if (d.is_sensor) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "sensor colliders are not supported");
         if (d.ccd_enabled) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "CCD-enabled colliders are not supported");
         if (slot >= w->cap_c) return fail(w, NPGPU_ERR_CAPACITY, "collider index beyond the world's capacity");
@@ -778,6 +795,7 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         u.friction = d.friction;
         u.restitution = d.restitution;
         if (d.shape == NPGPU_SHAPE_BALL) u.rank = d.shape_params[0];
+        else if (d.shape == NPGPU_SHAPE_CAPSULE) u.rank = d.shape_params[1] + d.shape_params[0];
         else u.rank = std::sqrt(d.shape_params[0] * d.shape_params[0] + d.shape_params[1] * d.shape_params[1] +
                                 d.shape_params[2] * d.shape_params[2]);
         w->nc_slots = std::max(w->nc_slots, (uint32_t)slot + 1);

@@ -421,9 +421,12 @@ def single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 5, 
     return Scene("single body", bodies, colliders)
 
 
-def random_cluster(n=64, seed=7, extent=3.0, boxes=True, balls=True, ground=True, rotate=True, world=0):
-    """A small random cluster of balls and cuboids with overlaps, for
-    collision-detection and solver parity checks."""
+def random_cluster(n=64, seed=7, extent=3.0, boxes=True, balls=True, ground=True, rotate=True, world=0,
+                   capsules=False):
+    """A small random cluster of balls and cuboids (and, with capsules=True,
+    every third body a capsule of radius U(0.15, 0.5) and half height
+    U(0.2, 0.8)) with overlaps, for collision-detection and solver parity
+    checks."""
     rng = np.random.default_rng(seed)
     parts_b, parts_c = [], []
     if ground:
@@ -452,6 +455,12 @@ def random_cluster(n=64, seed=7, extent=3.0, boxes=True, balls=True, ground=True
     p[is_ball, 0] = rng.uniform(0.2, 0.8, int(is_ball.sum()))
     p[~is_ball] = rng.uniform(0.2, 0.8, (int((~is_ball).sum()), 3))
     c["shape_params"] = p
+    if capsules:
+        cap = np.arange(n) % 3 == 2
+        c["shape"][cap] = abi.SHAPE_CAPSULE
+        c["shape_params"][cap] = np.stack([rng.uniform(0.15, 0.5, int(cap.sum())),
+                                           rng.uniform(0.2, 0.8, int(cap.sum())),
+                                           np.zeros(int(cap.sum()))], axis=1)
     parts_b.append(b)
     parts_c.append(c)
     bodies, colliders = _concat(parts_b, parts_c)

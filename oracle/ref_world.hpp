@@ -103,7 +103,8 @@ template <class R> inline Approx<R> box_feature(V3<R> h, int fid) {
 
 // Closest points of two segments (Ericson, Real-Time Collision Detection, 5.1.9).
 template <class R>
-inline void closest_segment_segment(V3<R> p1, V3<R> q1, V3<R> p2, V3<R> q2, V3<R>& c1, V3<R>& c2) {
+inline void closest_segment_segment(V3<R> p1, V3<R> q1, V3<R> p2, V3<R> q2, V3<R>& c1, V3<R>& c2,
+                                    R* so = nullptr, R* to = nullptr) {
     const R eps = std::numeric_limits<R>::epsilon();
     V3<R> d1 = q1 - p1, d2 = q2 - p2, r = p1 - p2;
     R a = dot(d1, d1), e = dot(d2, d2), f = dot(d2, r);
@@ -134,6 +135,8 @@ inline void closest_segment_segment(V3<R> p1, V3<R> q1, V3<R> p2, V3<R> q2, V3<R
     }
     c1 = p1 + d1 * s;
     c2 = p2 + d2 * t;
+    if (so) *so = s;
+    if (to) *to = t;
 }
 
 template <class R> struct ContactGeom {
@@ -236,7 +239,7 @@ template <class R> struct Collider {
     R aabb_min[3], aabb_max[3];   // fat AABB
     bool has_fat = false;
     R query_limit() const { return margin + linear_prediction; }
-    R dilation() const { return shape == NPGPU_SHAPE_BALL ? radius : R(0); }
+    R dilation() const { return (shape == NPGPU_SHAPE_BALL || shape == NPGPU_SHAPE_CAPSULE) ? radius : R(0); }
 };
 
 template <class R> struct MContact {
@@ -352,8 +355,8 @@ public:
     }
 
     npgpu_status upsert_collider(const npgpu_handle& h, const npgpu_collider_desc& d) {
-        if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID)
-            return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "only balls and cuboids are supported");
+        if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID && d.shape != NPGPU_SHAPE_CAPSULE)
+            return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "only balls, cuboids and capsules are supported");
         if (d.is_sensor) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "sensors are not supported");
         if (d.ccd_enabled) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "CCD colliders are not supported");
         if (d.body.index >= bodies.size() || !bodies[d.body.index].alive ||
@@ -472,6 +475,22 @@ public:
             mass = vol * c.density;
             R diag = r * r * R(2.0 / 5.0);
             unit.m[0][0] = unit.m[1][1] = unit.m[2][2] = diag;
+        } else if (c.shape == NPGPU_SHAPE_CAPSULE) {
+            // volumetric_capsule.rs:7-37: cylinder + ball volume; the
+            // cylinder's and the ball's unit inertia plus the hemispheres'
+            // parallel-axis term on x and z.
+            R r = c.radius, hh = c.half.y;
+            R vol = hh * r * r * pi * R(2) + pi * r * r * r * R(4.0 / 3.0);
+            mass = vol * c.density;
+            R sq_radius = r * r;
+            R sq_height = hh * hh * R(4);
+            R off = (sq_radius * R(3) + sq_height) / R(12);
+            R diag = r * r * R(2.0 / 5.0);
+            R h = hh * R(2);
+            R extra = h * h * R(0.5) + h * r * R(3.0 / 8.0);
+            unit.m[0][0] = (off + diag) + extra;
+            unit.m[1][1] = sq_radius / R(2) + diag;
+            unit.m[2][2] = (off + diag) + extra;
         } else {
             R vol = R(1);
             vol = vol * c.half.x * R(2);
@@ -590,6 +609,9 @@ public:
         V3<R> half;
         if (c.shape == NPGPU_SHAPE_BALL) {
             half = v3<R>(c.radius, c.radius, c.radius);
+        } else if (c.shape == NPGPU_SHAPE_CAPSULE) {
+            M3<R> rot = qmat(c.pose.q);
+            for (int a = 0; a < 3; ++a) setc(half, a, std::fabs(rot.m[a][1]) * c.half.y + c.radius);
         } else {
             M3<R> rot = qmat(c.pose.q);
             for (int a = 0; a < 3; ++a) {
@@ -686,6 +708,20 @@ public:
             ap.a = ap.b = v3<R>(R(0), R(0), R(0));
             return ap;
         }
+        if (c.shape == NPGPU_SHAPE_CAPSULE) {
+            // A capsule's axis (fid 0) or its ends (1 at -half height, 2 at +).
+            Approx<R> ap;
+            const V3<R> lo = v3<R>(R(0), -c.half.y, R(0)), hi = v3<R>(R(0), c.half.y, R(0));
+            if (fid == 0) {
+                ap.kind = AP_SEGMENT;
+                ap.a = lo;
+                ap.b = hi;
+            } else {
+                ap.kind = AP_POINT;
+                ap.a = ap.b = fid == 1 ? lo : hi;
+            }
+            return ap;
+        }
         return box_feature(c.half, fid);
     }
 
@@ -702,9 +738,11 @@ public:
         if (g.depth >= -prediction) out.push_back(Cand{f1, f2, g});
     }
 
-    // Ball-cuboid: closest point of the cuboid to the ball center.
-    void ball_box(const Collider<R>& cb, const Collider<R>& cx, bool box_first, R prediction, std::vector<Cand>& out) const {
-        V3<R> c = iso_inv_pt(cx.pose, cb.pose.t);
+    // A sphere around `centre` (feature sfid of cb: a ball, or a capsule's
+    // end) against cuboid cx: the closest point of the cuboid to the centre.
+    void sphere_box(const Collider<R>& cb, int sfid, V3<R> centre, const Collider<R>& cx, bool box_first, R prediction,
+                    std::vector<Cand>& out) const {
+        V3<R> c = iso_inv_pt(cx.pose, centre);
         V3<R> h = cx.half;
         int sign[3], nclamped = 0;
         V3<R> p = c;
@@ -742,8 +780,186 @@ public:
             nl = vdiv(v, norm(v));
         }
         V3<R> n = qrot(cx.pose.q, nl);   // from the cuboid toward the ball
-        if (box_first) push_eval(out, cx, cb, fid, 0, n, prediction);
-        else push_eval(out, cb, cx, 0, fid, -n, prediction);
+        if (box_first) push_eval(out, cx, cb, fid, sfid, n, prediction);
+        else push_eval(out, cb, cx, sfid, fid, -n, prediction);
+    }
+
+    // Ball-cuboid: closest point of the cuboid to the ball center.
+    void ball_box(const Collider<R>& cb, const Collider<R>& cx, bool box_first, R prediction, std::vector<Cand>& out) const {
+        sphere_box(cb, 0, cb.pose.t, cx, box_first, prediction, out);
+    }
+
+    // ---- capsules: a segment along the local y axis dilated by the radius ----
+    void capsule_axis(const Collider<R>& c, V3<R>& p0, V3<R>& p1) const {
+        p0 = iso_pt(c.pose, v3<R>(R(0), -c.half.y, R(0)));
+        p1 = iso_pt(c.pose, v3<R>(R(0), c.half.y, R(0)));
+    }
+    static V3<R> unit_or(V3<R> v, V3<R> fallback) {
+        const R eps = std::numeric_limits<R>::epsilon();
+        const R l2 = dot(v, v);
+        return l2 > eps * eps ? vdiv(v, std::sqrt(l2)) : fallback;
+    }
+    // Ball against capsule: the closest point of the capsule's axis.
+    void ball_capsule(const Collider<R>& cb, const Collider<R>& cc, bool capsule_first, R prediction,
+                      std::vector<Cand>& out) const {
+        V3<R> p0, p1, qa, qb;
+        capsule_axis(cc, p0, p1);
+        closest_segment_segment(p0, p1, cb.pose.t, cb.pose.t, qa, qb);
+        const V3<R> n0 = unit_or(qb - qa, v3<R>(R(1), R(0), R(0)));
+        if (capsule_first) push_eval(out, cc, cb, 0, 0, n0, prediction);
+        else push_eval(out, cb, cc, 0, 0, -n0, prediction);
+    }
+    // Capsule-capsule: the closest points of the axes; for parallel axes
+    // (sine below 1e-3), the two ends of their overlap.
+    void capsule_capsule(const Collider<R>& A, const Collider<R>& B, R prediction, std::vector<Cand>& out) const {
+        V3<R> a0, a1, b0, b1, qa, qb;
+        capsule_axis(A, a0, a1);
+        capsule_axis(B, b0, b1);
+        closest_segment_segment(a0, a1, b0, b1, qa, qb);
+        const V3<R> da = a1 - a0, db = b1 - b0;
+        const V3<R> cr = cross(da, db);
+        const V3<R> n0 = unit_or(qb - qa, unit_or(cr, v3<R>(R(1), R(0), R(0))));
+        const R la2 = dot(da, da), lb2 = dot(db, db);
+        if (dot(cr, cr) > R(1e-6f) * la2 * lb2 || la2 <= std::numeric_limits<R>::epsilon()) {
+            push_eval(out, A, B, 0, 0, n0, prediction);
+            return;
+        }
+        const R tb0 = dot(b0 - a0, da) / la2, tb1 = dot(b1 - a0, da) / la2;
+        const int flo = tb0 <= tb1 ? 1 : 2, fhi = tb0 <= tb1 ? 2 : 1;
+        const R blo = tb0 <= tb1 ? tb0 : tb1, bhi = tb0 <= tb1 ? tb1 : tb0;
+        if (bhi < R(0) || blo > R(1)) {
+            push_eval(out, A, B, 0, 0, n0, prediction);
+            return;
+        }
+        if (blo > R(0)) push_eval(out, A, B, 0, flo, n0, prediction);
+        else push_eval(out, A, B, 1, 0, n0, prediction);
+        if (bhi < R(1)) push_eval(out, A, B, 0, fhi, n0, prediction);
+        else push_eval(out, A, B, 2, 0, n0, prediction);
+    }
+    void push_eval_unique(std::vector<Cand>& out, const Collider<R>& c1, const Collider<R>& c2, int f1, int f2,
+                          V3<R> n0, R prediction) const {
+        for (const Cand& c : out)
+            if (c.fid1 == f1 && c.fid2 == f2) return;
+        push_eval(out, c1, c2, f1, f2, n0, prediction);
+    }
+    // The cuboid edge where face (k, sk) meets the side plane (o, so).
+    static int face_side_edge(int k, int sk, int o, int so) {
+        const int a = 3 - k - o;
+        int o1, o2;
+        edge_other_axes(a, o1, o2);
+        const int s1 = (o1 == k ? sk : so) > 0 ? 1 : 0, s2 = (o2 == k ? sk : so) > 0 ? 1 : 0;
+        return box_edge_id(a, s1, s2);
+    }
+    static int vertex_at(V3<R> p) { return box_vertex_id(p.x > R(0), p.y > R(0), p.z > R(0)); }
+    // Capsule-cuboid: the reference face is the cuboid face farthest from the
+    // capsule's axis (the largest of the six face separations of the axis's
+    // nearer end); the axis is clipped to that face's rectangle and each end of
+    // the clipped axis gives a candidate (a capsule end against the face, or
+    // the axis against the clipping edge). When the axis misses the rectangle:
+    // each capsule end as a sphere against the cuboid, and the axis against the
+    // nearest edge (edge-edge when both closest points are inside their
+    // segments; for a parallel axis, the two ends of the overlap).
+    void capsule_box(const Collider<R>& cc, const Collider<R>& cx, bool box_first, R prediction,
+                     std::vector<Cand>& out) const {
+        V3<R> p0, p1;
+        capsule_axis(cc, p0, p1);
+        const V3<R> l0 = iso_inv_pt(cx.pose, p0), l1 = iso_inv_pt(cx.pose, p1);
+        const V3<R> h = cx.half;
+        auto cand = [&](int fb, int fc, V3<R> nl) {
+            const V3<R> n = qrot(cx.pose.q, nl);
+            if (box_first) push_eval_unique(out, cx, cc, fb, fc, n, prediction);
+            else push_eval_unique(out, cc, cx, fc, fb, -n, prediction);
+        };
+        int k = 0, sk = 1;
+        R best = -std::numeric_limits<R>::max();
+        for (int a = 0; a < 3; ++a) {
+            for (int sg = 1; sg >= -1; sg -= 2) {
+                const R e0 = R(sg) * comp(l0, a), e1 = R(sg) * comp(l1, a);
+                const R sep = (e0 < e1 ? e0 : e1) - comp(h, a);
+                if (sep > best) {
+                    best = sep;
+                    k = a;
+                    sk = sg;
+                }
+            }
+        }
+        V3<R> nf = v3<R>(R(0), R(0), R(0));
+        setc(nf, k, R(sk));
+        const int face = box_face_id(k, sk > 0 ? 1 : 0);
+        R tlo = R(0), thi = R(1);
+        int elo = -1, ehi = -1;
+        bool empty = false;
+        for (int o = 0; o < 3 && !empty; ++o) {
+            if (o == k) continue;
+            for (int so = 1; so >= -1 && !empty; so -= 2) {
+                const R f0 = R(so) * comp(l0, o) - comp(h, o);
+                const R f1 = R(so) * comp(l1, o) - comp(h, o);
+                if (f0 > R(0) && f1 > R(0)) {
+                    empty = true;
+                } else if (f0 > R(0)) {
+                    const R t = f0 / (f0 - f1);
+                    if (t > tlo) {
+                        tlo = t;
+                        elo = face_side_edge(k, sk, o, so);
+                    }
+                } else if (f1 > R(0)) {
+                    const R t = f0 / (f0 - f1);
+                    if (t < thi) {
+                        thi = t;
+                        ehi = face_side_edge(k, sk, o, so);
+                    }
+                }
+            }
+        }
+        if (!empty && tlo <= thi) {
+            if (elo < 0) cand(face, 1, nf);
+            else cand(elo, 0, nf);
+            if (ehi < 0) cand(face, 2, nf);
+            else cand(ehi, 0, nf);
+            return;
+        }
+        sphere_box(cc, 1, p0, cx, box_first, prediction, out);
+        sphere_box(cc, 2, p1, cx, box_first, prediction, out);
+        int be = -1;
+        R bd = std::numeric_limits<R>::max(), bp = R(-1), bs = R(0), bt = R(0);
+        V3<R> bq = v3<R>(R(0), R(0), R(0)), bqe = bq;
+        const V3<R> dl0 = l1 - l0;
+        for (int e = 0; e < 12; ++e) {
+            const Approx<R> ed = box_feature(h, 8 + e);
+            V3<R> qa, qe;
+            R sa, te;
+            closest_segment_segment(l0, l1, ed.a, ed.b, qa, qe, &sa, &te);
+            const V3<R> v = qa - qe;
+            const R d2 = dot(v, v);
+            const V3<R> de0 = ed.b - ed.a;
+            const R c = dot(dl0, de0), par = c * c / (dot(dl0, dl0) * dot(de0, de0) + std::numeric_limits<R>::min());
+            if (d2 < bd || (d2 == bd && par > bp)) {
+                bp = par;
+                bd = d2;
+                be = e;
+                bs = sa;
+                bt = te;
+                bq = qa;
+                bqe = qe;
+            }
+        }
+        const Approx<R> ed = box_feature(h, 8 + be);
+        const V3<R> nl = unit_or(bq - bqe, unit_or(bq, v3<R>(R(0), R(1), R(0))));
+        const V3<R> dl = l1 - l0, de = ed.b - ed.a;
+        const V3<R> cr = cross(dl, de);
+        const R ll2 = dot(dl, dl);
+        if (dot(cr, cr) > R(1e-6f) * ll2 * dot(de, de) || ll2 <= std::numeric_limits<R>::epsilon()) {
+            if (bs > R(0) && bs < R(1) && bt > R(0) && bt < R(1)) cand(8 + be, 0, nl);
+            return;
+        }
+        const R ta = dot(ed.a - l0, dl) / ll2, tb = dot(ed.b - l0, dl) / ll2;
+        const V3<R> vlo = ta <= tb ? ed.a : ed.b, vhi = ta <= tb ? ed.b : ed.a;
+        const R lo = ta <= tb ? ta : tb, hi = ta <= tb ? tb : ta;
+        if (hi < R(0) || lo > R(1)) return;
+        if (lo > R(0)) cand(vertex_at(vlo), 0, nl);
+        else cand(8 + be, 1, nl);
+        if (hi < R(1)) cand(vertex_at(vhi), 0, nl);
+        else cand(8 + be, 2, nl);
     }
 
     // Cuboid-cuboid: SAT over the 15 axes, then clipping of the incident face
@@ -961,6 +1177,12 @@ public:
             ball_box(b, a, true, prediction, cands);
         } else if (a.shape == NPGPU_SHAPE_BALL && b.shape == NPGPU_SHAPE_CUBOID) {
             ball_box(a, b, false, prediction, cands);
+        } else if (a.shape == NPGPU_SHAPE_CAPSULE || b.shape == NPGPU_SHAPE_CAPSULE) {
+            if (a.shape == NPGPU_SHAPE_CAPSULE && b.shape == NPGPU_SHAPE_CAPSULE) capsule_capsule(a, b, prediction, cands);
+            else if (a.shape == NPGPU_SHAPE_BALL) ball_capsule(a, b, false, prediction, cands);
+            else if (b.shape == NPGPU_SHAPE_BALL) ball_capsule(b, a, true, prediction, cands);
+            else if (a.shape == NPGPU_SHAPE_CUBOID) capsule_box(b, a, true, prediction, cands);
+            else capsule_box(a, b, false, prediction, cands);
         } else {
             box_box(a, b, prediction, cands);
         }
@@ -1020,8 +1242,59 @@ public:
     // interferences_with_ray (geometrical_world.rs:327-341) for one ray on
     // solid shapes: the sphere's quadratic, or the cuboid's three slabs in its
     // frame (the face of the last slab entered gives the normal).
+    // First entry of a ray into a sphere from outside it (-1 when it misses).
+    static R ray_sphere_entry(V3<R> o, V3<R> d, V3<R> c, R r) {
+        const V3<R> m = o - c;
+        const R a = dot(d, d), b = dot(m, d), cc = dot(m, m) - r * r;
+        if ((cc > R(0) && b > R(0)) || a == R(0)) return R(-1);
+        const R disc = b * b - a * cc;
+        if (disc < R(0)) return R(-1);
+        return (-b - std::sqrt(disc)) / a;
+    }
     bool ray_shape(const Collider<R>& c, V3<R> o, V3<R> d, R max_toi, R& toi, V3<R>& n) const {
         const V3<R> zero = v3<R>(R(0), R(0), R(0));
+        if (c.shape == NPGPU_SHAPE_CAPSULE) {
+            // The union of the cylinder (clipped to the axis) and the end spheres.
+            const V3<R> lo = qrot_inv(c.pose.q, o - c.pose.t), ld = qrot_inv(c.pose.q, d);
+            const R r = c.half.x, hh = c.half.y;
+            {
+                V3<R> qa, qb;
+                closest_segment_segment(v3<R>(R(0), -hh, R(0)), v3<R>(R(0), hh, R(0)), lo, lo, qa, qb);
+                const V3<R> v = qb - qa;
+                if (dot(v, v) <= r * r) {
+                    toi = R(0);
+                    n = zero;
+                    return true;
+                }
+            }
+            R best = std::numeric_limits<R>::infinity();
+            V3<R> bn = zero;
+            const R a = ld.x * ld.x + ld.z * ld.z;
+            if (a > R(0)) {
+                const R b = lo.x * ld.x + lo.z * ld.z, cc = lo.x * lo.x + lo.z * lo.z - r * r;
+                const R disc = b * b - a * cc;
+                if (disc >= R(0)) {
+                    const R t = (-b - std::sqrt(disc)) / a;
+                    const R y = lo.y + t * ld.y;
+                    if (t >= R(0) && std::fabs(y) <= hh) {
+                        best = t;
+                        bn = vdiv(v3<R>(lo.x + t * ld.x, R(0), lo.z + t * ld.z), r);
+                    }
+                }
+            }
+            for (int e = 0; e < 2; ++e) {
+                const V3<R> cen = v3<R>(R(0), e ? hh : -hh, R(0));
+                const R t = ray_sphere_entry(lo, ld, cen, r);
+                if (t >= R(0) && t < best) {
+                    best = t;
+                    bn = vdiv((lo + ld * t) - cen, r);
+                }
+            }
+            if (!(best <= max_toi)) return false;
+            toi = best;
+            n = qrot(c.pose.q, bn);
+            return true;
+        }
         if (c.shape == NPGPU_SHAPE_BALL) {
             const V3<R> m = o - c.pose.t;
             const R a = dot(d, d), b = dot(m, d), cc = dot(m, m) - c.radius * c.radius;
@@ -1087,6 +1360,13 @@ public:
         if (c.shape == NPGPU_SHAPE_BALL) {
             const V3<R> m = p - c.pose.t;
             return dot(m, m) <= c.radius * c.radius;
+        }
+        if (c.shape == NPGPU_SHAPE_CAPSULE) {
+            const V3<R> l = qrot_inv(c.pose.q, p - c.pose.t);
+            V3<R> qa, qb;
+            closest_segment_segment(v3<R>(R(0), -c.half.y, R(0)), v3<R>(R(0), c.half.y, R(0)), l, l, qa, qb);
+            const V3<R> v = qb - qa;
+            return dot(v, v) <= c.half.x * c.half.x;
         }
         const V3<R> l = qrot_inv(c.pose.q, p - c.pose.t);
         return std::fabs(l.x) <= c.half.x && std::fabs(l.y) <= c.half.y && std::fabs(l.z) <= c.half.z;

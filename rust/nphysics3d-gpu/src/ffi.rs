@@ -19,6 +19,7 @@ pub const NPGPU_BODY_LINEAR_INTERP: u32 = 1 << 8;
 pub const NPGPU_SHAPE_BALL: u32 = 0;
 pub const NPGPU_SHAPE_CUBOID: u32 = 1;
 pub const NPGPU_SHAPE_OTHER: u32 = 2;
+pub const NPGPU_SHAPE_CAPSULE: u32 = 3;
 
 #[repr(C)]
 #[derive(Copy, Clone, Default, Debug, PartialEq, Eq, Hash)]

@@ -7,9 +7,10 @@
 //! position or velocity the caller set, applied forces), runs `npgpu_step`,
 //! and writes the new poses, velocities and activation back into the set, as
 //! `MechanicalWorld::step` leaves them. Scenes the GPU step does not support
-//! (multibodies, FEM or mass-spring bodies, shapes other than balls and
-//! cuboids, sensors, CCD colliders, joints, force generators) make `step`
+//! (multibodies, FEM or mass-spring bodies, shapes other than balls,
+//! cuboids and capsules, sensors, CCD colliders, joints, force generators) make `step`
 //! panic with the library's message, where nphysics would have run them.
+//! Balls, cuboids and capsules are supported.
 pub mod ffi;
 
 use std::collections::HashMap;
@@ -17,7 +18,7 @@ use std::ffi::CStr;
 
 use generational_arena::Index;
 use nalgebra::{Isometry3, Quaternion, Translation3, UnitQuaternion, Vector3};
-use ncollide3d::shape::{Ball, Cuboid};
+use ncollide3d::shape::{Ball, Capsule, Cuboid};
 use nphysics3d::algebra::{Force3, ForceType, Velocity3};
 use nphysics3d::force_generator::ForceGeneratorSet;
 use nphysics3d::joint::JointConstraintSet;
@@ -133,6 +134,9 @@ fn collider_desc(c: &Collider<f32, DefaultBodyHandle>) -> ffi::npgpu_collider_de
     } else if let Some(b) = shape.as_shape::<Cuboid<f32>>() {
         d.shape = ffi::NPGPU_SHAPE_CUBOID;
         d.shape_params = [b.half_extents.x, b.half_extents.y, b.half_extents.z];
+    } else if let Some(c) = shape.as_shape::<Capsule<f32>>() {
+        d.shape = ffi::NPGPU_SHAPE_CAPSULE;
+        d.shape_params = [c.radius, c.half_height, 0.0];
     } else {
         d.shape = ffi::NPGPU_SHAPE_OTHER;
     }

@@ -141,6 +141,33 @@ def test_converged_velocities_match_reference_order(gpu_lib):
     assert_close_rel(g.bodies()["velocity"], o.bodies()["velocity"], 1e-4, 1e-5, "converged velocities")
 
 
+@pytest.mark.parametrize("sched", [abi.SCHEDULE_GRID, abi.SCHEDULE_WORLDS])
+def test_capsule_cluster_matches_oracle(gpu_lib, sched):
+    # Balls, cuboids and capsules tumbling onto the ground: mass properties,
+    # contacts and 150 steps of poses against the oracle in the colour order,
+    # bit for bit.
+    sc = scenes.random_cluster(n=90, seed=23, extent=2.5, capsules=True)
+    p = sc.params()
+    p.solver_schedule = sched
+    g, o = make_pair(sc, params=p)
+    g.step(1)
+    o.step(1)
+    gi, gcom = g.mass_properties()
+    oi, ocom = o.mass_properties()
+    assert_close_rel(gi, oi, 1e-6, 1e-7, "local inertia")
+    kg, cg = contact_table(g.contacts())
+    ko, co = contact_table(o.contacts())
+    np.testing.assert_array_equal(kg, ko)
+    assert len(kg) > 30
+    for f in ("world1", "world2", "normal", "depth"):
+        assert_close_rel(cg[f], co[f], 1e-5, 1e-5, f)
+    g.step(149)
+    o.step(149)
+    np.testing.assert_array_equal(g.bodies()["position"], o.bodies()["position"])
+    np.testing.assert_array_equal(g.bodies()["velocity"], o.bodies()["velocity"])
+    np.testing.assert_array_equal(g.pairs(), o.pairs())
+
+
 def ball_stack(k, radius=0.5):
     """k balls stacked vertically, each touching the next, the lowest on the ground."""
     g, gc = scenes._ground(friction=0.5)

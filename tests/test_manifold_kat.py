@@ -174,7 +174,101 @@ def case_vertex_face():
     return sc, [vertex + np.array([0, DEPTH, 0])], [vertex], (0, 1, 0), DEPTH
 
 
+def _rot_z90():
+    # Turns the capsule's axis (local y) onto world x.
+    return np.array([[0.0, -1.0, 0.0], [1.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+
+
+def case_capsule_lying_on_box():
+    # A capsule (radius 0.3, half height 0.8) lying along x on the ground
+    # cuboid, 0.05 into it: one contact under each end.
+    r, hh = 0.3, 0.8
+    centre = np.array([1.0, r - DEPTH, -2.0])
+    sc = two_shapes(abi.SHAPE_CUBOID, (50, 1, 50), pose((0, -1, 0)), abi.SHAPE_CAPSULE, (r, hh, 0),
+                    pose(centre, _rot_z90()))
+    ends = [centre + np.array([-hh, 0, 0]), centre + np.array([hh, 0, 0])]
+    return (sc, [e - np.array([0, e[1], 0]) for e in ends], [e - np.array([0, r, 0]) for e in ends], (0, 1, 0),
+            DEPTH)
+
+
+def case_capsule_standing_on_box():
+    # Upright on the ground: one contact under its lower end.
+    r, hh = 0.3, 0.8
+    centre = np.array([0.5, hh + r - DEPTH, 0.2])
+    sc = two_shapes(abi.SHAPE_CUBOID, (50, 1, 50), pose((0, -1, 0)), abi.SHAPE_CAPSULE, (r, hh, 0), pose(centre))
+    low = centre - np.array([0, hh, 0])
+    return sc, [low * np.array([1, 0, 1])], [low - np.array([0, r, 0])], (0, 1, 0), DEPTH
+
+
+def case_capsule_along_box_edge():
+    # A capsule along z lying on the top +x edge of a box (half 1), longer
+    # than the edge: a contact at each end of the edge (the edge's vertices
+    # against the axis), the normal from the edge toward the axis.
+    r, hh = 0.25, 1.5
+    n = np.array([1.0, 1.0, 0.0]) / math.sqrt(2.0)
+    R = np.array([[1.0, 0.0, 0.0], [0.0, 0.0, -1.0], [0.0, 1.0, 0.0]])   # local y onto world z
+    centre = np.array([1.0, 1.0, 0.3]) + n * (r - DEPTH)
+    sc = two_shapes(abi.SHAPE_CUBOID, (1, 1, 1), pose((0, 0, 0)), abi.SHAPE_CAPSULE, (r, hh, 0), pose(centre, R))
+    ends = [np.array([1.0, 1.0, -1.0]), np.array([1.0, 1.0, 1.0])]
+    return sc, ends, [e - n * DEPTH for e in ends], n, DEPTH
+
+
+def case_capsule_across_box_edge():
+    # A horizontal capsule along x over the top +x edge of a box (half 1):
+    # its inner end rests on the top face, its axis crosses the edge; the
+    # face clipping gives the end's contact and one at the edge.
+    r, hh = 0.25, 0.6
+    centre = np.array([0.9, 1.0 + r - DEPTH, 0.2])
+    sc = two_shapes(abi.SHAPE_CUBOID, (1, 1, 1), pose((0, 0, 0)), abi.SHAPE_CAPSULE, (r, hh, 0),
+                    pose(centre, _rot_z90()))
+    inner = centre - np.array([hh, 0, 0])
+    at_edge = np.array([1.0, centre[1], centre[2]])
+    return (sc, [np.array([inner[0], 1.0, inner[2]]), np.array([1.0, 1.0, centre[2]])],
+            [inner - np.array([0, r, 0]), at_edge - np.array([0, r, 0])], (0, 1, 0), DEPTH)
+
+
+def case_ball_on_capsule():
+    # A ball resting on the middle of a horizontal capsule.
+    r, hh, rb = 0.3, 0.8, 0.4
+    c0 = np.array([0.0, 2.0, 0.0])
+    cb = c0 + np.array([0.2, r + rb - DEPTH, 0.0])
+    sc = two_shapes(abi.SHAPE_CAPSULE, (r, hh, 0), pose(c0, _rot_z90()), abi.SHAPE_BALL, (rb, 0, 0), pose(cb))
+    axis_pt = np.array([0.2, 2.0, 0.0])
+    return sc, [axis_pt + np.array([0, r, 0])], [cb - np.array([0, rb, 0])], (0, 1, 0), DEPTH
+
+
+def case_capsules_parallel():
+    # Two parallel horizontal capsules, one on the other, overlapping over
+    # x in [-0.2, 0.8]: a contact at each end of the overlap.
+    r, hh = 0.3, 0.8
+    c0 = np.array([0.0, 2.0, 0.0])
+    c1 = c0 + np.array([1.0, 2 * r - DEPTH, 0.0])
+    sc = two_shapes(abi.SHAPE_CAPSULE, (r, hh, 0), pose(c0, _rot_z90()), abi.SHAPE_CAPSULE, (r, hh, 0),
+                    pose(c1, _rot_z90()))
+    xs = [0.2, 0.8]
+    return (sc, [np.array([x, 2.0 + r, 0.0]) for x in xs], [np.array([x, c1[1] - r, 0.0]) for x in xs], (0, 1, 0),
+            DEPTH)
+
+
+def case_capsules_crossing():
+    # A capsule along x under one along z: one contact at the crossing.
+    r, hh = 0.3, 0.8
+    c0 = np.array([0.1, 2.0, -0.2])
+    Rz = np.array([[1.0, 0.0, 0.0], [0.0, 0.0, -1.0], [0.0, 1.0, 0.0]])
+    c1 = c0 + np.array([0.3, 2 * r - DEPTH, 0.4])
+    sc = two_shapes(abi.SHAPE_CAPSULE, (r, hh, 0), pose(c0, _rot_z90()), abi.SHAPE_CAPSULE, (r, hh, 0), pose(c1, Rz))
+    x = np.array([c1[0], c0[1], c0[2]])
+    return sc, [x + np.array([0, r, 0])], [np.array([c1[0], c1[1] - r, c0[2]])], (0, 1, 0), DEPTH
+
+
 CASES = {
+    "capsule_lying_on_box": case_capsule_lying_on_box,
+    "capsule_standing_on_box": case_capsule_standing_on_box,
+    "capsule_along_box_edge": case_capsule_along_box_edge,
+    "capsule_across_box_edge": case_capsule_across_box_edge,
+    "ball_on_capsule": case_ball_on_capsule,
+    "capsules_parallel": case_capsules_parallel,
+    "capsules_crossing": case_capsules_crossing,
     "face_face": case_face_face,
     "box_on_ground": case_box_on_ground,
     "ball_on_rotated_box": case_ball_on_rotated_box,

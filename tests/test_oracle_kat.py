@@ -396,3 +396,52 @@ def test_converged_stack_impulses_f32_colour_vs_f64(k):
     statics = (k - np.arange(k)) * m * 9.81 / 60.0
     np.testing.assert_allclose(out[0], out[1], rtol=1e-4)
     np.testing.assert_allclose(out[1], statics, rtol=1e-6)
+
+
+def test_capsule_mass_properties_follow_the_reference_formula():
+    # volumetric_capsule.rs:7-37 (with volumetric_cylinder.rs:7-60 and
+    # volumetric_ball.rs): volume = cylinder + ball; unit inertia = the
+    # cylinder's + the ball's + (h^2 / 2 + h r 3/8) on x and z, h = 2 half
+    # height; inertia = unit inertia x mass. Checked in f64 against that
+    # formula written out here, for a capsule turned about z by 30 degrees.
+    r, hh, rho = 0.35, 0.9, 2.5
+    vol = hh * r * r * math.pi * 2 + math.pi * r ** 3 * 4.0 / 3.0
+    m = vol * rho
+    off = (3 * r * r + 4 * hh * hh) / 12.0
+    diag = 0.4 * r * r
+    h = 2 * hh
+    extra = h * h * 0.5 + h * r * 3.0 / 8.0
+    unit = np.diag([off + diag + extra, r * r / 2 + diag, off + diag + extra])
+    a = math.radians(30.0)
+    R = np.array([[math.cos(a), -math.sin(a), 0], [math.sin(a), math.cos(a), 0], [0, 0, 1]])
+    want = R @ (unit * m) @ R.T
+    b = scenes.body_descs(1)
+    c = scenes.collider_descs(1, 0, abi.SHAPE_CAPSULE, (r, hh, 0), density=rho)
+    c["position_wrt_body"][0, 3:] = (0.0, 0.0, math.sin(a / 2), math.cos(a / 2))
+    o = OracleWorld(scenes.Scene("capsule", b, c).params(), (0.0, 0.0, 0.0), precision=64)
+    o.load_scene(scenes.Scene("capsule", b, c, gravity=(0.0, 0.0, 0.0)))
+    o.step(1)
+    inertia, com = o.mass_properties()
+    assert abs(inertia[0, 0] - m) <= 1e-6 * m
+    got = np.array([[inertia[0, 1], inertia[0, 2], inertia[0, 3]], [inertia[0, 2], inertia[0, 4], inertia[0, 5]],
+                    [inertia[0, 3], inertia[0, 5], inertia[0, 6]]])
+    np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-7)
+    np.testing.assert_allclose(com[0], 0.0, atol=1e-7)
+
+
+def test_capsule_comes_to_rest_lying_on_the_ground():
+    # A capsule dropped at a tilt onto the ground tumbles and comes to rest
+    # on its side: its axis horizontal, its centre one radius above the
+    # ground (f32 oracle, the GPU's colour order).
+    r, hh = 0.3, 0.7
+    sc = scenes.single_body(shape=abi.SHAPE_CAPSULE, params=(r, hh, 0), position=(0, 2.0, 0),
+                            rotation=(0.0, 0.0, math.sin(0.3), math.cos(0.3)))
+    o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_COLOUR)
+    o.load_scene(sc)
+    o.step(400)
+    pos = o.bodies()["position"][1]
+    assert abs(pos[1] - r) < 0.02, pos
+    q = pos[3:]
+    # The capsule's axis (its local y) in world coordinates is horizontal.
+    yaxis = np.array([2 * (q[0] * q[1] - q[2] * q[3]), 1 - 2 * (q[0] ** 2 + q[2] ** 2), 2 * (q[1] * q[2] + q[0] * q[3])])
+    assert abs(yaxis[1]) < 0.05, yaxis

@@ -117,7 +117,7 @@ def test_contact_events_gpu(gpu_lib):
 @pytest.mark.gpu
 def test_random_queries_match_oracle(gpu_lib):
     from nphysics_gb300.world import GpuWorld
-    sc = scenes.random_cluster(n=300, seed=12, extent=6.0)
+    sc = scenes.random_cluster(n=300, seed=12, extent=6.0, capsules=True)
     g = GpuWorld.for_scene(sc, sc.params())
     o = OracleWorld(sc.params(), sc.gravity, precision=32, order=ORDER_COLOUR)
     o.load_scene(sc)
