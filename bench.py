@@ -97,6 +97,10 @@ def parse():
                     help="skip the iterations-to-1e-4 comparison of the learned and plain warm starts")
     ap.add_argument("--no-batched", action="store_true",
                     help="skip the batched-worlds record of the default (pile) run")
+    ap.add_argument("--sweep-order", default="separate", choices=["separate", "manifold"],
+                    help="velocity-solve row order: every friction row, then every normal row, each "
+                         "iteration (separate: the reference's order), or each manifold's friction rows "
+                         "then its normal rows in one sweep (manifold)")
     args = ap.parse_args()
     if args.settle is None:
         args.settle = SETTLE[args.workload]
@@ -361,6 +365,69 @@ def pgs_iterations(mixed, settle=300, steps=20, cap=4096, samples_total=2_000_00
     return out
 
 
+def walls_record(steps=240, settle=30, tol_steps=20, cap=4096):
+    """BASELINE's C5 report on a two-wall subset (each wall 50 x 40 bricks and
+    64 balls, the bench's recipe): the GPU's maximum penetration, kinetic
+    energy and contacts beside the f64 oracle's (the reference's order) over
+    `steps` steps, and iterations to 1e-4 with the impulse cache alone and
+    with the learned start trained on the subset's own solver-converged
+    contacts (steps settle..settle + tol_steps - 1)."""
+    import numpy as np
+
+    from nphysics_gb300 import abi, scenes
+    from nphysics_gb300.world import GpuWorld
+    from oracle.oracle_py import ORDER_REFERENCE, OracleWorld
+    t0 = time.perf_counter()
+    sc = scenes.brick_walls(n_walls=2, seed=1234)
+    g = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
+    r = OracleWorld(sc.params(), sc.gravity, precision=64, order=ORDER_REFERENCE)
+    r.load_scene(sc)
+    ke_g, ke_r, pen_g, pen_r = [], [], [], []
+    for _ in range(steps):
+        g.step(1)
+        r.step(1)
+        cg, cr = g.counters(), r.counters()
+        ke_g.append(cg["kinetic_energy"])
+        ke_r.append(cr["kinetic_energy"])
+        pen_g.append(cg["max_penetration"])
+        pen_r.append(cr["max_penetration"])
+    g.close()
+    ke_g, ke_r = np.array(ke_g), np.array(ke_r)
+    out = {"scene": "2 brick walls (50 x 40 bricks, 64 balls each), dt 1/120", "steps": steps,
+           "max_penetration_gpu": max(pen_g), "max_penetration_f64": max(pen_r),
+           "kinetic_energy_drift_vs_f64": float(np.max(np.abs(ke_g - ke_r)) / ke_r[0]),
+           "kinetic_energy_initial": float(ke_r[0]), "kinetic_energy_final_gpu": float(ke_g[-1]),
+           "kinetic_energy_final_f64": float(ke_r[-1]), "contacts_final_gpu": cg["num_contacts"],
+           "contacts_final_f64": cr["num_contacts"]}
+    rec = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
+    p = rec.params
+    p.solve_to_tolerance, p.residual_tolerance, p.max_iterations_to_tolerance = 1, 1e-5, 1024
+    rec.set_params(p)
+    rec.mlp_record(4_000_000)
+    rec.step(settle + tol_steps)
+    rec.mlp_record(0)
+    rec.mlp_train(1, batch=4096, lr=1e-3, seed=1, init=True)
+    rec.mlp_train(3000, batch=4096, lr=1e-3, seed=2)
+    net = rec.mlp_get()
+    rec.close()
+    for name, mode in (("plain", abi.WARMSTART_CACHE), ("learned", abi.WARMSTART_LEARNED)):
+        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
+        w.mlp_set(net)
+        w.step(settle)
+        q = w.params
+        q.warmstart_mode, q.solve_to_tolerance = mode, 1
+        q.residual_tolerance, q.max_iterations_to_tolerance = 1e-4, cap
+        w.set_params(q)
+        its = []
+        for _ in range(tol_steps):
+            w.step(1)
+            its.append(w.counters()["velocity_iterations"])
+        out["iterations_to_1e-4_" + name] = _iteration_stats(its, cap)
+        w.close()
+    out["seconds"] = time.perf_counter() - t0
+    return out
+
+
 def gpu_window_rate(scene, first, steps, **kw):
     """Body-steps/s of the GPU step over steps first..first+steps-1 of the
     scene (CUDA events on the world's stream around the window), with the
@@ -526,24 +593,31 @@ def measure(args, sc, w, kind, rank, world_size, local_rank):
 SETTLE = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0, "mixed": 300}
 
 
+def _params(sc, args):
+    from nphysics_gb300 import abi
+    p = sc.params()
+    p.sweep_order = abi.SWEEP_MANIFOLD if args.sweep_order == "manifold" else abi.SWEEP_SEPARATE
+    return p
+
+
 def build_workload(kind, args, rank, world_size):
     from nphysics_gb300 import multirank, scenes
     from nphysics_gb300.world import GpuWorld
     if kind == "pile":
         # Replicas: every rank runs its own copy of the pile (one world per GPU).
         sc = scenes.ball_pile(side=args.side)
-        w = GpuWorld.for_scene(sc, sc.params())
+        w = GpuWorld.for_scene(sc, _params(sc, args))
         desc = (f"ball pile {args.side}^3 = {sc.num_dynamic} balls (radius 0.5, 1.2 lattice, seeded jitter) "
                 f"on a static ground, dt 1/60, 8 velocity / 3 position iterations")
     elif kind == "pyramid":
         sc = scenes.pyramid(base=20)
-        w = GpuWorld.for_scene(sc, sc.params())
+        w = GpuWorld.for_scene(sc, _params(sc, args))
         desc = ("box pyramid: 210 cuboids of half extent 0.5 in a 20-base triangle on a static ground, "
                 "density 1, friction 0.5, dt 1/60, 8 velocity / 3 position iterations")
     elif kind == "mixed":
         # Replicas: the 100k mixed pile of balls and cuboids on every rank.
         sc = scenes.mixed_pile(n=100_000)
-        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=12)
+        w = GpuWorld.for_scene(sc, _params(sc, args), pairs_per_collider=12)
         desc = ("mixed pile: 100000 bodies, half balls of radius U(0.2, 0.8), half cuboids of half extents "
                 "U(0.2, 0.8)^3 at uniform random orientations, density 1, friction 0.5, dropped from heights "
                 "U(1, 60) over a 100 x 100 footprint onto a static ground, dt 1/60, 8 velocity / 3 position "
@@ -551,7 +625,7 @@ def build_workload(kind, args, rank, world_size):
     elif kind == "walls":
         # Each rank steps its own 256 walls (weak scaling).
         sc = scenes.brick_walls(n_walls=256, seed=1234 + rank)
-        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8)
+        w = GpuWorld.for_scene(sc, _params(sc, args), pairs_per_collider=8)
         desc = ("brick walls: 256 walls per GPU of 50 x 40 bricks (half extents 0.5 x 0.25 x 0.25, running "
                 "bond), each struck by 64 balls of radius 0.4, density 10, at U(20, 40) m/s; friction 0.6, "
                 "dt 1/120, 8 velocity / 3 position iterations")
@@ -559,7 +633,7 @@ def build_workload(kind, args, rank, world_size):
         # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
         n_all = args.worlds_per_rank * world_size
         sc = scenes.batched_worlds(n_worlds=n_all, worlds=multirank.shard(n_all, rank, world_size))
-        w = GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=6)
+        w = GpuWorld.for_scene(sc, _params(sc, args), pairs_per_collider=6)
         desc = (f"batched worlds: {args.worlds_per_rank} worlds per GPU (of {n_all}), body counts "
                 f"log-uniform in [16, 2048] ({sc.num_dynamic} bodies on rank 0), ball piles and box stacks "
                 f"on their own grounds, dt 1/60, 8 velocity / 3 position iterations, one block per world")
@@ -592,6 +666,9 @@ def run_gpu(args):
                         "solver_schedule": {1: "one cooperative grid",
                                             2: "per world: a cluster, a block or a warp each"}[tuned[0]],
                         "world_threads": tuned[1],
+                        "sweep_order": {"separate": "every friction row, then every normal row (the reference's)",
+                                        "manifold": "each manifold's friction rows, then its normal rows"}[
+                                            args.sweep_order],
                         "parallelism": ("replicas" if args.workload in ("pile", "pyramid", "mixed")
                                         else f"worlds sharded over {world_size} GPUs")}, **m["counters"]),
         "e2e": m["e2e"], "roofline": m["roofline"], "clocks": m["clocks"], "gpu_launches": m["gpu_launches"],
@@ -610,6 +687,8 @@ def run_gpu(args):
                               "clocks": bm["clocks"], "gpu_launches": bm["gpu_launches"], "phase_ms": bm["phase_ms"],
                               "timed_steps": f"{bm['first_timed_step']}..{bm['first_timed_step'] + args.steps - 1}",
                               "world_threads": bm["tuned"][1], **bm["counters"]}
+    if rank == 0 and world_size == 1 and args.workload == "walls":
+        line["c5_report"] = walls_record()
     if rank == 0 and world_size == 1 and args.workload == "pile" and not args.no_pgs_iterations:
         line["pgs_iterations"] = pgs_iterations(scenes.mixed_pile(n=100_000))
     if rank == 0 and world_size == 1 and not args.no_cpu_baseline and args.workload == "pile":

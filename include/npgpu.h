@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 3u
+#define NPGPU_ABI_VERSION 4u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -157,6 +157,17 @@ enum {
                                      when the step does not qualify */
 };
 
+/* Row order within a velocity iteration. SEPARATE is SORProx::step's
+ * structure (sor_prox.rs:48-80): every friction row, then every normal row,
+ * each sweep over the manifolds in colour order. MANIFOLD solves a manifold's
+ * friction rows and then its normal rows before the next manifold, one sweep
+ * in colour order per iteration: another Gauss-Seidel order of the same rows,
+ * with the same fixed point and half the chain of dependent updates. */
+enum {
+    NPGPU_SWEEP_SEPARATE = 0,
+    NPGPU_SWEEP_MANIFOLD = 1
+};
+
 typedef struct npgpu_params {
     float dt;                              /* 1/60 */
     float erp;                             /* 0.2 */
@@ -188,6 +199,7 @@ typedef struct npgpu_params {
                                               world's shape, parameters, buffers); ignored when profiling */
     uint32_t world_threads;                /* threads per world block of NPGPU_SCHEDULE_WORLDS: 64, 128 or
                                               256 (0: 128); npgpu_autotune chooses it */
+    uint32_t sweep_order;                  /* NPGPU_SWEEP_*: the order of the rows within an iteration */
 } npgpu_params;
 
 /* Per-step counters: the stage names of src/counters/mod.rs:18-209 plus

@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 3
+NPGPU_ABI_VERSION = 4
 
 # npgpu_status
 OK = 0
@@ -119,6 +119,7 @@ class Params(C.Structure):
         ("solver_schedule", C.c_uint32),
         ("use_graph", C.c_uint32),
         ("world_threads", C.c_uint32),
+        ("sweep_order", C.c_uint32),
     ]
 
 
@@ -204,6 +205,7 @@ def default_params():
     p.solver_schedule = SCHEDULE_AUTO
     p.use_graph = 1
     p.world_threads = 0
+    p.sweep_order = SWEEP_SEPARATE
     return p
 
 
@@ -301,6 +303,7 @@ EXPORTED = [
 
 # Learned warm start (npgpu_mlp_*).
 WARMSTART_CACHE, WARMSTART_NONE, WARMSTART_LEARNED, WARMSTART_LEARNED_ALL = 0, 1, 2, 3
+SWEEP_SEPARATE, SWEEP_MANIFOLD = 0, 1
 MLP_IN, MLP_HIDDEN, MLP_OUT = 24, 64, 3
 MLP_PARAMS = 6009
 MLP_TRAINABLE = 5955

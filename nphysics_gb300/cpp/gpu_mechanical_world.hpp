@@ -493,6 +493,29 @@ public:
         integration_parameters.warmstart_mode = 2;
     }
 
+    // GeometricalWorld::interferences_with_ray (geometrical_world.rs:327-341)
+    // for one ray: every collider the ray hits within max_toi, with its time
+    // of impact and normal, sorted by collider.
+    std::vector<npgpu_ray_hit> interferences_with_ray(Vector3 origin, Vector3 dir, float max_toi) {
+        const float ray[6] = {origin.x, origin.y, origin.z, dir.x, dir.y, dir.z};
+        uint32_t n = 0;
+        check(npgpu_interferences_with_rays(w_, 1, ray, &max_toi, 0xffffffffu, nullptr, 0, &n));
+        std::vector<npgpu_ray_hit> hits(n);
+        if (n) check(npgpu_interferences_with_rays(w_, 1, ray, &max_toi, 0xffffffffu, hits.data(), n, &n));
+        return hits;
+    }
+
+    // GeometricalWorld::contact_events (geometrical_world.rs:373-376): the
+    // last step's events, once enable_contact_events was called.
+    void enable_contact_events(uint32_t capacity = 1u << 20) { check(npgpu_enable_contact_events(w_, capacity)); }
+    std::vector<npgpu_contact_event> contact_events() {
+        uint32_t n = 0;
+        check(npgpu_contact_events(w_, nullptr, 0, &n));
+        std::vector<npgpu_contact_event> ev(n);
+        if (n) check(npgpu_contact_events(w_, ev.data(), n, &n));
+        return ev;
+    }
+
 private:
     void check(npgpu_status s) {
         if (s != NPGPU_OK) throw Error(s, npgpu_last_error(w_));

@@ -1183,10 +1183,16 @@ __device__ __forceinline__ void normal_rows(const RS& src, uint32_t nc, bool h1,
 // the friction directions and the lever arms: KIND 0 is the warm start
 // (sor_prox.rs:19-45), 1 the friction rows of an iteration
 // (sor_prox.rs:232-343), 2 its normal rows (sor_prox.rs:181-230).
-enum { SWEEP_WARM = 0, SWEEP_FRICTION = 1, SWEEP_NORMAL = 2 };
+enum { SWEEP_WARM = 0, SWEEP_FRICTION = 1, SWEEP_NORMAL = 2, SWEEP_MANIFOLD = 3 };
 template <int KIND, class Src, class BM>
 __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, uint32_t mask, uint32_t sweep,
                                                   const BM& bm, bool h1, bool h2, DV& dv, Control* ctl) {
+    if (KIND == SWEEP_MANIFOLD) {
+        // The manifold's friction rows, then its normal rows.
+        velocity_task_src<SWEEP_FRICTION>(src, nc, mask, sweep, bm, h1, h2, dv, ctl);
+        velocity_task_src<SWEEP_NORMAL>(src, nc, mask, sweep, bm, h1, h2, dv, ctl);
+        return;
+    }
     const int kind = KIND;
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = src.rec(k);
@@ -1402,7 +1408,7 @@ struct TaskStats {
 };
 
 static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
-                                bool learned, TaskStats& ts, float4* cache) {
+                                bool learned, bool merged, TaskStats& ts, float4* cache) {
     const uint32_t T = gridDim.x * blockDim.x;
     const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
     MyTasks mt;
@@ -1447,12 +1453,15 @@ static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_
                 if (learned) warm_task(w, m, b1, b2, dv);
                 else warm_rows(global_rows(w, m), w.s.sm_nc[m], h1, h2, dv);
             } else if (k == 0 && cached) {
-                if (sw & 1u) friction_rows(cc, nc0, h1, h2, dv);
-                else normal_rows(cc, nc0, h1, h2, dv);
+                // Merged order: every sweep is the manifold's friction rows
+                // and then its normal rows; else odd sweeps are friction rows,
+                // even sweeps normal rows.
+                if (merged || (sw & 1u)) friction_rows(cc, nc0, h1, h2, dv);
+                if (merged || !(sw & 1u)) normal_rows(cc, nc0, h1, h2, dv);
             } else {
                 const uint32_t nc = w.s.sm_nc[m];
-                if (sw & 1u) friction_rows(global_rows(w, m), nc, h1, h2, dv);
-                else normal_rows(global_rows(w, m), nc, h1, h2, dv);
+                if (merged || (sw & 1u)) friction_rows(global_rows(w, m), nc, h1, h2, dv);
+                if (merged || !(sw & 1u)) normal_rows(global_rows(w, m), nc, h1, h2, dv);
             }
             publish_dvf(w.b.dvf, b1, t1 + 1u, dv.a);
             publish_dvf(w.b.dvf, b2, t2 + 1u, dv.b);
@@ -1526,19 +1535,21 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
     unsigned long long k0 = 0;
     if (prof && blockIdx.x == 0 && threadIdx.x == 0) k0 = global_ns();
     uint32_t epoch = 0;
-    if (!velocity_sweeps(w, 0, 1, ms, prof, learned, ts, s_cache)) return;
+    const bool merged = p.sweep_order == NPGPU_SWEEP_MANIFOLD;
+    const uint32_t spi = merged ? 1u : 2u;   // sweeps per iteration
+    if (!velocity_sweeps(w, 0, 1, ms, prof, learned, merged, ts, s_cache)) return;
     if (!grid_sync(w.ctl, epoch)) return;
     if (!eval_residual(w, ms, sh, epoch, true)) return;
     uint32_t iters = 0;
     if (!p.solve_to_tolerance) {
         iters = p.max_velocity_iterations;
-        if (!velocity_sweeps(w, 1, 1 + 2 * iters, ms, prof, learned, ts, s_cache)) return;
+        if (!velocity_sweeps(w, 1, 1 + spi * iters, ms, prof, learned, merged, ts, s_cache)) return;
         if (!grid_sync(w.ctl, epoch)) return;
         if (!eval_residual(w, ms, sh, epoch, false)) return;
     } else {
         for (uint32_t it = 0; it < p.max_iterations_to_tolerance; ++it) {
             if (((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
-            if (!velocity_sweeps(w, 1 + 2 * it, 3 + 2 * it, ms, prof, learned, ts, s_cache)) return;
+            if (!velocity_sweeps(w, 1 + spi * it, 1 + spi * (it + 1), ms, prof, learned, merged, ts, s_cache)) return;
             ++iters;
             if (!grid_sync(w.ctl, epoch)) return;
             if (!eval_residual(w, ms, sh, epoch, false)) return;
@@ -1728,8 +1739,12 @@ __device__ __forceinline__ void world_solve(const World& w, const StepParams& p,
     world_sweep<SWEEP_WARM>(w, wd, base, nbw, ncol, 0, dva, g);
     world_residual(w, wd, base, nbw, dva, sh, w.ctl->res_acc_init, g);
     for (uint32_t it = 0; it < p.max_velocity_iterations; ++it) {
-        world_sweep<SWEEP_FRICTION>(w, wd, base, nbw, ncol, 1 + 2 * it, dva, g);
-        world_sweep<SWEEP_NORMAL>(w, wd, base, nbw, ncol, 2 + 2 * it, dva, g);
+        if (p.sweep_order == NPGPU_SWEEP_MANIFOLD) {
+            world_sweep<SWEEP_MANIFOLD>(w, wd, base, nbw, ncol, 1 + it, dva, g);
+        } else {
+            world_sweep<SWEEP_FRICTION>(w, wd, base, nbw, ncol, 1 + 2 * it, dva, g);
+            world_sweep<SWEEP_NORMAL>(w, wd, base, nbw, ncol, 2 + 2 * it, dva, g);
+        }
     }
     world_residual(w, wd, base, nbw, dva, sh, w.ctl->res_acc, g);
 }

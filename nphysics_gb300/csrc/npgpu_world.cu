@@ -248,6 +248,7 @@ static StepParams step_params(const npgpu_world* w) {
     s.solve_to_tolerance = p.solve_to_tolerance;
     s.max_iterations_to_tolerance = p.max_iterations_to_tolerance;
     s.warmstart_mode = p.warmstart_mode;
+    s.sweep_order = p.sweep_order;
     s.profile = p.profile;
     return s;
 }
@@ -478,6 +479,7 @@ void npgpu_default_params(npgpu_params* p) {
     p->solver_schedule = NPGPU_SCHEDULE_AUTO;
     p->use_graph = 1;
     p->world_threads = 0;
+    p->sweep_order = NPGPU_SWEEP_SEPARATE;
 }
 
 static npgpu_status create_buffers(npgpu_world* w) {
@@ -627,6 +629,8 @@ npgpu_status npgpu_set_params(npgpu_world* w, const npgpu_params* params) {
     if (params->world_threads != 0 && params->world_threads != 64 && params->world_threads != 128 &&
         params->world_threads != 256)
         return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "world_threads must be 0, 64, 128 or 256");
+    if (params->sweep_order > NPGPU_SWEEP_MANIFOLD)
+        return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown sweep_order");
     w->params = *params;
     return NPGPU_OK;
 }

@@ -198,6 +198,7 @@ struct StepParams {
     uint32_t solve_to_tolerance, max_iterations_to_tolerance;
     uint32_t warmstart_mode;
     uint32_t profile;
+    uint32_t sweep_order;            // NPGPU_SWEEP_*
 };
 
 struct MlpDev;

@@ -1611,6 +1611,9 @@ public:
     std::vector<Row<R>> rows;
     std::vector<PosConstraint<R>> pos_constraints;
     std::vector<int> seq_warm, seq_friction, seq_normal, seq_pos;
+    // NPGPU_SWEEP_MANIFOLD: per manifold (in the order of `seq`), its friction
+    // rows, then its normal rows.
+    std::vector<int> seq_merged;
     std::vector<Manifold<R>*> solver_manifolds;
 
     // JP colouring with first-fit colours (the GPU solver's schedule), at
@@ -1680,7 +1683,7 @@ public:
     bool assemble() {
         rows.clear();
         pos_constraints.clear();
-        seq_warm.clear(); seq_friction.clear(); seq_normal.clear(); seq_pos.clear();
+        seq_warm.clear(); seq_friction.clear(); seq_normal.clear(); seq_pos.clear(); seq_merged.clear();
         solver_manifolds.clear();
         // Manifold collection (mechanical_world.rs:287-300).
         for (auto& kv : manifolds) {
@@ -1732,6 +1735,7 @@ public:
             R mu = combine(c1.friction, c1.friction_combine, c2.friction, c2.friction_combine);
             R e = combine(c1.restitution, c1.restitution_combine, c2.restitution, c2.restitution_combine);
             bool ground = b1.ndofs() == 0 || b2.ndofs() == 0;
+            std::vector<int> m_friction, m_normal;
             for (MContact<R>& k : m->contacts) {
                 V3<R> n = k.g.normal;
                 V3<R> center1 = k.g.world1 + n * c1.margin;
@@ -1799,8 +1803,13 @@ public:
                     (ground ? bg : bn).push_back(it[0]);
                     (ground ? bg : bn).push_back(it[1]);
                 }
+                m_friction.push_back(it[0]);
+                m_friction.push_back(it[1]);
+                m_normal.push_back(in);
                 seq_pos.push_back(int(pos_constraints.size()) - 1);
             }
+            seq_merged.insert(seq_merged.end(), m_friction.begin(), m_friction.end());
+            seq_merged.insert(seq_merged.end(), m_normal.begin(), m_normal.end());
         }
         if (order == ORDER_REFERENCE) {
             // SORProx::warmstart_set / step (sor_prox.rs:19-45, 159-179).
@@ -1958,8 +1967,15 @@ public:
         double res = counters.residual_initial;
         for (uint32_t it = 0; it < maxit; ++it) {
             if (params.solve_to_tolerance && res <= double(params.residual_tolerance)) break;
-            for (int i : seq_friction) solve_friction(rows[i]);
-            for (int i : seq_normal) solve_normal(rows[i]);
+            if (params.sweep_order == NPGPU_SWEEP_MANIFOLD) {
+                for (int i : seq_merged) {
+                    if (rows[i].friction) solve_friction(rows[i]);
+                    else solve_normal(rows[i]);
+                }
+            } else {
+                for (int i : seq_friction) solve_friction(rows[i]);
+                for (int i : seq_normal) solve_normal(rows[i]);
+            }
             ++iters;
             if (params.solve_to_tolerance) res = residual();
         }

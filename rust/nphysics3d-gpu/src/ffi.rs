@@ -20,6 +20,8 @@ pub const NPGPU_SHAPE_BALL: u32 = 0;
 pub const NPGPU_SHAPE_CUBOID: u32 = 1;
 pub const NPGPU_SHAPE_OTHER: u32 = 2;
 pub const NPGPU_SHAPE_CAPSULE: u32 = 3;
+pub const NPGPU_SWEEP_SEPARATE: u32 = 0;
+pub const NPGPU_SWEEP_MANIFOLD: u32 = 1;
 
 #[repr(C)]
 #[derive(Copy, Clone, Default, Debug, PartialEq, Eq, Hash)]
@@ -91,6 +93,7 @@ pub struct npgpu_params {
     pub solver_schedule: u32,
     pub use_graph: u32,
     pub world_threads: u32,
+    pub sweep_order: u32,
 }
 
 #[repr(C)]

@@ -352,6 +352,38 @@ impl GpuMechanicalWorld {
         assert_ok(unsafe { ffi::npgpu_apply_forces(self.raw, 1, h.as_ptr(), f.as_ptr(), wake as i32) }, self.raw);
     }
 
+    /// GeometricalWorld::interferences_with_ray (geometrical_world.rs:327-341)
+    /// for one ray: (collider slot, time of impact, normal) of every hit.
+    pub fn interferences_with_ray(&mut self, origin: &Vector3<f32>, dir: &Vector3<f32>, max_toi: f32)
+                                  -> Vec<(u32, f32, Vector3<f32>)> {
+        let ray = [origin.x, origin.y, origin.z, dir.x, dir.y, dir.z];
+        let mut n = 0u32;
+        assert_ok(unsafe {
+            ffi::npgpu_interferences_with_rays(self.raw, 1, ray.as_ptr(), &max_toi, u32::MAX,
+                                               std::ptr::null_mut(), 0, &mut n)
+        }, self.raw);
+        let mut hits = vec![ffi::npgpu_ray_hit::default(); n as usize];
+        assert_ok(unsafe {
+            ffi::npgpu_interferences_with_rays(self.raw, 1, ray.as_ptr(), &max_toi, u32::MAX, hits.as_mut_ptr(),
+                                               n, &mut n)
+        }, self.raw);
+        hits.iter().map(|h| (h.collider, h.toi, Vector3::new(h.normal[0], h.normal[1], h.normal[2]))).collect()
+    }
+
+    /// GeometricalWorld::contact_events (geometrical_world.rs:373-376) of the
+    /// last step as (collider1, collider2, stopped); `enable_contact_events`
+    /// first.
+    pub fn enable_contact_events(&mut self, capacity: u32) {
+        assert_ok(unsafe { ffi::npgpu_enable_contact_events(self.raw, capacity) }, self.raw);
+    }
+    pub fn contact_events(&mut self) -> Vec<(u32, u32, bool)> {
+        let mut n = 0u32;
+        assert_ok(unsafe { ffi::npgpu_contact_events(self.raw, std::ptr::null_mut(), 0, &mut n) }, self.raw);
+        let mut ev = vec![ffi::npgpu_contact_event::default(); n as usize];
+        assert_ok(unsafe { ffi::npgpu_contact_events(self.raw, ev.as_mut_ptr(), n, &mut n) }, self.raw);
+        ev.iter().map(|e| (e.collider1, e.collider2, e.stopped != 0)).collect()
+    }
+
     /// MechanicalWorld::counters (mechanical_world.rs:57).
     pub fn counters(&self) -> ffi::npgpu_counters {
         let mut c = ffi::npgpu_counters::default();

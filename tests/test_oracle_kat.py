@@ -162,22 +162,27 @@ def test_resting_body_falls_asleep_and_zeroes_velocity():
 
 
 def test_orders_converge_to_the_same_velocities():
-    # The colour order is a permutation of the reference's Gauss-Seidel order; run to a
-    # tight residual both converge to the same post-solve velocities.
+    # The colour order is a permutation of the reference's Gauss-Seidel order,
+    # and the per-manifold sweep order (each manifold's friction rows, then its
+    # normal rows) another; run to a tight residual they all converge to the
+    # same post-solve velocities.
     sc = scenes.pyramid(base=6)
     out = []
-    for order in (ORDER_REFERENCE, ORDER_COLOUR):
+    for order, sweep in ((ORDER_REFERENCE, abi.SWEEP_SEPARATE), (ORDER_COLOUR, abi.SWEEP_SEPARATE),
+                         (ORDER_COLOUR, abi.SWEEP_MANIFOLD)):
         p = sc.params()
         p.solve_to_tolerance = 1
         p.residual_tolerance = 1e-9
         p.max_iterations_to_tolerance = 5000
         p.max_position_iterations = 0
+        p.sweep_order = sweep
         w = OracleWorld(p, sc.gravity, precision=64, order=order)
         w.load_scene(sc)
         w.step(1)
         out.append(w.bodies()["velocity"])
         assert w.counters()["residual"] <= 1e-9
     np.testing.assert_allclose(out[0], out[1], atol=1e-6)
+    np.testing.assert_allclose(out[0], out[2], atol=1e-6)
 
 
 def test_sweep_and_prune_equals_brute_force():
