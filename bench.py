@@ -330,12 +330,19 @@ def pgs_iterations(mixed, settle=300, steps=20, cap=4096, samples_total=2_000_00
            "network": f"trained in this run: {len(data)} samples ({n3} from the mixed pile, {n1} from the "
                       f"210-box pyramid), solved to 1e-5, {train_steps} Adam steps (batch 4096, lr 1e-3), "
                       f"final loss {loss:.3f}, {t_train:.1f} s"}
-    for name, mode in (("plain", abi.WARMSTART_CACHE), ("learned", abi.WARMSTART_LEARNED)):
+    # The third arm keeps the plain start and solves each manifold's friction
+    # rows and then its normal rows in one sweep (the same rows, another
+    # Gauss-Seidel order), for its convergence per iteration beside the
+    # reference's order.
+    for name, mode, sweep in (("plain", abi.WARMSTART_CACHE, abi.SWEEP_SEPARATE),
+                              ("learned", abi.WARMSTART_LEARNED, abi.SWEEP_SEPARATE),
+                              ("plain_per_manifold_order", abi.WARMSTART_CACHE, abi.SWEEP_MANIFOLD)):
         w = GpuWorld.for_scene(mixed, mixed.params(), pairs_per_collider=12)
         w.mlp_set(net)
         w.step(settle)
         p = w.params
         p.warmstart_mode = mode
+        p.sweep_order = sweep
         p.solve_to_tolerance = 1
         p.residual_tolerance = 1e-4
         p.max_iterations_to_tolerance = cap
@@ -361,6 +368,8 @@ def pgs_iterations(mixed, settle=300, steps=20, cap=4096, samples_total=2_000_00
     out["iterations_ratio_plain_over_learned"] = out["plain"]["iterations_mean"] / out["learned"]["iterations_mean"]
     out["body_steps_ratio_learned_over_plain"] = (out["learned"]["body_steps_per_s"] /
                                                   out["plain"]["body_steps_per_s"])
+    out["iterations_ratio_plain_over_per_manifold_order"] = (out["plain"]["iterations_mean"] /
+                                                             out["plain_per_manifold_order"]["iterations_mean"])
     out["seconds"] = time.perf_counter() - t0
     return out
 

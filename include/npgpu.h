@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 4u
+#define NPGPU_ABI_VERSION 5u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -49,7 +49,7 @@ typedef enum npgpu_status {
     NPGPU_ERR_INVALID_HANDLE = 1,
     NPGPU_ERR_UNSUPPORTED_BODY = 2,   /* multibody, FEM, mass-spring, mass-constraint */
     NPGPU_ERR_UNSUPPORTED_SHAPE = 3,  /* anything but Ball, Cuboid and Capsule, or a sensor */
-    NPGPU_ERR_NONEMPTY_JOINTS = 4,
+    NPGPU_ERR_NONEMPTY_JOINTS = 4,    /* the step's joint count differs from the joints uploaded */
     NPGPU_ERR_NONEMPTY_FORCES = 5,
     NPGPU_ERR_CAPACITY = 6,           /* a fixed-capacity device buffer overflowed */
     NPGPU_ERR_NAN = 7,                /* non-finite input or state */
@@ -143,6 +143,38 @@ typedef struct npgpu_collider_desc {
     uint32_t is_sensor;         /* rejected when non-zero */
     uint32_t ccd_enabled;       /* rejected when non-zero: CCD is not built */
 } npgpu_collider_desc;
+
+/* Joint constraints (src/joint/): BallConstraint (ball_constraint.rs:13-178)
+ * keeps anchor1 and anchor2 together; FixedConstraint (fixed_constraint.rs)
+ * also keeps the frames (body rotation x reference frame) aligned. */
+enum {
+    NPGPU_JOINT_BALL = 0,
+    NPGPU_JOINT_FIXED = 1
+};
+
+/* One joint constraint as BallConstraint::new / FixedConstraint::new build it.
+ * Both bodies must belong to the same world, and body1 != body2. */
+typedef struct npgpu_joint_desc {
+    uint32_t kind;              /* NPGPU_JOINT_* */
+    uint32_t pad;
+    npgpu_handle body1;         /* BodyPartHandle(body1, 0) */
+    npgpu_handle body2;
+    float anchor1[3];           /* in body 1's local frame */
+    float anchor2[3];           /* in body 2's local frame */
+    float frame1[4];            /* FIXED: ref_frame1, a unit quaternion (i, j, k, w) */
+    float frame2[4];            /* FIXED: ref_frame2 */
+    float break_force;          /* set_break_force; FLT_MAX (the default) never breaks */
+    float break_torque;         /* FIXED: set_break_torque */
+} npgpu_joint_desc;
+
+/* A joint's state after the last step: the impulses JointConstraint::
+ * cache_impulses keeps (linear x y z, then angular x y z for FIXED) and
+ * is_broken(). */
+typedef struct npgpu_joint_state {
+    float impulses[6];
+    uint32_t broken;
+    uint32_t active;            /* solved in the last step (JointConstraint::is_active) */
+} npgpu_joint_state;
 
 /* IntegrationParameters (src/solver/integration_parameters.rs:5-190),
  * plus the GPU-only knobs at the end. */
@@ -308,9 +340,31 @@ npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
 npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
                                 const float* forces6, int auto_wake_up);
 
+/* DefaultJointConstraintSet::insert (joint_constraint.rs:54-72) of BallConstraint
+ * and FixedConstraint, with the handles the host set gave them; inserting
+ * wakes both bodies up at the next step (mechanical_world.rs:167-175). A
+ * joint's impulses start at zero and persist across steps. The solver holds
+ * the active joints beside the contact manifolds: capacity_pairs bounds the
+ * manifolds plus the active joints of a step. */
+npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                 const npgpu_joint_desc* descs);
+
+/* DefaultJointConstraintSet::remove: wakes both bodies up at the next step
+ * (mechanical_world.rs:156-165). Removing a body removes its joints
+ * (mechanical_world.rs:141-154). */
+npgpu_status npgpu_remove_joints(npgpu_world* w, uint32_t n, const npgpu_handle* handles);
+
+/* The joints' impulses (what JointConstraint::cache_impulses keeps,
+ * ball_constraint.rs:129-141, fixed_constraint.rs:174-199) and is_broken()
+ * after the last completed step (synchronises the world's stream). */
+npgpu_status npgpu_get_joints(npgpu_world* w, uint32_t n, const npgpu_handle* handles, npgpu_joint_state* out);
+
 /* MechanicalWorld::step (mechanical_world.rs:182-396) run `nsteps` times,
  * asynchronously on the world's stream. `num_joints` / `num_force_generators`
- * are the sizes of the caller's sets: non-zero is rejected. */
+ * are the sizes of the caller's sets: the joint count must equal the number
+ * of joints mirrored into the world with npgpu_upsert_joints
+ * (NONEMPTY_JOINTS otherwise), and a non-zero force-generator count is
+ * rejected. */
 npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints,
                         uint32_t num_force_generators);
 

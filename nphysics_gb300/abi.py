@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 4
+NPGPU_ABI_VERSION = 5
 
 # npgpu_status
 OK = 0
@@ -92,6 +92,47 @@ class ColliderDesc(C.Structure):
         ("is_sensor", C.c_uint32),
         ("ccd_enabled", C.c_uint32),
     ]
+
+
+# Joint kinds (BallConstraint, FixedConstraint)
+JOINT_BALL, JOINT_FIXED = 0, 1
+
+
+class JointDesc(C.Structure):
+    _fields_ = [
+        ("kind", C.c_uint32),
+        ("pad", C.c_uint32),
+        ("body1", Handle),
+        ("body2", Handle),
+        ("anchor1", C.c_float * 3),
+        ("anchor2", C.c_float * 3),
+        ("frame1", C.c_float * 4),
+        ("frame2", C.c_float * 4),
+        ("break_force", C.c_float),
+        ("break_torque", C.c_float),
+    ]
+
+
+class JointState(C.Structure):
+    _fields_ = [("impulses", C.c_float * 6), ("broken", C.c_uint32), ("active", C.c_uint32)]
+
+
+def joint_desc(kind, body1, body2, anchor1=(0, 0, 0), anchor2=(0, 0, 0), frame1=(0, 0, 0, 1), frame2=(0, 0, 0, 1),
+               break_force=None, break_torque=None):
+    """A JointDesc as BallConstraint::new / FixedConstraint::new build it
+    (body handles as (index, generation) pairs or Handle)."""
+    d = JointDesc()
+    d.kind = kind
+    for f, h in (("body1", body1), ("body2", body2)):
+        hh = h if isinstance(h, Handle) else Handle(int(h[0]), int(h[1]))
+        setattr(d, f, hh)
+    d.anchor1[:] = [float(x) for x in anchor1]
+    d.anchor2[:] = [float(x) for x in anchor2]
+    d.frame1[:] = [float(x) for x in frame1]
+    d.frame2[:] = [float(x) for x in frame2]
+    d.break_force = FLT_MAX if break_force is None else break_force
+    d.break_torque = FLT_MAX if break_torque is None else break_torque
+    return d
 
 
 class Params(C.Structure):
@@ -252,6 +293,9 @@ def load_library(path=LIB_PATH):
         "npgpu_remove_bodies": (C.c_int, [W, C.c_uint32, P(Handle)]),
         "npgpu_remove_colliders": (C.c_int, [W, C.c_uint32, P(Handle)]),
         "npgpu_apply_forces": (C.c_int, [W, C.c_uint32, P(Handle), P(C.c_float), C.c_int]),
+        "npgpu_upsert_joints": (C.c_int, [W, C.c_uint32, P(Handle), P(JointDesc)]),
+        "npgpu_remove_joints": (C.c_int, [W, C.c_uint32, P(Handle)]),
+        "npgpu_get_joints": (C.c_int, [W, C.c_uint32, P(Handle), P(JointState)]),
         "npgpu_step": (C.c_int, [W, C.c_uint32, C.c_uint32, C.c_uint32]),
         "npgpu_synchronize": (C.c_int, [W]),
         "npgpu_download_bodies": (C.c_int, [W, C.c_uint32, C.c_uint32, P(C.c_float), P(C.c_float),
@@ -293,7 +337,8 @@ def load_library(path=LIB_PATH):
 EXPORTED = [
     "npgpu_abi_version", "npgpu_default_params", "npgpu_create", "npgpu_destroy", "npgpu_stream",
     "npgpu_set_params", "npgpu_set_gravity", "npgpu_upsert_bodies", "npgpu_upsert_colliders",
-    "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_step",
+    "npgpu_remove_bodies", "npgpu_remove_colliders", "npgpu_apply_forces", "npgpu_upsert_joints",
+    "npgpu_remove_joints", "npgpu_get_joints", "npgpu_step",
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
     "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
     "npgpu_interferences_with_rays", "npgpu_interferences_with_points", "npgpu_interferences_with_aabbs",

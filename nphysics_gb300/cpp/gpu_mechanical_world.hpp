@@ -420,16 +420,105 @@ private:
 // The collision state lives on the device; this type exists for the signature.
 class DefaultGeometricalWorld {};
 
-// Joint constraints and force generators are not run on the GPU: a non-empty
-// set makes the step fail with NPGPU_ERR_NONEMPTY_JOINTS / _FORCES.
-class DefaultJointConstraintSet {
+// BallConstraint::new(b1, b2, anchor1, anchor2) (src/joint/ball_constraint.rs:26-48):
+// keeps the two anchors (in their bodies' frames) together.
+class BallConstraint {
 public:
-    size_t len() const { return n_; }
-    void insert_placeholder() { ++n_; }
+    BallConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 anchor2) {
+        std::memset(&desc, 0, sizeof(desc));
+        desc.kind = NPGPU_JOINT_BALL;
+        desc.body1 = b1.body.raw();
+        desc.body2 = b2.body.raw();
+        set(desc.anchor1, anchor1);
+        set(desc.anchor2, anchor2);
+        desc.frame1[3] = desc.frame2[3] = 1.0f;
+        desc.break_force = desc.break_torque = std::numeric_limits<float>::max();
+    }
+    void set_break_force(float f) { desc.break_force = f; }
+    bool is_broken() const { return broken_; }
+    // The impulses cache_impulses kept in the last step (linear x, y, z).
+    const float* impulses() const { return impulses_; }
+    npgpu_joint_desc desc;
 
 private:
+    friend class GpuMechanicalWorld;
+    static void set(float* o, Vector3 v) {
+        o[0] = v.x;
+        o[1] = v.y;
+        o[2] = v.z;
+    }
+    bool broken_ = false;
+    float impulses_[6] = {0, 0, 0, 0, 0, 0};
+};
+
+// FixedConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)
+// (src/joint/fixed_constraint.rs:29-58): also keeps the frames (body rotation
+// times reference frame) aligned. The reference frames are given as scaled
+// axes (UnitQuaternion::from_scaled_axis).
+class FixedConstraint {
+public:
+    FixedConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 ref_frame1, Vector3 anchor2,
+                    Vector3 ref_frame2) {
+        std::memset(&desc, 0, sizeof(desc));
+        desc.kind = NPGPU_JOINT_FIXED;
+        desc.body1 = b1.body.raw();
+        desc.body2 = b2.body.raw();
+        const float a1[3] = {anchor1.x, anchor1.y, anchor1.z}, a2[3] = {anchor2.x, anchor2.y, anchor2.z};
+        std::memcpy(desc.anchor1, a1, sizeof(a1));
+        std::memcpy(desc.anchor2, a2, sizeof(a2));
+        Isometry3 f1 = Isometry3::new_({}, ref_frame1), f2 = Isometry3::new_({}, ref_frame2);
+        std::memcpy(desc.frame1, f1.rotation, sizeof(desc.frame1));
+        std::memcpy(desc.frame2, f2.rotation, sizeof(desc.frame2));
+        desc.break_force = desc.break_torque = std::numeric_limits<float>::max();
+    }
+    void set_break_force(float f) { desc.break_force = f; }
+    void set_break_torque(float t) { desc.break_torque = t; }
+    bool is_broken() const { return broken_; }
+    // Linear x, y, z then angular x, y, z.
+    const float* impulses() const { return impulses_; }
+    npgpu_joint_desc desc;
+
+private:
+    friend class GpuMechanicalWorld;
+    bool broken_ = false;
+    float impulses_[6] = {0, 0, 0, 0, 0, 0};
+};
+
+using JointConstraint = std::variant<BallConstraint, FixedConstraint>;
+using DefaultJointConstraintHandle = Index;
+
+// DefaultJointConstraintSet (src/joint/joint_constraint.rs:31-130): the
+// joints live on the host with their handles; the step forwards insertions
+// and removals and reads the impulses and broken flags back.
+class DefaultJointConstraintSet {
+public:
+    DefaultJointConstraintHandle insert(JointConstraint j) {
+        DefaultJointConstraintHandle h = arena_.insert(std::move(j));
+        inserted_.push_back(h);
+        ++n_;
+        return h;
+    }
+    std::optional<JointConstraint> remove(DefaultJointConstraintHandle h) {
+        auto r = arena_.remove(h);
+        if (r) {
+            removed_.push_back(h);
+            --n_;
+        }
+        return r;
+    }
+    JointConstraint* get(DefaultJointConstraintHandle h) { return arena_.get(h); }
+    bool contains(DefaultJointConstraintHandle h) const { return arena_.contains(h); }
+    size_t len() const { return n_; }
+
+private:
+    friend class GpuMechanicalWorld;
+    Arena<JointConstraint> arena_;
+    std::vector<DefaultJointConstraintHandle> inserted_, removed_;
     size_t n_ = 0;
 };
+
+// Force generators are not run on the GPU: a non-empty set makes the step
+// fail with NPGPU_ERR_NONEMPTY_FORCES.
 class DefaultForceGeneratorSet {
 public:
     size_t len() const { return n_; }
@@ -468,9 +557,13 @@ public:
               DefaultJointConstraintSet& joints, DefaultForceGeneratorSet& forces) {
         check(npgpu_set_params(w_, &integration_parameters));
         maintain(bodies, colliders);
+        maintain_joints(joints);
         check(npgpu_step(w_, 1, uint32_t(joints.len()), uint32_t(forces.len())));
         check(npgpu_synchronize(w_));
-        if (write_back) download(bodies);
+        if (write_back) {
+            download(bodies);
+            download_joints(joints);
+        }
     }
 
     // Times the solver's launch shapes on real steps and keeps the fastest in
@@ -519,6 +612,41 @@ public:
 private:
     void check(npgpu_status s) {
         if (s != NPGPU_OK) throw Error(s, npgpu_last_error(w_));
+    }
+
+    // The joint set's removals, then its insertions (mechanical_world.rs:156-175).
+    void maintain_joints(DefaultJointConstraintSet& joints) {
+        std::vector<npgpu_handle> h;
+        for (auto& j : joints.removed_) h.push_back(j.raw());
+        joints.removed_.clear();
+        if (!h.empty()) check(npgpu_remove_joints(w_, uint32_t(h.size()), h.data()));
+        h.clear();
+        std::vector<npgpu_joint_desc> d;
+        for (auto& j : joints.inserted_) {
+            const JointConstraint* c = joints.arena_.get(j);
+            if (!c) continue;
+            h.push_back(j.raw());
+            d.push_back(std::visit([](const auto& x) { return x.desc; }, *c));
+        }
+        joints.inserted_.clear();
+        if (!h.empty()) check(npgpu_upsert_joints(w_, uint32_t(h.size()), h.data(), d.data()));
+    }
+
+    // JointConstraint::cache_impulses / is_broken as the step left them.
+    void download_joints(DefaultJointConstraintSet& joints) {
+        std::vector<npgpu_handle> h;
+        for (size_t i = 0; i < joints.arena_.capacity_used(); ++i)
+            if (joints.arena_.occupied(i)) h.push_back(joints.arena_.handle_at(i).raw());
+        if (h.empty()) return;
+        std::vector<npgpu_joint_state> st(h.size());
+        check(npgpu_get_joints(w_, uint32_t(h.size()), h.data(), st.data()));
+        for (size_t k = 0; k < h.size(); ++k) {
+            JointConstraint* c = joints.arena_.get(Index{h[k].index, h[k].generation});
+            std::visit([&](auto& x) {
+                x.broken_ = st[k].broken != 0;
+                std::memcpy(x.impulses_, st[k].impulses, sizeof(x.impulses_));
+            }, *c);
+        }
     }
 
     // MechanicalWorld::maintain: removals first, then insertions and edits.

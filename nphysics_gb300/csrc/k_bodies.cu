@@ -248,6 +248,33 @@ cudaError_t launch_forces(const World& w, const npgpu_handle* h, const float* f,
     k_forces<<<serial ? 1u : nblocks(n), kThreads, 0, st>>>(w, h, f, n, wake, serial);
     return cudaGetLastError();
 }
+__global__ void k_upload_joints(World w, const JointUpload* d, uint32_t n) {
+    uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const JointUpload u = d[t];
+    const uint32_t i = u.slot;
+    const Joints& j = w.j;
+    j.info[i] = u.info;
+    j.body[2 * i] = u.body1;
+    j.body[2 * i + 1] = u.body2;
+    j.anchor[2 * i] = make_float4(u.anchor1[0], u.anchor1[1], u.anchor1[2], 0.0f);
+    j.anchor[2 * i + 1] = make_float4(u.anchor2[0], u.anchor2[1], u.anchor2[2], 0.0f);
+    j.frame[2 * i] = make_float4(u.frame1[0], u.frame1[1], u.frame1[2], u.frame1[3]);
+    j.frame[2 * i + 1] = make_float4(u.frame2[0], u.frame2[1], u.frame2[2], u.frame2[3]);
+    j.brk[i] = make_float2(u.brk_force2, u.brk_torque2);
+    if (u.reset) {
+        j.imp[2 * i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        j.imp[2 * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        j.state[i] = 0u;
+    }
+}
+
+cudaError_t launch_upload_joints(const World& w, const JointUpload* d, uint32_t n, cudaStream_t st) {
+    if (n == 0) return cudaSuccess;
+    k_upload_joints<<<nblocks(n), kThreads, 0, st>>>(w, d, n);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_kill(const World& w, const uint32_t* slots, uint32_t n, int colliders, cudaStream_t st) {
     if (n == 0) return cudaSuccess;
     k_kill<<<nblocks(n), kThreads, 0, st>>>(w, slots, n, colliders);

@@ -28,6 +28,8 @@
 // dependent manifolds rather than a barrier per colour. The colouring uses the
 // same scheme over priorities. Threads poll their tasks without blocking, so
 // any assignment of manifolds to resident threads makes progress.
+#include <cfloat>
+
 #include <cooperative_groups.h>
 
 #include "mlp.cuh"
@@ -258,13 +260,11 @@ __device__ __forceinline__ BodyView load_view(const Bodies& b, uint32_t i) {
     return v;
 }
 
-// RigidBody::fill_constraint_geometry for one side of one row.
-__device__ __forceinline__ void fill_row_side(const BodyView& b, np::V point, np::V dir, float* J, float* WJ, float& inv_r,
-                                              float& rhs, bool with_ext, float dt) {
+// RigidBody::fill_constraint_geometry for one side of one row, given the
+// side's unit force f (ForceDirection::at_point, helper.rs:24-33).
+__device__ __forceinline__ void fill_force_side(const BodyView& b, const float* f, float* J, float* WJ, float& inv_r,
+                                                float& rhs, bool with_ext, float dt) {
     uint32_t st = bi_status(b.info);
-    np::V pos = np::sub(point, b.com);
-    np::V fa = np::cross(pos, dir);
-    float f[6] = {dir.x, dir.y, dir.z, fa.x, fa.y, fa.z};
     float mf[6];
 #pragma unroll
     for (int k = 0; k < 6; ++k) mf[k] = f[k] * body_mask(b.info, k);
@@ -297,6 +297,22 @@ __device__ __forceinline__ void fill_row_side(const BodyView& b, np::V point, np
     }
 }
 
+// A linear force along dir at point: Force::linear_at_point.
+__device__ __forceinline__ void fill_row_side(const BodyView& b, np::V point, np::V dir, float* J, float* WJ, float& inv_r,
+                                              float& rhs, bool with_ext, float dt) {
+    np::V pos = np::sub(point, b.com);
+    np::V fa = np::cross(pos, dir);
+    const float f[6] = {dir.x, dir.y, dir.z, fa.x, fa.y, fa.z};
+    fill_force_side(b, f, J, WJ, inv_r, rhs, with_ext, dt);
+}
+
+// A torque about axis: Force::torque_from_vector.
+__device__ __forceinline__ void fill_torque_side(const BodyView& b, np::V axis, float* J, float* WJ, float& inv_r,
+                                                 float& rhs, bool with_ext, float dt) {
+    const float f[6] = {0.0f, 0.0f, 0.0f, axis.x, axis.y, axis.z};
+    fill_force_side(b, f, J, WJ, inv_r, rhs, with_ext, dt);
+}
+
 // helper::constraint_pair_geometry for one row; writes J1 J2 WJ1 WJ2 r rhs.
 __device__ __forceinline__ void make_row(float* row, const BodyView& b1, const BodyView& b2, np::V c1, np::V c2, np::V dir,
                                          float dt) {
@@ -307,6 +323,23 @@ __device__ __forceinline__ void make_row(float* row, const BodyView& b1, const B
     fill_row_side(b2, c2, np::neg(dir), row + RF_J2, row + RF_WJ2, inv_r, rhs, true, dt);
     row[RF_R] = (inv_r != 0.0f) ? 1.0f / inv_r : 1.0f;
     row[RF_RHS] = rhs;
+}
+
+// helper::constraint_pair_geometry for a torque row (ForceDirection::Angular
+// about axis on body 1, about -axis on body 2).
+__device__ __forceinline__ void make_row_angular(float* row, const BodyView& b1, const BodyView& b2, np::V axis, float dt) {
+#pragma unroll
+    for (int k = 0; k < kRowFloats; ++k) row[k] = 0.0f;
+    float inv_r = 0.0f, rhs = 0.0f;
+    fill_torque_side(b1, axis, row + RF_J1, row + RF_WJ1, inv_r, rhs, true, dt);
+    fill_torque_side(b2, np::neg(axis), row + RF_J2, row + RF_WJ2, inv_r, rhs, true, dt);
+    row[RF_R] = (inv_r != 0.0f) ? 1.0f / inv_r : 1.0f;
+    row[RF_RHS] = rhs;
+}
+
+// The canonical basis vector e_r (helper.rs:247-296, 502-551).
+__device__ __forceinline__ np::V basis_axis(int r) {
+    return np::mk(r == 0 ? 1.0f : 0.0f, r == 1 ? 1.0f : 0.0f, r == 2 ? 1.0f : 0.0f);
 }
 
 // nalgebra Vector3::orthonormal_subspace_basis of one vector.
@@ -352,23 +385,46 @@ __device__ __forceinline__ void side_j(np::V pos, np::V dir, uint32_t m6, float*
     for (int k = 0; k < 6; ++k) J[k] = f[k] * (((m6 >> k) & 1u) ? 1.0f : 0.0f);
 }
 
-__device__ __forceinline__ float side_dot(np::V pos, np::V dir, uint32_t m6, const float* dv) {
-    float J[6];
-    side_j(pos, dir, m6, J);
+__device__ __forceinline__ float side_dot_j(const float* J, const float* dv) {
     float s = 0.0f;
 #pragma unroll
     for (int k = 0; k < 6; ++k) s = s + J[k] * dv[k];
     return s;
 }
 
-__device__ __forceinline__ void side_axpy(np::V pos, np::V dir, uint32_t m6, const SB& sb, float a, float* dv) {
-    float J[6];
-    side_j(pos, dir, m6, J);
+__device__ __forceinline__ void side_axpy_j(const float* J, const SB& sb, float a, float* dv) {
     np::V wl = np::mul(np::mk(J[0], J[1], J[2]), sb.im);
     np::V wa = np::mv(sb.I, np::mk(J[3], J[4], J[5]));
     float W[6] = {wl.x, wl.y, wl.z, wa.x, wa.y, wa.z};
 #pragma unroll
     for (int k = 0; k < 6; ++k) dv[k] = a * W[k] + dv[k];
+}
+
+__device__ __forceinline__ float side_dot(np::V pos, np::V dir, uint32_t m6, const float* dv) {
+    float J[6];
+    side_j(pos, dir, m6, J);
+    return side_dot_j(J, dv);
+}
+
+__device__ __forceinline__ void side_axpy(np::V pos, np::V dir, uint32_t m6, const SB& sb, float a, float* dv) {
+    float J[6];
+    side_j(pos, dir, m6, J);
+    side_axpy_j(J, sb, a, dv);
+}
+
+// The Jacobian of one side of a joint row: row r of the linear triple (a
+// force along +-e_r at the anchor, lever arm pos) or of the angular triple
+// (a torque about +-e_r); side 2 takes the negated direction.
+__device__ __forceinline__ void joint_side_j(bool angular, int r, np::V pos, bool side2, uint32_t m6, float* J) {
+    np::V e = basis_axis(r);
+    if (side2) e = np::neg(e);
+    if (angular) {
+        const float f[6] = {0.0f, 0.0f, 0.0f, e.x, e.y, e.z};
+#pragma unroll
+        for (int k = 0; k < 6; ++k) J[k] = f[k] * (((m6 >> k) & 1u) ? 1.0f : 0.0f);
+    } else {
+        side_j(pos, e, m6, J);
+    }
 }
 
 // J . dv over both sides: side sums, then their sum, when both sides have dofs.
@@ -494,19 +550,16 @@ struct Dot2 {
 // phi = lambda - proj(lambda - r (J dv + rhs)) of one row, squared and summed
 // with lambda^2 into `acc`; proj = max(., 0) for a normal row and the clamp
 // to +-mu lambda_n for a friction row.
-__device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, uint32_t mask, float r, float rhs,
-                                             float lam, const DV& dv, bool has1, bool has2, bool friction,
-                                             float normal_impulse, float mu, ResidualSums& acc) {
+// Row kinds of the residual's projection.
+enum { RES_NORMAL = 0, RES_FRICTION = 1, RES_BILATERAL = 2 };
+__device__ __forceinline__ void residual_row_j(const float* J1, const float* J2, float r, float rhs, float lam,
+                                               const DV& dv, bool has1, bool has2, int kind, float normal_impulse,
+                                               float mu, ResidualSums& acc) {
     Dot2 dot;
-    float J[6];
-    if (has1) {
-        side_j(pos1, dir, mask & 0x3fu, J);
-        for (int k = 0; k < 6; ++k) dot.prod(J[k], dv.a[k]);
-    }
-    if (has2) {
-        side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J);
-        for (int k = 0; k < 6; ++k) dot.prod(J[k], dv.b[k]);
-    }
+    if (has1)
+        for (int k = 0; k < 6; ++k) dot.prod(J1[k], dv.a[k]);
+    if (has2)
+        for (int k = 0; k < 6; ++k) dot.prod(J2[k], dv.b[k]);
     dot.sum(rhs, 0.0f);
     const FF d = two_sum(dot.s, dot.c);
     // rd = r d; x = lambda - rd; lambda - x = rd when the projection keeps x.
@@ -515,7 +568,9 @@ __device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, 
     FF x = two_sum(lam, -rd.hi);
     x = ff_norm(FF{x.hi, __fsub_rn(x.lo, rd.lo)});
     FF phi = rd;
-    if (!friction) {
+    if (kind == RES_BILATERAL) {
+        // Independent limits of +-FLT_MAX (helper.rs:186-189): x stays.
+    } else if (kind == RES_NORMAL) {
         if (!(x.hi > 0.0f || (x.hi == 0.0f && x.lo > 0.0f))) phi = FF{lam, 0.0f};
     } else {
         const FF mx = two_prod(mu, normal_impulse);
@@ -529,6 +584,15 @@ __device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, 
     }
     acc.s2 = ff_add(acc.s2, ff_sq(phi));
     acc.l2 = ff_add(acc.l2, two_prod(lam, lam));
+}
+
+__device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, uint32_t mask, float r, float rhs,
+                                             float lam, const DV& dv, bool has1, bool has2, bool friction,
+                                             float normal_impulse, float mu, ResidualSums& acc) {
+    float J1[6], J2[6];
+    if (has1) side_j(pos1, dir, mask & 0x3fu, J1);
+    if (has2) side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J2);
+    residual_row_j(J1, J2, r, rhs, lam, dv, has1, has2, friction ? RES_FRICTION : RES_NORMAL, normal_impulse, mu, acc);
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -628,6 +692,16 @@ __global__ void k_act_union(World w) {
         if (!body_sleepy(b, b1, i1) && !body_sleepy(b, b2, i2)) continue;
         uf_union(b.uf_parent, b1, b2, &w.ctl->err);
     }
+    // Unbroken joints join their bodies' islands (activation_manager.rs:154-159).
+    GRID_FOR(jj, w.nj_slots) {
+        if (!(w.j.info[jj] & JI_ALIVE) || (w.j.state[jj] & JS_BROKEN)) continue;
+        uint32_t b1 = w.j.body[2 * jj], b2 = w.j.body[2 * jj + 1];
+        uint32_t i1 = b.info[b1], i2 = b.info[b2];
+        uint32_t s1 = bi_status(i1), s2 = bi_status(i2);
+        if (!((s1 == 2u || s1 == 3u) && (s2 == 2u || s2 == 3u))) continue;
+        if (!body_sleepy(b, b1, i1) && !body_sleepy(b, b2, i2)) continue;
+        uf_union(b.uf_parent, b1, b2, &w.ctl->err);
+    }
 }
 #endif
 
@@ -719,6 +793,48 @@ __global__ void k_collect(World w) {
 }
 #endif
 
+// The active joints (JointConstraint::is_active, joint_constraint.rs:218-227:
+// a dynamic body of the joint is awake, mechanical_world.rs:274-279) join
+// the solver manifolds after the contact manifolds; their state records
+// whether they were solved this step.
+#if !NPGPU_EXCHANGE_TU
+__global__ void k_collect_joints(World w) {
+    const Bodies& b = w.b;
+    GRID_FOR(jj, w.nj_slots) {
+        const uint32_t ji = w.j.info[jj];
+        if (!(ji & JI_ALIVE)) continue;
+        uint32_t st = w.j.state[jj] & ~JS_ACTIVE;
+        if (!(st & JS_BROKEN)) {
+            const uint32_t b1 = w.j.body[2 * jj], b2 = w.j.body[2 * jj + 1];
+            const uint32_t s1 = bi_status(b.info[b1]), s2 = bi_status(b.info[b2]);
+            const bool a1 = s1 == 2u && b.energy[b1] != 0.0f;
+            const bool a2 = s2 == 2u && b.energy[b2] != 0.0f;
+            if (a1 || a2) {
+                const uint32_t m = atomicAdd(&w.ctl->nsolver, 1u);
+                if (m >= w.cap_pairs) {
+                    atomicOr(&w.ctl->err, ERRF_PAIR_CAPACITY);
+                } else {
+                    w.s.sm_list[m] = kJointBit | jj;
+                    w.s.sm_b1[m] = s1 == 2u ? (int)b1 : -1;
+                    w.s.sm_b2[m] = s2 == 2u ? (int)b2 : -1;
+                    w.s.sm_nc[m] = (ji & JI_KIND_MASK) == NPGPU_JOINT_FIXED ? 2u : 1u;
+                    if (s1 == 2u) atomicAdd(&b.adj_count[b1], 1u);
+                    if (s2 == 2u) atomicAdd(&b.adj_count[b2], 1u);
+                    st |= JS_ACTIVE;
+                }
+            }
+        }
+        w.j.state[jj] = st;
+    }
+}
+
+// The solver manifold count stays within the solver arrays after an overflow
+// (reported as a capacity error).
+__global__ void k_clamp_solver(World w) {
+    if (w.ctl->nsolver > w.cap_pairs) w.ctl->nsolver = w.cap_pairs;
+}
+#endif
+
 #if !NPGPU_EXCHANGE_TU
 __global__ void k_adj_fill(World w) {
     const uint32_t ms = w.ctl->nsolver;
@@ -730,8 +846,17 @@ __global__ void k_adj_fill(World w) {
 }
 #endif
 
+// A joint's priority hashes its world-local slot with a second input no
+// collider pair has, and keeps the joint slot under a collider field no
+// collider slot reaches, so that it never equals a pair's.
+__device__ __forceinline__ unsigned long long joint_priority(uint32_t local, uint32_t j) {
+    return ((unsigned long long)pair_hash22(local, 0x3fffffu) << 42) | (0x1fffffull << 21) | (unsigned long long)j;
+}
+
 __device__ __forceinline__ unsigned long long sm_priority(const World& w, uint32_t m) {
-    uint2 pr = w.cur.pair[w.s.sm_list[m]];
+    const uint32_t q = w.s.sm_list[m];
+    if (q & kJointBit) return joint_priority(w.j.local[q & ~kJointBit], q & ~kJointBit);
+    uint2 pr = w.cur.pair[q];
     return pair_priority(w.c.local[pr.x], w.c.local[pr.y], pr.x, pr.y);
 }
 
@@ -839,9 +964,69 @@ __global__ void __launch_bounds__(kCoopThreads) k_colour(World w) {
 #endif
 
 // ================================================================ assembly
+// A point given in a body's frame, in world space: Isometry * Point
+// (world_point_at_material_point, rigid_body.rs:641-643).
+__device__ __forceinline__ np::V body_point(np::V t, np::Q q, np::V local) {
+    return np::add(np::qrot(q, local), t);
+}
+
 // `rows`: also store each contact's three rows in full, for the one-grid
 // schedule's iterations.
 #if !NPGPU_EXCHANGE_TU
+
+// The rows of active joint j as solver manifold m: BallConstraint /
+// FixedConstraint::velocity_constraints (ball_constraint.rs:80-127,
+// fixed_constraint.rs:107-172) through helper::cancel_relative_linear_velocity
+// and cancel_relative_angular_velocity (helper.rs:167-296, 422-551): one row
+// per axis e_x, e_y, e_z, each with the joint's cached impulse as its start
+// (no warm-start coefficient). The linear triple is record 0, the angular
+// triple (FixedConstraint) record 1.
+static __device__ void assemble_joint(const World& w, const StepParams& p, uint32_t m, uint32_t j, int b1, int b2, bool rows) {
+    const Bodies& b = w.b;
+    const uint32_t bb1 = w.j.body[2 * j], bb2 = w.j.body[2 * j + 1];
+    const BodyView v1 = load_view(b, bb1), v2 = load_view(b, bb2);
+    uint32_t mask = 0;
+    if (b1 >= 0) mask |= ~(bi_flags(v1.info) >> 1) & 0x3fu;
+    if (b2 >= 0) mask |= (~(bi_flags(v2.info) >> 1) & 0x3fu) << 8;
+    w.s.sm_mask[m] = mask;
+    const uint32_t nc = w.s.sm_nc[m];
+    const np::V a1 = body_point(v3(b.pos_t[bb1]), q4(b.pos_q[bb1]), v3(w.j.anchor[2 * j]));
+    const np::V a2 = body_point(v3(b.pos_t[bb2]), q4(b.pos_q[bb2]), v3(w.j.anchor[2 * j + 1]));
+    float4* pr4 = w.s.pos_rec + (size_t)m * kPosRec;
+    pr4[4] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kJointBit | j));
+    pr4[6] = make_float4(__uint_as_float(bb1), __uint_as_float(bb2), __uint_as_float(v1.info), __uint_as_float(v2.info));
+    float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+    float4* lam = w.s.lam + (size_t)m * kMaxContacts;
+    for (uint32_t k = 0; k < nc; ++k) {
+        const bool ang = k == 1u;
+        float R[3][kRowFloats];
+#pragma unroll
+        for (int r = 0; r < 3; ++r) {
+            if (ang) make_row_angular(R[r], v1, v2, basis_axis(r), p.dt);
+            else make_row(R[r], v1, v2, a1, a2, basis_axis(r), p.dt);
+        }
+        const np::V zero = np::mk(0.0f, 0.0f, 0.0f);
+        const np::V pos1 = ang ? zero : np::sub(a1, v1.com), pos2 = ang ? zero : np::sub(a2, v2.com);
+        const float kindf = ang ? kJointAngular : kJointLinear;
+        con[4 * k] = make_float4(0.0f, 0.0f, 0.0f, kindf);
+        con[4 * k + 1] = make_float4(pos1.x, pos1.y, pos1.z, R[0][RF_R]);
+        con[4 * k + 2] = make_float4(pos2.x, pos2.y, pos2.z, R[0][RF_RHS]);
+        con[4 * k + 3] = make_float4(R[1][RF_R], R[1][RF_RHS], R[2][RF_R], R[2][RF_RHS]);
+        if (rows) {
+            float4* ro = w.s.rows + ((size_t)m * kMaxContacts + k) * kRowsF4;
+#pragma unroll
+            for (int r = 0; r < 3; ++r) {
+#pragma unroll
+                for (int e = 0; e < 6; ++e)
+                    ro[kRowF4 * r + e] = make_float4(R[r][4 * e], R[r][4 * e + 1], R[r][4 * e + 2], R[r][4 * e + 3]);
+                ro[kRowF4 * r + 6] = make_float4(R[r][RF_R], R[r][RF_RHS], kindf, 0.0f);
+            }
+        }
+        const float4 im = w.j.imp[2 * j + k];
+        lam[k] = make_float4(im.x, im.y, im.z, 0.0f);
+    }
+}
+
 __global__ void k_assemble(World w, StepParams p, bool rows) {
     const uint32_t ms = w.ctl->nsolver;
     const Bodies& b = w.b;
@@ -849,10 +1034,6 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
     const float dt = p.dt;
     GRID_FOR(m, ms) {
         uint32_t q = w.s.sm_list[m];
-        uint2 pr = w.cur.pair[q];
-        uint32_t c1 = pr.x, c2 = pr.y;
-        uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
-        BodyView v1 = load_view(b, bb1), v2 = load_view(b, bb2);
         int b1 = w.s.sm_b1[m], b2 = w.s.sm_b2[m];
         // Colour rank and manifold count on each dynamic body.
         uint32_t col = w.s.sm_colour[m];
@@ -873,6 +1054,14 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
                   ((uint32_t)(__popcll(ua) + __popcll(ub)) << 24);
         }
         w.s.sm_rk[m] = rk;
+        if (q & kJointBit) {
+            assemble_joint(w, p, m, q & ~kJointBit, b1, b2, rows);
+            continue;
+        }
+        uint2 pr = w.cur.pair[q];
+        uint32_t c1 = pr.x, c2 = pr.y;
+        uint32_t bb1 = c.body[c1], bb2 = c.body[c2];
+        BodyView v1 = load_view(b, bb1), v2 = load_view(b, bb2);
         uint32_t nc = w.s.sm_nc[m];
         uint32_t ci1 = c.info[c1], ci2 = c.info[c2];
         float mu = combine(c.friction[c1], (ci1 >> 4) & 0xfu, c.friction[c2], (ci2 >> 4) & 0xfu);
@@ -1135,10 +1324,32 @@ __device__ __forceinline__ void warm_rows(const RS& src, uint32_t nc, bool h1, b
 
 // The friction rows (sor_prox.rs:232-343) and the normal rows
 // (sor_prox.rs:181-230) of one task's contacts, from stored rows.
+// A joint's three bilateral rows from stored rows (Independent limits of
+// +-FLT_MAX, helper.rs:186-189).
+template <class RS>
+__device__ __forceinline__ void joint_rows(const RS& src, uint32_t k, float4 l, bool h1, bool h2, DV& dv) {
+    float li[3] = {l.x, l.y, l.z};
+#pragma unroll 1
+    for (int r = 0; r < 3; ++r) {
+        const RowRec R = src.row(k, r);
+        float ni = li[r] - R.r * (row_dot(R, dv, h1, h2) + R.rhs);
+        ni = ni < -FLT_MAX ? -FLT_MAX : (ni > FLT_MAX ? FLT_MAX : ni);
+        const float dl = ni - li[r];
+        li[r] = ni;
+        row_axpy(R, dv, dl, h1, h2);
+    }
+    src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
+}
+
 template <class RS>
 __device__ __forceinline__ void friction_rows(const RS& src, uint32_t nc, bool h1, bool h2, DV& dv) {
     for (uint32_t k = 0; k < nc; ++k) {
         const float4 l = src.get_lam(k);
+        const RowRec R1 = src.row(k, 1);
+        if (R1.mu < 0.0f) {
+            joint_rows(src, k, l, h1, h2, dv);
+            continue;
+        }
         const float li = l.x;
         float imps[2] = {l.y, l.z};
 #pragma unroll
@@ -1146,12 +1357,12 @@ __device__ __forceinline__ void friction_rows(const RS& src, uint32_t nc, bool h
             const float imp = imps[sdir];
             if (li == 0.0f) {
                 if (imp != 0.0f) {
-                    row_axpy(src.row(k, 1 + sdir), dv, -imp, h1, h2);
+                    row_axpy(sdir == 0 ? R1 : src.row(k, 2), dv, -imp, h1, h2);
                     imps[sdir] = 0.0f;
                 }
                 continue;
             }
-            const RowRec R = src.row(k, 1 + sdir);
+            const RowRec R = sdir == 0 ? R1 : src.row(k, 2);
             float mx = R.mu * li, mn = -mx;
             float dimp = row_dot(R, dv, h1, h2) + R.rhs;
             float ni = imp - R.r * dimp;
@@ -1169,6 +1380,7 @@ __device__ __forceinline__ void normal_rows(const RS& src, uint32_t nc, bool h1,
     for (uint32_t k = 0; k < nc; ++k) {
         const float4 l = src.get_lam(k);
         const RowRec R = src.row(k, 0);
+        if (R.mu < 0.0f) continue;   // a joint's rows run with the friction rows
         float imp = l.x;
         float dimp = row_dot(R, dv, h1, h2) + R.rhs;
         float ni = imp - R.r * dimp;
@@ -1197,6 +1409,37 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = src.rec(k);
         float4 l = src.get_lam(k);
+        if (c.mu < 0.0f) {
+            // A joint's three bilateral rows (sor_prox.rs:232-293 with
+            // Independent limits): warm-started, then solved once per
+            // iteration with the friction rows.
+            if (kind == SWEEP_NORMAL) continue;
+            const bool ang = c.mu == kJointAngular;
+            float li[3] = {l.x, l.y, l.z};
+#pragma unroll 1
+            for (int r = 0; r < 3; ++r) {
+                float J1[6], J2[6];
+                if (h1) joint_side_j(ang, r, c.pos1, false, mask & 0x3fu, J1);
+                if (h2) joint_side_j(ang, r, c.pos2, true, (mask >> 8) & 0x3fu, J2);
+                float dl = li[r];
+                if (kind == SWEEP_WARM) {
+                    if (li[r] == 0.0f) continue;
+                } else {
+                    float d = 0.0f;
+                    if (h1 && h2) d = side_dot_j(J1, dv.a) + side_dot_j(J2, dv.b);
+                    else if (h1) d = side_dot_j(J1, dv.a);
+                    else if (h2) d = side_dot_j(J2, dv.b);
+                    float ni = li[r] - c.r[r] * (d + c.rhs[r]);
+                    ni = ni < -FLT_MAX ? -FLT_MAX : (ni > FLT_MAX ? FLT_MAX : ni);
+                    dl = ni - li[r];
+                    li[r] = ni;
+                }
+                if (h1) side_axpy_j(J1, bm.get(0), dl, dv.a);
+                if (h2) side_axpy_j(J2, bm.get(1), dl, dv.b);
+            }
+            if (kind != SWEEP_WARM) src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
+            continue;
+        }
         if (kind == SWEEP_WARM) {
             np::V t[2];
             src.tangents(c, k, t);
@@ -1371,6 +1614,18 @@ __device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, in
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = load_con(con, k);
         float4 l = lam[k];
+        if (c.mu < 0.0f) {
+            // A joint's three bilateral rows.
+            const bool ang = c.mu == kJointAngular;
+            const float li[3] = {l.x, l.y, l.z};
+            for (int r = 0; r < 3; ++r) {
+                float J1[6], J2[6];
+                if (h1) joint_side_j(ang, r, c.pos1, false, mask & 0x3fu, J1);
+                if (h2) joint_side_j(ang, r, c.pos2, true, (mask >> 8) & 0x3fu, J2);
+                residual_row_j(J1, J2, c.r[r], c.rhs[r], li[r], dv, h1, h2, RES_BILATERAL, 0.0f, 0.0f, acc);
+            }
+            continue;
+        }
         const float4 ta = w.s.tan[((size_t)m * kMaxContacts + k) * 2], tb = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
         const np::V t[2] = {np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
         residual_row(np::neg(c.n), c.pos1, c.pos2, mask, c.r[0], c.rhs[0], l.x, dv, h1, h2, false, 0.0f, c.mu, acc);
@@ -1910,6 +2165,28 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
     GRID_FOR(m, ms) {
         uint32_t q = w.s.sm_list[m];
         uint32_t nc = w.s.sm_nc[m];
+        if (q & kJointBit) {
+            // JointConstraint::cache_impulses (ball_constraint.rs:129-141,
+            // fixed_constraint.rs:174-199): the impulses, and the joint breaks
+            // when |impulse|^2 / dt^2 exceeds the squared break force / torque.
+            const uint32_t j = q & ~kJointBit;
+            const float4 li = w.s.lam[(size_t)m * kMaxContacts];
+            w.j.imp[2 * j] = make_float4(li.x, li.y, li.z, 0.0f);
+            const float n2 = 0.0f + li.x * li.x + li.y * li.y + li.z * li.z;
+            const float2 brk = w.j.brk[j];
+            bool broken;
+            if (nc == 2u) {
+                const float4 la = w.s.lam[(size_t)m * kMaxContacts + 1];
+                w.j.imp[2 * j + 1] = make_float4(la.x, la.y, la.z, 0.0f);
+                const float a2 = 0.0f + la.x * la.x + la.y * la.y + la.z * la.z;
+                const float inv_dt2 = p.inv_dt * p.inv_dt;
+                broken = n2 * inv_dt2 > brk.x || a2 * inv_dt2 > brk.y;
+            } else {
+                broken = n2 * p.inv_dt * p.inv_dt > brk.x;
+            }
+            if (broken) w.j.state[j] |= JS_BROKEN;
+            continue;
+        }
         for (uint32_t k = 0; k < nc; ++k) {
             float4 l = w.s.lam[(size_t)m * kMaxContacts + k];
             if (w.s.feat != nullptr) {
@@ -1956,14 +2233,124 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
 //   0 (wrt1.t, dil1)  1 wrt1.q  2 (wrt2.t, dil2)  3 wrt2.q
 //   4 (half extents 1, shape1 | nc << 8)  5 (half extents 2, shape2)
 //   6 (body1, body2, info1, info2)  7..10 per contact (normal in body 1's frame, feature key)
+// NonlinearSORProx::solve_generic (nonlinear_sor_prox.rs:78-117) of one
+// position row whose sides J1/W1, J2/W2 and 1/r were formed by
+// constraint_pair_geometry: clamp_rhs (nonlinear_sor_prox.rs:297-309), then
+// each side with dofs moves by its W times -rhs r.
+__device__ __forceinline__ void generic_position_row(const StepParams& p, float depth, bool angular, float inv_r, bool d1,
+                                                     bool d2, float* W1, float* W2, np::V& t1, np::Q& q1, np::V& com1,
+                                                     np::V lc1, np::V& t2, np::Q& q2, np::V& com2, np::V lc2,
+                                                     bool& moved1, bool& moved2) {
+    float rhs = -depth;
+    if (angular) {
+        rhs = (rhs + p.allowed_angular_error) * p.erp;
+        rhs = rhs < -p.max_angular_correction ? -p.max_angular_correction : rhs;
+    } else {
+        rhs = (rhs + p.allowed_linear_error) * p.erp;
+        rhs = rhs < -p.max_linear_correction ? -p.max_linear_correction : rhs;
+    }
+    if (!(rhs < 0.0f)) return;
+    const float r = inv_r != 0.0f ? 1.0f / inv_r : 1.0f;
+    const float impulse = -rhs * r;
+    if (d1) {
+        for (int k = 0; k < 6; ++k) W1[k] = W1[k] * impulse;
+        apply_displacement(t1, q1, com1, lc1, np::mk(W1[0], W1[1], W1[2]), np::mk(W1[3], W1[4], W1[5]));
+        moved1 = true;
+    }
+    if (d2) {
+        for (int k = 0; k < 6; ++k) W2[k] = W2[k] * impulse;
+        apply_displacement(t2, q2, com2, lc2, np::mk(W2[0], W2[1], W2[2]), np::mk(W2[3], W2[4], W2[5]));
+        moved2 = true;
+    }
+}
+
+// The position constraints of joint j on the poses P1, P2
+// (NonlinearSORProx::solve_generator, nonlinear_sor_prox.rs:57-76):
+// FixedConstraint::position_constraint (fixed_constraint.rs:207-249) first
+// cancels the relative rotation of the two frames (helper::cancel_relative_
+// rotation, helper.rs:553-611), then, with the poses it left, both kinds
+// cancel the anchors' separation (helper::cancel_relative_translation,
+// helper.rs:364-418). Each is skipped below the allowed error
+// (Unit::try_new_and_get).
+__device__ __forceinline__ void joint_position(const World& w, const StepParams& p, uint32_t j, uint32_t bb1, uint32_t bb2,
+                                               uint32_t i1, uint32_t i2, Pose& P1, Pose& P2, bool& moved1,
+                                               bool& moved2) {
+    const Bodies& b = w.b;
+    const bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
+    np::V t1 = P1.t, t2 = P2.t;
+    np::Q q1 = P1.q, q2 = P2.q;
+    np::V com1 = P1.com, com2 = P2.com;
+    np::V lc1 = np::mk(0.0f, 0.0f, 0.0f), lc2 = lc1;
+    BodyView v1, v2;
+    v1.lin = v1.ang = v1.acc_lin = v1.acc_ang = lc1;
+    v2.lin = v2.ang = v2.acc_lin = v2.acc_ang = lc1;
+    v1.inv_mass = v2.inv_mass = 0.0f;
+    v1.info = i1;
+    v2.info = i2;
+    if (d1) {
+        lc1 = v3(__ldg(b.local_com + bb1));
+        const SB s = load_sb(b.sb, (int)bb1);
+        v1.inv_mass = s.im;
+        v1.inv_I = s.I;
+    }
+    if (d2) {
+        lc2 = v3(__ldg(b.local_com + bb2));
+        const SB s = load_sb(b.sb, (int)bb2);
+        v2.inv_mass = s.im;
+        v2.inv_I = s.I;
+    }
+    const np::V la1 = v3(w.j.anchor[2 * j]), la2 = v3(w.j.anchor[2 * j + 1]);
+    moved1 = moved2 = false;
+    float J1[6], J2[6], W1[6], W2[6];
+    if ((w.j.info[j] & JI_KIND_MASK) == NPGPU_JOINT_FIXED) {
+        const np::Q r1 = np::qmul(q1, q4(w.j.frame[2 * j])), r2 = np::qmul(q2, q4(w.j.frame[2 * j + 1]));
+        const np::V err = np::qscaled_axis(np::qmul(r2, np::qconj(r1)));
+        const float sq = np::dot(err, err);
+        if (sq > p.allowed_angular_error * p.allowed_angular_error) {
+            const float depth = sqrtf(sq);
+            const np::V dir = np::divs(err, depth);
+            float inv_r = 0.0f, dummy = 0.0f;
+            v1.com = com1;
+            v2.com = com2;
+            if (d1) fill_torque_side(v1, dir, J1, W1, inv_r, dummy, false, p.dt);
+            if (d2) fill_torque_side(v2, np::neg(dir), J2, W2, inv_r, dummy, false, p.dt);
+            generic_position_row(p, depth, true, inv_r, d1, d2, W1, W2, t1, q1, com1, lc1, t2, q2, com2, lc2, moved1,
+                                 moved2);
+        }
+    }
+    {
+        const np::V a1 = body_point(t1, q1, la1), a2 = body_point(t2, q2, la2);
+        const np::V err = np::sub(a2, a1);
+        const float sq = np::dot(err, err);
+        if (sq > p.allowed_linear_error * p.allowed_linear_error) {
+            const float depth = sqrtf(sq);
+            const np::V dir = np::divs(err, depth);
+            float inv_r = 0.0f, dummy = 0.0f;
+            v1.com = com1;
+            v2.com = com2;
+            if (d1) fill_row_side(v1, a1, dir, J1, W1, inv_r, dummy, false, p.dt);
+            if (d2) fill_row_side(v2, a2, np::neg(dir), J2, W2, inv_r, dummy, false, p.dt);
+            generic_position_row(p, depth, false, inv_r, d1, d2, W1, W2, t1, q1, com1, lc1, t2, q2, com2, lc2, moved1,
+                                 moved2);
+        }
+    }
+    P1.t = t1; P1.q = q1; P1.com = com1;
+    P2.t = t2; P2.q = q2; P2.com = com2;
+}
+
 __device__ __forceinline__ void position_core(const World& w, const StepParams& p, uint32_t m, Pose& P1, Pose& P2,
                                               bool& moved1, bool& moved2) {
     const Bodies& b = w.b;
     const float4* rec = w.s.pos_rec + (size_t)m * kPosRec;
-    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2), r3 = __ldg(rec + 3);
-    const float4 r4 = __ldg(rec + 4), r5 = __ldg(rec + 5), r6 = __ldg(rec + 6);
+    const float4 r4 = __ldg(rec + 4), r6 = __ldg(rec + 6);
     const uint32_t bb1 = __float_as_uint(r6.x), bb2 = __float_as_uint(r6.y);
     const uint32_t i1 = __float_as_uint(r6.z), i2 = __float_as_uint(r6.w);
+    if (__float_as_uint(r4.w) & kJointBit) {
+        joint_position(w, p, __float_as_uint(r4.w) & ~kJointBit, bb1, bb2, i1, i2, P1, P2, moved1, moved2);
+        return;
+    }
+    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2), r3 = __ldg(rec + 3);
+    const float4 r5 = __ldg(rec + 5);
     bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
     np::V t1 = P1.t, t2 = P2.t;
     np::Q q1 = P1.q, q2 = P2.q;
@@ -2352,6 +2739,10 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     if (e != cudaSuccess) return e;
     rec(1);
     k_collect<<<npb, kItemThreads, 0, st>>>(wc);
+    if (w.nj_slots) {
+        k_collect_joints<<<item_blocks(w.nj_slots), kItemThreads, 0, st>>>(wc);
+        k_clamp_solver<<<1, 1, 0, st>>>(wc);
+    }
     size_t scan_bytes = L.scan_bytes;
     e = exclusive_scan(L.scan_temp, scan_bytes, w.b.adj_count, w.b.adj_start,
                                    w.nb_slots ? w.nb_slots : 1u, st);

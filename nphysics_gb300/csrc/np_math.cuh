@@ -87,6 +87,19 @@ NP_HD Q qexp(V axisangle) {
     return Q{v.x, v.y, v.z, c};
 }
 
+// UnitQuaternion::scaled_axis: the axis (the vector part, negated when
+// w < 0, normalised; zero when it vanishes) times the angle 2 acos(|w|)
+// (0 when |w| >= 1). acos is taken in double and rounded to f32.
+NP_HD V qscaled_axis(Q q) {
+    V v = q.w >= 0.0f ? qv(q) : neg(qv(q));
+    float sq = dot(v, v);
+    if (!(sq > 0.0f)) return V{0.0f, 0.0f, 0.0f};
+    V axis = divs(v, sqrtf(sq));
+    float aw = fabsf(q.w);
+    float angle = aw >= 1.0f ? 0.0f : (float)acos((double)aw) * 2.0f;
+    return mul(axis, angle);
+}
+
 struct M {
     float m[3][3];
 };

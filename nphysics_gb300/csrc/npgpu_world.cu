@@ -37,6 +37,12 @@ struct HostCollider {
     npgpu_collider_desc desc;
 };
 
+struct HostJoint {
+    bool alive = false;
+    uint64_t gen = 0;
+    npgpu_joint_desc desc;
+};
+
 bool finite_n(const float* v, int n) {
     for (int k = 0; k < n; ++k)
         if (!std::isfinite(v[k])) return false;
@@ -192,6 +198,12 @@ struct npgpu_world {
     bool graphs_broken = false;          // capture failed once: run eagerly from then on
     bool last_step_graphed = false;
     int grid_world = 0;
+    // Joint constraints: the host mirror of the set, and device arrays grown
+    // on demand (Joints, cap_j slots).
+    std::vector<HostJoint> hj;
+    uint32_t nj_slots = 0, nj_alive = 0, cap_j = 0;
+    bool joints_local_dirty = false;     // the joints' world-local slots (Joints::local) need recomputing
+    std::vector<uint32_t> h_jlocal;
 };
 
 // The message of the last failure without a world (npgpu_create, the
@@ -250,6 +262,8 @@ static StepParams step_params(const npgpu_world* w) {
     s.warmstart_mode = p.warmstart_mode;
     s.sweep_order = p.sweep_order;
     s.profile = p.profile;
+    s.allowed_angular_error = p.allowed_angular_error;
+    s.max_angular_correction = p.max_angular_correction;
     return s;
 }
 
@@ -271,6 +285,9 @@ static npgpu_status stage_reserve(npgpu_world* w, size_t bytes, void** hptr) {
         if (w->d_stage) cudaFree(w->d_stage);
     if (w->d_query) cudaFree(w->d_query);
     if (w->dw.events) cudaFree(w->dw.events);
+    for (void* p : {(void*)w->dw.j.info, (void*)w->dw.j.state, (void*)w->dw.j.body, (void*)w->dw.j.local,
+                    (void*)w->dw.j.anchor, (void*)w->dw.j.frame, (void*)w->dw.j.imp, (void*)w->dw.j.brk})
+        cudaFree(p);
         w->d_stage = nullptr;
         size_t nb = std::max(bytes, w->d_stage_bytes * 2);
         CK(cudaMalloc(&w->d_stage, nb), "device staging");
@@ -322,6 +339,7 @@ static void sync_world_view(npgpu_world* w) {
     w->dw.nb_slots = w->nb_slots;
     w->dw.nc_slots = w->nc_slots;
     w->dw.nc_alive = w->nc_alive;
+    w->dw.nj_slots = w->nj_alive ? w->nj_slots : 0u;
     uint32_t wb = 0;
     while (wb < 16 && (w->max_world >> wb) != 0u) ++wb;
     w->dw.world_bits = wb;
@@ -827,6 +845,203 @@ static npgpu_status kill_slots(npgpu_world* w, const std::vector<uint32_t>& slot
     return NPGPU_OK;
 }
 
+// Body::activate of an alive body at the next step, keeping its mass state
+// (the update carries it whole).
+static void wake_body(npgpu_world* w, uint64_t slot) {
+    if (slot >= w->cap_b || !w->hb[slot].alive) return;
+    const HostBody& b = w->hb[slot];
+    MassUpdate u;
+    std::memset(&u, 0, sizeof(u));
+    u.slot = (uint32_t)slot;
+    u.activate = 2u;
+    u.mass = b.mass;
+    for (int r = 0; r < 3; ++r)
+        for (int cc = 0; cc < 3; ++cc) u.local_I[3 * r + cc] = b.local_I.m[r][cc];
+    u.local_com[0] = b.local_com.x;
+    u.local_com[1] = b.local_com.y;
+    u.local_com[2] = b.local_com.z;
+    w->pending_mass.push_back(u);
+}
+
+// Device joint arrays for at least `need` slots; existing joints keep their
+// description, impulses and state.
+static npgpu_status ensure_joint_capacity(npgpu_world* w, uint32_t need) {
+    if (need <= w->cap_j) return NPGPU_OK;
+    uint32_t cap = std::max<uint32_t>(need, std::max<uint32_t>(64u, 2u * w->cap_j));
+    Joints nj{};
+    std::vector<void*> fresh;
+    bool ok = true;
+#define JA(ptr, n)                                                                                        \
+    if (ok) {                                                                                             \
+        void* p_ = nullptr;                                                                               \
+        ok = cudaMalloc(&p_, std::max<size_t>((size_t)(n) * sizeof(*(ptr)), 16)) == cudaSuccess;          \
+        if (ok) {                                                                                         \
+            (ptr) = (decltype(ptr))p_;                                                                    \
+            fresh.push_back(p_);                                                                          \
+        }                                                                                                 \
+    }
+    JA(nj.info, cap) JA(nj.state, cap) JA(nj.body, 2 * (size_t)cap) JA(nj.local, cap)
+    JA(nj.anchor, 2 * (size_t)cap) JA(nj.frame, 2 * (size_t)cap) JA(nj.imp, 2 * (size_t)cap) JA(nj.brk, cap)
+#undef JA
+    if (!ok) {
+        for (void* p : fresh) cudaFree(p);
+        cudaGetLastError();
+        return fail(w, NPGPU_ERR_CUDA, "joint arrays: cudaMalloc failed");
+    }
+    CK(cudaMemsetAsync(nj.info, 0, sizeof(uint32_t) * cap, w->stream), "joint arrays");
+    CK(cudaMemsetAsync(nj.state, 0, sizeof(uint32_t) * cap, w->stream), "joint arrays");
+    CK(cudaMemsetAsync(nj.imp, 0, sizeof(float4) * 2 * (size_t)cap, w->stream), "joint arrays");
+    const Joints& oj = w->dw.j;
+    const size_t n = w->cap_j;
+    if (n) {
+        CK(cudaMemcpyAsync(nj.info, oj.info, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.state, oj.state, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.body, oj.body, sizeof(uint32_t) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.local, oj.local, sizeof(uint32_t) * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.anchor, oj.anchor, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.frame, oj.frame, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.imp, oj.imp, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.brk, oj.brk, sizeof(float2) * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+    }
+    CK(cudaStreamSynchronize(w->stream), "joint arrays");
+    for (void* p : {(void*)oj.info, (void*)oj.state, (void*)oj.body, (void*)oj.local, (void*)oj.anchor, (void*)oj.frame,
+                    (void*)oj.imp, (void*)oj.brk})
+        cudaFree(p);
+    w->dw.j = nj;
+    w->cap_j = cap;
+    w->hj.resize(cap);
+    return NPGPU_OK;
+}
+
+static npgpu_status upload_joints(npgpu_world* w, const std::vector<JointUpload>& up) {
+    if (up.empty()) return NPGPU_OK;
+    void* dp = nullptr;
+    npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(JointUpload), &dp);
+    if (st != NPGPU_OK) return st;
+    CK(launch_upload_joints(w->dw, (const JointUpload*)dp, (uint32_t)up.size(), w->stream), "upload joints");
+    CK(cudaEventRecord(w->ev_stage, w->stream), "staging event");
+    return NPGPU_OK;
+}
+
+// Removes the joints in `slots` (alive), waking their bodies.
+static npgpu_status drop_joints(npgpu_world* w, const std::vector<uint32_t>& slots) {
+    std::vector<JointUpload> up;
+    for (uint32_t j : slots) {
+        HostJoint& hj = w->hj[j];
+        hj.alive = false;
+        w->nj_alive -= 1;
+        wake_body(w, hj.desc.body1.index);
+        wake_body(w, hj.desc.body2.index);
+        JointUpload u;
+        std::memset(&u, 0, sizeof(u));
+        u.slot = j;
+        u.reset = 1u;
+        up.push_back(u);
+    }
+    w->joints_local_dirty = true;
+    sync_world_view(w);
+    return upload_joints(w, up);
+}
+
+npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
+                                 const npgpu_joint_desc* descs) {
+    if (!w || (n && (!handles || !descs))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    for (uint32_t k = 0; k < n; ++k) {
+        const npgpu_joint_desc& d = descs[k];
+        if (handles[k].index >= (1u << 21) - 1u)
+            return fail(w, NPGPU_ERR_CAPACITY, "joint index must be below 2^21 - 1");
+        if (d.kind != NPGPU_JOINT_BALL && d.kind != NPGPU_JOINT_FIXED)
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind (ball and fixed joints are supported)");
+        if (!body_handle_ok(w, d.body1) || !body_handle_ok(w, d.body2))
+            return fail(w, NPGPU_ERR_INVALID_HANDLE, "joint body handle is invalid");
+        if (d.body1.index == d.body2.index)
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "a joint needs two different bodies");
+        if (w->hb[d.body1.index].world != w->hb[d.body2.index].world)
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "a joint's bodies must belong to the same world");
+        if (!finite_n(d.anchor1, 3) || !finite_n(d.anchor2, 3) || !finite_n(d.frame1, 4) || !finite_n(d.frame2, 4) ||
+            std::isnan(d.break_force) || std::isnan(d.break_torque))
+            return fail(w, NPGPU_ERR_NAN, "joint description has a non-finite value");
+    }
+    uint32_t need = 0;
+    for (uint32_t k = 0; k < n; ++k) need = std::max<uint32_t>(need, (uint32_t)handles[k].index + 1u);
+    npgpu_status st = ensure_joint_capacity(w, need);
+    if (st != NPGPU_OK) return st;
+    std::vector<JointUpload> up;
+    up.reserve(n);
+    for (uint32_t k = 0; k < n; ++k) {
+        const npgpu_joint_desc& d = descs[k];
+        const uint32_t slot = (uint32_t)handles[k].index;
+        HostJoint& hj = w->hj[slot];
+        if (hj.alive) {
+            wake_body(w, hj.desc.body1.index);
+            wake_body(w, hj.desc.body2.index);
+        } else {
+            w->nj_alive += 1;
+        }
+        hj.alive = true;
+        hj.gen = handles[k].generation;
+        hj.desc = d;
+        wake_body(w, d.body1.index);
+        wake_body(w, d.body2.index);
+        JointUpload u;
+        std::memset(&u, 0, sizeof(u));
+        u.slot = slot;
+        u.info = d.kind | JI_ALIVE;
+        u.body1 = (uint32_t)d.body1.index;
+        u.body2 = (uint32_t)d.body2.index;
+        u.reset = 1u;
+        std::memcpy(u.anchor1, d.anchor1, sizeof(u.anchor1));
+        std::memcpy(u.anchor2, d.anchor2, sizeof(u.anchor2));
+        std::memcpy(u.frame1, d.frame1, sizeof(u.frame1));
+        std::memcpy(u.frame2, d.frame2, sizeof(u.frame2));
+        // set_break_force / set_break_torque keep the squares (f32).
+        u.brk_force2 = d.break_force * d.break_force;
+        u.brk_torque2 = d.break_torque * d.break_torque;
+        w->nj_slots = std::max(w->nj_slots, slot + 1u);
+        up.push_back(u);
+    }
+    if (up.empty()) return NPGPU_OK;
+    w->joints_local_dirty = true;
+    sync_world_view(w);
+    return upload_joints(w, up);
+}
+
+static bool joint_handle_ok(const npgpu_world* w, const npgpu_handle& h) {
+    return h.index < w->cap_j && w->hj[h.index].alive && w->hj[h.index].gen == h.generation;
+}
+
+npgpu_status npgpu_remove_joints(npgpu_world* w, uint32_t n, const npgpu_handle* handles) {
+    if (!w || (n && !handles)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    for (uint32_t k = 0; k < n; ++k)
+        if (!joint_handle_ok(w, handles[k])) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid joint handle");
+    std::vector<uint32_t> slots;
+    for (uint32_t k = 0; k < n; ++k) slots.push_back((uint32_t)handles[k].index);
+    std::sort(slots.begin(), slots.end());
+    slots.erase(std::unique(slots.begin(), slots.end()), slots.end());
+    return drop_joints(w, slots);
+}
+
+npgpu_status npgpu_get_joints(npgpu_world* w, uint32_t n, const npgpu_handle* handles, npgpu_joint_state* out) {
+    if (!w || (n && (!handles || !out))) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    for (uint32_t k = 0; k < n; ++k)
+        if (!joint_handle_ok(w, handles[k])) return fail(w, NPGPU_ERR_INVALID_HANDLE, "invalid joint handle");
+    if (n == 0) return NPGPU_OK;
+    CK(cudaStreamSynchronize(w->stream), "get joints");
+    std::vector<float4> imp(2 * (size_t)w->nj_slots);
+    std::vector<uint32_t> state(w->nj_slots);
+    CK(cudaMemcpy(imp.data(), w->dw.j.imp, sizeof(float4) * imp.size(), cudaMemcpyDeviceToHost), "get joints");
+    CK(cudaMemcpy(state.data(), w->dw.j.state, sizeof(uint32_t) * state.size(), cudaMemcpyDeviceToHost), "get joints");
+    for (uint32_t k = 0; k < n; ++k) {
+        const size_t j = handles[k].index;
+        const float4 a = imp[2 * j], b = imp[2 * j + 1];
+        const float v[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
+        std::memcpy(out[k].impulses, v, sizeof(v));
+        out[k].broken = (state[j] & JS_BROKEN) ? 1u : 0u;
+        out[k].active = (state[j] & JS_ACTIVE) ? 1u : 0u;
+    }
+    return NPGPU_OK;
+}
+
 npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_handle* handles) {
     if (!w || (n && !handles)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
     for (uint32_t k = 0; k < n; ++k) {
@@ -868,6 +1083,20 @@ npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
         w->hb[bi].alive = false;
         w->layout_dirty = w->local_dirty = true;
         bslots.push_back((uint32_t)bi);
+    }
+    // Joints with a removed body are removed, waking their other body
+    // (mechanical_world.rs:141-165).
+    std::vector<uint32_t> jslots;
+    for (uint32_t j = 0; j < w->nj_slots; ++j) {
+        HostJoint& hj = w->hj[j];
+        if (!hj.alive) continue;
+        const bool gone1 = !w->hb[hj.desc.body1.index].alive, gone2 = !w->hb[hj.desc.body2.index].alive;
+        if (!gone1 && !gone2) continue;
+        jslots.push_back(j);
+    }
+    if (!jslots.empty()) {
+        npgpu_status sj = drop_joints(w, jslots);
+        if (sj != NPGPU_OK) return sj;
     }
     w->forget_pending = true;
     w->cd_dirty = true;
@@ -988,6 +1217,27 @@ static npgpu_status maintain(npgpu_world* w) {
         std::fill(w->forget.begin(), w->forget.end(), 0);
         w->forget_pending = false;
     }
+    if (w->joints_local_dirty && w->nj_slots) {
+        // World-local joint slots: slot minus the smallest alive joint slot
+        // of the same world (the colouring priority of a joint hashes it).
+        std::vector<uint32_t> base((size_t)w->max_world + 1, 0xffffffffu);
+        for (uint32_t j = 0; j < w->nj_slots; ++j) {
+            const HostJoint& hj = w->hj[j];
+            if (!hj.alive) continue;
+            uint32_t wd = w->hb[hj.desc.body1.index].world;
+            if (wd < base.size()) base[wd] = std::min(base[wd], j);
+        }
+        w->h_jlocal.assign(w->nj_slots, 0u);
+        for (uint32_t j = 0; j < w->nj_slots; ++j) {
+            const HostJoint& hj = w->hj[j];
+            uint32_t wd = hj.alive ? w->hb[hj.desc.body1.index].world : 0xffffffffu;
+            w->h_jlocal[j] = (wd < base.size() && base[wd] <= j) ? j - base[wd] : j;
+        }
+        CK(cudaMemcpyAsync(w->dw.j.local, w->h_jlocal.data(), sizeof(uint32_t) * w->h_jlocal.size(),
+                           cudaMemcpyHostToDevice, w->stream), "world-local joint slots");
+        CK(cudaStreamSynchronize(w->stream), "world-local joint slots");
+        w->joints_local_dirty = false;
+    }
     if (w->local_dirty) {
         // World-local collider slots: slot minus the smallest alive collider
         // slot of the same world (the colouring priority's hash input).
@@ -1101,7 +1351,9 @@ static npgpu_status step_graphed(npgpu_world* w, const StepParams& sp) {
 
 npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, uint32_t num_force_generators) {
     if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
-    if (num_joints) return fail(w, NPGPU_ERR_NONEMPTY_JOINTS, "joint constraints are not supported");
+    if (num_joints != w->nj_alive)
+        return fail(w, NPGPU_ERR_NONEMPTY_JOINTS,
+                    "the joint set's size differs from the joints uploaded with npgpu_upsert_joints");
     if (num_force_generators) return fail(w, NPGPU_ERR_NONEMPTY_FORCES, "force generators are not supported");
     if ((w->params.warmstart_mode == 2 || w->params.warmstart_mode == 3) && !w->net_ready)
         return fail(w, NPGPU_ERR_INVALID_ARGUMENT,

@@ -110,6 +110,26 @@ struct Colliders {
 };
 enum : uint32_t { CI_ALIVE = 1u << 16 };
 
+// Joint constraints by joint slot (= the generational-arena index of the
+// host joint set). The host writes the description; the impulses and the
+// state bits are the device's.
+struct Joints {
+    uint32_t *info;                  // kind | JI_ALIVE (host-written)
+    uint32_t *state;                 // JS_BROKEN | JS_ACTIVE (device-written)
+    uint32_t *body;                  // 2 per joint: body slots
+    uint32_t *local;                 // slot minus the smallest alive joint slot of its world (colouring priority)
+    float4 *anchor;                  // 2 per joint: the anchors in their bodies' frames (xyz)
+    float4 *frame;                   // 2 per joint: the reference frames (quaternion i j k w)
+    float4 *imp;                     // 2 per joint: the impulses (linear xyz, angular xyz)
+    float2 *brk;                     // break force^2, break torque^2
+};
+enum : uint32_t { JI_KIND_MASK = 0xffu, JI_ALIVE = 1u << 8, JS_BROKEN = 1u << 0, JS_ACTIVE = 1u << 1 };
+// A solver manifold list entry of a joint: kJointBit | joint slot.
+constexpr uint32_t kJointBit = 0x80000000u;
+// The joint rows' kinds in the solver records (the friction slot, which is
+// non-negative for a contact): a linear triple (x, y, z) and an angular one.
+constexpr float kJointLinear = -1.0f, kJointAngular = -2.0f;
+
 struct Pairs {
     uint2 *pair;                     // (collider1, collider2), collider1 < collider2
     uint32_t *owner_start, *owner_count;   // by collider slot: the pairs it owns
@@ -199,6 +219,7 @@ struct StepParams {
     uint32_t warmstart_mode;
     uint32_t profile;
     uint32_t sweep_order;            // NPGPU_SWEEP_*
+    float allowed_angular_error, max_angular_correction;
 };
 
 struct MlpDev;
@@ -214,6 +235,8 @@ struct World {
     uint32_t world_bits;             // bits of the largest world index of any body so far
     uint2* events;                   // contact events (collider1, collider2 | stopped << 31), null when off
     uint32_t events_cap;
+    Joints j;
+    uint32_t nj_slots;               // joint slots in use (0: no joint kernels run)
 };
 
 // ---- launchers (defined in the kernel translation units) ----
@@ -286,6 +309,12 @@ struct ColliderUpload {
     float params[4], wrt[7];
     float margin, lin_pred, friction, restitution, rank;
 };
+struct JointUpload {                 // one joint's description (info 0: removed)
+    uint32_t slot, info, body1, body2;
+    uint32_t reset;                  // 1: the impulses and the state start from zero
+    float anchor1[3], anchor2[3], frame1[4], frame2[4];
+    float brk_force2, brk_torque2;
+};
 struct MassUpdate {                  // new local inertia / com of a body
     uint32_t slot;
     uint32_t activate;               // bit 0: inertia changed; bit 1: Body::activate (collider removal)
@@ -294,6 +323,7 @@ struct MassUpdate {                  // new local inertia / com of a body
 cudaError_t launch_upload_bodies(const World& w, const BodyUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_upload_colliders(const World& w, const ColliderUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n, cudaStream_t st);
+cudaError_t launch_upload_joints(const World& w, const JointUpload* d, uint32_t n, cudaStream_t st);
 // Poses (7 floats) and velocities (6) of slots [first, first + n) into
 // page-locked host arrays, given by their device-side addresses.
 cudaError_t launch_pack_bodies_host(const World& w, uint32_t first, uint32_t n, float* pos7, float* vel6,

@@ -16,6 +16,7 @@ from . import abi
 BODY_DTYPE = np.dtype(abi.BodyDesc)
 COLLIDER_DTYPE = np.dtype(abi.ColliderDesc)
 HANDLE_DTYPE = np.dtype(abi.Handle)
+JOINT_DTYPE = np.dtype(abi.JointDesc)
 DEFAULT_SLEEP_THRESHOLD = 0.01   # ActivationStatus::default_threshold (src/object/body.rs:72-74)
 DEFAULT_MARGIN = 0.01
 DEFAULT_LINEAR_PREDICTION = 0.001
@@ -29,6 +30,8 @@ class Scene:
         self.colliders = colliders
         self.body_handles = make_handles(len(bodies))
         self.collider_handles = make_handles(len(colliders))
+        self.joints = np.zeros(0, JOINT_DTYPE)
+        self.joint_handles = make_handles(0)
         self.gravity = tuple(float(g) for g in gravity)
         self.dt = float(dt)
         self.steps = int(steps)
@@ -42,6 +45,23 @@ class Scene:
         p = abi.default_params()
         p.dt = self.dt
         return p
+
+
+def joint_descs(n):
+    """n joint descriptions with identity frames and unbreakable limits."""
+    j = np.zeros(n, JOINT_DTYPE)
+    j["frame1"][:, 3] = 1.0
+    j["frame2"][:, 3] = 1.0
+    j["break_force"] = abi.FLT_MAX
+    j["break_torque"] = abi.FLT_MAX
+    return j
+
+
+def set_joints(scene, joints):
+    """Attaches joint descriptions (JOINT_DTYPE) to a scene, with handles 0..n-1."""
+    scene.joints = np.ascontiguousarray(joints)
+    scene.joint_handles = make_handles(len(joints))
+    return scene
 
 
 def make_handles(n, generation=0):
@@ -465,3 +485,163 @@ def random_cluster(n=64, seed=7, extent=3.0, boxes=True, balls=True, ground=True
     parts_c.append(c)
     bodies, colliders = _concat(parts_b, parts_c)
     return Scene(f"random cluster ({n})", bodies, colliders)
+
+
+def _qmul(a, b):
+    """Hamilton product of (i, j, k, w) quaternions (float64)."""
+    ai, aj, ak, aw = a
+    bi, bj, bk, bw = b
+    return np.array([aw * bi + ai * bw + aj * bk - ak * bj, aw * bj - ai * bk + aj * bw + ak * bi,
+                     aw * bk + ai * bj - aj * bi + ak * bw, aw * bw - ai * bi - aj * bj - ak * bk])
+
+
+def _qconj(q):
+    return np.array([-q[0], -q[1], -q[2], q[3]])
+
+
+def _qrot(q, v):
+    u, w = np.asarray(q[:3], np.float64), float(q[3])
+    t = 2.0 * np.cross(u, v)
+    return np.asarray(v, np.float64) + w * t + np.cross(u, t)
+
+
+def _jointed_world(rng, world, chains, links, clusters, balls, ground_half=(20.0, 1.0, 20.0)):
+    """One world of jointed bodies on its own ground (body 0 of the world):
+    `chains` chains of `links` cuboids joined end to end by ball joints, the
+    first hanging from a pivot on the ground body, laid out horizontally so
+    they swing down onto the ground; `clusters` pairs of a cuboid and a ball
+    held by a fixed joint at their midpoint (random reference frames chosen
+    so the start satisfies the joint), thrown tumbling onto the ground; and
+    `balls` free balls. Adjacent links keep a gap so their boxes do not touch."""
+    g, gc = _ground(half=ground_half, world=world)
+    bodies, colliders, joints = [g], [gc], []
+    nb = 1
+    hl, gap = 0.25, 0.05                  # link half length, gap at each joint
+    for c in range(chains):
+        pivot = np.array([rng.uniform(-6, 6), rng.uniform(3.0, 5.0), rng.uniform(-6, 6)])
+        yaw = rng.uniform(0, 2 * np.pi)
+        axis = np.array([np.cos(yaw), 0.0, np.sin(yaw)])
+        q = np.array([0.0, np.sin(-yaw / 2), 0.0, np.cos(-yaw / 2)])   # local x -> axis
+        b = body_descs(links)
+        b["world"] = world
+        for i in range(links):
+            centre = pivot + axis * (gap + hl + i * (2 * hl + 2 * gap))
+            b["position"][i, :3] = centre
+            b["position"][i, 3:7] = q
+        cl = collider_descs(links, np.arange(links) + nb, abi.SHAPE_CUBOID, (hl, 0.08, 0.08), density=2.0,
+                            friction=0.4)
+        bodies.append(b)
+        colliders.append(cl)
+        j = joint_descs(links)
+        j["kind"] = abi.JOINT_BALL
+        for i in range(links):
+            if i == 0:
+                j["body1"]["index"][i] = 0
+                j["anchor1"][i] = pivot
+            else:
+                j["body1"]["index"][i] = nb + i - 1
+                j["anchor1"][i] = (hl + gap, 0.0, 0.0)
+            j["body2"]["index"][i] = nb + i
+            j["anchor2"][i] = (-(hl + gap), 0.0, 0.0)
+        joints.append(j)
+        nb += links
+    for c in range(clusters):
+        t1 = np.array([rng.uniform(-6, 6), rng.uniform(2.0, 6.0), rng.uniform(-6, 6)])
+        q1 = uniform_quaternions(rng, 1)[0].astype(np.float64)
+        off = _qrot(q1, np.array([0.0, 0.0, 0.75]))
+        t2 = t1 + off
+        q2 = uniform_quaternions(rng, 1)[0].astype(np.float64)
+        b = body_descs(2)
+        b["world"] = world
+        b["position"][0, :3], b["position"][0, 3:7] = t1, q1
+        b["position"][1, :3], b["position"][1, 3:7] = t2, q2
+        v = rng.uniform(-2, 2, 6)
+        b["velocity"][:] = v
+        cl = collider_descs(2, np.arange(2) + nb, abi.SHAPE_CUBOID, (0.3, 0.2, 0.25), density=1.0, friction=0.5)
+        cl["shape"][1] = abi.SHAPE_BALL
+        cl["shape_params"][1] = (0.3, 0.0, 0.0)
+        bodies.append(b)
+        colliders.append(cl)
+        mid = (t1 + t2) / 2
+        f1 = uniform_quaternions(rng, 1)[0].astype(np.float64)
+        f2 = _qmul(_qmul(_qconj(q2), q1), f1)           # q2 f2 = q1 f1 at the start
+        j = joint_descs(1)
+        j["kind"] = abi.JOINT_FIXED
+        j["body1"]["index"][0], j["body2"]["index"][0] = nb, nb + 1
+        j["anchor1"][0] = _qrot(_qconj(q1), mid - t1)
+        j["anchor2"][0] = _qrot(_qconj(q2), mid - t2)
+        j["frame1"][0], j["frame2"][0] = f1, f2 / np.linalg.norm(f2)
+        joints.append(j)
+        nb += 2
+    if balls:
+        b = body_descs(balls)
+        b["world"] = world
+        b["position"][:, 0] = rng.uniform(-6, 6, balls)
+        b["position"][:, 1] = rng.uniform(1.0, 6.0, balls)
+        b["position"][:, 2] = rng.uniform(-6, 6, balls)
+        b["velocity"][:, :3] = rng.uniform(-3, 3, (balls, 3))
+        cl = collider_descs(balls, np.arange(balls) + nb, abi.SHAPE_BALL, (0.3, 0, 0), density=1.0, friction=0.5)
+        bodies.append(b)
+        colliders.append(cl)
+        nb += balls
+    return np.concatenate(bodies), np.concatenate(colliders), np.concatenate(joints), nb
+
+
+def jointed(chains=4, links=8, clusters=6, balls=10, seed=3):
+    """Ball-jointed chains swinging from pivots on the ground body, fixed-jointed
+    cuboid-ball pairs and free balls, falling onto the ground: the joint
+    parity scene (one world)."""
+    rng = np.random.default_rng(seed)
+    bodies, colliders, joints, _ = _jointed_world(rng, 0, chains, links, clusters, balls)
+    sc = Scene("jointed bodies", bodies, colliders, steps=120)
+    return set_joints(sc, joints)
+
+
+def batched_jointed(n_worlds=8, seed=5, chains=2, links=6, clusters=3, balls=4, worlds=None):
+    """Independent worlds of the jointed scene, each on its own ground (joint
+    and body slots renumbered per world in order): the per-world schedule
+    with joints. `worlds` builds only those worlds, renumbered from world 0."""
+    worlds = range(n_worlds) if worlds is None else worlds
+    parts_b, parts_c, parts_j = [], [], []
+    off = 0
+    for local, w in enumerate(worlds):
+        rng = np.random.default_rng([seed, w])
+        b, c, j, nb = _jointed_world(rng, local, chains, links, clusters, balls)
+        c = c.copy()
+        c["body"]["index"] += off
+        j = j.copy()
+        j["body1"]["index"] += off
+        j["body2"]["index"] += off
+        parts_b.append(b)
+        parts_c.append(c)
+        parts_j.append(j)
+        off += nb
+    sc = Scene(f"{len(worlds)} jointed worlds", np.concatenate(parts_b), np.concatenate(parts_c), steps=120)
+    return set_joints(sc, np.concatenate(parts_j))
+
+
+def pendulum(length=2.0, angle=0.2, radius=0.1, density=100.0, chain=1):
+    """A ball on a massless rod: a ball joint between a pivot on the ground
+    body (at height 10) and the ball, `length` below it, released at `angle`
+    from the vertical; with chain > 1 the balls hang one below the other.
+    No collisions occur (the balls stay far from the ground)."""
+    g = ground_descs(1)
+    gc = collider_descs(1, 0, abi.SHAPE_CUBOID, (1.0, 1.0, 1.0))
+    gc["position_wrt_body"][0, 1] = -1.0
+    b = body_descs(chain)
+    pivot = np.array([0.0, 10.0, 0.0])
+    d = np.array([np.sin(angle), -np.cos(angle), 0.0])
+    for i in range(chain):
+        b["position"][i, :3] = pivot + d * length * (i + 1)
+    b["flags"] = abi.BODY_GRAVITY          # never sleeps
+    c = collider_descs(chain, np.arange(chain), abi.SHAPE_BALL, (radius, 0, 0), density=density)
+    bodies, colliders = _concat([g, b], [gc, c])
+    j = joint_descs(chain)
+    j["kind"] = abi.JOINT_BALL
+    for i in range(chain):
+        j["body1"]["index"][i] = i          # the ground, then the ball above
+        j["anchor1"][i] = pivot if i == 0 else (0.0, 0.0, 0.0)
+        j["body2"]["index"][i] = i + 1
+        j["anchor2"][i] = -d * length if i == 0 else -d * length
+    sc = Scene("pendulum", bodies, colliders, steps=600)
+    return set_joints(sc, j)

@@ -45,12 +45,13 @@ class GpuWorld:
             raise NpgpuError(st.value, self.L.npgpu_last_error(None).decode())
         self.num_bodies = 0
         self.num_colliders = 0
+        self._joints = {}                # joint slot -> generation of the joints uploaded
 
     @classmethod
     def for_scene(cls, scene, params=None, pairs_per_collider=16):
         p = params if params is not None else scene.params()
         w = cls(p, scene.gravity, capacity_bodies=len(scene.bodies), capacity_colliders=len(scene.colliders),
-                capacity_pairs=max(1024, pairs_per_collider * len(scene.colliders)))
+                capacity_pairs=max(1024, pairs_per_collider * len(scene.colliders)) + len(getattr(scene, "joints", ())))
         w.load_scene(scene)
         return w
 
@@ -99,6 +100,34 @@ class GpuWorld:
     def load_scene(self, scene):
         self.upsert_bodies(scene.body_handles, scene.bodies)
         self.upsert_colliders(scene.collider_handles, scene.colliders)
+        if len(getattr(scene, "joints", ())):
+            self.upsert_joints(scene.joint_handles, scene.joints)
+
+    # ---- joint constraints ----
+    def upsert_joints(self, handles, descs):
+        descs = np.ascontiguousarray(descs)
+        handles = np.ascontiguousarray(handles)
+        self._check(self.L.npgpu_upsert_joints(self.w, len(descs), _ptr(handles, abi.Handle),
+                                               _ptr(descs, abi.JointDesc)), "upsert_joints")
+        for h in handles:
+            self._joints[int(h["index"])] = int(h["generation"])
+
+    def remove_joints(self, handles):
+        handles = np.ascontiguousarray(handles)
+        self._check(self.L.npgpu_remove_joints(self.w, len(handles), _ptr(handles, abi.Handle)), "remove_joints")
+        for h in handles:
+            self._joints.pop(int(h["index"]), None)
+
+    def joints(self, handles):
+        """(impulses (n, 6), broken (n,), active (n,)) after the last step."""
+        handles = np.ascontiguousarray(handles)
+        out = (abi.JointState * max(len(handles), 1))()
+        self._check(self.L.npgpu_get_joints(self.w, len(handles), _ptr(handles, abi.Handle), out), "get_joints")
+        n = len(handles)
+        imp = np.array([list(out[k].impulses) for k in range(n)], np.float32).reshape(n, 6)
+        broken = np.array([out[k].broken for k in range(n)], bool)
+        active = np.array([out[k].active for k in range(n)], bool)
+        return imp, broken, active
 
     def remove_bodies(self, handles):
         handles = np.ascontiguousarray(handles)
@@ -114,7 +143,10 @@ class GpuWorld:
         self._check(self.L.npgpu_apply_forces(self.w, len(handles), _ptr(handles, abi.Handle), _ptr(f, C.c_float),
                                               int(wake)), "apply_forces")
 
-    def step(self, n=1, joints=0, force_generators=0, sync=True):
+    def step(self, n=1, joints=None, force_generators=0, sync=True):
+        """`joints`: the caller's joint-set size (default: the joints uploaded)."""
+        if joints is None:
+            joints = len(self._joints)
         self._check(self.L.npgpu_step(self.w, n, joints, force_generators), "step")
         if sync:
             self.synchronize()

@@ -103,6 +103,43 @@ int orc_remove_colliders(orc_world* o, uint32_t n, const npgpu_handle* h) {
     return 0;
 }
 
+int orc_upsert_joints(orc_world* o, uint32_t n, const npgpu_handle* h, const npgpu_joint_desc* d) {
+    for (uint32_t i = 0; i < n; ++i) {
+        int s = 0;
+        DISPATCH(o, s = w.upsert_joint(h[i], d[i]));
+        if (s) return s;
+    }
+    return 0;
+}
+
+int orc_remove_joints(orc_world* o, uint32_t n, const npgpu_handle* h) {
+    for (uint32_t i = 0; i < n; ++i) {
+        int s = 0;
+        DISPATCH(o, s = w.remove_joint(h[i]));
+        if (s) return s;
+    }
+    return 0;
+}
+
+// Per joint slot: 6 impulses (f64), then broken and active flags.
+int orc_get_joints(orc_world* o, uint32_t n, const npgpu_handle* h, double* imp6, uint32_t* flags2) {
+    int s = 0;
+    DISPATCH(o, {
+        for (uint32_t i = 0; i < n && !s; ++i) {
+            if (h[i].index >= w.joints.size() || !w.joints[h[i].index].alive ||
+                w.joints[h[i].index].generation != h[i].generation) {
+                s = NPGPU_ERR_INVALID_HANDLE;
+                break;
+            }
+            const auto& j = w.joints[h[i].index];
+            for (int k = 0; k < 6; ++k) imp6[6 * i + k] = double(j.imp[k]);
+            flags2[2 * i] = j.broken ? 1u : 0u;
+            flags2[2 * i + 1] = j.active ? 1u : 0u;
+        }
+    });
+    return s;
+}
+
 int orc_apply_forces(orc_world* o, uint32_t n, const npgpu_handle* h, const float* f, int wake) {
     for (uint32_t i = 0; i < n; ++i) {
         int s = 0;

@@ -36,6 +36,9 @@ def lib():
             "orc_remove_bodies": (C.c_int, [W, C.c_uint32, C.c_void_p]),
             "orc_remove_colliders": (C.c_int, [W, C.c_uint32, C.c_void_p]),
             "orc_apply_forces": (C.c_int, [W, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]),
+            "orc_upsert_joints": (C.c_int, [W, C.c_uint32, C.c_void_p, C.c_void_p]),
+            "orc_remove_joints": (C.c_int, [W, C.c_uint32, C.c_void_p]),
+            "orc_get_joints": (C.c_int, [W, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p]),
             "orc_step": (C.c_int, [W, C.c_uint32]),
             "orc_collision_detection": (None, [W]),
             "orc_download_bodies": (C.c_int, [W, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
@@ -114,6 +117,25 @@ class OracleWorld:
                     "upsert colliders")
         self.num_bodies = max(self.num_bodies, len(b))
         self.num_colliders = max(self.num_colliders, len(c))
+        if len(getattr(scene, "joints", ())):
+            self.upsert_joints(scene.joint_handles, scene.joints)
+
+    def upsert_joints(self, handles, descs):
+        d = np.ascontiguousarray(descs)
+        self._check(self.L.orc_upsert_joints(self.w, len(d), _ptr(np.ascontiguousarray(handles)), _ptr(d)),
+                    "upsert joints")
+
+    def remove_joints(self, handles):
+        self._check(self.L.orc_remove_joints(self.w, len(handles), _ptr(np.ascontiguousarray(handles))),
+                    "remove joints")
+
+    def joints(self, handles):
+        """(impulses (n, 6) f64, broken (n,), active (n,)) after the last step."""
+        h = np.ascontiguousarray(handles)
+        imp = np.zeros((len(h), 6), np.float64)
+        flags = np.zeros((len(h), 2), np.uint32)
+        self._check(self.L.orc_get_joints(self.w, len(h), _ptr(h), _ptr(imp), _ptr(flags)), "get joints")
+        return imp, flags[:, 0].astype(bool), flags[:, 1].astype(bool)
 
     def upsert_bodies(self, handles, descs):
         self._check(self.L.orc_upsert_bodies(self.w, len(descs), _ptr(handles), _ptr(descs)), "upsert bodies")

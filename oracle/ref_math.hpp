@@ -100,6 +100,19 @@ template <class R> inline Quat<R> qexp_scaled_axis(V3<R> axisangle) {
 }
 
 // Row-major 3x3.
+// UnitQuaternion::scaled_axis: the axis (the vector part, negated when
+// w < 0, normalised; zero when it vanishes) times the angle 2 acos(|w|)
+// (0 when |w| >= 1). In f32 acos is taken in double and rounded, as the GPU does.
+template <class R> inline V3<R> qscaled_axis(Quat<R> q) {
+    V3<R> v = q.w >= R(0) ? qvec(q) : -qvec(q);
+    R sq = dot(v, v);
+    if (!(sq > R(0))) return v3<R>(R(0), R(0), R(0));
+    V3<R> axis = vdiv(v, R(std::sqrt(sq)));
+    R aw = std::fabs(q.w);
+    R angle = aw >= R(1) ? R(0) : R(std::acos(double(aw))) * R(2);
+    return axis * angle;
+}
+
 template <class R> struct M3 {
     R m[3][3];
 };

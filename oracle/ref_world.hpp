@@ -265,16 +265,31 @@ template <class R> struct Row {
     int dep;               // friction: index of its normal row
     R mu;
     bool friction;
+    bool bilateral;        // a joint row: Independent limits of +-max (helper.rs:186-189)
+    int joint, joint_slot; // its joint and impulse slot (0-2 linear, 3-5 angular)
     void* cache;           // MContact the impulse is cached to
     int cache_slot;
     bool predicted;        // normal row of a contact started from the learned network
     R alt[3];              // ... and the start the prediction replaced (cached impulses, or zero)
 };
 
+// A joint constraint (BallConstraint / FixedConstraint, src/joint/).
+template <class R> struct Joint {
+    bool alive = false;
+    uint64_t generation = 0;
+    uint32_t kind = NPGPU_JOINT_BALL, b1 = 0, b2 = 0;
+    V3<R> anchor1, anchor2;     // in the bodies' frames
+    Quat<R> frame1, frame2;     // FixedConstraint's reference frames
+    R brk_force2, brk_torque2;  // set_break_force / set_break_torque keep the squares
+    R imp[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};   // linear x y z, angular x y z
+    bool broken = false, active = false;
+};
+
 template <class R> struct PosConstraint {
     uint32_t c1, c2;
     int fid1, fid2;
     V3<R> normal1_local;
+    int joint = -1;           // >= 0: the position constraints of that joint
 };
 
 template <class R> class World {
@@ -292,6 +307,7 @@ public:
     bool cd_dirty = true;
     uint32_t num_colours = 0;
     uint32_t num_solver_contacts = 0;   // contacts the last solve took, counted when they were collected
+    std::vector<Joint<R>> joints;        // by joint slot (the host set's arena index)
 
     World(const npgpu_params& p, const float g[3]) : params(p) {
         gravity = v3<R>(R(g[0]), R(g[1]), R(g[2]));
@@ -396,6 +412,9 @@ public:
         for (size_t i = 0; i < colliders.size(); ++i)
             if (colliders[i].alive && colliders[i].body == h.index) remove_collider_slot(uint32_t(i), false);
         bodies[h.index].alive = false;
+        // Joints with a removed body go too (mechanical_world.rs:141-154).
+        for (uint32_t j = 0; j < joints.size(); ++j)
+            if (joints[j].alive && (joints[j].b1 == h.index || joints[j].b2 == h.index)) drop_joint(j);
         cd_dirty = true;
         return NPGPU_OK;
     }
@@ -418,6 +437,57 @@ public:
         b.f_lin = b.f_lin + v3<R>(R(f[0]) * b.mask[0], R(f[1]) * b.mask[1], R(f[2]) * b.mask[2]);
         b.f_ang = b.f_ang + v3<R>(R(f[3]) * b.mask[3], R(f[4]) * b.mask[4], R(f[5]) * b.mask[5]);
         return NPGPU_OK;
+    }
+
+    // DefaultJointConstraintSet::insert / remove, waking both bodies
+    // (mechanical_world.rs:156-175).
+    npgpu_status upsert_joint(const npgpu_handle& h, const npgpu_joint_desc& d) {
+        auto body_ok = [&](const npgpu_handle& b) {
+            return b.index < bodies.size() && bodies[b.index].alive && bodies[b.index].generation == b.generation;
+        };
+        if (d.kind != NPGPU_JOINT_BALL && d.kind != NPGPU_JOINT_FIXED)
+            return fail(NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind");
+        if (!body_ok(d.body1) || !body_ok(d.body2)) return fail(NPGPU_ERR_INVALID_HANDLE, "joint body handle is invalid");
+        if (d.body1.index == d.body2.index) return fail(NPGPU_ERR_INVALID_ARGUMENT, "a joint needs two different bodies");
+        if (bodies[d.body1.index].world != bodies[d.body2.index].world)
+            return fail(NPGPU_ERR_INVALID_ARGUMENT, "a joint's bodies must belong to the same world");
+        if (h.index >= (1u << 21) - 1u) return fail(NPGPU_ERR_CAPACITY, "joint index too large");
+        if (h.index >= joints.size()) joints.resize(h.index + 1);
+        Joint<R>& j = joints[h.index];
+        if (j.alive) {
+            activate_alive(j.b1);
+            activate_alive(j.b2);
+        }
+        j = Joint<R>();
+        j.alive = true;
+        j.generation = h.generation;
+        j.kind = d.kind;
+        j.b1 = uint32_t(d.body1.index);
+        j.b2 = uint32_t(d.body2.index);
+        j.anchor1 = v3<R>(R(d.anchor1[0]), R(d.anchor1[1]), R(d.anchor1[2]));
+        j.anchor2 = v3<R>(R(d.anchor2[0]), R(d.anchor2[1]), R(d.anchor2[2]));
+        j.frame1 = Quat<R>{R(d.frame1[0]), R(d.frame1[1]), R(d.frame1[2]), R(d.frame1[3])};
+        j.frame2 = Quat<R>{R(d.frame2[0]), R(d.frame2[1]), R(d.frame2[2]), R(d.frame2[3])};
+        const R f = R(d.break_force), t = R(d.break_torque);
+        j.brk_force2 = f * f;
+        j.brk_torque2 = t * t;
+        activate_alive(j.b1);
+        activate_alive(j.b2);
+        return NPGPU_OK;
+    }
+    npgpu_status remove_joint(const npgpu_handle& h) {
+        if (h.index >= joints.size() || !joints[h.index].alive || joints[h.index].generation != h.generation)
+            return fail(NPGPU_ERR_INVALID_HANDLE, "invalid joint handle");
+        drop_joint(uint32_t(h.index));
+        return NPGPU_OK;
+    }
+    void drop_joint(uint32_t j) {
+        joints[j].alive = false;
+        activate_alive(joints[j].b1);
+        activate_alive(joints[j].b2);
+    }
+    void activate_alive(uint32_t b) {
+        if (b < bodies.size() && bodies[b].alive) activate(bodies[b]);
     }
 
     // ------------------------------------------------------- body dynamics
@@ -1421,6 +1491,11 @@ public:
             int a = comp_id[colliders[m.c1].body], b = comp_id[colliders[m.c2].body];
             if (a >= 0 && b >= 0) uf_union(uint32_t(a), uint32_t(b));
         }
+        for (const Joint<R>& j : joints) {   // activation_manager.rs:154-159
+            if (!j.alive || j.broken) continue;
+            int a = comp_id[j.b1], b = comp_id[j.b2];
+            if (a >= 0 && b >= 0) uf_union(uint32_t(a), uint32_t(b));
+        }
         std::vector<char> can_deactivate(id_to_body.size(), 1);
         for (uint32_t i = 0; i < id_to_body.size(); ++i) {
             uint32_t root = uf_find(i);
@@ -1449,10 +1524,18 @@ public:
     }
 
     // RigidBody::fill_constraint_geometry (rigid_body.rs:672-722).
+    // The side's unit force f: ForceDirection::at_point (helper.rs:24-33).
     void fill(const Body<R>& b, V3<R> point, V3<R> dir, R* J, R* WJ, R& inv_r, R& rhs, bool with_ext) const {
         V3<R> pos = point - b.com;
         V3<R> fl = dir, fa = cross(pos, dir);
-        R f[6] = {fl.x, fl.y, fl.z, fa.x, fa.y, fa.z};
+        const R f[6] = {fl.x, fl.y, fl.z, fa.x, fa.y, fa.z};
+        fill_force(b, f, J, WJ, inv_r, rhs, with_ext);
+    }
+    void fill_torque(const Body<R>& b, V3<R> axis, R* J, R* WJ, R& inv_r, R& rhs, bool with_ext) const {
+        const R f[6] = {R(0), R(0), R(0), axis.x, axis.y, axis.z};
+        fill_force(b, f, J, WJ, inv_r, rhs, with_ext);
+    }
+    void fill_force(const Body<R>& b, const R* f, R* J, R* WJ, R& inv_r, R& rhs, bool with_ext) const {
         R mf[6];
         for (int k = 0; k < 6; ++k) mf[k] = f[k] * b.mask[k];
         R vel[6] = {b.lin.x, b.lin.y, b.lin.z, b.ang.x, b.ang.y, b.ang.z};
@@ -1491,6 +1574,20 @@ public:
         R inv_r = R(0), rhs = rhs0;
         fill(b1, center1, dir, r.J1, r.WJ1, inv_r, rhs, true);
         fill(b2, center2, -dir, r.J2, r.WJ2, inv_r, rhs, true);
+        r.r = (inv_r != R(0)) ? R(1) / inv_r : R(1);
+        r.rhs = rhs;
+        return r;
+    }
+
+    // constraint_pair_geometry for ForceDirection::Angular(axis).
+    Row<R> make_row_angular(const Body<R>& b1, uint32_t s1, const Body<R>& b2, uint32_t s2, V3<R> axis) const {
+        Row<R> r;
+        std::memset(&r, 0, sizeof(r));
+        r.b1 = b1.dynamic() ? int(s1) : -1;
+        r.b2 = b2.dynamic() ? int(s2) : -1;
+        R inv_r = R(0), rhs = R(0);
+        fill_torque(b1, axis, r.J1, r.WJ1, inv_r, rhs, true);
+        fill_torque(b2, -axis, r.J2, r.WJ2, inv_r, rhs, true);
         r.r = (inv_r != R(0)) ? R(1) / inv_r : R(1);
         r.rhs = rhs;
         return r;
@@ -1616,15 +1713,23 @@ public:
     std::vector<int> seq_merged;
     std::vector<Manifold<R>*> solver_manifolds;
 
+    // A solver item: a contact manifold or an active joint, with its two
+    // bodies and its Jones-Plassmann priority.
+    struct Item {
+        Manifold<R>* m = nullptr;
+        int joint = -1;
+        uint32_t b1 = 0, b2 = 0;
+        uint64_t prio = 0;
+        uint32_t colour = 0xffffffffu;
+    };
+
     // JP colouring with first-fit colours (the GPU solver's schedule), at
     // most kOracleColours colours (the GPU keeps a body's colour mask in two
-    // 56-bit words).
+    // 56-bit words). Priorities: a manifold hashes its colliders' world-local
+    // slots; a joint hashes its world-local joint slot with a second input no
+    // collider pair has (the GPU's joint_priority).
     static constexpr uint32_t kOracleColours = 112;
-    uint32_t colour_manifolds(std::vector<Manifold<R>*>& ms) {
-        std::vector<uint64_t> best(bodies.size(), 0);
-        std::vector<uint64_t> used(2 * bodies.size(), 0);   // colours 0-63 and 64-127 of each body
-        std::vector<Manifold<R>*> todo = ms;
-        // World-local collider slots.
+    uint32_t colour_items(std::vector<Item>& items) {
         std::vector<uint32_t> base, local(colliders.size());
         for (uint32_t c = 0; c < colliders.size(); ++c) {
             if (!colliders[c].alive) continue;
@@ -1636,45 +1741,88 @@ public:
             uint32_t wd = colliders[c].alive ? bodies[colliders[c].body].world : 0xffffffffu;
             local[c] = (wd < base.size() && base[wd] <= c) ? c - base[wd] : c;
         }
-        auto prio = [&](const Manifold<R>* m) { return pair_priority(local[m->c1], local[m->c2], m->c1, m->c2); };
+        std::vector<uint32_t> jbase, jlocal(joints.size());
+        for (uint32_t j = 0; j < joints.size(); ++j) {
+            if (!joints[j].alive) continue;
+            uint32_t wd = bodies[joints[j].b1].world;
+            if (wd >= jbase.size()) jbase.resize(wd + 1, 0xffffffffu);
+            jbase[wd] = std::min(jbase[wd], j);
+        }
+        for (uint32_t j = 0; j < joints.size(); ++j) {
+            uint32_t wd = joints[j].alive ? bodies[joints[j].b1].world : 0xffffffffu;
+            jlocal[j] = (wd < jbase.size() && jbase[wd] <= j) ? j - jbase[wd] : j;
+        }
+        for (Item& it : items) {
+            if (it.joint >= 0)
+                it.prio = (uint64_t(pair_hash22(jlocal[it.joint], 0x3fffffu)) << 42) | (uint64_t(0x1fffff) << 21) |
+                          uint64_t(it.joint);
+            else
+                it.prio = pair_priority(local[it.m->c1], local[it.m->c2], it.m->c1, it.m->c2);
+        }
+        std::vector<uint64_t> best(bodies.size(), 0);
+        std::vector<uint64_t> used(2 * bodies.size(), 0);   // colours 0-63 and 64-127 of each body
+        std::vector<Item*> todo;
+        for (Item& it : items) todo.push_back(&it);
         uint32_t ncol = 0;
         while (!todo.empty()) {
-            for (Manifold<R>* m : todo) {
-                uint64_t p = prio(m);
-                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
-                if (bodies[b1].dynamic()) best[b1] = std::max(best[b1], p);
-                if (bodies[b2].dynamic()) best[b2] = std::max(best[b2], p);
+            for (Item* m : todo) {
+                if (bodies[m->b1].dynamic()) best[m->b1] = std::max(best[m->b1], m->prio);
+                if (bodies[m->b2].dynamic()) best[m->b2] = std::max(best[m->b2], m->prio);
             }
-            std::vector<Manifold<R>*> rest, won;
-            for (Manifold<R>* m : todo) {
-                uint64_t p = prio(m);
-                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
-                bool w = (!bodies[b1].dynamic() || best[b1] == p) && (!bodies[b2].dynamic() || best[b2] == p);
+            std::vector<Item*> rest, won;
+            for (Item* m : todo) {
+                bool w = (!bodies[m->b1].dynamic() || best[m->b1] == m->prio) &&
+                         (!bodies[m->b2].dynamic() || best[m->b2] == m->prio);
                 (w ? won : rest).push_back(m);
             }
-            for (Manifold<R>* m : won) {
-                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
+            for (Item* m : won) {
                 uint64_t mask[2] = {0, 0};
                 for (int h = 0; h < 2; ++h) {
-                    if (bodies[b1].dynamic()) mask[h] |= used[2 * b1 + h];
-                    if (bodies[b2].dynamic()) mask[h] |= used[2 * b2 + h];
+                    if (bodies[m->b1].dynamic()) mask[h] |= used[2 * m->b1 + h];
+                    if (bodies[m->b2].dynamic()) mask[h] |= used[2 * m->b2 + h];
                 }
                 uint32_t c = 0;
                 while (c < kOracleColours && (mask[c >> 6] >> (c & 63u)) & 1u) ++c;
                 m->colour = c;
+                if (m->m) m->m->colour = c;
                 if (c >= kOracleColours) continue;
-                if (bodies[b1].dynamic()) used[2 * b1 + (c >> 6)] |= (uint64_t(1) << (c & 63u));
-                if (bodies[b2].dynamic()) used[2 * b2 + (c >> 6)] |= (uint64_t(1) << (c & 63u));
+                if (bodies[m->b1].dynamic()) used[2 * m->b1 + (c >> 6)] |= (uint64_t(1) << (c & 63u));
+                if (bodies[m->b2].dynamic()) used[2 * m->b2 + (c >> 6)] |= (uint64_t(1) << (c & 63u));
                 ncol = std::max(ncol, c + 1);
             }
-            for (Manifold<R>* m : todo) {
-                uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
-                best[b1] = 0;
-                best[b2] = 0;
+            for (Item* m : todo) {
+                best[m->b1] = 0;
+                best[m->b2] = 0;
             }
             todo.swap(rest);
         }
         return ncol;
+    }
+
+    // The rows of active joint j (BallConstraint / FixedConstraint::
+    // velocity_constraints, ball_constraint.rs:80-127, fixed_constraint.rs:
+    // 107-172, through helper::cancel_relative_linear_velocity and
+    // cancel_relative_angular_velocity, helper.rs:167-296, 422-551): one
+    // bilateral row per axis, started from the joint's impulse.
+    void joint_rows(uint32_t j, std::vector<int>& out) {
+        const Joint<R>& jt = joints[j];
+        const Body<R>& b1 = bodies[jt.b1];
+        const Body<R>& b2 = bodies[jt.b2];
+        const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
+        const int nt = jt.kind == NPGPU_JOINT_FIXED ? 2 : 1;
+        for (int t = 0; t < nt; ++t)
+            for (int r = 0; r < 3; ++r) {
+                V3<R> e = v3<R>(r == 0 ? R(1) : R(0), r == 1 ? R(1) : R(0), r == 2 ? R(1) : R(0));
+                Row<R> row = t == 0 ? make_row(b1, jt.b1, b2, jt.b2, a1, a2, e, R(0))
+                                    : make_row_angular(b1, jt.b1, b2, jt.b2, e);
+                row.impulse = jt.imp[3 * t + r];
+                row.bilateral = true;
+                row.joint = int(j);
+                row.joint_slot = 3 * t + r;
+                row.cache = nullptr;
+                out.push_back(int(rows.size()));
+                rows.push_back(row);
+            }
     }
 
     // MoreauJeanSolver::assemble_system + SignoriniCoulombPyramidModel::constraints
@@ -1701,17 +1849,44 @@ public:
         }
         num_solver_contacts = 0;
         for (const Manifold<R>* m : solver_manifolds) num_solver_contacts += uint32_t(m->contacts.size());
+        // Active joints (mechanical_world.rs:274-279, joint_constraint.rs:218-227),
+        // in slot order (the arena's iteration order).
+        std::vector<Item> items;
+        for (Manifold<R>* m : solver_manifolds) {
+            Item it;
+            it.m = m;
+            it.b1 = colliders[m->c1].body;
+            it.b2 = colliders[m->c2].body;
+            items.push_back(it);
+        }
+        for (uint32_t j = 0; j < joints.size(); ++j) {
+            Joint<R>& jt = joints[j];
+            jt.active = false;
+            if (!jt.alive || jt.broken) continue;
+            const Body<R>& b1 = bodies[jt.b1];
+            const Body<R>& b2 = bodies[jt.b2];
+            if ((b1.ndofs() != 0 && b1.is_active()) || (b2.ndofs() != 0 && b2.is_active())) {
+                jt.active = true;
+                Item it;
+                it.joint = int(j);
+                it.b1 = jt.b1;
+                it.b2 = jt.b2;
+                items.push_back(it);
+            }
+        }
         num_colours = 0;
-        std::vector<Manifold<R>*> seq = solver_manifolds;
         if (order == ORDER_COLOUR) {
-            num_colours = colour_manifolds(seq);
-            if (std::any_of(seq.begin(), seq.end(), [](Manifold<R>* m) { return m->colour >= kOracleColours; })) {
+            num_colours = colour_items(items);
+            if (std::any_of(items.begin(), items.end(), [](const Item& m) { return m.colour >= kOracleColours; })) {
                 last_error = "colour overflow";
                 return false;
             }
-            std::stable_sort(seq.begin(), seq.end(),
-                             [](Manifold<R>* a, Manifold<R>* b) { return a->colour < b->colour; });
+            std::stable_sort(items.begin(), items.end(),
+                             [](const Item& a, const Item& b) { return a.colour < b.colour; });
         }
+        std::vector<Manifold<R>*> seq;
+        for (const Item& it : items)
+            if (it.m) seq.push_back(it.m);
         R inv_dt = (params.dt == 0.0f) ? R(0) : R(1) / R(params.dt);
         // Learned starts: mode 2 for contacts without a cache entry, mode 3
         // for every contact.
@@ -1720,14 +1895,39 @@ public:
             last_error = "learned warm start needs a network and the colour order";
             return false;
         }
-        std::vector<uint32_t> kb(bodies.size(), 0);   // solver manifolds per dynamic body
-        for (Manifold<R>* m : seq) {
-            uint32_t b1 = colliders[m->c1].body, b2 = colliders[m->c2].body;
-            if (bodies[b1].dynamic()) ++kb[b1];
-            if (bodies[b2].dynamic()) ++kb[b2];
+        std::vector<uint32_t> kb(bodies.size(), 0);   // solver manifolds (and joints) per dynamic body
+        for (const Item& it : items) {
+            if (bodies[it.b1].dynamic()) ++kb[it.b1];
+            if (bodies[it.b2].dynamic()) ++kb[it.b2];
         }
         std::vector<int> ug, un, bg, bn;   // unilateral ground / non-ground, bilateral ...
-        for (Manifold<R>* m : seq) {
+        std::vector<int> jn, jg;           // joint rows, non-ground / ground
+        std::vector<int> jpos;             // joints' position constraints (reference order)
+        for (const Item& item : items) {
+            if (item.joint >= 0) {
+                // A joint: its rows run with the friction rows (colour order),
+                // or before them (SORProx::step, sor_prox.rs:159-179).
+                std::vector<int> jr;
+                joint_rows(uint32_t(item.joint), jr);
+                PosConstraint<R> pc{};
+                pc.joint = item.joint;
+                pos_constraints.push_back(pc);
+                const int pi = int(pos_constraints.size()) - 1;
+                if (order == ORDER_COLOUR) {
+                    for (int i : jr) {
+                        seq_warm.push_back(i);
+                        seq_friction.push_back(i);
+                    }
+                    seq_pos.push_back(pi);
+                } else {
+                    const bool ground = bodies[item.b1].ndofs() == 0 || bodies[item.b2].ndofs() == 0;
+                    for (int i : jr) (ground ? jg : jn).push_back(i);
+                    jpos.push_back(pi);
+                }
+                seq_merged.insert(seq_merged.end(), jr.begin(), jr.end());
+                continue;
+            }
+            Manifold<R>* m = item.m;
             const Collider<R>& c1 = colliders[m->c1];
             const Collider<R>& c2 = colliders[m->c2];
             const Body<R>& b1 = bodies[c1.body];
@@ -1812,15 +2012,24 @@ public:
             seq_merged.insert(seq_merged.end(), m_normal.begin(), m_normal.end());
         }
         if (order == ORDER_REFERENCE) {
-            // SORProx::warmstart_set / step (sor_prox.rs:19-45, 159-179).
+            // SORProx::warmstart_set / step (sor_prox.rs:19-45, 159-179):
+            // the contacts' warm start, then the joints'; each iteration the
+            // joints' bilateral rows, the contacts' friction rows, then the
+            // contacts' normal rows. NonlinearSORProx::solve takes the joints
+            // before the contacts (nonlinear_sor_prox.rs:33-54).
             for (int i : un) seq_warm.push_back(i);
             for (int i : ug) seq_warm.push_back(i);
             for (int i : bn) seq_warm.push_back(i);
             for (int i : bg) seq_warm.push_back(i);
+            for (int i : jn) seq_warm.push_back(i);
+            for (int i : jg) seq_warm.push_back(i);
+            for (int i : jn) seq_friction.push_back(i);
+            for (int i : jg) seq_friction.push_back(i);
             for (int i : bn) seq_friction.push_back(i);
             for (int i : bg) seq_friction.push_back(i);
             for (int i : un) seq_normal.push_back(i);
             for (int i : ug) seq_normal.push_back(i);
+            seq_pos.insert(seq_pos.begin(), jpos.begin(), jpos.end());
         }
         return true;
     }
@@ -1875,6 +2084,17 @@ public:
         r.impulse = ni;
         axpy(r, dl);
     }
+    // SORProx::solve_bilateral[_ground] with ImpulseLimits::Independent of
+    // +-max (a joint row, helper.rs:186-189).
+    void solve_bilateral(Row<R>& r) {
+        const R mx = std::numeric_limits<R>::max();
+        R dimpulse = jdot(r) + r.rhs;
+        R ni = r.impulse - r.r * dimpulse;
+        ni = ni < -mx ? -mx : (ni > mx ? mx : ni);
+        R dl = ni - r.impulse;
+        r.impulse = ni;
+        axpy(r, dl);
+    }
     // J dv + rhs of a row, for the residual. f32: the compensated dot product
     // Dot2 of Ogita, Rump and Oishi (SIAM J. Sci. Comput. 26(6), 2005) as the
     // unevaluated float sum s + c (TwoProduct by a fused multiply-add, TwoSum,
@@ -1917,7 +2137,8 @@ public:
             double lam = double(r.impulse);
             double x = lam - double(r.r) * d;
             double p;
-            if (!r.friction) p = x > 0 ? x : 0;
+            if (r.bilateral) p = x;
+            else if (!r.friction) p = x > 0 ? x : 0;
             else {
                 double mx = double(r.mu) * double(rows[r.dep].impulse);
                 p = std::min(std::max(x, -mx), mx);
@@ -1969,11 +2190,15 @@ public:
             if (params.solve_to_tolerance && res <= double(params.residual_tolerance)) break;
             if (params.sweep_order == NPGPU_SWEEP_MANIFOLD) {
                 for (int i : seq_merged) {
-                    if (rows[i].friction) solve_friction(rows[i]);
+                    if (rows[i].bilateral) solve_bilateral(rows[i]);
+                    else if (rows[i].friction) solve_friction(rows[i]);
                     else solve_normal(rows[i]);
                 }
             } else {
-                for (int i : seq_friction) solve_friction(rows[i]);
+                for (int i : seq_friction) {
+                    if (rows[i].bilateral) solve_bilateral(rows[i]);
+                    else solve_friction(rows[i]);
+                }
                 for (int i : seq_normal) solve_normal(rows[i]);
             }
             ++iters;
@@ -1984,13 +2209,100 @@ public:
         counters.velocity_iterations = iters;
     }
     // SignoriniCoulombPyramidModel::cache_impulses (signorini_coulomb_pyramid_model.rs:226-261).
+    // JointConstraint::cache_impulses (ball_constraint.rs:129-141,
+    // fixed_constraint.rs:174-199): the joint keeps its rows' impulses and
+    // breaks when |impulse|^2 / dt^2 exceeds the squared break force / torque.
     void cache_impulses() {
-        for (const Row<R>& r : rows) static_cast<MContact<R>*>(r.cache)->impulse[r.cache_slot] = r.impulse;
+        for (const Row<R>& r : rows) {
+            if (r.bilateral) joints[r.joint].imp[r.joint_slot] = r.impulse;
+            else static_cast<MContact<R>*>(r.cache)->impulse[r.cache_slot] = r.impulse;
+        }
+        const R inv_dt = (params.dt == 0.0f) ? R(0) : R(1) / R(params.dt);
+        for (Joint<R>& j : joints) {
+            if (!j.alive || !j.active) continue;
+            const R n2 = R(0) + j.imp[0] * j.imp[0] + j.imp[1] * j.imp[1] + j.imp[2] * j.imp[2];
+            if (j.kind == NPGPU_JOINT_FIXED) {
+                const R a2 = R(0) + j.imp[3] * j.imp[3] + j.imp[4] * j.imp[4] + j.imp[5] * j.imp[5];
+                const R inv_dt2 = inv_dt * inv_dt;
+                if (n2 * inv_dt2 > j.brk_force2 || a2 * inv_dt2 > j.brk_torque2) j.broken = true;
+            } else if (n2 * inv_dt * inv_dt > j.brk_force2) {
+                j.broken = true;
+            }
+        }
+    }
+
+    // NonlinearSORProx::solve_generic (nonlinear_sor_prox.rs:78-117) of one
+    // position row: clamp_rhs (nonlinear_sor_prox.rs:297-309), then each side
+    // with dofs moves by its W times -rhs r.
+    void generic_position_row(R depth, bool angular, R inv_r, Body<R>& b1, Body<R>& b2, R* W1, R* W2) {
+        R rhs = -depth;
+        if (angular) {
+            rhs = (rhs + R(params.allowed_angular_error)) * R(params.erp);
+            rhs = rhs < -R(params.max_angular_correction) ? -R(params.max_angular_correction) : rhs;
+        } else {
+            rhs = (rhs + R(params.allowed_linear_error)) * R(params.erp);
+            rhs = rhs < -R(params.max_linear_correction) ? -R(params.max_linear_correction) : rhs;
+        }
+        if (!(rhs < R(0))) return;
+        const R r = inv_r != R(0) ? R(1) / inv_r : R(1);
+        const R impulse = -rhs * r;
+        if (b1.ndofs() != 0) {
+            for (int k = 0; k < 6; ++k) W1[k] = W1[k] * impulse;
+            apply_displacement(b1, v3<R>(W1[0], W1[1], W1[2]), v3<R>(W1[3], W1[4], W1[5]));
+        }
+        if (b2.ndofs() != 0) {
+            for (int k = 0; k < 6; ++k) W2[k] = W2[k] * impulse;
+            apply_displacement(b2, v3<R>(W2[0], W2[1], W2[2]), v3<R>(W2[3], W2[4], W2[5]));
+        }
+    }
+
+    // The position constraints of joint j (NonlinearSORProx::solve_generator,
+    // nonlinear_sor_prox.rs:57-76): FixedConstraint::position_constraint
+    // (fixed_constraint.rs:207-249) first cancels the frames' relative
+    // rotation (helper::cancel_relative_rotation, helper.rs:553-611); then,
+    // from the poses it left, both kinds cancel the anchors' separation
+    // (helper::cancel_relative_translation, helper.rs:364-418). Each is
+    // skipped below the allowed error (Unit::try_new_and_get).
+    void joint_position(uint32_t j) {
+        Joint<R>& jt = joints[j];
+        Body<R>& b1 = bodies[jt.b1];
+        Body<R>& b2 = bodies[jt.b2];
+        R J1[6], J2[6], W1[6], W2[6];
+        if (jt.kind == NPGPU_JOINT_FIXED) {
+            const Quat<R> r1 = qmul(b1.pos.q, jt.frame1), r2 = qmul(b2.pos.q, jt.frame2);
+            const V3<R> err = qscaled_axis(qmul(r2, qconj(r1)));
+            const R sq = dot(err, err);
+            const R eps = R(params.allowed_angular_error);
+            if (sq > eps * eps) {
+                const R depth = std::sqrt(sq);
+                const V3<R> dir = vdiv(err, depth);
+                R inv_r = R(0), dummy = R(0);
+                if (b1.ndofs() != 0) fill_torque(b1, dir, J1, W1, inv_r, dummy, false);
+                if (b2.ndofs() != 0) fill_torque(b2, -dir, J2, W2, inv_r, dummy, false);
+                generic_position_row(depth, true, inv_r, b1, b2, W1, W2);
+            }
+        }
+        const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
+        const V3<R> err = a2 - a1;
+        const R sq = dot(err, err);
+        const R eps = R(params.allowed_linear_error);
+        if (sq > eps * eps) {
+            const R depth = std::sqrt(sq);
+            const V3<R> dir = vdiv(err, depth);
+            R inv_r = R(0), dummy = R(0);
+            if (b1.ndofs() != 0) fill(b1, a1, dir, J1, W1, inv_r, dummy, false);
+            if (b2.ndofs() != 0) fill(b2, a2, -dir, J2, W2, inv_r, dummy, false);
+            generic_position_row(depth, false, inv_r, b1, b2, W1, W2);
+        }
     }
 
     // NonlinearSORProx::solve_unilateral + update_contact_constraint
     // (nonlinear_sor_prox.rs:121-294).
     void solve_position(const PosConstraint<R>& pc) {
+        if (pc.joint >= 0) {
+            joint_position(uint32_t(pc.joint));
+            return;
+        }
         const Collider<R>& c1 = colliders[pc.c1];
         const Collider<R>& c2 = colliders[pc.c2];
         Body<R>& b1 = bodies[c1.body];

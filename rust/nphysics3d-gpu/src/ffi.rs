@@ -67,6 +67,32 @@ pub struct npgpu_collider_desc {
     pub ccd_enabled: u32,
 }
 
+pub const NPGPU_JOINT_BALL: u32 = 0;
+pub const NPGPU_JOINT_FIXED: u32 = 1;
+
+#[repr(C)]
+#[derive(Copy, Clone, Default)]
+pub struct npgpu_joint_desc {
+    pub kind: u32,
+    pub pad: u32,
+    pub body1: npgpu_handle,
+    pub body2: npgpu_handle,
+    pub anchor1: [f32; 3],
+    pub anchor2: [f32; 3],
+    pub frame1: [f32; 4],
+    pub frame2: [f32; 4],
+    pub break_force: f32,
+    pub break_torque: f32,
+}
+
+#[repr(C)]
+#[derive(Copy, Clone, Default)]
+pub struct npgpu_joint_state {
+    pub impulses: [f32; 6],
+    pub broken: u32,
+    pub active: u32,
+}
+
 #[repr(C)]
 #[derive(Copy, Clone, Default)]
 pub struct npgpu_params {
@@ -186,6 +212,11 @@ extern "C" {
     pub fn npgpu_remove_colliders(w: *mut npgpu_world, n: u32, h: *const npgpu_handle) -> c_int;
     pub fn npgpu_apply_forces(w: *mut npgpu_world, n: u32, h: *const npgpu_handle, f: *const f32,
                               wake: c_int) -> c_int;
+    pub fn npgpu_upsert_joints(w: *mut npgpu_world, n: u32, h: *const npgpu_handle,
+                               d: *const npgpu_joint_desc) -> c_int;
+    pub fn npgpu_remove_joints(w: *mut npgpu_world, n: u32, h: *const npgpu_handle) -> c_int;
+    pub fn npgpu_get_joints(w: *mut npgpu_world, n: u32, h: *const npgpu_handle,
+                            out: *mut npgpu_joint_state) -> c_int;
     pub fn npgpu_step(w: *mut npgpu_world, nsteps: u32, num_joints: u32, num_forces: u32) -> c_int;
     pub fn npgpu_synchronize(w: *mut npgpu_world) -> c_int;
     pub fn npgpu_autotune(w: *mut npgpu_world, steps_per_candidate: u32, schedule: *mut u32,

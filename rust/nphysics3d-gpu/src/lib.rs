@@ -8,23 +8,27 @@
 //! and writes the new poses, velocities and activation back into the set, as
 //! `MechanicalWorld::step` leaves them. Scenes the GPU step does not support
 //! (multibodies, FEM or mass-spring bodies, shapes other than balls,
-//! cuboids and capsules, sensors, CCD colliders, joints, force generators) make `step`
-//! panic with the library's message, where nphysics would have run them.
-//! Balls, cuboids and capsules are supported.
+//! cuboids and capsules, sensors, CCD colliders, joints other than ball and
+//! fixed joints, force generators) make `step` panic with the library's
+//! message, where nphysics would have run them. Balls, cuboids and capsules
+//! are supported; ball and fixed joints go in as `GpuJoint`s.
 pub mod ffi;
 
 use std::collections::HashMap;
 use std::ffi::CStr;
 
 use generational_arena::Index;
-use nalgebra::{Isometry3, Quaternion, Translation3, UnitQuaternion, Vector3};
+use nalgebra::{DVector, Isometry3, Point3, Quaternion, Translation3, UnitQuaternion, Vector3};
 use ncollide3d::shape::{Ball, Capsule, Cuboid};
 use nphysics3d::algebra::{Force3, ForceType, Velocity3};
 use nphysics3d::force_generator::ForceGeneratorSet;
-use nphysics3d::joint::JointConstraintSet;
+use nphysics3d::joint::{BallConstraint, DefaultJointConstraintHandle, FixedConstraint, JointConstraint,
+                        JointConstraintSet};
 use nphysics3d::material::{BasicMaterial, MaterialCombineMode};
-use nphysics3d::object::{Body, BodySet, BodyStatus, Collider, ColliderSet, DefaultBodyHandle,
+use nphysics3d::object::{Body, BodyPartHandle, BodySet, BodyStatus, Collider, ColliderSet, DefaultBodyHandle,
                          DefaultColliderHandle, Ground, RigidBody};
+use nphysics3d::solver::{GenericNonlinearConstraint, IntegrationParameters, LinearConstraints,
+                         NonlinearConstraintGenerator};
 use nphysics3d::world::GeometricalWorld;
 
 fn handle(i: Index) -> ffi::npgpu_handle {
@@ -145,8 +149,118 @@ fn collider_desc(c: &Collider<f32, DefaultBodyHandle>) -> ffi::npgpu_collider_de
     d
 }
 
+/// A ball or fixed joint the GPU world can forward. nphysics keeps a
+/// BallConstraint's and a FixedConstraint's anchors and frames private, so
+/// this type builds the reference's constraint and records its description
+/// beside it; it implements JointConstraint by delegating to that constraint,
+/// so the same set still steps on the CPU. Insert it into a
+/// DefaultJointConstraintSet as usual.
+pub struct GpuJoint {
+    inner: Box<dyn JointConstraint<f32, DefaultBodyHandle>>,
+    desc: ffi::npgpu_joint_desc,
+    gpu: ffi::npgpu_joint_state,
+}
+
+fn quat4(q: &UnitQuaternion<f32>) -> [f32; 4] {
+    let c = q.quaternion().coords; // (i, j, k, w)
+    [c.x, c.y, c.z, c.w]
+}
+
+impl GpuJoint {
+    /// BallConstraint::new (src/joint/ball_constraint.rs:26-48).
+    pub fn ball(b1: BodyPartHandle<DefaultBodyHandle>, b2: BodyPartHandle<DefaultBodyHandle>, anchor1: Point3<f32>,
+                anchor2: Point3<f32>) -> Self {
+        let mut desc = ffi::npgpu_joint_desc::default();
+        desc.kind = ffi::NPGPU_JOINT_BALL;
+        desc.body1 = handle(b1.0);
+        desc.body2 = handle(b2.0);
+        desc.anchor1 = [anchor1.x, anchor1.y, anchor1.z];
+        desc.anchor2 = [anchor2.x, anchor2.y, anchor2.z];
+        desc.frame1 = [0.0, 0.0, 0.0, 1.0];
+        desc.frame2 = [0.0, 0.0, 0.0, 1.0];
+        desc.break_force = f32::MAX;
+        desc.break_torque = f32::MAX;
+        GpuJoint { inner: Box::new(BallConstraint::new(b1, b2, anchor1, anchor2)), desc,
+                   gpu: ffi::npgpu_joint_state::default() }
+    }
+
+    /// FixedConstraint::new (src/joint/fixed_constraint.rs:35-58).
+    pub fn fixed(b1: BodyPartHandle<DefaultBodyHandle>, b2: BodyPartHandle<DefaultBodyHandle>, anchor1: Point3<f32>,
+                 ref_frame1: UnitQuaternion<f32>, anchor2: Point3<f32>, ref_frame2: UnitQuaternion<f32>) -> Self {
+        let mut desc = ffi::npgpu_joint_desc::default();
+        desc.kind = ffi::NPGPU_JOINT_FIXED;
+        desc.body1 = handle(b1.0);
+        desc.body2 = handle(b2.0);
+        desc.anchor1 = [anchor1.x, anchor1.y, anchor1.z];
+        desc.anchor2 = [anchor2.x, anchor2.y, anchor2.z];
+        desc.frame1 = quat4(&ref_frame1);
+        desc.frame2 = quat4(&ref_frame2);
+        desc.break_force = f32::MAX;
+        desc.break_torque = f32::MAX;
+        GpuJoint { inner: Box::new(FixedConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)), desc,
+                   gpu: ffi::npgpu_joint_state::default() }
+    }
+
+    /// set_break_force of either constraint.
+    pub fn set_break_force(&mut self, f: f32) {
+        self.desc.break_force = f;
+        if let Some(b) = self.inner.downcast_mut::<BallConstraint<f32, DefaultBodyHandle>>() {
+            b.set_break_force(f);
+        } else if let Some(x) = self.inner.downcast_mut::<FixedConstraint<f32, DefaultBodyHandle>>() {
+            x.set_break_force(f);
+        }
+    }
+
+    /// FixedConstraint::set_break_torque.
+    pub fn set_break_torque(&mut self, t: f32) {
+        self.desc.break_torque = t;
+        if let Some(x) = self.inner.downcast_mut::<FixedConstraint<f32, DefaultBodyHandle>>() {
+            x.set_break_torque(t);
+        }
+    }
+
+    /// The impulses the GPU step cached for this joint (linear x, y, z, then
+    /// angular x, y, z for a fixed joint).
+    pub fn impulses(&self) -> [f32; 6] {
+        self.gpu.impulses
+    }
+}
+
+impl NonlinearConstraintGenerator<f32, DefaultBodyHandle> for GpuJoint {
+    fn num_position_constraints(&self, bodies: &dyn BodySet<f32, Handle = DefaultBodyHandle>) -> usize {
+        self.inner.num_position_constraints(bodies)
+    }
+    fn position_constraint(&self, parameters: &IntegrationParameters<f32>, i: usize,
+                           bodies: &mut dyn BodySet<f32, Handle = DefaultBodyHandle>, jacobians: &mut [f32])
+                           -> Option<GenericNonlinearConstraint<f32, DefaultBodyHandle>> {
+        self.inner.position_constraint(parameters, i, bodies, jacobians)
+    }
+}
+
+impl JointConstraint<f32, DefaultBodyHandle> for GpuJoint {
+    fn num_velocity_constraints(&self) -> usize {
+        self.inner.num_velocity_constraints()
+    }
+    fn anchors(&self) -> (BodyPartHandle<DefaultBodyHandle>, BodyPartHandle<DefaultBodyHandle>) {
+        self.inner.anchors()
+    }
+    fn velocity_constraints(&mut self, parameters: &IntegrationParameters<f32>,
+                            bodies: &dyn BodySet<f32, Handle = DefaultBodyHandle>, ext_vels: &DVector<f32>,
+                            ground_j_id: &mut usize, j_id: &mut usize, jacobians: &mut [f32],
+                            velocity_constraints: &mut LinearConstraints<f32, usize>) {
+        self.inner.velocity_constraints(parameters, bodies, ext_vels, ground_j_id, j_id, jacobians,
+                                        velocity_constraints)
+    }
+    fn cache_impulses(&mut self, constraints: &LinearConstraints<f32, usize>, inv_dt: f32) {
+        self.inner.cache_impulses(constraints, inv_dt)
+    }
+    fn is_broken(&self) -> bool {
+        self.gpu.broken != 0 || self.inner.is_broken()
+    }
+}
+
 /// Number of elements of a joint or force-generator set (they have no `len`).
-fn count_joints<C: JointConstraintSet<f32, DefaultBodyHandle>>(set: &C) -> u32 {
+fn count_joints<C: JointConstraintSet<f32, DefaultBodyHandle, Handle = DefaultJointConstraintHandle>>(set: &C) -> u32 {
     let mut n = 0u32;
     set.foreach(|_, _| n += 1);
     n
@@ -162,9 +276,10 @@ pub struct GpuMechanicalWorld {
     raw: *mut ffi::npgpu_world,
     /// IntegrationParameters (npgpu_default_params = IntegrationParameters::default()).
     pub integration_parameters: ffi::npgpu_params,
-    /// Body and collider slots the device holds, with their generation.
+    /// Body, collider and joint slots the device holds, with their generation.
     bodies_on_device: HashMap<u64, u64>,
     colliders_on_device: HashMap<u64, u64>,
+    joints_on_device: HashMap<u64, u64>,
     /// Scratch arrays of the per-step exchange, reused across steps.
     upserts: (Vec<ffi::npgpu_handle>, Vec<ffi::npgpu_body_desc>),
     forces: (Vec<ffi::npgpu_handle>, Vec<f32>),
@@ -190,6 +305,7 @@ impl GpuMechanicalWorld {
             integration_parameters: p,
             bodies_on_device: HashMap::new(),
             colliders_on_device: HashMap::new(),
+            joints_on_device: HashMap::new(),
             upserts: (Vec::new(), Vec::new()),
             forces: (Vec::new(), Vec::new()),
             poses: Vec::new(),
@@ -209,15 +325,74 @@ impl GpuMechanicalWorld {
     ) where
         Bodies: BodySet<f32, Handle = DefaultBodyHandle>,
         Colliders: ColliderSet<f32, DefaultBodyHandle, Handle = DefaultColliderHandle>,
-        Constraints: JointConstraintSet<f32, DefaultBodyHandle>,
+        Constraints: JointConstraintSet<f32, DefaultBodyHandle, Handle = DefaultJointConstraintHandle>,
         Forces: ForceGeneratorSet<f32, DefaultBodyHandle>,
     {
         assert_ok(unsafe { ffi::npgpu_set_params(self.raw, &self.integration_parameters) }, self.raw);
         self.forward_events(bodies, colliders);
+        self.forward_joints(constraints);
         let (nj, nf) = (count_joints(constraints), count_forces(forces));
         assert_ok(unsafe { ffi::npgpu_step(self.raw, 1, nj, nf) }, self.raw);
         assert_ok(unsafe { ffi::npgpu_synchronize(self.raw) }, self.raw);
         self.write_back_poses(bodies);
+        self.write_back_joints(constraints);
+    }
+
+    /// The joint set's removals and insertions (mechanical_world.rs:156-175).
+    /// A joint that is not a GpuJoint goes in as an unknown kind, which the
+    /// library rejects.
+    fn forward_joints<Constraints>(&mut self, constraints: &mut Constraints)
+    where
+        Constraints: JointConstraintSet<f32, DefaultBodyHandle, Handle = DefaultJointConstraintHandle>,
+    {
+        let mut removed = Vec::new();
+        while let Some((h, _, _)) = constraints.pop_removal_event() {
+            if self.joints_on_device.remove(&(h.into_raw_parts().0 as u64)).is_some() {
+                removed.push(handle(h));
+            }
+        }
+        if !removed.is_empty() {
+            let st = unsafe { ffi::npgpu_remove_joints(self.raw, removed.len() as u32, removed.as_ptr()) };
+            assert_ok(st, self.raw);
+        }
+        let (mut jh, mut jd) = (Vec::new(), Vec::new());
+        while let Some((h, _, _)) = constraints.pop_insertion_event() {
+            if let Some(j) = constraints.get(h) {
+                let desc = match j.downcast_ref::<GpuJoint>() {
+                    Some(g) => g.desc,
+                    None => ffi::npgpu_joint_desc { kind: u32::MAX, ..Default::default() },
+                };
+                jh.push(handle(h));
+                jd.push(desc);
+                let (index, generation) = h.into_raw_parts();
+                self.joints_on_device.insert(index as u64, generation);
+            }
+        }
+        if !jh.is_empty() {
+            let st = unsafe { ffi::npgpu_upsert_joints(self.raw, jh.len() as u32, jh.as_ptr(), jd.as_ptr()) };
+            assert_ok(st, self.raw);
+        }
+    }
+
+    /// JointConstraint::cache_impulses / is_broken as the step left them.
+    fn write_back_joints<Constraints>(&mut self, constraints: &mut Constraints)
+    where
+        Constraints: JointConstraintSet<f32, DefaultBodyHandle, Handle = DefaultJointConstraintHandle>,
+    {
+        let mut hs = Vec::new();
+        constraints.foreach(|h, _| hs.push(h));
+        if hs.is_empty() {
+            return;
+        }
+        let raw: Vec<ffi::npgpu_handle> = hs.iter().map(|h| handle(*h)).collect();
+        let mut st = vec![ffi::npgpu_joint_state::default(); raw.len()];
+        assert_ok(unsafe { ffi::npgpu_get_joints(self.raw, raw.len() as u32, raw.as_ptr(), st.as_mut_ptr()) },
+                  self.raw);
+        for (h, s) in hs.iter().zip(st.iter()) {
+            if let Some(g) = constraints.get_mut(*h).and_then(|j| j.downcast_mut::<GpuJoint>()) {
+                g.gpu = *s;
+            }
+        }
     }
 
     /// MechanicalWorld::maintain (mechanical_world.rs:114-179) as the device
