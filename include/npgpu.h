@@ -144,16 +144,30 @@ typedef struct npgpu_collider_desc {
     uint32_t ccd_enabled;       /* rejected when non-zero: CCD is not built */
 } npgpu_collider_desc;
 
-/* Joint constraints (src/joint/): BallConstraint (ball_constraint.rs:13-178)
- * keeps anchor1 and anchor2 together; FixedConstraint (fixed_constraint.rs)
- * also keeps the frames (body rotation x reference frame) aligned. */
+/* Joint constraints (src/joint/), the ones made of unlimited bilateral
+ * rows: BallConstraint (ball_constraint.rs) keeps anchor1 and anchor2
+ * together; FixedConstraint (fixed_constraint.rs) also keeps the frames
+ * (body rotation x reference frame) aligned; RevoluteConstraint
+ * (revolute_constraint.rs) keeps the anchors together and axis1, axis2
+ * aligned; CartesianConstraint (cartesian_constraint.rs) keeps only the
+ * frames aligned; PlanarConstraint (planar_constraint.rs) keeps anchor2 in
+ * the plane through anchor1 normal to axis1 and the axes aligned;
+ * RectangularConstraint (rectangular_constraint.rs) keeps anchor2 in that
+ * plane and the bodies' rotations equal; UniversalConstraint
+ * (universal_constraint.rs) keeps the anchors together and the angle between
+ * the axes. */
 enum {
     NPGPU_JOINT_BALL = 0,
-    NPGPU_JOINT_FIXED = 1
+    NPGPU_JOINT_FIXED = 1,
+    NPGPU_JOINT_REVOLUTE = 2,
+    NPGPU_JOINT_CARTESIAN = 3,
+    NPGPU_JOINT_PLANAR = 4,
+    NPGPU_JOINT_RECTANGULAR = 5,
+    NPGPU_JOINT_UNIVERSAL = 6
 };
 
-/* One joint constraint as BallConstraint::new / FixedConstraint::new build it.
- * Both bodies must belong to the same world, and body1 != body2. */
+/* One joint constraint as its ::new builds it. Both bodies must belong to
+ * the same world, and body1 != body2. */
 typedef struct npgpu_joint_desc {
     uint32_t kind;              /* NPGPU_JOINT_* */
     uint32_t pad;
@@ -161,15 +175,19 @@ typedef struct npgpu_joint_desc {
     npgpu_handle body2;
     float anchor1[3];           /* in body 1's local frame */
     float anchor2[3];           /* in body 2's local frame */
-    float frame1[4];            /* FIXED: ref_frame1, a unit quaternion (i, j, k, w) */
-    float frame2[4];            /* FIXED: ref_frame2 */
+    float frame1[4];            /* FIXED, CARTESIAN: ref_frame1, a unit quaternion (i, j, k, w) */
+    float frame2[4];            /* FIXED, CARTESIAN: ref_frame2 */
     float break_force;          /* set_break_force; FLT_MAX (the default) never breaks */
-    float break_torque;         /* FIXED: set_break_torque */
+    float break_torque;         /* set_break_torque */
+    float axis1[3];             /* REVOLUTE, PLANAR, RECTANGULAR, UNIVERSAL: unit axis in body 1's frame */
+    float axis2[3];             /* REVOLUTE, PLANAR, UNIVERSAL: unit axis in body 2's frame */
+    float angle;                /* UNIVERSAL: the angle kept between the axes */
+    uint32_t pad2;
 } npgpu_joint_desc;
 
 /* A joint's state after the last step: the impulses JointConstraint::
- * cache_impulses keeps (linear x y z, then angular x y z for FIXED) and
- * is_broken(). */
+ * cache_impulses keeps (linear, then angular: x y z for a canonical-axis
+ * row group, the rows in their order otherwise) and is_broken(). */
 typedef struct npgpu_joint_state {
     float impulses[6];
     uint32_t broken;
@@ -340,8 +358,8 @@ npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
 npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* handles,
                                 const float* forces6, int auto_wake_up);
 
-/* DefaultJointConstraintSet::insert (joint_constraint.rs:54-72) of BallConstraint
- * and FixedConstraint, with the handles the host set gave them; inserting
+/* DefaultJointConstraintSet::insert (joint_constraint.rs:54-72) of the joints
+ * above, with the handles the host set gave them; inserting
  * wakes both bodies up at the next step (mechanical_world.rs:167-175). A
  * joint's impulses start at zero and persist across steps. The solver holds
  * the active joints beside the contact manifolds: capacity_pairs bounds the

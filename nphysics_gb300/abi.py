@@ -94,8 +94,9 @@ class ColliderDesc(C.Structure):
     ]
 
 
-# Joint kinds (BallConstraint, FixedConstraint)
-JOINT_BALL, JOINT_FIXED = 0, 1
+# Joint kinds (BallConstraint, FixedConstraint, RevoluteConstraint, CartesianConstraint,
+# PlanarConstraint, RectangularConstraint, UniversalConstraint)
+JOINT_BALL, JOINT_FIXED, JOINT_REVOLUTE, JOINT_CARTESIAN, JOINT_PLANAR, JOINT_RECTANGULAR, JOINT_UNIVERSAL = range(7)
 
 
 class JointDesc(C.Structure):
@@ -110,6 +111,10 @@ class JointDesc(C.Structure):
         ("frame2", C.c_float * 4),
         ("break_force", C.c_float),
         ("break_torque", C.c_float),
+        ("axis1", C.c_float * 3),
+        ("axis2", C.c_float * 3),
+        ("angle", C.c_float),
+        ("pad2", C.c_uint32),
     ]
 
 
@@ -118,9 +123,9 @@ class JointState(C.Structure):
 
 
 def joint_desc(kind, body1, body2, anchor1=(0, 0, 0), anchor2=(0, 0, 0), frame1=(0, 0, 0, 1), frame2=(0, 0, 0, 1),
-               break_force=None, break_torque=None):
-    """A JointDesc as BallConstraint::new / FixedConstraint::new build it
-    (body handles as (index, generation) pairs or Handle)."""
+               break_force=None, break_torque=None, axis1=(1, 0, 0), axis2=(1, 0, 0), angle=0.0):
+    """A JointDesc as the joint kind's ::new builds it (body handles as
+    (index, generation) pairs or Handle)."""
     d = JointDesc()
     d.kind = kind
     for f, h in (("body1", body1), ("body2", body2)):
@@ -132,6 +137,9 @@ def joint_desc(kind, body1, body2, anchor1=(0, 0, 0), anchor2=(0, 0, 0), frame1=
     d.frame2[:] = [float(x) for x in frame2]
     d.break_force = FLT_MAX if break_force is None else break_force
     d.break_torque = FLT_MAX if break_torque is None else break_torque
+    d.axis1[:] = [float(x) for x in axis1]
+    d.axis2[:] = [float(x) for x in axis2]
+    d.angle = float(angle)
     return d
 
 

@@ -420,63 +420,39 @@ private:
 // The collision state lives on the device; this type exists for the signature.
 class DefaultGeometricalWorld {};
 
-// BallConstraint::new(b1, b2, anchor1, anchor2) (src/joint/ball_constraint.rs:26-48):
-// keeps the two anchors (in their bodies' frames) together.
-class BallConstraint {
+// What every joint constraint below keeps: its description, and the state
+// the GPU step leaves (JointConstraint::is_broken, the cached impulses).
+class JointConstraintBase {
 public:
-    BallConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 anchor2) {
-        std::memset(&desc, 0, sizeof(desc));
-        desc.kind = NPGPU_JOINT_BALL;
-        desc.body1 = b1.body.raw();
-        desc.body2 = b2.body.raw();
-        set(desc.anchor1, anchor1);
-        set(desc.anchor2, anchor2);
-        desc.frame1[3] = desc.frame2[3] = 1.0f;
-        desc.break_force = desc.break_torque = std::numeric_limits<float>::max();
-    }
     void set_break_force(float f) { desc.break_force = f; }
+    void set_break_torque(float t) { desc.break_torque = t; }
     bool is_broken() const { return broken_; }
-    // The impulses cache_impulses kept in the last step (linear x, y, z).
+    // The impulses cache_impulses kept in the last step: linear, then angular.
     const float* impulses() const { return impulses_; }
     npgpu_joint_desc desc;
 
-private:
-    friend class GpuMechanicalWorld;
-    static void set(float* o, Vector3 v) {
+protected:
+    JointConstraintBase(uint32_t kind, BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 anchor2) {
+        std::memset(&desc, 0, sizeof(desc));
+        desc.kind = kind;
+        desc.body1 = b1.body.raw();
+        desc.body2 = b2.body.raw();
+        set3(desc.anchor1, anchor1);
+        set3(desc.anchor2, anchor2);
+        desc.frame1[3] = desc.frame2[3] = 1.0f;
+        desc.axis1[0] = desc.axis2[0] = 1.0f;
+        desc.break_force = desc.break_torque = std::numeric_limits<float>::max();
+    }
+    static void set3(float* o, Vector3 v) {
         o[0] = v.x;
         o[1] = v.y;
         o[2] = v.z;
     }
-    bool broken_ = false;
-    float impulses_[6] = {0, 0, 0, 0, 0, 0};
-};
-
-// FixedConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)
-// (src/joint/fixed_constraint.rs:29-58): also keeps the frames (body rotation
-// times reference frame) aligned. The reference frames are given as scaled
-// axes (UnitQuaternion::from_scaled_axis).
-class FixedConstraint {
-public:
-    FixedConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 ref_frame1, Vector3 anchor2,
-                    Vector3 ref_frame2) {
-        std::memset(&desc, 0, sizeof(desc));
-        desc.kind = NPGPU_JOINT_FIXED;
-        desc.body1 = b1.body.raw();
-        desc.body2 = b2.body.raw();
-        const float a1[3] = {anchor1.x, anchor1.y, anchor1.z}, a2[3] = {anchor2.x, anchor2.y, anchor2.z};
-        std::memcpy(desc.anchor1, a1, sizeof(a1));
-        std::memcpy(desc.anchor2, a2, sizeof(a2));
-        Isometry3 f1 = Isometry3::new_({}, ref_frame1), f2 = Isometry3::new_({}, ref_frame2);
-        std::memcpy(desc.frame1, f1.rotation, sizeof(desc.frame1));
-        std::memcpy(desc.frame2, f2.rotation, sizeof(desc.frame2));
-        desc.break_force = desc.break_torque = std::numeric_limits<float>::max();
+    // UnitQuaternion::from_scaled_axis.
+    static void set_frame(float* o, Vector3 scaled_axis) {
+        Isometry3 f = Isometry3::new_({}, scaled_axis);
+        std::memcpy(o, f.rotation, 4 * sizeof(float));
     }
-    void set_break_force(float f) { desc.break_force = f; }
-    void set_break_torque(float t) { desc.break_torque = t; }
-    bool is_broken() const { return broken_; }
-    // Linear x, y, z then angular x, y, z.
-    const float* impulses() const { return impulses_; }
-    npgpu_joint_desc desc;
 
 private:
     friend class GpuMechanicalWorld;
@@ -484,7 +460,88 @@ private:
     float impulses_[6] = {0, 0, 0, 0, 0, 0};
 };
 
-using JointConstraint = std::variant<BallConstraint, FixedConstraint>;
+// BallConstraint::new(b1, b2, anchor1, anchor2) (src/joint/ball_constraint.rs:26-48):
+// keeps the two anchors (in their bodies' frames) together.
+class BallConstraint : public JointConstraintBase {
+public:
+    BallConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 anchor2)
+        : JointConstraintBase(NPGPU_JOINT_BALL, b1, b2, anchor1, anchor2) {}
+};
+
+// FixedConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)
+// (src/joint/fixed_constraint.rs:35-58): also keeps the frames (body rotation
+// times reference frame) aligned. Reference frames are scaled axes.
+class FixedConstraint : public JointConstraintBase {
+public:
+    FixedConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 ref_frame1, Vector3 anchor2,
+                    Vector3 ref_frame2)
+        : JointConstraintBase(NPGPU_JOINT_FIXED, b1, b2, anchor1, anchor2) {
+        set_frame(desc.frame1, ref_frame1);
+        set_frame(desc.frame2, ref_frame2);
+    }
+};
+
+// RevoluteConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2)
+// (src/joint/revolute_constraint.rs:52-80): a hinge about axis1 = axis2.
+class RevoluteConstraint : public JointConstraintBase {
+public:
+    RevoluteConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis1, Vector3 anchor2,
+                       Vector3 axis2)
+        : JointConstraintBase(NPGPU_JOINT_REVOLUTE, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis1);
+        set3(desc.axis2, axis2);
+    }
+};
+
+// CartesianConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2):
+// keeps the frames aligned, the translation free.
+class CartesianConstraint : public JointConstraintBase {
+public:
+    CartesianConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 ref_frame1, Vector3 anchor2,
+                        Vector3 ref_frame2)
+        : JointConstraintBase(NPGPU_JOINT_CARTESIAN, b1, b2, anchor1, anchor2) {
+        set_frame(desc.frame1, ref_frame1);
+        set_frame(desc.frame2, ref_frame2);
+    }
+};
+
+// PlanarConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2): anchor2 in
+// the plane through anchor1 normal to axis1, the axes aligned.
+class PlanarConstraint : public JointConstraintBase {
+public:
+    PlanarConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis1, Vector3 anchor2,
+                     Vector3 axis2)
+        : JointConstraintBase(NPGPU_JOINT_PLANAR, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis1);
+        set3(desc.axis2, axis2);
+    }
+};
+
+// RectangularConstraint::new(b1, b2, anchor1, axis1, anchor2): anchor2 in
+// that plane, the rotations equal.
+class RectangularConstraint : public JointConstraintBase {
+public:
+    RectangularConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis1, Vector3 anchor2)
+        : JointConstraintBase(NPGPU_JOINT_RECTANGULAR, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis1);
+    }
+};
+
+// UniversalConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2, angle):
+// the anchors together, the angle between the axes kept.
+class UniversalConstraint : public JointConstraintBase {
+public:
+    UniversalConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis1, Vector3 anchor2,
+                        Vector3 axis2, float angle)
+        : JointConstraintBase(NPGPU_JOINT_UNIVERSAL, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis1);
+        set3(desc.axis2, axis2);
+        desc.angle = angle;
+    }
+};
+
+using JointConstraint = std::variant<BallConstraint, FixedConstraint, RevoluteConstraint, CartesianConstraint,
+                                     PlanarConstraint, RectangularConstraint, UniversalConstraint>;
 using DefaultJointConstraintHandle = Index;
 
 // DefaultJointConstraintSet (src/joint/joint_constraint.rs:31-130): the
@@ -643,8 +700,9 @@ private:
         for (size_t k = 0; k < h.size(); ++k) {
             JointConstraint* c = joints.arena_.get(Index{h[k].index, h[k].generation});
             std::visit([&](auto& x) {
-                x.broken_ = st[k].broken != 0;
-                std::memcpy(x.impulses_, st[k].impulses, sizeof(x.impulses_));
+                JointConstraintBase& jb = x;
+                jb.broken_ = st[k].broken != 0;
+                std::memcpy(jb.impulses_, st[k].impulses, sizeof(jb.impulses_));
             }, *c);
         }
     }

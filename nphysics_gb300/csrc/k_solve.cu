@@ -342,6 +342,15 @@ __device__ __forceinline__ np::V basis_axis(int r) {
     return np::mk(r == 0 ? 1.0f : 0.0f, r == 1 ? 1.0f : 0.0f, r == 2 ? 1.0f : 0.0f);
 }
 
+// Unit::try_new_and_get(v, eps): v / |v| when |v|^2 > eps^2.
+__device__ __forceinline__ bool unit_try(np::V v, float eps, np::V& u, float& n) {
+    const float sq = np::dot(v, v);
+    if (!(sq > eps * eps)) return false;
+    n = sqrtf(sq);
+    u = np::divs(v, n);
+    return true;
+}
+
 // nalgebra Vector3::orthonormal_subspace_basis of one vector.
 __device__ __forceinline__ void tangent_basis(np::V n, np::V& t1, np::V& t2) {
     np::V a;
@@ -412,11 +421,9 @@ __device__ __forceinline__ void side_axpy(np::V pos, np::V dir, uint32_t m6, con
     side_axpy_j(J, sb, a, dv);
 }
 
-// The Jacobian of one side of a joint row: row r of the linear triple (a
-// force along +-e_r at the anchor, lever arm pos) or of the angular triple
-// (a torque about +-e_r); side 2 takes the negated direction.
-__device__ __forceinline__ void joint_side_j(bool angular, int r, np::V pos, bool side2, uint32_t m6, float* J) {
-    np::V e = basis_axis(r);
+// The Jacobian of one side of a joint row: a force along +-e at the anchor
+// (lever arm pos) or a torque about +-e; side 2 takes the negated direction.
+__device__ __forceinline__ void joint_side_j(bool angular, np::V e, np::V pos, bool side2, uint32_t m6, float* J) {
     if (side2) e = np::neg(e);
     if (angular) {
         const float f[6] = {0.0f, 0.0f, 0.0f, e.x, e.y, e.z};
@@ -817,7 +824,7 @@ __global__ void k_collect_joints(World w) {
                     w.s.sm_list[m] = kJointBit | jj;
                     w.s.sm_b1[m] = s1 == 2u ? (int)b1 : -1;
                     w.s.sm_b2[m] = s2 == 2u ? (int)b2 : -1;
-                    w.s.sm_nc[m] = (ji & JI_KIND_MASK) == NPGPU_JOINT_FIXED ? 2u : 1u;
+                    w.s.sm_nc[m] = joint_group_count(ji & JI_KIND_MASK);
                     if (s1 == 2u) atomicAdd(&b.adj_count[b1], 1u);
                     if (s2 == 2u) atomicAdd(&b.adj_count[b2], 1u);
                     st |= JS_ACTIVE;
@@ -974,14 +981,66 @@ __device__ __forceinline__ np::V body_point(np::V t, np::Q q, np::V local) {
 // schedule's iterations.
 #if !NPGPU_EXCHANGE_TU
 
-// The rows of active joint j as solver manifold m: BallConstraint /
-// FixedConstraint::velocity_constraints (ball_constraint.rs:80-127,
-// fixed_constraint.rs:107-172) through helper::cancel_relative_linear_velocity
-// and cancel_relative_angular_velocity (helper.rs:167-296, 422-551): one row
-// per axis e_x, e_y, e_z, each with the joint's cached impulse as its start
-// (no warm-start coefficient). The linear triple is record 0, the angular
-// triple (FixedConstraint) record 1.
-static __device__ void assemble_joint(const World& w, const StepParams& p, uint32_t m, uint32_t j, int b1, int b2, bool rows) {
+// A joint's row group: `rows` forces along (JR_LINEAR) or torques about
+// (JR_ANGULAR) the directions d, their impulses in the joint's slots
+// slot..slot + rows - 1 (0-2 linear, 3-5 angular).
+struct JointGroup {
+    uint32_t kind, rows, slot;
+    np::V d[3];
+};
+
+// The row groups of joint kind `kind` (at most two) with body rotations q1, q2
+// and local axes ax1, ax2, as each constraint's velocity_constraints builds
+// them (ball_constraint.rs:80-127, fixed_constraint.rs:107-172,
+// revolute_constraint.rs:181-266, cartesian_constraint.rs,
+// planar_constraint.rs, rectangular_constraint.rs, universal_constraint.rs)
+// from helper::cancel_relative_linear_velocity[_wrt_axis],
+// cancel_relative_angular_velocity[_wrt_axis] and
+// restrict_relative_angular_velocity_to_axis (helper.rs:167-296, 422-551,
+// 614-699); the subspace basis of an axis is the contact model's tangent basis.
+__device__ __forceinline__ uint32_t joint_groups(uint32_t kind, np::Q q1, np::Q q2, np::V ax1, np::V ax2,
+                                                 JointGroup* g) {
+    const np::V ex = basis_axis(0), ey = basis_axis(1), ez = basis_axis(2), zero = np::mk(0.0f, 0.0f, 0.0f);
+    const JointGroup lin3{JR_LINEAR, 3u, 0u, {ex, ey, ez}}, ang3{JR_ANGULAR, 3u, 3u, {ex, ey, ez}};
+    switch (kind) {
+    case NPGPU_JOINT_BALL: g[0] = lin3; return 1;
+    case NPGPU_JOINT_FIXED: g[0] = lin3; g[1] = ang3; return 2;
+    case NPGPU_JOINT_CARTESIAN: g[0] = ang3; return 1;
+    case NPGPU_JOINT_REVOLUTE: {
+        np::V t1, t2;
+        tangent_basis(np::qrot(q1, ax1), t1, t2);
+        g[0] = lin3;
+        g[1] = JointGroup{JR_ANGULAR, 2u, 3u, {t1, t2, zero}};
+        return 2;
+    }
+    case NPGPU_JOINT_PLANAR: {
+        const np::V a = np::qrot(q1, ax1);
+        np::V t1, t2;
+        tangent_basis(a, t1, t2);
+        g[0] = JointGroup{JR_LINEAR, 1u, 0u, {a, zero, zero}};
+        g[1] = JointGroup{JR_ANGULAR, 2u, 3u, {t1, t2, zero}};
+        return 2;
+    }
+    case NPGPU_JOINT_RECTANGULAR:
+        g[0] = JointGroup{JR_LINEAR, 1u, 0u, {np::qrot(q1, ax1), zero, zero}};
+        g[1] = ang3;
+        return 2;
+    default: {   // NPGPU_JOINT_UNIVERSAL
+        np::V o;
+        float n;
+        const bool has = unit_try(np::cross(np::qrot(q1, ax1), np::qrot(q2, ax2)), FLT_EPSILON, o, n);
+        g[0] = lin3;
+        g[1] = JointGroup{JR_ANGULAR, has ? 1u : 0u, 3u, {has ? o : zero, zero, zero}};
+        return 2;
+    }
+    }
+}
+
+// The rows of active joint j as solver manifold m: one record per row group,
+// the rows' directions in the normal and friction-direction slots, each row
+// started from the joint's cached impulse (no warm-start coefficient).
+static __device__ void assemble_joint(const World& w, const StepParams& p, uint32_t m, uint32_t j, int b1, int b2,
+                                      bool rows) {
     const Bodies& b = w.b;
     const uint32_t bb1 = w.j.body[2 * j], bb2 = w.j.body[2 * j + 1];
     const BodyView v1 = load_view(b, bb1), v2 = load_view(b, bb2);
@@ -989,29 +1048,42 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
     if (b1 >= 0) mask |= ~(bi_flags(v1.info) >> 1) & 0x3fu;
     if (b2 >= 0) mask |= (~(bi_flags(v2.info) >> 1) & 0x3fu) << 8;
     w.s.sm_mask[m] = mask;
-    const uint32_t nc = w.s.sm_nc[m];
-    const np::V a1 = body_point(v3(b.pos_t[bb1]), q4(b.pos_q[bb1]), v3(w.j.anchor[2 * j]));
-    const np::V a2 = body_point(v3(b.pos_t[bb2]), q4(b.pos_q[bb2]), v3(w.j.anchor[2 * j + 1]));
+    const np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
+    const np::V a1 = body_point(v3(b.pos_t[bb1]), q1, v3(w.j.anchor[2 * j]));
+    const np::V a2 = body_point(v3(b.pos_t[bb2]), q2, v3(w.j.anchor[2 * j + 1]));
+    JointGroup grp[2];
+    const uint32_t ng = joint_groups(w.j.info[j] & JI_KIND_MASK, q1, q2, v3(w.j.axis[2 * j]), v3(w.j.axis[2 * j + 1]), grp);
     float4* pr4 = w.s.pos_rec + (size_t)m * kPosRec;
     pr4[4] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kJointBit | j));
     pr4[6] = make_float4(__uint_as_float(bb1), __uint_as_float(bb2), __uint_as_float(v1.info), __uint_as_float(v2.info));
     float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
     float4* lam = w.s.lam + (size_t)m * kMaxContacts;
-    for (uint32_t k = 0; k < nc; ++k) {
-        const bool ang = k == 1u;
+    float4* tan = w.s.tan + (size_t)m * kMaxContacts * 2;
+    const float4 imp[2] = {w.j.imp[2 * j], w.j.imp[2 * j + 1]};
+    for (uint32_t k = 0; k < ng; ++k) {
+        const JointGroup& G = grp[k];
+        const bool ang = G.kind == JR_ANGULAR;
         float R[3][kRowFloats];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
-            if (ang) make_row_angular(R[r], v1, v2, basis_axis(r), p.dt);
-            else make_row(R[r], v1, v2, a1, a2, basis_axis(r), p.dt);
+            if ((uint32_t)r >= G.rows) {
+#pragma unroll
+                for (int e = 0; e < kRowFloats; ++e) R[r][e] = 0.0f;
+            } else if (ang) {
+                make_row_angular(R[r], v1, v2, G.d[r], p.dt);
+            } else {
+                make_row(R[r], v1, v2, a1, a2, G.d[r], p.dt);
+            }
         }
         const np::V zero = np::mk(0.0f, 0.0f, 0.0f);
         const np::V pos1 = ang ? zero : np::sub(a1, v1.com), pos2 = ang ? zero : np::sub(a2, v2.com);
-        const float kindf = ang ? kJointAngular : kJointLinear;
-        con[4 * k] = make_float4(0.0f, 0.0f, 0.0f, kindf);
+        const float code = joint_code(G.kind, G.rows);
+        con[4 * k] = make_float4(G.d[0].x, G.d[0].y, G.d[0].z, code);
         con[4 * k + 1] = make_float4(pos1.x, pos1.y, pos1.z, R[0][RF_R]);
         con[4 * k + 2] = make_float4(pos2.x, pos2.y, pos2.z, R[0][RF_RHS]);
         con[4 * k + 3] = make_float4(R[1][RF_R], R[1][RF_RHS], R[2][RF_R], R[2][RF_RHS]);
+        tan[2 * k] = make_float4(G.d[1].x, G.d[1].y, G.d[1].z, 0.0f);
+        tan[2 * k + 1] = make_float4(G.d[2].x, G.d[2].y, G.d[2].z, 0.0f);
         if (rows) {
             float4* ro = w.s.rows + ((size_t)m * kMaxContacts + k) * kRowsF4;
 #pragma unroll
@@ -1019,11 +1091,12 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
 #pragma unroll
                 for (int e = 0; e < 6; ++e)
                     ro[kRowF4 * r + e] = make_float4(R[r][4 * e], R[r][4 * e + 1], R[r][4 * e + 2], R[r][4 * e + 3]);
-                ro[kRowF4 * r + 6] = make_float4(R[r][RF_R], R[r][RF_RHS], kindf, 0.0f);
+                ro[kRowF4 * r + 6] = make_float4(R[r][RF_R], R[r][RF_RHS], code, 0.0f);
             }
         }
-        const float4 im = w.j.imp[2 * j + k];
-        lam[k] = make_float4(im.x, im.y, im.z, 0.0f);
+        const float4 im = imp[G.slot / 3u];
+        const float iv[3] = {im.x, im.y, im.z};
+        lam[k] = make_float4(G.rows > 0u ? iv[0] : 0.0f, G.rows > 1u ? iv[1] : 0.0f, G.rows > 2u ? iv[2] : 0.0f, 0.0f);
     }
 }
 
@@ -1327,11 +1400,12 @@ __device__ __forceinline__ void warm_rows(const RS& src, uint32_t nc, bool h1, b
 // A joint's three bilateral rows from stored rows (Independent limits of
 // +-FLT_MAX, helper.rs:186-189).
 template <class RS>
-__device__ __forceinline__ void joint_rows(const RS& src, uint32_t k, float4 l, bool h1, bool h2, DV& dv) {
+__device__ __forceinline__ void joint_rows(const RS& src, uint32_t k, float4 l, uint32_t rows, bool h1, bool h2,
+                                           DV& dv) {
     float li[3] = {l.x, l.y, l.z};
 #pragma unroll 1
-    for (int r = 0; r < 3; ++r) {
-        const RowRec R = src.row(k, r);
+    for (uint32_t r = 0; r < rows; ++r) {
+        const RowRec R = src.row(k, (int)r);
         float ni = li[r] - R.r * (row_dot(R, dv, h1, h2) + R.rhs);
         ni = ni < -FLT_MAX ? -FLT_MAX : (ni > FLT_MAX ? FLT_MAX : ni);
         const float dl = ni - li[r];
@@ -1347,7 +1421,7 @@ __device__ __forceinline__ void friction_rows(const RS& src, uint32_t nc, bool h
         const float4 l = src.get_lam(k);
         const RowRec R1 = src.row(k, 1);
         if (R1.mu < 0.0f) {
-            joint_rows(src, k, l, h1, h2, dv);
+            joint_rows(src, k, l, joint_rows_of(R1.mu), h1, h2, dv);
             continue;
         }
         const float li = l.x;
@@ -1414,13 +1488,17 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
             // Independent limits): warm-started, then solved once per
             // iteration with the friction rows.
             if (kind == SWEEP_NORMAL) continue;
-            const bool ang = c.mu == kJointAngular;
+            const bool ang = joint_angular(c.mu);
+            const uint32_t rows = joint_rows_of(c.mu);
             float li[3] = {l.x, l.y, l.z};
+            np::V d[3];
+            d[0] = c.n;
+            src.tangents(c, k, d + 1);
 #pragma unroll 1
-            for (int r = 0; r < 3; ++r) {
+            for (uint32_t r = 0; r < rows; ++r) {
                 float J1[6], J2[6];
-                if (h1) joint_side_j(ang, r, c.pos1, false, mask & 0x3fu, J1);
-                if (h2) joint_side_j(ang, r, c.pos2, true, (mask >> 8) & 0x3fu, J2);
+                if (h1) joint_side_j(ang, d[r], c.pos1, false, mask & 0x3fu, J1);
+                if (h2) joint_side_j(ang, d[r], c.pos2, true, (mask >> 8) & 0x3fu, J2);
                 float dl = li[r];
                 if (kind == SWEEP_WARM) {
                     if (li[r] == 0.0f) continue;
@@ -1615,13 +1693,16 @@ __device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, in
         const ContactRec c = load_con(con, k);
         float4 l = lam[k];
         if (c.mu < 0.0f) {
-            // A joint's three bilateral rows.
-            const bool ang = c.mu == kJointAngular;
+            // A joint's bilateral rows.
+            const bool ang = joint_angular(c.mu);
+            const uint32_t rows = joint_rows_of(c.mu);
             const float li[3] = {l.x, l.y, l.z};
-            for (int r = 0; r < 3; ++r) {
+            const float4 ta = w.s.tan[((size_t)m * kMaxContacts + k) * 2], tb = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
+            const np::V d[3] = {c.n, np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
+            for (uint32_t r = 0; r < rows; ++r) {
                 float J1[6], J2[6];
-                if (h1) joint_side_j(ang, r, c.pos1, false, mask & 0x3fu, J1);
-                if (h2) joint_side_j(ang, r, c.pos2, true, (mask >> 8) & 0x3fu, J2);
+                if (h1) joint_side_j(ang, d[r], c.pos1, false, mask & 0x3fu, J1);
+                if (h2) joint_side_j(ang, d[r], c.pos2, true, (mask >> 8) & 0x3fu, J2);
                 residual_row_j(J1, J2, c.r[r], c.rhs[r], li[r], dv, h1, h2, RES_BILATERAL, 0.0f, 0.0f, acc);
             }
             continue;
@@ -2157,6 +2238,27 @@ __device__ __forceinline__ void publish_posef(unsigned long long* pf, int b, uin
                      : "memory");
 }
 
+// JointConstraint::cache_impulses' break test of each kind, in its own
+// arithmetic: |linear|^2 / dt^2 against the squared break force, |angular|^2
+// / dt^2 against the squared break torque (ball_constraint.rs:129-141,
+// fixed_constraint.rs:174-199, revolute_constraint.rs:268-292,
+// cartesian_constraint.rs, planar_constraint.rs, rectangular_constraint.rs,
+// universal_constraint.rs).
+__device__ __forceinline__ bool joint_breaks(uint32_t kind, float4 l, float4 a, float2 brk, float inv_dt) {
+    const float l2 = 0.0f + l.x * l.x + l.y * l.y + l.z * l.z;
+    const float a2 = 0.0f + a.x * a.x + a.y * a.y + a.z * a.z;
+    const float inv_dt2 = inv_dt * inv_dt;
+    switch (kind) {
+    case NPGPU_JOINT_BALL: return l2 * inv_dt * inv_dt > brk.x;
+    case NPGPU_JOINT_CARTESIAN: return a2 * inv_dt * inv_dt > brk.y;
+    case NPGPU_JOINT_PLANAR:
+        return l.x * l.x * inv_dt2 > brk.x || a.x * a.x * inv_dt2 + a.y * a.y * inv_dt2 > brk.y;
+    case NPGPU_JOINT_RECTANGULAR: return l.x * l.x * inv_dt2 > brk.x || a2 * inv_dt2 > brk.y;
+    case NPGPU_JOINT_UNIVERSAL: return l2 * inv_dt2 > brk.x || a.x * a.x * inv_dt2 > brk.y;
+    default: return l2 * inv_dt2 > brk.x || a2 * inv_dt2 > brk.y;   // fixed, revolute
+    }
+}
+
 // ================================================================ integrate
 #if !NPGPU_EXCHANGE_TU
 __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
@@ -2170,21 +2272,20 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
             // fixed_constraint.rs:174-199): the impulses, and the joint breaks
             // when |impulse|^2 / dt^2 exceeds the squared break force / torque.
             const uint32_t j = q & ~kJointBit;
-            const float4 li = w.s.lam[(size_t)m * kMaxContacts];
-            w.j.imp[2 * j] = make_float4(li.x, li.y, li.z, 0.0f);
-            const float n2 = 0.0f + li.x * li.x + li.y * li.y + li.z * li.z;
-            const float2 brk = w.j.brk[j];
-            bool broken;
-            if (nc == 2u) {
-                const float4 la = w.s.lam[(size_t)m * kMaxContacts + 1];
-                w.j.imp[2 * j + 1] = make_float4(la.x, la.y, la.z, 0.0f);
-                const float a2 = 0.0f + la.x * la.x + la.y * la.y + la.z * la.z;
-                const float inv_dt2 = p.inv_dt * p.inv_dt;
-                broken = n2 * inv_dt2 > brk.x || a2 * inv_dt2 > brk.y;
-            } else {
-                broken = n2 * p.inv_dt * p.inv_dt > brk.x;
+            float4 imp[2] = {w.j.imp[2 * j], w.j.imp[2 * j + 1]};
+            for (uint32_t k = 0; k < nc; ++k) {
+                const float code = w.s.con[((size_t)m * kMaxContacts + k) * 4].w;
+                const uint32_t rows = joint_rows_of(code);
+                const float4 l = w.s.lam[(size_t)m * kMaxContacts + k];
+                float4& o = imp[joint_angular(code) ? 1 : 0];
+                if (rows > 0u) o.x = l.x;
+                if (rows > 1u) o.y = l.y;
+                if (rows > 2u) o.z = l.z;
             }
-            if (broken) w.j.state[j] |= JS_BROKEN;
+            w.j.imp[2 * j] = imp[0];
+            w.j.imp[2 * j + 1] = imp[1];
+            if (joint_breaks(w.j.info[j] & JI_KIND_MASK, imp[0], imp[1], w.j.brk[j], p.inv_dt))
+                w.j.state[j] |= JS_BROKEN;
             continue;
         }
         for (uint32_t k = 0; k < nc; ++k) {
@@ -2264,13 +2365,68 @@ __device__ __forceinline__ void generic_position_row(const StepParams& p, float 
     }
 }
 
+// UnitQuaternion::rotation_between_axis(a, b) followed by scaled_axis
+// (helper.rs:701-769): the unit axis of a x b times acos(a . b), zero when
+// the axes coincide; false when they are opposite (the callers then take a
+// rotation by pi). The angle is the axis-angle form's directly, without the
+// quaternion in between.
+__device__ __forceinline__ bool rotation_between_scaled(np::V a, np::V b, np::V& out) {
+    np::V ax;
+    float n;
+    const np::V zero = np::mk(0.0f, 0.0f, 0.0f);
+    if (unit_try(np::cross(a, b), FLT_EPSILON, ax, n)) {
+        const float c = np::dot(a, b);
+        if (c <= -1.0f) return false;
+        if (c >= 1.0f) {
+            out = zero;
+            return true;
+        }
+        out = np::mul(ax, (float)acos((double)c));
+        return true;
+    }
+    if (np::dot(a, b) < 0.0f) return false;
+    out = zero;
+    return true;
+}
+
+// The separation of two axes as a scaled axis; for opposite axes, a rotation
+// by pi about the cross product of axis1 with the canonical axis of its
+// smallest component (helper.rs:717-724).
+__device__ __forceinline__ np::V axis_separation(np::V a1, np::V a2) {
+    np::V e;
+    if (rotation_between_scaled(a1, a2, e)) return e;
+    const float c[3] = {fabsf(a1.x), fabsf(a1.y), fabsf(a1.z)};
+    int imin = 0;
+    if (c[1] < c[imin]) imin = 1;
+    if (c[2] < c[imin]) imin = 2;
+    const np::V o = np::cross(basis_axis(imin), a1);
+    return np::mul(np::divs(o, np::norm(o)), 3.14159265358979f);
+}
+
+// Which position constraints a joint kind generates, in order (each
+// constraint's position_constraint(i), with the poses its predecessors left):
+// T the anchors' separation (cancel_relative_translation), TA the separation
+// along body 1's axis (cancel_relative_translation_wrt_axis), R the frames'
+// relative rotation (cancel_relative_rotation), AL the axes' alignment
+// (align_axis), RA the angle between the axes (restore_angle_between_axis).
+enum { JP_T = 1, JP_TA = 2, JP_R_FRAMES = 3, JP_R_BODIES = 4, JP_AL = 5, JP_RA = 6 };
+__device__ __forceinline__ void joint_position_ops(uint32_t kind, int* op) {
+    op[0] = op[1] = 0;
+    switch (kind) {
+    case NPGPU_JOINT_BALL: op[0] = JP_T; break;
+    case NPGPU_JOINT_FIXED: op[0] = JP_R_FRAMES; op[1] = JP_T; break;
+    case NPGPU_JOINT_REVOLUTE: op[0] = JP_T; op[1] = JP_AL; break;
+    case NPGPU_JOINT_CARTESIAN: op[0] = JP_R_FRAMES; break;
+    case NPGPU_JOINT_PLANAR: op[0] = JP_TA; op[1] = JP_AL; break;
+    case NPGPU_JOINT_RECTANGULAR: op[0] = JP_TA; op[1] = JP_R_BODIES; break;
+    default: op[0] = JP_T; op[1] = JP_RA; break;   // universal
+    }
+}
+
 // The position constraints of joint j on the poses P1, P2
-// (NonlinearSORProx::solve_generator, nonlinear_sor_prox.rs:57-76):
-// FixedConstraint::position_constraint (fixed_constraint.rs:207-249) first
-// cancels the relative rotation of the two frames (helper::cancel_relative_
-// rotation, helper.rs:553-611), then, with the poses it left, both kinds
-// cancel the anchors' separation (helper::cancel_relative_translation,
-// helper.rs:364-418). Each is skipped below the allowed error
+// (NonlinearSORProx::solve_generator, nonlinear_sor_prox.rs:57-76), each
+// through helper.rs's position helpers (helper.rs:298-418, 553-611, 701-769,
+// 921-998) and solve_generic. An error below the allowed one is skipped
 // (Unit::try_new_and_get).
 __device__ __forceinline__ void joint_position(const World& w, const StepParams& p, uint32_t j, uint32_t bb1, uint32_t bb2,
                                                uint32_t i1, uint32_t i2, Pose& P1, Pose& P2, bool& moved1,
@@ -2299,40 +2455,68 @@ __device__ __forceinline__ void joint_position(const World& w, const StepParams&
         v2.inv_mass = s.im;
         v2.inv_I = s.I;
     }
+    const uint32_t kind = w.j.info[j] & JI_KIND_MASK;
     const np::V la1 = v3(w.j.anchor[2 * j]), la2 = v3(w.j.anchor[2 * j + 1]);
+    const float4 ax1 = w.j.axis[2 * j], ax2 = w.j.axis[2 * j + 1];
     moved1 = moved2 = false;
+    int ops[2];
+    joint_position_ops(kind, ops);
     float J1[6], J2[6], W1[6], W2[6];
-    if ((w.j.info[j] & JI_KIND_MASK) == NPGPU_JOINT_FIXED) {
-        const np::Q r1 = np::qmul(q1, q4(w.j.frame[2 * j])), r2 = np::qmul(q2, q4(w.j.frame[2 * j + 1]));
-        const np::V err = np::qscaled_axis(np::qmul(r2, np::qconj(r1)));
-        const float sq = np::dot(err, err);
-        if (sq > p.allowed_angular_error * p.allowed_angular_error) {
-            const float depth = sqrtf(sq);
-            const np::V dir = np::divs(err, depth);
-            float inv_r = 0.0f, dummy = 0.0f;
-            v1.com = com1;
-            v2.com = com2;
+    for (int o = 0; o < 2 && ops[o] != 0; ++o) {
+        const int op = ops[o];
+        const np::V a1 = body_point(t1, q1, la1), a2 = body_point(t2, q2, la2);
+        bool angular = false, have = false;
+        np::V dir;
+        float depth = 0.0f;
+        if (op == JP_T) {
+            have = unit_try(np::sub(a2, a1), p.allowed_linear_error, dir, depth);
+        } else if (op == JP_TA) {
+            const np::V ax = np::qrot(q1, v3(ax1));
+            depth = np::dot(ax, np::sub(a2, a1));
+            dir = ax;
+            if (depth < 0.0f) {
+                depth = -depth;
+                dir = np::neg(ax);
+            }
+            have = depth > p.allowed_linear_error;
+        } else if (op == JP_R_FRAMES || op == JP_R_BODIES) {
+            np::Q r1 = q1, r2 = q2;
+            if (op == JP_R_FRAMES) {
+                r1 = np::qmul(q1, q4(w.j.frame[2 * j]));
+                r2 = np::qmul(q2, q4(w.j.frame[2 * j + 1]));
+            }
+            angular = true;
+            have = unit_try(np::qscaled_axis(np::qmul(r2, np::qconj(r1))), p.allowed_angular_error, dir, depth);
+        } else if (op == JP_AL) {
+            angular = true;
+            const np::V e = axis_separation(np::qrot(q1, v3(ax1)), np::qrot(q2, v3(ax2)));
+            have = unit_try(e, p.allowed_angular_error, dir, depth);
+        } else {   // JP_RA
+            angular = true;
+            float cur;
+            const np::V e = axis_separation(np::qrot(q1, v3(ax1)), np::qrot(q2, v3(ax2)));
+            if (unit_try(e, FLT_EPSILON, dir, cur)) {
+                depth = cur - ax1.w;
+                if (depth < 0.0f) {
+                    depth = -depth;
+                    dir = np::neg(dir);
+                }
+                have = !(depth < p.allowed_angular_error);
+            }
+        }
+        if (!have) continue;
+        float inv_r = 0.0f, dummy = 0.0f;
+        v1.com = com1;
+        v2.com = com2;
+        if (angular) {
             if (d1) fill_torque_side(v1, dir, J1, W1, inv_r, dummy, false, p.dt);
             if (d2) fill_torque_side(v2, np::neg(dir), J2, W2, inv_r, dummy, false, p.dt);
-            generic_position_row(p, depth, true, inv_r, d1, d2, W1, W2, t1, q1, com1, lc1, t2, q2, com2, lc2, moved1,
-                                 moved2);
-        }
-    }
-    {
-        const np::V a1 = body_point(t1, q1, la1), a2 = body_point(t2, q2, la2);
-        const np::V err = np::sub(a2, a1);
-        const float sq = np::dot(err, err);
-        if (sq > p.allowed_linear_error * p.allowed_linear_error) {
-            const float depth = sqrtf(sq);
-            const np::V dir = np::divs(err, depth);
-            float inv_r = 0.0f, dummy = 0.0f;
-            v1.com = com1;
-            v2.com = com2;
+        } else {
             if (d1) fill_row_side(v1, a1, dir, J1, W1, inv_r, dummy, false, p.dt);
             if (d2) fill_row_side(v2, a2, np::neg(dir), J2, W2, inv_r, dummy, false, p.dt);
-            generic_position_row(p, depth, false, inv_r, d1, d2, W1, W2, t1, q1, com1, lc1, t2, q2, com2, lc2, moved1,
-                                 moved2);
         }
+        generic_position_row(p, depth, angular, inv_r, d1, d2, W1, W2, t1, q1, com1, lc1, t2, q2, com2, lc2, moved1,
+                             moved2);
     }
     P1.t = t1; P1.q = q1; P1.com = com1;
     P2.t = t2; P2.q = q2; P2.com = com2;

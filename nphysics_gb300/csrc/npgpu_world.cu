@@ -286,7 +286,8 @@ static npgpu_status stage_reserve(npgpu_world* w, size_t bytes, void** hptr) {
     if (w->d_query) cudaFree(w->d_query);
     if (w->dw.events) cudaFree(w->dw.events);
     for (void* p : {(void*)w->dw.j.info, (void*)w->dw.j.state, (void*)w->dw.j.body, (void*)w->dw.j.local,
-                    (void*)w->dw.j.anchor, (void*)w->dw.j.frame, (void*)w->dw.j.imp, (void*)w->dw.j.brk})
+                    (void*)w->dw.j.anchor, (void*)w->dw.j.frame, (void*)w->dw.j.imp, (void*)w->dw.j.brk,
+                    (void*)w->dw.j.axis})
         cudaFree(p);
         w->d_stage = nullptr;
         size_t nb = std::max(bytes, w->d_stage_bytes * 2);
@@ -882,6 +883,7 @@ static npgpu_status ensure_joint_capacity(npgpu_world* w, uint32_t need) {
     }
     JA(nj.info, cap) JA(nj.state, cap) JA(nj.body, 2 * (size_t)cap) JA(nj.local, cap)
     JA(nj.anchor, 2 * (size_t)cap) JA(nj.frame, 2 * (size_t)cap) JA(nj.imp, 2 * (size_t)cap) JA(nj.brk, cap)
+    JA(nj.axis, 2 * (size_t)cap)
 #undef JA
     if (!ok) {
         for (void* p : fresh) cudaFree(p);
@@ -902,10 +904,11 @@ static npgpu_status ensure_joint_capacity(npgpu_world* w, uint32_t need) {
         CK(cudaMemcpyAsync(nj.frame, oj.frame, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
         CK(cudaMemcpyAsync(nj.imp, oj.imp, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
         CK(cudaMemcpyAsync(nj.brk, oj.brk, sizeof(float2) * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.axis, oj.axis, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
     }
     CK(cudaStreamSynchronize(w->stream), "joint arrays");
     for (void* p : {(void*)oj.info, (void*)oj.state, (void*)oj.body, (void*)oj.local, (void*)oj.anchor, (void*)oj.frame,
-                    (void*)oj.imp, (void*)oj.brk})
+                    (void*)oj.imp, (void*)oj.brk, (void*)oj.axis})
         cudaFree(p);
     w->dw.j = nj;
     w->cap_j = cap;
@@ -950,8 +953,10 @@ npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle*
         const npgpu_joint_desc& d = descs[k];
         if (handles[k].index >= (1u << 21) - 1u)
             return fail(w, NPGPU_ERR_CAPACITY, "joint index must be below 2^21 - 1");
-        if (d.kind != NPGPU_JOINT_BALL && d.kind != NPGPU_JOINT_FIXED)
-            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind (ball and fixed joints are supported)");
+        if (d.kind > NPGPU_JOINT_UNIVERSAL)
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT,
+                        "unknown joint kind (ball, fixed, revolute, cartesian, planar, rectangular and universal "
+                        "joints are supported)");
         if (!body_handle_ok(w, d.body1) || !body_handle_ok(w, d.body2))
             return fail(w, NPGPU_ERR_INVALID_HANDLE, "joint body handle is invalid");
         if (d.body1.index == d.body2.index)
@@ -959,6 +964,7 @@ npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle*
         if (w->hb[d.body1.index].world != w->hb[d.body2.index].world)
             return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "a joint's bodies must belong to the same world");
         if (!finite_n(d.anchor1, 3) || !finite_n(d.anchor2, 3) || !finite_n(d.frame1, 4) || !finite_n(d.frame2, 4) ||
+            !finite_n(d.axis1, 3) || !finite_n(d.axis2, 3) || !std::isfinite(d.angle) ||
             std::isnan(d.break_force) || std::isnan(d.break_torque))
             return fail(w, NPGPU_ERR_NAN, "joint description has a non-finite value");
     }
@@ -994,6 +1000,9 @@ npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle*
         std::memcpy(u.anchor2, d.anchor2, sizeof(u.anchor2));
         std::memcpy(u.frame1, d.frame1, sizeof(u.frame1));
         std::memcpy(u.frame2, d.frame2, sizeof(u.frame2));
+        std::memcpy(u.axis1, d.axis1, sizeof(u.axis1));
+        std::memcpy(u.axis2, d.axis2, sizeof(u.axis2));
+        u.angle = d.angle;
         // set_break_force / set_break_torque keep the squares (f32).
         u.brk_force2 = d.break_force * d.break_force;
         u.brk_torque2 = d.break_torque * d.break_torque;

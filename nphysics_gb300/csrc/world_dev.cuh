@@ -120,15 +120,25 @@ struct Joints {
     uint32_t *local;                 // slot minus the smallest alive joint slot of its world (colouring priority)
     float4 *anchor;                  // 2 per joint: the anchors in their bodies' frames (xyz)
     float4 *frame;                   // 2 per joint: the reference frames (quaternion i j k w)
+    float4 *axis;                    // 2 per joint: the axes in their bodies' frames (xyz); .w of the first: angle
     float4 *imp;                     // 2 per joint: the impulses (linear xyz, angular xyz)
     float2 *brk;                     // break force^2, break torque^2
 };
 enum : uint32_t { JI_KIND_MASK = 0xffu, JI_ALIVE = 1u << 8, JS_BROKEN = 1u << 0, JS_ACTIVE = 1u << 1 };
 // A solver manifold list entry of a joint: kJointBit | joint slot.
 constexpr uint32_t kJointBit = 0x80000000u;
-// The joint rows' kinds in the solver records (the friction slot, which is
-// non-negative for a contact): a linear triple (x, y, z) and an angular one.
-constexpr float kJointLinear = -1.0f, kJointAngular = -2.0f;
+// A joint's row group in the solver records: up to three rows of one kind
+// (forces along, or torques about, the record's directions: the normal slot
+// and the two friction-direction slots). The friction slot, non-negative for
+// a contact, holds -(4 kind + rows): kind 1 linear, 2 angular.
+enum : uint32_t { JR_LINEAR = 1u, JR_ANGULAR = 2u };
+__host__ __device__ inline float joint_code(uint32_t kind, uint32_t rows) { return -(float)(4u * kind + rows); }
+__host__ __device__ inline uint32_t joint_rows_of(float code) { return (uint32_t)(-code) & 3u; }
+__host__ __device__ inline bool joint_angular(float code) { return ((uint32_t)(-code) >> 2) == JR_ANGULAR; }
+// Row groups (solver records) of a joint kind.
+__host__ __device__ inline uint32_t joint_group_count(uint32_t kind) {
+    return (kind == NPGPU_JOINT_BALL || kind == NPGPU_JOINT_CARTESIAN) ? 1u : 2u;
+}
 
 struct Pairs {
     uint2 *pair;                     // (collider1, collider2), collider1 < collider2
@@ -314,6 +324,7 @@ struct JointUpload {                 // one joint's description (info 0: removed
     uint32_t reset;                  // 1: the impulses and the state start from zero
     float anchor1[3], anchor2[3], frame1[4], frame2[4];
     float brk_force2, brk_torque2;
+    float axis1[3], axis2[3], angle;
 };
 struct MassUpdate {                  // new local inertia / com of a body
     uint32_t slot;

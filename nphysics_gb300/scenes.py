@@ -54,6 +54,8 @@ def joint_descs(n):
     j["frame2"][:, 3] = 1.0
     j["break_force"] = abi.FLT_MAX
     j["break_torque"] = abi.FLT_MAX
+    j["axis1"][:, 0] = 1.0
+    j["axis2"][:, 0] = 1.0
     return j
 
 
@@ -645,3 +647,128 @@ def pendulum(length=2.0, angle=0.2, radius=0.1, density=100.0, chain=1):
         j["anchor2"][i] = -d * length if i == 0 else -d * length
     sc = Scene("pendulum", bodies, colliders, steps=600)
     return set_joints(sc, j)
+
+
+def hinge(kind=abi.JOINT_REVOLUTE, half=(0.5, 0.1, 0.1), angle=0.3, density=1.0, spin=(0.0, 0.0, 0.0)):
+    """A box hung from the ground body (the pivot at height 10) by one joint of
+    `kind`: its -x end at the pivot, the body tilted by `angle` about z from
+    the horizontal +x direction; the joint axes are z in both frames
+    (revolute: a physical pendulum swinging in the x-y plane), and the box
+    starts with angular velocity `spin`. No collisions occur."""
+    g = ground_descs(1)
+    gc = collider_descs(1, 0, abi.SHAPE_CUBOID, (1.0, 1.0, 1.0))
+    gc["position_wrt_body"][0, 1] = -1.0
+    b = body_descs(1)
+    pivot = np.array([0.0, 10.0, 0.0])
+    c, s_ = math.cos(-angle), math.sin(-angle)
+    b["position"][0, :3] = pivot + np.array([c, s_, 0.0]) * half[0]
+    b["position"][0, 3:7] = (0.0, 0.0, math.sin(-angle / 2), math.cos(-angle / 2))
+    b["velocity"][0, 3:] = spin
+    b["flags"] = abi.BODY_GRAVITY
+    cl = collider_descs(1, 0, abi.SHAPE_CUBOID, half, density=density)
+    bodies, colliders = _concat([g, b], [gc, cl])
+    j = joint_descs(1)
+    j["kind"] = kind
+    j["body1"]["index"], j["body2"]["index"] = 0, 1
+    j["anchor1"][0] = pivot
+    j["anchor2"][0] = (-half[0], 0.0, 0.0)
+    q = np.array([0.0, 0.0, math.sin(-angle / 2), math.cos(-angle / 2)])
+    j["frame1"][0] = q                        # frames equal at the start: ground frame = body rotation
+    j["frame2"][0] = (0.0, 0.0, 0.0, 1.0)
+    j["axis1"][0] = (0.0, 0.0, 1.0)
+    j["axis2"][0] = (0.0, 0.0, 1.0)
+    sc = Scene("hinge", bodies, colliders, steps=600)
+    return set_joints(sc, j)
+
+
+def joint_zoo(seed=11, world=0, ground=True):
+    """One of each joint kind on boxes and balls over the ground, with
+    random initial velocities, plus a few free boxes falling on them: the
+    joint-kind parity scene. Revolute, universal and fixed pairs join two
+    dynamic bodies; cartesian, planar and rectangular joints hold a body to
+    the ground body."""
+    rng = np.random.default_rng(seed)
+    parts_b, parts_c, joints = [], [], []
+    g, gc = _ground(half=(15.0, 1.0, 15.0), world=world)
+    parts_b.append(g)
+    parts_c.append(gc)
+    nb = 1
+    kinds = [abi.JOINT_BALL, abi.JOINT_FIXED, abi.JOINT_REVOLUTE, abi.JOINT_CARTESIAN, abi.JOINT_PLANAR,
+             abi.JOINT_RECTANGULAR, abi.JOINT_UNIVERSAL]
+    for i, kind in enumerate(kinds):
+        x = -9.0 + 3.0 * i
+        two = kind in (abi.JOINT_BALL, abi.JOINT_FIXED, abi.JOINT_REVOLUTE, abi.JOINT_UNIVERSAL)
+        n = 2 if two else 1
+        b = body_descs(n)
+        b["world"] = world
+        b["position"][0, :3] = (x, 2.5, 0.0)
+        if two:
+            b["position"][1, :3] = (x + 0.8, 2.5, 0.0)
+        b["velocity"][:] = rng.uniform(-1.5, 1.5, (n, 6))
+        cl = collider_descs(n, np.arange(n), abi.SHAPE_CUBOID, (0.3, 0.2, 0.25), density=1.0, friction=0.5)
+        if two:
+            cl["shape"][1] = abi.SHAPE_BALL
+            cl["shape_params"][1] = (0.25, 0.0, 0.0)
+        parts_b.append(b)
+        parts_c.append(cl)
+        j = joint_descs(1)
+        j["kind"] = kind
+        ax = rng.normal(size=3)
+        ax /= np.linalg.norm(ax)
+        if two:
+            j["body1"]["index"], j["body2"]["index"] = nb, nb + 1
+            j["anchor1"][0] = (0.4, 0.0, 0.0)
+            j["anchor2"][0] = (-0.4, 0.0, 0.0)
+            j["axis1"][0] = ax
+            j["axis2"][0] = ax if kind != abi.JOINT_UNIVERSAL else np.cross(ax, (0.0, 1.0, 0.0)) / np.linalg.norm(
+                np.cross(ax, (0.0, 1.0, 0.0)))
+            if kind == abi.JOINT_UNIVERSAL:
+                j["angle"][0] = math.pi / 2
+        else:
+            j["body1"]["index"], j["body2"]["index"] = 0, nb
+            j["anchor1"][0] = (x, 2.5, 0.0)
+            j["anchor2"][0] = (0.0, 0.0, 0.0)
+            j["axis1"][0] = (0.0, 1.0, 0.0) if kind != abi.JOINT_RECTANGULAR else ax
+            j["axis2"][0] = (0.0, 1.0, 0.0)
+        joints.append(j)
+        nb += n
+    drops = body_descs(6)
+    drops["world"] = world
+    drops["position"][:, 0] = -9.0 + 3.0 * rng.integers(0, 7, 6) + rng.uniform(-0.3, 0.3, 6)
+    drops["position"][:, 1] = rng.uniform(4.0, 7.0, 6)
+    drops["position"][:, 2] = rng.uniform(-0.3, 0.3, 6)
+    drops["position"][:, 3:7] = uniform_quaternions(rng, 6)
+    dc = collider_descs(6, np.arange(6), abi.SHAPE_CUBOID, (0.2, 0.2, 0.2), density=1.0, friction=0.5)
+    parts_b.append(drops)
+    parts_c.append(dc)
+    bodies, colliders = _concat(parts_b, parts_c)
+    sc = Scene("joint zoo", bodies, colliders, steps=240)
+    return set_joints(sc, np.concatenate(joints))
+
+
+def concat_worlds(parts, name="batched worlds"):
+    """Scenes of one world each, side by side as the worlds 0, 1, ... of one
+    batch: body slots follow each other, collider parents and joint bodies are
+    renumbered, and each scene's bodies take its world index."""
+    bodies, colliders, joints = [], [], []
+    off = 0
+    for wd, sc in enumerate(parts):
+        b = sc.bodies.copy()
+        b["world"] = wd
+        c = sc.colliders.copy()
+        c["body"]["index"] += off
+        j = sc.joints.copy()
+        j["body1"]["index"] += off
+        j["body2"]["index"] += off
+        bodies.append(b)
+        colliders.append(c)
+        joints.append(j)
+        off += len(b)
+    sc = Scene(name, np.concatenate(bodies), np.concatenate(colliders), steps=parts[0].steps)
+    return set_joints(sc, np.concatenate(joints))
+
+
+def batched_zoo(n_worlds=6, seed=11, worlds=None):
+    """Worlds of the joint zoo (seeds seed, seed + 1, ...); `worlds` builds only those."""
+    worlds = range(n_worlds) if worlds is None else worlds
+    return concat_worlds([joint_zoo(seed=seed + w) for w in worlds], f"{len(worlds)} joint-zoo worlds")

@@ -279,7 +279,9 @@ template <class R> struct Joint {
     uint64_t generation = 0;
     uint32_t kind = NPGPU_JOINT_BALL, b1 = 0, b2 = 0;
     V3<R> anchor1, anchor2;     // in the bodies' frames
-    Quat<R> frame1, frame2;     // FixedConstraint's reference frames
+    Quat<R> frame1, frame2;     // the reference frames (fixed, cartesian)
+    V3<R> axis1, axis2;         // the axes in the bodies' frames (revolute, planar, rectangular, universal)
+    R angle = R(0);             // universal: the angle kept between the axes
     R brk_force2, brk_torque2;  // set_break_force / set_break_torque keep the squares
     R imp[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};   // linear x y z, angular x y z
     bool broken = false, active = false;
@@ -445,8 +447,7 @@ public:
         auto body_ok = [&](const npgpu_handle& b) {
             return b.index < bodies.size() && bodies[b.index].alive && bodies[b.index].generation == b.generation;
         };
-        if (d.kind != NPGPU_JOINT_BALL && d.kind != NPGPU_JOINT_FIXED)
-            return fail(NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind");
+        if (d.kind > NPGPU_JOINT_UNIVERSAL) return fail(NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind");
         if (!body_ok(d.body1) || !body_ok(d.body2)) return fail(NPGPU_ERR_INVALID_HANDLE, "joint body handle is invalid");
         if (d.body1.index == d.body2.index) return fail(NPGPU_ERR_INVALID_ARGUMENT, "a joint needs two different bodies");
         if (bodies[d.body1.index].world != bodies[d.body2.index].world)
@@ -468,6 +469,9 @@ public:
         j.anchor2 = v3<R>(R(d.anchor2[0]), R(d.anchor2[1]), R(d.anchor2[2]));
         j.frame1 = Quat<R>{R(d.frame1[0]), R(d.frame1[1]), R(d.frame1[2]), R(d.frame1[3])};
         j.frame2 = Quat<R>{R(d.frame2[0]), R(d.frame2[1]), R(d.frame2[2]), R(d.frame2[3])};
+        j.axis1 = v3<R>(R(d.axis1[0]), R(d.axis1[1]), R(d.axis1[2]));
+        j.axis2 = v3<R>(R(d.axis2[0]), R(d.axis2[1]), R(d.axis2[2]));
+        j.angle = R(d.angle);
         const R f = R(d.break_force), t = R(d.break_torque);
         j.brk_force2 = f * f;
         j.brk_torque2 = t * t;
@@ -1799,26 +1803,84 @@ public:
         return ncol;
     }
 
-    // The rows of active joint j (BallConstraint / FixedConstraint::
-    // velocity_constraints, ball_constraint.rs:80-127, fixed_constraint.rs:
-    // 107-172, through helper::cancel_relative_linear_velocity and
-    // cancel_relative_angular_velocity, helper.rs:167-296, 422-551): one
-    // bilateral row per axis, started from the joint's impulse.
+    // Unit::try_new_and_get(v, eps): v / |v| when |v|^2 > eps^2.
+    static bool unit_try(V3<R> v, R eps, V3<R>& u, R& n) {
+        const R sq = dot(v, v);
+        if (!(sq > eps * eps)) return false;
+        n = std::sqrt(sq);
+        u = vdiv(v, n);
+        return true;
+    }
+    static V3<R> basis(int r) { return v3<R>(r == 0 ? R(1) : R(0), r == 1 ? R(1) : R(0), r == 2 ? R(1) : R(0)); }
+
+    // A joint's row group: `rows` forces along (linear) or torques about the
+    // directions d, their impulses in slots slot..slot + rows - 1.
+    struct JointGroup {
+        bool angular;
+        int rows, slot;
+        V3<R> d[3];
+    };
+    // The row groups of a joint kind as each constraint's velocity_constraints
+    // builds them (ball_constraint.rs:80-127, fixed_constraint.rs:107-172,
+    // revolute_constraint.rs:181-266, cartesian_constraint.rs,
+    // planar_constraint.rs, rectangular_constraint.rs,
+    // universal_constraint.rs) from helper.rs:167-296, 422-551, 614-699; the
+    // subspace basis of an axis is the contact model's tangent basis.
+    int joint_groups(const Joint<R>& jt, Quat<R> q1, Quat<R> q2, JointGroup* g) const {
+        const V3<R> ex = basis(0), ey = basis(1), ez = basis(2), zero = v3<R>(R(0), R(0), R(0));
+        const JointGroup lin3{false, 3, 0, {ex, ey, ez}}, ang3{true, 3, 3, {ex, ey, ez}};
+        switch (jt.kind) {
+        case NPGPU_JOINT_BALL: g[0] = lin3; return 1;
+        case NPGPU_JOINT_FIXED: g[0] = lin3; g[1] = ang3; return 2;
+        case NPGPU_JOINT_CARTESIAN: g[0] = ang3; return 1;
+        case NPGPU_JOINT_REVOLUTE: {
+            V3<R> t1, t2;
+            tangent_basis(qrot(q1, jt.axis1), t1, t2);
+            g[0] = lin3;
+            g[1] = JointGroup{true, 2, 3, {t1, t2, zero}};
+            return 2;
+        }
+        case NPGPU_JOINT_PLANAR: {
+            const V3<R> a = qrot(q1, jt.axis1);
+            V3<R> t1, t2;
+            tangent_basis(a, t1, t2);
+            g[0] = JointGroup{false, 1, 0, {a, zero, zero}};
+            g[1] = JointGroup{true, 2, 3, {t1, t2, zero}};
+            return 2;
+        }
+        case NPGPU_JOINT_RECTANGULAR:
+            g[0] = JointGroup{false, 1, 0, {qrot(q1, jt.axis1), zero, zero}};
+            g[1] = ang3;
+            return 2;
+        default: {   // universal
+            V3<R> o;
+            R n;
+            const bool has = unit_try(cross(qrot(q1, jt.axis1), qrot(q2, jt.axis2)),
+                                      std::numeric_limits<R>::epsilon(), o, n);
+            g[0] = lin3;
+            g[1] = JointGroup{true, has ? 1 : 0, 3, {has ? o : zero, zero, zero}};
+            return 2;
+        }
+        }
+    }
+
+    // The rows of active joint j: one bilateral row per direction, started
+    // from the joint's impulse.
     void joint_rows(uint32_t j, std::vector<int>& out) {
         const Joint<R>& jt = joints[j];
         const Body<R>& b1 = bodies[jt.b1];
         const Body<R>& b2 = bodies[jt.b2];
         const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
-        const int nt = jt.kind == NPGPU_JOINT_FIXED ? 2 : 1;
-        for (int t = 0; t < nt; ++t)
-            for (int r = 0; r < 3; ++r) {
-                V3<R> e = v3<R>(r == 0 ? R(1) : R(0), r == 1 ? R(1) : R(0), r == 2 ? R(1) : R(0));
-                Row<R> row = t == 0 ? make_row(b1, jt.b1, b2, jt.b2, a1, a2, e, R(0))
-                                    : make_row_angular(b1, jt.b1, b2, jt.b2, e);
-                row.impulse = jt.imp[3 * t + r];
+        JointGroup g[2];
+        const int ng = joint_groups(jt, b1.pos.q, b2.pos.q, g);
+        for (int t = 0; t < ng; ++t)
+            for (int r = 0; r < g[t].rows; ++r) {
+                Row<R> row = g[t].angular ? make_row_angular(b1, jt.b1, b2, jt.b2, g[t].d[r])
+                                          : make_row(b1, jt.b1, b2, jt.b2, a1, a2, g[t].d[r], R(0));
+                row.impulse = jt.imp[g[t].slot + r];
                 row.bilateral = true;
                 row.joint = int(j);
-                row.joint_slot = 3 * t + r;
+                row.joint_slot = g[t].slot + r;
                 row.cache = nullptr;
                 out.push_back(int(rows.size()));
                 rows.push_back(row);
@@ -2218,16 +2280,25 @@ public:
             else static_cast<MContact<R>*>(r.cache)->impulse[r.cache_slot] = r.impulse;
         }
         const R inv_dt = (params.dt == 0.0f) ? R(0) : R(1) / R(params.dt);
-        for (Joint<R>& j : joints) {
-            if (!j.alive || !j.active) continue;
-            const R n2 = R(0) + j.imp[0] * j.imp[0] + j.imp[1] * j.imp[1] + j.imp[2] * j.imp[2];
-            if (j.kind == NPGPU_JOINT_FIXED) {
-                const R a2 = R(0) + j.imp[3] * j.imp[3] + j.imp[4] * j.imp[4] + j.imp[5] * j.imp[5];
-                const R inv_dt2 = inv_dt * inv_dt;
-                if (n2 * inv_dt2 > j.brk_force2 || a2 * inv_dt2 > j.brk_torque2) j.broken = true;
-            } else if (n2 * inv_dt * inv_dt > j.brk_force2) {
-                j.broken = true;
-            }
+        for (Joint<R>& j : joints)
+            if (j.alive && j.active && joint_breaks(j, inv_dt)) j.broken = true;
+    }
+    // Each kind's break test in its own arithmetic (ball_constraint.rs:129-141,
+    // fixed_constraint.rs:174-199, revolute_constraint.rs:268-292, ...).
+    static bool joint_breaks(const Joint<R>& j, R inv_dt) {
+        const R* l = j.imp;
+        const R* a = j.imp + 3;
+        const R l2 = R(0) + l[0] * l[0] + l[1] * l[1] + l[2] * l[2];
+        const R a2 = R(0) + a[0] * a[0] + a[1] * a[1] + a[2] * a[2];
+        const R inv_dt2 = inv_dt * inv_dt;
+        switch (j.kind) {
+        case NPGPU_JOINT_BALL: return l2 * inv_dt * inv_dt > j.brk_force2;
+        case NPGPU_JOINT_CARTESIAN: return a2 * inv_dt * inv_dt > j.brk_torque2;
+        case NPGPU_JOINT_PLANAR:
+            return l[0] * l[0] * inv_dt2 > j.brk_force2 || a[0] * a[0] * inv_dt2 + a[1] * a[1] * inv_dt2 > j.brk_torque2;
+        case NPGPU_JOINT_RECTANGULAR: return l[0] * l[0] * inv_dt2 > j.brk_force2 || a2 * inv_dt2 > j.brk_torque2;
+        case NPGPU_JOINT_UNIVERSAL: return l2 * inv_dt2 > j.brk_force2 || a[0] * a[0] * inv_dt2 > j.brk_torque2;
+        default: return l2 * inv_dt2 > j.brk_force2 || a2 * inv_dt2 > j.brk_torque2;
         }
     }
 
@@ -2256,48 +2327,119 @@ public:
         }
     }
 
-    // The position constraints of joint j (NonlinearSORProx::solve_generator,
-    // nonlinear_sor_prox.rs:57-76): FixedConstraint::position_constraint
-    // (fixed_constraint.rs:207-249) first cancels the frames' relative
-    // rotation (helper::cancel_relative_rotation, helper.rs:553-611); then,
-    // from the poses it left, both kinds cancel the anchors' separation
-    // (helper::cancel_relative_translation, helper.rs:364-418). Each is
-    // skipped below the allowed error (Unit::try_new_and_get).
+    // UnitQuaternion::rotation_between_axis + scaled_axis (helper.rs:701-769):
+    // the unit axis of a x b times acos(a . b); false for opposite axes. The
+    // angle is the axis-angle form's directly (acos in double, rounded as the
+    // GPU rounds it in f32).
+    static bool rotation_between_scaled(V3<R> a, V3<R> b, V3<R>& out) {
+        V3<R> ax;
+        R n;
+        const V3<R> zero = v3<R>(R(0), R(0), R(0));
+        if (unit_try(cross(a, b), std::numeric_limits<R>::epsilon(), ax, n)) {
+            const R c = dot(a, b);
+            if (c <= -R(1)) return false;
+            if (c >= R(1)) {
+                out = zero;
+                return true;
+            }
+            out = ax * R(std::acos(double(c)));
+            return true;
+        }
+        if (dot(a, b) < R(0)) return false;
+        out = zero;
+        return true;
+    }
+    static V3<R> axis_separation(V3<R> a1, V3<R> a2) {
+        V3<R> e;
+        if (rotation_between_scaled(a1, a2, e)) return e;
+        const R c[3] = {std::fabs(a1.x), std::fabs(a1.y), std::fabs(a1.z)};
+        int imin = 0;
+        if (c[1] < c[imin]) imin = 1;
+        if (c[2] < c[imin]) imin = 2;
+        const V3<R> o = cross(basis(imin), a1);
+        return vdiv(o, norm(o)) * R(3.14159265358979);
+    }
+
+    // The position constraints of joint j, in each kind's order
+    // (NonlinearSORProx::solve_generator, nonlinear_sor_prox.rs:57-76; each
+    // constraint's position_constraint(i) with the poses its predecessors
+    // left): the anchors' separation (cancel_relative_translation), the
+    // separation along body 1's axis (cancel_relative_translation_wrt_axis),
+    // the frames' or bodies' relative rotation (cancel_relative_rotation), the
+    // axes' alignment (align_axis) or the angle between them
+    // (restore_angle_between_axis), helper.rs:298-418, 553-611, 701-769,
+    // 921-998. An error below the allowed one is skipped.
+    enum { JP_T = 1, JP_TA = 2, JP_R_FRAMES = 3, JP_R_BODIES = 4, JP_AL = 5, JP_RA = 6 };
     void joint_position(uint32_t j) {
         Joint<R>& jt = joints[j];
         Body<R>& b1 = bodies[jt.b1];
         Body<R>& b2 = bodies[jt.b2];
+        int ops[2] = {0, 0};
+        switch (jt.kind) {
+        case NPGPU_JOINT_BALL: ops[0] = JP_T; break;
+        case NPGPU_JOINT_FIXED: ops[0] = JP_R_FRAMES; ops[1] = JP_T; break;
+        case NPGPU_JOINT_REVOLUTE: ops[0] = JP_T; ops[1] = JP_AL; break;
+        case NPGPU_JOINT_CARTESIAN: ops[0] = JP_R_FRAMES; break;
+        case NPGPU_JOINT_PLANAR: ops[0] = JP_TA; ops[1] = JP_AL; break;
+        case NPGPU_JOINT_RECTANGULAR: ops[0] = JP_TA; ops[1] = JP_R_BODIES; break;
+        default: ops[0] = JP_T; ops[1] = JP_RA; break;
+        }
         R J1[6], J2[6], W1[6], W2[6];
-        if (jt.kind == NPGPU_JOINT_FIXED) {
-            const Quat<R> r1 = qmul(b1.pos.q, jt.frame1), r2 = qmul(b2.pos.q, jt.frame2);
-            const V3<R> err = qscaled_axis(qmul(r2, qconj(r1)));
-            const R sq = dot(err, err);
-            const R eps = R(params.allowed_angular_error);
-            if (sq > eps * eps) {
-                const R depth = std::sqrt(sq);
-                const V3<R> dir = vdiv(err, depth);
-                R inv_r = R(0), dummy = R(0);
+        for (int o = 0; o < 2 && ops[o] != 0; ++o) {
+            const int op = ops[o];
+            const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
+            bool angular = false, have = false;
+            V3<R> dir;
+            R depth = R(0);
+            if (op == JP_T) {
+                have = unit_try(a2 - a1, R(params.allowed_linear_error), dir, depth);
+            } else if (op == JP_TA) {
+                const V3<R> ax = qrot(b1.pos.q, jt.axis1);
+                depth = dot(ax, a2 - a1);
+                dir = ax;
+                if (depth < R(0)) {
+                    depth = -depth;
+                    dir = -ax;
+                }
+                have = depth > R(params.allowed_linear_error);
+            } else if (op == JP_R_FRAMES || op == JP_R_BODIES) {
+                Quat<R> r1 = b1.pos.q, r2 = b2.pos.q;
+                if (op == JP_R_FRAMES) {
+                    r1 = qmul(b1.pos.q, jt.frame1);
+                    r2 = qmul(b2.pos.q, jt.frame2);
+                }
+                angular = true;
+                have = unit_try(qscaled_axis(qmul(r2, qconj(r1))), R(params.allowed_angular_error), dir, depth);
+            } else if (op == JP_AL) {
+                angular = true;
+                have = unit_try(axis_separation(qrot(b1.pos.q, jt.axis1), qrot(b2.pos.q, jt.axis2)),
+                                R(params.allowed_angular_error), dir, depth);
+            } else {
+                angular = true;
+                R cur;
+                if (unit_try(axis_separation(qrot(b1.pos.q, jt.axis1), qrot(b2.pos.q, jt.axis2)),
+                             std::numeric_limits<R>::epsilon(), dir, cur)) {
+                    depth = cur - jt.angle;
+                    if (depth < R(0)) {
+                        depth = -depth;
+                        dir = -dir;
+                    }
+                    have = !(depth < R(params.allowed_angular_error));
+                }
+            }
+            if (!have) continue;
+            R inv_r = R(0), dummy = R(0);
+            if (angular) {
                 if (b1.ndofs() != 0) fill_torque(b1, dir, J1, W1, inv_r, dummy, false);
                 if (b2.ndofs() != 0) fill_torque(b2, -dir, J2, W2, inv_r, dummy, false);
-                generic_position_row(depth, true, inv_r, b1, b2, W1, W2);
+            } else {
+                if (b1.ndofs() != 0) fill(b1, a1, dir, J1, W1, inv_r, dummy, false);
+                if (b2.ndofs() != 0) fill(b2, a2, -dir, J2, W2, inv_r, dummy, false);
             }
-        }
-        const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
-        const V3<R> err = a2 - a1;
-        const R sq = dot(err, err);
-        const R eps = R(params.allowed_linear_error);
-        if (sq > eps * eps) {
-            const R depth = std::sqrt(sq);
-            const V3<R> dir = vdiv(err, depth);
-            R inv_r = R(0), dummy = R(0);
-            if (b1.ndofs() != 0) fill(b1, a1, dir, J1, W1, inv_r, dummy, false);
-            if (b2.ndofs() != 0) fill(b2, a2, -dir, J2, W2, inv_r, dummy, false);
-            generic_position_row(depth, false, inv_r, b1, b2, W1, W2);
+            generic_position_row(depth, angular, inv_r, b1, b2, W1, W2);
         }
     }
 
-    // NonlinearSORProx::solve_unilateral + update_contact_constraint
-    // (nonlinear_sor_prox.rs:121-294).
     void solve_position(const PosConstraint<R>& pc) {
         if (pc.joint >= 0) {
             joint_position(uint32_t(pc.joint));

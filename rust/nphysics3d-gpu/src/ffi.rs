@@ -69,6 +69,11 @@ pub struct npgpu_collider_desc {
 
 pub const NPGPU_JOINT_BALL: u32 = 0;
 pub const NPGPU_JOINT_FIXED: u32 = 1;
+pub const NPGPU_JOINT_REVOLUTE: u32 = 2;
+pub const NPGPU_JOINT_CARTESIAN: u32 = 3;
+pub const NPGPU_JOINT_PLANAR: u32 = 4;
+pub const NPGPU_JOINT_RECTANGULAR: u32 = 5;
+pub const NPGPU_JOINT_UNIVERSAL: u32 = 6;
 
 #[repr(C)]
 #[derive(Copy, Clone, Default)]
@@ -83,6 +88,10 @@ pub struct npgpu_joint_desc {
     pub frame2: [f32; 4],
     pub break_force: f32,
     pub break_torque: f32,
+    pub axis1: [f32; 3],
+    pub axis2: [f32; 3],
+    pub angle: f32,
+    pub pad2: u32,
 }
 
 #[repr(C)]

@@ -8,22 +8,24 @@
 //! and writes the new poses, velocities and activation back into the set, as
 //! `MechanicalWorld::step` leaves them. Scenes the GPU step does not support
 //! (multibodies, FEM or mass-spring bodies, shapes other than balls,
-//! cuboids and capsules, sensors, CCD colliders, joints other than ball and
-//! fixed joints, force generators) make `step` panic with the library's
+//! cuboids and capsules, sensors, CCD colliders, prismatic, cylindrical or
+//! pin-slot joints, force generators) make `step` panic with the library's
 //! message, where nphysics would have run them. Balls, cuboids and capsules
-//! are supported; ball and fixed joints go in as `GpuJoint`s.
+//! are supported; ball, fixed, revolute, cartesian, planar, rectangular and
+//! universal joints go in as `GpuJoint`s.
 pub mod ffi;
 
 use std::collections::HashMap;
 use std::ffi::CStr;
 
 use generational_arena::Index;
-use nalgebra::{DVector, Isometry3, Point3, Quaternion, Translation3, UnitQuaternion, Vector3};
+use nalgebra::{DVector, Isometry3, Point3, Quaternion, Translation3, Unit, UnitQuaternion, Vector3};
 use ncollide3d::shape::{Ball, Capsule, Cuboid};
 use nphysics3d::algebra::{Force3, ForceType, Velocity3};
 use nphysics3d::force_generator::ForceGeneratorSet;
-use nphysics3d::joint::{BallConstraint, DefaultJointConstraintHandle, FixedConstraint, JointConstraint,
-                        JointConstraintSet};
+use nphysics3d::joint::{BallConstraint, CartesianConstraint, DefaultJointConstraintHandle, FixedConstraint,
+                        JointConstraint, JointConstraintSet, PlanarConstraint, RectangularConstraint,
+                        RevoluteConstraint, UniversalConstraint};
 use nphysics3d::material::{BasicMaterial, MaterialCombineMode};
 use nphysics3d::object::{Body, BodyPartHandle, BodySet, BodyStatus, Collider, ColliderSet, DefaultBodyHandle,
                          DefaultColliderHandle, Ground, RigidBody};
@@ -149,12 +151,12 @@ fn collider_desc(c: &Collider<f32, DefaultBodyHandle>) -> ffi::npgpu_collider_de
     d
 }
 
-/// A ball or fixed joint the GPU world can forward. nphysics keeps a
-/// BallConstraint's and a FixedConstraint's anchors and frames private, so
-/// this type builds the reference's constraint and records its description
-/// beside it; it implements JointConstraint by delegating to that constraint,
-/// so the same set still steps on the CPU. Insert it into a
-/// DefaultJointConstraintSet as usual.
+/// A joint the GPU world can forward: ball, fixed, revolute, cartesian,
+/// planar, rectangular or universal. nphysics keeps its constraints' anchors,
+/// axes and frames private, so this type builds the reference's constraint
+/// and records its description beside it; it implements JointConstraint by
+/// delegating to that constraint, so the same set still steps on the CPU.
+/// Insert it into a DefaultJointConstraintSet as usual.
 pub struct GpuJoint {
     inner: Box<dyn JointConstraint<f32, DefaultBodyHandle>>,
     desc: ffi::npgpu_joint_desc,
@@ -166,61 +168,122 @@ fn quat4(q: &UnitQuaternion<f32>) -> [f32; 4] {
     [c.x, c.y, c.z, c.w]
 }
 
+fn v3a(v: &Vector3<f32>) -> [f32; 3] {
+    [v.x, v.y, v.z]
+}
+
+type Part = BodyPartHandle<DefaultBodyHandle>;
+
+/// set_break_force / set_break_torque on whichever constraint `inner` holds.
+macro_rules! on_inner {
+    ($inner:expr, $x:ident => $body:expr, $($t:ty),*) => {
+        $(if let Some($x) = $inner.downcast_mut::<$t>() { $body; })*
+    };
+}
+
 impl GpuJoint {
-    /// BallConstraint::new (src/joint/ball_constraint.rs:26-48).
-    pub fn ball(b1: BodyPartHandle<DefaultBodyHandle>, b2: BodyPartHandle<DefaultBodyHandle>, anchor1: Point3<f32>,
-                anchor2: Point3<f32>) -> Self {
+    fn with(kind: u32, b1: Part, b2: Part, anchor1: &Point3<f32>, anchor2: &Point3<f32>,
+            inner: Box<dyn JointConstraint<f32, DefaultBodyHandle>>) -> Self {
         let mut desc = ffi::npgpu_joint_desc::default();
-        desc.kind = ffi::NPGPU_JOINT_BALL;
+        desc.kind = kind;
         desc.body1 = handle(b1.0);
         desc.body2 = handle(b2.0);
         desc.anchor1 = [anchor1.x, anchor1.y, anchor1.z];
         desc.anchor2 = [anchor2.x, anchor2.y, anchor2.z];
         desc.frame1 = [0.0, 0.0, 0.0, 1.0];
         desc.frame2 = [0.0, 0.0, 0.0, 1.0];
+        desc.axis1 = [1.0, 0.0, 0.0];
+        desc.axis2 = [1.0, 0.0, 0.0];
         desc.break_force = f32::MAX;
         desc.break_torque = f32::MAX;
-        GpuJoint { inner: Box::new(BallConstraint::new(b1, b2, anchor1, anchor2)), desc,
-                   gpu: ffi::npgpu_joint_state::default() }
+        GpuJoint { inner, desc, gpu: ffi::npgpu_joint_state::default() }
+    }
+
+    /// BallConstraint::new (src/joint/ball_constraint.rs:26-48).
+    pub fn ball(b1: Part, b2: Part, anchor1: Point3<f32>, anchor2: Point3<f32>) -> Self {
+        Self::with(ffi::NPGPU_JOINT_BALL, b1, b2, &anchor1, &anchor2,
+                   Box::new(BallConstraint::new(b1, b2, anchor1, anchor2)))
     }
 
     /// FixedConstraint::new (src/joint/fixed_constraint.rs:35-58).
-    pub fn fixed(b1: BodyPartHandle<DefaultBodyHandle>, b2: BodyPartHandle<DefaultBodyHandle>, anchor1: Point3<f32>,
-                 ref_frame1: UnitQuaternion<f32>, anchor2: Point3<f32>, ref_frame2: UnitQuaternion<f32>) -> Self {
-        let mut desc = ffi::npgpu_joint_desc::default();
-        desc.kind = ffi::NPGPU_JOINT_FIXED;
-        desc.body1 = handle(b1.0);
-        desc.body2 = handle(b2.0);
-        desc.anchor1 = [anchor1.x, anchor1.y, anchor1.z];
-        desc.anchor2 = [anchor2.x, anchor2.y, anchor2.z];
-        desc.frame1 = quat4(&ref_frame1);
-        desc.frame2 = quat4(&ref_frame2);
-        desc.break_force = f32::MAX;
-        desc.break_torque = f32::MAX;
-        GpuJoint { inner: Box::new(FixedConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)), desc,
-                   gpu: ffi::npgpu_joint_state::default() }
+    pub fn fixed(b1: Part, b2: Part, anchor1: Point3<f32>, ref_frame1: UnitQuaternion<f32>, anchor2: Point3<f32>,
+                 ref_frame2: UnitQuaternion<f32>) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_FIXED, b1, b2, &anchor1, &anchor2,
+                               Box::new(FixedConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)));
+        j.desc.frame1 = quat4(&ref_frame1);
+        j.desc.frame2 = quat4(&ref_frame2);
+        j
     }
 
-    /// set_break_force of either constraint.
+    /// RevoluteConstraint::new (src/joint/revolute_constraint.rs:52-80).
+    pub fn revolute(b1: Part, b2: Part, anchor1: Point3<f32>, axis1: Unit<Vector3<f32>>, anchor2: Point3<f32>,
+                    axis2: Unit<Vector3<f32>>) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_REVOLUTE, b1, b2, &anchor1, &anchor2,
+                               Box::new(RevoluteConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2)));
+        j.desc.axis1 = v3a(&axis1);
+        j.desc.axis2 = v3a(&axis2);
+        j
+    }
+
+    /// CartesianConstraint::new (src/joint/cartesian_constraint.rs).
+    pub fn cartesian(b1: Part, b2: Part, anchor1: Point3<f32>, ref_frame1: UnitQuaternion<f32>, anchor2: Point3<f32>,
+                     ref_frame2: UnitQuaternion<f32>) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_CARTESIAN, b1, b2, &anchor1, &anchor2,
+                               Box::new(CartesianConstraint::new(b1, b2, anchor1, ref_frame1, anchor2, ref_frame2)));
+        j.desc.frame1 = quat4(&ref_frame1);
+        j.desc.frame2 = quat4(&ref_frame2);
+        j
+    }
+
+    /// PlanarConstraint::new (src/joint/planar_constraint.rs).
+    pub fn planar(b1: Part, b2: Part, anchor1: Point3<f32>, axis1: Unit<Vector3<f32>>, anchor2: Point3<f32>,
+                  axis2: Unit<Vector3<f32>>) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_PLANAR, b1, b2, &anchor1, &anchor2,
+                               Box::new(PlanarConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2)));
+        j.desc.axis1 = v3a(&axis1);
+        j.desc.axis2 = v3a(&axis2);
+        j
+    }
+
+    /// RectangularConstraint::new (src/joint/rectangular_constraint.rs).
+    pub fn rectangular(b1: Part, b2: Part, anchor1: Point3<f32>, axis1: Unit<Vector3<f32>>, anchor2: Point3<f32>)
+                       -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_RECTANGULAR, b1, b2, &anchor1, &anchor2,
+                               Box::new(RectangularConstraint::new(b1, b2, anchor1, axis1, anchor2)));
+        j.desc.axis1 = v3a(&axis1);
+        j
+    }
+
+    /// UniversalConstraint::new (src/joint/universal_constraint.rs).
+    pub fn universal(b1: Part, b2: Part, anchor1: Point3<f32>, axis1: Unit<Vector3<f32>>, anchor2: Point3<f32>,
+                     axis2: Unit<Vector3<f32>>, angle: f32) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_UNIVERSAL, b1, b2, &anchor1, &anchor2,
+                               Box::new(UniversalConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2, angle)));
+        j.desc.axis1 = v3a(&axis1);
+        j.desc.axis2 = v3a(&axis2);
+        j.desc.angle = angle;
+        j
+    }
+
+    /// set_break_force of the constraint.
     pub fn set_break_force(&mut self, f: f32) {
         self.desc.break_force = f;
-        if let Some(b) = self.inner.downcast_mut::<BallConstraint<f32, DefaultBodyHandle>>() {
-            b.set_break_force(f);
-        } else if let Some(x) = self.inner.downcast_mut::<FixedConstraint<f32, DefaultBodyHandle>>() {
-            x.set_break_force(f);
-        }
+        on_inner!(self.inner, x => x.set_break_force(f), BallConstraint<f32, DefaultBodyHandle>,
+                  FixedConstraint<f32, DefaultBodyHandle>, RevoluteConstraint<f32, DefaultBodyHandle>,
+                  PlanarConstraint<f32, DefaultBodyHandle>, RectangularConstraint<f32, DefaultBodyHandle>,
+                  UniversalConstraint<f32, DefaultBodyHandle>);
     }
 
-    /// FixedConstraint::set_break_torque.
+    /// set_break_torque of the constraint (every kind but the ball joint).
     pub fn set_break_torque(&mut self, t: f32) {
         self.desc.break_torque = t;
-        if let Some(x) = self.inner.downcast_mut::<FixedConstraint<f32, DefaultBodyHandle>>() {
-            x.set_break_torque(t);
-        }
+        on_inner!(self.inner, x => x.set_break_torque(t), FixedConstraint<f32, DefaultBodyHandle>,
+                  RevoluteConstraint<f32, DefaultBodyHandle>, CartesianConstraint<f32, DefaultBodyHandle>,
+                  PlanarConstraint<f32, DefaultBodyHandle>, RectangularConstraint<f32, DefaultBodyHandle>,
+                  UniversalConstraint<f32, DefaultBodyHandle>);
     }
 
-    /// The impulses the GPU step cached for this joint (linear x, y, z, then
-    /// angular x, y, z for a fixed joint).
+    /// The impulses the GPU step cached for this joint (linear, then angular).
     pub fn impulses(&self) -> [f32; 6] {
         self.gpu.impulses
     }

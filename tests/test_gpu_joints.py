@@ -122,6 +122,40 @@ def test_break_and_removal_match_oracle(gpu_lib):
     np.testing.assert_array_equal(gi, oi.astype(np.float32))
 
 
+@pytest.mark.parametrize("sweep", [abi.SWEEP_SEPARATE, abi.SWEEP_MANIFOLD])
+def test_every_joint_kind_matches_oracle(gpu_lib, sweep):
+    # Ball, fixed, revolute, cartesian, planar, rectangular and universal
+    # joints with contacts, on the one grid, and batched on the per-world
+    # schedule.
+    for sc, sched in ((scenes.joint_zoo(), abi.SCHEDULE_GRID), (scenes.batched_zoo(n_worlds=6), abi.SCHEDULE_WORLDS)):
+        p = sc.params()
+        p.solver_schedule = sched
+        p.sweep_order = sweep
+        g, o = make_pair(sc, p)
+        for _ in range(4):
+            g.step(40)
+            o.step(40)
+            assert_same(g, o, sc)
+
+
+def test_hinge_pendulum_on_the_gpu(gpu_lib):
+    # The oracle's revolute KAT on the GPU: the hinged box's period.
+    from nphysics_gb300.world import GpuWorld
+    a, b = 0.5, 0.1
+    sc = scenes.hinge(kind=abi.JOINT_REVOLUTE, half=(a, b, 0.1), angle=math.pi / 2 - 0.15)
+    g = GpuWorld.for_scene(sc)
+    th = []
+    for _ in range(600):
+        g.step(1)
+        q = g.bodies()["position"][1, 3:7]
+        th.append(2.0 * math.atan2(q[2], q[3]) + math.pi / 2)
+    crossings = [i for i in range(1, 600) if th[i - 1] > 0 >= th[i]]
+    period = np.diff(crossings).mean() / 60.0
+    ip = (a * a + b * b) / 3 + a * a
+    expected = 2 * math.pi * math.sqrt(ip / (9.81 * a)) * (1 + 0.15 ** 2 / 16)
+    assert abs(period - expected) < 0.01 * expected
+
+
 def test_joint_errors_are_statuses(gpu_lib):
     from nphysics_gb300.world import GpuWorld, NpgpuError
     sc = scenes.batched_jointed(n_worlds=2)

@@ -221,3 +221,124 @@ def test_a_jointed_chain_sleeps_and_wakes_as_one_island():
     w.apply_forces(sc.body_handles[3:4], np.array([[5.0, 0, 0, 0, 0, 0]], np.float32), wake=True)
     w.step(1)
     assert w.bodies()["active"][1:].all()
+
+
+def _angle_about_z(q):
+    return 2.0 * math.atan2(q[2], q[3])
+
+
+@pytest.mark.parametrize("precision", [32, 64])
+def test_revolute_hinge_is_a_physical_pendulum(precision):
+    # A 1 x 0.2 x 0.2 box hinged at one end about z, released 0.15 rad from
+    # the vertical, swings as a physical pendulum about the pivot:
+    # T = 2 pi sqrt(I_p / (m g d)) (1 + theta^2 / 16), with
+    # I_p = m (a^2 + b^2) / 3 + m a^2 and d = a (half length a, half height b);
+    # measured 0.1 % short, the amplitude kept to 2e-4 rad over six swings. It
+    # stays in the x-y plane.
+    a, b = 0.5, 0.1
+    sc = scenes.hinge(kind=abi.JOINT_REVOLUTE, half=(a, b, 0.1), angle=math.pi / 2 - 0.15)
+    w = OracleWorld(sc.params(), sc.gravity, precision=precision)
+    w.load_scene(sc)
+    th, out_of_plane = [], 0.0
+    for _ in range(600):
+        w.step(1)
+        p = w.bodies()["position"][1]
+        th.append(_angle_about_z(p[3:7]))
+        out_of_plane = max(out_of_plane, abs(p[2]), abs(p[3]), abs(p[4]))
+    th = np.array(th) + math.pi / 2          # swing angle from the vertical
+    crossings = [i for i in range(1, len(th)) if th[i - 1] > 0 >= th[i]]
+    period = np.diff(crossings).mean() / 60.0
+    ip = (a * a + b * b) / 3 + a * a
+    expected = 2 * math.pi * math.sqrt(ip / (9.81 * a)) * (1 + 0.15 ** 2 / 16)
+    assert abs(period - expected) < 0.01 * expected
+    assert out_of_plane < 1e-3
+
+
+def test_cartesian_joint_keeps_the_orientation_and_frees_the_translation():
+    # CartesianConstraint locks the relative rotation only: a spinning box
+    # held by one to the ground stops turning and falls freely.
+    sc = scenes.hinge(kind=abi.JOINT_CARTESIAN, angle=0.0, spin=(0.0, 0.0, 0.0))
+    sc.bodies["velocity"][1] = (1.0, 0.0, 0.0, 0.0, 3.0, 2.0)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(30)
+    b = w.bodies()
+    q = b["position"][1, 3:7]
+    assert 2 * math.acos(min(1.0, abs(q[3]))) < 0.01
+    assert np.abs(b["velocity"][1, 3:]).max() < 1e-3
+    assert abs(b["velocity"][1, 1] - (-9.81 * 30 / 60.0)) < 0.01
+
+
+def test_planar_joint_keeps_the_body_in_its_plane():
+    # PlanarConstraint: anchor2 stays in the plane through anchor1 normal to
+    # axis1 (y here), and the body turns only about the axis.
+    sc = scenes.hinge(kind=abi.JOINT_PLANAR, angle=0.0)
+    sc.joints["axis1"][0] = (0.0, 1.0, 0.0)
+    sc.joints["axis2"][0] = (0.0, 1.0, 0.0)
+    sc.bodies["velocity"][1] = (1.0, -2.0, 0.5, 1.0, 2.0, -1.0)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    for _ in range(4):
+        w.step(30)
+        p = w.bodies()["position"][1]
+        a2 = p[:3] + _rot(p[3:7], sc.joints["anchor2"][0])
+        assert abs(a2[1] - 10.0) < 2e-3
+        y_axis = _rot(p[3:7], np.array([0.0, 1.0, 0.0]))
+        assert math.acos(min(1.0, y_axis[1])) < 0.01
+    v = w.bodies()["velocity"][1]
+    assert abs(v[0]) > 0.5 and abs(v[4]) > 0.5          # it slides and turns about y
+
+
+def test_rectangular_joint_translates_in_its_plane_without_turning():
+    sc = scenes.hinge(kind=abi.JOINT_RECTANGULAR, angle=0.0)
+    sc.joints["axis1"][0] = (0.0, 0.0, 1.0)             # the plane normal: z
+    sc.bodies["velocity"][1] = (0.5, 1.0, 2.0, 1.0, 1.0, 1.0)
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    w.step(60)
+    p = w.bodies()["position"][1]
+    a2 = p[:3] + _rot(p[3:7], sc.joints["anchor2"][0])
+    assert abs(a2[2]) < 2e-3
+    assert 2 * math.acos(min(1.0, abs(p[6]))) < 0.01
+    assert p[1] < 9.0                                    # it falls within its plane
+
+
+def test_universal_joint_keeps_the_angle_between_its_axes():
+    # Two bodies joined at a point, body 1's x axis and body 2's y axis kept
+    # at 90 degrees while the pair tumbles.
+    sc = scenes.joint_zoo()
+    k = int(np.nonzero(sc.joints["kind"] == abi.JOINT_UNIVERSAL)[0][0])
+    j = sc.joints[k]
+    w = OracleWorld(sc.params(), sc.gravity, precision=64)
+    w.load_scene(sc)
+    for _ in range(8):
+        w.step(30)
+        pos = w.bodies()["position"]
+        i1, i2 = int(j["body1"]["index"]), int(j["body2"]["index"])
+        a1 = _rot(pos[i1, 3:7], j["axis1"])
+        a2 = _rot(pos[i2, 3:7], j["axis2"])
+        ang = math.acos(max(-1.0, min(1.0, float(np.dot(a1, a2)))))
+        assert abs(ang - math.pi / 2) < 0.02
+        p1 = pos[i1, :3] + _rot(pos[i1, 3:7], j["anchor1"])
+        p2 = pos[i2, :3] + _rot(pos[i2, 3:7], j["anchor2"])
+        assert np.linalg.norm(p1 - p2) < 0.01
+
+
+def test_every_joint_kind_converges_to_one_solution_in_every_order():
+    sc = scenes.joint_zoo()
+    out = []
+    for order, sweep in ((ORDER_REFERENCE, abi.SWEEP_SEPARATE), (ORDER_COLOUR, abi.SWEEP_SEPARATE),
+                         (ORDER_COLOUR, abi.SWEEP_MANIFOLD)):
+        p = sc.params()
+        p.max_position_iterations = 0
+        p.solve_to_tolerance = 1
+        p.residual_tolerance = 1e-11
+        p.max_iterations_to_tolerance = 20000
+        p.sweep_order = sweep
+        w = OracleWorld(p, sc.gravity, precision=64, order=order)
+        w.load_scene(sc)
+        w.step(1)
+        assert w.counters()["residual"] <= 1e-11
+        out.append(w.bodies()["velocity"])
+    np.testing.assert_allclose(out[0], out[1], atol=1e-7)
+    np.testing.assert_allclose(out[0], out[2], atol=1e-7)
