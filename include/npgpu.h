@@ -144,8 +144,7 @@ typedef struct npgpu_collider_desc {
     uint32_t ccd_enabled;       /* rejected when non-zero: CCD is not built */
 } npgpu_collider_desc;
 
-/* Joint constraints (src/joint/), the ones made of unlimited bilateral
- * rows: BallConstraint (ball_constraint.rs) keeps anchor1 and anchor2
+/* Joint constraints (src/joint/): BallConstraint (ball_constraint.rs) keeps anchor1 and anchor2
  * together; FixedConstraint (fixed_constraint.rs) also keeps the frames
  * (body rotation x reference frame) aligned; RevoluteConstraint
  * (revolute_constraint.rs) keeps the anchors together and axis1, axis2
@@ -155,7 +154,12 @@ typedef struct npgpu_collider_desc {
  * RectangularConstraint (rectangular_constraint.rs) keeps anchor2 in that
  * plane and the bodies' rotations equal; UniversalConstraint
  * (universal_constraint.rs) keeps the anchors together and the angle between
- * the axes. */
+ * the axes; PrismaticConstraint (prismatic_constraint.rs) lets anchor2 slide
+ * along axis1 only, within the optional offset limits, the rotations equal;
+ * CylindricalConstraint (cylindrical_constraint.rs) lets it slide along and
+ * turn about axis1; PinSlotConstraint (pin_slot_constraint.rs) lets it slide
+ * along axis1 (axis_v1) and turn about axis3 (axis_w1, body 1) = axis2
+ * (axis_w2, body 2). */
 enum {
     NPGPU_JOINT_BALL = 0,
     NPGPU_JOINT_FIXED = 1,
@@ -163,7 +167,16 @@ enum {
     NPGPU_JOINT_CARTESIAN = 3,
     NPGPU_JOINT_PLANAR = 4,
     NPGPU_JOINT_RECTANGULAR = 5,
-    NPGPU_JOINT_UNIVERSAL = 6
+    NPGPU_JOINT_UNIVERSAL = 6,
+    NPGPU_JOINT_PRISMATIC = 7,
+    NPGPU_JOINT_CYLINDRICAL = 8,
+    NPGPU_JOINT_PIN_SLOT = 9
+};
+
+/* Prismatic offset limits (enable_min_offset / enable_max_offset). */
+enum {
+    NPGPU_JOINT_MIN_OFFSET = 1u << 0,
+    NPGPU_JOINT_MAX_OFFSET = 1u << 1
 };
 
 /* One joint constraint as its ::new builds it. Both bodies must belong to
@@ -179,19 +192,27 @@ typedef struct npgpu_joint_desc {
     float frame2[4];            /* FIXED, CARTESIAN: ref_frame2 */
     float break_force;          /* set_break_force; FLT_MAX (the default) never breaks */
     float break_torque;         /* set_break_torque */
-    float axis1[3];             /* REVOLUTE, PLANAR, RECTANGULAR, UNIVERSAL: unit axis in body 1's frame */
-    float axis2[3];             /* REVOLUTE, PLANAR, UNIVERSAL: unit axis in body 2's frame */
+    float axis1[3];             /* unit axis in body 1's frame (REVOLUTE, PLANAR, RECTANGULAR, UNIVERSAL,
+                                   PRISMATIC, CYLINDRICAL; PIN_SLOT: axis_v1) */
+    float axis2[3];             /* unit axis in body 2's frame (REVOLUTE, PLANAR, UNIVERSAL, CYLINDRICAL;
+                                   PIN_SLOT: axis_w2) */
     float angle;                /* UNIVERSAL: the angle kept between the axes */
+    uint32_t limit_flags;       /* PRISMATIC: NPGPU_JOINT_MIN_OFFSET | NPGPU_JOINT_MAX_OFFSET */
+    float axis3[3];             /* PIN_SLOT: axis_w1, in body 1's frame */
+    float min_offset;           /* PRISMATIC: the limits of the offset of anchor2 along axis1 */
+    float max_offset;
     uint32_t pad2;
 } npgpu_joint_desc;
 
 /* A joint's state after the last step: the impulses JointConstraint::
- * cache_impulses keeps (linear, then angular: x y z for a canonical-axis
- * row group, the rows in their order otherwise) and is_broken(). */
+ * cache_impulses keeps (its linear impulses, then its angular ones, in the
+ * joint's own order), the prismatic limit's impulse, and is_broken(). */
 typedef struct npgpu_joint_state {
     float impulses[6];
+    float limit_impulse;
     uint32_t broken;
     uint32_t active;            /* solved in the last step (JointConstraint::is_active) */
+    uint32_t pad;
 } npgpu_joint_state;
 
 /* IntegrationParameters (src/solver/integration_parameters.rs:5-190),
@@ -359,7 +380,8 @@ npgpu_status npgpu_apply_forces(npgpu_world* w, uint32_t n, const npgpu_handle* 
                                 const float* forces6, int auto_wake_up);
 
 /* DefaultJointConstraintSet::insert (joint_constraint.rs:54-72) of the joints
- * above, with the handles the host set gave them; inserting
+ * above (every joint constraint of the reference but the mouse constraint),
+ * with the handles the host set gave them; inserting
  * wakes both bodies up at the next step (mechanical_world.rs:167-175). A
  * joint's impulses start at zero and persist across steps. The solver holds
  * the active joints beside the contact manifolds: capacity_pairs bounds the

@@ -96,7 +96,9 @@ class ColliderDesc(C.Structure):
 
 # Joint kinds (BallConstraint, FixedConstraint, RevoluteConstraint, CartesianConstraint,
 # PlanarConstraint, RectangularConstraint, UniversalConstraint)
-JOINT_BALL, JOINT_FIXED, JOINT_REVOLUTE, JOINT_CARTESIAN, JOINT_PLANAR, JOINT_RECTANGULAR, JOINT_UNIVERSAL = range(7)
+(JOINT_BALL, JOINT_FIXED, JOINT_REVOLUTE, JOINT_CARTESIAN, JOINT_PLANAR, JOINT_RECTANGULAR, JOINT_UNIVERSAL,
+ JOINT_PRISMATIC, JOINT_CYLINDRICAL, JOINT_PIN_SLOT) = range(10)
+JOINT_MIN_OFFSET, JOINT_MAX_OFFSET = 1, 2
 
 
 class JointDesc(C.Structure):
@@ -114,16 +116,22 @@ class JointDesc(C.Structure):
         ("axis1", C.c_float * 3),
         ("axis2", C.c_float * 3),
         ("angle", C.c_float),
+        ("limit_flags", C.c_uint32),
+        ("axis3", C.c_float * 3),
+        ("min_offset", C.c_float),
+        ("max_offset", C.c_float),
         ("pad2", C.c_uint32),
     ]
 
 
 class JointState(C.Structure):
-    _fields_ = [("impulses", C.c_float * 6), ("broken", C.c_uint32), ("active", C.c_uint32)]
+    _fields_ = [("impulses", C.c_float * 6), ("limit_impulse", C.c_float), ("broken", C.c_uint32),
+                ("active", C.c_uint32), ("pad", C.c_uint32)]
 
 
 def joint_desc(kind, body1, body2, anchor1=(0, 0, 0), anchor2=(0, 0, 0), frame1=(0, 0, 0, 1), frame2=(0, 0, 0, 1),
-               break_force=None, break_torque=None, axis1=(1, 0, 0), axis2=(1, 0, 0), angle=0.0):
+               break_force=None, break_torque=None, axis1=(1, 0, 0), axis2=(1, 0, 0), angle=0.0, axis3=(1, 0, 0),
+               min_offset=None, max_offset=None):
     """A JointDesc as the joint kind's ::new builds it (body handles as
     (index, generation) pairs or Handle)."""
     d = JointDesc()
@@ -139,7 +147,11 @@ def joint_desc(kind, body1, body2, anchor1=(0, 0, 0), anchor2=(0, 0, 0), frame1=
     d.break_torque = FLT_MAX if break_torque is None else break_torque
     d.axis1[:] = [float(x) for x in axis1]
     d.axis2[:] = [float(x) for x in axis2]
+    d.axis3[:] = [float(x) for x in axis3]
     d.angle = float(angle)
+    d.limit_flags = (JOINT_MIN_OFFSET if min_offset is not None else 0) | (JOINT_MAX_OFFSET if max_offset is not None else 0)
+    d.min_offset = 0.0 if min_offset is None else float(min_offset)
+    d.max_offset = 0.0 if max_offset is None else float(max_offset)
     return d
 
 

@@ -427,7 +427,8 @@ public:
     void set_break_force(float f) { desc.break_force = f; }
     void set_break_torque(float t) { desc.break_torque = t; }
     bool is_broken() const { return broken_; }
-    // The impulses cache_impulses kept in the last step: linear, then angular.
+    // The impulses cache_impulses kept in the last step: linear, then angular,
+    // then a prismatic limit's.
     const float* impulses() const { return impulses_; }
     npgpu_joint_desc desc;
 
@@ -440,7 +441,7 @@ protected:
         set3(desc.anchor1, anchor1);
         set3(desc.anchor2, anchor2);
         desc.frame1[3] = desc.frame2[3] = 1.0f;
-        desc.axis1[0] = desc.axis2[0] = 1.0f;
+        desc.axis1[0] = desc.axis2[0] = desc.axis3[0] = 1.0f;
         desc.break_force = desc.break_torque = std::numeric_limits<float>::max();
     }
     static void set3(float* o, Vector3 v) {
@@ -457,7 +458,7 @@ protected:
 private:
     friend class GpuMechanicalWorld;
     bool broken_ = false;
-    float impulses_[6] = {0, 0, 0, 0, 0, 0};
+    float impulses_[7] = {0, 0, 0, 0, 0, 0, 0};
 };
 
 // BallConstraint::new(b1, b2, anchor1, anchor2) (src/joint/ball_constraint.rs:26-48):
@@ -540,8 +541,55 @@ public:
     }
 };
 
+// PrismaticConstraint::new(b1, b2, anchor1, axis1, anchor2)
+// (src/joint/prismatic_constraint.rs:30-56): anchor2 slides along axis1, the
+// rotations equal, within the optional offset limits.
+class PrismaticConstraint : public JointConstraintBase {
+public:
+    PrismaticConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis1, Vector3 anchor2)
+        : JointConstraintBase(NPGPU_JOINT_PRISMATIC, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis1);
+    }
+    void enable_min_offset(float limit) {
+        desc.min_offset = limit;
+        desc.limit_flags |= NPGPU_JOINT_MIN_OFFSET;
+    }
+    void enable_max_offset(float limit) {
+        desc.max_offset = limit;
+        desc.limit_flags |= NPGPU_JOINT_MAX_OFFSET;
+    }
+    void disable_min_offset() { desc.limit_flags &= ~uint32_t(NPGPU_JOINT_MIN_OFFSET); }
+    void disable_max_offset() { desc.limit_flags &= ~uint32_t(NPGPU_JOINT_MAX_OFFSET); }
+};
+
+// CylindricalConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2): slides
+// along and turns about axis1 = axis2.
+class CylindricalConstraint : public JointConstraintBase {
+public:
+    CylindricalConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis1, Vector3 anchor2,
+                          Vector3 axis2)
+        : JointConstraintBase(NPGPU_JOINT_CYLINDRICAL, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis1);
+        set3(desc.axis2, axis2);
+    }
+};
+
+// PinSlotConstraint::new(b1, b2, anchor1, axis_v1, axis_w1, anchor2, axis_w2):
+// slides along axis_v1, turns about axis_w1 = axis_w2.
+class PinSlotConstraint : public JointConstraintBase {
+public:
+    PinSlotConstraint(BodyPartHandle b1, BodyPartHandle b2, Vector3 anchor1, Vector3 axis_v1, Vector3 axis_w1,
+                      Vector3 anchor2, Vector3 axis_w2)
+        : JointConstraintBase(NPGPU_JOINT_PIN_SLOT, b1, b2, anchor1, anchor2) {
+        set3(desc.axis1, axis_v1);
+        set3(desc.axis3, axis_w1);
+        set3(desc.axis2, axis_w2);
+    }
+};
+
 using JointConstraint = std::variant<BallConstraint, FixedConstraint, RevoluteConstraint, CartesianConstraint,
-                                     PlanarConstraint, RectangularConstraint, UniversalConstraint>;
+                                     PlanarConstraint, RectangularConstraint, UniversalConstraint,
+                                     PrismaticConstraint, CylindricalConstraint, PinSlotConstraint>;
 using DefaultJointConstraintHandle = Index;
 
 // DefaultJointConstraintSet (src/joint/joint_constraint.rs:31-130): the
@@ -702,7 +750,8 @@ private:
             std::visit([&](auto& x) {
                 JointConstraintBase& jb = x;
                 jb.broken_ = st[k].broken != 0;
-                std::memcpy(jb.impulses_, st[k].impulses, sizeof(jb.impulses_));
+                std::memcpy(jb.impulses_, st[k].impulses, sizeof(st[k].impulses));
+                jb.impulses_[6] = st[k].limit_impulse;
             }, *c);
         }
     }

@@ -262,8 +262,9 @@ __global__ void k_upload_joints(World w, const JointUpload* d, uint32_t n) {
     j.frame[2 * i] = make_float4(u.frame1[0], u.frame1[1], u.frame1[2], u.frame1[3]);
     j.frame[2 * i + 1] = make_float4(u.frame2[0], u.frame2[1], u.frame2[2], u.frame2[3]);
     j.brk[i] = make_float2(u.brk_force2, u.brk_torque2);
-    j.axis[2 * i] = make_float4(u.axis1[0], u.axis1[1], u.axis1[2], u.angle);
-    j.axis[2 * i + 1] = make_float4(u.axis2[0], u.axis2[1], u.axis2[2], 0.0f);
+    j.axis[3 * i] = make_float4(u.axis1[0], u.axis1[1], u.axis1[2], u.angle);
+    j.axis[3 * i + 1] = make_float4(u.axis2[0], u.axis2[1], u.axis2[2], u.min_offset);
+    j.axis[3 * i + 2] = make_float4(u.axis3[0], u.axis3[1], u.axis3[2], u.max_offset);
     if (u.reset) {
         j.imp[2 * i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         j.imp[2 * i + 1] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);

@@ -998,10 +998,42 @@ struct JointGroup {
 // cancel_relative_angular_velocity[_wrt_axis] and
 // restrict_relative_angular_velocity_to_axis (helper.rs:167-296, 422-551,
 // 614-699); the subspace basis of an axis is the contact model's tangent basis.
-__device__ __forceinline__ uint32_t joint_groups(uint32_t kind, np::Q q1, np::Q q2, np::V ax1, np::V ax2,
-                                                 JointGroup* g) {
+// relative_eq!(a, b) of two f32 (approx's defaults: epsilon and max
+// relative difference f32::EPSILON).
+__device__ __forceinline__ bool relative_eq_f(float a, float b) {
+    const float d = fabsf(a - b);
+    if (d <= FLT_EPSILON) return true;
+    const float m = fabsf(a) > fabsf(b) ? fabsf(a) : fabsf(b);
+    return d <= m * FLT_EPSILON;
+}
+
+// The offset-limit row of a prismatic joint (unit_constraint.rs:33-123): none
+// while the offset of anchor2 along the axis is within the limits; else a
+// force along -axis (below the minimum) or +axis (above the maximum) whose
+// impulse stays in [0, max], or an unlimited one when the limits are equal.
+__device__ __forceinline__ JointGroup limit_group(np::V axis, float offset, uint32_t info, float mn, float mx) {
+    const np::V zero = np::mk(0.0f, 0.0f, 0.0f);
+    JointGroup g{JR_LIMIT, 0u, 6u, {zero, zero, zero}};
+    const bool has_min = (info & JI_MIN_OFFSET) != 0u, has_max = (info & JI_MAX_OFFSET) != 0u;
+    if (has_min && has_max && relative_eq_f(mn, mx)) {
+        g.kind = JR_LINEAR;
+        g.rows = 1u;
+        g.d[0] = axis;
+    } else if (has_min && offset <= mn) {
+        g.rows = 1u;
+        g.d[0] = np::neg(axis);
+    } else if (has_max && offset >= mx) {
+        g.rows = 1u;
+        g.d[0] = axis;
+    }
+    return g;
+}
+
+__device__ __forceinline__ uint32_t joint_groups(uint32_t kind, np::Q q1, np::Q q2, np::V a1, np::V a2,
+                                                 const float4* ax, uint32_t info, JointGroup* g) {
     const np::V ex = basis_axis(0), ey = basis_axis(1), ez = basis_axis(2), zero = np::mk(0.0f, 0.0f, 0.0f);
     const JointGroup lin3{JR_LINEAR, 3u, 0u, {ex, ey, ez}}, ang3{JR_ANGULAR, 3u, 3u, {ex, ey, ez}};
+    const np::V ax1 = v3(ax[0]), ax2 = v3(ax[1]), ax3 = v3(ax[2]);
     switch (kind) {
     case NPGPU_JOINT_BALL: g[0] = lin3; return 1;
     case NPGPU_JOINT_FIXED: g[0] = lin3; g[1] = ang3; return 2;
@@ -1025,12 +1057,34 @@ __device__ __forceinline__ uint32_t joint_groups(uint32_t kind, np::Q q1, np::Q 
         g[0] = JointGroup{JR_LINEAR, 1u, 0u, {np::qrot(q1, ax1), zero, zero}};
         g[1] = ang3;
         return 2;
-    default: {   // NPGPU_JOINT_UNIVERSAL
+    case NPGPU_JOINT_UNIVERSAL: {
         np::V o;
         float n;
         const bool has = unit_try(np::cross(np::qrot(q1, ax1), np::qrot(q2, ax2)), FLT_EPSILON, o, n);
         g[0] = lin3;
         g[1] = JointGroup{JR_ANGULAR, has ? 1u : 0u, 3u, {has ? o : zero, zero, zero}};
+        return 2;
+    }
+    case NPGPU_JOINT_PRISMATIC: {
+        // restrict_relative_linear_velocity_to_axis, cancel_relative_angular_velocity,
+        // then the offset limit (prismatic_constraint.rs).
+        const np::V a = np::qrot(q1, ax1);
+        np::V t1, t2;
+        tangent_basis(a, t1, t2);
+        g[0] = JointGroup{JR_LINEAR, 2u, 0u, {t1, t2, zero}};
+        g[1] = ang3;
+        g[2] = limit_group(a, np::dot(a, np::sub(a2, a1)), info, ax[1].w, ax[2].w);
+        return 3;
+    }
+    default: {
+        // Cylindrical: both restricted to axis1; pin-slot: the linear rows to
+        // axis1 (axis_v1), the angular rows to axis3 (axis_w1).
+        const np::V al = np::qrot(q1, ax1), aa = np::qrot(q1, kind == NPGPU_JOINT_PIN_SLOT ? ax3 : ax1);
+        np::V t1, t2, u1, u2;
+        tangent_basis(al, t1, t2);
+        tangent_basis(aa, u1, u2);
+        g[0] = JointGroup{JR_LINEAR, 2u, 0u, {t1, t2, zero}};
+        g[1] = JointGroup{JR_ANGULAR, 2u, 3u, {u1, u2, zero}};
         return 2;
     }
     }
@@ -1051,8 +1105,10 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
     const np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
     const np::V a1 = body_point(v3(b.pos_t[bb1]), q1, v3(w.j.anchor[2 * j]));
     const np::V a2 = body_point(v3(b.pos_t[bb2]), q2, v3(w.j.anchor[2 * j + 1]));
-    JointGroup grp[2];
-    const uint32_t ng = joint_groups(w.j.info[j] & JI_KIND_MASK, q1, q2, v3(w.j.axis[2 * j]), v3(w.j.axis[2 * j + 1]), grp);
+    JointGroup grp[3];
+    const uint32_t info = w.j.info[j], kind = info & JI_KIND_MASK;
+    const float4 axes[3] = {w.j.axis[3 * j], w.j.axis[3 * j + 1], w.j.axis[3 * j + 2]};
+    const uint32_t ng = joint_groups(kind, q1, q2, a1, a2, axes, info, grp);
     float4* pr4 = w.s.pos_rec + (size_t)m * kPosRec;
     pr4[4] = make_float4(0.0f, 0.0f, 0.0f, __uint_as_float(kJointBit | j));
     pr4[6] = make_float4(__uint_as_float(bb1), __uint_as_float(bb2), __uint_as_float(v1.info), __uint_as_float(v2.info));
@@ -1062,7 +1118,7 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
     const float4 imp[2] = {w.j.imp[2 * j], w.j.imp[2 * j + 1]};
     for (uint32_t k = 0; k < ng; ++k) {
         const JointGroup& G = grp[k];
-        const bool ang = G.kind == JR_ANGULAR;
+        const bool ang = G.kind == JR_ANGULAR;   // limit rows are linear
         float R[3][kRowFloats];
 #pragma unroll
         for (int r = 0; r < 3; ++r) {
@@ -1094,9 +1150,10 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
                 ro[kRowF4 * r + 6] = make_float4(R[r][RF_R], R[r][RF_RHS], code, 0.0f);
             }
         }
-        const float4 im = imp[G.slot / 3u];
-        const float iv[3] = {im.x, im.y, im.z};
-        lam[k] = make_float4(G.rows > 0u ? iv[0] : 0.0f, G.rows > 1u ? iv[1] : 0.0f, G.rows > 2u ? iv[2] : 0.0f, 0.0f);
+        const float iv[7] = {imp[0].x, imp[0].y, imp[0].z, imp[1].x, imp[1].y, imp[1].z, imp[0].w};
+        float l[3] = {0.0f, 0.0f, 0.0f};
+        for (uint32_t r = 0; r < G.rows; ++r) l[r] = iv[joint_slot(kind, k, r, false)];
+        lam[k] = make_float4(l[0], l[1], l[2], 0.0f);
     }
 }
 
@@ -1407,7 +1464,8 @@ __device__ __forceinline__ void joint_rows(const RS& src, uint32_t k, float4 l, 
     for (uint32_t r = 0; r < rows; ++r) {
         const RowRec R = src.row(k, (int)r);
         float ni = li[r] - R.r * (row_dot(R, dv, h1, h2) + R.rhs);
-        ni = ni < -FLT_MAX ? -FLT_MAX : (ni > FLT_MAX ? FLT_MAX : ni);
+        const float lo = joint_limit(R.mu) ? 0.0f : -FLT_MAX;
+        ni = ni < lo ? lo : (ni > FLT_MAX ? FLT_MAX : ni);
         const float dl = ni - li[r];
         li[r] = ni;
         row_axpy(R, dv, dl, h1, h2);
@@ -1508,7 +1566,8 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
                     else if (h1) d = side_dot_j(J1, dv.a);
                     else if (h2) d = side_dot_j(J2, dv.b);
                     float ni = li[r] - c.r[r] * (d + c.rhs[r]);
-                    ni = ni < -FLT_MAX ? -FLT_MAX : (ni > FLT_MAX ? FLT_MAX : ni);
+                    const float lo = joint_limit(c.mu) ? 0.0f : -FLT_MAX;
+                    ni = ni < lo ? lo : (ni > FLT_MAX ? FLT_MAX : ni);
                     dl = ni - li[r];
                     li[r] = ni;
                 }
@@ -1703,7 +1762,8 @@ __device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, in
                 float J1[6], J2[6];
                 if (h1) joint_side_j(ang, d[r], c.pos1, false, mask & 0x3fu, J1);
                 if (h2) joint_side_j(ang, d[r], c.pos2, true, (mask >> 8) & 0x3fu, J2);
-                residual_row_j(J1, J2, c.r[r], c.rhs[r], li[r], dv, h1, h2, RES_BILATERAL, 0.0f, 0.0f, acc);
+                residual_row_j(J1, J2, c.r[r], c.rhs[r], li[r], dv, h1, h2,
+                               joint_limit(c.mu) ? RES_NORMAL : RES_BILATERAL, 0.0f, 0.0f, acc);
             }
             continue;
         }
@@ -2272,19 +2332,19 @@ __global__ void k_cache_integrate(World w, StepParams p, bool posef) {
             // fixed_constraint.rs:174-199): the impulses, and the joint breaks
             // when |impulse|^2 / dt^2 exceeds the squared break force / torque.
             const uint32_t j = q & ~kJointBit;
-            float4 imp[2] = {w.j.imp[2 * j], w.j.imp[2 * j + 1]};
+            const float4 i0 = w.j.imp[2 * j], i1 = w.j.imp[2 * j + 1];
+            float iv[7] = {i0.x, i0.y, i0.z, i1.x, i1.y, i1.z, i0.w};
+            const uint32_t kind = w.j.info[j] & JI_KIND_MASK;
             for (uint32_t k = 0; k < nc; ++k) {
-                const float code = w.s.con[((size_t)m * kMaxContacts + k) * 4].w;
-                const uint32_t rows = joint_rows_of(code);
-                const float4 l = w.s.lam[(size_t)m * kMaxContacts + k];
-                float4& o = imp[joint_angular(code) ? 1 : 0];
-                if (rows > 0u) o.x = l.x;
-                if (rows > 1u) o.y = l.y;
-                if (rows > 2u) o.z = l.z;
+                const uint32_t rows = joint_rows_of(w.s.con[((size_t)m * kMaxContacts + k) * 4].w);
+                const float4 l4 = w.s.lam[(size_t)m * kMaxContacts + k];
+                const float l[3] = {l4.x, l4.y, l4.z};
+                for (uint32_t r = 0; r < rows; ++r) iv[joint_slot(kind, k, r, true)] = l[r];
             }
+            const float4 imp[2] = {make_float4(iv[0], iv[1], iv[2], iv[6]), make_float4(iv[3], iv[4], iv[5], 0.0f)};
             w.j.imp[2 * j] = imp[0];
             w.j.imp[2 * j + 1] = imp[1];
-            if (joint_breaks(w.j.info[j] & JI_KIND_MASK, imp[0], imp[1], w.j.brk[j], p.inv_dt))
+            if (joint_breaks(kind, imp[0], imp[1], w.j.brk[j], p.inv_dt))
                 w.j.state[j] |= JS_BROKEN;
             continue;
         }
@@ -2409,9 +2469,12 @@ __device__ __forceinline__ np::V axis_separation(np::V a1, np::V a2) {
 // along body 1's axis (cancel_relative_translation_wrt_axis), R the frames'
 // relative rotation (cancel_relative_rotation), AL the axes' alignment
 // (align_axis), RA the angle between the axes (restore_angle_between_axis).
-enum { JP_T = 1, JP_TA = 2, JP_R_FRAMES = 3, JP_R_BODIES = 4, JP_AL = 5, JP_RA = 6 };
-__device__ __forceinline__ void joint_position_ops(uint32_t kind, int* op) {
-    op[0] = op[1] = 0;
+// PA the anchor's distance from the axis line (project_anchor_to_axis), AL3
+// the alignment of axis3 with axis2, LIM the prismatic offset limits
+// (unit_constraint.rs:125-198).
+enum { JP_T = 1, JP_TA = 2, JP_R_FRAMES = 3, JP_R_BODIES = 4, JP_AL = 5, JP_RA = 6, JP_PA = 7, JP_AL3 = 8, JP_LIM = 9 };
+__device__ __forceinline__ void joint_position_ops(uint32_t kind, uint32_t info, int* op) {
+    op[0] = op[1] = op[2] = 0;
     switch (kind) {
     case NPGPU_JOINT_BALL: op[0] = JP_T; break;
     case NPGPU_JOINT_FIXED: op[0] = JP_R_FRAMES; op[1] = JP_T; break;
@@ -2419,7 +2482,14 @@ __device__ __forceinline__ void joint_position_ops(uint32_t kind, int* op) {
     case NPGPU_JOINT_CARTESIAN: op[0] = JP_R_FRAMES; break;
     case NPGPU_JOINT_PLANAR: op[0] = JP_TA; op[1] = JP_AL; break;
     case NPGPU_JOINT_RECTANGULAR: op[0] = JP_TA; op[1] = JP_R_BODIES; break;
-    default: op[0] = JP_T; op[1] = JP_RA; break;   // universal
+    case NPGPU_JOINT_UNIVERSAL: op[0] = JP_T; op[1] = JP_RA; break;
+    case NPGPU_JOINT_PRISMATIC:
+        op[0] = JP_PA;
+        op[1] = JP_R_BODIES;
+        if (info & (JI_MIN_OFFSET | JI_MAX_OFFSET)) op[2] = JP_LIM;
+        break;
+    case NPGPU_JOINT_CYLINDRICAL: op[0] = JP_AL; op[1] = JP_PA; break;
+    default: op[0] = JP_AL3; op[1] = JP_PA; break;   // pin-slot
     }
 }
 
@@ -2455,14 +2525,14 @@ __device__ __forceinline__ void joint_position(const World& w, const StepParams&
         v2.inv_mass = s.im;
         v2.inv_I = s.I;
     }
-    const uint32_t kind = w.j.info[j] & JI_KIND_MASK;
+    const uint32_t info = w.j.info[j], kind = info & JI_KIND_MASK;
     const np::V la1 = v3(w.j.anchor[2 * j]), la2 = v3(w.j.anchor[2 * j + 1]);
-    const float4 ax1 = w.j.axis[2 * j], ax2 = w.j.axis[2 * j + 1];
+    const float4 ax1 = w.j.axis[3 * j], ax2 = w.j.axis[3 * j + 1], ax3 = w.j.axis[3 * j + 2];
     moved1 = moved2 = false;
-    int ops[2];
-    joint_position_ops(kind, ops);
+    int ops[3];
+    joint_position_ops(kind, info, ops);
     float J1[6], J2[6], W1[6], W2[6];
-    for (int o = 0; o < 2 && ops[o] != 0; ++o) {
+    for (int o = 0; o < 3 && ops[o] != 0; ++o) {
         const int op = ops[o];
         const np::V a1 = body_point(t1, q1, la1), a2 = body_point(t2, q2, la2);
         bool angular = false, have = false;
@@ -2487,10 +2557,28 @@ __device__ __forceinline__ void joint_position(const World& w, const StepParams&
             }
             angular = true;
             have = unit_try(np::qscaled_axis(np::qmul(r2, np::qconj(r1))), p.allowed_angular_error, dir, depth);
-        } else if (op == JP_AL) {
+        } else if (op == JP_AL || op == JP_AL3) {
             angular = true;
-            const np::V e = axis_separation(np::qrot(q1, v3(ax1)), np::qrot(q2, v3(ax2)));
+            const np::V e = axis_separation(np::qrot(q1, v3(op == JP_AL ? ax1 : ax3)), np::qrot(q2, v3(ax2)));
             have = unit_try(e, p.allowed_angular_error, dir, depth);
+        } else if (op == JP_PA) {
+            const np::V ax = np::qrot(q1, v3(ax1));
+            const np::V proj = np::add(a1, np::mul(ax, np::dot(ax, np::sub(a2, a1))));
+            have = unit_try(np::sub(a2, proj), p.allowed_linear_error, dir, depth);
+        } else if (op == JP_LIM) {
+            const np::V ax = np::qrot(q1, v3(ax1));
+            const float offset = np::dot(ax, np::sub(a2, a1));
+            depth = 0.0f;
+            dir = ax;
+            if (info & JI_MIN_OFFSET) {
+                depth = ax2.w - offset;
+                dir = np::neg(ax);
+            }
+            if (depth < 0.0f && (info & JI_MAX_OFFSET)) {
+                depth = offset - ax3.w;
+                dir = ax;
+            }
+            have = depth > p.allowed_linear_error;
         } else {   // JP_RA
             angular = true;
             float cur;

@@ -883,7 +883,7 @@ static npgpu_status ensure_joint_capacity(npgpu_world* w, uint32_t need) {
     }
     JA(nj.info, cap) JA(nj.state, cap) JA(nj.body, 2 * (size_t)cap) JA(nj.local, cap)
     JA(nj.anchor, 2 * (size_t)cap) JA(nj.frame, 2 * (size_t)cap) JA(nj.imp, 2 * (size_t)cap) JA(nj.brk, cap)
-    JA(nj.axis, 2 * (size_t)cap)
+    JA(nj.axis, 3 * (size_t)cap)
 #undef JA
     if (!ok) {
         for (void* p : fresh) cudaFree(p);
@@ -904,7 +904,7 @@ static npgpu_status ensure_joint_capacity(npgpu_world* w, uint32_t need) {
         CK(cudaMemcpyAsync(nj.frame, oj.frame, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
         CK(cudaMemcpyAsync(nj.imp, oj.imp, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
         CK(cudaMemcpyAsync(nj.brk, oj.brk, sizeof(float2) * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
-        CK(cudaMemcpyAsync(nj.axis, oj.axis, sizeof(float4) * 2 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
+        CK(cudaMemcpyAsync(nj.axis, oj.axis, sizeof(float4) * 3 * n, cudaMemcpyDeviceToDevice, w->stream), "joints");
     }
     CK(cudaStreamSynchronize(w->stream), "joint arrays");
     for (void* p : {(void*)oj.info, (void*)oj.state, (void*)oj.body, (void*)oj.local, (void*)oj.anchor, (void*)oj.frame,
@@ -953,10 +953,11 @@ npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle*
         const npgpu_joint_desc& d = descs[k];
         if (handles[k].index >= (1u << 21) - 1u)
             return fail(w, NPGPU_ERR_CAPACITY, "joint index must be below 2^21 - 1");
-        if (d.kind > NPGPU_JOINT_UNIVERSAL)
-            return fail(w, NPGPU_ERR_INVALID_ARGUMENT,
-                        "unknown joint kind (ball, fixed, revolute, cartesian, planar, rectangular and universal "
-                        "joints are supported)");
+        if (d.kind > NPGPU_JOINT_PIN_SLOT)
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind");
+        if ((d.limit_flags & NPGPU_JOINT_MIN_OFFSET) && (d.limit_flags & NPGPU_JOINT_MAX_OFFSET) &&
+            !(d.min_offset <= d.max_offset))
+            return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "a prismatic joint's min offset must not exceed its max offset");
         if (!body_handle_ok(w, d.body1) || !body_handle_ok(w, d.body2))
             return fail(w, NPGPU_ERR_INVALID_HANDLE, "joint body handle is invalid");
         if (d.body1.index == d.body2.index)
@@ -964,7 +965,8 @@ npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle*
         if (w->hb[d.body1.index].world != w->hb[d.body2.index].world)
             return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "a joint's bodies must belong to the same world");
         if (!finite_n(d.anchor1, 3) || !finite_n(d.anchor2, 3) || !finite_n(d.frame1, 4) || !finite_n(d.frame2, 4) ||
-            !finite_n(d.axis1, 3) || !finite_n(d.axis2, 3) || !std::isfinite(d.angle) ||
+            !finite_n(d.axis1, 3) || !finite_n(d.axis2, 3) || !finite_n(d.axis3, 3) || !std::isfinite(d.angle) ||
+            !std::isfinite(d.min_offset) || !std::isfinite(d.max_offset) ||
             std::isnan(d.break_force) || std::isnan(d.break_torque))
             return fail(w, NPGPU_ERR_NAN, "joint description has a non-finite value");
     }
@@ -1002,7 +1004,14 @@ npgpu_status npgpu_upsert_joints(npgpu_world* w, uint32_t n, const npgpu_handle*
         std::memcpy(u.frame2, d.frame2, sizeof(u.frame2));
         std::memcpy(u.axis1, d.axis1, sizeof(u.axis1));
         std::memcpy(u.axis2, d.axis2, sizeof(u.axis2));
+        std::memcpy(u.axis3, d.axis3, sizeof(u.axis3));
         u.angle = d.angle;
+        u.min_offset = d.min_offset;
+        u.max_offset = d.max_offset;
+        if (d.kind == NPGPU_JOINT_PRISMATIC) {
+            if (d.limit_flags & NPGPU_JOINT_MIN_OFFSET) u.info |= JI_MIN_OFFSET;
+            if (d.limit_flags & NPGPU_JOINT_MAX_OFFSET) u.info |= JI_MAX_OFFSET;
+        }
         // set_break_force / set_break_torque keep the squares (f32).
         u.brk_force2 = d.break_force * d.break_force;
         u.brk_torque2 = d.break_torque * d.break_torque;
@@ -1045,6 +1054,8 @@ npgpu_status npgpu_get_joints(npgpu_world* w, uint32_t n, const npgpu_handle* ha
         const float4 a = imp[2 * j], b = imp[2 * j + 1];
         const float v[6] = {a.x, a.y, a.z, b.x, b.y, b.z};
         std::memcpy(out[k].impulses, v, sizeof(v));
+        out[k].limit_impulse = a.w;
+        out[k].pad = 0;
         out[k].broken = (state[j] & JS_BROKEN) ? 1u : 0u;
         out[k].active = (state[j] & JS_ACTIVE) ? 1u : 0u;
     }

@@ -120,24 +120,48 @@ struct Joints {
     uint32_t *local;                 // slot minus the smallest alive joint slot of its world (colouring priority)
     float4 *anchor;                  // 2 per joint: the anchors in their bodies' frames (xyz)
     float4 *frame;                   // 2 per joint: the reference frames (quaternion i j k w)
-    float4 *axis;                    // 2 per joint: the axes in their bodies' frames (xyz); .w of the first: angle
+    float4 *axis;                    // 3 per joint: axis1 (.w: angle), axis2 (.w: min offset), axis3 (.w: max offset)
     float4 *imp;                     // 2 per joint: the impulses (linear xyz, angular xyz)
     float2 *brk;                     // break force^2, break torque^2
 };
-enum : uint32_t { JI_KIND_MASK = 0xffu, JI_ALIVE = 1u << 8, JS_BROKEN = 1u << 0, JS_ACTIVE = 1u << 1 };
+enum : uint32_t {
+    JI_KIND_MASK = 0xffu, JI_ALIVE = 1u << 8, JI_MIN_OFFSET = 1u << 9, JI_MAX_OFFSET = 1u << 10,
+    JS_BROKEN = 1u << 0, JS_ACTIVE = 1u << 1
+};
 // A solver manifold list entry of a joint: kJointBit | joint slot.
 constexpr uint32_t kJointBit = 0x80000000u;
 // A joint's row group in the solver records: up to three rows of one kind
 // (forces along, or torques about, the record's directions: the normal slot
 // and the two friction-direction slots). The friction slot, non-negative for
 // a contact, holds -(4 kind + rows): kind 1 linear, 2 angular.
-enum : uint32_t { JR_LINEAR = 1u, JR_ANGULAR = 2u };
+// kind 3 is a linear row whose impulse stays in [0, max] (a prismatic offset
+// limit, unit_constraint.rs:33-123).
+enum : uint32_t { JR_LINEAR = 1u, JR_ANGULAR = 2u, JR_LIMIT = 3u };
 __host__ __device__ inline float joint_code(uint32_t kind, uint32_t rows) { return -(float)(4u * kind + rows); }
 __host__ __device__ inline uint32_t joint_rows_of(float code) { return (uint32_t)(-code) & 3u; }
 __host__ __device__ inline bool joint_angular(float code) { return ((uint32_t)(-code) >> 2) == JR_ANGULAR; }
+__host__ __device__ inline bool joint_limit(float code) { return ((uint32_t)(-code) >> 2) == JR_LIMIT; }
 // Row groups (solver records) of a joint kind.
 __host__ __device__ inline uint32_t joint_group_count(uint32_t kind) {
-    return (kind == NPGPU_JOINT_BALL || kind == NPGPU_JOINT_CARTESIAN) ? 1u : 2u;
+    if (kind == NPGPU_JOINT_BALL || kind == NPGPU_JOINT_CARTESIAN) return 1u;
+    return kind == NPGPU_JOINT_PRISMATIC ? 3u : 2u;
+}
+// The impulse slot row r of group g of a joint kind starts from (store
+// false) and is cached to (store true): 0-2 the joint's linear impulses, 3-5
+// its angular ones, 6 the prismatic limit's. The cylindrical and pin-slot
+// joints number their angular rows from DIM - 1 (cylindrical_constraint.rs,
+// pin_slot_constraint.rs): they start from angular impulses 0 and 1 and are
+// cached to linear impulse 2 and angular impulse 0.
+__host__ __device__ inline uint32_t joint_slot(uint32_t kind, uint32_t g, uint32_t r, bool store) {
+    switch (kind) {
+    case NPGPU_JOINT_CYLINDRICAL:
+    case NPGPU_JOINT_PIN_SLOT:
+        if (g == 1u) return store ? (r == 0u ? 2u : 3u) : 3u + r;
+        return r;
+    case NPGPU_JOINT_PRISMATIC: return g == 0u ? r : (g == 1u ? 3u + r : 6u);
+    case NPGPU_JOINT_CARTESIAN: return 3u + r;
+    default: return g == 0u ? r : 3u + r;
+    }
 }
 
 struct Pairs {
@@ -325,6 +349,7 @@ struct JointUpload {                 // one joint's description (info 0: removed
     float anchor1[3], anchor2[3], frame1[4], frame2[4];
     float brk_force2, brk_torque2;
     float axis1[3], axis2[3], angle;
+    float axis3[3], min_offset, max_offset;
 };
 struct MassUpdate {                  // new local inertia / com of a body
     uint32_t slot;

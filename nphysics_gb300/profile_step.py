@@ -23,7 +23,8 @@ captures that region's launches and nothing else. Regions:
 Workloads: pile (the 32^3 ball pile, one cooperative grid), cluster (the same
 pile under the per-world schedule: one thread-block cluster), batched
 (--worlds batched worlds, one block or warp per world), mixed (--bodies
-bodies of the mixed pile's recipe at its density).
+bodies of the mixed pile's recipe at its density), joints (--worlds worlds
+of every joint kind with contacts).
 """
 import argparse
 import math
@@ -54,6 +55,10 @@ def build(args):
         p.solver_schedule = abi.SCHEDULE_WORLDS
         p.world_threads = 256
         return sc, GpuWorld.for_scene(sc, p, pairs_per_collider=6), 60
+    if args.workload == "joints":
+        # Worlds of every joint kind with contacts, one block (or warp) per world.
+        sc = scenes.batched_zoo(n_worlds=args.worlds)
+        return sc, GpuWorld.for_scene(sc), 60
     n = args.bodies
     sc = scenes.mixed_pile(n=n, footprint=100.0 * math.sqrt(n / 100_000))
     return sc, GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=12), 300
@@ -63,7 +68,7 @@ def main(argv=None):
     import torch
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--workload", default="pile", choices=["pile", "cluster", "batched", "mixed"])
+    ap.add_argument("--workload", default="pile", choices=["pile", "cluster", "batched", "mixed", "joints"])
     ap.add_argument("--region", default="step", choices=["step", "e2e", "train", "query", "events", "static"])
     ap.add_argument("--queries", type=int, default=100_000)
     ap.add_argument("--side", type=int, default=32)

@@ -56,6 +56,7 @@ def joint_descs(n):
     j["break_torque"] = abi.FLT_MAX
     j["axis1"][:, 0] = 1.0
     j["axis2"][:, 0] = 1.0
+    j["axis3"][:, 0] = 1.0
     return j
 
 
@@ -689,15 +690,16 @@ def joint_zoo(seed=11, world=0, ground=True):
     the ground body."""
     rng = np.random.default_rng(seed)
     parts_b, parts_c, joints = [], [], []
-    g, gc = _ground(half=(15.0, 1.0, 15.0), world=world)
+    g, gc = _ground(half=(20.0, 1.0, 20.0), world=world)
     parts_b.append(g)
     parts_c.append(gc)
     nb = 1
     kinds = [abi.JOINT_BALL, abi.JOINT_FIXED, abi.JOINT_REVOLUTE, abi.JOINT_CARTESIAN, abi.JOINT_PLANAR,
-             abi.JOINT_RECTANGULAR, abi.JOINT_UNIVERSAL]
+             abi.JOINT_RECTANGULAR, abi.JOINT_UNIVERSAL, abi.JOINT_PRISMATIC, abi.JOINT_CYLINDRICAL, abi.JOINT_PIN_SLOT]
     for i, kind in enumerate(kinds):
-        x = -9.0 + 3.0 * i
-        two = kind in (abi.JOINT_BALL, abi.JOINT_FIXED, abi.JOINT_REVOLUTE, abi.JOINT_UNIVERSAL)
+        x = -13.5 + 3.0 * i
+        two = kind in (abi.JOINT_BALL, abi.JOINT_FIXED, abi.JOINT_REVOLUTE, abi.JOINT_UNIVERSAL,
+                       abi.JOINT_CYLINDRICAL, abi.JOINT_PIN_SLOT)
         n = 2 if two else 1
         b = body_descs(n)
         b["world"] = world
@@ -719,22 +721,30 @@ def joint_zoo(seed=11, world=0, ground=True):
             j["body1"]["index"], j["body2"]["index"] = nb, nb + 1
             j["anchor1"][0] = (0.4, 0.0, 0.0)
             j["anchor2"][0] = (-0.4, 0.0, 0.0)
+            perp = np.cross(ax, (0.0, 1.0, 0.0)) / np.linalg.norm(np.cross(ax, (0.0, 1.0, 0.0)))
             j["axis1"][0] = ax
-            j["axis2"][0] = ax if kind != abi.JOINT_UNIVERSAL else np.cross(ax, (0.0, 1.0, 0.0)) / np.linalg.norm(
-                np.cross(ax, (0.0, 1.0, 0.0)))
+            j["axis2"][0] = ax if kind != abi.JOINT_UNIVERSAL else perp
             if kind == abi.JOINT_UNIVERSAL:
                 j["angle"][0] = math.pi / 2
+            if kind == abi.JOINT_PIN_SLOT:
+                j["axis1"][0] = (1.0, 0.0, 0.0)      # the slot (axis_v1)
+                j["axis3"][0] = perp                 # the pin's axis on body 1 (axis_w1) ...
+                j["axis2"][0] = perp                 # ... and on body 2 (axis_w2)
         else:
             j["body1"]["index"], j["body2"]["index"] = 0, nb
             j["anchor1"][0] = (x, 2.5, 0.0)
             j["anchor2"][0] = (0.0, 0.0, 0.0)
             j["axis1"][0] = (0.0, 1.0, 0.0) if kind != abi.JOINT_RECTANGULAR else ax
             j["axis2"][0] = (0.0, 1.0, 0.0)
+            if kind == abi.JOINT_PRISMATIC:
+                # A vertical slider that falls onto its lower offset limit.
+                j["limit_flags"][0] = abi.JOINT_MIN_OFFSET | abi.JOINT_MAX_OFFSET
+                j["min_offset"][0], j["max_offset"][0] = -1.0, 0.5
         joints.append(j)
         nb += n
     drops = body_descs(6)
     drops["world"] = world
-    drops["position"][:, 0] = -9.0 + 3.0 * rng.integers(0, 7, 6) + rng.uniform(-0.3, 0.3, 6)
+    drops["position"][:, 0] = -13.5 + 3.0 * rng.integers(0, len(kinds), 6) + rng.uniform(-0.3, 0.3, 6)
     drops["position"][:, 1] = rng.uniform(4.0, 7.0, 6)
     drops["position"][:, 2] = rng.uniform(-0.3, 0.3, 6)
     drops["position"][:, 3:7] = uniform_quaternions(rng, 6)

@@ -119,12 +119,12 @@ class GpuWorld:
             self._joints.pop(int(h["index"]), None)
 
     def joints(self, handles):
-        """(impulses (n, 6), broken (n,), active (n,)) after the last step."""
+        """(impulses (n, 7): linear, angular, the limit's; broken (n,), active (n,)) after the last step."""
         handles = np.ascontiguousarray(handles)
         out = (abi.JointState * max(len(handles), 1))()
         self._check(self.L.npgpu_get_joints(self.w, len(handles), _ptr(handles, abi.Handle), out), "get_joints")
         n = len(handles)
-        imp = np.array([list(out[k].impulses) for k in range(n)], np.float32).reshape(n, 6)
+        imp = np.array([list(out[k].impulses) + [out[k].limit_impulse] for k in range(n)], np.float32).reshape(n, 7)
         broken = np.array([out[k].broken for k in range(n)], bool)
         active = np.array([out[k].active for k in range(n)], bool)
         return imp, broken, active

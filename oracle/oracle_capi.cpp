@@ -121,8 +121,8 @@ int orc_remove_joints(orc_world* o, uint32_t n, const npgpu_handle* h) {
     return 0;
 }
 
-// Per joint slot: 6 impulses (f64), then broken and active flags.
-int orc_get_joints(orc_world* o, uint32_t n, const npgpu_handle* h, double* imp6, uint32_t* flags2) {
+// Per joint: 7 impulses (f64: linear 3, angular 3, the limit's), then broken and active flags.
+int orc_get_joints(orc_world* o, uint32_t n, const npgpu_handle* h, double* imp7, uint32_t* flags2) {
     int s = 0;
     DISPATCH(o, {
         for (uint32_t i = 0; i < n && !s; ++i) {
@@ -132,7 +132,7 @@ int orc_get_joints(orc_world* o, uint32_t n, const npgpu_handle* h, double* imp6
                 break;
             }
             const auto& j = w.joints[h[i].index];
-            for (int k = 0; k < 6; ++k) imp6[6 * i + k] = double(j.imp[k]);
+            for (int k = 0; k < 7; ++k) imp7[7 * i + k] = double(j.imp[k]);
             flags2[2 * i] = j.broken ? 1u : 0u;
             flags2[2 * i + 1] = j.active ? 1u : 0u;
         }

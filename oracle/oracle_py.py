@@ -130,9 +130,9 @@ class OracleWorld:
                     "remove joints")
 
     def joints(self, handles):
-        """(impulses (n, 6) f64, broken (n,), active (n,)) after the last step."""
+        """(impulses (n, 7) f64: linear, angular, the limit's; broken (n,), active (n,)) after the last step."""
         h = np.ascontiguousarray(handles)
-        imp = np.zeros((len(h), 6), np.float64)
+        imp = np.zeros((len(h), 7), np.float64)
         flags = np.zeros((len(h), 2), np.uint32)
         self._check(self.L.orc_get_joints(self.w, len(h), _ptr(h), _ptr(imp), _ptr(flags)), "get joints")
         return imp, flags[:, 0].astype(bool), flags[:, 1].astype(bool)

@@ -266,6 +266,7 @@ template <class R> struct Row {
     R mu;
     bool friction;
     bool bilateral;        // a joint row: Independent limits of +-max (helper.rs:186-189)
+    bool limit;            // ... or of [0, max] (a prismatic offset limit, unit_constraint.rs:94-103)
     int joint, joint_slot; // its joint and impulse slot (0-2 linear, 3-5 angular)
     void* cache;           // MContact the impulse is cached to
     int cache_slot;
@@ -280,10 +281,12 @@ template <class R> struct Joint {
     uint32_t kind = NPGPU_JOINT_BALL, b1 = 0, b2 = 0;
     V3<R> anchor1, anchor2;     // in the bodies' frames
     Quat<R> frame1, frame2;     // the reference frames (fixed, cartesian)
-    V3<R> axis1, axis2;         // the axes in the bodies' frames (revolute, planar, rectangular, universal)
+    V3<R> axis1, axis2, axis3;  // the axes in the bodies' frames (axis3: the pin-slot's axis_w1)
     R angle = R(0);             // universal: the angle kept between the axes
+    bool has_min = false, has_max = false;   // prismatic offset limits
+    R min_offset = R(0), max_offset = R(0);
     R brk_force2, brk_torque2;  // set_break_force / set_break_torque keep the squares
-    R imp[6] = {R(0), R(0), R(0), R(0), R(0), R(0)};   // linear x y z, angular x y z
+    R imp[7] = {R(0), R(0), R(0), R(0), R(0), R(0), R(0)};   // linear 0-2, angular 3-5, the limit's 6
     bool broken = false, active = false;
 };
 
@@ -447,7 +450,10 @@ public:
         auto body_ok = [&](const npgpu_handle& b) {
             return b.index < bodies.size() && bodies[b.index].alive && bodies[b.index].generation == b.generation;
         };
-        if (d.kind > NPGPU_JOINT_UNIVERSAL) return fail(NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind");
+        if (d.kind > NPGPU_JOINT_PIN_SLOT) return fail(NPGPU_ERR_INVALID_ARGUMENT, "unknown joint kind");
+        if ((d.limit_flags & NPGPU_JOINT_MIN_OFFSET) && (d.limit_flags & NPGPU_JOINT_MAX_OFFSET) &&
+            !(d.min_offset <= d.max_offset))
+            return fail(NPGPU_ERR_INVALID_ARGUMENT, "min offset above max offset");
         if (!body_ok(d.body1) || !body_ok(d.body2)) return fail(NPGPU_ERR_INVALID_HANDLE, "joint body handle is invalid");
         if (d.body1.index == d.body2.index) return fail(NPGPU_ERR_INVALID_ARGUMENT, "a joint needs two different bodies");
         if (bodies[d.body1.index].world != bodies[d.body2.index].world)
@@ -471,7 +477,12 @@ public:
         j.frame2 = Quat<R>{R(d.frame2[0]), R(d.frame2[1]), R(d.frame2[2]), R(d.frame2[3])};
         j.axis1 = v3<R>(R(d.axis1[0]), R(d.axis1[1]), R(d.axis1[2]));
         j.axis2 = v3<R>(R(d.axis2[0]), R(d.axis2[1]), R(d.axis2[2]));
+        j.axis3 = v3<R>(R(d.axis3[0]), R(d.axis3[1]), R(d.axis3[2]));
         j.angle = R(d.angle);
+        j.has_min = d.kind == NPGPU_JOINT_PRISMATIC && (d.limit_flags & NPGPU_JOINT_MIN_OFFSET) != 0;
+        j.has_max = d.kind == NPGPU_JOINT_PRISMATIC && (d.limit_flags & NPGPU_JOINT_MAX_OFFSET) != 0;
+        j.min_offset = R(d.min_offset);
+        j.max_offset = R(d.max_offset);
         const R f = R(d.break_force), t = R(d.break_torque);
         j.brk_force2 = f * f;
         j.brk_torque2 = t * t;
@@ -1814,21 +1825,48 @@ public:
     static V3<R> basis(int r) { return v3<R>(r == 0 ? R(1) : R(0), r == 1 ? R(1) : R(0), r == 2 ? R(1) : R(0)); }
 
     // A joint's row group: `rows` forces along (linear) or torques about the
-    // directions d, their impulses in slots slot..slot + rows - 1.
+    // directions d; a limit group's impulse stays in [0, max].
     struct JointGroup {
         bool angular;
-        int rows, slot;
+        int rows;
+        bool limit;
         V3<R> d[3];
     };
+    // The impulse slot row r of group g starts from (store false) and is
+    // cached to (store true): 0-2 linear, 3-5 angular, 6 the prismatic
+    // limit's. The cylindrical and pin-slot joints number their angular rows
+    // from DIM - 1 (cylindrical_constraint.rs, pin_slot_constraint.rs): they
+    // start from angular impulses 0 and 1 and are cached to linear impulse 2
+    // and angular impulse 0.
+    static int joint_slot(uint32_t kind, int g, int r, bool store) {
+        switch (kind) {
+        case NPGPU_JOINT_CYLINDRICAL:
+        case NPGPU_JOINT_PIN_SLOT:
+            if (g == 1) return store ? (r == 0 ? 2 : 3) : 3 + r;
+            return r;
+        case NPGPU_JOINT_PRISMATIC: return g == 0 ? r : (g == 1 ? 3 + r : 6);
+        case NPGPU_JOINT_CARTESIAN: return 3 + r;
+        default: return g == 0 ? r : 3 + r;
+        }
+    }
+    // relative_eq! with approx's default epsilon and max relative difference.
+    static bool relative_eq(R a, R b) {
+        const R eps = std::numeric_limits<R>::epsilon();
+        const R d = std::fabs(a - b);
+        if (d <= eps) return true;
+        return d <= std::max(std::fabs(a), std::fabs(b)) * eps;
+    }
     // The row groups of a joint kind as each constraint's velocity_constraints
     // builds them (ball_constraint.rs:80-127, fixed_constraint.rs:107-172,
     // revolute_constraint.rs:181-266, cartesian_constraint.rs,
-    // planar_constraint.rs, rectangular_constraint.rs,
-    // universal_constraint.rs) from helper.rs:167-296, 422-551, 614-699; the
-    // subspace basis of an axis is the contact model's tangent basis.
-    int joint_groups(const Joint<R>& jt, Quat<R> q1, Quat<R> q2, JointGroup* g) const {
+    // planar_constraint.rs, rectangular_constraint.rs, universal_constraint.rs,
+    // prismatic_constraint.rs, cylindrical_constraint.rs,
+    // pin_slot_constraint.rs) from helper.rs:167-296, 422-551, 614-857 and the
+    // prismatic offset limit (unit_constraint.rs:33-123); the subspace basis
+    // of an axis is the contact model's tangent basis.
+    int joint_groups(const Joint<R>& jt, Quat<R> q1, Quat<R> q2, V3<R> a1, V3<R> a2, JointGroup* g) const {
         const V3<R> ex = basis(0), ey = basis(1), ez = basis(2), zero = v3<R>(R(0), R(0), R(0));
-        const JointGroup lin3{false, 3, 0, {ex, ey, ez}}, ang3{true, 3, 3, {ex, ey, ez}};
+        const JointGroup lin3{false, 3, false, {ex, ey, ez}}, ang3{true, 3, false, {ex, ey, ez}};
         switch (jt.kind) {
         case NPGPU_JOINT_BALL: g[0] = lin3; return 1;
         case NPGPU_JOINT_FIXED: g[0] = lin3; g[1] = ang3; return 2;
@@ -1837,28 +1875,54 @@ public:
             V3<R> t1, t2;
             tangent_basis(qrot(q1, jt.axis1), t1, t2);
             g[0] = lin3;
-            g[1] = JointGroup{true, 2, 3, {t1, t2, zero}};
+            g[1] = JointGroup{true, 2, false, {t1, t2, zero}};
             return 2;
         }
         case NPGPU_JOINT_PLANAR: {
             const V3<R> a = qrot(q1, jt.axis1);
             V3<R> t1, t2;
             tangent_basis(a, t1, t2);
-            g[0] = JointGroup{false, 1, 0, {a, zero, zero}};
-            g[1] = JointGroup{true, 2, 3, {t1, t2, zero}};
+            g[0] = JointGroup{false, 1, false, {a, zero, zero}};
+            g[1] = JointGroup{true, 2, false, {t1, t2, zero}};
             return 2;
         }
         case NPGPU_JOINT_RECTANGULAR:
-            g[0] = JointGroup{false, 1, 0, {qrot(q1, jt.axis1), zero, zero}};
+            g[0] = JointGroup{false, 1, false, {qrot(q1, jt.axis1), zero, zero}};
             g[1] = ang3;
             return 2;
-        default: {   // universal
+        case NPGPU_JOINT_UNIVERSAL: {
             V3<R> o;
             R n;
             const bool has = unit_try(cross(qrot(q1, jt.axis1), qrot(q2, jt.axis2)),
                                       std::numeric_limits<R>::epsilon(), o, n);
             g[0] = lin3;
-            g[1] = JointGroup{true, has ? 1 : 0, 3, {has ? o : zero, zero, zero}};
+            g[1] = JointGroup{true, has ? 1 : 0, false, {has ? o : zero, zero, zero}};
+            return 2;
+        }
+        case NPGPU_JOINT_PRISMATIC: {
+            const V3<R> a = qrot(q1, jt.axis1);
+            V3<R> t1, t2;
+            tangent_basis(a, t1, t2);
+            g[0] = JointGroup{false, 2, false, {t1, t2, zero}};
+            g[1] = ang3;
+            const R offset = dot(a, a2 - a1);
+            g[2] = JointGroup{false, 0, true, {zero, zero, zero}};
+            if (jt.has_min && jt.has_max && relative_eq(jt.min_offset, jt.max_offset)) {
+                g[2] = JointGroup{false, 1, false, {a, zero, zero}};
+            } else if (jt.has_min && offset <= jt.min_offset) {
+                g[2] = JointGroup{false, 1, true, {-a, zero, zero}};
+            } else if (jt.has_max && offset >= jt.max_offset) {
+                g[2] = JointGroup{false, 1, true, {a, zero, zero}};
+            }
+            return 3;
+        }
+        default: {   // cylindrical, pin-slot
+            const V3<R> al = qrot(q1, jt.axis1), aa = qrot(q1, jt.kind == NPGPU_JOINT_PIN_SLOT ? jt.axis3 : jt.axis1);
+            V3<R> t1, t2, u1, u2;
+            tangent_basis(al, t1, t2);
+            tangent_basis(aa, u1, u2);
+            g[0] = JointGroup{false, 2, false, {t1, t2, zero}};
+            g[1] = JointGroup{true, 2, false, {u1, u2, zero}};
             return 2;
         }
         }
@@ -1871,16 +1935,17 @@ public:
         const Body<R>& b1 = bodies[jt.b1];
         const Body<R>& b2 = bodies[jt.b2];
         const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
-        JointGroup g[2];
-        const int ng = joint_groups(jt, b1.pos.q, b2.pos.q, g);
+        JointGroup g[3];
+        const int ng = joint_groups(jt, b1.pos.q, b2.pos.q, a1, a2, g);
         for (int t = 0; t < ng; ++t)
             for (int r = 0; r < g[t].rows; ++r) {
                 Row<R> row = g[t].angular ? make_row_angular(b1, jt.b1, b2, jt.b2, g[t].d[r])
                                           : make_row(b1, jt.b1, b2, jt.b2, a1, a2, g[t].d[r], R(0));
-                row.impulse = jt.imp[g[t].slot + r];
+                row.impulse = jt.imp[joint_slot(jt.kind, t, r, false)];
                 row.bilateral = true;
+                row.limit = g[t].limit;
                 row.joint = int(j);
-                row.joint_slot = g[t].slot + r;
+                row.joint_slot = joint_slot(jt.kind, t, r, true);
                 row.cache = nullptr;
                 out.push_back(int(rows.size()));
                 rows.push_back(row);
@@ -2150,9 +2215,10 @@ public:
     // +-max (a joint row, helper.rs:186-189).
     void solve_bilateral(Row<R>& r) {
         const R mx = std::numeric_limits<R>::max();
+        const R lo = r.limit ? R(0) : -mx;
         R dimpulse = jdot(r) + r.rhs;
         R ni = r.impulse - r.r * dimpulse;
-        ni = ni < -mx ? -mx : (ni > mx ? mx : ni);
+        ni = ni < lo ? lo : (ni > mx ? mx : ni);
         R dl = ni - r.impulse;
         r.impulse = ni;
         axpy(r, dl);
@@ -2199,7 +2265,7 @@ public:
             double lam = double(r.impulse);
             double x = lam - double(r.r) * d;
             double p;
-            if (r.bilateral) p = x;
+            if (r.bilateral) p = r.limit ? (x > 0 ? x : 0) : x;
             else if (!r.friction) p = x > 0 ? x : 0;
             else {
                 double mx = double(r.mu) * double(rows[r.dep].impulse);
@@ -2369,12 +2435,16 @@ public:
     // axes' alignment (align_axis) or the angle between them
     // (restore_angle_between_axis), helper.rs:298-418, 553-611, 701-769,
     // 921-998. An error below the allowed one is skipped.
-    enum { JP_T = 1, JP_TA = 2, JP_R_FRAMES = 3, JP_R_BODIES = 4, JP_AL = 5, JP_RA = 6 };
+    // PA the anchor's distance from the axis line (project_anchor_to_axis,
+    // helper.rs:858-919), AL3 the alignment of axis3 with axis2, LIM the
+    // prismatic offset limits (unit_constraint.rs:125-198).
+    enum { JP_T = 1, JP_TA = 2, JP_R_FRAMES = 3, JP_R_BODIES = 4, JP_AL = 5, JP_RA = 6, JP_PA = 7, JP_AL3 = 8,
+           JP_LIM = 9 };
     void joint_position(uint32_t j) {
         Joint<R>& jt = joints[j];
         Body<R>& b1 = bodies[jt.b1];
         Body<R>& b2 = bodies[jt.b2];
-        int ops[2] = {0, 0};
+        int ops[3] = {0, 0, 0};
         switch (jt.kind) {
         case NPGPU_JOINT_BALL: ops[0] = JP_T; break;
         case NPGPU_JOINT_FIXED: ops[0] = JP_R_FRAMES; ops[1] = JP_T; break;
@@ -2382,10 +2452,17 @@ public:
         case NPGPU_JOINT_CARTESIAN: ops[0] = JP_R_FRAMES; break;
         case NPGPU_JOINT_PLANAR: ops[0] = JP_TA; ops[1] = JP_AL; break;
         case NPGPU_JOINT_RECTANGULAR: ops[0] = JP_TA; ops[1] = JP_R_BODIES; break;
-        default: ops[0] = JP_T; ops[1] = JP_RA; break;
+        case NPGPU_JOINT_UNIVERSAL: ops[0] = JP_T; ops[1] = JP_RA; break;
+        case NPGPU_JOINT_PRISMATIC:
+            ops[0] = JP_PA;
+            ops[1] = JP_R_BODIES;
+            if (jt.has_min || jt.has_max) ops[2] = JP_LIM;
+            break;
+        case NPGPU_JOINT_CYLINDRICAL: ops[0] = JP_AL; ops[1] = JP_PA; break;
+        default: ops[0] = JP_AL3; ops[1] = JP_PA; break;
         }
         R J1[6], J2[6], W1[6], W2[6];
-        for (int o = 0; o < 2 && ops[o] != 0; ++o) {
+        for (int o = 0; o < 3 && ops[o] != 0; ++o) {
             const int op = ops[o];
             const V3<R> a1 = iso_pt(b1.pos, jt.anchor1), a2 = iso_pt(b2.pos, jt.anchor2);
             bool angular = false, have = false;
@@ -2410,10 +2487,29 @@ public:
                 }
                 angular = true;
                 have = unit_try(qscaled_axis(qmul(r2, qconj(r1))), R(params.allowed_angular_error), dir, depth);
-            } else if (op == JP_AL) {
+            } else if (op == JP_AL || op == JP_AL3) {
                 angular = true;
-                have = unit_try(axis_separation(qrot(b1.pos.q, jt.axis1), qrot(b2.pos.q, jt.axis2)),
+                have = unit_try(axis_separation(qrot(b1.pos.q, op == JP_AL ? jt.axis1 : jt.axis3),
+                                                qrot(b2.pos.q, jt.axis2)),
                                 R(params.allowed_angular_error), dir, depth);
+            } else if (op == JP_PA) {
+                const V3<R> ax = qrot(b1.pos.q, jt.axis1);
+                const V3<R> proj = a1 + ax * dot(ax, a2 - a1);
+                have = unit_try(a2 - proj, R(params.allowed_linear_error), dir, depth);
+            } else if (op == JP_LIM) {
+                const V3<R> ax = qrot(b1.pos.q, jt.axis1);
+                const R offset = dot(ax, a2 - a1);
+                depth = R(0);
+                dir = ax;
+                if (jt.has_min) {
+                    depth = jt.min_offset - offset;
+                    dir = -ax;
+                }
+                if (depth < R(0) && jt.has_max) {
+                    depth = offset - jt.max_offset;
+                    dir = ax;
+                }
+                have = depth > R(params.allowed_linear_error);
             } else {
                 angular = true;
                 R cur;

@@ -74,6 +74,11 @@ pub const NPGPU_JOINT_CARTESIAN: u32 = 3;
 pub const NPGPU_JOINT_PLANAR: u32 = 4;
 pub const NPGPU_JOINT_RECTANGULAR: u32 = 5;
 pub const NPGPU_JOINT_UNIVERSAL: u32 = 6;
+pub const NPGPU_JOINT_PRISMATIC: u32 = 7;
+pub const NPGPU_JOINT_CYLINDRICAL: u32 = 8;
+pub const NPGPU_JOINT_PIN_SLOT: u32 = 9;
+pub const NPGPU_JOINT_MIN_OFFSET: u32 = 1;
+pub const NPGPU_JOINT_MAX_OFFSET: u32 = 2;
 
 #[repr(C)]
 #[derive(Copy, Clone, Default)]
@@ -91,6 +96,10 @@ pub struct npgpu_joint_desc {
     pub axis1: [f32; 3],
     pub axis2: [f32; 3],
     pub angle: f32,
+    pub limit_flags: u32,
+    pub axis3: [f32; 3],
+    pub min_offset: f32,
+    pub max_offset: f32,
     pub pad2: u32,
 }
 
@@ -98,8 +107,10 @@ pub struct npgpu_joint_desc {
 #[derive(Copy, Clone, Default)]
 pub struct npgpu_joint_state {
     pub impulses: [f32; 6],
+    pub limit_impulse: f32,
     pub broken: u32,
     pub active: u32,
+    pub pad: u32,
 }
 
 #[repr(C)]

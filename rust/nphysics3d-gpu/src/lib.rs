@@ -8,11 +8,11 @@
 //! and writes the new poses, velocities and activation back into the set, as
 //! `MechanicalWorld::step` leaves them. Scenes the GPU step does not support
 //! (multibodies, FEM or mass-spring bodies, shapes other than balls,
-//! cuboids and capsules, sensors, CCD colliders, prismatic, cylindrical or
-//! pin-slot joints, force generators) make `step` panic with the library's
-//! message, where nphysics would have run them. Balls, cuboids and capsules
-//! are supported; ball, fixed, revolute, cartesian, planar, rectangular and
-//! universal joints go in as `GpuJoint`s.
+//! cuboids and capsules, sensors, CCD colliders, mouse constraints, force
+//! generators) make `step` panic with the library's message, where nphysics
+//! would have run them. Balls, cuboids and capsules are supported; the ten
+//! joint constraints (ball, fixed, revolute, cartesian, planar, rectangular,
+//! universal, prismatic, cylindrical, pin-slot) go in as `GpuJoint`s.
 pub mod ffi;
 
 use std::collections::HashMap;
@@ -23,9 +23,9 @@ use nalgebra::{DVector, Isometry3, Point3, Quaternion, Translation3, Unit, UnitQ
 use ncollide3d::shape::{Ball, Capsule, Cuboid};
 use nphysics3d::algebra::{Force3, ForceType, Velocity3};
 use nphysics3d::force_generator::ForceGeneratorSet;
-use nphysics3d::joint::{BallConstraint, CartesianConstraint, DefaultJointConstraintHandle, FixedConstraint,
-                        JointConstraint, JointConstraintSet, PlanarConstraint, RectangularConstraint,
-                        RevoluteConstraint, UniversalConstraint};
+use nphysics3d::joint::{BallConstraint, CartesianConstraint, CylindricalConstraint, DefaultJointConstraintHandle,
+                        FixedConstraint, JointConstraint, JointConstraintSet, PinSlotConstraint, PlanarConstraint,
+                        PrismaticConstraint, RectangularConstraint, RevoluteConstraint, UniversalConstraint};
 use nphysics3d::material::{BasicMaterial, MaterialCombineMode};
 use nphysics3d::object::{Body, BodyPartHandle, BodySet, BodyStatus, Collider, ColliderSet, DefaultBodyHandle,
                          DefaultColliderHandle, Ground, RigidBody};
@@ -265,13 +265,57 @@ impl GpuJoint {
         j
     }
 
+    /// PrismaticConstraint::new (src/joint/prismatic_constraint.rs:30-56);
+    /// `enable_min_offset` / `enable_max_offset` set its limits.
+    pub fn prismatic(b1: Part, b2: Part, anchor1: Point3<f32>, axis1: Unit<Vector3<f32>>, anchor2: Point3<f32>)
+                     -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_PRISMATIC, b1, b2, &anchor1, &anchor2,
+                               Box::new(PrismaticConstraint::new(b1, b2, anchor1, axis1, anchor2)));
+        j.desc.axis1 = v3a(&axis1);
+        j
+    }
+
+    /// PrismaticConstraint::enable_min_offset / enable_max_offset.
+    pub fn enable_min_offset(&mut self, limit: f32) {
+        self.desc.min_offset = limit;
+        self.desc.limit_flags |= ffi::NPGPU_JOINT_MIN_OFFSET;
+        on_inner!(self.inner, x => x.enable_min_offset(limit), PrismaticConstraint<f32, DefaultBodyHandle>);
+    }
+    pub fn enable_max_offset(&mut self, limit: f32) {
+        self.desc.max_offset = limit;
+        self.desc.limit_flags |= ffi::NPGPU_JOINT_MAX_OFFSET;
+        on_inner!(self.inner, x => x.enable_max_offset(limit), PrismaticConstraint<f32, DefaultBodyHandle>);
+    }
+
+    /// CylindricalConstraint::new (src/joint/cylindrical_constraint.rs).
+    pub fn cylindrical(b1: Part, b2: Part, anchor1: Point3<f32>, axis1: Unit<Vector3<f32>>, anchor2: Point3<f32>,
+                       axis2: Unit<Vector3<f32>>) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_CYLINDRICAL, b1, b2, &anchor1, &anchor2,
+                               Box::new(CylindricalConstraint::new(b1, b2, anchor1, axis1, anchor2, axis2)));
+        j.desc.axis1 = v3a(&axis1);
+        j.desc.axis2 = v3a(&axis2);
+        j
+    }
+
+    /// PinSlotConstraint::new (src/joint/pin_slot_constraint.rs).
+    pub fn pin_slot(b1: Part, b2: Part, anchor1: Point3<f32>, axis_v1: Unit<Vector3<f32>>,
+                    axis_w1: Unit<Vector3<f32>>, anchor2: Point3<f32>, axis_w2: Unit<Vector3<f32>>) -> Self {
+        let mut j = Self::with(ffi::NPGPU_JOINT_PIN_SLOT, b1, b2, &anchor1, &anchor2,
+                               Box::new(PinSlotConstraint::new(b1, b2, anchor1, axis_v1, axis_w1, anchor2, axis_w2)));
+        j.desc.axis1 = v3a(&axis_v1);
+        j.desc.axis3 = v3a(&axis_w1);
+        j.desc.axis2 = v3a(&axis_w2);
+        j
+    }
+
     /// set_break_force of the constraint.
     pub fn set_break_force(&mut self, f: f32) {
         self.desc.break_force = f;
         on_inner!(self.inner, x => x.set_break_force(f), BallConstraint<f32, DefaultBodyHandle>,
                   FixedConstraint<f32, DefaultBodyHandle>, RevoluteConstraint<f32, DefaultBodyHandle>,
                   PlanarConstraint<f32, DefaultBodyHandle>, RectangularConstraint<f32, DefaultBodyHandle>,
-                  UniversalConstraint<f32, DefaultBodyHandle>);
+                  UniversalConstraint<f32, DefaultBodyHandle>, PrismaticConstraint<f32, DefaultBodyHandle>,
+                  CylindricalConstraint<f32, DefaultBodyHandle>, PinSlotConstraint<f32, DefaultBodyHandle>);
     }
 
     /// set_break_torque of the constraint (every kind but the ball joint).
@@ -280,12 +324,18 @@ impl GpuJoint {
         on_inner!(self.inner, x => x.set_break_torque(t), FixedConstraint<f32, DefaultBodyHandle>,
                   RevoluteConstraint<f32, DefaultBodyHandle>, CartesianConstraint<f32, DefaultBodyHandle>,
                   PlanarConstraint<f32, DefaultBodyHandle>, RectangularConstraint<f32, DefaultBodyHandle>,
-                  UniversalConstraint<f32, DefaultBodyHandle>);
+                  UniversalConstraint<f32, DefaultBodyHandle>, PrismaticConstraint<f32, DefaultBodyHandle>,
+                  CylindricalConstraint<f32, DefaultBodyHandle>, PinSlotConstraint<f32, DefaultBodyHandle>);
     }
 
     /// The impulses the GPU step cached for this joint (linear, then angular).
     pub fn impulses(&self) -> [f32; 6] {
         self.gpu.impulses
+    }
+
+    /// The prismatic limit's impulse of the last GPU step.
+    pub fn limit_impulse(&self) -> f32 {
+        self.gpu.limit_impulse
     }
 }
 
