@@ -50,8 +50,11 @@ namespace cg = cooperative_groups;
 #ifndef NPGPU_EXCHANGE_TU
 #define NPGPU_EXCHANGE_TU 0
 #endif
+// The solver kernels come in two instantiations: with joint rows (JOINTS,
+// launched when the world has joint slots) and without, so that contact-only
+// worlds run code with no joint branch or call in it.
 enum ExchangeKernel { XK_COLOUR, XK_VELOCITY, XK_POSITION, XK_CLUSTER_VELOCITY, XK_CLUSTER_POSITION };
-const void* exchange_kernel(ExchangeKernel k);
+const void* exchange_kernel(ExchangeKernel k, bool joints = false);
 cudaError_t launch_activation(const World& w, const StepParams& p, unsigned nbb, unsigned npb, cudaStream_t st);
 
 constexpr int kItemThreads = 256;
@@ -555,18 +558,24 @@ struct Dot2 {
 };
 
 // phi = lambda - proj(lambda - r (J dv + rhs)) of one row, squared and summed
-// with lambda^2 into `acc`; proj = max(., 0) for a normal row and the clamp
-// to +-mu lambda_n for a friction row.
-// Row kinds of the residual's projection.
+// with lambda^2 into `acc`; proj = max(., 0) for a normal row (and a
+// prismatic limit row), the clamp to +-mu lambda_n for a friction row, and
+// the identity for a joint's bilateral row (Independent limits of +-FLT_MAX,
+// helper.rs:186-189). jac(side, J) forms the row's Jacobian on side 0 or 1.
 enum { RES_NORMAL = 0, RES_FRICTION = 1, RES_BILATERAL = 2 };
-__device__ __forceinline__ void residual_row_j(const float* J1, const float* J2, float r, float rhs, float lam,
-                                               const DV& dv, bool has1, bool has2, int kind, float normal_impulse,
-                                               float mu, ResidualSums& acc) {
+template <class Jac>
+__device__ __forceinline__ void residual_row_f(const Jac& jac, float r, float rhs, float lam, const DV& dv, bool has1,
+                                               bool has2, int kind, float normal_impulse, float mu, ResidualSums& acc) {
     Dot2 dot;
-    if (has1)
-        for (int k = 0; k < 6; ++k) dot.prod(J1[k], dv.a[k]);
-    if (has2)
-        for (int k = 0; k < 6; ++k) dot.prod(J2[k], dv.b[k]);
+    float J[6];
+    if (has1) {
+        jac(0, J);
+        for (int k = 0; k < 6; ++k) dot.prod(J[k], dv.a[k]);
+    }
+    if (has2) {
+        jac(1, J);
+        for (int k = 0; k < 6; ++k) dot.prod(J[k], dv.b[k]);
+    }
     dot.sum(rhs, 0.0f);
     const FF d = two_sum(dot.s, dot.c);
     // rd = r d; x = lambda - rd; lambda - x = rd when the projection keeps x.
@@ -576,7 +585,7 @@ __device__ __forceinline__ void residual_row_j(const float* J1, const float* J2,
     x = ff_norm(FF{x.hi, __fsub_rn(x.lo, rd.lo)});
     FF phi = rd;
     if (kind == RES_BILATERAL) {
-        // Independent limits of +-FLT_MAX (helper.rs:186-189): x stays.
+        // x stays: phi = rd.
     } else if (kind == RES_NORMAL) {
         if (!(x.hi > 0.0f || (x.hi == 0.0f && x.lo > 0.0f))) phi = FF{lam, 0.0f};
     } else {
@@ -593,13 +602,15 @@ __device__ __forceinline__ void residual_row_j(const float* J1, const float* J2,
     acc.l2 = ff_add(acc.l2, two_prod(lam, lam));
 }
 
+// A contact row: a force along dir at the lever arms pos1, pos2.
 __device__ __forceinline__ void residual_row(np::V dir, np::V pos1, np::V pos2, uint32_t mask, float r, float rhs,
                                              float lam, const DV& dv, bool has1, bool has2, bool friction,
                                              float normal_impulse, float mu, ResidualSums& acc) {
-    float J1[6], J2[6];
-    if (has1) side_j(pos1, dir, mask & 0x3fu, J1);
-    if (has2) side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J2);
-    residual_row_j(J1, J2, r, rhs, lam, dv, has1, has2, friction ? RES_FRICTION : RES_NORMAL, normal_impulse, mu, acc);
+    const auto jac = [&](int side, float* J) {
+        if (side == 0) side_j(pos1, dir, mask & 0x3fu, J);
+        else side_j(pos2, np::neg(dir), (mask >> 8) & 0x3fu, J);
+    };
+    residual_row_f(jac, r, rhs, lam, dv, has1, has2, friction ? RES_FRICTION : RES_NORMAL, normal_impulse, mu, acc);
 }
 
 __device__ __forceinline__ double block_sum(double v, double* sh) {
@@ -1101,7 +1112,7 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
     uint32_t mask = 0;
     if (b1 >= 0) mask |= ~(bi_flags(v1.info) >> 1) & 0x3fu;
     if (b2 >= 0) mask |= (~(bi_flags(v2.info) >> 1) & 0x3fu) << 8;
-    w.s.sm_mask[m] = mask;
+    w.s.sm_mask[m] = mask | kJointBit;   // the solver tasks take a joint's records apart from contacts'
     const np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
     const np::V a1 = body_point(v3(b.pos_t[bb1]), q1, v3(w.j.anchor[2 * j]));
     const np::V a2 = body_point(v3(b.pos_t[bb2]), q2, v3(w.j.anchor[2 * j + 1]));
@@ -1153,10 +1164,12 @@ static __device__ void assemble_joint(const World& w, const StepParams& p, uint3
         const float iv[7] = {imp[0].x, imp[0].y, imp[0].z, imp[1].x, imp[1].y, imp[1].z, imp[0].w};
         float l[3] = {0.0f, 0.0f, 0.0f};
         for (uint32_t r = 0; r < G.rows; ++r) l[r] = iv[joint_slot(kind, k, r, false)];
-        lam[k] = make_float4(l[0], l[1], l[2], 0.0f);
+        lam[k] = make_float4(l[0], l[1], l[2], -(float)(1u + G.rows));   // a joint record: w = -(1 + rows)
     }
 }
 
+// JOINTS: the world has joint slots (their manifolds are assembled too).
+template <bool JOINTS>
 __global__ void k_assemble(World w, StepParams p, bool rows) {
     const uint32_t ms = w.ctl->nsolver;
     const Bodies& b = w.b;
@@ -1184,7 +1197,7 @@ __global__ void k_assemble(World w, StepParams p, bool rows) {
                   ((uint32_t)(__popcll(ua) + __popcll(ub)) << 24);
         }
         w.s.sm_rk[m] = rk;
-        if (q & kJointBit) {
+        if (JOINTS && (q & kJointBit)) {
             assemble_joint(w, p, m, q & ~kJointBit, b1, b2, rows);
             continue;
         }
@@ -1454,34 +1467,10 @@ __device__ __forceinline__ void warm_rows(const RS& src, uint32_t nc, bool h1, b
 
 // The friction rows (sor_prox.rs:232-343) and the normal rows
 // (sor_prox.rs:181-230) of one task's contacts, from stored rows.
-// A joint's three bilateral rows from stored rows (Independent limits of
-// +-FLT_MAX, helper.rs:186-189).
-template <class RS>
-__device__ __forceinline__ void joint_rows(const RS& src, uint32_t k, float4 l, uint32_t rows, bool h1, bool h2,
-                                           DV& dv) {
-    float li[3] = {l.x, l.y, l.z};
-#pragma unroll 1
-    for (uint32_t r = 0; r < rows; ++r) {
-        const RowRec R = src.row(k, (int)r);
-        float ni = li[r] - R.r * (row_dot(R, dv, h1, h2) + R.rhs);
-        const float lo = joint_limit(R.mu) ? 0.0f : -FLT_MAX;
-        ni = ni < lo ? lo : (ni > FLT_MAX ? FLT_MAX : ni);
-        const float dl = ni - li[r];
-        li[r] = ni;
-        row_axpy(R, dv, dl, h1, h2);
-    }
-    src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
-}
-
 template <class RS>
 __device__ __forceinline__ void friction_rows(const RS& src, uint32_t nc, bool h1, bool h2, DV& dv) {
     for (uint32_t k = 0; k < nc; ++k) {
         const float4 l = src.get_lam(k);
-        const RowRec R1 = src.row(k, 1);
-        if (R1.mu < 0.0f) {
-            joint_rows(src, k, l, joint_rows_of(R1.mu), h1, h2, dv);
-            continue;
-        }
         const float li = l.x;
         float imps[2] = {l.y, l.z};
 #pragma unroll
@@ -1489,12 +1478,12 @@ __device__ __forceinline__ void friction_rows(const RS& src, uint32_t nc, bool h
             const float imp = imps[sdir];
             if (li == 0.0f) {
                 if (imp != 0.0f) {
-                    row_axpy(sdir == 0 ? R1 : src.row(k, 2), dv, -imp, h1, h2);
+                    row_axpy(src.row(k, 1 + sdir), dv, -imp, h1, h2);
                     imps[sdir] = 0.0f;
                 }
                 continue;
             }
-            const RowRec R = sdir == 0 ? R1 : src.row(k, 2);
+            const RowRec R = src.row(k, 1 + sdir);
             float mx = R.mu * li, mn = -mx;
             float dimp = row_dot(R, dv, h1, h2) + R.rhs;
             float ni = imp - R.r * dimp;
@@ -1512,7 +1501,6 @@ __device__ __forceinline__ void normal_rows(const RS& src, uint32_t nc, bool h1,
     for (uint32_t k = 0; k < nc; ++k) {
         const float4 l = src.get_lam(k);
         const RowRec R = src.row(k, 0);
-        if (R.mu < 0.0f) continue;   // a joint's rows run with the friction rows
         float imp = l.x;
         float dimp = row_dot(R, dv, h1, h2) + R.rhs;
         float ni = imp - R.r * dimp;
@@ -1523,11 +1511,85 @@ __device__ __forceinline__ void normal_rows(const RS& src, uint32_t nc, bool h1,
     }
 }
 
+// One pass over a joint's rows (its row groups' records) from stored rows:
+// the bilateral rows of sor_prox.rs:232-293 with Independent limits of
+// +-FLT_MAX (helper.rs:186-189), a prismatic limit row's within [0, max]. A
+// record's impulses carry w = -(1 + rows). The solver tasks dispatch a joint's
+// manifold here (sm_mask's kJointBit) and the call is out of line, Δv passed
+// and returned by value, so that the contact sweeps keep their registers.
+static __device__ __noinline__ DV joint_rows(const GlobalRows src, uint32_t nc, bool h1, bool h2, DV dv) {
+#pragma unroll 1
+    for (uint32_t k = 0; k < nc; ++k) {
+        const float4 l = src.get_lam(k);
+        const uint32_t rows = (uint32_t)(-l.w) - 1u;
+        float li[3] = {l.x, l.y, l.z};
+#pragma unroll 1
+        for (uint32_t r = 0; r < rows; ++r) {
+            const RowRec R = src.row(k, (int)r);
+            float ni = li[r] - R.r * (row_dot(R, dv, h1, h2) + R.rhs);
+            const float lo = joint_limit(R.mu) ? 0.0f : -FLT_MAX;
+            ni = ni < lo ? lo : (ni > FLT_MAX ? FLT_MAX : ni);
+            const float dl = ni - li[r];
+            li[r] = ni;
+            row_axpy(R, dv, dl, h1, h2);
+        }
+        src.set_lam(k, make_float4(li[0], li[1], li[2], l.w));
+    }
+    return dv;
+}
+
 // One velocity task from the compact records, rows rebuilt from the normal,
 // the friction directions and the lever arms: KIND 0 is the warm start
 // (sor_prox.rs:19-45), 1 the friction rows of an iteration
 // (sor_prox.rs:232-343), 2 its normal rows (sor_prox.rs:181-230).
 enum { SWEEP_WARM = 0, SWEEP_FRICTION = 1, SWEEP_NORMAL = 2, SWEEP_MANIFOLD = 3 };
+// A joint's rows from its compact records, rows rebuilt from the stored
+// directions and lever arms: the warm start (warm true) or one pass of the
+// bilateral rows (sor_prox.rs:232-293 with Independent limits: +-FLT_MAX, or
+// [0, max] for a prismatic limit). Dispatched per manifold and out of line,
+// Δv by value, so that the contact tasks keep their registers.
+static __device__ __noinline__ DV joint_task(const float4* con, float4* lam, const float4* tan, uint32_t nc,
+                                             uint32_t mask, const float4* sb, int g1, int g2, bool warm, DV dv) {
+    const bool h1 = g1 >= 0, h2 = g2 >= 0;
+    SB s1, s2;
+    if (h1) s1 = load_sb(sb, g1);
+    if (h2) s2 = load_sb(sb, g2);
+#pragma unroll 1
+    for (uint32_t k = 0; k < nc; ++k) {
+        const ContactRec c = load_con(con, k);
+        const float4 l = lam[k];
+        const float4 ta = __ldg(tan + 2 * k), tb = __ldg(tan + 2 * k + 1);
+        const np::V d[3] = {c.n, np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
+        const bool ang = joint_angular(c.mu), lim = joint_limit(c.mu);
+        const uint32_t rows = joint_rows_of(c.mu);
+        float li[3] = {l.x, l.y, l.z};
+#pragma unroll 1
+        for (uint32_t r = 0; r < rows; ++r) {
+            float J1[6], J2[6];
+            if (h1) joint_side_j(ang, d[r], c.pos1, false, mask & 0x3fu, J1);
+            if (h2) joint_side_j(ang, d[r], c.pos2, true, (mask >> 8) & 0x3fu, J2);
+            float dl = li[r];
+            if (warm) {
+                if (li[r] == 0.0f) continue;
+            } else {
+                float dd = 0.0f;
+                if (h1 && h2) dd = side_dot_j(J1, dv.a) + side_dot_j(J2, dv.b);
+                else if (h1) dd = side_dot_j(J1, dv.a);
+                else if (h2) dd = side_dot_j(J2, dv.b);
+                float ni = li[r] - c.r[r] * (dd + c.rhs[r]);
+                const float lo = lim ? 0.0f : -FLT_MAX;
+                ni = ni < lo ? lo : (ni > FLT_MAX ? FLT_MAX : ni);
+                dl = ni - li[r];
+                li[r] = ni;
+            }
+            if (h1) side_axpy_j(J1, s1, dl, dv.a);
+            if (h2) side_axpy_j(J2, s2, dl, dv.b);
+        }
+        if (!warm) lam[k] = make_float4(li[0], li[1], li[2], l.w);
+    }
+    return dv;
+}
+
 template <int KIND, class Src, class BM>
 __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, uint32_t mask, uint32_t sweep,
                                                   const BM& bm, bool h1, bool h2, DV& dv, Control* ctl) {
@@ -1541,42 +1603,6 @@ __device__ __forceinline__ void velocity_task_src(const Src& src, uint32_t nc, u
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = src.rec(k);
         float4 l = src.get_lam(k);
-        if (c.mu < 0.0f) {
-            // A joint's three bilateral rows (sor_prox.rs:232-293 with
-            // Independent limits): warm-started, then solved once per
-            // iteration with the friction rows.
-            if (kind == SWEEP_NORMAL) continue;
-            const bool ang = joint_angular(c.mu);
-            const uint32_t rows = joint_rows_of(c.mu);
-            float li[3] = {l.x, l.y, l.z};
-            np::V d[3];
-            d[0] = c.n;
-            src.tangents(c, k, d + 1);
-#pragma unroll 1
-            for (uint32_t r = 0; r < rows; ++r) {
-                float J1[6], J2[6];
-                if (h1) joint_side_j(ang, d[r], c.pos1, false, mask & 0x3fu, J1);
-                if (h2) joint_side_j(ang, d[r], c.pos2, true, (mask >> 8) & 0x3fu, J2);
-                float dl = li[r];
-                if (kind == SWEEP_WARM) {
-                    if (li[r] == 0.0f) continue;
-                } else {
-                    float d = 0.0f;
-                    if (h1 && h2) d = side_dot_j(J1, dv.a) + side_dot_j(J2, dv.b);
-                    else if (h1) d = side_dot_j(J1, dv.a);
-                    else if (h2) d = side_dot_j(J2, dv.b);
-                    float ni = li[r] - c.r[r] * (d + c.rhs[r]);
-                    const float lo = joint_limit(c.mu) ? 0.0f : -FLT_MAX;
-                    ni = ni < lo ? lo : (ni > FLT_MAX ? FLT_MAX : ni);
-                    dl = ni - li[r];
-                    li[r] = ni;
-                }
-                if (h1) side_axpy_j(J1, bm.get(0), dl, dv.a);
-                if (h2) side_axpy_j(J2, bm.get(1), dl, dv.b);
-            }
-            if (kind != SWEEP_WARM) src.set_lam(k, make_float4(li[0], li[1], li[2], 0.0f));
-            continue;
-        }
         if (kind == SWEEP_WARM) {
             np::V t[2];
             src.tangents(c, k, t);
@@ -1714,7 +1740,7 @@ __device__ __forceinline__ GlobalRows global_rows(const World& w, uint32_t m) {
 // The per-world kernels rebuild the rows from the compact records (their
 // batches are large enough for the stored rows' bytes to cost more than the
 // arithmetic they save).
-template <int KIND, class DvA>
+template <int KIND, bool JOINTS, class DvA>
 __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32_t sweep, int g1, int g2, int l1, int l2,
                                               const DvA& dva) {
     BodyMasses bm;
@@ -1726,7 +1752,15 @@ __device__ __forceinline__ void velocity_task(const World& w, uint32_t m, uint32
     DV dv;
     dva.load(g1 >= 0 ? l1 : -1, dv.a);
     dva.load(g2 >= 0 ? l2 : -1, dv.b);
-    velocity_task_src<KIND>(src, w.s.sm_nc[m], w.s.sm_mask[m], sweep, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
+    const uint32_t mask = w.s.sm_mask[m];
+    if (JOINTS && (mask & kJointBit)) {
+        // A joint's rows: warm-started, then solved once per iteration with
+        // the friction rows.
+        if (KIND == SWEEP_NORMAL) return;
+        dv = joint_task(src.con, src.lam, src.tan, w.s.sm_nc[m], mask, w.b.sb, g1, g2, KIND == SWEEP_WARM, dv);
+    } else {
+        velocity_task_src<KIND>(src, w.s.sm_nc[m], mask, sweep, bm, g1 >= 0, g2 >= 0, dv, w.ctl);
+    }
     dva.store(g1 >= 0 ? l1 : -1, dv.a);
     dva.store(g2 >= 0 ? l2 : -1, dv.b);
 }
@@ -1740,33 +1774,50 @@ __device__ __forceinline__ void cache_task(const World& w, uint32_t m, uint32_t 
     }
 }
 
+// The residual terms of a joint's rows (its row groups' records).
+__device__ __forceinline__ void joint_residual(const float4* con, const float4* lam, const float4* tan, uint32_t nc,
+                                               uint32_t mask, const DV& dv, bool h1, bool h2, ResidualSums& acc) {
+#pragma unroll 1
+    for (uint32_t k = 0; k < nc; ++k) {
+        const ContactRec c = load_con(con, k);
+        const float4 l = lam[k];
+        const bool ang = joint_angular(c.mu);
+        const uint32_t rows = joint_rows_of(c.mu);
+#pragma unroll 1
+        for (uint32_t r = 0; r < rows; ++r) {
+            np::V d = c.n;
+            if (r > 0) {
+                const float4 t = tan[2 * k + r - 1];
+                d = np::mk(t.x, t.y, t.z);
+            }
+            const auto jac = [&](int side, float* J) {
+                joint_side_j(ang, d, side ? c.pos2 : c.pos1, side != 0, side ? (mask >> 8) & 0x3fu : mask & 0x3fu, J);
+            };
+            const float li = r == 0 ? l.x : (r == 1 ? l.y : l.z);
+            const float rr = r == 0 ? c.r[0] : (r == 1 ? c.r[1] : c.r[2]);
+            const float rhs = r == 0 ? c.rhs[0] : (r == 1 ? c.rhs[1] : c.rhs[2]);
+            residual_row_f(jac, rr, rhs, li, dv, h1, h2, joint_limit(c.mu) ? RES_NORMAL : RES_BILATERAL, 0.0f, 0.0f,
+                           acc);
+        }
+    }
+}
+
 // FP64 residual terms of one manifold (normal rows, then friction rows with
 // the normal impulse as the limit).
+template <bool JOINTS>
 __device__ __forceinline__ void manifold_residual(const World& w, uint32_t m, int g1, int g2, const DV& dv,
                                                   ResidualSums& acc) {
     const bool h1 = g1 >= 0, h2 = g2 >= 0;
     const uint32_t nc = w.s.sm_nc[m], mask = w.s.sm_mask[m];
     const float4* lam = w.s.lam + (size_t)m * kMaxContacts;
     const float4* con = w.s.con + (size_t)m * kMaxContacts * 4;
+    if (JOINTS && (mask & kJointBit)) {
+        joint_residual(con, lam, w.s.tan + (size_t)m * kMaxContacts * 2, nc, mask, dv, h1, h2, acc);
+        return;
+    }
     for (uint32_t k = 0; k < nc; ++k) {
         const ContactRec c = load_con(con, k);
         float4 l = lam[k];
-        if (c.mu < 0.0f) {
-            // A joint's bilateral rows.
-            const bool ang = joint_angular(c.mu);
-            const uint32_t rows = joint_rows_of(c.mu);
-            const float li[3] = {l.x, l.y, l.z};
-            const float4 ta = w.s.tan[((size_t)m * kMaxContacts + k) * 2], tb = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
-            const np::V d[3] = {c.n, np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
-            for (uint32_t r = 0; r < rows; ++r) {
-                float J1[6], J2[6];
-                if (h1) joint_side_j(ang, d[r], c.pos1, false, mask & 0x3fu, J1);
-                if (h2) joint_side_j(ang, d[r], c.pos2, true, (mask >> 8) & 0x3fu, J2);
-                residual_row_j(J1, J2, c.r[r], c.rhs[r], li[r], dv, h1, h2,
-                               joint_limit(c.mu) ? RES_NORMAL : RES_BILATERAL, 0.0f, 0.0f, acc);
-            }
-            continue;
-        }
         const float4 ta = w.s.tan[((size_t)m * kMaxContacts + k) * 2], tb = w.s.tan[((size_t)m * kMaxContacts + k) * 2 + 1];
         const np::V t[2] = {np::mk(ta.x, ta.y, ta.z), np::mk(tb.x, tb.y, tb.z)};
         residual_row(np::neg(c.n), c.pos1, c.pos2, mask, c.r[0], c.rhs[0], l.x, dv, h1, h2, false, 0.0f, c.mu, acc);
@@ -1803,6 +1854,7 @@ struct TaskStats {
     unsigned long long exec_ns, wait_ns, tasks;
 };
 
+template <bool JOINTS>
 static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_t s_end, uint32_t ms, bool prof,
                                 bool learned, bool merged, TaskStats& ts, float4* cache) {
     const uint32_t T = gridDim.x * blockDim.x;
@@ -1816,7 +1868,10 @@ static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_
     const CachedRows cc{cache + threadIdx.x, global_rows(w, t)};
     uint32_t nc0 = 0;
     bool cached = false;
-    if (mt.n > 0 && cache != nullptr && s_begin > 0) {
+    // Joints' manifolds (sm_mask's kJointBit) take their own pass, from
+    // global memory.
+    const bool joints = JOINTS;
+    if (mt.n > 0 && cache != nullptr && s_begin > 0 && !(joints && (w.s.sm_mask[t] & kJointBit))) {
         nc0 = w.s.sm_nc[t];
         cached = true;
         cache_task(w, t, nc0, cc);
@@ -1844,10 +1899,15 @@ static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_
             if (prof) ts.wait_ns += te - tw;
             const uint32_t m = t + k * T;
             const bool h1 = b1 >= 0, h2 = b2 >= 0;
+            const bool jt = joints && (w.s.sm_mask[m] & kJointBit);
             if (sw == 0) {
-                // Learned starts need the check on the compact records.
-                if (learned) warm_task(w, m, b1, b2, dv);
+                // Learned starts need the check on the compact records; a
+                // joint's records start from their cached impulses.
+                if (learned && !jt) warm_task(w, m, b1, b2, dv);
                 else warm_rows(global_rows(w, m), w.s.sm_nc[m], h1, h2, dv);
+            } else if (jt) {
+                // A joint's rows run once per iteration, with the friction rows.
+                if (merged || (sw & 1u)) dv = joint_rows(global_rows(w, m), w.s.sm_nc[m], h1, h2, dv);
             } else if (k == 0 && cached) {
                 // Merged order: every sweep is the manifold's friction rows
                 // and then its normal rows; else odd sweeps are friction rows,
@@ -1885,6 +1945,7 @@ static __device__ bool velocity_sweeps(const World& w, uint32_t s_begin, uint32_
 }
 
 // FP64 residual over all rows; the result lands in ctl->residual.
+template <bool JOINTS>
 static __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, uint32_t& epoch, bool initial) {
     ResidualSums acc;
     GRID_FOR(m, ms) {
@@ -1892,7 +1953,7 @@ static __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, ui
         DV dv;
         load_dvf(w.b.dvf, b1, dv.a);
         load_dvf(w.b.dvf, b2, dv.b);
-        manifold_residual(w, m, b1, b2, dv, acc);
+        manifold_residual<JOINTS>(w, m, b1, b2, dv, acc);
     }
     double ts = block_sum(acc.phi2(), sh);
     double tl = block_sum(acc.lam2(), sh);
@@ -1913,6 +1974,7 @@ static __device__ bool eval_residual(const World& w, uint32_t ms, double* sh, ui
 }
 
 #if NPGPU_EXCHANGE_TU
+template <bool JOINTS>
 __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParams p) {
     __shared__ double sh[32];
     extern __shared__ float4 s_cache[];   // kCacheF4 per thread
@@ -1933,22 +1995,22 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_velocity(World w, StepParam
     uint32_t epoch = 0;
     const bool merged = p.sweep_order == NPGPU_SWEEP_MANIFOLD;
     const uint32_t spi = merged ? 1u : 2u;   // sweeps per iteration
-    if (!velocity_sweeps(w, 0, 1, ms, prof, learned, merged, ts, s_cache)) return;
+    if (!velocity_sweeps<JOINTS>(w, 0, 1, ms, prof, learned, merged, ts, s_cache)) return;
     if (!grid_sync(w.ctl, epoch)) return;
-    if (!eval_residual(w, ms, sh, epoch, true)) return;
+    if (!eval_residual<JOINTS>(w, ms, sh, epoch, true)) return;
     uint32_t iters = 0;
     if (!p.solve_to_tolerance) {
         iters = p.max_velocity_iterations;
-        if (!velocity_sweeps(w, 1, 1 + spi * iters, ms, prof, learned, merged, ts, s_cache)) return;
+        if (!velocity_sweeps<JOINTS>(w, 1, 1 + spi * iters, ms, prof, learned, merged, ts, s_cache)) return;
         if (!grid_sync(w.ctl, epoch)) return;
-        if (!eval_residual(w, ms, sh, epoch, false)) return;
+        if (!eval_residual<JOINTS>(w, ms, sh, epoch, false)) return;
     } else {
         for (uint32_t it = 0; it < p.max_iterations_to_tolerance; ++it) {
             if (((volatile double*)&w.ctl->residual)[0] <= (double)p.residual_tolerance) break;
-            if (!velocity_sweeps(w, 1 + spi * it, 1 + spi * (it + 1), ms, prof, learned, merged, ts, s_cache)) return;
+            if (!velocity_sweeps<JOINTS>(w, 1 + spi * it, 1 + spi * (it + 1), ms, prof, learned, merged, ts, s_cache)) return;
             ++iters;
             if (!grid_sync(w.ctl, epoch)) return;
-            if (!eval_residual(w, ms, sh, epoch, false)) return;
+            if (!eval_residual<JOINTS>(w, ms, sh, epoch, false)) return;
         }
     }
     if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->iterations = iters;
@@ -2078,7 +2140,7 @@ struct WorldGroup {
 
 // One sweep (warm start, friction or normal rows) over a world's manifolds,
 // colour by colour.
-template <int KIND, class DvA>
+template <int KIND, bool JOINTS, class DvA>
 __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_t base, uint32_t nbw, uint32_t ncol,
                                             uint32_t sweep, const DvA& dva, const WorldGroup& g) {
     const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
@@ -2088,14 +2150,14 @@ __device__ __forceinline__ void world_sweep(const World& w, uint32_t wd, uint32_
         for (uint32_t m = lo + g.lane; m < hi; m += g.width) {
             int l1, l2;
             if (world_locals(w, m, base, nbw, l1, l2))
-                velocity_task<KIND>(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, dva);
+                velocity_task<KIND, JOINTS>(w, m, sweep, w.s.sm_b1[m], w.s.sm_b2[m], l1, l2, dva);
         }
         g.sync();
     }
 }
 
 // FP64 residual partial sums of one world, added to acc[0..1].
-template <class DvA>
+template <bool JOINTS, class DvA>
 __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint32_t base, uint32_t nbw,
                                                const DvA& dva, double* sh, double* acc, const WorldGroup& g) {
     uint32_t lo = w.s.bucket_start[wd * kMaxColours], hi = w.s.bucket_start[wd * kMaxColours + kMaxColours];
@@ -2106,7 +2168,7 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
         DV dv;
         dva.load(b1, dv.a);
         dva.load(b2, dv.b);
-        manifold_residual(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, rs);
+        manifold_residual<JOINTS>(w, m, w.s.sm_b1[m], w.s.sm_b2[m], dv, rs);
     }
     double s2 = rs.phi2(), l2 = rs.lam2();
     double ts, tl;
@@ -2128,24 +2190,25 @@ __device__ __forceinline__ void world_residual(const World& w, uint32_t wd, uint
 }
 
 // The sweeps and residuals of one world's velocity solve by one group.
-template <class DvA>
+template <bool JOINTS, class DvA>
 __device__ __forceinline__ void world_solve(const World& w, const StepParams& p, uint32_t wd, uint32_t base,
                                             uint32_t nbw, uint32_t ncol, const DvA& dva, double* sh,
                                             const WorldGroup& g) {
-    world_sweep<SWEEP_WARM>(w, wd, base, nbw, ncol, 0, dva, g);
-    world_residual(w, wd, base, nbw, dva, sh, w.ctl->res_acc_init, g);
+    world_sweep<SWEEP_WARM, JOINTS>(w, wd, base, nbw, ncol, 0, dva, g);
+    world_residual<JOINTS>(w, wd, base, nbw, dva, sh, w.ctl->res_acc_init, g);
     for (uint32_t it = 0; it < p.max_velocity_iterations; ++it) {
         if (p.sweep_order == NPGPU_SWEEP_MANIFOLD) {
-            world_sweep<SWEEP_MANIFOLD>(w, wd, base, nbw, ncol, 1 + it, dva, g);
+            world_sweep<SWEEP_MANIFOLD, JOINTS>(w, wd, base, nbw, ncol, 1 + it, dva, g);
         } else {
-            world_sweep<SWEEP_FRICTION>(w, wd, base, nbw, ncol, 1 + 2 * it, dva, g);
-            world_sweep<SWEEP_NORMAL>(w, wd, base, nbw, ncol, 2 + 2 * it, dva, g);
+            world_sweep<SWEEP_FRICTION, JOINTS>(w, wd, base, nbw, ncol, 1 + 2 * it, dva, g);
+            world_sweep<SWEEP_NORMAL, JOINTS>(w, wd, base, nbw, ncol, 2 + 2 * it, dva, g);
         }
     }
-    world_residual(w, wd, base, nbw, dva, sh, w.ctl->res_acc, g);
+    world_residual<JOINTS>(w, wd, base, nbw, dva, sh, w.ctl->res_acc, g);
 }
 
 // The whole velocity solve of one world by one group, its Δv in s_dv.
+template <bool JOINTS>
 __device__ __forceinline__ void world_velocity(const World& w, const StepParams& p, uint32_t wd, uint32_t max_bodies,
                                                float* s_dv, double* sh, const WorldGroup& g) {
     const uint32_t base = w.s.world_start[wd];
@@ -2157,7 +2220,7 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
     const uint32_t ncol = w.ctl->ncolours;
     for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) s_dv[i] = 0.0f;
     g.sync();
-    world_solve(w, p, wd, base, nbw, ncol, SharedDv{s_dv}, sh, g);
+    world_solve<JOINTS>(w, p, wd, base, nbw, ncol, SharedDv{s_dv}, sh, g);
     for (uint32_t i = g.lane; i < 6 * nbw; i += g.width) w.b.dv[6 * base + i] = s_dv[i];
     g.sync();
 }
@@ -2169,7 +2232,7 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
 // Dynamic shared memory: the larger of 6 floats per body slot of the largest
 // world and 6 floats per slot of a small world for each warp.
 #if !NPGPU_EXCHANGE_TU
-template <int THREADS>
+template <int THREADS, bool JOINTS>
 __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
                                                                   uint32_t max_world_bodies, uint32_t n_big,
                                                                   uint32_t n_cluster) {
@@ -2188,7 +2251,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World
         const uint32_t wd = s_world;
         __syncthreads();
         if (wd >= n_worlds) break;
-        world_velocity(w, p, wd, max_world_bodies, s_dv, sh, block);
+        world_velocity<JOINTS>(w, p, wd, max_world_bodies, s_dv, sh, block);
     }
     const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
     const WorldGroup wg{lane, 32u, GROUP_WARP};
@@ -2198,7 +2261,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World
         if (lane == 0) k = atomicAdd(&w.ctl->world_next[2], 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (n_cluster + n_big + k >= n_worlds) break;
-        world_velocity(w, p, order[n_big + k], kWarpWorldBodies, my_dv, nullptr, wg);
+        world_velocity<JOINTS>(w, p, order[n_big + k], kWarpWorldBodies, my_dv, nullptr, wg);
     }
 }
 #endif
@@ -2208,7 +2271,7 @@ __global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World
 // memories, 2^shift bodies per block, and the cluster barrier orders the
 // colours. Each block writes its own rows back to global memory.
 #if NPGPU_EXCHANGE_TU
-template <int THREADS>
+template <int THREADS, bool JOINTS>
 __global__ void __launch_bounds__(THREADS, 1) k_cluster_velocity(World w, StepParams p, uint32_t shift) {
     extern __shared__ float s_dv[];
     __shared__ double sh[32];
@@ -2225,7 +2288,7 @@ __global__ void __launch_bounds__(THREADS, 1) k_cluster_velocity(World w, StepPa
     for (uint32_t i = threadIdx.x; i < (6u << shift); i += blockDim.x) s_dv[i] = 0.0f;
     cl.sync();
     const WorldGroup g{rank * blockDim.x + threadIdx.x, nct * blockDim.x, GROUP_CLUSTER};
-    world_solve(w, p, wd, base, nbw, w.ctl->ncolours, ClusterDv{s_dv, shift}, sh, g);
+    world_solve<JOINTS>(w, p, wd, base, nbw, w.ctl->ncolours, ClusterDv{s_dv, shift}, sh, g);
     const uint32_t lo = rank << shift, hi = nbw < lo + (1u << shift) ? nbw : lo + (1u << shift);
     for (uint32_t i = threadIdx.x; lo + i / 6u < hi && i < (6u << shift); i += blockDim.x)
         w.b.dv[6 * (size_t)(base + lo) + i] = s_dv[i];
@@ -2497,11 +2560,16 @@ __device__ __forceinline__ void joint_position_ops(uint32_t kind, uint32_t info,
 // (NonlinearSORProx::solve_generator, nonlinear_sor_prox.rs:57-76), each
 // through helper.rs's position helpers (helper.rs:298-418, 553-611, 701-769,
 // 921-998) and solve_generic. An error below the allowed one is skipped
-// (Unit::try_new_and_get).
-__device__ __forceinline__ void joint_position(const World& w, const StepParams& p, uint32_t j, uint32_t bb1, uint32_t bb2,
-                                               uint32_t i1, uint32_t i2, Pose& P1, Pose& P2, bool& moved1,
-                                               bool& moved2) {
-    const Bodies& b = w.b;
+// (Unit::try_new_and_get). Out of line, everything passed and returned by
+// value, so that the contact tasks keep their registers.
+struct JointPoses {
+    Pose P1, P2;
+    bool moved1, moved2;
+};
+static __device__ __noinline__ JointPoses joint_position(const Joints J, const float4* local_com, const float4* sb,
+                                                         const StepParams p, uint32_t j, uint32_t bb1, uint32_t bb2,
+                                                         uint32_t i1, uint32_t i2, Pose P1, Pose P2) {
+    bool moved1 = false, moved2 = false;
     const bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
     np::V t1 = P1.t, t2 = P2.t;
     np::Q q1 = P1.q, q2 = P2.q;
@@ -2514,21 +2582,20 @@ __device__ __forceinline__ void joint_position(const World& w, const StepParams&
     v1.info = i1;
     v2.info = i2;
     if (d1) {
-        lc1 = v3(__ldg(b.local_com + bb1));
-        const SB s = load_sb(b.sb, (int)bb1);
+        lc1 = v3(__ldg(local_com + bb1));
+        const SB s = load_sb(sb, (int)bb1);
         v1.inv_mass = s.im;
         v1.inv_I = s.I;
     }
     if (d2) {
-        lc2 = v3(__ldg(b.local_com + bb2));
-        const SB s = load_sb(b.sb, (int)bb2);
+        lc2 = v3(__ldg(local_com + bb2));
+        const SB s = load_sb(sb, (int)bb2);
         v2.inv_mass = s.im;
         v2.inv_I = s.I;
     }
-    const uint32_t info = w.j.info[j], kind = info & JI_KIND_MASK;
-    const np::V la1 = v3(w.j.anchor[2 * j]), la2 = v3(w.j.anchor[2 * j + 1]);
-    const float4 ax1 = w.j.axis[3 * j], ax2 = w.j.axis[3 * j + 1], ax3 = w.j.axis[3 * j + 2];
-    moved1 = moved2 = false;
+    const uint32_t info = J.info[j], kind = info & JI_KIND_MASK;
+    const np::V la1 = v3(J.anchor[2 * j]), la2 = v3(J.anchor[2 * j + 1]);
+    const float4 ax1 = J.axis[3 * j], ax2 = J.axis[3 * j + 1], ax3 = J.axis[3 * j + 2];
     int ops[3];
     joint_position_ops(kind, info, ops);
     float J1[6], J2[6], W1[6], W2[6];
@@ -2552,8 +2619,8 @@ __device__ __forceinline__ void joint_position(const World& w, const StepParams&
         } else if (op == JP_R_FRAMES || op == JP_R_BODIES) {
             np::Q r1 = q1, r2 = q2;
             if (op == JP_R_FRAMES) {
-                r1 = np::qmul(q1, q4(w.j.frame[2 * j]));
-                r2 = np::qmul(q2, q4(w.j.frame[2 * j + 1]));
+                r1 = np::qmul(q1, q4(J.frame[2 * j]));
+                r2 = np::qmul(q2, q4(J.frame[2 * j + 1]));
             }
             angular = true;
             have = unit_try(np::qscaled_axis(np::qmul(r2, np::qconj(r1))), p.allowed_angular_error, dir, depth);
@@ -2608,21 +2675,27 @@ __device__ __forceinline__ void joint_position(const World& w, const StepParams&
     }
     P1.t = t1; P1.q = q1; P1.com = com1;
     P2.t = t2; P2.q = q2; P2.com = com2;
+    return JointPoses{P1, P2, moved1, moved2};
 }
 
+template <bool JOINTS>
 __device__ __forceinline__ void position_core(const World& w, const StepParams& p, uint32_t m, Pose& P1, Pose& P2,
                                               bool& moved1, bool& moved2) {
     const Bodies& b = w.b;
     const float4* rec = w.s.pos_rec + (size_t)m * kPosRec;
-    const float4 r4 = __ldg(rec + 4), r6 = __ldg(rec + 6);
+    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2), r3 = __ldg(rec + 3);
+    const float4 r4 = __ldg(rec + 4), r5 = __ldg(rec + 5), r6 = __ldg(rec + 6);
     const uint32_t bb1 = __float_as_uint(r6.x), bb2 = __float_as_uint(r6.y);
     const uint32_t i1 = __float_as_uint(r6.z), i2 = __float_as_uint(r6.w);
-    if (__float_as_uint(r4.w) & kJointBit) {
-        joint_position(w, p, __float_as_uint(r4.w) & ~kJointBit, bb1, bb2, i1, i2, P1, P2, moved1, moved2);
+    if (JOINTS && (__float_as_uint(r4.w) & kJointBit)) {
+        const JointPoses o =
+            joint_position(w.j, b.local_com, b.sb, p, __float_as_uint(r4.w) & ~kJointBit, bb1, bb2, i1, i2, P1, P2);
+        P1 = o.P1;
+        P2 = o.P2;
+        moved1 = o.moved1;
+        moved2 = o.moved2;
         return;
     }
-    const float4 r0 = __ldg(rec), r1 = __ldg(rec + 1), r2 = __ldg(rec + 2), r3 = __ldg(rec + 3);
-    const float4 r5 = __ldg(rec + 5);
     bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
     np::V t1 = P1.t, t2 = P2.t;
     np::Q q1 = P1.q, q2 = P2.q;
@@ -2693,17 +2766,19 @@ __device__ __forceinline__ void position_core(const World& w, const StepParams& 
 
 // Position task on poses in global memory (one block per world, where
 // __syncthreads orders the tasks of successive colours).
+template <bool JOINTS>
 __device__ __forceinline__ void position_task(const World& w, const StepParams& p, uint32_t m) {
     const float4 r6 = __ldg(w.s.pos_rec + (size_t)m * kPosRec + 6);
     const uint32_t bb1 = __float_as_uint(r6.x), bb2 = __float_as_uint(r6.y);
     Pose P1 = load_pose(w.b, bb1), P2 = load_pose(w.b, bb2);
     bool moved1, moved2;
-    position_core(w, p, m, P1, P2, moved1, moved2);
+    position_core<JOINTS>(w, p, m, P1, P2, moved1, moved2);
     if (moved1) store_pose(w.b, bb1, P1);
     if (moved2) store_pose(w.b, bb2, P2);
 }
 
 #if NPGPU_EXCHANGE_TU
+template <bool JOINTS>
 __global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParams p) {
     const uint32_t ms = w.ctl->nsolver;
     const uint32_t T = gridDim.x * blockDim.x;
@@ -2741,7 +2816,7 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParam
                 if (b2 < 0) P2 = load_pose(w.b, __float_as_uint(r6.y));
             }
             bool n1, n2;
-            position_core(w, p, m, P1, P2, n1, n2);
+            position_core<JOINTS>(w, p, m, P1, P2, n1, n2);
             if (b1 >= 0) publish_posef(w.b.posef, b1, t1 + 1u, P1, mv1 || n1);
             if (b2 >= 0) publish_posef(w.b.posef, b2, t2 + 1u, P2, mv2 || n2);
             mt.next[k] = (uint16_t)(sw + 1u);
@@ -2760,6 +2835,7 @@ __global__ void __launch_bounds__(kCoopThreads, 2) k_position(World w, StepParam
 
 // Batched worlds: block per world, colour by colour, poses in global memory.
 // NonlinearSORProx sweeps of one world by one group, poses in global memory.
+template <bool JOINTS>
 __device__ __forceinline__ void world_position(const World& w, const StepParams& p, uint32_t wd, const WorldGroup& g) {
     const uint32_t ncol = w.ctl->ncolours;
     const uint32_t* bs = w.s.bucket_start + wd * kMaxColours;
@@ -2767,7 +2843,7 @@ __device__ __forceinline__ void world_position(const World& w, const StepParams&
         for (uint32_t c = 0; c < ncol; ++c) {
             uint32_t lo = bs[c], hi = bs[c + 1];
             if (lo == hi) continue;
-            for (uint32_t m = lo + g.lane; m < hi; m += g.width) position_task(w, p, m);
+            for (uint32_t m = lo + g.lane; m < hi; m += g.width) position_task<JOINTS>(w, p, m);
             g.sync();
         }
     }
@@ -2775,10 +2851,11 @@ __device__ __forceinline__ void world_position(const World& w, const StepParams&
 }
 
 // Batched worlds: large worlds one per block, then small worlds one per warp,
-// as in the velocity kernel.
+// as in the velocity kernel. Three blocks of 128 threads stay resident per SM
+// (at most 170 registers a thread; the contacts' tasks need about 164).
 #if !NPGPU_EXCHANGE_TU
-template <int THREADS>
-__global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big,
+template <int THREADS, bool JOINTS>
+__global__ void __launch_bounds__(THREADS, 384 / THREADS) k_world_position(World w, StepParams p, uint32_t n_worlds, uint32_t n_big,
                                                             uint32_t n_cluster) {
     __shared__ uint32_t s_world;
     if (w.ctl->err & ERRF_COLOURS) return;
@@ -2793,7 +2870,7 @@ __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams 
         const uint32_t wd = s_world;
         __syncthreads();
         if (wd >= n_worlds) break;
-        world_position(w, p, wd, block);
+        world_position<JOINTS>(w, p, wd, block);
     }
     const uint32_t lane = threadIdx.x & 31u;
     const WorldGroup wg{lane, 32u, GROUP_WARP};
@@ -2802,7 +2879,7 @@ __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams 
         if (lane == 0) k = atomicAdd(&w.ctl->world_next[3], 1u);
         k = __shfl_sync(0xffffffffu, k, 0);
         if (n_cluster + n_big + k >= n_worlds) break;
-        world_position(w, p, order[n_big + k], wg);
+        world_position<JOINTS>(w, p, order[n_big + k], wg);
     }
 }
 #endif
@@ -2810,12 +2887,13 @@ __global__ void __launch_bounds__(THREADS) k_world_position(World w, StepParams 
 // The cluster worlds' position sweeps: cluster c takes world order[c], the
 // cluster barrier between colours (poses stay in global memory).
 #if NPGPU_EXCHANGE_TU
+template <bool JOINTS>
 __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_position(World w, StepParams p) {
     if (w.ctl->err & ERRF_COLOURS) return;
     cg::cluster_group cl = cg::this_cluster();
     const uint32_t nct = cl.num_blocks();
     const WorldGroup g{cl.block_rank() * blockDim.x + threadIdx.x, nct * blockDim.x, GROUP_CLUSTER};
-    world_position(w, p, w.s.world_order[blockIdx.x / nct], g);
+    world_position<JOINTS>(w, p, w.s.world_order[blockIdx.x / nct], g);
 }
 #endif
 
@@ -2868,13 +2946,15 @@ __global__ void k_post(World w, StepParams p, bool posef) {
 #endif
 
 #if NPGPU_EXCHANGE_TU
-const void* exchange_kernel(ExchangeKernel k) {
+const void* exchange_kernel(ExchangeKernel k, bool joints) {
     switch (k) {
     case XK_COLOUR: return (const void*)k_colour;
-    case XK_VELOCITY: return (const void*)k_velocity;
-    case XK_POSITION: return (const void*)k_position;
-    case XK_CLUSTER_VELOCITY: return (const void*)k_cluster_velocity<kClusterThreads>;
-    case XK_CLUSTER_POSITION: return (const void*)k_cluster_position;
+    case XK_VELOCITY: return joints ? (const void*)k_velocity<true> : (const void*)k_velocity<false>;
+    case XK_POSITION: return joints ? (const void*)k_position<true> : (const void*)k_position<false>;
+    case XK_CLUSTER_VELOCITY:
+        return joints ? (const void*)k_cluster_velocity<kClusterThreads, true>
+                      : (const void*)k_cluster_velocity<kClusterThreads, false>;
+    case XK_CLUSTER_POSITION: return joints ? (const void*)k_cluster_position<true> : (const void*)k_cluster_position<false>;
     }
     return nullptr;
 }
@@ -2902,12 +2982,27 @@ static const size_t kVelocitySmem = (size_t)kCoopThreads * kCacheF4 * sizeof(flo
 // Dynamic shared memory of the per-world velocity kernel: Δv (6 floats) per
 // body slot of the largest world, or per slot of a small world for each warp.
 // The per-world velocity kernel for a block size (64, 128 or 256).
-static const void* world_velocity_fn(int threads) {
+static const void* world_velocity_fn(int threads, bool joints) {
     switch (threads) {
-    case 64: return (const void*)k_world_velocity<64>;
-    case 256: return (const void*)k_world_velocity<256>;
-    default: return (const void*)k_world_velocity<128>;
+    case 64: return joints ? (const void*)k_world_velocity<64, true> : (const void*)k_world_velocity<64, false>;
+    case 256: return joints ? (const void*)k_world_velocity<256, true> : (const void*)k_world_velocity<256, false>;
+    default: return joints ? (const void*)k_world_velocity<128, true> : (const void*)k_world_velocity<128, false>;
     }
+}
+static const void* world_position_fn(bool joints) {
+    return joints ? (const void*)k_world_position<128, true> : (const void*)k_world_position<128, false>;
+}
+
+// Blocks of fn resident per SM, the smaller over both instantiations (a
+// kernel's grid fits either).
+static int resident(const void* (*pick)(bool), int threads, size_t smem) {
+    int lo = 0;
+    for (bool j : {false, true}) {
+        int per = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, pick(j), threads, smem);
+        if (!j || per < lo) lo = per;
+    }
+    return lo < 1 ? 1 : lo;
 }
 
 static size_t world_smem(uint32_t max_world_bodies, int threads) {
@@ -2920,16 +3015,16 @@ void solver_grid_sizes(int device, SolverLaunch& L) {
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, exchange_kernel(XK_COLOUR), kCoopThreads, 0);
     L.grid_colour = sms * (per < 1 ? 1 : per);
-    cudaFuncSetAttribute(exchange_kernel(XK_VELOCITY), cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kVelocitySmem);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, exchange_kernel(XK_VELOCITY), kCoopThreads, kVelocitySmem);
-    L.grid_velocity = sms * (per < 1 ? 1 : per);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, exchange_kernel(XK_POSITION), kCoopThreads, 0);
-    L.grid_position = sms * (per < 1 ? 1 : per);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_world_position<128>, 128, 0);
-    L.grid_world_position = sms * (per < 1 ? 1 : per);
+    for (bool j : {false, true})
+        cudaFuncSetAttribute(exchange_kernel(XK_VELOCITY, j), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)kVelocitySmem);
+    L.grid_velocity = sms * resident([](bool j) { return exchange_kernel(XK_VELOCITY, j); }, kCoopThreads, kVelocitySmem);
+    L.grid_position = sms * resident([](bool j) { return exchange_kernel(XK_POSITION, j); }, kCoopThreads, 0);
+    L.grid_world_position = sms * resident(world_position_fn, 128, 0);
     for (int t : {64, 128, 256})
-        cudaFuncSetAttribute(world_velocity_fn(t), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)world_smem(kMaxWorldBodies, t));
+        for (bool j : {false, true})
+            cudaFuncSetAttribute(world_velocity_fn(t, j), cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)world_smem(kMaxWorldBodies, t));
     L.cluster_ctas = cluster_ctas(device);
 }
 
@@ -2941,8 +3036,12 @@ uint64_t grid_task_capacity(const SolverLaunch& L) {
 int world_grid(int device, uint32_t max_world_bodies, uint32_t n_worlds, int threads) {
     int sms = 0, per = 0;
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, world_velocity_fn(threads), threads,
-                                                  world_smem(max_world_bodies, threads));
+    for (bool j : {false, true}) {
+        int pj = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pj, world_velocity_fn(threads, j), threads,
+                                                      world_smem(max_world_bodies, threads));
+        if (!j || pj < per) per = pj;
+    }
     long g = (long)sms * (per < 1 ? 1 : per);
     if (g > (long)n_worlds) g = n_worlds;
     return g < 1 ? 1 : (int)g;
@@ -2958,10 +3057,13 @@ int cluster_ctas(int device) {
     int ok = 0;
     cudaDeviceGetAttribute(&ok, cudaDevAttrClusterLaunch, device);
     if (!ok) return 0;
-    const void* fn = exchange_kernel(XK_CLUSTER_VELOCITY);
-    cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cluster_smem(kClusterShiftMax));
-    cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
-    cudaFuncSetAttribute(exchange_kernel(XK_CLUSTER_POSITION), cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    for (bool j : {false, true}) {
+        const void* fn = exchange_kernel(XK_CLUSTER_VELOCITY, j);
+        cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)cluster_smem(kClusterShiftMax));
+        cudaFuncSetAttribute(fn, cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+        cudaFuncSetAttribute(exchange_kernel(XK_CLUSTER_POSITION, j), cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+    }
+    // The cluster size both instantiations hold resident.
     for (int c : {16, 8}) {
         cudaLaunchConfig_t cfg = {};
         cudaLaunchAttribute at[1];
@@ -2974,8 +3076,11 @@ int cluster_ctas(int device) {
         cfg.dynamicSmemBytes = cluster_smem(kClusterShiftMax);
         cfg.attrs = at;
         cfg.numAttrs = 1;
-        int n = 0;
-        if (cudaOccupancyMaxActiveClusters(&n, fn, &cfg) == cudaSuccess && n > 0) return c;
+        int n = 0, nj = 0;
+        if (cudaOccupancyMaxActiveClusters(&n, exchange_kernel(XK_CLUSTER_VELOCITY, false), &cfg) == cudaSuccess &&
+            cudaOccupancyMaxActiveClusters(&nj, exchange_kernel(XK_CLUSTER_VELOCITY, true), &cfg) == cudaSuccess &&
+            n > 0 && nj > 0)
+            return c;
         cudaGetLastError();
     }
     return 0;
@@ -3037,28 +3142,30 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         k_world_permute_back<<<npb, kItemThreads, 0, st>>>(wc);
     }
     rec(2);
-    k_assemble<<<npb, kItemThreads, 0, st>>>(wc, pc, !L.batched);
+    const bool joints = w.nj_slots != 0u;
+    if (joints) k_assemble<true><<<npb, kItemThreads, 0, st>>>(wc, pc, !L.batched);
+    else k_assemble<false><<<npb, kItemThreads, 0, st>>>(wc, pc, !L.batched);
     rec(3);
     if (L.batched) {
         if (L.n_cluster > 0) {
             uint32_t shift = L.cluster_shift;
             void* cargs[] = {&wc, &pc, &shift};
-            e = launch_cluster(exchange_kernel(XK_CLUSTER_VELOCITY), L, cluster_smem(shift), cargs, st);
+            e = launch_cluster(exchange_kernel(XK_CLUSTER_VELOCITY, joints), L, cluster_smem(shift), cargs, st);
             if (e != cudaSuccess) return e;
         }
         if (L.n_worlds > L.n_cluster) {
             const size_t smem = world_smem(L.max_world_bodies, L.world_threads);
             uint32_t nw = L.n_worlds, mwb = L.max_world_bodies, nbig = L.n_big, ncl = L.n_cluster;
             void* wargs[] = {&wc, &pc, &nw, &mwb, &nbig, &ncl};
-            e = cudaLaunchKernel(world_velocity_fn(L.world_threads), dim3(L.grid_world), dim3(L.world_threads), wargs,
-                                 smem, st);
+            e = cudaLaunchKernel(world_velocity_fn(L.world_threads, joints), dim3(L.grid_world), dim3(L.world_threads),
+                                 wargs, smem, st);
             if (e != cudaSuccess) return e;
         }
         k_world_finish<<<1, 1, 0, st>>>(wc, pc);
     } else {
         e = cudaMemsetAsync(&w.ctl->barrier_count, 0, sizeof(uint32_t), st);
         if (e != cudaSuccess) return e;
-        e = coop(exchange_kernel(XK_VELOCITY), L.grid_velocity, args2, st, kVelocitySmem);
+        e = coop(exchange_kernel(XK_VELOCITY, joints), L.grid_velocity, args2, st, kVelocitySmem);
         if (e != cudaSuccess) return e;
     }
     rec(4);
@@ -3070,13 +3177,17 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
         // kernel's block size: large worlds a block each, small ones a warp.
         if (L.n_cluster > 0) {
             void* cargs[] = {&wc, &pc};
-            e = launch_cluster(exchange_kernel(XK_CLUSTER_POSITION), L, 0, cargs, st);
+            e = launch_cluster(exchange_kernel(XK_CLUSTER_POSITION, joints), L, 0, cargs, st);
             if (e != cudaSuccess) return e;
         }
-        if (L.n_worlds > L.n_cluster)
-            k_world_position<128><<<L.grid_world_position, 128, 0, st>>>(wc, pc, L.n_worlds, L.n_big, L.n_cluster);
+        if (L.n_worlds > L.n_cluster) {
+            uint32_t nw = L.n_worlds, nbig = L.n_big, ncl = L.n_cluster;
+            void* pargs[] = {&wc, &pc, &nw, &nbig, &ncl};
+            e = cudaLaunchKernel(world_position_fn(joints), dim3(L.grid_world_position), dim3(128), pargs, 0, st);
+            if (e != cudaSuccess) return e;
+        }
     } else {
-        e = coop(exchange_kernel(XK_POSITION), L.grid_position, args2, st);
+        e = coop(exchange_kernel(XK_POSITION, joints), L.grid_position, args2, st);
         if (e != cudaSuccess) return e;
     }
     rec(6);

@@ -189,7 +189,7 @@ struct Solver {
                                      // impulses, or zero for a contact without a cache entry)
     float4 *tan;                     // 4 contacts x 2 per solver manifold: the friction directions (xyz)
     float4 *rows;                    // 4 contacts x kRowsF4 per solver manifold: normal, friction 1, friction 2 rows
-    uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13)
+    uint32_t *sm_mask;               // unlocked dofs of body 1 (bits 0-5) and body 2 (bits 8-13); kJointBit: a joint's rows
     float4 *pos_rec;                 // kPosRec per solver manifold: what the position solver reads besides poses
     uint32_t *adj;                   // body -> its solver manifolds (CSR over adj_start)
     // Batched worlds: manifolds bucketed by (world, colour).
