@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 5u
+#define NPGPU_ABI_VERSION 6u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -141,7 +141,7 @@ typedef struct npgpu_collider_desc {
     uint32_t restitution_combine;
     uint32_t shape;             /* NPGPU_SHAPE_* */
     uint32_t is_sensor;         /* rejected when non-zero */
-    uint32_t ccd_enabled;       /* rejected when non-zero: CCD is not built */
+    uint32_t ccd_enabled;       /* Collider::enable_ccd: time-of-impact substeps (MechanicalWorld::solve_ccd) */
 } npgpu_collider_desc;
 
 /* Joint constraints (src/joint/): BallConstraint (ball_constraint.rs) keeps anchor1 and anchor2
@@ -251,8 +251,8 @@ typedef struct npgpu_params {
     float max_stabilization_multiplier;    /* 0.2 */
     uint32_t max_velocity_iterations;      /* 8 */
     uint32_t max_position_iterations;      /* 3 */
-    uint32_t max_ccd_position_iterations;  /* 10 (CCD is not built) */
-    uint32_t max_ccd_substeps;             /* 1 */
+    uint32_t max_ccd_position_iterations;  /* 10 */
+    uint32_t max_ccd_substeps;             /* 1 (0: no CCD) */
     /* GPU-only. */
     uint32_t solve_to_tolerance;           /* 0: run max_velocity_iterations; 1: stop when residual <= tol */
     float residual_tolerance;              /* 1e-4 */
@@ -271,6 +271,8 @@ typedef struct npgpu_params {
     uint32_t world_threads;                /* threads per world block of NPGPU_SCHEDULE_WORLDS: 64, 128 or
                                               256 (0: 128); npgpu_autotune chooses it */
     uint32_t sweep_order;                  /* NPGPU_SWEEP_*: the order of the rows within an iteration */
+    uint32_t ccd_on_penetration_enabled;   /* 0: a CCD pair already overlapping at the step's start has no
+                                              time of impact (IntegrationParameters::ccd_on_penetration_enabled) */
 } npgpu_params;
 
 /* Per-step counters: the stage names of src/counters/mod.rs:18-209 plus
@@ -310,6 +312,8 @@ typedef struct npgpu_counters {
     uint32_t learned_starts;         /* new contacts started from the network's prediction */
     uint32_t learned_kept;           /* ... of which the warm-start sweep kept the prediction */
     uint32_t graph_replay;           /* 1 if the last step ran from a CUDA graph */
+    uint32_t ccd_substeps;           /* CCD substeps of the last step, over all worlds */
+    uint32_t ccd_impacts;            /* time-of-impact events those substeps resolved */
     uint32_t reserved;
 } npgpu_counters;
 

@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 5
+NPGPU_ABI_VERSION = 6
 
 # npgpu_status
 OK = 0
@@ -181,6 +181,7 @@ class Params(C.Structure):
         ("use_graph", C.c_uint32),
         ("world_threads", C.c_uint32),
         ("sweep_order", C.c_uint32),
+        ("ccd_on_penetration_enabled", C.c_uint32),
     ]
 
 
@@ -217,6 +218,8 @@ class Counters(C.Structure):
         ("learned_starts", C.c_uint32),
         ("learned_kept", C.c_uint32),
         ("graph_replay", C.c_uint32),
+        ("ccd_substeps", C.c_uint32),
+        ("ccd_impacts", C.c_uint32),
         ("reserved", C.c_uint32),
     ]
 
@@ -267,6 +270,7 @@ def default_params():
     p.use_graph = 1
     p.world_threads = 0
     p.sweep_order = SWEEP_SEPARATE
+    p.ccd_on_penetration_enabled = 0
     return p
 
 

@@ -425,6 +425,58 @@ def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234):
                  info={"walls": n_walls, "bodies": n_walls * (width * height + balls)})
 
 
+# ---------------------------------------------------------------- CCD scenes
+def ccd_wall(speed=120.0, half_thickness=0.05, radius=0.1, n=1, ccd=True, gravity=(0.0, 0.0, 0.0),
+             shape=abi.SHAPE_BALL, spin=0.0, seed=3, world=0, restitution=0.0, linear_interp=False):
+    """Fast projectiles at a thin static wall (a cuboid of half thickness
+    `half_thickness` centred on the plane x = 0): at `speed` a projectile moves
+    speed / 60 m a step, far more than the wall is thick, so it passes through
+    it unless its collider has CCD enabled. Balls of `radius` (or cubes of
+    that half extent, spun about z at `spin` rad/s) start at x = -1."""
+    rng = np.random.default_rng(seed)
+    g = ground_descs(1)
+    g["world"] = world
+    gc = collider_descs(1, 0, abi.SHAPE_CUBOID, (half_thickness, 2.0, 2.0), friction=0.5, restitution=restitution)
+    gc["position_wrt_body"][0, 1] = 2.0
+    b = body_descs(n)
+    b["world"] = world
+    b["position"][:, 0] = -1.0
+    b["position"][:, 1] = rng.uniform(0.6, 3.4, n).astype(np.float32)
+    b["position"][:, 2] = rng.uniform(-1.4, 1.4, n).astype(np.float32)
+    b["velocity"][:, 0] = speed
+    b["velocity"][:, 5] = spin
+    if linear_interp:
+        b["flags"] |= abi.BODY_LINEAR_INTERP
+    params = (radius, 0.0, 0.0) if shape == abi.SHAPE_BALL else (radius, radius, radius)
+    c = collider_descs(n, np.arange(n), shape, params, density=1.0, friction=0.5, restitution=restitution)
+    c["ccd_enabled"] = 1 if ccd else 0
+    bodies, colliders = _concat([g, b], [gc, c])
+    return Scene("ccd wall", bodies, colliders, gravity=gravity)
+
+
+def ccd_stack(height=4, speed=80.0, balls=3, ccd=True, seed=5, world=0):
+    """A tower of `height` unit boxes on the ground struck by `balls` fast
+    CCD balls (radius 0.2, 10 kg/m^3) flying at it along x: each impact's
+    substep takes the struck box and, through their contacts, the boxes and
+    balls touching it."""
+    rng = np.random.default_rng(seed)
+    g, gc = _ground(half=(20.0, 1.0, 20.0), world=world)
+    b = body_descs(height)
+    b["world"] = world
+    b["position"][:, 1] = 0.5 + np.arange(height) * 1.0
+    c = collider_descs(height, np.arange(height), abi.SHAPE_CUBOID, (0.5, 0.5, 0.5), density=1.0, friction=0.5)
+    bb = body_descs(balls)
+    bb["world"] = world
+    bb["position"][:, 0] = -3.0
+    bb["position"][:, 1] = (0.5 + rng.integers(0, height, balls) * 1.0 + rng.uniform(-0.3, 0.3, balls)).astype(np.float32)
+    bb["position"][:, 2] = rng.uniform(-0.3, 0.3, balls).astype(np.float32)
+    bb["velocity"][:, 0] = speed
+    cb = collider_descs(balls, np.arange(balls), abi.SHAPE_BALL, (0.2, 0.0, 0.0), density=10.0, friction=0.5)
+    cb["ccd_enabled"] = 1 if ccd else 0
+    bodies, colliders = _concat([g, b, bb], [gc, c, cb])
+    return Scene("ccd stack", bodies, colliders)
+
+
 # ---------------------------------------------------------------- small scenes
 def single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 5, 0), velocity=(0, 0, 0, 0, 0, 0),
                 rotation=(0, 0, 0, 1), ground=True, density=1.0, friction=0.5, restitution=0.0):

@@ -12,7 +12,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "liboracle.so")
 SOURCES = [os.path.join(HERE, "oracle_capi.cpp")]
-HEADERS = [os.path.join(HERE, f) for f in ("ref_math.hpp", "ref_world.hpp")] + [
+HEADERS = [os.path.join(HERE, f) for f in ("ref_math.hpp", "ref_ccd.hpp", "ref_world.hpp")] + [
     os.path.join(HERE, "..", "include", "npgpu.h")
 ]
 

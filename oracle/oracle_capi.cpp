@@ -67,6 +67,29 @@ void orc_mlp_set(orc_world* o, const float* params, uint32_t n) { DISPATCH(o, w.
 
 void orc_set_params(orc_world* o, const npgpu_params* p) { DISPATCH(o, w.params = *p); }
 
+double orc_collider_distance(orc_world* o, uint32_t c1, uint32_t c2, double dir[3]) {
+    double d = 0.0;
+    DISPATCH(o, {
+        auto v = decltype(w.bodies[0].lin){};
+        d = double(w.collider_distance(c1, c2, v));
+        dir[0] = double(v.x);
+        dir[1] = double(v.y);
+        dir[2] = double(v.z);
+    });
+    return d;
+}
+
+int orc_pair_toi(orc_world* o, uint32_t c1, uint32_t c2, double horizon, double* toi) {
+    int r = -1;
+    DISPATCH(o, {
+        using Rw = decltype(w.cur_dt);
+        Rw t = Rw(0);
+        r = w.pair_toi(c1, c2, Rw(horizon), t);
+        *toi = double(t);
+    });
+    return r;
+}
+
 int orc_upsert_bodies(orc_world* o, uint32_t n, const npgpu_handle* h, const npgpu_body_desc* d) {
     for (uint32_t i = 0; i < n; ++i) {
         int s = 0;

@@ -51,6 +51,8 @@ def lib():
             "orc_get_contacts": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
             "orc_get_contacts_f64": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
             "orc_get_counters": (None, [W, P(abi.Counters)]),
+            "orc_collider_distance": (C.c_double, [W, C.c_uint32, C.c_uint32, P(C.c_double * 3)]),
+            "orc_pair_toi": (C.c_int, [W, C.c_uint32, C.c_uint32, C.c_double, P(C.c_double)]),
             "orc_last_error": (C.c_char_p, [W]),
             "orc_record_events": (None, [W, C.c_int]),
             "orc_contact_events": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
@@ -213,6 +215,21 @@ class OracleWorld:
         out = np.zeros((max(n, 1), 13), np.float64)
         self.L.orc_get_contacts_f64(self.w, _ptr(out), n)
         return out[:n]
+
+    def collider_distance(self, c1, c2):
+        """Distance of two colliders' shapes at the current poses, and the
+        unit direction from the first toward the second."""
+        d = (C.c_double * 3)()
+        dist = self.L.orc_collider_distance(self.w, c1, c2, C.byref(d))
+        return dist, np.array(d[:])
+
+    def pair_toi(self, c1, c2, horizon):
+        """Time of impact of two colliders moving at their bodies' velocities
+        from the current poses: (status, toi), status -1 none, 0 an impact,
+        1 overlapping at the start."""
+        t = C.c_double(0.0)
+        r = self.L.orc_pair_toi(self.w, c1, c2, horizon, C.byref(t))
+        return r, t.value
 
     def counters(self):
         c = abi.Counters()

@@ -33,6 +33,7 @@
 #include <vector>
 #include <algorithm>
 #include "ref_math.hpp"
+#include "ref_ccd.hpp"
 #include "../include/npgpu.h"
 
 namespace oracle {
@@ -204,6 +205,7 @@ template <class R> struct Body {
     uint64_t generation = 0;
     uint32_t status = NPGPU_BODY_DYNAMIC, kind = NPGPU_KIND_RIGID_BODY, flags = 0, world = 0;
     Iso<R> pos;
+    Iso<R> pos0;                    // position0: the pose at the step's start, or where CCD advanced it
     V3<R> lin, ang;                 // velocity
     Inertia<R> local_inertia, inertia, aug, inv_aug;
     V3<R> local_com, com;
@@ -216,6 +218,7 @@ template <class R> struct Body {
     R mask[6];
     bool changed = true;            // BodyUpdateStatus::inertia_needs_update / colliders_need_update
     bool in_island = false;
+    bool linear_interp() const { return (flags & NPGPU_BODY_LINEAR_INTERP) != 0; }
     bool dynamic() const { return status == NPGPU_BODY_DYNAMIC; }
     bool kinematic() const { return status == NPGPU_BODY_KINEMATIC; }
     int ndofs() const { return dynamic() ? 6 : 0; }
@@ -238,6 +241,8 @@ template <class R> struct Collider {
     uint32_t friction_combine = 0, restitution_combine = 0;
     R aabb_min[3], aabb_max[3];   // fat AABB
     bool has_fat = false;
+    bool ccd = false;             // Collider::is_ccd_enabled
+    R sw_min[3], sw_max[3];       // CCD: the box swept from the safe pose to the current one
     R query_limit() const { return margin + linear_prediction; }
     R dilation() const { return (shape == NPGPU_SHAPE_BALL || shape == NPGPU_SHAPE_CAPSULE) ? radius : R(0); }
 };
@@ -313,9 +318,11 @@ public:
     uint32_t num_colours = 0;
     uint32_t num_solver_contacts = 0;   // contacts the last solve took, counted when they were collected
     std::vector<Joint<R>> joints;        // by joint slot (the host set's arena index)
+    R cur_dt = R(0);                     // the step length of the body and row arithmetic: dt, or a CCD substep's
 
     World(const npgpu_params& p, const float g[3]) : params(p) {
         gravity = v3<R>(R(g[0]), R(g[1]), R(g[2]));
+        cur_dt = R(p.dt);
         std::memset(&counters, 0, sizeof(counters));
     }
 
@@ -362,6 +369,7 @@ public:
             b.energy = (d.kind == NPGPU_KIND_GROUND) ? R(0) : R(0.01) * R(4);
         }
         b.com = iso_pt(b.pos, b.local_com);
+        b.pos0 = b.pos;
         update_inertia_from_local_inertia(b);
         b.lin_damp = R(d.linear_damping);
         b.ang_damp = R(d.angular_damping);
@@ -379,7 +387,6 @@ public:
         if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID && d.shape != NPGPU_SHAPE_CAPSULE)
             return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "only balls, cuboids and capsules are supported");
         if (d.is_sensor) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "sensors are not supported");
-        if (d.ccd_enabled) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "CCD colliders are not supported");
         if (d.body.index >= bodies.size() || !bodies[d.body.index].alive ||
             bodies[d.body.index].generation != d.body.generation)
             return fail(NPGPU_ERR_INVALID_HANDLE, "collider parent body handle is invalid");
@@ -404,6 +411,7 @@ public:
         c.restitution = R(d.restitution);
         c.friction_combine = d.friction_combine;
         c.restitution_combine = d.restitution_combine;
+        c.ccd = d.ccd_enabled != 0;
         // Drop manifolds involving the replaced collider.
         drop_manifolds_of(uint32_t(h.index));
         cd_dirty = true;
@@ -644,13 +652,14 @@ public:
         b.inv_aug = inverse(b.aug);
     }
     // RigidBody::update_acceleration (rigid_body.rs:590-619).
-    void update_acceleration(Body<R>& b) {
+    void update_acceleration(Body<R>& b) { update_acceleration(b, gravity); }
+    void update_acceleration(Body<R>& b, V3<R> g) {
         b.acc_lin = b.acc_ang = v3<R>(R(0), R(0), R(0));
         if (b.status != NPGPU_BODY_DYNAMIC) return;
         V3<R> iw = mv(b.inertia.angular, b.ang);
         V3<R> gyro = -cross(b.ang, iw);
         b.acc_ang = mv(b.inv_aug.angular, gyro);
-        if (b.inv_aug.linear != R(0) && (b.flags & NPGPU_BODY_GRAVITY)) b.acc_lin = gravity;
+        if (b.inv_aug.linear != R(0) && (b.flags & NPGPU_BODY_GRAVITY)) b.acc_lin = g;
         b.acc_lin = b.acc_lin + b.f_lin * b.inv_aug.linear;
         b.acc_ang = b.acc_ang + mv(b.inv_aug.angular, b.f_ang);
         b.acc_lin = v3<R>(b.acc_lin.x * b.mask[0], b.acc_lin.y * b.mask[1], b.acc_lin.z * b.mask[2]);
@@ -670,7 +679,7 @@ public:
     }
     // RigidBody::integrate (rigid_body.rs:467-505).
     void integrate(Body<R>& b) {
-        R dt = R(params.dt);
+        R dt = cur_dt;
         b.lin = b.lin * (R(1) / (R(1) + dt * b.lin_damp));
         b.ang = b.ang * (R(1) / (R(1) + dt * b.ang_damp));
         R ln = norm(b.lin);
@@ -687,18 +696,19 @@ public:
     }
 
     // ------------------------------------------------------- collision detection
-    void collider_aabb(const Collider<R>& c, R mn[3], R mx[3]) const {
+    void collider_aabb(const Collider<R>& c, R mn[3], R mx[3]) const { aabb_at(c, c.pose, mn, mx); }
+    void aabb_at(const Collider<R>& c, const Iso<R>& pose, R mn[3], R mx[3]) const {
         // Shape AABB at the collider pose (ncollide3d bounding_volume), loosened by
         // the query limit margin + linear prediction (collider.rs:542-549).
-        V3<R> ctr = c.pose.t;
+        V3<R> ctr = pose.t;
         V3<R> half;
         if (c.shape == NPGPU_SHAPE_BALL) {
             half = v3<R>(c.radius, c.radius, c.radius);
         } else if (c.shape == NPGPU_SHAPE_CAPSULE) {
-            M3<R> rot = qmat(c.pose.q);
+            M3<R> rot = qmat(pose.q);
             for (int a = 0; a < 3; ++a) setc(half, a, std::fabs(rot.m[a][1]) * c.half.y + c.radius);
         } else {
-            M3<R> rot = qmat(c.pose.q);
+            M3<R> rot = qmat(pose.q);
             for (int a = 0; a < 3; ++a) {
                 R s = std::fabs(rot.m[a][0]) * c.half.x + std::fabs(rot.m[a][1]) * c.half.y +
                       std::fabs(rot.m[a][2]) * c.half.z;
@@ -1569,7 +1579,7 @@ public:
             for (int k = 0; k < 6; ++k) s = s + f[k] * vel[k];
             rhs = rhs + s;
             if (with_ext) {
-                R dt = R(params.dt);
+                R dt = cur_dt;
                 R ext[6] = {b.acc_lin.x * dt, b.acc_lin.y * dt, b.acc_lin.z * dt,
                             b.acc_ang.x * dt, b.acc_ang.y * dt, b.acc_ang.z * dt};
                 R e = R(0);
@@ -2571,10 +2581,431 @@ public:
         }
     }
 
+    // ------------------------------------------------------- CCD
+    // MechanicalWorld::solve_ccd (mechanical_world.rs:561-908) with
+    // predict_next_impacts (:400-559) and TOIEntry::try_from_colliders
+    // (:942-1031), for one world (every world of a batch is stepped as its
+    // own MechanicalWorld). The interactions a collider has during CCD are its
+    // broad-phase pairs (fat AABBs overlapping) and, where either collider has
+    // CCD enabled, the pairs whose boxes swept from the safe pose to the
+    // current one overlap. Pairs are taken in collider-slot order and TOIs of
+    // equal time in the order they were found.
+    std::vector<R> ccd_time;                       // SubstepState::body_times, per body slot
+    std::vector<std::vector<uint32_t>> body_colliders;
+    struct TOIEntry {
+        R toi;
+        uint32_t c1, c2, b1, b2;
+        uint32_t ts;
+        uint64_t seq;
+    };
+    enum { PRED_NONE = 0, PRED_IMPACTS = 1, PRED_AFTER = 2 };
+
+    // RigidBody::safe_position (rigid_body.rs:904-910).
+    Iso<R> safe_pose(const Body<R>& b) const { return b.linear_interp() ? Iso<R>{b.pos0.t, b.pos.q} : b.pos0; }
+
+    void ccd_sweep_boxes() {
+        for (auto& c : colliders) {
+            if (!c.alive) continue;
+            const Body<R>& b = bodies[c.body];
+            R a0[3], b0[3], a1[3], b1[3];
+            aabb_at(c, iso_mul(safe_pose(b), c.pos_wrt_body), a0, b0);
+            aabb_at(c, iso_mul(b.pos, c.pos_wrt_body), a1, b1);
+            for (int k = 0; k < 3; ++k) {
+                c.sw_min[k] = std::min(a0[k], a1[k]);
+                c.sw_max[k] = std::max(b0[k], b1[k]);
+            }
+        }
+    }
+    bool interacts(uint32_t i, uint32_t j) const {
+        const Collider<R>& a = colliders[i];
+        const Collider<R>& b = colliders[j];
+        if (!pair_allowed(i, j)) return false;
+        if (aabb_overlap(a, b)) return true;
+        if (!a.ccd && !b.ccd) return false;
+        for (int k = 0; k < 3; ++k)
+            if (!(a.sw_min[k] <= b.sw_max[k] && b.sw_min[k] <= a.sw_max[k])) return false;
+        return true;
+    }
+    void interactions(uint32_t c, std::vector<uint32_t>& out) const {
+        out.clear();
+        for (uint32_t d = 0; d < colliders.size(); ++d)
+            if (d != c && colliders[d].alive && interacts(c, d)) out.push_back(d);
+    }
+
+    CcdShape<R> ccd_shape(const Collider<R>& c) const {
+        CcdShape<R> s;
+        const V3<R> zero = v3<R>(R(0), R(0), R(0));
+        s.local.a = s.local.b = s.local.h = zero;
+        s.local.q = Quat<R>{R(0), R(0), R(0), R(1)};
+        s.wrt = c.pos_wrt_body;
+        R extent;
+        if (c.shape == NPGPU_SHAPE_BALL) {
+            s.local.kind = CORE_POINT;
+            s.local.radius = c.radius;
+            extent = c.radius;
+        } else if (c.shape == NPGPU_SHAPE_CAPSULE) {
+            s.local.kind = CORE_SEGMENT;
+            s.local.a = v3<R>(R(0), -c.half.y, R(0));
+            s.local.b = v3<R>(R(0), c.half.y, R(0));
+            s.local.radius = c.radius;
+            extent = c.half.y + c.radius;
+        } else {
+            s.local.kind = CORE_BOX;
+            s.local.h = c.half;
+            s.local.radius = R(0);
+            extent = norm(c.half);
+        }
+        s.reach = norm(c.pos_wrt_body.t - bodies[c.body].local_com) + extent;
+        return s;
+    }
+    // BodyPart::part_motion (rigid_body.rs:539-553) shifted by tau, or the
+    // still pose a frozen body holds (displaced by `frozen_by` from position0).
+    CcdMotion<R> ccd_motion(uint32_t bi, bool frozen, R by) const {
+        const Body<R>& b = bodies[bi];
+        CcdMotion<R> m;
+        m.start = safe_pose(b);
+        m.local_com = b.local_com;
+        m.lin = b.lin;
+        m.ang = b.ang;
+        m.linear_only = b.linear_interp();
+        const bool still = b.lin.x == R(0) && b.lin.y == R(0) && b.lin.z == R(0) &&
+                           (m.linear_only || (b.ang.x == R(0) && b.ang.y == R(0) && b.ang.z == R(0)));
+        m.tau = frozen ? R(0) : by;
+        m.moving = !still;
+        if (frozen) {
+            if (m.moving) m.start = ccd_displace(m.start, m.local_com, m.lin * by, m.ang * by, m.linear_only);
+            m.moving = false;
+        }
+        return m;
+    }
+    // TOIEntry::try_from_colliders: the first time in [start, end_time] the
+    // colliders come within allowed_linear_error; f1 / f2 are the frozen times.
+    bool try_toi(uint32_t c1, uint32_t c2, const R* f1, const R* f2, R end_time, TOIEntry& e) const {
+        const Collider<R>& A = colliders[c1];
+        const Collider<R>& B = colliders[c2];
+        const uint32_t b1 = A.body, b2 = B.body;
+        const R bt1 = ccd_time[b1], bt2 = ccd_time[b2];
+        const R t1 = f1 ? *f1 : bt1, t2 = f2 ? *f2 : bt2;
+        const R start = std::max(t1, t2);
+        const CcdMotion<R> m1 = f1 ? ccd_motion(b1, true, *f1 - bt1) : ccd_motion(b1, false, start - bt1);
+        const CcdMotion<R> m2 = f2 ? ccd_motion(b2, true, *f2 - bt2) : ccd_motion(b2, false, start - bt2);
+        R t;
+        const CaResult r = conservative_advancement(ccd_shape(A), m1, ccd_shape(B), m2, end_time - start,
+                                                    R(params.allowed_linear_error), t);
+        if (!r.some) return false;
+        if (r.penetrating && !params.ccd_on_penetration_enabled) return false;
+        e = TOIEntry{start + t, c1, c2, b1, b2, 0u, 0u};
+        return true;
+    }
+
+    // predict_next_impacts: the impacts up to end_time in time order, the
+    // bodies frozen at their first impact, the smallest TOI beyond end_time.
+    int predict(R end_time, std::vector<TOIEntry>& impacts, std::vector<R>& frozen, std::vector<char>& is_frozen,
+                R& min_overstep) {
+        impacts.clear();
+        frozen.assign(bodies.size(), R(0));
+        is_frozen.assign(bodies.size(), 0);
+        std::map<uint64_t, uint32_t> ts;
+        std::vector<TOIEntry> heap;
+        uint64_t seq = 0;
+        std::map<uint64_t, char> seen;
+        const R dt0 = R(params.dt);
+        min_overstep = dt0;
+        std::vector<uint32_t> nbr;
+        for (uint32_t c = 0; c < colliders.size(); ++c) {
+            if (!colliders[c].alive || !colliders[c].ccd) continue;
+            interactions(c, nbr);
+            for (uint32_t d : nbr) {
+                const uint32_t i = std::min(c, d), j = std::max(c, d);
+                const uint64_t key = (uint64_t(i) << 32) | j;
+                if (!seen.emplace(key, 1).second) continue;
+                TOIEntry e;
+                if (!try_toi(i, j, nullptr, nullptr, min_overstep, e)) continue;
+                if (e.toi > end_time) {
+                    min_overstep = std::min(min_overstep, e.toi);
+                } else {
+                    min_overstep = end_time;
+                    e.seq = seq++;
+                    heap.push_back(e);
+                    ts[key] = 0;
+                }
+            }
+        }
+        if (min_overstep == dt0 && heap.empty()) return PRED_NONE;
+        if (min_overstep > end_time) return PRED_AFTER;
+        while (!heap.empty()) {
+            size_t best = 0;
+            for (size_t k = 1; k < heap.size(); ++k)
+                if (heap[k].toi < heap[best].toi || (heap[k].toi == heap[best].toi && heap[k].seq < heap[best].seq)) best = k;
+            const TOIEntry e = heap[best];
+            heap.erase(heap.begin() + long(best));
+            if (e.ts != ts[(uint64_t(e.c1) << 32) | e.c2]) continue;   // superseded by a resweep
+            if (is_frozen[e.b1] && is_frozen[e.b2]) {
+                if (e.toi == std::max(frozen[e.b1], frozen[e.b2])) impacts.push_back(e);
+                continue;
+            }
+            if (!is_frozen[e.b1]) {
+                is_frozen[e.b1] = 1;
+                frozen[e.b1] = e.toi;
+            }
+            if (!is_frozen[e.b2]) {
+                is_frozen[e.b2] = 1;
+                frozen[e.b2] = e.toi;
+            }
+            // Resweep every pair of the frozen bodies' colliders.
+            for (uint32_t fb : {e.b1, e.b2}) {
+                if (!bodies[fb].dynamic()) continue;
+                for (uint32_t cc : body_colliders[fb]) {
+                    interactions(cc, nbr);
+                    for (uint32_t d : nbr) {
+                        const uint32_t ch1 = std::min(cc, d), ch2 = std::max(cc, d);
+                        if (!colliders[ch1].ccd && !colliders[ch2].ccd) continue;
+                        const uint32_t x1 = colliders[ch1].body, x2 = colliders[ch2].body;
+                        const bool s1 = !bodies[x1].dynamic(), s2 = !bodies[x2].dynamic();
+                        if ((is_frozen[x1] || s1) && (is_frozen[x2] || s2)) continue;
+                        const uint64_t key = (uint64_t(ch1) << 32) | ch2;
+                        const uint32_t stamp = ++ts[key];
+                        TOIEntry ne;
+                        if (try_toi(ch1, ch2, is_frozen[x1] ? &frozen[x1] : nullptr, is_frozen[x2] ? &frozen[x2] : nullptr,
+                                    end_time, ne)) {
+                            ne.ts = stamp;
+                            ne.seq = seq++;
+                            heap.push_back(ne);
+                        }
+                    }
+                }
+            }
+            impacts.push_back(e);
+        }
+        return PRED_IMPACTS;
+    }
+
+    // RigidBody::advance then clamp_advancement (rigid_body.rs:521-537).
+    void advance_clamp(Body<R>& b, R by) {
+        b.pos0 = ccd_displace(safe_pose(b), b.local_com, b.lin * by, b.ang * by, b.linear_interp());
+        clamp_advancement(b);
+    }
+    void clamp_advancement(Body<R>& b) {
+        b.pos = b.linear_interp() ? Iso<R>{b.pos0.t, b.pos.q} : b.pos0;
+        b.com = iso_pt(b.pos, b.local_com);
+        b.changed = true;
+    }
+
+    // One CCD substep (mechanical_world.rs:624-889): the impacting bodies and
+    // those in contact with them, moved back to the latest TOI, solved
+    // (MoreauJeanSolver::step_ccd, moreau_jean_solver.rs:94-127) and
+    // integrated over the rest of the step.
+    void ccd_substep(const std::vector<TOIEntry>& impacts, const std::vector<R>& frozen,
+                     const std::vector<char>& is_frozen) {
+        const R dt0 = R(params.dt);
+        const R last = impacts.back().toi;
+        const R dts = dt0 - last;
+        cur_dt = dts;
+        std::vector<char> prepared(bodies.size(), 0), visited(colliders.size(), 0);
+        std::vector<uint32_t> stack, island, ccd_bodies, nbr;
+        for (const TOIEntry& e : impacts) {
+            stack.insert(stack.end(), body_colliders[e.b1].begin(), body_colliders[e.b1].end());
+            stack.insert(stack.end(), body_colliders[e.b2].begin(), body_colliders[e.b2].end());
+            ccd_bodies.push_back(e.b1);
+            ccd_bodies.push_back(e.b2);
+        }
+        const V3<R> zero = v3<R>(R(0), R(0), R(0));
+        auto prepare = [&](uint32_t h) {
+            Body<R>& b = bodies[h];
+            b.f_lin = b.f_ang = zero;
+            update_dynamics(b, dts);
+            update_acceleration(b, zero);
+            const R target = is_frozen[h] ? frozen[h] : last;
+            advance_clamp(b, target - ccd_time[h]);
+            ccd_time[h] = last;
+            prepared[h] = 1;
+            island.push_back(h);
+        };
+        std::vector<Manifold<R>> mlist;
+        while (!stack.empty()) {
+            const uint32_t c = stack.back();
+            stack.pop_back();
+            if (visited[c]) continue;
+            interactions(c, nbr);
+            for (uint32_t d : nbr) {
+                if (visited[d]) continue;
+                const uint32_t ch1 = std::min(c, d), ch2 = std::max(c, d);
+                const uint32_t x1 = colliders[ch1].body, x2 = colliders[ch2].body;
+                const bool p1 = !prepared[x1] && bodies[x1].dynamic();
+                if (p1) prepare(x1);
+                const bool p2 = !prepared[x2] && bodies[x2].dynamic();
+                if (p2) prepare(x2);
+                colliders[ch1].pose = iso_mul(bodies[x1].pos, colliders[ch1].pos_wrt_body);
+                colliders[ch2].pose = iso_mul(bodies[x2].pos, colliders[ch2].pos_wrt_body);
+                Manifold<R> m;
+                m.c1 = ch1;
+                m.c2 = ch2;
+                narrow_pair(m);
+                if (m.contacts.empty()) continue;
+                mlist.push_back(m);
+                if (ch1 != c && p1) stack.insert(stack.end(), body_colliders[x1].begin(), body_colliders[x1].end());
+                if (ch2 != c && p2) stack.insert(stack.end(), body_colliders[x2].begin(), body_colliders[x2].end());
+            }
+            visited[c] = 1;
+        }
+        // step_ccd: assembly, position solve, validate_advancement of the
+        // impacting bodies, velocity solve, integration of the island.
+        assemble_ccd(mlist);
+        for (uint32_t it = 0; it < params.max_ccd_position_iterations; ++it)
+            for (int i : seq_pos) solve_position(pos_constraints[i]);
+        for (uint32_t h : ccd_bodies) bodies[h].pos0 = bodies[h].pos;
+        dv.assign(6 * bodies.size(), R(0));
+        for (uint32_t it = 0; it < params.max_velocity_iterations; ++it) {
+            for (int i : seq_friction) solve_friction(rows[i]);
+            for (int i : seq_normal) solve_normal(rows[i]);
+        }
+        for (uint32_t h : island) {
+            Body<R>& b = bodies[h];
+            V3<R> el = b.acc_lin * dts, ea = b.acc_ang * dts;
+            b.lin = (b.lin + el) + v3<R>(dv[6 * h + 0], dv[6 * h + 1], dv[6 * h + 2]);
+            b.ang = (b.ang + ea) + v3<R>(dv[6 * h + 3], dv[6 * h + 4], dv[6 * h + 5]);
+            b.changed = true;
+            integrate(b);
+        }
+        for (auto& b : bodies) {
+            if (!b.alive) continue;
+            b.f_lin = b.f_ang = zero;
+            update_dynamics(b, dts);
+        }
+        cur_dt = dt0;
+        counters.ccd_substeps += 1;
+        counters.ccd_impacts += uint32_t(impacts.size());
+    }
+
+    // The island's contact rows in the reference's order (SORProx::step,
+    // sor_prox.rs:159-179), all started from zero (warmstart_coeff 0), and
+    // their position constraints in manifold order.
+    void assemble_ccd(std::vector<Manifold<R>>& ms) {
+        rows.clear();
+        pos_constraints.clear();
+        seq_warm.clear(); seq_friction.clear(); seq_normal.clear(); seq_pos.clear(); seq_merged.clear();
+        const R inv_dt = cur_dt == R(0) ? R(0) : R(1) / cur_dt;
+        std::vector<int> ug, un, bg, bn;
+        for (Manifold<R>& m : ms) {
+            const Collider<R>& c1 = colliders[m.c1];
+            const Collider<R>& c2 = colliders[m.c2];
+            const Body<R>& b1 = bodies[c1.body];
+            const Body<R>& b2 = bodies[c2.body];
+            const R mu = combine(c1.friction, c1.friction_combine, c2.friction, c2.friction_combine);
+            const R e = combine(c1.restitution, c1.restitution_combine, c2.restitution, c2.restitution_combine);
+            const bool ground = b1.ndofs() == 0 || b2.ndofs() == 0;
+            for (MContact<R>& k : m.contacts) {
+                const V3<R> n = k.g.normal;
+                const V3<R> center1 = k.g.world1 + n * c1.margin;
+                const V3<R> center2 = k.g.world2 - n * c2.margin;
+                Row<R> rn = make_row(b1, c1.body, b2, c2.body, center1, center2, -n, R(0));
+                if (rn.rhs <= -R(params.restitution_velocity_threshold)) rn.rhs = rn.rhs + e * rn.rhs;
+                const R depth = k.g.depth + c1.margin + c2.margin;
+                if (depth < R(0)) rn.rhs = rn.rhs + (-depth) * inv_dt;
+                rn.impulse = R(0);
+                rn.friction = false;
+                rn.cache = nullptr;
+                const int in = int(rows.size());
+                rows.push_back(rn);
+                pos_constraints.push_back(PosConstraint<R>{m.c1, m.c2, k.fid1, k.fid2, k.normal1_local});
+                seq_pos.push_back(int(pos_constraints.size()) - 1);
+                V3<R> t[2];
+                tangent_basis(n, t[0], t[1]);
+                (ground ? ug : un).push_back(in);
+                for (int s = 0; s < 2; ++s) {
+                    Row<R> rt = make_row(b1, c1.body, b2, c2.body, center1, center2, t[s], R(0));
+                    rt.impulse = R(0);
+                    rt.friction = true;
+                    rt.dep = in;
+                    rt.mu = mu;
+                    rt.cache = nullptr;
+                    (ground ? bg : bn).push_back(int(rows.size()));
+                    rows.push_back(rt);
+                }
+            }
+        }
+        for (int i : bn) seq_friction.push_back(i);
+        for (int i : bg) seq_friction.push_back(i);
+        for (int i : un) seq_normal.push_back(i);
+        for (int i : ug) seq_normal.push_back(i);
+    }
+
+    // Test hooks: the distance of two colliders' shapes at the current poses
+    // (direction from c1 toward c2), and the TOI of the pair over [0, horizon]
+    // from the current poses (returns -1: none, 0: an impact, 1: penetrating).
+    R collider_distance(uint32_t c1, uint32_t c2, V3<R>& dir) const {
+        const Collider<R>& A = colliders[c1];
+        const Collider<R>& B = colliders[c2];
+        const CcdShape<R> s1 = ccd_shape(A), s2 = ccd_shape(B);
+        const Iso<R> p1 = bodies[A.body].pos, p2 = bodies[B.body].pos;
+        const V3<R> origin = iso_pt(p1, s1.wrt.t);
+        const Core<R> k1 = place_core(s1, p1, origin), k2 = place_core(s2, p2, origin);
+        return (core_distance(k1, k2, dir) - k1.radius) - k2.radius;
+    }
+    int pair_toi(uint32_t c1, uint32_t c2, R horizon, R& toi) const {
+        const Collider<R>& A = colliders[c1];
+        const Collider<R>& B = colliders[c2];
+        auto motion = [&](const Body<R>& b) {
+            CcdMotion<R> m;
+            m.start = b.pos;
+            m.local_com = b.local_com;
+            m.lin = b.lin;
+            m.ang = b.ang;
+            m.tau = R(0);
+            m.linear_only = b.linear_interp();
+            m.moving = true;
+            return m;
+        };
+        const CaResult r = conservative_advancement(ccd_shape(A), motion(bodies[A.body]), ccd_shape(B),
+                                                    motion(bodies[B.body]), horizon, R(params.allowed_linear_error), toi);
+        return !r.some ? -1 : (r.penetrating ? 1 : 0);
+    }
+
+    void solve_ccd() {
+        const R dt0 = R(params.dt);
+        if (dt0 == R(0) || params.max_ccd_substeps == 0) return;
+        bool any = false;
+        for (const auto& c : colliders) any = any || (c.alive && c.ccd);
+        if (!any) return;
+        body_colliders.assign(bodies.size(), {});
+        for (uint32_t c = 0; c < colliders.size(); ++c)
+            if (colliders[c].alive) body_colliders[colliders[c].body].push_back(c);
+        const R sub = dt0 / R(params.max_ccd_substeps);
+        ccd_time.assign(bodies.size(), R(0));
+        R end_time = R(0);
+        bool last_iter = false;
+        std::vector<TOIEntry> impacts;
+        std::vector<R> frozen;
+        std::vector<char> is_frozen;
+        for (;;) {
+            if (end_time < dt0) end_time = std::min(end_time + sub, dt0);
+            else last_iter = true;
+            ccd_sweep_boxes();
+            R mo;
+            int pr = predict(end_time, impacts, frozen, is_frozen, mo);
+            if (pr == PRED_AFTER) {
+                end_time = std::floor(mo / sub) * sub;
+                end_time = std::min(end_time + sub, dt0);
+                pr = predict(end_time, impacts, frozen, is_frozen, mo);
+                if (pr != PRED_IMPACTS) impacts.clear();
+            }
+            if (!last_iter && !impacts.empty()) {
+                ccd_substep(impacts, frozen, is_frozen);
+                continue;
+            }
+            for (uint32_t h = 0; h < bodies.size(); ++h)
+                if (is_frozen.size() > h && is_frozen[h] && bodies[h].alive && bodies[h].status != NPGPU_BODY_STATIC)
+                    clamp_advancement(bodies[h]);
+            break;
+        }
+        ccd_time.assign(bodies.size(), R(0));
+    }
+
     // ------------------------------------------------------- the step
     // MechanicalWorld::step_with_filter (mechanical_world.rs:199-396).
     npgpu_status step() {
-        R dt = R(params.dt);
+        cur_dt = R(params.dt);
+        R dt = cur_dt;
         events.clear();
         // maintain: register new colliders (geometrical_world.rs:102-143).
         for (auto& c : colliders) {
@@ -2591,6 +3022,7 @@ public:
         }
         for (auto& b : bodies) {
             if (!b.alive) continue;
+            b.pos0 = b.pos;   // RigidBody::step_started (rigid_body.rs:517-519)
             update_dynamics(b, dt);
         }
         for (auto& b : bodies)
@@ -2618,6 +3050,8 @@ public:
             if (b.alive && b.kinematic()) integrate(b);
         for (auto& b : bodies)
             if (b.alive) update_dynamics(b, dt);
+        counters.ccd_substeps = counters.ccd_impacts = 0;
+        solve_ccd();
         for (auto& b : bodies)
             if (b.alive) b.f_lin = b.f_ang = v3<R>(R(0), R(0), R(0));
         collision_detection();

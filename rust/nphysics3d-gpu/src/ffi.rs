@@ -140,6 +140,7 @@ pub struct npgpu_params {
     pub use_graph: u32,
     pub world_threads: u32,
     pub sweep_order: u32,
+    pub ccd_on_penetration_enabled: u32,
 }
 
 #[repr(C)]
@@ -191,6 +192,8 @@ pub struct npgpu_counters {
     pub learned_starts: u32,
     pub learned_kept: u32,
     pub graph_replay: u32,
+    pub ccd_substeps: u32,
+    pub ccd_impacts: u32,
     pub reserved: u32,
 }
 
