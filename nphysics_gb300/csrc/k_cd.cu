@@ -369,31 +369,8 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
     float m1 = c.margin[c1], m2 = c.margin[c2];
     float prediction = (m1 + c.lin_pred[c1]) + (m2 + c.lin_pred[c2]);
     CandList out;
-    out.n = 0;
-    int keep[kMaxContacts] = {0, 1, 2, 3};
-    int nk;
-    if (a.shape == SHAPE_BALL && b.shape == SHAPE_BALL) {
-        np::V v = np::sub(b.pose.t, a.pose.t);
-        float l2 = np::dot(v, v);
-        np::V n0 = l2 > 0.0f ? np::divs(v, sqrtf(l2)) : np::mk(1.0f, 0.0f, 0.0f);
-        push_eval(out, a, b, 0, 0, n0, prediction);
-        nk = out.n;
-    } else if (a.shape == SHAPE_CUBOID && b.shape == SHAPE_BALL) {
-        ball_box(b, a, true, prediction, out);
-        nk = out.n;
-    } else if (a.shape == SHAPE_BALL && b.shape == SHAPE_CUBOID) {
-        ball_box(a, b, false, prediction, out);
-        nk = out.n;
-    } else if (a.shape == SHAPE_CAPSULE || b.shape == SHAPE_CAPSULE) {
-        if (a.shape == SHAPE_CAPSULE && b.shape == SHAPE_CAPSULE) capsule_capsule(a, b, prediction, out);
-        else if (a.shape == SHAPE_BALL) ball_capsule(a, b, false, prediction, out);
-        else if (b.shape == SHAPE_BALL) ball_capsule(b, a, true, prediction, out);
-        else if (a.shape == SHAPE_CUBOID) capsule_box(b, a, true, prediction, out);
-        else capsule_box(a, b, false, prediction, out);
-        nk = out.n;
-    } else {
-        nk = box_box(a, b, prediction, out, keep);
-    }
+    int keep[kMaxContacts];
+    const int nk = shape_pair_contacts(a, b, prediction, out, keep);
     // Previous manifold of this pair: among the pairs its owner wrote last pass.
     uint32_t owner = owns(c, c1, c2) ? c1 : c2;
     uint32_t qs = w.prev.owner_start[owner], qn = w.prev.owner_count[owner];

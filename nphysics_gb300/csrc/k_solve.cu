@@ -32,6 +32,7 @@
 
 #include <cooperative_groups.h>
 
+#include "ccd.cuh"
 #include "mlp.cuh"
 #include "narrow.cuh"
 #include "sortscan.cuh"
@@ -2897,6 +2898,10 @@ __global__ void __launch_bounds__(kClusterThreads, 1) k_cluster_position(World w
 }
 #endif
 
+#if !NPGPU_EXCHANGE_TU
+#include "k_ccd.cuh"
+#endif
+
 // ================================================================ post
 #if !NPGPU_EXCHANGE_TU
 __global__ void k_post(World w, StepParams p, bool posef) {
@@ -2925,12 +2930,15 @@ __global__ void k_post(World w, StepParams p, bool posef) {
         if ((info & BI_CHANGED) && st == 2u) body_update_dynamics(b, i, p.dt);
         b.f_lin[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
         b.f_ang[i] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-        b.info[i] = b.info[i] & ~BI_CHANGED;
+        // With CCD the update flags stay until its substeps have run, and the
+        // energy audit is taken after them (k_ccd_finish).
+        if (!p.ccd) b.info[i] = b.info[i] & ~BI_CHANGED;
         if (st == 2u) {
             float4 l = b.lin[i], a = b.ang[i], tt = b.pos_t[i];
             if (!(isfinite(l.x) && isfinite(l.y) && isfinite(l.z) && isfinite(a.x) && isfinite(a.y) && isfinite(a.z) &&
                   isfinite(tt.x) && isfinite(tt.y) && isfinite(tt.z)))
                 atomicOr(&w.ctl->err, ERRF_NAN);
+            if (p.ccd) continue;
             np::M I = load_m9(b.I + 9 * i);
             np::V av = v3(a);
             np::V iw = np::mv(I, av);
@@ -3192,6 +3200,18 @@ cudaError_t launch_solver(const World& w, const StepParams& p, const SolverLaunc
     }
     rec(6);
     k_post<<<nbb, kItemThreads, 0, st>>>(wc, pc, posef);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ccd_begin(const World& w, cudaStream_t st) {
+    k_ccd_begin<<<item_blocks(w.nb_slots), kItemThreads, 0, st>>>(w);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ccd(const World& w, const StepParams& p, cudaStream_t st) {
+    if (!p.ccd || w.ccd.n_worlds == 0) return cudaSuccess;
+    k_ccd_world<<<w.ccd.n_worlds, kCcdThreads, 0, st>>>(w, p);
+    k_ccd_finish<<<item_blocks(w.nb_slots), kItemThreads, 0, st>>>(w);
     return cudaGetLastError();
 }
 

@@ -719,4 +719,36 @@ static __device__ __noinline__ int box_box(const Shape& A, const Shape& B, float
     return reduce4(cands, keep);
 }
 
+// The contacts of two posed shapes within `prediction`: the candidates in
+// `out` and the ones the manifold keeps, keep[0 .. returned count).
+__device__ __forceinline__ int shape_pair_contacts(const Shape& a, const Shape& b, float prediction, CandList& out,
+                                                   int keep[kMaxContacts]) {
+    out.n = 0;
+    for (int k = 0; k < kMaxContacts; ++k) keep[k] = k;
+    if (a.shape == SHAPE_BALL && b.shape == SHAPE_BALL) {
+        np::V v = np::sub(b.pose.t, a.pose.t);
+        float l2 = np::dot(v, v);
+        np::V n0 = l2 > 0.0f ? np::divs(v, sqrtf(l2)) : np::mk(1.0f, 0.0f, 0.0f);
+        push_eval(out, a, b, 0, 0, n0, prediction);
+        return out.n;
+    }
+    if (a.shape == SHAPE_CUBOID && b.shape == SHAPE_BALL) {
+        ball_box(b, a, true, prediction, out);
+        return out.n;
+    }
+    if (a.shape == SHAPE_BALL && b.shape == SHAPE_CUBOID) {
+        ball_box(a, b, false, prediction, out);
+        return out.n;
+    }
+    if (a.shape == SHAPE_CAPSULE || b.shape == SHAPE_CAPSULE) {
+        if (a.shape == SHAPE_CAPSULE && b.shape == SHAPE_CAPSULE) capsule_capsule(a, b, prediction, out);
+        else if (a.shape == SHAPE_BALL) ball_capsule(a, b, false, prediction, out);
+        else if (b.shape == SHAPE_BALL) ball_capsule(b, a, true, prediction, out);
+        else if (a.shape == SHAPE_CUBOID) capsule_box(b, a, true, prediction, out);
+        else capsule_box(a, b, false, prediction, out);
+        return out.n;
+    }
+    return box_box(a, b, prediction, out, keep);
+}
+
 }  // namespace npgpu_dev

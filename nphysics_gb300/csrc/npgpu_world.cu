@@ -204,6 +204,16 @@ struct npgpu_world {
     uint32_t nj_slots = 0, nj_alive = 0, cap_j = 0;
     bool joints_local_dirty = false;     // the joints' world-local slots (Joints::local) need recomputing
     std::vector<uint32_t> h_jlocal;
+    // Continuous collision detection: the colliders by (world, slot) and the
+    // colliders of each body, rebuilt when colliders or worlds change, and the
+    // device scratch (Ccd), allocated with the first CCD collider and grown
+    // with the colliders and worlds.
+    bool ccd_dirty = true;
+    bool ccd_any = false;                // a CCD collider is alive
+    bool last_step_ccd = false;
+    size_t ccd_region = 0, ccd_worlds_cap = 0, ccd_bodies_cap = 0, ccd_colliders_cap = 0;
+    std::vector<void*> ccd_fixed, ccd_grown;
+    std::vector<uint32_t> h_ccd_order, h_ccd_wstart, h_ccd_wflag, h_bc_start, h_bc_list;
 };
 
 // The message of the last failure without a world (npgpu_create, the
@@ -264,6 +274,7 @@ static StepParams step_params(const npgpu_world* w) {
     s.profile = p.profile;
     s.allowed_angular_error = p.allowed_angular_error;
     s.max_angular_correction = p.max_angular_correction;
+    s.ccd = (w->ccd_any && p.max_ccd_substeps > 0 && p.dt > 0.0f) ? 1u : 0u;
     return s;
 }
 
@@ -616,6 +627,8 @@ void npgpu_destroy(npgpu_world* w) {
     if (!w) return;
     if (w->stream) cudaStreamSynchronize(w->stream);
     for (void* p : w->owned) cudaFree(p);
+    for (void* p : w->ccd_fixed) cudaFree(p);
+    for (void* p : w->ccd_grown) cudaFree(p);
     cudaFree(w->dw.s.world_start);
     cudaFree(w->dw.s.bucket_count);
     cudaFree(w->dw.s.bucket_start);
@@ -718,7 +731,7 @@ npgpu_status npgpu_upsert_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
         u.max_lin = d.max_linear_velocity;
         u.max_ang = d.max_angular_velocity;
         u.sleep_thr = d.sleep_threshold;
-        if (!hb.alive || hb.world != d.world) w->layout_dirty = w->local_dirty = true;
+        if (!hb.alive || hb.world != d.world) w->layout_dirty = w->local_dirty = w->ccd_dirty = true;
         w->max_world = std::max(w->max_world, d.world);
         hb.alive = true;
         hb.gen = handles[k].generation;
@@ -782,7 +795,6 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID && d.shape != NPGPU_SHAPE_CAPSULE)
             return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "only Ball, Cuboid and Capsule shapes are supported");
         if (d.is_sensor) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "sensor colliders are not supported");
-        if (d.ccd_enabled) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "CCD-enabled colliders are not supported");
         if (slot >= w->cap_c) return fail(w, NPGPU_ERR_CAPACITY, "collider index beyond the world's capacity");
         if (!body_handle_ok(w, d.body)) return fail(w, NPGPU_ERR_INVALID_HANDLE, "collider parent body handle is invalid");
         if (!finite_n(d.position_wrt_body, 7) || !finite_n(d.shape_params, 3) || !std::isfinite(d.margin) ||
@@ -808,7 +820,7 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         std::memset(&u, 0, sizeof(u));
         u.slot = (uint32_t)slot;
         u.body = (uint32_t)d.body.index;
-        u.info = d.shape | (d.friction_combine << 4) | (d.restitution_combine << 8);
+        u.info = d.shape | (d.friction_combine << 4) | (d.restitution_combine << 8) | (d.ccd_enabled ? CI_CCD : 0u);
         u.params[0] = d.shape_params[0];
         u.params[1] = d.shape_params[1];
         u.params[2] = d.shape_params[2];
@@ -825,7 +837,7 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         up.push_back(u);
     }
     if (up.empty()) return NPGPU_OK;
-    w->local_dirty = true;
+    w->local_dirty = w->ccd_dirty = true;
     void* dp = nullptr;
     npgpu_status st = stage_upload(w, up.data(), up.size() * sizeof(ColliderUpload), &dp);
     if (st != NPGPU_OK) return st;
@@ -1080,7 +1092,7 @@ npgpu_status npgpu_remove_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
     }
     w->forget_pending = true;
     w->cd_dirty = true;
-    w->local_dirty = true;
+    w->local_dirty = w->ccd_dirty = true;
     return kill_slots(w, slots, 1);
 }
 
@@ -1101,7 +1113,7 @@ npgpu_status npgpu_remove_bodies(npgpu_world* w, uint32_t n, const npgpu_handle*
             }
         }
         w->hb[bi].alive = false;
-        w->layout_dirty = w->local_dirty = true;
+        w->layout_dirty = w->local_dirty = w->ccd_dirty = true;
         bslots.push_back((uint32_t)bi);
     }
     // Joints with a removed body are removed, waking their other body
@@ -1282,6 +1294,122 @@ static npgpu_status maintain(npgpu_world* w) {
     return NPGPU_OK;
 }
 
+// The CCD layout: alive colliders by (world, slot) with each world's range
+// and whether it has a CCD collider, the colliders of each body in slot
+// order, and the device scratch for them (Ccd). Run when colliders or worlds
+// changed.
+static npgpu_status ccd_layout(npgpu_world* w) {
+    w->ccd_dirty = false;
+    std::vector<std::pair<uint32_t, uint32_t>> by_world;
+    bool any = false;
+    uint32_t maxw = 0;
+    for (uint32_t ci = 0; ci < w->nc_slots; ++ci) {
+        const HostCollider& c = w->hc[ci];
+        if (!c.alive) continue;
+        const uint32_t wd = w->hb[c.desc.body.index].world;
+        by_world.push_back({wd, ci});
+        any = any || c.desc.ccd_enabled != 0;
+        maxw = std::max(maxw, wd);
+    }
+    w->ccd_any = any;
+    if (!any) {
+        w->dw.ccd.n_worlds = 0;
+        return NPGPU_OK;
+    }
+    std::sort(by_world.begin(), by_world.end());
+    const uint32_t nw = maxw + 1, n = (uint32_t)by_world.size();
+    w->h_ccd_order.resize(std::max<uint32_t>(n, 1u));
+    w->h_ccd_wstart.assign(nw + 1, 0u);
+    w->h_ccd_wflag.assign(nw, 0u);
+    for (uint32_t i = 0; i < n; ++i) {
+        w->h_ccd_order[i] = by_world[i].second;
+        w->h_ccd_wstart[by_world[i].first + 1] += 1;
+        if (w->hc[by_world[i].second].desc.ccd_enabled) w->h_ccd_wflag[by_world[i].first] = 1u;
+    }
+    for (uint32_t k = 0; k < nw; ++k) w->h_ccd_wstart[k + 1] += w->h_ccd_wstart[k];
+    w->h_bc_start.assign(w->nb_slots + 1, 0u);
+    for (uint32_t ci = 0; ci < w->nc_slots; ++ci)
+        if (w->hc[ci].alive) w->h_bc_start[w->hc[ci].desc.body.index + 1] += 1;
+    for (uint32_t b = 0; b < w->nb_slots; ++b) w->h_bc_start[b + 1] += w->h_bc_start[b];
+    w->h_bc_list.assign(std::max<uint32_t>(w->h_bc_start[w->nb_slots], 1u), 0u);
+    {
+        std::vector<uint32_t> fill(w->h_bc_start.begin(), w->h_bc_start.end() - 1);
+        for (uint32_t ci = 0; ci < w->nc_slots; ++ci)
+            if (w->hc[ci].alive) w->h_bc_list[fill[w->hc[ci].desc.body.index]++] = ci;
+    }
+    Ccd& cd = w->dw.ccd;
+    bool ok = true;
+    auto alloc = [&](std::vector<void*>& owner, void** out, size_t bytes) {
+        if (!ok) return;
+        void* p = nullptr;
+        ok = cudaMalloc(&p, std::max<size_t>(bytes, 16)) == cudaSuccess;
+        if (ok) {
+            *out = p;
+            owner.push_back(p);
+        }
+    };
+    // Per body and per collider: sized by the world's capacities, once.
+    if (w->ccd_bodies_cap == 0) {
+        const size_t B = w->cap_b + 1, C = w->cap_c;
+        alloc(w->ccd_fixed, (void**)&cd.pos0_t, sizeof(float4) * B);
+        alloc(w->ccd_fixed, (void**)&cd.pos0_q, sizeof(float4) * B);
+        alloc(w->ccd_fixed, (void**)&cd.btime, sizeof(float) * B);
+        alloc(w->ccd_fixed, (void**)&cd.ftime, sizeof(float) * B);
+        alloc(w->ccd_fixed, (void**)&cd.bflag, sizeof(uint32_t) * B);
+        alloc(w->ccd_fixed, (void**)&cd.bc_start, sizeof(uint32_t) * (B + 1));
+        alloc(w->ccd_fixed, (void**)&cd.sw_min, sizeof(float4) * C);
+        alloc(w->ccd_fixed, (void**)&cd.sw_max, sizeof(float4) * C);
+        alloc(w->ccd_fixed, (void**)&cd.cflag, sizeof(uint32_t) * C);
+        alloc(w->ccd_fixed, (void**)&cd.order, sizeof(uint32_t) * C);
+        alloc(w->ccd_fixed, (void**)&cd.bc_list, sizeof(uint32_t) * C);
+        cd.pool_cap = (uint32_t)std::min<size_t>(std::max<size_t>(4096, C), 65536);
+        alloc(w->ccd_fixed, (void**)&cd.pool, sizeof(CcdManifold) * cd.pool_cap);
+        if (!ok) return fail(w, NPGPU_ERR_CUDA, "CCD arrays: cudaMalloc failed");
+        CK(cudaMemsetAsync(cd.bflag, 0, sizeof(uint32_t) * B, w->stream), "CCD arrays");
+        CK(cudaMemsetAsync(cd.cflag, 0, sizeof(uint32_t) * C, w->stream), "CCD arrays");
+        w->ccd_bodies_cap = B;
+        w->ccd_colliders_cap = C;
+    }
+    // Per world and the worlds' regions: grown with the worlds and colliders.
+    const size_t region = (size_t)kCcdRegion * n + (size_t)kCcdSlack * nw;
+    if (nw > w->ccd_worlds_cap || region > w->ccd_region) {
+        CK(cudaStreamSynchronize(w->stream), "CCD arrays");
+        for (void* p : w->ccd_grown) cudaFree(p);
+        w->ccd_grown.clear();
+        const size_t W = std::max<size_t>(nw, 2 * w->ccd_worlds_cap), R = std::max<size_t>(region, 2 * w->ccd_region);
+        alloc(w->ccd_grown, (void**)&cd.wstart, sizeof(uint32_t) * (W + 1));
+        alloc(w->ccd_grown, (void**)&cd.wflag, sizeof(uint32_t) * W);
+        alloc(w->ccd_grown, (void**)&cd.wdts, sizeof(float) * W);
+        alloc(w->ccd_grown, (void**)&cd.nbr, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.stack, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.island, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.ccdb, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.mlist, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.tres, sizeof(float2) * R);
+        alloc(w->ccd_grown, (void**)&cd.heap, sizeof(CcdToi) * R);
+        alloc(w->ccd_grown, (void**)&cd.impacts, sizeof(CcdToi) * R);
+        if (!ok) {
+            w->ccd_worlds_cap = w->ccd_region = 0;
+            return fail(w, NPGPU_ERR_CUDA, "CCD scratch: cudaMalloc failed");
+        }
+        w->ccd_worlds_cap = W;
+        w->ccd_region = R;
+    }
+    CK(cudaMemcpyAsync(cd.order, w->h_ccd_order.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, w->stream),
+       "CCD layout");
+    CK(cudaMemcpyAsync(cd.wstart, w->h_ccd_wstart.data(), sizeof(uint32_t) * (nw + 1), cudaMemcpyHostToDevice,
+                       w->stream), "CCD layout");
+    CK(cudaMemcpyAsync(cd.wflag, w->h_ccd_wflag.data(), sizeof(uint32_t) * nw, cudaMemcpyHostToDevice, w->stream),
+       "CCD layout");
+    CK(cudaMemcpyAsync(cd.bc_start, w->h_bc_start.data(), sizeof(uint32_t) * (w->nb_slots + 1),
+                       cudaMemcpyHostToDevice, w->stream), "CCD layout");
+    CK(cudaMemcpyAsync(cd.bc_list, w->h_bc_list.data(), sizeof(uint32_t) * w->h_bc_list.size(),
+                       cudaMemcpyHostToDevice, w->stream), "CCD layout");
+    CK(cudaStreamSynchronize(w->stream), "CCD layout");
+    cd.n_worlds = nw;
+    return NPGPU_OK;
+}
+
 static npgpu_status run_cd(npgpu_world* w, const StepParams& sp) {
     std::swap(w->dw.cur, w->dw.prev);
     sync_world_view(w);
@@ -1345,8 +1473,10 @@ static npgpu_status step_graphed(npgpu_world* w, const StepParams& sp) {
         cudaGraph_t graph = nullptr;
         cudaError_t e = cudaStreamBeginCapture(w->stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t e1 = launch_body_start(w->dw, sp, w->stream);
+            cudaError_t e0 = sp.ccd ? launch_ccd_begin(w->dw, w->stream) : cudaSuccess;
+            cudaError_t e1 = e0 == cudaSuccess ? launch_body_start(w->dw, sp, w->stream) : e0;
             cudaError_t e2 = e1 == cudaSuccess ? launch_solver(w->dw, sp, w->solver, w->stream) : e1;
+            if (e2 == cudaSuccess && sp.ccd) e2 = launch_ccd(w->dw, sp, w->stream);
             npgpu_status s3 = e2 == cudaSuccess ? run_cd(w, sp) : NPGPU_ERR_CUDA;
             e = cudaStreamEndCapture(w->stream, &graph);
             if (s3 != NPGPU_OK && e == cudaSuccess) e = cudaErrorStreamCaptureInvalidated;
@@ -1379,7 +1509,15 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
         return fail(w, NPGPU_ERR_INVALID_ARGUMENT,
                     "warmstart_mode 2 and 3 need a network (npgpu_mlp_set or npgpu_mlp_train)");
     if (w->params.warmstart_mode > 3) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "unknown warmstart_mode");
+    if (w->ccd_dirty) {
+        npgpu_status st = ccd_layout(w);
+        if (st != NPGPU_OK) return st;
+    }
+    w->dw.ccd.substeps = w->params.max_ccd_substeps;
+    w->dw.ccd.on_penetration = w->params.ccd_on_penetration_enabled ? 1u : 0u;
+    w->dw.ccd.max_position_iterations = w->params.max_ccd_position_iterations;
     StepParams sp = step_params(w);
+    w->last_step_ccd = sp.ccd != 0u;
     for (uint32_t s = 0; s < nsteps; ++s) {
         npgpu_status st = maintain(w);
         if (st != NPGPU_OK) return st;
@@ -1398,6 +1536,7 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
             }
         }
         if (prof) CK(cudaEventRecord(w->ev[0], w->stream), "event");
+        if (sp.ccd) CK(launch_ccd_begin(w->dw, w->stream), "CCD begin");
         CK(launch_body_start(w->dw, sp, w->stream), "body start");
         w->cd_start_ran = w->cd_dirty;
         if (w->cd_dirty) {
@@ -1408,6 +1547,7 @@ npgpu_status npgpu_step(npgpu_world* w, uint32_t nsteps, uint32_t num_joints, ui
         if (prof) CK(cudaEventRecord(w->ev[1], w->stream), "event");
         w->solver.ev = prof ? w->ev_solver : nullptr;
         CK(launch_solver(w->dw, sp, w->solver, w->stream), "solve");
+        if (sp.ccd) CK(launch_ccd(w->dw, sp, w->stream), "CCD");
         if (prof) CK(cudaEventRecord(w->ev[2], w->stream), "event");
         st = run_cd(w, sp);
         if (st != NPGPU_OK) return st;
@@ -1436,6 +1576,8 @@ npgpu_status npgpu_synchronize(npgpu_world* w) {
         if (err & ERRF_TASKS)
             return fail(w, NPGPU_ERR_CAPACITY, "more solver manifolds than the cooperative grid holds (16 per thread)");
         if (err & ERRF_WORLD_RANGE) return fail(w, NPGPU_ERR_CUDA, "a solver manifold left its world's slot range");
+        if (err & ERRF_CCD_CAPACITY)
+            return fail(w, NPGPU_ERR_CAPACITY, "a world's CCD lists or the CCD island pool overflowed");
     }
     return NPGPU_OK;
 }
@@ -1899,6 +2041,8 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
     k.learned_starts = c.learned_starts;
     k.learned_kept = c.learned_kept;
     k.graph_replay = w->last_step_graphed ? 1u : 0u;
+    k.ccd_substeps = w->last_step_ccd ? c.ccd_substeps : 0u;
+    k.ccd_impacts = w->last_step_ccd ? c.ccd_impacts : 0u;
     if (w->params.profile && w->ev_recorded) {
         float ms = 0.0f;
         cudaEventElapsedTime(&ms, w->ev[0], w->ev[3]);

@@ -41,6 +41,7 @@ enum : uint32_t {
     ERRF_UNION_FIND = 1u << 4,
     ERRF_WORLD_RANGE = 1u << 5,      // a batched world's body outside its slot range
     ERRF_TASKS = 1u << 6,            // more solver manifolds than a cooperative grid holds
+    ERRF_CCD_CAPACITY = 1u << 7,     // a world's CCD lists or the island pool overflowed (its CCD stopped)
 };
 
 constexpr int kMaxContacts = 4;      // contacts per manifold
@@ -108,7 +109,7 @@ struct Colliders {
     uint32_t *leaf_count, *leaf_offset;
     uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
 };
-enum : uint32_t { CI_ALIVE = 1u << 16 };
+enum : uint32_t { CI_ALIVE = 1u << 16, CI_CCD = 1u << 17 };
 
 // Joint constraints by joint slot (= the generational-arena index of the
 // host joint set). The host writes the description; the impulses and the
@@ -238,7 +239,9 @@ struct Control {
     uint32_t force_flags;            // checks of the last force batch: 1 bad handle, 2 non-finite, 4 a body twice
     double mlp_loss;                 // loss of the last training step
     uint32_t nevents;                // contact events of this step so far (may exceed World::events_cap)
-    uint32_t pad2;
+    uint32_t ccd_mcount;             // CCD island manifolds taken from the pool this step
+    uint32_t ccd_substeps, ccd_impacts;
+    uint32_t pad3;
 };
 
 struct StepParams {
@@ -254,6 +257,57 @@ struct StepParams {
     uint32_t profile;
     uint32_t sweep_order;            // NPGPU_SWEEP_*
     float allowed_angular_error, max_angular_correction;
+    uint32_t ccd;                    // 1: CCD runs after the solver (the update flags and the energy audit wait for it)
+};
+
+// Continuous collision detection (MechanicalWorld::solve_ccd), one block per
+// world that has a CCD collider. Allocated when the first CCD collider
+// appears. A world's lists live in its own region of each scratch array:
+// region base kCcdRegion * order index of its first collider + kCcdSlack *
+// world, length kCcdRegion * its colliders + kCcdSlack.
+constexpr uint32_t kCcdRegion = 4, kCcdSlack = 64;
+struct CcdToi {                      // a time of impact in a world's queue
+    float toi;
+    uint32_t c1, c2;
+    uint32_t seq;                    // order of discovery; bit 31: superseded by a resweep
+};
+struct CcdContact {                  // a contact of a substep's island
+    float4 n;                        // normal from collider 1 toward 2; depth in w
+    float4 w1, w2;                   // world points (xyz); w1.w: feature key fid1 * 26 + fid2
+    float4 nl;                       // normal in body 1's frame
+    float4 pos1, pos2;               // lever arms from the centres of mass; r and rhs of the normal row in w
+    float4 rr;                       // r, rhs of the two friction rows
+    float4 lam;                      // impulses (normal, friction 1, friction 2)
+    float4 t1, t2;                   // friction directions
+};
+struct CcdManifold {
+    uint32_t c1, c2, nc, mask;       // mask: unlocked dofs (sm_mask's layout)
+    int b1, b2;                      // dynamic body slots (-1: no dofs)
+    float mu, pad;
+    CcdContact k[kMaxContacts];
+};
+struct Ccd {
+    uint32_t *order;                 // collider slots sorted by (world, slot)
+    unsigned long long *keys, *keys_sorted;
+    uint32_t *slots;                 // 0..n-1, the sort's values
+    uint32_t *wstart;                // per world: first index into `order` (n_worlds + 1)
+    uint32_t *wflag;                 // per world: 1 when it has a CCD collider
+    float *wdts;                     // per world: the last substep's length (< 0: none this step)
+    uint32_t *bc_start, *bc_list;    // colliders of each body, in slot order (host-built CSR)
+    float4 *sw_min, *sw_max;         // per collider: the box swept from the safe pose to the current one
+    float4 *pos0_t, *pos0_q;         // per body: position0
+    float *btime, *ftime;            // per body: SubstepState::body_times, frozen time
+    uint32_t *bflag;                 // per body: 1 frozen, 2 prepared
+    uint32_t *cflag;                 // per collider: 1 visited
+    uint32_t *nbr, *stack, *island, *ccdb, *mlist;   // per-world regions
+    float2 *tres;                    // per-world region: TOI results aligned with nbr
+    CcdToi *heap, *impacts;          // per-world regions
+    CcdManifold *pool;               // island manifolds of all worlds, taken by an atomic counter
+    uint32_t pool_cap;
+    uint32_t n_worlds;               // world indices in use (max + 1)
+    uint32_t substeps;               // max_ccd_substeps
+    uint32_t on_penetration;         // ccd_on_penetration_enabled
+    uint32_t max_position_iterations;   // max_ccd_position_iterations
 };
 
 struct MlpDev;
@@ -271,6 +325,7 @@ struct World {
     uint32_t events_cap;
     Joints j;
     uint32_t nj_slots;               // joint slots in use (0: no joint kernels run)
+    Ccd ccd;                         // allocated when a CCD collider exists (ccd.order non-null)
 };
 
 // ---- launchers (defined in the kernel translation units) ----
@@ -360,6 +415,9 @@ cudaError_t launch_upload_bodies(const World& w, const BodyUpload* d, uint32_t n
 cudaError_t launch_upload_colliders(const World& w, const ColliderUpload* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_mass_updates(const World& w, const MassUpdate* d, uint32_t n, cudaStream_t st);
 cudaError_t launch_upload_joints(const World& w, const JointUpload* d, uint32_t n, cudaStream_t st);
+// CCD: position0 of every body at the step's start; the worlds' CCD after the solver.
+cudaError_t launch_ccd_begin(const World& w, cudaStream_t st);
+cudaError_t launch_ccd(const World& w, const StepParams& p, cudaStream_t st);
 // Poses (7 floats) and velocities (6) of slots [first, first + n) into
 // page-locked host arrays, given by their device-side addresses.
 cudaError_t launch_pack_bodies_host(const World& w, uint32_t first, uint32_t n, float* pos7, float* vel6,

@@ -477,6 +477,22 @@ def ccd_stack(height=4, speed=80.0, balls=3, ccd=True, seed=5, world=0):
     return Scene("ccd stack", bodies, colliders)
 
 
+def batched_ccd(n_worlds=6, seed=7, worlds=None):
+    """Worlds alternating a tower struck by CCD balls and fast CCD
+    projectiles at a thin wall (balls and spinning cubes), under gravity;
+    `worlds` builds only those."""
+    worlds = range(n_worlds) if worlds is None else worlds
+    parts = []
+    for w in worlds:
+        if w % 3 == 0:
+            parts.append(ccd_stack(height=3 + w % 2, speed=60.0 + 5.0 * w, balls=2, seed=seed + w))
+        else:
+            sc = ccd_wall(n=3, shape=abi.SHAPE_BALL if w % 3 == 1 else abi.SHAPE_CUBOID, spin=10.0 * (w % 3),
+                          speed=90.0 + 4.0 * w, seed=seed + w, gravity=(0.0, -9.81, 0.0))
+            parts.append(sc)
+    return concat_worlds(parts, f"{len(parts)} CCD worlds")
+
+
 # ---------------------------------------------------------------- small scenes
 def single_body(shape=abi.SHAPE_CUBOID, params=(0.5, 0.5, 0.5), position=(0, 5, 0), velocity=(0, 0, 0, 0, 0, 0),
                 rotation=(0, 0, 0, 1), ground=True, density=1.0, friction=0.5, restitution=0.0):
@@ -826,7 +842,7 @@ def concat_worlds(parts, name="batched worlds"):
         colliders.append(c)
         joints.append(j)
         off += len(b)
-    sc = Scene(name, np.concatenate(bodies), np.concatenate(colliders), steps=parts[0].steps)
+    sc = Scene(name, np.concatenate(bodies), np.concatenate(colliders), gravity=parts[0].gravity, steps=parts[0].steps)
     return set_joints(sc, np.concatenate(joints))
 
 

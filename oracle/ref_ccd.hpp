@@ -145,15 +145,21 @@ template <class R> inline bool outside_face(V3<R> a, V3<R> b, V3<R> c, V3<R> d) 
     return sp * sd < R(0);
 }
 
+// A flat tetrahedron (volume below 1e-4 times the product of its edge
+// lengths from a) holds no interior: its faces are all candidates.
 template <class R> inline V3<R> closest_tetrahedron(Simplex<R>& s, bool& inside) {
     const V3<R> a = s.p[0], b = s.p[1], c = s.p[2], d = s.p[3];
+    const V3<R> ab = b - a, ac = c - a, ad = d - a;
+    const R vol = dot(ad, cross(ab, ac));
+    const R scale = (norm(ab) * norm(ac)) * norm(ad);
+    const bool flat = !(std::fabs(vol) > R(1e-4) * scale);
     inside = true;
     R best = R(0);
     V3<R> out = v3<R>(R(0), R(0), R(0));
     Simplex<R> keep;
     const V3<R> f[4][4] = {{a, b, c, d}, {a, c, d, b}, {a, d, b, c}, {b, d, c, a}};
     for (int k = 0; k < 4; ++k) {
-        if (!outside_face(f[k][0], f[k][1], f[k][2], f[k][3])) continue;
+        if (!flat && !outside_face(f[k][0], f[k][1], f[k][2], f[k][3])) continue;
         Simplex<R> t;
         t.p[0] = f[k][0];
         t.p[1] = f[k][1];

@@ -2700,8 +2700,8 @@ public:
 
     // predict_next_impacts: the impacts up to end_time in time order, the
     // bodies frozen at their first impact, the smallest TOI beyond end_time.
-    int predict(R end_time, std::vector<TOIEntry>& impacts, std::vector<R>& frozen, std::vector<char>& is_frozen,
-                R& min_overstep) {
+    int predict(uint32_t world, R end_time, std::vector<TOIEntry>& impacts, std::vector<R>& frozen,
+                std::vector<char>& is_frozen, R& min_overstep) {
         impacts.clear();
         frozen.assign(bodies.size(), R(0));
         is_frozen.assign(bodies.size(), 0);
@@ -2713,7 +2713,7 @@ public:
         min_overstep = dt0;
         std::vector<uint32_t> nbr;
         for (uint32_t c = 0; c < colliders.size(); ++c) {
-            if (!colliders[c].alive || !colliders[c].ccd) continue;
+            if (!colliders[c].alive || !colliders[c].ccd || bodies[colliders[c].body].world != world) continue;
             interactions(c, nbr);
             for (uint32_t d : nbr) {
                 const uint32_t i = std::min(c, d), j = std::max(c, d);
@@ -2795,7 +2795,7 @@ public:
     // those in contact with them, moved back to the latest TOI, solved
     // (MoreauJeanSolver::step_ccd, moreau_jean_solver.rs:94-127) and
     // integrated over the rest of the step.
-    void ccd_substep(const std::vector<TOIEntry>& impacts, const std::vector<R>& frozen,
+    void ccd_substep(uint32_t world, const std::vector<TOIEntry>& impacts, const std::vector<R>& frozen,
                      const std::vector<char>& is_frozen) {
         const R dt0 = R(params.dt);
         const R last = impacts.back().toi;
@@ -2868,7 +2868,7 @@ public:
             integrate(b);
         }
         for (auto& b : bodies) {
-            if (!b.alive) continue;
+            if (!b.alive || b.world != world) continue;
             b.f_lin = b.f_ang = zero;
             update_dynamics(b, dts);
         }
@@ -2961,15 +2961,24 @@ public:
         return !r.some ? -1 : (r.penetrating ? 1 : 0);
     }
 
+    // Every world of a batch runs its own CCD loop (its own impacts, latest
+    // TOI and substep length), in world order.
     void solve_ccd() {
         const R dt0 = R(params.dt);
         if (dt0 == R(0) || params.max_ccd_substeps == 0) return;
-        bool any = false;
-        for (const auto& c : colliders) any = any || (c.alive && c.ccd);
-        if (!any) return;
+        std::vector<uint32_t> worlds;
+        for (const auto& c : colliders)
+            if (c.alive && c.ccd) worlds.push_back(bodies[c.body].world);
+        if (worlds.empty()) return;
+        std::sort(worlds.begin(), worlds.end());
+        worlds.erase(std::unique(worlds.begin(), worlds.end()), worlds.end());
         body_colliders.assign(bodies.size(), {});
         for (uint32_t c = 0; c < colliders.size(); ++c)
             if (colliders[c].alive) body_colliders[colliders[c].body].push_back(c);
+        for (uint32_t wd : worlds) solve_ccd_world(wd);
+    }
+    void solve_ccd_world(uint32_t world) {
+        const R dt0 = R(params.dt);
         const R sub = dt0 / R(params.max_ccd_substeps);
         ccd_time.assign(bodies.size(), R(0));
         R end_time = R(0);
@@ -2982,15 +2991,15 @@ public:
             else last_iter = true;
             ccd_sweep_boxes();
             R mo;
-            int pr = predict(end_time, impacts, frozen, is_frozen, mo);
+            int pr = predict(world, end_time, impacts, frozen, is_frozen, mo);
             if (pr == PRED_AFTER) {
                 end_time = std::floor(mo / sub) * sub;
                 end_time = std::min(end_time + sub, dt0);
-                pr = predict(end_time, impacts, frozen, is_frozen, mo);
+                pr = predict(world, end_time, impacts, frozen, is_frozen, mo);
                 if (pr != PRED_IMPACTS) impacts.clear();
             }
             if (!last_iter && !impacts.empty()) {
-                ccd_substep(impacts, frozen, is_frozen);
+                ccd_substep(world, impacts, frozen, is_frozen);
                 continue;
             }
             for (uint32_t h = 0; h < bodies.size(); ++h)

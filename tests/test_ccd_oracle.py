@@ -225,3 +225,24 @@ def test_f32_follows_f64():
     b, sb, ib = run(scenes.ccd_wall(n=4, gravity=(0, -9.81, 0)), 20, prec=64)
     assert (sa, ia) == (sb, ib)
     np.testing.assert_allclose(a.bodies()["position"][:, :3], b.bodies()["position"][:, :3], atol=1e-3)
+
+
+@pytest.mark.parametrize("prec", [32, 64])
+def test_distance_of_parallel_features(prec):
+    # Faces and axes parallel to a face: the configurations in which GJK's
+    # simplex turns flat (resting boxes, a capsule lying against a wall).
+    rng = np.random.default_rng(9)
+    for trial in range(20):
+        q = scenes.uniform_quaternions(rng, 1)[0].astype(np.float64)
+        R = qmat(q)
+        gap = rng.uniform(0.001, 0.05)
+        h = np.array([0.5, 0.3, 0.2])
+        # A cube resting on the first box's +x face, both rotated by q, shifted sideways.
+        side = rng.uniform(-0.2, 0.2, 2)
+        pos2 = R @ np.array([0.5 + 0.25 + gap, side[0], side[1]])
+        o = two(abi.SHAPE_CUBOID, h, (0, 0, 0), q, abi.SHAPE_CUBOID, (0.25, 0.25, 0.25), pos2, q, prec=prec)
+        assert o.collider_distance(0, 1)[0] == pytest.approx(gap, abs=2e-5 if prec == 32 else 1e-6), trial
+        # A capsule (axis along the box's y) lying against the same face.
+        pos3 = R @ np.array([0.5 + 0.1 + gap, side[0] * 0.5, side[1]])
+        o = two(abi.SHAPE_CUBOID, h, (0, 0, 0), q, abi.SHAPE_CAPSULE, (0.1, 0.2, 0.0), pos3, q, prec=prec)
+        assert o.collider_distance(0, 1)[0] == pytest.approx(gap, abs=2e-5 if prec == 32 else 1e-6), trial
