@@ -101,6 +101,8 @@ def parse():
                     help="velocity-solve row order: every friction row, then every normal row, each "
                          "iteration (separate: the reference's order), or each manifold's friction rows "
                          "then its normal rows in one sweep (manifold)")
+    ap.add_argument("--ccd", action="store_true",
+                    help="walls: the balls' colliders with continuous collision detection")
     args = ap.parse_args()
     if args.settle is None:
         args.settle = SETTLE[args.workload]
@@ -633,11 +635,12 @@ def build_workload(kind, args, rank, world_size):
                 "iterations")
     elif kind == "walls":
         # Each rank steps its own 256 walls (weak scaling).
-        sc = scenes.brick_walls(n_walls=256, seed=1234 + rank)
+        sc = scenes.brick_walls(n_walls=256, seed=1234 + rank, ccd=args.ccd)
         w = GpuWorld.for_scene(sc, _params(sc, args), pairs_per_collider=8)
         desc = ("brick walls: 256 walls per GPU of 50 x 40 bricks (half extents 0.5 x 0.25 x 0.25, running "
                 "bond), each struck by 64 balls of radius 0.4, density 10, at U(20, 40) m/s; friction 0.6, "
-                "dt 1/120, 8 velocity / 3 position iterations")
+                "dt 1/120, 8 velocity / 3 position iterations" +
+                ("; the balls' colliders with CCD (one substep a step at most)" if args.ccd else ""))
     else:
         # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
         n_all = args.worlds_per_rank * world_size

@@ -10,13 +10,15 @@
 // solve_ccd is sequential by nature (a priority queue of TOIs, bodies frozen
 // at their first impact, resweeps, an island grown through contacts, a
 // Gauss-Seidel solve in the reference's row order): thread 0 carries it, and
-// the block shares the data-parallel parts: the swept boxes, every neighbour
-// search over the world's colliders (an ordered compaction), every batch of
-// TOI queries, the island's contact rows and its integration. The
-// interactions of a collider during CCD are its broad-phase pairs (fat AABBs
-// overlapping) and, where either collider has CCD enabled, the pairs whose
-// boxes swept from the safe pose to the current one overlap; pairs are taken
-// in collider-slot order and TOIs of equal time in the order they were found.
+// the block shares the data-parallel parts: the swept boxes, the swept-box
+// neighbour searches (ordered compactions over the world's colliders), every
+// batch of TOI queries, the island's body preparation and contact updates,
+// its rows, its colour-ordered solves and its integration. The interactions
+// of a collider during CCD are its broad-phase pairs (fat AABBs overlapping,
+// read from the step's pair list) and, where either collider has CCD
+// enabled, the pairs whose boxes swept from the safe pose to the current one
+// overlap; pairs are taken in collider-slot order and TOIs of equal time in
+// the order they were found.
 
 constexpr int kCcdThreads = 128;
 constexpr uint32_t kTocPopped = 1u << 30, kTocSuperseded = 1u << 31, kTocSeq = kTocPopped - 1u;
@@ -64,20 +66,6 @@ __device__ __forceinline__ void ccd_sweep_box(const World& w, uint32_t c) {
     ccd_aabb(w, c, np::Iso{v3(w.b.pos_t[b]), q4(w.b.pos_q[b])}, a1, b1);
     w.ccd.sw_min[c] = make_float4(np_min(a0[0], a1[0]), np_min(a0[1], a1[1]), np_min(a0[2], a1[2]), 0.0f);
     w.ccd.sw_max[c] = make_float4(np_max(b0[0], b1[0]), np_max(b0[1], b1[1]), np_max(b0[2], b1[2]), 0.0f);
-}
-
-// Whether colliders c and d interact during CCD (c != d, both alive).
-__device__ __forceinline__ bool ccd_interacts(const World& w, uint32_t c, uint32_t d) {
-    if (d == c || !(w.c.info[d] & CI_ALIVE)) return false;
-    const uint32_t bc = ccd_body_of(w, c), bd = ccd_body_of(w, d);
-    if (bc == bd || w.b.world[bc] != w.b.world[bd]) return false;
-    if (!ccd_dynamic(w, bc) && !ccd_dynamic(w, bd)) return false;
-    const float4 amn = w.c.aabb_min[c], amx = w.c.aabb_max[c], bmn = w.c.aabb_min[d], bmx = w.c.aabb_max[d];
-    if (amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z && bmn.z <= amx.z)
-        return true;
-    if (!ccd_enabled(w, c) && !ccd_enabled(w, d)) return false;
-    const float4 smn = w.ccd.sw_min[c], smx = w.ccd.sw_max[c], tmn = w.ccd.sw_min[d], tmx = w.ccd.sw_max[d];
-    return smn.x <= tmx.x && tmn.x <= smx.x && smn.y <= tmx.y && tmn.y <= smx.y && smn.z <= tmx.z && tmn.z <= smx.z;
 }
 
 // Appends to out (up to cap) the colliders d of the world's segment
@@ -240,7 +228,6 @@ __device__ void ccd_prepare(const World& w, const StepParams& p0, uint32_t h, fl
     w.ccd.pos0_q[h] = f4q(p0s.q);
     ccd_clamp(w, h);
     w.ccd.btime[h] = last;
-    w.ccd.bflag[h] |= 2u;
 }
 
 // The island's rows of one manifold (built in parallel after the island is
@@ -346,101 +333,138 @@ __device__ void ccd_position_contact(const World& w, const StepParams& p, const 
     }
 }
 
-// SORProx over the island in the reference's order (sor_prox.rs:48-80,
-// 159-179): each iteration the friction rows of the non-ground manifolds and
-// then the ground ones, then the normal rows likewise. Δv in Bodies::dv.
-__device__ void ccd_velocity_solve(const World& w, const StepParams& p, const uint32_t* mlist, uint32_t nm) {
+// One pass of an island manifold's rows (SORProx, sor_prox.rs:181-343):
+// its friction rows (friction true) or its normal rows. Δv in Bodies::dv; two
+// manifolds of one colour share no dynamic body, so a colour's manifolds run
+// in parallel.
+__device__ void ccd_manifold_velocity(const World& w, CcdManifold& m, bool friction) {
     const Bodies& b = w.b;
-    auto load = [&](int slot, float* v) {
-        if (slot < 0) return;
-        for (int k = 0; k < 6; ++k) v[k] = b.dv[6 * (size_t)slot + k];
-    };
-    auto store = [&](int slot, const float* v) {
-        if (slot < 0) return;
-        for (int k = 0; k < 6; ++k) b.dv[6 * (size_t)slot + k] = v[k];
-    };
-    auto masses = [&](const CcdManifold& m) {
-        BodyMasses bm;
-        const int sl[2] = {m.b1, m.b2};
-        for (int s = 0; s < 2; ++s) {
-            if (sl[s] < 0) continue;
-            bm.s[s].im = b.inv_mass[sl[s]];
-            bm.s[s].I = load_m9(b.inv_I + 9 * (size_t)sl[s]);
-        }
-        return bm;
-    };
-    for (uint32_t it = 0; it < p.max_velocity_iterations; ++it) {
-        for (int pass = 0; pass < 4; ++pass) {
-            const bool friction = pass < 2, ground = (pass & 1) != 0;
-            for (uint32_t q = 0; q < nm; ++q) {
-                CcdManifold& m = w.ccd.pool[mlist[q]];
-                if (((m.b1 < 0) || (m.b2 < 0)) != ground) continue;
-                const bool h1 = m.b1 >= 0, h2 = m.b2 >= 0;
-                const BodyMasses bm = masses(m);
-                DV dv;
-                load(m.b1, dv.a);
-                load(m.b2, dv.b);
-                for (uint32_t k = 0; k < m.nc; ++k) {
-                    CcdContact& K = m.k[k];
-                    const np::V pos1 = v3(K.pos1), pos2 = v3(K.pos2);
-                    float4 l = K.lam;
-                    if (friction) {
-                        const np::V t[2] = {v3(K.t1), v3(K.t2)};
-                        const float rr[2] = {K.rr.x, K.rr.z}, rh[2] = {K.rr.y, K.rr.w};
-                        float imps[2] = {l.y, l.z};
-                        const float li = l.x;
-                        for (int s = 0; s < 2; ++s) {
-                            const float imp = imps[s];
-                            if (li == 0.0f) {
-                                if (imp != 0.0f) {
-                                    axpy(t[s], pos1, pos2, m.mask, bm, dv, -imp, h1, h2);
-                                    imps[s] = 0.0f;
-                                }
-                                continue;
-                            }
-                            const float mx = m.mu * li, mn = -mx;
-                            const float dimp = jdot(t[s], pos1, pos2, m.mask, dv, h1, h2) + rh[s];
-                            float ni = imp - rr[s] * dimp;
-                            if (ni < mn) ni = mn;
-                            else if (ni > mx) ni = mx;
-                            const float dl = ni - imp;
-                            imps[s] = ni;
-                            axpy(t[s], pos1, pos2, m.mask, bm, dv, dl, h1, h2);
-                        }
-                        K.lam = make_float4(li, imps[0], imps[1], 0.0f);
-                    } else {
-                        const np::V dn = np::neg(v3(K.n));
-                        const float imp = l.x;
-                        const float dimp = jdot(dn, pos1, pos2, m.mask, dv, h1, h2) + K.pos2.w;
-                        float ni = imp - K.pos1.w * dimp;
-                        ni = ni > 0.0f ? ni : 0.0f;
-                        const float dl = ni - imp;
-                        K.lam = make_float4(ni, l.y, l.z, 0.0f);
-                        axpy(dn, pos1, pos2, m.mask, bm, dv, dl, h1, h2);
+    const bool h1 = m.b1 >= 0, h2 = m.b2 >= 0;
+    BodyMasses bm;
+    const int sl[2] = {m.b1, m.b2};
+    for (int s = 0; s < 2; ++s) {
+        if (sl[s] < 0) continue;
+        bm.s[s].im = b.inv_mass[sl[s]];
+        bm.s[s].I = load_m9(b.inv_I + 9 * (size_t)sl[s]);
+    }
+    DV dv;
+    for (int k = 0; k < 6; ++k) {
+        if (h1) dv.a[k] = b.dv[6 * (size_t)m.b1 + k];
+        if (h2) dv.b[k] = b.dv[6 * (size_t)m.b2 + k];
+    }
+    for (uint32_t k = 0; k < m.nc; ++k) {
+        CcdContact& K = m.k[k];
+        const np::V pos1 = v3(K.pos1), pos2 = v3(K.pos2);
+        const float4 l = K.lam;
+        if (friction) {
+            const np::V t[2] = {v3(K.t1), v3(K.t2)};
+            const float rr[2] = {K.rr.x, K.rr.z}, rh[2] = {K.rr.y, K.rr.w};
+            float imps[2] = {l.y, l.z};
+            const float li = l.x;
+            for (int s = 0; s < 2; ++s) {
+                const float imp = imps[s];
+                if (li == 0.0f) {
+                    if (imp != 0.0f) {
+                        axpy(t[s], pos1, pos2, m.mask, bm, dv, -imp, h1, h2);
+                        imps[s] = 0.0f;
                     }
+                    continue;
                 }
-                store(m.b1, dv.a);
-                store(m.b2, dv.b);
+                const float mx = m.mu * li, mn = -mx;
+                const float dimp = jdot(t[s], pos1, pos2, m.mask, dv, h1, h2) + rh[s];
+                float ni = imp - rr[s] * dimp;
+                if (ni < mn) ni = mn;
+                else if (ni > mx) ni = mx;
+                const float dl = ni - imp;
+                imps[s] = ni;
+                axpy(t[s], pos1, pos2, m.mask, bm, dv, dl, h1, h2);
             }
+            K.lam = make_float4(li, imps[0], imps[1], 0.0f);
+        } else {
+            const np::V dn = np::neg(v3(K.n));
+            const float imp = l.x;
+            const float dimp = jdot(dn, pos1, pos2, m.mask, dv, h1, h2) + K.pos2.w;
+            float ni = imp - K.pos1.w * dimp;
+            ni = ni > 0.0f ? ni : 0.0f;
+            const float dl = ni - imp;
+            K.lam = make_float4(ni, l.y, l.z, 0.0f);
+            axpy(dn, pos1, pos2, m.mask, bm, dv, dl, h1, h2);
         }
+    }
+    for (int k = 0; k < 6; ++k) {
+        if (h1) b.dv[6 * (size_t)m.b1 + k] = dv.a[k];
+        if (h2) b.dv[6 * (size_t)m.b2 + k] = dv.b[k];
     }
 }
 
 // Shared state of a world's CCD loop.
+constexpr uint32_t kCcdColours = 64;
 struct CcdState {
     float end_time, min_overstep, last;
     uint32_t last_iter, result, nheap, nimp, seq, nstack, nisland, nccdb, nm;
-    uint32_t cur, n, stop;
+    uint32_t cur, n, stop, epoch, ncol;
     uint32_t cnt[kCcdThreads / 32];
+    uint32_t col_start[kCcdColours + 1];
 };
+
+// The colliders interacting with c during CCD, in slot order, into nbr
+// (tmp: scratch of the same size); returns their count (block-uniform; above
+// cap when they do not fit). The broad-phase partners come from the step's
+// pair list; the swept-box partners (not already there) from the world's
+// colliders when c has CCD enabled, else from the world's CCD colliders.
+__device__ uint32_t ccd_neighbours(const World& w, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t c, uint32_t* nbr,
+                                   uint32_t* tmp, uint32_t cap, CcdState& st) {
+    const Ccd& cd = w.ccd;
+    const uint32_t bc = ccd_body_of(w, c);
+    auto swept = [&](uint32_t d) {
+        if (d == c || !(w.c.info[d] & CI_ALIVE)) return false;
+        const uint32_t bd = ccd_body_of(w, d);
+        if (bc == bd || w.b.world[bc] != w.b.world[bd]) return false;
+        if (!ccd_dynamic(w, bc) && !ccd_dynamic(w, bd)) return false;
+        if (!ccd_enabled(w, c) && !ccd_enabled(w, d)) return false;
+        const float4 amn = w.c.aabb_min[c], amx = w.c.aabb_max[c], bmn = w.c.aabb_min[d], bmx = w.c.aabb_max[d];
+        if (amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z && bmn.z <= amx.z)
+            return false;   // a broad-phase pair, listed already
+        const float4 smn = cd.sw_min[c], smx = cd.sw_max[c], tmn = cd.sw_min[d], tmx = cd.sw_max[d];
+        return smn.x <= tmx.x && tmn.x <= smx.x && smn.y <= tmx.y && tmn.y <= smx.y && smn.z <= tmx.z && tmn.z <= smx.z;
+    };
+    const uint32_t ns = ccd_enabled(w, c)
+                            ? block_collect(cd.order, ws, wn, swept, tmp, cap, st.cnt)
+                            : block_collect(cd.ccd_list, cd.ccd_wstart[wd], cd.ccd_wstart[wd + 1] - cd.ccd_wstart[wd],
+                                            swept, tmp, cap, st.cnt);
+    if (threadIdx.x == 0) {
+        const uint32_t a0 = cd.adj_start[c], a1 = cd.adj_start[c + 1];
+        uint32_t n = 0;
+        if (ns > cap || (a1 - a0) + ns > cap) {
+            n = cap + 1u;
+        } else {
+            uint32_t i = a0, j = 0;
+            while (i < a1 || j < ns) {
+                const uint32_t x = i < a1 ? cd.adj_list[i] : 0xffffffffu, y = j < ns ? tmp[j] : 0xffffffffu;
+                if (x < y) {
+                    nbr[n++] = x;
+                    ++i;
+                } else {
+                    nbr[n++] = y;
+                    ++j;
+                }
+            }
+        }
+        st.n = n;
+    }
+    __syncthreads();
+    const uint32_t n = st.n;
+    __syncthreads();
+    return n;
+}
 enum : uint32_t { PRED_NONE = 0, PRED_IMPACTS = 1, PRED_AFTER = 2 };
 
 // predict_next_impacts for the world: the impacts up to end_time in time
 // order (st.nimp in `imp`), bodies frozen at their first impact (bflag bit 0,
 // ftime), or PRED_NONE / PRED_AFTER with the smallest TOI beyond end_time in
 // st.min_overstep.
-__device__ void ccd_predict(const World& w, const StepParams& p, uint32_t ws, uint32_t wn, uint32_t rb, uint32_t rcap,
-                            CcdState& st) {
+__device__ void ccd_predict(const World& w, const StepParams& p, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t rb,
+                            uint32_t rcap, CcdState& st) {
     const Ccd& cd = w.ccd;
     uint32_t* nbr = cd.nbr + rb;
     float2* tres = cd.tres + rb;
@@ -457,8 +481,7 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t ws, ui
     for (uint32_t i = 0; i < wn; ++i) {
         const uint32_t c = cd.order[ws + i];
         if (!ccd_enabled(w, c)) continue;
-        const uint32_t n = block_collect(cd.order, ws, wn, [&](uint32_t d) { return ccd_interacts(w, c, d); }, nbr,
-                                         rcap, st.cnt);
+        const uint32_t n = ccd_neighbours(w, wd, ws, wn, c, nbr, cd.nbr2 + rb, rcap, st);
         if (n > rcap) {
             if (threadIdx.x == 0) st.stop = 1;
             break;
@@ -544,8 +567,7 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t ws, ui
             if (!ccd_dynamic(w, fb)) continue;
             for (uint32_t q = cd.bc_start[fb]; q < cd.bc_start[fb + 1]; ++q) {
                 const uint32_t cc = cd.bc_list[q];
-                const uint32_t n = block_collect(cd.order, ws, wn, [&](uint32_t d) { return ccd_interacts(w, cc, d); },
-                                                 nbr, rcap, st.cnt);
+                const uint32_t n = ccd_neighbours(w, wd, ws, wn, cc, nbr, cd.nbr2 + rb, rcap, st);
                 if (n > rcap) {
                     if (threadIdx.x == 0) st.stop = 1;
                     break;
@@ -595,7 +617,14 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t ws, ui
 // One substep (mechanical_world.rs:624-889): the island grown from the
 // impacting bodies through contacts, moved back to the latest TOI, solved
 // (MoreauJeanSolver::step_ccd, moreau_jean_solver.rs:94-127) and integrated
-// over the rest of the step.
+// over the rest of the step. The island search keeps the reference's order
+// (a stack of colliders; each popped collider's pairs with unvisited ones in
+// slot order, the bodies prepared on first sight, a pair with contacts
+// extending the island to the colliders of a body it prepared); the block
+// prepares the bodies and updates the pairs of a popped collider together,
+// and thread 0 replays the order. The island's manifolds are then solved in
+// colour order: a greedy colouring over their dynamic bodies in the order
+// they were found.
 __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t rb,
                             uint32_t rcap, CcdState& st) {
     const Ccd& cd = w.ccd;
@@ -604,6 +633,8 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     uint32_t* island = cd.island + rb;
     uint32_t* ccdb = cd.ccdb + rb;
     uint32_t* mlist = cd.mlist + rb;
+    uint32_t* mord = cd.mord + rb;
+    uint2* res = cd.res + rb;
     const CcdToi* imp = cd.impacts + rb;
     for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) {
         const uint32_t c = cd.order[ws + i];
@@ -630,9 +661,6 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         }
     }
     __syncthreads();
-    // The island: colliders popped from the stack, each pair of a popped
-    // collider with an unvisited one updated, the bodies prepared on first
-    // sight, a pair with contacts extending the island to its other body.
     StepParams ps = p;
     ps.dt = dts;
     ps.inv_dt = dts == 0.0f ? 0.0f : 1.0f / dts;
@@ -652,46 +680,74 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         const uint32_t c = st.cur;
         __syncthreads();
         if (c == 0xffffffffu) break;
-        const uint32_t n = block_collect(cd.order, ws, wn, [&](uint32_t d) { return ccd_interacts(w, c, d); }, nbr,
-                                         rcap, st.cnt);
+        const uint32_t n = ccd_neighbours(w, wd, ws, wn, c, nbr, cd.nbr2 + rb, rcap, st);
+        if (n > rcap) {
+            if (threadIdx.x == 0) st.stop = 1;
+            break;
+        }
+        // Which bodies were prepared before this collider's pairs.
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            const uint32_t d = nbr[j];
+            if (cd.cflag[d] & 1u) {
+                res[j] = make_uint2(0xffffffffu, 0xffffffffu);
+                continue;
+            }
+            const uint32_t x1 = ccd_body_of(w, c < d ? c : d), x2 = ccd_body_of(w, c < d ? d : c);
+            res[j] = make_uint2(((cd.bflag[x1] >> 1) & 1u) | (((cd.bflag[x2] >> 1) & 1u) << 1), 0xffffffffu);
+        }
+        __syncthreads();
+        // Every body of these pairs prepared once.
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            if (res[j].x == 0xffffffffu) continue;
+            const uint32_t d = nbr[j];
+            const uint32_t xs[2] = {ccd_body_of(w, c < d ? c : d), ccd_body_of(w, c < d ? d : c)};
+            for (int s = 0; s < 2; ++s) {
+                if (!ccd_dynamic(w, xs[s]) || (atomicOr(&cd.bflag[xs[s]], 2u) & 2u)) continue;
+                ccd_prepare(w, p, xs[s], dts, last);
+                const uint32_t at = atomicAdd(&st.nisland, 1u);
+                if (at < rcap) island[at] = xs[s];
+            }
+        }
+        __syncthreads();
+        // The pairs' contacts at the prepared poses, into the pool.
+        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+            if (res[j].x == 0xffffffffu) continue;
+            const uint32_t d = nbr[j];
+            CcdManifold mf;
+            if (ccd_contacts(w, c < d ? c : d, c < d ? d : c, mf) == 0u) continue;
+            const uint32_t slot = atomicAdd(&w.ctl->ccd_mcount, 1u);
+            if (slot >= cd.pool_cap) {
+                st.stop = 1;
+                continue;
+            }
+            cd.pool[slot] = mf;
+            res[j].y = slot;
+        }
+        __syncthreads();
+        // The reference's order: found manifolds, and the colliders of bodies
+        // a pair with contacts prepared.
         if (threadIdx.x == 0) {
-            if (n > rcap) st.stop = 1;
+            const uint32_t epoch = ++st.epoch;
             for (uint32_t j = 0; j < n && !st.stop; ++j) {
+                const uint2 r = res[j];
+                if (r.x == 0xffffffffu) continue;
                 const uint32_t d = nbr[j];
-                if (cd.cflag[d] & 1u) continue;
                 const uint32_t ch1 = c < d ? c : d, ch2 = c < d ? d : c;
-                const uint32_t x1 = ccd_body_of(w, ch1), x2 = ccd_body_of(w, ch2);
-                const bool p1 = !(cd.bflag[x1] & 2u) && ccd_dynamic(w, x1);
-                if (p1) {
-                    if (st.nisland >= rcap) {
-                        st.stop = 1;
-                        break;
-                    }
-                    ccd_prepare(w, p, x1, dts, last);
-                    island[st.nisland++] = x1;
+                const uint32_t xs[2] = {ccd_body_of(w, ch1), ccd_body_of(w, ch2)};
+                bool prep[2];
+                for (int s = 0; s < 2; ++s) {
+                    prep[s] = !((r.x >> s) & 1u) && ccd_dynamic(w, xs[s]) && cd.bepoch[xs[s]] != epoch;
+                    cd.bepoch[xs[s]] = epoch;
                 }
-                const bool p2 = !(cd.bflag[x2] & 2u) && ccd_dynamic(w, x2);
-                if (p2) {
-                    if (st.nisland >= rcap) {
-                        st.stop = 1;
-                        break;
-                    }
-                    ccd_prepare(w, p, x2, dts, last);
-                    island[st.nisland++] = x2;
-                }
-                CcdManifold mf;
-                if (ccd_contacts(w, ch1, ch2, mf) == 0u) continue;
-                const uint32_t slot = st.nm < rcap ? atomicAdd(&w.ctl->ccd_mcount, 1u) : 0xffffffffu;
-                if (slot >= cd.pool_cap) {
+                if (r.y == 0xffffffffu) continue;
+                if (st.nm >= rcap) {
                     st.stop = 1;
                     break;
                 }
-                cd.pool[slot] = mf;
-                mlist[st.nm++] = slot;
-                const uint32_t xs[2] = {x1, x2};
-                const bool pr[2] = {ch1 != c && p1, ch2 != c && p2};
+                mlist[st.nm++] = r.y;
+                const bool push[2] = {ch1 != c && prep[0], ch2 != c && prep[1]};
                 for (int s = 0; s < 2; ++s) {
-                    if (!pr[s]) continue;
+                    if (!push[s]) continue;
                     for (uint32_t q = cd.bc_start[xs[s]]; q < cd.bc_start[xs[s] + 1]; ++q) {
                         if (st.nstack >= rcap) st.stop = 1;
                         else stack[st.nstack++] = cd.bc_list[q];
@@ -699,9 +755,41 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
                 }
             }
             cd.cflag[c] |= 1u;
+            if (st.nisland > rcap) st.stop = 1;
         }
         __syncthreads();
     }
+    // The island's colours, in found order.
+    for (uint32_t i = threadIdx.x; i < st.nisland && i < rcap; i += blockDim.x) cd.bcol[island[i]] = 0ull;
+    __syncthreads();
+    if (threadIdx.x == 0 && !st.stop) {
+        uint32_t count[kCcdColours];
+        for (uint32_t k = 0; k < kCcdColours; ++k) count[k] = 0;
+        uint32_t ncol = 0;
+        for (uint32_t q = 0; q < st.nm && !st.stop; ++q) {
+            CcdManifold& m = cd.pool[mlist[q]];
+            const uint32_t x1 = ccd_body_of(w, m.c1), x2 = ccd_body_of(w, m.c2);
+            const bool d1 = ccd_dynamic(w, x1), d2 = ccd_dynamic(w, x2);
+            const unsigned long long taken = (d1 ? cd.bcol[x1] : 0ull) | (d2 ? cd.bcol[x2] : 0ull);
+            if (taken == ~0ull) {
+                st.stop = 1;
+                break;
+            }
+            const uint32_t k = (uint32_t)__ffsll((long long)~taken) - 1u;
+            if (d1) cd.bcol[x1] |= 1ull << k;
+            if (d2) cd.bcol[x2] |= 1ull << k;
+            m.colour = k;
+            count[k] += 1;
+            ncol = ncol > k + 1 ? ncol : k + 1;
+        }
+        st.col_start[0] = 0;
+        for (uint32_t k = 0; k < kCcdColours; ++k) st.col_start[k + 1] = st.col_start[k] + count[k];
+        uint32_t cur[kCcdColours];
+        for (uint32_t k = 0; k < kCcdColours; ++k) cur[k] = st.col_start[k];
+        for (uint32_t q = 0; q < st.nm && !st.stop; ++q) mord[cur[cd.pool[mlist[q]].colour]++] = mlist[q];
+        st.ncol = ncol;
+    }
+    __syncthreads();
     if (st.stop) {
         if (threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_CCD_CAPACITY);
         __syncthreads();
@@ -709,25 +797,33 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     }
     // step_ccd: the rows, the position solve, validate_advancement of the
     // impacting bodies, the velocity solve and the island's integration.
-    for (uint32_t q = threadIdx.x; q < st.nm; q += blockDim.x) ccd_rows(w, ps, cd.pool[mlist[q]], dts);
-    for (uint32_t i = threadIdx.x; i < st.nisland; i += blockDim.x)
+    const uint32_t nm = st.nm, ncol = st.ncol, nisl = st.nisland;
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) ccd_rows(w, ps, cd.pool[mlist[q]], dts);
+    for (uint32_t i = threadIdx.x; i < nisl; i += blockDim.x)
         for (int k = 0; k < 6; ++k) w.b.dv[6 * (size_t)island[i] + k] = 0.0f;
     __syncthreads();
-    if (threadIdx.x == 0) {
-        for (uint32_t it = 0; it < cd.max_position_iterations; ++it)
-            for (uint32_t q = 0; q < st.nm; ++q) {
-                const CcdManifold& m = cd.pool[mlist[q]];
-                for (uint32_t k = 0; k < m.nc; ++k) ccd_position_contact(w, ps, m, m.k[k]);
+    for (uint32_t it = 0; it < cd.max_position_iterations; ++it)
+        for (uint32_t k = 0; k < ncol; ++k) {
+            for (uint32_t q = st.col_start[k] + threadIdx.x; q < st.col_start[k + 1]; q += blockDim.x) {
+                const CcdManifold& m = cd.pool[mord[q]];
+                for (uint32_t kk = 0; kk < m.nc; ++kk) ccd_position_contact(w, ps, m, m.k[kk]);
             }
-        for (uint32_t k = 0; k < st.nccdb; ++k) {
-            const uint32_t h = ccdb[k];
-            cd.pos0_t[h] = w.b.pos_t[h];
-            cd.pos0_q[h] = w.b.pos_q[h];
+            __syncthreads();
         }
-        ccd_velocity_solve(w, ps, mlist, st.nm);
+    for (uint32_t k = threadIdx.x; k < st.nccdb; k += blockDim.x) {
+        const uint32_t h = ccdb[k];
+        cd.pos0_t[h] = w.b.pos_t[h];
+        cd.pos0_q[h] = w.b.pos_q[h];
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < st.nisland; i += blockDim.x) {
+    for (uint32_t it = 0; it < p.max_velocity_iterations; ++it)
+        for (int pass = 0; pass < 2; ++pass)
+            for (uint32_t k = 0; k < ncol; ++k) {
+                for (uint32_t q = st.col_start[k] + threadIdx.x; q < st.col_start[k + 1]; q += blockDim.x)
+                    ccd_manifold_velocity(w, cd.pool[mord[q]], pass == 0);
+                __syncthreads();
+            }
+    for (uint32_t i = threadIdx.x; i < nisl; i += blockDim.x) {
         const uint32_t h = island[i];
         const Bodies& b = w.b;
         const np::V el = np::mul(v3(b.acc_lin[h]), dts), ea = np::mul(v3(b.acc_ang[h]), dts);
@@ -770,7 +866,9 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p
     if (threadIdx.x == 0) {
         st.end_time = 0.0f;
         st.last_iter = 0;
+        st.epoch = 0;
     }
+    for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) cd.bepoch[ccd_body_of(w, cd.order[ws + i])] = 0u;
     __syncthreads();
     // At most max_ccd_substeps + 1 passes: each either advances end_time by
     // a substep or is the last.
@@ -785,14 +883,14 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p
         }
         for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) ccd_sweep_box(w, cd.order[ws + i]);
         __syncthreads();
-        ccd_predict(w, p, ws, wn, rb, rcap, st);
+        ccd_predict(w, p, wd, ws, wn, rb, rcap, st);
         if (st.result == PRED_AFTER) {
             if (threadIdx.x == 0) {
                 const float e = floorf(st.min_overstep / sub) * sub + sub;
                 st.end_time = e < dt0 ? e : dt0;
             }
             __syncthreads();
-            ccd_predict(w, p, ws, wn, rb, rcap, st);
+            ccd_predict(w, p, wd, ws, wn, rb, rcap, st);
             if (threadIdx.x == 0 && st.result != PRED_IMPACTS) st.nimp = 0;
             __syncthreads();
         } else if (st.result == PRED_NONE) {
@@ -810,6 +908,41 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p
             if ((cd.bflag[b] & 1u) && bi_status(w.b.info[b]) != 1u) ccd_clamp(w, b);
         }
         break;
+    }
+}
+
+// The step's broad-phase pairs by collider (both ends), partners in slot
+// order: counts, then (after an exclusive scan of the counts into adj_start)
+// the lists, then each list sorted.
+__global__ void k_ccd_adj_count(World w) {
+    const uint32_t np_ = w.ctl->npairs < w.cap_pairs ? w.ctl->npairs : w.cap_pairs;
+    GRID_FOR(q, np_) {
+        const uint2 pr = w.cur.pair[q];
+        atomicAdd(&w.ccd.adj_count[pr.x], 1u);
+        atomicAdd(&w.ccd.adj_count[pr.y], 1u);
+    }
+}
+__global__ void k_ccd_adj_fill(World w) {
+    const uint32_t np_ = w.ctl->npairs < w.cap_pairs ? w.ctl->npairs : w.cap_pairs;
+    GRID_FOR(q, np_) {
+        const uint2 pr = w.cur.pair[q];
+        w.ccd.adj_list[w.ccd.adj_start[pr.x] + atomicAdd(&w.ccd.adj_count[pr.x], 1u)] = pr.y;
+        w.ccd.adj_list[w.ccd.adj_start[pr.y] + atomicAdd(&w.ccd.adj_count[pr.y], 1u)] = pr.x;
+    }
+}
+__global__ void k_ccd_adj_sort(World w) {
+    GRID_FOR(c, w.nc_slots) {
+        uint32_t* l = w.ccd.adj_list + w.ccd.adj_start[c];
+        const uint32_t n = w.ccd.adj_start[c + 1] - w.ccd.adj_start[c];
+        for (uint32_t i = 1; i < n; ++i) {
+            const uint32_t x = l[i];
+            uint32_t j = i;
+            while (j > 0 && l[j - 1] > x) {
+                l[j] = l[j - 1];
+                --j;
+            }
+            l[j] = x;
+        }
     }
 }
 

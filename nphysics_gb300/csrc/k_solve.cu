@@ -3210,6 +3210,17 @@ cudaError_t launch_ccd_begin(const World& w, cudaStream_t st) {
 
 cudaError_t launch_ccd(const World& w, const StepParams& p, cudaStream_t st) {
     if (!p.ccd || w.ccd.n_worlds == 0) return cudaSuccess;
+    const uint32_t nc = w.nc_slots;
+    cudaError_t e = cudaMemsetAsync(w.ccd.adj_count, 0, sizeof(uint32_t) * (nc + 1), st);
+    if (e != cudaSuccess) return e;
+    k_ccd_adj_count<<<item_blocks(w.cap_pairs), kItemThreads, 0, st>>>(w);
+    size_t bytes = w.ccd.adj_scan_bytes;
+    e = exclusive_scan(w.ccd.adj_scan, bytes, w.ccd.adj_count, w.ccd.adj_start, nc + 1, st);
+    if (e != cudaSuccess) return e;
+    e = cudaMemsetAsync(w.ccd.adj_count, 0, sizeof(uint32_t) * (nc + 1), st);
+    if (e != cudaSuccess) return e;
+    k_ccd_adj_fill<<<item_blocks(w.cap_pairs), kItemThreads, 0, st>>>(w);
+    k_ccd_adj_sort<<<item_blocks(nc), kItemThreads, 0, st>>>(w);
     k_ccd_world<<<w.ccd.n_worlds, kCcdThreads, 0, st>>>(w, p);
     k_ccd_finish<<<item_blocks(w.nb_slots), kItemThreads, 0, st>>>(w);
     return cudaGetLastError();

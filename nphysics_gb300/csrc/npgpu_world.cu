@@ -213,7 +213,7 @@ struct npgpu_world {
     bool last_step_ccd = false;
     size_t ccd_region = 0, ccd_worlds_cap = 0, ccd_bodies_cap = 0, ccd_colliders_cap = 0;
     std::vector<void*> ccd_fixed, ccd_grown;
-    std::vector<uint32_t> h_ccd_order, h_ccd_wstart, h_ccd_wflag, h_bc_start, h_bc_list;
+    std::vector<uint32_t> h_ccd_order, h_ccd_wstart, h_ccd_wflag, h_bc_start, h_bc_list, h_ccd_list, h_ccd_lstart;
 };
 
 // The message of the last failure without a world (npgpu_create, the
@@ -1327,6 +1327,14 @@ static npgpu_status ccd_layout(npgpu_world* w) {
         if (w->hc[by_world[i].second].desc.ccd_enabled) w->h_ccd_wflag[by_world[i].first] = 1u;
     }
     for (uint32_t k = 0; k < nw; ++k) w->h_ccd_wstart[k + 1] += w->h_ccd_wstart[k];
+    w->h_ccd_list.clear();
+    w->h_ccd_lstart.assign(nw + 1, 0u);
+    for (uint32_t i = 0; i < n; ++i)
+        if (w->hc[by_world[i].second].desc.ccd_enabled) {
+            w->h_ccd_list.push_back(by_world[i].second);
+            w->h_ccd_lstart[by_world[i].first + 1] += 1;
+        }
+    for (uint32_t k = 0; k < nw; ++k) w->h_ccd_lstart[k + 1] += w->h_ccd_lstart[k];
     w->h_bc_start.assign(w->nb_slots + 1, 0u);
     for (uint32_t ci = 0; ci < w->nc_slots; ++ci)
         if (w->hc[ci].alive) w->h_bc_start[w->hc[ci].desc.body.index + 1] += 1;
@@ -1362,7 +1370,17 @@ static npgpu_status ccd_layout(npgpu_world* w) {
         alloc(w->ccd_fixed, (void**)&cd.cflag, sizeof(uint32_t) * C);
         alloc(w->ccd_fixed, (void**)&cd.order, sizeof(uint32_t) * C);
         alloc(w->ccd_fixed, (void**)&cd.bc_list, sizeof(uint32_t) * C);
-        cd.pool_cap = (uint32_t)std::min<size_t>(std::max<size_t>(4096, C), 65536);
+        alloc(w->ccd_fixed, (void**)&cd.ccd_list, sizeof(uint32_t) * C);
+        alloc(w->ccd_fixed, (void**)&cd.adj_count, sizeof(uint32_t) * (C + 1));
+        alloc(w->ccd_fixed, (void**)&cd.adj_start, sizeof(uint32_t) * (C + 1));
+        alloc(w->ccd_fixed, (void**)&cd.adj_list, sizeof(uint32_t) * 2 * (size_t)w->cap_p);
+        cd.adj_scan_bytes = scan_temp_bytes((uint32_t)C + 1u);
+        alloc(w->ccd_fixed, (void**)&cd.adj_scan, cd.adj_scan_bytes);
+        alloc(w->ccd_fixed, (void**)&cd.bepoch, sizeof(uint32_t) * B);
+        alloc(w->ccd_fixed, (void**)&cd.bcol, sizeof(unsigned long long) * B);
+        // The substeps' island manifolds: up to four a collider (a wall of
+        // bricks has about three contact pairs a brick), 2^24 at most.
+        cd.pool_cap = (uint32_t)std::min<size_t>(std::max<size_t>(4096, 4 * C), (size_t)1 << 24);
         alloc(w->ccd_fixed, (void**)&cd.pool, sizeof(CcdManifold) * cd.pool_cap);
         if (!ok) return fail(w, NPGPU_ERR_CUDA, "CCD arrays: cudaMalloc failed");
         CK(cudaMemsetAsync(cd.bflag, 0, sizeof(uint32_t) * B, w->stream), "CCD arrays");
@@ -1378,9 +1396,13 @@ static npgpu_status ccd_layout(npgpu_world* w) {
         w->ccd_grown.clear();
         const size_t W = std::max<size_t>(nw, 2 * w->ccd_worlds_cap), R = std::max<size_t>(region, 2 * w->ccd_region);
         alloc(w->ccd_grown, (void**)&cd.wstart, sizeof(uint32_t) * (W + 1));
+        alloc(w->ccd_grown, (void**)&cd.ccd_wstart, sizeof(uint32_t) * (W + 1));
         alloc(w->ccd_grown, (void**)&cd.wflag, sizeof(uint32_t) * W);
         alloc(w->ccd_grown, (void**)&cd.wdts, sizeof(float) * W);
         alloc(w->ccd_grown, (void**)&cd.nbr, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.nbr2, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.mord, sizeof(uint32_t) * R);
+        alloc(w->ccd_grown, (void**)&cd.res, sizeof(uint2) * R);
         alloc(w->ccd_grown, (void**)&cd.stack, sizeof(uint32_t) * R);
         alloc(w->ccd_grown, (void**)&cd.island, sizeof(uint32_t) * R);
         alloc(w->ccd_grown, (void**)&cd.ccdb, sizeof(uint32_t) * R);
@@ -1401,6 +1423,11 @@ static npgpu_status ccd_layout(npgpu_world* w) {
                        w->stream), "CCD layout");
     CK(cudaMemcpyAsync(cd.wflag, w->h_ccd_wflag.data(), sizeof(uint32_t) * nw, cudaMemcpyHostToDevice, w->stream),
        "CCD layout");
+    if (!w->h_ccd_list.empty())
+        CK(cudaMemcpyAsync(cd.ccd_list, w->h_ccd_list.data(), sizeof(uint32_t) * w->h_ccd_list.size(),
+                           cudaMemcpyHostToDevice, w->stream), "CCD layout");
+    CK(cudaMemcpyAsync(cd.ccd_wstart, w->h_ccd_lstart.data(), sizeof(uint32_t) * (nw + 1), cudaMemcpyHostToDevice,
+                       w->stream), "CCD layout");
     CK(cudaMemcpyAsync(cd.bc_start, w->h_bc_start.data(), sizeof(uint32_t) * (w->nb_slots + 1),
                        cudaMemcpyHostToDevice, w->stream), "CCD layout");
     CK(cudaMemcpyAsync(cd.bc_list, w->h_bc_list.data(), sizeof(uint32_t) * w->h_bc_list.size(),

@@ -283,7 +283,8 @@ struct CcdContact {                  // a contact of a substep's island
 struct CcdManifold {
     uint32_t c1, c2, nc, mask;       // mask: unlocked dofs (sm_mask's layout)
     int b1, b2;                      // dynamic body slots (-1: no dofs)
-    float mu, pad;
+    float mu;
+    uint32_t colour;                 // in the island's greedy colouring
     CcdContact k[kMaxContacts];
 };
 struct Ccd {
@@ -294,12 +295,21 @@ struct Ccd {
     uint32_t *wflag;                 // per world: 1 when it has a CCD collider
     float *wdts;                     // per world: the last substep's length (< 0: none this step)
     uint32_t *bc_start, *bc_list;    // colliders of each body, in slot order (host-built CSR)
+    uint32_t *ccd_list, *ccd_wstart; // the CCD colliders by (world, slot), each world's range (host-built)
+    uint32_t *adj_count, *adj_start, *adj_list;   // the step's broad-phase pairs by collider (CSR, partners in
+                                                  // slot order), built on the device each step with CCD
+    void* adj_scan;                  // exclusive-scan scratch of adj_count
+    size_t adj_scan_bytes;
+    uint32_t *bepoch;                // per body: the last neighbour sweep of the island search that saw it
+    unsigned long long *bcol;        // per body: colours of the island manifolds on it
     float4 *sw_min, *sw_max;         // per collider: the box swept from the safe pose to the current one
     float4 *pos0_t, *pos0_q;         // per body: position0
     float *btime, *ftime;            // per body: SubstepState::body_times, frozen time
     uint32_t *bflag;                 // per body: 1 frozen, 2 prepared
     uint32_t *cflag;                 // per collider: 1 visited
-    uint32_t *nbr, *stack, *island, *ccdb, *mlist;   // per-world regions
+    uint32_t *nbr, *nbr2, *stack, *island, *ccdb, *mlist, *mord;   // per-world regions
+    uint2 *res;                      // per-world region: per neighbour, the prepared bits before a sweep and
+                                     // the pool slot of the pair's contacts
     float2 *tres;                    // per-world region: TOI results aligned with nbr
     CcdToi *heap, *impacts;          // per-world regions
     CcdManifold *pool;               // island manifolds of all worlds, taken by an atomic counter

@@ -387,10 +387,11 @@ def batched_worlds(n_worlds=4096, seed=1234, lo=16, hi=2048, worlds=None):
                  info={"worlds": len(worlds), "bodies": int(counts[list(worlds)].sum())})
 
 
-def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234):
+def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234, ccd=False):
     """C5: walls of width x height bricks (half extents 0.5 x 0.25 x 0.25,
     running bond) each struck by `balls` balls of radius 0.4, density 10, at
-    U(20, 40) m/s with a +-5 degree direction jitter; friction 0.6, dt 1/120."""
+    U(20, 40) m/s with a +-5 degree direction jitter; friction 0.6, dt 1/120.
+    With `ccd` the balls' colliders have CCD enabled."""
     rng = np.random.default_rng(seed)
     parts_b, parts_c = [], []
     for w in range(n_walls):
@@ -418,6 +419,7 @@ def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234):
         bb["position"][:, :3] = start.astype(np.float32)
         bb["velocity"][:, :3] = vel.astype(np.float32)
         cb = collider_descs(balls, np.arange(balls), abi.SHAPE_BALL, (0.4, 0, 0), density=10.0, friction=0.6)
+        cb["ccd_enabled"] = 1 if ccd else 0
         parts_b += [g, b, bb]
         parts_c += [gc, c, cb]
     bodies, colliders = _concat(parts_b, parts_c)

@@ -2850,7 +2850,11 @@ public:
         }
         // step_ccd: assembly, position solve, validate_advancement of the
         // impacting bodies, velocity solve, integration of the island.
-        assemble_ccd(mlist);
+        if (!assemble_ccd(mlist)) {
+            last_error = "a CCD island needs more than 64 colours";
+            cur_dt = dt0;
+            return;
+        }
         for (uint32_t it = 0; it < params.max_ccd_position_iterations; ++it)
             for (int i : seq_pos) solve_position(pos_constraints[i]);
         for (uint32_t h : ccd_bodies) bodies[h].pos0 = bodies[h].pos;
@@ -2877,16 +2881,42 @@ public:
         counters.ccd_impacts += uint32_t(impacts.size());
     }
 
-    // The island's contact rows in the reference's order (SORProx::step,
-    // sor_prox.rs:159-179), all started from zero (warmstart_coeff 0), and
-    // their position constraints in manifold order.
-    void assemble_ccd(std::vector<Manifold<R>>& ms) {
+    // The island's contact rows, all started from zero (warmstart_coeff 0),
+    // and their position constraints. ORDER_REFERENCE: the reference's order
+    // (SORProx::step, sor_prox.rs:159-179; manifolds in the order the island
+    // found them). ORDER_COLOUR: the GPU's order, manifolds by their colour
+    // in a greedy colouring over the dynamic bodies in the order the island
+    // found them (the lowest colour not used by an earlier manifold of either
+    // body; at most 64), ties in found order; each iteration the friction
+    // rows, then the normal rows, in that order. Returns false when 64
+    // colours do not suffice.
+    bool assemble_ccd(std::vector<Manifold<R>>& ms) {
         rows.clear();
         pos_constraints.clear();
         seq_warm.clear(); seq_friction.clear(); seq_normal.clear(); seq_pos.clear(); seq_merged.clear();
         const R inv_dt = cur_dt == R(0) ? R(0) : R(1) / cur_dt;
         std::vector<int> ug, un, bg, bn;
-        for (Manifold<R>& m : ms) {
+        std::vector<size_t> morder(ms.size());
+        for (size_t q = 0; q < ms.size(); ++q) morder[q] = q;
+        std::vector<uint32_t> mcol(ms.size(), 0u);
+        if (order == ORDER_COLOUR) {
+            std::map<uint32_t, uint64_t> used;
+            for (size_t q = 0; q < ms.size(); ++q) {
+                const uint32_t x1 = colliders[ms[q].c1].body, x2 = colliders[ms[q].c2].body;
+                uint64_t taken = 0;
+                if (bodies[x1].dynamic()) taken |= used[x1];
+                if (bodies[x2].dynamic()) taken |= used[x2];
+                if (taken == ~0ull) return false;
+                uint32_t k = 0;
+                while (taken & (1ull << k)) ++k;
+                mcol[q] = k;
+                if (bodies[x1].dynamic()) used[x1] |= 1ull << k;
+                if (bodies[x2].dynamic()) used[x2] |= 1ull << k;
+            }
+            std::stable_sort(morder.begin(), morder.end(), [&](size_t a, size_t b) { return mcol[a] < mcol[b]; });
+        }
+        for (size_t qi : morder) {
+            Manifold<R>& m = ms[qi];
             const Collider<R>& c1 = colliders[m.c1];
             const Collider<R>& c2 = colliders[m.c2];
             const Body<R>& b1 = bodies[c1.body];
@@ -2911,7 +2941,8 @@ public:
                 seq_pos.push_back(int(pos_constraints.size()) - 1);
                 V3<R> t[2];
                 tangent_basis(n, t[0], t[1]);
-                (ground ? ug : un).push_back(in);
+                if (order == ORDER_COLOUR) seq_normal.push_back(in);
+                else (ground ? ug : un).push_back(in);
                 for (int s = 0; s < 2; ++s) {
                     Row<R> rt = make_row(b1, c1.body, b2, c2.body, center1, center2, t[s], R(0));
                     rt.impulse = R(0);
@@ -2919,7 +2950,8 @@ public:
                     rt.dep = in;
                     rt.mu = mu;
                     rt.cache = nullptr;
-                    (ground ? bg : bn).push_back(int(rows.size()));
+                    if (order == ORDER_COLOUR) seq_friction.push_back(int(rows.size()));
+                    else (ground ? bg : bn).push_back(int(rows.size()));
                     rows.push_back(rt);
                 }
             }
@@ -2928,6 +2960,7 @@ public:
         for (int i : bg) seq_friction.push_back(i);
         for (int i : un) seq_normal.push_back(i);
         for (int i : ug) seq_normal.push_back(i);
+        return true;
     }
 
     // Test hooks: the distance of two colliders' shapes at the current poses
