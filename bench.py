@@ -579,6 +579,10 @@ def measure(args, sc, w, kind, rank, world_size, local_rank):
     achieved = bytes_launch / (solve_ms * 1e-3) / 1e9
     cl = clocks.summary()
     launches = LAUNCHES_PER_STEP if tuned[0] == 1 else LAUNCHES_PER_STEP_BATCHED
+    if getattr(args, "ccd", False) and kind == "walls":
+        # k_ccd_begin, the pair adjacency's count, scan (3), fill and sort,
+        # k_ccd_world, k_ccd_finish.
+        launches += 9
     return {
         "value": value, "ms_per_step": total_ms / args.steps, "first_timed_step": first_timed,
         "tuned": tuned,
@@ -593,7 +597,9 @@ def measure(args, sc, w, kind, rank, world_size, local_rank):
         "gpu_launches": launches * args.steps,
         "counters": {"contacts": int(statistics.mean(c["num_contacts"] for c in counters)),
                      "solver_contacts": int(K), "active_bodies": int(B),
-                     "colours": int(statistics.mean(c["num_colours"] for c in counters))},
+                     "colours": int(statistics.mean(c["num_colours"] for c in counters)),
+                     "ccd_substeps": statistics.mean(c["ccd_substeps"] for c in counters),
+                     "ccd_impacts": statistics.mean(c["ccd_impacts"] for c in counters)},
         "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
                      ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",
@@ -699,7 +705,7 @@ def run_gpu(args):
                               "clocks": bm["clocks"], "gpu_launches": bm["gpu_launches"], "phase_ms": bm["phase_ms"],
                               "timed_steps": f"{bm['first_timed_step']}..{bm['first_timed_step'] + args.steps - 1}",
                               "world_threads": bm["tuned"][1], **bm["counters"]}
-    if rank == 0 and world_size == 1 and args.workload == "walls":
+    if rank == 0 and world_size == 1 and args.workload == "walls" and not args.ccd:
         line["c5_report"] = walls_record()
     if rank == 0 and world_size == 1 and args.workload == "pile" and not args.no_pgs_iterations:
         line["pgs_iterations"] = pgs_iterations(scenes.mixed_pile(n=100_000))
