@@ -79,7 +79,7 @@ def parse():
                     help="untimed steps first (default: 200 for the ball pile and the pyramid, 300 for the mixed "
                          "pile, 60 for batched worlds, 0 for the brick walls, whose impact phase is the workload)")
     ap.add_argument("--side", type=int, default=32)
-    ap.add_argument("--workload", default="pile", choices=["pile", "batched", "pyramid", "walls", "mixed"],
+    ap.add_argument("--workload", default="pile", choices=["pile", "batched", "pyramid", "walls", "mixed", "joints"],
                     help="pile: the 32^3 ball pile (replicas on N GPUs); batched: --worlds-per-rank worlds "
                          "of the batched-worlds scene per GPU (the batch sharded across ranks); pyramid: the "
                          "210-box pyramid (replicas); walls: 256 brick walls struck by balls per GPU; mixed: "
@@ -607,7 +607,7 @@ def measure(args, sc, w, kind, rank, world_size, local_rank):
     }
 
 
-SETTLE = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0, "mixed": 300}
+SETTLE = {"pile": 200, "batched": 60, "pyramid": 200, "walls": 0, "mixed": 300, "joints": 60}
 
 
 def _params(sc, args):
@@ -647,6 +647,16 @@ def build_workload(kind, args, rank, world_size):
                 "bond), each struck by 64 balls of radius 0.4, density 10, at U(20, 40) m/s; friction 0.6, "
                 "dt 1/120, 8 velocity / 3 position iterations" +
                 ("; the balls' colliders with CCD (one substep a step at most)" if args.ccd else ""))
+    elif kind == "joints":
+        # Sharded like the batched worlds: worlds of every joint kind with contacts.
+        n_all = args.worlds_per_rank * world_size
+        sc = scenes.batched_zoo(n_worlds=n_all, worlds=multirank.shard(n_all, rank, world_size))
+        w = GpuWorld.for_scene(sc, _params(sc, args))
+        desc = (f"jointed worlds: {args.worlds_per_rank} worlds per GPU (of {n_all}), each a ground with one joint of "
+                f"each of the ten kinds (ball, fixed, revolute, cartesian, planar, rectangular, universal, prismatic "
+                f"with offset limits, cylindrical, pin-slot) on boxes and balls and free boxes falling on them "
+                f"({sc.num_dynamic} bodies, {len(sc.joints)} joints on rank 0), dt 1/60, 8 velocity / 3 position "
+                f"iterations")
     else:
         # Sharded: rank r steps worlds [r W, (r + 1) W) of an N W-world batch.
         n_all = args.worlds_per_rank * world_size

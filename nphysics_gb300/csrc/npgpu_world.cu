@@ -1624,7 +1624,7 @@ npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32
     {
         const npgpu_params saved = w->params;
         w->params.solver_schedule = NPGPU_SCHEDULE_AUTO;
-        npgpu_status st0 = npgpu_step(w, 1, 0, 0);
+        npgpu_status st0 = npgpu_step(w, 1, w->nj_alive, 0);
         if (st0 == NPGPU_OK) st0 = npgpu_synchronize(w);
         w->params = saved;
         if (st0 != NPGPU_OK) return st0;
@@ -1651,10 +1651,10 @@ npgpu_status npgpu_autotune(npgpu_world* w, uint32_t steps_per_candidate, uint32
     for (const Cand& c : cands) {
         w->params.solver_schedule = c.schedule;
         w->params.world_threads = c.threads;
-        st = npgpu_step(w, 1, 0, 0);   // capture (when graphs are on) outside the timing
+        st = npgpu_step(w, 1, w->nj_alive, 0);   // capture (when graphs are on) outside the timing
         if (st != NPGPU_OK) break;
         cudaEventRecord(e0, w->stream);
-        st = npgpu_step(w, steps_per_candidate, 0, 0);
+        st = npgpu_step(w, steps_per_candidate, w->nj_alive, 0);
         if (st != NPGPU_OK) break;
         cudaEventRecord(e1, w->stream);
         st = npgpu_synchronize(w);

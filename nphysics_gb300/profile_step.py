@@ -24,7 +24,8 @@ Workloads: pile (the 32^3 ball pile, one cooperative grid), cluster (the same
 pile under the per-world schedule: one thread-block cluster), batched
 (--worlds batched worlds, one block or warp per world), mixed (--bodies
 bodies of the mixed pile's recipe at its density), joints (--worlds worlds
-of every joint kind with contacts).
+of every joint kind with contacts), walls_ccd (--worlds brick walls struck by
+balls with CCD, from step 60 when the balls reach the walls).
 """
 import argparse
 import math
@@ -59,6 +60,9 @@ def build(args):
         # Worlds of every joint kind with contacts, one block (or warp) per world.
         sc = scenes.batched_zoo(n_worlds=args.worlds)
         return sc, GpuWorld.for_scene(sc), 60
+    if args.workload == "walls_ccd":
+        sc = scenes.brick_walls(n_walls=args.worlds, ccd=True)
+        return sc, GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=8), 60
     n = args.bodies
     sc = scenes.mixed_pile(n=n, footprint=100.0 * math.sqrt(n / 100_000))
     return sc, GpuWorld.for_scene(sc, sc.params(), pairs_per_collider=12), 300
@@ -68,7 +72,8 @@ def main(argv=None):
     import torch
 
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("--workload", default="pile", choices=["pile", "cluster", "batched", "mixed", "joints"])
+    ap.add_argument("--workload", default="pile",
+                    choices=["pile", "cluster", "batched", "mixed", "joints", "walls_ccd"])
     ap.add_argument("--region", default="step", choices=["step", "e2e", "train", "query", "events", "static"])
     ap.add_argument("--queries", type=int, default=100_000)
     ap.add_argument("--side", type=int, default=32)

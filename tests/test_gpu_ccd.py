@@ -93,3 +93,13 @@ def test_ccd_with_graphs_and_removal(gpu_lib):
         w.remove_colliders(sc.collider_handles[-2:])
     step_same(g, o, 5)
     assert g.counters()["ccd_substeps"] == 0
+
+
+def test_autotune_with_ccd_keeps_the_bits(gpu_lib):
+    sc = scenes.batched_ccd(n_worlds=3)
+    g, o = make_pair(sc)
+    g.autotune(steps_per_candidate=2)
+    g.step(5)
+    o.step(int(g.counters()["steps"]))
+    np.testing.assert_array_equal(g.bodies()["position"], o.bodies()["position"])
+    np.testing.assert_array_equal(g.bodies()["velocity"], o.bodies()["velocity"])

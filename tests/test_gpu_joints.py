@@ -187,3 +187,17 @@ def test_joint_errors_are_statuses(gpu_lib):
 
 def abi_status(name):
     return {"INVALID_HANDLE": 1, "INVALID_ARGUMENT": 10}[name]
+
+
+def test_autotune_with_joints_keeps_the_bits(gpu_lib):
+    # The tuner's steps carry the uploaded joints: the tuned jointed world
+    # equals the oracle stepped as many times.
+    sc = scenes.batched_zoo(n_worlds=4)
+    g, o = make_pair(sc)
+    sched, threads, ms = g.autotune(steps_per_candidate=2)
+    assert ms > 0
+    g.step(5)
+    o.step(int(g.counters()["steps"]))
+    gb, ob = g.bodies(), o.bodies()
+    np.testing.assert_array_equal(gb["position"], ob["position"])
+    np.testing.assert_array_equal(gb["velocity"], ob["velocity"])
