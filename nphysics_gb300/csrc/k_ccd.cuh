@@ -398,14 +398,53 @@ __device__ void ccd_manifold_velocity(const World& w, CcdManifold& m, bool frict
 }
 
 // Shared state of a world's CCD loop.
-constexpr uint32_t kCcdColours = 64;
+constexpr uint32_t kCcdColours = 256;
 struct CcdState {
     float end_time, min_overstep, last;
     uint32_t last_iter, result, nheap, nimp, seq, nstack, nisland, nccdb, nm;
-    uint32_t cur, n, stop, epoch, ncol;
+    uint32_t cur, n, stop, epoch, ncol, nnext, left;
     uint32_t cnt[kCcdThreads / 32];
+    uint32_t part[kCcdThreads];
     uint32_t col_start[kCcdColours + 1];
+    uint32_t col_fill[kCcdColours];
 };
+
+// Exclusive prefix sums of a[0, n) in place, by the whole block; returns
+// the total.
+__device__ uint32_t block_scan(uint32_t* a, uint32_t n, CcdState& st) {
+    const uint32_t per = (n + blockDim.x - 1) / blockDim.x;
+    const uint32_t lo = threadIdx.x * per, hi = lo + per < n ? lo + per : n;
+    uint32_t sum = 0;
+    for (uint32_t i = lo; i < hi; ++i) sum += a[i];
+    st.part[threadIdx.x] = sum;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t k = 0; k < blockDim.x; ++k) {
+            const uint32_t v = st.part[k];
+            st.part[k] = run;
+            run += v;
+        }
+        st.n = run;
+    }
+    __syncthreads();
+    uint32_t run = st.part[threadIdx.x];
+    for (uint32_t i = lo; i < hi; ++i) {
+        const uint32_t v = a[i];
+        a[i] = run;
+        run += v;
+    }
+    const uint32_t total = st.n;
+    __syncthreads();
+    return total;
+}
+
+// The Jones-Plassmann priority of an island manifold: a hash of its
+// colliders' world-local slots, ties by the slots.
+__device__ __forceinline__ unsigned long long ccd_priority(uint32_t base, const CcdManifold& m) {
+    const uint32_t l1 = m.c1 - base, l2 = m.c2 - base;
+    return ((unsigned long long)pair_hash22(l1, l2) << 42) | ((unsigned long long)l1 << 21) | (unsigned long long)l2;
+}
 
 // The colliders interacting with c during CCD, in slot order, into nbr
 // (tmp: scratch of the same size); returns their count (block-uniform; above
@@ -617,29 +656,29 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t wd, ui
 // One substep (mechanical_world.rs:624-889): the island grown from the
 // impacting bodies through contacts, moved back to the latest TOI, solved
 // (MoreauJeanSolver::step_ccd, moreau_jean_solver.rs:94-127) and integrated
-// over the rest of the step. The island search keeps the reference's order
-// (a stack of colliders; each popped collider's pairs with unvisited ones in
-// slot order, the bodies prepared on first sight, a pair with contacts
-// extending the island to the colliders of a body it prepared); the block
-// prepares the bodies and updates the pairs of a popped collider together,
-// and thread 0 replays the order. The island's manifolds are then solved in
-// colour order: a greedy colouring over their dynamic bodies in the order
-// they were found.
+// over the rest of the step. The island is the closure through contacts,
+// found level by level: a level's pairs are those of its colliders with
+// colliders not explored before it (each pair once), its bodies are
+// prepared first (forces cleared, dynamics over the substep, acceleration
+// without gravity, moved back to the frozen time or the latest TOI), and a
+// pair with contacts explores the colliders of its other body when that is
+// dynamic. The manifolds are put in collider-pair order, coloured by
+// Jones-Plassmann rounds and solved colour by colour.
 __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t rb,
                             uint32_t rcap, CcdState& st) {
     const Ccd& cd = w.ccd;
-    uint32_t* nbr = cd.nbr + rb;
-    uint32_t* stack = cd.stack + rb;
+    uint32_t* front = cd.stack + rb;        // the level's colliders
+    uint32_t* next = cd.nbr + rb;           // bodies the level explored
     uint32_t* island = cd.island + rb;
     uint32_t* ccdb = cd.ccdb + rb;
     uint32_t* mlist = cd.mlist + rb;
     uint32_t* mord = cd.mord + rb;
-    uint2* res = cd.res + rb;
+    uint2* pairs = cd.res + rb;
     const CcdToi* imp = cd.impacts + rb;
     for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) {
         const uint32_t c = cd.order[ws + i];
         cd.cflag[c] = 0u;
-        cd.bflag[ccd_body_of(w, c)] &= ~2u;
+        cd.bflag[ccd_body_of(w, c)] &= ~6u;
     }
     __syncthreads();
     const float last = imp[st.nimp - 1].toi;
@@ -651,12 +690,16 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         for (uint32_t k = 0; k < st.nimp && !st.stop; ++k) {
             const uint32_t bs[2] = {ccd_body_of(w, imp[k].c1), ccd_body_of(w, imp[k].c2)};
             for (int s = 0; s < 2; ++s) {
-                for (uint32_t q = cd.bc_start[bs[s]]; q < cd.bc_start[bs[s] + 1]; ++q) {
-                    if (st.nstack >= rcap) st.stop = 1;
-                    else stack[st.nstack++] = cd.bc_list[q];
-                }
                 if (st.nccdb >= rcap) st.stop = 1;
                 else ccdb[st.nccdb++] = bs[s];
+                if (cd.bflag[bs[s]] & 4u) continue;
+                cd.bflag[bs[s]] |= 4u;
+                for (uint32_t q = cd.bc_start[bs[s]]; q < cd.bc_start[bs[s] + 1]; ++q) {
+                    const uint32_t c = cd.bc_list[q];
+                    cd.cflag[c] |= 3u;
+                    if (st.nstack >= rcap) st.stop = 1;
+                    else front[st.nstack++] = c;
+                }
             }
         }
     }
@@ -664,140 +707,244 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     StepParams ps = p;
     ps.dt = dts;
     ps.inv_dt = dts == 0.0f ? 0.0f : 1.0f / dts;
-    for (;;) {
-        if (threadIdx.x == 0) {
-            uint32_t c = 0xffffffffu;
-            while (st.nstack > 0 && !st.stop) {
-                const uint32_t t = stack[--st.nstack];
-                if (!(cd.cflag[t] & 1u)) {
-                    c = t;
-                    break;
-                }
+    while (st.nstack > 0 && !st.stop) {
+        const uint32_t nf = st.nstack;
+        if (threadIdx.x == 0) st.n = 0;
+        __syncthreads();
+        // The level's pairs.
+        for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
+            const uint32_t c = front[i];
+            auto consider = [&](uint32_t d) {
+                const uint32_t f = cd.cflag[d];
+                if ((f & 1u) && !(f & 2u)) return;   // its pairs were a former level's
+                if ((f & 2u) && d < c) return;       // taken from d
+                const uint32_t at = atomicAdd(&st.n, 1u);
+                if (at < rcap) pairs[at] = make_uint2(c < d ? c : d, c < d ? d : c);
+            };
+            for (uint32_t q = cd.adj_start[c]; q < cd.adj_start[c + 1]; ++q) consider(cd.adj_list[q]);
+            const uint32_t bc = ccd_body_of(w, c);
+            auto swept = [&](uint32_t d) {
+                if (d == c || !(w.c.info[d] & CI_ALIVE)) return false;
+                const uint32_t bd = ccd_body_of(w, d);
+                if (bc == bd || w.b.world[bc] != w.b.world[bd]) return false;
+                if (!ccd_dynamic(w, bc) && !ccd_dynamic(w, bd)) return false;
+                if (!ccd_enabled(w, c) && !ccd_enabled(w, d)) return false;
+                const float4 amn = w.c.aabb_min[c], amx = w.c.aabb_max[c], bmn = w.c.aabb_min[d], bmx = w.c.aabb_max[d];
+                if (amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z &&
+                    bmn.z <= amx.z)
+                    return false;
+                const float4 smn = cd.sw_min[c], smx = cd.sw_max[c], tmn = cd.sw_min[d], tmx = cd.sw_max[d];
+                return smn.x <= tmx.x && tmn.x <= smx.x && smn.y <= tmx.y && tmn.y <= smx.y && smn.z <= tmx.z &&
+                       tmn.z <= smx.z;
+            };
+            if (ccd_enabled(w, c)) {
+                for (uint32_t k = 0; k < wn; ++k)
+                    if (swept(cd.order[ws + k])) consider(cd.order[ws + k]);
+            } else {
+                for (uint32_t k = cd.ccd_wstart[wd]; k < cd.ccd_wstart[wd + 1]; ++k)
+                    if (swept(cd.ccd_list[k])) consider(cd.ccd_list[k]);
             }
-            st.cur = c;
         }
         __syncthreads();
-        const uint32_t c = st.cur;
-        __syncthreads();
-        if (c == 0xffffffffu) break;
-        const uint32_t n = ccd_neighbours(w, wd, ws, wn, c, nbr, cd.nbr2 + rb, rcap, st);
-        if (n > rcap) {
+        const uint32_t np_ = st.n;
+        if (np_ > rcap) {
             if (threadIdx.x == 0) st.stop = 1;
+            __syncthreads();
             break;
         }
-        // Which bodies were prepared before this collider's pairs.
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            const uint32_t d = nbr[j];
-            if (cd.cflag[d] & 1u) {
-                res[j] = make_uint2(0xffffffffu, 0xffffffffu);
-                continue;
-            }
-            const uint32_t x1 = ccd_body_of(w, c < d ? c : d), x2 = ccd_body_of(w, c < d ? d : c);
-            res[j] = make_uint2(((cd.bflag[x1] >> 1) & 1u) | (((cd.bflag[x2] >> 1) & 1u) << 1), 0xffffffffu);
-        }
-        __syncthreads();
-        // Every body of these pairs prepared once.
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            if (res[j].x == 0xffffffffu) continue;
-            const uint32_t d = nbr[j];
-            const uint32_t xs[2] = {ccd_body_of(w, c < d ? c : d), ccd_body_of(w, c < d ? d : c)};
+        // Its bodies, each prepared once.
+        for (uint32_t i = threadIdx.x; i < np_; i += blockDim.x) {
+            const uint32_t xs[2] = {ccd_body_of(w, pairs[i].x), ccd_body_of(w, pairs[i].y)};
             for (int s = 0; s < 2; ++s) {
                 if (!ccd_dynamic(w, xs[s]) || (atomicOr(&cd.bflag[xs[s]], 2u) & 2u)) continue;
                 ccd_prepare(w, p, xs[s], dts, last);
                 const uint32_t at = atomicAdd(&st.nisland, 1u);
                 if (at < rcap) island[at] = xs[s];
+                else st.stop = 1;
             }
         }
+        if (threadIdx.x == 0) st.nnext = 0;
         __syncthreads();
-        // The pairs' contacts at the prepared poses, into the pool.
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            if (res[j].x == 0xffffffffu) continue;
-            const uint32_t d = nbr[j];
+        // Its contacts; a pair with contacts explores its other body.
+        for (uint32_t i = threadIdx.x; i < np_; i += blockDim.x) {
+            const uint2 pr = pairs[i];
             CcdManifold mf;
-            if (ccd_contacts(w, c < d ? c : d, c < d ? d : c, mf) == 0u) continue;
+            if (ccd_contacts(w, pr.x, pr.y, mf) == 0u) continue;
             const uint32_t slot = atomicAdd(&w.ctl->ccd_mcount, 1u);
-            if (slot >= cd.pool_cap) {
+            const uint32_t at = atomicAdd(&st.nm, 1u);
+            if (slot >= cd.pool_cap || at >= rcap) {
                 st.stop = 1;
                 continue;
             }
             cd.pool[slot] = mf;
-            res[j].y = slot;
+            mlist[at] = slot;
+            const uint32_t other = (cd.cflag[pr.x] & 2u) ? pr.y : pr.x;
+            const uint32_t xo = ccd_body_of(w, other);
+            if ((cd.cflag[other] & 2u) || !ccd_dynamic(w, xo) || (atomicOr(&cd.bflag[xo], 4u) & 4u)) continue;
+            const uint32_t k = atomicAdd(&st.nnext, 1u);
+            if (k < rcap) next[k] = xo;
+            else st.stop = 1;
         }
         __syncthreads();
-        // The reference's order: found manifolds, and the colliders of bodies
-        // a pair with contacts prepared.
-        if (threadIdx.x == 0) {
-            const uint32_t epoch = ++st.epoch;
-            for (uint32_t j = 0; j < n && !st.stop; ++j) {
-                const uint2 r = res[j];
-                if (r.x == 0xffffffffu) continue;
-                const uint32_t d = nbr[j];
-                const uint32_t ch1 = c < d ? c : d, ch2 = c < d ? d : c;
-                const uint32_t xs[2] = {ccd_body_of(w, ch1), ccd_body_of(w, ch2)};
-                bool prep[2];
-                for (int s = 0; s < 2; ++s) {
-                    prep[s] = !((r.x >> s) & 1u) && ccd_dynamic(w, xs[s]) && cd.bepoch[xs[s]] != epoch;
-                    cd.bepoch[xs[s]] = epoch;
-                }
-                if (r.y == 0xffffffffu) continue;
-                if (st.nm >= rcap) {
-                    st.stop = 1;
-                    break;
-                }
-                mlist[st.nm++] = r.y;
-                const bool push[2] = {ch1 != c && prep[0], ch2 != c && prep[1]};
-                for (int s = 0; s < 2; ++s) {
-                    if (!push[s]) continue;
-                    for (uint32_t q = cd.bc_start[xs[s]]; q < cd.bc_start[xs[s] + 1]; ++q) {
-                        if (st.nstack >= rcap) st.stop = 1;
-                        else stack[st.nstack++] = cd.bc_list[q];
-                    }
-                }
+        // The next level: the colliders of the bodies explored.
+        for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) cd.cflag[front[i]] &= ~2u;
+        if (threadIdx.x == 0) st.nstack = 0;
+        __syncthreads();
+        const uint32_t nn = st.nnext;
+        for (uint32_t i = threadIdx.x; i < nn && i < rcap; i += blockDim.x) {
+            const uint32_t b = next[i];
+            for (uint32_t q = cd.bc_start[b]; q < cd.bc_start[b + 1]; ++q) {
+                const uint32_t c = cd.bc_list[q];
+                cd.cflag[c] |= 3u;
+                const uint32_t at = atomicAdd(&st.nstack, 1u);
+                if (at < rcap) front[at] = c;
+                else st.stop = 1;
             }
-            cd.cflag[c] |= 1u;
-            if (st.nisland > rcap) st.stop = 1;
         }
         __syncthreads();
     }
-    // The island's colours, in found order.
-    for (uint32_t i = threadIdx.x; i < st.nisland && i < rcap; i += blockDim.x) cd.bcol[island[i]] = 0ull;
-    __syncthreads();
-    if (threadIdx.x == 0 && !st.stop) {
-        uint32_t count[kCcdColours];
-        for (uint32_t k = 0; k < kCcdColours; ++k) count[k] = 0;
-        uint32_t ncol = 0;
-        for (uint32_t q = 0; q < st.nm && !st.stop; ++q) {
-            CcdManifold& m = cd.pool[mlist[q]];
-            const uint32_t x1 = ccd_body_of(w, m.c1), x2 = ccd_body_of(w, m.c2);
-            const bool d1 = ccd_dynamic(w, x1), d2 = ccd_dynamic(w, x2);
-            const unsigned long long taken = (d1 ? cd.bcol[x1] : 0ull) | (d2 ? cd.bcol[x2] : 0ull);
-            if (taken == ~0ull) {
-                st.stop = 1;
-                break;
-            }
-            const uint32_t k = (uint32_t)__ffsll((long long)~taken) - 1u;
-            if (d1) cd.bcol[x1] |= 1ull << k;
-            if (d2) cd.bcol[x2] |= 1ull << k;
-            m.colour = k;
-            count[k] += 1;
-            ncol = ncol > k + 1 ? ncol : k + 1;
-        }
-        st.col_start[0] = 0;
-        for (uint32_t k = 0; k < kCcdColours; ++k) st.col_start[k + 1] = st.col_start[k] + count[k];
-        uint32_t cur[kCcdColours];
-        for (uint32_t k = 0; k < kCcdColours; ++k) cur[k] = st.col_start[k];
-        for (uint32_t q = 0; q < st.nm && !st.stop; ++q) mord[cur[cd.pool[mlist[q]].colour]++] = mlist[q];
-        st.ncol = ncol;
-    }
-    __syncthreads();
     if (st.stop) {
         if (threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_CCD_CAPACITY);
         __syncthreads();
         return;
     }
+    const uint32_t nm = st.nm, nisl = st.nisland;
+    // Collider-pair order: by the first collider's place in the world's
+    // slot-ordered segment, then by the second collider.
+    uint32_t* cnt = cd.nbr2 + rb;
+    for (uint32_t i = threadIdx.x; i <= wn; i += blockDim.x) cnt[i] = 0u;
+    __syncthreads();
+    auto place = [&](uint32_t c) {
+        uint32_t lo = 0, hi = wn;
+        while (lo < hi) {
+            const uint32_t mid = (lo + hi) >> 1;
+            if (cd.order[ws + mid] < c) lo = mid + 1;
+            else hi = mid;
+        }
+        return lo;
+    };
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) atomicAdd(&cnt[place(cd.pool[mlist[q]].c1)], 1u);
+    __syncthreads();
+    block_scan(cnt, wn + 1, st);
+    uint32_t* cursor = cd.nbr + rb;
+    for (uint32_t i = threadIdx.x; i <= wn; i += blockDim.x) cursor[i] = cnt[i];
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
+        const uint32_t slot = mlist[q];
+        mord[atomicAdd(&cursor[place(cd.pool[slot].c1)], 1u)] = slot;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) {
+        uint32_t* l = mord + cnt[i];
+        const uint32_t n = cnt[i + 1] - cnt[i];
+        for (uint32_t a = 1; a < n; ++a) {
+            const uint32_t x = l[a], kx = cd.pool[x].c2;
+            uint32_t b = a;
+            while (b > 0 && cd.pool[l[b - 1]].c2 > kx) {
+                l[b] = l[b - 1];
+                --b;
+            }
+            l[b] = x;
+        }
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) mlist[q] = mord[q];
+    // The manifolds on each island body (CSR: bcount over the island's
+    // bodies, numbered through bepoch).
+    uint32_t* bstart = cd.nbr + rb;
+    uint32_t* blist = reinterpret_cast<uint32_t*>(pairs);   // 2 rcap words
+    for (uint32_t i = threadIdx.x; i < nisl; i += blockDim.x) {
+        cd.bepoch[island[i]] = i;
+        bstart[i] = 0u;
+    }
+    if (threadIdx.x == 0) bstart[nisl] = 0u;
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
+        CcdManifold& m = cd.pool[mlist[q]];
+        m.colour = 0xffffffffu;
+        for (uint32_t c : {m.c1, m.c2}) {
+            const uint32_t x = ccd_body_of(w, c);
+            if (ccd_dynamic(w, x)) atomicAdd(&bstart[cd.bepoch[x]], 1u);
+        }
+    }
+    __syncthreads();
+    block_scan(bstart, nisl + 1, st);
+    uint32_t* bcur = cnt;
+    for (uint32_t i = threadIdx.x; i <= nisl; i += blockDim.x) bcur[i] = bstart[i];
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
+        const CcdManifold& m = cd.pool[mlist[q]];
+        for (uint32_t c : {m.c1, m.c2}) {
+            const uint32_t x = ccd_body_of(w, c);
+            if (ccd_dynamic(w, x)) blist[atomicAdd(&bcur[cd.bepoch[x]], 1u)] = q;
+        }
+    }
+    if (threadIdx.x == 0) st.left = nm;
+    __syncthreads();
+    // Jones-Plassmann rounds: round r colours the manifolds whose priority
+    // is above every uncoloured manifold's on a shared dynamic body.
+    const uint32_t base = cd.order[ws];
+    uint32_t ncol = 0;
+    for (; st.left > 0 && ncol < kCcdColours; ++ncol) {
+        for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
+            const CcdManifold& m = cd.pool[mlist[q]];
+            mord[q] = 0u;
+            if (m.colour != 0xffffffffu) continue;
+            const unsigned long long pq = ccd_priority(base, m);
+            bool top = true;
+            for (uint32_t c : {m.c1, m.c2}) {
+                const uint32_t x = ccd_body_of(w, c);
+                if (!ccd_dynamic(w, x)) continue;
+                const uint32_t k = cd.bepoch[x];
+                for (uint32_t e = bstart[k]; e < bstart[k + 1] && top; ++e) {
+                    const uint32_t o = blist[e];
+                    if (o == q) continue;
+                    const CcdManifold& mo = cd.pool[mlist[o]];
+                    if (mo.colour == 0xffffffffu && ccd_priority(base, mo) > pq) top = false;
+                }
+            }
+            mord[q] = top ? 1u : 0u;
+        }
+        __syncthreads();
+        uint32_t taken = 0;
+        for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x)
+            if (mord[q]) {
+                cd.pool[mlist[q]].colour = ncol;
+                ++taken;
+            }
+        atomicSub(&st.left, taken);
+        __syncthreads();
+    }
+    if (st.left > 0) {
+        if (threadIdx.x == 0) atomicOr(&w.ctl->err, ERRF_CCD_CAPACITY);
+        __syncthreads();
+        return;
+    }
+    // The manifolds by colour.
+    for (uint32_t k = threadIdx.x; k <= kCcdColours; k += blockDim.x) {
+        st.col_start[k] = 0u;
+        if (k < kCcdColours) st.col_fill[k] = 0u;
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) atomicAdd(&st.col_start[cd.pool[mlist[q]].colour], 1u);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        uint32_t run = 0;
+        for (uint32_t k = 0; k <= kCcdColours; ++k) {
+            const uint32_t v = st.col_start[k];
+            st.col_start[k] = run;
+            run += v;
+        }
+    }
+    __syncthreads();
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
+        // Within a colour the manifolds share no dynamic body: any order.
+        const uint32_t k = cd.pool[mlist[q]].colour;
+        mord[st.col_start[k] + atomicAdd(&st.col_fill[k], 1u)] = mlist[q];
+    }
+    __syncthreads();
     // step_ccd: the rows, the position solve, validate_advancement of the
     // impacting bodies, the velocity solve and the island's integration.
-    const uint32_t nm = st.nm, ncol = st.ncol, nisl = st.nisland;
     for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) ccd_rows(w, ps, cd.pool[mlist[q]], dts);
     for (uint32_t i = threadIdx.x; i < nisl; i += blockDim.x)
         for (int k = 0; k < 6; ++k) w.b.dv[6 * (size_t)island[i] + k] = 0.0f;

@@ -2822,7 +2822,64 @@ public:
             island.push_back(h);
         };
         std::vector<Manifold<R>> mlist;
-        while (!stack.empty()) {
+        if (order == ORDER_COLOUR) {
+            // The GPU's island: the closure through contacts, level by level
+            // (a level's pairs: those of its colliders with colliders not
+            // explored before it, each once; its bodies prepared first; a
+            // pair with contacts explores the colliders of its other body,
+            // when dynamic), the manifolds in collider-pair order.
+            std::vector<char> explored_body(bodies.size(), 0), explored(colliders.size(), 0), front(colliders.size(), 0);
+            std::vector<uint32_t> frontier;
+            for (const TOIEntry& e : impacts)
+                for (uint32_t b : {e.b1, e.b2})
+                    if (!explored_body[b]) {
+                        explored_body[b] = 1;
+                        for (uint32_t c : body_colliders[b]) frontier.push_back(c);
+                    }
+            for (uint32_t c : frontier) explored[c] = front[c] = 1;
+            std::map<uint64_t, Manifold<R>> found;
+            while (!frontier.empty()) {
+                std::vector<std::pair<uint32_t, uint32_t>> pairs;
+                for (uint32_t c : frontier) {
+                    interactions(c, nbr);
+                    for (uint32_t d : nbr) {
+                        if (explored[d] && !front[d]) continue;   // its pairs were a former level's
+                        if (front[d] && d < c) continue;          // taken from d
+                        pairs.push_back({std::min(c, d), std::max(c, d)});
+                    }
+                }
+                for (auto& pr : pairs)
+                    for (uint32_t x : {colliders[pr.first].body, colliders[pr.second].body})
+                        if (!prepared[x] && bodies[x].dynamic()) prepare(x);
+                std::vector<uint32_t> next;
+                for (auto& pr : pairs) {
+                    const uint32_t x1 = colliders[pr.first].body, x2 = colliders[pr.second].body;
+                    colliders[pr.first].pose = iso_mul(bodies[x1].pos, colliders[pr.first].pos_wrt_body);
+                    colliders[pr.second].pose = iso_mul(bodies[x2].pos, colliders[pr.second].pos_wrt_body);
+                    Manifold<R> m;
+                    m.c1 = pr.first;
+                    m.c2 = pr.second;
+                    narrow_pair(m);
+                    if (m.contacts.empty()) continue;
+                    found[(uint64_t(m.c1) << 32) | m.c2] = m;
+                    const uint32_t other = front[pr.first] ? pr.second : pr.first;
+                    const uint32_t xo = colliders[other].body;
+                    if (!front[other] && bodies[xo].dynamic() && !explored_body[xo]) {
+                        explored_body[xo] = 1;
+                        next.push_back(xo);
+                    }
+                }
+                for (uint32_t c : frontier) front[c] = 0;
+                frontier.clear();
+                for (uint32_t b : next)
+                    for (uint32_t c : body_colliders[b]) {
+                        explored[c] = front[c] = 1;
+                        frontier.push_back(c);
+                    }
+            }
+            for (auto& kv : found) mlist.push_back(kv.second);
+        }
+        while (order != ORDER_COLOUR && !stack.empty()) {
             const uint32_t c = stack.back();
             stack.pop_back();
             if (visited[c]) continue;
@@ -2851,7 +2908,7 @@ public:
         // step_ccd: assembly, position solve, validate_advancement of the
         // impacting bodies, velocity solve, integration of the island.
         if (!assemble_ccd(mlist)) {
-            last_error = "a CCD island needs more than 64 colours";
+            last_error = "a CCD island needs more than 256 colours";
             cur_dt = dt0;
             return;
         }
@@ -2884,12 +2941,20 @@ public:
     // The island's contact rows, all started from zero (warmstart_coeff 0),
     // and their position constraints. ORDER_REFERENCE: the reference's order
     // (SORProx::step, sor_prox.rs:159-179; manifolds in the order the island
-    // found them). ORDER_COLOUR: the GPU's order, manifolds by their colour
-    // in a greedy colouring over the dynamic bodies in the order the island
-    // found them (the lowest colour not used by an earlier manifold of either
-    // body; at most 64), ties in found order; each iteration the friction
-    // rows, then the normal rows, in that order. Returns false when 64
-    // colours do not suffice.
+    // found them). ORDER_COLOUR: the GPU's order, manifolds by their
+    // Jones-Plassmann colour, ties in collider-pair order; each iteration the
+    // friction rows, then the normal rows, in that order. Returns false when
+    // kCcdColours colours do not suffice.
+    static constexpr uint32_t kCcdColours = 256;
+    static uint32_t ccd_pair_hash(uint32_t c1, uint32_t c2) {
+        uint32_t h = c1 * 0x9E3779B1u ^ (c2 + 0x7F4A7C15u) * 0x85EBCA77u;
+        h ^= h >> 15;
+        h *= 0x2C1B3C6Du;
+        h ^= h >> 12;
+        h *= 0x297A2D39u;
+        h ^= h >> 15;
+        return h >> 10;
+    }
     bool assemble_ccd(std::vector<Manifold<R>>& ms) {
         rows.clear();
         pos_constraints.clear();
@@ -2900,19 +2965,44 @@ public:
         for (size_t q = 0; q < ms.size(); ++q) morder[q] = q;
         std::vector<uint32_t> mcol(ms.size(), 0u);
         if (order == ORDER_COLOUR) {
-            std::map<uint32_t, uint64_t> used;
+            // Jones-Plassmann rounds: a manifold takes the round's colour when
+            // its priority (a hash of its colliders' world-local slots, ties
+            // by the slots) is above every uncoloured manifold's sharing a
+            // dynamic body with it.
+            const uint32_t world = bodies[colliders[ms.empty() ? 0 : ms[0].c1].body].world;
+            uint32_t base = 0xffffffffu;
+            for (uint32_t c = 0; c < colliders.size(); ++c)
+                if (colliders[c].alive && bodies[colliders[c].body].world == world) {
+                    base = c;
+                    break;
+                }
+            std::vector<uint64_t> prio(ms.size());
+            std::map<uint32_t, std::vector<size_t>> on_body;
             for (size_t q = 0; q < ms.size(); ++q) {
-                const uint32_t x1 = colliders[ms[q].c1].body, x2 = colliders[ms[q].c2].body;
-                uint64_t taken = 0;
-                if (bodies[x1].dynamic()) taken |= used[x1];
-                if (bodies[x2].dynamic()) taken |= used[x2];
-                if (taken == ~0ull) return false;
-                uint32_t k = 0;
-                while (taken & (1ull << k)) ++k;
-                mcol[q] = k;
-                if (bodies[x1].dynamic()) used[x1] |= 1ull << k;
-                if (bodies[x2].dynamic()) used[x2] |= 1ull << k;
+                const uint32_t l1 = ms[q].c1 - base, l2 = ms[q].c2 - base;
+                prio[q] = (uint64_t(ccd_pair_hash(l1, l2)) << 42) | (uint64_t(l1) << 21) | uint64_t(l2);
+                for (uint32_t x : {colliders[ms[q].c1].body, colliders[ms[q].c2].body})
+                    if (bodies[x].dynamic()) on_body[x].push_back(q);
             }
+            std::vector<int> colour(ms.size(), -1);
+            size_t left = ms.size();
+            for (int round = 0; left > 0; ++round) {
+                if (round >= int(kCcdColours)) return false;
+                std::vector<size_t> take;
+                for (size_t q = 0; q < ms.size(); ++q) {
+                    if (colour[q] >= 0) continue;
+                    bool top = true;
+                    for (uint32_t x : {colliders[ms[q].c1].body, colliders[ms[q].c2].body}) {
+                        if (!bodies[x].dynamic()) continue;
+                        for (size_t o : on_body[x])
+                            if (o != q && colour[o] < 0 && prio[o] > prio[q]) top = false;
+                    }
+                    if (top) take.push_back(q);
+                }
+                for (size_t q : take) colour[q] = round;
+                left -= take.size();
+            }
+            for (size_t q = 0; q < ms.size(); ++q) mcol[q] = uint32_t(colour[q]);
             std::stable_sort(morder.begin(), morder.end(), [&](size_t a, size_t b) { return mcol[a] < mcol[b]; });
         }
         for (size_t qi : morder) {
