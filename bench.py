@@ -603,7 +603,8 @@ def measure(args, sc, w, kind, rank, world_size, local_rank):
         "phase_ms": {k: statistics.mean(c[k] for c in counters) for k in
                      ("step_time", "solver_time", "collision_detection_time", "broad_phase_time", "narrow_phase_time",
                       "island_construction_time", "colouring_time", "assembly_time", "velocity_resolution_time",
-                      "velocity_update_time", "position_resolution_time")},
+                      "velocity_update_time", "position_resolution_time", "ccd_toi_computation_time",
+                      "ccd_solver_time", "ccd_broad_phase_time", "ccd_narrow_phase_time", "ccd_world_time_max")},
     }
 
 

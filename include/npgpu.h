@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 6u
+#define NPGPU_ABI_VERSION 7u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -315,6 +315,13 @@ typedef struct npgpu_counters {
     uint32_t ccd_substeps;           /* CCD substeps of the last step, over all worlds */
     uint32_t ccd_impacts;            /* time-of-impact events those substeps resolved */
     uint32_t reserved;
+    /* Profile only: CCD time in ms summed over the worlds' CCD blocks
+     * (CCDCounters, counters/ccd_counters.rs:6-17), and the longest world. */
+    double ccd_toi_computation_time; /* times of impact and their queue */
+    double ccd_solver_time;          /* island bodies, colouring, solves, integration */
+    double ccd_broad_phase_time;     /* swept boxes and neighbour searches */
+    double ccd_narrow_phase_time;    /* the island's contacts */
+    double ccd_world_time_max;       /* the longest world's CCD */
 } npgpu_counters;
 
 /* Contact record returned for parity checks (a TrackedContact,

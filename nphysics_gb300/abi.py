@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 6
+NPGPU_ABI_VERSION = 7
 
 # npgpu_status
 OK = 0
@@ -221,6 +221,11 @@ class Counters(C.Structure):
         ("ccd_substeps", C.c_uint32),
         ("ccd_impacts", C.c_uint32),
         ("reserved", C.c_uint32),
+        ("ccd_toi_computation_time", C.c_double),
+        ("ccd_solver_time", C.c_double),
+        ("ccd_broad_phase_time", C.c_double),
+        ("ccd_narrow_phase_time", C.c_double),
+        ("ccd_world_time_max", C.c_double),
     ]
 
     def as_dict(self):

@@ -68,38 +68,6 @@ __device__ __forceinline__ void ccd_sweep_box(const World& w, uint32_t c) {
     w.ccd.sw_max[c] = make_float4(np_max(b0[0], b1[0]), np_max(b0[1], b1[1]), np_max(b0[2], b1[2]), 0.0f);
 }
 
-// Appends to out (up to cap) the colliders d of the world's segment
-// order[ws, ws + wn) with keep(d), in segment (slot) order, and returns their
-// count; called by the whole block.
-template <class F>
-__device__ uint32_t block_collect(const uint32_t* order, uint32_t ws, uint32_t wn, F keep, uint32_t* out, uint32_t cap,
-                                  uint32_t* s_cnt) {
-    const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    uint32_t total = 0;
-    for (uint32_t base = 0; base < wn; base += blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
-        uint32_t d = 0;
-        bool f = false;
-        if (i < wn) {
-            d = order[ws + i];
-            f = keep(d);
-        }
-        const uint32_t bal = __ballot_sync(0xffffffffu, f);
-        if (lane == 0) s_cnt[warp] = __popc(bal);
-        __syncthreads();
-        uint32_t off = total, chunk = 0;
-        for (uint32_t k = 0; k < nw; ++k) {
-            if (k < warp) off += s_cnt[k];
-            chunk += s_cnt[k];
-        }
-        off += __popc(bal & ((1u << lane) - 1u));
-        if (f && off < cap) out[off] = d;
-        total += chunk;
-        __syncthreads();
-    }
-    return total;
-}
-
 // The collider's core, pose on its body and reach from the body's centre of mass.
 __device__ __forceinline__ ccd::Shape ccd_shape(const World& w, uint32_t c) {
     ccd::Shape s;
@@ -407,7 +375,19 @@ struct CcdState {
     uint32_t part[kCcdThreads];
     uint32_t col_start[kCcdColours + 1];
     uint32_t col_fill[kCcdColours];
+    unsigned long long t_mark, t_acc[4];
 };
+
+enum : int { CCD_T_TOI = 0, CCD_T_SOLVER = 1, CCD_T_BROAD = 2, CCD_T_NARROW = 3 };
+// Profile mode: the time since the last mark goes to `part` (thread 0 keeps
+// the block's sums).
+__device__ __forceinline__ void ccd_mark(CcdState& st, const StepParams& p, int part) {
+    if (p.profile && threadIdx.x == 0) {
+        const unsigned long long t = global_ns();
+        st.t_acc[part] += t - st.t_mark;
+        st.t_mark = t;
+    }
+}
 
 // Exclusive prefix sums of a[0, n) in place, by the whole block; returns
 // the total.
@@ -446,55 +426,127 @@ __device__ __forceinline__ unsigned long long ccd_priority(uint32_t base, const 
     return ((unsigned long long)pair_hash22(l1, l2) << 42) | ((unsigned long long)l1 << 21) | (unsigned long long)l2;
 }
 
-// The colliders interacting with c during CCD, in slot order, into nbr
-// (tmp: scratch of the same size); returns their count (block-uniform; above
-// cap when they do not fit). The broad-phase partners come from the step's
-// pair list; the swept-box partners (not already there) from the world's
-// colliders when c has CCD enabled, else from the world's CCD colliders.
-__device__ uint32_t ccd_neighbours(const World& w, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t c, uint32_t* nbr,
-                                   uint32_t* tmp, uint32_t cap, CcdState& st) {
+// Is d (a collider of c's world) a swept-box partner of c: one of them with
+// CCD, boxes apart now (so not in the step's pair list), swept boxes
+// overlapping? The swept boxes are compared first: most colliders fail there.
+__device__ __forceinline__ bool ccd_swept_partner(const World& w, uint32_t c, uint32_t bc, float4 smn, float4 smx,
+                                                  uint32_t d) {
     const Ccd& cd = w.ccd;
+    if (d == c) return false;
+    const float4 tmn = cd.sw_min[d], tmx = cd.sw_max[d];
+    if (!(smn.x <= tmx.x && tmn.x <= smx.x && smn.y <= tmx.y && tmn.y <= smx.y && smn.z <= tmx.z && tmn.z <= smx.z))
+        return false;
+    if (!(w.c.info[d] & CI_ALIVE)) return false;
+    const uint32_t bd = ccd_body_of(w, d);
+    if (bc == bd || w.b.world[bc] != w.b.world[bd]) return false;
+    if (!ccd_dynamic(w, bc) && !ccd_dynamic(w, bd)) return false;
+    if (!ccd_enabled(w, c) && !ccd_enabled(w, d)) return false;
+    const float4 amn = w.c.aabb_min[c], amx = w.c.aabb_max[c], bmn = w.c.aabb_min[d], bmx = w.c.aabb_max[d];
+    return !(amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z && bmn.z <= amx.z);
+}
+
+// Which of c's partners a TOI search takes: the first search takes a pair of
+// two CCD colliders from the smaller one only; a resweep skips pairs without
+// CCD and pairs of two still bodies.
+enum : int { CAND_PREDICT = 0, CAND_RESWEEP = 1 };
+__device__ __forceinline__ bool ccd_keep(const World& w, int mode, uint32_t c, uint32_t d) {
+    if (mode == CAND_PREDICT) return !(ccd_enabled(w, d) && d < c);
+    const uint32_t ch1 = c < d ? c : d, ch2 = c < d ? d : c;
+    const uint32_t x1 = ccd_body_of(w, ch1), x2 = ccd_body_of(w, ch2);
+    const bool s1 = (w.ccd.bflag[x1] & 1u) || !ccd_dynamic(w, x1), s2 = (w.ccd.bflag[x2] & 1u) || !ccd_dynamic(w, x2);
+    return !((!ccd_enabled(w, ch1) && !ccd_enabled(w, ch2)) || (s1 && s2));
+}
+
+// One warp: c's partners during CCD that `mode` keeps, counted, or with `out`
+// written there as (c, d) in slot order of d. The partners are the step's
+// broad-phase pairs of c and the swept-box partners, taken from the world's
+// colliders when c has CCD, else from the world's CCD colliders.
+__device__ uint32_t ccd_warp_partners(const World& w, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t c, int mode,
+                                      uint2* out) {
+    const Ccd& cd = w.ccd;
+    const uint32_t lane = threadIdx.x & 31u;
     const uint32_t bc = ccd_body_of(w, c);
-    auto swept = [&](uint32_t d) {
-        if (d == c || !(w.c.info[d] & CI_ALIVE)) return false;
-        const uint32_t bd = ccd_body_of(w, d);
-        if (bc == bd || w.b.world[bc] != w.b.world[bd]) return false;
-        if (!ccd_dynamic(w, bc) && !ccd_dynamic(w, bd)) return false;
-        if (!ccd_enabled(w, c) && !ccd_enabled(w, d)) return false;
-        const float4 amn = w.c.aabb_min[c], amx = w.c.aabb_max[c], bmn = w.c.aabb_min[d], bmx = w.c.aabb_max[d];
-        if (amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z && bmn.z <= amx.z)
-            return false;   // a broad-phase pair, listed already
-        const float4 smn = cd.sw_min[c], smx = cd.sw_max[c], tmn = cd.sw_min[d], tmx = cd.sw_max[d];
-        return smn.x <= tmx.x && tmn.x <= smx.x && smn.y <= tmx.y && tmn.y <= smx.y && smn.z <= tmx.z && tmn.z <= smx.z;
-    };
-    const uint32_t ns = ccd_enabled(w, c)
-                            ? block_collect(cd.order, ws, wn, swept, tmp, cap, st.cnt)
-                            : block_collect(cd.ccd_list, cd.ccd_wstart[wd], cd.ccd_wstart[wd + 1] - cd.ccd_wstart[wd],
-                                            swept, tmp, cap, st.cnt);
-    if (threadIdx.x == 0) {
-        const uint32_t a0 = cd.adj_start[c], a1 = cd.adj_start[c + 1];
-        uint32_t n = 0;
-        if (ns > cap || (a1 - a0) + ns > cap) {
-            n = cap + 1u;
-        } else {
-            uint32_t i = a0, j = 0;
-            while (i < a1 || j < ns) {
-                const uint32_t x = i < a1 ? cd.adj_list[i] : 0xffffffffu, y = j < ns ? tmp[j] : 0xffffffffu;
-                if (x < y) {
-                    nbr[n++] = x;
-                    ++i;
-                } else {
-                    nbr[n++] = y;
-                    ++j;
-                }
-            }
+    uint32_t n = 0;
+    const uint32_t a0 = cd.adj_start[c], a1 = cd.adj_start[c + 1];
+    for (uint32_t base = a0; base < a1; base += 32u) {
+        const uint32_t i = base + lane;
+        uint32_t d = 0;
+        bool f = false;
+        if (i < a1) {
+            d = cd.adj_list[i];
+            f = ccd_keep(w, mode, c, d);
         }
-        st.n = n;
+        const uint32_t bal = __ballot_sync(0xffffffffu, f);
+        if (out && f) out[n + __popc(bal & ((1u << lane) - 1u))] = make_uint2(c, d);
+        n += __popc(bal);
     }
-    __syncthreads();
-    const uint32_t n = st.n;
-    __syncthreads();
+    const float4 smn = cd.sw_min[c], smx = cd.sw_max[c];
+    const bool all = ccd_enabled(w, c);
+    const uint32_t* src = all ? cd.order + ws : cd.ccd_list + cd.ccd_wstart[wd];
+    const uint32_t sn = all ? wn : cd.ccd_wstart[wd + 1] - cd.ccd_wstart[wd];
+    for (uint32_t base = 0; base < sn; base += 32u) {
+        const uint32_t i = base + lane;
+        uint32_t d = 0;
+        bool f = false;
+        if (i < sn) {
+            d = src[i];
+            f = ccd_swept_partner(w, c, bc, smn, smx, d) && ccd_keep(w, mode, c, d);
+        }
+        const uint32_t bal = __ballot_sync(0xffffffffu, f);
+        if (out && f) out[n + __popc(bal & ((1u << lane) - 1u))] = make_uint2(c, d);
+        n += __popc(bal);
+    }
+    if (out) {
+        // Both runs are in slot order: merge them by insertion.
+        __syncwarp();
+        if (lane == 0)
+            for (uint32_t a = 1; a < n; ++a) {
+                const uint2 x = out[a];
+                uint32_t b = a;
+                while (b > 0 && out[b - 1].y > x.y) {
+                    out[b] = out[b - 1];
+                    --b;
+                }
+                out[b] = x;
+            }
+        __syncwarp();
+    }
     return n;
+}
+
+// The pairs a TOI search takes for the colliders src[0, ns), in that order
+// and each collider's partners in slot order, handed to `batch(cand, n)` in
+// runs that fit `cap` (cand: the run, n: its length; every thread calls it).
+// cnt: ns + 1 words of scratch. Returns false when one collider's pairs do
+// not fit.
+template <class Batch>
+__device__ bool ccd_candidates(const World& w, uint32_t wd, uint32_t ws, uint32_t wn, const uint32_t* src, uint32_t ns,
+                               int mode, uint32_t* cnt, uint2* cand, uint32_t cap, CcdState& st, Batch batch) {
+    const uint32_t warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    for (uint32_t k = warp; k < ns; k += nw) {
+        const uint32_t n = ccd_warp_partners(w, wd, ws, wn, src[k], mode, nullptr);
+        if ((threadIdx.x & 31u) == 0) cnt[k] = n;
+    }
+    if (threadIdx.x == 0) cnt[ns] = 0u;
+    __syncthreads();
+    block_scan(cnt, ns + 1, st);
+    for (uint32_t k0 = 0; k0 < ns;) {
+        if (threadIdx.x == 0) {
+            uint32_t k1 = k0;
+            while (k1 < ns && cnt[k1 + 1] - cnt[k0] <= cap) ++k1;
+            st.n = k1;
+        }
+        __syncthreads();
+        const uint32_t k1 = st.n;
+        __syncthreads();
+        if (k1 == k0) return false;
+        for (uint32_t k = k0 + warp; k < k1; k += nw)
+            ccd_warp_partners(w, wd, ws, wn, src[k], mode, cand + (cnt[k] - cnt[k0]));
+        __syncthreads();
+        batch(cand, cnt[k1] - cnt[k0]);
+        k0 = k1;
+    }
+    return true;
 }
 enum : uint32_t { PRED_NONE = 0, PRED_IMPACTS = 1, PRED_AFTER = 2 };
 
@@ -505,7 +557,6 @@ enum : uint32_t { PRED_NONE = 0, PRED_IMPACTS = 1, PRED_AFTER = 2 };
 __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t wd, uint32_t ws, uint32_t wn, uint32_t rb,
                             uint32_t rcap, CcdState& st) {
     const Ccd& cd = w.ccd;
-    uint32_t* nbr = cd.nbr + rb;
     float2* tres = cd.tres + rb;
     CcdToi* heap = cd.heap + rb;
     CcdToi* imp = cd.impacts + rb;
@@ -517,41 +568,40 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t wd, ui
     }
     __syncthreads();
     // The CCD colliders' pairs, each once, in slot order.
-    for (uint32_t i = 0; i < wn; ++i) {
-        const uint32_t c = cd.order[ws + i];
-        if (!ccd_enabled(w, c)) continue;
-        const uint32_t n = ccd_neighbours(w, wd, ws, wn, c, nbr, cd.nbr2 + rb, rcap, st);
-        if (n > rcap) {
-            if (threadIdx.x == 0) st.stop = 1;
-            break;
-        }
-        for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-            const uint32_t d = nbr[j];
-            tres[j] = (ccd_enabled(w, d) && d < c) ? make_float2(-2.0f, 0.0f)
-                                                   : ccd_toi(w, p, c < d ? c : d, c < d ? d : c, p.dt);
-        }
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            for (uint32_t j = 0; j < n && !st.stop; ++j) {
-                const float2 r = tres[j];
-                if (r.x < 0.0f) continue;
-                if (r.x > st.min_overstep - r.y) continue;   // beyond this search's end
-                const float toi = r.y + r.x;
-                if (toi > st.end_time) {
-                    st.min_overstep = st.min_overstep < toi ? st.min_overstep : toi;
-                } else {
-                    st.min_overstep = st.end_time;
-                    if (st.nheap >= rcap) {
-                        st.stop = 1;
-                        break;
+    uint2* cand = cd.res + rb;
+    const bool fits = ccd_candidates(
+        w, wd, ws, wn, cd.ccd_list + cd.ccd_wstart[wd], cd.ccd_wstart[wd + 1] - cd.ccd_wstart[wd], CAND_PREDICT,
+        cd.nbr2 + rb, cand, rcap, st, [&](const uint2* cl, uint32_t n) {
+            ccd_mark(st, p, CCD_T_BROAD);
+            for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
+                const uint32_t c = cl[j].x, d = cl[j].y;
+                tres[j] = ccd_toi(w, p, c < d ? c : d, c < d ? d : c, p.dt);
+            }
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                for (uint32_t j = 0; j < n && !st.stop; ++j) {
+                    const float2 r = tres[j];
+                    if (r.x < 0.0f) continue;
+                    if (r.x > st.min_overstep - r.y) continue;   // beyond this search's end
+                    const float toi = r.y + r.x;
+                    if (toi > st.end_time) {
+                        st.min_overstep = st.min_overstep < toi ? st.min_overstep : toi;
+                    } else {
+                        st.min_overstep = st.end_time;
+                        if (st.nheap >= rcap) {
+                            st.stop = 1;
+                            break;
+                        }
+                        const uint32_t c = cl[j].x, d = cl[j].y;
+                        heap[st.nheap++] = CcdToi{toi, c < d ? c : d, c < d ? d : c, st.seq++};
                     }
-                    const uint32_t d = nbr[j];
-                    heap[st.nheap++] = CcdToi{toi, c < d ? c : d, c < d ? d : c, st.seq++};
                 }
             }
-        }
-        __syncthreads();
-    }
+            __syncthreads();
+            ccd_mark(st, p, CCD_T_TOI);
+        });
+    if (threadIdx.x == 0 && !fits) st.stop = 1;
+    __syncthreads();
     if (threadIdx.x == 0) {
         if (st.stop) st.result = PRED_NONE;
         else if (st.min_overstep == p.dt && st.nheap == 0) st.result = PRED_NONE;
@@ -601,31 +651,31 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t wd, ui
         if (cur == 0xfffffffeu) continue;
         const CcdToi e = heap[cur];
         // Resweep every pair of the frozen bodies' colliders.
-        for (int side = 0; side < 2; ++side) {
-            const uint32_t fb = ccd_body_of(w, side == 0 ? e.c1 : e.c2);
-            if (!ccd_dynamic(w, fb)) continue;
-            for (uint32_t q = cd.bc_start[fb]; q < cd.bc_start[fb + 1]; ++q) {
-                const uint32_t cc = cd.bc_list[q];
-                const uint32_t n = ccd_neighbours(w, wd, ws, wn, cc, nbr, cd.nbr2 + rb, rcap, st);
-                if (n > rcap) {
-                    if (threadIdx.x == 0) st.stop = 1;
-                    break;
-                }
+        uint32_t* src = cd.stack + rb;
+        if (threadIdx.x == 0) {
+            uint32_t ns = 0;
+            for (int side = 0; side < 2; ++side) {
+                const uint32_t fb = ccd_body_of(w, side == 0 ? e.c1 : e.c2);
+                if (!ccd_dynamic(w, fb)) continue;
+                for (uint32_t q = cd.bc_start[fb]; q < cd.bc_start[fb + 1]; ++q) src[ns++] = cd.bc_list[q];
+            }
+            st.nstack = ns;
+        }
+        __syncthreads();
+        ccd_mark(st, p, CCD_T_TOI);
+        const bool ok = ccd_candidates(
+            w, wd, ws, wn, src, st.nstack, CAND_RESWEEP, cd.nbr2 + rb, cand, rcap, st, [&](const uint2* cl, uint32_t n) {
+                ccd_mark(st, p, CCD_T_BROAD);
                 for (uint32_t j = threadIdx.x; j < n; j += blockDim.x) {
-                    const uint32_t d = nbr[j];
-                    const uint32_t ch1 = cc < d ? cc : d, ch2 = cc < d ? d : cc;
-                    const uint32_t x1 = ccd_body_of(w, ch1), x2 = ccd_body_of(w, ch2);
-                    const bool s1 = (cd.bflag[x1] & 1u) || !ccd_dynamic(w, x1), s2 = (cd.bflag[x2] & 1u) || !ccd_dynamic(w, x2);
-                    if ((!ccd_enabled(w, ch1) && !ccd_enabled(w, ch2)) || (s1 && s2)) tres[j] = make_float2(-2.0f, 0.0f);
-                    else tres[j] = ccd_toi(w, p, ch1, ch2, st.end_time);
+                    const uint32_t c = cl[j].x, d = cl[j].y;
+                    tres[j] = ccd_toi(w, p, c < d ? c : d, c < d ? d : c, st.end_time);
                 }
                 __syncthreads();
                 if (threadIdx.x == 0) {
                     for (uint32_t j = 0; j < n && !st.stop; ++j) {
                         const float2 r = tres[j];
-                        if (r.x == -2.0f) continue;
-                        const uint32_t d = nbr[j];
-                        const uint32_t ch1 = cc < d ? cc : d, ch2 = cc < d ? d : cc;
+                        const uint32_t c = cl[j].x, d = cl[j].y;
+                        const uint32_t ch1 = c < d ? c : d, ch2 = c < d ? d : c;
                         for (uint32_t k = 0; k < st.nheap; ++k)
                             if (heap[k].c1 == ch1 && heap[k].c2 == ch2) heap[k].seq |= kTocSuperseded;
                         if (r.x < 0.0f) continue;
@@ -637,8 +687,10 @@ __device__ void ccd_predict(const World& w, const StepParams& p, uint32_t wd, ui
                     }
                 }
                 __syncthreads();
-            }
-        }
+                ccd_mark(st, p, CCD_T_TOI);
+            });
+        if (threadIdx.x == 0 && !ok) st.stop = 1;
+        __syncthreads();
         if (threadIdx.x == 0) {
             if (st.nimp < rcap) imp[st.nimp++] = e;
             else st.stop = 1;
@@ -723,29 +775,17 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
             };
             for (uint32_t q = cd.adj_start[c]; q < cd.adj_start[c + 1]; ++q) consider(cd.adj_list[q]);
             const uint32_t bc = ccd_body_of(w, c);
-            auto swept = [&](uint32_t d) {
-                if (d == c || !(w.c.info[d] & CI_ALIVE)) return false;
-                const uint32_t bd = ccd_body_of(w, d);
-                if (bc == bd || w.b.world[bc] != w.b.world[bd]) return false;
-                if (!ccd_dynamic(w, bc) && !ccd_dynamic(w, bd)) return false;
-                if (!ccd_enabled(w, c) && !ccd_enabled(w, d)) return false;
-                const float4 amn = w.c.aabb_min[c], amx = w.c.aabb_max[c], bmn = w.c.aabb_min[d], bmx = w.c.aabb_max[d];
-                if (amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z &&
-                    bmn.z <= amx.z)
-                    return false;
-                const float4 smn = cd.sw_min[c], smx = cd.sw_max[c], tmn = cd.sw_min[d], tmx = cd.sw_max[d];
-                return smn.x <= tmx.x && tmn.x <= smx.x && smn.y <= tmx.y && tmn.y <= smx.y && smn.z <= tmx.z &&
-                       tmn.z <= smx.z;
-            };
+            const float4 smn = cd.sw_min[c], smx = cd.sw_max[c];
             if (ccd_enabled(w, c)) {
                 for (uint32_t k = 0; k < wn; ++k)
-                    if (swept(cd.order[ws + k])) consider(cd.order[ws + k]);
+                    if (ccd_swept_partner(w, c, bc, smn, smx, cd.order[ws + k])) consider(cd.order[ws + k]);
             } else {
                 for (uint32_t k = cd.ccd_wstart[wd]; k < cd.ccd_wstart[wd + 1]; ++k)
-                    if (swept(cd.ccd_list[k])) consider(cd.ccd_list[k]);
+                    if (ccd_swept_partner(w, c, bc, smn, smx, cd.ccd_list[k])) consider(cd.ccd_list[k]);
             }
         }
         __syncthreads();
+        ccd_mark(st, p, CCD_T_BROAD);
         const uint32_t np_ = st.n;
         if (np_ > rcap) {
             if (threadIdx.x == 0) st.stop = 1;
@@ -765,6 +805,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         }
         if (threadIdx.x == 0) st.nnext = 0;
         __syncthreads();
+        ccd_mark(st, p, CCD_T_SOLVER);
         // Its contacts; a pair with contacts explores its other body.
         for (uint32_t i = threadIdx.x; i < np_; i += blockDim.x) {
             const uint2 pr = pairs[i];
@@ -786,6 +827,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
             else st.stop = 1;
         }
         __syncthreads();
+        ccd_mark(st, p, CCD_T_NARROW);
         // The next level: the colliders of the bodies explored.
         for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) cd.cflag[front[i]] &= ~2u;
         if (threadIdx.x == 0) st.nstack = 0;
@@ -989,6 +1031,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         if (cd.bc_list[cd.bc_start[bb]] != c) continue;   // one collider per body acts
         if ((w.b.info[bb] & BI_CHANGED) && ccd_dynamic(w, bb)) body_update_dynamics(w.b, bb, dts);
     }
+    ccd_mark(st, p, CCD_T_SOLVER);
     if (threadIdx.x == 0) {
         w.ccd.wdts[wd] = dts;
         atomicAdd(&w.ctl->ccd_substeps, 1u);
@@ -1014,6 +1057,8 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p
         st.end_time = 0.0f;
         st.last_iter = 0;
         st.epoch = 0;
+        st.t_mark = p.profile ? global_ns() : 0ull;
+        for (int k = 0; k < 4; ++k) st.t_acc[k] = 0ull;
     }
     for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) cd.bepoch[ccd_body_of(w, cd.order[ws + i])] = 0u;
     __syncthreads();
@@ -1030,6 +1075,7 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p
         }
         for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) ccd_sweep_box(w, cd.order[ws + i]);
         __syncthreads();
+        ccd_mark(st, p, CCD_T_BROAD);
         ccd_predict(w, p, wd, ws, wn, rb, rcap, st);
         if (st.result == PRED_AFTER) {
             if (threadIdx.x == 0) {
@@ -1055,6 +1101,16 @@ __global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p
             if ((cd.bflag[b] & 1u) && bi_status(w.b.info[b]) != 1u) ccd_clamp(w, b);
         }
         break;
+    }
+    __syncthreads();
+    ccd_mark(st, p, CCD_T_SOLVER);
+    if (p.profile && threadIdx.x == 0) {
+        unsigned long long total = 0ull;
+        for (int k = 0; k < 4; ++k) {
+            atomicAdd(&w.ctl->ccd_ns[k], st.t_acc[k]);
+            total += st.t_acc[k];
+        }
+        atomicMax(&w.ctl->ccd_max_ns, total);
     }
 }
 
@@ -1104,6 +1160,8 @@ __global__ void k_ccd_begin(World w) {
         w.ctl->ccd_mcount = 0;
         w.ctl->ccd_substeps = 0;
         w.ctl->ccd_impacts = 0;
+        for (int k = 0; k < 4; ++k) w.ctl->ccd_ns[k] = 0ull;
+        w.ctl->ccd_max_ns = 0ull;
     }
 }
 

@@ -2097,6 +2097,13 @@ npgpu_status npgpu_get_counters(npgpu_world* w, npgpu_counters* out) {
         k.velocity_wait_ms = (double)c.wait_ns * 1e-6;
         k.velocity_kernel_ms = (double)c.t_phase[0] * 1e-6;
         k.velocity_tasks = c.tasks;
+        if (w->last_step_ccd) {
+            k.ccd_toi_computation_time = (double)c.ccd_ns[0] * 1e-6;
+            k.ccd_solver_time = (double)c.ccd_ns[1] * 1e-6;
+            k.ccd_broad_phase_time = (double)c.ccd_ns[2] * 1e-6;
+            k.ccd_narrow_phase_time = (double)c.ccd_ns[3] * 1e-6;
+            k.ccd_world_time_max = (double)c.ccd_max_ns * 1e-6;
+        }
     }
     *out = k;
     return NPGPU_OK;

@@ -242,6 +242,8 @@ struct Control {
     uint32_t ccd_mcount;             // CCD island manifolds taken from the pool this step
     uint32_t ccd_substeps, ccd_impacts;
     uint32_t pad3;
+    unsigned long long ccd_ns[4];    // profile mode: CCD time by part (toi, solver, broad, narrow), summed over worlds
+    unsigned long long ccd_max_ns;   // ... and the longest world's
 };
 
 struct StepParams {

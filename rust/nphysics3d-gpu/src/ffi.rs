@@ -195,6 +195,11 @@ pub struct npgpu_counters {
     pub ccd_substeps: u32,
     pub ccd_impacts: u32,
     pub reserved: u32,
+    pub ccd_toi_computation_time: f64,
+    pub ccd_solver_time: f64,
+    pub ccd_broad_phase_time: f64,
+    pub ccd_narrow_phase_time: f64,
+    pub ccd_world_time_max: f64,
 }
 
 #[repr(C)]
