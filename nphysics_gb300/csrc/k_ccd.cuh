@@ -240,14 +240,16 @@ __device__ void ccd_rows(const World& w, const StepParams& p, CcdManifold& m, fl
     }
 }
 
-// NonlinearSORProx::solve_unilateral for one island contact (the position
-// solver's contact arithmetic, on the bodies' poses in memory).
-__device__ void ccd_position_contact(const World& w, const StepParams& p, const CcdManifold& m, const CcdContact& K) {
+// NonlinearSORProx::solve_unilateral for an island manifold's contacts in
+// order (the position solver's contact arithmetic).
+__device__ void ccd_position_manifold(const World& w, const StepParams& p, const CcdManifold& m) {
     const Bodies& b = w.b;
     const Colliders& c = w.c;
     const uint32_t bb1 = ccd_body_of(w, m.c1), bb2 = ccd_body_of(w, m.c2);
     const uint32_t i1 = b.info[bb1], i2 = b.info[bb2];
     const bool d1 = bi_status(i1) == 2u, d2 = bi_status(i2) == 2u;
+    // The manifold's two bodies stay in registers over its contacts (no
+    // other manifold of its colour moves them).
     np::V t1 = v3(b.pos_t[bb1]), t2 = v3(b.pos_t[bb2]);
     np::Q q1 = q4(b.pos_q[bb1]), q2 = q4(b.pos_q[bb2]);
     np::V com1 = v3(b.com[bb1]), com2 = v3(b.com[bb2]);
@@ -256,44 +258,61 @@ __device__ void ccd_position_contact(const World& w, const StepParams& p, const 
     const float4 pp1 = c.params[m.c1], pp2 = c.params[m.c2];
     const float dil1 = (sh1 == SHAPE_BALL || sh1 == SHAPE_CAPSULE ? pp1.x : 0.0f) + c.margin[m.c1];
     const float dil2 = (sh2 == SHAPE_BALL || sh2 == SHAPE_CAPSULE ? pp2.x : 0.0f) + c.margin[m.c2];
-    const uint32_t key = __float_as_uint(K.w1.w);
-    const int f1 = (int)(key / 26u), f2 = (int)(key % 26u);
-    const np::Iso m1 = np::iso_mul(np::Iso{t1, q1}, wrt1), m2 = np::iso_mul(np::Iso{t2, q2}, wrt2);
-    const np::V n0 = np::qrot(m1.q, v3(K.nl));
-    const Geom g = kinematic_contact(feature_of(sh1, np::mk(pp1.x, pp1.y, pp1.z), f1), m1, dil1,
-                                     feature_of(sh2, np::mk(pp2.x, pp2.y, pp2.z), f2), m2, dil2, n0);
-    float rhs = (-g.depth + p.allowed_linear_error) * p.erp;
-    const float lim = -p.max_linear_correction;
-    rhs = (rhs < lim) ? lim : rhs;
-    if (rhs >= 0.0f) return;
-    float inv_r = 0.0f, dummy = 0.0f;
-    float J1[6], J2[6], W1[6], W2[6];
+    BodyView v1, v2;
     if (d1) {
-        BodyView v;
-        v.com = com1; v.inv_mass = b.inv_mass[bb1]; v.inv_I = load_m9(b.inv_I + 9 * bb1); v.info = i1;
-        v.lin = v.ang = v.acc_lin = v.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
-        fill_row_side(v, g.w1, np::neg(g.n), J1, W1, inv_r, dummy, false, p.dt);
+        v1.inv_mass = b.inv_mass[bb1]; v1.inv_I = load_m9(b.inv_I + 9 * bb1); v1.info = i1;
+        v1.lin = v1.ang = v1.acc_lin = v1.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
     }
     if (d2) {
-        BodyView v;
-        v.com = com2; v.inv_mass = b.inv_mass[bb2]; v.inv_I = load_m9(b.inv_I + 9 * bb2); v.info = i2;
-        v.lin = v.ang = v.acc_lin = v.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
-        fill_row_side(v, g.w2, g.n, J2, W2, inv_r, dummy, false, p.dt);
+        v2.inv_mass = b.inv_mass[bb2]; v2.inv_I = load_m9(b.inv_I + 9 * bb2); v2.info = i2;
+        v2.lin = v2.ang = v2.acc_lin = v2.acc_ang = np::mk(0.0f, 0.0f, 0.0f);
     }
-    if (inv_r == 0.0f) return;
-    const float r = 1.0f / inv_r;
-    const float impulse = -rhs * r;
-    if (d1) {
-        for (int k = 0; k < 6; ++k) W1[k] = W1[k] * impulse;
-        apply_displacement(t1, q1, com1, v3(b.local_com[bb1]), np::mk(W1[0], W1[1], W1[2]), np::mk(W1[3], W1[4], W1[5]));
+    const np::V lc1 = d1 ? v3(b.local_com[bb1]) : np::mk(0.0f, 0.0f, 0.0f);
+    const np::V lc2 = d2 ? v3(b.local_com[bb2]) : np::mk(0.0f, 0.0f, 0.0f);
+    bool moved1 = false, moved2 = false;
+    for (uint32_t kk = 0; kk < m.nc; ++kk) {
+        const CcdContact& K = m.k[kk];
+        const uint32_t key = __float_as_uint(K.w1.w);
+        const int f1 = (int)(key / 26u), f2 = (int)(key % 26u);
+        const np::Iso m1 = np::iso_mul(np::Iso{t1, q1}, wrt1), m2 = np::iso_mul(np::Iso{t2, q2}, wrt2);
+        const np::V n0 = np::qrot(m1.q, v3(K.nl));
+        const Geom g = kinematic_contact(feature_of(sh1, np::mk(pp1.x, pp1.y, pp1.z), f1), m1, dil1,
+                                         feature_of(sh2, np::mk(pp2.x, pp2.y, pp2.z), f2), m2, dil2, n0);
+        float rhs = (-g.depth + p.allowed_linear_error) * p.erp;
+        const float lim = -p.max_linear_correction;
+        rhs = (rhs < lim) ? lim : rhs;
+        if (rhs >= 0.0f) continue;
+        float inv_r = 0.0f, dummy = 0.0f;
+        float J1[6], J2[6], W1[6], W2[6];
+        if (d1) {
+            v1.com = com1;
+            fill_row_side(v1, g.w1, np::neg(g.n), J1, W1, inv_r, dummy, false, p.dt);
+        }
+        if (d2) {
+            v2.com = com2;
+            fill_row_side(v2, g.w2, g.n, J2, W2, inv_r, dummy, false, p.dt);
+        }
+        if (inv_r == 0.0f) continue;
+        const float r = 1.0f / inv_r;
+        const float impulse = -rhs * r;
+        if (d1) {
+            for (int k = 0; k < 6; ++k) W1[k] = W1[k] * impulse;
+            apply_displacement(t1, q1, com1, lc1, np::mk(W1[0], W1[1], W1[2]), np::mk(W1[3], W1[4], W1[5]));
+            moved1 = true;
+        }
+        if (d2) {
+            for (int k = 0; k < 6; ++k) W2[k] = W2[k] * impulse;
+            apply_displacement(t2, q2, com2, lc2, np::mk(W2[0], W2[1], W2[2]), np::mk(W2[3], W2[4], W2[5]));
+            moved2 = true;
+        }
+    }
+    if (moved1) {
         b.pos_t[bb1] = f4(t1);
         b.pos_q[bb1] = f4q(q1);
         b.com[bb1] = f4(com1);
         b.info[bb1] |= BI_CHANGED;
     }
-    if (d2) {
-        for (int k = 0; k < 6; ++k) W2[k] = W2[k] * impulse;
-        apply_displacement(t2, q2, com2, v3(b.local_com[bb2]), np::mk(W2[0], W2[1], W2[2]), np::mk(W2[3], W2[4], W2[5]));
+    if (moved2) {
         b.pos_t[bb2] = f4(t2);
         b.pos_q[bb2] = f4q(q2);
         b.com[bb2] = f4(com2);
@@ -763,25 +782,27 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         const uint32_t nf = st.nstack;
         if (threadIdx.x == 0) st.n = 0;
         __syncthreads();
-        // The level's pairs.
-        for (uint32_t i = threadIdx.x; i < nf; i += blockDim.x) {
-            const uint32_t c = front[i];
-            auto consider = [&](uint32_t d) {
-                const uint32_t f = cd.cflag[d];
-                if ((f & 1u) && !(f & 2u)) return;   // its pairs were a former level's
-                if ((f & 2u) && d < c) return;       // taken from d
-                const uint32_t at = atomicAdd(&st.n, 1u);
-                if (at < rcap) pairs[at] = make_uint2(c < d ? c : d, c < d ? d : c);
-            };
-            for (uint32_t q = cd.adj_start[c]; q < cd.adj_start[c + 1]; ++q) consider(cd.adj_list[q]);
-            const uint32_t bc = ccd_body_of(w, c);
-            const float4 smn = cd.sw_min[c], smx = cd.sw_max[c];
-            if (ccd_enabled(w, c)) {
-                for (uint32_t k = 0; k < wn; ++k)
-                    if (ccd_swept_partner(w, c, bc, smn, smx, cd.order[ws + k])) consider(cd.order[ws + k]);
-            } else {
-                for (uint32_t k = cd.ccd_wstart[wd]; k < cd.ccd_wstart[wd + 1]; ++k)
-                    if (ccd_swept_partner(w, c, bc, smn, smx, cd.ccd_list[k])) consider(cd.ccd_list[k]);
+        // The level's pairs: a warp per frontier collider, its lanes over the
+        // collider's step pairs and swept-box candidates.
+        {
+            const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+            for (uint32_t i = warp; i < nf; i += nw) {
+                const uint32_t c = front[i];
+                auto consider = [&](uint32_t d) {
+                    const uint32_t f = cd.cflag[d];
+                    if ((f & 1u) && !(f & 2u)) return;   // its pairs were a former level's
+                    if ((f & 2u) && d < c) return;       // taken from d
+                    const uint32_t at = atomicAdd(&st.n, 1u);
+                    if (at < rcap) pairs[at] = make_uint2(c < d ? c : d, c < d ? d : c);
+                };
+                for (uint32_t q = cd.adj_start[c] + lane; q < cd.adj_start[c + 1]; q += 32u) consider(cd.adj_list[q]);
+                const uint32_t bc = ccd_body_of(w, c);
+                const float4 smn = cd.sw_min[c], smx = cd.sw_max[c];
+                const bool all = ccd_enabled(w, c);
+                const uint32_t* src = all ? cd.order + ws : cd.ccd_list + cd.ccd_wstart[wd];
+                const uint32_t sn = all ? wn : cd.ccd_wstart[wd + 1] - cd.ccd_wstart[wd];
+                for (uint32_t k = lane; k < sn; k += 32u)
+                    if (ccd_swept_partner(w, c, bc, smn, smx, src[k])) consider(src[k]);
             }
         }
         __syncthreads();
@@ -895,6 +916,11 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     // bodies, numbered through bepoch).
     uint32_t* bstart = cd.nbr + rb;
     uint32_t* blist = reinterpret_cast<uint32_t*>(pairs);   // 2 rcap words
+    // Per manifold (by place q): its priority, colour and island bodies.
+    unsigned long long* prio = reinterpret_cast<unsigned long long*>(cd.tres + rb);
+    uint32_t* mcol = reinterpret_cast<uint32_t*>(cd.heap + rb);          // rcap words
+    uint2* mbody = reinterpret_cast<uint2*>(mcol + 2 * (size_t)rcap);   // rcap pairs
+    const uint32_t base = cd.order[ws];
     for (uint32_t i = threadIdx.x; i < nisl; i += blockDim.x) {
         cd.bepoch[island[i]] = i;
         bstart[i] = 0u;
@@ -902,12 +928,17 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     if (threadIdx.x == 0) bstart[nisl] = 0u;
     __syncthreads();
     for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
-        CcdManifold& m = cd.pool[mlist[q]];
-        m.colour = 0xffffffffu;
-        for (uint32_t c : {m.c1, m.c2}) {
-            const uint32_t x = ccd_body_of(w, c);
-            if (ccd_dynamic(w, x)) atomicAdd(&bstart[cd.bepoch[x]], 1u);
+        const CcdManifold& m = cd.pool[mlist[q]];
+        prio[q] = ccd_priority(base, m);
+        mcol[q] = 0xffffffffu;
+        uint32_t k[2] = {0xffffffffu, 0xffffffffu};
+        for (int s = 0; s < 2; ++s) {
+            const uint32_t x = ccd_body_of(w, s == 0 ? m.c1 : m.c2);
+            if (!ccd_dynamic(w, x)) continue;
+            k[s] = cd.bepoch[x];
+            atomicAdd(&bstart[k[s]], 1u);
         }
+        mbody[q] = make_uint2(k[0], k[1]);
     }
     __syncthreads();
     block_scan(bstart, nisl + 1, st);
@@ -915,34 +946,31 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     for (uint32_t i = threadIdx.x; i <= nisl; i += blockDim.x) bcur[i] = bstart[i];
     __syncthreads();
     for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
-        const CcdManifold& m = cd.pool[mlist[q]];
-        for (uint32_t c : {m.c1, m.c2}) {
-            const uint32_t x = ccd_body_of(w, c);
-            if (ccd_dynamic(w, x)) blist[atomicAdd(&bcur[cd.bepoch[x]], 1u)] = q;
-        }
+        const uint2 k = mbody[q];
+        if (k.x != 0xffffffffu) blist[atomicAdd(&bcur[k.x], 1u)] = q;
+        if (k.y != 0xffffffffu) blist[atomicAdd(&bcur[k.y], 1u)] = q;
     }
     if (threadIdx.x == 0) st.left = nm;
     __syncthreads();
     // Jones-Plassmann rounds: round r colours the manifolds whose priority
     // is above every uncoloured manifold's on a shared dynamic body.
-    const uint32_t base = cd.order[ws];
     uint32_t ncol = 0;
     for (; st.left > 0 && ncol < kCcdColours; ++ncol) {
         for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
-            const CcdManifold& m = cd.pool[mlist[q]];
             mord[q] = 0u;
-            if (m.colour != 0xffffffffu) continue;
-            const unsigned long long pq = ccd_priority(base, m);
+            if (mcol[q] != 0xffffffffu) continue;
+            const unsigned long long pq = prio[q];
+            const uint2 kb = mbody[q];
             bool top = true;
-            for (uint32_t c : {m.c1, m.c2}) {
-                const uint32_t x = ccd_body_of(w, c);
-                if (!ccd_dynamic(w, x)) continue;
-                const uint32_t k = cd.bepoch[x];
-                for (uint32_t e = bstart[k]; e < bstart[k + 1] && top; ++e) {
+            for (int s = 0; s < 2 && top; ++s) {
+                const uint32_t k = s == 0 ? kb.x : kb.y;
+                if (k == 0xffffffffu) continue;
+                for (uint32_t e = bstart[k]; e < bstart[k + 1]; ++e) {
                     const uint32_t o = blist[e];
-                    if (o == q) continue;
-                    const CcdManifold& mo = cd.pool[mlist[o]];
-                    if (mo.colour == 0xffffffffu && ccd_priority(base, mo) > pq) top = false;
+                    if (o != q && mcol[o] == 0xffffffffu && prio[o] > pq) {
+                        top = false;
+                        break;
+                    }
                 }
             }
             mord[q] = top ? 1u : 0u;
@@ -951,7 +979,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         uint32_t taken = 0;
         for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x)
             if (mord[q]) {
-                cd.pool[mlist[q]].colour = ncol;
+                mcol[q] = ncol;
                 ++taken;
             }
         atomicSub(&st.left, taken);
@@ -968,7 +996,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         if (k < kCcdColours) st.col_fill[k] = 0u;
     }
     __syncthreads();
-    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) atomicAdd(&st.col_start[cd.pool[mlist[q]].colour], 1u);
+    for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) atomicAdd(&st.col_start[mcol[q]], 1u);
     __syncthreads();
     if (threadIdx.x == 0) {
         uint32_t run = 0;
@@ -981,7 +1009,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     __syncthreads();
     for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) {
         // Within a colour the manifolds share no dynamic body: any order.
-        const uint32_t k = cd.pool[mlist[q]].colour;
+        const uint32_t k = mcol[q];
         mord[st.col_start[k] + atomicAdd(&st.col_fill[k], 1u)] = mlist[q];
     }
     __syncthreads();
@@ -994,8 +1022,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     for (uint32_t it = 0; it < cd.max_position_iterations; ++it)
         for (uint32_t k = 0; k < ncol; ++k) {
             for (uint32_t q = st.col_start[k] + threadIdx.x; q < st.col_start[k + 1]; q += blockDim.x) {
-                const CcdManifold& m = cd.pool[mord[q]];
-                for (uint32_t kk = 0; kk < m.nc; ++kk) ccd_position_contact(w, ps, m, m.k[kk]);
+                ccd_position_manifold(w, ps, cd.pool[mord[q]]);
             }
             __syncthreads();
         }
