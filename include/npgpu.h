@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define NPGPU_ABI_VERSION 7u
+#define NPGPU_ABI_VERSION 8u
 
 /* generational_arena::Index (src/object/body_set.rs:178). */
 typedef struct npgpu_handle {
@@ -140,7 +140,8 @@ typedef struct npgpu_collider_desc {
     uint32_t friction_combine;  /* NPGPU_COMBINE_* */
     uint32_t restitution_combine;
     uint32_t shape;             /* NPGPU_SHAPE_* */
-    uint32_t is_sensor;         /* rejected when non-zero */
+    uint32_t is_sensor;         /* ColliderDesc::sensor: proximity events, no contacts; its query limit is
+                                 * linear_prediction alone (collider.rs:542-543); CCD ignores its pairs */
     uint32_t ccd_enabled;       /* Collider::enable_ccd: time-of-impact substeps (MechanicalWorld::solve_ccd) */
 } npgpu_collider_desc;
 
@@ -534,6 +535,24 @@ npgpu_status npgpu_enable_contact_events(npgpu_world* w, uint32_t capacity);
  * than the capacity (the first `capacity` recorded are returned).
  * Replaces GeometricalWorld::contact_events (geometrical_world.rs:373-376). */
 npgpu_status npgpu_contact_events(npgpu_world* w, npgpu_contact_event* out, uint32_t max, uint32_t* count);
+
+/* ncollide3d query::Proximity of a pair with a sensor. */
+enum {
+    NPGPU_PROXIMITY_INTERSECTING = 0,  /* the shapes touch or overlap */
+    NPGPU_PROXIMITY_WITHIN_MARGIN = 1, /* apart by at most the pair's query limits */
+    NPGPU_PROXIMITY_DISJOINT = 2
+};
+/* ProximityEvent: a pair with a sensor whose proximity changed in a
+ * collision-detection pass of the last step. */
+typedef struct npgpu_proximity_event {
+    uint32_t collider1, collider2;   /* collider1 < collider2 */
+    uint32_t prev_status, new_status;  /* NPGPU_PROXIMITY_* */
+} npgpu_proximity_event;
+/* The last step's proximity events (recorded with the contact events, into
+ * the same capacity), by (collider1, collider2) and, for one pair, in the
+ * order of the passes. A pair that leaves the broad phase goes to Disjoint.
+ * Replaces GeometricalWorld::proximity_events (geometrical_world.rs:378-381). */
+npgpu_status npgpu_proximity_events(npgpu_world* w, npgpu_proximity_event* out, uint32_t max, uint32_t* count);
 
 /* Broad phase over caller-provided boxes that allocates nothing. This entry
  * point has no counterpart in the reference: it exists for callers that

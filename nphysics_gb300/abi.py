@@ -11,7 +11,7 @@ import numpy as np
 PKG_DIR = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG_DIR, "_build", "libnpgpu.so")
 
-NPGPU_ABI_VERSION = 7
+NPGPU_ABI_VERSION = 8
 
 # npgpu_status
 OK = 0
@@ -287,6 +287,15 @@ class ContactEvent(C.Structure):
     _fields_ = [("collider1", C.c_uint32), ("collider2", C.c_uint32), ("stopped", C.c_uint32)]
 
 
+# ncollide3d query::Proximity of a pair with a sensor.
+PROXIMITY_INTERSECTING, PROXIMITY_WITHIN_MARGIN, PROXIMITY_DISJOINT = 0, 1, 2
+
+
+class ProximityEvent(C.Structure):
+    _fields_ = [("collider1", C.c_uint32), ("collider2", C.c_uint32), ("prev_status", C.c_uint32),
+                ("new_status", C.c_uint32)]
+
+
 ALL_WORLDS = 0xffffffff
 
 
@@ -346,6 +355,7 @@ def load_library(path=LIB_PATH):
                                                      C.c_uint32, P(C.c_uint32)]),
         "npgpu_enable_contact_events": (C.c_int, [W, C.c_uint32]),
         "npgpu_contact_events": (C.c_int, [W, P(ContactEvent), C.c_uint32, P(C.c_uint32)]),
+        "npgpu_proximity_events": (C.c_int, [W, P(ProximityEvent), C.c_uint32, P(C.c_uint32)]),
         "npgpu_mlp_set": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_get": (C.c_int, [W, P(C.c_float), C.c_uint32]),
         "npgpu_mlp_record": (C.c_int, [W, C.c_uint32]),
@@ -371,7 +381,7 @@ EXPORTED = [
     "npgpu_synchronize", "npgpu_download_bodies", "npgpu_download_mass_properties", "npgpu_get_pairs",
     "npgpu_get_aabbs", "npgpu_get_contacts", "npgpu_get_counters", "npgpu_last_error", "npgpu_find_pairs_static",
     "npgpu_interferences_with_rays", "npgpu_interferences_with_points", "npgpu_interferences_with_aabbs",
-    "npgpu_enable_contact_events", "npgpu_contact_events",
+    "npgpu_enable_contact_events", "npgpu_contact_events", "npgpu_proximity_events",
     "npgpu_autotune", "npgpu_mlp_set", "npgpu_mlp_get", "npgpu_mlp_record", "npgpu_mlp_samples", "npgpu_mlp_load_samples", "npgpu_mlp_train", "npgpu_mlp_grad",
 ]
 

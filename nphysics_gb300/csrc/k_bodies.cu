@@ -156,6 +156,7 @@ __global__ void k_forget_pairs(World w, const uint8_t* flags) {
         }
         w.cur.pair[p] = make_uint2(0xffffffffu, 0xffffffffu);
         w.cur.ncont[p] = 0;
+        w.cur.prox[p] = (uint8_t)PROX_DISJOINT;
     }
 }
 

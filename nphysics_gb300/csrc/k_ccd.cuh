@@ -464,11 +464,12 @@ __device__ __forceinline__ bool ccd_swept_partner(const World& w, uint32_t c, ui
     return !(amn.x <= bmx.x && bmn.x <= amx.x && amn.y <= bmx.y && bmn.y <= amx.y && amn.z <= bmx.z && bmn.z <= amx.z);
 }
 
-// Which of c's partners a TOI search takes: the first search takes a pair of
-// two CCD colliders from the smaller one only; a resweep skips pairs without
-// CCD and pairs of two still bodies.
+// Which of c's partners a TOI search takes: never a pair with a sensor; the
+// first search takes a pair of two CCD colliders from the smaller one only;
+// a resweep skips pairs without CCD and pairs of two still bodies.
 enum : int { CAND_PREDICT = 0, CAND_RESWEEP = 1 };
 __device__ __forceinline__ bool ccd_keep(const World& w, int mode, uint32_t c, uint32_t d) {
+    if ((w.c.info[c] | w.c.info[d]) & CI_SENSOR) return false;   // proximity pairs take no part
     if (mode == CAND_PREDICT) return !(ccd_enabled(w, d) && d < c);
     const uint32_t ch1 = c < d ? c : d, ch2 = c < d ? d : c;
     const uint32_t x1 = ccd_body_of(w, ch1), x2 = ccd_body_of(w, ch2);
@@ -789,6 +790,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
             for (uint32_t i = warp; i < nf; i += nw) {
                 const uint32_t c = front[i];
                 auto consider = [&](uint32_t d) {
+                    if ((w.c.info[c] | w.c.info[d]) & CI_SENSOR) return;   // a proximity pair
                     const uint32_t f = cd.cflag[d];
                     if ((f & 1u) && !(f & 2u)) return;   // its pairs were a former level's
                     if ((f & 2u) && d < c) return;       // taken from d

@@ -358,6 +358,14 @@ __device__ __forceinline__ void emit_event(const World& w, uint32_t c1, uint32_t
     const uint32_t at = atomicAdd(&w.ctl->nevents, 1u);
     if (at < w.events_cap) w.events[at] = make_uint2(c1, c2 | (stopped ? 0x80000000u : 0u));
 }
+// ProximityEvent (ncollide3d, read through GeometricalWorld::proximity_events,
+// geometrical_world.rs:378-381): a pair with a sensor whose proximity changed.
+// Shares the event buffer: bit 30 marks it, bits 26-27 and 28-29 hold the
+// previous and new PROX_* (collider slots stay below 2^26).
+__device__ __forceinline__ void emit_proximity(const World& w, uint32_t c1, uint32_t c2, uint32_t prev, uint32_t now) {
+    const uint32_t at = atomicAdd(&w.ctl->nevents, 1u);
+    if (at < w.events_cap) w.events[at] = make_uint2(c1, c2 | 0x40000000u | (prev << 26) | (now << 28));
+}
 
 // One-shot manifold of pair p, keeping the impulses cached under the same
 // feature key in the pair's previous manifold.
@@ -382,6 +390,24 @@ __device__ __noinline__ void narrow_pair(const World& w, uint32_t p, NarrowTotal
             break;
         }
     }
+    if ((c.info[c1] | c.info[c2]) & CI_SENSOR) {
+        // A proximity pair (ProximityDetector): Intersecting when the shapes
+        // touch or overlap, WithinMargin when the contact generator finds
+        // them within the query limits, Disjoint otherwise. It makes no
+        // contacts.
+        uint32_t st = PROX_DISJOINT;
+        for (int k = 0; k < nk && k < kMaxContacts; ++k) {
+            const float d = out.c[keep[k]].g.depth;
+            if (d >= 0.0f) st = PROX_INTERSECTING;
+            else if (st == PROX_DISJOINT) st = PROX_WITHIN_MARGIN;
+        }
+        const uint32_t was = prev >= 0 ? (uint32_t)w.prev.prox[prev] : PROX_DISJOINT;
+        w.cur.ncont[p] = 0;
+        w.cur.prox[p] = (uint8_t)st;
+        if (w.events != nullptr && st != was) emit_proximity(w, c1, c2, was, st);
+        return;
+    }
+    w.cur.prox[p] = (uint8_t)PROX_DISJOINT;
     uint32_t pkeys[kMaxContacts];
     int pn = 0;
     if (prev >= 0) {
@@ -494,7 +520,8 @@ cudaError_t launch_pairs(const World& w, void* temp, size_t temp_bytes, cudaStre
 }
 
 // Stopped events of the pairs that had contacts in the previous pass and are
-// no longer broad-phase pairs (the pairs present in both passes are handled
+// no longer broad-phase pairs, and proximity events to Disjoint of the
+// sensor pairs that were not Disjoint (the pairs present in both passes are handled
 // by the narrow phase). A pair's owner is the same collider in both passes,
 // so it is looked up among its owner's pairs of this pass.
 __global__ void k_events_vanished(World w) {
@@ -504,13 +531,16 @@ __global__ void k_events_vanished(World w) {
         const uint32_t cs = w.cur.owner_start[a], cn = w.cur.owner_count[a];
         for (uint32_t q = 0; q < qn; ++q) {
             const uint2 o = w.prev.pair[qs + q];
-            if (o.x == 0xffffffffu || w.prev.ncont[qs + q] == 0) continue;
+            const uint32_t was = w.prev.prox[qs + q];
+            if (o.x == 0xffffffffu || (w.prev.ncont[qs + q] == 0 && was == PROX_DISJOINT)) continue;
             bool found = false;
             for (uint32_t r = 0; r < cn && !found; ++r) {
                 const uint2 x = w.cur.pair[cs + r];
                 found = x.x == o.x && x.y == o.y;
             }
-            if (!found) emit_event(w, o.x, o.y, true);
+            if (found) continue;
+            if (was != PROX_DISJOINT) emit_proximity(w, o.x, o.y, was, PROX_DISJOINT);
+            else emit_event(w, o.x, o.y, true);
         }
     }
 }

@@ -532,7 +532,7 @@ static npgpu_status create_buffers(npgpu_world* w) {
     A(c.node_max, 2 * (size_t)Cn); A(c.wide, 5 * (size_t)Cn); A(c.node_slot, 2 * (size_t)Cn); A(c.node_flag, Cn); A(c.leaf_count, Cn); A(c.leaf_offset, Cn);
     A(c.leaf_tmp, (size_t)kLeafCap * Cn);
     for (Pairs* pp : {&w->pa, &w->pb}) {
-        A(pp->pair, P); A(pp->owner_start, Cn); A(pp->owner_count, Cn); A(pp->ncont, P);
+        A(pp->pair, P); A(pp->owner_start, Cn); A(pp->owner_count, Cn); A(pp->ncont, P); A(pp->prox, P);
         A(pp->key, 4 * (size_t)P); A(pp->w1, 4 * (size_t)P); A(pp->w2, 4 * (size_t)P); A(pp->n, 4 * (size_t)P);
         A(pp->imp, 4 * (size_t)P); A(pp->nl, 4 * (size_t)P);
     }
@@ -794,7 +794,6 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         uint64_t slot = handles[k].index;
         if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID && d.shape != NPGPU_SHAPE_CAPSULE)
             return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "only Ball, Cuboid and Capsule shapes are supported");
-        if (d.is_sensor) return fail(w, NPGPU_ERR_UNSUPPORTED_SHAPE, "sensor colliders are not supported");
         if (slot >= w->cap_c) return fail(w, NPGPU_ERR_CAPACITY, "collider index beyond the world's capacity");
         if (!body_handle_ok(w, d.body)) return fail(w, NPGPU_ERR_INVALID_HANDLE, "collider parent body handle is invalid");
         if (!finite_n(d.position_wrt_body, 7) || !finite_n(d.shape_params, 3) || !std::isfinite(d.margin) ||
@@ -820,12 +819,15 @@ npgpu_status npgpu_upsert_colliders(npgpu_world* w, uint32_t n, const npgpu_hand
         std::memset(&u, 0, sizeof(u));
         u.slot = (uint32_t)slot;
         u.body = (uint32_t)d.body.index;
-        u.info = d.shape | (d.friction_combine << 4) | (d.restitution_combine << 8) | (d.ccd_enabled ? CI_CCD : 0u);
+        u.info = d.shape | (d.friction_combine << 4) | (d.restitution_combine << 8) | (d.ccd_enabled ? CI_CCD : 0u) |
+                 (d.is_sensor ? CI_SENSOR : 0u);
         u.params[0] = d.shape_params[0];
         u.params[1] = d.shape_params[1];
         u.params[2] = d.shape_params[2];
         std::memcpy(u.wrt, d.position_wrt_body, sizeof(u.wrt));
-        u.margin = d.margin;
+        // A sensor's query limit is its linear prediction alone
+        // (GeometricQueryType::Proximity, collider.rs:542-543).
+        u.margin = d.is_sensor ? 0.0f : d.margin;
         u.lin_pred = d.linear_prediction;
         u.friction = d.friction;
         u.restitution = d.restitution;
@@ -2217,6 +2219,8 @@ npgpu_status npgpu_interferences_with_aabbs(npgpu_world* w, uint32_t n, const fl
 
 npgpu_status npgpu_enable_contact_events(npgpu_world* w, uint32_t capacity) {
     if (!w) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null world");
+    if (capacity && w->cap_c > (1u << 26))
+        return fail(w, NPGPU_ERR_CAPACITY, "events need collider slots below 2^26");
     CK(cudaStreamSynchronize(w->stream), "synchronize");
     if (w->dw.events) cudaFree(w->dw.events);
     w->dw.events = nullptr;
@@ -2230,19 +2234,31 @@ npgpu_status npgpu_enable_contact_events(npgpu_world* w, uint32_t capacity) {
     return NPGPU_OK;
 }
 
-npgpu_status npgpu_contact_events(npgpu_world* w, npgpu_contact_event* out, uint32_t max, uint32_t* count) {
-    if (!w || !count || (max && !out)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
-    if (!w->dw.events) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "contact events are off (npgpu_enable_contact_events)");
+// The step's recorded events in recording order (ev), and how many were
+// emitted (n; above the capacity when some were lost).
+static npgpu_status read_events(npgpu_world* w, std::vector<uint2>& ev, uint32_t& n) {
+    if (!w->dw.events) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "events are off (npgpu_enable_contact_events)");
     CK(cudaStreamSynchronize(w->stream), "synchronize");
-    uint32_t n = 0;
+    n = 0;
     CK(cudaMemcpy(&n, &w->ctl->nevents, sizeof(n), cudaMemcpyDeviceToHost), "d2h");
     const uint32_t kept = std::min(n, w->dw.events_cap);
-    std::vector<uint2> ev(kept);
+    ev.resize(kept);
     if (kept) CK(cudaMemcpy(ev.data(), w->dw.events, sizeof(uint2) * kept, cudaMemcpyDeviceToHost), "d2h");
-    std::vector<uint64_t> keys(kept);
-    for (uint32_t k = 0; k < kept; ++k)
-        keys[k] = ((uint64_t)ev[k].x << 33) | ((uint64_t)(ev[k].y & 0x7fffffffu) << 1) | (ev[k].y >> 31);
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_contact_events(npgpu_world* w, npgpu_contact_event* out, uint32_t max, uint32_t* count) {
+    if (!w || !count || (max && !out)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<uint2> ev;
+    uint32_t n = 0;
+    npgpu_status st = read_events(w, ev, n);
+    if (st != NPGPU_OK) return st;
+    std::vector<uint64_t> keys;
+    for (const uint2& e : ev)
+        if (!(e.y & 0x40000000u))
+            keys.push_back(((uint64_t)e.x << 33) | ((uint64_t)(e.y & 0x3fffffffu) << 1) | (e.y >> 31));
     std::sort(keys.begin(), keys.end());
+    const uint32_t kept = (uint32_t)keys.size();
     *count = kept;
     for (uint32_t k = 0; k < kept && k < max; ++k) {
         out[k].collider1 = (uint32_t)(keys[k] >> 33);
@@ -2251,6 +2267,33 @@ npgpu_status npgpu_contact_events(npgpu_world* w, npgpu_contact_event* out, uint
     }
     if (n > w->dw.events_cap)
         return fail(w, NPGPU_ERR_CAPACITY, "more contact events than the capacity given to npgpu_enable_contact_events");
+    return NPGPU_OK;
+}
+
+npgpu_status npgpu_proximity_events(npgpu_world* w, npgpu_proximity_event* out, uint32_t max, uint32_t* count) {
+    if (!w || !count || (max && !out)) return fail(w, NPGPU_ERR_INVALID_ARGUMENT, "null argument");
+    std::vector<uint2> ev;
+    uint32_t n = 0;
+    npgpu_status st = read_events(w, ev, n);
+    if (st != NPGPU_OK) return st;
+    // Stable by pair: the passes append in order, and a pair has at most one
+    // event a pass.
+    std::vector<uint2> px;
+    for (const uint2& e : ev)
+        if (e.y & 0x40000000u) px.push_back(e);
+    std::stable_sort(px.begin(), px.end(), [](const uint2& a, const uint2& b) {
+        const uint32_t a2 = a.y & 0x03ffffffu, b2 = b.y & 0x03ffffffu;
+        return a.x != b.x ? a.x < b.x : a2 < b2;
+    });
+    *count = (uint32_t)px.size();
+    for (uint32_t k = 0; k < px.size() && k < max; ++k) {
+        out[k].collider1 = px[k].x;
+        out[k].collider2 = px[k].y & 0x03ffffffu;
+        out[k].prev_status = (px[k].y >> 26) & 3u;
+        out[k].new_status = (px[k].y >> 28) & 3u;
+    }
+    if (n > w->dw.events_cap)
+        return fail(w, NPGPU_ERR_CAPACITY, "more events than the capacity given to npgpu_enable_contact_events");
     return NPGPU_OK;
 }
 

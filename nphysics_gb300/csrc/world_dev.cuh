@@ -109,7 +109,9 @@ struct Colliders {
     uint32_t *leaf_count, *leaf_offset;
     uint32_t *leaf_tmp;              // up to kLeafCap partners per leaf from the counting traversal
 };
-enum : uint32_t { CI_ALIVE = 1u << 16, CI_CCD = 1u << 17 };
+enum : uint32_t { CI_ALIVE = 1u << 16, CI_CCD = 1u << 17, CI_SENSOR = 1u << 18 };
+// Proximity of a pair with a sensor (ncollide3d query::Proximity).
+enum : uint32_t { PROX_INTERSECTING = 0, PROX_WITHIN_MARGIN = 1, PROX_DISJOINT = 2 };
 
 // Joint constraints by joint slot (= the generational-arena index of the
 // host joint set). The host writes the description; the impulses and the
@@ -169,6 +171,7 @@ struct Pairs {
     uint2 *pair;                     // (collider1, collider2), collider1 < collider2
     uint32_t *owner_start, *owner_count;   // by collider slot: the pairs it owns
     uint8_t *ncont;                  // contacts in the manifold
+    uint8_t *prox;                   // PROX_* of a pair with a sensor (PROX_DISJOINT otherwise)
     uint32_t *key;                   // 4 per pair: feature key (fid1 * 26 + fid2)
     float4 *w1;                      // world1 xyz, depth
     float4 *w2;                      // world2 xyz

@@ -427,6 +427,33 @@ def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234, ccd=False
                  info={"walls": n_walls, "bodies": n_walls * (width * height + balls)})
 
 
+# ---------------------------------------------------------------- sensors
+def sensor_gates(balls=6, sensors=True, seed=11, world=0):
+    """Balls dropped through a static sensor box (a trigger zone above the
+    ground) onto the ground; the first ball also carries a massless sensor
+    ball of radius 0.9 around it (a proximity trigger moving with it). With
+    `sensors` False the two sensor colliders are left out: the bodies' motion
+    is the same, since sensors make no contacts and add no mass."""
+    rng = np.random.default_rng(seed)
+    g, gc = _ground(half=(10.0, 0.5, 10.0), world=world)
+    zone = collider_descs(1, 0, abi.SHAPE_CUBOID, (1.5, 0.4, 1.5))
+    zone["position_wrt_body"][0, 1] = 2.0
+    zone["is_sensor"] = 1
+    b = body_descs(balls)
+    b["world"] = world
+    b["position"][:, 0] = rng.uniform(-1.2, 1.2, balls).astype(np.float32)
+    b["position"][:, 1] = (4.0 + 0.9 * np.arange(balls)).astype(np.float32)
+    b["position"][:, 2] = rng.uniform(-1.2, 1.2, balls).astype(np.float32)
+    c = collider_descs(balls, np.arange(balls), abi.SHAPE_BALL, (0.25, 0.0, 0.0), density=1.0, friction=0.5)
+    trig = collider_descs(1, 0, abi.SHAPE_BALL, (0.9, 0.0, 0.0))
+    trig["is_sensor"] = 1
+    if sensors:
+        bodies, colliders = _concat([g, b], [np.concatenate([gc, zone]), np.concatenate([c, trig])])
+    else:
+        bodies, colliders = _concat([g, b], [gc, c])
+    return Scene("sensor gates", bodies, colliders)
+
+
 # ---------------------------------------------------------------- CCD scenes
 def ccd_wall(speed=120.0, half_thickness=0.05, radius=0.1, n=1, ccd=True, gravity=(0.0, 0.0, 0.0),
              shape=abi.SHAPE_BALL, spin=0.0, seed=3, world=0, restitution=0.0, linear_interp=False):

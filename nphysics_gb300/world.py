@@ -252,6 +252,20 @@ class GpuWorld:
             out[k] = (arr[k].collider1, arr[k].collider2, arr[k].stopped)
         return out
 
+    def proximity_events(self):
+        """The last step's (collider1, collider2, previous, new) proximity
+        events of pairs with a sensor, by pair and, within a pair, in pass
+        order."""
+        cnt = C.c_uint32(0)
+        self._check(self.L.npgpu_proximity_events(self.w, None, 0, C.byref(cnt)), "proximity_events")
+        n = cnt.value
+        arr = (abi.ProximityEvent * max(n, 1))()
+        self._check(self.L.npgpu_proximity_events(self.w, arr, n, C.byref(cnt)), "proximity_events")
+        out = np.zeros((n, 4), np.uint32)
+        for k in range(n):
+            out[k] = (arr[k].collider1, arr[k].collider2, arr[k].prev_status, arr[k].new_status)
+        return out
+
     def autotune(self, steps_per_candidate=5):
         """Times the solver's launch shapes on real steps (all give the same
         bits) and keeps the fastest: (schedule, world_threads, ms per step)."""

@@ -264,13 +264,31 @@ uint32_t orc_get_pairs(orc_world* o, uint32_t* out, uint32_t max) {
 
 // Contact events of the last step as (collider1, collider2, stopped), in the
 // order the passes produced them.
-void orc_record_events(orc_world* o, int on) { DISPATCH(o, { w.record_events = on != 0; w.events.clear(); }); }
+void orc_record_events(orc_world* o, int on) {
+    DISPATCH(o, {
+        w.record_events = on != 0;
+        w.events.clear();
+        w.prox_events.clear();
+    });
+}
 uint32_t orc_contact_events(orc_world* o, uint32_t* out3, uint32_t max) {
     uint32_t n = 0;
     DISPATCH(o, {
         n = uint32_t(w.events.size());
         for (uint32_t i = 0; i < n && i < max; ++i)
             for (int k = 0; k < 3; ++k) out3[3 * i + k] = w.events[i][k];
+    });
+    return n;
+}
+
+// Proximity events of the last step as (collider1, collider2, previous, new),
+// in the order the passes produced them.
+uint32_t orc_proximity_events(orc_world* o, uint32_t* out4, uint32_t max) {
+    uint32_t n = 0;
+    DISPATCH(o, {
+        n = uint32_t(w.prox_events.size());
+        for (uint32_t i = 0; i < n && i < max; ++i)
+            for (int k = 0; k < 4; ++k) out4[4 * i + k] = w.prox_events[i][k];
     });
     return n;
 }

@@ -56,6 +56,7 @@ def lib():
             "orc_last_error": (C.c_char_p, [W]),
             "orc_record_events": (None, [W, C.c_int]),
             "orc_contact_events": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
+            "orc_proximity_events": (C.c_uint32, [W, C.c_void_p, C.c_uint32]),
             "orc_rays": (C.c_uint32, [W, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
             "orc_overlaps": (C.c_uint32, [W, C.c_int, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
         }
@@ -247,6 +248,15 @@ class OracleWorld:
         self.L.orc_contact_events(self.w, _ptr(out), n)
         out = out[:n]
         return out[np.lexsort((out[:, 2], out[:, 1], out[:, 0]))] if n else out
+
+    def proximity_events(self):
+        """(collider1, collider2, previous, new) rows by pair, each pair's in
+        pass order."""
+        n = self.L.orc_proximity_events(self.w, None, 0)
+        out = np.zeros((max(n, 1), 4), np.uint32)
+        self.L.orc_proximity_events(self.w, _ptr(out), n)
+        out = out[:n]
+        return out[np.lexsort((out[:, 1], out[:, 0]))] if n else out
 
     def rays(self, rays6, max_toi, world=0xffffffff):
         rays6 = np.ascontiguousarray(rays6, np.float32).reshape(-1, 6)

@@ -242,6 +242,7 @@ template <class R> struct Collider {
     R aabb_min[3], aabb_max[3];   // fat AABB
     bool has_fat = false;
     bool ccd = false;             // Collider::is_ccd_enabled
+    bool sensor = false;          // Collider::is_sensor: a proximity query (margin taken as 0)
     R sw_min[3], sw_max[3];       // CCD: the box swept from the safe pose to the current one
     R query_limit() const { return margin + linear_prediction; }
     R dilation() const { return (shape == NPGPU_SHAPE_BALL || shape == NPGPU_SHAPE_CAPSULE) ? radius : R(0); }
@@ -261,6 +262,7 @@ template <class R> struct Manifold {
     std::vector<MContact<R>> contacts;
     uint32_t colour = 0xffffffffu;
     bool in_solver = false;
+    uint32_t prox = NPGPU_PROXIMITY_DISJOINT;   // a pair with a sensor: its ncollide3d Proximity
 };
 
 template <class R> struct Row {
@@ -386,7 +388,6 @@ public:
     npgpu_status upsert_collider(const npgpu_handle& h, const npgpu_collider_desc& d) {
         if (d.shape != NPGPU_SHAPE_BALL && d.shape != NPGPU_SHAPE_CUBOID && d.shape != NPGPU_SHAPE_CAPSULE)
             return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "only balls, cuboids and capsules are supported");
-        if (d.is_sensor) return fail(NPGPU_ERR_UNSUPPORTED_SHAPE, "sensors are not supported");
         if (d.body.index >= bodies.size() || !bodies[d.body.index].alive ||
             bodies[d.body.index].generation != d.body.generation)
             return fail(NPGPU_ERR_INVALID_HANDLE, "collider parent body handle is invalid");
@@ -404,7 +405,10 @@ public:
         c.shape = d.shape;
         c.radius = R(d.shape_params[0]);
         c.half = v3<R>(R(d.shape_params[0]), R(d.shape_params[1]), R(d.shape_params[2]));
-        c.margin = R(d.margin);
+        // A sensor's query limit is its linear prediction alone
+        // (GeometricQueryType::Proximity, collider.rs:542-543).
+        c.sensor = d.is_sensor != 0;
+        c.margin = c.sensor ? R(0) : R(d.margin);
         c.density = R(d.density);
         c.linear_prediction = R(d.linear_prediction);
         c.friction = R(d.friction);
@@ -1281,6 +1285,20 @@ public:
         } else {
             box_box(a, b, prediction, cands);
         }
+        if (a.sensor || b.sensor) {
+            // A proximity pair (ProximityDetector): Intersecting when the
+            // shapes touch or overlap, WithinMargin when the contact
+            // generator finds them within the query limits, Disjoint
+            // otherwise; no contacts.
+            uint32_t st = NPGPU_PROXIMITY_DISJOINT;
+            for (const Cand& cd : cands) {
+                if (cd.g.depth >= R(0)) st = NPGPU_PROXIMITY_INTERSECTING;
+                else if (st == NPGPU_PROXIMITY_DISJOINT) st = NPGPU_PROXIMITY_WITHIN_MARGIN;
+            }
+            m.prox = st;
+            m.contacts.clear();
+            return;
+        }
         std::vector<MContact<R>> nc;
         const Body<R>& b1 = bodies[a.body];
         for (const Cand& cd : cands) {
@@ -1311,18 +1329,24 @@ public:
             Manifold<R> m;
             auto it = manifolds.find(key);
             const bool had = it != manifolds.end() && !it->second.contacts.empty();
+            const uint32_t was = it != manifolds.end() ? it->second.prox : uint32_t(NPGPU_PROXIMITY_DISJOINT);
             if (it != manifolds.end()) m = it->second;
             m.c1 = uint32_t(key >> 32);
             m.c2 = uint32_t(key & 0xffffffffu);
             narrow_pair(m);
-            // ContactEvent::Started / Stopped of this pass.
+            // ContactEvent::Started / Stopped and ProximityEvent of this pass.
             if (record_events && had != !m.contacts.empty()) events.push_back({m.c1, m.c2, had ? 1u : 0u});
+            if (record_events && was != m.prox) prox_events.push_back({m.c1, m.c2, was, m.prox});
             next[key] = m;
         }
         if (record_events)
             for (auto& kv : manifolds)
-                if (!kv.second.contacts.empty() && next.find(kv.first) == next.end())
-                    events.push_back({kv.second.c1, kv.second.c2, 1u});
+                if (next.find(kv.first) == next.end()) {
+                    if (!kv.second.contacts.empty()) events.push_back({kv.second.c1, kv.second.c2, 1u});
+                    if (kv.second.prox != NPGPU_PROXIMITY_DISJOINT)
+                        prox_events.push_back({kv.second.c1, kv.second.c2, kv.second.prox,
+                                               uint32_t(NPGPU_PROXIMITY_DISJOINT)});
+                }
         manifolds.swap(next);
         cd_dirty = false;
     }
@@ -1333,6 +1357,9 @@ public:
     // cleared when the step begins (mechanical_world.rs:250).
     bool record_events = false;
     std::vector<std::array<uint32_t, 3>> events;
+    // GeometricalWorld::proximity_events (geometrical_world.rs:378-381):
+    // (collider1, collider2, previous, new) in the order the passes made them.
+    std::vector<std::array<uint32_t, 4>> prox_events;
 
     // interferences_with_ray (geometrical_world.rs:327-341) for one ray on
     // solid shapes: the sphere's quadratic, or the cuboid's three slabs in its
@@ -2619,6 +2646,7 @@ public:
     bool interacts(uint32_t i, uint32_t j) const {
         const Collider<R>& a = colliders[i];
         const Collider<R>& b = colliders[j];
+        if (a.sensor || b.sensor) return false;   // proximity pairs take no part in CCD
         if (!pair_allowed(i, j)) return false;
         if (aabb_overlap(a, b)) return true;
         if (!a.ccd && !b.ccd) return false;
@@ -3139,6 +3167,7 @@ public:
         cur_dt = R(params.dt);
         R dt = cur_dt;
         events.clear();
+        prox_events.clear();
         // maintain: register new colliders (geometrical_world.rs:102-143).
         for (auto& c : colliders) {
             if (!c.alive || c.registered) continue;

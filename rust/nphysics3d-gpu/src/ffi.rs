@@ -219,6 +219,15 @@ pub struct npgpu_contact_event {
     pub stopped: u32,
 }
 
+#[repr(C)]
+#[derive(Copy, Clone, Default)]
+pub struct npgpu_proximity_event {
+    pub collider1: u32,
+    pub collider2: u32,
+    pub prev_status: u32,
+    pub new_status: u32,
+}
+
 /// Opaque world handle (`npgpu_world*`).
 pub enum npgpu_world {}
 
@@ -270,6 +279,8 @@ extern "C" {
     pub fn npgpu_enable_contact_events(w: *mut npgpu_world, capacity: u32) -> c_int;
     pub fn npgpu_contact_events(w: *mut npgpu_world, out: *mut npgpu_contact_event, max: u32,
                                 count: *mut u32) -> c_int;
+    pub fn npgpu_proximity_events(w: *mut npgpu_world, out: *mut npgpu_proximity_event, max: u32,
+                                  count: *mut u32) -> c_int;
     pub fn npgpu_mlp_set(w: *mut npgpu_world, params: *const f32, n: u32) -> c_int;
     pub fn npgpu_mlp_get(w: *mut npgpu_world, params: *mut f32, n: u32) -> c_int;
     pub fn npgpu_mlp_record(w: *mut npgpu_world, capacity: u32) -> c_int;
