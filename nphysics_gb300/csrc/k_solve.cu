@@ -2234,7 +2234,7 @@ __device__ __forceinline__ void world_velocity(const World& w, const StepParams&
 // world and 6 floats per slot of a small world for each warp.
 #if !NPGPU_EXCHANGE_TU
 template <int THREADS, bool JOINTS>
-__global__ void __launch_bounds__(THREADS, 512 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
+__global__ void __launch_bounds__(THREADS, 384 / THREADS) k_world_velocity(World w, StepParams p, uint32_t n_worlds,
                                                                   uint32_t max_world_bodies, uint32_t n_big,
                                                                   uint32_t n_cluster) {
     extern __shared__ float s_dv[];
