@@ -427,6 +427,134 @@ def brick_walls(n_walls=256, width=50, height=40, balls=64, seed=1234, ccd=False
                  info={"walls": n_walls, "bodies": n_walls * (width * height + balls)})
 
 
+# ---------------------------------------------------------------- compounds
+def _qmul(a, b):
+    """Quaternion product a * b, (i, j, k, w) order, float32."""
+    ai, aj, ak, aw = a
+    bi, bj, bk, bw = b
+    return np.array([aw * bi + ai * bw + aj * bk - ak * bj, aw * bj - ai * bk + aj * bw + ak * bi,
+                     aw * bk + ai * bj - aj * bi + ak * bw, aw * bw - ai * bi - aj * bj - ak * bk], np.float32)
+
+
+def _qrot(q, v):
+    i, j, k, w = q
+    u = np.array([i, j, k], np.float32)
+    t = 2.0 * np.cross(u, v)
+    return (v + w * t + np.cross(u, t)).astype(np.float32)
+
+
+def shape_mass_properties(shape, params, density):
+    """(mass, centre, angular inertia about the centre) of a ball, cuboid or
+    capsule in f64: volumetric_ball.rs, volumetric_cuboid.rs and
+    volumetric_capsule.rs (the capsule's axis along local y)."""
+    if shape == abi.SHAPE_BALL:
+        r = float(params[0])
+        m = density * 4.0 / 3.0 * np.pi * r ** 3
+        return m, np.zeros(3), np.eye(3) * (m * 0.4 * r * r)
+    if shape == abi.SHAPE_CUBOID:
+        hx, hy, hz = (float(v) for v in params)
+        m = density * 8.0 * hx * hy * hz
+        return m, np.zeros(3), np.diag([hy * hy + hz * hz, hx * hx + hz * hz, hx * hx + hy * hy]) * (m / 3.0)
+    r, hh = float(params[0]), float(params[1])
+    m = density * (np.pi * r * r * 2.0 * hh + 4.0 / 3.0 * np.pi * r ** 3)
+    h = 2.0 * hh
+    unit = np.diag([(3.0 * r * r + h * h) / 12.0, r * r / 2.0, (3.0 * r * r + h * h) / 12.0]) + np.eye(3) * 0.4 * r * r
+    extra = h * h * 0.5 + h * r * 3.0 / 8.0
+    unit[0, 0] += extra
+    unit[2, 2] += extra
+    return m, np.zeros(3), unit * m
+
+
+def _rotm(q):
+    i, j, k, w = (float(v) for v in q)
+    return np.array([[1 - 2 * (j * j + k * k), 2 * (i * j - k * w), 2 * (i * k + j * w)],
+                     [2 * (i * j + k * w), 1 - 2 * (i * i + k * k), 2 * (j * k - i * w)],
+                     [2 * (i * k - j * w), 2 * (j * k + i * w), 1 - 2 * (i * i + j * j)]])
+
+
+def compound_mass_properties(parts, density):
+    """Compound::mass_properties (volumetric_compound.rs): the parts' masses
+    summed, their centres averaged by mass, their inertias rotated into the
+    compound's frame, moved to the common centre and summed; in f64."""
+    props = [(np.asarray(t, np.float64), _rotm(q)) + shape_mass_properties(sh, pr, 1.0) for t, q, sh, pr in parts]
+    mt = sum(p[2] for p in props)
+    com = sum((R @ c + t) * m for t, R, m, c, _ in props) / mt
+    I = np.zeros((3, 3))
+    for t, R, m, c, Ip in props:
+        d = R @ c + t - com
+        I += R @ Ip @ R.T + m * (np.dot(d, d) * np.eye(3) - np.outer(d, d))
+    return mt * density, com, I * density
+
+
+def add_collider_mass(body, mass, com, inertia):
+    """RigidBody::add_local_inertia_and_com (rigid_body.rs:747-766) on a body
+    description: the centre becomes the mass-weighted average, the inertias
+    add (about their own centres, as the reference adds them)."""
+    m0 = float(body["local_inertia"][0])
+    c0 = np.asarray(body["local_com"], np.float64)
+    ms = m0 + mass
+    body["local_com"] = (c0 * m0 + np.asarray(com) * mass) / ms if ms != 0.0 else 0.0
+    li = body["local_inertia"]
+    li[0] = ms
+    for k, (a, b) in enumerate(((0, 0), (0, 1), (0, 2), (1, 1), (1, 2), (2, 2))):
+        li[1 + k] += inertia[a, b]
+
+
+def compound_colliders(body_index, parts, position=((0.0, 0.0, 0.0), (0.0, 0.0, 0.0, 1.0)), density=0.0,
+                       friction=0.5, restitution=0.0):
+    """ColliderDesc::new(ShapeHandle::new(Compound::new(parts))) on a body
+    (ncollide3d's Compound): one collider per part, at the compound
+    collider's position times the part's, sharing its material; each part
+    collides on its own. The parts carry no density: the compound's mass
+    properties (compound_mass_properties at `density`, moved by `position`
+    as Volumetric::transformed_mass_properties does) are returned for
+    add_collider_mass, which adds them to the body as the reference adds a
+    collider's. `parts`: (translation, quaternion (i, j, k, w), shape,
+    shape_params) per part. Returns (colliders, (mass, centre, inertia))."""
+    t0 = np.asarray(position[0], np.float32)
+    q0 = np.asarray(position[1], np.float32)
+    out = []
+    for t, q, shape, params in parts:
+        c = collider_descs(1, body_index, shape, params, density=0.0, friction=friction, restitution=restitution)
+        c["position_wrt_body"][0, :3] = t0 + _qrot(q0, np.asarray(t, np.float32))
+        c["position_wrt_body"][0, 3:] = _qmul(q0, np.asarray(q, np.float32))
+        out.append(c)
+    m, com, I = compound_mass_properties(parts, density)
+    R0 = _rotm(q0)
+    return np.concatenate(out), (m, R0 @ com + t0.astype(np.float64), R0 @ I @ R0.T)
+
+
+def compound_drop(n=6, seed=17, world=0):
+    """Compound bodies dropped on the ground: L shapes of two cuboids,
+    dumbbells of two balls on a capsule bar, and T shapes of a cuboid and a
+    capsule, each with a random orientation."""
+    rng = np.random.default_rng(seed)
+    g, gc = _ground(half=(20.0, 1.0, 20.0), world=world)
+    b = body_descs(n)
+    b["world"] = world
+    b["position"][:, 0] = (np.arange(n) % 3 - 1) * 3.0
+    b["position"][:, 1] = 2.0 + 1.5 * (np.arange(n) // 3)
+    b["position"][:, 3:] = uniform_quaternions(rng, n)
+    qz = np.array([0.0, 0.0, np.sin(np.pi / 4), np.cos(np.pi / 4)], np.float32)   # local y onto x
+    ident = (0.0, 0.0, 0.0, 1.0)
+    kinds = [
+        [((0.0, 0.0, 0.0), ident, abi.SHAPE_CUBOID, (0.6, 0.15, 0.2)),
+         ((0.45, 0.45, 0.0), ident, abi.SHAPE_CUBOID, (0.15, 0.3, 0.2))],
+        [((-0.6, 0.0, 0.0), ident, abi.SHAPE_BALL, (0.3, 0.0, 0.0)),
+         ((0.6, 0.0, 0.0), ident, abi.SHAPE_BALL, (0.3, 0.0, 0.0)),
+         ((0.0, 0.0, 0.0), qz, abi.SHAPE_CAPSULE, (0.08, 0.5, 0.0))],
+        [((0.0, 0.3, 0.0), ident, abi.SHAPE_CUBOID, (0.5, 0.1, 0.1)),
+         ((0.0, -0.2, 0.0), ident, abi.SHAPE_CAPSULE, (0.1, 0.3, 0.0))],
+    ]
+    cs = []
+    for i in range(n):
+        c, mp = compound_colliders(i, kinds[i % 3], density=1.0)
+        add_collider_mass(b[i], *mp)
+        cs.append(c)
+    bodies, colliders = _concat([g, b], [gc, np.concatenate(cs)])
+    return Scene("compound drop", bodies, colliders)
+
+
 # ---------------------------------------------------------------- sensors
 def sensor_gates(balls=6, sensors=True, seed=11, world=0):
     """Balls dropped through a static sensor box (a trigger zone above the
