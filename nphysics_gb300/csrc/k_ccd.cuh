@@ -20,7 +20,8 @@
 // overlap; pairs are taken in collider-slot order and TOIs of equal time in
 // the order they were found.
 
-constexpr int kCcdThreads = 128;
+// The largest CCD block (a world's block has 128 or 256 threads).
+constexpr int kCcdThreads = 256;
 constexpr uint32_t kTocPopped = 1u << 30, kTocSuperseded = 1u << 31, kTocSeq = kTocPopped - 1u;
 
 __device__ __forceinline__ uint32_t ccd_body_of(const World& w, uint32_t c) { return w.c.body[c]; }

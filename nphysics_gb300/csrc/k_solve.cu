@@ -3221,7 +3221,18 @@ cudaError_t launch_ccd(const World& w, const StepParams& p, cudaStream_t st) {
     if (e != cudaSuccess) return e;
     k_ccd_adj_fill<<<item_blocks(w.cap_pairs), kItemThreads, 0, st>>>(w);
     k_ccd_adj_sort<<<item_blocks(nc), kItemThreads, 0, st>>>(w);
-    k_ccd_world<<<w.ccd.n_worlds, kCcdThreads, 0, st>>>(w, p);
+    // 256 threads a world when every world gets an SM of its own (the
+    // kernel's registers allow one such block an SM), else 128 (two an SM):
+    // the same results either way.
+    static int sms = 0;
+    if (sms == 0) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+            sms = 1;
+    }
+    const int threads = w.ccd.n_worlds <= (uint32_t)sms ? kCcdThreads : kCcdThreads / 2;
+    k_ccd_world<<<w.ccd.n_worlds, threads, 0, st>>>(w, p);
     k_ccd_finish<<<item_blocks(w.nb_slots), kItemThreads, 0, st>>>(w);
     return cudaGetLastError();
 }
