@@ -581,8 +581,9 @@ def measure(args, sc, w, kind, rank, world_size, local_rank):
     launches = LAUNCHES_PER_STEP if tuned[0] == 1 else LAUNCHES_PER_STEP_BATCHED
     if getattr(args, "ccd", False) and kind == "walls":
         # k_ccd_begin, the pair adjacency's count, scan (3), fill and sort,
-        # k_ccd_world, k_ccd_finish.
-        launches += 9
+        # k_ccd_world and k_ccd_solve once a pass (max_ccd_substeps + 2
+        # passes), k_ccd_finish.
+        launches += 8 + 2 * (int(p.max_ccd_substeps) + 2)
     return {
         "value": value, "ms_per_step": total_ms / args.steps, "first_timed_step": first_timed,
         "tuned": tuned,

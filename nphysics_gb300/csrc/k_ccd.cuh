@@ -386,7 +386,6 @@ __device__ void ccd_manifold_velocity(const World& w, CcdManifold& m, bool frict
 }
 
 // Shared state of a world's CCD loop.
-constexpr uint32_t kCcdColours = 256;
 struct CcdState {
     float end_time, min_overstep, last;
     uint32_t last_iter, result, nheap, nimp, seq, nstack, nisland, nccdb, nm;
@@ -399,6 +398,21 @@ struct CcdState {
 };
 
 enum : int { CCD_T_TOI = 0, CCD_T_SOLVER = 1, CCD_T_BROAD = 2, CCD_T_NARROW = 3 };
+
+// A world's CCD state between the pass and solve kernels (Ccd::wstate,
+// kCcdStateWords words a world; the island's colour starts in Ccd::wcols).
+constexpr int kCcdSolveThreads = 256;
+enum : uint32_t {
+    CS_END = 0, CS_DTS = 1, CS_LAST_ITER = 2, CS_DONE = 3, CS_PENDING = 4, CS_NM = 5, CS_NCOL = 6, CS_NISL = 7,
+    CS_NCCDB = 8, CS_NIMP = 9, CS_TOTAL = 10   // CS_TOTAL, CS_TOTAL + 1: the world's CCD time (profile mode)
+};
+// Profile mode: ns of a world's CCD spent in `part`, and the world's total.
+__device__ __forceinline__ void ccd_account(const World& w, uint32_t* S, int part, unsigned long long ns) {
+    atomicAdd(&w.ctl->ccd_ns[part], ns);
+    unsigned long long* total = reinterpret_cast<unsigned long long*>(S + CS_TOTAL);
+    *total += ns;
+    atomicMax(&w.ctl->ccd_max_ns, *total);
+}
 // Profile mode: the time since the last mark goes to `part` (thread 0 keeps
 // the block's sums).
 __device__ __forceinline__ void ccd_mark(CcdState& st, const StepParams& p, int part) {
@@ -1016,20 +1030,61 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         mord[st.col_start[k] + atomicAdd(&st.col_fill[k], 1u)] = mlist[q];
     }
     __syncthreads();
-    // step_ccd: the rows, the position solve, validate_advancement of the
-    // impacting bodies, the velocity solve and the island's integration.
+    // The island's solve runs in k_ccd_solve, with more threads a world.
+    uint32_t* S = cd.wstate + kCcdStateWords * (size_t)wd;
+    for (uint32_t k = threadIdx.x; k <= ncol; k += blockDim.x) cd.wcols[(kCcdColours + 1) * (size_t)wd + k] = st.col_start[k];
+    ccd_mark(st, p, CCD_T_SOLVER);
+    if (threadIdx.x == 0) {
+        S[CS_DTS] = __float_as_uint(dts);
+        S[CS_NM] = nm;
+        S[CS_NCOL] = ncol;
+        S[CS_NISL] = nisl;
+        S[CS_NCCDB] = st.nccdb;
+        S[CS_NIMP] = st.nimp;
+        S[CS_PENDING] = 1u;
+    }
+    __syncthreads();
+}
+
+// step_ccd for a world whose pass prepared a substep island
+// (MoreauJeanSolver::step_ccd, moreau_jean_solver.rs:94-127): the rows, the
+// position solve, validate_advancement of the impacting bodies, the velocity
+// solve, the island's integration and update_dynamics over the substep. A
+// kernel of its own so that a world gets more threads than the pass kernel's
+// registers allow.
+__global__ void __launch_bounds__(kCcdSolveThreads, 2) k_ccd_solve(World w, StepParams p) {
+    __shared__ uint32_t col_start[kCcdColours + 1];
+    const Ccd& cd = w.ccd;
+    const uint32_t wd = blockIdx.x;
+    if (wd >= cd.n_worlds || !cd.wflag[wd]) return;
+    uint32_t* S = cd.wstate + kCcdStateWords * (size_t)wd;
+    if (!S[CS_PENDING]) return;
+    const unsigned long long t0 = p.profile ? global_ns() : 0ull;
+    const uint32_t ws = cd.wstart[wd], wn = cd.wstart[wd + 1] - ws;
+    const uint32_t rb = kCcdRegion * ws + kCcdSlack * wd;
+    const float dts = __uint_as_float(S[CS_DTS]);
+    const uint32_t nm = S[CS_NM], ncol = S[CS_NCOL], nisl = S[CS_NISL], nccdb = S[CS_NCCDB], nimp = S[CS_NIMP];
+    for (uint32_t k = threadIdx.x; k <= ncol; k += blockDim.x) col_start[k] = cd.wcols[(kCcdColours + 1) * (size_t)wd + k];
+    const uint32_t* island = cd.island + rb;
+    const uint32_t* ccdb = cd.ccdb + rb;
+    const uint32_t* mlist = cd.mlist + rb;
+    const uint32_t* mord = cd.mord + rb;
+    StepParams ps = p;
+    ps.dt = dts;
+    ps.inv_dt = dts == 0.0f ? 0.0f : 1.0f / dts;
+    __syncthreads();
     for (uint32_t q = threadIdx.x; q < nm; q += blockDim.x) ccd_rows(w, ps, cd.pool[mlist[q]], dts);
     for (uint32_t i = threadIdx.x; i < nisl; i += blockDim.x)
         for (int k = 0; k < 6; ++k) w.b.dv[6 * (size_t)island[i] + k] = 0.0f;
     __syncthreads();
     for (uint32_t it = 0; it < cd.max_position_iterations; ++it)
         for (uint32_t k = 0; k < ncol; ++k) {
-            for (uint32_t q = st.col_start[k] + threadIdx.x; q < st.col_start[k + 1]; q += blockDim.x) {
+            for (uint32_t q = col_start[k] + threadIdx.x; q < col_start[k + 1]; q += blockDim.x) {
                 ccd_position_manifold(w, ps, cd.pool[mord[q]]);
             }
             __syncthreads();
         }
-    for (uint32_t k = threadIdx.x; k < st.nccdb; k += blockDim.x) {
+    for (uint32_t k = threadIdx.x; k < nccdb; k += blockDim.x) {
         const uint32_t h = ccdb[k];
         cd.pos0_t[h] = w.b.pos_t[h];
         cd.pos0_q[h] = w.b.pos_q[h];
@@ -1038,7 +1093,7 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
     for (uint32_t it = 0; it < p.max_velocity_iterations; ++it)
         for (int pass = 0; pass < 2; ++pass)
             for (uint32_t k = 0; k < ncol; ++k) {
-                for (uint32_t q = st.col_start[k] + threadIdx.x; q < st.col_start[k + 1]; q += blockDim.x)
+                for (uint32_t q = col_start[k] + threadIdx.x; q < col_start[k + 1]; q += blockDim.x)
                     ccd_manifold_velocity(w, cd.pool[mord[q]], pass == 0);
                 __syncthreads();
             }
@@ -1061,86 +1116,95 @@ __device__ void ccd_substep(const World& w, const StepParams& p, uint32_t wd, ui
         if (cd.bc_list[cd.bc_start[bb]] != c) continue;   // one collider per body acts
         if ((w.b.info[bb] & BI_CHANGED) && ccd_dynamic(w, bb)) body_update_dynamics(w.b, bb, dts);
     }
-    ccd_mark(st, p, CCD_T_SOLVER);
+    __syncthreads();
     if (threadIdx.x == 0) {
         w.ccd.wdts[wd] = dts;
         atomicAdd(&w.ctl->ccd_substeps, 1u);
-        atomicAdd(&w.ctl->ccd_impacts, st.nimp);
+        atomicAdd(&w.ctl->ccd_impacts, nimp);
+        S[CS_PENDING] = 0u;
+        if (p.profile) ccd_account(w, S, CCD_T_SOLVER, global_ns() - t0);
     }
-    __syncthreads();
 }
 
-// solve_ccd of world blockIdx.x.
-__global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p) {
+
+// One pass of solve_ccd's loop for world blockIdx.x (at most
+// max_ccd_substeps + 2 passes, one launch each): the swept boxes, the
+// prediction, then either a substep's island for k_ccd_solve or, on the last
+// pass, the clamp of the frozen bodies.
+__global__ void __launch_bounds__(kCcdThreads) k_ccd_world(World w, StepParams p, uint32_t pass) {
     __shared__ CcdState st;
     const Ccd& cd = w.ccd;
     const uint32_t wd = blockIdx.x;
     if (wd >= cd.n_worlds) return;
-    if (threadIdx.x == 0) cd.wdts[wd] = -1.0f;   // no substep (yet) this step
+    if (pass == 0 && threadIdx.x == 0) cd.wdts[wd] = -1.0f;   // no substep (yet) this step
     if (!cd.wflag[wd]) return;
+    uint32_t* S = cd.wstate + kCcdStateWords * (size_t)wd;
+    if (pass > 0 && S[CS_DONE]) return;
     const uint32_t ws = cd.wstart[wd], wn = cd.wstart[wd + 1] - ws;
     const uint32_t rb = kCcdRegion * ws + kCcdSlack * wd, rcap = kCcdRegion * wn + kCcdSlack;
     const float dt0 = p.dt;
     const float sub = dt0 / (float)cd.substeps;
-    for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) cd.btime[ccd_body_of(w, cd.order[ws + i])] = 0.0f;
+    if (pass == 0)
+        for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) {
+            const uint32_t b = ccd_body_of(w, cd.order[ws + i]);
+            cd.btime[b] = 0.0f;
+            cd.bepoch[b] = 0u;
+        }
     if (threadIdx.x == 0) {
-        st.end_time = 0.0f;
-        st.last_iter = 0;
+        if (pass == 0) {
+            S[CS_PENDING] = 0u;
+            *reinterpret_cast<unsigned long long*>(S + CS_TOTAL) = 0ull;
+        }
+        st.end_time = pass == 0 ? 0.0f : __uint_as_float(S[CS_END]);
+        st.last_iter = pass == 0 ? 0u : S[CS_LAST_ITER];
         st.epoch = 0;
         st.t_mark = p.profile ? global_ns() : 0ull;
         for (int k = 0; k < 4; ++k) st.t_acc[k] = 0ull;
+        // Each pass either advances end_time by a substep or is the last.
+        if (st.end_time < dt0) {
+            const float e = st.end_time + sub;
+            st.end_time = e < dt0 ? e : dt0;
+        } else {
+            st.last_iter = 1;
+        }
     }
-    for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) cd.bepoch[ccd_body_of(w, cd.order[ws + i])] = 0u;
+    for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) ccd_sweep_box(w, cd.order[ws + i]);
     __syncthreads();
-    // At most max_ccd_substeps + 1 passes: each either advances end_time by
-    // a substep or is the last.
-    for (uint32_t pass = 0; pass <= cd.substeps + 1u; ++pass) {
+    ccd_mark(st, p, CCD_T_BROAD);
+    ccd_predict(w, p, wd, ws, wn, rb, rcap, st);
+    if (st.result == PRED_AFTER) {
         if (threadIdx.x == 0) {
-            if (st.end_time < dt0) {
-                const float e = st.end_time + sub;
-                st.end_time = e < dt0 ? e : dt0;
-            } else {
-                st.last_iter = 1;
-            }
+            const float e = floorf(st.min_overstep / sub) * sub + sub;
+            st.end_time = e < dt0 ? e : dt0;
         }
-        for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) ccd_sweep_box(w, cd.order[ws + i]);
         __syncthreads();
-        ccd_mark(st, p, CCD_T_BROAD);
         ccd_predict(w, p, wd, ws, wn, rb, rcap, st);
-        if (st.result == PRED_AFTER) {
-            if (threadIdx.x == 0) {
-                const float e = floorf(st.min_overstep / sub) * sub + sub;
-                st.end_time = e < dt0 ? e : dt0;
-            }
-            __syncthreads();
-            ccd_predict(w, p, wd, ws, wn, rb, rcap, st);
-            if (threadIdx.x == 0 && st.result != PRED_IMPACTS) st.nimp = 0;
-            __syncthreads();
-        } else if (st.result == PRED_NONE) {
-            if (threadIdx.x == 0) st.nimp = 0;
-            __syncthreads();
-        }
-        if (!st.last_iter && st.nimp > 0) {
-            ccd_substep(w, p, wd, ws, wn, rb, rcap, st);
-            continue;
-        }
+        if (threadIdx.x == 0 && st.result != PRED_IMPACTS) st.nimp = 0;
+        __syncthreads();
+    } else if (st.result == PRED_NONE) {
+        if (threadIdx.x == 0) st.nimp = 0;
+        __syncthreads();
+    }
+    bool done = false;
+    if (!st.last_iter && st.nimp > 0) {
+        ccd_substep(w, p, wd, ws, wn, rb, rcap, st);
+    } else {
         // The bodies frozen by the last prediction stay at their safe poses.
         for (uint32_t i = threadIdx.x; i < wn; i += blockDim.x) {
             const uint32_t c = cd.order[ws + i], b = ccd_body_of(w, c);
             if (cd.bc_list[cd.bc_start[b]] != c) continue;   // one collider per body acts
             if ((cd.bflag[b] & 1u) && bi_status(w.b.info[b]) != 1u) ccd_clamp(w, b);
         }
-        break;
+        done = true;
     }
     __syncthreads();
     ccd_mark(st, p, CCD_T_SOLVER);
-    if (p.profile && threadIdx.x == 0) {
-        unsigned long long total = 0ull;
-        for (int k = 0; k < 4; ++k) {
-            atomicAdd(&w.ctl->ccd_ns[k], st.t_acc[k]);
-            total += st.t_acc[k];
-        }
-        atomicMax(&w.ctl->ccd_max_ns, total);
+    if (threadIdx.x == 0) {
+        S[CS_END] = __float_as_uint(st.end_time);
+        S[CS_LAST_ITER] = st.last_iter;
+        S[CS_DONE] = done ? 1u : 0u;
+        if (p.profile)
+            for (int k = 0; k < 4; ++k) ccd_account(w, S, k, st.t_acc[k]);
     }
 }
 

@@ -3232,7 +3232,12 @@ cudaError_t launch_ccd(const World& w, const StepParams& p, cudaStream_t st) {
             sms = 1;
     }
     const int threads = w.ccd.n_worlds <= (uint32_t)sms ? kCcdThreads : kCcdThreads / 2;
-    k_ccd_world<<<w.ccd.n_worlds, threads, 0, st>>>(w, p);
+    // solve_ccd's loop: a pass kernel, then the solve of the islands the
+    // pass prepared, at most max_ccd_substeps + 2 times.
+    for (uint32_t pass = 0; pass <= w.ccd.substeps + 1u; ++pass) {
+        k_ccd_world<<<w.ccd.n_worlds, threads, 0, st>>>(w, p, pass);
+        k_ccd_solve<<<w.ccd.n_worlds, kCcdSolveThreads, 0, st>>>(w, p);
+    }
     k_ccd_finish<<<item_blocks(w.nb_slots), kItemThreads, 0, st>>>(w);
     return cudaGetLastError();
 }

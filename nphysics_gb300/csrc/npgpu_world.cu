@@ -1401,6 +1401,8 @@ static npgpu_status ccd_layout(npgpu_world* w) {
         alloc(w->ccd_grown, (void**)&cd.ccd_wstart, sizeof(uint32_t) * (W + 1));
         alloc(w->ccd_grown, (void**)&cd.wflag, sizeof(uint32_t) * W);
         alloc(w->ccd_grown, (void**)&cd.wdts, sizeof(float) * W);
+        alloc(w->ccd_grown, (void**)&cd.wstate, sizeof(uint32_t) * kCcdStateWords * W);
+        alloc(w->ccd_grown, (void**)&cd.wcols, sizeof(uint32_t) * (kCcdColours + 1) * W);
         alloc(w->ccd_grown, (void**)&cd.nbr, sizeof(uint32_t) * R);
         alloc(w->ccd_grown, (void**)&cd.nbr2, sizeof(uint32_t) * R);
         alloc(w->ccd_grown, (void**)&cd.mord, sizeof(uint32_t) * R);

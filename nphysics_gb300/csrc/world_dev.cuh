@@ -271,6 +271,7 @@ struct StepParams {
 // region base kCcdRegion * order index of its first collider + kCcdSlack *
 // world, length kCcdRegion * its colliders + kCcdSlack.
 constexpr uint32_t kCcdRegion = 4, kCcdSlack = 64;
+constexpr uint32_t kCcdStateWords = 16, kCcdColours = 256;
 struct CcdToi {                      // a time of impact in a world's queue
     float toi;
     uint32_t c1, c2;
@@ -299,6 +300,8 @@ struct Ccd {
     uint32_t *wstart;                // per world: first index into `order` (n_worlds + 1)
     uint32_t *wflag;                 // per world: 1 when it has a CCD collider
     float *wdts;                     // per world: the last substep's length (< 0: none this step)
+    uint32_t *wstate;                // per world: kCcdStateWords words carried between the CCD kernels
+    uint32_t *wcols;                 // per world: its substep island's colour starts (kCcdColours + 1)
     uint32_t *bc_start, *bc_list;    // colliders of each body, in slot order (host-built CSR)
     uint32_t *ccd_list, *ccd_wstart; // the CCD colliders by (world, slot), each world's range (host-built)
     uint32_t *adj_count, *adj_start, *adj_list;   // the step's broad-phase pairs by collider (CSR, partners in
