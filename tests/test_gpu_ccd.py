@@ -63,6 +63,16 @@ def test_batched_ccd_worlds_match_oracle(gpu_lib):
     assert step_same(g, o, 30) >= 3
 
 
+def test_ccd_batch_wider_than_the_gpu_matches_oracle(gpu_lib):
+    # More CCD worlds than SMs: the pass kernel runs 128 threads a world
+    # (256 for smaller batches); the results are the oracle's either way.
+    sc = scenes.batched_ccd(n_worlds=160)
+    p = sc.params()
+    p.solver_schedule = abi.SCHEDULE_WORLDS
+    g, o = make_pair(sc, p)
+    assert step_same(g, o, 12) >= 12
+
+
 def test_ccd_options_match_oracle(gpu_lib):
     # Four substeps, linear motion interpolation, the penetration switch.
     sc = scenes.ccd_wall(n=4, gravity=(0.0, -9.81, 0.0))
