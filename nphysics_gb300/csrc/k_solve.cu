@@ -3224,13 +3224,10 @@ cudaError_t launch_ccd(const World& w, const StepParams& p, cudaStream_t st) {
     // 256 threads a world when every world gets an SM of its own (the
     // kernel's registers allow one such block an SM), else 128 (two an SM):
     // the same results either way.
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-            sms = 1;
-    }
+    int dev = 0, sms = 1;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        sms = 1;
     const int threads = w.ccd.n_worlds <= (uint32_t)sms ? kCcdThreads : kCcdThreads / 2;
     // solve_ccd's loop: a pass kernel, then the solve of the islands the
     // pass prepared, at most max_ccd_substeps + 2 times.
